@@ -1,0 +1,247 @@
+"""ctypes view of the C ABI declared in ``include/braincell_gb300.h``.
+
+The shared library is built in-tree (``braincell_gb300/_native/libbraincell_gb300.so``)
+by :func:`braincell_gb300.build.build_native`.  Loading fails loudly when it is
+missing: there is no CPU fallback for the solver.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+__all__ = ["lib", "check", "BCError", "BatchSpec", "PlanOptions", "PlanInfo", "LIB_PATH"]
+
+# ---------------------------------------------------------------- constants (mirror the header)
+BC_OK = 0
+BC_ERR_INVALID = 1
+BC_ERR_CUDA = 2
+BC_ERR_NONFINITE = 3
+BC_ERR_CAPACITY = 4
+BC_ERR_TIMEOUT = 5
+BC_ERR_UNSUPPORTED = 6
+
+BC_M_IL = 1 << 0
+BC_M_KLEAK = 1 << 1
+BC_M_NA = 1 << 2
+BC_M_KDR = 1 << 3
+BC_M_CAL = 1 << 4
+BC_M_CAT = 1 << 5
+BC_M_HCN = 1 << 6
+BC_M_AHP = 1 << 7
+BC_M_CADET = 1 << 8
+BC_M_ALL = 0x1FF
+
+BC_NPARAM = 40
+BC_P_INVCM = 0
+BC_P_VREST = 1
+BC_P_ENA = 2
+BC_P_EK = 3
+BC_P_ECA = 4
+BC_P_IL_G = 5
+BC_P_IL_E = 6
+BC_P_KLEAK_G = 7
+BC_P_NA_G = 8
+BC_P_NA_VSH = 9
+BC_P_NA_PHI = 10
+BC_P_KDR_G = 11
+BC_P_KDR_VSH = 12
+BC_P_KDR_PHI = 13
+BC_P_CAL_G = 14
+BC_P_CAL_VSH = 15
+BC_P_CAL_PHIP = 16
+BC_P_CAL_PHIQ = 17
+BC_P_CAT_G = 18
+BC_P_CAT_VSH = 19
+BC_P_CAT_PHIP = 20
+BC_P_CAT_PHIQ = 21
+BC_P_HCN_G = 22
+BC_P_HCN_E = 23
+BC_P_HCN_PHI = 24
+BC_P_AHP_G = 25
+BC_P_AHP_N = 26
+BC_P_AHP_ALPHA = 27
+BC_P_AHP_BETA = 28
+BC_P_AHP_PHI = 29
+BC_P_CA_D = 30
+BC_P_CA_TAU = 31
+BC_P_CA_CREST = 32
+BC_P_CA_CO = 33
+BC_P_CA_TEMP = 34
+BC_P_CA_CI0 = 35
+
+BC_PREC_F32 = 0
+BC_PREC_F64 = 1
+
+BC_STATE_V = 0
+BC_STATE_NA_P = 1
+BC_STATE_NA_Q = 2
+BC_STATE_KDR_P = 3
+BC_STATE_CAL_P = 4
+BC_STATE_CAL_Q = 5
+BC_STATE_CAT_P = 6
+BC_STATE_CAT_Q = 7
+BC_STATE_HCN_P = 8
+BC_STATE_AHP_P = 9
+BC_STATE_CA_CI = 10
+BC_NSTATE_VIEW = 11
+
+STATE_NAMES = {
+    "V": BC_STATE_V,
+    "Na_p": BC_STATE_NA_P,
+    "Na_q": BC_STATE_NA_Q,
+    "KDR_p": BC_STATE_KDR_P,
+    "CaL_p": BC_STATE_CAL_P,
+    "CaL_q": BC_STATE_CAL_Q,
+    "CaT_p": BC_STATE_CAT_P,
+    "CaT_q": BC_STATE_CAT_Q,
+    "HCN_p": BC_STATE_HCN_P,
+    "AHP_p": BC_STATE_AHP_P,
+    "Ci": BC_STATE_CA_CI,
+}
+
+_p = C.POINTER
+
+
+class BatchSpec(C.Structure):
+    _fields_ = [
+        ("n_cells", C.c_int64),
+        ("n_branches", C.c_int64),
+        ("n_segments", C.c_int64),
+        ("n_regions", C.c_int32),
+        ("cell_branch_offsets", _p(C.c_int64)),
+        ("branch_parent", _p(C.c_int32)),
+        ("branch_parent_x", _p(C.c_double)),
+        ("branch_child_x", _p(C.c_double)),
+        ("branch_ncv", _p(C.c_int32)),
+        ("branch_region", _p(C.c_int32)),
+        ("branch_seg_offsets", _p(C.c_int64)),
+        ("seg_length", _p(C.c_double)),
+        ("seg_r_prox", _p(C.c_double)),
+        ("seg_r_dist", _p(C.c_double)),
+        ("region_cm", _p(C.c_double)),
+        ("region_ra", _p(C.c_double)),
+        ("region_mech", _p(C.c_uint32)),
+        ("region_params", _p(C.c_double)),
+        ("n_pulses", C.c_int64),
+        ("pulse_cell", _p(C.c_int32)),
+        ("pulse_branch", _p(C.c_int32)),
+        ("pulse_x", _p(C.c_double)),
+        ("pulse_t_on", _p(C.c_double)),
+        ("pulse_t_off", _p(C.c_double)),
+        ("pulse_amp", _p(C.c_double)),
+        ("n_probes", C.c_int64),
+        ("probe_cell", _p(C.c_int32)),
+        ("probe_branch", _p(C.c_int32)),
+        ("probe_x", _p(C.c_double)),
+    ]
+
+
+class PlanOptions(C.Structure):
+    _fields_ = [
+        ("precision", C.c_int32),
+        ("threads_per_tile", C.c_int32),
+        ("tile_nodes", C.c_int32),
+        ("thread_cell_max", C.c_int32),
+        ("steps_per_launch", C.c_int32),
+        ("record_every", C.c_int32),
+        ("max_spikes", C.c_int32),
+        ("use_graph", C.c_int32),
+        ("device", C.c_int32),
+        ("threads_big", C.c_int32),
+        ("threads_global", C.c_int32),
+        ("split_min", C.c_int32),
+        ("split_factor", C.c_float),
+        ("dry_run", C.c_int32),
+        ("reserved", C.c_int32 * 2),
+    ]
+
+
+class PlanInfo(C.Structure):
+    _fields_ = [
+        ("n_cells", C.c_int64),
+        ("n_cv", C.c_int64),
+        ("n_nodes", C.c_int64),
+        ("n_tiles", C.c_int64),
+        ("n_probes", C.c_int64),
+        ("n_pulses", C.c_int64),
+        ("threads_per_tile", C.c_int32),
+        ("tile_nodes", C.c_int32),
+        ("steps_per_launch", C.c_int32),
+        ("precision", C.c_int32),
+        ("smem_bytes_per_tile", C.c_int64),
+        ("device_bytes", C.c_int64),
+        ("max_phases", C.c_int64),
+        ("max_chain_nodes", C.c_int64),
+        ("state_slots", C.c_int32),
+        ("reserved", C.c_int32 * 7),
+    ]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_ if name != "reserved"}
+
+
+# Exported symbols and their ctypes signatures (kept in step with the header).
+SIGNATURES = {
+    "bc_last_error": (C.c_char_p, []),
+    "bc_version": (C.c_int32, []),
+    "bc_default_options": (None, [_p(PlanOptions)]),
+    "bc_plan_create": (C.c_int32, [_p(BatchSpec), _p(PlanOptions), _p(C.c_void_p)]),
+    "bc_plan_destroy": (C.c_int32, [C.c_void_p]),
+    "bc_plan_info": (C.c_int32, [C.c_void_p, _p(PlanInfo)]),
+    "bc_plan_cell_ncv": (C.c_int32, [C.c_void_p, _p(C.c_int64)]),
+    "bc_plan_tile_stats": (C.c_int32, [C.c_void_p, _p(C.c_int64)]),
+    "bc_reset": (C.c_int32, [C.c_void_p, C.c_void_p]),
+    "bc_run": (C.c_int32, [C.c_void_p, C.c_int64, C.c_double, C.c_void_p]),
+    "bc_run_async": (C.c_int32, [C.c_void_p, C.c_int64, C.c_double, C.c_void_p]),
+    "bc_check": (C.c_int32, [C.c_void_p, C.c_void_p]),
+    "bc_state_download": (C.c_int32, [C.c_void_p, C.c_int32, _p(C.c_double), C.c_void_p]),
+    "bc_state_upload": (C.c_int32, [C.c_void_p, C.c_int32, _p(C.c_double), C.c_void_p]),
+    "bc_probe_count": (C.c_int32, [C.c_void_p, _p(C.c_int64)]),
+    "bc_probe_download": (C.c_int32, [C.c_void_p, _p(C.c_double), C.c_int64, C.c_void_p]),
+    "bc_spike_download": (C.c_int32, [C.c_void_p, _p(C.c_int32), _p(C.c_double), C.c_void_p]),
+    "bc_probe_clear": (C.c_int32, [C.c_void_p, C.c_void_p]),
+    "bc_step_count": (C.c_int32, [C.c_void_p, _p(C.c_int64)]),
+    "bc_debug_phase_cycles": (C.c_int32, [C.c_void_p, _p(C.c_uint64), C.c_int32]),
+    "bc_run_timed": (C.c_int32, [C.c_void_p, C.c_int64, C.c_double, C.c_void_p, _p(C.c_double)]),
+}
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_native", "libbraincell_gb300.so")
+
+_lock = threading.Lock()
+_lib = None
+
+
+class BCError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"[bc status {status}] {message}")
+        self.status = status
+
+
+def lib():
+    """Load (once) and return the native library; raise if it was not built."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(
+                f"braincell_gb300 native library not found at {LIB_PATH}; build it with "
+                "`python -c 'import braincell_gb300.build as b; b.build_native()'`. "
+                "There is no CPU fallback for the GB300 solver."
+            )
+        handle = C.CDLL(LIB_PATH)
+        for name, (restype, argtypes) in SIGNATURES.items():
+            fn = getattr(handle, name)
+            fn.restype = restype
+            fn.argtypes = argtypes
+        _lib = handle
+        return _lib
+
+
+def check(status: int) -> None:
+    if status != BC_OK:
+        msg = lib().bc_last_error()
+        raise BCError(int(status), msg.decode() if msg else "unknown error")

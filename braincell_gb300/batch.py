@@ -1,0 +1,277 @@
+"""Flat, morphology-level description of a batch of cells (the ``bc_batch_spec`` payload).
+
+A :class:`CellBatch` is what crosses the C ABI: branches with their frustum
+segments and CV counts, per-cell region tables (cable + mechanism records),
+current-clamp segments and voltage probes.  Everything downstream of it --
+geometry, CVs, node tree, axial coefficients, scheduling -- is done natively by
+``bc_plan_create``.
+
+:func:`lower_cell` converts one declared :class:`~braincell_gb300.cell.Cell`
+(paint / place rules on a :class:`~braincell_gb300.morph.Morphology`) into a
+batch with ``pop_size`` identical replicas, mirroring how the reference lowers
+paint rules onto CVs (``_discretization/mechanism.py:514``) and place rules onto
+points (``_compute/layouts.py:171``).
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _abi
+from .catalogue import region_record
+from .mech import CableProperty, CurrentClamp, StateProbe
+
+__all__ = ["CellBatch", "lower_cell", "concat_batches"]
+
+
+def _ptr(a: np.ndarray, ctype):
+    return a.ctypes.data_as(C.POINTER(ctype))
+
+
+@dataclass
+class CellBatch:
+    n_regions: int
+    cell_branch_offsets: np.ndarray
+    branch_parent: np.ndarray
+    branch_parent_x: np.ndarray
+    branch_child_x: np.ndarray
+    branch_ncv: np.ndarray
+    branch_region: np.ndarray
+    branch_seg_offsets: np.ndarray
+    seg_length: np.ndarray
+    seg_r_prox: np.ndarray
+    seg_r_dist: np.ndarray
+    region_cm: np.ndarray
+    region_ra: np.ndarray
+    region_mech: np.ndarray
+    region_params: np.ndarray
+    pulse_cell: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
+    pulse_branch: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
+    pulse_x: np.ndarray = field(default_factory=lambda: np.zeros(0, np.float64))
+    pulse_t_on: np.ndarray = field(default_factory=lambda: np.zeros(0, np.float64))
+    pulse_t_off: np.ndarray = field(default_factory=lambda: np.zeros(0, np.float64))
+    pulse_amp: np.ndarray = field(default_factory=lambda: np.zeros(0, np.float64))
+    probe_cell: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
+    probe_branch: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
+    probe_x: np.ndarray = field(default_factory=lambda: np.zeros(0, np.float64))
+
+    _DTYPES = {
+        "cell_branch_offsets": np.int64,
+        "branch_parent": np.int32,
+        "branch_parent_x": np.float64,
+        "branch_child_x": np.float64,
+        "branch_ncv": np.int32,
+        "branch_region": np.int32,
+        "branch_seg_offsets": np.int64,
+        "seg_length": np.float64,
+        "seg_r_prox": np.float64,
+        "seg_r_dist": np.float64,
+        "region_cm": np.float64,
+        "region_ra": np.float64,
+        "region_mech": np.uint32,
+        "region_params": np.float64,
+        "pulse_cell": np.int32,
+        "pulse_branch": np.int32,
+        "pulse_x": np.float64,
+        "pulse_t_on": np.float64,
+        "pulse_t_off": np.float64,
+        "pulse_amp": np.float64,
+        "probe_cell": np.int32,
+        "probe_branch": np.int32,
+        "probe_x": np.float64,
+    }
+
+    def __post_init__(self) -> None:
+        for name, dt in self._DTYPES.items():
+            setattr(self, name, np.ascontiguousarray(getattr(self, name), dtype=dt))
+        self.region_params = self.region_params.reshape(-1, _abi.BC_NPARAM)
+        self.n_regions = int(self.n_regions)
+
+    # ------------------------------------------------------------------ sizes
+    @property
+    def n_cells(self) -> int:
+        return int(self.cell_branch_offsets.size - 1)
+
+    @property
+    def n_branches(self) -> int:
+        return int(self.branch_parent.size)
+
+    @property
+    def n_cv(self) -> int:
+        return int(self.branch_ncv.sum())
+
+    def cell_ncv(self) -> np.ndarray:
+        cs = np.concatenate([[0], np.cumsum(self.branch_ncv, dtype=np.int64)])
+        return cs[self.cell_branch_offsets[1:]] - cs[self.cell_branch_offsets[:-1]]
+
+    def cell_nbranch(self) -> np.ndarray:
+        return np.diff(self.cell_branch_offsets)
+
+    def validate(self) -> None:
+        nb = self.n_branches
+        if self.cell_branch_offsets[0] != 0 or self.cell_branch_offsets[-1] != nb:
+            raise ValueError("cell_branch_offsets must start at 0 and end at n_branches.")
+        if np.any(np.diff(self.cell_branch_offsets) <= 0):
+            raise ValueError("every cell needs at least one branch.")
+        if np.any(self.branch_ncv < 1):
+            raise ValueError("branch_ncv must be >= 1.")
+        if self.region_params.shape != (self.n_cells * self.n_regions, _abi.BC_NPARAM):
+            raise ValueError("region_params has the wrong shape.")
+
+    # ------------------------------------------------------------------ ABI
+    def to_spec(self) -> tuple[_abi.BatchSpec, tuple]:
+        """Return the ctypes spec plus the arrays it points into (keep them alive)."""
+        self.validate()
+        s = _abi.BatchSpec()
+        s.n_cells = self.n_cells
+        s.n_branches = self.n_branches
+        s.n_segments = int(self.seg_length.size)
+        s.n_regions = self.n_regions
+        keep = []
+        ctypes_of = {np.int64: C.c_int64, np.int32: C.c_int32, np.float64: C.c_double, np.uint32: C.c_uint32}
+        for name, dt in self._DTYPES.items():
+            arr = getattr(self, name)
+            keep.append(arr)
+            setattr(s, name, _ptr(arr, ctypes_of[dt]))
+        s.n_pulses = int(self.pulse_cell.size)
+        s.n_probes = int(self.probe_cell.size)
+        return s, tuple(keep)
+
+
+def concat_batches(batches: list[CellBatch]) -> CellBatch:
+    """Concatenate batches cell-wise (region tables padded to the widest)."""
+    if not batches:
+        raise ValueError("concat_batches needs at least one batch.")
+    R = max(b.n_regions for b in batches)
+    parts: dict[str, list] = {k: [] for k in CellBatch._DTYPES}
+    br_off = 0
+    seg_off = 0
+    cell_off = 0
+    for b in batches:
+        parts["cell_branch_offsets"].append(b.cell_branch_offsets[(1 if br_off or cell_off else 0):] + br_off)
+        parts["branch_seg_offsets"].append(b.branch_seg_offsets[(1 if seg_off or cell_off else 0):] + seg_off)
+        for k in ("branch_parent", "branch_parent_x", "branch_child_x", "branch_ncv", "branch_region",
+                  "seg_length", "seg_r_prox", "seg_r_dist"):
+            parts[k].append(getattr(b, k))
+        nc = b.n_cells
+        pad = R - b.n_regions
+        for k in ("region_cm", "region_ra", "region_mech"):
+            a = getattr(b, k).reshape(nc, b.n_regions)
+            if pad:
+                a = np.concatenate([a, np.repeat(a[:, :1], pad, axis=1)], axis=1)
+            parts[k].append(a.reshape(-1))
+        a = b.region_params.reshape(nc, b.n_regions, _abi.BC_NPARAM)
+        if pad:
+            a = np.concatenate([a, np.repeat(a[:, :1], pad, axis=1)], axis=1)
+        parts["region_params"].append(a.reshape(-1, _abi.BC_NPARAM))
+        parts["pulse_cell"].append(b.pulse_cell + cell_off)
+        parts["probe_cell"].append(b.probe_cell + cell_off)
+        for k in ("pulse_branch", "pulse_x", "pulse_t_on", "pulse_t_off", "pulse_amp", "probe_branch", "probe_x"):
+            parts[k].append(getattr(b, k))
+        br_off += b.n_branches
+        seg_off += int(b.seg_length.size)
+        cell_off += nc
+    kw = {k: np.concatenate(v) for k, v in parts.items()}
+    return CellBatch(n_regions=R, **kw)
+
+
+def _branch_regions(cell) -> tuple[np.ndarray, list[tuple[CableProperty, list]]]:
+    """Resolve paint rules to one (cable, mechanisms) region per branch."""
+    morpho = cell.morpho
+    nb = len(morpho.branches)
+    cables: list[CableProperty] = [CableProperty() for _ in range(nb)]
+    mechs: list[list] = [[] for _ in range(nb)]
+    for region, decls in cell.paint_rules:
+        mask = region.branch_mask(morpho)
+        for d in decls:
+            for b in np.nonzero(mask)[0]:
+                if isinstance(d, CableProperty):
+                    cables[b] = d
+                else:
+                    mechs[b].append(d)
+    keys: dict = {}
+    regions: list[tuple[CableProperty, list]] = []
+    branch_region = np.zeros(nb, dtype=np.int32)
+    for b in range(nb):
+        key = (cables[b], tuple((type(m).__name__, m.class_name, tuple(sorted(m.params.items()))) for m in mechs[b]))
+        if key not in keys:
+            keys[key] = len(regions)
+            regions.append((cables[b], mechs[b]))
+        branch_region[b] = keys[key]
+    return branch_region, regions
+
+
+def lower_cell(cell, replicas: int | None = None) -> CellBatch:
+    """Lower a declared Cell into a batch of ``replicas`` (default ``pop_size``) copies."""
+    morpho = cell.morpho
+    P = int(np.prod(cell.pop_size)) if replicas is None else int(replicas)
+    nb = len(morpho.branches)
+    parent = morpho.parent_index
+    parent_x = np.zeros(nb)
+    child_x = np.zeros(nb)
+    for e in morpho.edges:
+        parent_x[e.child.index] = e.parent_x
+        child_x[e.child.index] = e.child_x
+    ncv = np.asarray(cell.cv_policy.cv_counts(morpho), dtype=np.int32)
+    seg_len, seg_rp, seg_rd, seg_off = [], [], [], [0]
+    for br in morpho.branches:
+        seg_len.append(br.lengths)
+        seg_rp.append(br.radii_proximal)
+        seg_rd.append(br.radii_distal)
+        seg_off.append(seg_off[-1] + br.n_segments)
+    branch_region, regions = _branch_regions(cell)
+    R = len(regions)
+    cm = np.zeros(R)
+    ra = np.zeros(R)
+    bits = np.zeros(R, dtype=np.uint32)
+    params = np.zeros((R, _abi.BC_NPARAM))
+    for r, (cable, mechs) in enumerate(regions):
+        bits[r], params[r] = region_record(mechs, cable)
+        cm[r] = cable.membrane_capacitance
+        ra[r] = cable.axial_resistivity
+        if cell.V_init is not None:
+            params[r, _abi.BC_P_VREST] = float(cell.V_init)
+    pulses: list[tuple[int, float, float, float, float]] = []
+    probes: list[tuple[int, float]] = []
+    for locset, decls in cell.place_rules:
+        for (b, x) in locset.points(morpho):
+            for d in decls:
+                if isinstance(d, CurrentClamp):
+                    for (t_on, t_off, amp) in d.segments():
+                        pulses.append((b, x, t_on, t_off, amp))
+                elif isinstance(d, StateProbe):
+                    probes.append((b, x))
+                else:
+                    raise TypeError(f"Unsupported point mechanism {type(d).__name__}.")
+    one = CellBatch(
+        n_regions=R,
+        cell_branch_offsets=np.asarray([0, nb]),
+        branch_parent=parent,
+        branch_parent_x=parent_x,
+        branch_child_x=child_x,
+        branch_ncv=ncv,
+        branch_region=branch_region,
+        branch_seg_offsets=np.asarray(seg_off),
+        seg_length=np.concatenate(seg_len),
+        seg_r_prox=np.concatenate(seg_rp),
+        seg_r_dist=np.concatenate(seg_rd),
+        region_cm=cm,
+        region_ra=ra,
+        region_mech=bits,
+        region_params=params,
+        pulse_cell=np.zeros(len(pulses), np.int32),
+        pulse_branch=np.asarray([p[0] for p in pulses], np.int32),
+        pulse_x=np.asarray([p[1] for p in pulses]),
+        pulse_t_on=np.asarray([p[2] for p in pulses]),
+        pulse_t_off=np.asarray([p[3] for p in pulses]),
+        pulse_amp=np.asarray([p[4] for p in pulses]),
+        probe_cell=np.zeros(len(probes), np.int32),
+        probe_branch=np.asarray([p[0] for p in probes], np.int32),
+        probe_x=np.asarray([p[1] for p in probes]),
+    )
+    if P == 1:
+        return one
+    return concat_batches([one] * P)

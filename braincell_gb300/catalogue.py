@@ -1,0 +1,152 @@
+"""Mechanism catalogue: declaration -> per-region parameter record.
+
+Every class name, parameter name and default below is the reference's:
+
+* ``IL``          -- channel/leaky.py:144   (g_max 0.1 mS/cm^2, E -70 mV)
+* ``K_Leak``      -- channel/potassium.py:1167 (g_max 0.005 mS/cm^2, E = E_K)
+* ``Na_Ba2002``   -- channel/sodium.py:59   (g_max 90, q10 3, temp = temp_ref = 36 degC, V_sh -50)
+* ``KDR_Ba2002``  -- channel/potassium.py:95 (g_max 10, q10 3, temp = temp_ref = 36 degC, V_sh -50)
+* ``CaL_IS2008``  -- channel/calcium.py:790 (g_max 1, q10_p 3.55, q10_q 3, temp_ref 24 degC, V_sh 0)
+* ``CaT_HM1992``  -- channel/calcium.py:222 (g_max 2, q10_p 3.55, q10_q 3, temp_ref 24 degC, V_sh -3)
+* ``HCN_HM1992``  -- channel/hyperpolarization_activated.py:45 (g_max 10, E +43 mV, q10 1)
+* ``AHP_De1994``  -- channel/potassium_calcium.py:78 (n 2, g_max 10, alpha 48, beta 0.09, phi 1)
+* ions: ``SodiumFixed`` E 50 (ion/sodium.py:149), ``PotassiumFixed`` E -95
+  (ion/potassium.py:151), ``CalciumFixed`` E 120 (ion/calcium.py:187) -- the
+  defaults used when no ion is painted (_compute/ions.py:107-113);
+  ``CalciumDetailed`` (ion/calcium.py:286: temp 36 degC, d 1 um, tau 5 ms,
+  C_rest 2.4e-4 mM, Co 2 mM, Ci0 2.4e-4 mM).
+
+The gate temperature factor is ``phi = q10 ** ((temp - temp_ref) / 10 K)``
+(channel/_base.py:517-532).
+"""
+
+from __future__ import annotations
+
+import numpy as np
+
+from . import _abi
+from .mech import CableProperty, Channel, Ion, celsius2kelvin
+
+__all__ = ["CHANNELS", "IONS", "region_record", "q10_phi"]
+
+T36 = celsius2kelvin(36.0)
+T24 = celsius2kelvin(24.0)
+
+CHANNELS: dict[str, dict[str, float]] = {
+    "IL": {"g_max": 0.1, "E": -70.0},
+    "K_Leak": {"g_max": 0.005},
+    "Na_Ba2002": {"g_max": 90.0, "temp": T36, "q10": 3.0, "temp_ref": T36, "V_sh": -50.0},
+    "KDR_Ba2002": {"g_max": 10.0, "temp": T36, "q10": 3.0, "temp_ref": T36, "V_sh": -50.0},
+    "CaL_IS2008": {
+        "g_max": 1.0, "temp": T36, "q10_p": 3.55, "temp_ref_p": T24, "q10_q": 3.0, "temp_ref_q": T24, "V_sh": 0.0,
+    },
+    "CaT_HM1992": {
+        "g_max": 2.0, "temp": T36, "q10_p": 3.55, "temp_ref_p": T24, "q10_q": 3.0, "temp_ref_q": T24, "V_sh": -3.0,
+    },
+    "HCN_HM1992": {"g_max": 10.0, "E": 43.0, "temp": T36, "q10": 1.0, "temp_ref": T36},
+    "AHP_De1994": {"n": 2.0, "g_max": 10.0, "alpha": 48.0, "beta": 0.09, "phi": 1.0},
+}
+_ALIASES = {"leaky": "IL"}
+
+IONS: dict[str, dict[str, float]] = {
+    "SodiumFixed": {"E": 50.0},
+    "PotassiumFixed": {"E": -95.0},
+    "CalciumFixed": {"E": 120.0},
+    "CalciumDetailed": {
+        "temp": T36, "d": 1.0, "tau": 5.0, "C_rest": 2.4e-4, "Co": 2.0, "Ci_initializer": 2.4e-4,
+    },
+}
+
+
+def q10_phi(q10: float, temp: float, temp_ref: float) -> float:
+    return float(q10) ** ((float(temp) - float(temp_ref)) / 10.0)
+
+
+def _params(table: dict, name: str, decl) -> dict[str, float]:
+    out = dict(table[name])
+    for k, v in decl.params.items():
+        if k not in out:
+            raise ValueError(f"{name} has no parameter {k!r}; known: {sorted(out)}.")
+        out[k] = float(v)
+    return out
+
+
+def region_record(mechs, cable: CableProperty) -> tuple[int, np.ndarray]:
+    """Return ``(mechanism_bits, params[BC_NPARAM])`` for one region.
+
+    ``mechs`` is the ordered list of Channel / Ion declarations painted on the
+    region; a later declaration of the same class replaces an earlier one.
+    """
+    rec = np.zeros(_abi.BC_NPARAM, dtype=np.float64)
+    rec[_abi.BC_P_INVCM] = 1.0 / float(cable.membrane_capacitance)
+    rec[_abi.BC_P_VREST] = float(cable.resting_potential)
+    rec[_abi.BC_P_ENA] = IONS["SodiumFixed"]["E"]
+    rec[_abi.BC_P_EK] = IONS["PotassiumFixed"]["E"]
+    rec[_abi.BC_P_ECA] = IONS["CalciumFixed"]["E"]
+    bits = 0
+    last: dict[str, object] = {}
+    for m in mechs:
+        last[m.class_name if m.class_name not in _ALIASES else _ALIASES[m.class_name]] = m
+    for name, decl in last.items():
+        if isinstance(decl, Ion):
+            if name not in IONS:
+                raise ValueError(f"Unsupported ion class {name!r}; supported: {sorted(IONS)}.")
+            p = _params(IONS, name, decl)
+            if name == "SodiumFixed":
+                rec[_abi.BC_P_ENA] = p["E"]
+            elif name == "PotassiumFixed":
+                rec[_abi.BC_P_EK] = p["E"]
+            elif name == "CalciumFixed":
+                rec[_abi.BC_P_ECA] = p["E"]
+            else:
+                bits |= _abi.BC_M_CADET
+                rec[_abi.BC_P_CA_D] = p["d"]
+                rec[_abi.BC_P_CA_TAU] = p["tau"]
+                rec[_abi.BC_P_CA_CREST] = p["C_rest"]
+                rec[_abi.BC_P_CA_CO] = p["Co"]
+                rec[_abi.BC_P_CA_TEMP] = p["temp"]
+                rec[_abi.BC_P_CA_CI0] = p["Ci_initializer"]
+            continue
+        if not isinstance(decl, Channel):
+            raise TypeError(f"Expected Channel or Ion declaration, got {type(decl).__name__}.")
+        if name not in CHANNELS:
+            raise ValueError(f"Unsupported channel class {name!r}; supported: {sorted(CHANNELS)}.")
+        p = _params(CHANNELS, name, decl)
+        if name == "IL":
+            bits |= _abi.BC_M_IL
+            rec[_abi.BC_P_IL_G], rec[_abi.BC_P_IL_E] = p["g_max"], p["E"]
+        elif name == "K_Leak":
+            bits |= _abi.BC_M_KLEAK
+            rec[_abi.BC_P_KLEAK_G] = p["g_max"]
+        elif name == "Na_Ba2002":
+            bits |= _abi.BC_M_NA
+            rec[_abi.BC_P_NA_G], rec[_abi.BC_P_NA_VSH] = p["g_max"], p["V_sh"]
+            rec[_abi.BC_P_NA_PHI] = q10_phi(p["q10"], p["temp"], p["temp_ref"])
+        elif name == "KDR_Ba2002":
+            bits |= _abi.BC_M_KDR
+            rec[_abi.BC_P_KDR_G], rec[_abi.BC_P_KDR_VSH] = p["g_max"], p["V_sh"]
+            rec[_abi.BC_P_KDR_PHI] = q10_phi(p["q10"], p["temp"], p["temp_ref"])
+        elif name == "CaL_IS2008":
+            bits |= _abi.BC_M_CAL
+            rec[_abi.BC_P_CAL_G], rec[_abi.BC_P_CAL_VSH] = p["g_max"], p["V_sh"]
+            rec[_abi.BC_P_CAL_PHIP] = q10_phi(p["q10_p"], p["temp"], p["temp_ref_p"])
+            rec[_abi.BC_P_CAL_PHIQ] = q10_phi(p["q10_q"], p["temp"], p["temp_ref_q"])
+        elif name == "CaT_HM1992":
+            bits |= _abi.BC_M_CAT
+            rec[_abi.BC_P_CAT_G], rec[_abi.BC_P_CAT_VSH] = p["g_max"], p["V_sh"]
+            rec[_abi.BC_P_CAT_PHIP] = q10_phi(p["q10_p"], p["temp"], p["temp_ref_p"])
+            rec[_abi.BC_P_CAT_PHIQ] = q10_phi(p["q10_q"], p["temp"], p["temp_ref_q"])
+        elif name == "HCN_HM1992":
+            bits |= _abi.BC_M_HCN
+            rec[_abi.BC_P_HCN_G], rec[_abi.BC_P_HCN_E] = p["g_max"], p["E"]
+            rec[_abi.BC_P_HCN_PHI] = q10_phi(p["q10"], p["temp"], p["temp_ref"])
+        elif name == "AHP_De1994":
+            bits |= _abi.BC_M_AHP
+            rec[_abi.BC_P_AHP_G], rec[_abi.BC_P_AHP_N] = p["g_max"], p["n"]
+            rec[_abi.BC_P_AHP_ALPHA], rec[_abi.BC_P_AHP_BETA] = p["alpha"], p["beta"]
+            rec[_abi.BC_P_AHP_PHI] = p["phi"]
+    if bits & (_abi.BC_M_AHP) and not bits & _abi.BC_M_CADET:
+        # AHP reads Ci from the calcium ion; with a fixed Ca ion Ci is the class default.
+        rec[_abi.BC_P_CA_CI0] = 5e-5
+        rec[_abi.BC_P_CA_CREST] = 5e-5
+    return bits, rec

@@ -1,0 +1,149 @@
+// Internal structures shared by the host planner (bc_plan.cpp, bc_lower.cpp) and
+// the device code (bc_kernels.cu).  Not part of the public ABI.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/braincell_gb300.h"
+
+namespace bc {
+
+// ----------------------------------------------------------------- errors
+void set_error(const std::string& msg);
+bc_status fail(bc_status code, const std::string& msg);
+
+// ----------------------------------------------------------------- lowering
+// One cell lowered to its point tree (node numbering as the reference's
+// build_node_tree_from_cvs: root endpoint = 0, then per branch its CV
+// midpoints in walk order followed by its terminal endpoint).
+struct LoweredCell {
+  int32_t n_cv = 0;
+  int32_t n_node = 0;
+  std::vector<int32_t> parent;   // [n_node] parent node, -1 root
+  std::vector<double> alpha;     // [n_node] g_e / C_self    (ms^-1), 0 for root
+  std::vector<double> beta;      // [n_node] g_e / C_parent  (ms^-1), 0 for root
+  std::vector<double> diag;      // [n_node] sum of axial coefficients of the row (ms^-1)
+  std::vector<int32_t> region;   // [n_node] region id, -1 for boundary (algebraic) rows
+  std::vector<int32_t> cv_node;  // [n_cv]  midpoint node of each CV (reference CV order)
+  std::vector<double> cv_area;   // [n_cv]  um^2
+  std::vector<double> node_vrest;// [n_node] initial voltage
+};
+
+// Lower cell `c` of the batch.  Returns BC_OK or an error (message set).
+bc_status lower_cell(const bc_batch_spec& spec, int64_t c, LoweredCell& out);
+
+// Locate the node selected by (branch, x) in a lowered cell (midpoint of the
+// owning CV for interior x, the branch endpoint node for x = 0 / 1).
+int32_t locate_node(const bc_batch_spec& spec, int64_t c, const LoweredCell& lc, int32_t branch, double x);
+
+// ----------------------------------------------------------------- device records
+// Chain of nodes walked by one thread: nodes [start, start+count) of the tile,
+// bottom (deepest) first; node start+k+1 is the parent of node start+k.
+// A chain record (32 bytes, read as two 16-byte vectors).
+// kind = kChainRegular: a whole chain.  Its bottom pulls the contributions that its
+//   n_child child chains left in the consecutive slots aux .. aux + n_child.
+// kind = kChainSegment: one piece of a long chain split for parallel elimination.
+//   The lowest segment pulls children like a regular chain (aux = slot base); a
+//   higher one has aux = the top node of the segment below (its "outside" node).
+//   Its fill-in results (dd, dr, H) go to slot `slot`.
+// kind = kChainReduced: the reduced system joining the segments whose record ids
+//   are listed (bottom to top) in child[aux .. aux + n_child).
+// slot: where this record leaves its contribution to the parent junction
+//   (-1 at a root); `first` marks the lowest segment.
+struct ChainRec {
+  int32_t start;
+  int32_t count;
+  int32_t top_parent;   // tile node that is the parent of the top node, -1 at a root
+  int32_t aux;
+  int32_t n_child;
+  int32_t kind;
+  int32_t slot;
+  int32_t first;
+};
+constexpr int32_t kChainRegular = 0;
+constexpr int32_t kChainSegment = 1;
+constexpr int32_t kChainReduced = 2;
+
+// Per-tile descriptor (global memory, read-only).
+struct TileDesc {
+  int64_t blob_offset;      // bytes into the plan's blob buffer (16-B aligned)
+  int32_t blob_bytes;       // total bytes of the tile blob (dynamic + static)
+  int32_t dyn_bytes;        // leading bytes written back (V, states)
+  int32_t n_nodes;          // N (padded node count used for array strides)
+  int32_t n_real_nodes;     // nodes actually used
+  int32_t n_chains;
+  int32_t n_phases;
+  int32_t n_params;         // param records in this tile
+  int32_t n_pulses;
+  int64_t pulse_offset;     // into plan pulse array
+  int32_t n_probes;
+  int32_t pad0;
+  int64_t probe_offset;     // into plan probe array
+  // byte offsets inside the blob
+  int32_t off_vhi, off_vlo;
+  int64_t state_offset;     // elements into the plan's global mechanism-state array ([slot][n_nodes])
+  int32_t off_alpha, off_beta, off_diag0, off_pidx, off_spec, off_specs;
+  int32_t off_chains, off_child, off_lists, off_params, off_mech;
+  int32_t scratch_bytes;    // diag/rhs/cD/cR scratch (shared memory after the blob)
+  int32_t off_sdiag, off_srhs, off_scd, off_scr, off_sfill, off_sh;  // offsets inside the scratch area
+  int32_t n_slots;          // contribution slots (scd / scr / sh entries)
+  int32_t pad1;
+  int64_t scratch_offset;   // bytes into the plan's global scratch (global-resident tiles)
+};
+
+struct PulseRec {
+  int32_t node;      // tile-local node
+  int32_t is_mid;    // 1: density term (rhs += dt*invcm*amp), 0: boundary row (rhs += dt*amp)
+  int64_t on_step;   // active for on_step <= step < off_step
+  int64_t off_step;
+  double amp;        // midpoint: uA/cm^2 (nA * 1e5 / area_um2); boundary: nA * 1e-3 (mV/ms per uF)
+  double t_on, t_off;
+};
+
+// A node with clamp pulses and/or a probe: its pulses are pulse_begin .. pulse_end
+// of the tile's pulse list (sorted by node), its probe id is `probe` (-1: none).
+struct SpecRec {
+  int32_t pulse_begin;
+  int32_t pulse_end;
+  int32_t probe;
+  int32_t pad;
+};
+
+// Kernel launch parameters (by value).
+struct LaunchArgs {
+  const TileDesc* tiles;
+  int32_t n_tiles;
+  unsigned char* blob;        // plan blob buffer
+  unsigned char* scratch;     // global scratch (global-resident tiles)
+  void* state;                // mechanism states, [slot][node] per tile (Real)
+  const PulseRec* pulses;
+  double* traces;             // [trace_cap][n_probes_total], record-major
+  int64_t trace_cap;          // records that fit
+  int64_t trace_base;         // step count at the last probe clear
+  int64_t n_probes_total;
+  int32_t record_every;
+  int32_t max_spikes;
+  int32_t* spike_count;       // [n_probes]
+  double* spike_times;        // [n_probes * max_spikes]
+  int32_t* status;            // device status word (BC_* codes, OR-ed bits)
+  int64_t step0;              // global index of the first step of this launch
+  int32_t n_steps;
+  int32_t state_slots;
+  double dt;
+  unsigned long long* timers;  // [4] cycle sums (elimination, back-sub, update, other); phase-timer builds only
+};
+
+// Host-callable launchers implemented in bc_kernels.cu.
+int launch_tiles(const LaunchArgs& a, int precision, bool smem, int threads, size_t smem_bytes, void* stream);
+int launch_reset_impl(const LaunchArgs& a, int precision, int threads, const double* vinit, const int64_t* voff,
+                      void* stream);
+// View offsets: byte offsets into the blob, or kStateTag + byte offset into the state array.
+constexpr int64_t kStateTag = int64_t(1) << 62;
+int launch_view_impl(unsigned char* blob, unsigned char* state, int precision, const int64_t* off_hi,
+                     const int64_t* off_lo, double* view, int64_t n, bool write, void* stream);
+
+
+}  // namespace bc

@@ -1,0 +1,154 @@
+// Per-compartment mechanism arithmetic (device).  Rate functions and state
+// equations are the reference's:
+//   HH template      channel/_base.py:575-588 (alpha/beta or inf/tau derivative),
+//                    :550-558 (gate product), :658-674 (ohmic current)
+//   exp-Euler        quad/_exp_euler.py:461-465  y += dt * exprel(dt * lambda) * f
+//   Na_Ba2002        channel/sodium.py:154-170
+//   KDR_Ba2002       channel/potassium.py:206-214
+//   CaL_IS2008       channel/calcium.py:(CaL f_p_inf .. f_q_tau)
+//   CaT_HM1992       channel/calcium.py:(CaT f_p_inf .. f_q_tau)
+//   HCN_HM1992       channel/hyperpolarization_activated.py:126-133
+//   AHP_De1994       channel/potassium_calcium.py:181-186
+//   CalciumDetailed  ion/calcium.py:499-505, Nernst E: ion/_base.py:463-469
+// CUDA's own exp / expm1 / log are called; nothing of the math library is
+// re-implemented here.
+#pragma once
+
+#include <cstdint>
+
+#include "../../include/braincell_gb300.h"
+
+namespace bc {
+
+// Accurate functions (both precisions): used where FP32 rounding matters
+// (exp-Euler decay factors, exprel near its removable singularity, Nernst log).
+__device__ __forceinline__ float dexpm1(float x) { return expm1f(x); }
+__device__ __forceinline__ double dexpm1(double x) { return expm1(x); }
+__device__ __forceinline__ float dlog(float x) { return logf(x); }
+__device__ __forceinline__ double dlog(double x) { return log(x); }
+__device__ __forceinline__ float dpow(float x, float y) { return powf(x, y); }
+__device__ __forceinline__ double dpow(double x, double y) { return pow(x, y); }
+// Rate-function arithmetic: FP32 uses the hardware approximations (__expf,
+// __fdividef: a few ulp, far below what the rates need); FP64 stays exact so the
+// FP64 build remains an oracle-grade run of the same kernels.
+__device__ __forceinline__ float rexp(float x) { return __expf(x); }
+__device__ __forceinline__ double rexp(double x) { return exp(x); }
+__device__ __forceinline__ float rdiv(float a, float b) { return __fdividef(a, b); }
+__device__ __forceinline__ double rdiv(double a, double b) { return a / b; }
+
+// e^x - 1 for the exp-Euler decay of a gate (x = dt * lambda <= 0).  FP32: for
+// |x| < 1/4 the Taylor series of e^x - 1 to x^6 (truncation < 5e-8 relative, the
+// float rounding level); otherwise __expf(x) - 1, which has no cancellation there.
+// FP64: expm1.
+__device__ __forceinline__ float decay_em1(float x) {
+  const float p = x * (1.0f + x * (0.5f + x * (1.0f / 6.0f + x * (1.0f / 24.0f + x * (1.0f / 120.0f + x * (1.0f / 720.0f))))));
+  return fabsf(x) < 0.25f ? p : __expf(x) - 1.0f;
+}
+__device__ __forceinline__ double decay_em1(double x) { return expm1(x); }
+
+// exprel(x) = (e^x - 1) / x, exprel(0) = 1
+template <typename Real>
+__device__ __forceinline__ Real exprel(Real x) {
+  return x == Real(0) ? Real(1) : dexpm1(x) / x;
+}
+
+// One exp-Euler step y += dt * exprel(dt * lam) * f of a gate whose right-hand
+// side is affine in the gate: with lam = -phi (a + b) and f = -lam (x_inf - x) the
+// step is x - expm1(dt * lam) * (x_inf - x).
+template <typename Real>
+__device__ __forceinline__ Real gate_ab(Real x, Real a, Real b, Real phi, Real dt) {
+  const Real s = a + b;
+  const Real xinf = rdiv(a, s);
+  return x - decay_em1(-dt * phi * s) * (xinf - x);
+}
+
+// Same step for a gate in inf/tau form: lam = -phi / tau, f = phi (inf - x) / tau.
+template <typename Real>
+__device__ __forceinline__ Real gate_it(Real x, Real inf, Real tau, Real phi, Real dt) {
+  return x - decay_em1(-rdiv(dt * phi, tau)) * (inf - x);
+}
+
+template <typename Real>
+struct NaRates {
+  Real ap, bp, aq, bq;
+  __device__ __forceinline__ NaRates(Real v, Real vsh) {
+    const Real vp = v - vsh;
+    ap = Real(0.32 * 4.0) / exprel(-(vp - Real(13)) * Real(1.0 / 4));
+    bp = Real(0.28 * 5.0) / exprel((vp - Real(40)) * Real(1.0 / 5));
+    aq = Real(0.128) * rexp(-(vp - Real(17)) * Real(1.0 / 18));
+    bq = rdiv(Real(4), Real(1) + rexp(-(vp - Real(40)) * Real(1.0 / 5)));
+  }
+};
+
+template <typename Real>
+struct KdrRates {
+  Real a, b;
+  __device__ __forceinline__ KdrRates(Real v, Real vsh) {
+    const Real vp = v - vsh;
+    a = Real(0.032 * 5.0) / exprel(-(vp - Real(15)) * Real(1.0 / 5));
+    b = Real(0.5) * rexp(-(vp - Real(10)) * Real(1.0 / 40));
+  }
+};
+
+// 1 / (e^-y + e^y) = z / (1 + z^2) with z = e^y
+template <typename Real>
+__device__ __forceinline__ Real inv_cosh2(Real y) {
+  const Real z = rexp(y);
+  return rdiv(z, Real(1) + z * z);
+}
+
+template <typename Real>
+struct CaLRates {
+  Real pinf, ptau, qinf, qtau;
+  __device__ __forceinline__ CaLRates(Real v, Real vsh) {
+    const Real vs = v - vsh;
+    pinf = rdiv(Real(1), Real(1) + rexp(-(vs + Real(10)) * Real(1.0 / 4)));
+    ptau = Real(0.4) + Real(0.7) * inv_cosh2((vs + Real(5)) * Real(1.0 / 15));
+    qinf = rdiv(Real(1), Real(1) + rexp((vs + Real(25)) * Real(1.0 / 2)));
+    qtau = Real(300) + Real(100) * inv_cosh2((vs + Real(40)) * Real(1.0 / 9.5));
+  }
+};
+
+template <typename Real>
+struct CaTRates {
+  Real pinf, ptau, qinf, qtau;
+  __device__ __forceinline__ CaTRates(Real v, Real vsh) {
+    const Real vs = v - vsh;
+    pinf = rdiv(Real(1), Real(1) + rexp(-(vs + Real(59)) * Real(1.0 / 6.2)));
+    ptau = rdiv(Real(1), rexp(-(vs + Real(132)) * Real(1.0 / 16.7)) + rexp((vs + Real(16.8)) * Real(1.0 / 18.2))) + Real(0.612);
+    qinf = rdiv(Real(1), Real(1) + rexp((vs + Real(83)) * Real(1.0 / 4)));
+    qtau = vs >= Real(-80) ? rexp(-(vs + Real(22)) * Real(1.0 / 10.5)) + Real(28) : rexp((vs + Real(467)) * Real(1.0 / 66.6));
+  }
+};
+
+template <typename Real>
+struct HcnRates {
+  Real pinf, ptau;
+  __device__ __forceinline__ HcnRates(Real v) {
+    pinf = rdiv(Real(1), Real(1) + rexp((v + Real(75)) * Real(1.0 / 5.5)));
+    ptau = rdiv(Real(1), rexp(Real(-0.086) * v - Real(14.59)) + rexp(Real(0.0701) * v - Real(1.87)));
+  }
+};
+
+// Fixed state slot of every mechanism state in the [slot][node] state array.
+constexpr int kSlotNaP = 0;
+constexpr int kSlotNaQ = 1;
+constexpr int kSlotKdrP = 2;
+constexpr int kSlotCalP = 3;
+constexpr int kSlotCalQ = 4;
+constexpr int kSlotCatP = 5;
+constexpr int kSlotCatQ = 6;
+constexpr int kSlotHcnP = 7;
+constexpr int kSlotAhpP = 8;
+constexpr int kSlotCaHi = 9;   // CalciumDetailed Ci, float-float high word
+constexpr int kSlotCaLo = 10;  // low word
+constexpr int kNumSlots = 11;
+
+constexpr double kFaraday = 96485.33212;   // C/mol
+constexpr double kGasR = 8.314462618;      // J/(mol K)
+// 1e3 * R / (2 F): Nernst slope for z = 2 in mV/K
+constexpr double kNernstCa = 1e3 * kGasR / (2.0 * kFaraday);
+// uA/cm^2 -> mM/ms influx per um of shell depth: 10 / (2 F)
+constexpr double kCaDrive = 10.0 / (2.0 * kFaraday);
+
+}  // namespace bc

@@ -1,0 +1,1316 @@
+// Planner and C ABI of the GB300 Cell step.
+//
+// bc_plan_create lowers every cell (bc_lower.cpp), decomposes each point tree
+// into chains (maximal single-child paths), assigns chains to threads in
+// barrier-separated phases (chain level = 1 + max level of the chains hanging
+// below its bottom node; longest-processing-time assignment within a phase),
+// packs cells into shared-memory tiles by first-fit-decreasing on node count,
+// lays each tile out as one contiguous 16-byte-aligned blob and uploads it.
+// Small cells can be walked whole by one thread ("thread-per-cell"), larger ones
+// are split into chains over threads ("branch-parallel"); the switch point is
+// bc_plan_options::thread_cell_max.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <queue>
+#include <string>
+#include <vector>
+
+#include "bc_internal.h"
+#include "bc_mech.cuh"
+
+namespace bc {
+
+static thread_local std::string g_error = "";
+
+void set_error(const std::string& msg) { g_error = msg; }
+
+bc_status fail(bc_status code, const std::string& msg) {
+  g_error = msg;
+  return code;
+}
+
+#define BC_CUDA(call)                                                                     \
+  do {                                                                                    \
+    cudaError_t e_ = (call);                                                              \
+    if (e_ != cudaSuccess)                                                                \
+      return fail(BC_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));       \
+  } while (0)
+
+static size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
+
+struct CellSched;
+
+}  // namespace bc
+
+struct LaunchClass {
+  int first = 0, count = 0, threads = 256;
+  bool smem = true;
+  size_t smem_bytes = 0;
+};
+
+struct bc_plan {
+  std::vector<LaunchClass> classes;
+  int precision = BC_PREC_F32;
+  int device = 0;
+  int threads = 128;
+  int threads_global = 512;
+  int tile_nodes = 0;
+  int thread_cell_max = 0;
+  int steps_per_launch = 1000;
+  int record_every = 1;
+  int max_spikes = 64;
+  int use_graph = 0;
+  int state_slots = 1;
+  int64_t n_cells = 0, n_cv = 0, n_nodes = 0, n_probes = 0, n_pulses = 0;
+  int64_t max_phases = 0, max_chain_nodes = 0;
+  size_t real_size = 4;
+  std::vector<bc::TileDesc> tiles;  // smem tiles first, then global tiles
+  int n_smem_tiles = 0;
+  size_t smem_bytes = 0;
+  std::vector<int64_t> cell_ncv;
+  std::vector<int32_t> cv_tile, cv_node;
+  std::vector<uint32_t> cv_mech;
+  std::vector<bc::PulseRec> pulses;
+  double pulses_dt = -1.0;
+  std::vector<double> probe_vrest;
+  // device buffers
+  unsigned char* d_blob = nullptr;
+  size_t blob_bytes = 0;
+  unsigned char* d_scratch = nullptr;
+  size_t scratch_bytes = 0;
+  unsigned char* d_state = nullptr;
+  size_t state_bytes = 0;
+  bc::TileDesc* d_tiles = nullptr;
+  bc::PulseRec* d_pulses = nullptr;
+  double* d_vinit = nullptr;
+  int64_t* d_vinit_off = nullptr;
+  double* d_traces = nullptr;
+  int64_t trace_cap = 0;
+  int64_t trace_origin = 0;
+  int32_t* d_spike_count = nullptr;
+  double* d_spike_times = nullptr;
+  int32_t* d_status = nullptr;
+  int64_t step = 0;
+  size_t device_bytes = 0;
+  // launch classes after the first run concurrently on these streams
+  cudaStream_t aux[2] = {nullptr, nullptr};
+  bool dry = false;
+  unsigned long long* d_timers = nullptr;
+  std::vector<std::array<int64_t, 6>> tile_stats;
+  cudaEvent_t ev_fork = nullptr, ev_join[2] = {nullptr, nullptr};
+};
+
+namespace bc {
+
+template <typename T>
+static bc_status dalloc(bc_plan* p, T** ptr, size_t count) {
+  *ptr = nullptr;
+  if (count == 0) count = 1;
+  cudaError_t e = cudaMalloc(reinterpret_cast<void**>(ptr), count * sizeof(T));
+  if (e != cudaSuccess) return fail(BC_ERR_CUDA, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  p->device_bytes += count * sizeof(T);
+  return BC_OK;
+}
+
+static void free_plan(bc_plan* p) {
+  cudaFree(p->d_blob);
+  cudaFree(p->d_scratch);
+  cudaFree(p->d_state);
+  cudaFree(p->d_tiles);
+  cudaFree(p->d_pulses);
+  cudaFree(p->d_vinit);
+  cudaFree(p->d_vinit_off);
+  cudaFree(p->d_traces);
+  cudaFree(p->d_spike_count);
+  cudaFree(p->d_spike_times);
+  cudaFree(p->d_status);
+  cudaFree(p->d_timers);
+  for (int k = 0; k < 2; ++k) {
+    if (p->aux[k]) cudaStreamDestroy(p->aux[k]);
+    if (p->ev_join[k]) cudaEventDestroy(p->ev_join[k]);
+  }
+  if (p->ev_fork) cudaEventDestroy(p->ev_fork);
+  delete p;
+}
+
+// ------------------------------------------------------------------ chain schedule
+struct Chain {
+  std::vector<int32_t> nodes;  // bottom -> top (cell-local node ids)
+  std::vector<int32_t> kids;   // chain ids (cell-local) whose top's parent is nodes[0]
+  int32_t level = 0;
+};
+
+struct CellSched {
+  std::vector<Chain> chains;   // ordered by level ascending
+  int32_t max_level = 0;
+};
+
+static void decompose(const LoweredCell& lc, CellSched& cs) {
+  const int32_t n = lc.n_node;
+  std::vector<int32_t> nchild(n, 0);
+  for (int32_t i = 0; i < n; ++i)
+    if (lc.parent[i] >= 0) nchild[lc.parent[i]]++;
+  std::vector<int32_t> chain_of(n, -1);
+  std::vector<Chain> chains;
+  for (int32_t i = 0; i < n; ++i) {
+    if (nchild[i] == 1) continue;  // interior of some chain
+    Chain ch;
+    int32_t cur = i;
+    ch.nodes.push_back(cur);
+    while (true) {
+      const int32_t p = lc.parent[cur];
+      if (p < 0 || nchild[p] != 1) break;
+      cur = p;
+      ch.nodes.push_back(cur);
+    }
+    for (int32_t v : ch.nodes) chain_of[v] = int32_t(chains.size());
+    chains.push_back(std::move(ch));
+  }
+  // child chains: top's parent is a bottom of another chain
+  for (size_t c = 0; c < chains.size(); ++c) {
+    const int32_t top = chains[c].nodes.back();
+    const int32_t p = lc.parent[top];
+    if (p >= 0) chains[chain_of[p]].kids.push_back(int32_t(c));
+  }
+  // levels (iterative: process chains in order of decreasing depth)
+  std::vector<int32_t> order(chains.size());
+  std::iota(order.begin(), order.end(), 0);
+  // depth of the bottom node from the root
+  std::vector<int32_t> depth(n, -1);
+  for (int32_t i = 0; i < n; ++i) {
+    if (depth[i] >= 0) continue;
+    std::vector<int32_t> path;
+    int32_t cur = i;
+    while (cur >= 0 && depth[cur] < 0) {
+      path.push_back(cur);
+      cur = lc.parent[cur];
+    }
+    int32_t d = cur >= 0 ? depth[cur] : -1;
+    for (auto it = path.rbegin(); it != path.rend(); ++it) depth[*it] = ++d;
+  }
+  std::sort(order.begin(), order.end(),
+            [&](int32_t a, int32_t b) { return depth[chains[a].nodes[0]] > depth[chains[b].nodes[0]]; });
+  for (int32_t c : order) {
+    int32_t lv = 0;
+    for (int32_t k : chains[c].kids) lv = std::max(lv, chains[k].level + 1);
+    chains[c].level = lv;
+  }
+  // reorder by level ascending, remap kid ids
+  std::vector<int32_t> by_level(chains.size());
+  std::iota(by_level.begin(), by_level.end(), 0);
+  std::stable_sort(by_level.begin(), by_level.end(),
+                   [&](int32_t a, int32_t b) { return chains[a].level < chains[b].level; });
+  std::vector<int32_t> newid(chains.size());
+  for (size_t k = 0; k < by_level.size(); ++k) newid[by_level[k]] = int32_t(k);
+  cs.chains.clear();
+  cs.chains.reserve(chains.size());
+  cs.max_level = 0;
+  for (int32_t old : by_level) {
+    Chain ch = std::move(chains[old]);
+    for (auto& k : ch.kids) k = newid[k];
+    cs.max_level = std::max(cs.max_level, ch.level);
+    cs.chains.push_back(std::move(ch));
+  }
+}
+
+// ------------------------------------------------------------------ tile building
+struct TileBuild {
+  std::vector<int64_t> cells;  // global cell ids
+  int cls = 0;                 // launch class
+};
+
+struct TileOut {
+  TileDesc desc{};
+  std::vector<unsigned char> blob;
+  std::vector<double> vinit;
+  std::vector<PulseRec> pulses;
+  std::vector<std::pair<int64_t, int32_t>> cv_local;  // (global cv id, local node)
+  std::vector<uint32_t> cv_mech;
+  int64_t crit = 0;
+};
+
+struct BuildCtx {
+  const bc_batch_spec* spec;
+  const std::vector<LoweredCell>* cells;
+  const std::vector<CellSched>* sched;
+  const std::vector<int64_t>* cv_base;  // global cv id of each cell's first CV
+  const std::vector<std::vector<int64_t>>* cell_pulses;
+  const std::vector<std::vector<int64_t>>* cell_probes;
+  const std::vector<std::vector<int32_t>>* pulse_node;  // per cell, node per pulse (parallel to cell_pulses)
+  const std::vector<std::vector<int32_t>>* probe_node;
+  int precision;
+  int state_slots;
+  int thread_cell_max;
+  int split_min;        // chains longer than this are split (0 = never)
+  double split_factor;  // segments = factor * sqrt(length)
+};
+
+template <typename Real>
+static void put(std::vector<unsigned char>& b, size_t off, size_t idx, Real v) {
+  std::memcpy(b.data() + off + idx * sizeof(Real), &v, sizeof(Real));
+}
+
+static bc_status build_tile(const BuildCtx& cx, const TileBuild& tb, int T, TileOut& out) {
+  const bc_batch_spec& s = *cx.spec;
+  const int R = s.n_regions;
+  const size_t rs = cx.precision == BC_PREC_F64 ? 8 : 4;
+  std::vector<int64_t> cell_list = tb.cells;
+  std::vector<std::pair<int64_t, size_t>> cmap;
+  for (size_t i = 0; i < cell_list.size(); ++i) cmap.push_back({cell_list[i], i});
+  std::sort(cmap.begin(), cmap.end());
+  // -------- record specs and work items
+  // A record is a regular chain, one segment of a split chain, or the reduced
+  // system of a split chain.  Items are what LPT assigns to threads.
+  struct RecSpec {
+    int32_t li, chain, kind, seg, K, lo, hi;  // node range [lo, hi) of the chain's nodes
+  };
+  struct Item {
+    std::vector<RecSpec> recs;
+    int64_t cost;
+  };
+  std::vector<std::vector<Item>> items;  // indexed by raw phase 2*level (+1 for reduced)
+  auto item_at = [&](int ph) -> std::vector<Item>& {
+    if (int(items.size()) <= ph) items.resize(ph + 1);
+    return items[ph];
+  };
+  for (size_t li = 0; li < cell_list.size(); ++li) {
+    const int64_t c = cell_list[li];
+    const LoweredCell& lc = (*cx.cells)[c];
+    const CellSched& cs = (*cx.sched)[c];
+    if (lc.n_node <= cx.thread_cell_max) {
+      Item it;
+      for (size_t k = 0; k < cs.chains.size(); ++k)
+        it.recs.push_back({int32_t(li), int32_t(k), kChainRegular, 0, 1, 0, int32_t(cs.chains[k].nodes.size())});
+      it.cost = lc.n_node + int64_t(cs.chains.size());
+      item_at(0).push_back(std::move(it));
+      continue;
+    }
+    for (size_t k = 0; k < cs.chains.size(); ++k) {
+      const Chain& ch = cs.chains[k];
+      const int32_t L = int32_t(ch.nodes.size());
+      const int ph = 2 * ch.level;
+      if (cx.split_min > 0 && L > cx.split_min) {
+        int32_t K = int32_t(std::lround(std::sqrt(double(L)) * cx.split_factor));
+        K = std::max<int32_t>(2, std::min<int32_t>(K, L / 2));
+        for (int32_t sgi = 0; sgi < K; ++sgi) {
+          const int32_t lo = int32_t(int64_t(L) * sgi / K), hi = int32_t(int64_t(L) * (sgi + 1) / K);
+          Item it;
+          it.recs.push_back({int32_t(li), int32_t(k), kChainSegment, sgi, K, lo, hi});
+          it.cost = (hi - lo) + 4 + (sgi == 0 ? int64_t(ch.kids.size()) : 0);
+          item_at(ph).push_back(std::move(it));
+        }
+        Item red;
+        red.recs.push_back({int32_t(li), int32_t(k), kChainReduced, 0, K, 0, L});
+        red.cost = 2 * K + 4;
+        item_at(ph + 1).push_back(std::move(red));
+      } else {
+        Item it;
+        it.recs.push_back({int32_t(li), int32_t(k), kChainRegular, 0, 1, 0, L});
+        it.cost = L + int64_t(ch.kids.size()) + 2;
+        item_at(ph).push_back(std::move(it));
+      }
+    }
+  }
+  // drop empty raw phases
+  std::vector<std::vector<Item>> phases;
+  for (auto& v : items)
+    if (!v.empty()) phases.push_back(std::move(v));
+  if (phases.empty()) phases.resize(1);
+  const int n_phases = int(phases.size());
+  // -------- LPT per phase -> per-thread item lists
+  std::vector<std::vector<std::vector<const Item*>>> lists(n_phases, std::vector<std::vector<const Item*>>(T));
+  int64_t crit = 0;
+  for (int p = 0; p < n_phases; ++p) {
+    std::vector<const Item*> v;
+    for (auto& it : phases[p]) v.push_back(&it);
+    std::stable_sort(v.begin(), v.end(), [](const Item* a, const Item* b) { return a->cost > b->cost; });
+    using QE = std::pair<int64_t, int>;
+    std::priority_queue<QE, std::vector<QE>, std::greater<QE>> q;
+    for (int t = 0; t < T; ++t) q.push({0, t});
+    int64_t mx = 0;
+    for (const Item* it : v) {
+      QE e = q.top();
+      q.pop();
+      lists[p][e.second].push_back(it);
+      e.first += it->cost;
+      mx = std::max(mx, e.first);
+      q.push(e);
+    }
+    crit += mx;
+  }
+  out.crit = crit;
+  // -------- records and node order
+  int64_t n_real = 0;
+  std::vector<std::vector<int32_t>> node_tile(cell_list.size());
+  std::vector<std::vector<int32_t>> handle(cell_list.size());            // chain -> record referenced by parents
+  std::vector<std::vector<std::vector<int32_t>>> seg_rec(cell_list.size());  // chain -> segment records
+  for (size_t i = 0; i < cell_list.size(); ++i) {
+    const LoweredCell& lc = (*cx.cells)[cell_list[i]];
+    const size_t nch = (*cx.sched)[cell_list[i]].chains.size();
+    node_tile[i].assign(lc.n_node, -1);
+    handle[i].assign(nch, -1);
+    seg_rec[i].assign(nch, {});
+    n_real += lc.n_node;
+  }
+  std::vector<ChainRec> chains;
+  std::vector<RecSpec> rec_src;
+  std::vector<int32_t> list_ptr(size_t(n_phases) * (T + 1));
+  int32_t next_node = 0;
+  for (int p = 0; p < n_phases; ++p) {
+    for (int t = 0; t < T; ++t) {
+      list_ptr[size_t(p) * (T + 1) + t] = int32_t(chains.size());
+      for (const Item* it : lists[p][t]) {
+        for (const RecSpec& rsp : it->recs) {
+          const Chain& ch = (*cx.sched)[cell_list[rsp.li]].chains[rsp.chain];
+          ChainRec rec{};
+          rec.kind = rsp.kind;
+          rec.slot = -1;
+          rec.start = -1;
+          rec.count = 0;
+          if (rsp.kind != kChainReduced) {
+            rec.start = next_node;
+            rec.count = rsp.hi - rsp.lo;
+            for (int32_t q = rsp.lo; q < rsp.hi; ++q) node_tile[rsp.li][ch.nodes[q]] = next_node++;
+          }
+          const int32_t id = int32_t(chains.size());
+          if (rsp.kind == kChainRegular || rsp.kind == kChainReduced) handle[rsp.li][rsp.chain] = id;
+          if (rsp.kind == kChainSegment) {
+            auto& v = seg_rec[rsp.li][rsp.chain];
+            if (int(v.size()) < rsp.K) v.assign(rsp.K, -1);
+            v[rsp.seg] = id;
+          }
+          chains.push_back(rec);
+          rec_src.push_back(rsp);
+        }
+      }
+    }
+    list_ptr[size_t(p) * (T + 1) + T] = int32_t(chains.size());
+  }
+  // -------- links: parents, outside nodes, contribution slots
+  // A record that pulls children (regular chain, lowest segment) owns the
+  // consecutive slots aux .. aux + n_child, one per child; each child writes its
+  // contribution into its own slot.  Every segment also owns a slot for (dd, dr, H).
+  std::vector<int32_t> child;
+  int32_t n_slots = 0;
+  for (auto& rec : chains) rec.slot = -1;
+  for (size_t k = 0; k < chains.size(); ++k) {
+    const RecSpec& rsp = rec_src[k];
+    const LoweredCell& lc = (*cx.cells)[cell_list[rsp.li]];
+    const Chain& ch = (*cx.sched)[cell_list[rsp.li]].chains[rsp.chain];
+    const int32_t chain_top_parent = lc.parent[ch.nodes.back()];
+    const int32_t tp = chain_top_parent >= 0 ? node_tile[rsp.li][chain_top_parent] : -1;
+    ChainRec& rec = chains[k];
+    rec.n_child = 0;
+    rec.aux = -1;
+    rec.first = 0;
+    if (rsp.kind == kChainRegular || (rsp.kind == kChainSegment && rsp.seg == 0)) {
+      rec.first = 1;
+      rec.aux = n_slots;
+      rec.n_child = int32_t(ch.kids.size());
+      n_slots += rec.n_child;
+    }
+    if (rsp.kind == kChainReduced) {
+      rec.aux = int32_t(child.size());
+      for (int32_t q : seg_rec[rsp.li][rsp.chain]) child.push_back(q);
+      rec.n_child = rsp.K;
+      rec.top_parent = tp;
+    } else if (rsp.kind == kChainSegment) {
+      rec.top_parent = rsp.seg + 1 < rsp.K ? node_tile[rsp.li][ch.nodes[rsp.hi]] : tp;
+      if (rsp.seg > 0) rec.aux = node_tile[rsp.li][ch.nodes[rsp.lo - 1]];
+    } else {
+      rec.top_parent = tp;
+    }
+  }
+  for (size_t k = 0; k < chains.size(); ++k) {
+    const RecSpec& rsp = rec_src[k];
+    if (!chains[k].first) continue;
+    const Chain& ch = (*cx.sched)[cell_list[rsp.li]].chains[rsp.chain];
+    for (size_t j = 0; j < ch.kids.size(); ++j) {
+      const int32_t kid_rec = handle[rsp.li][ch.kids[j]];
+      if (kid_rec < 0) return fail(BC_ERR_INVALID, "internal: unresolved chain link");
+      chains[kid_rec].slot = chains[k].aux + int32_t(j);
+    }
+  }
+  for (size_t k = 0; k < chains.size(); ++k)
+    if (chains[k].kind == kChainSegment) chains[k].slot = n_slots++;
+  for (int32_t v : child)
+    if (v < 0) return fail(BC_ERR_INVALID, "internal: unresolved segment link");
+  // -------- special nodes: clamp pulses (sorted by node) and probes
+  std::vector<std::pair<int32_t, int64_t>> tpulse, tprobe;  // (tile node, pulse / probe id)
+  for (size_t li = 0; li < cell_list.size(); ++li) {
+    const int64_t c = cell_list[li];
+    const auto& pl = (*cx.cell_pulses)[c];
+    const auto& pn = (*cx.pulse_node)[c];
+    for (size_t k = 0; k < pl.size(); ++k) tpulse.push_back({node_tile[li][pn[k]], pl[k]});
+    const auto& ql = (*cx.cell_probes)[c];
+    const auto& qn = (*cx.probe_node)[c];
+    for (size_t k = 0; k < ql.size(); ++k) tprobe.push_back({node_tile[li][qn[k]], ql[k]});
+  }
+  std::stable_sort(tpulse.begin(), tpulse.end(),
+                   [](const std::pair<int32_t, int64_t>& x, const std::pair<int32_t, int64_t>& y) { return x.first < y.first; });
+  std::sort(tprobe.begin(), tprobe.end());
+  for (size_t k = 1; k < tprobe.size(); ++k)
+    if (tprobe[k].first == tprobe[k - 1].first)
+      return fail(BC_ERR_INVALID, "two probes at the same point of a cell are not supported");
+  std::vector<int32_t> spec_nodes;
+  for (auto& x : tpulse) spec_nodes.push_back(x.first);
+  for (auto& x : tprobe) spec_nodes.push_back(x.first);
+  std::sort(spec_nodes.begin(), spec_nodes.end());
+  spec_nodes.erase(std::unique(spec_nodes.begin(), spec_nodes.end()), spec_nodes.end());
+  if (spec_nodes.size() >= 0xFFFF) return fail(BC_ERR_CAPACITY, "too many clamped / probed points in one tile");
+  // -------- layout
+  const int64_t N = (n_real + 3) & ~int64_t(3);
+  const int S = cx.state_slots;
+  const int64_t n_params = int64_t(cell_list.size()) * R;
+  if (n_params >= 0xFFFF) return fail(BC_ERR_CAPACITY, "too many parameter records in one tile");
+  TileDesc d{};
+  size_t off = 0;
+  d.off_vhi = int32_t(off);
+  off = align16(off + N * rs);
+  d.off_vlo = int32_t(off);
+  off = align16(off + N * rs);
+  d.dyn_bytes = int32_t(off);
+  d.off_alpha = int32_t(off);
+  off = align16(off + N * rs);
+  d.off_beta = int32_t(off);
+  off = align16(off + N * rs);
+  d.off_diag0 = int32_t(off);
+  off = align16(off + N * rs);
+  d.off_pidx = int32_t(off);
+  off = align16(off + N * 2);
+  d.off_spec = int32_t(off);
+  off = align16(off + N * 2);
+  d.off_specs = int32_t(off);
+  off = align16(off + spec_nodes.size() * sizeof(SpecRec));
+  d.off_chains = int32_t(off);
+  off = align16(off + chains.size() * sizeof(ChainRec));
+  d.off_child = int32_t(off);
+  off = align16(off + child.size() * 4);
+  d.off_lists = int32_t(off);
+  off = align16(off + list_ptr.size() * 4);
+  d.off_params = int32_t(off);
+  off = align16(off + size_t(n_params) * BC_NPARAM * rs);
+  d.off_mech = int32_t(off);
+  off = align16(off + size_t(n_params) * 4);
+  if (off > size_t(0x7fffffff)) return fail(BC_ERR_CAPACITY, "tile blob exceeds 2 GiB");
+  d.blob_bytes = int32_t(off);
+  size_t so = 0;
+  d.off_sdiag = int32_t(so);
+  so = align16(so + N * rs);
+  d.off_srhs = int32_t(so);
+  so = align16(so + N * rs);
+  d.off_scd = int32_t(so);
+  so = align16(so + size_t(std::max(n_slots, 1)) * rs);
+  d.off_scr = int32_t(so);
+  so = align16(so + size_t(std::max(n_slots, 1)) * rs);
+  d.off_sfill = int32_t(so);
+  so = align16(so + N * rs);
+  d.off_sh = int32_t(so);
+  so = align16(so + size_t(std::max(n_slots, 1)) * rs);
+  d.n_slots = n_slots;
+  d.scratch_bytes = int32_t(so);
+  d.n_nodes = int32_t(N);
+  d.n_real_nodes = int32_t(n_real);
+  d.n_chains = int32_t(chains.size());
+  d.n_phases = n_phases;
+  d.n_params = int32_t(n_params);
+  // -------- fill
+  std::vector<unsigned char>& b = out.blob;
+  b.assign(d.blob_bytes, 0);
+  out.vinit.assign(n_real, 0.0);
+  auto putr = [&](size_t base_off, size_t idx, double v) {
+    if (rs == 8)
+      put<double>(b, base_off, idx, v);
+    else
+      put<float>(b, base_off, idx, float(v));
+  };
+  for (size_t li = 0; li < cell_list.size(); ++li) {
+    const int64_t c = cell_list[li];
+    const LoweredCell& lc = (*cx.cells)[c];
+    for (int32_t v = 0; v < lc.n_node; ++v) {
+      const int32_t j = node_tile[li][v];
+      putr(d.off_vhi, j, lc.node_vrest[v]);
+      putr(d.off_alpha, j, lc.alpha[v]);
+      putr(d.off_beta, j, lc.beta[v]);
+      putr(d.off_diag0, j, lc.diag[v]);
+      const uint16_t pi = lc.region[v] >= 0 ? uint16_t(li * R + lc.region[v]) : uint16_t(0xFFFF);
+      std::memcpy(b.data() + d.off_pidx + size_t(j) * 2, &pi, 2);
+      out.vinit[j] = lc.node_vrest[v];
+    }
+    for (int r = 0; r < R; ++r) {
+      const int64_t rc = c * R + r;
+      for (int k = 0; k < BC_NPARAM; ++k) putr(d.off_params, (li * R + r) * BC_NPARAM + k, s.region_params[rc * BC_NPARAM + k]);
+      const uint32_t m = s.region_mech[rc];
+      std::memcpy(b.data() + d.off_mech + (li * R + r) * 4, &m, 4);
+    }
+    // CV view map
+    const int64_t base = (*cx.cv_base)[c];
+    for (int32_t k = 0; k < lc.n_cv; ++k) {
+      const int32_t v = lc.cv_node[k];
+      out.cv_local.push_back({base + k, node_tile[li][v]});
+      out.cv_mech.push_back(s.region_mech[c * R + lc.region[v]]);
+    }
+  }
+  // special records: pulses in node order, probe ids
+  {
+    std::vector<uint16_t> spec(N, 0xFFFF);
+    std::vector<SpecRec> specs(spec_nodes.size());
+    std::vector<int32_t> node_cell(n_real, -1), node_local(n_real, -1);
+    for (size_t li = 0; li < cell_list.size(); ++li) {
+      const LoweredCell& lc = (*cx.cells)[cell_list[li]];
+      for (int32_t v = 0; v < lc.n_node; ++v) {
+        node_cell[node_tile[li][v]] = int32_t(li);
+        node_local[node_tile[li][v]] = v;
+      }
+    }
+    for (size_t q = 0; q < spec_nodes.size(); ++q) {
+      spec[spec_nodes[q]] = uint16_t(q);
+      specs[q] = SpecRec{0, 0, -1, 0};
+    }
+    size_t kp = 0;
+    for (size_t q = 0; q < spec_nodes.size(); ++q) {
+      const int32_t node = spec_nodes[q];
+      specs[q].pulse_begin = int32_t(out.pulses.size());
+      while (kp < tpulse.size() && tpulse[kp].first == node) {
+        const int64_t pid = tpulse[kp].second;
+        const size_t li = size_t(node_cell[node]);
+        const LoweredCell& lc = (*cx.cells)[cell_list[li]];
+        const int32_t v = node_local[node];
+        PulseRec pr{};
+        pr.node = node;
+        pr.is_mid = lc.region[v] >= 0 ? 1 : 0;
+        if (pr.is_mid) {
+          double area = 0.0;
+          for (int32_t k = 0; k < lc.n_cv; ++k)
+            if (lc.cv_node[k] == v) {
+              area = lc.cv_area[k];
+              break;
+            }
+          pr.amp = s.pulse_amp[pid] * 1e5 / area;  // uA/cm^2
+        } else {
+          pr.amp = s.pulse_amp[pid] * 1e-3;  // mV/ms on a row with the 1 uF dummy capacitance
+        }
+        pr.t_on = s.pulse_t_on[pid];
+        pr.t_off = s.pulse_t_off[pid];
+        out.pulses.push_back(pr);
+        ++kp;
+      }
+      specs[q].pulse_end = int32_t(out.pulses.size());
+    }
+    for (auto& x : tprobe) specs[spec[x.first]].probe = int32_t(x.second);
+    std::memcpy(b.data() + d.off_spec, spec.data(), spec.size() * 2);
+    if (!specs.empty()) std::memcpy(b.data() + d.off_specs, specs.data(), specs.size() * sizeof(SpecRec));
+  }
+  std::memcpy(b.data() + d.off_chains, chains.data(), chains.size() * sizeof(ChainRec));
+  if (!child.empty()) std::memcpy(b.data() + d.off_child, child.data(), child.size() * 4);
+  std::memcpy(b.data() + d.off_lists, list_ptr.data(), list_ptr.size() * 4);
+  out.desc = d;
+  return BC_OK;
+}
+
+static size_t max_optin_smem(int device) {
+  int v = 0;
+  if (cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, device) != cudaSuccess) return 0;
+  return size_t(v);
+}
+
+// First step index s with s * dt >= t (float64), for clamp windows.
+static int64_t first_step_at(double t, double dt) {
+  if (t <= 0.0) return 0;
+  int64_t s = int64_t(std::floor(t / dt));
+  if (s < 0) s = 0;
+  while (s > 0 && double(s - 1) * dt >= t) --s;
+  while (double(s) * dt < t) ++s;
+  return s;
+}
+
+static bc_status update_pulses(bc_plan* p, double dt, void* stream) {
+  if (p->pulses.empty() || p->pulses_dt == dt) return BC_OK;
+  for (auto& pr : p->pulses) {
+    pr.on_step = first_step_at(pr.t_on, dt);
+    pr.off_step = first_step_at(pr.t_off, dt);
+  }
+  BC_CUDA(cudaMemcpyAsync(p->d_pulses, p->pulses.data(), p->pulses.size() * sizeof(PulseRec), cudaMemcpyHostToDevice,
+                          static_cast<cudaStream_t>(stream)));
+  BC_CUDA(cudaStreamSynchronize(static_cast<cudaStream_t>(stream)));
+  p->pulses_dt = dt;
+  return BC_OK;
+}
+
+static bc_status ensure_traces(bc_plan* p, int64_t records, void* stream) {
+  if (p->n_probes == 0 || records <= p->trace_cap) return BC_OK;
+  int64_t cap = std::max<int64_t>(records, p->trace_cap * 2);
+  double* nb = nullptr;
+  BC_CUDA(cudaMalloc(reinterpret_cast<void**>(&nb), size_t(cap) * p->n_probes * sizeof(double)));
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (p->d_traces && p->trace_cap > 0) {
+    BC_CUDA(cudaMemcpyAsync(nb, p->d_traces, size_t(p->trace_cap) * p->n_probes * sizeof(double),
+                            cudaMemcpyDeviceToDevice, st));
+    BC_CUDA(cudaStreamSynchronize(st));
+  }
+  cudaFree(p->d_traces);
+  p->device_bytes += size_t(cap - p->trace_cap) * p->n_probes * sizeof(double);
+  p->d_traces = nb;
+  p->trace_cap = cap;
+  return BC_OK;
+}
+
+static LaunchArgs base_args(bc_plan* p) {
+  LaunchArgs a{};
+  a.blob = p->d_blob;
+  a.scratch = p->d_scratch;
+  a.state = p->d_state;
+  a.pulses = p->d_pulses;
+  a.traces = p->d_traces;
+  a.trace_cap = p->trace_cap;
+  a.trace_base = p->trace_origin;
+  a.n_probes_total = p->n_probes;
+  a.record_every = p->record_every;
+  a.max_spikes = p->max_spikes;
+  a.spike_count = p->d_spike_count;
+  a.spike_times = p->d_spike_times;
+  a.status = p->d_status;
+  a.state_slots = p->state_slots;
+  a.timers = p->d_timers;
+  return a;
+}
+
+static bc_status enqueue_run(bc_plan* p, int64_t n_steps, double dt, void* stream) {
+  if (n_steps < 0) return fail(BC_ERR_INVALID, "n_steps must be >= 0");
+  if (!(dt > 0.0) || !std::isfinite(dt)) return fail(BC_ERR_INVALID, "dt must be a positive finite number (ms)");
+  bc_status st = update_pulses(p, dt, stream);
+  if (st != BC_OK) return st;
+  const int64_t recs = p->record_every > 0 ? (p->step + n_steps - p->trace_origin) / p->record_every : 0;
+  st = ensure_traces(p, recs, stream);
+  if (st != BC_OK) return st;
+  int64_t done = 0;
+  while (done < n_steps) {
+    const int32_t k = int32_t(std::min<int64_t>(p->steps_per_launch, n_steps - done));
+    LaunchArgs a = base_args(p);
+    a.step0 = p->step + done;
+    a.n_steps = k;
+    a.dt = dt;
+    // Classes are independent cells: the first runs on the caller's stream, the
+    // others on forked streams so their CTAs can share SMs.
+    cudaStream_t main_st = static_cast<cudaStream_t>(stream);
+    const int nc = int(p->classes.size());
+    if (nc > 1) BC_CUDA(cudaEventRecord(p->ev_fork, main_st));
+    for (int ci = 0; ci < nc; ++ci) {
+      const LaunchClass& lcz = p->classes[ci];
+      cudaStream_t st = main_st;
+      if (ci > 0) {
+        st = p->aux[ci - 1];
+        BC_CUDA(cudaStreamWaitEvent(st, p->ev_fork, 0));
+      }
+      a.tiles = p->d_tiles + lcz.first;
+      a.n_tiles = lcz.count;
+      int e = launch_tiles(a, p->precision, lcz.smem, lcz.threads, lcz.smem_bytes, st);
+      if (e) return fail(BC_ERR_CUDA, std::string("tile kernel launch: ") + cudaGetErrorString(cudaError_t(e)));
+      if (ci > 0) {
+        BC_CUDA(cudaEventRecord(p->ev_join[ci - 1], st));
+        BC_CUDA(cudaStreamWaitEvent(main_st, p->ev_join[ci - 1], 0));
+      }
+    }
+    done += k;
+  }
+  p->step += n_steps;
+  return BC_OK;
+}
+
+}  // namespace bc
+
+using namespace bc;
+
+extern "C" {
+
+const char* bc_last_error(void) { return g_error.c_str(); }
+
+int32_t bc_version(void) { return 100; }
+
+void bc_default_options(bc_plan_options* o) {
+  std::memset(o, 0, sizeof(*o));
+  o->precision = BC_PREC_F32;
+  o->threads_per_tile = 0;
+  o->tile_nodes = 0;
+  o->thread_cell_max = 48;
+  o->steps_per_launch = 0;
+  o->record_every = 1;
+  o->max_spikes = 64;
+  o->use_graph = 0;
+  o->device = 0;
+  o->split_min = 24;
+  o->split_factor = 1.0f;
+}
+
+bc_status bc_plan_create(const bc_batch_spec* spec, const bc_plan_options* opts_in, bc_plan_t* out) {
+  if (!spec || !out) return fail(BC_ERR_INVALID, "null argument");
+  *out = nullptr;
+  bc_plan_options opts;
+  if (opts_in)
+    opts = *opts_in;
+  else
+    bc_default_options(&opts);
+  const bc_batch_spec& s = *spec;
+  if (s.n_cells <= 0) return fail(BC_ERR_INVALID, "n_cells must be > 0");
+  if (s.n_regions <= 0) return fail(BC_ERR_INVALID, "n_regions must be > 0");
+  if (opts.precision != BC_PREC_F32 && opts.precision != BC_PREC_F64)
+    return fail(BC_ERR_INVALID, "precision must be BC_PREC_F32 or BC_PREC_F64");
+  if (opts.threads_per_tile < 0 || opts.threads_per_tile > 1024 || opts.threads_per_tile % 32)
+    return fail(BC_ERR_INVALID, "threads_per_tile must be 0 or a multiple of 32 up to 1024");
+  if (opts.record_every < 0 || opts.max_spikes < 0) return fail(BC_ERR_INVALID, "record_every/max_spikes must be >= 0");
+  if (s.cell_branch_offsets[0] != 0 || s.cell_branch_offsets[s.n_cells] != s.n_branches)
+    return fail(BC_ERR_INVALID, "cell_branch_offsets must span [0, n_branches]");
+  const bool dry = opts.dry_run != 0;
+  if (!dry) BC_CUDA(cudaSetDevice(opts.device));
+  bc_plan* p = new bc_plan();
+  p->dry = dry;
+  p->precision = opts.precision;
+  p->device = opts.device;
+  p->real_size = opts.precision == BC_PREC_F64 ? 8 : 4;
+  p->record_every = opts.record_every;
+  p->max_spikes = opts.max_spikes;
+  p->use_graph = opts.use_graph;
+  p->steps_per_launch = opts.steps_per_launch > 0 ? opts.steps_per_launch : 1000;
+  p->thread_cell_max = opts.thread_cell_max;
+  p->n_cells = s.n_cells;
+  // ---------------------------------------------------- lower
+  std::vector<LoweredCell> cells(s.n_cells);
+  std::vector<int64_t> cv_base(s.n_cells + 1, 0);
+  for (int64_t c = 0; c < s.n_cells; ++c) {
+    bc_status st = lower_cell(s, c, cells[c]);
+    if (st != BC_OK) {
+      delete p;
+      return st;
+    }
+    cv_base[c + 1] = cv_base[c] + cells[c].n_cv;
+    p->n_nodes += cells[c].n_node;
+  }
+  p->n_cv = cv_base[s.n_cells];
+  p->cell_ncv.resize(s.n_cells);
+  for (int64_t c = 0; c < s.n_cells; ++c) p->cell_ncv[c] = cells[c].n_cv;
+  for (int64_t k = 0; k < s.n_cells * s.n_regions; ++k)
+    if (s.region_mech[k] & ~BC_M_ALL) {
+      delete p;
+      return fail(BC_ERR_INVALID, "unknown mechanism bits in region_mech");
+    }
+  const int S = kNumSlots;
+  p->state_slots = S;
+  // ---------------------------------------------------- pulses / probes -> nodes
+  std::vector<std::vector<int64_t>> cell_pulses(s.n_cells), cell_probes(s.n_cells);
+  std::vector<std::vector<int32_t>> pulse_node(s.n_cells), probe_node(s.n_cells);
+  for (int64_t k = 0; k < s.n_pulses; ++k) {
+    const int64_t c = s.pulse_cell[k];
+    if (c < 0 || c >= s.n_cells) {
+      delete p;
+      return fail(BC_ERR_INVALID, "pulse_cell out of range");
+    }
+    const int32_t v = locate_node(s, c, cells[c], s.pulse_branch[k], s.pulse_x[k]);
+    if (v < 0) {
+      delete p;
+      return fail(BC_ERR_INVALID, "pulse location not found");
+    }
+    if (!(s.pulse_t_off[k] >= s.pulse_t_on[k])) {
+      delete p;
+      return fail(BC_ERR_INVALID, "pulse_t_off must be >= pulse_t_on");
+    }
+    cell_pulses[c].push_back(k);
+    pulse_node[c].push_back(v);
+  }
+  p->probe_vrest.assign(s.n_probes, 0.0);
+  for (int64_t k = 0; k < s.n_probes; ++k) {
+    const int64_t c = s.probe_cell[k];
+    if (c < 0 || c >= s.n_cells) {
+      delete p;
+      return fail(BC_ERR_INVALID, "probe_cell out of range");
+    }
+    const int32_t v = locate_node(s, c, cells[c], s.probe_branch[k], s.probe_x[k]);
+    if (v < 0) {
+      delete p;
+      return fail(BC_ERR_INVALID, "probe location not found");
+    }
+    cell_probes[c].push_back(k);
+    probe_node[c].push_back(v);
+    p->probe_vrest[k] = cells[c].node_vrest[v];
+  }
+  p->n_probes = s.n_probes;
+  p->n_pulses = s.n_pulses;
+  // ---------------------------------------------------- schedules
+  std::vector<CellSched> sched(s.n_cells);
+  for (int64_t c = 0; c < s.n_cells; ++c) decompose(cells[c], sched[c]);
+  // ---------------------------------------------------- tile packing
+  const size_t rs = p->real_size;
+  const size_t smem_cap = dry ? size_t(232448) : max_optin_smem(opts.device);
+  if (smem_cap == 0) {
+    delete p;
+    return fail(BC_ERR_CUDA, "could not query the shared-memory limit of the device");
+  }
+  const size_t static_smem = 1024;  // static shared memory of the kernel (mbarrier, status) + slack
+  const size_t smem_budget = smem_cap - static_smem;
+  // bytes per node (approx.) for packing: V hi/lo, states, alpha/beta/diag0, parent, pidx, scratch diag/rhs
+  // shared bytes per node: V hi/lo, alpha/beta/diag0, scratch diag/rhs/fill (Real),
+  // region index (2 B), plus ~1 chain record per 5 nodes (record, child slot, cD/cR/H)
+  const double bpn = double(8 * rs + 2) + (28.0 + 4.0 + 3.0 * double(rs)) / 5.0;
+  int tile_nodes = opts.tile_nodes;
+  if (tile_nodes <= 0) tile_nodes = 900;
+  tile_nodes = std::max(tile_nodes, 16);
+  p->tile_nodes = tile_nodes;
+  // Launch classes: 0 = packed shared-memory tiles (cells <= tile_nodes), 1 = one big
+  // cell per shared-memory tile, 2 = global-memory tiles (too big for shared memory).
+  const int T_packed = opts.threads_per_tile > 0 ? opts.threads_per_tile : 128;
+  const int T_big = opts.threads_big > 0 ? opts.threads_big : 256;
+  const int T_glob = opts.threads_global > 0 ? opts.threads_global : 512;
+  if (T_big % 32 || T_big > 1024 || T_glob % 32 || T_glob > 1024) {
+    delete p;
+    return fail(BC_ERR_INVALID, "thread counts must be multiples of 32 up to 1024");
+  }
+  const int class_threads[3] = {T_packed, T_big, T_glob};
+  p->threads = T_packed;
+  p->threads_global = T_glob;
+  std::vector<int64_t> order(s.n_cells);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int64_t a, int64_t b) { return cells[a].n_node > cells[b].n_node; });
+  std::vector<TileBuild> builds;
+  std::vector<int64_t> fill;
+  // first-fit decreasing over the most recently opened tiles
+  for (int64_t c : order) {
+    const int64_t nn = cells[c].n_node;
+    if (nn > tile_nodes) {
+      TileBuild tb;
+      tb.cells.push_back(c);
+      tb.cls = 1;
+      builds.push_back(tb);
+      fill.push_back(nn);
+      continue;
+    }
+    bool placed = false;
+    const size_t lo = builds.size() > 64 ? builds.size() - 64 : 0;
+    for (size_t t = lo; t < builds.size(); ++t) {
+      if (builds[t].cls == 0 && fill[t] + nn <= tile_nodes && builds[t].cells.size() < 4096) {
+        builds[t].cells.push_back(c);
+        fill[t] += nn;
+        placed = true;
+        break;
+      }
+    }
+    if (!placed) {
+      TileBuild tb;
+      tb.cells.push_back(c);
+      tb.cls = 0;
+      builds.push_back(tb);
+      fill.push_back(nn);
+    }
+  }
+  BuildCtx cx{&s, &cells, &sched, &cv_base, &cell_pulses, &cell_probes, &pulse_node, &probe_node,
+              p->precision, S, p->thread_cell_max, opts.split_min, opts.split_factor > 0 ? opts.split_factor : 1.0};
+  std::vector<TileOut> outs;
+  outs.reserve(builds.size());
+  const size_t packed_budget = std::min(smem_budget, size_t(double(tile_nodes) * bpn) + 2048);
+  for (size_t t = 0; t < builds.size(); ++t) {
+    TileOut to;
+    bc_status st = build_tile(cx, builds[t], class_threads[builds[t].cls], to);
+    if (st != BC_OK) {
+      delete p;
+      return st;
+    }
+    const size_t need = size_t(to.desc.blob_bytes) + size_t(to.desc.scratch_bytes);
+    const size_t limit = builds[t].cls == 0 ? packed_budget : smem_budget;
+    if (builds[t].cls != 2 && need > limit) {
+      if (builds[t].cells.size() > 1) {
+        // split: move the last cell into a new packed tile and rebuild this one
+        TileBuild nb;
+        nb.cells.push_back(builds[t].cells.back());
+        nb.cls = 0;
+        builds.push_back(nb);
+        builds[t].cells.pop_back();
+        --t;
+        continue;
+      }
+      builds[t].cls = need > smem_budget ? 2 : 1;
+      st = build_tile(cx, builds[t], class_threads[builds[t].cls], to);
+      if (st != BC_OK) {
+        delete p;
+        return st;
+      }
+    }
+    outs.push_back(std::move(to));
+  }
+  // tiles ordered by class; one launch per class
+  std::vector<size_t> tord;
+  for (int cl = 0; cl < 3; ++cl) {
+    LaunchClass lcz;
+    lcz.first = int(tord.size());
+    lcz.threads = class_threads[cl];
+    lcz.smem = cl < 2;
+    for (size_t t = 0; t < builds.size(); ++t)
+      if (builds[t].cls == cl) {
+        tord.push_back(t);
+        const size_t need = size_t(outs[t].desc.blob_bytes) + size_t(outs[t].desc.scratch_bytes);
+        if (lcz.smem) lcz.smem_bytes = std::max(lcz.smem_bytes, need);
+      }
+    lcz.count = int(tord.size()) - lcz.first;
+    if (lcz.count > 0) p->classes.push_back(lcz);
+  }
+  p->n_smem_tiles = 0;
+  for (auto& lcz : p->classes)
+    if (lcz.smem) p->n_smem_tiles += lcz.count;
+  // ---------------------------------------------------- concatenate + upload
+  size_t blob_total = 0, scratch_total = 0, vinit_total = 0;
+  int64_t state_total = 0;
+  std::vector<int64_t> vinit_off;
+  p->tiles.clear();
+  p->cv_tile.assign(p->n_cv, -1);
+  p->cv_node.assign(p->n_cv, -1);
+  p->cv_mech.assign(p->n_cv, 0);
+  for (size_t k = 0; k < tord.size(); ++k) {
+    TileOut& to = outs[tord[k]];
+    TileDesc d = to.desc;
+    d.blob_offset = int64_t(blob_total);
+    blob_total = align16(blob_total + d.blob_bytes);
+    d.state_offset = state_total;
+    state_total += int64_t(S) * d.n_nodes;
+    if (builds[tord[k]].cls == 2) {
+      d.scratch_offset = int64_t(scratch_total);
+      scratch_total = align16(scratch_total + d.scratch_bytes);
+    } else {
+      p->smem_bytes = std::max(p->smem_bytes, size_t(d.blob_bytes) + size_t(d.scratch_bytes));
+    }
+    d.pulse_offset = int64_t(p->pulses.size());
+    d.n_pulses = int32_t(to.pulses.size());
+    p->pulses.insert(p->pulses.end(), to.pulses.begin(), to.pulses.end());
+    vinit_off.push_back(int64_t(vinit_total));
+    vinit_total += to.vinit.size();
+    for (size_t q = 0; q < to.cv_local.size(); ++q) {
+      p->cv_tile[to.cv_local[q].first] = int32_t(k);
+      p->cv_node[to.cv_local[q].first] = to.cv_local[q].second;
+      p->cv_mech[to.cv_local[q].first] = to.cv_mech[q];
+    }
+    p->max_phases = std::max<int64_t>(p->max_phases, d.n_phases);
+    p->max_chain_nodes = std::max<int64_t>(p->max_chain_nodes, to.crit);
+    p->tiles.push_back(d);
+  }
+  std::vector<unsigned char> blob(blob_total, 0);
+  std::vector<double> vinit(vinit_total);
+  for (size_t k = 0; k < tord.size(); ++k) {
+    const TileOut& to = outs[tord[k]];
+    std::memcpy(blob.data() + p->tiles[k].blob_offset, to.blob.data(), to.blob.size());
+    std::copy(to.vinit.begin(), to.vinit.end(), vinit.begin() + vinit_off[k]);
+  }
+  std::vector<int64_t> outs_crit(outs.size());
+  for (size_t q = 0; q < outs.size(); ++q) outs_crit[q] = outs[q].crit;
+  outs.clear();
+  bc_status st = BC_OK;
+#define BC_TRY(x)          \
+  do {                     \
+    st = (x);              \
+    if (st != BC_OK) {     \
+      free_plan(p);        \
+      return st;           \
+    }                      \
+  } while (0)
+#define BC_TRYC(call)                                                                                \
+  do {                                                                                               \
+    cudaError_t e_ = (call);                                                                         \
+    if (e_ != cudaSuccess) {                                                                         \
+      free_plan(p);                                                                                  \
+      return fail(BC_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));                   \
+    }                                                                                                \
+  } while (0)
+  p->tile_stats.clear();
+  for (size_t k = 0; k < tord.size(); ++k) {
+    const TileDesc& d = p->tiles[k];
+    p->tile_stats.push_back({int64_t(d.n_real_nodes), int64_t(d.n_chains), int64_t(d.n_phases),
+                             int64_t(outs_crit[tord[k]]), int64_t(builds[tord[k]].cls),
+                             int64_t(d.blob_bytes) + int64_t(d.scratch_bytes)});
+  }
+  if (dry) {
+    *out = p;
+    return BC_OK;
+  }
+  p->blob_bytes = blob_total;
+  p->scratch_bytes = scratch_total;
+  BC_TRY(dalloc(p, &p->d_blob, blob_total));
+  BC_TRY(dalloc(p, &p->d_scratch, scratch_total));
+  p->state_bytes = size_t(state_total) * rs;
+  BC_TRY(dalloc(p, &p->d_state, p->state_bytes));
+  BC_TRY(dalloc(p, &p->d_tiles, p->tiles.size()));
+  BC_TRY(dalloc(p, &p->d_pulses, p->pulses.size()));
+  BC_TRY(dalloc(p, &p->d_vinit, vinit.size()));
+  BC_TRY(dalloc(p, &p->d_vinit_off, vinit_off.size()));
+  BC_TRY(dalloc(p, &p->d_spike_count, size_t(p->n_probes)));
+  BC_TRY(dalloc(p, &p->d_spike_times, size_t(p->n_probes) * std::max(1, p->max_spikes)));
+  BC_TRY(dalloc(p, &p->d_status, 1));
+  BC_TRY(dalloc(p, &p->d_timers, 4));
+  BC_TRYC(cudaMemset(p->d_timers, 0, 4 * sizeof(unsigned long long)));
+  BC_TRYC(cudaMemcpy(p->d_blob, blob.data(), blob_total, cudaMemcpyHostToDevice));
+  BC_TRYC(cudaMemcpy(p->d_tiles, p->tiles.data(), p->tiles.size() * sizeof(TileDesc), cudaMemcpyHostToDevice));
+  BC_TRYC(cudaMemcpy(p->d_vinit, vinit.data(), vinit.size() * sizeof(double), cudaMemcpyHostToDevice));
+  BC_TRYC(cudaMemcpy(p->d_vinit_off, vinit_off.data(), vinit_off.size() * sizeof(int64_t), cudaMemcpyHostToDevice));
+  BC_TRYC(cudaMemset(p->d_status, 0, sizeof(int32_t)));
+  if (p->n_smem_tiles > 0 && p->smem_bytes + static_smem > smem_cap) {
+    free_plan(p);
+    return fail(BC_ERR_CAPACITY, "tile shared memory exceeds the device limit");
+  }
+  for (int k = 0; k < 2; ++k) {
+    BC_TRYC(cudaStreamCreateWithFlags(&p->aux[k], cudaStreamNonBlocking));
+    BC_TRYC(cudaEventCreateWithFlags(&p->ev_join[k], cudaEventDisableTiming));
+  }
+  BC_TRYC(cudaEventCreateWithFlags(&p->ev_fork, cudaEventDisableTiming));
+  *out = p;
+  return bc_reset(p, nullptr);
+}
+
+bc_status bc_plan_destroy(bc_plan_t p) {
+  if (!p) return fail(BC_ERR_INVALID, "null plan");
+  free_plan(p);
+  return BC_OK;
+}
+
+bc_status bc_plan_info(bc_plan_t p, bc_plan_info_t* info) {
+  if (!p || !info) return fail(BC_ERR_INVALID, "null argument");
+  std::memset(info, 0, sizeof(*info));
+  info->n_cells = p->n_cells;
+  info->n_cv = p->n_cv;
+  info->n_nodes = p->n_nodes;
+  info->n_tiles = int64_t(p->tiles.size());
+  info->n_probes = p->n_probes;
+  info->n_pulses = p->n_pulses;
+  info->threads_per_tile = p->threads;
+  info->tile_nodes = p->tile_nodes;
+  info->steps_per_launch = p->steps_per_launch;
+  info->precision = p->precision;
+  info->smem_bytes_per_tile = int64_t(p->smem_bytes);
+  info->device_bytes = int64_t(p->device_bytes);
+  info->max_phases = p->max_phases;
+  info->max_chain_nodes = p->max_chain_nodes;
+  info->state_slots = p->state_slots;
+  info->reserved[0] = p->n_smem_tiles;
+  return BC_OK;
+}
+
+bc_status bc_plan_cell_ncv(bc_plan_t p, int64_t* ncv) {
+  if (!p || !ncv) return fail(BC_ERR_INVALID, "null argument");
+  std::copy(p->cell_ncv.begin(), p->cell_ncv.end(), ncv);
+  return BC_OK;
+}
+
+#define BC_NEED_DEVICE(p) \
+  if ((p)->dry) return fail(BC_ERR_INVALID, "plan was created with dry_run; it has no device state")
+
+bc_status bc_reset(bc_plan_t p, void* stream) {
+  if (!p) return fail(BC_ERR_INVALID, "null plan");
+  BC_NEED_DEVICE(p);
+  BC_CUDA(cudaSetDevice(p->device));
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  LaunchArgs a = base_args(p);
+  a.tiles = p->d_tiles;
+  a.n_tiles = int32_t(p->tiles.size());
+  int e = launch_reset_impl(a, p->precision, 256, p->d_vinit, p->d_vinit_off, stream);
+  if (e) return fail(BC_ERR_CUDA, std::string("reset kernel: ") + cudaGetErrorString(cudaError_t(e)));
+  if (p->n_probes > 0) {
+    BC_CUDA(cudaMemsetAsync(p->d_spike_count, 0, size_t(p->n_probes) * sizeof(int32_t), st));
+  }
+  BC_CUDA(cudaMemsetAsync(p->d_status, 0, sizeof(int32_t), st));
+  BC_CUDA(cudaStreamSynchronize(st));
+  p->step = 0;
+  p->trace_origin = 0;
+  return BC_OK;
+}
+
+bc_status bc_check(bc_plan_t p, void* stream) {
+  if (!p) return fail(BC_ERR_INVALID, "null plan");
+  BC_NEED_DEVICE(p);
+  int32_t status = 0;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  BC_CUDA(cudaMemcpyAsync(&status, p->d_status, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+  BC_CUDA(cudaStreamSynchronize(st));
+  if (status & 2) return fail(BC_ERR_TIMEOUT, "a bounded device wait gave up (bulk copy did not complete)");
+  if (status & 1) return fail(BC_ERR_NONFINITE, "non-finite membrane voltage");
+  return BC_OK;
+}
+
+bc_status bc_run_async(bc_plan_t p, int64_t n_steps, double dt, void* stream) {
+  if (!p) return fail(BC_ERR_INVALID, "null plan");
+  BC_NEED_DEVICE(p);
+  BC_CUDA(cudaSetDevice(p->device));
+  return enqueue_run(p, n_steps, dt, stream);
+}
+
+bc_status bc_run(bc_plan_t p, int64_t n_steps, double dt, void* stream) {
+  bc_status st = bc_run_async(p, n_steps, dt, stream);
+  if (st != BC_OK) return st;
+  return bc_check(p, stream);
+}
+
+bc_status bc_run_timed(bc_plan_t p, int64_t n_steps, double dt, void* stream, double* ms_out) {
+  if (!p || !ms_out) return fail(BC_ERR_INVALID, "null argument");
+  BC_NEED_DEVICE(p);
+  BC_CUDA(cudaSetDevice(p->device));
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  // prepare tables outside the timed region
+  bc_status s0 = update_pulses(p, dt, stream);
+  if (s0 != BC_OK) return s0;
+  const int64_t recs = p->record_every > 0 ? (p->step + n_steps - p->trace_origin) / p->record_every : 0;
+  s0 = ensure_traces(p, recs, stream);
+  if (s0 != BC_OK) return s0;
+  cudaEvent_t e0, e1;
+  BC_CUDA(cudaEventCreate(&e0));
+  BC_CUDA(cudaEventCreate(&e1));
+  BC_CUDA(cudaEventRecord(e0, st));
+  bc_status s1 = enqueue_run(p, n_steps, dt, stream);
+  BC_CUDA(cudaEventRecord(e1, st));
+  BC_CUDA(cudaEventSynchronize(e1));
+  float ms = 0.f;
+  BC_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  *ms_out = ms;
+  if (s1 != BC_OK) return s1;
+  return bc_check(p, stream);
+}
+
+static bc_status view_offsets(bc_plan* p, int32_t which, std::vector<int64_t>& hi, std::vector<int64_t>& lo) {
+  if (which < 0 || which >= BC_NSTATE_VIEW) return fail(BC_ERR_INVALID, "unknown state view");
+  hi.assign(p->n_cv, -1);
+  lo.assign(p->n_cv, -1);
+  const size_t rs = p->real_size;
+  for (int64_t k = 0; k < p->n_cv; ++k) {
+    const TileDesc& d = p->tiles[p->cv_tile[k]];
+    const int64_t j = p->cv_node[k];
+    const int64_t base = d.blob_offset;
+    if (which == BC_STATE_V) {
+      hi[k] = base + d.off_vhi + j * rs;
+      lo[k] = base + d.off_vlo + j * rs;
+      continue;
+    }
+    const uint32_t m = p->cv_mech[k];
+    int slot = -1;
+    bool has_lo = false;
+    switch (which) {
+      case BC_STATE_NA_P: slot = (m & BC_M_NA) ? kSlotNaP : -1; break;
+      case BC_STATE_NA_Q: slot = (m & BC_M_NA) ? kSlotNaQ : -1; break;
+      case BC_STATE_KDR_P: slot = (m & BC_M_KDR) ? kSlotKdrP : -1; break;
+      case BC_STATE_CAL_P: slot = (m & BC_M_CAL) ? kSlotCalP : -1; break;
+      case BC_STATE_CAL_Q: slot = (m & BC_M_CAL) ? kSlotCalQ : -1; break;
+      case BC_STATE_CAT_P: slot = (m & BC_M_CAT) ? kSlotCatP : -1; break;
+      case BC_STATE_CAT_Q: slot = (m & BC_M_CAT) ? kSlotCatQ : -1; break;
+      case BC_STATE_HCN_P: slot = (m & BC_M_HCN) ? kSlotHcnP : -1; break;
+      case BC_STATE_AHP_P: slot = (m & BC_M_AHP) ? kSlotAhpP : -1; break;
+      case BC_STATE_CA_CI:
+        slot = (m & BC_M_CADET) ? kSlotCaHi : -1;
+        has_lo = true;
+        break;
+    }
+    if (slot < 0) continue;
+    // states live in the separate state array: offsets are tagged by +state_tag
+    hi[k] = kStateTag + (d.state_offset + int64_t(slot) * d.n_nodes + j) * int64_t(rs);
+    if (has_lo) lo[k] = kStateTag + (d.state_offset + int64_t(kSlotCaLo) * d.n_nodes + j) * int64_t(rs);
+  }
+  return BC_OK;
+}
+
+static bc_status view_io(bc_plan* p, int32_t which, double* host, bool write, void* stream) {
+  if (!p || !host) return fail(BC_ERR_INVALID, "null argument");
+  BC_NEED_DEVICE(p);
+  BC_CUDA(cudaSetDevice(p->device));
+  std::vector<int64_t> hi, lo;
+  bc_status st = view_offsets(p, which, hi, lo);
+  if (st != BC_OK) return st;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const size_t n = size_t(p->n_cv);
+  int64_t *dhi = nullptr, *dlo = nullptr;
+  double* dv = nullptr;
+  BC_CUDA(cudaMalloc(reinterpret_cast<void**>(&dhi), n * 8));
+  BC_CUDA(cudaMalloc(reinterpret_cast<void**>(&dlo), n * 8));
+  BC_CUDA(cudaMalloc(reinterpret_cast<void**>(&dv), n * 8));
+  cudaError_t e = cudaMemcpyAsync(dhi, hi.data(), n * 8, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dlo, lo.data(), n * 8, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess && write) e = cudaMemcpyAsync(dv, host, n * 8, cudaMemcpyHostToDevice, s);
+  int ke = 0;
+  if (e == cudaSuccess)
+    ke = launch_view_impl(p->d_blob, p->d_state, p->precision, dhi, dlo, dv, int64_t(n), write, stream);
+  if (e == cudaSuccess && !ke && !write) e = cudaMemcpyAsync(host, dv, n * 8, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  cudaFree(dhi);
+  cudaFree(dlo);
+  cudaFree(dv);
+  if (ke) return fail(BC_ERR_CUDA, std::string("view kernel: ") + cudaGetErrorString(cudaError_t(ke)));
+  if (e != cudaSuccess) return fail(BC_ERR_CUDA, std::string("state view: ") + cudaGetErrorString(e));
+  return BC_OK;
+}
+
+bc_status bc_state_download(bc_plan_t p, int32_t which, double* out, void* stream) {
+  return view_io(p, which, out, false, stream);
+}
+
+bc_status bc_state_upload(bc_plan_t p, int32_t which, const double* in, void* stream) {
+  return view_io(p, which, const_cast<double*>(in), true, stream);
+}
+
+bc_status bc_probe_count(bc_plan_t p, int64_t* n) {
+  if (!p || !n) return fail(BC_ERR_INVALID, "null argument");
+  *n = p->record_every > 0 ? (p->step - p->trace_origin) / p->record_every : 0;
+  if (*n > p->trace_cap) *n = p->trace_cap;
+  return BC_OK;
+}
+
+bc_status bc_probe_download(bc_plan_t p, double* traces, int64_t max_records, void* stream) {
+  if (!p || (!traces && max_records > 0)) return fail(BC_ERR_INVALID, "null argument");
+  int64_t n = 0;
+  bc_probe_count(p, &n);
+  n = std::min(n, max_records);
+  if (n <= 0 || p->n_probes == 0) return BC_OK;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  BC_CUDA(cudaMemcpyAsync(traces, p->d_traces, size_t(n) * p->n_probes * sizeof(double), cudaMemcpyDeviceToHost, s));
+  BC_CUDA(cudaStreamSynchronize(s));
+  return BC_OK;
+}
+
+bc_status bc_spike_download(bc_plan_t p, int32_t* counts, double* times, void* stream) {
+  if (!p) return fail(BC_ERR_INVALID, "null plan");
+  if (p->n_probes == 0) return BC_OK;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (counts)
+    BC_CUDA(cudaMemcpyAsync(counts, p->d_spike_count, size_t(p->n_probes) * 4, cudaMemcpyDeviceToHost, s));
+  if (times && p->max_spikes > 0)
+    BC_CUDA(cudaMemcpyAsync(times, p->d_spike_times, size_t(p->n_probes) * p->max_spikes * 8, cudaMemcpyDeviceToHost, s));
+  BC_CUDA(cudaStreamSynchronize(s));
+  return BC_OK;
+}
+
+bc_status bc_probe_clear(bc_plan_t p, void* stream) {
+  if (!p) return fail(BC_ERR_INVALID, "null plan");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (p->n_probes > 0) BC_CUDA(cudaMemsetAsync(p->d_spike_count, 0, size_t(p->n_probes) * 4, s));
+  BC_CUDA(cudaStreamSynchronize(s));
+  p->trace_origin = p->step;
+  return BC_OK;
+}
+
+bc_status bc_plan_tile_stats(bc_plan_t p, int64_t* out) {
+  if (!p || !out) return fail(BC_ERR_INVALID, "null argument");
+  for (size_t k = 0; k < p->tile_stats.size(); ++k)
+    for (int j = 0; j < 6; ++j) out[k * 6 + j] = p->tile_stats[k][j];
+  return BC_OK;
+}
+
+bc_status bc_debug_phase_cycles(bc_plan_t p, uint64_t* out4, int32_t reset) {
+  if (!p || !out4) return fail(BC_ERR_INVALID, "null argument");
+  BC_NEED_DEVICE(p);
+  BC_CUDA(cudaMemcpy(out4, p->d_timers, 4 * sizeof(uint64_t), cudaMemcpyDeviceToHost));
+  if (reset) BC_CUDA(cudaMemset(p->d_timers, 0, 4 * sizeof(uint64_t)));
+  return BC_OK;
+}
+
+bc_status bc_step_count(bc_plan_t p, int64_t* steps) {
+  if (!p || !steps) return fail(BC_ERR_INVALID, "null argument");
+  *steps = p->step;
+  return BC_OK;
+}
+
+}  // extern "C"

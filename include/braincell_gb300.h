@@ -1,0 +1,262 @@
+/*
+ * braincell_gb300 -- C ABI of the GB300 (sm_103a) multi-compartment Cell time step.
+ *
+ * This library replaces, for a batch of cells, the reference's staggered solver
+ * path: `staggered_step` (braincell/quad/_staggered.py:54-154), i.e. the step-start
+ * ion-current cache (cell.py:2261-2280), the DHS implicit-Euler voltage step
+ * (_staggered.py:193-320: linearisation :763-795, numeric state :449-513, forward
+ * elimination `comp_triang_raw` :641-657, back-substitution `comp_backsub_raw`
+ * :742-760), and the family-ordered exponential-Euler update of ions and channels
+ * (cell.py:2157-2217 -> quad/_exp_euler.py:330-478).  The one-time lowering it also
+ * replaces is the geometry / node-tree / axial-matrix assembly:
+ * _discretization/geometry.py:214-434,614-736, _discretization/base.py:530-559,
+ * _discretization/node_build.py:58-285, quad/_staggered.py:323-390,546-593.
+ *
+ * Conventions: plain pointers and sizes, host memory unless stated, no torch types.
+ * Every entry point returns a bc_status (0 = OK); bc_last_error() gives the text of
+ * the most recent failure on the calling thread.  A plan is used from one host
+ * thread at a time; device work is ordered on the CUDA stream passed in.
+ *
+ * Units: um, mV, ms, nA, mS/cm^2 (conductance density), uF/cm^2, ohm*cm, kelvin, mM.
+ */
+#ifndef BRAINCELL_GB300_H
+#define BRAINCELL_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ status codes */
+typedef int32_t bc_status;
+#define BC_OK 0
+#define BC_ERR_INVALID 1        /* bad argument / malformed spec (host-side check)      */
+#define BC_ERR_CUDA 2           /* a CUDA runtime call failed                           */
+#define BC_ERR_NONFINITE 3      /* a NaN/Inf voltage was detected by the kernel          */
+#define BC_ERR_CAPACITY 4       /* a cell does not fit any supported tile                */
+#define BC_ERR_TIMEOUT 5        /* a bounded device wait gave up                         */
+#define BC_ERR_UNSUPPORTED 6    /* feature not available in this build / precision       */
+
+/* ------------------------------------------------------------------ mechanisms */
+/* Bit per mechanism present in a region (painted density mechanisms). */
+#define BC_M_IL (1u << 0)        /* channel/leaky.py:144      g (E - V)                       */
+#define BC_M_KLEAK (1u << 1)     /* channel/potassium.py:1167 g (E_K - V)                     */
+#define BC_M_NA (1u << 2)        /* channel/sodium.py:59      Na_Ba2002   p^3 q, E_Na          */
+#define BC_M_KDR (1u << 3)       /* channel/potassium.py:95   KDR_Ba2002  p^4, E_K             */
+#define BC_M_CAL (1u << 4)       /* channel/calcium.py:790    CaL_IS2008  p^2 q, E_Ca          */
+#define BC_M_CAT (1u << 5)       /* channel/calcium.py:222    CaT_HM1992  p^2 q, E_Ca          */
+#define BC_M_HCN (1u << 6)       /* channel/hyperpolarization_activated.py:45 HCN_HM1992 p, E  */
+#define BC_M_AHP (1u << 7)       /* channel/potassium_calcium.py:78 AHP_De1994 p^2, E_K, Ci   */
+#define BC_M_CADET (1u << 8)     /* ion/calcium.py:286        CalciumDetailed (dynamic Ci)     */
+#define BC_M_ALL 0x1FFu
+
+/* Per-region parameter record (double[BC_NPARAM]); index names below. */
+#define BC_NPARAM 40
+#define BC_P_INVCM 0      /* 1 / membrane capacitance, cm^2/uF                 */
+#define BC_P_VREST 1      /* voltage used by reset (mV)                        */
+#define BC_P_ENA 2        /* fixed reversal potentials (mV)                    */
+#define BC_P_EK 3
+#define BC_P_ECA 4        /* used only when BC_M_CADET is absent               */
+#define BC_P_IL_G 5
+#define BC_P_IL_E 6
+#define BC_P_KLEAK_G 7
+#define BC_P_NA_G 8
+#define BC_P_NA_VSH 9
+#define BC_P_NA_PHI 10
+#define BC_P_KDR_G 11
+#define BC_P_KDR_VSH 12
+#define BC_P_KDR_PHI 13
+#define BC_P_CAL_G 14
+#define BC_P_CAL_VSH 15
+#define BC_P_CAL_PHIP 16
+#define BC_P_CAL_PHIQ 17
+#define BC_P_CAT_G 18
+#define BC_P_CAT_VSH 19
+#define BC_P_CAT_PHIP 20
+#define BC_P_CAT_PHIQ 21
+#define BC_P_HCN_G 22
+#define BC_P_HCN_E 23
+#define BC_P_HCN_PHI 24
+#define BC_P_AHP_G 25
+#define BC_P_AHP_N 26
+#define BC_P_AHP_ALPHA 27
+#define BC_P_AHP_BETA 28
+#define BC_P_AHP_PHI 29
+#define BC_P_CA_D 30      /* shell depth (um)                                  */
+#define BC_P_CA_TAU 31    /* ms                                                */
+#define BC_P_CA_CREST 32  /* mM                                                */
+#define BC_P_CA_CO 33     /* mM                                                */
+#define BC_P_CA_TEMP 34   /* K                                                 */
+#define BC_P_CA_CI0 35    /* mM, reset value of Ci                             */
+
+/* ------------------------------------------------------------------ batch spec */
+/*
+ * A batch of independent cells described at morphology level.  Cell c owns
+ * branches [cell_branch_offsets[c], cell_branch_offsets[c+1]); branch indices in
+ * branch_parent are cell-local (root = -1 and must be branch 0 of the cell).
+ * Branch b owns segments [branch_seg_offsets[b], branch_seg_offsets[b+1]) and is
+ * tiled into branch_ncv[b] uniform CVs (the reference's uniform CV policies).
+ * Region r of cell c uses record region_params[(c*n_regions + r)*BC_NPARAM ...],
+ * mechanisms region_mech[c*n_regions + r], cable region_cm / region_ra.
+ */
+typedef struct bc_batch_spec {
+  int64_t n_cells;
+  int64_t n_branches;
+  int64_t n_segments;
+  int32_t n_regions;
+  const int64_t* cell_branch_offsets; /* [n_cells + 1]                          */
+  const int32_t* branch_parent;       /* [n_branches] cell-local, -1 = root     */
+  const double* branch_parent_x;      /* [n_branches]                           */
+  const double* branch_child_x;       /* [n_branches] 0 or 1                    */
+  const int32_t* branch_ncv;          /* [n_branches] >= 1                      */
+  const int32_t* branch_region;       /* [n_branches] in [0, n_regions)         */
+  const int64_t* branch_seg_offsets;  /* [n_branches + 1]                       */
+  const double* seg_length;           /* [n_segments] um                        */
+  const double* seg_r_prox;           /* [n_segments] um                        */
+  const double* seg_r_dist;           /* [n_segments] um                        */
+  const double* region_cm;            /* [n_cells * n_regions] uF/cm^2          */
+  const double* region_ra;            /* [n_cells * n_regions] ohm*cm           */
+  const uint32_t* region_mech;        /* [n_cells * n_regions] BC_M_* bits      */
+  const double* region_params;        /* [n_cells * n_regions * BC_NPARAM]      */
+  /* current-clamp segments: active for t_on <= t < t_off (absolute ms).       */
+  int64_t n_pulses;
+  const int32_t* pulse_cell;          /* [n_pulses]                             */
+  const int32_t* pulse_branch;        /* [n_pulses] cell-local branch           */
+  const double* pulse_x;              /* [n_pulses] location on the branch      */
+  const double* pulse_t_on;           /* [n_pulses] ms                          */
+  const double* pulse_t_off;          /* [n_pulses] ms                          */
+  const double* pulse_amp;            /* [n_pulses] nA                          */
+  /* probes: voltage recorded at (cell, branch, x); spikes detected there.     */
+  int64_t n_probes;
+  const int32_t* probe_cell;
+  const int32_t* probe_branch;
+  const double* probe_x;
+} bc_batch_spec;
+
+/* ------------------------------------------------------------------ plan options */
+#define BC_PREC_F32 0 /* FP32 state + arithmetic, float-float (Kahan) V and Ci */
+#define BC_PREC_F64 1 /* FP64 throughout: the on-GPU oracle run                 */
+
+typedef struct bc_plan_options {
+  int32_t precision;        /* BC_PREC_*                                             */
+  int32_t threads_per_tile; /* CTA size (multiple of 32, <= 1024); 0 = auto          */
+  int32_t tile_nodes;       /* node budget per tile (shared-memory size); 0 = auto   */
+  int32_t thread_cell_max;  /* cells with <= this many nodes are walked by one thread;
+                               larger cells are split into chains over threads       */
+  int32_t steps_per_launch; /* time steps fused per kernel launch; 0 = auto          */
+  int32_t record_every;     /* probe sampling period in steps (>= 1)                 */
+  int32_t max_spikes;       /* spike times kept per probe                            */
+  int32_t use_graph;        /* capture multi-launch runs in a CUDA graph             */
+  int32_t device;           /* CUDA device ordinal                                   */
+  int32_t threads_big;      /* CTA size for tiles holding one cell larger than
+                               tile_nodes; 0 = auto                                   */
+  int32_t threads_global;   /* CTA size for global-memory tiles; 0 = auto            */
+  int32_t split_min;        /* unbranched chains longer than this many nodes are split
+                               into segments eliminated in parallel (0 = never)        */
+  float split_factor;       /* segments per split chain = split_factor * sqrt(length) */
+  int32_t dry_run;          /* 1: lower and schedule only (no CUDA calls); the plan
+                               answers bc_plan_info / bc_plan_tile_stats only         */
+  int32_t reserved[2];
+} bc_plan_options;
+
+typedef struct bc_plan* bc_plan_t;
+
+/* Plan statistics (host-side, filled by bc_plan_info). */
+typedef struct bc_plan_info_t {
+  int64_t n_cells, n_cv, n_nodes, n_tiles, n_probes, n_pulses;
+  int32_t threads_per_tile, tile_nodes, steps_per_launch, precision;
+  int64_t smem_bytes_per_tile;   /* dynamic shared memory per CTA                    */
+  int64_t device_bytes;          /* device memory held by the plan                   */
+  int64_t max_phases;            /* largest barrier-phase count of any tile          */
+  int64_t max_chain_nodes;       /* longest per-thread node walk (critical path)     */
+  int32_t state_slots;           /* per-node mechanism state slots                   */
+  int32_t reserved[7];
+} bc_plan_info_t;
+
+/* ------------------------------------------------------------------ entry points */
+/* Thread-local text of the last failure (never NULL). */
+const char* bc_last_error(void);
+/* ABI version: major * 10000 + minor * 100 + patch. */
+int32_t bc_version(void);
+/* Fill opts with defaults. */
+void bc_default_options(bc_plan_options* opts);
+
+/* Lower a batch (geometry -> CVs -> node tree -> axial coefficients), schedule it
+ * into shared-memory tiles and allocate the device buffers.  Replaces the
+ * reference's one-time lowering (Cell.init_state, cell.py:490-552) and the cached
+ * DHS static source (_staggered.py:323-446). */
+bc_status bc_plan_create(const bc_batch_spec* spec, const bc_plan_options* opts, bc_plan_t* out);
+bc_status bc_plan_destroy(bc_plan_t plan);
+bc_status bc_plan_info(bc_plan_t plan, bc_plan_info_t* info);
+
+/* Per-tile schedule statistics, 6 int64 per tile in launch order: real nodes,
+ * chain records, barrier phases, critical-path estimate (node visits of the
+ * busiest thread summed over phases), launch class (0 packed shared-memory tile,
+ * 1 single-cell shared-memory tile, 2 global-memory tile), shared bytes. */
+bc_status bc_plan_tile_stats(bc_plan_t plan, int64_t* out /* [n_tiles * 6] */);
+
+/* Sizes of the host-side views (CV count per cell, in reference CV order). */
+bc_status bc_plan_cell_ncv(bc_plan_t plan, int64_t* ncv_out /* [n_cells] */);
+
+/* Reset all states: V = region V_rest, gates at steady state at V, Ci = Ci0,
+ * spike counters and step counter cleared.  Mirrors Cell.reset_state
+ * (cell.py:2529-2550) with HH.reset_state (channel/_base.py:560-573). */
+bc_status bc_reset(bc_plan_t plan, void* stream);
+
+/* Advance n_steps time steps of size dt (ms) from the plan's step counter, in
+ * launches of steps_per_launch fused steps.  Mirrors n_steps calls of
+ * staggered_step with t = t0 + k * dt.  Returns BC_ERR_NONFINITE if any probe
+ * or node voltage became non-finite (checked when the call completes). */
+bc_status bc_run(bc_plan_t plan, int64_t n_steps, double dt, void* stream);
+
+/* Same as bc_run but enqueues only; no host synchronisation and no status check.
+ * Use bc_check to read the device status later. */
+bc_status bc_run_async(bc_plan_t plan, int64_t n_steps, double dt, void* stream);
+bc_status bc_check(bc_plan_t plan, void* stream);
+
+/* Read/write state in reference order (float64 host arrays).
+ *   V per CV:         [n_cv]   (cell-major, CV ids as the reference numbers them)
+ *   state per CV:     [n_cv * BC_NSTATE_VIEW], the named view below            */
+#define BC_STATE_V 0
+#define BC_STATE_NA_P 1
+#define BC_STATE_NA_Q 2
+#define BC_STATE_KDR_P 3
+#define BC_STATE_CAL_P 4
+#define BC_STATE_CAL_Q 5
+#define BC_STATE_CAT_P 6
+#define BC_STATE_CAT_Q 7
+#define BC_STATE_HCN_P 8
+#define BC_STATE_AHP_P 9
+#define BC_STATE_CA_CI 10
+#define BC_NSTATE_VIEW 11
+bc_status bc_state_download(bc_plan_t plan, int32_t which, double* out /* [n_cv] */, void* stream);
+bc_status bc_state_upload(bc_plan_t plan, int32_t which, const double* in /* [n_cv] */, void* stream);
+
+/* Probe outputs.  Traces: [n_probes, n_records] float64 where n_records is the
+ * number of samples taken since the last bc_probe_clear.  Spikes: count per probe
+ * and up to max_spikes upward 0 mV crossing times (ms, linear interpolation). */
+bc_status bc_probe_count(bc_plan_t plan, int64_t* n_records);
+bc_status bc_probe_download(bc_plan_t plan, double* traces, int64_t max_records, void* stream);
+bc_status bc_spike_download(bc_plan_t plan, int32_t* counts /* [n_probes] */,
+                            double* times /* [n_probes * max_spikes] */, void* stream);
+bc_status bc_probe_clear(bc_plan_t plan, void* stream);
+
+/* Diagnostics: cycles summed over CTAs (as seen by each CTA's first thread) in
+ * forward elimination, back-substitution, node update and probes/pulses.  Only a
+ * library compiled with -DBC_PHASE_TIMERS records them; otherwise all zero. */
+bc_status bc_debug_phase_cycles(bc_plan_t plan, uint64_t* out4, int32_t reset);
+
+/* Current step counter (number of steps taken since reset). */
+bc_status bc_step_count(bc_plan_t plan, int64_t* steps);
+
+/* Timing helper for measurement: runs n_steps like bc_run_async between two CUDA
+ * events recorded on the stream and returns the elapsed device milliseconds of the
+ * solver kernels alone (ms_out). */
+bc_status bc_run_timed(bc_plan_t plan, int64_t n_steps, double dt, void* stream, double* ms_out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BRAINCELL_GB300_H */

@@ -1,0 +1,840 @@
+"""CPU float64 restatement of the reference staggered Cell step -- the oracle.
+
+TEST INFRASTRUCTURE ONLY.  Imported by ``tests/``, ``__graft_entry__.smoke()`` and
+the CPU-baseline leg of ``bench.py`` as the checker; never by the product.
+
+Parity status: the reference (JAX + brainstate + brainunit) cannot be imported in
+this build environment and ships no stored traces for the full Cell solve, so the
+end-to-end solve is **parity unpinned**.  The pieces below are pinned against the
+reference's own known-answer tests (see ``tests/test_oracle_pins.py``): frustum
+clipping / area / axial factor / midpoint radius (``_discretization/geometry_test.py``),
+peel levels and schedule groups (``_compute/scheduling_test.py``), recursive-doubling
+indices (``quad/_staggered_test.py:182-200``), gate rate known answers and Q10
+factors (``channel/*_test.py``), and the step-level behaviours the reference tests
+assert (clamp raises V, population widening is neutral, replicas are identical).
+
+Restated algorithm, in the reference's order:
+
+* geometry -- ``_discretization/geometry.py:214-336`` (frusta, lateral area),
+  ``:339-349`` (axial factor), ``:352-376`` (midpoint radius), ``:382-434`` (split),
+  ``:614-736`` (per-CV assembly); ``_discretization/base.py:530-559`` (R = Ra * factor);
+* node tree -- ``_discretization/node_build.py:58-285`` (midpoints + root endpoint +
+  one terminal per branch; edge roles), ``:352-371`` (attachment node);
+* scheduling -- ``_compute/scheduling.py:45-213`` (peel levels, row order, groups);
+* DHS static source -- ``quad/_staggered.py:323-390`` (axial operator),
+  ``:546-593`` (edge conductance, row capacitance), ``:596-612`` (edge order),
+  ``:726-739`` (recursive-doubling table);
+* one step -- ``quad/_staggered.py:54-154`` with ``cell.py:2261-2280`` (cached ion
+  current), ``:763-795`` + ``cell.py:1907-1963`` (linearisation), ``:449-543``
+  (numeric state, edge clamps, restore), ``:641-657`` (forward elimination),
+  ``:742-760`` (back-substitution), ``cell.py:2157-2217`` (family order: ion self
+  states, then channels) and ``quad/_exp_euler.py:330-478`` (y += dt*exprel(dt*l)*f);
+* mechanisms -- ``channel/_base.py:517-674`` (HH template), the channel files named
+  in :data:`CHANNEL_DEFAULTS`, ``ion/_base.py:463-506`` and ``ion/calcium.py:499-505``.
+
+Where the reference differentiates with ``vector_grad`` the oracle writes the
+derivative in closed form: every config current is ohmic in V with the gates held
+fixed, so dI/dV = -sum(g * prod(x^p)), and every gate/Ci right-hand side is affine
+in its own state, so d f / d x is the coefficient of x.
+
+Units: um, mV, ms, nA, mS/cm^2 (so g*(E-V) is uA/cm^2 and dV/dt = I/cm in mV/ms),
+uF/cm^2, ohm*cm, K, mM.
+"""
+
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass
+
+import numpy as np
+
+__all__ = [
+    "OracleCell",
+    "Frustum",
+    "build_frusta",
+    "lateral_area_um2",
+    "axial_factor_per_cm",
+    "midpoint_radius_um",
+    "split_frusta",
+    "compute_peel_levels",
+    "build_backsub_indices",
+    "exprel",
+    "rates",
+    "CHANNEL_DEFAULTS",
+    "ION_DEFAULTS",
+]
+
+EPS_PARAM = 1e-9
+EPS_LEN_UM = 1e-6
+FARADAY = 96485.33212  # C/mol (CODATA 2018)
+GAS_R = 8.314462618  # J/(mol K)
+
+
+def _c2k(c: float) -> float:
+    return c + 273.15
+
+
+# Defaults restated from the reference constructors.
+CHANNEL_DEFAULTS = {
+    "IL": dict(g_max=0.1, E=-70.0),  # channel/leaky.py:183-190
+    "K_Leak": dict(g_max=0.005),  # channel/potassium.py:1210-1216
+    "Na_Ba2002": dict(g_max=90.0, temp=_c2k(36.0), q10=3.0, temp_ref=_c2k(36.0), V_sh=-50.0),  # sodium.py:139-148
+    "KDR_Ba2002": dict(g_max=10.0, temp=_c2k(36.0), q10=3.0, temp_ref=_c2k(36.0), V_sh=-50.0),  # potassium.py:191-200
+    "CaL_IS2008": dict(g_max=1.0, temp=_c2k(36.0), q10_p=3.55, temp_ref_p=_c2k(24.0), q10_q=3.0,
+                       temp_ref_q=_c2k(24.0), V_sh=0.0),  # calcium.py:(CaL __init__)
+    "CaT_HM1992": dict(g_max=2.0, temp=_c2k(36.0), q10_p=3.55, temp_ref_p=_c2k(24.0), q10_q=3.0,
+                       temp_ref_q=_c2k(24.0), V_sh=-3.0),  # calcium.py:(CaT __init__)
+    "HCN_HM1992": dict(g_max=10.0, E=43.0, temp=_c2k(36.0), q10=1.0, temp_ref=_c2k(36.0)),  # hyperpol..:104-112
+    "AHP_De1994": dict(n=2.0, g_max=10.0, alpha=48.0, beta=0.09, phi=1.0),  # potassium_calcium.py:163-172
+}
+ION_DEFAULTS = {
+    "SodiumFixed": dict(E=50.0),
+    "PotassiumFixed": dict(E=-95.0),
+    "CalciumFixed": dict(E=120.0),
+    "CalciumDetailed": dict(temp=_c2k(36.0), d=1.0, tau=5.0, C_rest=2.4e-4, Co=2.0, Ci_initializer=2.4e-4),
+}
+_CA_FIXED_CI = 5e-5  # Calcium.default_Ci (ion/calcium.py:120)
+
+
+# ----------------------------------------------------------------------------- geometry
+
+
+@dataclass(frozen=True)
+class Frustum:
+    prox: float
+    dist: float
+    length_um: float
+    r_prox_um: float
+    r_dist_um: float
+
+
+def build_frusta(lengths, r_prox, r_dist, prox: float, dist: float) -> tuple[Frustum, ...]:
+    """``_build_frusta`` (geometry.py:214-321) without 3-D points."""
+    prox_f, dist_f = float(prox), float(dist)
+    if not (0.0 - EPS_PARAM <= prox_f < dist_f - EPS_PARAM and dist_f <= 1.0 + EPS_PARAM):
+        raise ValueError(f"CV bounds must satisfy 0 <= prox < dist <= 1, got {(prox, dist)!r}.")
+    prox_f = max(0.0, min(1.0, prox_f))
+    dist_f = max(0.0, min(1.0, dist_f))
+    lengths = np.asarray(lengths, dtype=float)
+    r_prox = np.asarray(r_prox, dtype=float)
+    r_dist = np.asarray(r_dist, dtype=float)
+    if np.any(r_prox <= 0.0) or np.any(r_dist <= 0.0):
+        raise ValueError("All branch radii must be > 0.")
+    total = float(np.sum(lengths))
+    if total <= EPS_LEN_UM:
+        raise ValueError("Branch total length must be > EPS_LEN_UM.")
+    start_um, end_um = prox_f * total, dist_f * total
+    seg_starts = np.concatenate(([0.0], np.cumsum(lengths)[:-1]))
+    seg_ends = seg_starts + lengths
+    out: list[Frustum] = []
+    for i, seg_len in enumerate(lengths):
+        s0, s1 = float(seg_starts[i]), float(seg_ends[i])
+        rp, rd = float(r_prox[i]), float(r_dist[i])
+        if seg_len <= EPS_LEN_UM:
+            if np.isclose(rp, rd):
+                continue
+            # zero-length radius jump (geometry.py:198-211)
+            if s0 < start_um - EPS_LEN_UM or s0 > end_um + EPS_LEN_UM:
+                continue
+            if s0 <= start_um + EPS_LEN_UM and not start_um <= EPS_LEN_UM:
+                continue
+            xj = max(prox_f, min(dist_f, s0 / total))
+            out.append(Frustum(xj, xj, 0.0, rp, rd))
+            continue
+        left, right = max(s0, start_um), min(s1, end_um)
+        if right - left <= EPS_LEN_UM:
+            continue
+        t0, t1 = (left - s0) / float(seg_len), (right - s0) / float(seg_len)
+        r0, r1 = rp + (rd - rp) * t0, rp + (rd - rp) * t1
+        x0 = max(prox_f, min(dist_f, left / total))
+        x1 = max(prox_f, min(dist_f, right / total))
+        out.append(Frustum(x0, x1, right - left, r0, r1))
+    if not out:
+        raise ValueError("CV produced no frusta.")
+    return tuple(out)
+
+
+def lateral_area_um2(frusta) -> float:
+    total = 0.0
+    for p in frusta:
+        slant = math.sqrt(p.length_um ** 2 + (p.r_dist_um - p.r_prox_um) ** 2)
+        total += math.pi * (p.r_prox_um + p.r_dist_um) * slant
+    return total
+
+
+def axial_factor_per_cm(frusta) -> float:
+    f = 0.0
+    for p in frusta:
+        f += (p.length_um * 1e-4) / (math.pi * (p.r_prox_um * 1e-4) * (p.r_dist_um * 1e-4))
+    return f
+
+
+def midpoint_radius_um(frusta) -> float:
+    total = sum(p.length_um for p in frusta)
+    if total <= EPS_LEN_UM:
+        return 0.5 * (frusta[0].r_prox_um + frusta[-1].r_dist_um)
+    target, walked = 0.5 * total, 0.0
+    for p in frusta:
+        nxt = walked + p.length_um
+        if nxt >= target - EPS_LEN_UM:
+            if p.length_um <= EPS_LEN_UM:
+                return 0.5 * (p.r_prox_um + p.r_dist_um)
+            ratio = max(0.0, min(1.0, (target - walked) / p.length_um))
+            return p.r_prox_um + (p.r_dist_um - p.r_prox_um) * ratio
+        walked = nxt
+    return frusta[-1].r_dist_um
+
+
+def split_frusta(frusta, x: float):
+    left, right = [], []
+    for p in frusta:
+        if p.dist <= x + EPS_PARAM:
+            left.append(p)
+            continue
+        if p.prox >= x - EPS_PARAM:
+            right.append(p)
+            continue
+        span = p.dist - p.prox
+        if span <= EPS_PARAM:
+            continue
+        ratio = max(0.0, min(1.0, (x - p.prox) / span))
+        ll = p.length_um * ratio
+        lr = p.length_um - ll
+        rm = p.r_prox_um + (p.r_dist_um - p.r_prox_um) * ratio
+        if ll > EPS_LEN_UM:
+            left.append(Frustum(p.prox, x, ll, p.r_prox_um, rm))
+        if lr > EPS_LEN_UM:
+            right.append(Frustum(x, p.dist, lr, rm, p.r_dist_um))
+    return tuple(left), tuple(right)
+
+
+# ----------------------------------------------------------------------------- schedule
+
+
+def compute_peel_levels(node_parent: np.ndarray, node_children) -> np.ndarray:
+    """``_compute_peel_levels`` (scheduling.py:120-159)."""
+    n = len(node_parent)
+    levels = np.full(n, -1, dtype=np.int32)
+    remaining = np.asarray([len(c) for c in node_children], dtype=np.int32)
+    frontier = [pid for pid in range(n) if remaining[pid] == 0]
+    for pid in frontier:
+        levels[pid] = 0
+    cur = 0
+    while cur < len(frontier):
+        pid = frontier[cur]
+        cur += 1
+        par = int(node_parent[pid])
+        if par < 0:
+            continue
+        cand = int(levels[pid]) + 1
+        if levels[par] < cand:
+            levels[par] = cand
+        remaining[par] -= 1
+        if remaining[par] == 0:
+            frontier.append(par)
+    if (levels < 0).any():
+        raise ValueError("compute_peel_levels: cycle detected or node unreachable from any leaf.")
+    return levels
+
+
+def build_backsub_indices(parent_lookup: np.ndarray, n_nodes: int) -> np.ndarray:
+    """``_build_backsub_indices`` (_staggered.py:726-739)."""
+    parent_lookup = np.asarray(parent_lookup, dtype=np.int32)
+    idx = []
+    old, new = 0, 1
+    k = np.arange(n_nodes + 1, dtype=np.int32)
+    while new <= max(1, n_nodes):
+        for _ in range(new - old):
+            k = parent_lookup[k]
+        old, new = new, 2 * new
+        idx.append(k)
+    return np.asarray(idx, dtype=np.int32)
+
+
+# ----------------------------------------------------------------------------- rates
+
+
+def exprel(x):
+    """(e^x - 1)/x with exprel(0) = 1."""
+    x = np.asarray(x, dtype=np.float64)
+    small = np.abs(x) < 1e-300
+    xs = np.where(small, 1.0, x)
+    return np.where(small, 1.0, np.expm1(xs) / xs)
+
+
+def rates(name: str, V, p: dict, Ci=None):
+    """Gate rate functions, keyed by gate: returns {gate: ("ab", alpha, beta) | ("it", inf, tau)}."""
+    if name == "Na_Ba2002":  # sodium.py:154-170
+        Vp = V - p["V_sh"]
+        return {
+            "p": ("ab", 0.32 * 4.0 / exprel(-(Vp - 13.0) / 4.0), 0.28 * 5.0 / exprel((Vp - 40.0) / 5.0)),
+            "q": ("ab", 0.128 * np.exp(-(Vp - 17.0) / 18.0), 4.0 / (1.0 + np.exp(-(Vp - 40.0) / 5.0))),
+        }
+    if name == "KDR_Ba2002":  # potassium.py:206-214
+        Vp = V - p["V_sh"]
+        return {"p": ("ab", 0.032 * 5.0 / exprel(-(Vp - 15.0) / 5.0), 0.5 * np.exp(-(Vp - 10.0) / 40.0))}
+    if name == "CaL_IS2008":  # calcium.py:(CaL f_p_inf .. f_q_tau)
+        Vs = V - p["V_sh"]
+        return {
+            "p": ("it", 1.0 / (1.0 + np.exp(-(Vs + 10.0) / 4.0)),
+                  0.4 + 0.7 / (np.exp(-(Vs + 5.0) / 15.0) + np.exp((Vs + 5.0) / 15.0))),
+            "q": ("it", 1.0 / (1.0 + np.exp((Vs + 25.0) / 2.0)),
+                  300.0 + 100.0 / (np.exp((Vs + 40.0) / 9.5) + np.exp(-(Vs + 40.0) / 9.5))),
+        }
+    if name == "CaT_HM1992":  # calcium.py:(CaT f_p_inf .. f_q_tau)
+        Vs = V - p["V_sh"]
+        return {
+            "p": ("it", 1.0 / (1.0 + np.exp(-(Vs + 59.0) / 6.2)),
+                  1.0 / (np.exp(-(Vs + 132.0) / 16.7) + np.exp((Vs + 16.8) / 18.2)) + 0.612),
+            "q": ("it", 1.0 / (1.0 + np.exp((Vs + 83.0) / 4.0)),
+                  np.where(Vs >= -80.0, np.exp(-(Vs + 22.0) / 10.5) + 28.0, np.exp((Vs + 467.0) / 66.6))),
+        }
+    if name == "HCN_HM1992":  # hyperpolarization_activated.py:126-133
+        return {"p": ("it", 1.0 / (1.0 + np.exp((V + 75.0) / 5.5)),
+                      1.0 / (np.exp(-0.086 * V - 14.59) + np.exp(0.0701 * V - 1.87)))}
+    if name == "AHP_De1994":  # potassium_calcium.py:181-186
+        return {"p": ("ab", p["alpha"] * np.power(Ci, p["n"]), p["beta"] * np.ones_like(V))}
+    raise KeyError(name)
+
+
+_GATES = {  # (gate, power, phi-key)
+    "Na_Ba2002": (("p", 3, "phi"), ("q", 1, "phi")),
+    "KDR_Ba2002": (("p", 4, "phi"),),
+    "CaL_IS2008": (("p", 2, "phi_p"), ("q", 1, "phi_q")),
+    "CaT_HM1992": (("p", 2, "phi_p"), ("q", 1, "phi_q")),
+    "HCN_HM1992": (("p", 1, "phi"),),
+    "AHP_De1994": (("p", 2, "phi"),),
+}
+_ION_OF = {"Na_Ba2002": "na", "KDR_Ba2002": "k", "CaL_IS2008": "ca", "CaT_HM1992": "ca",
+           "K_Leak": "k", "AHP_De1994": "k"}
+
+
+def _resolve(table: dict, decl) -> dict:
+    p = dict(table[decl.class_name])
+    for k, v in decl.params.items():
+        if k not in p:
+            raise ValueError(f"{decl.class_name}: unknown parameter {k!r}.")
+        p[k] = float(v)
+    name = decl.class_name
+    if name in ("Na_Ba2002", "KDR_Ba2002", "HCN_HM1992"):
+        p["phi"] = p["q10"] ** ((p["temp"] - p["temp_ref"]) / 10.0)
+    elif name in ("CaL_IS2008", "CaT_HM1992"):
+        p["phi_p"] = p["q10_p"] ** ((p["temp"] - p["temp_ref_p"]) / 10.0)
+        p["phi_q"] = p["q10_q"] ** ((p["temp"] - p["temp_ref_q"]) / 10.0)
+    return p
+
+
+# ----------------------------------------------------------------------------- the cell
+
+
+class OracleCell:
+    """Float64 restatement of one reference ``Cell`` stepped with ``"staggered"``.
+
+    ``cell`` is a declared :class:`braincell_gb300.cell.Cell` (morphology, CV
+    policy, paint and place rules, population size); only its declarations are
+    read.  States are dense over points with ``g = 0`` off the painted mask, as in
+    ``_compute/bindings.py:569-757``.
+    """
+
+    MAX_GROUP = 256  # Cell.node_scheduling default (cell.py:1282)
+
+    def __init__(self, cell, *, replicas: int | None = None) -> None:
+        self.P = int(np.prod(cell.pop_size)) if replicas is None else int(replicas)
+        self.V_th = float(cell.V_th)
+        self._discretize(cell)
+        self._node_tree()
+        self._schedule()
+        self._static_source()
+        self._mechanisms(cell)
+        self._points(cell)
+        self.t_step = 0
+        self.reset_state()
+
+    # ------------------------------------------------------------ discretization
+    def _discretize(self, cell) -> None:
+        from braincell_gb300.mech import CableProperty
+
+        morpho = cell.morpho
+        self.morpho = morpho
+        branches = morpho.branches
+        counts = cell.cv_policy.cv_counts(morpho)
+        # cable per branch: last painted CableProperty wins (default cable otherwise)
+        cable = [CableProperty() for _ in branches]
+        mech_by_branch: list[list] = [[] for _ in branches]
+        for region, decls in cell.paint_rules:
+            mask = region.branch_mask(morpho)
+            for d in decls:
+                for b in np.nonzero(mask)[0]:
+                    if isinstance(d, CableProperty):
+                        cable[b] = d
+                    else:
+                        mech_by_branch[b].append(d)
+        self.cv_branch, self.cv_prox, self.cv_dist = [], [], []
+        self.cv_area, self.cv_rprox, self.cv_rdist, self.cv_cm, self.cv_v = [], [], [], [], []
+        self.branch_cv_ids: list[list[int]] = []
+        self.branch_mechs = mech_by_branch
+        cid = 0
+        for b, br in enumerate(branches):
+            ids = []
+            n = int(counts[b])
+            for k in range(n):
+                prox, dist = k / n, (k + 1) / n
+                fr = build_frusta(br.lengths, br.radii_proximal, br.radii_distal, prox, dist)
+                area = lateral_area_um2(fr)
+                left, right = split_frusta(fr, 0.5 * (prox + dist))
+                fp = axial_factor_per_cm(left) if left else 0.0
+                fd = axial_factor_per_cm(right) if right else 0.0
+                ra = float(cable[b].axial_resistivity)
+                self.cv_branch.append(b)
+                self.cv_prox.append(prox)
+                self.cv_dist.append(dist)
+                self.cv_area.append(area)
+                self.cv_rprox.append(ra * fp)
+                self.cv_rdist.append(ra * fd)
+                self.cv_cm.append(float(cable[b].membrane_capacitance))
+                self.cv_v.append(float(cable[b].resting_potential))
+                ids.append(cid)
+                cid += 1
+            self.branch_cv_ids.append(ids)
+        self.n_cv = cid
+        self.cv_area = np.asarray(self.cv_area)
+        self.cv_cm = np.asarray(self.cv_cm)
+        self.cv_v = np.asarray(self.cv_v)
+        if cell.V_init is not None:
+            self.cv_v[:] = float(cell.V_init)
+
+    def _locate_cv(self, b: int, x: float) -> int:
+        ids = self.branch_cv_ids[b]
+        if x <= 0.0 + EPS_PARAM:
+            return ids[0]
+        if x >= 1.0 - EPS_PARAM:
+            return ids[-1]
+        for c in ids:
+            if self.cv_prox[c] - EPS_PARAM <= x < self.cv_dist[c] - EPS_PARAM:
+                return c
+        for c in ids:
+            if abs(x - self.cv_dist[c]) <= EPS_PARAM:
+                return c
+        raise ValueError(f"x={x} not owned by any CV of branch {b}.")
+
+    def _node_tree(self) -> None:
+        """``build_node_tree_from_cvs`` (node_build.py:58-285)."""
+        morpho = self.morpho
+        roles: list[set] = []
+        cv_mid = np.full(self.n_cv, -1, dtype=np.int64)
+        endpoint: dict[tuple[int, float], int] = {}
+        edge_roles: dict[tuple[int, int], list] = {}
+        edge_order: list[tuple[int, int]] = []
+
+        def new_node(cv_id, pos):
+            roles.append({(cv_id, pos)})
+            return len(roles) - 1
+
+        def add_edge(p, c, cv_id, half):
+            key = (p, c)
+            if key not in edge_roles:
+                edge_roles[key] = []
+                edge_order.append(key)
+            if (cv_id, half) not in edge_roles[key]:
+                edge_roles[key].append((cv_id, half))
+
+        parent_x = {e.child.index: e.parent_x for e in morpho.edges}
+        child_x = {e.child.index: e.child_x for e in morpho.edges}
+        parent_of = {e.child.index: e.parent.index for e in morpho.edges}
+        root = new_node(self.branch_cv_ids[0][0], "prox")
+        endpoint[(0, 0.0)] = root
+        for b in range(len(morpho.branches)):
+            ids = self.branch_cv_ids[b]
+            if b == 0:
+                att, ax, order = root, 0.0, ids
+            else:
+                px = float(parent_x[b])
+                pb = parent_of[b]
+                if px <= EPS_PARAM:
+                    att = endpoint[(pb, 0.0)]
+                elif px >= 1.0 - EPS_PARAM:
+                    att = endpoint[(pb, 1.0)]
+                else:
+                    att = int(cv_mid[self._locate_cv(pb, px)])
+                ax = float(child_x[b])
+                order = ids if ax <= EPS_PARAM else list(reversed(ids))
+            entry = "prox" if ax <= EPS_PARAM else "dist"
+            exit_ = "dist" if ax <= EPS_PARAM else "prox"
+            roles[att].add((order[0], entry))
+            endpoint[(b, float(ax))] = att
+            for c in order:
+                cv_mid[c] = new_node(c, "mid")
+            term = new_node(order[-1], exit_)
+            endpoint[(b, float(1.0 - ax))] = term
+            for i, c in enumerate(order):
+                mid = int(cv_mid[c])
+                par = att if i == 0 else int(cv_mid[order[i - 1]])
+                chi = term if i == len(order) - 1 else int(cv_mid[order[i + 1]])
+                add_edge(par, mid, c, entry)
+                add_edge(mid, chi, c, exit_)
+        self.n_point = len(roles)
+        self.cv_mid = cv_mid
+        self.is_mid = np.zeros(self.n_point, dtype=bool)
+        self.is_mid[cv_mid] = True
+        self.endpoint = endpoint
+        self.edges = []
+        for key in edge_order:
+            rl = sorted(edge_roles[key])
+            self.edges.append((key[0], key[1], rl))
+
+    def _schedule(self) -> None:
+        n = self.n_point
+        node_parent = np.full(n, -1, dtype=np.int32)
+        children: list[list[int]] = [[] for _ in range(n)]
+        for p, c, _ in self.edges:
+            if node_parent[c] != -1:
+                raise ValueError("node has two parents")
+            node_parent[c] = p
+            children[p].append(c)
+        peel = compute_peel_levels(node_parent, children)
+        order = np.lexsort((np.arange(n, dtype=np.int32), -peel)).astype(np.int32)
+        row_of = np.empty(n, dtype=np.int32)
+        row_of[order] = np.arange(n, dtype=np.int32)
+        parent_rows = np.full(n, -1, dtype=np.int32)
+        for row, pid in enumerate(order.tolist()):
+            if node_parent[pid] >= 0:
+                parent_rows[row] = row_of[node_parent[pid]]
+        peels_ordered = peel[order]
+        starts = [0] + [i for i in range(1, n) if peels_ordered[i] != peels_ordered[i - 1]] + [n]
+        groups = []
+        for a, b in zip(starts[:-1], starts[1:]):
+            for s in range(a, b, self.MAX_GROUP):
+                groups.append(row_of[order[s:min(b, s + self.MAX_GROUP)]])
+        self.row_to_point = order
+        self.point_to_row = row_of
+        self.parent_rows = parent_rows
+        self.groups = groups
+        self.node_parent = node_parent
+        self.peel = peel
+
+    def _static_source(self) -> None:
+        n = self.n_point
+        row_of = self.point_to_row
+        dyn_rows = row_of[self.cv_mid]
+        cap_F = np.full(n, 1e-6)  # boundary rows: dummy 1 uF (_staggered.py:579-593)
+        cap_F[dyn_rows] = self.cv_area * 1e-8 * self.cv_cm * 1e-6
+        diag = np.zeros(n)
+        A_pc = {}
+        for p_id, c_id, rl in self.edges:
+            pr, cr = int(row_of[p_id]), int(row_of[c_id])
+            res = [self.cv_rprox[c] if h == "prox" else self.cv_rdist[c] for c, h in rl]
+            br_ids = {self.cv_branch[c] for c, _ in rl}
+            if len(res) > 1 and len(br_ids) == 1:
+                g = 1.0 / sum(res)
+            else:
+                g = sum(1.0 / r for r in res)
+            pc = g / cap_F[pr] * 1e-3  # ms^-1
+            cc = g / cap_F[cr] * 1e-3
+            diag[pr] += pc
+            diag[cr] += cc
+            A_pc[(pr, cr)] = -pc
+            A_pc[(cr, pr)] = -cc
+        lowers = np.zeros(n)
+        uppers = np.zeros(n)
+        for row, prow in enumerate(self.parent_rows.tolist()):
+            if prow < 0:
+                continue
+            lowers[row] = A_pc[(row, prow)]
+            uppers[row] = A_pc[(prow, row)]
+        parent_lookup = np.empty(n + 1, dtype=np.int32)
+        parent_lookup[:n] = np.where(self.parent_rows >= 0, self.parent_rows, n)
+        parent_lookup[n] = n
+        edges, level_size = [], []
+        for grp in reversed(self.groups):
+            le = [[int(r), int(self.parent_rows[r])] for r in grp.tolist() if self.parent_rows[r] >= 0]
+            if le:
+                edges.extend(le)
+                level_size.append(len(le))
+        self.dhs_edges = np.asarray(edges, dtype=np.int64).reshape(-1, 2)
+        self.level_offsets = np.cumsum([0] + level_size).astype(np.int64)
+        self.backsub = build_backsub_indices(parent_lookup, n)
+        self.dyn_rows = dyn_rows
+        self.diag_ms = diag
+        self.lowers_ms = lowers
+        self.uppers_ms = uppers
+        self.row_cap_uF = cap_F * 1e6
+
+    # ------------------------------------------------------------ mechanisms
+    def _mechanisms(self, cell) -> None:
+        """Dense point-space parameters (g = 0 off the painted points)."""
+        from braincell_gb300.mech import Channel, Ion
+
+        n = self.n_point
+        self.chan = {}  # name -> dict(param arrays over points, mask)
+        self.E_na = np.full(n, ION_DEFAULTS["SodiumFixed"]["E"])
+        self.E_k = np.full(n, ION_DEFAULTS["PotassiumFixed"]["E"])
+        self.E_ca_fixed = np.full(n, ION_DEFAULTS["CalciumFixed"]["E"])
+        self.ca_dyn = None
+        for b, decls in enumerate(self.branch_mechs):
+            last = {}
+            for d in decls:
+                last[("IL" if d.class_name == "leaky" else d.class_name)] = d
+            pts = self.cv_mid[self.branch_cv_ids[b]]
+            for name, d in last.items():
+                if isinstance(d, Ion):
+                    p = _resolve(ION_DEFAULTS, d)
+                    if name == "SodiumFixed":
+                        self.E_na[pts] = p["E"]
+                    elif name == "PotassiumFixed":
+                        self.E_k[pts] = p["E"]
+                    elif name == "CalciumFixed":
+                        self.E_ca_fixed[pts] = p["E"]
+                    elif name == "CalciumDetailed":
+                        if self.ca_dyn is None:
+                            self.ca_dyn = {k: np.zeros(n) for k in ("d", "tau", "C_rest", "Co", "temp", "Ci0")}
+                            self.ca_dyn["d"][:] = 1.0
+                            self.ca_dyn["tau"][:] = 1.0
+                            self.ca_dyn["C_rest"][:] = ION_DEFAULTS["CalciumDetailed"]["C_rest"]
+                            self.ca_dyn["Co"][:] = ION_DEFAULTS["CalciumDetailed"]["Co"]
+                            self.ca_dyn["temp"][:] = ION_DEFAULTS["CalciumDetailed"]["temp"]
+                            self.ca_dyn["Ci0"][:] = _CA_FIXED_CI
+                            self.ca_dyn["mask"] = np.zeros(n, dtype=bool)
+                        for k, src in (("d", "d"), ("tau", "tau"), ("C_rest", "C_rest"), ("Co", "Co"),
+                                       ("temp", "temp"), ("Ci0", "Ci_initializer")):
+                            self.ca_dyn[k][pts] = p[src]
+                        self.ca_dyn["mask"][pts] = True
+                    else:
+                        raise ValueError(f"unsupported ion {name}")
+                    continue
+                assert isinstance(d, Channel)
+                p = _resolve(CHANNEL_DEFAULTS, d)
+                if name not in self.chan:
+                    self.chan[name] = {"mask": np.zeros(n, dtype=bool)}
+                    for k in p:
+                        self.chan[name][k] = np.zeros(n)
+                ch = self.chan[name]
+                ch["mask"][pts] = True
+                for k, v in p.items():
+                    if k not in ch:
+                        ch[k] = np.zeros(n)
+                    ch[k][pts] = v
+        # the fixed-Ca Ci seen by AHP where no dynamic calcium is painted
+        self.Ci_fixed = np.full(n, _CA_FIXED_CI)
+
+    def _points(self, cell) -> None:
+        from braincell_gb300.mech import CurrentClamp, StateProbe
+
+        self.clamps_mid = []  # (point, t_on, t_off, amp_nA)
+        self.clamps_edge = []
+        self.probe_points = []
+        for locset, decls in cell.place_rules:
+            for (b, x) in locset.points(self.morpho):
+                if x <= EPS_PARAM:
+                    pid = self.endpoint[(b, 0.0)] if (b, 0.0) in self.endpoint else None
+                elif x >= 1.0 - EPS_PARAM:
+                    pid = self.endpoint[(b, 1.0)] if (b, 1.0) in self.endpoint else None
+                else:
+                    pid = int(self.cv_mid[self._locate_cv(b, x)])
+                if pid is None:
+                    raise ValueError("locset point not found")
+                for d in decls:
+                    if isinstance(d, CurrentClamp):
+                        for (t_on, t_off, amp) in d.segments():
+                            (self.clamps_mid if self.is_mid[pid] else self.clamps_edge).append((pid, t_on, t_off, amp))
+                    elif isinstance(d, StateProbe):
+                        self.probe_points.append(pid)
+        self.point_area_um2 = np.zeros(self.n_point)
+        self.point_area_um2[self.cv_mid] = self.cv_area
+
+    # ------------------------------------------------------------ state
+    def reset_state(self) -> None:
+        """``Cell.reset_state`` (cell.py:2529-2550) + ``HH.reset_state`` (channel/_base.py:560-573)."""
+        P, n = self.P, self.n_point
+        self.V = np.broadcast_to(self.cv_v, (P, self.n_cv)).copy()
+        self.t_step = 0
+        pv = self.cv_to_point(self.V)
+        self.Ci = None
+        if self.ca_dyn is not None:
+            self.Ci = np.broadcast_to(self.ca_dyn["Ci0"], (P, n)).copy()
+        self.gates = {}
+        for name, ch in self.chan.items():
+            if name not in _GATES:
+                continue
+            r = rates(name, pv, ch, Ci=self._ci_for_channels())
+            for gate, _power, _phik in _GATES[name]:
+                kind, a, b = r[gate]
+                self.gates[(name, gate)] = (a / (a + b) if kind == "ab" else a) * np.ones((P, n))
+        self.spike = np.zeros((P, self.n_cv))
+
+    def cv_to_point(self, v):
+        out = np.zeros(v.shape[:-1] + (self.n_point,))
+        out[..., self.cv_mid] = v
+        return out
+
+    def _ci_for_channels(self):
+        if self.Ci is None:
+            return self.Ci_fixed
+        return np.where(self.ca_dyn["mask"], self.Ci, self.Ci_fixed)
+
+    def _E_ca(self):
+        if self.Ci is None:
+            return self.E_ca_fixed
+        cd = self.ca_dyn
+        nernst = 1e3 * GAS_R * cd["temp"] / (2.0 * FARADAY) * np.log(cd["Co"] / np.where(cd["mask"], self.Ci, 1.0))
+        return np.where(cd["mask"], nernst, self.E_ca_fixed)
+
+    def _gate_product(self, name):
+        prod = 1.0
+        for gate, power, _ in _GATES[name]:
+            x = self.gates[(name, gate)]
+            prod = prod * (x if power == 1 else x ** power)
+        return prod
+
+    def _channel_currents(self, pv):
+        """Total ionic current density and its V-derivative (uA/cm^2, uA/cm^2/mV) per point."""
+        I = np.zeros_like(pv)
+        dI = np.zeros_like(pv)
+        E_ca = self._E_ca()
+        E_of = {"na": self.E_na, "k": self.E_k, "ca": E_ca}
+        for name, ch in self.chan.items():
+            g = ch["g_max"]
+            if name == "IL":
+                E = ch["E"]
+                fac = 1.0
+            elif name == "K_Leak":
+                E, fac = self.E_k, 1.0
+            elif name == "HCN_HM1992":
+                E, fac = ch["E"], self._gate_product(name)
+            else:
+                E, fac = E_of[_ION_OF[name]], self._gate_product(name)
+            geff = g * fac
+            I = I + geff * (E - pv)
+            dI = dI - geff
+        return I, dI
+
+    def _ca_current(self, pv):
+        """``Ion.current`` of the calcium ion (sum of CaL + CaT), uA/cm^2."""
+        I = np.zeros_like(pv)
+        E_ca = self._E_ca()
+        for name in ("CaL_IS2008", "CaT_HM1992"):
+            if name in self.chan:
+                I = I + self.chan[name]["g_max"] * self._gate_product(name) * (E_ca - pv)
+        return I
+
+    def _clamp_nA(self, clamps, t: float):
+        cur = np.zeros((self.P, self.n_point))
+        for pid, t_on, t_off, amp in clamps:
+            lt = t  # absolute time; delay folded into t_on/t_off
+            if t_on <= lt < t_off:
+                cur[:, pid] += amp
+        return cur
+
+    # ------------------------------------------------------------ one step
+    def step(self, dt: float, t: float | None = None) -> np.ndarray:
+        """Advance one staggered step; returns the spike indicator ``(P, n_cv)``."""
+        if t is None:
+            t = self.t_step * dt
+        P = self.P
+        n = self.n_point
+        V_n = self.V
+        last_V = V_n
+        pv = self.cv_to_point(V_n)
+        # a2: cache ion total current at step start
+        I_ca_cached = self._ca_current(pv) if self.Ci is not None else None
+        # a6: linearise (point mode): derivative = I/C at midpoints, linear = dI/dV / C
+        I_pt, dI_pt = self._channel_currents(pv)
+        clamp_nA = self._clamp_nA(self.clamps_mid, t)
+        safe_area = np.where(self.is_mid, self.point_area_um2, 1.0)
+        I_pt = I_pt + np.where(self.is_mid, clamp_nA * 1e5 / safe_area, 0.0)
+        C_pt = np.ones(n)
+        C_pt[self.cv_mid] = self.cv_cm
+        deriv = np.where(self.is_mid, I_pt / C_pt, 0.0)
+        lin = np.where(self.is_mid, dI_pt / C_pt, 0.0)
+        linear = lin[:, self.cv_mid]
+        derivative = deriv[:, self.cv_mid]
+        const = derivative - V_n * linear
+        # a7: numeric state
+        diags = np.broadcast_to(np.concatenate([self.diag_ms * dt, [1.0]]), (P, n + 1)).copy()
+        diags[:, self.dyn_rows] += 1.0 - dt * linear
+        solves = np.zeros((P, n + 1))
+        solves[:, self.dyn_rows] = V_n + dt * const
+        if self.clamps_edge:
+            edge_nA = self._clamp_nA(self.clamps_edge, t)
+            by_row = edge_nA[:, self.row_to_point]
+            solves[:, :n] += dt * (by_row / self.row_cap_uF) * 1e-3
+        lowers = np.concatenate([self.lowers_ms * dt, [0.0]])
+        uppers = np.concatenate([self.uppers_ms * dt, [0.0]])
+        # a8: forward elimination, one level at a time (leaves first)
+        E = self.dhs_edges
+        for i in range(len(self.level_offsets) - 1):
+            a, b = self.level_offsets[i], self.level_offsets[i + 1]
+            ch, par = E[a:b, 0], E[a:b, 1]
+            m = uppers[ch] / diags[:, ch]
+            np.add.at(diags, (slice(None), par), -lowers[ch] * m)
+            np.add.at(solves, (slice(None), par), -solves[:, ch] * m)
+        # a9: recursive-doubling back substitution
+        low = lowers.copy()
+        low[0] = 0.0
+        le = -low / diags
+        se = solves / diags
+        for k in self.backsub:
+            se = se + le * se[:, k]
+            le = le * le[:, k]
+        # a10: restore midpoint voltage
+        V_new = se[:, self.dyn_rows]
+        self.V = V_new
+        pv_new = self.cv_to_point(V_new)
+        # a11 (a): dependent ion self states -- Ci with the cached step-start current
+        if self.Ci is not None:
+            cd = self.ca_dyn
+            d_m = cd["d"]
+            drive = I_ca_cached * 10.0 / (2.0 * FARADAY * d_m)
+            drive = np.maximum(drive, 0.0)
+            f = drive + (cd["C_rest"] - self.Ci) / cd["tau"]
+            lam = -1.0 / cd["tau"]
+            Ci_new = self.Ci + dt * exprel(dt * lam) * f
+            self.Ci = np.where(cd["mask"], Ci_new, self.Ci)
+        # a11 (c): dependent channels, exp-Euler per gate at the new voltage (and new Ci)
+        Ci_now = self._ci_for_channels()
+        new_gates = {}
+        for name, ch in self.chan.items():
+            if name not in _GATES:
+                continue
+            r = rates(name, pv_new, ch, Ci=Ci_now)
+            for gate, _power, phik in _GATES[name]:
+                x = self.gates[(name, gate)]
+                phi = ch[phik]
+                kind, a, b = r[gate]
+                if kind == "ab":
+                    f = phi * (a * (1.0 - x) - b * x)
+                    lam = -phi * (a + b)
+                else:
+                    f = phi * (a - x) / b
+                    lam = -phi / b
+                new_gates[(name, gate)] = x + dt * exprel(dt * lam) * f
+        self.gates.update(new_gates)
+        # a16: spike = last_V < V_th <= V
+        spk = ((V_new - self.V_th) >= 0.0) & ((self.V_th - last_V) > 0.0)
+        self.spike = spk.astype(np.float64)
+        self.t_step += 1
+        return self.spike
+
+    # ------------------------------------------------------------ driver
+    def run(self, dt: float, n_steps: int, record_every: int = 1):
+        """Run ``n_steps``; return (probe traces [P, n_probe, n_rec], spike times per (P, probe))."""
+        traces = []
+        spikes = [[[] for _ in self.probe_points] for _ in range(self.P)]
+        probe_cv = [int(np.nonzero(self.cv_mid == pid)[0][0]) if self.is_mid[pid] else None
+                    for pid in self.probe_points]
+        for s in range(n_steps):
+            t = self.t_step * dt
+            Vold = self.V.copy()
+            self.step(dt, t)
+            for j, c in enumerate(probe_cv):
+                if c is None:
+                    continue
+                v0, v1 = Vold[:, c], self.V[:, c]
+                hit = (v0 < self.V_th) & (v1 >= self.V_th)
+                for p in np.nonzero(hit)[0]:
+                    frac = (self.V_th - v0[p]) / (v1[p] - v0[p])
+                    spikes[p][j].append(t + dt * frac)
+            if (s + 1) % record_every == 0:
+                traces.append(np.stack([self.V[:, c] if c is not None else np.full(self.P, np.nan)
+                                        for c in probe_cv], axis=1))
+        tr = np.stack(traces, axis=-1) if traces else np.zeros((self.P, len(probe_cv), 0))
+        return tr, spikes
