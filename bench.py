@@ -1,0 +1,323 @@
+"""Benchmark: compartment-steps/s of the GB300 Cell step on the uneven-morphology workload.
+
+Workload (the configuration the headline metric is quoted on): 10,000 cells with
+random binary/ternary dendritic trees (branch probability 0.7, max depth 8, seed 1),
+50-2,000 compartments each (log-uniform, ~10 per 100 um), Na/KDR soma, CaL
+dendrites, HCN + K_Leak + leak everywhere with per-cell lognormal conductance
+factors, soma clamp 0.05-0.4 nA from 5-20 ms; 200 ms at dt = 0.025 ms (8,000
+staggered steps), FP32 with float-float voltage.  One benchmark "step" is one
+full 200 ms simulation of all 10,000 cells from reset.  Inputs are generated
+(seeded), there is no dataset.
+
+``python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]``
+prints one JSON line.  Under torchrun (N > 1) every rank simulates its own copy of
+the workload (replicas only: cells are independent, no data-path collective) and
+rank 0 prints the aggregate.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "compartment-steps/s on 1 GB300, plain vs surrogate at <=0.1 ms spike-time error"
+UNIT = "compartment-steps/s"
+BYTES_PER_COMPARTMENT_STEP = 56  # algorithmic bytes per compartment-step of this workload
+DT = 0.025
+SIM_STEPS = 8000
+
+
+def _args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--cells", type=int, default=10000)
+    ap.add_argument("--sim-steps", type=int, default=SIM_STEPS)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--tile-nodes", type=int, default=2000)
+    ap.add_argument("--threads", type=int, default=256)
+    ap.add_argument("--threads-big", type=int, default=512)
+    ap.add_argument("--steps-per-launch", type=int, default=1000)
+    return ap.parse_args()
+
+
+def _dist():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def _traffic_per_compartment_step():
+    """DRAM bytes per compartment-step from the committed ncu summary, if present."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "tile_step_uneven.json")) as f:
+            return float(json.load(f)["dram_bytes_per_compartment_step"])
+    except Exception:
+        return None
+
+
+class ClockSampler:
+    """nvidia-smi SM clock / throttle sampling while the timed region runs."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(
+                    ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits"],
+                    capture_output=True, text=True, timeout=5)
+                if out.returncode == 0:
+                    self.samples.append([x.strip() for x in out.stdout.strip().split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *exc):
+        self._stop.set()
+        if self._t is not None:
+            self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for s in self.samples for k in range(4) if len(s) > 3 + k and s[3 + k] == "Active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def cpu_baseline(cells: int = 6, steps: int = 200, seed: int = 1):
+    """The float64 oracle (one core) on a bounded sample of the same workload."""
+    from braincell_gb300 import workloads as W
+    from oracle.staggered import OracleCell
+
+    descs = W.uneven(indices=range(cells), seed=seed)
+    ncv = 0
+    t0 = time.perf_counter()
+    for d in descs:
+        oc = OracleCell(W.desc_to_cell(d))
+        for _ in range(steps):
+            oc.step(DT)
+        ncv += oc.n_cv
+    el = time.perf_counter() - t0
+    return {"value": ncv * steps / el, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"first {cells} cells of the workload x {steps} steps, float64 NumPy oracle on one core"}
+
+
+def _oracle_cells_worker(args):
+    idx, steps = args
+    from braincell_gb300 import workloads as W
+    from oracle.staggered import OracleCell
+
+    d = W.uneven(indices=[idx])[0]
+    oc = OracleCell(W.desc_to_cell(d))
+    for _ in range(steps):
+        oc.step(DT)
+    return oc.n_cv
+
+
+def run_reference(a):
+    """Reference arm: the CPU restatement of the reference path on all host cores."""
+    import multiprocessing as mp
+
+    rank, world, _ = _dist()
+    if rank != 0:
+        return
+    cores = os.cpu_count() or 1
+    steps_per = 100
+    cells_per_step = cores
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores) as pool:
+        jobs = [(i, steps_per) for i in range(cells_per_step)]
+        pool.map(_oracle_cells_worker, [(i, 5) for i in range(cells_per_step)])  # warm-up (imports)
+        times, work = [], 0
+        t_all = time.perf_counter()
+        for s in range(a.steps):
+            jobs = [(s * cells_per_step + i, steps_per) for i in range(cells_per_step)]
+            t0 = time.perf_counter()
+            ncv = pool.map(_oracle_cells_worker, jobs)
+            times.append(time.perf_counter() - t0)
+            work += sum(ncv) * steps_per
+        el = time.perf_counter() - t_all
+    value = work / el
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": a.gpus, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": 1e3 * el / a.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "uneven-morphology batch (10,000 cells, 50-2000 compartments, 200 ms at dt 0.025 ms)",
+                   "sample": f"{cells_per_step} cells x {steps_per} steps per step"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{cells_per_step} cells x {steps_per} steps per bench step, one process per core"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference (JAX/brainstate) is not installable offline; its CPU path is timed through the "
+                "float64 restatement of the same algorithm",
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(a):
+    import torch
+
+    from braincell_gb300 import workloads as W
+    from braincell_gb300.build import build_native
+    from braincell_gb300.runtime import Plan
+    from braincell_gb300.shard import reduce_max
+
+    rank, world, local = _dist()
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    build_native()
+    # replicas only: every rank runs its own copy of the workload (its own seed)
+    descs = W.uneven(a.cells, seed=1 + rank)
+    batch = W.descs_to_batch(descs)
+    plan = Plan(batch, precision="f32", device=local, tile_nodes=a.tile_nodes, threads_per_tile=a.threads,
+                threads_big=a.threads_big, steps_per_launch=a.steps_per_launch, record_every=0)
+    info = plan.info
+    n_cv = plan.n_cv
+    stream = torch.cuda.current_stream(local)
+    sid = int(stream.cuda_stream)
+
+    def one_step():
+        plan.reset(stream=sid)
+        plan.run(a.sim_steps, DT, stream=sid, check=False)
+
+    for _ in range(a.warmup):
+        one_step()
+    plan.check(stream=sid)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clocks:
+        t_wall = time.perf_counter()
+        ev0.record(stream)
+        for _ in range(a.steps):
+            one_step()
+        ev1.record(stream)
+        ev1.synchronize()
+        t_wall = time.perf_counter() - t_wall
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    plan.check(stream=sid)
+    ms = ev0.elapsed_time(ev1)
+    ms = reduce_max(ms)
+    comp_steps = n_cv * a.sim_steps * a.steps
+    value = comp_steps * world / (ms * 1e-3)
+
+    # kernel-only time of one simulation (the dominant kernel's launches), same stream
+    plan.reset(stream=sid)
+    kernel_ms = plan.run_timed(a.sim_steps, DT, stream=sid)
+    launches_per_sim = -(-a.sim_steps // info["steps_per_launch"]) * info["n_launch_classes"]
+
+    # end to end through the C ABI with host buffers: upload the initial voltages,
+    # run the simulation, download the final voltages and spike counts
+    v_host = plan.state("V", stream=sid)
+    plan.reset(stream=sid)
+    torch.cuda.synchronize()
+    e2e_t = []
+    for _ in range(max(1, a.steps)):
+        t0 = time.perf_counter()
+        plan.set_state("V", v_host, stream=sid)
+        plan.run(a.sim_steps, DT, stream=sid)
+        v_out = plan.state("V", stream=sid)
+        counts = plan.spike_counts(stream=sid)
+        e2e_t.append(time.perf_counter() - t0)
+        plan.reset(stream=sid)
+    e2e_s = reduce_max(float(np.median(e2e_t)))
+    e2e_value = n_cv * a.sim_steps * world / e2e_s
+    # bytes the API moves: upload = values + hi/lo offset tables (24 B/CV); download = its
+    # offset tables up (16 B/CV) and values down (8 B/CV); spike counts down (4 B/probe)
+    h2d_total = 24 * n_cv + 16 * n_cv
+    d2h = 8 * n_cv + 4 * int(counts.size)
+
+    peak, peak_kind = _peaks()
+    achieved_gbs = BYTES_PER_COMPARTMENT_STEP * n_cv * a.sim_steps / (kernel_ms * 1e-3) / 1e9
+    traffic_per_cs = _traffic_per_compartment_step()
+    units_per_launch = n_cv * info["steps_per_launch"]
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
+        "ms_per_step": ms / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded generator; no dataset)",
+        "config": {"workload": "uneven-morphology batch: 10,000 cells, 50-2000 compartments, 200 ms at dt 0.025 ms "
+                               "(8,000 staggered steps), FP32 + float-float V",
+                   "cells_per_gpu": a.cells, "compartments_per_gpu": n_cv, "sim_steps": a.sim_steps,
+                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                   "l2": "inputs larger than L2 (tile blobs + state arrays > 129 MB)",
+                   "tiles": info["n_tiles"], "threads_per_tile": info["threads_per_tile"],
+                   "tile_nodes": info["tile_nodes"], "steps_per_launch": info["steps_per_launch"]},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d_total), "d2h_bytes_per_step": int(d2h),
+                "path": "bc_state_upload (V) -> bc_run (8,000 steps) -> bc_state_download (V) + bc_spike_download"},
+        "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": peak, "unit": "GB/s",
+                     "frac": achieved_gbs / peak, "peak_kind": peak_kind,
+                     "traffic": (traffic_per_cs * units_per_launch) if traffic_per_cs else None,
+                     "algorithmic_bytes_per_launch": BYTES_PER_COMPARTMENT_STEP * units_per_launch,
+                     "kernel_ms_per_sim": kernel_ms, "launches_per_sim": launches_per_sim},
+        "gpu_launches": a.steps * (1 + launches_per_sim),
+        "clocks": clocks.summary(),
+        "wall_s_timed": t_wall,
+    }
+    if rank == 0 and world == 1 and not a.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    plan.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    a = _args()
+    if a.warmup < 3:
+        a.warmup = 3
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_ours(a)
+
+
+if __name__ == "__main__":
+    main()

@@ -192,6 +192,11 @@ SIGNATURES = {
     "bc_plan_info": (C.c_int32, [C.c_void_p, _p(PlanInfo)]),
     "bc_plan_cell_ncv": (C.c_int32, [C.c_void_p, _p(C.c_int64)]),
     "bc_plan_tile_stats": (C.c_int32, [C.c_void_p, _p(C.c_int64)]),
+    "bc_lower_cell": (
+        C.c_int32,
+        [_p(BatchSpec), C.c_int64, _p(C.c_int32), _p(C.c_int32), _p(C.c_double), _p(C.c_int32), _p(C.c_int32),
+         _p(C.c_double), _p(C.c_double), _p(C.c_double), _p(C.c_int32)],
+    ),
     "bc_reset": (C.c_int32, [C.c_void_p, C.c_void_p]),
     "bc_run": (C.c_int32, [C.c_void_p, C.c_int64, C.c_double, C.c_void_p]),
     "bc_run_async": (C.c_int32, [C.c_void_p, C.c_int64, C.c_double, C.c_void_p]),

@@ -24,7 +24,7 @@ from . import _abi
 from .catalogue import region_record
 from .mech import CableProperty, CurrentClamp, StateProbe
 
-__all__ = ["CellBatch", "lower_cell", "concat_batches"]
+__all__ = ["CellBatch", "lower_cell", "concat_batches", "native_lowering"]
 
 
 def _ptr(a: np.ndarray, ctype):
@@ -139,6 +139,27 @@ class CellBatch:
         s.n_pulses = int(self.pulse_cell.size)
         s.n_probes = int(self.probe_cell.size)
         return s, tuple(keep)
+
+
+def native_lowering(batch: CellBatch, cell: int) -> dict:
+    """The native library's lowering of one cell (point tree + axial coefficients)."""
+    lib = _abi.lib()
+    spec, keep = batch.to_spec()
+    ncv, nn = C.c_int32(), C.c_int32()
+    _abi.check(lib.bc_lower_cell(C.byref(spec), int(cell), C.byref(ncv), C.byref(nn), None, None, None, None, None,
+                                 None, None))
+    out = {
+        "cv_area": np.zeros(ncv.value), "cv_node": np.zeros(ncv.value, np.int32), "parent": np.zeros(nn.value, np.int32),
+        "alpha": np.zeros(nn.value), "beta": np.zeros(nn.value), "diag": np.zeros(nn.value),
+        "region": np.zeros(nn.value, np.int32),
+    }
+    d, i32 = C.POINTER(C.c_double), C.POINTER(C.c_int32)
+    _abi.check(lib.bc_lower_cell(
+        C.byref(spec), int(cell), C.byref(ncv), C.byref(nn), out["cv_area"].ctypes.data_as(d),
+        out["cv_node"].ctypes.data_as(i32), out["parent"].ctypes.data_as(i32), out["alpha"].ctypes.data_as(d),
+        out["beta"].ctypes.data_as(d), out["diag"].ctypes.data_as(d), out["region"].ctypes.data_as(i32)))
+    del keep
+    return out
 
 
 def concat_batches(batches: list[CellBatch]) -> CellBatch:

@@ -193,14 +193,14 @@ __device__ __forceinline__ void node_mechanisms(Real* st, int N, const Real* P, 
     if (m & BC_M_NA) {
       const NaRates<Real> r(v_new, P[BC_P_NA_VSH]);
       const Real phi = P[BC_P_NA_PHI];
-      nap = gate_ab(nap, r.ap, r.bp, phi, dt);
-      naq = gate_ab(naq, r.aq, r.bq, phi, dt);
+      nap = gate_ab<Real, true>(nap, r.ap, r.bp, phi, dt);
+      naq = gate_ab<Real, true>(naq, r.aq, r.bq, phi, dt);
       st[kSlotNaP * N] = nap;
       st[kSlotNaQ * N] = naq;
     }
     if (m & BC_M_KDR) {
       const KdrRates<Real> r(v_new, P[BC_P_KDR_VSH]);
-      kdrp = gate_ab(kdrp, r.a, r.b, P[BC_P_KDR_PHI], dt);
+      kdrp = gate_ab<Real, true>(kdrp, r.a, r.b, P[BC_P_KDR_PHI], dt);
       st[kSlotKdrP * N] = kdrp;
     }
     if (m & BC_M_CAL) {

@@ -32,6 +32,8 @@ __device__ __forceinline__ double dpow(double x, double y) { return pow(x, y); }
 // __fdividef: a few ulp, far below what the rates need); FP64 stays exact so the
 // FP64 build remains an oracle-grade run of the same kernels.
 __device__ __forceinline__ float rexp(float x) { return __expf(x); }
+__device__ __forceinline__ float aexp(float x) { return expf(x); }
+__device__ __forceinline__ double aexp(double x) { return exp(x); }
 __device__ __forceinline__ double rexp(double x) { return exp(x); }
 __device__ __forceinline__ float rdiv(float a, float b) { return __fdividef(a, b); }
 __device__ __forceinline__ double rdiv(double a, double b) { return a / b; }
@@ -54,10 +56,12 @@ __device__ __forceinline__ Real exprel(Real x) {
 
 // One exp-Euler step y += dt * exprel(dt * lam) * f of a gate whose right-hand
 // side is affine in the gate: with lam = -phi (a + b) and f = -lam (x_inf - x) the
-// step is x - expm1(dt * lam) * (x_inf - x).
-template <typename Real>
+// step is x - expm1(dt * lam) * (x_inf - x).  kExact selects IEEE division and
+// expm1 (the spike-generating Na / K gates) over the fast forms.
+template <typename Real, bool kExact = false>
 __device__ __forceinline__ Real gate_ab(Real x, Real a, Real b, Real phi, Real dt) {
   const Real s = a + b;
+  if (kExact) return x - dexpm1(-dt * phi * s) * (a / s - x);
   const Real xinf = rdiv(a, s);
   return x - decay_em1(-dt * phi * s) * (xinf - x);
 }
@@ -75,8 +79,8 @@ struct NaRates {
     const Real vp = v - vsh;
     ap = Real(0.32 * 4.0) / exprel(-(vp - Real(13)) * Real(1.0 / 4));
     bp = Real(0.28 * 5.0) / exprel((vp - Real(40)) * Real(1.0 / 5));
-    aq = Real(0.128) * rexp(-(vp - Real(17)) * Real(1.0 / 18));
-    bq = rdiv(Real(4), Real(1) + rexp(-(vp - Real(40)) * Real(1.0 / 5)));
+    aq = Real(0.128) * aexp(-(vp - Real(17)) * Real(1.0 / 18));
+    bq = Real(4) / (Real(1) + aexp(-(vp - Real(40)) * Real(1.0 / 5)));
   }
 };
 
@@ -86,7 +90,7 @@ struct KdrRates {
   __device__ __forceinline__ KdrRates(Real v, Real vsh) {
     const Real vp = v - vsh;
     a = Real(0.032 * 5.0) / exprel(-(vp - Real(15)) * Real(1.0 / 5));
-    b = Real(0.5) * rexp(-(vp - Real(10)) * Real(1.0 / 40));
+    b = Real(0.5) * aexp(-(vp - Real(10)) * Real(1.0 / 40));
   }
 };
 

@@ -1065,6 +1065,26 @@ bc_status bc_plan_create(const bc_batch_spec* spec, const bc_plan_options* opts_
   return bc_reset(p, nullptr);
 }
 
+bc_status bc_lower_cell(const bc_batch_spec* spec, int64_t cell, int32_t* n_cv, int32_t* n_node, double* cv_area,
+                        int32_t* cv_node, int32_t* parent, double* alpha, double* beta, double* diag,
+                        int32_t* region) {
+  if (!spec || !n_cv || !n_node) return fail(BC_ERR_INVALID, "null argument");
+  if (cell < 0 || cell >= spec->n_cells) return fail(BC_ERR_INVALID, "cell out of range");
+  LoweredCell lc;
+  bc_status st = lower_cell(*spec, cell, lc);
+  if (st != BC_OK) return st;
+  *n_cv = lc.n_cv;
+  *n_node = lc.n_node;
+  if (cv_area) std::copy(lc.cv_area.begin(), lc.cv_area.end(), cv_area);
+  if (cv_node) std::copy(lc.cv_node.begin(), lc.cv_node.end(), cv_node);
+  if (parent) std::copy(lc.parent.begin(), lc.parent.end(), parent);
+  if (alpha) std::copy(lc.alpha.begin(), lc.alpha.end(), alpha);
+  if (beta) std::copy(lc.beta.begin(), lc.beta.end(), beta);
+  if (diag) std::copy(lc.diag.begin(), lc.diag.end(), diag);
+  if (region) std::copy(lc.region.begin(), lc.region.end(), region);
+  return BC_OK;
+}
+
 bc_status bc_plan_destroy(bc_plan_t p) {
   if (!p) return fail(BC_ERR_INVALID, "null plan");
   free_plan(p);
@@ -1090,6 +1110,7 @@ bc_status bc_plan_info(bc_plan_t p, bc_plan_info_t* info) {
   info->max_chain_nodes = p->max_chain_nodes;
   info->state_slots = p->state_slots;
   info->reserved[0] = p->n_smem_tiles;
+  info->reserved[1] = int32_t(p->classes.size());
   return BC_OK;
 }
 

@@ -74,6 +74,20 @@ class Branch:
             raise ValueError("Branch total length must be > 1e-6 um.")
         if type not in _TYPES:
             raise ValueError(f"Unknown branch type {type!r}; expected one of {_TYPES}.")
+        if radii is None and lengths_a.size > 1:
+            # zero-length jump segments at radius discontinuities (morph/branch.py:440-500)
+            disc = ~np.isclose(rd[:-1], rp[1:])
+            if disc.any():
+                L, P, D = [], [], []
+                for i in range(lengths_a.size):
+                    L.append(lengths_a[i])
+                    P.append(rp[i])
+                    D.append(rd[i])
+                    if i < lengths_a.size - 1 and disc[i]:
+                        L.append(0.0)
+                        P.append(rd[i])
+                        D.append(rp[i + 1])
+                lengths_a, rp, rd = np.asarray(L), np.asarray(P), np.asarray(D)
         return cls(lengths=lengths_a, radii_proximal=rp, radii_distal=rd, type=type)
 
     @property

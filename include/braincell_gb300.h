@@ -197,6 +197,17 @@ bc_status bc_plan_info(bc_plan_t plan, bc_plan_info_t* info);
  * 1 single-cell shared-memory tile, 2 global-memory tile), shared bytes. */
 bc_status bc_plan_tile_stats(bc_plan_t plan, int64_t* out /* [n_tiles * 6] */);
 
+/* The native lowering of one cell, for checking against other assemblies (host
+ * only, no CUDA).  Points are numbered like the reference's node tree
+ * (_discretization/node_build.py:58-285).  Pass NULL arrays to query the sizes.
+ *   cv_area [n_cv] um^2, cv_node [n_cv] midpoint point of each CV,
+ *   parent [n_node], alpha / beta / diag [n_node] axial coefficients in 1/ms
+ *   (row i: diag_i x_i - alpha_i x_parent - sum_c beta_c x_c), region [n_node]
+ *   (-1 on boundary points). */
+bc_status bc_lower_cell(const bc_batch_spec* spec, int64_t cell, int32_t* n_cv, int32_t* n_node, double* cv_area,
+                        int32_t* cv_node, int32_t* parent, double* alpha, double* beta, double* diag,
+                        int32_t* region);
+
 /* Sizes of the host-side views (CV count per cell, in reference CV order). */
 bc_status bc_plan_cell_ncv(bc_plan_t plan, int64_t* ncv_out /* [n_cells] */);
 

@@ -52,6 +52,7 @@ __all__ = [
     "OracleCell",
     "Frustum",
     "build_frusta",
+    "insert_radius_jumps",
     "lateral_area_um2",
     "axial_factor_per_cm",
     "midpoint_radius_um",
@@ -106,6 +107,26 @@ class Frustum:
     length_um: float
     r_prox_um: float
     r_dist_um: float
+
+
+def insert_radius_jumps(lengths, r_prox, r_dist):
+    """Zero-length jump segments at radius discontinuities (``morph/branch.py:440-500``)."""
+    lengths = np.asarray(lengths, dtype=float)
+    r_prox = np.asarray(r_prox, dtype=float)
+    r_dist = np.asarray(r_dist, dtype=float)
+    if lengths.size <= 1:
+        return lengths, r_prox, r_dist
+    disc = ~np.isclose(r_dist[:-1], r_prox[1:])
+    L, P, D = [], [], []
+    for i in range(lengths.size):
+        L.append(lengths[i])
+        P.append(r_prox[i])
+        D.append(r_dist[i])
+        if i < lengths.size - 1 and disc[i]:
+            L.append(0.0)
+            P.append(r_dist[i])
+            D.append(r_prox[i + 1])
+    return np.asarray(L), np.asarray(P), np.asarray(D)
 
 
 def build_frusta(lengths, r_prox, r_dist, prox: float, dist: float) -> tuple[Frustum, ...]:
@@ -604,9 +625,11 @@ class OracleCell:
                 assert isinstance(d, Channel)
                 p = _resolve(CHANNEL_DEFAULTS, d)
                 if name not in self.chan:
+                    # dense over points: conductance 0 off the painted mask, every other
+                    # parameter broadcast from the first painted value (bindings.py:723-741)
                     self.chan[name] = {"mask": np.zeros(n, dtype=bool)}
-                    for k in p:
-                        self.chan[name][k] = np.zeros(n)
+                    for k, v in p.items():
+                        self.chan[name][k] = np.zeros(n) if k == "g_max" else np.full(n, float(v))
                 ch = self.chan[name]
                 ch["mask"][pts] = True
                 for k, v in p.items():

@@ -1,0 +1,32 @@
+"""Shared test setup: the ``gpu`` marker and the native library fixture."""
+
+import os
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
+
+
+@pytest.fixture(scope="session")
+def native_lib():
+    """Build (if stale) and load the native library."""
+    from braincell_gb300 import _abi
+    from braincell_gb300.build import build_native
+
+    build_native()
+    return _abi.lib()
+
+
+@pytest.fixture(scope="session")
+def cuda_device():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return 0

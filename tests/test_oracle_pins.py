@@ -1,0 +1,178 @@
+"""Pins the float64 oracle to the reference's own known answers (tests/golden)."""
+
+import json
+import math
+import os
+
+import numpy as np
+import pytest
+
+from oracle import staggered as O
+
+GOLD = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "reference_known_answers.json")))
+
+
+def _radii(case):
+    if "radii" in case:
+        r = np.asarray(case["radii"])
+        return r[:-1], r[1:]
+    _, rp, rd = O.insert_radius_jumps(case["lengths"], case["radii_proximal"], case["radii_distal"])
+    return rp, rd
+
+
+def _lengths(case):
+    if "radii" in case:
+        return case["lengths"]
+    return O.insert_radius_jumps(case["lengths"], case["radii_proximal"], case["radii_distal"])[0]
+
+
+@pytest.mark.parametrize("case", GOLD["frusta"], ids=lambda c: c["src"].split()[-1])
+def test_frusta(case):
+    rp, rd = _radii(case)
+    if "split_x" in case:
+        x = case["split_x"]
+        left = O.build_frusta(_lengths(case), rp, rd, 0.0, x)
+        right = O.build_frusta(_lengths(case), rp, rd, x, 1.0)
+        assert len(left) == case["n_left"] and len(right) == case["n_right"]
+        assert left[-1].length_um == pytest.approx(case["left_last_length_um"])
+        assert right[0].length_um == pytest.approx(case["right_first_length_um"])
+        whole = O.build_frusta(_lengths(case), rp, rd, 0.0, 1.0)
+        assert O.lateral_area_um2(left) + O.lateral_area_um2(right) == pytest.approx(O.lateral_area_um2(whole), abs=1e-4)
+        return
+    fr = O.build_frusta(_lengths(case), rp, rd, case["prox"], case["dist"])
+    assert len(fr) == case["n"]
+    assert [f.length_um for f in fr] == pytest.approx(case["length_um"])
+    if "r_prox_um" in case:
+        assert [f.r_prox_um for f in fr] == pytest.approx(case["r_prox_um"])
+        assert [f.r_dist_um for f in fr] == pytest.approx(case["r_dist_um"])
+    if "jump_index" in case:
+        j = fr[case["jump_index"]]
+        assert j.r_prox_um == pytest.approx(case["jump_r_prox_um"])
+        assert j.r_dist_um == pytest.approx(case["jump_r_dist_um"])
+
+
+def test_jump_branch_area_and_axial_factor():
+    # geometry_test.py:95-115: the zero-length jump adds the annulus area but no axial resistance
+    lengths, rp, rd = [10.0, 20.0], np.array([2.0, 4.0]), np.array([1.0, 2.0])
+    fr = O.build_frusta(*O.insert_radius_jumps(lengths, rp, rd), 0.0, 1.0)
+    expected = sum((L * 1e-4) / (math.pi * (a * 1e-4) * (b * 1e-4)) for L, a, b in zip(lengths, rp, rd))
+    assert O.axial_factor_per_cm(fr) == pytest.approx(expected, abs=1e-9)
+    area = sum(math.pi * (a + b) * math.sqrt(L * L + (b - a) ** 2) for L, a, b in zip(lengths, rp, rd))
+    area += math.pi * (4.0 ** 2 - 1.0 ** 2)  # annulus of the 1 -> 4 um jump
+    assert O.lateral_area_um2(fr) == pytest.approx(area, abs=1e-4)
+
+
+@pytest.mark.parametrize("case", GOLD["frusta_rejects"], ids=lambda c: f"{c['prox']}-{c['dist']}")
+def test_frusta_rejects(case):
+    rp, rd = _radii(case)
+    with pytest.raises(ValueError):
+        O.build_frusta(case["lengths"], rp, rd, case["prox"], case["dist"])
+
+
+@pytest.mark.parametrize("case", GOLD["frustum_scalars"], ids=lambda c: c["src"].split()[-1])
+def test_frustum_scalars(case):
+    fr = (O.Frustum(0.0, 1.0, case["length_um"], case["r0"], case["r1"]),)
+    if "area_um2" in case:
+        assert round(O.lateral_area_um2(fr) - case["area_um2"], case["area_places"]) == 0
+    if "axial_factor_per_cm" in case:
+        assert round(O.axial_factor_per_cm(fr) - case["axial_factor_per_cm"], case["axial_places"]) == 0
+    if "midpoint_radius_um" in case:
+        assert O.midpoint_radius_um(fr) == pytest.approx(case["midpoint_radius_um"])
+
+
+@pytest.mark.parametrize("case", GOLD["peel_levels"], ids=lambda c: c["src"])
+def test_peel_levels(case):
+    lv = O.compute_peel_levels(np.asarray(case["node_parent"]), case["node_children"])
+    assert lv.tolist() == case["levels"]
+
+
+def test_peel_levels_cycle():
+    c = GOLD["peel_levels_cycle"]
+    with pytest.raises(ValueError, match="cycle"):
+        O.compute_peel_levels(np.asarray(c["node_parent"]), c["node_children"])
+
+
+def test_backsub_indices():
+    a, b = GOLD["backsub_indices"]
+    idx = O.build_backsub_indices(np.asarray(a["parent_lookup"]), a["n_nodes"])
+    assert idx.shape[1] == a["ncols"] and int(idx[0, 0]) == a["idx00"]
+    idx = O.build_backsub_indices(np.asarray(b["parent_lookup"]), b["n_nodes"])
+    assert idx[0].tolist() == b["row0"] and int(idx[1, 0]) == b["idx10"]
+
+
+def test_rate_known_answers():
+    kdr, na = GOLD["rates"]
+    r = O.rates("KDR_Ba2002", np.asarray([kdr["V"]]), {"V_sh": kdr["V_sh"]})
+    assert float(r["p"][1][0]) == pytest.approx(kdr["alpha"], rel=1e-12)
+    (v1, s1), (v2, s2) = na["pair"]
+    a1 = O.rates("Na_Ba2002", np.asarray([v1]), {"V_sh": s1})["p"][1]
+    a2 = O.rates("Na_Ba2002", np.asarray([v2]), {"V_sh": s2})["p"][1]
+    assert abs(float(a1[0] - a2[0])) <= na["atol"]
+
+
+def test_q10_factor():
+    q = GOLD["q10"]
+    phi = q["q10"] ** ((q["temp"] - q["temp_ref"]) / 10.0)
+    assert phi == pytest.approx(q["phi"], abs=q["atol"])
+    from braincell_gb300.catalogue import q10_phi
+
+    assert q10_phi(q["q10"], q["temp"], q["temp_ref"]) == pytest.approx(q["phi"], abs=q["atol"])
+
+
+def test_exprel():
+    assert float(O.exprel(0.0)) == 1.0
+    x = np.asarray([1e-8, -1e-3, 0.5, -3.0])
+    assert np.allclose(O.exprel(x), np.expm1(x) / x, rtol=1e-14)
+
+
+def _soma_cell(case, pop=1):
+    from braincell_gb300 import Branch, Cell, Morphology
+    from braincell_gb300.mech import CurrentClamp, CVPerBranch, RootLocation
+
+    soma = Branch.from_lengths(lengths=[case["soma_length"]], radii=[case["soma_radius"]] * 2, type="soma")
+    cell = Cell(Morphology.from_root(soma, name="soma"), pop_size=pop, cv_policy=CVPerBranch(),
+                V_init=case.get("V_init"))
+    cell.place(RootLocation(case["clamp_x"]),
+               CurrentClamp(delay=case["delay"], durations=case["durations"], amplitudes=case["amplitudes"]))
+    return cell
+
+
+@pytest.mark.parametrize("case", GOLD["step_behaviour"][:2], ids=["endpoint", "multistep"])
+def test_oracle_clamp_raises_voltage(case):
+    oc = O.OracleCell(_soma_cell(case))
+    before = oc.V[0, 0]
+    oc.step(case["dt"], 0.0)
+    assert oc.V[0, 0] > before
+
+
+def test_oracle_population_widening_is_neutral():
+    case = GOLD["step_behaviour"][2]
+    single = O.OracleCell(_soma_cell(case))
+    pop = O.OracleCell(_soma_cell(case, pop=case["pop"]))
+    single.step(case["dt"], 0.0)
+    pop.step(case["dt"], 0.0)
+    for m in range(case["pop"]):
+        np.testing.assert_allclose(pop.V[m], single.V[0], rtol=case["rtol"], atol=case["atol"])
+
+
+def test_oracle_small_config_structure():
+    """The small workload lowers to 129 points, 29 DHS levels, 8 back-substitution passes."""
+    from braincell_gb300 import workloads as W
+
+    oc = O.OracleCell(W.desc_to_cell(W.small(1)[0]))
+    assert oc.n_cv == 113 and oc.n_point == 129
+    assert len(oc.level_offsets) - 1 == 29
+    assert oc.backsub.shape[0] == 8
+
+
+def test_oracle_rest_is_steady_without_input():
+    """With no stimulus the passive cell stays near rest and nothing diverges."""
+    from braincell_gb300 import workloads as W
+
+    d = W.small(1)[0]
+    d.pulses = []
+    oc = O.OracleCell(W.desc_to_cell(d))
+    for _ in range(200):
+        oc.step(0.025)
+    assert np.all(np.isfinite(oc.V))
+    assert np.all(np.abs(oc.V + 67.5) < 3.0)

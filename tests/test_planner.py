@@ -1,0 +1,87 @@
+"""Schedule planning without a GPU (dry-run plans): tiles, phases, chain splitting,
+input validation."""
+
+import numpy as np
+import pytest
+
+from braincell_gb300 import _abi
+from braincell_gb300 import workloads as W
+from braincell_gb300.batch import CellBatch
+from braincell_gb300.runtime import Plan
+
+
+def test_small_workload_plan(native_lib):
+    b = W.descs_to_batch(W.small(16))
+    p = Plan(b, dry_run=True)
+    assert p.info["n_cells"] == 16 and p.info["n_cv"] == 16 * 113 and p.info["n_nodes"] == 16 * 129
+    st = p.tile_stats()
+    assert st[:, 0].sum() == 16 * 129
+    assert np.all(st[:, 2] >= 1) and np.all(st[:, 3] > 0)
+    assert np.all(st[:, 5] < 227 * 1024)
+
+
+def test_uneven_sample_plan(native_lib):
+    b = W.descs_to_batch(W.uneven(300))
+    p = Plan(b, dry_run=True)
+    st = p.tile_stats()
+    n_nodes = (b.cell_ncv() + b.cell_nbranch() + 1).sum()
+    assert st[:, 0].sum() == n_nodes == p.info["n_nodes"]
+    assert set(np.unique(st[:, 4])) <= {0, 1, 2}
+    # packed tiles respect the node budget
+    packed = st[st[:, 4] == 0]
+    assert np.all(packed[:, 0] <= p.info["tile_nodes"])
+
+
+def test_long_chain_is_split(native_lib):
+    d = W.small(1)[0]
+    d.ncv = [1] + [200] + [8] * (len(d.parent) - 2)
+    b = W.descs_to_batch([d])
+    whole = Plan(b, dry_run=True, split_min=0).tile_stats()
+    split = Plan(b, dry_run=True, split_min=24).tile_stats()
+    assert split[0, 1] > whole[0, 1]          # more chain records
+    assert split[0, 3] < whole[0, 3] / 2       # much shorter critical path
+
+
+def test_thread_per_cell_for_tiny_cells(native_lib):
+    b = W.descs_to_batch(W.small(8))
+    p = Plan(b, dry_run=True, thread_cell_max=200)
+    st = p.tile_stats()
+    assert np.all(st[:, 2] == 1)  # whole cells walked by one thread: a single phase
+
+
+def _bad(b: CellBatch, **kw):
+    for k, v in kw.items():
+        setattr(b, k, v)
+    return b
+
+
+@pytest.mark.parametrize("mutate,msg", [
+    (lambda b: _bad(b, branch_region=np.full_like(b.branch_region, 7)), "region"),
+    (lambda b: _bad(b, region_mech=np.full_like(b.region_mech, 1 << 20)), "mechanism"),
+    (lambda b: _bad(b, pulse_t_off=b.pulse_t_on - 1.0), "pulse_t_off"),
+    (lambda b: _bad(b, probe_branch=np.full_like(b.probe_branch, 99)), "probe"),
+])
+def test_invalid_batches_rejected(native_lib, mutate, msg):
+    b = mutate(W.descs_to_batch(W.small(2)))
+    with pytest.raises(_abi.BCError, match=msg) as e:
+        Plan(b, dry_run=True)
+    assert e.value.status == _abi.BC_ERR_INVALID
+
+
+def test_parent_order_and_radii_validation(native_lib):
+    b = W.descs_to_batch(W.small(1))
+    b.branch_parent = b.branch_parent.copy()
+    b.branch_parent[1] = 5  # a parent that comes after its child
+    with pytest.raises(_abi.BCError, match="precede"):
+        Plan(b, dry_run=True)
+    b = W.descs_to_batch(W.small(1))
+    b.seg_r_prox = b.seg_r_prox.copy()
+    b.seg_r_prox[3] = 0.0
+    with pytest.raises(_abi.BCError, match="radii"):
+        Plan(b, dry_run=True)
+
+
+def test_dry_plan_has_no_device_state(native_lib):
+    p = Plan(W.descs_to_batch(W.small(1)), dry_run=True)
+    with pytest.raises(_abi.BCError, match="dry_run"):
+        p.run(1, 0.025)
