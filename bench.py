@@ -33,7 +33,7 @@ import numpy as np  # noqa: E402
 
 METRIC = "compartment-steps/s on 1 GB300, plain vs surrogate at <=0.1 ms spike-time error"
 UNIT = "compartment-steps/s"
-BYTES_PER_COMPARTMENT_STEP = 56  # algorithmic bytes per compartment-step of this workload
+BYTES_PER_COMPARTMENT_STEP = 56  # state read+written per compartment-step by a per-step kernel (V, gates, Ca, coefficients)
 DT = 0.025
 SIM_STEPS = 8000
 
@@ -70,11 +70,15 @@ def _peaks():
         return 6800.0, "fallback"
 
 
-def _traffic_per_compartment_step():
-    """DRAM bytes per compartment-step from the committed ncu summary, if present."""
+def _traffic_per_node_launch():
+    """Measured DRAM bytes per tile node per launch (ncu summary under profiles/), if present.
+
+    A launch stages each tile's blob into shared memory once and writes V back once,
+    whatever number of steps it fuses, so its traffic scales with the nodes it holds.
+    """
     try:
         with open(os.path.join(ROOT, "profiles", "tile_step_uneven.json")) as f:
-            return float(json.load(f)["dram_bytes_per_compartment_step"])
+            return float(json.load(f)["dram_bytes_per_node_per_launch"])
     except Exception:
         return None
 
@@ -276,7 +280,7 @@ def run_ours(a):
 
     peak, peak_kind = _peaks()
     achieved_gbs = BYTES_PER_COMPARTMENT_STEP * n_cv * a.sim_steps / (kernel_ms * 1e-3) / 1e9
-    traffic_per_cs = _traffic_per_compartment_step()
+    traffic_per_node = _traffic_per_node_launch()
     units_per_launch = n_cv * info["steps_per_launch"]
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
@@ -293,7 +297,7 @@ def run_ours(a):
                 "path": "bc_state_upload (V) -> bc_run (8,000 steps) -> bc_state_download (V) + bc_spike_download"},
         "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": peak, "unit": "GB/s",
                      "frac": achieved_gbs / peak, "peak_kind": peak_kind,
-                     "traffic": (traffic_per_cs * units_per_launch) if traffic_per_cs else None,
+                     "traffic": (traffic_per_node * info["n_nodes"]) if traffic_per_node else None,
                      "algorithmic_bytes_per_launch": BYTES_PER_COMPARTMENT_STEP * units_per_launch,
                      "kernel_ms_per_sim": kernel_ms, "launches_per_sim": launches_per_sim},
         "gpu_launches": a.steps * (1 + launches_per_sim),

@@ -837,7 +837,7 @@ class OracleCell:
         self.t_step += 1
         return self.spike
 
-    # ------------------------------------------------------------ driver
+    # ------------------------------------------------------------ time loop
     def run(self, dt: float, n_steps: int, record_every: int = 1):
         """Run ``n_steps``; return (probe traces [P, n_probe, n_rec], spike times per (P, probe))."""
         traces = []
