@@ -86,6 +86,7 @@ BC_STATE_HCN_P = 8
 BC_STATE_AHP_P = 9
 BC_STATE_CA_CI = 10
 BC_NSTATE_VIEW = 11
+BC_NOALLOC_MAX_CV = 262144
 
 STATE_NAMES = {
     "V": BC_STATE_V,
@@ -203,6 +204,7 @@ SIGNATURES = {
     "bc_check": (C.c_int32, [C.c_void_p, C.c_void_p]),
     "bc_state_download": (C.c_int32, [C.c_void_p, C.c_int32, _p(C.c_double), C.c_void_p]),
     "bc_state_upload": (C.c_int32, [C.c_void_p, C.c_int32, _p(C.c_double), C.c_void_p]),
+    "bc_state_download_noalloc": (C.c_int32, [C.c_void_p, C.c_int32, _p(C.c_double), C.c_void_p]),
     "bc_probe_count": (C.c_int32, [C.c_void_p, _p(C.c_int64)]),
     "bc_probe_download": (C.c_int32, [C.c_void_p, _p(C.c_double), C.c_int64, C.c_void_p]),
     "bc_spike_download": (C.c_int32, [C.c_void_p, _p(C.c_int32), _p(C.c_double), C.c_void_p]),

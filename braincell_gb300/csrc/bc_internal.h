@@ -144,6 +144,9 @@ int launch_reset_impl(const LaunchArgs& a, int precision, int threads, const dou
 constexpr int64_t kStateTag = int64_t(1) << 62;
 int launch_view_impl(unsigned char* blob, unsigned char* state, int precision, const int64_t* off_hi,
                      const int64_t* off_lo, double* view, int64_t n, bool write, void* stream);
-
+// Device address (on the current device) of the fixed scratch behind
+// bc_state_download_noalloc: [hi offsets | lo offsets | values], BC_NOALLOC_MAX_CV
+// 8-byte entries each.  Returns the cudaError_t of cudaGetSymbolAddress.
+int noalloc_view_scratch_address(void** out);
 
 }  // namespace bc

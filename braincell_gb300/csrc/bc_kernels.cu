@@ -868,4 +868,12 @@ int launch_view_impl(unsigned char* blob, unsigned char* state, int precision, c
   return int(cudaGetLastError());
 }
 
+// Scratch of bc_state_download_noalloc, part of the module image (no allocation
+// call): three 8-byte arrays of BC_NOALLOC_MAX_CV entries, 256-byte aligned.
+static __device__ __align__(256) unsigned char g_noalloc_view_scratch[3 * 8 * size_t(BC_NOALLOC_MAX_CV)];
+
+int noalloc_view_scratch_address(void** out) {
+  return int(cudaGetSymbolAddress(out, g_noalloc_view_scratch));
+}
+
 }  // namespace bc

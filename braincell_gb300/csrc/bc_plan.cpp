@@ -15,6 +15,7 @@
 #include <array>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <numeric>
 #include <queue>
 #include <string>
@@ -1271,6 +1272,85 @@ bc_status bc_state_download(bc_plan_t p, int32_t which, double* out, void* strea
 
 bc_status bc_state_upload(bc_plan_t p, int32_t which, const double* in, void* stream) {
   return view_io(p, which, const_cast<double*>(in), true, stream);
+}
+
+// ------------------------------------------------------------------ no-allocation download
+// Host staging of the offset tables, [hi | lo] with BC_NOALLOC_MAX_CV entries each
+// (zero-initialised static storage; nothing is allocated at run time).
+static int64_t g_noalloc_host_off[2 * size_t(BC_NOALLOC_MAX_CV)];
+constexpr int kNoAllocDevices = 64;
+static unsigned char* g_noalloc_scratch[kNoAllocDevices];
+static std::mutex g_noalloc_setup_mu;
+
+// One-time (per device) lookup of the scratch address; the caller has set the device.
+static bc_status noalloc_scratch(int device, unsigned char** out) {
+  if (device < 0 || device >= kNoAllocDevices) return fail(BC_ERR_INVALID, "device ordinal out of range");
+  std::lock_guard<std::mutex> lock(g_noalloc_setup_mu);
+  if (!g_noalloc_scratch[device]) {
+    void* addr = nullptr;
+    const int e = noalloc_view_scratch_address(&addr);
+    if (e != 0 || !addr)
+      return fail(BC_ERR_CUDA, std::string("cudaGetSymbolAddress(no-allocation scratch): ") +
+                                   cudaGetErrorString(cudaError_t(e)));
+    g_noalloc_scratch[device] = static_cast<unsigned char*>(addr);
+  }
+  *out = g_noalloc_scratch[device];
+  return BC_OK;
+}
+
+// Offsets of CV k in view `which`: the per-CV form of view_offsets.
+static void noalloc_offset(const bc_plan* p, int32_t which, int64_t k, int64_t* hi, int64_t* lo) {
+  const TileDesc& d = p->tiles[p->cv_tile[k]];
+  const int64_t j = p->cv_node[k];
+  const int64_t rs = int64_t(p->real_size);
+  *hi = -1;
+  *lo = -1;
+  if (which == BC_STATE_V) {
+    *hi = d.blob_offset + d.off_vhi + j * rs;
+    *lo = d.blob_offset + d.off_vlo + j * rs;
+    return;
+  }
+  static const uint32_t kBit[BC_NSTATE_VIEW] = {0,         BC_M_NA,  BC_M_NA,  BC_M_KDR, BC_M_CAL, BC_M_CAL,
+                                                BC_M_CAT,  BC_M_CAT, BC_M_HCN, BC_M_AHP, BC_M_CADET};
+  static const int kSlot[BC_NSTATE_VIEW] = {-1,         kSlotNaP,  kSlotNaQ,  kSlotKdrP, kSlotCalP, kSlotCalQ,
+                                            kSlotCatP,  kSlotCatQ, kSlotHcnP, kSlotAhpP, kSlotCaHi};
+  if (!(p->cv_mech[k] & kBit[which])) return;
+  *hi = kStateTag + (d.state_offset + int64_t(kSlot[which]) * d.n_nodes + j) * rs;
+  if (which == BC_STATE_CA_CI) *lo = kStateTag + (d.state_offset + int64_t(kSlotCaLo) * d.n_nodes + j) * rs;
+}
+
+bc_status bc_state_download_noalloc(bc_plan_t p, int32_t which, double* out, void* stream) {
+  if (!p || !out) return fail(BC_ERR_INVALID, "null argument");
+  if (which < 0 || which >= BC_NSTATE_VIEW) return fail(BC_ERR_INVALID, "unknown state view");
+  if (p->n_cv > BC_NOALLOC_MAX_CV)
+    return fail(BC_ERR_INVALID, "bc_state_download_noalloc: plan has " + std::to_string(p->n_cv) +
+                                    " CVs, above the fixed scratch capacity of " +
+                                    std::to_string(BC_NOALLOC_MAX_CV) +
+                                    " (BC_NOALLOC_MAX_CV); use bc_state_download");
+  BC_NEED_DEVICE(p);
+  BC_CUDA(cudaSetDevice(p->device));
+  unsigned char* scratch = nullptr;
+  bc_status st = noalloc_scratch(p->device, &scratch);
+  if (st != BC_OK) return st;
+  const int64_t n = p->n_cv;
+  if (n == 0) return BC_OK;
+  int64_t* h_hi = g_noalloc_host_off;
+  int64_t* h_lo = g_noalloc_host_off + BC_NOALLOC_MAX_CV;
+  for (int64_t k = 0; k < n; ++k) noalloc_offset(p, which, k, &h_hi[k], &h_lo[k]);
+  // Entries [0, n) of all three arrays are written before they are read (offsets by
+  // the copies, values by the view kernel, which fills absent states with NaN), so
+  // nothing has to start at zero.
+  int64_t* d_hi = reinterpret_cast<int64_t*>(scratch);
+  int64_t* d_lo = d_hi + BC_NOALLOC_MAX_CV;
+  double* d_val = reinterpret_cast<double*>(d_lo + BC_NOALLOC_MAX_CV);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  BC_CUDA(cudaMemcpyAsync(d_hi, h_hi, size_t(n) * 8, cudaMemcpyHostToDevice, s));
+  BC_CUDA(cudaMemcpyAsync(d_lo, h_lo, size_t(n) * 8, cudaMemcpyHostToDevice, s));
+  const int ke = launch_view_impl(p->d_blob, p->d_state, p->precision, d_hi, d_lo, d_val, n, false, stream);
+  if (ke) return fail(BC_ERR_CUDA, std::string("view kernel: ") + cudaGetErrorString(cudaError_t(ke)));
+  BC_CUDA(cudaMemcpyAsync(out, d_val, size_t(n) * 8, cudaMemcpyDeviceToHost, s));
+  BC_CUDA(cudaStreamSynchronize(s));
+  return BC_OK;
 }
 
 bc_status bc_probe_count(bc_plan_t p, int64_t* n) {

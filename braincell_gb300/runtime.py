@@ -150,6 +150,22 @@ class Plan:
         )
         return out
 
+    def state_into(self, name: str, out: np.ndarray, stream=None) -> np.ndarray:
+        """Like :meth:`state`, into a caller-held float64 array, with no device allocation.
+
+        Goes through ``bc_state_download_noalloc``: fixed library scratch instead of
+        per-call buffers, for plans of at most ``BC_NOALLOC_MAX_CV`` CVs.  Calls from
+        several threads at once race on that scratch and must be serialised.
+        """
+        if out.dtype != np.float64 or out.shape != (self.n_cv,) or not out.flags.c_contiguous:
+            raise ValueError(f"out must be a contiguous float64 array of shape ({self.n_cv},)")
+        which = _abi.STATE_NAMES[name]
+        _abi.check(
+            self._lib.bc_state_download_noalloc(
+                self._h, which, out.ctypes.data_as(C.POINTER(C.c_double)), self._stream(stream))
+        )
+        return out
+
     def set_state(self, name: str, values, stream=None) -> None:
         which = _abi.STATE_NAMES[name]
         arr = np.ascontiguousarray(np.broadcast_to(np.asarray(values, dtype=np.float64), (self.n_cv,)))

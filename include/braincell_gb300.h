@@ -245,6 +245,25 @@ bc_status bc_check(bc_plan_t plan, void* stream);
 bc_status bc_state_download(bc_plan_t plan, int32_t which, double* out /* [n_cv] */, void* stream);
 bc_status bc_state_upload(bc_plan_t plan, int32_t which, const double* in /* [n_cv] */, void* stream);
 
+/* bc_state_download without any allocation.  No counterpart in the reference: its
+ * states are ordinary arrays the caller already holds.
+ * Who needs it: a caller that reads state while simulations run on other streams
+ * (a monitor, a closed-loop controller) and cannot afford cudaMalloc/cudaFree,
+ * which synchronise the whole device and so stall every queued launch; and a
+ * process whose device memory is already held by a caching allocator, where a
+ * fresh cudaMalloc may fail.  bc_state_download allocates its offset tables and
+ * value buffer per call; this variant uses one fixed scratch array in the
+ * library's device image plus a host staging array of the same capacity, both
+ * sized for BC_NOALLOC_MAX_CV compartments (24 bytes each on the device: 6 MiB).
+ * Plans with more CVs are rejected with BC_ERR_INVALID (use bc_state_download).
+ * The first call on each device looks up the scratch address (cudaGetSymbolAddress)
+ * and caches it; make that first call before any stream capture begins.  The
+ * scratch is shared by every plan of the process: calls that overlap in time (from
+ * several host threads) race on it, so the caller must serialise them.  Returns
+ * once `out` holds the values (the stream is synchronised). */
+#define BC_NOALLOC_MAX_CV 262144
+bc_status bc_state_download_noalloc(bc_plan_t plan, int32_t which, double* out /* [n_cv] */, void* stream);
+
 /* Probe outputs.  Traces: [n_probes, n_records] float64 where n_records is the
  * number of samples taken since the last bc_probe_clear.  Spikes: count per probe
  * and up to max_spikes upward 0 mV crossing times (ms, linear interpolation). */

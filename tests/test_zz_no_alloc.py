@@ -1,0 +1,66 @@
+"""bc_state_download_noalloc: the state download that allocates nothing.
+
+Collected last (file name), so on a GPU it runs both after every other test and,
+when run alone, in a fresh process where its first call does the scratch set-up.
+Its values must equal bc_state_download's (same view kernel, same offsets) on two
+calls in a row, for every state view, in both precisions.
+"""
+
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from braincell_gb300 import _abi
+from braincell_gb300 import workloads as W
+from braincell_gb300.runtime import Plan
+
+
+def _download_noalloc(lib, plan, which):
+    out = np.full(plan.n_cv, -7.0)
+    st = lib.bc_state_download_noalloc(plan._h, which, out.ctypes.data_as(C.POINTER(C.c_double)), None)
+    return st, out
+
+
+def test_plan_above_capacity_is_rejected(native_lib):
+    descs = W.uneven(480)
+    plan = Plan(W.descs_to_batch(descs), dry_run=True)
+    assert plan.n_cv > _abi.BC_NOALLOC_MAX_CV
+    st, out = _download_noalloc(native_lib, plan, _abi.BC_STATE_V)
+    assert st == _abi.BC_ERR_INVALID
+    msg = native_lib.bc_last_error()
+    assert b"BC_NOALLOC_MAX_CV" in msg and str(plan.n_cv).encode() in msg
+    assert (out == -7.0).all()
+
+
+def test_invalid_arguments_are_rejected(native_lib):
+    plan = Plan(W.descs_to_batch(W.small(2)), dry_run=True)
+    assert _download_noalloc(native_lib, plan, _abi.BC_NSTATE_VIEW)[0] == _abi.BC_ERR_INVALID
+    assert _download_noalloc(native_lib, plan, -1)[0] == _abi.BC_ERR_INVALID
+    st, _ = _download_noalloc(native_lib, plan, _abi.BC_STATE_V)
+    assert st == _abi.BC_ERR_INVALID and b"dry_run" in native_lib.bc_last_error()
+    assert native_lib.bc_state_download_noalloc(None, 0, None, None) == _abi.BC_ERR_INVALID
+
+
+def _calcium_desc():
+    return W.large(indices=[0], n_range=(300, 400), n_branches=20, n_pulses=60, duration=20.0)[0]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["f32", "f64"])
+def test_noalloc_download_matches_download(native_lib, cuda_device, precision):
+    descs = W.small(4) + [_calcium_desc()] + W.uneven(indices=[0, 1])
+    plan = Plan(W.descs_to_batch(descs), precision=precision, device=cuda_device)
+    assert plan.n_cv <= _abi.BC_NOALLOC_MAX_CV
+    for segment in range(2):
+        plan.run(300, 0.025)
+        for name, which in _abi.STATE_NAMES.items():
+            ref = plan.state(name)
+            first = plan.state_into(name, np.empty(plan.n_cv))
+            st, second = _download_noalloc(native_lib, plan, which)
+            assert st == _abi.BC_OK, native_lib.bc_last_error()
+            # bit-identical to the allocating download, NaN where the mechanism is absent
+            np.testing.assert_array_equal(first, ref, err_msg=f"{name}, segment {segment}, first call")
+            np.testing.assert_array_equal(second, ref, err_msg=f"{name}, segment {segment}, second call")
+            assert np.isfinite(ref).any(), name
+    plan.close()
