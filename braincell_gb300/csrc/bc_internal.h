@@ -83,12 +83,15 @@ struct TileDesc {
   int32_t pad0;
   int64_t probe_offset;     // into plan probe array
   // byte offsets inside the blob
-  int32_t off_vhi, off_vlo;
+  int32_t off_v;            // (V_hi, V_lo) pairs
+  int32_t pad2;
   int64_t state_offset;     // elements into the plan's global mechanism-state array ([slot][n_nodes])
-  int32_t off_alpha, off_beta, off_diag0, off_pidx, off_spec, off_specs;
+  int32_t off_ab;           // (alpha, beta) pairs
+  int32_t off_diag0, off_pidx, off_spec, off_specs;
   int32_t off_chains, off_child, off_lists, off_params, off_mech;
   int32_t scratch_bytes;    // diag/rhs/cD/cR scratch (shared memory after the blob)
-  int32_t off_sdiag, off_srhs, off_scd, off_scr, off_sfill, off_sh;  // offsets inside the scratch area
+  int32_t off_dr;           // (diagonal, rhs) pairs, inside the scratch area
+  int32_t off_scd, off_scr, off_sfill, off_sh;  // offsets inside the scratch area
   int32_t n_slots;          // contribution slots (scd / scr / sh entries)
   int32_t pad1;
   int64_t scratch_offset;   // bytes into the plan's global scratch (global-resident tiles)

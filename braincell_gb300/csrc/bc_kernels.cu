@@ -90,24 +90,48 @@ __device__ __forceinline__ void fence_proxy_async_smem() {
 constexpr uint32_t kBulkChunk = 32768;  // bytes per bulk copy instruction (multiple of 16)
 
 // ------------------------------------------------------------------ tile view
+// Per-node pairs, loaded and stored as one vector access.
+template <typename Real>
+struct PairOf;
+template <>
+struct PairOf<float> {
+  using type = float2;
+};
+template <>
+struct PairOf<double> {
+  using type = double2;
+};
+template <typename Real>
+using Pair = typename PairOf<Real>::type;
+
+template <typename Real>
+__device__ __forceinline__ Pair<Real> make_pair(Real a, Real b) {
+  Pair<Real> p;
+  p.x = a;
+  p.y = b;
+  return p;
+}
+
 template <typename Real>
 struct TileView {
-  Real *vhi, *vlo, *state;
-  const Real *alpha, *beta, *diag0, *params;
+  Pair<Real>* v;   // (V_hi, V_lo)
+  Pair<Real>* ab;  // (alpha, beta); (alpha dt, beta dt) once pre-scaled
+  Pair<Real>* dr;  // (diagonal, rhs) of the row; (1 / pivot, rhs or x) during the sweeps
+  Real* state;
+  const Real *diag0, *params;
   const int32_t *child, *lists;
   const uint16_t *pidx, *spec;
   const ChainRec* chains;
   const SpecRec* specs;
   const uint32_t* mech;
-  Real *sdiag, *srhs, *scd, *scr, *sfill, *sh;
+  Real *scd, *scr, *sfill, *sh;
   int N, n_real, n_phases;
 
   __device__ __forceinline__ void bind(const TileDesc& td, unsigned char* base, unsigned char* scratch, void* gstate) {
-    vhi = reinterpret_cast<Real*>(base + td.off_vhi);
-    vlo = reinterpret_cast<Real*>(base + td.off_vlo);
+    v = reinterpret_cast<Pair<Real>*>(base + td.off_v);
+    ab = reinterpret_cast<Pair<Real>*>(base + td.off_ab);
+    dr = reinterpret_cast<Pair<Real>*>(scratch + td.off_dr);
     state = reinterpret_cast<Real*>(gstate) + td.state_offset;
-    alpha = reinterpret_cast<const Real*>(base + td.off_alpha);
-    beta = reinterpret_cast<const Real*>(base + td.off_beta);
     diag0 = reinterpret_cast<const Real*>(base + td.off_diag0);
     params = reinterpret_cast<const Real*>(base + td.off_params);
     child = reinterpret_cast<const int32_t*>(base + td.off_child);
@@ -117,8 +141,6 @@ struct TileView {
     chains = reinterpret_cast<const ChainRec*>(base + td.off_chains);
     specs = reinterpret_cast<const SpecRec*>(base + td.off_specs);
     mech = reinterpret_cast<const uint32_t*>(base + td.off_mech);
-    sdiag = reinterpret_cast<Real*>(scratch + td.off_sdiag);
-    srhs = reinterpret_cast<Real*>(scratch + td.off_srhs);
     scd = reinterpret_cast<Real*>(scratch + td.off_scd);
     scr = reinterpret_cast<Real*>(scratch + td.off_scr);
     sfill = reinterpret_cast<Real*>(scratch + td.off_sfill);
@@ -147,34 +169,47 @@ __device__ __forceinline__ void ff_add(Real& hi, Real& lo, Real d) {
 }
 
 // ------------------------------------------------------------------ mechanisms
+// The mechanism states of one node, held in registers (absent ones are 0).
+template <typename Real>
+struct NodeStates {
+  Real nap, naq, kdrp, calp, calq, catp, catq, hcnp, ahpp, cahi, calo;
+};
+
+template <typename Real>
+__device__ __forceinline__ void load_states(const Real* st, int N, uint32_t m, NodeStates<Real>& s) {
+  s.nap = s.naq = s.kdrp = s.calp = s.calq = s.catp = s.catq = s.hcnp = s.ahpp = s.cahi = s.calo = Real(0);
+  if (m & BC_M_NA) {
+    s.nap = st[kSlotNaP * N];
+    s.naq = st[kSlotNaQ * N];
+  }
+  if (m & BC_M_KDR) s.kdrp = st[kSlotKdrP * N];
+  if (m & BC_M_CAL) {
+    s.calp = st[kSlotCalP * N];
+    s.calq = st[kSlotCalQ * N];
+  }
+  if (m & BC_M_CAT) {
+    s.catp = st[kSlotCatP * N];
+    s.catq = st[kSlotCatQ * N];
+  }
+  if (m & BC_M_HCN) s.hcnp = st[kSlotHcnP * N];
+  if (m & BC_M_AHP) s.ahpp = st[kSlotAhpP * N];
+  if (m & BC_M_CADET) {
+    s.cahi = st[kSlotCaHi * N];
+    s.calo = st[kSlotCaLo * N];
+  }
+}
+
 // One node's mechanisms.  `st` points at the node's slot-0 state (stride N).
 // With advance = true the states move from (v_old) to (v_new) first: calcium
 // from the step-start current (old gates, old V, old Ci), then every gate at
 // v_new (and the new Ci).  Returns the membrane conductance G (mS/cm^2) and
 // ionic current I (uA/cm^2) at v_new with the resulting states.
 template <typename Real>
-__device__ __forceinline__ void node_mechanisms(Real* st, int N, const Real* P, uint32_t m, Real v_old, Real v_new,
-                                                Real dt, bool advance, Real& G, Real& I) {
-  Real nap = 0, naq = 0, kdrp = 0, calp = 0, calq = 0, catp = 0, catq = 0, hcnp = 0, ahpp = 0, cahi = 0, calo = 0;
-  if (m & BC_M_NA) {
-    nap = st[kSlotNaP * N];
-    naq = st[kSlotNaQ * N];
-  }
-  if (m & BC_M_KDR) kdrp = st[kSlotKdrP * N];
-  if (m & BC_M_CAL) {
-    calp = st[kSlotCalP * N];
-    calq = st[kSlotCalQ * N];
-  }
-  if (m & BC_M_CAT) {
-    catp = st[kSlotCatP * N];
-    catq = st[kSlotCatQ * N];
-  }
-  if (m & BC_M_HCN) hcnp = st[kSlotHcnP * N];
-  if (m & BC_M_AHP) ahpp = st[kSlotAhpP * N];
-  if (m & BC_M_CADET) {
-    cahi = st[kSlotCaHi * N];
-    calo = st[kSlotCaLo * N];
-  }
+__device__ __forceinline__ void node_mechanisms_loaded(const NodeStates<Real>& s0, Real* st, int N, const Real* P,
+                                                       uint32_t m, Real v_old, Real v_new, Real dt, bool advance,
+                                                       Real& G, Real& I) {
+  Real nap = s0.nap, naq = s0.naq, kdrp = s0.kdrp, calp = s0.calp, calq = s0.calq, catp = s0.catp, catq = s0.catq,
+       hcnp = s0.hcnp, ahpp = s0.ahpp, cahi = s0.cahi, calo = s0.calo;
   if (advance) {
     if (m & BC_M_CADET) {
       const Real ci = cahi + calo;
@@ -281,6 +316,14 @@ __device__ __forceinline__ void node_mechanisms(Real* st, int N, const Real* P, 
   }
 }
 
+template <typename Real>
+__device__ __forceinline__ void node_mechanisms(Real* st, int N, const Real* P, uint32_t m, Real v_old, Real v_new,
+                                                Real dt, bool advance, Real& G, Real& I) {
+  NodeStates<Real> s;
+  load_states(st, N, m, s);
+  node_mechanisms_loaded(s, st, N, P, m, v_old, v_new, dt, advance, G, I);
+}
+
 // Steady state of every gate at v (HH.reset_state), Ci = Ci0.
 template <typename Real>
 __device__ __forceinline__ void steady_states(const Real* P, uint32_t m, Real* st, int N, Real v) {
@@ -324,12 +367,10 @@ __device__ __forceinline__ void steady_states(const Real* P, uint32_t m, Real* s
 template <typename Real>
 __device__ __forceinline__ void write_row(const TileView<Real>& tv, int i, uint16_t pr, Real dt, Real G, Real I) {
   if (pr == kBoundary) {
-    tv.sdiag[i] = dt * tv.diag0[i];
-    tv.srhs[i] = Real(0);
+    tv.dr[i] = make_pair(dt * tv.diag0[i], Real(0));
   } else {
     const Real invcm = tv.params[size_t(pr) * BC_NPARAM + BC_P_INVCM];
-    tv.sdiag[i] = Real(1) + dt * (tv.diag0[i] + invcm * G);
-    tv.srhs[i] = dt * invcm * I;
+    tv.dr[i] = make_pair(Real(1) + dt * (tv.diag0[i] + invcm * G), dt * invcm * I);
   }
 }
 
@@ -341,9 +382,9 @@ __device__ __forceinline__ void add_node_pulses(const TileView<Real>& tv, const 
     const PulseRec p = pulses[k];
     if (step < p.on_step || step >= p.off_step) continue;
     if (pr == kBoundary)
-      tv.srhs[i] += dt * Real(p.amp);
+      tv.dr[i].y += dt * Real(p.amp);
     else
-      tv.srhs[i] += dt * tv.params[size_t(pr) * BC_NPARAM + BC_P_INVCM] * Real(p.amp);
+      tv.dr[i].y += dt * tv.params[size_t(pr) * BC_NPARAM + BC_P_INVCM] * Real(p.amp);
   }
 }
 
@@ -352,9 +393,9 @@ __device__ __forceinline__ void add_node_pulses(const TileView<Real>& tv, const 
 //   d_i x_i - alpha_i x_parent - sum_c beta_c x_c = rhs_i - alpha_i Delta_i + sum_c beta_c Delta_c
 // with Delta_i = V_i - V_parent (float-float).  Chains are walked bottom -> top;
 // eliminating node i hands (cD, cR) = (alpha_i w, w r_i + beta_i Delta_i),
-// w = beta_i / d_i, to its parent.  The walks prefetch node i+1 (which is node
-// i's parent) while node i is computed, so shared-memory latency stays off the
-// pivot recurrence.
+// w = beta_i / d_i, to its parent.  Per node a walk touches three pairs -- (d, r),
+// (alpha dt, beta dt) and (V_hi, V_lo) -- loaded two nodes ahead, so that the
+// shared-memory latency stays off the pivot recurrence.
 
 __device__ __forceinline__ ChainRec load_rec(const ChainRec* recs, int c) {
   const int4* p = reinterpret_cast<const int4*>(recs + c);
@@ -371,48 +412,61 @@ __device__ __forceinline__ ChainRec load_rec(const ChainRec* recs, int c) {
   return r;
 }
 
-template <typename Real>
+// (alpha dt, beta dt) of node i: pre-scaled in shared-memory tiles, scaled here otherwise.
+template <typename Real, bool kPre>
+__device__ __forceinline__ Pair<Real> coef(const TileView<Real>& tv, int i, Real dt) {
+  Pair<Real> c = tv.ab[i];
+  if (!kPre) {
+    c.x *= dt;
+    c.y *= dt;
+  }
+  return c;
+}
+
+template <typename Real, bool kPre>
 __device__ __forceinline__ void eliminate_regular(const TileView<Real>& tv, const ChainRec& ch, Real dt) {
   const int s0 = ch.start, end = ch.start + ch.count;
-  Real D = tv.sdiag[s0], R = tv.srhs[s0];
-  Real al = tv.alpha[s0] * dt, be = tv.beta[s0] * dt, vh = tv.vhi[s0], vl = tv.vlo[s0];
+  Pair<Real> q = tv.dr[s0];
+  Real D = q.x, R = q.y;
   for (int k = 0; k < ch.n_child; ++k) {
     D -= tv.scd[ch.aux + k];
     R += tv.scr[ch.aux + k];
   }
+  Pair<Real> c = coef<Real, kPre>(tv, s0, dt), v = tv.v[s0];
+  // node s0 + 1 (or the chain's parent, or -- at the root -- the node itself)
+  const Pair<Real> v_top = ch.top_parent >= 0 ? tv.v[ch.top_parent] : tv.v[end - 1];
+  Pair<Real> q1 = q, c1 = c, v1 = v_top;
+  if (s0 + 1 < end) {
+    q1 = tv.dr[s0 + 1];
+    c1 = coef<Real, kPre>(tv, s0 + 1, dt);
+    v1 = tv.v[s0 + 1];
+  }
   for (int i = s0;; ++i) {
-    const bool nxt = i + 1 < end;
-    Real Dn = Real(0), Rn = Real(0), aln = Real(0), ben = Real(0), vhp = vh, vlp = vl;
-    if (nxt) {
-      Dn = tv.sdiag[i + 1];
-      Rn = tv.srhs[i + 1];
-      aln = tv.alpha[i + 1] * dt;
-      ben = tv.beta[i + 1] * dt;
-      vhp = tv.vhi[i + 1];
-      vlp = tv.vlo[i + 1];
-    } else if (ch.top_parent >= 0) {
-      vhp = tv.vhi[ch.top_parent];
-      vlp = tv.vlo[ch.top_parent];
+    Pair<Real> q2 = q1, c2 = c1, v2 = v_top;
+    if (i + 2 < end) {
+      q2 = tv.dr[i + 2];
+      c2 = coef<Real, kPre>(tv, i + 2, dt);
+      v2 = tv.v[i + 2];
     }
     const Real inv = pivot_rcp(D);
-    const Real delta = (vh - vhp) + (vl - vlp);
-    R -= al * delta;
-    tv.sdiag[i] = inv;
-    tv.srhs[i] = R;
-    const Real w = be * inv;
-    if (!nxt) {
+    const Real delta = (v.x - v1.x) + (v.y - v1.y);
+    R -= c.x * delta;
+    tv.dr[i] = make_pair(inv, R);
+    const Real w = c.y * inv;
+    if (i + 1 == end) {
       if (ch.slot >= 0) {
-        tv.scd[ch.slot] = al * w;
-        tv.scr[ch.slot] = w * R + be * delta;
+        tv.scd[ch.slot] = c.x * w;
+        tv.scr[ch.slot] = w * R + c.y * delta;
       }
       break;
     }
-    D = Dn - al * w;
-    R = Rn + w * R + be * delta;
-    al = aln;
-    be = ben;
-    vh = vhp;
-    vl = vlp;
+    D = q1.x - c.x * w;
+    R = q1.y + w * R + c.y * delta;
+    c = c1;
+    v = v1;
+    q1 = q2;
+    c1 = c2;
+    v1 = v2;
   }
 }
 
@@ -421,11 +475,12 @@ __device__ __forceinline__ void eliminate_regular(const TileView<Real>& tv, cons
 // and the changes this causes in row o -- diagonal, right-hand side, and the
 // coefficient H of x_b -- go to slot `slot` of scd / scr / sh.  Node b keeps its
 // (not inverted) pivot for the reduced system.
-template <typename Real>
+template <typename Real, bool kPre>
 __device__ __forceinline__ void eliminate_segment(const TileView<Real>& tv, const ChainRec& ch, Real dt) {
-  const int a = ch.start, b = ch.start + ch.count - 1;
-  Real D = tv.sdiag[a], R = tv.srhs[a];
-  Real al = tv.alpha[a] * dt, be = tv.beta[a] * dt, vh = tv.vhi[a], vl = tv.vlo[a];
+  const int a = ch.start, b = ch.start + ch.count - 1, end = b + 1;
+  Pair<Real> q = tv.dr[a];
+  Real D = q.x, R = q.y;
+  Pair<Real> c = coef<Real, kPre>(tv, a, dt), v = tv.v[a];
   Real g = Real(0), h = Real(0), dd = Real(0), dr = Real(0);
   if (ch.first) {
     for (int k = 0; k < ch.n_child; ++k) {
@@ -434,49 +489,49 @@ __device__ __forceinline__ void eliminate_segment(const TileView<Real>& tv, cons
     }
   } else {
     const int o = ch.aux;
-    const Real be_o = tv.beta[o] * dt;
-    R += be_o * ((tv.vhi[o] - vh) + (tv.vlo[o] - vl));
-    g = -be_o;
-    h = -tv.alpha[o] * dt;
+    const Pair<Real> co = coef<Real, kPre>(tv, o, dt);
+    const Pair<Real> vo = tv.v[o];
+    R += co.y * ((vo.x - v.x) + (vo.y - v.y));
+    g = -co.y;
+    h = -co.x;
+  }
+  const Pair<Real> v_top = ch.top_parent >= 0 ? tv.v[ch.top_parent] : tv.v[b];
+  Pair<Real> q1 = q, c1 = c, v1 = v_top;
+  if (a + 1 < end) {
+    q1 = tv.dr[a + 1];
+    c1 = coef<Real, kPre>(tv, a + 1, dt);
+    v1 = tv.v[a + 1];
   }
   for (int i = a;; ++i) {
-    const bool nxt = i < b;
-    Real Dn = Real(0), Rn = Real(0), aln = Real(0), ben = Real(0), vhp = vh, vlp = vl;
-    if (nxt) {
-      Dn = tv.sdiag[i + 1];
-      Rn = tv.srhs[i + 1];
-      aln = tv.alpha[i + 1] * dt;
-      ben = tv.beta[i + 1] * dt;
-      vhp = tv.vhi[i + 1];
-      vlp = tv.vlo[i + 1];
-    } else if (ch.top_parent >= 0) {
-      vhp = tv.vhi[ch.top_parent];
-      vlp = tv.vlo[ch.top_parent];
+    Pair<Real> q2 = q1, c2 = c1, v2 = v_top;
+    if (i + 2 < end) {
+      q2 = tv.dr[i + 2];
+      c2 = coef<Real, kPre>(tv, i + 2, dt);
+      v2 = tv.v[i + 2];
     }
-    const Real delta = (vh - vhp) + (vl - vlp);
-    R -= al * delta;
-    if (!nxt) {
-      tv.sdiag[i] = D;
-      tv.srhs[i] = R;
+    const Real delta = (v.x - v1.x) + (v.y - v1.y);
+    R -= c.x * delta;
+    if (i == b) {
+      tv.dr[i] = make_pair(D, R);
       tv.sfill[i] = g;
       break;
     }
     const Real inv = pivot_rcp(D);
-    const Real w = be * inv;
+    const Real w = c.y * inv;
     const Real hh = h * inv;
     dd -= hh * g;
     dr -= hh * R;
-    h = hh * al;
-    tv.sdiag[i] = inv;
-    tv.srhs[i] = R;
+    h = hh * c.x;
+    tv.dr[i] = make_pair(inv, R);
     tv.sfill[i] = g;
-    D = Dn - al * w;
-    R = Rn + w * R + be * delta;
+    D = q1.x - c.x * w;
+    R = q1.y + w * R + c.y * delta;
     g = w * g;
-    al = aln;
-    be = ben;
-    vh = vhp;
-    vl = vlp;
+    c = c1;
+    v = v1;
+    q1 = q2;
+    c1 = c2;
+    v1 = v2;
   }
   tv.scd[ch.slot] = dd;
   tv.scr[ch.slot] = dr;
@@ -485,7 +540,7 @@ __device__ __forceinline__ void eliminate_segment(const TileView<Real>& tv, cons
 
 // Reduced system over the segment tops y_1 .. y_K (bottom to top):
 //   row s: (d_s + dd_{s+1}) y_s + g_s y_{s-1} + H_{s+1} y_{s+1} = r_s + dr_{s+1}.
-template <typename Real>
+template <typename Real, bool kPre>
 __device__ __forceinline__ void eliminate_reduced(const TileView<Real>& tv, const ChainRec& ch, Real dt) {
   const int K = ch.n_child;
   Real inv_prev = Real(0), f_prev = Real(0);
@@ -493,7 +548,8 @@ __device__ __forceinline__ void eliminate_reduced(const TileView<Real>& tv, cons
   ChainRec sg = load_rec(tv.chains, tv.child[ch.aux]);
   for (int s = 0; s < K; ++s) {
     top = sg.start + sg.count - 1;
-    Real e = tv.sdiag[top], f = tv.srhs[top];
+    const Pair<Real> q = tv.dr[top];
+    Real e = q.x, f = q.y;
     ChainRec up = sg;
     if (s + 1 < K) {
       up = load_rec(tv.chains, tv.child[ch.aux + s + 1]);
@@ -507,96 +563,105 @@ __device__ __forceinline__ void eliminate_reduced(const TileView<Real>& tv, cons
     }
     inv_prev = pivot_rcp(e);
     f_prev = f;
-    tv.sdiag[top] = inv_prev;
-    tv.srhs[top] = f;
+    tv.dr[top] = make_pair(inv_prev, f);
     sg = up;
   }
   if (ch.slot >= 0) {
-    const Real al = tv.alpha[top] * dt, be = tv.beta[top] * dt;
-    const Real w = be * inv_prev;
-    tv.scd[ch.slot] = al * w;
-    tv.scr[ch.slot] = w * f_prev + be * ((tv.vhi[top] - tv.vhi[ch.top_parent]) + (tv.vlo[top] - tv.vlo[ch.top_parent]));
+    const Pair<Real> c = coef<Real, kPre>(tv, top, dt);
+    const Pair<Real> vt = tv.v[top], vp = tv.v[ch.top_parent];
+    const Real w = c.y * inv_prev;
+    tv.scd[ch.slot] = c.x * w;
+    tv.scr[ch.slot] = w * f_prev + c.y * ((vt.x - vp.x) + (vt.y - vp.y));
   }
 }
 
-template <typename Real>
+template <typename Real, bool kPre>
 __device__ __forceinline__ void eliminate_rec(const TileView<Real>& tv, const ChainRec& ch, Real dt) {
   if (ch.kind == kChainRegular)
-    eliminate_regular(tv, ch, dt);
+    eliminate_regular<Real, kPre>(tv, ch, dt);
   else if (ch.kind == kChainSegment)
-    eliminate_segment(tv, ch, dt);
+    eliminate_segment<Real, kPre>(tv, ch, dt);
   else
-    eliminate_reduced(tv, ch, dt);
+    eliminate_reduced<Real, kPre>(tv, ch, dt);
 }
 
-template <typename Real>
+template <typename Real, bool kPre>
 __device__ __forceinline__ void backsub_rec(const TileView<Real>& tv, const ChainRec& ch, Real dt) {
   if (ch.kind == kChainReduced) {
     const int K = ch.n_child;
     ChainRec sg = load_rec(tv.chains, tv.child[ch.aux + K - 1]);
     int top = sg.start + sg.count - 1;
-    const Real xp = ch.top_parent >= 0 ? tv.srhs[ch.top_parent] : Real(0);
-    Real y = (tv.srhs[top] + tv.alpha[top] * dt * xp) * tv.sdiag[top];
-    tv.srhs[top] = y;
+    const Real xp = ch.top_parent >= 0 ? tv.dr[ch.top_parent].y : Real(0);
+    Pair<Real> q = tv.dr[top];
+    Real y = (q.y + coef<Real, kPre>(tv, top, dt).x * xp) * q.x;
+    tv.dr[top].y = y;
     for (int s = K - 2; s >= 0; --s) {
       const Real H = tv.sh[sg.slot];  // coefficient of y_{s+1} in row s, left by segment s+1
       sg = load_rec(tv.chains, tv.child[ch.aux + s]);
       top = sg.start + sg.count - 1;
-      y = (tv.srhs[top] - H * y) * tv.sdiag[top];
-      tv.srhs[top] = y;
+      q = tv.dr[top];
+      y = (q.y - H * y) * q.x;
+      tv.dr[top].y = y;
     }
     return;
   }
   if (ch.kind == kChainSegment) {
     const int b = ch.start + ch.count - 1;
     if (b == ch.start) return;
-    const Real yo = ch.first ? Real(0) : tv.srhs[ch.aux];
-    Real xn = tv.srhs[b];
+    const Real yo = ch.first ? Real(0) : tv.dr[ch.aux].y;
+    Real xn = tv.dr[b].y;
     int i = b - 1;
-    Real r = tv.srhs[i], f = tv.sfill[i], inv = tv.sdiag[i], al = tv.alpha[i] * dt;
+    Pair<Real> q = tv.dr[i];
+    Real f = tv.sfill[i], al = coef<Real, kPre>(tv, i, dt).x;
     for (;; --i) {
       const bool nxt = i > ch.start;
-      Real rn = Real(0), fn = Real(0), invn = Real(0), aln = Real(0);
+      Pair<Real> qn = q;
+      Real fn = Real(0), aln = Real(0);
       if (nxt) {
-        rn = tv.srhs[i - 1];
+        qn = tv.dr[i - 1];
         fn = tv.sfill[i - 1];
-        invn = tv.sdiag[i - 1];
-        aln = tv.alpha[i - 1] * dt;
+        aln = coef<Real, kPre>(tv, i - 1, dt).x;
       }
-      const Real x = (r - f * yo + al * xn) * inv;
-      tv.srhs[i] = x;
+      const Real x = (q.y - f * yo + al * xn) * q.x;
+      tv.dr[i].y = x;
       xn = x;
       if (!nxt) break;
-      r = rn;
+      q = qn;
       f = fn;
-      inv = invn;
       al = aln;
     }
     return;
   }
   const int top = ch.start + ch.count - 1;
-  Real dp = ch.top_parent >= 0 ? tv.srhs[ch.top_parent] : Real(0);
-  Real r = tv.srhs[top], inv = tv.sdiag[top], al = tv.alpha[top] * dt;
+  Real dp = ch.top_parent >= 0 ? tv.dr[ch.top_parent].y : Real(0);
+  Pair<Real> q = tv.dr[top];
+  Real al = coef<Real, kPre>(tv, top, dt).x;
+  Pair<Real> q1 = q;
+  Real al1 = al;
+  if (top - 1 >= ch.start) {
+    q1 = tv.dr[top - 1];
+    al1 = coef<Real, kPre>(tv, top - 1, dt).x;
+  }
   for (int i = top;; --i) {
-    const bool nxt = i > ch.start;
-    Real rn = Real(0), invn = Real(0), aln = Real(0);
-    if (nxt) {
-      rn = tv.srhs[i - 1];
-      invn = tv.sdiag[i - 1];
-      aln = tv.alpha[i - 1] * dt;
+    Pair<Real> q2 = q1;
+    Real al2 = al1;
+    if (i - 2 >= ch.start) {
+      q2 = tv.dr[i - 2];
+      al2 = coef<Real, kPre>(tv, i - 2, dt).x;
     }
-    const Real x = (r + al * dp) * inv;
-    tv.srhs[i] = x;
+    const Real x = (q.y + al * dp) * q.x;
+    tv.dr[i].y = x;
     dp = x;
-    if (!nxt) break;
-    r = rn;
-    inv = invn;
-    al = aln;
+    if (i == ch.start) break;
+    q = q1;
+    al = al1;
+    q1 = q2;
+    al1 = al2;
   }
 }
 
 // A thread's records of one phase, with the next record prefetched.
-template <typename Real>
+template <typename Real, bool kPre>
 __device__ __forceinline__ void eliminate_list(const TileView<Real>& tv, int c0, int c1, Real dt) {
   if (c0 >= c1) return;
   ChainRec ch = load_rec(tv.chains, c0);
@@ -604,13 +669,13 @@ __device__ __forceinline__ void eliminate_list(const TileView<Real>& tv, int c0,
     const bool more = c + 1 < c1;
     ChainRec nx = ch;
     if (more) nx = load_rec(tv.chains, c + 1);
-    eliminate_rec(tv, ch, dt);
+    eliminate_rec<Real, kPre>(tv, ch, dt);
     if (!more) break;
     ch = nx;
   }
 }
 
-template <typename Real>
+template <typename Real, bool kPre>
 __device__ __forceinline__ void backsub_list(const TileView<Real>& tv, int c0, int c1, Real dt) {
   if (c0 >= c1) return;
   ChainRec ch = load_rec(tv.chains, c1 - 1);
@@ -618,7 +683,7 @@ __device__ __forceinline__ void backsub_list(const TileView<Real>& tv, int c0, i
     const bool more = c > c0;
     ChainRec nx = ch;
     if (more) nx = load_rec(tv.chains, c - 1);
-    backsub_rec(tv, ch, dt);
+    backsub_rec<Real, kPre>(tv, ch, dt);
     if (!more) break;
     ch = nx;
   }
@@ -676,13 +741,22 @@ __global__ void __launch_bounds__(1024) tile_step_kernel(LaunchArgs a) {
   const Real dt = Real(a.dt);
   const int T = blockDim.x, tid = threadIdx.x;
   const PulseRec* pulses = a.pulses + td.pulse_offset;
+  if constexpr (kSmem) {
+    // the staged axial coefficients become (alpha dt, beta dt) for this launch
+    for (int i = tid; i < tv.N; i += T) {
+      Pair<Real> c = tv.ab[i];
+      c.x *= dt;
+      c.y *= dt;
+      tv.ab[i] = c;
+    }
+  }
 
   // Prologue: the linear system of the first step from the current state.
   for (int i = tid; i < tv.n_real; i += T) {
     const uint16_t pr = tv.pidx[i];
     Real G = Real(0), I = Real(0);
     if (pr != kBoundary) {
-      const Real v = tv.vhi[i];
+      const Real v = tv.v[i].x;
       node_mechanisms(tv.state + i, tv.N, tv.params + size_t(pr) * BC_NPARAM, tv.mech[pr], v, v, dt, false, G, I);
     }
     write_row(tv, i, pr, dt, G, I);
@@ -709,13 +783,13 @@ __global__ void __launch_bounds__(1024) tile_step_kernel(LaunchArgs a) {
     const int64_t step = a.step0 + s;
     // forward elimination, leaves first
     for (int p = 0; p < tv.n_phases; ++p) {
-      eliminate_list(tv, tv.lists[p * (T + 1) + tid], tv.lists[p * (T + 1) + tid + 1], dt);
+      eliminate_list<Real, kSmem>(tv, tv.lists[p * (T + 1) + tid], tv.lists[p * (T + 1) + tid + 1], dt);
       __syncthreads();
     }
     BC_TICK(0);
     // back-substitution, root first
     for (int p = tv.n_phases - 1; p >= 0; --p) {
-      backsub_list(tv, tv.lists[p * (T + 1) + tid], tv.lists[p * (T + 1) + tid + 1], dt);
+      backsub_list<Real, kSmem>(tv, tv.lists[p * (T + 1) + tid], tv.lists[p * (T + 1) + tid + 1], dt);
       __syncthreads();
     }
     BC_TICK(1);
@@ -723,18 +797,34 @@ __global__ void __launch_bounds__(1024) tile_step_kernel(LaunchArgs a) {
     const bool last = s + 1 == a.n_steps;
     const int64_t k_since = step + 1 - a.trace_base;
     const bool record = a.record_every > 0 && k_since % a.record_every == 0;
+    // The states live in global memory (L2): the next node's are loaded one
+    // iteration ahead so that their latency overlaps this node's arithmetic.
+    NodeStates<Real> cur;
+    uint16_t pr_cur = kBoundary;
+    if (tid < tv.n_real) {
+      pr_cur = tv.pidx[tid];
+      if (pr_cur != kBoundary) load_states(tv.state + tid, tv.N, tv.mech[pr_cur], cur);
+    }
     for (int i = tid; i < tv.n_real; i += T) {
-      Real hi = tv.vhi[i], lo = tv.vlo[i];
+      NodeStates<Real> nxt;
+      uint16_t pr_nxt = kBoundary;
+      if (i + T < tv.n_real) {
+        pr_nxt = tv.pidx[i + T];
+        if (pr_nxt != kBoundary) load_states(tv.state + i + T, tv.N, tv.mech[pr_nxt], nxt);
+      }
+      const Pair<Real> vv = tv.v[i];
+      Real hi = vv.x, lo = vv.y;
       const Real v_old = hi, lo_old = lo;
-      ff_add(hi, lo, tv.srhs[i]);
-      tv.vhi[i] = hi;
-      tv.vlo[i] = lo;
+      ff_add(hi, lo, tv.dr[i].y);
+      tv.v[i] = make_pair(hi, lo);
       if (!is_finite_real(hi)) s_status = kStatusNonfinite;
-      const uint16_t pr = tv.pidx[i];
+      const uint16_t pr = pr_cur;
       Real G = Real(0), I = Real(0);
       if (pr != kBoundary)
-        node_mechanisms(tv.state + i, tv.N, tv.params + size_t(pr) * BC_NPARAM, tv.mech[pr], v_old, hi, dt, true, G,
-                        I);
+        node_mechanisms_loaded(cur, tv.state + i, tv.N, tv.params + size_t(pr) * BC_NPARAM, tv.mech[pr], v_old, hi, dt,
+                               true, G, I);
+      cur = nxt;
+      pr_cur = pr_nxt;
       if (!last) write_row(tv, i, pr, dt, G, I);
       const uint16_t sp = tv.spec[i];
       if (sp != kNoSpecial) {
@@ -787,8 +877,7 @@ __global__ void reset_kernel(LaunchArgs a, const double* vinit, const int64_t* v
   const double* vi = vinit + vinit_off[blockIdx.x];
   for (int i = threadIdx.x; i < tv.n_real; i += blockDim.x) {
     const Real v = Real(vi[i]);
-    tv.vhi[i] = v;
-    tv.vlo[i] = Real(0);
+    tv.v[i] = make_pair(v, Real(0));
     const uint16_t pr = tv.pidx[i];
     if (pr == kBoundary) continue;
     const Real* P = tv.params + size_t(pr) * BC_NPARAM;

@@ -15,6 +15,7 @@
 #include <array>
 #include <cmath>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <numeric>
 #include <queue>
@@ -471,15 +472,11 @@ static bc_status build_tile(const BuildCtx& cx, const TileBuild& tb, int T, Tile
   if (n_params >= 0xFFFF) return fail(BC_ERR_CAPACITY, "too many parameter records in one tile");
   TileDesc d{};
   size_t off = 0;
-  d.off_vhi = int32_t(off);
-  off = align16(off + N * rs);
-  d.off_vlo = int32_t(off);
-  off = align16(off + N * rs);
+  d.off_v = int32_t(off);
+  off = align16(off + 2 * N * rs);
   d.dyn_bytes = int32_t(off);
-  d.off_alpha = int32_t(off);
-  off = align16(off + N * rs);
-  d.off_beta = int32_t(off);
-  off = align16(off + N * rs);
+  d.off_ab = int32_t(off);
+  off = align16(off + 2 * N * rs);
   d.off_diag0 = int32_t(off);
   off = align16(off + N * rs);
   d.off_pidx = int32_t(off);
@@ -501,10 +498,8 @@ static bc_status build_tile(const BuildCtx& cx, const TileBuild& tb, int T, Tile
   if (off > size_t(0x7fffffff)) return fail(BC_ERR_CAPACITY, "tile blob exceeds 2 GiB");
   d.blob_bytes = int32_t(off);
   size_t so = 0;
-  d.off_sdiag = int32_t(so);
-  so = align16(so + N * rs);
-  d.off_srhs = int32_t(so);
-  so = align16(so + N * rs);
+  d.off_dr = int32_t(so);
+  so = align16(so + 2 * N * rs);
   d.off_scd = int32_t(so);
   so = align16(so + size_t(std::max(n_slots, 1)) * rs);
   d.off_scr = int32_t(so);
@@ -535,9 +530,9 @@ static bc_status build_tile(const BuildCtx& cx, const TileBuild& tb, int T, Tile
     const LoweredCell& lc = (*cx.cells)[c];
     for (int32_t v = 0; v < lc.n_node; ++v) {
       const int32_t j = node_tile[li][v];
-      putr(d.off_vhi, j, lc.node_vrest[v]);
-      putr(d.off_alpha, j, lc.alpha[v]);
-      putr(d.off_beta, j, lc.beta[v]);
+      putr(d.off_v, 2 * size_t(j), lc.node_vrest[v]);
+      putr(d.off_ab, 2 * size_t(j), lc.alpha[v]);
+      putr(d.off_ab, 2 * size_t(j) + 1, lc.beta[v]);
       putr(d.off_diag0, j, lc.diag[v]);
       const uint16_t pi = lc.region[v] >= 0 ? uint16_t(li * R + lc.region[v]) : uint16_t(0xFFFF);
       std::memcpy(b.data() + d.off_pidx + size_t(j) * 2, &pi, 2);
@@ -617,6 +612,12 @@ static bc_status build_tile(const BuildCtx& cx, const TileBuild& tb, int T, Tile
 static size_t max_optin_smem(int device) {
   int v = 0;
   if (cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, device) != cudaSuccess) return 0;
+  return size_t(v);
+}
+
+static size_t sm_smem(int device) {
+  int v = 0;
+  if (cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerMultiprocessor, device) != cudaSuccess) return 0;
   return size_t(v);
 }
 
@@ -878,7 +879,9 @@ bc_status bc_plan_create(const bc_batch_spec* spec, const bc_plan_options* opts_
                    [&](int64_t a, int64_t b) { return cells[a].n_node > cells[b].n_node; });
   std::vector<TileBuild> builds;
   std::vector<int64_t> fill;
-  // first-fit decreasing over the most recently opened tiles
+  // best-fit decreasing: each cell goes to the open packed tile with the least room
+  // that still holds it (free room -> tile index), else opens a new tile
+  std::multimap<int64_t, size_t> room;
   for (int64_t c : order) {
     const int64_t nn = cells[c].n_node;
     if (nn > tile_nodes) {
@@ -889,29 +892,35 @@ bc_status bc_plan_create(const bc_batch_spec* spec, const bc_plan_options* opts_
       fill.push_back(nn);
       continue;
     }
-    bool placed = false;
-    const size_t lo = builds.size() > 64 ? builds.size() - 64 : 0;
-    for (size_t t = lo; t < builds.size(); ++t) {
-      if (builds[t].cls == 0 && fill[t] + nn <= tile_nodes && builds[t].cells.size() < 4096) {
-        builds[t].cells.push_back(c);
-        fill[t] += nn;
-        placed = true;
-        break;
-      }
+    auto it = room.lower_bound(nn);
+    if (it != room.end()) {
+      const size_t t = it->second;
+      room.erase(it);
+      builds[t].cells.push_back(c);
+      fill[t] += nn;
+      if (tile_nodes - fill[t] > 0 && builds[t].cells.size() < 4096) room.emplace(tile_nodes - fill[t], t);
+      continue;
     }
-    if (!placed) {
-      TileBuild tb;
-      tb.cells.push_back(c);
-      tb.cls = 0;
-      builds.push_back(tb);
-      fill.push_back(nn);
-    }
+    TileBuild tb;
+    tb.cells.push_back(c);
+    tb.cls = 0;
+    builds.push_back(tb);
+    fill.push_back(nn);
+    if (tile_nodes - nn > 0) room.emplace(tile_nodes - nn, builds.size() - 1);
   }
   BuildCtx cx{&s, &cells, &sched, &cv_base, &cell_pulses, &cell_probes, &pulse_node, &probe_node,
               p->precision, S, p->thread_cell_max, opts.split_min, opts.split_factor > 0 ? opts.split_factor : 1.0};
   std::vector<TileOut> outs;
   outs.reserve(builds.size());
-  const size_t packed_budget = std::min(smem_budget, size_t(double(tile_nodes) * bpn) + 2048);
+  // Packed tiles: tile_nodes sets how many CTAs share an SM (by the per-node
+  // estimate); the shared-memory budget of one tile is then that SM's share, so
+  // tiles fill up to tile_nodes without lowering the occupancy.
+  const size_t per_sm = dry ? size_t(233472) : sm_smem(opts.device);
+  const size_t cta_reserve = 2 * static_smem;  // static shared memory + the system's per-CTA reserve
+  const size_t est = size_t(double(tile_nodes) * bpn) + 2048;
+  const size_t ctas_per_sm = std::max<size_t>(1, per_sm / (est + cta_reserve));
+  const size_t packed_budget =
+      std::min(smem_budget, std::max(est, per_sm / ctas_per_sm > cta_reserve ? per_sm / ctas_per_sm - cta_reserve : est));
   for (size_t t = 0; t < builds.size(); ++t) {
     TileOut to;
     bc_status st = build_tile(cx, builds[t], class_threads[builds[t].cls], to);
@@ -923,12 +932,28 @@ bc_status bc_plan_create(const bc_batch_spec* spec, const bc_plan_options* opts_
     const size_t limit = builds[t].cls == 0 ? packed_budget : smem_budget;
     if (builds[t].cls != 2 && need > limit) {
       if (builds[t].cells.size() > 1) {
-        // split: move the last cell into a new packed tile and rebuild this one
-        TileBuild nb;
-        nb.cells.push_back(builds[t].cells.back());
-        nb.cls = 0;
-        builds.push_back(nb);
+        // split: move the last cell into the best-fitting packed tile not built yet
+        // (or a new one) and rebuild this one
+        const int64_t c = builds[t].cells.back();
+        const int64_t nn = cells[c].n_node;
         builds[t].cells.pop_back();
+        fill[t] -= nn;
+        size_t dest = builds.size();
+        for (auto it = room.lower_bound(nn); it != room.end(); ++it)
+          if (it->second > t) {
+            dest = it->second;
+            room.erase(it);
+            break;
+          }
+        if (dest == builds.size()) {
+          TileBuild nb;
+          nb.cls = 0;
+          builds.push_back(nb);
+          fill.push_back(0);
+        }
+        builds[dest].cells.push_back(c);
+        fill[dest] += nn;
+        if (tile_nodes - fill[dest] > 0) room.emplace(tile_nodes - fill[dest], dest);
         --t;
         continue;
       }
@@ -1206,8 +1231,8 @@ static bc_status view_offsets(bc_plan* p, int32_t which, std::vector<int64_t>& h
     const int64_t j = p->cv_node[k];
     const int64_t base = d.blob_offset;
     if (which == BC_STATE_V) {
-      hi[k] = base + d.off_vhi + j * rs;
-      lo[k] = base + d.off_vlo + j * rs;
+      hi[k] = base + d.off_v + 2 * j * rs;
+      lo[k] = hi[k] + rs;
       continue;
     }
     const uint32_t m = p->cv_mech[k];
@@ -1306,8 +1331,8 @@ static void noalloc_offset(const bc_plan* p, int32_t which, int64_t k, int64_t* 
   *hi = -1;
   *lo = -1;
   if (which == BC_STATE_V) {
-    *hi = d.blob_offset + d.off_vhi + j * rs;
-    *lo = d.blob_offset + d.off_vlo + j * rs;
+    *hi = d.blob_offset + d.off_v + 2 * j * rs;
+    *lo = *hi + rs;
     return;
   }
   static const uint32_t kBit[BC_NSTATE_VIEW] = {0,         BC_M_NA,  BC_M_NA,  BC_M_KDR, BC_M_CAL, BC_M_CAL,
