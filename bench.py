@@ -48,7 +48,7 @@ def _args():
     ap.add_argument("--sim-steps", type=int, default=SIM_STEPS)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--tile-nodes", type=int, default=2500)
-    ap.add_argument("--threads", type=int, default=384)
+    ap.add_argument("--threads", type=int, default=512)
     ap.add_argument("--threads-big", type=int, default=512)
     ap.add_argument("--steps-per-launch", type=int, default=1000)
     return ap.parse_args()

@@ -40,19 +40,11 @@ bc_status lower_cell(const bc_batch_spec& spec, int64_t c, LoweredCell& out);
 int32_t locate_node(const bc_batch_spec& spec, int64_t c, const LoweredCell& lc, int32_t branch, double x);
 
 // ----------------------------------------------------------------- device records
-// Chain of nodes walked by one thread: nodes [start, start+count) of the tile,
-// bottom (deepest) first; node start+k+1 is the parent of node start+k.
-// A chain record (32 bytes, read as two 16-byte vectors).
-// kind = kChainRegular: a whole chain.  Its bottom pulls the contributions that its
-//   n_child child chains left in the consecutive slots aux .. aux + n_child.
-// kind = kChainSegment: one piece of a long chain split for parallel elimination.
-//   The lowest segment pulls children like a regular chain (aux = slot base); a
-//   higher one has aux = the top node of the segment below (its "outside" node).
-//   Its fill-in results (dd, dr, H) go to slot `slot`.
-// kind = kChainReduced: the reduced system joining the segments whose record ids
-//   are listed (bottom to top) in child[aux .. aux + n_child).
-// slot: where this record leaves its contribution to the parent junction
-//   (-1 at a root); `first` marks the lowest segment.
+// A chain: nodes [start, start+count) of the tile, bottom (deepest) first; node
+// start+k+1 is the parent of node start+k and top_parent is the parent of the top
+// node (-1 at a root).  The record owns the consecutive contribution slots
+// aux .. aux + n_child, one per child chain, and writes its own contribution to
+// the parent's slot `slot` (-1 at a root).  32 bytes, read as two 16-byte vectors.
 struct ChainRec {
   int32_t start;
   int32_t count;
@@ -64,8 +56,16 @@ struct ChainRec {
   int32_t first;
 };
 constexpr int32_t kChainRegular = 0;
-constexpr int32_t kChainSegment = 1;
-constexpr int32_t kChainReduced = 2;
+
+// A warp slot of one phase: nodes [n_begin, n_begin + n_count) in lane order.
+// chunk == 1: lane l owns node n_begin + l (several chains side by side);
+// chunk > 1: a single chain, lane l owns the chunk-node range starting at
+// n_begin + l * chunk.
+struct SlotRec {
+  int32_t n_begin;
+  int16_t n_count;
+  int16_t chunk;
+};
 
 // Per-tile descriptor (global memory, read-only).
 struct TileDesc {
@@ -88,10 +88,10 @@ struct TileDesc {
   int64_t state_offset;     // elements into the plan's global mechanism-state array ([slot][n_nodes])
   int32_t off_ab;           // (alpha, beta) pairs
   int32_t off_diag0, off_pidx, off_spec, off_specs;
-  int32_t off_chains, off_child, off_lists, off_params, off_mech;
+  int32_t off_chains, off_slots, off_phase, off_crec, off_params, off_mech;
   int32_t scratch_bytes;    // diag/rhs/cD/cR scratch (shared memory after the blob)
   int32_t off_dr;           // (diagonal, rhs) pairs, inside the scratch area
-  int32_t off_scd, off_scr, off_sfill, off_sh;  // offsets inside the scratch area
+  int32_t off_scd, off_scr;  // contribution slots, inside the scratch area
   int32_t n_slots;          // contribution slots (scd / scr / sh entries)
   int32_t pad1;
   int64_t scratch_offset;   // bytes into the plan's global scratch (global-resident tiles)

@@ -119,12 +119,13 @@ struct TileView {
   Pair<Real>* dr;  // (diagonal, rhs) of the row; (1 / pivot, rhs or x) during the sweeps
   Real* state;
   const Real *diag0, *params;
-  const int32_t *child, *lists;
-  const uint16_t *pidx, *spec;
+  const SlotRec* slots;   // warp slots, phase by phase
+  const int32_t* phase;    // [n_phases + 1] slot ranges
+  const uint16_t *pidx, *spec, *crec;
   const ChainRec* chains;
   const SpecRec* specs;
   const uint32_t* mech;
-  Real *scd, *scr, *sfill, *sh;
+  Real *scd, *scr;
   int N, n_real, n_phases;
 
   __device__ __forceinline__ void bind(const TileDesc& td, unsigned char* base, unsigned char* scratch, void* gstate) {
@@ -134,8 +135,9 @@ struct TileView {
     state = reinterpret_cast<Real*>(gstate) + td.state_offset;
     diag0 = reinterpret_cast<const Real*>(base + td.off_diag0);
     params = reinterpret_cast<const Real*>(base + td.off_params);
-    child = reinterpret_cast<const int32_t*>(base + td.off_child);
-    lists = reinterpret_cast<const int32_t*>(base + td.off_lists);
+    slots = reinterpret_cast<const SlotRec*>(base + td.off_slots);
+    phase = reinterpret_cast<const int32_t*>(base + td.off_phase);
+    crec = reinterpret_cast<const uint16_t*>(base + td.off_crec);
     pidx = reinterpret_cast<const uint16_t*>(base + td.off_pidx);
     spec = reinterpret_cast<const uint16_t*>(base + td.off_spec);
     chains = reinterpret_cast<const ChainRec*>(base + td.off_chains);
@@ -143,8 +145,6 @@ struct TileView {
     mech = reinterpret_cast<const uint32_t*>(base + td.off_mech);
     scd = reinterpret_cast<Real*>(scratch + td.off_scd);
     scr = reinterpret_cast<Real*>(scratch + td.off_scr);
-    sfill = reinterpret_cast<Real*>(scratch + td.off_sfill);
-    sh = reinterpret_cast<Real*>(scratch + td.off_sh);
     N = td.n_nodes;
     n_real = td.n_real_nodes;
     n_phases = td.n_phases;
@@ -391,11 +391,21 @@ __device__ __forceinline__ void add_node_pulses(const TileView<Real>& tv, const 
 // ---------------------------------------------------------------- Hines sweeps
 // Row i of the increment system (V_{n+1} = V_n + x):
 //   d_i x_i - alpha_i x_parent - sum_c beta_c x_c = rhs_i - alpha_i Delta_i + sum_c beta_c Delta_c
-// with Delta_i = V_i - V_parent (float-float).  Chains are walked bottom -> top;
-// eliminating node i hands (cD, cR) = (alpha_i w, w r_i + beta_i Delta_i),
-// w = beta_i / d_i, to its parent.  Per node a walk touches three pairs -- (d, r),
-// (alpha dt, beta dt) and (V_hi, V_lo) -- loaded two nodes ahead, so that the
-// shared-memory latency stays off the pivot recurrence.
+// with Delta_i = V_i - V_parent (float-float).  Along a chain (node k+1 is the
+// parent of node k; a = alpha dt, b = beta dt) elimination is the recurrence
+//   D_0 = d_0 - sum cD(children),  R_0 = r_0 + sum cR(children),
+//   R'_k = R_k - a_k Delta_k,  w_k = b_k / D_k,
+//   D_{k+1} = d_{k+1} - a_k b_k / D_k,  R_{k+1} = r_{k+1} + w_k R'_k + b_k Delta_k,
+// the chain top hands (cD, cR) = (a w, w R' + b Delta) to its parent, and back-
+// substitution is x_k = (R'_k + a_k x_{k+1}) / D_k.  All three are associative
+// scans along the chain: D through the projective (Moebius) form
+//   [p; q]_{k+1} = [[d_{k+1}, -a_k b_k], [1, 0]] [p; q]_k,  D = p / q,
+// R' and x through affine maps.  A warp slot scans its chains with shuffles,
+// segmented at chain bottoms (forward) or tops (backward).  In a slot whose single
+// chain is longer than 32 nodes each lane first composes its chunk serially, the
+// lanes then scan the chunk maps, and each lane re-walks its chunk from the carry.
+
+constexpr unsigned kFullMask = 0xffffffffu;
 
 __device__ __forceinline__ ChainRec load_rec(const ChainRec* recs, int c) {
   const int4* p = reinterpret_cast<const int4*>(recs + c);
@@ -423,269 +433,348 @@ __device__ __forceinline__ Pair<Real> coef(const TileView<Real>& tv, int i, Real
   return c;
 }
 
-template <typename Real, bool kPre>
-__device__ __forceinline__ void eliminate_regular(const TileView<Real>& tv, const ChainRec& ch, Real dt) {
-  const int s0 = ch.start, end = ch.start + ch.count;
-  Pair<Real> q = tv.dr[s0];
-  Real D = q.x, R = q.y;
-  for (int k = 0; k < ch.n_child; ++k) {
-    D -= tv.scd[ch.aux + k];
-    R += tv.scr[ch.aux + k];
-  }
-  Pair<Real> c = coef<Real, kPre>(tv, s0, dt), v = tv.v[s0];
-  // node s0 + 1 (or the chain's parent, or -- at the root -- the node itself)
-  const Pair<Real> v_top = ch.top_parent >= 0 ? tv.v[ch.top_parent] : tv.v[end - 1];
-  Pair<Real> q1 = q, c1 = c, v1 = v_top;
-  if (s0 + 1 < end) {
-    q1 = tv.dr[s0 + 1];
-    c1 = coef<Real, kPre>(tv, s0 + 1, dt);
-    v1 = tv.v[s0 + 1];
-  }
-  for (int i = s0;; ++i) {
-    Pair<Real> q2 = q1, c2 = c1, v2 = v_top;
-    if (i + 2 < end) {
-      q2 = tv.dr[i + 2];
-      c2 = coef<Real, kPre>(tv, i + 2, dt);
-      v2 = tv.v[i + 2];
+__device__ __forceinline__ float rabs(float x) { return fabsf(x); }
+__device__ __forceinline__ double rabs(double x) { return fabs(x); }
+__device__ __forceinline__ float rmax(float x, float y) { return fmaxf(x, y); }
+__device__ __forceinline__ double rmax(double x, double y) { return fmax(x, y); }
+
+// 2^-floor(log2 m) for m > 0 (exact scaling by a power of two; the exponent is
+// clamped so that the result stays a normal number).
+__device__ __forceinline__ float pow2_inv(float m) {
+  int e = (__float_as_int(m) >> 23) & 0xff;
+  e = min(max(e, 1), 253);
+  return __int_as_float((254 - e) << 23);
+}
+__device__ __forceinline__ double pow2_inv(double m) {
+  long long e = (__double_as_longlong(m) >> 52) & 0x7ff;
+  e = min(max(e, 1LL), 2045LL);
+  return __longlong_as_double((2046LL - e) << 52);
+}
+
+template <typename Real>
+struct Mob {
+  Real m00, m01, m10, m11;  // [[m00, m01], [m10, m11]]
+};
+
+// hi * lo (hi is the later map), rescaled by a power of two: the projective
+// ratio it defines does not change, and the entries stay in range.
+template <typename Real>
+__device__ __forceinline__ Mob<Real> mob_mul(const Mob<Real>& hi, const Mob<Real>& lo) {
+  Mob<Real> r;
+  r.m00 = hi.m00 * lo.m00 + hi.m01 * lo.m10;
+  r.m01 = hi.m00 * lo.m01 + hi.m01 * lo.m11;
+  r.m10 = hi.m10 * lo.m00 + hi.m11 * lo.m10;
+  r.m11 = hi.m10 * lo.m01 + hi.m11 * lo.m11;
+  const Real s = pow2_inv(rmax(rmax(rabs(r.m00), rabs(r.m01)), rmax(rabs(r.m10), rabs(r.m11))));
+  r.m00 *= s;
+  r.m01 *= s;
+  r.m10 *= s;
+  r.m11 *= s;
+  return r;
+}
+
+template <typename Real>
+__device__ __forceinline__ Mob<Real> mob_shfl_up(const Mob<Real>& m, int off) {
+  Mob<Real> o;
+  o.m00 = __shfl_up_sync(kFullMask, m.m00, off);
+  o.m01 = __shfl_up_sync(kFullMask, m.m01, off);
+  o.m10 = __shfl_up_sync(kFullMask, m.m10, off);
+  o.m11 = __shfl_up_sync(kFullMask, m.m11, off);
+  return o;
+}
+
+// Inclusive segmented scan of Moebius maps over the lanes (lane order = chain
+// order); a lane with `head` set starts a new segment.
+template <typename Real>
+__device__ __forceinline__ Mob<Real> scan_mob(Mob<Real> m, bool head, int lane) {
+  int f = head ? 1 : 0;
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    const Mob<Real> o = mob_shfl_up(m, off);
+    const int of = __shfl_up_sync(kFullMask, f, off);
+    if (lane >= off && !f) {
+      m = mob_mul(m, o);
+      f = of;
     }
-    const Real inv = pivot_rcp(D);
-    const Real delta = (v.x - v1.x) + (v.y - v1.y);
-    R -= c.x * delta;
-    tv.dr[i] = make_pair(inv, R);
-    const Real w = c.y * inv;
-    if (i + 1 == end) {
-      if (ch.slot >= 0) {
-        tv.scd[ch.slot] = c.x * w;
-        tv.scr[ch.slot] = w * R + c.y * delta;
-      }
-      break;
+  }
+  return m;
+}
+
+// Inclusive segmented scan of affine maps x -> a x + b, later lanes applied last.
+template <typename Real>
+__device__ __forceinline__ void scan_aff_up(Real& a, Real& b, bool head, int lane) {
+  int f = head ? 1 : 0;
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    const Real oa = __shfl_up_sync(kFullMask, a, off);
+    const Real ob = __shfl_up_sync(kFullMask, b, off);
+    const int of = __shfl_up_sync(kFullMask, f, off);
+    if (lane >= off && !f) {
+      b = a * ob + b;
+      a = a * oa;
+      f = of;
     }
-    D = q1.x - c.x * w;
-    R = q1.y + w * R + c.y * delta;
-    c = c1;
-    v = v1;
-    q1 = q2;
-    c1 = c2;
-    v1 = v2;
   }
 }
 
-// One segment [a, b] of a split chain.  Nodes a .. b-1 are eliminated; the fill
-// coefficient g_i of row i on x_o (o = top of the segment below) is kept in sfill,
-// and the changes this causes in row o -- diagonal, right-hand side, and the
-// coefficient H of x_b -- go to slot `slot` of scd / scr / sh.  Node b keeps its
-// (not inverted) pivot for the reduced system.
-template <typename Real, bool kPre>
-__device__ __forceinline__ void eliminate_segment(const TileView<Real>& tv, const ChainRec& ch, Real dt) {
-  const int a = ch.start, b = ch.start + ch.count - 1, end = b + 1;
-  Pair<Real> q = tv.dr[a];
-  Real D = q.x, R = q.y;
-  Pair<Real> c = coef<Real, kPre>(tv, a, dt), v = tv.v[a];
-  Real g = Real(0), h = Real(0), dd = Real(0), dr = Real(0);
-  if (ch.first) {
-    for (int k = 0; k < ch.n_child; ++k) {
-      D -= tv.scd[ch.aux + k];
-      R += tv.scr[ch.aux + k];
+// The same towards lower lanes (back-substitution runs from chain tops down);
+// a lane with `top` set starts a new segment.
+template <typename Real>
+__device__ __forceinline__ void scan_aff_down(Real& a, Real& b, bool top, int lane) {
+  int f = top ? 1 : 0;
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    const Real oa = __shfl_down_sync(kFullMask, a, off);
+    const Real ob = __shfl_down_sync(kFullMask, b, off);
+    const int of = __shfl_down_sync(kFullMask, f, off);
+    if (lane + off < 32 && !f) {
+      b = a * ob + b;
+      a = a * oa;
+      f = of;
     }
+  }
+}
+
+template <typename Real>
+__device__ __forceinline__ Pair<Real> shfl_up_pair(const Pair<Real>& p, int off) {
+  return make_pair<Real>(__shfl_up_sync(kFullMask, p.x, off), __shfl_up_sync(kFullMask, p.y, off));
+}
+template <typename Real>
+__device__ __forceinline__ Pair<Real> shfl_down_pair(const Pair<Real>& p, int off) {
+  return make_pair<Real>(__shfl_down_sync(kFullMask, p.x, off), __shfl_down_sync(kFullMask, p.y, off));
+}
+
+template <typename Real>
+__device__ __forceinline__ Real vdelta(const Pair<Real>& v, const Pair<Real>& up) {
+  return (v.x - up.x) + (v.y - up.y);
+}
+
+// Children's contributions pulled by a chain bottom.
+template <typename Real>
+__device__ __forceinline__ void pull_children(const TileView<Real>& tv, const ChainRec& ch, Real& D, Real& R) {
+  for (int j = 0; j < ch.n_child; ++j) {
+    D -= tv.scd[ch.aux + j];
+    R += tv.scr[ch.aux + j];
+  }
+}
+
+// Elimination of one warp slot holding one node per lane.
+template <typename Real, bool kPre>
+__device__ __forceinline__ void eliminate_lanes(const TileView<Real>& tv, const SlotRec& sr, int lane, Real dt) {
+  const bool valid = lane < sr.n_count;
+  const int k = sr.n_begin + (valid ? lane : 0);
+  const ChainRec ch = load_rec(tv.chains, tv.crec[k]);
+  const bool head = !valid || k == ch.start;
+  const bool tail = valid && k == ch.start + ch.count - 1;
+  const Pair<Real> q = tv.dr[k];
+  const Pair<Real> c = coef<Real, kPre>(tv, k, dt);
+  const Pair<Real> v = tv.v[k];
+  Pair<Real> vup = shfl_down_pair<Real>(v, 1);  // node k+1 sits in the next lane
+  if (tail) vup = ch.top_parent >= 0 ? tv.v[ch.top_parent] : v;
+  const Real delta = vdelta<Real>(v, vup);
+  const Pair<Real> cp = shfl_up_pair<Real>(c, 1);  // node k-1 sits in the previous lane
+  const Real deltap = __shfl_up_sync(kFullMask, delta, 1);
+  Real D0 = q.x, R0 = q.y;
+  if (head && valid) pull_children(tv, ch, D0, R0);
+  Mob<Real> m;
+  m.m10 = Real(1);
+  m.m11 = Real(0);
+  if (head) {
+    m.m00 = D0;
+    m.m01 = Real(0);
   } else {
-    const int o = ch.aux;
-    const Pair<Real> co = coef<Real, kPre>(tv, o, dt);
-    const Pair<Real> vo = tv.v[o];
-    R += co.y * ((vo.x - v.x) + (vo.y - v.y));
-    g = -co.y;
-    h = -co.x;
+    m.m00 = q.x;
+    m.m01 = -cp.x * cp.y;
   }
-  const Pair<Real> v_top = ch.top_parent >= 0 ? tv.v[ch.top_parent] : tv.v[b];
-  Pair<Real> q1 = q, c1 = c, v1 = v_top;
-  if (a + 1 < end) {
-    q1 = tv.dr[a + 1];
-    c1 = coef<Real, kPre>(tv, a + 1, dt);
-    v1 = tv.v[a + 1];
+  m = scan_mob(m, head, lane);
+  const Real inv = m.m10 * pivot_rcp(m.m00);
+  const Real w = c.y * inv;
+  const Real wp = __shfl_up_sync(kFullMask, w, 1);
+  Real a, b;
+  if (head) {
+    a = Real(0);
+    b = R0 - c.x * delta;
+  } else {
+    a = wp;
+    b = q.y + cp.y * deltap - c.x * delta;
   }
-  for (int i = a;; ++i) {
-    Pair<Real> q2 = q1, c2 = c1, v2 = v_top;
-    if (i + 2 < end) {
-      q2 = tv.dr[i + 2];
-      c2 = coef<Real, kPre>(tv, i + 2, dt);
-      v2 = tv.v[i + 2];
+  scan_aff_up(a, b, head, lane);
+  if (valid) {
+    tv.dr[k] = make_pair(inv, b);
+    if (tail && ch.slot >= 0) {
+      tv.scd[ch.slot] = c.x * w;
+      tv.scr[ch.slot] = w * b + c.y * delta;
     }
-    const Real delta = (v.x - v1.x) + (v.y - v1.y);
-    R -= c.x * delta;
-    if (i == b) {
-      tv.dr[i] = make_pair(D, R);
-      tv.sfill[i] = g;
-      break;
-    }
-    const Real inv = pivot_rcp(D);
-    const Real w = c.y * inv;
-    const Real hh = h * inv;
-    dd -= hh * g;
-    dr -= hh * R;
-    h = hh * c.x;
-    tv.dr[i] = make_pair(inv, R);
-    tv.sfill[i] = g;
-    D = q1.x - c.x * w;
-    R = q1.y + w * R + c.y * delta;
-    g = w * g;
-    c = c1;
-    v = v1;
-    q1 = q2;
-    c1 = c2;
-    v1 = v2;
-  }
-  tv.scd[ch.slot] = dd;
-  tv.scr[ch.slot] = dr;
-  tv.sh[ch.slot] = h;
-}
-
-// Reduced system over the segment tops y_1 .. y_K (bottom to top):
-//   row s: (d_s + dd_{s+1}) y_s + g_s y_{s-1} + H_{s+1} y_{s+1} = r_s + dr_{s+1}.
-template <typename Real, bool kPre>
-__device__ __forceinline__ void eliminate_reduced(const TileView<Real>& tv, const ChainRec& ch, Real dt) {
-  const int K = ch.n_child;
-  Real inv_prev = Real(0), f_prev = Real(0);
-  int top = -1;
-  ChainRec sg = load_rec(tv.chains, tv.child[ch.aux]);
-  for (int s = 0; s < K; ++s) {
-    top = sg.start + sg.count - 1;
-    const Pair<Real> q = tv.dr[top];
-    Real e = q.x, f = q.y;
-    ChainRec up = sg;
-    if (s + 1 < K) {
-      up = load_rec(tv.chains, tv.child[ch.aux + s + 1]);
-      e += tv.scd[up.slot];
-      f += tv.scr[up.slot];
-    }
-    if (s > 0) {
-      const Real mlt = tv.sfill[top] * inv_prev;
-      e -= mlt * tv.sh[sg.slot];
-      f -= mlt * f_prev;
-    }
-    inv_prev = pivot_rcp(e);
-    f_prev = f;
-    tv.dr[top] = make_pair(inv_prev, f);
-    sg = up;
-  }
-  if (ch.slot >= 0) {
-    const Pair<Real> c = coef<Real, kPre>(tv, top, dt);
-    const Pair<Real> vt = tv.v[top], vp = tv.v[ch.top_parent];
-    const Real w = c.y * inv_prev;
-    tv.scd[ch.slot] = c.x * w;
-    tv.scr[ch.slot] = w * f_prev + c.y * ((vt.x - vp.x) + (vt.y - vp.y));
   }
 }
 
+// Elimination of a slot holding one chain longer than 32 nodes, a chunk per lane.
 template <typename Real, bool kPre>
-__device__ __forceinline__ void eliminate_rec(const TileView<Real>& tv, const ChainRec& ch, Real dt) {
-  if (ch.kind == kChainRegular)
-    eliminate_regular<Real, kPre>(tv, ch, dt);
-  else if (ch.kind == kChainSegment)
-    eliminate_segment<Real, kPre>(tv, ch, dt);
-  else
-    eliminate_reduced<Real, kPre>(tv, ch, dt);
-}
-
-template <typename Real, bool kPre>
-__device__ __forceinline__ void backsub_rec(const TileView<Real>& tv, const ChainRec& ch, Real dt) {
-  if (ch.kind == kChainReduced) {
-    const int K = ch.n_child;
-    ChainRec sg = load_rec(tv.chains, tv.child[ch.aux + K - 1]);
-    int top = sg.start + sg.count - 1;
-    const Real xp = ch.top_parent >= 0 ? tv.dr[ch.top_parent].y : Real(0);
-    Pair<Real> q = tv.dr[top];
-    Real y = (q.y + coef<Real, kPre>(tv, top, dt).x * xp) * q.x;
-    tv.dr[top].y = y;
-    for (int s = K - 2; s >= 0; --s) {
-      const Real H = tv.sh[sg.slot];  // coefficient of y_{s+1} in row s, left by segment s+1
-      sg = load_rec(tv.chains, tv.child[ch.aux + s]);
-      top = sg.start + sg.count - 1;
-      q = tv.dr[top];
-      y = (q.y - H * y) * q.x;
-      tv.dr[top].y = y;
-    }
-    return;
-  }
-  if (ch.kind == kChainSegment) {
-    const int b = ch.start + ch.count - 1;
-    if (b == ch.start) return;
-    const Real yo = ch.first ? Real(0) : tv.dr[ch.aux].y;
-    Real xn = tv.dr[b].y;
-    int i = b - 1;
-    Pair<Real> q = tv.dr[i];
-    Real f = tv.sfill[i], al = coef<Real, kPre>(tv, i, dt).x;
-    for (;; --i) {
-      const bool nxt = i > ch.start;
-      Pair<Real> qn = q;
-      Real fn = Real(0), aln = Real(0);
-      if (nxt) {
-        qn = tv.dr[i - 1];
-        fn = tv.sfill[i - 1];
-        aln = coef<Real, kPre>(tv, i - 1, dt).x;
-      }
-      const Real x = (q.y - f * yo + al * xn) * q.x;
-      tv.dr[i].y = x;
-      xn = x;
-      if (!nxt) break;
-      q = qn;
-      f = fn;
-      al = aln;
-    }
-    return;
-  }
+__device__ __forceinline__ void eliminate_chunked(const TileView<Real>& tv, const SlotRec& sr, int lane, Real dt) {
+  const ChainRec ch = load_rec(tv.chains, tv.crec[sr.n_begin]);
+  const int C = sr.chunk;
+  const int k0 = sr.n_begin + lane * C;
+  const int len = max(0, min(C, int(sr.n_count) - lane * C));
   const int top = ch.start + ch.count - 1;
-  Real dp = ch.top_parent >= 0 ? tv.dr[ch.top_parent].y : Real(0);
-  Pair<Real> q = tv.dr[top];
-  Real al = coef<Real, kPre>(tv, top, dt).x;
-  Pair<Real> q1 = q;
-  Real al1 = al;
-  if (top - 1 >= ch.start) {
-    q1 = tv.dr[top - 1];
-    al1 = coef<Real, kPre>(tv, top - 1, dt).x;
+  const bool head = lane == 0;
+  const bool seg = head || len == 0;
+  Real D0 = Real(0), R0 = Real(0);
+  if (head) {
+    const Pair<Real> q = tv.dr[ch.start];
+    D0 = q.x;
+    R0 = q.y;
+    pull_children(tv, ch, D0, R0);
   }
-  for (int i = top;; --i) {
-    Pair<Real> q2 = q1;
-    Real al2 = al1;
-    if (i - 2 >= ch.start) {
-      q2 = tv.dr[i - 2];
-      al2 = coef<Real, kPre>(tv, i - 2, dt).x;
+  // chunk map of the pivot recurrence
+  Mob<Real> m{Real(1), Real(0), Real(0), Real(1)};
+  for (int j = 0; j < len; ++j) {
+    const int k = k0 + j;
+    Mob<Real> e;
+    e.m10 = Real(1);
+    e.m11 = Real(0);
+    if (k == ch.start) {
+      e.m00 = D0;
+      e.m01 = Real(0);
+    } else {
+      const Pair<Real> cp = coef<Real, kPre>(tv, k - 1, dt);
+      e.m00 = tv.dr[k].x;
+      e.m01 = -cp.x * cp.y;
     }
-    const Real x = (q.y + al * dp) * q.x;
-    tv.dr[i].y = x;
-    dp = x;
-    if (i == ch.start) break;
-    q = q1;
-    al = al1;
-    q1 = q2;
-    al1 = al2;
+    m = mob_mul(e, m);
+  }
+  m = scan_mob(m, seg, lane);
+  Mob<Real> mx = mob_shfl_up(m, 1);
+  // re-walk: pivots of the chunk from the state after the previous lane's chunk
+  Real p = mx.m00, pq = mx.m10;
+  for (int j = 0; j < len; ++j) {
+    const int k = k0 + j;
+    if (k == ch.start) {
+      p = D0;
+      pq = Real(1);
+    } else {
+      const Pair<Real> cp = coef<Real, kPre>(tv, k - 1, dt);
+      const Real np = tv.dr[k].x * p - cp.x * cp.y * pq;
+      pq = p;
+      p = np;
+      const Real s = pow2_inv(rmax(rabs(p), rabs(pq)));
+      p *= s;
+      pq *= s;
+    }
+    tv.dr[k].x = pq * pivot_rcp(p);  // 1 / D_k
+  }
+  __syncwarp();
+  // chunk map of the right-hand-side recurrence R'_k = a_k R'_{k-1} + b_k
+  Real fa = Real(1), fb = Real(0);
+  for (int j = 0; j < len; ++j) {
+    const int k = k0 + j;
+    const Pair<Real> c = coef<Real, kPre>(tv, k, dt);
+    const Pair<Real> v = tv.v[k];
+    const Pair<Real> vup = k == top ? (ch.top_parent >= 0 ? tv.v[ch.top_parent] : v) : tv.v[k + 1];
+    const Real delta = vdelta<Real>(v, vup);
+    Real a, b;
+    if (k == ch.start) {
+      a = Real(0);
+      b = R0 - c.x * delta;
+    } else {
+      const Pair<Real> cp = coef<Real, kPre>(tv, k - 1, dt);
+      a = cp.y * tv.dr[k - 1].x;
+      b = tv.dr[k].y + cp.y * vdelta<Real>(tv.v[k - 1], v) - c.x * delta;
+    }
+    tv.dr[k].y = b;
+    fb = a * fb + b;
+    fa = a * fa;
+  }
+  scan_aff_up(fa, fb, seg, lane);
+  Real r = __shfl_up_sync(kFullMask, fb, 1);
+  for (int j = 0; j < len; ++j) {
+    const int k = k0 + j;
+    Real a = Real(0);
+    if (k != ch.start) a = coef<Real, kPre>(tv, k - 1, dt).y * tv.dr[k - 1].x;
+    r = a * r + tv.dr[k].y;
+    tv.dr[k].y = r;
+    if (k == top && ch.slot >= 0) {
+      const Pair<Real> c = coef<Real, kPre>(tv, k, dt);
+      const Pair<Real> v = tv.v[k];
+      const Pair<Real> vup = ch.top_parent >= 0 ? tv.v[ch.top_parent] : v;
+      const Real w = c.y * tv.dr[k].x;
+      tv.scd[ch.slot] = c.x * w;
+      tv.scr[ch.slot] = w * r + c.y * vdelta<Real>(v, vup);
+    }
   }
 }
 
-// A thread's records of one phase, with the next record prefetched.
+// Back-substitution of one warp slot holding one node per lane.
 template <typename Real, bool kPre>
-__device__ __forceinline__ void eliminate_list(const TileView<Real>& tv, int c0, int c1, Real dt) {
-  if (c0 >= c1) return;
-  ChainRec ch = load_rec(tv.chains, c0);
-  for (int c = c0;; ++c) {
-    const bool more = c + 1 < c1;
-    ChainRec nx = ch;
-    if (more) nx = load_rec(tv.chains, c + 1);
-    eliminate_rec<Real, kPre>(tv, ch, dt);
-    if (!more) break;
-    ch = nx;
+__device__ __forceinline__ void backsub_lanes(const TileView<Real>& tv, const SlotRec& sr, int lane, Real dt) {
+  const bool valid = lane < sr.n_count;
+  const int k = sr.n_begin + (valid ? lane : 0);
+  const ChainRec ch = load_rec(tv.chains, tv.crec[k]);
+  const bool tail = valid && k == ch.start + ch.count - 1;
+  const Pair<Real> q = tv.dr[k];  // (1 / D, R')
+  Real A = coef<Real, kPre>(tv, k, dt).x * q.x, B = q.y * q.x;
+  if (tail) {
+    const Real xp = ch.top_parent >= 0 ? tv.dr[ch.top_parent].y : Real(0);
+    B = A * xp + B;
+    A = Real(0);
+  }
+  scan_aff_down(A, B, !valid || tail, lane);
+  if (valid) tv.dr[k].y = B;
+}
+
+// Back-substitution of a slot holding one long chain, a chunk per lane.
+template <typename Real, bool kPre>
+__device__ __forceinline__ void backsub_chunked(const TileView<Real>& tv, const SlotRec& sr, int lane, Real dt) {
+  const ChainRec ch = load_rec(tv.chains, tv.crec[sr.n_begin]);
+  const int C = sr.chunk;
+  const int k0 = sr.n_begin + lane * C;
+  const int len = max(0, min(C, int(sr.n_count) - lane * C));
+  const int top = ch.start + ch.count - 1;
+  const Real xp = ch.top_parent >= 0 ? tv.dr[ch.top_parent].y : Real(0);
+  const bool has_top = len > 0 && k0 + len - 1 == top;
+  Real fa = Real(1), fb = Real(0);
+  for (int j = len - 1; j >= 0; --j) {
+    const int k = k0 + j;
+    const Pair<Real> q = tv.dr[k];
+    Real A = coef<Real, kPre>(tv, k, dt).x * q.x, B = q.y * q.x;
+    if (k == top) {
+      B = A * xp + B;
+      A = Real(0);
+    }
+    fb = A * fb + B;
+    fa = A * fa;
+  }
+  scan_aff_down(fa, fb, len == 0 || has_top, lane);
+  Real x = __shfl_down_sync(kFullMask, fb, 1);  // x of the node after this chunk
+  for (int j = len - 1; j >= 0; --j) {
+    const int k = k0 + j;
+    const Pair<Real> q = tv.dr[k];
+    const Real A = coef<Real, kPre>(tv, k, dt).x * q.x;
+    x = k == top ? A * xp + q.y * q.x : A * x + q.y * q.x;
+    tv.dr[k].y = x;
   }
 }
 
 template <typename Real, bool kPre>
-__device__ __forceinline__ void backsub_list(const TileView<Real>& tv, int c0, int c1, Real dt) {
-  if (c0 >= c1) return;
-  ChainRec ch = load_rec(tv.chains, c1 - 1);
-  for (int c = c1 - 1;; --c) {
-    const bool more = c > c0;
-    ChainRec nx = ch;
-    if (more) nx = load_rec(tv.chains, c - 1);
-    backsub_rec<Real, kPre>(tv, ch, dt);
-    if (!more) break;
-    ch = nx;
+__device__ __forceinline__ void eliminate_phase(const TileView<Real>& tv, int p, int warp, int n_warps, int lane,
+                                                Real dt) {
+  for (int s = tv.phase[p] + warp; s < tv.phase[p + 1]; s += n_warps) {
+    const SlotRec sr = tv.slots[s];
+    if (sr.chunk <= 1)
+      eliminate_lanes<Real, kPre>(tv, sr, lane, dt);
+    else
+      eliminate_chunked<Real, kPre>(tv, sr, lane, dt);
+  }
+}
+
+template <typename Real, bool kPre>
+__device__ __forceinline__ void backsub_phase(const TileView<Real>& tv, int p, int warp, int n_warps, int lane,
+                                              Real dt) {
+  for (int s = tv.phase[p] + warp; s < tv.phase[p + 1]; s += n_warps) {
+    const SlotRec sr = tv.slots[s];
+    if (sr.chunk <= 1)
+      backsub_lanes<Real, kPre>(tv, sr, lane, dt);
+    else
+      backsub_chunked<Real, kPre>(tv, sr, lane, dt);
   }
 }
 
@@ -740,6 +829,7 @@ __global__ void __launch_bounds__(1024) tile_step_kernel(LaunchArgs a) {
   tv.bind(td, base, scratch, a.state);
   const Real dt = Real(a.dt);
   const int T = blockDim.x, tid = threadIdx.x;
+  const int lane = tid & 31, warp = tid >> 5, n_warps = T >> 5;
   const PulseRec* pulses = a.pulses + td.pulse_offset;
   if constexpr (kSmem) {
     // the staged axial coefficients become (alpha dt, beta dt) for this launch
@@ -783,13 +873,13 @@ __global__ void __launch_bounds__(1024) tile_step_kernel(LaunchArgs a) {
     const int64_t step = a.step0 + s;
     // forward elimination, leaves first
     for (int p = 0; p < tv.n_phases; ++p) {
-      eliminate_list<Real, kSmem>(tv, tv.lists[p * (T + 1) + tid], tv.lists[p * (T + 1) + tid + 1], dt);
+      eliminate_phase<Real, kSmem>(tv, p, warp, n_warps, lane, dt);
       __syncthreads();
     }
     BC_TICK(0);
     // back-substitution, root first
     for (int p = tv.n_phases - 1; p >= 0; --p) {
-      backsub_list<Real, kSmem>(tv, tv.lists[p * (T + 1) + tid], tv.lists[p * (T + 1) + tid + 1], dt);
+      backsub_phase<Real, kSmem>(tv, p, warp, n_warps, lane, dt);
       __syncthreads();
     }
     BC_TICK(1);

@@ -1,14 +1,13 @@
 // Planner and C ABI of the GB300 Cell step.
 //
 // bc_plan_create lowers every cell (bc_lower.cpp), decomposes each point tree
-// into chains (maximal single-child paths), assigns chains to threads in
-// barrier-separated phases (chain level = 1 + max level of the chains hanging
-// below its bottom node; longest-processing-time assignment within a phase),
-// packs cells into shared-memory tiles by first-fit-decreasing on node count,
-// lays each tile out as one contiguous 16-byte-aligned blob and uploads it.
-// Small cells can be walked whole by one thread ("thread-per-cell"), larger ones
-// are split into chains over threads ("branch-parallel"); the switch point is
-// bc_plan_options::thread_cell_max.
+// into chains (maximal single-child paths), groups the chains into barrier-
+// separated phases by chain level (1 + the highest level of the chains hanging
+// below a chain's bottom node), packs each phase's chains into 32-lane warp slots
+// (one node per lane; a chain longer than 32 nodes gets a slot of its own with a
+// chunk of nodes per lane), packs cells into shared-memory tiles by best-fit-
+// decreasing on node count, lays each tile out as one contiguous 16-byte-aligned
+// blob and uploads it.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -265,172 +264,123 @@ static bc_status build_tile(const BuildCtx& cx, const TileBuild& tb, int T, Tile
   std::vector<std::pair<int64_t, size_t>> cmap;
   for (size_t i = 0; i < cell_list.size(); ++i) cmap.push_back({cell_list[i], i});
   std::sort(cmap.begin(), cmap.end());
-  // -------- record specs and work items
-  // A record is a regular chain, one segment of a split chain, or the reduced
-  // system of a split chain.  Items are what LPT assigns to threads.
+  // -------- chains -> phases -> warp slots
+  // One record per chain.  The phase of a chain is its chain level (children first).
+  // Inside a phase, chains of at most 32 nodes are packed first-fit-decreasing into
+  // 32-lane warp slots, one node per lane; a longer chain gets a slot of its own in
+  // which every lane takes a contiguous chunk of ceil(L / 32) nodes.
+  struct CRef {
+    int32_t li, chain, L;
+  };
   struct RecSpec {
-    int32_t li, chain, kind, seg, K, lo, hi;  // node range [lo, hi) of the chain's nodes
+    int32_t li, chain, kind, seg, K, lo, hi;
   };
-  struct Item {
-    std::vector<RecSpec> recs;
-    int64_t cost;
-  };
-  std::vector<std::vector<Item>> items;  // indexed by raw phase 2*level (+1 for reduced)
-  auto item_at = [&](int ph) -> std::vector<Item>& {
-    if (int(items.size()) <= ph) items.resize(ph + 1);
-    return items[ph];
-  };
-  for (size_t li = 0; li < cell_list.size(); ++li) {
-    const int64_t c = cell_list[li];
-    const LoweredCell& lc = (*cx.cells)[c];
-    const CellSched& cs = (*cx.sched)[c];
-    if (lc.n_node <= cx.thread_cell_max) {
-      Item it;
-      for (size_t k = 0; k < cs.chains.size(); ++k)
-        it.recs.push_back({int32_t(li), int32_t(k), kChainRegular, 0, 1, 0, int32_t(cs.chains[k].nodes.size())});
-      it.cost = lc.n_node + int64_t(cs.chains.size());
-      item_at(0).push_back(std::move(it));
-      continue;
-    }
-    for (size_t k = 0; k < cs.chains.size(); ++k) {
-      const Chain& ch = cs.chains[k];
-      const int32_t L = int32_t(ch.nodes.size());
-      const int ph = 2 * ch.level;
-      if (cx.split_min > 0 && L > cx.split_min) {
-        int32_t K = int32_t(std::lround(std::sqrt(double(L)) * cx.split_factor));
-        K = std::max<int32_t>(2, std::min<int32_t>(K, L / 2));
-        for (int32_t sgi = 0; sgi < K; ++sgi) {
-          const int32_t lo = int32_t(int64_t(L) * sgi / K), hi = int32_t(int64_t(L) * (sgi + 1) / K);
-          Item it;
-          it.recs.push_back({int32_t(li), int32_t(k), kChainSegment, sgi, K, lo, hi});
-          it.cost = (hi - lo) + 4 + (sgi == 0 ? int64_t(ch.kids.size()) : 0);
-          item_at(ph).push_back(std::move(it));
-        }
-        Item red;
-        red.recs.push_back({int32_t(li), int32_t(k), kChainReduced, 0, K, 0, L});
-        red.cost = 2 * K + 4;
-        item_at(ph + 1).push_back(std::move(red));
-      } else {
-        Item it;
-        it.recs.push_back({int32_t(li), int32_t(k), kChainRegular, 0, 1, 0, L});
-        it.cost = L + int64_t(ch.kids.size()) + 2;
-        item_at(ph).push_back(std::move(it));
-      }
-    }
-  }
-  // drop empty raw phases
-  std::vector<std::vector<Item>> phases;
-  for (auto& v : items)
-    if (!v.empty()) phases.push_back(std::move(v));
-  if (phases.empty()) phases.resize(1);
-  const int n_phases = int(phases.size());
-  // -------- LPT per phase -> per-thread item lists
-  std::vector<std::vector<std::vector<const Item*>>> lists(n_phases, std::vector<std::vector<const Item*>>(T));
-  int64_t crit = 0;
-  for (int p = 0; p < n_phases; ++p) {
-    std::vector<const Item*> v;
-    for (auto& it : phases[p]) v.push_back(&it);
-    std::stable_sort(v.begin(), v.end(), [](const Item* a, const Item* b) { return a->cost > b->cost; });
-    using QE = std::pair<int64_t, int>;
-    std::priority_queue<QE, std::vector<QE>, std::greater<QE>> q;
-    for (int t = 0; t < T; ++t) q.push({0, t});
-    int64_t mx = 0;
-    for (const Item* it : v) {
-      QE e = q.top();
-      q.pop();
-      lists[p][e.second].push_back(it);
-      e.first += it->cost;
-      mx = std::max(mx, e.first);
-      q.push(e);
-    }
-    crit += mx;
-  }
-  out.crit = crit;
-  // -------- records and node order
+  std::vector<std::vector<CRef>> levels;
   int64_t n_real = 0;
   std::vector<std::vector<int32_t>> node_tile(cell_list.size());
-  std::vector<std::vector<int32_t>> handle(cell_list.size());            // chain -> record referenced by parents
-  std::vector<std::vector<std::vector<int32_t>>> seg_rec(cell_list.size());  // chain -> segment records
-  for (size_t i = 0; i < cell_list.size(); ++i) {
-    const LoweredCell& lc = (*cx.cells)[cell_list[i]];
-    const size_t nch = (*cx.sched)[cell_list[i]].chains.size();
-    node_tile[i].assign(lc.n_node, -1);
-    handle[i].assign(nch, -1);
-    seg_rec[i].assign(nch, {});
+  std::vector<std::vector<int32_t>> handle(cell_list.size());  // chain -> record
+  for (size_t li = 0; li < cell_list.size(); ++li) {
+    const LoweredCell& lc = (*cx.cells)[cell_list[li]];
+    const CellSched& cs = (*cx.sched)[cell_list[li]];
+    node_tile[li].assign(lc.n_node, -1);
+    handle[li].assign(cs.chains.size(), -1);
     n_real += lc.n_node;
+    for (size_t k = 0; k < cs.chains.size(); ++k) {
+      const int32_t lv = cs.chains[k].level;
+      if (int(levels.size()) <= lv) levels.resize(lv + 1);
+      levels[lv].push_back({int32_t(li), int32_t(k), int32_t(cs.chains[k].nodes.size())});
+    }
   }
+  std::vector<std::vector<CRef>> phases;
+  for (auto& v : levels)
+    if (!v.empty()) phases.push_back(std::move(v));
+  const int n_phases = int(phases.size());
+  const int W = std::max(1, T / 32);
   std::vector<ChainRec> chains;
   std::vector<RecSpec> rec_src;
-  std::vector<int32_t> list_ptr(size_t(n_phases) * (T + 1));
+  std::vector<SlotRec> slots;
+  std::vector<int32_t> phase_ptr(size_t(n_phases) + 1, 0);
   int32_t next_node = 0;
+  int64_t crit = 0;
   for (int p = 0; p < n_phases; ++p) {
-    for (int t = 0; t < T; ++t) {
-      list_ptr[size_t(p) * (T + 1) + t] = int32_t(chains.size());
-      for (const Item* it : lists[p][t]) {
-        for (const RecSpec& rsp : it->recs) {
-          const Chain& ch = (*cx.sched)[cell_list[rsp.li]].chains[rsp.chain];
-          ChainRec rec{};
-          rec.kind = rsp.kind;
-          rec.slot = -1;
-          rec.start = -1;
-          rec.count = 0;
-          if (rsp.kind != kChainReduced) {
-            rec.start = next_node;
-            rec.count = rsp.hi - rsp.lo;
-            for (int32_t q = rsp.lo; q < rsp.hi; ++q) node_tile[rsp.li][ch.nodes[q]] = next_node++;
-          }
-          const int32_t id = int32_t(chains.size());
-          if (rsp.kind == kChainRegular || rsp.kind == kChainReduced) handle[rsp.li][rsp.chain] = id;
-          if (rsp.kind == kChainSegment) {
-            auto& v = seg_rec[rsp.li][rsp.chain];
-            if (int(v.size()) < rsp.K) v.assign(rsp.K, -1);
-            v[rsp.seg] = id;
-          }
-          chains.push_back(rec);
-          rec_src.push_back(rsp);
+    std::vector<CRef>& v = phases[p];
+    std::stable_sort(v.begin(), v.end(), [](const CRef& a, const CRef& b) { return a.L > b.L; });
+    struct Bin {
+      std::vector<CRef> members;
+      int32_t used = 0, chunk = 1;
+    };
+    std::vector<Bin> bins;
+    for (const CRef& c : v) {
+      if (c.L > 32) {
+        Bin b;
+        b.members.push_back(c);
+        b.used = c.L;
+        b.chunk = (c.L + 31) / 32;
+        bins.push_back(std::move(b));
+        continue;
+      }
+      bool placed = false;
+      for (Bin& b : bins)
+        if (b.chunk == 1 && b.used + c.L <= 32) {
+          b.members.push_back(c);
+          b.used += c.L;
+          placed = true;
+          break;
         }
+      if (!placed) {
+        Bin b;
+        b.members.push_back(c);
+        b.used = c.L;
+        bins.push_back(std::move(b));
       }
     }
-    list_ptr[size_t(p) * (T + 1) + T] = int32_t(chains.size());
+    // longest slots first: warp w takes slots w, w + W, ...
+    std::stable_sort(bins.begin(), bins.end(), [](const Bin& a, const Bin& b) { return a.chunk > b.chunk; });
+    std::vector<int64_t> warp_cost(W, 0);
+    phase_ptr[p] = int32_t(slots.size());
+    for (size_t s = 0; s < bins.size(); ++s) {
+      SlotRec sr{};
+      sr.n_begin = next_node;
+      for (const CRef& c : bins[s].members) {
+        const Chain& ch = (*cx.sched)[cell_list[c.li]].chains[c.chain];
+        ChainRec rec{};
+        rec.start = next_node;
+        rec.count = c.L;
+        rec.kind = kChainRegular;
+        rec.slot = -1;
+        for (int32_t q = 0; q < c.L; ++q) node_tile[c.li][ch.nodes[q]] = next_node++;
+        handle[c.li][c.chain] = int32_t(chains.size());
+        chains.push_back(rec);
+        rec_src.push_back({c.li, c.chain, kChainRegular, 0, 1, 0, c.L});
+      }
+      sr.n_count = int16_t(next_node - sr.n_begin);
+      sr.chunk = int16_t(bins[s].chunk);
+      slots.push_back(sr);
+      warp_cost[s % W] += bins[s].chunk;
+    }
+    crit += *std::max_element(warp_cost.begin(), warp_cost.end());
   }
-  // -------- links: parents, outside nodes, contribution slots
-  // A record that pulls children (regular chain, lowest segment) owns the
-  // consecutive slots aux .. aux + n_child, one per child; each child writes its
-  // contribution into its own slot.  Every segment also owns a slot for (dd, dr, H).
-  std::vector<int32_t> child;
+  phase_ptr[n_phases] = int32_t(slots.size());
+  out.crit = crit;
+  if (chains.size() >= 0xFFFF) return fail(BC_ERR_CAPACITY, "too many chains in one tile");
+  // -------- links: parents and contribution slots
+  // A record owns the consecutive contribution slots aux .. aux + n_child, one per
+  // child chain; each child writes its (cD, cR) into its own slot.
   int32_t n_slots = 0;
-  for (auto& rec : chains) rec.slot = -1;
   for (size_t k = 0; k < chains.size(); ++k) {
     const RecSpec& rsp = rec_src[k];
     const LoweredCell& lc = (*cx.cells)[cell_list[rsp.li]];
     const Chain& ch = (*cx.sched)[cell_list[rsp.li]].chains[rsp.chain];
     const int32_t chain_top_parent = lc.parent[ch.nodes.back()];
-    const int32_t tp = chain_top_parent >= 0 ? node_tile[rsp.li][chain_top_parent] : -1;
     ChainRec& rec = chains[k];
-    rec.n_child = 0;
-    rec.aux = -1;
-    rec.first = 0;
-    if (rsp.kind == kChainRegular || (rsp.kind == kChainSegment && rsp.seg == 0)) {
-      rec.first = 1;
-      rec.aux = n_slots;
-      rec.n_child = int32_t(ch.kids.size());
-      n_slots += rec.n_child;
-    }
-    if (rsp.kind == kChainReduced) {
-      rec.aux = int32_t(child.size());
-      for (int32_t q : seg_rec[rsp.li][rsp.chain]) child.push_back(q);
-      rec.n_child = rsp.K;
-      rec.top_parent = tp;
-    } else if (rsp.kind == kChainSegment) {
-      rec.top_parent = rsp.seg + 1 < rsp.K ? node_tile[rsp.li][ch.nodes[rsp.hi]] : tp;
-      if (rsp.seg > 0) rec.aux = node_tile[rsp.li][ch.nodes[rsp.lo - 1]];
-    } else {
-      rec.top_parent = tp;
-    }
+    rec.top_parent = chain_top_parent >= 0 ? node_tile[rsp.li][chain_top_parent] : -1;
+    rec.first = 1;
+    rec.aux = n_slots;
+    rec.n_child = int32_t(ch.kids.size());
+    n_slots += rec.n_child;
   }
   for (size_t k = 0; k < chains.size(); ++k) {
     const RecSpec& rsp = rec_src[k];
-    if (!chains[k].first) continue;
     const Chain& ch = (*cx.sched)[cell_list[rsp.li]].chains[rsp.chain];
     for (size_t j = 0; j < ch.kids.size(); ++j) {
       const int32_t kid_rec = handle[rsp.li][ch.kids[j]];
@@ -438,10 +388,10 @@ static bc_status build_tile(const BuildCtx& cx, const TileBuild& tb, int T, Tile
       chains[kid_rec].slot = chains[k].aux + int32_t(j);
     }
   }
+  // per-node record index
+  std::vector<uint16_t> crec(size_t(n_real), 0);
   for (size_t k = 0; k < chains.size(); ++k)
-    if (chains[k].kind == kChainSegment) chains[k].slot = n_slots++;
-  for (int32_t v : child)
-    if (v < 0) return fail(BC_ERR_INVALID, "internal: unresolved segment link");
+    for (int32_t q = 0; q < chains[k].count; ++q) crec[size_t(chains[k].start + q)] = uint16_t(k);
   // -------- special nodes: clamp pulses (sorted by node) and probes
   std::vector<std::pair<int32_t, int64_t>> tpulse, tprobe;  // (tile node, pulse / probe id)
   for (size_t li = 0; li < cell_list.size(); ++li) {
@@ -487,10 +437,12 @@ static bc_status build_tile(const BuildCtx& cx, const TileBuild& tb, int T, Tile
   off = align16(off + spec_nodes.size() * sizeof(SpecRec));
   d.off_chains = int32_t(off);
   off = align16(off + chains.size() * sizeof(ChainRec));
-  d.off_child = int32_t(off);
-  off = align16(off + child.size() * 4);
-  d.off_lists = int32_t(off);
-  off = align16(off + list_ptr.size() * 4);
+  d.off_slots = int32_t(off);
+  off = align16(off + slots.size() * sizeof(SlotRec));
+  d.off_phase = int32_t(off);
+  off = align16(off + phase_ptr.size() * 4);
+  d.off_crec = int32_t(off);
+  off = align16(off + N * 2);
   d.off_params = int32_t(off);
   off = align16(off + size_t(n_params) * BC_NPARAM * rs);
   d.off_mech = int32_t(off);
@@ -503,10 +455,6 @@ static bc_status build_tile(const BuildCtx& cx, const TileBuild& tb, int T, Tile
   d.off_scd = int32_t(so);
   so = align16(so + size_t(std::max(n_slots, 1)) * rs);
   d.off_scr = int32_t(so);
-  so = align16(so + size_t(std::max(n_slots, 1)) * rs);
-  d.off_sfill = int32_t(so);
-  so = align16(so + N * rs);
-  d.off_sh = int32_t(so);
   so = align16(so + size_t(std::max(n_slots, 1)) * rs);
   d.n_slots = n_slots;
   d.scratch_bytes = int32_t(so);
@@ -603,8 +551,9 @@ static bc_status build_tile(const BuildCtx& cx, const TileBuild& tb, int T, Tile
     if (!specs.empty()) std::memcpy(b.data() + d.off_specs, specs.data(), specs.size() * sizeof(SpecRec));
   }
   std::memcpy(b.data() + d.off_chains, chains.data(), chains.size() * sizeof(ChainRec));
-  if (!child.empty()) std::memcpy(b.data() + d.off_child, child.data(), child.size() * 4);
-  std::memcpy(b.data() + d.off_lists, list_ptr.data(), list_ptr.size() * 4);
+  if (!slots.empty()) std::memcpy(b.data() + d.off_slots, slots.data(), slots.size() * sizeof(SlotRec));
+  std::memcpy(b.data() + d.off_phase, phase_ptr.data(), phase_ptr.size() * 4);
+  std::memcpy(b.data() + d.off_crec, crec.data(), crec.size() * 2);
   out.desc = d;
   return BC_OK;
 }

@@ -1,5 +1,5 @@
-"""Schedule planning without a GPU (dry-run plans): tiles, phases, chain splitting,
-input validation."""
+"""Schedule planning without a GPU (dry-run plans): tiles, phases, warp slots for
+long chains, input validation."""
 
 import numpy as np
 import pytest
@@ -32,21 +32,23 @@ def test_uneven_sample_plan(native_lib):
     assert np.all(packed[:, 0] <= p.info["tile_nodes"])
 
 
-def test_long_chain_is_split(native_lib):
+def test_long_chain_is_chunked_over_lanes(native_lib):
+    # a 200-CV branch is one chain of ~201 nodes: its warp slot gives each lane a
+    # chunk of ceil(201 / 32) = 7 nodes, so the critical path grows by ~7, not ~200
     d = W.small(1)[0]
+    base = Plan(W.descs_to_batch([d]), dry_run=True).tile_stats()
     d.ncv = [1] + [200] + [8] * (len(d.parent) - 2)
-    b = W.descs_to_batch([d])
-    whole = Plan(b, dry_run=True, split_min=0).tile_stats()
-    split = Plan(b, dry_run=True, split_min=24).tile_stats()
-    assert split[0, 1] > whole[0, 1]          # more chain records
-    assert split[0, 3] < whole[0, 3] / 2       # much shorter critical path
+    st = Plan(W.descs_to_batch([d]), dry_run=True).tile_stats()
+    assert st[0, 0] == base[0, 0] + 192
+    assert st[0, 3] <= base[0, 3] + 7
 
 
-def test_thread_per_cell_for_tiny_cells(native_lib):
-    b = W.descs_to_batch(W.small(8))
-    p = Plan(b, dry_run=True, thread_cell_max=200)
-    st = p.tile_stats()
-    assert np.all(st[:, 2] == 1)  # whole cells walked by one thread: a single phase
+def test_phases_follow_chain_levels(native_lib):
+    # binary tree of depth 3 under a one-CV soma: branch chains at levels 0..2 and
+    # the soma chain on top -> 4 phases, whatever the number of cells in the tile
+    for n in (1, 8):
+        st = Plan(W.descs_to_batch(W.small(n)), dry_run=True).tile_stats()
+        assert np.all(st[:, 2] == 4)
 
 
 def _bad(b: CellBatch, **kw):
