@@ -51,6 +51,7 @@ def _args():
     ap.add_argument("--threads", type=int, default=512)
     ap.add_argument("--threads-big", type=int, default=512)
     ap.add_argument("--steps-per-launch", type=int, default=1000)
+    ap.add_argument("--lane-nodes", type=int, default=1)
     return ap.parse_args()
 
 
@@ -217,7 +218,8 @@ def run_ours(a):
     descs = W.uneven(a.cells, seed=1 + rank)
     batch = W.descs_to_batch(descs)
     plan = Plan(batch, precision="f32", device=local, tile_nodes=a.tile_nodes, threads_per_tile=a.threads,
-                threads_big=a.threads_big, steps_per_launch=a.steps_per_launch, record_every=0)
+                threads_big=a.threads_big, steps_per_launch=a.steps_per_launch, record_every=0,
+                lane_nodes=a.lane_nodes)
     info = plan.info
     n_cv = plan.n_cv
     stream = torch.cuda.current_stream(local)
@@ -292,7 +294,8 @@ def run_ours(a):
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                    "l2": "inputs larger than L2 (tile blobs + state arrays > 129 MB)",
                    "tiles": info["n_tiles"], "threads_per_tile": info["threads_per_tile"],
-                   "tile_nodes": info["tile_nodes"], "steps_per_launch": info["steps_per_launch"]},
+                   "tile_nodes": info["tile_nodes"], "steps_per_launch": info["steps_per_launch"],
+                   "lane_nodes": a.lane_nodes},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d_total), "d2h_bytes_per_step": int(d2h),
                 "path": "bc_state_upload (V) -> bc_run (8,000 steps) -> bc_state_download (V) + bc_spike_download"},
         "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": peak, "unit": "GB/s",

@@ -144,7 +144,7 @@ class PlanOptions(C.Structure):
         ("precision", C.c_int32),
         ("threads_per_tile", C.c_int32),
         ("tile_nodes", C.c_int32),
-        ("thread_cell_max", C.c_int32),
+        ("lane_nodes", C.c_int32),
         ("steps_per_launch", C.c_int32),
         ("record_every", C.c_int32),
         ("max_spikes", C.c_int32),
@@ -152,8 +152,8 @@ class PlanOptions(C.Structure):
         ("device", C.c_int32),
         ("threads_big", C.c_int32),
         ("threads_global", C.c_int32),
-        ("split_min", C.c_int32),
-        ("split_factor", C.c_float),
+        ("reserved_a", C.c_int32),
+        ("reserved_b", C.c_float),
         ("dry_run", C.c_int32),
         ("reserved", C.c_int32 * 2),
     ]

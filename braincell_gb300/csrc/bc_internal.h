@@ -58,13 +58,17 @@ struct ChainRec {
 constexpr int32_t kChainRegular = 0;
 
 // A warp slot of one phase: nodes [n_begin, n_begin + n_count) in lane order.
-// chunk == 1: lane l owns node n_begin + l (several chains side by side);
-// chunk > 1: a single chain, lane l owns the chunk-node range starting at
-// n_begin + l * chunk.
+// Lane l owns the chunk [n_begin + off[l], n_begin + off[l+1]) (the last used
+// lane ends at n_count; idle lanes have off[l] = n_count).  steps = 0: every
+// lane's chunk holds whole chains, walked serially; steps > 0: chains spread
+// over up to 2^steps lanes each, joined by shuffle scans; unit = 1: one node
+// per lane (lane l owns node n_begin + l).
 struct SlotRec {
   int32_t n_begin;
   int16_t n_count;
-  int16_t chunk;
+  uint8_t steps;
+  uint8_t unit;
+  uint16_t off[32];
 };
 
 // Per-tile descriptor (global memory, read-only).

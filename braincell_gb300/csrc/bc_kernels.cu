@@ -400,10 +400,12 @@ __device__ __forceinline__ void add_node_pulses(const TileView<Real>& tv, const 
 // substitution is x_k = (R'_k + a_k x_{k+1}) / D_k.  All three are associative
 // scans along the chain: D through the projective (Moebius) form
 //   [p; q]_{k+1} = [[d_{k+1}, -a_k b_k], [1, 0]] [p; q]_k,  D = p / q,
-// R' and x through affine maps.  A warp slot scans its chains with shuffles,
-// segmented at chain bottoms (forward) or tops (backward).  In a slot whose single
-// chain is longer than 32 nodes each lane first composes its chunk serially, the
-// lanes then scan the chunk maps, and each lane re-walks its chunk from the carry.
+// R' and x through affine maps.  Each phase's chains are packed into 32-lane warp
+// slots.  In a "serial" slot every lane owns whole chains (at most lane_nodes
+// nodes) and walks them one after another.  In a "scan" slot a chain spans
+// several lanes: each lane composes the maps of its chunk, the lanes scan them
+// with shuffles (segmented at chain bottoms going up, at chain tops going down),
+// and each lane re-walks its chunk from the carry of its neighbours.
 
 constexpr unsigned kFullMask = 0xffffffffu;
 
@@ -456,8 +458,18 @@ struct Mob {
   Real m00, m01, m10, m11;  // [[m00, m01], [m10, m11]]
 };
 
-// hi * lo (hi is the later map), rescaled by a power of two: the projective
-// ratio it defines does not change, and the entries stay in range.
+// Rescale by a power of two: the projective ratio a map defines does not change,
+// and the entries stay in range.
+template <typename Real>
+__device__ __forceinline__ void mob_norm(Mob<Real>& r) {
+  const Real s = pow2_inv(rmax(rmax(rabs(r.m00), rabs(r.m01)), rmax(rabs(r.m10), rabs(r.m11))));
+  r.m00 *= s;
+  r.m01 *= s;
+  r.m10 *= s;
+  r.m11 *= s;
+}
+
+// hi * lo (hi is the later map).
 template <typename Real>
 __device__ __forceinline__ Mob<Real> mob_mul(const Mob<Real>& hi, const Mob<Real>& lo) {
   Mob<Real> r;
@@ -465,11 +477,6 @@ __device__ __forceinline__ Mob<Real> mob_mul(const Mob<Real>& hi, const Mob<Real
   r.m01 = hi.m00 * lo.m01 + hi.m01 * lo.m11;
   r.m10 = hi.m10 * lo.m00 + hi.m11 * lo.m10;
   r.m11 = hi.m10 * lo.m01 + hi.m11 * lo.m11;
-  const Real s = pow2_inv(rmax(rmax(rabs(r.m00), rabs(r.m01)), rmax(rabs(r.m10), rabs(r.m11))));
-  r.m00 *= s;
-  r.m01 *= s;
-  r.m10 *= s;
-  r.m11 *= s;
   return r;
 }
 
@@ -483,54 +490,53 @@ __device__ __forceinline__ Mob<Real> mob_shfl_up(const Mob<Real>& m, int off) {
   return o;
 }
 
+// Lane of the segment start at or below `lane` (bit l of `heads` marks a start).
+__device__ __forceinline__ int seg_first(unsigned heads, int lane) {
+  return 31 - __clz(heads & (0xffffffffu >> (31 - lane)));
+}
+// Lane of the segment end at or above `lane` (bit l of `tops` marks an end).
+__device__ __forceinline__ int seg_last(unsigned tops, int lane) {
+  return lane + __ffs(tops >> lane) - 1;
+}
+
 // Inclusive segmented scan of Moebius maps over the lanes (lane order = chain
-// order); a lane with `head` set starts a new segment.
+// order); `reach` = lane - first lane of the segment; 2^steps >= segment lanes.
+// Inputs are normalised maps; a product of four of them stays far inside the
+// FP32 range (each factor changes the scale by at most ~1e6 either way), so the
+// partial products are renormalised after every second step only.
 template <typename Real>
-__device__ __forceinline__ Mob<Real> scan_mob(Mob<Real> m, bool head, int lane) {
-  int f = head ? 1 : 0;
-#pragma unroll
-  for (int off = 1; off < 32; off <<= 1) {
+__device__ __forceinline__ Mob<Real> scan_mob(Mob<Real> m, int reach, int steps) {
+  for (int s = 0, off = 1; s < steps; ++s, off <<= 1) {
     const Mob<Real> o = mob_shfl_up(m, off);
-    const int of = __shfl_up_sync(kFullMask, f, off);
-    if (lane >= off && !f) {
-      m = mob_mul(m, o);
-      f = of;
-    }
+    if (off <= reach) m = mob_mul(m, o);
+    if (s & 1) mob_norm(m);
   }
   return m;
 }
 
 // Inclusive segmented scan of affine maps x -> a x + b, later lanes applied last.
 template <typename Real>
-__device__ __forceinline__ void scan_aff_up(Real& a, Real& b, bool head, int lane) {
-  int f = head ? 1 : 0;
-#pragma unroll
-  for (int off = 1; off < 32; off <<= 1) {
+__device__ __forceinline__ void scan_aff_up(Real& a, Real& b, int reach, int steps) {
+  for (int s = 0, off = 1; s < steps; ++s, off <<= 1) {
     const Real oa = __shfl_up_sync(kFullMask, a, off);
     const Real ob = __shfl_up_sync(kFullMask, b, off);
-    const int of = __shfl_up_sync(kFullMask, f, off);
-    if (lane >= off && !f) {
+    if (off <= reach) {
       b = a * ob + b;
       a = a * oa;
-      f = of;
     }
   }
 }
 
 // The same towards lower lanes (back-substitution runs from chain tops down);
-// a lane with `top` set starts a new segment.
+// `reach` = last lane of the segment - lane.
 template <typename Real>
-__device__ __forceinline__ void scan_aff_down(Real& a, Real& b, bool top, int lane) {
-  int f = top ? 1 : 0;
-#pragma unroll
-  for (int off = 1; off < 32; off <<= 1) {
+__device__ __forceinline__ void scan_aff_down(Real& a, Real& b, int reach, int steps) {
+  for (int s = 0, off = 1; s < steps; ++s, off <<= 1) {
     const Real oa = __shfl_down_sync(kFullMask, a, off);
     const Real ob = __shfl_down_sync(kFullMask, b, off);
-    const int of = __shfl_down_sync(kFullMask, f, off);
-    if (lane + off < 32 && !f) {
+    if (off <= reach) {
       b = a * ob + b;
       a = a * oa;
-      f = of;
     }
   }
 }
@@ -549,13 +555,34 @@ __device__ __forceinline__ Real vdelta(const Pair<Real>& v, const Pair<Real>& up
   return (v.x - up.x) + (v.y - up.y);
 }
 
-// Children's contributions pulled by a chain bottom.
+// Children's contributions pulled by a chain bottom: the first four slots are
+// loaded together (predicated), further ones in a loop.
 template <typename Real>
 __device__ __forceinline__ void pull_children(const TileView<Real>& tv, const ChainRec& ch, Real& D, Real& R) {
-  for (int j = 0; j < ch.n_child; ++j) {
-    D -= tv.scd[ch.aux + j];
-    R += tv.scr[ch.aux + j];
+  const int n = ch.n_child, a0 = ch.aux;
+  Real cd[4], cr[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    cd[j] = j < n ? tv.scd[a0 + j] : Real(0);
+    cr[j] = j < n ? tv.scr[a0 + j] : Real(0);
   }
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    D -= cd[j];
+    R += cr[j];
+  }
+  for (int j = 4; j < n; ++j) {
+    D -= tv.scd[a0 + j];
+    R += tv.scr[a0 + j];
+  }
+}
+
+// Lane chunk of a warp slot: nodes [k0, k0 + len) (len = 0 for an idle lane).
+__device__ __forceinline__ void lane_chunk(const SlotRec& sr, int lane, int& k0, int& len) {
+  const int o0 = sr.off[lane];
+  const int o1 = lane < 31 ? int(sr.off[lane + 1]) : int(sr.n_count);
+  k0 = sr.n_begin + o0;
+  len = o1 - o0;
 }
 
 // Elimination of one warp slot holding one node per lane.
@@ -586,7 +613,9 @@ __device__ __forceinline__ void eliminate_lanes(const TileView<Real>& tv, const 
     m.m00 = q.x;
     m.m01 = -cp.x * cp.y;
   }
-  m = scan_mob(m, head, lane);
+  mob_norm(m);
+  const int reach = lane - seg_first(__ballot_sync(kFullMask, head), lane);
+  m = scan_mob(m, reach, sr.steps);
   const Real inv = m.m10 * pivot_rcp(m.m00);
   const Real w = c.y * inv;
   const Real wp = __shfl_up_sync(kFullMask, w, 1);
@@ -598,7 +627,7 @@ __device__ __forceinline__ void eliminate_lanes(const TileView<Real>& tv, const 
     a = wp;
     b = q.y + cp.y * deltap - c.x * delta;
   }
-  scan_aff_up(a, b, head, lane);
+  scan_aff_up(a, b, reach, sr.steps);
   if (valid) {
     tv.dr[k] = make_pair(inv, b);
     if (tail && ch.slot >= 0) {
@@ -608,19 +637,142 @@ __device__ __forceinline__ void eliminate_lanes(const TileView<Real>& tv, const 
   }
 }
 
-// Elimination of a slot holding one chain longer than 32 nodes, a chunk per lane.
+// Back-substitution of one warp slot holding one node per lane.
 template <typename Real, bool kPre>
-__device__ __forceinline__ void eliminate_chunked(const TileView<Real>& tv, const SlotRec& sr, int lane, Real dt) {
-  const ChainRec ch = load_rec(tv.chains, tv.crec[sr.n_begin]);
-  const int C = sr.chunk;
-  const int k0 = sr.n_begin + lane * C;
-  const int len = max(0, min(C, int(sr.n_count) - lane * C));
+__device__ __forceinline__ void backsub_lanes(const TileView<Real>& tv, const SlotRec& sr, int lane, Real dt) {
+  const bool valid = lane < sr.n_count;
+  const int k = sr.n_begin + (valid ? lane : 0);
+  const ChainRec ch = load_rec(tv.chains, tv.crec[k]);
+  const bool tail = valid && k == ch.start + ch.count - 1;
+  const Pair<Real> q = tv.dr[k];  // (1 / D, R')
+  Real A = coef<Real, kPre>(tv, k, dt).x * q.x, B = q.y * q.x;
+  if (tail) {
+    const Real xp = ch.top_parent >= 0 ? tv.dr[ch.top_parent].y : Real(0);
+    B = A * xp + B;
+    A = Real(0);
+  }
+  const bool top = !valid || tail;
+  scan_aff_down(A, B, seg_last(__ballot_sync(kFullMask, top), lane) - lane, sr.steps);
+  if (valid) tv.dr[k].y = B;
+}
+
+// Serial elimination of one whole chain by one lane.
+template <typename Real, bool kPre>
+__device__ __forceinline__ void eliminate_chain(const TileView<Real>& tv, const ChainRec& ch, Real dt) {
+  const int s0 = ch.start, end = ch.start + ch.count;
+  const Pair<Real> q = tv.dr[s0];
+  Real D = q.x, R = q.y;
+  pull_children(tv, ch, D, R);
+  Pair<Real> c = coef<Real, kPre>(tv, s0, dt), v = tv.v[s0];
+  // node s0 + 1 (or the chain's parent, or -- at the root -- the top node itself)
+  const Pair<Real> v_top = ch.top_parent >= 0 ? tv.v[ch.top_parent] : tv.v[end - 1];
+  Pair<Real> q1 = q, c1 = c, v1 = v_top;
+  if (s0 + 1 < end) {
+    q1 = tv.dr[s0 + 1];
+    c1 = coef<Real, kPre>(tv, s0 + 1, dt);
+    v1 = tv.v[s0 + 1];
+  }
+  for (int i = s0;; ++i) {
+    Pair<Real> q2 = q1, c2 = c1, v2 = v_top;
+    if (i + 2 < end) {
+      q2 = tv.dr[i + 2];
+      c2 = coef<Real, kPre>(tv, i + 2, dt);
+      v2 = tv.v[i + 2];
+    }
+    const Real inv = pivot_rcp(D);
+    const Real delta = vdelta<Real>(v, v1);
+    R -= c.x * delta;
+    tv.dr[i] = make_pair(inv, R);
+    const Real w = c.y * inv;
+    if (i + 1 == end) {
+      if (ch.slot >= 0) {
+        tv.scd[ch.slot] = c.x * w;
+        tv.scr[ch.slot] = w * R + c.y * delta;
+      }
+      break;
+    }
+    D = q1.x - c.x * w;
+    R = q1.y + w * R + c.y * delta;
+    c = c1;
+    v = v1;
+    q1 = q2;
+    c1 = c2;
+    v1 = v2;
+  }
+}
+
+// Serial back-substitution of one whole chain by one lane (top down).
+template <typename Real, bool kPre>
+__device__ __forceinline__ void backsub_chain(const TileView<Real>& tv, const ChainRec& ch, Real dt) {
   const int top = ch.start + ch.count - 1;
-  const bool head = lane == 0;
+  Real dp = ch.top_parent >= 0 ? tv.dr[ch.top_parent].y : Real(0);
+  Pair<Real> q = tv.dr[top];
+  Real al = coef<Real, kPre>(tv, top, dt).x;
+  Pair<Real> q1 = q;
+  Real al1 = al;
+  if (top - 1 >= ch.start) {
+    q1 = tv.dr[top - 1];
+    al1 = coef<Real, kPre>(tv, top - 1, dt).x;
+  }
+  for (int i = top;; --i) {
+    Pair<Real> q2 = q1;
+    Real al2 = al1;
+    if (i - 2 >= ch.start) {
+      q2 = tv.dr[i - 2];
+      al2 = coef<Real, kPre>(tv, i - 2, dt).x;
+    }
+    const Real x = (q.y + al * dp) * q.x;
+    tv.dr[i].y = x;
+    dp = x;
+    if (i == ch.start) break;
+    q = q1;
+    al = al1;
+    q1 = q2;
+    al1 = al2;
+  }
+}
+
+// A slot of whole chains: every lane walks the chains of its chunk one after another.
+template <typename Real, bool kPre>
+__device__ __forceinline__ void eliminate_serial(const TileView<Real>& tv, const SlotRec& sr, int lane, Real dt) {
+  int k, len;
+  lane_chunk(sr, lane, k, len);
+  const int end = k + len;
+  while (k < end) {
+    const ChainRec ch = load_rec(tv.chains, tv.crec[k]);
+    eliminate_chain<Real, kPre>(tv, ch, dt);
+    k += ch.count;
+  }
+}
+
+template <typename Real, bool kPre>
+__device__ __forceinline__ void backsub_serial(const TileView<Real>& tv, const SlotRec& sr, int lane, Real dt) {
+  int k0, len;
+  lane_chunk(sr, lane, k0, len);
+  int k = k0 + len - 1;
+  while (k >= k0) {
+    const ChainRec ch = load_rec(tv.chains, tv.crec[k]);
+    backsub_chain<Real, kPre>(tv, ch, dt);
+    k = ch.start - 1;
+  }
+}
+
+// A slot of chains spread over several lanes each: every lane composes the maps
+// of its chunk, the lanes scan them (segmented per chain), and every lane
+// re-walks its chunk from the carry of the lanes below.
+template <typename Real, bool kPre>
+__device__ __forceinline__ void eliminate_scan(const TileView<Real>& tv, const SlotRec& sr, int lane, Real dt) {
+  int k0, len;
+  lane_chunk(sr, lane, k0, len);
+  ChainRec ch{};
+  if (len > 0) ch = load_rec(tv.chains, tv.crec[k0]);
+  const int top = ch.start + ch.count - 1;
+  const bool head = len > 0 && k0 == ch.start;
   const bool seg = head || len == 0;
+  const int reach = lane - seg_first(__ballot_sync(kFullMask, seg), lane);
   Real D0 = Real(0), R0 = Real(0);
   if (head) {
-    const Pair<Real> q = tv.dr[ch.start];
+    const Pair<Real> q = tv.dr[k0];
     D0 = q.x;
     R0 = q.y;
     pull_children(tv, ch, D0, R0);
@@ -641,10 +793,11 @@ __device__ __forceinline__ void eliminate_chunked(const TileView<Real>& tv, cons
       e.m01 = -cp.x * cp.y;
     }
     m = mob_mul(e, m);
+    mob_norm(m);
   }
-  m = scan_mob(m, seg, lane);
-  Mob<Real> mx = mob_shfl_up(m, 1);
-  // re-walk: pivots of the chunk from the state after the previous lane's chunk
+  m = scan_mob(m, reach, sr.steps);
+  const Mob<Real> mx = mob_shfl_up(m, 1);
+  // re-walk: pivots of the chunk from the state after the lane below
   Real p = mx.m00, pq = mx.m10;
   for (int j = 0; j < len; ++j) {
     const int k = k0 + j;
@@ -684,7 +837,7 @@ __device__ __forceinline__ void eliminate_chunked(const TileView<Real>& tv, cons
     fb = a * fb + b;
     fa = a * fa;
   }
-  scan_aff_up(fa, fb, seg, lane);
+  scan_aff_up(fa, fb, reach, sr.steps);
   Real r = __shfl_up_sync(kFullMask, fb, 1);
   for (int j = 0; j < len; ++j) {
     const int k = k0 + j;
@@ -703,34 +856,17 @@ __device__ __forceinline__ void eliminate_chunked(const TileView<Real>& tv, cons
   }
 }
 
-// Back-substitution of one warp slot holding one node per lane.
 template <typename Real, bool kPre>
-__device__ __forceinline__ void backsub_lanes(const TileView<Real>& tv, const SlotRec& sr, int lane, Real dt) {
-  const bool valid = lane < sr.n_count;
-  const int k = sr.n_begin + (valid ? lane : 0);
-  const ChainRec ch = load_rec(tv.chains, tv.crec[k]);
-  const bool tail = valid && k == ch.start + ch.count - 1;
-  const Pair<Real> q = tv.dr[k];  // (1 / D, R')
-  Real A = coef<Real, kPre>(tv, k, dt).x * q.x, B = q.y * q.x;
-  if (tail) {
-    const Real xp = ch.top_parent >= 0 ? tv.dr[ch.top_parent].y : Real(0);
-    B = A * xp + B;
-    A = Real(0);
-  }
-  scan_aff_down(A, B, !valid || tail, lane);
-  if (valid) tv.dr[k].y = B;
-}
-
-// Back-substitution of a slot holding one long chain, a chunk per lane.
-template <typename Real, bool kPre>
-__device__ __forceinline__ void backsub_chunked(const TileView<Real>& tv, const SlotRec& sr, int lane, Real dt) {
-  const ChainRec ch = load_rec(tv.chains, tv.crec[sr.n_begin]);
-  const int C = sr.chunk;
-  const int k0 = sr.n_begin + lane * C;
-  const int len = max(0, min(C, int(sr.n_count) - lane * C));
+__device__ __forceinline__ void backsub_scan(const TileView<Real>& tv, const SlotRec& sr, int lane, Real dt) {
+  int k0, len;
+  lane_chunk(sr, lane, k0, len);
+  ChainRec ch{};
+  if (len > 0) ch = load_rec(tv.chains, tv.crec[k0]);
   const int top = ch.start + ch.count - 1;
-  const Real xp = ch.top_parent >= 0 ? tv.dr[ch.top_parent].y : Real(0);
   const bool has_top = len > 0 && k0 + len - 1 == top;
+  const bool seg_top = len == 0 || has_top;
+  const int reach = seg_last(__ballot_sync(kFullMask, seg_top), lane) - lane;
+  const Real xp = has_top && ch.top_parent >= 0 ? tv.dr[ch.top_parent].y : Real(0);
   Real fa = Real(1), fb = Real(0);
   for (int j = len - 1; j >= 0; --j) {
     const int k = k0 + j;
@@ -743,7 +879,7 @@ __device__ __forceinline__ void backsub_chunked(const TileView<Real>& tv, const 
     fb = A * fb + B;
     fa = A * fa;
   }
-  scan_aff_down(fa, fb, len == 0 || has_top, lane);
+  scan_aff_down(fa, fb, reach, sr.steps);
   Real x = __shfl_down_sync(kFullMask, fb, 1);  // x of the node after this chunk
   for (int j = len - 1; j >= 0; --j) {
     const int k = k0 + j;
@@ -758,11 +894,13 @@ template <typename Real, bool kPre>
 __device__ __forceinline__ void eliminate_phase(const TileView<Real>& tv, int p, int warp, int n_warps, int lane,
                                                 Real dt) {
   for (int s = tv.phase[p] + warp; s < tv.phase[p + 1]; s += n_warps) {
-    const SlotRec sr = tv.slots[s];
-    if (sr.chunk <= 1)
+    const SlotRec& sr = tv.slots[s];
+    if (sr.steps == 0)
+      eliminate_serial<Real, kPre>(tv, sr, lane, dt);
+    else if (sr.unit)
       eliminate_lanes<Real, kPre>(tv, sr, lane, dt);
     else
-      eliminate_chunked<Real, kPre>(tv, sr, lane, dt);
+      eliminate_scan<Real, kPre>(tv, sr, lane, dt);
   }
 }
 
@@ -770,11 +908,13 @@ template <typename Real, bool kPre>
 __device__ __forceinline__ void backsub_phase(const TileView<Real>& tv, int p, int warp, int n_warps, int lane,
                                               Real dt) {
   for (int s = tv.phase[p] + warp; s < tv.phase[p + 1]; s += n_warps) {
-    const SlotRec sr = tv.slots[s];
-    if (sr.chunk <= 1)
+    const SlotRec& sr = tv.slots[s];
+    if (sr.steps == 0)
+      backsub_serial<Real, kPre>(tv, sr, lane, dt);
+    else if (sr.unit)
       backsub_lanes<Real, kPre>(tv, sr, lane, dt);
     else
-      backsub_chunked<Real, kPre>(tv, sr, lane, dt);
+      backsub_scan<Real, kPre>(tv, sr, lane, dt);
   }
 }
 

@@ -61,7 +61,7 @@ struct bc_plan {
   int threads = 128;
   int threads_global = 512;
   int tile_nodes = 0;
-  int thread_cell_max = 0;
+  int lane_nodes = 1;
   int steps_per_launch = 1000;
   int record_every = 1;
   int max_spikes = 64;
@@ -246,9 +246,7 @@ struct BuildCtx {
   const std::vector<std::vector<int32_t>>* probe_node;
   int precision;
   int state_slots;
-  int thread_cell_max;
-  int split_min;        // chains longer than this are split (0 = never)
-  double split_factor;  // segments = factor * sqrt(length)
+  int lane_nodes;  // nodes a lane walks serially in a warp slot
 };
 
 template <typename Real>
@@ -296,52 +294,97 @@ static bc_status build_tile(const BuildCtx& cx, const TileBuild& tb, int T, Tile
     if (!v.empty()) phases.push_back(std::move(v));
   const int n_phases = int(phases.size());
   const int W = std::max(1, T / 32);
+  const int C = std::max(1, cx.lane_nodes);
   std::vector<ChainRec> chains;
   std::vector<RecSpec> rec_src;
   std::vector<SlotRec> slots;
   std::vector<int32_t> phase_ptr(size_t(n_phases) + 1, 0);
   int32_t next_node = 0;
   int64_t crit = 0;
+  // A lane plan: the chains (whole, or one chain's part) of one lane.
+  struct Lane {
+    std::vector<CRef> whole;  // serial slots: whole chains
+    int32_t nodes = 0;
+  };
+  struct Slot {
+    bool scan = false;
+    std::vector<Lane> lanes;              // serial slots
+    std::vector<CRef> spread;             // scan slots: chains, each over `parts` lanes
+    std::vector<std::vector<int32_t>> parts;  // per spread chain: part sizes
+    int32_t used = 0, steps = 0, cost = 0;
+  };
   for (int p = 0; p < n_phases; ++p) {
     std::vector<CRef>& v = phases[p];
     std::stable_sort(v.begin(), v.end(), [](const CRef& a, const CRef& b) { return a.L > b.L; });
-    struct Bin {
-      std::vector<CRef> members;
-      int32_t used = 0, chunk = 1;
-    };
-    std::vector<Bin> bins;
+    std::vector<Slot> ps;
+    // chains longer than a lane's share: split into near-equal parts over lanes
+    std::vector<Lane> lanes;
     for (const CRef& c : v) {
-      if (c.L > 32) {
-        Bin b;
-        b.members.push_back(c);
-        b.used = c.L;
-        b.chunk = (c.L + 31) / 32;
-        bins.push_back(std::move(b));
+      if (c.L > C) {
+        int32_t m = (c.L + C - 1) / C;
+        int32_t chunk = C;
+        if (m > 32) {
+          chunk = (c.L + 31) / 32;
+          m = (c.L + chunk - 1) / chunk;
+        }
+        std::vector<int32_t> sizes(m);
+        for (int32_t q = 0; q < m; ++q) sizes[q] = int32_t(int64_t(c.L) * (q + 1) / m - int64_t(c.L) * q / m);
+        int32_t st = 0;
+        while ((1 << st) < m) ++st;
+        Slot* tgt = nullptr;
+        for (Slot& s : ps)
+          if (s.scan && s.used + m <= 32) {
+            tgt = &s;
+            break;
+          }
+        if (!tgt) {
+          ps.emplace_back();
+          tgt = &ps.back();
+          tgt->scan = true;
+        }
+        tgt->spread.push_back(c);
+        tgt->parts.push_back(sizes);
+        tgt->used += m;
+        tgt->steps = std::max(tgt->steps, st);
+        tgt->cost = std::max<int32_t>(tgt->cost, 4 * sizes[0] + 8 * st);
         continue;
       }
+      // whole chain: first lane with room (lanes fill to C nodes)
       bool placed = false;
-      for (Bin& b : bins)
-        if (b.chunk == 1 && b.used + c.L <= 32) {
-          b.members.push_back(c);
-          b.used += c.L;
+      for (Lane& ln : lanes)
+        if (ln.nodes + c.L <= C) {
+          ln.whole.push_back(c);
+          ln.nodes += c.L;
           placed = true;
           break;
         }
       if (!placed) {
-        Bin b;
-        b.members.push_back(c);
-        b.used = c.L;
-        bins.push_back(std::move(b));
+        Lane ln;
+        ln.whole.push_back(c);
+        ln.nodes = c.L;
+        lanes.push_back(std::move(ln));
       }
     }
-    // longest slots first: warp w takes slots w, w + W, ...
-    std::stable_sort(bins.begin(), bins.end(), [](const Bin& a, const Bin& b) { return a.chunk > b.chunk; });
+    for (size_t q = 0; q < lanes.size(); q += 32) {
+      Slot s;
+      for (size_t r = q; r < std::min(lanes.size(), q + 32); ++r) {
+        s.cost = std::max<int32_t>(s.cost, 2 * lanes[r].nodes);
+        s.lanes.push_back(std::move(lanes[r]));
+      }
+      s.used = int32_t(s.lanes.size());
+      ps.push_back(std::move(s));
+    }
+    // dearest slots first: warp w takes slots w, w + W, ...
+    std::stable_sort(ps.begin(), ps.end(), [](const Slot& a, const Slot& b) { return a.cost > b.cost; });
     std::vector<int64_t> warp_cost(W, 0);
     phase_ptr[p] = int32_t(slots.size());
-    for (size_t s = 0; s < bins.size(); ++s) {
+    for (size_t si = 0; si < ps.size(); ++si) {
+      const Slot& s = ps[si];
       SlotRec sr{};
       sr.n_begin = next_node;
-      for (const CRef& c : bins[s].members) {
+      sr.steps = uint8_t(s.scan ? std::max(1, s.steps) : 0);
+      int lane = 0;
+      auto emit_chain = [&](const CRef& c) {
         const Chain& ch = (*cx.sched)[cell_list[c.li]].chains[c.chain];
         ChainRec rec{};
         rec.start = next_node;
@@ -352,11 +395,29 @@ static bc_status build_tile(const BuildCtx& cx, const TileBuild& tb, int T, Tile
         handle[c.li][c.chain] = int32_t(chains.size());
         chains.push_back(rec);
         rec_src.push_back({c.li, c.chain, kChainRegular, 0, 1, 0, c.L});
+      };
+      if (s.scan) {
+        for (size_t ci = 0; ci < s.spread.size(); ++ci) {
+          const int32_t base = next_node - sr.n_begin;
+          int32_t o = base;
+          for (int32_t sz : s.parts[ci]) {
+            sr.off[lane++] = uint16_t(o);
+            o += sz;
+          }
+          emit_chain(s.spread[ci]);
+        }
+      } else {
+        for (const Lane& ln : s.lanes) {
+          sr.off[lane++] = uint16_t(next_node - sr.n_begin);
+          for (const CRef& c : ln.whole) emit_chain(c);
+        }
       }
+      if (next_node - sr.n_begin > 0x7fff) return fail(BC_ERR_CAPACITY, "a warp slot holds more than 32767 nodes");
       sr.n_count = int16_t(next_node - sr.n_begin);
-      sr.chunk = int16_t(bins[s].chunk);
+      sr.unit = uint8_t(s.scan && sr.n_count == lane ? 1 : 0);
+      for (; lane < 32; ++lane) sr.off[lane] = uint16_t(sr.n_count);
       slots.push_back(sr);
-      warp_cost[s % W] += bins[s].chunk;
+      warp_cost[si % W] += s.cost;
     }
     crit += *std::max_element(warp_cost.begin(), warp_cost.end());
   }
@@ -688,14 +749,12 @@ void bc_default_options(bc_plan_options* o) {
   o->precision = BC_PREC_F32;
   o->threads_per_tile = 0;
   o->tile_nodes = 0;
-  o->thread_cell_max = 48;
+  o->lane_nodes = 1;
   o->steps_per_launch = 0;
   o->record_every = 1;
   o->max_spikes = 64;
   o->use_graph = 0;
   o->device = 0;
-  o->split_min = 24;
-  o->split_factor = 1.0f;
 }
 
 bc_status bc_plan_create(const bc_batch_spec* spec, const bc_plan_options* opts_in, bc_plan_t* out) {
@@ -727,7 +786,7 @@ bc_status bc_plan_create(const bc_batch_spec* spec, const bc_plan_options* opts_
   p->max_spikes = opts.max_spikes;
   p->use_graph = opts.use_graph;
   p->steps_per_launch = opts.steps_per_launch > 0 ? opts.steps_per_launch : 1000;
-  p->thread_cell_max = opts.thread_cell_max;
+  p->lane_nodes = opts.lane_nodes > 0 ? opts.lane_nodes : 1;
   p->n_cells = s.n_cells;
   // ---------------------------------------------------- lower
   std::vector<LoweredCell> cells(s.n_cells);
@@ -858,7 +917,7 @@ bc_status bc_plan_create(const bc_batch_spec* spec, const bc_plan_options* opts_
     if (tile_nodes - nn > 0) room.emplace(tile_nodes - nn, builds.size() - 1);
   }
   BuildCtx cx{&s, &cells, &sched, &cv_base, &cell_pulses, &cell_probes, &pulse_node, &probe_node,
-              p->precision, S, p->thread_cell_max, opts.split_min, opts.split_factor > 0 ? opts.split_factor : 1.0};
+              p->precision, S, p->lane_nodes};
   std::vector<TileOut> outs;
   outs.reserve(builds.size());
   // Packed tiles: tile_nodes sets how many CTAs share an SM (by the per-node

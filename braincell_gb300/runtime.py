@@ -40,7 +40,7 @@ class Plan:
         precision: str = "f32",
         threads_per_tile: int = 0,
         tile_nodes: int = 0,
-        thread_cell_max: int = 48,
+        lane_nodes: int = 0,
         steps_per_launch: int = 0,
         record_every: int = 1,
         max_spikes: int = 64,
@@ -48,8 +48,6 @@ class Plan:
         device: int = 0,
         threads_big: int = 0,
         threads_global: int = 0,
-        split_min: int = 24,
-        split_factor: float = 1.0,
         dry_run: bool = False,
     ) -> None:
         if precision not in _PREC:
@@ -63,7 +61,7 @@ class Plan:
         opts.precision = _PREC[precision]
         opts.threads_per_tile = int(threads_per_tile)
         opts.tile_nodes = int(tile_nodes)
-        opts.thread_cell_max = int(thread_cell_max)
+        opts.lane_nodes = int(lane_nodes)
         opts.steps_per_launch = int(steps_per_launch)
         opts.record_every = int(record_every)
         opts.max_spikes = int(max_spikes)
@@ -71,8 +69,6 @@ class Plan:
         opts.device = self.device
         opts.threads_big = int(threads_big)
         opts.threads_global = int(threads_global)
-        opts.split_min = int(split_min)
-        opts.split_factor = float(split_factor)
         opts.dry_run = int(bool(dry_run))
         spec, keep = batch.to_spec()
         handle = C.c_void_p()

@@ -143,8 +143,9 @@ typedef struct bc_plan_options {
   int32_t precision;        /* BC_PREC_*                                             */
   int32_t threads_per_tile; /* CTA size (multiple of 32, <= 1024); 0 = auto          */
   int32_t tile_nodes;       /* node budget per tile (shared-memory size); 0 = auto   */
-  int32_t thread_cell_max;  /* cells with <= this many nodes are walked by one thread;
-                               larger cells are split into chains over threads       */
+  int32_t lane_nodes;       /* nodes a lane walks serially inside a warp slot; longer
+                               chains are spread over lanes joined by shuffle scans;
+                               0 = auto (1)                                          */
   int32_t steps_per_launch; /* time steps fused per kernel launch; 0 = auto          */
   int32_t record_every;     /* probe sampling period in steps (>= 1)                 */
   int32_t max_spikes;       /* spike times kept per probe                            */
@@ -153,9 +154,8 @@ typedef struct bc_plan_options {
   int32_t threads_big;      /* CTA size for tiles holding one cell larger than
                                tile_nodes; 0 = auto                                   */
   int32_t threads_global;   /* CTA size for global-memory tiles; 0 = auto            */
-  int32_t split_min;        /* unbranched chains longer than this many nodes are split
-                               into segments eliminated in parallel (0 = never)        */
-  float split_factor;       /* segments per split chain = split_factor * sqrt(length) */
+  int32_t reserved_a;       /* must be 0                                             */
+  float reserved_b;         /* must be 0                                             */
   int32_t dry_run;          /* 1: lower and schedule only (no CUDA calls); the plan
                                answers bc_plan_info / bc_plan_tile_stats only         */
   int32_t reserved[2];

@@ -61,7 +61,7 @@ def test_version_and_defaults(native_lib):
     assert native_lib.bc_version() >= 100
     o = _abi.PlanOptions()
     native_lib.bc_default_options(C.byref(o))
-    assert o.precision == _abi.BC_PREC_F32 and o.record_every == 1 and o.split_min > 0
+    assert o.precision == _abi.BC_PREC_F32 and o.record_every == 1 and o.lane_nodes > 0
 
 
 def test_invalid_spec_is_rejected_on_host(native_lib):

@@ -124,12 +124,14 @@ def test_calcium_ahp_cat_pulses_f32():
     np.testing.assert_allclose(ci[m], oc.Ci[0, oc.cv_mid][m], rtol=1e-4)
 
 
-def test_split_and_unsplit_chains_agree_f64():
+def test_serial_and_scan_slots_agree_f64():
+    # lane_nodes=1000: every chain walked serially by one lane; lane_nodes=1: every
+    # chain of more than one node spread over lanes and joined by shuffle scans
     d = W._small_desc(3)
     d.ncv = [1, 150, 90] + [8] * (len(d.parent) - 3)
     d.pulses = [(0, 0.5, 1.0, 30.0, 0.5), (1, 0.3, 2.0, 10.0, 0.2)]
-    a = _gpu([d], 400, "f64", split_min=0)
-    b = _gpu([d], 400, "f64", split_min=12)
+    a = _gpu([d], 400, "f64", lane_nodes=1000)
+    b = _gpu([d], 400, "f64", lane_nodes=1)
     np.testing.assert_allclose(a[3], b[3], rtol=0, atol=1e-10)
     oc, otr, _ = _oracle(d, 400)
     assert np.abs(otr - b[1][0]).max() <= TOL_F64_MV

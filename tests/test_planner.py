@@ -34,13 +34,15 @@ def test_uneven_sample_plan(native_lib):
 
 def test_long_chain_is_chunked_over_lanes(native_lib):
     # a 200-CV branch is one chain of ~201 nodes: its warp slot gives each lane a
-    # chunk of ceil(201 / 32) = 7 nodes, so the critical path grows by ~7, not ~200
+    # chunk of ceil(201 / 32) = 7 nodes joined by a 5-step scan, so the critical
+    # path (cost units: 4 per serial node, 8 per scan step) grows by far less than
+    # a serial walk of the chain would add (4 * 201)
     d = W.small(1)[0]
     base = Plan(W.descs_to_batch([d]), dry_run=True).tile_stats()
     d.ncv = [1] + [200] + [8] * (len(d.parent) - 2)
     st = Plan(W.descs_to_batch([d]), dry_run=True).tile_stats()
     assert st[0, 0] == base[0, 0] + 192
-    assert st[0, 3] <= base[0, 3] + 7
+    assert st[0, 3] - base[0, 3] <= 4 * 7 + 8 * 5
 
 
 def test_phases_follow_chain_levels(native_lib):
