@@ -154,7 +154,7 @@ struct TileView {
 // Reciprocal of a Hines pivot.  FP32: the hardware approximation (about 1 ulp;
 // pivots are >= 1 on membrane rows and O(dt * g / C) on boundary rows, far from
 // the denormal range); FP64: IEEE round-to-nearest.
-__device__ __forceinline__ float pivot_rcp(float d) { return __fdividef(1.0f, d); }
+__device__ __forceinline__ float pivot_rcp(float d) { return rcp_approx(d); }
 __device__ __forceinline__ double pivot_rcp(double d) { return __drcp_rn(d); }
 
 // float-float accumulation: (hi, lo) += d

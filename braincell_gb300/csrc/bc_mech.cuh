@@ -28,14 +28,19 @@ __device__ __forceinline__ float dlog(float x) { return logf(x); }
 __device__ __forceinline__ double dlog(double x) { return log(x); }
 __device__ __forceinline__ float dpow(float x, float y) { return powf(x, y); }
 __device__ __forceinline__ double dpow(double x, double y) { return pow(x, y); }
-// Rate-function arithmetic: FP32 uses the hardware approximations (__expf,
-// __fdividef: a few ulp, far below what the rates need); FP64 stays exact so the
-// FP64 build remains an oracle-grade run of the same kernels.
+// Rate-function arithmetic: FP32 uses the hardware approximations (__expf, and
+// a * rcp.approx(b) for a / b: a few ulp, far below what the rates need); FP64
+// stays exact so the FP64 build remains an oracle-grade run of the same kernels.
 __device__ __forceinline__ float rexp(float x) { return __expf(x); }
 __device__ __forceinline__ float aexp(float x) { return expf(x); }
 __device__ __forceinline__ double aexp(double x) { return exp(x); }
 __device__ __forceinline__ double rexp(double x) { return exp(x); }
-__device__ __forceinline__ float rdiv(float a, float b) { return __fdividef(a, b); }
+__device__ __forceinline__ float rcp_approx(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+__device__ __forceinline__ float rdiv(float a, float b) { return a * rcp_approx(b); }
 __device__ __forceinline__ double rdiv(double a, double b) { return a / b; }
 
 // e^x - 1 for the exp-Euler decay of a gate (x = dt * lambda <= 0).  FP32: for
