@@ -110,6 +110,40 @@ class CellBatch:
     def cell_nbranch(self) -> np.ndarray:
         return np.diff(self.cell_branch_offsets)
 
+    def select(self, cells) -> "CellBatch":
+        """The batch of the given cells (in the given order), with their clamps and probes."""
+        cells = np.asarray(cells, dtype=np.int64)
+        if cells.ndim != 1 or np.any(cells < 0) or np.any(cells >= self.n_cells):
+            raise ValueError("cells must be a 1-D array of cell indices of this batch.")
+        R = self.n_regions
+        b0, b1 = self.cell_branch_offsets[cells], self.cell_branch_offsets[cells + 1]
+        br = np.concatenate([np.arange(a, b) for a, b in zip(b0, b1)]) if cells.size else np.zeros(0, np.int64)
+        s0, s1 = self.branch_seg_offsets[br], self.branch_seg_offsets[br + 1]
+        seg = np.concatenate([np.arange(a, b) for a, b in zip(s0, s1)]) if br.size else np.zeros(0, np.int64)
+        rg = (cells[:, None] * R + np.arange(R)[None, :]).reshape(-1)
+        new_id = np.full(self.n_cells, -1, np.int64)
+        new_id[cells] = np.arange(cells.size)
+        pk = new_id[self.pulse_cell] >= 0 if self.pulse_cell.size else np.zeros(0, bool)
+        qk = new_id[self.probe_cell] >= 0 if self.probe_cell.size else np.zeros(0, bool)
+        pord = np.argsort(new_id[self.pulse_cell[pk]], kind="stable")
+        qord = np.argsort(new_id[self.probe_cell[qk]], kind="stable")
+        return CellBatch(
+            n_regions=R,
+            cell_branch_offsets=np.concatenate([[0], np.cumsum(b1 - b0)]),
+            branch_parent=self.branch_parent[br], branch_parent_x=self.branch_parent_x[br],
+            branch_child_x=self.branch_child_x[br], branch_ncv=self.branch_ncv[br],
+            branch_region=self.branch_region[br],
+            branch_seg_offsets=np.concatenate([[0], np.cumsum(s1 - s0)]),
+            seg_length=self.seg_length[seg], seg_r_prox=self.seg_r_prox[seg], seg_r_dist=self.seg_r_dist[seg],
+            region_cm=self.region_cm[rg], region_ra=self.region_ra[rg], region_mech=self.region_mech[rg],
+            region_params=self.region_params[rg],
+            pulse_cell=new_id[self.pulse_cell[pk]][pord], pulse_branch=self.pulse_branch[pk][pord],
+            pulse_x=self.pulse_x[pk][pord], pulse_t_on=self.pulse_t_on[pk][pord],
+            pulse_t_off=self.pulse_t_off[pk][pord], pulse_amp=self.pulse_amp[pk][pord],
+            probe_cell=new_id[self.probe_cell[qk]][qord], probe_branch=self.probe_branch[qk][qord],
+            probe_x=self.probe_x[qk][qord],
+        )
+
     def validate(self) -> None:
         nb = self.n_branches
         if self.cell_branch_offsets[0] != 0 or self.cell_branch_offsets[-1] != nb:

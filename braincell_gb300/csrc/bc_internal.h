@@ -2,6 +2,8 @@
 // the device code (bc_kernels.cu).  Not part of the public ABI.
 #pragma once
 
+#include <cuda_runtime.h>
+
 #include <cstddef>
 #include <cstdint>
 #include <string>
@@ -145,6 +147,11 @@ struct LaunchArgs {
 
 // Host-callable launchers implemented in bc_kernels.cu.
 int launch_tiles(const LaunchArgs& a, int precision, bool smem, int threads, size_t smem_bytes, void* stream);
+// Kernel-node parameters of the same launch for a CUDA graph.  kernelParams
+// points at *hold, which points at *a: both must stay valid until the graph
+// call that consumes the parameters returns (it copies the argument).
+int tile_node_params(const LaunchArgs* a, int precision, bool smem, int threads, size_t smem_bytes,
+                     cudaKernelNodeParams* np, const LaunchArgs** hold);
 int launch_reset_impl(const LaunchArgs& a, int precision, int threads, const double* vinit, const int64_t* voff,
                       void* stream);
 // View offsets: byte offsets into the blob, or kStateTag + byte offset into the state array.

@@ -1163,6 +1163,36 @@ int launch_tiles(const LaunchArgs& a, int precision, bool smem, int threads, siz
               : launch_impl<float, false>(a, threads, smem_bytes, st);
 }
 
+// Kernel-node parameters of one tile launch for a CUDA graph: the same kernel,
+// grid, block and shared memory as launch_tiles; `*a` is copied by the graph call
+// that consumes the parameters.
+template <typename Real, bool kSmem>
+static int node_impl(const LaunchArgs* a, int threads, size_t smem_bytes, cudaKernelNodeParams* np) {
+  auto k = tile_step_kernel<Real, kSmem>;
+  if (kSmem) {
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem_bytes));
+    if (e != cudaSuccess) return int(e);
+  }
+  np->func = reinterpret_cast<void*>(k);
+  np->gridDim = dim3(a->n_tiles, 1, 1);
+  np->blockDim = dim3(threads, 1, 1);
+  np->sharedMemBytes = kSmem ? unsigned(smem_bytes) : 0u;
+  np->extra = nullptr;
+  return 0;
+}
+
+int tile_node_params(const LaunchArgs* a, int precision, bool smem, int threads, size_t smem_bytes,
+                     cudaKernelNodeParams* np, const LaunchArgs** hold) {
+  *hold = a;
+  int e;
+  if (precision == BC_PREC_F64)
+    e = smem ? node_impl<double, true>(a, threads, smem_bytes, np) : node_impl<double, false>(a, threads, smem_bytes, np);
+  else
+    e = smem ? node_impl<float, true>(a, threads, smem_bytes, np) : node_impl<float, false>(a, threads, smem_bytes, np);
+  np->kernelParams = reinterpret_cast<void**>(const_cast<LaunchArgs**>(hold));
+  return e;
+}
+
 int launch_reset_impl(const LaunchArgs& a, int precision, int threads, const double* vinit, const int64_t* voff,
                       void* stream) {
   cudaStream_t st = static_cast<cudaStream_t>(stream);

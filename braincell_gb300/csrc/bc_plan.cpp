@@ -104,6 +104,13 @@ struct bc_plan {
   unsigned long long* d_timers = nullptr;
   std::vector<std::array<int64_t, 6>> tile_stats;
   cudaEvent_t ev_fork = nullptr, ev_join[2] = {nullptr, nullptr};
+  // CUDA graph of one run (use_graph): per launch class a chain of kernel nodes,
+  // rebuilt when the launch pattern changes, otherwise only re-parameterised.
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t graph_exec = nullptr;
+  std::vector<cudaGraphNode_t> graph_nodes;  // [launch][class]
+  int64_t graph_launches = -1;
+  int32_t graph_k = -1, graph_k_last = -1;
 };
 
 namespace bc {
@@ -136,6 +143,8 @@ static void free_plan(bc_plan* p) {
     if (p->ev_join[k]) cudaEventDestroy(p->ev_join[k]);
   }
   if (p->ev_fork) cudaEventDestroy(p->ev_fork);
+  if (p->graph_exec) cudaGraphExecDestroy(p->graph_exec);
+  if (p->graph) cudaGraphDestroy(p->graph);
   delete p;
 }
 
@@ -692,6 +701,68 @@ static LaunchArgs base_args(bc_plan* p) {
   return a;
 }
 
+// The launches of one run as a CUDA graph: each launch class is a chain of
+// kernel nodes (the classes hold independent cells, so the chains run side by
+// side).  The graph is built when the number of launches or their step counts
+// change; otherwise only the kernel arguments (first step, trace buffer, ...)
+// of its nodes are updated before the replay.
+static bc_status enqueue_run_graph(bc_plan* p, int64_t n_steps, double dt, void* stream) {
+  const int32_t K = p->steps_per_launch;
+  const int64_t L = (n_steps + K - 1) / K;
+  const int32_t k_last = int32_t(n_steps - (L - 1) * K);
+  const int nc = int(p->classes.size());
+  std::vector<LaunchArgs> args(size_t(L) * nc);
+  for (int64_t j = 0; j < L; ++j)
+    for (int ci = 0; ci < nc; ++ci) {
+      LaunchArgs a = base_args(p);
+      a.step0 = p->step + j * K;
+      a.n_steps = j + 1 == L ? k_last : K;
+      a.dt = dt;
+      a.tiles = p->d_tiles + p->classes[ci].first;
+      a.n_tiles = p->classes[ci].count;
+      args[size_t(j) * nc + ci] = a;
+    }
+  const bool rebuild = !p->graph_exec || p->graph_launches != L || p->graph_k != K || p->graph_k_last != k_last;
+  if (rebuild) {
+    if (p->graph_exec) cudaGraphExecDestroy(p->graph_exec);
+    if (p->graph) cudaGraphDestroy(p->graph);
+    p->graph_exec = nullptr;
+    p->graph = nullptr;
+    p->graph_launches = -1;
+    BC_CUDA(cudaGraphCreate(&p->graph, 0));
+    p->graph_nodes.assign(size_t(L) * nc, nullptr);
+    for (int64_t j = 0; j < L; ++j)
+      for (int ci = 0; ci < nc; ++ci) {
+        const LaunchClass& lcz = p->classes[ci];
+        cudaKernelNodeParams np{};
+        const LaunchArgs* hold = nullptr;
+        int e = tile_node_params(&args[size_t(j) * nc + ci], p->precision, lcz.smem, lcz.threads, lcz.smem_bytes, &np,
+                                 &hold);
+        if (e) return fail(BC_ERR_CUDA, std::string("graph node: ") + cudaGetErrorString(cudaError_t(e)));
+        cudaGraphNode_t dep = j > 0 ? p->graph_nodes[size_t(j - 1) * nc + ci] : nullptr;
+        BC_CUDA(cudaGraphAddKernelNode(&p->graph_nodes[size_t(j) * nc + ci], p->graph, dep ? &dep : nullptr,
+                                       dep ? 1 : 0, &np));
+      }
+    BC_CUDA(cudaGraphInstantiate(&p->graph_exec, p->graph, 0));
+    p->graph_launches = L;
+    p->graph_k = K;
+    p->graph_k_last = k_last;
+  } else {
+    for (int64_t j = 0; j < L; ++j)
+      for (int ci = 0; ci < nc; ++ci) {
+        const LaunchClass& lcz = p->classes[ci];
+        cudaKernelNodeParams np{};
+        const LaunchArgs* hold = nullptr;
+        int e = tile_node_params(&args[size_t(j) * nc + ci], p->precision, lcz.smem, lcz.threads, lcz.smem_bytes, &np,
+                                 &hold);
+        if (e) return fail(BC_ERR_CUDA, std::string("graph node: ") + cudaGetErrorString(cudaError_t(e)));
+        BC_CUDA(cudaGraphExecKernelNodeSetParams(p->graph_exec, p->graph_nodes[size_t(j) * nc + ci], &np));
+      }
+  }
+  BC_CUDA(cudaGraphLaunch(p->graph_exec, static_cast<cudaStream_t>(stream)));
+  return BC_OK;
+}
+
 static bc_status enqueue_run(bc_plan* p, int64_t n_steps, double dt, void* stream) {
   if (n_steps < 0) return fail(BC_ERR_INVALID, "n_steps must be >= 0");
   if (!(dt > 0.0) || !std::isfinite(dt)) return fail(BC_ERR_INVALID, "dt must be a positive finite number (ms)");
@@ -700,6 +771,11 @@ static bc_status enqueue_run(bc_plan* p, int64_t n_steps, double dt, void* strea
   const int64_t recs = p->record_every > 0 ? (p->step + n_steps - p->trace_origin) / p->record_every : 0;
   st = ensure_traces(p, recs, stream);
   if (st != BC_OK) return st;
+  if (p->use_graph && n_steps > 0) {
+    st = enqueue_run_graph(p, n_steps, dt, stream);
+    if (st == BC_OK) p->step += n_steps;
+    return st;
+  }
   int64_t done = 0;
   while (done < n_steps) {
     const int32_t k = int32_t(std::min<int64_t>(p->steps_per_launch, n_steps - done));

@@ -149,7 +149,10 @@ typedef struct bc_plan_options {
   int32_t steps_per_launch; /* time steps fused per kernel launch; 0 = auto          */
   int32_t record_every;     /* probe sampling period in steps (>= 1)                 */
   int32_t max_spikes;       /* spike times kept per probe                            */
-  int32_t use_graph;        /* capture multi-launch runs in a CUDA graph             */
+  int32_t use_graph;        /* 1: each bc_run replays a CUDA graph of its launches
+                               (one kernel-node chain per launch class), built when
+                               the launch pattern changes and otherwise only
+                               re-parameterised; results are bit-identical        */
   int32_t device;           /* CUDA device ordinal                                   */
   int32_t threads_big;      /* CTA size for tiles holding one cell larger than
                                tile_nodes; 0 = auto                                   */

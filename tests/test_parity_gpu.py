@@ -221,3 +221,30 @@ def test_probe_record_every_and_clear():
     full = Plan(W.descs_to_batch(W.small(2)), precision="f64", record_every=1)
     full.run(115, DT)
     np.testing.assert_allclose(full.traces()[:, 104], p.traces()[:, 0], atol=0)
+
+
+def test_cuda_graph_runs_match_stream_runs():
+    # graph rebuilds (new launch patterns) and re-parameterised replays (same pattern,
+    # new first step) must give bit-identical states, traces and spikes
+    descs = W.uneven(indices=[5, 6]) + W.small(2)
+    outs = []
+    for use_graph in (False, True):
+        p = Plan(W.descs_to_batch(descs), precision="f32", use_graph=use_graph, steps_per_launch=50, record_every=10)
+        for n in (120, 120, 37, 1, 1, 200):
+            p.run(n, DT)
+        outs.append((p.state("V"), p.state("CaL_p"), p.traces(), p.spike_counts()))
+        p.close()
+    for a, b in zip(outs[0], outs[1]):
+        np.testing.assert_array_equal(a, b)
+
+
+def test_autotune_returns_working_options():
+    from braincell_gb300 import tune
+
+    b = W.descs_to_batch(W.uneven(60))
+    r = tune.autotune(b, steps=20, max_cells=60, tile_threads=((2500, 512), (1500, 256)), lane_nodes=(1,),
+                      steps_per_launch=(1000,))
+    assert r.rate > 0 and len(r.trials) == 2
+    p = Plan(b, **r.options)
+    p.run(10, DT)
+    assert np.isfinite(p.state("V")).all()
