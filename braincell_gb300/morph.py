@@ -38,6 +38,7 @@ class Branch:
     radii_proximal: np.ndarray
     radii_distal: np.ndarray
     type: str = "custom"
+    points: np.ndarray | None = None  # [n_segments + 1, 3] um, when built from points
 
     @classmethod
     def from_lengths(
@@ -89,6 +90,26 @@ class Branch:
                         D.append(rp[i + 1])
                 lengths_a, rp, rd = np.asarray(L), np.asarray(P), np.asarray(D)
         return cls(lengths=lengths_a, radii_proximal=rp, radii_distal=rd, type=type)
+
+    @classmethod
+    def from_points(cls, *, points: Sequence[Sequence[float]], radii: Sequence[float],
+                    type: str = "custom") -> "Branch":
+        """Branch through ordered 3-D points (um) with a radius at every point.
+
+        Follows ``morph/branch.py:287`` (``Branch.from_points``): segment lengths
+        are the distances between consecutive points; a repeated point with a
+        different radius is a zero-length segment (a radius jump).
+        """
+        pts = np.asarray(points, dtype=np.float64)
+        r = np.asarray(radii, dtype=np.float64)
+        if pts.ndim != 2 or pts.shape[1] != 3 or pts.shape[0] < 2:
+            raise ValueError("points must have shape (n_points >= 2, 3).")
+        if r.shape != (pts.shape[0],):
+            raise ValueError("radii must give one radius per point.")
+        lengths = np.linalg.norm(np.diff(pts, axis=0), axis=1)
+        b = cls.from_lengths(lengths=lengths, radii=r, type=type)
+        return cls(lengths=b.lengths, radii_proximal=b.radii_proximal, radii_distal=b.radii_distal, type=type,
+                   points=pts)
 
     @property
     def length(self) -> float:

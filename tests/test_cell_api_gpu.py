@@ -90,3 +90,28 @@ def test_cell_declaration_errors():
         cell.update()
     with pytest.raises(ValueError):
         Cell(Morphology.from_root(soma), solver="no_such_solver")
+
+
+def _swc_cell(precision):
+    from braincell_gb300.mech import AllRegion, CableProperty, Channel, branch_in
+    from braincell_gb300.swc import read_swc
+
+    m = read_swc(os.path.join(os.path.dirname(__file__), "golden", "pyramid_small.swc"))
+    cell = Cell(m, cv_policy=CVPerBranch(), pop_size=1, precision=precision)
+    cell.paint(AllRegion(), CableProperty(), Channel("IL", g_max=0.3, E=-70.0))
+    cell.paint(branch_in("type", "soma"), Channel("Na_Ba2002", g_max=120.0), Channel("KDR_Ba2002", g_max=36.0))
+    cell.paint(branch_in("type", ("basal_dendrite", "apical_dendrite")), Channel("CaL_IS2008", g_max=2.0))
+    cell.place(RootLocation(0.5), CurrentClamp(delay=1.0, durations=8.0, amplitudes=0.3))
+    cell.place(RootLocation(0.5), StateProbe())
+    return cell
+
+
+def test_swc_morphology_matches_oracle():
+    # a cell read from SWC (3-point soma, basal and apical trees, axon) through the
+    # Cell front end: FP64 GPU run vs the float64 oracle
+    cell = _swc_cell("f64")
+    res = cell.run(dt=0.025, duration=10.0)
+    tr = res.traces["probe_0"][0]
+    oc = OracleCell(_swc_cell("f64"))
+    otr, _ = oc.run(0.025, 400)
+    np.testing.assert_allclose(tr, otr[0, 0], atol=1e-8)
