@@ -136,6 +136,17 @@ class BatchSpec(C.Structure):
         ("probe_cell", _p(C.c_int32)),
         ("probe_branch", _p(C.c_int32)),
         ("probe_x", _p(C.c_double)),
+        ("n_synapses", C.c_int64),
+        ("syn_cell", _p(C.c_int32)),
+        ("syn_branch", _p(C.c_int32)),
+        ("syn_x", _p(C.c_double)),
+        ("syn_tau", _p(C.c_double)),
+        ("syn_e", _p(C.c_double)),
+        ("n_connections", C.c_int64),
+        ("conn_pre", _p(C.c_int32)),
+        ("conn_post", _p(C.c_int64)),
+        ("conn_weight", _p(C.c_double)),
+        ("conn_delay", _p(C.c_double)),
     ]
 
 
@@ -205,6 +216,8 @@ SIGNATURES = {
     "bc_state_download": (C.c_int32, [C.c_void_p, C.c_int32, _p(C.c_double), C.c_void_p]),
     "bc_state_upload": (C.c_int32, [C.c_void_p, C.c_int32, _p(C.c_double), C.c_void_p]),
     "bc_state_download_noalloc": (C.c_int32, [C.c_void_p, C.c_int32, _p(C.c_double), C.c_void_p]),
+    "bc_network_spikes": (C.c_int32, [C.c_void_p, _p(C.c_int32), _p(C.c_int64), C.c_int64, _p(C.c_int64), C.c_void_p]),
+    "bc_synapse_download": (C.c_int32, [C.c_void_p, _p(C.c_double), C.c_void_p]),
     "bc_probe_count": (C.c_int32, [C.c_void_p, _p(C.c_int64)]),
     "bc_probe_download": (C.c_int32, [C.c_void_p, _p(C.c_double), C.c_int64, C.c_void_p]),
     "bc_spike_download": (C.c_int32, [C.c_void_p, _p(C.c_int32), _p(C.c_double), C.c_void_p]),

@@ -22,7 +22,7 @@ import numpy as np
 
 from . import _abi
 from .catalogue import region_record
-from .mech import CableProperty, CurrentClamp, StateProbe
+from .mech import CableProperty, CurrentClamp, ExpSyn, StateProbe
 
 __all__ = ["CellBatch", "lower_cell", "concat_batches", "native_lowering"]
 
@@ -57,6 +57,15 @@ class CellBatch:
     probe_cell: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
     probe_branch: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
     probe_x: np.ndarray = field(default_factory=lambda: np.zeros(0, np.float64))
+    syn_cell: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
+    syn_branch: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
+    syn_x: np.ndarray = field(default_factory=lambda: np.zeros(0, np.float64))
+    syn_tau: np.ndarray = field(default_factory=lambda: np.zeros(0, np.float64))
+    syn_e: np.ndarray = field(default_factory=lambda: np.zeros(0, np.float64))
+    conn_pre: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
+    conn_post: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int64))
+    conn_weight: np.ndarray = field(default_factory=lambda: np.zeros(0, np.float64))
+    conn_delay: np.ndarray = field(default_factory=lambda: np.zeros(0, np.float64))
 
     _DTYPES = {
         "cell_branch_offsets": np.int64,
@@ -82,6 +91,15 @@ class CellBatch:
         "probe_cell": np.int32,
         "probe_branch": np.int32,
         "probe_x": np.float64,
+        "syn_cell": np.int32,
+        "syn_branch": np.int32,
+        "syn_x": np.float64,
+        "syn_tau": np.float64,
+        "syn_e": np.float64,
+        "conn_pre": np.int32,
+        "conn_post": np.int64,
+        "conn_weight": np.float64,
+        "conn_delay": np.float64,
     }
 
     def __post_init__(self) -> None:
@@ -127,6 +145,12 @@ class CellBatch:
         qk = new_id[self.probe_cell] >= 0 if self.probe_cell.size else np.zeros(0, bool)
         pord = np.argsort(new_id[self.pulse_cell[pk]], kind="stable")
         qord = np.argsort(new_id[self.probe_cell[qk]], kind="stable")
+        sk = new_id[self.syn_cell] >= 0 if self.syn_cell.size else np.zeros(0, bool)
+        sord = np.argsort(new_id[self.syn_cell[sk]], kind="stable")
+        syn_old = np.nonzero(sk)[0][sord]
+        new_syn = np.full(self.syn_cell.size, -1, np.int64)
+        new_syn[syn_old] = np.arange(syn_old.size)
+        ck = (new_id[self.conn_pre] >= 0) & (new_syn[self.conn_post] >= 0) if self.conn_pre.size else np.zeros(0, bool)
         return CellBatch(
             n_regions=R,
             cell_branch_offsets=np.concatenate([[0], np.cumsum(b1 - b0)]),
@@ -142,6 +166,10 @@ class CellBatch:
             pulse_t_off=self.pulse_t_off[pk][pord], pulse_amp=self.pulse_amp[pk][pord],
             probe_cell=new_id[self.probe_cell[qk]][qord], probe_branch=self.probe_branch[qk][qord],
             probe_x=self.probe_x[qk][qord],
+            syn_cell=new_id[self.syn_cell[syn_old]], syn_branch=self.syn_branch[syn_old], syn_x=self.syn_x[syn_old],
+            syn_tau=self.syn_tau[syn_old], syn_e=self.syn_e[syn_old],
+            conn_pre=new_id[self.conn_pre[ck]], conn_post=new_syn[self.conn_post[ck]],
+            conn_weight=self.conn_weight[ck], conn_delay=self.conn_delay[ck],
         )
 
     def validate(self) -> None:
@@ -154,6 +182,12 @@ class CellBatch:
             raise ValueError("branch_ncv must be >= 1.")
         if self.region_params.shape != (self.n_cells * self.n_regions, _abi.BC_NPARAM):
             raise ValueError("region_params has the wrong shape.")
+        ns = self.syn_cell.size
+        if any(getattr(self, k).size != ns for k in ("syn_branch", "syn_x", "syn_tau", "syn_e")):
+            raise ValueError("synapse arrays must all have n_synapses entries.")
+        nc = self.conn_pre.size
+        if any(getattr(self, k).size != nc for k in ("conn_post", "conn_weight", "conn_delay")):
+            raise ValueError("connection arrays must all have n_connections entries.")
 
     # ------------------------------------------------------------------ ABI
     def to_spec(self) -> tuple[_abi.BatchSpec, tuple]:
@@ -172,6 +206,8 @@ class CellBatch:
             setattr(s, name, _ptr(arr, ctypes_of[dt]))
         s.n_pulses = int(self.pulse_cell.size)
         s.n_probes = int(self.probe_cell.size)
+        s.n_synapses = int(self.syn_cell.size)
+        s.n_connections = int(self.conn_pre.size)
         return s, tuple(keep)
 
 
@@ -205,6 +241,7 @@ def concat_batches(batches: list[CellBatch]) -> CellBatch:
     br_off = 0
     seg_off = 0
     cell_off = 0
+    syn_off = 0
     for b in batches:
         parts["cell_branch_offsets"].append(b.cell_branch_offsets[(1 if br_off or cell_off else 0):] + br_off)
         parts["branch_seg_offsets"].append(b.branch_seg_offsets[(1 if seg_off or cell_off else 0):] + seg_off)
@@ -224,8 +261,13 @@ def concat_batches(batches: list[CellBatch]) -> CellBatch:
         parts["region_params"].append(a.reshape(-1, _abi.BC_NPARAM))
         parts["pulse_cell"].append(b.pulse_cell + cell_off)
         parts["probe_cell"].append(b.probe_cell + cell_off)
-        for k in ("pulse_branch", "pulse_x", "pulse_t_on", "pulse_t_off", "pulse_amp", "probe_branch", "probe_x"):
+        parts["syn_cell"].append(b.syn_cell + cell_off)
+        parts["conn_pre"].append(b.conn_pre + cell_off)
+        parts["conn_post"].append(b.conn_post + syn_off)
+        for k in ("pulse_branch", "pulse_x", "pulse_t_on", "pulse_t_off", "pulse_amp", "probe_branch", "probe_x",
+                  "syn_branch", "syn_x", "syn_tau", "syn_e", "conn_weight", "conn_delay"):
             parts[k].append(getattr(b, k))
+        syn_off += int(b.syn_cell.size)
         br_off += b.n_branches
         seg_off += int(b.seg_length.size)
         cell_off += nc
@@ -291,6 +333,7 @@ def lower_cell(cell, replicas: int | None = None) -> CellBatch:
             params[r, _abi.BC_P_VREST] = float(cell.V_init)
     pulses: list[tuple[int, float, float, float, float]] = []
     probes: list[tuple[int, float]] = []
+    syns: list[tuple[int, float, float, float]] = []
     for locset, decls in cell.place_rules:
         for (b, x) in locset.points(morpho):
             for d in decls:
@@ -299,6 +342,8 @@ def lower_cell(cell, replicas: int | None = None) -> CellBatch:
                         pulses.append((b, x, t_on, t_off, amp))
                 elif isinstance(d, StateProbe):
                     probes.append((b, x))
+                elif isinstance(d, ExpSyn):
+                    syns.append((b, x, d.tau, d.e))
                 else:
                     raise TypeError(f"Unsupported point mechanism {type(d).__name__}.")
     one = CellBatch(
@@ -326,6 +371,11 @@ def lower_cell(cell, replicas: int | None = None) -> CellBatch:
         probe_cell=np.zeros(len(probes), np.int32),
         probe_branch=np.asarray([p[0] for p in probes], np.int32),
         probe_x=np.asarray([p[1] for p in probes]),
+        syn_cell=np.zeros(len(syns), np.int32),
+        syn_branch=np.asarray([q[0] for q in syns], np.int32),
+        syn_x=np.asarray([q[1] for q in syns]),
+        syn_tau=np.asarray([q[2] for q in syns]),
+        syn_e=np.asarray([q[3] for q in syns]),
     )
     if P == 1:
         return one

@@ -99,7 +99,11 @@ struct TileDesc {
   int32_t off_dr;           // (diagonal, rhs) pairs, inside the scratch area
   int32_t off_scd, off_scr;  // contribution slots, inside the scratch area
   int32_t n_slots;          // contribution slots (scd / scr / sh entries)
-  int32_t pad1;
+  int32_t n_cells;          // cells in the tile
+  // network: tile synapse list (global ids), per-node tile-local cell index and
+  // per-cell global id of spike sources (-1: not a source); off_ncell = -1 when
+  // the tile has no spike source.  off_stamp: per-cell spike step (scratch).
+  int32_t off_syn, off_ncell, off_srccell, off_stamp;
   int64_t scratch_offset;   // bytes into the plan's global scratch (global-resident tiles)
 };
 
@@ -112,13 +116,17 @@ struct PulseRec {
   double t_on, t_off;
 };
 
-// A node with clamp pulses and/or a probe: its pulses are pulse_begin .. pulse_end
-// of the tile's pulse list (sorted by node), its probe id is `probe` (-1: none).
+// A node with clamp pulses, a probe and/or synapses: its pulses are
+// pulse_begin .. pulse_end of the tile's pulse list (sorted by node), its probe id
+// is `probe` (-1: none), its synapses are entries syn_begin .. syn_end of the
+// tile's synapse list (global synapse ids).
 struct SpecRec {
   int32_t pulse_begin;
   int32_t pulse_end;
   int32_t probe;
-  int32_t pad;
+  int32_t syn_begin;
+  int32_t syn_end;
+  int32_t pad[3];
 };
 
 // Kernel launch parameters (by value).
@@ -143,6 +151,18 @@ struct LaunchArgs {
   int32_t state_slots;
   double dt;
   unsigned long long* timers;  // [4] cycle sums (elimination, back-sub, update, other); phase-timer builds only
+  // synapses (Real arrays indexed by global synapse id) and network delivery
+  void* syn_g;                 // conductance, uS
+  const void* syn_tau;         // ms
+  const void* syn_e;           // mV
+  const void* syn_scale;       // 1e5 / CV area: uS -> mS/cm^2
+  void* arrivals;              // [arr_slots][n_syn] event weights due per step (null: no network)
+  int64_t arr_slots;
+  int64_t n_syn;
+  int32_t* rec_cell;           // spike records (source cell, step)
+  int64_t* rec_step;
+  unsigned long long* rec_count;
+  int64_t rec_cap;
 };
 
 // Host-callable launchers implemented in bc_kernels.cu.
@@ -158,6 +178,12 @@ int launch_reset_impl(const LaunchArgs& a, int precision, int threads, const dou
 constexpr int64_t kStateTag = int64_t(1) << 62;
 int launch_view_impl(unsigned char* blob, unsigned char* state, int precision, const int64_t* off_hi,
                      const int64_t* off_lo, double* view, int64_t n, bool write, void* stream);
+// Event delivery after a launch: every spike record in [*rec_done, *rec_count)
+// adds the weights of its source cell's connections into the arrival ring.
+int launch_deliver_impl(int precision, const int32_t* rec_cell, const int64_t* rec_step,
+                        const unsigned long long* rec_count, const unsigned long long* rec_done, int64_t rec_cap,
+                        const int64_t* out_ptr, const int64_t* out_syn, const void* out_w, const int32_t* out_d,
+                        void* arrivals, int64_t arr_slots, int64_t n_syn, void* stream);
 // Device address (on the current device) of the fixed scratch behind
 // bc_state_download_noalloc: [hi offsets | lo offsets | values], BC_NOALLOC_MAX_CV
 // 8-byte entries each.  Returns the cudaError_t of cudaGetSymbolAddress.

@@ -34,6 +34,7 @@ namespace bc {
 
 constexpr int kStatusNonfinite = 1;
 constexpr int kStatusTimeout = 2;
+constexpr int kStatusRecordOverflow = 4;
 constexpr uint16_t kBoundary = 0xFFFF;
 constexpr uint16_t kNoSpecial = 0xFFFF;
 
@@ -126,7 +127,12 @@ struct TileView {
   const SpecRec* specs;
   const uint32_t* mech;
   Real *scd, *scr;
-  int N, n_real, n_phases;
+  const int32_t* syn;       // tile synapse list (global synapse ids)
+  const uint16_t* ncell;    // per node: tile-local cell (spike-source tiles only)
+  const int32_t* srccell;   // per tile cell: global id of a spike source, -1 otherwise
+  int32_t* stamp;           // per tile cell: last step with a crossing
+  int N, n_real, n_phases, n_cells;
+  bool has_src;
 
   __device__ __forceinline__ void bind(const TileDesc& td, unsigned char* base, unsigned char* scratch, void* gstate) {
     v = reinterpret_cast<Pair<Real>*>(base + td.off_v);
@@ -145,6 +151,12 @@ struct TileView {
     mech = reinterpret_cast<const uint32_t*>(base + td.off_mech);
     scd = reinterpret_cast<Real*>(scratch + td.off_scd);
     scr = reinterpret_cast<Real*>(scratch + td.off_scr);
+    syn = reinterpret_cast<const int32_t*>(base + td.off_syn);
+    has_src = td.off_ncell >= 0;
+    ncell = has_src ? reinterpret_cast<const uint16_t*>(base + td.off_ncell) : nullptr;
+    srccell = has_src ? reinterpret_cast<const int32_t*>(base + td.off_srccell) : nullptr;
+    stamp = has_src ? reinterpret_cast<int32_t*>(scratch + td.off_stamp) : nullptr;
+    n_cells = td.n_cells;
     N = td.n_nodes;
     n_real = td.n_real_nodes;
     n_phases = td.n_phases;
@@ -371,6 +383,39 @@ __device__ __forceinline__ void write_row(const TileView<Real>& tv, int i, uint1
   } else {
     const Real invcm = tv.params[size_t(pr) * BC_NPARAM + BC_P_INVCM];
     tv.dr[i] = make_pair(Real(1) + dt * (tv.diag0[i] + invcm * G), dt * invcm * I);
+  }
+}
+
+// ExpSyn synapses of a node (synapse/markov.py:65-117).  `g` is stored as the
+// conductance at the start of a step including that step's events.  advance:
+// one dt of decay (exp-Euler of g' = -g / tau, exact); then, unless `last`, the
+// events due at `next_step` are added (their ring slot is cleared) and the
+// synapse current g (e - V) at v (a total current spread over the CV) is added
+// to the node's conductance G and current I for the next row.
+template <typename Real>
+__device__ __forceinline__ void node_synapses(const LaunchArgs& a, const TileView<Real>& tv, const SpecRec& sr,
+                                              Real v, Real dt, bool advance, bool last, int64_t next_step, Real& G,
+                                              Real& I) {
+  Real* g_all = static_cast<Real*>(a.syn_g);
+  const Real* tau = static_cast<const Real*>(a.syn_tau);
+  const Real* e = static_cast<const Real*>(a.syn_e);
+  const Real* scale = static_cast<const Real*>(a.syn_scale);
+  Real* arr = static_cast<Real*>(a.arrivals);
+  for (int k = sr.syn_begin; k < sr.syn_end; ++k) {
+    const int32_t id = tv.syn[k];
+    Real g = g_all[id];
+    if (advance) g += decay_em1(-dt / tau[id]) * g;
+    if (!last) {
+      if (arr) {
+        Real* slot = arr + (next_step % a.arr_slots) * a.n_syn + id;
+        g += *slot;
+        *slot = Real(0);
+      }
+      const Real gd = g * scale[id];
+      G += gd;
+      I += gd * (e[id] - v);
+    }
+    g_all[id] = g;
   }
 }
 
@@ -989,10 +1034,16 @@ __global__ void __launch_bounds__(1024) tile_step_kernel(LaunchArgs a) {
       const Real v = tv.v[i].x;
       node_mechanisms(tv.state + i, tv.N, tv.params + size_t(pr) * BC_NPARAM, tv.mech[pr], v, v, dt, false, G, I);
     }
-    write_row(tv, i, pr, dt, G, I);
     const uint16_t sp = tv.spec[i];
+    if (sp != kNoSpecial) {
+      const SpecRec sr = tv.specs[sp];
+      if (sr.syn_begin < sr.syn_end) node_synapses(a, tv, sr, tv.v[i].x, dt, false, false, a.step0, G, I);
+    }
+    write_row(tv, i, pr, dt, G, I);
     if (sp != kNoSpecial) add_node_pulses(tv, pulses, tv.specs[sp], i, pr, a.step0, dt);
   }
+  if (tv.has_src)
+    for (int c = tid; c < tv.n_cells; c += T) tv.stamp[c] = -1;
   __syncthreads();
 
 #ifdef BC_PHASE_TIMERS
@@ -1055,10 +1106,20 @@ __global__ void __launch_bounds__(1024) tile_step_kernel(LaunchArgs a) {
                                true, G, I);
       cur = nxt;
       pr_cur = pr_nxt;
-      if (!last) write_row(tv, i, pr, dt, G, I);
       const uint16_t sp = tv.spec[i];
+      SpecRec sr;
       if (sp != kNoSpecial) {
-        const SpecRec sr = tv.specs[sp];
+        sr = tv.specs[sp];
+        if (sr.syn_begin < sr.syn_end) node_synapses(a, tv, sr, hi, dt, true, last, step + 1, G, I);
+      }
+      if (!last) write_row(tv, i, pr, dt, G, I);
+      if (tv.has_src && pr != kBoundary) {
+        // a spike of the cell: any of its CVs crossing 0 mV upward in this step
+        const uint16_t lc = tv.ncell[i];
+        if (lc != 0xFFFF && Real(v_old + lo_old) < Real(0) && Real(hi + lo) >= Real(0))
+          tv.stamp[lc] = int32_t(step & 0x7fffffff);
+      }
+      if (sp != kNoSpecial) {
         if (sr.probe >= 0) {
           const double v1 = double(hi) + double(lo), v0 = double(v_old) + double(lo_old);
           if (v0 < 0.0 && v1 >= 0.0) {
@@ -1076,6 +1137,17 @@ __global__ void __launch_bounds__(1024) tile_step_kernel(LaunchArgs a) {
       }
     }
     __syncthreads();
+    if (tv.has_src)
+      for (int c = tid; c < tv.n_cells; c += T)
+        if (tv.stamp[c] == int32_t(step & 0x7fffffff) && tv.srccell[c] >= 0) {
+          const unsigned long long r = atomicAdd(a.rec_count, 1ull);
+          if (int64_t(r) < a.rec_cap) {
+            a.rec_cell[r] = tv.srccell[c];
+            a.rec_step[r] = step;
+          } else {
+            s_status = kStatusRecordOverflow;
+          }
+        }
     BC_TICK(2);
   }
 #ifdef BC_PHASE_TIMERS
@@ -1191,6 +1263,44 @@ int tile_node_params(const LaunchArgs* a, int precision, bool smem, int threads,
     e = smem ? node_impl<float, true>(a, threads, smem_bytes, np) : node_impl<float, false>(a, threads, smem_bytes, np);
   np->kernelParams = reinterpret_cast<void**>(const_cast<LaunchArgs**>(hold));
   return e;
+}
+
+// Event delivery (network/delivery.py:361-394): each spike record (cell, step)
+// of the last launch adds, for every connection of its cell, the weight into the
+// ring slot of the arrival step step + max(delay, 1).  Several records can hit one
+// slot: the additions are atomic, so their order (and the last bits of a sum of
+// three or more weights) may vary between runs.
+template <typename Real>
+__global__ void deliver_kernel(const int32_t* rec_cell, const int64_t* rec_step, const unsigned long long* rec_count,
+                               const unsigned long long* rec_done, int64_t rec_cap, const int64_t* out_ptr,
+                               const int64_t* out_syn, const Real* out_w, const int32_t* out_d, Real* arrivals,
+                               int64_t arr_slots, int64_t n_syn) {
+  const int64_t r0 = int64_t(*rec_done);
+  const int64_t r1 = min(int64_t(*rec_count), rec_cap);
+  for (int64_t r = r0 + blockIdx.x * int64_t(blockDim.x) + threadIdx.x; r < r1; r += int64_t(gridDim.x) * blockDim.x) {
+    const int32_t c = rec_cell[r];
+    const int64_t s = rec_step[r];
+    for (int64_t j = out_ptr[c]; j < out_ptr[c + 1]; ++j) {
+      const int64_t arrive = s + max(out_d[j], 1);
+      atomicAdd(arrivals + (arrive % arr_slots) * n_syn + out_syn[j], out_w[j]);
+    }
+  }
+}
+
+int launch_deliver_impl(int precision, const int32_t* rec_cell, const int64_t* rec_step,
+                        const unsigned long long* rec_count, const unsigned long long* rec_done, int64_t rec_cap,
+                        const int64_t* out_ptr, const int64_t* out_syn, const void* out_w, const int32_t* out_d,
+                        void* arrivals, int64_t arr_slots, int64_t n_syn, void* stream) {
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (precision == BC_PREC_F64)
+    deliver_kernel<double><<<152, 256, 0, st>>>(rec_cell, rec_step, rec_count, rec_done, rec_cap, out_ptr, out_syn,
+                                                static_cast<const double*>(out_w), out_d,
+                                                static_cast<double*>(arrivals), arr_slots, n_syn);
+  else
+    deliver_kernel<float><<<152, 256, 0, st>>>(rec_cell, rec_step, rec_count, rec_done, rec_cap, out_ptr, out_syn,
+                                               static_cast<const float*>(out_w), out_d, static_cast<float*>(arrivals),
+                                               arr_slots, n_syn);
+  return int(cudaGetLastError());
 }
 
 int launch_reset_impl(const LaunchArgs& a, int precision, int threads, const double* vinit, const int64_t* voff,

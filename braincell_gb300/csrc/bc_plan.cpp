@@ -79,6 +79,26 @@ struct bc_plan {
   std::vector<bc::PulseRec> pulses;
   double pulses_dt = -1.0;
   std::vector<double> probe_vrest;
+  // synapses and connections (host copies; device mirrors below)
+  int64_t n_synapses = 0, n_connections = 0;
+  std::vector<double> syn_tau, syn_e, syn_scale, conn_delay;
+  std::vector<int64_t> out_ptr, out_syn, out_order;  // CSR of connections by presynaptic cell
+  std::vector<double> out_w;
+  void* d_syn_g = nullptr;
+  void* d_syn_tau = nullptr;
+  void* d_syn_e = nullptr;
+  void* d_syn_scale = nullptr;
+  int64_t* d_out_ptr = nullptr;
+  int64_t* d_out_syn = nullptr;
+  void* d_out_w = nullptr;
+  int32_t* d_out_d = nullptr;
+  void* d_arrivals = nullptr;
+  int64_t arr_slots = 0, net_k = 0;
+  double net_dt = 0.0;  // dt the delays were quantised for (0: not yet)
+  int32_t* d_rec_cell = nullptr;
+  int64_t* d_rec_step = nullptr;
+  unsigned long long* d_rec_count = nullptr;  // [0] produced, [1] delivered
+  int64_t rec_cap = 0;
   // device buffers
   unsigned char* d_blob = nullptr;
   size_t blob_bytes = 0;
@@ -138,6 +158,18 @@ static void free_plan(bc_plan* p) {
   cudaFree(p->d_spike_times);
   cudaFree(p->d_status);
   cudaFree(p->d_timers);
+  cudaFree(p->d_syn_g);
+  cudaFree(p->d_syn_tau);
+  cudaFree(p->d_syn_e);
+  cudaFree(p->d_syn_scale);
+  cudaFree(p->d_out_ptr);
+  cudaFree(p->d_out_syn);
+  cudaFree(p->d_out_w);
+  cudaFree(p->d_out_d);
+  cudaFree(p->d_arrivals);
+  cudaFree(p->d_rec_cell);
+  cudaFree(p->d_rec_step);
+  cudaFree(p->d_rec_count);
   for (int k = 0; k < 2; ++k) {
     if (p->aux[k]) cudaStreamDestroy(p->aux[k]);
     if (p->ev_join[k]) cudaEventDestroy(p->ev_join[k]);
@@ -253,6 +285,8 @@ struct BuildCtx {
   const std::vector<std::vector<int64_t>>* cell_probes;
   const std::vector<std::vector<int32_t>>* pulse_node;  // per cell, node per pulse (parallel to cell_pulses)
   const std::vector<std::vector<int32_t>>* probe_node;
+  const std::vector<std::vector<std::pair<int64_t, int32_t>>>* cell_syns;  // per cell: (synapse id, node)
+  const std::vector<char>* is_src;                                        // per cell: source of a connection
   int precision;
   int state_slots;
   int lane_nodes;  // nodes a lane walks serially in a warp slot
@@ -473,6 +507,15 @@ static bc_status build_tile(const BuildCtx& cx, const TileBuild& tb, int T, Tile
     const auto& qn = (*cx.probe_node)[c];
     for (size_t k = 0; k < ql.size(); ++k) tprobe.push_back({node_tile[li][qn[k]], ql[k]});
   }
+  std::vector<std::pair<int32_t, int64_t>> tsyn;  // (tile node, synapse id)
+  bool has_src = false;
+  for (size_t li = 0; li < cell_list.size(); ++li) {
+    const int64_t c = cell_list[li];
+    for (const auto& sv : (*cx.cell_syns)[c]) tsyn.push_back({node_tile[li][sv.second], sv.first});
+    has_src = has_src || (*cx.is_src)[c];
+  }
+  std::stable_sort(tsyn.begin(), tsyn.end(),
+                   [](const std::pair<int32_t, int64_t>& x, const std::pair<int32_t, int64_t>& y) { return x.first < y.first; });
   std::stable_sort(tpulse.begin(), tpulse.end(),
                    [](const std::pair<int32_t, int64_t>& x, const std::pair<int32_t, int64_t>& y) { return x.first < y.first; });
   std::sort(tprobe.begin(), tprobe.end());
@@ -482,9 +525,11 @@ static bc_status build_tile(const BuildCtx& cx, const TileBuild& tb, int T, Tile
   std::vector<int32_t> spec_nodes;
   for (auto& x : tpulse) spec_nodes.push_back(x.first);
   for (auto& x : tprobe) spec_nodes.push_back(x.first);
+  for (auto& x : tsyn) spec_nodes.push_back(x.first);
   std::sort(spec_nodes.begin(), spec_nodes.end());
   spec_nodes.erase(std::unique(spec_nodes.begin(), spec_nodes.end()), spec_nodes.end());
-  if (spec_nodes.size() >= 0xFFFF) return fail(BC_ERR_CAPACITY, "too many clamped / probed points in one tile");
+  if (spec_nodes.size() >= 0xFFFF) return fail(BC_ERR_CAPACITY, "too many clamped / probed / synapse points in one tile");
+  if (cell_list.size() >= 0xFFFF) return fail(BC_ERR_CAPACITY, "too many cells in one tile");
   // -------- layout
   const int64_t N = (n_real + 3) & ~int64_t(3);
   const int S = cx.state_slots;
@@ -517,6 +562,17 @@ static bc_status build_tile(const BuildCtx& cx, const TileBuild& tb, int T, Tile
   off = align16(off + size_t(n_params) * BC_NPARAM * rs);
   d.off_mech = int32_t(off);
   off = align16(off + size_t(n_params) * 4);
+  d.off_syn = int32_t(off);
+  off = align16(off + tsyn.size() * 4);
+  d.n_cells = int32_t(cell_list.size());
+  d.off_ncell = -1;
+  d.off_srccell = -1;
+  if (has_src) {
+    d.off_ncell = int32_t(off);
+    off = align16(off + size_t(N) * 2);
+    d.off_srccell = int32_t(off);
+    off = align16(off + cell_list.size() * 4);
+  }
   if (off > size_t(0x7fffffff)) return fail(BC_ERR_CAPACITY, "tile blob exceeds 2 GiB");
   d.blob_bytes = int32_t(off);
   size_t so = 0;
@@ -527,6 +583,11 @@ static bc_status build_tile(const BuildCtx& cx, const TileBuild& tb, int T, Tile
   d.off_scr = int32_t(so);
   so = align16(so + size_t(std::max(n_slots, 1)) * rs);
   d.n_slots = n_slots;
+  d.off_stamp = -1;
+  if (has_src) {
+    d.off_stamp = int32_t(so);
+    so = align16(so + cell_list.size() * 4);
+  }
   d.scratch_bytes = int32_t(so);
   d.n_nodes = int32_t(N);
   d.n_real_nodes = int32_t(n_real);
@@ -584,7 +645,7 @@ static bc_status build_tile(const BuildCtx& cx, const TileBuild& tb, int T, Tile
     }
     for (size_t q = 0; q < spec_nodes.size(); ++q) {
       spec[spec_nodes[q]] = uint16_t(q);
-      specs[q] = SpecRec{0, 0, -1, 0};
+      specs[q] = SpecRec{0, 0, -1, 0, 0, {0, 0, 0}};
     }
     size_t kp = 0;
     for (size_t q = 0; q < spec_nodes.size(); ++q) {
@@ -615,6 +676,24 @@ static bc_status build_tile(const BuildCtx& cx, const TileBuild& tb, int T, Tile
         ++kp;
       }
       specs[q].pulse_end = int32_t(out.pulses.size());
+    }
+    size_t ks = 0;
+    for (size_t q = 0; q < spec_nodes.size(); ++q) {
+      specs[q].syn_begin = int32_t(ks);
+      while (ks < tsyn.size() && tsyn[ks].first == spec_nodes[q]) ++ks;
+      specs[q].syn_end = int32_t(ks);
+    }
+    std::vector<int32_t> syn_ids(tsyn.size());
+    for (size_t k = 0; k < tsyn.size(); ++k) syn_ids[k] = int32_t(tsyn[k].second);
+    if (!syn_ids.empty()) std::memcpy(b.data() + d.off_syn, syn_ids.data(), syn_ids.size() * 4);
+    if (has_src) {
+      std::vector<uint16_t> ncell(N, 0xFFFF);
+      std::vector<int32_t> src(cell_list.size(), -1);
+      for (int64_t j = 0; j < n_real; ++j) ncell[j] = uint16_t(node_cell[j]);
+      for (size_t li = 0; li < cell_list.size(); ++li)
+        if ((*cx.is_src)[cell_list[li]]) src[li] = int32_t(cell_list[li]);
+      std::memcpy(b.data() + d.off_ncell, ncell.data(), ncell.size() * 2);
+      std::memcpy(b.data() + d.off_srccell, src.data(), src.size() * 4);
     }
     for (auto& x : tprobe) specs[spec[x.first]].probe = int32_t(x.second);
     std::memcpy(b.data() + d.off_spec, spec.data(), spec.size() * 2);
@@ -698,7 +777,57 @@ static LaunchArgs base_args(bc_plan* p) {
   a.status = p->d_status;
   a.state_slots = p->state_slots;
   a.timers = p->d_timers;
+  a.syn_g = p->d_syn_g;
+  a.syn_tau = p->d_syn_tau;
+  a.syn_e = p->d_syn_e;
+  a.syn_scale = p->d_syn_scale;
+  a.arrivals = p->n_connections > 0 ? p->d_arrivals : nullptr;
+  a.arr_slots = std::max<int64_t>(p->arr_slots, 1);
+  a.n_syn = p->n_synapses;
+  a.rec_cell = p->d_rec_cell;
+  a.rec_step = p->d_rec_step;
+  a.rec_count = p->d_rec_count;
+  a.rec_cap = p->rec_cap;
   return a;
+}
+
+// Delays in whole steps for dt (network/lowering.py:185-226, "ceil": delays within
+// 1e-7 of a whole number of steps count as that number), and the arrival ring:
+// launches of at most the shortest delay (so a launch never receives an event its
+// own spikes cause) and room for the longest delay past the current launch.
+static bc_status prepare_network(bc_plan* p, double dt, void* stream) {
+  if (p->n_connections == 0 || p->net_dt == dt) return BC_OK;
+  if (p->net_dt != 0.0 && p->step != 0)
+    return fail(BC_ERR_INVALID, "a network plan keeps its dt between resets; call bc_reset before changing dt");
+  std::vector<int32_t> d(p->n_connections);
+  int64_t dmin = INT64_MAX, dmax = 1;
+  for (int64_t q = 0; q < p->n_connections; ++q) {
+    double raw = p->conn_delay[p->out_order[q]] / dt;
+    const double near = std::nearbyint(raw);
+    if (std::fabs(raw - near) <= 1e-7 + 1e-7 * std::fabs(near)) raw = near;
+    const double st = std::ceil(raw - 1e-12);
+    if (st > 1e9) return fail(BC_ERR_INVALID, "connection delay too long for this dt");
+    d[q] = int32_t(st);
+    const int64_t eff = std::max<int64_t>(d[q], 1);
+    dmin = std::min(dmin, eff);
+    dmax = std::max(dmax, eff);
+  }
+  const int64_t k = std::min<int64_t>(p->steps_per_launch, dmin);
+  const int64_t slots = k + dmax + 1;
+  const size_t rs = p->real_size;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  BC_CUDA(cudaStreamSynchronize(s));
+  cudaFree(p->d_arrivals);
+  p->d_arrivals = nullptr;
+  const size_t bytes = size_t(slots) * size_t(std::max<int64_t>(p->n_synapses, 1)) * rs;
+  BC_CUDA(cudaMalloc(&p->d_arrivals, bytes));
+  BC_CUDA(cudaMemsetAsync(p->d_arrivals, 0, bytes, s));
+  BC_CUDA(cudaMemcpyAsync(p->d_out_d, d.data(), d.size() * 4, cudaMemcpyHostToDevice, s));
+  BC_CUDA(cudaStreamSynchronize(s));
+  p->arr_slots = slots;
+  p->net_k = k;
+  p->net_dt = dt;
+  return BC_OK;
 }
 
 // The launches of one run as a CUDA graph: each launch class is a chain of
@@ -771,14 +900,18 @@ static bc_status enqueue_run(bc_plan* p, int64_t n_steps, double dt, void* strea
   const int64_t recs = p->record_every > 0 ? (p->step + n_steps - p->trace_origin) / p->record_every : 0;
   st = ensure_traces(p, recs, stream);
   if (st != BC_OK) return st;
-  if (p->use_graph && n_steps > 0) {
+  st = prepare_network(p, dt, stream);
+  if (st != BC_OK) return st;
+  const bool net = p->n_connections > 0;
+  if (p->use_graph && n_steps > 0 && !net) {
     st = enqueue_run_graph(p, n_steps, dt, stream);
     if (st == BC_OK) p->step += n_steps;
     return st;
   }
+  const int64_t per_launch = net ? std::min<int64_t>(p->steps_per_launch, p->net_k) : p->steps_per_launch;
   int64_t done = 0;
   while (done < n_steps) {
-    const int32_t k = int32_t(std::min<int64_t>(p->steps_per_launch, n_steps - done));
+    const int32_t k = int32_t(std::min<int64_t>(per_launch, n_steps - done));
     LaunchArgs a = base_args(p);
     a.step0 = p->step + done;
     a.n_steps = k;
@@ -803,6 +936,15 @@ static bc_status enqueue_run(bc_plan* p, int64_t n_steps, double dt, void* strea
         BC_CUDA(cudaEventRecord(p->ev_join[ci - 1], st));
         BC_CUDA(cudaStreamWaitEvent(main_st, p->ev_join[ci - 1], 0));
       }
+    }
+    if (net) {
+      // deliver this launch's spikes into the arrival ring, then mark them delivered
+      int e = launch_deliver_impl(p->precision, p->d_rec_cell, p->d_rec_step, p->d_rec_count, p->d_rec_count + 1,
+                                  p->rec_cap, p->d_out_ptr, p->d_out_syn, p->d_out_w, p->d_out_d, p->d_arrivals,
+                                  p->arr_slots, p->n_synapses, stream);
+      if (e) return fail(BC_ERR_CUDA, std::string("delivery kernel: ") + cudaGetErrorString(cudaError_t(e)));
+      BC_CUDA(cudaMemcpyAsync(p->d_rec_count + 1, p->d_rec_count, sizeof(unsigned long long),
+                              cudaMemcpyDeviceToDevice, main_st));
     }
     done += k;
   }
@@ -925,6 +1067,74 @@ bc_status bc_plan_create(const bc_batch_spec* spec, const bc_plan_options* opts_
   }
   p->n_probes = s.n_probes;
   p->n_pulses = s.n_pulses;
+  // ---------------------------------------------------- synapses / connections
+  std::vector<std::vector<std::pair<int64_t, int32_t>>> cell_syns(s.n_cells);
+  std::vector<char> is_src(s.n_cells, 0);
+  if (s.n_synapses < 0 || s.n_connections < 0) {
+    delete p;
+    return fail(BC_ERR_INVALID, "n_synapses and n_connections must be >= 0");
+  }
+  std::vector<double> syn_scale(s.n_synapses, 0.0);
+  for (int64_t k = 0; k < s.n_synapses; ++k) {
+    const int64_t c = s.syn_cell[k];
+    if (c < 0 || c >= s.n_cells) {
+      delete p;
+      return fail(BC_ERR_INVALID, "syn_cell out of range");
+    }
+    if (!(s.syn_tau[k] > 0.0) || !std::isfinite(s.syn_e[k])) {
+      delete p;
+      return fail(BC_ERR_INVALID, "synapse tau must be > 0 ms and e finite");
+    }
+    if (!(s.syn_x[k] > 0.0 && s.syn_x[k] < 1.0)) {
+      delete p;
+      return fail(BC_ERR_INVALID, "a synapse must sit inside a CV (0 < syn_x < 1)");
+    }
+    const int32_t v = locate_node(s, c, cells[c], s.syn_branch[k], s.syn_x[k]);
+    int32_t cv = -1;
+    for (int32_t q = 0; q < cells[c].n_cv && v >= 0; ++q)
+      if (cells[c].cv_node[q] == v) cv = q;
+    if (v < 0 || cv < 0) {
+      delete p;
+      return fail(BC_ERR_INVALID, "synapse location not found");
+    }
+    cell_syns[c].push_back({k, v});
+    syn_scale[k] = 1e5 / cells[c].cv_area[cv];
+  }
+  for (int64_t j = 0; j < s.n_connections; ++j) {
+    if (s.conn_pre[j] < 0 || s.conn_pre[j] >= s.n_cells || s.conn_post[j] < 0 || s.conn_post[j] >= s.n_synapses) {
+      delete p;
+      return fail(BC_ERR_INVALID, "connection pre cell or post synapse out of range");
+    }
+    if (!(s.conn_delay[j] >= 0.0) || !std::isfinite(s.conn_weight[j])) {
+      delete p;
+      return fail(BC_ERR_INVALID, "connection delay must be >= 0 ms and weight finite");
+    }
+  }
+  // every cell of a network records its spikes (the output of a network run);
+  // only cells with connections have events to deliver
+  if (s.n_connections > 0) std::fill(is_src.begin(), is_src.end(), char(1));
+  p->n_synapses = s.n_synapses;
+  p->n_connections = s.n_connections;
+  p->syn_tau.assign(s.syn_tau, s.syn_tau + s.n_synapses);
+  p->syn_e.assign(s.syn_e, s.syn_e + s.n_synapses);
+  p->syn_scale = syn_scale;
+  p->conn_delay.assign(s.conn_delay, s.conn_delay + s.n_connections);
+  {
+    // connections in CSR by presynaptic cell
+    std::vector<int64_t> order(s.n_connections);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int64_t a, int64_t b) { return s.conn_pre[a] < s.conn_pre[b]; });
+    p->out_ptr.assign(s.n_cells + 1, 0);
+    for (int64_t j = 0; j < s.n_connections; ++j) p->out_ptr[s.conn_pre[j] + 1]++;
+    for (int64_t c = 0; c < s.n_cells; ++c) p->out_ptr[c + 1] += p->out_ptr[c];
+    p->out_order = order;
+    p->out_syn.resize(s.n_connections);
+    p->out_w.resize(s.n_connections);
+    for (int64_t q = 0; q < s.n_connections; ++q) {
+      p->out_syn[q] = s.conn_post[order[q]];
+      p->out_w[q] = s.conn_weight[order[q]];
+    }
+  }
   // ---------------------------------------------------- schedules
   std::vector<CellSched> sched(s.n_cells);
   for (int64_t c = 0; c < s.n_cells; ++c) decompose(cells[c], sched[c]);
@@ -992,7 +1202,7 @@ bc_status bc_plan_create(const bc_batch_spec* spec, const bc_plan_options* opts_
     fill.push_back(nn);
     if (tile_nodes - nn > 0) room.emplace(tile_nodes - nn, builds.size() - 1);
   }
-  BuildCtx cx{&s, &cells, &sched, &cv_base, &cell_pulses, &cell_probes, &pulse_node, &probe_node,
+  BuildCtx cx{&s, &cells, &sched, &cv_base, &cell_pulses, &cell_probes, &pulse_node, &probe_node, &cell_syns, &is_src,
               p->precision, S, p->lane_nodes};
   std::vector<TileOut> outs;
   outs.reserve(builds.size());
@@ -1162,6 +1372,45 @@ bc_status bc_plan_create(const bc_batch_spec* spec, const bc_plan_options* opts_
   BC_TRYC(cudaMemcpy(p->d_vinit, vinit.data(), vinit.size() * sizeof(double), cudaMemcpyHostToDevice));
   BC_TRYC(cudaMemcpy(p->d_vinit_off, vinit_off.data(), vinit_off.size() * sizeof(int64_t), cudaMemcpyHostToDevice));
   BC_TRYC(cudaMemset(p->d_status, 0, sizeof(int32_t)));
+  {
+    // synapse parameters and the connection CSR, in the plan's precision
+    auto up_real = [&](void** dst, const std::vector<double>& src) -> bc_status {
+      const size_t n = std::max<size_t>(src.size(), 1);
+      cudaError_t e = cudaMalloc(dst, n * rs);
+      if (e != cudaSuccess) return fail(BC_ERR_CUDA, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+      p->device_bytes += n * rs;
+      std::vector<unsigned char> tmp(n * rs, 0);
+      for (size_t k = 0; k < src.size(); ++k) {
+        if (rs == 8)
+          std::memcpy(tmp.data() + k * 8, &src[k], 8);
+        else {
+          const float f = float(src[k]);
+          std::memcpy(tmp.data() + k * 4, &f, 4);
+        }
+      }
+      e = cudaMemcpy(*dst, tmp.data(), n * rs, cudaMemcpyHostToDevice);
+      if (e != cudaSuccess) return fail(BC_ERR_CUDA, std::string("cudaMemcpy: ") + cudaGetErrorString(e));
+      return BC_OK;
+    };
+    BC_TRY(up_real(&p->d_syn_g, std::vector<double>(p->n_synapses, 0.0)));
+    BC_TRY(up_real(&p->d_syn_tau, p->syn_tau));
+    BC_TRY(up_real(&p->d_syn_e, p->syn_e));
+    BC_TRY(up_real(&p->d_syn_scale, p->syn_scale));
+    BC_TRY(up_real(&p->d_out_w, p->out_w));
+    BC_TRY(dalloc(p, &p->d_out_ptr, p->out_ptr.size()));
+    BC_TRY(dalloc(p, &p->d_out_syn, p->out_syn.size()));
+    BC_TRY(dalloc(p, &p->d_out_d, size_t(p->n_connections)));
+    BC_TRYC(cudaMemcpy(p->d_out_ptr, p->out_ptr.data(), p->out_ptr.size() * 8, cudaMemcpyHostToDevice));
+    if (p->n_connections > 0)
+      BC_TRYC(cudaMemcpy(p->d_out_syn, p->out_syn.data(), p->out_syn.size() * 8, cudaMemcpyHostToDevice));
+    int64_t n_src = 0;
+    for (int64_t c = 0; c + 1 < int64_t(p->out_ptr.size()); ++c) n_src += p->out_ptr[c + 1] > p->out_ptr[c];
+    p->rec_cap = p->n_connections > 0 ? std::max<int64_t>(int64_t(1) << 16, 256 * n_src) : 1;
+    BC_TRY(dalloc(p, &p->d_rec_cell, size_t(p->rec_cap)));
+    BC_TRY(dalloc(p, &p->d_rec_step, size_t(p->rec_cap)));
+    BC_TRY(dalloc(p, &p->d_rec_count, 2));
+    BC_TRYC(cudaMemset(p->d_rec_count, 0, 2 * sizeof(unsigned long long)));
+  }
   if (p->n_smem_tiles > 0 && p->smem_bytes + static_smem > smem_cap) {
     free_plan(p);
     return fail(BC_ERR_CAPACITY, "tile shared memory exceeds the device limit");
@@ -1247,9 +1496,52 @@ bc_status bc_reset(bc_plan_t p, void* stream) {
     BC_CUDA(cudaMemsetAsync(p->d_spike_count, 0, size_t(p->n_probes) * sizeof(int32_t), st));
   }
   BC_CUDA(cudaMemsetAsync(p->d_status, 0, sizeof(int32_t), st));
+  if (p->n_synapses > 0) BC_CUDA(cudaMemsetAsync(p->d_syn_g, 0, size_t(p->n_synapses) * p->real_size, st));
+  if (p->d_arrivals)
+    BC_CUDA(cudaMemsetAsync(p->d_arrivals, 0,
+                            size_t(p->arr_slots) * size_t(std::max<int64_t>(p->n_synapses, 1)) * p->real_size, st));
+  BC_CUDA(cudaMemsetAsync(p->d_rec_count, 0, 2 * sizeof(unsigned long long), st));
   BC_CUDA(cudaStreamSynchronize(st));
   p->step = 0;
   p->trace_origin = 0;
+  return BC_OK;
+}
+
+bc_status bc_network_spikes(bc_plan_t p, int32_t* cells, int64_t* steps, int64_t cap, int64_t* n_out,
+                            void* stream) {
+  if (!p || !n_out || (cap > 0 && (!cells || !steps))) return fail(BC_ERR_INVALID, "null argument");
+  BC_NEED_DEVICE(p);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  unsigned long long n = 0;
+  BC_CUDA(cudaMemcpyAsync(&n, p->d_rec_count, sizeof(n), cudaMemcpyDeviceToHost, s));
+  BC_CUDA(cudaStreamSynchronize(s));
+  *n_out = int64_t(n);
+  const int64_t m = std::min<int64_t>(std::min<int64_t>(int64_t(n), cap), p->rec_cap);
+  if (m > 0) {
+    BC_CUDA(cudaMemcpyAsync(cells, p->d_rec_cell, size_t(m) * 4, cudaMemcpyDeviceToHost, s));
+    BC_CUDA(cudaMemcpyAsync(steps, p->d_rec_step, size_t(m) * 8, cudaMemcpyDeviceToHost, s));
+    BC_CUDA(cudaStreamSynchronize(s));
+  }
+  return BC_OK;
+}
+
+bc_status bc_synapse_download(bc_plan_t p, double* g, void* stream) {
+  if (!p || (!g && p->n_synapses > 0)) return fail(BC_ERR_INVALID, "null argument");
+  BC_NEED_DEVICE(p);
+  if (p->n_synapses == 0) return BC_OK;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  std::vector<unsigned char> tmp(size_t(p->n_synapses) * p->real_size);
+  BC_CUDA(cudaMemcpyAsync(tmp.data(), p->d_syn_g, tmp.size(), cudaMemcpyDeviceToHost, s));
+  BC_CUDA(cudaStreamSynchronize(s));
+  for (int64_t k = 0; k < p->n_synapses; ++k) {
+    if (p->real_size == 8) {
+      std::memcpy(&g[k], tmp.data() + k * 8, 8);
+    } else {
+      float f;
+      std::memcpy(&f, tmp.data() + k * 4, 4);
+      g[k] = double(f);
+    }
+  }
   return BC_OK;
 }
 
@@ -1261,6 +1553,7 @@ bc_status bc_check(bc_plan_t p, void* stream) {
   BC_CUDA(cudaMemcpyAsync(&status, p->d_status, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
   BC_CUDA(cudaStreamSynchronize(st));
   if (status & 2) return fail(BC_ERR_TIMEOUT, "a bounded device wait gave up (bulk copy did not complete)");
+  if (status & 4) return fail(BC_ERR_CAPACITY, "the spike record buffer of the network run overflowed");
   if (status & 1) return fail(BC_ERR_NONFINITE, "non-finite membrane voltage");
   return BC_OK;
 }

@@ -133,6 +133,25 @@ class CurrentClamp:
 
 
 @dataclass(frozen=True)
+class ExpSyn:
+    """Exponential synapse placed at a point (``synapse/markov.py:65``, NEURON
+    ``expsyn.mod``): state ``g`` (uS) with ``g' = -g / tau``; an arriving event adds
+    its weight to ``g`` at the start of a step; current ``i = g (V - e)`` (nA,
+    outward positive).  ``weight`` is the default event weight of connections that
+    give none.
+    """
+
+    tau: float = 0.1      # ms
+    e: float = 0.0        # mV
+    weight: float = 1.0   # uS
+    name: str | None = None
+
+    def __post_init__(self) -> None:
+        if not (self.tau > 0.0):
+            raise ValueError(f"ExpSyn tau must be > 0 ms, got {self.tau}.")
+
+
+@dataclass(frozen=True)
 class StateProbe:
     """Voltage probe at a placed location (``mech/_point.py:314``; only ``field="v"``)."""
 

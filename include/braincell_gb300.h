@@ -133,6 +133,24 @@ typedef struct bc_batch_spec {
   const int32_t* probe_cell;
   const int32_t* probe_branch;
   const double* probe_x;
+  /* ExpSyn synapses (synapse/markov.py:65-117): state g (uS), g' = -g / tau; an
+     arriving event adds its weight to g at the start of a step; current
+     i = g (V - e) enters the CV holding the synapse as i / area.  Must sit
+     inside a CV (0 < x < 1 on its branch).                                      */
+  int64_t n_synapses;
+  const int32_t* syn_cell;
+  const int32_t* syn_branch;
+  const double* syn_x;
+  const double* syn_tau;              /* ms                                     */
+  const double* syn_e;                /* mV                                     */
+  /* connections (network/engine.py:474-530): when any CV of cell conn_pre
+     crosses 0 mV upward within step s, conn_weight (uS) reaches synapse
+     conn_post at step s + max(ceil(conn_delay / dt), 1).                        */
+  int64_t n_connections;
+  const int32_t* conn_pre;            /* cell index                             */
+  const int64_t* conn_post;           /* synapse index                          */
+  const double* conn_weight;          /* uS                                     */
+  const double* conn_delay;           /* ms, >= 0                               */
 } bc_batch_spec;
 
 /* ------------------------------------------------------------------ plan options */
@@ -275,6 +293,15 @@ bc_status bc_probe_download(bc_plan_t plan, double* traces, int64_t max_records,
 bc_status bc_spike_download(bc_plan_t plan, int32_t* counts /* [n_probes] */,
                             double* times /* [n_probes * max_spikes] */, void* stream);
 bc_status bc_probe_clear(bc_plan_t plan, void* stream);
+
+/* Network outputs.  Spike records (cell, step) of every cell of a plan with
+ * connections, in the order the device produced them (by launch; within a
+ * launch not sorted), since the last bc_reset; *n_out receives the number of
+ * records (also when it exceeds cap, in which case only cap are copied).
+ * Synapse conductances g (uS) in synapse order. */
+bc_status bc_network_spikes(bc_plan_t plan, int32_t* cells, int64_t* steps, int64_t cap, int64_t* n_out,
+                            void* stream);
+bc_status bc_synapse_download(bc_plan_t plan, double* g /* [n_synapses] */, void* stream);
 
 /* Diagnostics: cycles summed over CTAs (as seen by each CTA's first thread) in
  * forward elimination, back-substitution, node update and probes/pulses.  Only a

@@ -640,11 +640,12 @@ class OracleCell:
         self.Ci_fixed = np.full(n, _CA_FIXED_CI)
 
     def _points(self, cell) -> None:
-        from braincell_gb300.mech import CurrentClamp, StateProbe
+        from braincell_gb300.mech import CurrentClamp, ExpSyn, StateProbe
 
         self.clamps_mid = []  # (point, t_on, t_off, amp_nA)
         self.clamps_edge = []
         self.probe_points = []
+        self.syn_points, self.syn_tau, self.syn_e = [], [], []  # ExpSyn at CV midpoints
         for locset, decls in cell.place_rules:
             for (b, x) in locset.points(self.morpho):
                 if x <= EPS_PARAM:
@@ -661,6 +662,12 @@ class OracleCell:
                             (self.clamps_mid if self.is_mid[pid] else self.clamps_edge).append((pid, t_on, t_off, amp))
                     elif isinstance(d, StateProbe):
                         self.probe_points.append(pid)
+                    elif isinstance(d, ExpSyn):
+                        if not self.is_mid[pid]:
+                            raise ValueError("ExpSyn must sit inside a CV, not on a branch end point.")
+                        self.syn_points.append(pid)
+                        self.syn_tau.append(d.tau)
+                        self.syn_e.append(d.e)
         self.point_area_um2 = np.zeros(self.n_point)
         self.point_area_um2[self.cv_mid] = self.cv_area
 
@@ -683,6 +690,18 @@ class OracleCell:
                 kind, a, b = r[gate]
                 self.gates[(name, gate)] = (a / (a + b) if kind == "ab" else a) * np.ones((P, n))
         self.spike = np.zeros((P, self.n_cv))
+        self.syn_g = np.zeros((P, len(self.syn_points)))  # uS
+        self.syn_pending = np.zeros((P, len(self.syn_points)))
+
+    def add_events(self, weights) -> None:
+        """Event weights (uS, ``[P, n_syn]``) applied at the start of the next step
+        (``Cell._begin_step``, cell.py:2331-2346; ``ExpSyn.apply_discrete_events``,
+        synapse/markov.py:104-106)."""
+        self.syn_pending = self.syn_pending + np.asarray(weights, dtype=np.float64)
+
+    def population_spike(self) -> np.ndarray:
+        """One spike flag per replica: any CV crossed (network/delivery.py:103-123)."""
+        return self.spike.any(axis=1)
 
     def cv_to_point(self, v):
         out = np.zeros(v.shape[:-1] + (self.n_point,))
@@ -764,6 +783,15 @@ class OracleCell:
         clamp_nA = self._clamp_nA(self.clamps_mid, t)
         safe_area = np.where(self.is_mid, self.point_area_um2, 1.0)
         I_pt = I_pt + np.where(self.is_mid, clamp_nA * 1e5 / safe_area, 0.0)
+        if self.syn_points:
+            # events of this step first, then the synapse current g (e - V) as a
+            # total (nA) point current turned into a density like a clamp
+            self.syn_g = self.syn_g + self.syn_pending
+            self.syn_pending = np.zeros_like(self.syn_pending)
+            for k, pid in enumerate(self.syn_points):
+                g = self.syn_g[:, k] * 1e5 / self.point_area_um2[pid]  # uS -> mS/cm^2 over the CV
+                I_pt[:, pid] += g * (self.syn_e[k] - pv[:, pid])
+                dI_pt[:, pid] -= g
         C_pt = np.ones(n)
         C_pt[self.cv_mid] = self.cv_cm
         deriv = np.where(self.is_mid, I_pt / C_pt, 0.0)
@@ -802,6 +830,11 @@ class OracleCell:
         V_new = se[:, self.dyn_rows]
         self.V = V_new
         pv_new = self.cv_to_point(V_new)
+        # runtime synapse dynamics after the voltage (quad/_staggered.py:144-145):
+        # exp-Euler of g' = -g / tau, exact for this linear ODE
+        for k in range(len(self.syn_points)):
+            lam = -1.0 / self.syn_tau[k]
+            self.syn_g[:, k] = self.syn_g[:, k] + dt * exprel(dt * lam) * (lam * self.syn_g[:, k])
         # a11 (a): dependent ion self states -- Ci with the cached step-start current
         if self.Ci is not None:
             cd = self.ca_dyn
