@@ -31,9 +31,12 @@ BC_M_CAT = 1 << 5
 BC_M_HCN = 1 << 6
 BC_M_AHP = 1 << 7
 BC_M_CADET = 1 << 8
-BC_M_ALL = 0x1FF
+BC_M_NAHH = 1 << 9
+BC_M_KHH = 1 << 10
+BC_M_KM = 1 << 11
+BC_M_ALL = 0xFFF
 
-BC_NPARAM = 40
+BC_NPARAM = 48
 BC_P_INVCM = 0
 BC_P_VREST = 1
 BC_P_ENA = 2
@@ -70,6 +73,14 @@ BC_P_CA_CREST = 32
 BC_P_CA_CO = 33
 BC_P_CA_TEMP = 34
 BC_P_CA_CI0 = 35
+BC_P_NAHH_G = 36
+BC_P_NAHH_VSH = 37
+BC_P_NAHH_PHI = 38
+BC_P_KHH_G = 39
+BC_P_KHH_VSH = 40
+BC_P_KHH_PHI = 41
+BC_P_KM_G = 42
+BC_P_KM_PHI = 43
 
 BC_PREC_F32 = 0
 BC_PREC_F64 = 1
@@ -85,7 +96,11 @@ BC_STATE_CAT_Q = 7
 BC_STATE_HCN_P = 8
 BC_STATE_AHP_P = 9
 BC_STATE_CA_CI = 10
-BC_NSTATE_VIEW = 11
+BC_STATE_NAHH_P = 11
+BC_STATE_NAHH_Q = 12
+BC_STATE_KHH_P = 13
+BC_STATE_KM_N = 14
+BC_NSTATE_VIEW = 15
 BC_NOALLOC_MAX_CV = 262144
 
 STATE_NAMES = {
@@ -100,6 +115,10 @@ STATE_NAMES = {
     "HCN_p": BC_STATE_HCN_P,
     "AHP_p": BC_STATE_AHP_P,
     "Ci": BC_STATE_CA_CI,
+    "NaHH_p": BC_STATE_NAHH_P,
+    "NaHH_q": BC_STATE_NAHH_Q,
+    "KHH_p": BC_STATE_KHH_P,
+    "KM_n": BC_STATE_KM_N,
 }
 
 _p = C.POINTER

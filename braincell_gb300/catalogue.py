@@ -10,6 +10,9 @@ Every class name, parameter name and default below is the reference's:
 * ``CaT_HM1992``  -- channel/calcium.py:222 (g_max 2, q10_p 3.55, q10_q 3, temp_ref 24 degC, V_sh -3)
 * ``HCN_HM1992``  -- channel/hyperpolarization_activated.py:45 (g_max 10, E +43 mV, q10 1)
 * ``AHP_De1994``  -- channel/potassium_calcium.py:78 (n 2, g_max 10, alpha 48, beta 0.09, phi 1)
+* ``Na_HH1952``   -- channel/sodium.py:293  (g_max 120, q10 3, temp = temp_ref = 36 degC, V_sh -45)
+* ``K_HH1952``    -- channel/potassium.py:341 (g_max 10, q10 3, temp = temp_ref = 36 degC, V_sh -45)
+* ``KM_RI2021_SC``-- channel/potassium.py:1597 (g_max 0.25, temp 30 degC; gate q10 3 at 22 degC)
 * ions: ``SodiumFixed`` E 50 (ion/sodium.py:149), ``PotassiumFixed`` E -95
   (ion/potassium.py:151), ``CalciumFixed`` E 120 (ion/calcium.py:187) -- the
   defaults used when no ion is painted (_compute/ions.py:107-113);
@@ -31,6 +34,8 @@ __all__ = ["CHANNELS", "IONS", "region_record", "q10_phi"]
 
 T36 = celsius2kelvin(36.0)
 T24 = celsius2kelvin(24.0)
+T22 = celsius2kelvin(22.0)
+T30 = celsius2kelvin(30.0)
 
 CHANNELS: dict[str, dict[str, float]] = {
     "IL": {"g_max": 0.1, "E": -70.0},
@@ -45,7 +50,12 @@ CHANNELS: dict[str, dict[str, float]] = {
     },
     "HCN_HM1992": {"g_max": 10.0, "E": 43.0, "temp": T36, "q10": 1.0, "temp_ref": T36},
     "AHP_De1994": {"n": 2.0, "g_max": 10.0, "alpha": 48.0, "beta": 0.09, "phi": 1.0},
+    "Na_HH1952": {"g_max": 120.0, "temp": T36, "q10": 3.0, "temp_ref": T36, "V_sh": -45.0},
+    "K_HH1952": {"g_max": 10.0, "temp": T36, "q10": 3.0, "temp_ref": T36, "V_sh": -45.0},
+    "KM_RI2021_SC": {"g_max": 0.25, "temp": T30},
 }
+# gate temperature factors fixed by a class (not constructor parameters)
+KM_Q10, KM_TEMP_REF = 3.0, T22
 _ALIASES = {"leaky": "IL"}
 
 IONS: dict[str, dict[str, float]] = {
@@ -145,6 +155,18 @@ def region_record(mechs, cable: CableProperty) -> tuple[int, np.ndarray]:
             rec[_abi.BC_P_AHP_G], rec[_abi.BC_P_AHP_N] = p["g_max"], p["n"]
             rec[_abi.BC_P_AHP_ALPHA], rec[_abi.BC_P_AHP_BETA] = p["alpha"], p["beta"]
             rec[_abi.BC_P_AHP_PHI] = p["phi"]
+        elif name == "Na_HH1952":
+            bits |= _abi.BC_M_NAHH
+            rec[_abi.BC_P_NAHH_G], rec[_abi.BC_P_NAHH_VSH] = p["g_max"], p["V_sh"]
+            rec[_abi.BC_P_NAHH_PHI] = q10_phi(p["q10"], p["temp"], p["temp_ref"])
+        elif name == "K_HH1952":
+            bits |= _abi.BC_M_KHH
+            rec[_abi.BC_P_KHH_G], rec[_abi.BC_P_KHH_VSH] = p["g_max"], p["V_sh"]
+            rec[_abi.BC_P_KHH_PHI] = q10_phi(p["q10"], p["temp"], p["temp_ref"])
+        elif name == "KM_RI2021_SC":
+            bits |= _abi.BC_M_KM
+            rec[_abi.BC_P_KM_G] = p["g_max"]
+            rec[_abi.BC_P_KM_PHI] = q10_phi(KM_Q10, p["temp"], KM_TEMP_REF)
     if bits & (_abi.BC_M_AHP) and not bits & _abi.BC_M_CADET:
         # AHP reads Ci from the calcium ion; with a fixed Ca ion Ci is the class default.
         rec[_abi.BC_P_CA_CI0] = 5e-5

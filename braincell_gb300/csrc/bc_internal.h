@@ -166,11 +166,15 @@ struct LaunchArgs {
 };
 
 // Host-callable launchers implemented in bc_kernels.cu.
-int launch_tiles(const LaunchArgs& a, int precision, bool smem, int threads, size_t smem_bytes, void* stream);
+// extra: the plan uses synapses, a network, or a mechanism of the out-of-line set
+// (classic HH Na / K, M current); otherwise the kernel variant without that code
+// runs.
+int launch_tiles(const LaunchArgs& a, int precision, bool smem, int threads, size_t smem_bytes, bool extra,
+                 void* stream);
 // Kernel-node parameters of the same launch for a CUDA graph.  kernelParams
 // points at *hold, which points at *a: both must stay valid until the graph
 // call that consumes the parameters returns (it copies the argument).
-int tile_node_params(const LaunchArgs* a, int precision, bool smem, int threads, size_t smem_bytes,
+int tile_node_params(const LaunchArgs* a, int precision, bool smem, int threads, size_t smem_bytes, bool extra,
                      cudaKernelNodeParams* np, const LaunchArgs** hold);
 int launch_reset_impl(const LaunchArgs& a, int precision, int threads, const double* vinit, const int64_t* voff,
                       void* stream);

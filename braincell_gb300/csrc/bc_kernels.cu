@@ -211,17 +211,65 @@ __device__ __forceinline__ void load_states(const Real* st, int N, uint32_t m, N
   }
 }
 
+// Channels outside the main workloads' mix (classic Hodgkin-Huxley Na / K and the
+// M current): kept out of line so that their registers do not weigh on the
+// common path; same exp-Euler steps and ohmic currents as the others.
+constexpr uint32_t kExtraChannels = BC_M_NAHH | BC_M_KHH | BC_M_KM;
+
+template <typename Real>
+__device__ __noinline__ void extra_channels(Real* st, int N, const Real* P, uint32_t m, Real v, Real dt, bool advance,
+                                            Real& G, Real& I) {
+  if (m & BC_M_NAHH) {
+    Real p = st[kSlotNaHHP * N], q = st[kSlotNaHHQ * N];
+    if (advance) {
+      const NaHHRates<Real> r(v, P[BC_P_NAHH_VSH]);
+      const Real phi = P[BC_P_NAHH_PHI];
+      p = gate_ab<Real, true>(p, r.ap, r.bp, phi, dt);
+      q = gate_ab<Real, true>(q, r.aq, r.bq, phi, dt);
+      st[kSlotNaHHP * N] = p;
+      st[kSlotNaHHQ * N] = q;
+    }
+    const Real g = P[BC_P_NAHH_G] * p * p * p * q;
+    G += g;
+    I += g * (P[BC_P_ENA] - v);
+  }
+  if (m & BC_M_KHH) {
+    Real p = st[kSlotKHHP * N];
+    if (advance) {
+      const KHHRates<Real> r(v, P[BC_P_KHH_VSH]);
+      p = gate_ab<Real, true>(p, r.a, r.b, P[BC_P_KHH_PHI], dt);
+      st[kSlotKHHP * N] = p;
+    }
+    const Real p2 = p * p;
+    const Real g = P[BC_P_KHH_G] * p2 * p2;
+    G += g;
+    I += g * (P[BC_P_EK] - v);
+  }
+  if (m & BC_M_KM) {
+    Real n = st[kSlotKMN * N];
+    if (advance) {
+      const KMRates<Real> r(v);
+      n = gate_it(n, r.ninf, r.ntau, P[BC_P_KM_PHI], dt);
+      st[kSlotKMN * N] = n;
+    }
+    const Real g = P[BC_P_KM_G] * n;
+    G += g;
+    I += g * (P[BC_P_EK] - v);
+  }
+}
+
 // One node's mechanisms.  `st` points at the node's slot-0 state (stride N).
 // With advance = true the states move from (v_old) to (v_new) first: calcium
 // from the step-start current (old gates, old V, old Ci), then every gate at
 // v_new (and the new Ci).  Returns the membrane conductance G (mS/cm^2) and
 // ionic current I (uA/cm^2) at v_new with the resulting states.
-template <typename Real>
+template <typename Real, bool kExtra = true>
 __device__ __forceinline__ void node_mechanisms_loaded(const NodeStates<Real>& s0, Real* st, int N, const Real* P,
                                                        uint32_t m, Real v_old, Real v_new, Real dt, bool advance,
                                                        Real& G, Real& I) {
   Real nap = s0.nap, naq = s0.naq, kdrp = s0.kdrp, calp = s0.calp, calq = s0.calq, catp = s0.catp, catq = s0.catq,
        hcnp = s0.hcnp, ahpp = s0.ahpp, cahi = s0.cahi, calo = s0.calo;
+
   if (advance) {
     if (m & BC_M_CADET) {
       const Real ci = cahi + calo;
@@ -326,6 +374,7 @@ __device__ __forceinline__ void node_mechanisms_loaded(const NodeStates<Real>& s
     G += g;
     I += g * (P[BC_P_EK] - v);
   }
+  if (kExtra && (m & kExtraChannels)) extra_channels(st, N, P, m, v_new, dt, advance, G, I);
 }
 
 template <typename Real>
@@ -372,6 +421,16 @@ __device__ __forceinline__ void steady_states(const Real* P, uint32_t m, Real* s
     const Real a = P[BC_P_AHP_ALPHA] * (n == Real(2) ? ci * ci : dpow(ci, n));
     st[kSlotAhpP * N] = a / (a + P[BC_P_AHP_BETA]);
   }
+  if (m & BC_M_NAHH) {
+    const NaHHRates<Real> r(v, P[BC_P_NAHH_VSH]);
+    st[kSlotNaHHP * N] = r.ap / (r.ap + r.bp);
+    st[kSlotNaHHQ * N] = r.aq / (r.aq + r.bq);
+  }
+  if (m & BC_M_KHH) {
+    const KHHRates<Real> r(v, P[BC_P_KHH_VSH]);
+    st[kSlotKHHP * N] = r.a / (r.a + r.b);
+  }
+  if (m & BC_M_KM) st[kSlotKMN * N] = KMRates<Real>(v).ninf;
 }
 
 // Row i of the next linear system: diag = 1 + dt (D + G / cm), rhs = dt I / cm
@@ -969,7 +1028,7 @@ __device__ __forceinline__ bool is_finite_real(Real x) {
 }
 
 // ------------------------------------------------------------------ the step kernel
-template <typename Real, bool kSmem>
+template <typename Real, bool kSmem, bool kExtra>
 __global__ void __launch_bounds__(1024) tile_step_kernel(LaunchArgs a) {
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) uint64_t bar;
@@ -1037,7 +1096,7 @@ __global__ void __launch_bounds__(1024) tile_step_kernel(LaunchArgs a) {
     const uint16_t sp = tv.spec[i];
     if (sp != kNoSpecial) {
       const SpecRec sr = tv.specs[sp];
-      if (sr.syn_begin < sr.syn_end) node_synapses(a, tv, sr, tv.v[i].x, dt, false, false, a.step0, G, I);
+      if (kExtra && sr.syn_begin < sr.syn_end) node_synapses(a, tv, sr, tv.v[i].x, dt, false, false, a.step0, G, I);
     }
     write_row(tv, i, pr, dt, G, I);
     if (sp != kNoSpecial) add_node_pulses(tv, pulses, tv.specs[sp], i, pr, a.step0, dt);
@@ -1102,18 +1161,18 @@ __global__ void __launch_bounds__(1024) tile_step_kernel(LaunchArgs a) {
       const uint16_t pr = pr_cur;
       Real G = Real(0), I = Real(0);
       if (pr != kBoundary)
-        node_mechanisms_loaded(cur, tv.state + i, tv.N, tv.params + size_t(pr) * BC_NPARAM, tv.mech[pr], v_old, hi, dt,
-                               true, G, I);
+        node_mechanisms_loaded<Real, kExtra>(cur, tv.state + i, tv.N, tv.params + size_t(pr) * BC_NPARAM, tv.mech[pr],
+                                             v_old, hi, dt, true, G, I);
       cur = nxt;
       pr_cur = pr_nxt;
       const uint16_t sp = tv.spec[i];
       SpecRec sr;
       if (sp != kNoSpecial) {
         sr = tv.specs[sp];
-        if (sr.syn_begin < sr.syn_end) node_synapses(a, tv, sr, hi, dt, true, last, step + 1, G, I);
+        if (kExtra && sr.syn_begin < sr.syn_end) node_synapses(a, tv, sr, hi, dt, true, last, step + 1, G, I);
       }
       if (!last) write_row(tv, i, pr, dt, G, I);
-      if (tv.has_src && pr != kBoundary) {
+      if (kExtra && tv.has_src && pr != kBoundary) {
         // a spike of the cell: any of its CVs crossing 0 mV upward in this step
         const uint16_t lc = tv.ncell[i];
         if (lc != 0xFFFF && Real(v_old + lo_old) < Real(0) && Real(hi + lo) >= Real(0))
@@ -1137,7 +1196,7 @@ __global__ void __launch_bounds__(1024) tile_step_kernel(LaunchArgs a) {
       }
     }
     __syncthreads();
-    if (tv.has_src)
+    if (kExtra && tv.has_src)
       for (int c = tid; c < tv.n_cells; c += T)
         if (tv.stamp[c] == int32_t(step & 0x7fffffff) && tv.srccell[c] >= 0) {
           const unsigned long long r = atomicAdd(a.rec_count, 1ull);
@@ -1213,9 +1272,9 @@ __global__ void view_kernel(unsigned char* blob, unsigned char* state, const int
 }
 
 // ------------------------------------------------------------------ launchers
-template <typename Real, bool kSmem>
+template <typename Real, bool kSmem, bool kExtra>
 static int launch_impl(const LaunchArgs& a, int threads, size_t smem_bytes, cudaStream_t st) {
-  auto k = tile_step_kernel<Real, kSmem>;
+  auto k = tile_step_kernel<Real, kSmem, kExtra>;
   if (kSmem) {
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem_bytes));
     if (e != cudaSuccess) return int(e);
@@ -1225,22 +1284,30 @@ static int launch_impl(const LaunchArgs& a, int threads, size_t smem_bytes, cuda
   return int(cudaGetLastError());
 }
 
-int launch_tiles(const LaunchArgs& a, int precision, bool smem, int threads, size_t smem_bytes, void* stream) {
+template <bool kExtra>
+static int launch_tiles_x(const LaunchArgs& a, int precision, bool smem, int threads, size_t smem_bytes,
+                          cudaStream_t st) {
+  if (precision == BC_PREC_F64)
+    return smem ? launch_impl<double, true, kExtra>(a, threads, smem_bytes, st)
+                : launch_impl<double, false, kExtra>(a, threads, smem_bytes, st);
+  return smem ? launch_impl<float, true, kExtra>(a, threads, smem_bytes, st)
+              : launch_impl<float, false, kExtra>(a, threads, smem_bytes, st);
+}
+
+int launch_tiles(const LaunchArgs& a, int precision, bool smem, int threads, size_t smem_bytes, bool extra,
+                 void* stream) {
   if (a.n_tiles <= 0) return 0;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  if (precision == BC_PREC_F64)
-    return smem ? launch_impl<double, true>(a, threads, smem_bytes, st)
-                : launch_impl<double, false>(a, threads, smem_bytes, st);
-  return smem ? launch_impl<float, true>(a, threads, smem_bytes, st)
-              : launch_impl<float, false>(a, threads, smem_bytes, st);
+  return extra ? launch_tiles_x<true>(a, precision, smem, threads, smem_bytes, st)
+               : launch_tiles_x<false>(a, precision, smem, threads, smem_bytes, st);
 }
 
 // Kernel-node parameters of one tile launch for a CUDA graph: the same kernel,
 // grid, block and shared memory as launch_tiles; `*a` is copied by the graph call
 // that consumes the parameters.
-template <typename Real, bool kSmem>
+template <typename Real, bool kSmem, bool kExtra>
 static int node_impl(const LaunchArgs* a, int threads, size_t smem_bytes, cudaKernelNodeParams* np) {
-  auto k = tile_step_kernel<Real, kSmem>;
+  auto k = tile_step_kernel<Real, kSmem, kExtra>;
   if (kSmem) {
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem_bytes));
     if (e != cudaSuccess) return int(e);
@@ -1253,14 +1320,25 @@ static int node_impl(const LaunchArgs* a, int threads, size_t smem_bytes, cudaKe
   return 0;
 }
 
-int tile_node_params(const LaunchArgs* a, int precision, bool smem, int threads, size_t smem_bytes,
+int tile_node_params(const LaunchArgs* a, int precision, bool smem, int threads, size_t smem_bytes, bool extra,
                      cudaKernelNodeParams* np, const LaunchArgs** hold) {
   *hold = a;
   int e;
-  if (precision == BC_PREC_F64)
-    e = smem ? node_impl<double, true>(a, threads, smem_bytes, np) : node_impl<double, false>(a, threads, smem_bytes, np);
-  else
-    e = smem ? node_impl<float, true>(a, threads, smem_bytes, np) : node_impl<float, false>(a, threads, smem_bytes, np);
+  if (precision == BC_PREC_F64) {
+    if (extra)
+      e = smem ? node_impl<double, true, true>(a, threads, smem_bytes, np)
+               : node_impl<double, false, true>(a, threads, smem_bytes, np);
+    else
+      e = smem ? node_impl<double, true, false>(a, threads, smem_bytes, np)
+               : node_impl<double, false, false>(a, threads, smem_bytes, np);
+  } else {
+    if (extra)
+      e = smem ? node_impl<float, true, true>(a, threads, smem_bytes, np)
+               : node_impl<float, false, true>(a, threads, smem_bytes, np);
+    else
+      e = smem ? node_impl<float, true, false>(a, threads, smem_bytes, np)
+               : node_impl<float, false, false>(a, threads, smem_bytes, np);
+  }
   np->kernelParams = reinterpret_cast<void**>(const_cast<LaunchArgs**>(hold));
   return e;
 }

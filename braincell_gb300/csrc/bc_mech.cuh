@@ -9,6 +9,9 @@
 //   CaT_HM1992       channel/calcium.py:(CaT f_p_inf .. f_q_tau)
 //   HCN_HM1992       channel/hyperpolarization_activated.py:126-133
 //   AHP_De1994       channel/potassium_calcium.py:181-186
+//   Na_HH1952        channel/sodium.py:384-399
+//   K_HH1952         channel/potassium.py:450-456
+//   KM_RI2021_SC     channel/potassium.py:1735-1748
 //   CalciumDetailed  ion/calcium.py:499-505, Nernst E: ion/_base.py:463-469
 // CUDA's own exp / expm1 / log are called; nothing of the math library is
 // re-implemented here.
@@ -139,6 +142,38 @@ struct HcnRates {
   }
 };
 
+template <typename Real>
+struct NaHHRates {
+  Real ap, bp, aq, bq;
+  __device__ __forceinline__ NaHHRates(Real v, Real vsh) {
+    const Real vp = v - vsh;
+    ap = Real(1) / exprel(-(vp - Real(5)) * Real(0.1));
+    bp = Real(4) * aexp(-(vp + Real(20)) * Real(1.0 / 18));
+    aq = Real(0.07) * aexp(-(vp + Real(20)) * Real(0.05));
+    bq = Real(1) / (Real(1) + aexp(-(vp - Real(10)) * Real(0.1)));
+  }
+};
+
+template <typename Real>
+struct KHHRates {
+  Real a, b;
+  __device__ __forceinline__ KHHRates(Real v, Real vsh) {
+    const Real vp = v - vsh;
+    a = Real(0.1) / exprel(-(vp + Real(10)) * Real(0.1));
+    b = Real(0.125) * aexp(-(vp + Real(20)) * Real(1.0 / 80));
+  }
+};
+
+template <typename Real>
+struct KMRates {
+  Real ninf, ntau;
+  __device__ __forceinline__ KMRates(Real v) {
+    ninf = rdiv(Real(1), Real(1) + rexp(-(v + Real(35)) * Real(1.0 / 6)));
+    ntau = rdiv(Real(1), Real(0.0033) * rexp((v + Real(30)) * Real(1.0 / 40)) +
+                             Real(0.0033) * rexp(-(v + Real(30)) * Real(1.0 / 20)));
+  }
+};
+
 // Fixed state slot of every mechanism state in the [slot][node] state array.
 constexpr int kSlotNaP = 0;
 constexpr int kSlotNaQ = 1;
@@ -151,7 +186,11 @@ constexpr int kSlotHcnP = 7;
 constexpr int kSlotAhpP = 8;
 constexpr int kSlotCaHi = 9;   // CalciumDetailed Ci, float-float high word
 constexpr int kSlotCaLo = 10;  // low word
-constexpr int kNumSlots = 11;
+constexpr int kSlotNaHHP = 11;
+constexpr int kSlotNaHHQ = 12;
+constexpr int kSlotKHHP = 13;
+constexpr int kSlotKMN = 14;
+constexpr int kNumSlots = 15;
 
 constexpr double kFaraday = 96485.33212;   // C/mol
 constexpr double kGasR = 8.314462618;      // J/(mol K)

@@ -66,6 +66,7 @@ struct bc_plan {
   int record_every = 1;
   int max_spikes = 64;
   int use_graph = 0;
+  bool extra = false;  // synapses, a network, or a region using the out-of-line mechanism set
   int state_slots = 1;
   int64_t n_cells = 0, n_cv = 0, n_nodes = 0, n_probes = 0, n_pulses = 0;
   int64_t max_phases = 0, max_chain_nodes = 0;
@@ -865,7 +866,7 @@ static bc_status enqueue_run_graph(bc_plan* p, int64_t n_steps, double dt, void*
         const LaunchClass& lcz = p->classes[ci];
         cudaKernelNodeParams np{};
         const LaunchArgs* hold = nullptr;
-        int e = tile_node_params(&args[size_t(j) * nc + ci], p->precision, lcz.smem, lcz.threads, lcz.smem_bytes, &np,
+        int e = tile_node_params(&args[size_t(j) * nc + ci], p->precision, lcz.smem, lcz.threads, lcz.smem_bytes, p->extra, &np,
                                  &hold);
         if (e) return fail(BC_ERR_CUDA, std::string("graph node: ") + cudaGetErrorString(cudaError_t(e)));
         cudaGraphNode_t dep = j > 0 ? p->graph_nodes[size_t(j - 1) * nc + ci] : nullptr;
@@ -882,7 +883,7 @@ static bc_status enqueue_run_graph(bc_plan* p, int64_t n_steps, double dt, void*
         const LaunchClass& lcz = p->classes[ci];
         cudaKernelNodeParams np{};
         const LaunchArgs* hold = nullptr;
-        int e = tile_node_params(&args[size_t(j) * nc + ci], p->precision, lcz.smem, lcz.threads, lcz.smem_bytes, &np,
+        int e = tile_node_params(&args[size_t(j) * nc + ci], p->precision, lcz.smem, lcz.threads, lcz.smem_bytes, p->extra, &np,
                                  &hold);
         if (e) return fail(BC_ERR_CUDA, std::string("graph node: ") + cudaGetErrorString(cudaError_t(e)));
         BC_CUDA(cudaGraphExecKernelNodeSetParams(p->graph_exec, p->graph_nodes[size_t(j) * nc + ci], &np));
@@ -930,7 +931,7 @@ static bc_status enqueue_run(bc_plan* p, int64_t n_steps, double dt, void* strea
       }
       a.tiles = p->d_tiles + lcz.first;
       a.n_tiles = lcz.count;
-      int e = launch_tiles(a, p->precision, lcz.smem, lcz.threads, lcz.smem_bytes, st);
+      int e = launch_tiles(a, p->precision, lcz.smem, lcz.threads, lcz.smem_bytes, p->extra, st);
       if (e) return fail(BC_ERR_CUDA, std::string("tile kernel launch: ") + cudaGetErrorString(cudaError_t(e)));
       if (ci > 0) {
         BC_CUDA(cudaEventRecord(p->ev_join[ci - 1], st));
@@ -1021,6 +1022,8 @@ bc_status bc_plan_create(const bc_batch_spec* spec, const bc_plan_options* opts_
   p->n_cv = cv_base[s.n_cells];
   p->cell_ncv.resize(s.n_cells);
   for (int64_t c = 0; c < s.n_cells; ++c) p->cell_ncv[c] = cells[c].n_cv;
+  for (int64_t k = 0; k < s.n_cells * s.n_regions; ++k)
+    p->extra = p->extra || (s.region_mech[k] & (BC_M_NAHH | BC_M_KHH | BC_M_KM)) != 0;
   for (int64_t k = 0; k < s.n_cells * s.n_regions; ++k)
     if (s.region_mech[k] & ~BC_M_ALL) {
       delete p;
@@ -1115,6 +1118,7 @@ bc_status bc_plan_create(const bc_batch_spec* spec, const bc_plan_options* opts_
   if (s.n_connections > 0) std::fill(is_src.begin(), is_src.end(), char(1));
   p->n_synapses = s.n_synapses;
   p->n_connections = s.n_connections;
+  p->extra = p->extra || s.n_synapses > 0 || s.n_connections > 0;
   p->syn_tau.assign(s.syn_tau, s.syn_tau + s.n_synapses);
   p->syn_e.assign(s.syn_e, s.syn_e + s.n_synapses);
   p->syn_scale = syn_scale;
@@ -1629,6 +1633,10 @@ static bc_status view_offsets(bc_plan* p, int32_t which, std::vector<int64_t>& h
         slot = (m & BC_M_CADET) ? kSlotCaHi : -1;
         has_lo = true;
         break;
+      case BC_STATE_NAHH_P: slot = (m & BC_M_NAHH) ? kSlotNaHHP : -1; break;
+      case BC_STATE_NAHH_Q: slot = (m & BC_M_NAHH) ? kSlotNaHHQ : -1; break;
+      case BC_STATE_KHH_P: slot = (m & BC_M_KHH) ? kSlotKHHP : -1; break;
+      case BC_STATE_KM_N: slot = (m & BC_M_KM) ? kSlotKMN : -1; break;
     }
     if (slot < 0) continue;
     // states live in the separate state array: offsets are tagged by +state_tag
@@ -1712,10 +1720,12 @@ static void noalloc_offset(const bc_plan* p, int32_t which, int64_t k, int64_t* 
     *lo = *hi + rs;
     return;
   }
-  static const uint32_t kBit[BC_NSTATE_VIEW] = {0,         BC_M_NA,  BC_M_NA,  BC_M_KDR, BC_M_CAL, BC_M_CAL,
-                                                BC_M_CAT,  BC_M_CAT, BC_M_HCN, BC_M_AHP, BC_M_CADET};
-  static const int kSlot[BC_NSTATE_VIEW] = {-1,         kSlotNaP,  kSlotNaQ,  kSlotKdrP, kSlotCalP, kSlotCalQ,
-                                            kSlotCatP,  kSlotCatQ, kSlotHcnP, kSlotAhpP, kSlotCaHi};
+  static const uint32_t kBit[BC_NSTATE_VIEW] = {0,        BC_M_NA,    BC_M_NA,   BC_M_KDR,  BC_M_CAL,
+                                                BC_M_CAL, BC_M_CAT,   BC_M_CAT,  BC_M_HCN,  BC_M_AHP,
+                                                BC_M_CADET, BC_M_NAHH, BC_M_NAHH, BC_M_KHH, BC_M_KM};
+  static const int kSlot[BC_NSTATE_VIEW] = {-1,        kSlotNaP,   kSlotNaQ,   kSlotKdrP,  kSlotCalP,
+                                            kSlotCalQ, kSlotCatP,  kSlotCatQ,  kSlotHcnP,  kSlotAhpP,
+                                            kSlotCaHi, kSlotNaHHP, kSlotNaHHQ, kSlotKHHP,  kSlotKMN};
   if (!(p->cv_mech[k] & kBit[which])) return;
   *hi = kStateTag + (d.state_offset + int64_t(kSlot[which]) * d.n_nodes + j) * rs;
   if (which == BC_STATE_CA_CI) *lo = kStateTag + (d.state_offset + int64_t(kSlotCaLo) * d.n_nodes + j) * rs;

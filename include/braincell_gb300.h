@@ -50,10 +50,13 @@ typedef int32_t bc_status;
 #define BC_M_HCN (1u << 6)       /* channel/hyperpolarization_activated.py:45 HCN_HM1992 p, E  */
 #define BC_M_AHP (1u << 7)       /* channel/potassium_calcium.py:78 AHP_De1994 p^2, E_K, Ci   */
 #define BC_M_CADET (1u << 8)     /* ion/calcium.py:286        CalciumDetailed (dynamic Ci)     */
-#define BC_M_ALL 0x1FFu
+#define BC_M_NAHH (1u << 9)      /* channel/sodium.py:293     Na_HH1952   p^3 q, E_Na          */
+#define BC_M_KHH (1u << 10)      /* channel/potassium.py:341  K_HH1952    p^4, E_K             */
+#define BC_M_KM (1u << 11)       /* channel/potassium.py:1597 KM_RI2021_SC n, E_K              */
+#define BC_M_ALL 0xFFFu
 
 /* Per-region parameter record (double[BC_NPARAM]); index names below. */
-#define BC_NPARAM 40
+#define BC_NPARAM 48
 #define BC_P_INVCM 0      /* 1 / membrane capacitance, cm^2/uF                 */
 #define BC_P_VREST 1      /* voltage used by reset (mV)                        */
 #define BC_P_ENA 2        /* fixed reversal potentials (mV)                    */
@@ -90,6 +93,14 @@ typedef int32_t bc_status;
 #define BC_P_CA_CO 33     /* mM                                                */
 #define BC_P_CA_TEMP 34   /* K                                                 */
 #define BC_P_CA_CI0 35    /* mM, reset value of Ci                             */
+#define BC_P_NAHH_G 36
+#define BC_P_NAHH_VSH 37
+#define BC_P_NAHH_PHI 38
+#define BC_P_KHH_G 39
+#define BC_P_KHH_VSH 40
+#define BC_P_KHH_PHI 41
+#define BC_P_KM_G 42
+#define BC_P_KM_PHI 43
 
 /* ------------------------------------------------------------------ batch spec */
 /*
@@ -262,7 +273,11 @@ bc_status bc_check(bc_plan_t plan, void* stream);
 #define BC_STATE_HCN_P 8
 #define BC_STATE_AHP_P 9
 #define BC_STATE_CA_CI 10
-#define BC_NSTATE_VIEW 11
+#define BC_STATE_NAHH_P 11
+#define BC_STATE_NAHH_Q 12
+#define BC_STATE_KHH_P 13
+#define BC_STATE_KM_N 14
+#define BC_NSTATE_VIEW 15
 bc_status bc_state_download(bc_plan_t plan, int32_t which, double* out /* [n_cv] */, void* stream);
 bc_status bc_state_upload(bc_plan_t plan, int32_t which, const double* in /* [n_cv] */, void* stream);
 

@@ -87,6 +87,9 @@ CHANNEL_DEFAULTS = {
                        temp_ref_q=_c2k(24.0), V_sh=-3.0),  # calcium.py:(CaT __init__)
     "HCN_HM1992": dict(g_max=10.0, E=43.0, temp=_c2k(36.0), q10=1.0, temp_ref=_c2k(36.0)),  # hyperpol..:104-112
     "AHP_De1994": dict(n=2.0, g_max=10.0, alpha=48.0, beta=0.09, phi=1.0),  # potassium_calcium.py:163-172
+    "Na_HH1952": dict(g_max=120.0, temp=_c2k(36.0), q10=3.0, temp_ref=_c2k(36.0), V_sh=-45.0),  # sodium.py:371-380
+    "K_HH1952": dict(g_max=10.0, temp=_c2k(36.0), q10=3.0, temp_ref=_c2k(36.0), V_sh=-45.0),  # potassium.py:433-441
+    "KM_RI2021_SC": dict(g_max=0.25, temp=_c2k(30.0)),  # potassium.py:1716-1721
 }
 ION_DEFAULTS = {
     "SodiumFixed": dict(E=50.0),
@@ -315,6 +318,19 @@ def rates(name: str, V, p: dict, Ci=None):
                       1.0 / (np.exp(-0.086 * V - 14.59) + np.exp(0.0701 * V - 1.87)))}
     if name == "AHP_De1994":  # potassium_calcium.py:181-186
         return {"p": ("ab", p["alpha"] * np.power(Ci, p["n"]), p["beta"] * np.ones_like(V))}
+    if name == "Na_HH1952":  # sodium.py:384-399
+        Vp = V - p["V_sh"]
+        return {
+            "p": ("ab", 1.0 / exprel(-(Vp - 5.0) / 10.0), 4.0 * np.exp(-(Vp + 20.0) / 18.0)),
+            "q": ("ab", 0.07 * np.exp(-(Vp + 20.0) / 20.0), 1.0 / (1.0 + np.exp(-(Vp - 10.0) / 10.0))),
+        }
+    if name == "K_HH1952":  # potassium.py:450-456
+        Vp = V - p["V_sh"]
+        return {"p": ("ab", 0.1 / exprel(-(Vp + 10.0) / 10.0), 0.125 * np.exp(-(Vp + 20.0) / 80.0))}
+    if name == "KM_RI2021_SC":  # potassium.py:1735-1748
+        a = 0.0033 * np.exp((V + 30.0) / 40.0)
+        b = 0.0033 * np.exp((V + 30.0) / -20.0)
+        return {"n": ("it", 1.0 / (1.0 + np.exp(-(V + 35.0) / 6.0)), 1.0 / (a + b))}
     raise KeyError(name)
 
 
@@ -325,9 +341,12 @@ _GATES = {  # (gate, power, phi-key)
     "CaT_HM1992": (("p", 2, "phi_p"), ("q", 1, "phi_q")),
     "HCN_HM1992": (("p", 1, "phi"),),
     "AHP_De1994": (("p", 2, "phi"),),
+    "Na_HH1952": (("p", 3, "phi"), ("q", 1, "phi")),
+    "K_HH1952": (("p", 4, "phi"),),
+    "KM_RI2021_SC": (("n", 1, "phi"),),
 }
 _ION_OF = {"Na_Ba2002": "na", "KDR_Ba2002": "k", "CaL_IS2008": "ca", "CaT_HM1992": "ca",
-           "K_Leak": "k", "AHP_De1994": "k"}
+           "K_Leak": "k", "AHP_De1994": "k", "Na_HH1952": "na", "K_HH1952": "k", "KM_RI2021_SC": "k"}
 
 
 def _resolve(table: dict, decl) -> dict:
@@ -337,8 +356,10 @@ def _resolve(table: dict, decl) -> dict:
             raise ValueError(f"{decl.class_name}: unknown parameter {k!r}.")
         p[k] = float(v)
     name = decl.class_name
-    if name in ("Na_Ba2002", "KDR_Ba2002", "HCN_HM1992"):
+    if name in ("Na_Ba2002", "KDR_Ba2002", "HCN_HM1992", "Na_HH1952", "K_HH1952"):
         p["phi"] = p["q10"] ** ((p["temp"] - p["temp_ref"]) / 10.0)
+    elif name == "KM_RI2021_SC":  # Gate("n", q10=3.0, temp_ref=22 degC), potassium.py:1710
+        p["phi"] = 3.0 ** ((p["temp"] - (273.15 + 22.0)) / 10.0)
     elif name in ("CaL_IS2008", "CaT_HM1992"):
         p["phi_p"] = p["q10_p"] ** ((p["temp"] - p["temp_ref_p"]) / 10.0)
         p["phi_q"] = p["q10_q"] ** ((p["temp"] - p["temp_ref_q"]) / 10.0)

@@ -176,3 +176,38 @@ def test_oracle_rest_is_steady_without_input():
         oc.step(0.025)
     assert np.all(np.isfinite(oc.V))
     assert np.all(np.abs(oc.V + 67.5) < 3.0)
+
+
+def test_hh1952_rates_match_published_forms():
+    # channel/sodium.py:293-330 and channel/potassium.py:341-380 docstrings: with the
+    # default V_sh = -45 mV the rates are Hodgkin & Huxley's published forms
+    from oracle.staggered import rates
+
+    V = np.array([-80.0, -65.0, -52.5, -20.0, 10.0])
+    na = rates("Na_HH1952", V, {"V_sh": -45.0})
+    np.testing.assert_allclose(na["p"][1], 0.1 * (V + 40) / (1 - np.exp(-(V + 40) / 10)), rtol=1e-12)
+    np.testing.assert_allclose(na["p"][2], 4 * np.exp(-(V + 65) / 18), rtol=1e-12)
+    np.testing.assert_allclose(na["q"][1], 0.07 * np.exp(-(V + 65) / 20), rtol=1e-12)
+    np.testing.assert_allclose(na["q"][2], 1 / (1 + np.exp(-(V + 35) / 10)), rtol=1e-12)
+    k = rates("K_HH1952", V, {"V_sh": -45.0})
+    np.testing.assert_allclose(k["p"][1], 0.01 * (V + 55) / (1 - np.exp(-(V + 55) / 10)), rtol=1e-12)
+    np.testing.assert_allclose(k["p"][2], 0.125 * np.exp(-(V + 65) / 80), rtol=1e-12)
+    # removable singularities: alpha_m(-40) = 1, alpha_n(-55) = 0.1 (potassium.py docstring)
+    assert rates("Na_HH1952", np.array([-40.0]), {"V_sh": -45.0})["p"][1][0] == pytest.approx(1.0)
+    assert rates("K_HH1952", np.array([-55.0]), {"V_sh": -45.0})["p"][1][0] == pytest.approx(0.1)
+
+
+def test_km_rates_and_temperature_factor():
+    # channel/potassium.py:1597-1748: n_inf = 1 / (1 + exp(-(V + 35) / 6)),
+    # tau_n = 1 / (alpha_n + beta_n), gate q10 3 at 22 degC (phi = 3^0.8 at 30 degC)
+    from braincell_gb300.catalogue import KM_Q10, KM_TEMP_REF, q10_phi
+    from braincell_gb300.mech import celsius2kelvin
+    from oracle.staggered import rates
+
+    V = np.array([-60.0, -35.0, 0.0])
+    r = rates("KM_RI2021_SC", V, {})
+    np.testing.assert_allclose(r["n"][1], 1 / (1 + np.exp(-(V + 35) / 6)), rtol=1e-12)
+    a, b = 0.0033 * np.exp((V + 30) / 40), 0.0033 * np.exp((V + 30) / -20)
+    np.testing.assert_allclose(r["n"][2], 1 / (a + b), rtol=1e-12)
+    assert q10_phi(KM_Q10, celsius2kelvin(30.0), KM_TEMP_REF) == pytest.approx(3.0 ** 0.8)
+    assert q10_phi(3.0, celsius2kelvin(46.0), celsius2kelvin(36.0)) == pytest.approx(3.0)  # potassium_test.py:113-121

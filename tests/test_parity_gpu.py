@@ -248,3 +248,43 @@ def test_autotune_returns_working_options():
     p = Plan(b, **r.options)
     p.run(10, DT)
     assert np.isfinite(p.state("V")).all()
+
+
+def _hh_cell(precision):
+    from braincell_gb300 import Branch, Cell, Morphology
+    from braincell_gb300.mech import AllRegion, CableProperty, Channel, CurrentClamp, CVPerBranch, RootLocation, StateProbe, branch_in
+
+    soma = Branch.from_lengths(lengths=[20.0], radii=[10.0, 10.0], type="soma")
+    m = Morphology.from_root(soma, name="soma")
+    for _ in range(3):
+        m.attach(parent="soma", child_branch=Branch.from_lengths(lengths=[150.0], radii=[1.2, 0.5], type="basal_dendrite"))
+    c = Cell(m, cv_policy=CVPerBranch(), precision=precision)
+    c.paint(AllRegion(), CableProperty(), Channel("IL", g_max=0.3, E=-54.4))
+    c.paint(branch_in("type", "soma"), Channel("Na_HH1952", g_max=120.0), Channel("K_HH1952", g_max=36.0))
+    c.paint(branch_in("type", "basal_dendrite"), Channel("KM_RI2021_SC", g_max=0.5))
+    c.place(RootLocation(0.5), CurrentClamp(delay=2.0, durations=20.0, amplitudes=0.6))
+    c.place(RootLocation(0.5), StateProbe())
+    return c
+
+
+@pytest.mark.parametrize("precision,tol", [("f64", TOL_F64_MV), ("f32", TOL_F32_MV)])
+def test_classic_hh_and_m_current(precision, tol):
+    from braincell_gb300.batch import lower_cell
+
+    n = 1000
+    p = Plan(lower_cell(_hh_cell(precision)), precision=precision)
+    p.run(n, DT)
+    tr = p.traces()[0]
+    oc = OracleCell(_hh_cell("f64"))
+    otr, osp = oc.run(DT, n)
+    ref = otr[0, 0]
+    assert len(osp[0][0]) >= 2  # the classic HH soma fires under this clamp
+    if precision == "f64":
+        assert np.abs(ref - tr).max() <= tol
+        km = p.state("KM_n")
+        assert np.isnan(km[0]) and np.isfinite(km[1:]).all()  # soma CV first, then the dendrites
+    else:
+        first = _onset(ref)
+        assert np.abs(ref[:first] - tr[:first]).max() <= tol
+        sp = p.spikes()[0]
+        assert len(sp) == len(osp[0][0]) and np.abs(np.asarray(sp) - np.asarray(osp[0][0])).max() <= 0.05

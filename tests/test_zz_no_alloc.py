@@ -46,11 +46,29 @@ def _calcium_desc():
     return W.large(indices=[0], n_range=(300, 400), n_branches=20, n_pulses=60, duration=20.0)[0]
 
 
+def _hh_batch():
+    # a cell with the classic Hodgkin-Huxley channels and the M current, so that
+    # every state view has values somewhere in the batch
+    from braincell_gb300 import Branch, Cell, Morphology
+    from braincell_gb300.batch import lower_cell
+    from braincell_gb300.mech import AllRegion, CableProperty, Channel, CVPerBranch, branch_in
+
+    m = Morphology.from_root(Branch.from_lengths(lengths=[20.0], radii=[10.0, 10.0], type="soma"), name="soma")
+    m.attach(parent="soma", child_branch=Branch.from_lengths(lengths=[100.0], radii=[1.0, 0.6], type="basal_dendrite"))
+    c = Cell(m, cv_policy=CVPerBranch())
+    c.paint(AllRegion(), CableProperty(), Channel("IL", g_max=0.3, E=-54.4))
+    c.paint(branch_in("type", "soma"), Channel("Na_HH1952"), Channel("K_HH1952", g_max=36.0))
+    c.paint(branch_in("type", "basal_dendrite"), Channel("KM_RI2021_SC"))
+    return lower_cell(c)
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("precision", ["f32", "f64"])
 def test_noalloc_download_matches_download(native_lib, cuda_device, precision):
+    from braincell_gb300.batch import concat_batches
+
     descs = W.small(4) + [_calcium_desc()] + W.uneven(indices=[0, 1])
-    plan = Plan(W.descs_to_batch(descs), precision=precision, device=cuda_device)
+    plan = Plan(concat_batches([W.descs_to_batch(descs), _hh_batch()]), precision=precision, device=cuda_device)
     assert plan.n_cv <= _abi.BC_NOALLOC_MAX_CV
     for segment in range(2):
         plan.run(300, 0.025)
