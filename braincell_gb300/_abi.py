@@ -85,6 +85,10 @@ BC_P_KM_PHI = 43
 BC_PREC_F32 = 0
 BC_PREC_F64 = 1
 
+BC_GRU_HIDDEN = 64
+BC_GRU_INPUTS = 4
+BC_SURROGATE_NORM = 5
+
 BC_STATE_V = 0
 BC_STATE_NA_P = 1
 BC_STATE_NA_Q = 2
@@ -166,6 +170,17 @@ class BatchSpec(C.Structure):
         ("conn_post", _p(C.c_int64)),
         ("conn_weight", _p(C.c_double)),
         ("conn_delay", _p(C.c_double)),
+        ("n_ports", C.c_int64),
+        ("port_cell", _p(C.c_int32)),
+        ("port_branch", _p(C.c_int32)),
+        ("port_g", _p(C.c_double)),
+        ("port_e", _p(C.c_double)),
+        ("port_feat", _p(C.c_double)),
+        ("n_port_pulses", C.c_int64),
+        ("port_pulse_port", _p(C.c_int32)),
+        ("port_pulse_t_on", _p(C.c_double)),
+        ("port_pulse_t_off", _p(C.c_double)),
+        ("port_pulse_amp", _p(C.c_double)),
     ]
 
 
@@ -244,6 +259,19 @@ SIGNATURES = {
     "bc_step_count": (C.c_int32, [C.c_void_p, _p(C.c_int64)]),
     "bc_debug_phase_cycles": (C.c_int32, [C.c_void_p, _p(C.c_uint64), C.c_int32]),
     "bc_run_timed": (C.c_int32, [C.c_void_p, C.c_int64, C.c_double, C.c_void_p, _p(C.c_double)]),
+    "bc_gru_nparam": (C.c_int32, []),
+    "bc_surrogate_set": (C.c_int32, [C.c_void_p, _p(C.c_float), _p(C.c_float), C.c_void_p]),
+    "bc_surrogate_flags": (C.c_int32, [C.c_void_p, _p(C.c_int32), C.c_void_p]),
+    "bc_gru_pack": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "bc_gru_forward": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int32,
+                                   C.c_int64, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                   C.c_void_p]),
+    "bc_gru_backward": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int32,
+                                    C.c_int64, C.c_int32, C.c_void_p, C.c_void_p, C.c_float, C.c_void_p,
+                                    C.c_void_p]),
+    "bc_gru_grad_sqnorm": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "bc_gru_adam": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_float, C.c_float,
+                                C.c_float, C.c_float, C.c_float, C.c_void_p]),
 }
 
 _HERE = os.path.dirname(os.path.abspath(__file__))

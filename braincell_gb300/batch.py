@@ -66,6 +66,15 @@ class CellBatch:
     conn_post: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int64))
     conn_weight: np.ndarray = field(default_factory=lambda: np.zeros(0, np.float64))
     conn_delay: np.ndarray = field(default_factory=lambda: np.zeros(0, np.float64))
+    port_cell: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
+    port_branch: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
+    port_g: np.ndarray = field(default_factory=lambda: np.zeros(0, np.float64))
+    port_e: np.ndarray = field(default_factory=lambda: np.zeros(0, np.float64))
+    port_feat: np.ndarray = field(default_factory=lambda: np.zeros((0, 2), np.float64))
+    port_pulse_port: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
+    port_pulse_t_on: np.ndarray = field(default_factory=lambda: np.zeros(0, np.float64))
+    port_pulse_t_off: np.ndarray = field(default_factory=lambda: np.zeros(0, np.float64))
+    port_pulse_amp: np.ndarray = field(default_factory=lambda: np.zeros(0, np.float64))
 
     _DTYPES = {
         "cell_branch_offsets": np.int64,
@@ -100,12 +109,22 @@ class CellBatch:
         "conn_post": np.int64,
         "conn_weight": np.float64,
         "conn_delay": np.float64,
+        "port_cell": np.int32,
+        "port_branch": np.int32,
+        "port_g": np.float64,
+        "port_e": np.float64,
+        "port_feat": np.float64,
+        "port_pulse_port": np.int32,
+        "port_pulse_t_on": np.float64,
+        "port_pulse_t_off": np.float64,
+        "port_pulse_amp": np.float64,
     }
 
     def __post_init__(self) -> None:
         for name, dt in self._DTYPES.items():
             setattr(self, name, np.ascontiguousarray(getattr(self, name), dtype=dt))
         self.region_params = self.region_params.reshape(-1, _abi.BC_NPARAM)
+        self.port_feat = self.port_feat.reshape(-1, 2)
         self.n_regions = int(self.n_regions)
 
     # ------------------------------------------------------------------ sizes
@@ -151,6 +170,12 @@ class CellBatch:
         new_syn = np.full(self.syn_cell.size, -1, np.int64)
         new_syn[syn_old] = np.arange(syn_old.size)
         ck = (new_id[self.conn_pre] >= 0) & (new_syn[self.conn_post] >= 0) if self.conn_pre.size else np.zeros(0, bool)
+        ok = new_id[self.port_cell] >= 0 if self.port_cell.size else np.zeros(0, bool)
+        port_old = np.nonzero(ok)[0][np.argsort(new_id[self.port_cell[ok]], kind="stable")]
+        new_port = np.full(self.port_cell.size, -1, np.int64)
+        new_port[port_old] = np.arange(port_old.size)
+        ppk = new_port[self.port_pulse_port] >= 0 if self.port_pulse_port.size else np.zeros(0, bool)
+        pp_old = np.nonzero(ppk)[0][np.argsort(new_port[self.port_pulse_port[ppk]], kind="stable")]
         return CellBatch(
             n_regions=R,
             cell_branch_offsets=np.concatenate([[0], np.cumsum(b1 - b0)]),
@@ -170,6 +195,10 @@ class CellBatch:
             syn_tau=self.syn_tau[syn_old], syn_e=self.syn_e[syn_old],
             conn_pre=new_id[self.conn_pre[ck]], conn_post=new_syn[self.conn_post[ck]],
             conn_weight=self.conn_weight[ck], conn_delay=self.conn_delay[ck],
+            port_cell=new_id[self.port_cell[port_old]], port_branch=self.port_branch[port_old],
+            port_g=self.port_g[port_old], port_e=self.port_e[port_old], port_feat=self.port_feat[port_old],
+            port_pulse_port=new_port[self.port_pulse_port[pp_old]], port_pulse_t_on=self.port_pulse_t_on[pp_old],
+            port_pulse_t_off=self.port_pulse_t_off[pp_old], port_pulse_amp=self.port_pulse_amp[pp_old],
         )
 
     def validate(self) -> None:
@@ -188,6 +217,12 @@ class CellBatch:
         nc = self.conn_pre.size
         if any(getattr(self, k).size != nc for k in ("conn_post", "conn_weight", "conn_delay")):
             raise ValueError("connection arrays must all have n_connections entries.")
+        npt = self.port_cell.size
+        if any(getattr(self, k).shape[0] != npt for k in ("port_branch", "port_g", "port_e", "port_feat")):
+            raise ValueError("port arrays must all have n_ports entries.")
+        npp = self.port_pulse_port.size
+        if any(getattr(self, k).size != npp for k in ("port_pulse_t_on", "port_pulse_t_off", "port_pulse_amp")):
+            raise ValueError("port pulse arrays must all have n_port_pulses entries.")
 
     # ------------------------------------------------------------------ ABI
     def to_spec(self) -> tuple[_abi.BatchSpec, tuple]:
@@ -208,6 +243,8 @@ class CellBatch:
         s.n_probes = int(self.probe_cell.size)
         s.n_synapses = int(self.syn_cell.size)
         s.n_connections = int(self.conn_pre.size)
+        s.n_ports = int(self.port_cell.size)
+        s.n_port_pulses = int(self.port_pulse_port.size)
         return s, tuple(keep)
 
 
@@ -242,6 +279,7 @@ def concat_batches(batches: list[CellBatch]) -> CellBatch:
     seg_off = 0
     cell_off = 0
     syn_off = 0
+    port_off = 0
     for b in batches:
         parts["cell_branch_offsets"].append(b.cell_branch_offsets[(1 if br_off or cell_off else 0):] + br_off)
         parts["branch_seg_offsets"].append(b.branch_seg_offsets[(1 if seg_off or cell_off else 0):] + seg_off)
@@ -264,10 +302,14 @@ def concat_batches(batches: list[CellBatch]) -> CellBatch:
         parts["syn_cell"].append(b.syn_cell + cell_off)
         parts["conn_pre"].append(b.conn_pre + cell_off)
         parts["conn_post"].append(b.conn_post + syn_off)
+        parts["port_cell"].append(b.port_cell + cell_off)
+        parts["port_pulse_port"].append(b.port_pulse_port + port_off)
         for k in ("pulse_branch", "pulse_x", "pulse_t_on", "pulse_t_off", "pulse_amp", "probe_branch", "probe_x",
-                  "syn_branch", "syn_x", "syn_tau", "syn_e", "conn_weight", "conn_delay"):
+                  "syn_branch", "syn_x", "syn_tau", "syn_e", "conn_weight", "conn_delay", "port_branch", "port_g",
+                  "port_e", "port_feat", "port_pulse_t_on", "port_pulse_t_off", "port_pulse_amp"):
             parts[k].append(getattr(b, k))
         syn_off += int(b.syn_cell.size)
+        port_off += int(b.port_cell.size)
         br_off += b.n_branches
         seg_off += int(b.seg_length.size)
         cell_off += nc

@@ -19,7 +19,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 NATIVE_DIR = os.path.join(HERE, "_native")
 LIB = os.path.join(NATIVE_DIR, "libbraincell_gb300.so")
-SOURCES = ["bc_kernels.cu", "bc_plan.cpp", "bc_lower.cpp"]
+SOURCES = ["bc_kernels.cu", "bc_gru.cu", "bc_plan.cpp", "bc_lower.cpp"]
 GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
 
 

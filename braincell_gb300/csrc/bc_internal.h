@@ -105,6 +105,82 @@ struct TileDesc {
   // the tile has no spike source.  off_stamp: per-cell spike step (scratch).
   int32_t off_syn, off_ncell, off_srccell, off_stamp;
   int64_t scratch_offset;   // bytes into the plan's global scratch (global-resident tiles)
+  int64_t port_offset;      // into the plan's port array (subtree-surrogate ports of this tile)
+  int32_t n_ports;
+  int32_t off_pstage;       // per-port staging records (PortStage), inside the scratch area; -1: none
+};
+
+// ------------------------------------------------------------- subtree surrogate
+// GRU sizes and the layout of its flat FP32 parameter vector (training master
+// copy, host files): Wh [3H][H] | Wx [3H][X] | bx [3H] | bh [3H] | wo [H] | bo,
+// gate blocks in the order r, z, n.
+constexpr int kGruH = 64;
+constexpr int kGruX = 4;
+constexpr int kGru3H = 3 * kGruH;
+constexpr int kGruOffWh = 0;
+constexpr int kGruOffWx = kGruOffWh + kGru3H * kGruH;
+constexpr int kGruOffBx = kGruOffWx + kGru3H * kGruX;
+constexpr int kGruOffBh = kGruOffBx + kGru3H;
+constexpr int kGruOffWo = kGruOffBh + kGru3H;
+constexpr int kGruOffBo = kGruOffWo + kGruH;
+constexpr int kGruNParam = kGruOffBo + 1;
+// Extended K of the tensor-core products: h (H) plus a 16-wide block of inputs
+// and biases; rows of the extended weight matrix: r, z, hn, nx (4H).
+constexpr int kGruK = kGruH + 16;
+constexpr int kGruRows = 4 * kGruH;
+// Per-port recurrent state (floats): h [2][H] in FP32 (read / write halves
+// alternate by step parity), then the same two halves as BF16 pairs (the
+// tensor-core operand, H / 2 words each), then the attachment voltage of the
+// last step and a "seen" mark.
+constexpr int kPortHBf = 2 * kGruH;            // offset of the BF16 halves
+constexpr int kPortVPrev = kPortHBf + kGruH;    // offset of (v_prev, seen)
+constexpr int kPortStride = kPortVPrev + 4;
+
+// Launch shape of the kernel variant with ports: at most BC_PORT_MAX_THREADS
+// threads per tile, register budget for BC_PORT_MIN_CTAS resident tiles per SM.
+#ifndef BC_PORT_MAX_THREADS
+#define BC_PORT_MAX_THREADS 384
+#endif
+#ifndef BC_PORT_MIN_CTAS
+#define BC_PORT_MIN_CTAS 2
+#endif
+
+// Per-step staging of a port inside the tile's scratch: the GRU inputs, the
+// endpoint node and the factor that turns y into the row's right-hand side.
+struct PortStage {
+  float x[4];
+  int32_t node;
+  float coef;
+  int32_t pad[2];
+};
+
+// Inference weights of a plan (global memory, read through L1).
+struct GruWeights {
+  uint32_t wext[kGruRows * kGruK / 2];  // BF16 pairs, row-major [4H][K]
+  float wo[kGruH];
+  float bo;
+  float v_scale;    // mV: voltage input = (V_att - e) / v_scale
+  float y_scale;    // mV: port current = g (e + y_scale y - V_end)
+  float env_v_lo;   // envelope of V_att - e, mV
+  float env_v_hi;
+  float env_dvdt;   // bound of |dV_att/dt|, mV/ms
+  float pad[2];
+};
+
+// A port: the stand-in for a removed subtree.  node: tile-local endpoint node it
+// feeds; att: tile-local node of the attachment CV; cell: batch cell id;
+// id: plan port id (recurrent state row); its stimulus pulses are
+// stim_begin .. stim_end of the plan's port-pulse array (amp in nA).
+struct PortRec {
+  int32_t node;
+  int32_t att;
+  int32_t cell;
+  int32_t id;
+  int32_t stim_begin;
+  int32_t stim_end;
+  double g;        // uS
+  double e;        // mV
+  float feat[2];
 };
 
 struct PulseRec {
@@ -163,18 +239,24 @@ struct LaunchArgs {
   int64_t* rec_step;
   unsigned long long* rec_count;
   int64_t rec_cap;
+  // subtree-surrogate ports
+  const PortRec* ports;
+  const PulseRec* port_pulses;
+  float* port_h;               // [n_ports][kPortStride]
+  int32_t* port_flags;         // [n_cells] envelope exits
+  const GruWeights* gru;
 };
 
 // Host-callable launchers implemented in bc_kernels.cu.
-// extra: the plan uses synapses, a network, or a mechanism of the out-of-line set
-// (classic HH Na / K, M current); otherwise the kernel variant without that code
-// runs.
-int launch_tiles(const LaunchArgs& a, int precision, bool smem, int threads, size_t smem_bytes, bool extra,
+// variant: 0 = the lean kernel; 1 = the plan uses synapses, a network, or a
+// mechanism of the out-of-line set (classic HH Na / K, M current); 2 = as 1 plus
+// subtree-surrogate ports.
+int launch_tiles(const LaunchArgs& a, int precision, bool smem, int threads, size_t smem_bytes, int variant,
                  void* stream);
 // Kernel-node parameters of the same launch for a CUDA graph.  kernelParams
 // points at *hold, which points at *a: both must stay valid until the graph
 // call that consumes the parameters returns (it copies the argument).
-int tile_node_params(const LaunchArgs* a, int precision, bool smem, int threads, size_t smem_bytes, bool extra,
+int tile_node_params(const LaunchArgs* a, int precision, bool smem, int threads, size_t smem_bytes, int variant,
                      cudaKernelNodeParams* np, const LaunchArgs** hold);
 int launch_reset_impl(const LaunchArgs& a, int precision, int threads, const double* vinit, const int64_t* voff,
                       void* stream);

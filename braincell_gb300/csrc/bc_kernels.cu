@@ -27,6 +27,7 @@
 #include <algorithm>
 #include <cstdint>
 
+#include "bc_gru.cuh"
 #include "bc_internal.h"
 #include "bc_mech.cuh"
 
@@ -1022,14 +1023,138 @@ __device__ __forceinline__ void backsub_phase(const TileView<Real>& tv, int p, i
   }
 }
 
+// ------------------------------------------------------------ surrogate ports
+// One GRU step per port of the tile and the port's terms in the row of step m
+// (the port variant only).  The port injects I = g (e + y_scale y - V_end) into
+// its endpoint row: the -g V_end part implicitly (diagonal), the rest at V^m.
+// Inputs: ((V_att - e) / v_scale, S / 0.1 nA, feat0, feat1) with V_att the
+// attachment CV's voltage at the start of step m and S the port's stimulus
+// pulses active at step m (nA).
+//
+// Pass A (a thread per port) stages the inputs, checks the envelope (an input
+// outside it flags the port's cell for the full solve) and adds the row terms
+// that do not depend on y.  Pass B, after a barrier, deals work items (M tile of
+// 16 ports, group jb of 8 hidden units) round-robin over the warps; lane
+// (g, tq) holds ports g and g + 8 of the tile and units 8 jb + 2 tq, +1.  The
+// hidden state is read from the half (m & 1) and written to the other half, so
+// items do not race; each item adds its part of y's current atomically.
+constexpr float kPortStimScale = 0.1f;  // nA
+
+template <typename Real>
+__device__ __forceinline__ void port_stage(const PortRec* ports, int n_ports, const PulseRec* stim, float* port_h,
+                                          int32_t* flags, const GruWeights* __restrict__ W, const Pair<Real>* v,
+                                          Pair<Real>* dr, PortStage* stage, int64_t m, Real dt, int tid, int T) {
+  for (int q = tid; q < n_ports; q += T) {
+    const PortRec r = ports[q];
+    float* hp = port_h + size_t(r.id) * kPortStride;
+    const float2 pv = *reinterpret_cast<const float2*>(hp + kPortVPrev);
+    const Pair<Real> va = v[r.att], ve = v[r.node];
+    float S = 0.f;
+    for (int k = r.stim_begin; k < r.stim_end; ++k) {
+      const PulseRec pr = stim[k];
+      if (m >= pr.on_step && m < pr.off_step) S += float(pr.amp);
+    }
+    const float vatt = float(va.x + va.y);
+    const float dv = vatt - float(r.e);
+    const float rate = pv.y != 0.f ? fabsf(vatt - pv.x) / float(dt) : 0.f;
+    if (dv < W->env_v_lo || dv > W->env_v_hi || rate > W->env_dvdt) flags[r.cell] = 1;
+    *reinterpret_cast<float2*>(hp + kPortVPrev) = make_float2(vatt, 1.f);
+    const Real gg = Real(r.g) * Real(1e-3) * dt;  // uS -> row units (1 uF dummy capacitance)
+    Pair<Real> row = dr[r.node];
+    row.x += gg;
+    row.y += gg * (Real(r.e) + Real(W->y_scale) * Real(W->bo) - (ve.x + ve.y));
+    dr[r.node] = row;
+    PortStage st;
+    st.x[0] = dv / W->v_scale;
+    st.x[1] = S * (1.0f / kPortStimScale);
+    st.x[2] = r.feat[0];
+    st.x[3] = r.feat[1];
+    st.node = r.node;
+    st.coef = float(gg) * W->y_scale;
+    st.pad[0] = r.id;
+    st.pad[1] = 0;
+    stage[q] = st;
+  }
+}
+
+template <typename Real>
+__device__ __forceinline__ void port_gru(const PortStage* stage, int n_ports, float* port_h,
+                                        const GruWeights* __restrict__ W, Pair<Real>* dr, int64_t m, int warp,
+                                        int n_warps, int lane) {
+  const int g = lane >> 2, tq = lane & 3;
+  const int rd = int(m & 1), wr = rd ^ 1;
+  const int n_items = ((n_ports + 15) >> 4) * 8;
+  for (int it = warp; it < n_items; it += n_warps) {
+    const int mt = it >> 3, jb = it & 7;
+    const int qa = mt * 16 + g, qb = qa + 8;
+    const bool oka = qa < n_ports, okb = qb < n_ports;
+    const int j0 = jb * 8 + 2 * tq;
+    float* ha = oka ? port_h + size_t(stage[qa].pad[0]) * kPortStride : nullptr;
+    float* hb = okb ? port_h + size_t(stage[qb].pad[0]) * kPortStride : nullptr;
+    // A operand straight from the BF16 halves; the FP32 values of this lane's units
+    uint32_t ah[4][4];
+    const uint32_t* ba = oka ? reinterpret_cast<const uint32_t*>(ha + kPortHBf) + rd * (kGruH / 2) : nullptr;
+    const uint32_t* bb = okb ? reinterpret_cast<const uint32_t*>(hb + kPortHBf) + rd * (kGruH / 2) : nullptr;
+#pragma unroll
+    for (int kk = 0; kk < 4; ++kk) {
+      ah[kk][0] = oka ? ba[kk * 8 + tq] : 0u;
+      ah[kk][1] = okb ? bb[kk * 8 + tq] : 0u;
+      ah[kk][2] = oka ? ba[kk * 8 + 4 + tq] : 0u;
+      ah[kk][3] = okb ? bb[kk * 8 + 4 + tq] : 0u;
+    }
+    const float2 hoa = oka ? *reinterpret_cast<const float2*>(ha + rd * kGruH + j0) : make_float2(0.f, 0.f);
+    const float2 hob = okb ? *reinterpret_cast<const float2*>(hb + rd * kGruH + j0) : make_float2(0.f, 0.f);
+    uint32_t ax[4];
+    {
+      const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+      const float4 xa = oka ? *reinterpret_cast<const float4*>(stage[qa].x) : z4;
+      const float4 xb = okb ? *reinterpret_cast<const float4*>(stage[qb].x) : z4;
+      const float fa[4] = {xa.x, xa.y, xa.z, xa.w}, fb[4] = {xb.x, xb.y, xb.z, xb.w};
+      xblock_frag(fa, fb, tq, ax);
+    }
+    float acc[4][4];
+    gru_preact(W->wext, jb, g, tq, ah, ax, acc);
+    const float2 wo = *reinterpret_cast<const float2*>(W->wo + j0);
+    const GruGate G0 = gru_gate(acc[0][0], acc[1][0], acc[2][0], acc[3][0], hoa.x);
+    const GruGate G1 = gru_gate(acc[0][1], acc[1][1], acc[2][1], acc[3][1], hoa.y);
+    const GruGate G2 = gru_gate(acc[0][2], acc[1][2], acc[2][2], acc[3][2], hob.x);
+    const GruGate G3 = gru_gate(acc[0][3], acc[1][3], acc[2][3], acc[3][3], hob.y);
+    if (oka) {
+      *reinterpret_cast<float2*>(ha + wr * kGruH + j0) = make_float2(G0.h_new, G1.h_new);
+      reinterpret_cast<uint32_t*>(ha + kPortHBf)[wr * (kGruH / 2) + j0 / 2] = pack_bf16(G0.h_new, G1.h_new);
+    }
+    if (okb) {
+      *reinterpret_cast<float2*>(hb + wr * kGruH + j0) = make_float2(G2.h_new, G3.h_new);
+      reinterpret_cast<uint32_t*>(hb + kPortHBf)[wr * (kGruH / 2) + j0 / 2] = pack_bf16(G2.h_new, G3.h_new);
+    }
+    float ysa = wo.x * G0.h_new + wo.y * G1.h_new;
+    float ysb = wo.x * G2.h_new + wo.y * G3.h_new;
+    ysa += __shfl_xor_sync(kFullMask, ysa, 1);
+    ysa += __shfl_xor_sync(kFullMask, ysa, 2);
+    ysb += __shfl_xor_sync(kFullMask, ysb, 1);
+    ysb += __shfl_xor_sync(kFullMask, ysb, 2);
+    if (tq == 0) {
+      if (oka) atomicAdd(&dr[stage[qa].node].y, Real(stage[qa].coef) * Real(ysa));
+      if (okb) atomicAdd(&dr[stage[qb].node].y, Real(stage[qb].coef) * Real(ysb));
+    }
+  }
+}
+
 template <typename Real>
 __device__ __forceinline__ bool is_finite_real(Real x) {
   return isfinite(x);
 }
 
 // ------------------------------------------------------------------ the step kernel
-template <typename Real, bool kSmem, bool kExtra>
-__global__ void __launch_bounds__(1024) tile_step_kernel(LaunchArgs a) {
+// kVar: 0 = lean (no optional mechanism), 1 = extra (synapses, network,
+// out-of-line channels), 2 = extra + subtree-surrogate ports.
+// The port variant runs at most BC_PORT_MAX_THREADS threads per CTA and asks for
+// BC_PORT_MIN_CTAS resident CTAs per SM (its register budget).
+template <typename Real, bool kSmem, int kVar>
+__global__ void __launch_bounds__(kVar == 2 ? BC_PORT_MAX_THREADS : 1024, kVar == 2 ? BC_PORT_MIN_CTAS : 1)
+    tile_step_kernel(LaunchArgs a) {
+  constexpr bool kExtra = kVar >= 1;
+  constexpr bool kPorts = kVar == 2;
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) uint64_t bar;
   __shared__ int s_status;
@@ -1104,6 +1229,17 @@ __global__ void __launch_bounds__(1024) tile_step_kernel(LaunchArgs a) {
   if (tv.has_src)
     for (int c = tid; c < tv.n_cells; c += T) tv.stamp[c] = -1;
   __syncthreads();
+  PortStage* pstage = nullptr;
+  if constexpr (kPorts) {
+    if (td.n_ports > 0) {
+      pstage = reinterpret_cast<PortStage*>(scratch + td.off_pstage);
+      port_stage<Real>(a.ports + td.port_offset, td.n_ports, a.port_pulses, a.port_h, a.port_flags, a.gru, tv.v,
+                       tv.dr, pstage, a.step0, dt, tid, T);
+      __syncthreads();
+      port_gru<Real>(pstage, td.n_ports, a.port_h, a.gru, tv.dr, a.step0, warp, n_warps, lane);
+      __syncthreads();
+    }
+  }
 
 #ifdef BC_PHASE_TIMERS
   unsigned long long tm[4] = {0, 0, 0, 0};
@@ -1208,6 +1344,17 @@ __global__ void __launch_bounds__(1024) tile_step_kernel(LaunchArgs a) {
           }
         }
     BC_TICK(2);
+    if constexpr (kPorts) {
+      if (td.n_ports > 0 && !last) {
+        port_stage<Real>(a.ports + td.port_offset, td.n_ports, a.port_pulses, a.port_h, a.port_flags, a.gru, tv.v,
+                         tv.dr, pstage, step + 1, dt, tid, T);
+        __syncthreads();
+        BC_TICK(2);
+        port_gru<Real>(pstage, td.n_ports, a.port_h, a.gru, tv.dr, step + 1, warp, n_warps, lane);
+        __syncthreads();
+      }
+    }
+    BC_TICK(3);
   }
 #ifdef BC_PHASE_TIMERS
   if (threadIdx.x == 0 && a.timers)
@@ -1272,9 +1419,9 @@ __global__ void view_kernel(unsigned char* blob, unsigned char* state, const int
 }
 
 // ------------------------------------------------------------------ launchers
-template <typename Real, bool kSmem, bool kExtra>
+template <typename Real, bool kSmem, int kVar>
 static int launch_impl(const LaunchArgs& a, int threads, size_t smem_bytes, cudaStream_t st) {
-  auto k = tile_step_kernel<Real, kSmem, kExtra>;
+  auto k = tile_step_kernel<Real, kSmem, kVar>;
   if (kSmem) {
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem_bytes));
     if (e != cudaSuccess) return int(e);
@@ -1284,30 +1431,36 @@ static int launch_impl(const LaunchArgs& a, int threads, size_t smem_bytes, cuda
   return int(cudaGetLastError());
 }
 
-template <bool kExtra>
+template <int kVar>
 static int launch_tiles_x(const LaunchArgs& a, int precision, bool smem, int threads, size_t smem_bytes,
                           cudaStream_t st) {
   if (precision == BC_PREC_F64)
-    return smem ? launch_impl<double, true, kExtra>(a, threads, smem_bytes, st)
-                : launch_impl<double, false, kExtra>(a, threads, smem_bytes, st);
-  return smem ? launch_impl<float, true, kExtra>(a, threads, smem_bytes, st)
-              : launch_impl<float, false, kExtra>(a, threads, smem_bytes, st);
+    return smem ? launch_impl<double, true, kVar>(a, threads, smem_bytes, st)
+                : launch_impl<double, false, kVar>(a, threads, smem_bytes, st);
+  return smem ? launch_impl<float, true, kVar>(a, threads, smem_bytes, st)
+              : launch_impl<float, false, kVar>(a, threads, smem_bytes, st);
 }
 
-int launch_tiles(const LaunchArgs& a, int precision, bool smem, int threads, size_t smem_bytes, bool extra,
+int launch_tiles(const LaunchArgs& a, int precision, bool smem, int threads, size_t smem_bytes, int variant,
                  void* stream) {
   if (a.n_tiles <= 0) return 0;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  return extra ? launch_tiles_x<true>(a, precision, smem, threads, smem_bytes, st)
-               : launch_tiles_x<false>(a, precision, smem, threads, smem_bytes, st);
+  switch (variant) {
+    case 0:
+      return launch_tiles_x<0>(a, precision, smem, threads, smem_bytes, st);
+    case 1:
+      return launch_tiles_x<1>(a, precision, smem, threads, smem_bytes, st);
+    default:
+      return launch_tiles_x<2>(a, precision, smem, threads, smem_bytes, st);
+  }
 }
 
 // Kernel-node parameters of one tile launch for a CUDA graph: the same kernel,
 // grid, block and shared memory as launch_tiles; `*a` is copied by the graph call
 // that consumes the parameters.
-template <typename Real, bool kSmem, bool kExtra>
+template <typename Real, bool kSmem, int kVar>
 static int node_impl(const LaunchArgs* a, int threads, size_t smem_bytes, cudaKernelNodeParams* np) {
-  auto k = tile_step_kernel<Real, kSmem, kExtra>;
+  auto k = tile_step_kernel<Real, kSmem, kVar>;
   if (kSmem) {
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem_bytes));
     if (e != cudaSuccess) return int(e);
@@ -1320,24 +1473,30 @@ static int node_impl(const LaunchArgs* a, int threads, size_t smem_bytes, cudaKe
   return 0;
 }
 
-int tile_node_params(const LaunchArgs* a, int precision, bool smem, int threads, size_t smem_bytes, bool extra,
+template <int kVar>
+static int node_x(const LaunchArgs* a, int precision, bool smem, int threads, size_t smem_bytes,
+                  cudaKernelNodeParams* np) {
+  if (precision == BC_PREC_F64)
+    return smem ? node_impl<double, true, kVar>(a, threads, smem_bytes, np)
+                : node_impl<double, false, kVar>(a, threads, smem_bytes, np);
+  return smem ? node_impl<float, true, kVar>(a, threads, smem_bytes, np)
+              : node_impl<float, false, kVar>(a, threads, smem_bytes, np);
+}
+
+int tile_node_params(const LaunchArgs* a, int precision, bool smem, int threads, size_t smem_bytes, int variant,
                      cudaKernelNodeParams* np, const LaunchArgs** hold) {
   *hold = a;
   int e;
-  if (precision == BC_PREC_F64) {
-    if (extra)
-      e = smem ? node_impl<double, true, true>(a, threads, smem_bytes, np)
-               : node_impl<double, false, true>(a, threads, smem_bytes, np);
-    else
-      e = smem ? node_impl<double, true, false>(a, threads, smem_bytes, np)
-               : node_impl<double, false, false>(a, threads, smem_bytes, np);
-  } else {
-    if (extra)
-      e = smem ? node_impl<float, true, true>(a, threads, smem_bytes, np)
-               : node_impl<float, false, true>(a, threads, smem_bytes, np);
-    else
-      e = smem ? node_impl<float, true, false>(a, threads, smem_bytes, np)
-               : node_impl<float, false, false>(a, threads, smem_bytes, np);
+  switch (variant) {
+    case 0:
+      e = node_x<0>(a, precision, smem, threads, smem_bytes, np);
+      break;
+    case 1:
+      e = node_x<1>(a, precision, smem, threads, smem_bytes, np);
+      break;
+    default:
+      e = node_x<2>(a, precision, smem, threads, smem_bytes, np);
+      break;
   }
   np->kernelParams = reinterpret_cast<void**>(const_cast<LaunchArgs**>(hold));
   return e;

@@ -100,6 +100,17 @@ struct bc_plan {
   int64_t* d_rec_step = nullptr;
   unsigned long long* d_rec_count = nullptr;  // [0] produced, [1] delivered
   int64_t rec_cap = 0;
+  // subtree-surrogate ports: records (tile order), stimulus pulses (nA), GRU
+  int64_t n_ports = 0;
+  std::vector<bc::PortRec> ports;
+  std::vector<bc::PulseRec> port_pulses;
+  double port_pulses_dt = -1.0;
+  bc::PortRec* d_ports = nullptr;
+  bc::PulseRec* d_port_pulses = nullptr;
+  float* d_port_h = nullptr;
+  int32_t* d_port_flags = nullptr;
+  bc::GruWeights* d_gru = nullptr;
+  bool gru_set = false;
   // device buffers
   unsigned char* d_blob = nullptr;
   size_t blob_bytes = 0;
@@ -171,6 +182,11 @@ static void free_plan(bc_plan* p) {
   cudaFree(p->d_rec_cell);
   cudaFree(p->d_rec_step);
   cudaFree(p->d_rec_count);
+  cudaFree(p->d_ports);
+  cudaFree(p->d_port_pulses);
+  cudaFree(p->d_port_h);
+  cudaFree(p->d_port_flags);
+  cudaFree(p->d_gru);
   for (int k = 0; k < 2; ++k) {
     if (p->aux[k]) cudaStreamDestroy(p->aux[k]);
     if (p->ev_join[k]) cudaEventDestroy(p->ev_join[k]);
@@ -272,6 +288,8 @@ struct TileOut {
   std::vector<unsigned char> blob;
   std::vector<double> vinit;
   std::vector<PulseRec> pulses;
+  std::vector<PortRec> ports;         // stim_begin / stim_end relative to port_pulses
+  std::vector<PulseRec> port_pulses;  // amp in nA
   std::vector<std::pair<int64_t, int32_t>> cv_local;  // (global cv id, local node)
   std::vector<uint32_t> cv_mech;
   int64_t crit = 0;
@@ -288,6 +306,9 @@ struct BuildCtx {
   const std::vector<std::vector<int32_t>>* probe_node;
   const std::vector<std::vector<std::pair<int64_t, int32_t>>>* cell_syns;  // per cell: (synapse id, node)
   const std::vector<char>* is_src;                                        // per cell: source of a connection
+  // per cell: (port id, endpoint node, attachment CV node); port pulses by port
+  const std::vector<std::vector<std::array<int32_t, 3>>>* cell_ports;
+  const std::vector<std::vector<int64_t>>* port_pulse_ids;
   int precision;
   int state_slots;
   int lane_nodes;  // nodes a lane walks serially in a warp slot
@@ -589,6 +610,13 @@ static bc_status build_tile(const BuildCtx& cx, const TileBuild& tb, int T, Tile
     d.off_stamp = int32_t(so);
     so = align16(so + cell_list.size() * 4);
   }
+  size_t n_tile_ports = 0;
+  for (size_t li = 0; li < cell_list.size(); ++li) n_tile_ports += (*cx.cell_ports)[cell_list[li]].size();
+  d.off_pstage = -1;
+  if (n_tile_ports > 0) {
+    d.off_pstage = int32_t(so);
+    so = align16(so + n_tile_ports * sizeof(PortStage));
+  }
   d.scratch_bytes = int32_t(so);
   d.n_nodes = int32_t(N);
   d.n_real_nodes = int32_t(n_real);
@@ -700,6 +728,33 @@ static bc_status build_tile(const BuildCtx& cx, const TileBuild& tb, int T, Tile
     std::memcpy(b.data() + d.off_spec, spec.data(), spec.size() * 2);
     if (!specs.empty()) std::memcpy(b.data() + d.off_specs, specs.data(), specs.size() * sizeof(SpecRec));
   }
+  // surrogate ports of the tile's cells (the plan assigns port_offset)
+  for (size_t li = 0; li < cell_list.size(); ++li) {
+    const int64_t c = cell_list[li];
+    for (const auto& pt : (*cx.cell_ports)[c]) {
+      PortRec r{};
+      r.node = node_tile[li][pt[1]];
+      r.att = node_tile[li][pt[2]];
+      r.cell = int32_t(c);
+      r.id = pt[0];
+      r.g = s.port_g[pt[0]];
+      r.e = s.port_e[pt[0]];
+      r.feat[0] = float(s.port_feat[2 * size_t(pt[0])]);
+      r.feat[1] = float(s.port_feat[2 * size_t(pt[0]) + 1]);
+      r.stim_begin = int32_t(out.port_pulses.size());
+      for (int64_t q : (*cx.port_pulse_ids)[pt[0]]) {
+        PulseRec pr{};
+        pr.node = r.node;
+        pr.amp = s.port_pulse_amp[q];
+        pr.t_on = s.port_pulse_t_on[q];
+        pr.t_off = s.port_pulse_t_off[q];
+        out.port_pulses.push_back(pr);
+      }
+      r.stim_end = int32_t(out.port_pulses.size());
+      out.ports.push_back(r);
+    }
+  }
+  d.n_ports = int32_t(out.ports.size());
   std::memcpy(b.data() + d.off_chains, chains.data(), chains.size() * sizeof(ChainRec));
   if (!slots.empty()) std::memcpy(b.data() + d.off_slots, slots.data(), slots.size() * sizeof(SlotRec));
   std::memcpy(b.data() + d.off_phase, phase_ptr.data(), phase_ptr.size() * 4);
@@ -731,6 +786,16 @@ static int64_t first_step_at(double t, double dt) {
 }
 
 static bc_status update_pulses(bc_plan* p, double dt, void* stream) {
+  if (!p->port_pulses.empty() && p->port_pulses_dt != dt) {
+    for (auto& pr : p->port_pulses) {
+      pr.on_step = first_step_at(pr.t_on, dt);
+      pr.off_step = first_step_at(pr.t_off, dt);
+    }
+    BC_CUDA(cudaMemcpyAsync(p->d_port_pulses, p->port_pulses.data(), p->port_pulses.size() * sizeof(PulseRec),
+                            cudaMemcpyHostToDevice, static_cast<cudaStream_t>(stream)));
+    BC_CUDA(cudaStreamSynchronize(static_cast<cudaStream_t>(stream)));
+    p->port_pulses_dt = dt;
+  }
   if (p->pulses.empty() || p->pulses_dt == dt) return BC_OK;
   for (auto& pr : p->pulses) {
     pr.on_step = first_step_at(pr.t_on, dt);
@@ -761,6 +826,9 @@ static bc_status ensure_traces(bc_plan* p, int64_t records, void* stream) {
   return BC_OK;
 }
 
+// Kernel variant of a plan (see launch_tiles).
+static int kernel_variant(const bc_plan* p) { return p->n_ports > 0 ? 2 : (p->extra ? 1 : 0); }
+
 static LaunchArgs base_args(bc_plan* p) {
   LaunchArgs a{};
   a.blob = p->d_blob;
@@ -789,6 +857,11 @@ static LaunchArgs base_args(bc_plan* p) {
   a.rec_step = p->d_rec_step;
   a.rec_count = p->d_rec_count;
   a.rec_cap = p->rec_cap;
+  a.ports = p->d_ports;
+  a.port_pulses = p->d_port_pulses;
+  a.port_h = p->d_port_h;
+  a.port_flags = p->d_port_flags;
+  a.gru = p->d_gru;
   return a;
 }
 
@@ -866,7 +939,7 @@ static bc_status enqueue_run_graph(bc_plan* p, int64_t n_steps, double dt, void*
         const LaunchClass& lcz = p->classes[ci];
         cudaKernelNodeParams np{};
         const LaunchArgs* hold = nullptr;
-        int e = tile_node_params(&args[size_t(j) * nc + ci], p->precision, lcz.smem, lcz.threads, lcz.smem_bytes, p->extra, &np,
+        int e = tile_node_params(&args[size_t(j) * nc + ci], p->precision, lcz.smem, lcz.threads, lcz.smem_bytes, kernel_variant(p), &np,
                                  &hold);
         if (e) return fail(BC_ERR_CUDA, std::string("graph node: ") + cudaGetErrorString(cudaError_t(e)));
         cudaGraphNode_t dep = j > 0 ? p->graph_nodes[size_t(j - 1) * nc + ci] : nullptr;
@@ -883,7 +956,7 @@ static bc_status enqueue_run_graph(bc_plan* p, int64_t n_steps, double dt, void*
         const LaunchClass& lcz = p->classes[ci];
         cudaKernelNodeParams np{};
         const LaunchArgs* hold = nullptr;
-        int e = tile_node_params(&args[size_t(j) * nc + ci], p->precision, lcz.smem, lcz.threads, lcz.smem_bytes, p->extra, &np,
+        int e = tile_node_params(&args[size_t(j) * nc + ci], p->precision, lcz.smem, lcz.threads, lcz.smem_bytes, kernel_variant(p), &np,
                                  &hold);
         if (e) return fail(BC_ERR_CUDA, std::string("graph node: ") + cudaGetErrorString(cudaError_t(e)));
         BC_CUDA(cudaGraphExecKernelNodeSetParams(p->graph_exec, p->graph_nodes[size_t(j) * nc + ci], &np));
@@ -896,6 +969,7 @@ static bc_status enqueue_run_graph(bc_plan* p, int64_t n_steps, double dt, void*
 static bc_status enqueue_run(bc_plan* p, int64_t n_steps, double dt, void* stream) {
   if (n_steps < 0) return fail(BC_ERR_INVALID, "n_steps must be >= 0");
   if (!(dt > 0.0) || !std::isfinite(dt)) return fail(BC_ERR_INVALID, "dt must be a positive finite number (ms)");
+  if (p->n_ports > 0 && !p->gru_set) return fail(BC_ERR_INVALID, "the plan has surrogate ports: call bc_surrogate_set first");
   bc_status st = update_pulses(p, dt, stream);
   if (st != BC_OK) return st;
   const int64_t recs = p->record_every > 0 ? (p->step + n_steps - p->trace_origin) / p->record_every : 0;
@@ -931,7 +1005,7 @@ static bc_status enqueue_run(bc_plan* p, int64_t n_steps, double dt, void* strea
       }
       a.tiles = p->d_tiles + lcz.first;
       a.n_tiles = lcz.count;
-      int e = launch_tiles(a, p->precision, lcz.smem, lcz.threads, lcz.smem_bytes, p->extra, st);
+      int e = launch_tiles(a, p->precision, lcz.smem, lcz.threads, lcz.smem_bytes, kernel_variant(p), st);
       if (e) return fail(BC_ERR_CUDA, std::string("tile kernel launch: ") + cudaGetErrorString(cudaError_t(e)));
       if (ci > 0) {
         BC_CUDA(cudaEventRecord(p->ev_join[ci - 1], st));
@@ -1113,6 +1187,58 @@ bc_status bc_plan_create(const bc_batch_spec* spec, const bc_plan_options* opts_
       return fail(BC_ERR_INVALID, "connection delay must be >= 0 ms and weight finite");
     }
   }
+  // ---------------------------------------------------- surrogate ports
+  std::vector<std::vector<std::array<int32_t, 3>>> cell_ports(s.n_cells);
+  std::vector<std::vector<int64_t>> port_pulse_ids(std::max<int64_t>(s.n_ports, 0));
+  if (s.n_ports < 0 || s.n_port_pulses < 0 || s.n_ports >= (int64_t(1) << 31)) {
+    delete p;
+    return fail(BC_ERR_INVALID, "n_ports and n_port_pulses must be >= 0");
+  }
+  for (int64_t k = 0; k < s.n_ports; ++k) {
+    const int64_t c = s.port_cell[k];
+    if (c < 0 || c >= s.n_cells) {
+      delete p;
+      return fail(BC_ERR_INVALID, "port_cell out of range");
+    }
+    if (!(s.port_g[k] > 0.0) || !std::isfinite(s.port_g[k]) || !std::isfinite(s.port_e[k]) ||
+        !std::isfinite(s.port_feat[2 * k]) || !std::isfinite(s.port_feat[2 * k + 1])) {
+      delete p;
+      return fail(BC_ERR_INVALID, "port g must be > 0 and e, features finite");
+    }
+    const int32_t br = s.port_branch[k];
+    const int32_t nb = int32_t(s.cell_branch_offsets[c + 1] - s.cell_branch_offsets[c]);
+    if (br < 0 || br >= nb) {
+      delete p;
+      return fail(BC_ERR_INVALID, "port_branch out of range");
+    }
+    const int32_t ncv = s.branch_ncv[s.cell_branch_offsets[c] + br];
+    const int32_t end = locate_node(s, c, cells[c], br, 1.0);
+    const int32_t att = locate_node(s, c, cells[c], br, 1.0 - 0.5 / double(ncv));
+    if (end < 0 || att < 0 || cells[c].region[att] < 0) {
+      delete p;
+      return fail(BC_ERR_INVALID, "port location not found");
+    }
+    for (const auto& q : cell_ports[c])
+      if (q[1] == end) {
+        delete p;
+        return fail(BC_ERR_INVALID, "two ports at the same branch end are not supported");
+      }
+    cell_ports[c].push_back({int32_t(k), end, att});
+  }
+  for (int64_t q = 0; q < s.n_port_pulses; ++q) {
+    const int64_t k = s.port_pulse_port[q];
+    if (k < 0 || k >= s.n_ports) {
+      delete p;
+      return fail(BC_ERR_INVALID, "port_pulse_port out of range");
+    }
+    if (!(s.port_pulse_t_off[q] >= s.port_pulse_t_on[q]) || !std::isfinite(s.port_pulse_amp[q])) {
+      delete p;
+      return fail(BC_ERR_INVALID, "port pulse needs t_off >= t_on and a finite amplitude");
+    }
+    port_pulse_ids[k].push_back(q);
+  }
+  p->n_ports = s.n_ports;
+  p->extra = p->extra || s.n_ports > 0;
   // every cell of a network records its spikes (the output of a network run);
   // only cells with connections have events to deliver
   if (s.n_connections > 0) std::fill(is_src.begin(), is_src.end(), char(1));
@@ -1163,10 +1289,15 @@ bc_status bc_plan_create(const bc_batch_spec* spec, const bc_plan_options* opts_
   // cell per shared-memory tile, 2 = global-memory tiles (too big for shared memory).
   const int T_packed = opts.threads_per_tile > 0 ? opts.threads_per_tile : 128;
   const int T_big = opts.threads_big > 0 ? opts.threads_big : 256;
-  const int T_glob = opts.threads_global > 0 ? opts.threads_global : 512;
+  const int T_glob = opts.threads_global > 0 ? opts.threads_global : (s.n_ports > 0 ? BC_PORT_MAX_THREADS : 512);
   if (T_big % 32 || T_big > 1024 || T_glob % 32 || T_glob > 1024) {
     delete p;
     return fail(BC_ERR_INVALID, "thread counts must be multiples of 32 up to 1024");
+  }
+  if (s.n_ports > 0 && (T_packed > BC_PORT_MAX_THREADS || T_big > BC_PORT_MAX_THREADS || T_glob > BC_PORT_MAX_THREADS)) {
+    delete p;
+    return fail(BC_ERR_INVALID, "plans with surrogate ports run at most " + std::to_string(BC_PORT_MAX_THREADS) +
+                                    " threads per tile");
   }
   const int class_threads[3] = {T_packed, T_big, T_glob};
   p->threads = T_packed;
@@ -1207,7 +1338,7 @@ bc_status bc_plan_create(const bc_batch_spec* spec, const bc_plan_options* opts_
     if (tile_nodes - nn > 0) room.emplace(tile_nodes - nn, builds.size() - 1);
   }
   BuildCtx cx{&s, &cells, &sched, &cv_base, &cell_pulses, &cell_probes, &pulse_node, &probe_node, &cell_syns, &is_src,
-              p->precision, S, p->lane_nodes};
+              &cell_ports, &port_pulse_ids, p->precision, S, p->lane_nodes};
   std::vector<TileOut> outs;
   outs.reserve(builds.size());
   // Packed tiles: tile_nodes sets how many CTAs share an SM (by the per-node
@@ -1307,6 +1438,14 @@ bc_status bc_plan_create(const bc_batch_spec* spec, const bc_plan_options* opts_
     d.pulse_offset = int64_t(p->pulses.size());
     d.n_pulses = int32_t(to.pulses.size());
     p->pulses.insert(p->pulses.end(), to.pulses.begin(), to.pulses.end());
+    d.port_offset = int64_t(p->ports.size());
+    d.n_ports = int32_t(to.ports.size());
+    for (PortRec r : to.ports) {
+      r.stim_begin += int32_t(p->port_pulses.size());
+      r.stim_end += int32_t(p->port_pulses.size());
+      p->ports.push_back(r);
+    }
+    p->port_pulses.insert(p->port_pulses.end(), to.port_pulses.begin(), to.port_pulses.end());
     vinit_off.push_back(int64_t(vinit_total));
     vinit_total += to.vinit.size();
     for (size_t q = 0; q < to.cv_local.size(); ++q) {
@@ -1415,6 +1554,14 @@ bc_status bc_plan_create(const bc_batch_spec* spec, const bc_plan_options* opts_
     BC_TRY(dalloc(p, &p->d_rec_count, 2));
     BC_TRYC(cudaMemset(p->d_rec_count, 0, 2 * sizeof(unsigned long long)));
   }
+  if (p->n_ports > 0) {
+    BC_TRY(dalloc(p, &p->d_ports, p->ports.size()));
+    BC_TRY(dalloc(p, &p->d_port_pulses, std::max<size_t>(p->port_pulses.size(), 1)));
+    BC_TRY(dalloc(p, &p->d_port_h, size_t(p->n_ports) * kPortStride));
+    BC_TRY(dalloc(p, &p->d_port_flags, size_t(p->n_cells)));
+    BC_TRY(dalloc(p, &p->d_gru, 1));
+    BC_TRYC(cudaMemcpy(p->d_ports, p->ports.data(), p->ports.size() * sizeof(PortRec), cudaMemcpyHostToDevice));
+  }
   if (p->n_smem_tiles > 0 && p->smem_bytes + static_smem > smem_cap) {
     free_plan(p);
     return fail(BC_ERR_CAPACITY, "tile shared memory exceeds the device limit");
@@ -1505,6 +1652,10 @@ bc_status bc_reset(bc_plan_t p, void* stream) {
     BC_CUDA(cudaMemsetAsync(p->d_arrivals, 0,
                             size_t(p->arr_slots) * size_t(std::max<int64_t>(p->n_synapses, 1)) * p->real_size, st));
   BC_CUDA(cudaMemsetAsync(p->d_rec_count, 0, 2 * sizeof(unsigned long long), st));
+  if (p->n_ports > 0) {
+    BC_CUDA(cudaMemsetAsync(p->d_port_h, 0, size_t(p->n_ports) * kPortStride * sizeof(float), st));
+    BC_CUDA(cudaMemsetAsync(p->d_port_flags, 0, size_t(p->n_cells) * sizeof(int32_t), st));
+  }
   BC_CUDA(cudaStreamSynchronize(st));
   p->step = 0;
   p->trace_origin = 0;
@@ -1526,6 +1677,79 @@ bc_status bc_network_spikes(bc_plan_t p, int32_t* cells, int64_t* steps, int64_t
     BC_CUDA(cudaMemcpyAsync(steps, p->d_rec_step, size_t(m) * 8, cudaMemcpyDeviceToHost, s));
     BC_CUDA(cudaStreamSynchronize(s));
   }
+  return BC_OK;
+}
+
+// BF16 of a finite float, round to nearest even (as the device conversion).
+static uint16_t bf16_rne(float f) {
+  uint32_t u;
+  std::memcpy(&u, &f, 4);
+  u += 0x7fffu + ((u >> 16) & 1u);
+  return uint16_t(u >> 16);
+}
+
+bc_status bc_surrogate_set(bc_plan_t p, const float* params, const float* norm, void* stream) {
+  if (!p || !params || !norm) return fail(BC_ERR_INVALID, "null argument");
+  if (p->n_ports == 0) return fail(BC_ERR_INVALID, "the plan has no surrogate ports");
+  BC_NEED_DEVICE(p);
+  BC_CUDA(cudaSetDevice(p->device));
+  for (int k = 0; k < kGruNParam; ++k)
+    if (!std::isfinite(params[k])) return fail(BC_ERR_INVALID, "non-finite GRU parameter");
+  const float v_scale = norm[0], y_scale = norm[1], lo = norm[2], hi = norm[3], dvdt = norm[4];
+  if (!(v_scale > 0.f) || !std::isfinite(v_scale) || !std::isfinite(y_scale) || !(hi >= lo) || !(dvdt > 0.f))
+    return fail(BC_ERR_INVALID, "surrogate norm: v_scale > 0, finite y_scale, env_v_hi >= env_v_lo, env_dvdt > 0");
+  // the extended weight matrix, as gru_pack_kernel builds it for training
+  auto bf = [](float f) {
+    const uint32_t u = uint32_t(bf16_rne(f)) << 16;
+    float r;
+    std::memcpy(&r, &u, 4);
+    return r;
+  };
+  auto value = [&](int n, int k) -> float {
+    const int q = n / kGruH, u = n % kGruH;
+    if (k < kGruH) return q < 3 ? params[kGruOffWh + (q * kGruH + u) * kGruH + k] : 0.0f;
+    const int c = k - kGruH;
+    const int xrow = q == 0 ? u : q == 1 ? kGruH + u : 2 * kGruH + u;
+    if (c < 2 * kGruX) return q == 2 ? 0.0f : bf(params[kGruOffWx + xrow * kGruX + (c % kGruX)]);
+    if (c < 2 * kGruX + 2) {
+      const float bsum = q == 0   ? params[kGruOffBx + u] + params[kGruOffBh + u]
+                         : q == 1 ? params[kGruOffBx + kGruH + u] + params[kGruOffBh + kGruH + u]
+                         : q == 2 ? params[kGruOffBh + 2 * kGruH + u]
+                                  : params[kGruOffBx + 2 * kGruH + u];
+      const float hi = bf(bsum);
+      return c == 2 * kGruX ? hi : bsum - hi;
+    }
+    return 0.0f;
+  };
+  GruWeights w{};
+  for (int n = 0; n < kGruRows; ++n)
+    for (int k = 0; k < kGruK; k += 2)
+      w.wext[(n * kGruK + k) / 2] = uint32_t(bf16_rne(value(n, k))) | (uint32_t(bf16_rne(value(n, k + 1))) << 16);
+  std::memcpy(w.wo, params + kGruOffWo, sizeof(w.wo));
+  w.bo = params[kGruOffBo];
+  w.v_scale = v_scale;
+  w.y_scale = y_scale;
+  w.env_v_lo = lo;
+  w.env_v_hi = hi;
+  w.env_dvdt = dvdt;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  BC_CUDA(cudaMemcpyAsync(p->d_gru, &w, sizeof(w), cudaMemcpyHostToDevice, st));
+  BC_CUDA(cudaStreamSynchronize(st));
+  p->gru_set = true;
+  return BC_OK;
+}
+
+bc_status bc_surrogate_flags(bc_plan_t p, int32_t* flags, void* stream) {
+  if (!p || !flags) return fail(BC_ERR_INVALID, "null argument");
+  if (p->n_ports == 0) {
+    std::fill(flags, flags + p->n_cells, 0);
+    return BC_OK;
+  }
+  BC_NEED_DEVICE(p);
+  BC_CUDA(cudaSetDevice(p->device));
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  BC_CUDA(cudaMemcpyAsync(flags, p->d_port_flags, size_t(p->n_cells) * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+  BC_CUDA(cudaStreamSynchronize(st));
   return BC_OK;
 }
 

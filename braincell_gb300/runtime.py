@@ -125,6 +125,25 @@ class Plan:
         _abi.check(self._lib.bc_run_timed(self._h, int(n_steps), float(dt), self._stream(stream), C.byref(ms)))
         return float(ms.value)
 
+    # ------------------------------------------------------------------ surrogate ports
+    def set_surrogate(self, theta, norm, stream=None) -> None:
+        """Give the plan's ports their GRU: flat FP32 parameters and the five norm
+        values (v_scale, y_scale, env_v_lo, env_v_hi, env_dvdt)."""
+        th = np.ascontiguousarray(theta, dtype=np.float32)
+        nm = np.ascontiguousarray(norm, dtype=np.float32)
+        if th.size != int(self._lib.bc_gru_nparam()) or nm.size != _abi.BC_SURROGATE_NORM:
+            raise ValueError("GRU parameter vector or norm of the wrong size.")
+        fp = C.POINTER(C.c_float)
+        _abi.check(self._lib.bc_surrogate_set(self._h, th.ctypes.data_as(fp), nm.ctypes.data_as(fp),
+                                              self._stream(stream)))
+
+    def surrogate_flags(self, stream=None) -> np.ndarray:
+        """Per cell: 1 when a port input left the envelope since the last reset."""
+        out = np.zeros(self.n_cells, dtype=np.int32)
+        _abi.check(self._lib.bc_surrogate_flags(self._h, out.ctypes.data_as(C.POINTER(C.c_int32)),
+                                                self._stream(stream)))
+        return out
+
     @property
     def step_count(self) -> int:
         n = C.c_int64()

@@ -162,6 +162,27 @@ typedef struct bc_batch_spec {
   const int64_t* conn_post;           /* synapse index                          */
   const double* conn_weight;          /* uS                                     */
   const double* conn_delay;           /* ms, >= 0                               */
+  /* subtree-surrogate ports (no counterpart in the reference: the learned
+     stand-in for distal dendritic subtrees).  Port k replaces a removed subtree
+     of cell port_cell[k] that hung off the distal end (x = 1) of branch
+     port_branch[k]: the port node is that endpoint, the attachment compartment
+     is the branch's last CV.  Every step the port injects
+       I = g (e + y_scale * y - V_end)   nA (g in uS, V in mV)
+     into the endpoint row, its conductance part implicit, y being the output of
+     the plan's GRU (bc_surrogate_set) fed with
+       ((V_att - e) / v_scale, S / 0.1 nA, feat[0], feat[1]),
+     S = the port's stimulus, i.e. the sum of its active port pulses (nA).      */
+  int64_t n_ports;
+  const int32_t* port_cell;
+  const int32_t* port_branch;
+  const double* port_g;               /* uS, > 0                                */
+  const double* port_e;               /* mV                                     */
+  const double* port_feat;            /* [n_ports][2] static features           */
+  int64_t n_port_pulses;
+  const int32_t* port_pulse_port;     /* port index                             */
+  const double* port_pulse_t_on;      /* ms                                     */
+  const double* port_pulse_t_off;     /* ms                                     */
+  const double* port_pulse_amp;       /* nA                                     */
 } bc_batch_spec;
 
 /* ------------------------------------------------------------------ plan options */
@@ -317,6 +338,46 @@ bc_status bc_probe_clear(bc_plan_t plan, void* stream);
 bc_status bc_network_spikes(bc_plan_t plan, int32_t* cells, int64_t* steps, int64_t cap, int64_t* n_out,
                             void* stream);
 bc_status bc_synapse_download(bc_plan_t plan, double* g /* [n_synapses] */, void* stream);
+
+/* ------------------------------------------------- subtree surrogate (GRU ports)
+ * No counterpart in the reference.  The GRU: hidden BC_GRU_HIDDEN, inputs
+ * BC_GRU_INPUTS, parameters as one FP32 vector of bc_gru_nparam() entries:
+ *   Wh [3H][H] | Wx [3H][X] | bx [3H] | bh [3H] | wo [H] | bo
+ * (gate blocks r, z, n).  Weights are used as BF16 on the tensor cores.         */
+#define BC_GRU_HIDDEN 64
+#define BC_GRU_INPUTS 4
+#define BC_SURROGATE_NORM 5 /* v_scale, y_scale, env_v_lo, env_v_hi, env_dvdt */
+int32_t bc_gru_nparam(void);
+/* Give the plan its GRU (host arrays) and enable its ports.  norm: v_scale (mV),
+   y_scale (mV), the envelope of V_att - e (mV, lo / hi) and of |dV_att/dt|
+   (mV/ms): a port input outside it flags the port's cell for the full solve. */
+bc_status bc_surrogate_set(bc_plan_t plan, const float* params, const float* norm, void* stream);
+/* flags[c] = 1 when a port of cell c saw an input outside the envelope since the
+   last reset, else 0 (host array of n_cells).                                  */
+bc_status bc_surrogate_flags(bc_plan_t plan, int32_t* flags, void* stream);
+
+/* Training kernels (device pointers; stream-ordered).  x [n_seq][t_total][X]
+   and y [n_seq][t_total] hold the sequences; a batch is the sequence ids
+   seq[batch]; a window is steps t0 .. t0+T-1.  h [batch][H] carries the hidden
+   state in and out.  wext [4H][H+16] / wht [H][3H]: BF16 pairs made by
+   bc_gru_pack -- the extended weight matrix of the forward (recurrent weights,
+   input weights and biases of the r, z, hn and input-n blocks) and the
+   transposed recurrent weights of the backward.  acts [5][batch][T][H] and yout [batch][T] are the forward's
+   saved activations (acts may be null when no backward follows).  loss (may be
+   null) accumulates the sum of squared errors in FP64.  The backward adds the
+   gradient of gscale/2 * sum (y - y_target)^2 into grads.                      */
+bc_status bc_gru_pack(const float* params, uint32_t* wext, uint32_t* wht, void* stream);
+bc_status bc_gru_forward(const float* params, const uint32_t* wext, const float* x, const float* y, int64_t t_total,
+                         const int32_t* seq, int32_t batch, int64_t t0, int32_t T, float* h, float* acts,
+                         float* yout, double* loss, void* stream);
+bc_status bc_gru_backward(const float* params, const uint32_t* wht, const float* x, const float* y,
+                          int64_t t_total, const int32_t* seq, int32_t batch, int64_t t0, int32_t T,
+                          const float* acts, const float* yout, float gscale, float* grads, void* stream);
+bc_status bc_gru_grad_sqnorm(const float* grads, float* out, void* stream);
+/* One Adam step (bias-corrected, step >= 1) on params with grads * clip_scale;
+   clears grads.                                                                */
+bc_status bc_gru_adam(float* params, float* grads, float* m, float* v, int64_t step, float lr, float beta1,
+                      float beta2, float eps, float clip_scale, void* stream);
 
 /* Diagnostics: cycles summed over CTAs (as seen by each CTA's first thread) in
  * forward elimination, back-substitution, node update and probes/pulses.  Only a

@@ -692,6 +692,52 @@ class OracleCell:
         self.point_area_um2 = np.zeros(self.n_point)
         self.point_area_um2[self.cv_mid] = self.cv_area
 
+    # ------------------------------------------------------------ surrogate ports
+    def set_ports(self, ports, theta, v_scale: float, y_scale: float) -> None:
+        """Subtree-surrogate ports (no counterpart in the reference).
+
+        ``ports``: dicts with ``branch`` (the port feeds that branch's x = 1
+        endpoint; its attachment CV is the branch's last CV), ``g`` (uS), ``e``
+        (mV), ``feat`` (two floats) and ``stim`` [(t_on, t_off, amp_nA)].  Every
+        step each port runs one GRU step (``oracle/gru.py``, BF16 rounding as the
+        kernels) on ((V_att - e) / v_scale, S / 0.1 nA, feat) and injects
+        g (e + y_scale y - V_end) nA into its endpoint row, the -g V_end part
+        implicitly.
+        """
+        from oracle import gru as G
+
+        row_of = np.empty(self.n_point, np.int64)
+        row_of[self.row_to_point] = np.arange(self.n_point)
+        self.ports = []
+        for pt in ports:
+            b = int(pt["branch"])
+            end = self.endpoint[(b, 1.0)]
+            att = int(self.branch_cv_ids[b][-1])
+            self.ports.append(dict(row=int(row_of[end]), att=att, g=float(pt["g"]), e=float(pt["e"]),
+                                   feat=np.asarray(pt["feat"], float), stim=list(pt.get("stim", ()))))
+        self.port_theta = np.asarray(theta, float)
+        self.port_norm = (float(v_scale), float(y_scale))
+        self.port_h = np.zeros((self.P, len(self.ports), G.H))
+
+    def _port_rows(self, diags, solves, V_n, t: float, dt: float) -> None:
+        from oracle import gru as G
+
+        v_scale, y_scale = self.port_norm
+        P, K = self.P, len(self.ports)
+        x = np.zeros((P, K, G.X))
+        for k, pt in enumerate(self.ports):
+            S = sum(amp for (t_on, t_off, amp) in pt["stim"] if t_on <= t < t_off)
+            x[:, k, 0] = (V_n[:, pt["att"]] - pt["e"]) / v_scale
+            x[:, k, 1] = S / 0.1  # nA, the stimulus input scale
+            x[:, k, 2:] = pt["feat"]
+        h, y = G.step(self.port_theta, x.reshape(P * K, G.X), self.port_h.reshape(P * K, G.H), quantize=True)
+        self.port_h = h.reshape(P, K, G.H)
+        y = y.reshape(P, K)
+        for k, pt in enumerate(self.ports):
+            gg = dt * pt["g"] * 1e-3  # uS on a row with the 1 uF dummy capacitance
+            diags[:, pt["row"]] += gg
+            solves[:, pt["row"]] += gg * (pt["e"] + y_scale * y[:, k])
+
     # ------------------------------------------------------------ state
     def reset_state(self) -> None:
         """``Cell.reset_state`` (cell.py:2529-2550) + ``HH.reset_state`` (channel/_base.py:560-573)."""
@@ -829,6 +875,8 @@ class OracleCell:
             edge_nA = self._clamp_nA(self.clamps_edge, t)
             by_row = edge_nA[:, self.row_to_point]
             solves[:, :n] += dt * (by_row / self.row_cap_uF) * 1e-3
+        if getattr(self, "ports", None):
+            self._port_rows(diags, solves, V_n, t, dt)
         lowers = np.concatenate([self.lowers_ms * dt, [0.0]])
         uppers = np.concatenate([self.uppers_ms * dt, [0.0]])
         # a8: forward elimination, one level at a time (leaves first)

@@ -1,0 +1,142 @@
+"""Subtree-surrogate ports in the step kernel against the float64 oracle (closed loop).
+
+A small cell keeps three leaf branches whose subtrees a GRU stands in for; the
+oracle (``OracleCell.set_ports``) runs the same GRU in float64 with the kernels'
+BF16 rounding points and injects the same port currents, so the whole loop --
+voltage in, GRU step, implicit port conductance, current out -- is compared.
+"""
+
+import numpy as np
+import pytest
+
+from braincell_gb300 import workloads as W
+from braincell_gb300.runtime import Plan
+from oracle import gru as G
+from oracle.staggered import OracleCell
+
+pytestmark = pytest.mark.gpu
+
+DT = 0.025
+V_SCALE, Y_SCALE = 10.0, 5.0
+WIDE = (V_SCALE, Y_SCALE, -1e4, 1e4, 1e9)
+
+
+def _desc(amp=0.25):
+    parent = [-1, 0, 1, 1, 0]
+    length = [20.0, 100.0, 80.0, 60.0, 120.0]
+    ncv = [1, 6, 4, 3, 5]
+    rp, rd = W._finish_tree(parent, length, ncv)
+    leak = ("IL", {"g_max": 0.3, "E": -70.0})
+    return W.CellDesc(parent=parent, length=length, r_prox=rp, r_dist=rd, ncv=ncv,
+                      types=["soma"] + ["dendrite"] * 4,
+                      channels_soma=[leak, ("Na_Ba2002", {"g_max": 120.0}), ("KDR_Ba2002", {"g_max": 36.0})],
+                      channels_dend=[leak, ("CaL_IS2008", {"g_max": 2.0}), ("HCN_HM1992", {"g_max": 0.01, "E": -43.0}),
+                                     ("K_Leak", {"g_max": 0.005})],
+                      pulses=[(0, 0.5, 2.0, 1e9, amp)])
+
+
+PORTS = [
+    dict(branch=2, g=0.004, e=-70.0, feat=(0.3, -0.2), stim=[]),
+    dict(branch=3, g=0.006, e=-68.0, feat=(-0.5, 0.1), stim=[(5.0, 8.0, 0.05), (10.0, 11.0, 0.1)]),
+    dict(branch=4, g=0.003, e=-72.0, feat=(0.0, 0.7), stim=[(3.0, 4.0, 0.08)]),
+]
+
+
+def _with_ports(batch, ports, cell=0):
+    batch.port_cell = np.full(len(ports), cell, np.int32)
+    batch.port_branch = np.array([p["branch"] for p in ports], np.int32)
+    batch.port_g = np.array([p["g"] for p in ports])
+    batch.port_e = np.array([p["e"] for p in ports])
+    batch.port_feat = np.array([p["feat"] for p in ports], float)
+    pp = [(k, *s) for k, p in enumerate(ports) for s in p["stim"]]
+    batch.port_pulse_port = np.array([q[0] for q in pp], np.int32)
+    batch.port_pulse_t_on = np.array([q[1] for q in pp], float)
+    batch.port_pulse_t_off = np.array([q[2] for q in pp], float)
+    batch.port_pulse_amp = np.array([q[3] for q in pp], float)
+    return batch
+
+
+def _run_pair(precision, n_steps, theta, amp=0.25, **kw):
+    d = _desc(amp)
+    b = _with_ports(W.descs_to_batch([d]), PORTS)
+    p = Plan(b, precision=precision, record_every=1, **kw)
+    p.set_surrogate(theta, WIDE)
+    p.run(n_steps, DT)
+    oc = OracleCell(W.desc_to_cell(d))
+    oc.set_ports(PORTS, theta.astype(np.float64), V_SCALE, Y_SCALE)
+    tr, sp = oc.run(DT, n_steps)
+    return p, p.traces()[0], tr[0, 0], p.spikes()[0], np.asarray(sp[0][0])
+
+
+def test_ports_closed_loop_f64_matches_oracle(native_lib, cuda_device):
+    theta = G.init_params(11, scale=1.5).astype(np.float32)
+    p, gpu, ora, gsp, osp = _run_pair("f64", 1200, theta, amp=0.05)
+    # the GRU itself is FP32/BF16 in both runs: agreement is to its rounding, far below 1e-3 mV
+    assert np.abs(gpu - ora).max() < 1e-4, np.abs(gpu - ora).max()
+    assert np.abs(gpu[-1] - gpu[0]) > 1e-3  # the cell moved
+    assert len(gsp) == len(osp)
+
+
+def test_ports_closed_loop_f32_spiking(native_lib, cuda_device):
+    theta = G.init_params(12, scale=1.0).astype(np.float32)
+    p, gpu, ora, gsp, osp = _run_pair("f32", 2400, theta, amp=0.4)
+    assert len(osp) >= 1
+    assert len(gsp) == len(osp)
+    assert np.abs(gsp - osp).max() < 0.05
+    # before the first spike's upstroke (dV/dt above 10 mV/ms), to 1e-3 mV
+    first = int(np.nonzero(np.diff(ora) / DT > 10.0)[0][0]) + 1
+    assert np.abs(gpu[:first] - ora[:first]).max() < 1e-3
+
+
+def test_ports_change_the_cell(native_lib, cuda_device):
+    """A port with a GRU that outputs a constant +y feeds current: the soma depolarises."""
+    theta = np.zeros(G.NPARAM, np.float32)
+    d = _desc(0.0)
+    base = Plan(W.descs_to_batch([d]), precision="f64", record_every=1)
+    base.run(400, DT)
+    theta[G.OFF_BO] = 4.0  # y = 4 -> I = g (e + 20 mV - V_end)
+    b = _with_ports(W.descs_to_batch([d]), PORTS)
+    p = Plan(b, precision="f64", record_every=1)
+    p.set_surrogate(theta, WIDE)
+    p.run(400, DT)
+    assert p.traces()[0][-1] > base.traces()[0][-1] + 0.05
+
+
+def test_envelope_flags_and_reset(native_lib, cuda_device):
+    theta = G.init_params(13).astype(np.float32)
+    d = _desc(0.3)
+    b = _with_ports(W.descs_to_batch([d, d]), PORTS, cell=1)  # ports on the second cell only
+    p = Plan(b, precision="f32", record_every=0)
+    # an envelope the spiking cell leaves (|dV/dt| bound of 1 mV/ms)
+    p.set_surrogate(theta, (V_SCALE, Y_SCALE, -50.0, 50.0, 1.0))
+    p.run(1200, DT)
+    np.testing.assert_array_equal(p.surrogate_flags(), [0, 1])
+    p.reset()
+    np.testing.assert_array_equal(p.surrogate_flags(), [0, 0])
+    p.set_surrogate(theta, WIDE)
+    p.run(200, DT)
+    np.testing.assert_array_equal(p.surrogate_flags(), [0, 0])
+
+
+def test_ports_need_a_gru(native_lib, cuda_device):
+    from braincell_gb300._abi import BCError
+
+    b = _with_ports(W.descs_to_batch([_desc()]), PORTS)
+    p = Plan(b, precision="f32")
+    with pytest.raises(BCError, match="bc_surrogate_set"):
+        p.run(10, DT)
+
+
+def test_ports_in_graph_and_big_tile_class(native_lib, cuda_device):
+    """Same ports through a CUDA graph and through the one-cell tile class: same trace."""
+    theta = G.init_params(14, scale=1.5).astype(np.float32)
+    d = _desc(0.3)
+    out = []
+    for kw in (dict(), dict(use_graph=True), dict(tile_nodes=16, threads_big=256)):
+        b = _with_ports(W.descs_to_batch([d]), PORTS)
+        p = Plan(b, precision="f64", record_every=1, steps_per_launch=150, **kw)
+        p.set_surrogate(theta, WIDE)
+        p.run(700, DT)
+        out.append(p.traces()[0])
+    np.testing.assert_allclose(out[1], out[0], rtol=0, atol=1e-9)
+    np.testing.assert_allclose(out[2], out[0], rtol=0, atol=1e-7)
