@@ -52,6 +52,9 @@ def _args():
     ap.add_argument("--threads-big", type=int, default=512)
     ap.add_argument("--steps-per-launch", type=int, default=1000)
     ap.add_argument("--lane-nodes", type=int, default=1)
+    ap.add_argument("--no-surrogate", action="store_true")
+    ap.add_argument("--surrogate-threads", type=int, default=384)
+    ap.add_argument("--accuracy-cells", type=int, default=300)
     return ap.parse_args()
 
 
@@ -199,6 +202,115 @@ def run_reference(a):
     print(json.dumps(line), flush=True)
 
 
+def _spike_errors(sp, ref):
+    """Spike-time errors (ms) of spikes paired in order within cells of equal count, and
+    the number of cells whose counts differ."""
+    errs, mis = [], 0
+    for x, y in zip(sp, ref):
+        if len(x) != len(y):
+            mis += 1
+        k = min(len(x), len(y))
+        if k:
+            errs.extend(np.abs(np.asarray(x[:k]) - np.asarray(y[:k])).tolist())
+    return np.asarray(errs), mis
+
+
+def surrogate_leg(a, descs, local, sid, stream, plain_ms):
+    """The surrogate-assisted form on the same workload: distal subtrees replaced by
+    GRU ports (the packaged model trained by the library's kernels), per-cell
+    fallback of envelope exits to the full solve, timed like the plain form;
+    accuracy against the FP64 plain solve on the first cells of the workload."""
+    import torch
+    from dataclasses import replace
+
+    from braincell_gb300 import surrogate as S
+    from braincell_gb300 import workloads as W
+    from braincell_gb300.runtime import Plan
+
+    model = S.load_model(os.path.join(ROOT, "braincell_gb300", "data", "surrogate_uneven.npz"))
+    t0 = time.perf_counter()
+    red, ports = zip(*[S.reduce_desc(d, model.cut_depth) for d in descs])
+    batch = S.ports_to_batch(list(red), list(ports))
+    t_reduce = time.perf_counter() - t0
+    T = a.surrogate_threads
+    kw = dict(precision="f32", device=local, tile_nodes=a.tile_nodes, threads_per_tile=T, threads_big=T,
+              threads_global=T, steps_per_launch=a.steps_per_launch, record_every=0, lane_nodes=a.lane_nodes)
+    plan = Plan(batch, **kw)
+    plan.set_surrogate(model.theta, model.norm())
+    full_cv = int(sum(int(sum(d.ncv)) for d in descs))
+
+    def run_reduced():
+        plan.reset(stream=sid)
+        plan.run(a.sim_steps, DT, stream=sid, check=False)
+        return plan.surrogate_flags(stream=sid)
+
+    flags = run_reduced()
+    fb = np.nonzero(flags)[0]
+    fplan = None
+    if fb.size:
+        fkw = dict(kw, threads_per_tile=a.threads, threads_big=a.threads_big, threads_global=512)
+        fplan = Plan(W.descs_to_batch([descs[i] for i in fb]), **fkw)
+
+    def one_step():
+        run_reduced()
+        if fplan is not None:
+            fplan.reset(stream=sid)
+            fplan.run(a.sim_steps, DT, stream=sid, check=False)
+
+    for _ in range(a.warmup):
+        one_step()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clocks:
+        ev0.record(stream)
+        for _ in range(a.steps):
+            one_step()
+        ev1.record(stream)
+        ev1.synchronize()
+    plan.check(stream=sid)
+    ms = ev0.elapsed_time(ev1) / a.steps
+    launches = 1 + -(-a.sim_steps // plan.info["steps_per_launch"]) * plan.info["n_launch_classes"]
+    if fplan is not None:
+        launches += 1 + -(-a.sim_steps // fplan.info["steps_per_launch"]) * fplan.info["n_launch_classes"]
+    out = {"value": full_cv * a.sim_steps / (ms * 1e-3), "unit": UNIT + " (full-morphology compartments)",
+           "ms_per_step": ms, "speedup_vs_plain": plain_ms / ms, "n_ports": int(batch.port_cell.size),
+           "reduced_compartments": int(plan.n_cv), "full_compartments": full_cv,
+           "fallback_cells": int(fb.size), "fallback_rate": float(fb.size) / len(descs),
+           "cut_depth": model.cut_depth, "threads_per_tile": T, "tiles": plan.info["n_tiles"],
+           "gpu_launches_per_step": launches,
+           "clocks": clocks.summary(), "setup_s_reduce": round(t_reduce, 2),
+           "timed": "per step: reset + 8,000 steps of the reduced cells with GRU ports + flag read-back + the "
+                    "full solve of the flagged cells (their plan built once; flags are deterministic)"}
+    plan.close()
+    if fplan is not None:
+        fplan.close()
+    # accuracy on the first cells against the FP64 plain solve (the on-GPU oracle run)
+    n_acc = min(a.accuracy_cells, len(descs))
+    if n_acc:
+        sub = list(descs[:n_acc])
+        full = [replace(d, probes=[(0, 0.5)]) for d in sub]
+        ref = Plan(W.descs_to_batch(full), precision="f64", device=local, record_every=1, max_spikes=256)
+        ref.run(a.sim_steps, DT)
+        tr64, sp64 = ref.traces(), ref.spikes()
+        ref.close()
+        r = S.run_surrogate(sub, model, a.sim_steps, record_every=1, fallback=True, device=local)
+        e, mis = _spike_errors(r.spikes, sp64)
+        rms = np.sqrt(np.mean((r.traces - tr64) ** 2, axis=1))
+        lin = S.run_surrogate(sub, None, a.sim_steps, record_every=1, fallback=False, device=local)
+        rms_lin = np.sqrt(np.mean((lin.traces - tr64) ** 2, axis=1))
+        out["accuracy"] = {
+            "cells": n_acc, "against": "FP64 plain solve on the GPU", "fallback_rate": r.fallback_rate,
+            "spike_time_error_ms": {"median": float(np.median(e)) if e.size else None,
+                                    "p99": float(np.percentile(e, 99)) if e.size else None,
+                                    "spikes_paired": int(e.size)},
+            "cells_with_spike_count_mismatch": mis,
+            "soma_rms_mV": {"median": float(np.median(rms)), "mean": float(np.mean(rms))},
+            "without_network_soma_rms_mV": {"median": float(np.median(rms_lin)), "mean": float(np.mean(rms_lin))},
+        }
+    out["model"] = {k: model.info.get(k) for k in ("n_traj", "epochs", "updates", "train_s", "val_mse_after")}
+    return out
+
+
 def run_ours(a):
     import torch
 
@@ -307,6 +419,11 @@ def run_ours(a):
         "clocks": clocks.summary(),
         "wall_s_timed": t_wall,
     }
+    if not a.no_surrogate:
+        sur = surrogate_leg(a, descs, local, sid, stream, ms / a.steps)
+        sur["value"] = sur["value"] * world  # every rank runs its own replica
+        line["surrogate"] = sur
+        line["gpu_launches"] += a.steps * sur["gpu_launches_per_step"]
     if rank == 0 and world == 1 and not a.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline()
     if rank == 0:

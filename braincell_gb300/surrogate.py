@@ -32,11 +32,15 @@ import numpy as np
 from . import _abi
 from .workloads import CellDesc, descs_to_batch
 
-__all__ = ["CUT_DEPTH", "Port", "SurrogateModel", "branch_depths", "reduce_desc", "passive_subtree",
+__all__ = ["CUT_DEPTH", "PACKAGED_MODEL", "Port", "SurrogateModel", "branch_depths", "reduce_desc", "passive_subtree",
            "ports_to_batch", "make_training_descs", "collect_trajectories", "train_surrogate", "run_surrogate",
            "SurrogateRun", "save_model", "load_model"]
 
+import os
+
 CUT_DEPTH = 4
+PACKAGED_MODEL = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data", "surrogate_uneven.npz")
+NPARAM = 3 * 64 * 64 + 3 * 64 * 4 + 2 * 3 * 64 + 64 + 1
 V_SCALE = 10.0       # mV
 S_SCALE = 0.1        # nA: stimulus input scale (the step kernel's constant)
 G_REF = 0.005        # uS, feature reference

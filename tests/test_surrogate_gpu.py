@@ -140,3 +140,64 @@ def test_ports_in_graph_and_big_tile_class(native_lib, cuda_device):
         out.append(p.traces()[0])
     np.testing.assert_allclose(out[1], out[0], rtol=0, atol=1e-9)
     np.testing.assert_allclose(out[2], out[0], rtol=0, atol=1e-7)
+
+
+def _soma_rms(traces, ref):
+    return np.sqrt(np.mean((traces - ref) ** 2, axis=1))
+
+
+def test_packaged_model_gains_over_the_method_without_it(native_lib, cuda_device):
+    """On held-out cells of the 10k workload (seed 1, never trained on), the trained
+    GRU ports track the FP64 plain solve's soma voltage better than the same ports
+    with the network switched off (only the passive load), and far better than
+    cutting the subtrees off."""
+    from dataclasses import replace
+
+    from braincell_gb300 import surrogate as S
+
+    m = S.load_model(S.PACKAGED_MODEL)
+    descs = W.uneven(40, seed=1)
+    n = 4000
+    full = [replace(d, probes=[(0, 0.5)]) for d in descs]
+    ref = Plan(W.descs_to_batch(full), precision="f64", record_every=1)
+    ref.run(n, DT)
+    tr64 = ref.traces()
+    gru = S.run_surrogate(descs, m, n, record_every=1, fallback=False)
+    lin = S.run_surrogate(descs, None, n, record_every=1, fallback=False)
+    red = [replace(S.reduce_desc(d)[0], probes=[(0, 0.5)]) for d in descs]
+    cut = Plan(W.descs_to_batch(red), precision="f32", record_every=1)
+    cut.run(n, DT)
+    e_gru = np.median(_soma_rms(gru.traces, tr64))
+    e_lin = np.median(_soma_rms(lin.traces, tr64))
+    e_cut = np.median(_soma_rms(cut.traces(), tr64))
+    assert gru.n_ports > 0 and gru.reduced_cv < 0.5 * gru.full_cv
+    assert e_gru < 0.5 * e_lin, (e_gru, e_lin)
+    assert e_lin < e_cut
+    assert e_gru < 1.0  # mV, the somatic bar
+
+
+def test_fallback_replaces_flagged_cells_with_the_full_solve(native_lib, cuda_device):
+    from dataclasses import replace
+
+    from braincell_gb300 import surrogate as S
+
+    m = S.load_model(S.PACKAGED_MODEL)
+    tight = replace(m, env_dvdt=0.5)  # most spiking cells leave this envelope
+    descs = W.uneven(12, seed=1)
+    r = S.run_surrogate(descs, tight, 2000, record_every=1, fallback=True)
+    assert 0 < r.fallback_cells.size <= len(descs)
+    full = Plan(W.descs_to_batch([replace(descs[i], probes=[(0, 0.5)]) for i in r.fallback_cells]),
+                precision="f32", record_every=1)
+    full.run(2000, DT)
+    np.testing.assert_allclose(r.traces[r.fallback_cells], full.traces(), rtol=0, atol=1e-9)
+
+
+def test_training_pipeline_learns(native_lib, cuda_device):
+    """Trajectories from the plain solver, GPU training with the library's kernels:
+    a short run lowers the held-out loss."""
+    from braincell_gb300 import surrogate as S
+
+    m = S.train_surrogate(40, n_steps=1600, epochs=6, batch=64, window=200, lr=3e-3, val_frac=0.2, seed=5)
+    assert m.info["n_traj"] > 20
+    assert m.info["val_mse_after"] < 0.5 * m.info["val_mse_before"], m.info
+    assert np.isfinite(m.theta).all()
