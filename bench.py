@@ -228,62 +228,33 @@ def surrogate_leg(a, descs, local, sid, stream, plain_ms):
     from braincell_gb300.runtime import Plan
 
     model = S.load_model(os.path.join(ROOT, "braincell_gb300", "data", "surrogate_uneven.npz"))
-    t0 = time.perf_counter()
-    red, ports = zip(*[S.reduce_desc(d, model.cut_depth) for d in descs])
-    batch = S.ports_to_batch(list(red), list(ports))
-    t_reduce = time.perf_counter() - t0
     T = a.surrogate_threads
-    kw = dict(precision="f32", device=local, tile_nodes=a.tile_nodes, threads_per_tile=T, threads_big=T,
-              threads_global=T, steps_per_launch=a.steps_per_launch, record_every=0, lane_nodes=a.lane_nodes)
-    plan = Plan(batch, **kw)
-    plan.set_surrogate(model.theta, model.norm())
-    full_cv = int(sum(int(sum(d.ncv)) for d in descs))
-
-    def run_reduced():
-        plan.reset(stream=sid)
-        plan.run(a.sim_steps, DT, stream=sid, check=False)
-        return plan.surrogate_flags(stream=sid)
-
-    flags = run_reduced()
-    fb = np.nonzero(flags)[0]
-    fplan = None
-    if fb.size:
-        fkw = dict(kw, threads_per_tile=a.threads, threads_big=a.threads_big, threads_global=512)
-        fplan = Plan(W.descs_to_batch([descs[i] for i in fb]), **fkw)
-
-    def one_step():
-        run_reduced()
-        if fplan is not None:
-            fplan.reset(stream=sid)
-            fplan.run(a.sim_steps, DT, stream=sid, check=False)
-
+    kw = dict(tile_nodes=a.tile_nodes, threads_per_tile=T, threads_big=T, threads_global=T,
+              steps_per_launch=a.steps_per_launch, lane_nodes=a.lane_nodes)
+    t0 = time.perf_counter()
+    runner = S.SurrogateRunner(descs, model, precision="f32", device=local, plan_kw=kw)
+    t_setup = time.perf_counter() - t0
     for _ in range(a.warmup):
-        one_step()
+        runner.run(a.sim_steps, DT)
     torch.cuda.synchronize()
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    walls, res = [], None
     with ClockSampler(local) as clocks:
-        ev0.record(stream)
         for _ in range(a.steps):
-            one_step()
-        ev1.record(stream)
-        ev1.synchronize()
-    plan.check(stream=sid)
-    ms = ev0.elapsed_time(ev1) / a.steps
-    launches = 1 + -(-a.sim_steps // plan.info["steps_per_launch"]) * plan.info["n_launch_classes"]
-    if fplan is not None:
-        launches += 1 + -(-a.sim_steps // fplan.info["steps_per_launch"]) * fplan.info["n_launch_classes"]
-    out = {"value": full_cv * a.sim_steps / (ms * 1e-3), "unit": UNIT + " (full-morphology compartments)",
-           "ms_per_step": ms, "speedup_vs_plain": plain_ms / ms, "n_ports": int(batch.port_cell.size),
-           "reduced_compartments": int(plan.n_cv), "full_compartments": full_cv,
-           "fallback_cells": int(fb.size), "fallback_rate": float(fb.size) / len(descs),
-           "cut_depth": model.cut_depth, "threads_per_tile": T, "tiles": plan.info["n_tiles"],
-           "gpu_launches_per_step": launches,
-           "clocks": clocks.summary(), "setup_s_reduce": round(t_reduce, 2),
-           "timed": "per step: reset + 8,000 steps of the reduced cells with GRU ports + flag read-back + the "
-                    "full solve of the flagged cells (their plan built once; flags are deterministic)"}
-    plan.close()
-    if fplan is not None:
-        fplan.close()
+            res = runner.run(a.sim_steps, DT)
+            walls.append(res.wall_ms)
+    ms = float(np.median(walls))
+    info = runner.plan.info
+    out = {"value": runner.full_cv * a.sim_steps / (ms * 1e-3),
+           "unit": UNIT + " (full-morphology compartments)", "ms_per_step": ms, "speedup_vs_plain": plain_ms / ms,
+           "n_ports": runner.n_ports, "reduced_compartments": int(runner.plan.n_cv),
+           "full_compartments": runner.full_cv, "fallback_cells": int(res.fallback_cells.size),
+           "fallback_rate": res.fallback_rate, "cut_depth": model.cut_depth, "threads_per_tile": T,
+           "tiles": info["n_tiles"], "gpu_launches_per_step": res.launches,
+           "clocks": clocks.summary(), "setup_s": round(t_setup, 2),
+           "timed": "per step, host clock: reset + the reduced cells with GRU ports launch by launch, flags read "
+                    "after each launch, the full solve of newly flagged cells from t = 0 on a second stream "
+                    "(plans built inside the timed region), until every stream is done"}
+    runner.close()
     # accuracy on the first cells against the FP64 plain solve (the on-GPU oracle run)
     n_acc = min(a.accuracy_cells, len(descs))
     if n_acc:

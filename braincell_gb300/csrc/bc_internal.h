@@ -107,7 +107,8 @@ struct TileDesc {
   int64_t scratch_offset;   // bytes into the plan's global scratch (global-resident tiles)
   int64_t port_offset;      // into the plan's port array (subtree-surrogate ports of this tile)
   int32_t n_ports;
-  int32_t off_pstage;       // per-port staging records (PortStage), inside the scratch area; -1: none
+  int32_t off_pstage;       // per-port staging records (PortStage) followed by PortLocal records,
+                            // inside the scratch area; -1: none
 };
 
 // ------------------------------------------------------------- subtree surrogate
@@ -146,11 +147,23 @@ constexpr int kPortStride = kPortVPrev + 4;
 #endif
 
 // Per-step staging of a port inside the tile's scratch: the GRU inputs, the
-// endpoint node and the factor that turns y into the row's right-hand side.
+// endpoint node, the factor that turns y into the row's right-hand side and the
+// port id (row of its hidden state).
 struct PortStage {
   float x[4];
   int32_t node;
   float coef;
+  int32_t id;
+  int32_t pad;
+};
+
+// A port's record and envelope state in the tile's scratch for the length of a
+// launch (copied in at the start, the envelope state written back at the end).
+struct PortLocal {
+  int32_t node, att, cell, id, stim_begin, stim_end;
+  double g, e;
+  float feat[2];
+  float v_prev, seen;
   int32_t pad[2];
 };
 

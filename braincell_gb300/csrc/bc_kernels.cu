@@ -1040,14 +1040,43 @@ __device__ __forceinline__ void backsub_phase(const TileView<Real>& tv, int p, i
 // items do not race; each item adds its part of y's current atomically.
 constexpr float kPortStimScale = 0.1f;  // nA
 
-template <typename Real>
-__device__ __forceinline__ void port_stage(const PortRec* ports, int n_ports, const PulseRec* stim, float* port_h,
-                                          int32_t* flags, const GruWeights* __restrict__ W, const Pair<Real>* v,
-                                          Pair<Real>* dr, PortStage* stage, int64_t m, Real dt, int tid, int T) {
+// Launch start / end: the tile's port records and envelope state between global
+// memory and the tile scratch.
+__device__ __forceinline__ void port_local_load(const PortRec* ports, int n_ports, const float* port_h,
+                                                PortLocal* pl, int tid, int T) {
   for (int q = tid; q < n_ports; q += T) {
     const PortRec r = ports[q];
-    float* hp = port_h + size_t(r.id) * kPortStride;
-    const float2 pv = *reinterpret_cast<const float2*>(hp + kPortVPrev);
+    PortLocal l;
+    l.node = r.node;
+    l.att = r.att;
+    l.cell = r.cell;
+    l.id = r.id;
+    l.stim_begin = r.stim_begin;
+    l.stim_end = r.stim_end;
+    l.g = r.g;
+    l.e = r.e;
+    l.feat[0] = r.feat[0];
+    l.feat[1] = r.feat[1];
+    const float2 pv = *reinterpret_cast<const float2*>(port_h + size_t(r.id) * kPortStride + kPortVPrev);
+    l.v_prev = pv.x;
+    l.seen = pv.y;
+    l.pad[0] = l.pad[1] = 0;
+    pl[q] = l;
+  }
+}
+
+__device__ __forceinline__ void port_local_store(int n_ports, float* port_h, const PortLocal* pl, int tid, int T) {
+  for (int q = tid; q < n_ports; q += T)
+    *reinterpret_cast<float2*>(port_h + size_t(pl[q].id) * kPortStride + kPortVPrev) =
+        make_float2(pl[q].v_prev, pl[q].seen);
+}
+
+template <typename Real>
+__device__ __forceinline__ void port_stage(PortLocal* pl, int n_ports, const PulseRec* stim, int32_t* flags,
+                                          const GruWeights* __restrict__ W, const Pair<Real>* v, Pair<Real>* dr,
+                                          PortStage* stage, int64_t m, Real dt, int tid, int T) {
+  for (int q = tid; q < n_ports; q += T) {
+    PortLocal& r = pl[q];
     const Pair<Real> va = v[r.att], ve = v[r.node];
     float S = 0.f;
     for (int k = r.stim_begin; k < r.stim_end; ++k) {
@@ -1056,9 +1085,10 @@ __device__ __forceinline__ void port_stage(const PortRec* ports, int n_ports, co
     }
     const float vatt = float(va.x + va.y);
     const float dv = vatt - float(r.e);
-    const float rate = pv.y != 0.f ? fabsf(vatt - pv.x) / float(dt) : 0.f;
+    const float rate = r.seen != 0.f ? fabsf(vatt - r.v_prev) / float(dt) : 0.f;
     if (dv < W->env_v_lo || dv > W->env_v_hi || rate > W->env_dvdt) flags[r.cell] = 1;
-    *reinterpret_cast<float2*>(hp + kPortVPrev) = make_float2(vatt, 1.f);
+    r.v_prev = vatt;
+    r.seen = 1.f;
     const Real gg = Real(r.g) * Real(1e-3) * dt;  // uS -> row units (1 uF dummy capacitance)
     Pair<Real> row = dr[r.node];
     row.x += gg;
@@ -1071,8 +1101,8 @@ __device__ __forceinline__ void port_stage(const PortRec* ports, int n_ports, co
     st.x[3] = r.feat[1];
     st.node = r.node;
     st.coef = float(gg) * W->y_scale;
-    st.pad[0] = r.id;
-    st.pad[1] = 0;
+    st.id = r.id;
+    st.pad = 0;
     stage[q] = st;
   }
 }
@@ -1089,8 +1119,8 @@ __device__ __forceinline__ void port_gru(const PortStage* stage, int n_ports, fl
     const int qa = mt * 16 + g, qb = qa + 8;
     const bool oka = qa < n_ports, okb = qb < n_ports;
     const int j0 = jb * 8 + 2 * tq;
-    float* ha = oka ? port_h + size_t(stage[qa].pad[0]) * kPortStride : nullptr;
-    float* hb = okb ? port_h + size_t(stage[qb].pad[0]) * kPortStride : nullptr;
+    float* ha = oka ? port_h + size_t(stage[qa].id) * kPortStride : nullptr;
+    float* hb = okb ? port_h + size_t(stage[qb].id) * kPortStride : nullptr;
     // A operand straight from the BF16 halves; the FP32 values of this lane's units
     uint32_t ah[4][4];
     const uint32_t* ba = oka ? reinterpret_cast<const uint32_t*>(ha + kPortHBf) + rd * (kGruH / 2) : nullptr;
@@ -1230,11 +1260,15 @@ __global__ void __launch_bounds__(kVar == 2 ? BC_PORT_MAX_THREADS : 1024, kVar =
     for (int c = tid; c < tv.n_cells; c += T) tv.stamp[c] = -1;
   __syncthreads();
   PortStage* pstage = nullptr;
+  PortLocal* plocal = nullptr;
   if constexpr (kPorts) {
     if (td.n_ports > 0) {
       pstage = reinterpret_cast<PortStage*>(scratch + td.off_pstage);
-      port_stage<Real>(a.ports + td.port_offset, td.n_ports, a.port_pulses, a.port_h, a.port_flags, a.gru, tv.v,
-                       tv.dr, pstage, a.step0, dt, tid, T);
+      plocal = reinterpret_cast<PortLocal*>(pstage + td.n_ports);
+      port_local_load(a.ports + td.port_offset, td.n_ports, a.port_h, plocal, tid, T);
+      __syncthreads();
+      port_stage<Real>(plocal, td.n_ports, a.port_pulses, a.port_flags, a.gru, tv.v, tv.dr, pstage, a.step0, dt,
+                       tid, T);
       __syncthreads();
       port_gru<Real>(pstage, td.n_ports, a.port_h, a.gru, tv.dr, a.step0, warp, n_warps, lane);
       __syncthreads();
@@ -1346,8 +1380,8 @@ __global__ void __launch_bounds__(kVar == 2 ? BC_PORT_MAX_THREADS : 1024, kVar =
     BC_TICK(2);
     if constexpr (kPorts) {
       if (td.n_ports > 0 && !last) {
-        port_stage<Real>(a.ports + td.port_offset, td.n_ports, a.port_pulses, a.port_h, a.port_flags, a.gru, tv.v,
-                         tv.dr, pstage, step + 1, dt, tid, T);
+        port_stage<Real>(plocal, td.n_ports, a.port_pulses, a.port_flags, a.gru, tv.v, tv.dr, pstage, step + 1, dt,
+                         tid, T);
         __syncthreads();
         BC_TICK(2);
         port_gru<Real>(pstage, td.n_ports, a.port_h, a.gru, tv.dr, step + 1, warp, n_warps, lane);
@@ -1360,6 +1394,9 @@ __global__ void __launch_bounds__(kVar == 2 ? BC_PORT_MAX_THREADS : 1024, kVar =
   if (threadIdx.x == 0 && a.timers)
     for (int q = 0; q < 4; ++q) atomicAdd(a.timers + q, tm[q]);
 #endif
+  if constexpr (kPorts) {
+    if (td.n_ports > 0) port_local_store(td.n_ports, a.port_h, plocal, tid, T);
+  }
   if (s_status) atomicOr(a.status, s_status);
 
   if constexpr (kSmem) {

@@ -615,7 +615,7 @@ static bc_status build_tile(const BuildCtx& cx, const TileBuild& tb, int T, Tile
   d.off_pstage = -1;
   if (n_tile_ports > 0) {
     d.off_pstage = int32_t(so);
-    so = align16(so + n_tile_ports * sizeof(PortStage));
+    so = align16(so + n_tile_ports * (sizeof(PortStage) + sizeof(PortLocal)));
   }
   d.scratch_bytes = int32_t(so);
   d.n_nodes = int32_t(N);

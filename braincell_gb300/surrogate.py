@@ -34,6 +34,7 @@ from .workloads import CellDesc, descs_to_batch
 
 __all__ = ["CUT_DEPTH", "PACKAGED_MODEL", "Port", "SurrogateModel", "branch_depths", "reduce_desc", "passive_subtree",
            "ports_to_batch", "make_training_descs", "collect_trajectories", "train_surrogate", "run_surrogate",
+           "fallback_plan_options", "SurrogateRunner",
            "SurrogateRun", "save_model", "load_model"]
 
 import os
@@ -372,14 +373,27 @@ def train_surrogate(n_cells: int = 460, *, seed: int = 3, n_steps: int = 8000, d
 
 
 # ----------------------------------------------------------------------------- running
+def fallback_plan_options(descs, base: dict | None = None, threads: int = 256, n_sm: int = 152) -> dict:
+    """Plan options for the full solve of a few fallback cells: tiles small enough
+    that they cover every SM about twice (a small batch is bound by the latency of
+    one tile, not by throughput)."""
+    kw = dict(base or {})
+    nodes = sum(int(sum(d.ncv)) + len(d.parent) + 1 for d in descs)
+    kw["tile_nodes"] = int(min(kw.get("tile_nodes", 2500) or 2500, max(128, nodes // (2 * n_sm))))
+    kw["threads_per_tile"] = threads
+    kw["threads_big"] = max(threads, 256)
+    kw["threads_global"] = 512
+    return kw
+
+
 @dataclass
 class SurrogateRun:
     reduced_cv: int
     full_cv: int
     n_ports: int
     fallback_cells: np.ndarray
-    ms_surrogate: float
-    ms_fallback: float
+    wall_ms: float                # reset to the end of the last fallback run (host clock)
+    launches: int                 # kernel launches: resets, reduced-plan launches, fallback launches
     spikes: list                  # per cell: soma spike times (ms), fallback cells from the full solve
     traces: np.ndarray | None = None  # [n_cells, T] soma voltage when record_every > 0
 
@@ -388,49 +402,112 @@ class SurrogateRun:
         return float(self.fallback_cells.size) / max(len(self.spikes), 1)
 
 
+class SurrogateRunner:
+    """Cells with their distal subtrees replaced by GRU ports, with per-cell fallback.
+
+    The reduced plan runs launch by launch; after each launch the envelope flags
+    are read, the next launch is queued first, and the cells that newly left the
+    envelope start their full-morphology solve from t = 0 on a second stream, so
+    the fallback runs alongside the remaining reduced launches.  ``model=None``
+    runs the ports with y = 0 (only the passive linear load): the method without
+    the network."""
+
+    def __init__(self, descs, model: SurrogateModel | None, *, precision: str = "f32", record_every: int = 0,
+                 device: int = 0, plan_kw: dict | None = None, fallback: bool = True):
+        from .gru import NPARAM
+        from .runtime import Plan
+
+        self.descs = list(descs)
+        self.model = model
+        self.precision, self.record_every, self.device = precision, int(record_every), int(device)
+        self.plan_kw = dict(plan_kw or {})
+        self.fallback = fallback and model is not None
+        red, ports = zip(*[reduce_desc(d, model.cut_depth if model else CUT_DEPTH) for d in self.descs])
+        red = [replace(r, probes=[(0, 0.5)]) for r in red]
+        self.batch = ports_to_batch(list(red), list(ports))
+        self.plan = Plan(self.batch, precision=precision, record_every=record_every, max_spikes=256, device=device,
+                         **self.plan_kw)
+        self.n_ports = int(self.batch.port_cell.size)
+        if self.n_ports:
+            if model is None:
+                self.plan.set_surrogate(np.zeros(NPARAM, np.float32), (V_SCALE, 1.0, -1e4, 1e4, 1e9))
+            else:
+                self.plan.set_surrogate(model.theta, model.norm())
+        self.full_cv = int(sum(int(sum(d.ncv)) for d in self.descs))
+
+    def _fallback_plan(self, cells):
+        from .runtime import Plan
+
+        fd = [replace(self.descs[i], probes=[(0, 0.5)]) for i in cells]
+        kw = fallback_plan_options(fd, self.plan_kw, threads=int(self.plan_kw.get("threads_per_tile", 0) or 256))
+        kw.pop("threads_global", None)
+        return Plan(descs_to_batch(fd), precision=self.precision, record_every=self.record_every, max_spikes=256,
+                    device=self.device, **kw)
+
+    def run(self, n_steps: int, dt: float = 0.025) -> SurrogateRun:
+        import torch
+
+        plan = self.plan
+        main = torch.cuda.current_stream(self.device)
+        sid = int(main.cuda_stream)
+        n = len(self.descs)
+        spl = int(plan.info["steps_per_launch"])
+        watch = self.fallback and self.n_ports > 0
+        t0 = time.perf_counter()
+        plan.reset(stream=sid)
+        flagged = np.zeros(n, bool)
+        fallbacks = []
+        done = min(spl, n_steps)
+        plan.run(done, dt, stream=sid, check=False)
+        while True:
+            flags = plan.surrogate_flags(stream=sid) if watch else None
+            more = done < n_steps
+            if more:
+                k = min(spl, n_steps - done)
+                plan.run(k, dt, stream=sid, check=False)
+                done += k
+            if flags is not None:
+                new = np.nonzero((flags != 0) & ~flagged)[0]
+                if new.size:
+                    flagged[new] = True
+                    side = torch.cuda.Stream(self.device)
+                    fp = self._fallback_plan(new)
+                    fp.run(n_steps, dt, stream=int(side.cuda_stream), check=False)
+                    fallbacks.append((new, fp, side))
+            if not more:
+                break
+        plan.check(stream=sid)
+        for _, fp, side in fallbacks:
+            fp.check(stream=int(side.cuda_stream))
+        torch.cuda.synchronize(self.device)
+        wall = (time.perf_counter() - t0) * 1e3
+        spikes = plan.spikes(stream=sid)
+        traces = plan.traces(stream=sid) if self.record_every else None
+        fb_launches = 0
+        for cells, fp, side in fallbacks:
+            fb_launches += 1 + -(-n_steps // int(fp.info["steps_per_launch"])) * int(fp.info["n_launch_classes"])
+            fsp = fp.spikes(stream=int(side.cuda_stream))
+            ftr = fp.traces(stream=int(side.cuda_stream)) if self.record_every else None
+            for j, i in enumerate(cells):
+                spikes[i] = fsp[j]
+                if traces is not None:
+                    traces[i] = ftr[j]
+            fp.close()
+        launches = 1 + -(-n_steps // spl) * int(plan.info["n_launch_classes"])
+        return SurrogateRun(reduced_cv=int(plan.n_cv), full_cv=self.full_cv, n_ports=self.n_ports,
+                            fallback_cells=np.nonzero(flagged)[0], wall_ms=wall, launches=launches + fb_launches,
+                            spikes=list(spikes), traces=traces)
+
+    def close(self) -> None:
+        self.plan.close()
+
+
 def run_surrogate(descs, model: SurrogateModel | None, n_steps: int, dt: float = 0.025, *, precision: str = "f32",
                   record_every: int = 0, fallback: bool = True, device: int = 0, plan_kw: dict | None = None):
-    """Run the cells with their distal subtrees replaced by GRU ports.
-
-    ``model=None`` runs the ports with y = 0 (only the passive linear load):
-    the method without the network.  Cells that leave the envelope are run again
-    with their full morphology when ``fallback`` is set."""
-    import torch
-
-    from .gru import NPARAM
-    from .runtime import Plan
-
-    plan_kw = dict(plan_kw or {})
-    red, ports = zip(*[reduce_desc(d, model.cut_depth if model else CUT_DEPTH) for d in descs])
-    red = [replace(r, probes=[(0, 0.5)]) for r in red]
-    batch = ports_to_batch(list(red), list(ports))
-    plan = Plan(batch, precision=precision, record_every=record_every, max_spikes=256, device=device, **plan_kw)
-    if batch.port_cell.size:
-        if model is None:
-            plan.set_surrogate(np.zeros(NPARAM, np.float32), (V_SCALE, 1.0, -1e4, 1e4, 1e9))
-        else:
-            plan.set_surrogate(model.theta, model.norm())
-    torch.cuda.synchronize(device)
-    ms = plan.run_timed(n_steps, dt)
-    spikes = plan.spikes()
-    traces = plan.traces() if record_every else None
-    flags = plan.surrogate_flags() if batch.port_cell.size else np.zeros(len(descs), np.int32)
-    reduced_cv = plan.n_cv
-    plan.close()
-    fb = np.nonzero(flags)[0] if fallback else np.zeros(0, np.int64)
-    ms_fb = 0.0
-    if fb.size:
-        full = [replace(descs[i], probes=[(0, 0.5)]) for i in fb]
-        fplan = Plan(descs_to_batch(full), precision=precision, record_every=record_every, max_spikes=256,
-                     device=device, **plan_kw)
-        ms_fb = fplan.run_timed(n_steps, dt)
-        fsp = fplan.spikes()
-        ftr = fplan.traces() if record_every else None
-        fplan.close()
-        for j, i in enumerate(fb):
-            spikes[i] = fsp[j]
-            if traces is not None:
-                traces[i] = ftr[j]
-    full_cv = int(sum(int(sum(d.ncv)) for d in descs))
-    return SurrogateRun(reduced_cv=reduced_cv, full_cv=full_cv, n_ports=int(batch.port_cell.size),
-                        fallback_cells=fb, ms_surrogate=ms, ms_fallback=ms_fb, spikes=list(spikes), traces=traces)
+    """One run of :class:`SurrogateRunner` (the plan is built and released here)."""
+    r = SurrogateRunner(descs, model, precision=precision, record_every=record_every, device=device,
+                        plan_kw=plan_kw, fallback=fallback)
+    try:
+        return r.run(n_steps, dt)
+    finally:
+        r.close()
