@@ -380,8 +380,8 @@ def fallback_plan_options(descs, base: dict | None = None, threads: int = 256, n
     kw = dict(base or {})
     nodes = sum(int(sum(d.ncv)) + len(d.parent) + 1 for d in descs)
     kw["tile_nodes"] = int(min(kw.get("tile_nodes", 2500) or 2500, max(128, nodes // (2 * n_sm))))
-    kw["threads_per_tile"] = threads
-    kw["threads_big"] = max(threads, 256)
+    kw["threads_per_tile"] = max(threads, 256)
+    kw["threads_big"] = 1024  # a cell alone in a tile: its step latency bounds the fallback
     kw["threads_global"] = 512
     return kw
 
@@ -439,8 +439,7 @@ class SurrogateRunner:
         from .runtime import Plan
 
         fd = [replace(self.descs[i], probes=[(0, 0.5)]) for i in cells]
-        kw = fallback_plan_options(fd, self.plan_kw, threads=int(self.plan_kw.get("threads_per_tile", 0) or 256))
-        kw.pop("threads_global", None)
+        kw = fallback_plan_options(fd, self.plan_kw, threads=512)
         return Plan(descs_to_batch(fd), precision=self.precision, record_every=self.record_every, max_spikes=256,
                     device=self.device, **kw)
 

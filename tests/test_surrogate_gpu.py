@@ -187,7 +187,7 @@ def test_fallback_replaces_flagged_cells_with_the_full_solve(native_lib, cuda_de
     r = S.run_surrogate(descs, tight, 2000, record_every=1, fallback=True)
     assert 0 < r.fallback_cells.size <= len(descs)
     fd = [replace(descs[i], probes=[(0, 0.5)]) for i in r.fallback_cells]
-    full = Plan(W.descs_to_batch(fd), precision="f32", record_every=1, **S.fallback_plan_options(fd))
+    full = Plan(W.descs_to_batch(fd), precision="f32", record_every=1, **S.fallback_plan_options(fd, threads=512))
     full.run(2000, DT)
     np.testing.assert_allclose(r.traces[r.fallback_cells], full.traces(), rtol=0, atol=1e-9)
 
