@@ -1110,7 +1110,20 @@ __device__ __forceinline__ void port_stage(PortLocal* pl, int n_ports, const Pul
 template <typename Real>
 __device__ __forceinline__ void port_gru(const PortStage* stage, int n_ports, float* port_h,
                                         const GruWeights* __restrict__ W, Pair<Real>* dr, int64_t m, int warp,
-                                        int n_warps, int lane) {
+                                        int n_warps, int lane, unsigned long long* ptimers) {
+#ifdef BC_PORT_TIMERS
+  long long pt0 = clock64();
+#define BC_PTICK(slot)                                                                                  \
+  do {                                                                                                  \
+    const long long pt1 = clock64();                                                                    \
+    if (warp == 0 && lane == 0 && ptimers) atomicAdd(ptimers + (slot), (unsigned long long)(pt1 - pt0)); \
+    pt0 = pt1;                                                                                          \
+  } while (0)
+#else
+#define BC_PTICK(slot) \
+  do {                 \
+  } while (0)
+#endif
   const int g = lane >> 2, tq = lane & 3;
   const int rd = int(m & 1), wr = rd ^ 1;
   const int n_items = ((n_ports + 15) >> 4) * 8;
@@ -1142,8 +1155,10 @@ __device__ __forceinline__ void port_gru(const PortStage* stage, int n_ports, fl
       const float fa[4] = {xa.x, xa.y, xa.z, xa.w}, fb[4] = {xb.x, xb.y, xb.z, xb.w};
       xblock_frag(fa, fb, tq, ax);
     }
+    BC_PTICK(0);
     float acc[4][4];
     gru_preact(W->wext, jb, g, tq, ah, ax, acc);
+    BC_PTICK(1);
     const float2 wo = *reinterpret_cast<const float2*>(W->wo + j0);
     const GruGate G0 = gru_gate(acc[0][0], acc[1][0], acc[2][0], acc[3][0], hoa.x);
     const GruGate G1 = gru_gate(acc[0][1], acc[1][1], acc[2][1], acc[3][1], hoa.y);
@@ -1159,6 +1174,7 @@ __device__ __forceinline__ void port_gru(const PortStage* stage, int n_ports, fl
     }
     float ysa = wo.x * G0.h_new + wo.y * G1.h_new;
     float ysb = wo.x * G2.h_new + wo.y * G3.h_new;
+    BC_PTICK(2);
     ysa += __shfl_xor_sync(kFullMask, ysa, 1);
     ysa += __shfl_xor_sync(kFullMask, ysa, 2);
     ysb += __shfl_xor_sync(kFullMask, ysb, 1);
@@ -1167,7 +1183,9 @@ __device__ __forceinline__ void port_gru(const PortStage* stage, int n_ports, fl
       if (oka) atomicAdd(&dr[stage[qa].node].y, Real(stage[qa].coef) * Real(ysa));
       if (okb) atomicAdd(&dr[stage[qb].node].y, Real(stage[qb].coef) * Real(ysb));
     }
+    BC_PTICK(3);
   }
+#undef BC_PTICK
 }
 
 template <typename Real>
@@ -1270,7 +1288,7 @@ __global__ void __launch_bounds__(kVar == 2 ? BC_PORT_MAX_THREADS : 1024, kVar =
       port_stage<Real>(plocal, td.n_ports, a.port_pulses, a.port_flags, a.gru, tv.v, tv.dr, pstage, a.step0, dt,
                        tid, T);
       __syncthreads();
-      port_gru<Real>(pstage, td.n_ports, a.port_h, a.gru, tv.dr, a.step0, warp, n_warps, lane);
+      port_gru<Real>(pstage, td.n_ports, a.port_h, a.gru, tv.dr, a.step0, warp, n_warps, lane, a.timers);
       __syncthreads();
     }
   }
@@ -1384,7 +1402,7 @@ __global__ void __launch_bounds__(kVar == 2 ? BC_PORT_MAX_THREADS : 1024, kVar =
                          tid, T);
         __syncthreads();
         BC_TICK(2);
-        port_gru<Real>(pstage, td.n_ports, a.port_h, a.gru, tv.dr, step + 1, warp, n_warps, lane);
+        port_gru<Real>(pstage, td.n_ports, a.port_h, a.gru, tv.dr, step + 1, warp, n_warps, lane, a.timers);
         __syncthreads();
       }
     }

@@ -30,6 +30,7 @@ from .batch import CellBatch
 __all__ = ["TuneResult", "autotune", "sample_cells", "measure_plan"]
 
 TILE_THREADS = ((2500, 512), (2000, 512), (2500, 384), (2000, 256), (1500, 256), (4800, 1024))
+PORT_MAX_THREADS = 384
 LANE_NODES = (1, 2)
 STEPS_PER_LAUNCH = (1000, 250)
 
@@ -80,6 +81,8 @@ def autotune(batch: CellBatch, *, steps: int = 200, dt: float = 0.025, device: i
     ``time_budget_s`` stops the search early (the best options so far are kept).
     """
     sample = sample_cells(batch, max_cells, seed)
+    if sample.port_cell.size:  # the kernel variant with GRU ports runs at most 384 threads per tile
+        tile_threads = [(tn, min(th, PORT_MAX_THREADS)) for tn, th in tile_threads]
     if measure is None:
         def measure(b, o):
             return measure_plan(b, o, steps=steps, dt=dt, device=device, precision=precision)
@@ -97,13 +100,15 @@ def autotune(batch: CellBatch, *, steps: int = 200, dt: float = 0.025, device: i
     def out_of_time() -> bool:
         return time_budget_s is not None and time.perf_counter() - t0 > time_budget_s
 
-    best = {"tile_nodes": tile_threads[0][0], "threads_per_tile": tile_threads[0][1], "threads_big": 512,
+    best = {"tile_nodes": tile_threads[0][0], "threads_per_tile": tile_threads[0][1],
+            "threads_big": tile_threads[0][1] if sample.port_cell.size else 512,
             "lane_nodes": lane_nodes[0], "steps_per_launch": steps_per_launch[0]}
     best_rate = rate_of(best)
     for tn, th in tile_threads:
         if out_of_time():
             break
-        cand = dict(best, tile_nodes=tn, threads_per_tile=th, threads_big=max(th, 512))
+        cand = dict(best, tile_nodes=tn, threads_per_tile=th,
+                    threads_big=th if sample.port_cell.size else max(th, 512))
         r = rate_of(cand)
         if r > best_rate:
             best, best_rate = cand, r
