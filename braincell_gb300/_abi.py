@@ -181,6 +181,7 @@ class BatchSpec(C.Structure):
         ("port_pulse_t_on", _p(C.c_double)),
         ("port_pulse_t_off", _p(C.c_double)),
         ("port_pulse_amp", _p(C.c_double)),
+        ("probe_field", _p(C.c_int32)),
     ]
 
 

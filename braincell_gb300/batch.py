@@ -22,7 +22,7 @@ import numpy as np
 
 from . import _abi
 from .catalogue import region_record
-from .mech import CableProperty, CurrentClamp, ExpSyn, StateProbe
+from .mech import CableProperty, CurrentClamp, ExpSyn, MechanismProbe, StateProbe
 
 __all__ = ["CellBatch", "lower_cell", "concat_batches", "native_lowering"]
 
@@ -57,6 +57,7 @@ class CellBatch:
     probe_cell: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
     probe_branch: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
     probe_x: np.ndarray = field(default_factory=lambda: np.zeros(0, np.float64))
+    probe_field: np.ndarray | None = None  # BC_STATE_* view per probe (None: all V)
     syn_cell: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
     syn_branch: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
     syn_x: np.ndarray = field(default_factory=lambda: np.zeros(0, np.float64))
@@ -118,9 +119,12 @@ class CellBatch:
         "port_pulse_t_on": np.float64,
         "port_pulse_t_off": np.float64,
         "port_pulse_amp": np.float64,
+        "probe_field": np.int32,
     }
 
     def __post_init__(self) -> None:
+        if self.probe_field is None or np.size(self.probe_field) == 0:
+            self.probe_field = np.zeros(np.size(self.probe_cell), np.int32)
         for name, dt in self._DTYPES.items():
             setattr(self, name, np.ascontiguousarray(getattr(self, name), dtype=dt))
         self.region_params = self.region_params.reshape(-1, _abi.BC_NPARAM)
@@ -190,7 +194,7 @@ class CellBatch:
             pulse_x=self.pulse_x[pk][pord], pulse_t_on=self.pulse_t_on[pk][pord],
             pulse_t_off=self.pulse_t_off[pk][pord], pulse_amp=self.pulse_amp[pk][pord],
             probe_cell=new_id[self.probe_cell[qk]][qord], probe_branch=self.probe_branch[qk][qord],
-            probe_x=self.probe_x[qk][qord],
+            probe_x=self.probe_x[qk][qord], probe_field=self.probe_field[qk][qord],
             syn_cell=new_id[self.syn_cell[syn_old]], syn_branch=self.syn_branch[syn_old], syn_x=self.syn_x[syn_old],
             syn_tau=self.syn_tau[syn_old], syn_e=self.syn_e[syn_old],
             conn_pre=new_id[self.conn_pre[ck]], conn_post=new_syn[self.conn_post[ck]],
@@ -217,6 +221,8 @@ class CellBatch:
         nc = self.conn_pre.size
         if any(getattr(self, k).size != nc for k in ("conn_post", "conn_weight", "conn_delay")):
             raise ValueError("connection arrays must all have n_connections entries.")
+        if self.probe_field.size != self.probe_cell.size:
+            raise ValueError("probe_field must have one entry per probe.")
         npt = self.port_cell.size
         if any(getattr(self, k).shape[0] != npt for k in ("port_branch", "port_g", "port_e", "port_feat")):
             raise ValueError("port arrays must all have n_ports entries.")
@@ -305,7 +311,7 @@ def concat_batches(batches: list[CellBatch]) -> CellBatch:
         parts["port_cell"].append(b.port_cell + cell_off)
         parts["port_pulse_port"].append(b.port_pulse_port + port_off)
         for k in ("pulse_branch", "pulse_x", "pulse_t_on", "pulse_t_off", "pulse_amp", "probe_branch", "probe_x",
-                  "syn_branch", "syn_x", "syn_tau", "syn_e", "conn_weight", "conn_delay", "port_branch", "port_g",
+                  "syn_branch", "syn_x", "syn_tau", "syn_e", "conn_weight", "conn_delay", "probe_field", "port_branch", "port_g",
                   "port_e", "port_feat", "port_pulse_t_on", "port_pulse_t_off", "port_pulse_amp"):
             parts[k].append(getattr(b, k))
         syn_off += int(b.syn_cell.size)
@@ -315,6 +321,36 @@ def concat_batches(batches: list[CellBatch]) -> CellBatch:
         cell_off += nc
     kw = {k: np.concatenate(v) for k, v in parts.items()}
     return CellBatch(n_regions=R, **kw)
+
+
+# (mechanism class, field) -> BC_STATE_* view recorded by a MechanismProbe
+PROBE_STATES = {
+    ("Na_Ba2002", "p"): _abi.BC_STATE_NA_P, ("Na_Ba2002", "q"): _abi.BC_STATE_NA_Q,
+    ("KDR_Ba2002", "p"): _abi.BC_STATE_KDR_P,
+    ("CaL_IS2008", "p"): _abi.BC_STATE_CAL_P, ("CaL_IS2008", "q"): _abi.BC_STATE_CAL_Q,
+    ("CaT_HM1992", "p"): _abi.BC_STATE_CAT_P, ("CaT_HM1992", "q"): _abi.BC_STATE_CAT_Q,
+    ("HCN_HM1992", "p"): _abi.BC_STATE_HCN_P,
+    ("AHP_De1994", "p"): _abi.BC_STATE_AHP_P,
+    ("CalciumDetailed", "Ci"): _abi.BC_STATE_CA_CI,
+    ("Na_HH1952", "p"): _abi.BC_STATE_NAHH_P, ("Na_HH1952", "q"): _abi.BC_STATE_NAHH_Q,
+    ("K_HH1952", "p"): _abi.BC_STATE_KHH_P,
+    ("KM_RI2021_SC", "n"): _abi.BC_STATE_KM_N,
+}
+
+
+def probe_field_of(decl, mechs) -> int:
+    """The BC_STATE_* view a MechanismProbe records, resolved against the mechanisms
+    painted where it sits: ``decl.mechanism`` is a painted mechanism's instance name or
+    class name (``_multi_compartment/probes.py:136-181`` looks it up the same way)."""
+    hits = [m for m in mechs if getattr(m, "instance_name", None) == decl.mechanism]
+    if len(hits) > 1:
+        raise ValueError(f"Probe {decl.name!r} matched multiple mechanisms named {decl.mechanism!r}.")
+    if not hits:
+        raise KeyError(f"Probe {decl.name!r} could not find a mechanism or ion named {decl.mechanism!r} here.")
+    key = (hits[0].class_name, decl.field)
+    if key not in PROBE_STATES:
+        raise KeyError(f"Probe {decl.name!r} field {decl.field!r} was not found on {hits[0].class_name}.")
+    return int(PROBE_STATES[key])
 
 
 def _branch_regions(cell) -> tuple[np.ndarray, list[tuple[CableProperty, list]]]:
@@ -374,7 +410,7 @@ def lower_cell(cell, replicas: int | None = None) -> CellBatch:
         if cell.V_init is not None:
             params[r, _abi.BC_P_VREST] = float(cell.V_init)
     pulses: list[tuple[int, float, float, float, float]] = []
-    probes: list[tuple[int, float]] = []
+    probes: list[tuple[int, float, int]] = []
     syns: list[tuple[int, float, float, float]] = []
     for locset, decls in cell.place_rules:
         for (b, x) in locset.points(morpho):
@@ -383,7 +419,9 @@ def lower_cell(cell, replicas: int | None = None) -> CellBatch:
                     for (t_on, t_off, amp) in d.segments():
                         pulses.append((b, x, t_on, t_off, amp))
                 elif isinstance(d, StateProbe):
-                    probes.append((b, x))
+                    probes.append((b, x, 0))
+                elif isinstance(d, MechanismProbe):
+                    probes.append((b, x, probe_field_of(d, regions[int(branch_region[b])][1])))
                 elif isinstance(d, ExpSyn):
                     syns.append((b, x, d.tau, d.e))
                 else:
@@ -413,6 +451,7 @@ def lower_cell(cell, replicas: int | None = None) -> CellBatch:
         probe_cell=np.zeros(len(probes), np.int32),
         probe_branch=np.asarray([p[0] for p in probes], np.int32),
         probe_x=np.asarray([p[1] for p in probes]),
+        probe_field=np.asarray([p[2] for p in probes], np.int32),
         syn_cell=np.zeros(len(syns), np.int32),
         syn_branch=np.asarray([q[0] for q in syns], np.int32),
         syn_x=np.asarray([q[1] for q in syns]),

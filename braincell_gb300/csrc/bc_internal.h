@@ -90,7 +90,7 @@ struct TileDesc {
   int64_t probe_offset;     // into plan probe array
   // byte offsets inside the blob
   int32_t off_v;            // (V_hi, V_lo) pairs
-  int32_t pad2;
+  int32_t off_plist;        // the tile's probe list (ProbeRef)
   int64_t state_offset;     // elements into the plan's global mechanism-state array ([slot][n_nodes])
   int32_t off_ab;           // (alpha, beta) pairs
   int32_t off_diag0, off_pidx, off_spec, off_specs;
@@ -205,17 +205,24 @@ struct PulseRec {
   double t_on, t_off;
 };
 
-// A node with clamp pulses, a probe and/or synapses: its pulses are
-// pulse_begin .. pulse_end of the tile's pulse list (sorted by node), its probe id
-// is `probe` (-1: none), its synapses are entries syn_begin .. syn_end of the
-// tile's synapse list (global synapse ids).
+// A node with clamp pulses, probes and/or synapses: its pulses are pulse_begin ..
+// pulse_end of the tile's pulse list (sorted by node), its probes are entries
+// probe_begin .. probe_end of the tile's probe list, its synapses are entries
+// syn_begin .. syn_end of the tile's synapse list (global synapse ids).
 struct SpecRec {
   int32_t pulse_begin;
   int32_t pulse_end;
-  int32_t probe;
+  int32_t probe_begin;
   int32_t syn_begin;
   int32_t syn_end;
-  int32_t pad[3];
+  int32_t probe_end;
+  int32_t pad[2];
+};
+
+// An entry of a tile's probe list: the plan probe id and the BC_STATE_* view it records.
+struct ProbeRef {
+  int32_t id;
+  int32_t field;
 };
 
 // Kernel launch parameters (by value).

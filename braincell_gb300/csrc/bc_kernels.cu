@@ -126,6 +126,7 @@ struct TileView {
   const uint16_t *pidx, *spec, *crec;
   const ChainRec* chains;
   const SpecRec* specs;
+  const ProbeRef* plist;
   const uint32_t* mech;
   Real *scd, *scr;
   const int32_t* syn;       // tile synapse list (global synapse ids)
@@ -149,6 +150,7 @@ struct TileView {
     spec = reinterpret_cast<const uint16_t*>(base + td.off_spec);
     chains = reinterpret_cast<const ChainRec*>(base + td.off_chains);
     specs = reinterpret_cast<const SpecRec*>(base + td.off_specs);
+    plist = reinterpret_cast<const ProbeRef*>(base + td.off_plist);
     mech = reinterpret_cast<const uint32_t*>(base + td.off_mech);
     scd = reinterpret_cast<Real*>(scratch + td.off_scd);
     scr = reinterpret_cast<Real*>(scratch + td.off_scr);
@@ -210,6 +212,15 @@ __device__ __forceinline__ void load_states(const Real* st, int N, uint32_t m, N
     s.cahi = st[kSlotCaHi * N];
     s.calo = st[kSlotCaLo * N];
   }
+}
+
+// The value a mechanism probe records: state view `field` (a BC_STATE_* other
+// than V) of the node whose states start at st, after the node's update.
+template <typename Real>
+__device__ __forceinline__ double probe_state(const Real* st, int N, int field) {
+  if (field == BC_STATE_CA_CI) return double(st[kSlotCaHi * N]) + double(st[kSlotCaLo * N]);
+  const int slot = field <= BC_STATE_AHP_P ? field - 1 : field;  // slots 9, 10 hold Ci
+  return double(st[slot * N]);
 }
 
 // Channels outside the main workloads' mix (classic Hodgkin-Huxley Na / K and the
@@ -1367,17 +1378,23 @@ __global__ void __launch_bounds__(kVar == 2 ? BC_PORT_MAX_THREADS : 1024, kVar =
           tv.stamp[lc] = int32_t(step & 0x7fffffff);
       }
       if (sp != kNoSpecial) {
-        if (sr.probe >= 0) {
+        for (int k = sr.probe_begin; k < sr.probe_end; ++k) {
+          const ProbeRef pf = tv.plist[k];
           const double v1 = double(hi) + double(lo), v0 = double(v_old) + double(lo_old);
-          if (v0 < 0.0 && v1 >= 0.0) {
-            const int n = a.spike_count[sr.probe];
-            if (n < a.max_spikes)
-              a.spike_times[int64_t(sr.probe) * a.max_spikes + n] = double(step) * a.dt + a.dt * (0.0 - v0) / (v1 - v0);
-            a.spike_count[sr.probe] = n + 1;
+          double val = v1;
+          if (pf.field == BC_STATE_V) {
+            if (v0 < 0.0 && v1 >= 0.0) {
+              const int n = a.spike_count[pf.id];
+              if (n < a.max_spikes)
+                a.spike_times[int64_t(pf.id) * a.max_spikes + n] = double(step) * a.dt + a.dt * (0.0 - v0) / (v1 - v0);
+              a.spike_count[pf.id] = n + 1;
+            }
+          } else {
+            val = probe_state(tv.state + i, tv.N, pf.field);
           }
           if (record) {
             const int64_t slot = k_since / a.record_every - 1;
-            if (slot >= 0 && slot < a.trace_cap) a.traces[slot * a.n_probes_total + sr.probe] = v1;
+            if (slot >= 0 && slot < a.trace_cap) a.traces[slot * a.n_probes_total + pf.id] = val;
           }
         }
         if (!last) add_node_pulses(tv, pulses, sr, i, pr, step + 1, dt);

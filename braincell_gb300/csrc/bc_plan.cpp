@@ -541,9 +541,6 @@ static bc_status build_tile(const BuildCtx& cx, const TileBuild& tb, int T, Tile
   std::stable_sort(tpulse.begin(), tpulse.end(),
                    [](const std::pair<int32_t, int64_t>& x, const std::pair<int32_t, int64_t>& y) { return x.first < y.first; });
   std::sort(tprobe.begin(), tprobe.end());
-  for (size_t k = 1; k < tprobe.size(); ++k)
-    if (tprobe[k].first == tprobe[k - 1].first)
-      return fail(BC_ERR_INVALID, "two probes at the same point of a cell are not supported");
   std::vector<int32_t> spec_nodes;
   for (auto& x : tpulse) spec_nodes.push_back(x.first);
   for (auto& x : tprobe) spec_nodes.push_back(x.first);
@@ -586,6 +583,8 @@ static bc_status build_tile(const BuildCtx& cx, const TileBuild& tb, int T, Tile
   off = align16(off + size_t(n_params) * 4);
   d.off_syn = int32_t(off);
   off = align16(off + tsyn.size() * 4);
+  d.off_plist = int32_t(off);
+  off = align16(off + tprobe.size() * sizeof(ProbeRef));
   d.n_cells = int32_t(cell_list.size());
   d.off_ncell = -1;
   d.off_srccell = -1;
@@ -674,7 +673,7 @@ static bc_status build_tile(const BuildCtx& cx, const TileBuild& tb, int T, Tile
     }
     for (size_t q = 0; q < spec_nodes.size(); ++q) {
       spec[spec_nodes[q]] = uint16_t(q);
-      specs[q] = SpecRec{0, 0, -1, 0, 0, {0, 0, 0}};
+      specs[q] = SpecRec{0, 0, 0, 0, 0, 0, {0, 0}};
     }
     size_t kp = 0;
     for (size_t q = 0; q < spec_nodes.size(); ++q) {
@@ -724,7 +723,21 @@ static bc_status build_tile(const BuildCtx& cx, const TileBuild& tb, int T, Tile
       std::memcpy(b.data() + d.off_ncell, ncell.data(), ncell.size() * 2);
       std::memcpy(b.data() + d.off_srccell, src.data(), src.size() * 4);
     }
-    for (auto& x : tprobe) specs[spec[x.first]].probe = int32_t(x.second);
+    {
+      // probes in node order (tprobe is sorted): each special node owns a range
+      std::vector<ProbeRef> plist(tprobe.size());
+      size_t kq = 0;
+      for (size_t q = 0; q < spec_nodes.size(); ++q) {
+        specs[q].probe_begin = int32_t(kq);
+        while (kq < tprobe.size() && tprobe[kq].first == spec_nodes[q]) {
+          const int64_t pid = tprobe[kq].second;
+          plist[kq] = ProbeRef{int32_t(pid), s.probe_field ? s.probe_field[pid] : BC_STATE_V};
+          ++kq;
+        }
+        specs[q].probe_end = int32_t(kq);
+      }
+      if (!plist.empty()) std::memcpy(b.data() + d.off_plist, plist.data(), plist.size() * sizeof(ProbeRef));
+    }
     std::memcpy(b.data() + d.off_spec, spec.data(), spec.size() * 2);
     if (!specs.empty()) std::memcpy(b.data() + d.off_specs, specs.data(), specs.size() * sizeof(SpecRec));
   }
@@ -1137,6 +1150,22 @@ bc_status bc_plan_create(const bc_batch_spec* spec, const bc_plan_options* opts_
     if (v < 0) {
       delete p;
       return fail(BC_ERR_INVALID, "probe location not found");
+    }
+    const int32_t field = s.probe_field ? s.probe_field[k] : BC_STATE_V;
+    if (field < 0 || field >= BC_NSTATE_VIEW) {
+      delete p;
+      return fail(BC_ERR_INVALID, "probe_field is not a BC_STATE_* view");
+    }
+    if (field != BC_STATE_V) {
+      // the mechanism that owns the state must be present at the probed CV
+      static const uint32_t owner[BC_NSTATE_VIEW] = {0,          BC_M_NA,    BC_M_NA,    BC_M_KDR,   BC_M_CAL,
+                                                     BC_M_CAL,   BC_M_CAT,   BC_M_CAT,   BC_M_HCN,   BC_M_AHP,
+                                                     BC_M_CADET, BC_M_NAHH,  BC_M_NAHH,  BC_M_KHH,   BC_M_KM};
+      const int32_t rg = cells[c].region[v];
+      if (rg < 0 || !(s.region_mech[c * s.n_regions + rg] & owner[field])) {
+        delete p;
+        return fail(BC_ERR_INVALID, "probe field: no such mechanism at the probed location");
+      }
     }
     cell_probes[c].push_back(k);
     probe_node[c].push_back(v);

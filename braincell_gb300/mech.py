@@ -30,6 +30,7 @@ __all__ = [
     "Ion",
     "CurrentClamp",
     "StateProbe",
+    "MechanismProbe",
     "AllRegion",
     "BranchInFilter",
     "branch_in",
@@ -163,6 +164,29 @@ class StateProbe:
             raise ValueError(f"StateProbe.name must be a non-empty string or None, got {self.name!r}.")
         if self.field != "v":
             raise ValueError(f"Unsupported StateProbe field {self.field!r}; only 'v' is supported.")
+
+
+@dataclass(frozen=True)
+class MechanismProbe:
+    """Probe of a named mechanism's state at a placed location
+    (``mech/_point.py:330``, sampled as ``_multi_compartment/probes.py:136-181``).
+
+    ``mechanism`` is a channel class name (or the ``name`` of a painted Channel) and
+    ``field`` one of its gates ("p", "q", "n"), or an ion class with field "Ci".  The
+    probe records the state after every recorded step.
+    """
+
+    mechanism: str
+    field: str
+    name: str | None = None
+
+    def __post_init__(self) -> None:
+        if self.name is not None and (not isinstance(self.name, str) or not self.name):
+            raise ValueError(f"MechanismProbe.name must be a non-empty string or None, got {self.name!r}.")
+        for field_name in ("mechanism", "field"):
+            value = getattr(self, field_name)
+            if not isinstance(value, str) or not value:
+                raise ValueError(f"MechanismProbe.{field_name} must be a non-empty string, got {value!r}.")
 
 
 # ----------------------------------------------------------------------------

@@ -183,6 +183,11 @@ typedef struct bc_batch_spec {
   const double* port_pulse_t_on;      /* ms                                     */
   const double* port_pulse_t_off;     /* ms                                     */
   const double* port_pulse_amp;       /* nA                                     */
+  /* what each probe records (mech/_point.py StateProbe / MechanismProbe,
+     sampled as _multi_compartment/probes.py:44-137 does): a BC_STATE_* view --
+     0 = V, else the named gate or Ci of the mechanism at the probe's CV, after
+     the step.  Null: every probe records V.                                    */
+  const int32_t* probe_field;         /* [n_probes]                             */
 } bc_batch_spec;
 
 /* ------------------------------------------------------------------ plan options */

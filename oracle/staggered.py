@@ -661,11 +661,12 @@ class OracleCell:
         self.Ci_fixed = np.full(n, _CA_FIXED_CI)
 
     def _points(self, cell) -> None:
-        from braincell_gb300.mech import CurrentClamp, ExpSyn, StateProbe
+        from braincell_gb300.mech import CurrentClamp, ExpSyn, MechanismProbe, StateProbe
 
         self.clamps_mid = []  # (point, t_on, t_off, amp_nA)
         self.clamps_edge = []
         self.probe_points = []
+        self.probe_what = []  # None: V; else ("gate", channel, gate) or ("Ci",)
         self.syn_points, self.syn_tau, self.syn_e = [], [], []  # ExpSyn at CV midpoints
         for locset, decls in cell.place_rules:
             for (b, x) in locset.points(self.morpho):
@@ -683,6 +684,11 @@ class OracleCell:
                             (self.clamps_mid if self.is_mid[pid] else self.clamps_edge).append((pid, t_on, t_off, amp))
                     elif isinstance(d, StateProbe):
                         self.probe_points.append(pid)
+                        self.probe_what.append(None)
+                    elif isinstance(d, MechanismProbe):
+                        # probes.py:136-181: the named mechanism's (or ion's) field at the point
+                        self.probe_points.append(pid)
+                        self.probe_what.append(self._probe_key(cell, b, d))
                     elif isinstance(d, ExpSyn):
                         if not self.is_mid[pid]:
                             raise ValueError("ExpSyn must sit inside a CV, not on a branch end point.")
@@ -691,6 +697,20 @@ class OracleCell:
                         self.syn_e.append(d.e)
         self.point_area_um2 = np.zeros(self.n_point)
         self.point_area_um2[self.cv_mid] = self.cv_area
+
+    def _probe_key(self, cell, b: int, d):
+        names = {}
+        for region, decls in cell.paint_rules:
+            if region.branch_mask(self.morpho)[b]:
+                for m in decls:
+                    if hasattr(m, "class_name"):
+                        names[m.instance_name] = m.class_name
+        if d.mechanism not in names:
+            raise KeyError(f"no mechanism named {d.mechanism!r} at the probe")
+        cls = names[d.mechanism]
+        if d.field == "Ci":
+            return ("Ci",)
+        return ("gate", cls, d.field)
 
     # ------------------------------------------------------------ surrogate ports
     def set_ports(self, ports, theta, v_scale: float, y_scale: float) -> None:
@@ -951,7 +971,7 @@ class OracleCell:
             Vold = self.V.copy()
             self.step(dt, t)
             for j, c in enumerate(probe_cv):
-                if c is None:
+                if c is None or (j < len(self.probe_what) and self.probe_what[j] is not None):
                     continue
                 v0, v1 = Vold[:, c], self.V[:, c]
                 hit = (v0 < self.V_th) & (v1 >= self.V_th)
@@ -959,7 +979,16 @@ class OracleCell:
                     frac = (self.V_th - v0[p]) / (v1[p] - v0[p])
                     spikes[p][j].append(t + dt * frac)
             if (s + 1) % record_every == 0:
-                traces.append(np.stack([self.V[:, c] if c is not None else np.full(self.P, np.nan)
-                                        for c in probe_cv], axis=1))
+                row = []
+                for j, c in enumerate(probe_cv):
+                    what = self.probe_what[j] if j < len(self.probe_what) else None
+                    pid = self.probe_points[j]
+                    if what is None:
+                        row.append(self.V[:, c] if c is not None else np.full(self.P, np.nan))
+                    elif what[0] == "Ci":
+                        row.append(self.Ci[:, pid])
+                    else:
+                        row.append(self.gates[(what[1], what[2])][:, pid])
+                traces.append(np.stack(row, axis=1))
         tr = np.stack(traces, axis=-1) if traces else np.zeros((self.P, len(probe_cv), 0))
         return tr, spikes
