@@ -85,12 +85,12 @@ struct TileDesc {
   int32_t n_params;         // param records in this tile
   int32_t n_pulses;
   int64_t pulse_offset;     // into plan pulse array
-  int32_t n_probes;
+  int32_t n_xprobes;        // mechanism probes of the tile (ProbeRef list at off_plist)
   int32_t pad0;
   int64_t probe_offset;     // into plan probe array
   // byte offsets inside the blob
   int32_t off_v;            // (V_hi, V_lo) pairs
-  int32_t off_plist;        // the tile's probe list (ProbeRef)
+  int32_t off_plist;        // the tile's mechanism-probe list (ProbeRef)
   int64_t state_offset;     // elements into the plan's global mechanism-state array ([slot][n_nodes])
   int32_t off_ab;           // (alpha, beta) pairs
   int32_t off_diag0, off_pidx, off_spec, off_specs;
@@ -205,24 +205,26 @@ struct PulseRec {
   double t_on, t_off;
 };
 
-// A node with clamp pulses, probes and/or synapses: its pulses are pulse_begin ..
-// pulse_end of the tile's pulse list (sorted by node), its probes are entries
-// probe_begin .. probe_end of the tile's probe list, its synapses are entries
-// syn_begin .. syn_end of the tile's synapse list (global synapse ids).
+// A node with clamp pulses, a voltage probe and/or synapses: its pulses are
+// pulse_begin .. pulse_end of the tile's pulse list (sorted by node), its voltage
+// probe id is `probe` (-1: none), its synapses are entries syn_begin .. syn_end of
+// the tile's synapse list (global synapse ids).
 struct SpecRec {
   int32_t pulse_begin;
   int32_t pulse_end;
-  int32_t probe_begin;
+  int32_t probe;
   int32_t syn_begin;
   int32_t syn_end;
-  int32_t probe_end;
-  int32_t pad[2];
+  int32_t pad[3];
 };
 
-// An entry of a tile's probe list: the plan probe id and the BC_STATE_* view it records.
+// A mechanism probe of a tile: its node, plan probe id and BC_STATE_* view
+// (recorded in a pass of its own after the update pass).
 struct ProbeRef {
+  int32_t node;
   int32_t id;
   int32_t field;
+  int32_t pad;
 };
 
 // Kernel launch parameters (by value).
@@ -268,9 +270,9 @@ struct LaunchArgs {
 };
 
 // Host-callable launchers implemented in bc_kernels.cu.
-// variant: 0 = the lean kernel; 1 = the plan uses synapses, a network, or a
-// mechanism of the out-of-line set (classic HH Na / K, M current); 2 = as 1 plus
-// subtree-surrogate ports.
+// variant: 0 = the lean kernel; 1 = the plan uses synapses, a network, mechanism
+// probes, or a mechanism of the out-of-line set (classic HH Na / K, M current);
+// 2 = as 1 plus subtree-surrogate ports.
 int launch_tiles(const LaunchArgs& a, int precision, bool smem, int threads, size_t smem_bytes, int variant,
                  void* stream);
 // Kernel-node parameters of the same launch for a CUDA graph.  kernelParams

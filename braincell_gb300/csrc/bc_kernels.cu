@@ -126,7 +126,6 @@ struct TileView {
   const uint16_t *pidx, *spec, *crec;
   const ChainRec* chains;
   const SpecRec* specs;
-  const ProbeRef* plist;
   const uint32_t* mech;
   Real *scd, *scr;
   const int32_t* syn;       // tile synapse list (global synapse ids)
@@ -150,7 +149,6 @@ struct TileView {
     spec = reinterpret_cast<const uint16_t*>(base + td.off_spec);
     chains = reinterpret_cast<const ChainRec*>(base + td.off_chains);
     specs = reinterpret_cast<const SpecRec*>(base + td.off_specs);
-    plist = reinterpret_cast<const ProbeRef*>(base + td.off_plist);
     mech = reinterpret_cast<const uint32_t*>(base + td.off_mech);
     scd = reinterpret_cast<Real*>(scratch + td.off_scd);
     scr = reinterpret_cast<Real*>(scratch + td.off_scr);
@@ -1378,29 +1376,34 @@ __global__ void __launch_bounds__(kVar == 2 ? BC_PORT_MAX_THREADS : 1024, kVar =
           tv.stamp[lc] = int32_t(step & 0x7fffffff);
       }
       if (sp != kNoSpecial) {
-        for (int k = sr.probe_begin; k < sr.probe_end; ++k) {
-          const ProbeRef pf = tv.plist[k];
+        if (sr.probe >= 0) {
           const double v1 = double(hi) + double(lo), v0 = double(v_old) + double(lo_old);
-          double val = v1;
-          if (pf.field == BC_STATE_V) {
-            if (v0 < 0.0 && v1 >= 0.0) {
-              const int n = a.spike_count[pf.id];
-              if (n < a.max_spikes)
-                a.spike_times[int64_t(pf.id) * a.max_spikes + n] = double(step) * a.dt + a.dt * (0.0 - v0) / (v1 - v0);
-              a.spike_count[pf.id] = n + 1;
-            }
-          } else {
-            val = probe_state(tv.state + i, tv.N, pf.field);
+          if (v0 < 0.0 && v1 >= 0.0) {
+            const int n = a.spike_count[sr.probe];
+            if (n < a.max_spikes)
+              a.spike_times[int64_t(sr.probe) * a.max_spikes + n] = double(step) * a.dt + a.dt * (0.0 - v0) / (v1 - v0);
+            a.spike_count[sr.probe] = n + 1;
           }
           if (record) {
             const int64_t slot = k_since / a.record_every - 1;
-            if (slot >= 0 && slot < a.trace_cap) a.traces[slot * a.n_probes_total + pf.id] = val;
+            if (slot >= 0 && slot < a.trace_cap) a.traces[slot * a.n_probes_total + sr.probe] = v1;
           }
         }
         if (!last) add_node_pulses(tv, pulses, sr, i, pr, step + 1, dt);
       }
     }
     __syncthreads();
+    if (kExtra && record && td.n_xprobes > 0) {
+      // mechanism probes (plans with them run the extra variant): state views after the update
+      const ProbeRef* pl = reinterpret_cast<const ProbeRef*>(reinterpret_cast<const unsigned char*>(tv.specs) +
+                                                             (td.off_plist - td.off_specs));
+      const int64_t slot = k_since / a.record_every - 1;
+      for (int q = tid; q < td.n_xprobes; q += T) {
+        const ProbeRef r = pl[q];
+        if (slot >= 0 && slot < a.trace_cap)
+          a.traces[slot * a.n_probes_total + r.id] = probe_state(tv.state + r.node, tv.N, r.field);
+      }
+    }
     if (kExtra && tv.has_src)
       for (int c = tid; c < tv.n_cells; c += T)
         if (tv.stamp[c] == int32_t(step & 0x7fffffff) && tv.srccell[c] >= 0) {

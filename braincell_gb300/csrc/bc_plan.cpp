@@ -66,7 +66,7 @@ struct bc_plan {
   int record_every = 1;
   int max_spikes = 64;
   int use_graph = 0;
-  bool extra = false;  // synapses, a network, or a region using the out-of-line mechanism set
+  bool extra = false;  // synapses, a network, mechanism probes, or a region using the out-of-line mechanism set
   int state_slots = 1;
   int64_t n_cells = 0, n_cv = 0, n_nodes = 0, n_probes = 0, n_pulses = 0;
   int64_t max_phases = 0, max_chain_nodes = 0;
@@ -673,7 +673,7 @@ static bc_status build_tile(const BuildCtx& cx, const TileBuild& tb, int T, Tile
     }
     for (size_t q = 0; q < spec_nodes.size(); ++q) {
       spec[spec_nodes[q]] = uint16_t(q);
-      specs[q] = SpecRec{0, 0, 0, 0, 0, 0, {0, 0}};
+      specs[q] = SpecRec{0, 0, -1, 0, 0, {0, 0, 0}};
     }
     size_t kp = 0;
     for (size_t q = 0; q < spec_nodes.size(); ++q) {
@@ -725,17 +725,19 @@ static bc_status build_tile(const BuildCtx& cx, const TileBuild& tb, int T, Tile
     }
     {
       // probes in node order (tprobe is sorted): each special node owns a range
-      std::vector<ProbeRef> plist(tprobe.size());
-      size_t kq = 0;
-      for (size_t q = 0; q < spec_nodes.size(); ++q) {
-        specs[q].probe_begin = int32_t(kq);
-        while (kq < tprobe.size() && tprobe[kq].first == spec_nodes[q]) {
-          const int64_t pid = tprobe[kq].second;
-          plist[kq] = ProbeRef{int32_t(pid), s.probe_field ? s.probe_field[pid] : BC_STATE_V};
-          ++kq;
+      std::vector<ProbeRef> plist;
+      for (const auto& x : tprobe) {
+        const int64_t pid = x.second;
+        const int32_t field = s.probe_field ? s.probe_field[pid] : BC_STATE_V;
+        if (field != BC_STATE_V) {
+          plist.push_back(ProbeRef{x.first, int32_t(pid), field, 0});
+        } else {
+          SpecRec& sr = specs[spec[x.first]];
+          if (sr.probe >= 0) return fail(BC_ERR_INVALID, "two voltage probes at the same point of a cell are not supported");
+          sr.probe = int32_t(pid);
         }
-        specs[q].probe_end = int32_t(kq);
       }
+      d.n_xprobes = int32_t(plist.size());
       if (!plist.empty()) std::memcpy(b.data() + d.off_plist, plist.data(), plist.size() * sizeof(ProbeRef));
     }
     std::memcpy(b.data() + d.off_spec, spec.data(), spec.size() * 2);
@@ -1173,6 +1175,8 @@ bc_status bc_plan_create(const bc_batch_spec* spec, const bc_plan_options* opts_
   }
   p->n_probes = s.n_probes;
   p->n_pulses = s.n_pulses;
+  // mechanism probes are recorded by the extra kernel variant only
+  for (int64_t k = 0; s.probe_field && k < s.n_probes; ++k) p->extra = p->extra || s.probe_field[k] != BC_STATE_V;
   // ---------------------------------------------------- synapses / connections
   std::vector<std::vector<std::pair<int64_t, int32_t>>> cell_syns(s.n_cells);
   std::vector<char> is_src(s.n_cells, 0);
