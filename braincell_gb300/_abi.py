@@ -198,7 +198,7 @@ class PlanOptions(C.Structure):
         ("device", C.c_int32),
         ("threads_big", C.c_int32),
         ("threads_global", C.c_int32),
-        ("reserved_a", C.c_int32),
+        ("narrow_lane_nodes", C.c_int32),
         ("reserved_b", C.c_float),
         ("dry_run", C.c_int32),
         ("reserved", C.c_int32 * 2),

@@ -62,6 +62,7 @@ struct bc_plan {
   int threads_global = 512;
   int tile_nodes = 0;
   int lane_nodes = 1;
+  int narrow_lane_nodes = 1;
   int steps_per_launch = 1000;
   int record_every = 1;
   int max_spikes = 64;
@@ -312,6 +313,7 @@ struct BuildCtx {
   int precision;
   int state_slots;
   int lane_nodes;  // nodes a lane walks serially in a warp slot
+  int narrow_lane_nodes;  // the same in phases with fewer nodes than 32 x warps
 };
 
 template <typename Real>
@@ -359,7 +361,8 @@ static bc_status build_tile(const BuildCtx& cx, const TileBuild& tb, int T, Tile
     if (!v.empty()) phases.push_back(std::move(v));
   const int n_phases = int(phases.size());
   const int W = std::max(1, T / 32);
-  const int C = std::max(1, cx.lane_nodes);
+  const int C_wide = std::max(1, cx.lane_nodes);
+  const int C_narrow = cx.narrow_lane_nodes > 0 ? cx.narrow_lane_nodes : C_wide;
   std::vector<ChainRec> chains;
   std::vector<RecSpec> rec_src;
   std::vector<SlotRec> slots;
@@ -381,6 +384,11 @@ static bc_status build_tile(const BuildCtx& cx, const TileBuild& tb, int T, Tile
   for (int p = 0; p < n_phases; ++p) {
     std::vector<CRef>& v = phases[p];
     std::stable_sort(v.begin(), v.end(), [](const CRef& a, const CRef& b) { return a.L > b.L; });
+    // a phase with fewer nodes than one unit slot per warp is latency-bound: short
+    // chains there are walked serially (C_narrow) rather than scanned
+    int64_t phase_nodes = 0;
+    for (const CRef& c : v) phase_nodes += c.L;
+    const int C = phase_nodes < int64_t(32) * W ? C_narrow : C_wide;
     std::vector<Slot> ps;
     // chains longer than a lane's share: split into near-equal parts over lanes
     std::vector<Lane> lanes;
@@ -1095,6 +1103,7 @@ bc_status bc_plan_create(const bc_batch_spec* spec, const bc_plan_options* opts_
   p->use_graph = opts.use_graph;
   p->steps_per_launch = opts.steps_per_launch > 0 ? opts.steps_per_launch : 1000;
   p->lane_nodes = opts.lane_nodes > 0 ? opts.lane_nodes : 1;
+  p->narrow_lane_nodes = opts.narrow_lane_nodes > 0 ? opts.narrow_lane_nodes : p->lane_nodes;
   p->n_cells = s.n_cells;
   // ---------------------------------------------------- lower
   std::vector<LoweredCell> cells(s.n_cells);
@@ -1371,7 +1380,7 @@ bc_status bc_plan_create(const bc_batch_spec* spec, const bc_plan_options* opts_
     if (tile_nodes - nn > 0) room.emplace(tile_nodes - nn, builds.size() - 1);
   }
   BuildCtx cx{&s, &cells, &sched, &cv_base, &cell_pulses, &cell_probes, &pulse_node, &probe_node, &cell_syns, &is_src,
-              &cell_ports, &port_pulse_ids, p->precision, S, p->lane_nodes};
+              &cell_ports, &port_pulse_ids, p->precision, S, p->lane_nodes, p->narrow_lane_nodes};
   std::vector<TileOut> outs;
   outs.reserve(builds.size());
   // Packed tiles: tile_nodes sets how many CTAs share an SM (by the per-node
@@ -1605,7 +1614,9 @@ bc_status bc_plan_create(const bc_batch_spec* spec, const bc_plan_options* opts_
   }
   BC_TRYC(cudaEventCreateWithFlags(&p->ev_fork, cudaEventDisableTiming));
   *out = p;
-  return bc_reset(p, nullptr);
+  // the initial reset runs on the plan's own non-blocking stream, so that creating
+  // a plan does not wait for work other plans have queued on the legacy stream
+  return bc_reset(p, p->aux[0]);
 }
 
 bc_status bc_lower_cell(const bc_batch_spec* spec, int64_t cell, int32_t* n_cv, int32_t* n_node, double* cv_area,

@@ -41,6 +41,7 @@ class Plan:
         threads_per_tile: int = 0,
         tile_nodes: int = 0,
         lane_nodes: int = 0,
+        narrow_lane_nodes: int = 0,
         steps_per_launch: int = 0,
         record_every: int = 1,
         max_spikes: int = 64,
@@ -62,6 +63,7 @@ class Plan:
         opts.threads_per_tile = int(threads_per_tile)
         opts.tile_nodes = int(tile_nodes)
         opts.lane_nodes = int(lane_nodes)
+        opts.narrow_lane_nodes = int(narrow_lane_nodes)
         opts.steps_per_launch = int(steps_per_launch)
         opts.record_every = int(record_every)
         opts.max_spikes = int(max_spikes)

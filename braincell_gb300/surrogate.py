@@ -373,16 +373,17 @@ def train_surrogate(n_cells: int = 460, *, seed: int = 3, n_steps: int = 8000, d
 
 
 # ----------------------------------------------------------------------------- running
-def fallback_plan_options(descs, base: dict | None = None, threads: int = 256, n_sm: int = 152) -> dict:
-    """Plan options for the full solve of a few fallback cells: tiles small enough
-    that they cover every SM about twice (a small batch is bound by the latency of
-    one tile, not by throughput)."""
+def fallback_plan_options(descs, base: dict | None = None, threads: int = 512, n_sm: int = 152) -> dict:
+    """Plan options for the full solve of fallback cells.  The solve runs next to
+    the reduced launches, and its time is bounded by the step latency of its
+    tiles, not by throughput: cells are packed into few full-size tiles so that
+    they hold as few of the SMs the reduced run needs as possible."""
     kw = dict(base or {})
-    nodes = sum(int(sum(d.ncv)) + len(d.parent) + 1 for d in descs)
-    kw["tile_nodes"] = int(min(kw.get("tile_nodes", 2500) or 2500, max(128, nodes // (2 * n_sm))))
-    kw["threads_per_tile"] = max(threads, 256)
-    kw["threads_big"] = 1024  # a cell alone in a tile: its step latency bounds the fallback
+    kw.setdefault("tile_nodes", 2500)
+    kw["threads_per_tile"] = threads
+    kw["threads_big"] = max(threads, 512)
     kw["threads_global"] = 512
+    kw.pop("lane_nodes", None)
     return kw
 
 
@@ -447,8 +448,13 @@ class SurrogateRunner:
         import torch
 
         plan = self.plan
-        main = torch.cuda.current_stream(self.device)
+        if not hasattr(self, "_main"):
+            # a non-blocking stream: the legacy default stream would order the
+            # fallback streams' work behind the reduced launches
+            self._main = torch.cuda.Stream(self.device)
+        main = self._main
         sid = int(main.cuda_stream)
+        torch.cuda.current_stream(self.device).synchronize()
         n = len(self.descs)
         spl = int(plan.info["steps_per_launch"])
         watch = self.fallback and self.n_ports > 0
@@ -456,15 +462,35 @@ class SurrogateRunner:
         plan.reset(stream=sid)
         flagged = np.zeros(n, bool)
         fallbacks = []
-        done = min(spl, n_steps)
-        plan.run(done, dt, stream=sid, check=False)
-        while True:
-            flags = plan.surrogate_flags(stream=sid) if watch else None
-            more = done < n_steps
-            if more:
-                k = min(spl, n_steps - done)
-                plan.run(k, dt, stream=sid, check=False)
-                done += k
+        if not hasattr(self, "_flag_stream"):
+            self._flag_stream = torch.cuda.Stream(self.device)
+        # two launches stay queued: the flags after launch i are read on a stream that
+        # waits for launch i only, while launch i + 1 keeps the GPU busy
+        queued = []
+        done = 0
+
+        def enqueue():
+            nonlocal done
+            k = min(spl, n_steps - done)
+            plan.run(k, dt, stream=sid, check=False)
+            done += k
+            ev = torch.cuda.Event()
+            ev.record(main)
+            queued.append(ev)
+
+        enqueue()
+        if done < n_steps:
+            enqueue()
+        while queued:
+            ev = queued.pop(0)
+            flags = None
+            if watch:
+                self._flag_stream.wait_event(ev)
+                flags = plan.surrogate_flags(stream=int(self._flag_stream.cuda_stream))
+            else:
+                ev.synchronize()
+            if done < n_steps:
+                enqueue()
             if flags is not None:
                 new = np.nonzero((flags != 0) & ~flagged)[0]
                 if new.size:
@@ -473,8 +499,6 @@ class SurrogateRunner:
                     fp = self._fallback_plan(new)
                     fp.run(n_steps, dt, stream=int(side.cuda_stream), check=False)
                     fallbacks.append((new, fp, side))
-            if not more:
-                break
         plan.check(stream=sid)
         for _, fp, side in fallbacks:
             fp.check(stream=int(side.cuda_stream))

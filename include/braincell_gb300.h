@@ -212,7 +212,8 @@ typedef struct bc_plan_options {
   int32_t threads_big;      /* CTA size for tiles holding one cell larger than
                                tile_nodes; 0 = auto                                   */
   int32_t threads_global;   /* CTA size for global-memory tiles; 0 = auto            */
-  int32_t reserved_a;       /* must be 0                                             */
+  int32_t narrow_lane_nodes; /* lane_nodes for narrow phases (fewer nodes than one
+                               warp slot per warp); 0 = same as lane_nodes        */
   float reserved_b;         /* must be 0                                             */
   int32_t dry_run;          /* 1: lower and schedule only (no CUDA calls); the plan
                                answers bc_plan_info / bc_plan_tile_stats only         */
