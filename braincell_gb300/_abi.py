@@ -89,6 +89,23 @@ BC_GRU_HIDDEN = 64
 BC_GRU_INPUTS = 4
 BC_SURROGATE_NORM = 5
 
+BC_PROBE_CURRENT = 32
+BC_CUR_IL = 0
+BC_CUR_KLEAK = 1
+BC_CUR_NA = 2
+BC_CUR_KDR = 3
+BC_CUR_CAL = 4
+BC_CUR_CAT = 5
+BC_CUR_HCN = 6
+BC_CUR_AHP = 7
+BC_CUR_NAHH = 8
+BC_CUR_KHH = 9
+BC_CUR_KM = 10
+BC_CUR_ION_NA = 11
+BC_CUR_ION_K = 12
+BC_CUR_ION_CA = 13
+BC_NCUR = 14
+
 BC_STATE_V = 0
 BC_STATE_NA_P = 1
 BC_STATE_NA_Q = 2

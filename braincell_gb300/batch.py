@@ -22,7 +22,7 @@ import numpy as np
 
 from . import _abi
 from .catalogue import region_record
-from .mech import CableProperty, CurrentClamp, ExpSyn, MechanismProbe, StateProbe
+from .mech import CableProperty, CurrentClamp, CurrentProbe, ExpSyn, MechanismProbe, StateProbe
 
 __all__ = ["CellBatch", "lower_cell", "concat_batches", "native_lowering"]
 
@@ -338,10 +338,32 @@ PROBE_STATES = {
 }
 
 
+# CurrentProbe: mechanism class -> BC_CUR_* code; ion name -> the ion's total
+PROBE_CURRENTS = {
+    "IL": _abi.BC_CUR_IL, "K_Leak": _abi.BC_CUR_KLEAK, "Na_Ba2002": _abi.BC_CUR_NA, "KDR_Ba2002": _abi.BC_CUR_KDR,
+    "CaL_IS2008": _abi.BC_CUR_CAL, "CaT_HM1992": _abi.BC_CUR_CAT, "HCN_HM1992": _abi.BC_CUR_HCN,
+    "AHP_De1994": _abi.BC_CUR_AHP, "Na_HH1952": _abi.BC_CUR_NAHH, "K_HH1952": _abi.BC_CUR_KHH,
+    "KM_RI2021_SC": _abi.BC_CUR_KM,
+}
+ION_CURRENTS = {"na": _abi.BC_CUR_ION_NA, "k": _abi.BC_CUR_ION_K, "ca": _abi.BC_CUR_ION_CA}
+
+
 def probe_field_of(decl, mechs) -> int:
     """The BC_STATE_* view a MechanismProbe records, resolved against the mechanisms
     painted where it sits: ``decl.mechanism`` is a painted mechanism's instance name or
     class name (``_multi_compartment/probes.py:136-181`` looks it up the same way)."""
+    if isinstance(decl, CurrentProbe):
+        if decl.mechanism is None:
+            if decl.ion not in ION_CURRENTS:
+                raise KeyError(f"Probe {decl.name!r}: unknown ion {decl.ion!r} (one of {sorted(ION_CURRENTS)}).")
+            return int(_abi.BC_PROBE_CURRENT + ION_CURRENTS[decl.ion])
+        hits = [m for m in mechs if getattr(m, "instance_name", None) == decl.mechanism]
+        if len(hits) != 1:
+            raise KeyError(f"Probe {decl.name!r} could not find one mechanism named {decl.mechanism!r} here.")
+        cls = "IL" if hits[0].class_name == "leaky" else hits[0].class_name
+        if cls not in PROBE_CURRENTS:
+            raise KeyError(f"Probe {decl.name!r}: no current for mechanism class {cls!r}.")
+        return int(_abi.BC_PROBE_CURRENT + PROBE_CURRENTS[cls])
     hits = [m for m in mechs if getattr(m, "instance_name", None) == decl.mechanism]
     if len(hits) > 1:
         raise ValueError(f"Probe {decl.name!r} matched multiple mechanisms named {decl.mechanism!r}.")
@@ -420,7 +442,7 @@ def lower_cell(cell, replicas: int | None = None) -> CellBatch:
                         pulses.append((b, x, t_on, t_off, amp))
                 elif isinstance(d, StateProbe):
                     probes.append((b, x, 0))
-                elif isinstance(d, MechanismProbe):
+                elif isinstance(d, (MechanismProbe, CurrentProbe)):
                     probes.append((b, x, probe_field_of(d, regions[int(branch_region[b])][1])))
                 elif isinstance(d, ExpSyn):
                     syns.append((b, x, d.tau, d.e))

@@ -18,7 +18,7 @@ import numpy as np
 
 from . import environ
 from .batch import lower_cell
-from .mech import CVPerBranch, CVPolicy, MechanismProbe, StateProbe
+from .mech import CurrentProbe, CVPerBranch, CVPolicy, MechanismProbe, StateProbe
 from .morph import Morphology
 
 __all__ = ["Cell", "RunResult"]
@@ -122,7 +122,7 @@ class Cell:
         for locset, decls in self.place_rules:
             for _pt in locset.points(self.morpho):
                 for d in decls:
-                    if isinstance(d, (StateProbe, MechanismProbe)):
+                    if isinstance(d, (StateProbe, MechanismProbe, CurrentProbe)):
                         names.append(d.name if d.name is not None else f"probe_{k}")
                         k += 1
         return names

@@ -221,6 +221,77 @@ __device__ __forceinline__ double probe_state(const Real* st, int N, int field) 
   return double(st[slot * N]);
 }
 
+// The value a current probe records: current density `code` (BC_CUR_*, uA/cm^2)
+// of the node whose states start at st, at voltage v after the node's update,
+// with the same terms as the step's currents.
+template <typename Real>
+__device__ __forceinline__ double probe_current(const Real* st, int N, const Real* P, uint32_t m, Real v, int code) {
+  auto eca = [&]() -> Real {
+    if (m & BC_M_CADET)
+      return Real(kNernstCa) * P[BC_P_CA_TEMP] * dlog(P[BC_P_CA_CO] / (st[kSlotCaHi * N] + st[kSlotCaLo * N]));
+    return P[BC_P_ECA];
+  };
+  auto cur = [&](int c) -> Real {
+    switch (c) {
+      case BC_CUR_IL:
+        return (m & BC_M_IL) ? P[BC_P_IL_G] * (P[BC_P_IL_E] - v) : Real(0);
+      case BC_CUR_KLEAK:
+        return (m & BC_M_KLEAK) ? P[BC_P_KLEAK_G] * (P[BC_P_EK] - v) : Real(0);
+      case BC_CUR_NA: {
+        if (!(m & BC_M_NA)) return Real(0);
+        const Real p = st[kSlotNaP * N];
+        return P[BC_P_NA_G] * p * p * p * st[kSlotNaQ * N] * (P[BC_P_ENA] - v);
+      }
+      case BC_CUR_KDR: {
+        if (!(m & BC_M_KDR)) return Real(0);
+        const Real p2 = st[kSlotKdrP * N] * st[kSlotKdrP * N];
+        return P[BC_P_KDR_G] * p2 * p2 * (P[BC_P_EK] - v);
+      }
+      case BC_CUR_CAL: {
+        if (!(m & BC_M_CAL)) return Real(0);
+        const Real p = st[kSlotCalP * N];
+        return P[BC_P_CAL_G] * p * p * st[kSlotCalQ * N] * (eca() - v);
+      }
+      case BC_CUR_CAT: {
+        if (!(m & BC_M_CAT)) return Real(0);
+        const Real p = st[kSlotCatP * N];
+        return P[BC_P_CAT_G] * p * p * st[kSlotCatQ * N] * (eca() - v);
+      }
+      case BC_CUR_HCN:
+        return (m & BC_M_HCN) ? P[BC_P_HCN_G] * st[kSlotHcnP * N] * (P[BC_P_HCN_E] - v) : Real(0);
+      case BC_CUR_AHP: {
+        if (!(m & BC_M_AHP)) return Real(0);
+        const Real p = st[kSlotAhpP * N];
+        return P[BC_P_AHP_G] * p * p * (P[BC_P_EK] - v);
+      }
+      case BC_CUR_NAHH: {
+        if (!(m & BC_M_NAHH)) return Real(0);
+        const Real p = st[kSlotNaHHP * N];
+        return P[BC_P_NAHH_G] * p * p * p * st[kSlotNaHHQ * N] * (P[BC_P_ENA] - v);
+      }
+      case BC_CUR_KHH: {
+        if (!(m & BC_M_KHH)) return Real(0);
+        const Real p2 = st[kSlotKHHP * N] * st[kSlotKHHP * N];
+        return P[BC_P_KHH_G] * p2 * p2 * (P[BC_P_EK] - v);
+      }
+      case BC_CUR_KM:
+        return (m & BC_M_KM) ? P[BC_P_KM_G] * st[kSlotKMN * N] * (P[BC_P_EK] - v) : Real(0);
+    }
+    return Real(0);
+  };
+  switch (code) {
+    case BC_CUR_ION_NA:
+      return double(cur(BC_CUR_NA)) + double(cur(BC_CUR_NAHH));
+    case BC_CUR_ION_K:
+      return double(cur(BC_CUR_KDR)) + double(cur(BC_CUR_KLEAK)) + double(cur(BC_CUR_AHP)) + double(cur(BC_CUR_KHH)) +
+             double(cur(BC_CUR_KM));
+    case BC_CUR_ION_CA:
+      return double(cur(BC_CUR_CAL)) + double(cur(BC_CUR_CAT));
+    default:
+      return double(cur(code));
+  }
+}
+
 // Channels outside the main workloads' mix (classic Hodgkin-Huxley Na / K and the
 // M current): kept out of line so that their registers do not weigh on the
 // common path; same exp-Euler steps and ohmic currents as the others.
@@ -1400,8 +1471,17 @@ __global__ void __launch_bounds__(kVar == 2 ? BC_PORT_MAX_THREADS : 1024, kVar =
       const int64_t slot = k_since / a.record_every - 1;
       for (int q = tid; q < td.n_xprobes; q += T) {
         const ProbeRef r = pl[q];
-        if (slot >= 0 && slot < a.trace_cap)
-          a.traces[slot * a.n_probes_total + r.id] = probe_state(tv.state + r.node, tv.N, r.field);
+        if (slot < 0 || slot >= a.trace_cap) continue;
+        double val;
+        if (r.field >= BC_PROBE_CURRENT) {
+          const uint16_t pr = tv.pidx[r.node];
+          const Pair<Real> vv = tv.v[r.node];
+          val = probe_current(tv.state + r.node, tv.N, tv.params + size_t(pr) * BC_NPARAM, tv.mech[pr], vv.x + vv.y,
+                              r.field - BC_PROBE_CURRENT);
+        } else {
+          val = probe_state(tv.state + r.node, tv.N, r.field);
+        }
+        a.traces[slot * a.n_probes_total + r.id] = val;
       }
     }
     if (kExtra && tv.has_src)

@@ -1163,11 +1163,22 @@ bc_status bc_plan_create(const bc_batch_spec* spec, const bc_plan_options* opts_
       return fail(BC_ERR_INVALID, "probe location not found");
     }
     const int32_t field = s.probe_field ? s.probe_field[k] : BC_STATE_V;
-    if (field < 0 || field >= BC_NSTATE_VIEW) {
+    const bool is_current = field >= BC_PROBE_CURRENT && field < BC_PROBE_CURRENT + BC_NCUR;
+    if (!is_current && (field < 0 || field >= BC_NSTATE_VIEW)) {
       delete p;
-      return fail(BC_ERR_INVALID, "probe_field is not a BC_STATE_* view");
+      return fail(BC_ERR_INVALID, "probe_field is not a BC_STATE_* view or a BC_PROBE_CURRENT code");
     }
-    if (field != BC_STATE_V) {
+    if (is_current) {
+      static const uint32_t cur_owner[BC_NCUR] = {
+          BC_M_IL,  BC_M_KLEAK, BC_M_NA,   BC_M_KDR, BC_M_CAL,           BC_M_CAT,
+          BC_M_HCN, BC_M_AHP,   BC_M_NAHH, BC_M_KHH, BC_M_KM,            BC_M_NA | BC_M_NAHH,
+          BC_M_KDR | BC_M_KLEAK | BC_M_AHP | BC_M_KHH | BC_M_KM,         BC_M_CAL | BC_M_CAT};
+      const int32_t rg = cells[c].region[v];
+      if (rg < 0 || !(s.region_mech[c * s.n_regions + rg] & cur_owner[field - BC_PROBE_CURRENT])) {
+        delete p;
+        return fail(BC_ERR_INVALID, "probe current: no such mechanism at the probed location");
+      }
+    } else if (field != BC_STATE_V) {
       // the mechanism that owns the state must be present at the probed CV
       static const uint32_t owner[BC_NSTATE_VIEW] = {0,          BC_M_NA,    BC_M_NA,    BC_M_KDR,   BC_M_CAL,
                                                      BC_M_CAL,   BC_M_CAT,   BC_M_CAT,   BC_M_HCN,   BC_M_AHP,

@@ -31,6 +31,7 @@ __all__ = [
     "CurrentClamp",
     "StateProbe",
     "MechanismProbe",
+    "CurrentProbe",
     "AllRegion",
     "BranchInFilter",
     "branch_in",
@@ -187,6 +188,29 @@ class MechanismProbe:
             value = getattr(self, field_name)
             if not isinstance(value, str) or not value:
                 raise ValueError(f"MechanismProbe.{field_name} must be a non-empty string, got {value!r}.")
+
+
+@dataclass(frozen=True)
+class CurrentProbe:
+    """Probe of a current density at a placed location (``mech/_point.py:347``,
+    sampled as ``_multi_compartment/probes.py:184-258``): the current of the named
+    mechanism, or with only ``ion`` the total current of that ion ("na", "k",
+    "ca"), in uA/cm^2 as g (E - V), after every recorded step.
+    """
+
+    ion: str | None = None
+    mechanism: str | None = None
+    name: str | None = None
+
+    def __post_init__(self) -> None:
+        if self.name is not None and (not isinstance(self.name, str) or not self.name):
+            raise ValueError(f"CurrentProbe.name must be a non-empty string or None, got {self.name!r}.")
+        if self.ion is not None and (not isinstance(self.ion, str) or not self.ion):
+            raise ValueError(f"CurrentProbe.ion must be a non-empty string or None, got {self.ion!r}.")
+        if self.mechanism is not None and (not isinstance(self.mechanism, str) or not self.mechanism):
+            raise ValueError(f"CurrentProbe.mechanism must be a non-empty string or None, got {self.mechanism!r}.")
+        if self.ion is None and self.mechanism is None:
+            raise ValueError("CurrentProbe requires at least one of 'ion' or 'mechanism'.")
 
 
 # ----------------------------------------------------------------------------

@@ -183,9 +183,10 @@ typedef struct bc_batch_spec {
   const double* port_pulse_t_on;      /* ms                                     */
   const double* port_pulse_t_off;     /* ms                                     */
   const double* port_pulse_amp;       /* nA                                     */
-  /* what each probe records (mech/_point.py StateProbe / MechanismProbe,
-     sampled as _multi_compartment/probes.py:44-137 does): a BC_STATE_* view --
-     0 = V, else the named gate or Ci of the mechanism at the probe's CV, after
+  /* what each probe records (mech/_point.py StateProbe / MechanismProbe /
+     CurrentProbe, sampled as _multi_compartment/probes.py:44-258 does): a
+     BC_STATE_* view -- 0 = V, else the named gate or Ci of the mechanism at the
+     probe's CV -- or BC_PROBE_CURRENT + BC_CUR_* for a current density, after
      the step.  Null: every probe records V.                                    */
   const int32_t* probe_field;         /* [n_probes]                             */
 } bc_batch_spec;
@@ -305,6 +306,25 @@ bc_status bc_check(bc_plan_t plan, void* stream);
 #define BC_STATE_KHH_P 13
 #define BC_STATE_KM_N 14
 #define BC_NSTATE_VIEW 15
+/* Current probes (mech/_point.py CurrentProbe, _multi_compartment/probes.py:184-258):
+   probe_field = BC_PROBE_CURRENT + one of the codes below records that current
+   density (uA/cm^2, outward negative as g (E - V)) after the step.             */
+#define BC_PROBE_CURRENT 32
+#define BC_CUR_IL 0
+#define BC_CUR_KLEAK 1
+#define BC_CUR_NA 2      /* Na_Ba2002   */
+#define BC_CUR_KDR 3     /* KDR_Ba2002  */
+#define BC_CUR_CAL 4     /* CaL_IS2008  */
+#define BC_CUR_CAT 5     /* CaT_HM1992  */
+#define BC_CUR_HCN 6     /* HCN_HM1992  */
+#define BC_CUR_AHP 7     /* AHP_De1994  */
+#define BC_CUR_NAHH 8    /* Na_HH1952   */
+#define BC_CUR_KHH 9     /* K_HH1952    */
+#define BC_CUR_KM 10     /* KM_RI2021_SC */
+#define BC_CUR_ION_NA 11 /* sum over the sodium channels    */
+#define BC_CUR_ION_K 12  /* sum over the potassium channels */
+#define BC_CUR_ION_CA 13 /* sum over the calcium channels   */
+#define BC_NCUR 14
 bc_status bc_state_download(bc_plan_t plan, int32_t which, double* out /* [n_cv] */, void* stream);
 bc_status bc_state_upload(bc_plan_t plan, int32_t which, const double* in /* [n_cv] */, void* stream);
 

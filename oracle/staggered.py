@@ -661,7 +661,7 @@ class OracleCell:
         self.Ci_fixed = np.full(n, _CA_FIXED_CI)
 
     def _points(self, cell) -> None:
-        from braincell_gb300.mech import CurrentClamp, ExpSyn, MechanismProbe, StateProbe
+        from braincell_gb300.mech import CurrentClamp, CurrentProbe, ExpSyn, MechanismProbe, StateProbe
 
         self.clamps_mid = []  # (point, t_on, t_off, amp_nA)
         self.clamps_edge = []
@@ -689,6 +689,14 @@ class OracleCell:
                         # probes.py:136-181: the named mechanism's (or ion's) field at the point
                         self.probe_points.append(pid)
                         self.probe_what.append(self._probe_key(cell, b, d))
+                    elif isinstance(d, CurrentProbe):
+                        # probes.py:184-258: a channel's current, or an ion's total
+                        self.probe_points.append(pid)
+                        if d.mechanism is not None:
+                            key = self._probe_key(cell, b, MechanismProbe(d.mechanism, "p", name=d.name))
+                            self.probe_what.append(("cur", key[1]))
+                        else:
+                            self.probe_what.append(("ion", d.ion))
                     elif isinstance(d, ExpSyn):
                         if not self.is_mid[pid]:
                             raise ValueError("ExpSyn must sit inside a CV, not on a branch end point.")
@@ -835,6 +843,33 @@ class OracleCell:
             I = I + geff * (E - pv)
             dI = dI - geff
         return I, dI
+
+    def _probe_current(self, what, pid):
+        """A current probe's value at point pid after the step (uA/cm^2)."""
+        pv = self.cv_to_point(self.V)
+        E_ca = self._E_ca()
+        E_of = {"na": self.E_na, "k": self.E_k, "ca": E_ca}
+
+        def one(name):
+            ch = self.chan[name]
+            if name == "IL":
+                E, fac = ch["E"], 1.0
+            elif name == "K_Leak":
+                E, fac = self.E_k, 1.0
+            elif name == "HCN_HM1992":
+                E, fac = ch["E"], self._gate_product(name)
+            else:
+                E, fac = E_of[_ION_OF[name]], self._gate_product(name)
+            cur = ch["g_max"] * fac * (E - pv)
+            return cur[:, pid] if np.ndim(cur) == 2 else np.full(self.P, float(cur))
+
+        if what[0] == "cur":
+            return one(what[1])
+        total = np.zeros(self.P)
+        for name in self.chan:
+            if _ION_OF.get(name) == what[1]:
+                total = total + one(name)
+        return total
 
     def _ca_current(self, pv):
         """``Ion.current`` of the calcium ion (sum of CaL + CaT), uA/cm^2."""
@@ -987,6 +1022,8 @@ class OracleCell:
                         row.append(self.V[:, c] if c is not None else np.full(self.P, np.nan))
                     elif what[0] == "Ci":
                         row.append(self.Ci[:, pid])
+                    elif what[0] in ("cur", "ion"):
+                        row.append(self._probe_current(what, pid))
                     else:
                         row.append(self.gates[(what[1], what[2])][:, pid])
                 traces.append(np.stack(row, axis=1))

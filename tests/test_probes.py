@@ -6,8 +6,8 @@ import pytest
 
 from braincell_gb300 import Branch, Cell, Morphology
 from braincell_gb300 import _abi
-from braincell_gb300.mech import (AllRegion, CableProperty, Channel, CurrentClamp, CVPerBranch, Ion, MechanismProbe,
-                                  RootLocation, StateProbe, at, branch_in)
+from braincell_gb300.mech import (AllRegion, CableProperty, Channel, CurrentClamp, CurrentProbe, CVPerBranch, Ion,
+                                  MechanismProbe, RootLocation, StateProbe, at, branch_in)
 
 
 def _cell(precision="f64"):
@@ -89,3 +89,41 @@ def test_mechanism_probes_match_oracle(native_lib, cuda_device, precision, tol):
     # mechanism probes do not produce spikes; the soma voltage probe does
     sp = p.spikes()
     assert len(sp[0]) >= 1 and all(len(sp[k]) == 0 for k in (1, 2, 4, 5, 6))
+
+
+def _current_cell(precision="f64"):
+    c = _cell(precision)
+    c.place(RootLocation(0.5), CurrentProbe(mechanism="na_soma", name="i_na"), CurrentProbe(ion="k", name="i_k"))
+    c.place(at(1, 0.3), CurrentProbe(mechanism="CaL_IS2008", name="i_cal"), CurrentProbe(ion="ca", name="i_ca"),
+            CurrentProbe(mechanism="IL", name="i_leak"))
+    return c
+
+
+def test_current_probe_lowering_and_errors():
+    b = _current_cell().batch()
+    C = _abi.BC_PROBE_CURRENT
+    np.testing.assert_array_equal(b.probe_field[7:], [C + _abi.BC_CUR_NA, C + _abi.BC_CUR_ION_K, C + _abi.BC_CUR_CAL,
+                                                      C + _abi.BC_CUR_ION_CA, C + _abi.BC_CUR_IL])
+    with pytest.raises(ValueError):
+        CurrentProbe()
+    c = _cell()
+    c.place(RootLocation(0.5), CurrentProbe(ion="xx"))
+    with pytest.raises(KeyError):
+        c.batch()
+
+
+@pytest.mark.gpu
+def test_current_probes_match_oracle(native_lib, cuda_device):
+    from braincell_gb300.runtime import Plan
+    from oracle.staggered import OracleCell
+
+    n = 1200
+    p = Plan(_current_cell("f64").batch(), precision="f64", record_every=1)
+    p.run(n, 0.025)
+    gpu = p.traces()[7:]
+    ref = OracleCell(_current_cell("f64")).run(0.025, n)[0][0][7:]
+    for k in range(5):
+        scale = max(np.abs(ref[k]).max(), 1e-12)
+        assert np.abs(gpu[k] - ref[k]).max() <= 1e-6 * scale, (k, np.abs(gpu[k] - ref[k]).max(), scale)
+    # the sodium current is inward (positive as g (E - V)) and large during the spikes
+    assert ref[0].max() > 10.0
