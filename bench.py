@@ -54,6 +54,7 @@ def _args():
     ap.add_argument("--lane-nodes", type=int, default=1)
     ap.add_argument("--no-surrogate", action="store_true")
     ap.add_argument("--surrogate-threads", type=int, default=384)
+    ap.add_argument("--surrogate-tile-nodes", type=int, default=1800)
     ap.add_argument("--accuracy-cells", type=int, default=300)
     return ap.parse_args()
 
@@ -229,7 +230,7 @@ def surrogate_leg(a, descs, local, sid, stream, plain_ms):
 
     model = S.load_model(os.path.join(ROOT, "braincell_gb300", "data", "surrogate_uneven.npz"))
     T = a.surrogate_threads
-    kw = dict(tile_nodes=a.tile_nodes, threads_per_tile=T, threads_big=T, threads_global=T,
+    kw = dict(tile_nodes=a.surrogate_tile_nodes, threads_per_tile=T, threads_big=T, threads_global=T,
               steps_per_launch=a.steps_per_launch, lane_nodes=a.lane_nodes)
     t0 = time.perf_counter()
     runner = S.SurrogateRunner(descs, model, precision="f32", device=local, plan_kw=kw)

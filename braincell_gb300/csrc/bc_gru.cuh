@@ -110,6 +110,39 @@ __device__ __forceinline__ void gru_preact(const uint32_t* __restrict__ wext, in
   mma_bf16_16816(acc[3], ax, __ldg(w + 32 + tq), __ldg(w + 36 + tq));
 }
 
+// Copy the row-major extended matrix into the fragment-major layout of a tile's
+// scratch (kGruFragPairs word pairs; see kGruFragSlots).
+__device__ __forceinline__ void gru_frag_fill(const uint32_t* __restrict__ wext, uint2* frag, int tid, int T) {
+  constexpr int kRow = kGruK / 2;
+  for (int i = tid; i < kGruFragPairs; i += T) {
+    const int lane = i & 31, slot = (i >> 5) % kGruFragSlots, jb = i / (32 * kGruFragSlots);
+    const int q = slot < 15 ? slot / 5 : 3, kk = slot < 15 ? slot % 5 : 4;
+    const uint32_t* w = wext + size_t(q * kGruH + jb * 8 + (lane >> 2)) * kRow + kk * 8 + (lane & 3);
+    frag[i] = make_uint2(__ldg(w), __ldg(w + 4));
+  }
+}
+
+// gru_preact with the B fragments of N group jb taken from the fragment-major
+// copy (frag = the tile's copy + jb * 16 slots * 32 lanes): the same products
+// in the same order, so the same results.
+__device__ __forceinline__ void gru_preact_frag(const uint2* frag, int lane, const uint32_t (*ah)[4],
+                                                const uint32_t* ax, float (*acc)[4]) {
+#pragma unroll
+  for (int q = 0; q < 4; ++q) acc[q][0] = acc[q][1] = acc[q][2] = acc[q][3] = 0.0f;
+#pragma unroll
+  for (int q = 0; q < 3; ++q) {
+#pragma unroll
+    for (int kk = 0; kk < 4; ++kk) {
+      const uint2 b = frag[gru_frag_slot(q, kk) * 32 + lane];
+      mma_bf16_16816(acc[q], ah[kk], b.x, b.y);
+    }
+    const uint2 b = frag[gru_frag_slot(q, 4) * 32 + lane];
+    mma_bf16_16816(acc[q], ax, b.x, b.y);
+  }
+  const uint2 b = frag[gru_frag_slot(3, 4) * 32 + lane];
+  mma_bf16_16816(acc[3], ax, b.x, b.y);
+}
+
 struct GruGate {
   float r, z, n, hn, h_new;
 };

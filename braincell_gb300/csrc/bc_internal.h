@@ -107,8 +107,9 @@ struct TileDesc {
   int64_t scratch_offset;   // bytes into the plan's global scratch (global-resident tiles)
   int64_t port_offset;      // into the plan's port array (subtree-surrogate ports of this tile)
   int32_t n_ports;
-  int32_t off_pstage;       // per-port staging records (PortStage) followed by PortLocal records,
-                            // inside the scratch area; -1: none
+  int32_t off_pstage;       // the GRU weight fragments and wo (kGruSmemBytes), then per-port staging
+                            // records (PortStage), then PortLocal records, inside the
+                            // scratch area; -1: none
 };
 
 // ------------------------------------------------------------- subtree surrogate
@@ -136,6 +137,17 @@ constexpr int kGruRows = 4 * kGruH;
 constexpr int kPortHBf = 2 * kGruH;            // offset of the BF16 halves
 constexpr int kPortVPrev = kPortHBf + kGruH;    // offset of (v_prev, seen)
 constexpr int kPortStride = kPortVPrev + 4;
+// A tile with ports holds the B fragments of the extended weight matrix in its
+// scratch, fragment-major: for N group jb (8 units) there are 16 fragment slots,
+// (block q < 3, k step kk < 5) at slot 5 q + kk and the nx block's x step at
+// slot 15; a slot is 32 lanes x one (b0, b1) word pair, so a warp reads it as
+// 256 contiguous bytes (no bank conflicts).  Rows that the slot omits (the nx
+// rows' h steps) are zero in the row-major matrix.
+constexpr int kGruFragSlots = 16;
+constexpr int kGruFragPairs = 8 * kGruFragSlots * 32;                       // uint2 per tile
+constexpr int kGruFragBytes = kGruFragPairs * 8;                            // 32 KB
+constexpr int kGruSmemBytes = kGruFragBytes + kGruH * 4;                    // + output weights wo
+__host__ __device__ constexpr int gru_frag_slot(int q, int kk) { return q < 3 ? 5 * q + kk : 15; }
 
 // Launch shape of the kernel variant with ports: at most BC_PORT_MAX_THREADS
 // threads per tile, register budget for BC_PORT_MIN_CTAS resident tiles per SM.

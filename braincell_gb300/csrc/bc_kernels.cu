@@ -1188,9 +1188,9 @@ __device__ __forceinline__ void port_stage(PortLocal* pl, int n_ports, const Pul
 }
 
 template <typename Real>
-__device__ __forceinline__ void port_gru(const PortStage* stage, int n_ports, float* port_h,
-                                        const GruWeights* __restrict__ W, Pair<Real>* dr, int64_t m, int warp,
-                                        int n_warps, int lane, unsigned long long* ptimers) {
+__device__ __forceinline__ void port_gru(const PortStage* stage, int n_ports, float* port_h, const uint2* wfrag,
+                                        const float* wo_s, Pair<Real>* dr, int64_t m, int warp, int n_warps, int lane,
+                                        unsigned long long* ptimers) {
 #ifdef BC_PORT_TIMERS
   long long pt0 = clock64();
 #define BC_PTICK(slot)                                                                                  \
@@ -1206,15 +1206,20 @@ __device__ __forceinline__ void port_gru(const PortStage* stage, int n_ports, fl
 #endif
   const int g = lane >> 2, tq = lane & 3;
   const int rd = int(m & 1), wr = rd ^ 1;
-  const int n_items = ((n_ports + 15) >> 4) * 8;
+  // Work items: (M tile of 16 ports, range of N groups).  Each M tile is split
+  // into as many ranges as there are warps for it (1..8), so every warp is busy;
+  // the A operand is loaded once per item and reused across its N groups.
+  const int n_mt = (n_ports + 15) >> 4;
+  const int n_split = max(1, min(8, n_warps / max(n_mt, 1)));
+  const int n_items = n_mt * n_split;
   for (int it = warp; it < n_items; it += n_warps) {
-    const int mt = it >> 3, jb = it & 7;
+    const int mt = it / n_split, sp = it - mt * n_split;
+    const int jb_begin = (sp * 8) / n_split, jb_end = ((sp + 1) * 8) / n_split;
     const int qa = mt * 16 + g, qb = qa + 8;
     const bool oka = qa < n_ports, okb = qb < n_ports;
-    const int j0 = jb * 8 + 2 * tq;
     float* ha = oka ? port_h + size_t(stage[qa].id) * kPortStride : nullptr;
     float* hb = okb ? port_h + size_t(stage[qb].id) * kPortStride : nullptr;
-    // A operand straight from the BF16 halves; the FP32 values of this lane's units
+    // A operand straight from the BF16 halves
     uint32_t ah[4][4];
     const uint32_t* ba = oka ? reinterpret_cast<const uint32_t*>(ha + kPortHBf) + rd * (kGruH / 2) : nullptr;
     const uint32_t* bb = okb ? reinterpret_cast<const uint32_t*>(hb + kPortHBf) + rd * (kGruH / 2) : nullptr;
@@ -1225,8 +1230,6 @@ __device__ __forceinline__ void port_gru(const PortStage* stage, int n_ports, fl
       ah[kk][2] = oka ? ba[kk * 8 + 4 + tq] : 0u;
       ah[kk][3] = okb ? bb[kk * 8 + 4 + tq] : 0u;
     }
-    const float2 hoa = oka ? *reinterpret_cast<const float2*>(ha + rd * kGruH + j0) : make_float2(0.f, 0.f);
-    const float2 hob = okb ? *reinterpret_cast<const float2*>(hb + rd * kGruH + j0) : make_float2(0.f, 0.f);
     uint32_t ax[4];
     {
       const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -1236,25 +1239,34 @@ __device__ __forceinline__ void port_gru(const PortStage* stage, int n_ports, fl
       xblock_frag(fa, fb, tq, ax);
     }
     BC_PTICK(0);
-    float acc[4][4];
-    gru_preact(W->wext, jb, g, tq, ah, ax, acc);
-    BC_PTICK(1);
-    const float2 wo = *reinterpret_cast<const float2*>(W->wo + j0);
-    const GruGate G0 = gru_gate(acc[0][0], acc[1][0], acc[2][0], acc[3][0], hoa.x);
-    const GruGate G1 = gru_gate(acc[0][1], acc[1][1], acc[2][1], acc[3][1], hoa.y);
-    const GruGate G2 = gru_gate(acc[0][2], acc[1][2], acc[2][2], acc[3][2], hob.x);
-    const GruGate G3 = gru_gate(acc[0][3], acc[1][3], acc[2][3], acc[3][3], hob.y);
-    if (oka) {
-      *reinterpret_cast<float2*>(ha + wr * kGruH + j0) = make_float2(G0.h_new, G1.h_new);
-      reinterpret_cast<uint32_t*>(ha + kPortHBf)[wr * (kGruH / 2) + j0 / 2] = pack_bf16(G0.h_new, G1.h_new);
+    float ysa = 0.0f, ysb = 0.0f;
+#pragma unroll 1
+    for (int jb = jb_begin; jb < jb_end; ++jb) {
+      const int j0 = jb * 8 + 2 * tq;
+      // FP32 values of this lane's two units (issued ahead of the products)
+      const float2 z2 = make_float2(0.f, 0.f);
+      const float2 hoa = oka ? *reinterpret_cast<const float2*>(ha + rd * kGruH + j0) : z2;
+      const float2 hob = okb ? *reinterpret_cast<const float2*>(hb + rd * kGruH + j0) : z2;
+      float acc[4][4];
+      gru_preact_frag(wfrag + jb * (kGruFragSlots * 32), lane, ah, ax, acc);
+      BC_PTICK(1);
+      const float2 wo = *reinterpret_cast<const float2*>(wo_s + j0);
+      const GruGate G0 = gru_gate(acc[0][0], acc[1][0], acc[2][0], acc[3][0], hoa.x);
+      const GruGate G1 = gru_gate(acc[0][1], acc[1][1], acc[2][1], acc[3][1], hoa.y);
+      const GruGate G2 = gru_gate(acc[0][2], acc[1][2], acc[2][2], acc[3][2], hob.x);
+      const GruGate G3 = gru_gate(acc[0][3], acc[1][3], acc[2][3], acc[3][3], hob.y);
+      if (oka) {
+        *reinterpret_cast<float2*>(ha + wr * kGruH + j0) = make_float2(G0.h_new, G1.h_new);
+        reinterpret_cast<uint32_t*>(ha + kPortHBf)[wr * (kGruH / 2) + j0 / 2] = pack_bf16(G0.h_new, G1.h_new);
+      }
+      if (okb) {
+        *reinterpret_cast<float2*>(hb + wr * kGruH + j0) = make_float2(G2.h_new, G3.h_new);
+        reinterpret_cast<uint32_t*>(hb + kPortHBf)[wr * (kGruH / 2) + j0 / 2] = pack_bf16(G2.h_new, G3.h_new);
+      }
+      ysa += wo.x * G0.h_new + wo.y * G1.h_new;
+      ysb += wo.x * G2.h_new + wo.y * G3.h_new;
+      BC_PTICK(2);
     }
-    if (okb) {
-      *reinterpret_cast<float2*>(hb + wr * kGruH + j0) = make_float2(G2.h_new, G3.h_new);
-      reinterpret_cast<uint32_t*>(hb + kPortHBf)[wr * (kGruH / 2) + j0 / 2] = pack_bf16(G2.h_new, G3.h_new);
-    }
-    float ysa = wo.x * G0.h_new + wo.y * G1.h_new;
-    float ysb = wo.x * G2.h_new + wo.y * G3.h_new;
-    BC_PTICK(2);
     ysa += __shfl_xor_sync(kFullMask, ysa, 1);
     ysa += __shfl_xor_sync(kFullMask, ysa, 2);
     ysb += __shfl_xor_sync(kFullMask, ysb, 1);
@@ -1359,16 +1371,22 @@ __global__ void __launch_bounds__(kVar == 2 ? BC_PORT_MAX_THREADS : 1024, kVar =
   __syncthreads();
   PortStage* pstage = nullptr;
   PortLocal* plocal = nullptr;
+  uint2* wfrag = nullptr;
+  float* wo_s = nullptr;
   if constexpr (kPorts) {
     if (td.n_ports > 0) {
-      pstage = reinterpret_cast<PortStage*>(scratch + td.off_pstage);
+      wfrag = reinterpret_cast<uint2*>(scratch + td.off_pstage);
+      wo_s = reinterpret_cast<float*>(scratch + td.off_pstage + kGruFragBytes);
+      pstage = reinterpret_cast<PortStage*>(scratch + td.off_pstage + kGruSmemBytes);
       plocal = reinterpret_cast<PortLocal*>(pstage + td.n_ports);
+      gru_frag_fill(a.gru->wext, wfrag, tid, T);
+      for (int j = tid; j < kGruH; j += T) wo_s[j] = a.gru->wo[j];
       port_local_load(a.ports + td.port_offset, td.n_ports, a.port_h, plocal, tid, T);
       __syncthreads();
       port_stage<Real>(plocal, td.n_ports, a.port_pulses, a.port_flags, a.gru, tv.v, tv.dr, pstage, a.step0, dt,
                        tid, T);
       __syncthreads();
-      port_gru<Real>(pstage, td.n_ports, a.port_h, a.gru, tv.dr, a.step0, warp, n_warps, lane, a.timers);
+      port_gru<Real>(pstage, td.n_ports, a.port_h, wfrag, wo_s, tv.dr, a.step0, warp, n_warps, lane, a.timers);
       __syncthreads();
     }
   }
@@ -1502,7 +1520,7 @@ __global__ void __launch_bounds__(kVar == 2 ? BC_PORT_MAX_THREADS : 1024, kVar =
                          tid, T);
         __syncthreads();
         BC_TICK(2);
-        port_gru<Real>(pstage, td.n_ports, a.port_h, a.gru, tv.dr, step + 1, warp, n_warps, lane, a.timers);
+        port_gru<Real>(pstage, td.n_ports, a.port_h, wfrag, wo_s, tv.dr, step + 1, warp, n_warps, lane, a.timers);
         __syncthreads();
       }
     }

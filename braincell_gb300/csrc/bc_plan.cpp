@@ -622,7 +622,7 @@ static bc_status build_tile(const BuildCtx& cx, const TileBuild& tb, int T, Tile
   d.off_pstage = -1;
   if (n_tile_ports > 0) {
     d.off_pstage = int32_t(so);
-    so = align16(so + n_tile_ports * (sizeof(PortStage) + sizeof(PortLocal)));
+    so = align16(so + size_t(kGruSmemBytes) + n_tile_ports * (sizeof(PortStage) + sizeof(PortLocal)));
   }
   d.scratch_bytes = int32_t(so);
   d.n_nodes = int32_t(N);
@@ -1399,7 +1399,8 @@ bc_status bc_plan_create(const bc_batch_spec* spec, const bc_plan_options* opts_
   // tiles fill up to tile_nodes without lowering the occupancy.
   const size_t per_sm = dry ? size_t(233472) : sm_smem(opts.device);
   const size_t cta_reserve = 2 * static_smem;  // static shared memory + the system's per-CTA reserve
-  const size_t est = size_t(double(tile_nodes) * bpn) + 2048;
+  // a tile with ports also holds the weight fragments of the GRU
+  const size_t est = size_t(double(tile_nodes) * bpn) + 2048 + (s.n_ports > 0 ? size_t(kGruSmemBytes) : 0);
   const size_t ctas_per_sm = std::max<size_t>(1, per_sm / (est + cta_reserve));
   const size_t packed_budget =
       std::min(smem_budget, std::max(est, per_sm / ctas_per_sm > cta_reserve ? per_sm / ctas_per_sm - cta_reserve : est));

@@ -43,6 +43,13 @@ CUT_DEPTH = 4
 PACKAGED_MODEL = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data", "surrogate_uneven.npz")
 NPARAM = 3 * 64 * 64 + 3 * 64 * 4 + 2 * 3 * 64 + 64 + 1
 V_SCALE = 10.0       # mV
+# Default launch shape of reduced plans: a tile with ports also holds the GRU
+# weight fragments (32 KB of shared memory), so two tiles per SM fit ~1,800
+# nodes each; 384 threads is the port kernel's register budget at two per SM.
+PORT_TILE_NODES = 1800
+PORT_THREADS = 384
+# Fallback (full-morphology) plans run the kernel without ports in large tiles.
+FALLBACK_TILE_NODES = 2500
 S_SCALE = 0.1        # nA: stimulus input scale (the step kernel's constant)
 G_REF = 0.005        # uS, feature reference
 TAU_REF = 5.0        # ms, feature reference
@@ -379,7 +386,7 @@ def fallback_plan_options(descs, base: dict | None = None, threads: int = 512, n
     tiles, not by throughput: cells are packed into few full-size tiles so that
     they hold as few of the SMs the reduced run needs as possible."""
     kw = dict(base or {})
-    kw.setdefault("tile_nodes", 2500)
+    kw["tile_nodes"] = FALLBACK_TILE_NODES
     kw["threads_per_tile"] = threads
     kw["threads_big"] = max(threads, 512)
     kw["threads_global"] = 512
@@ -422,6 +429,9 @@ class SurrogateRunner:
         self.model = model
         self.precision, self.record_every, self.device = precision, int(record_every), int(device)
         self.plan_kw = dict(plan_kw or {})
+        self.plan_kw.setdefault("tile_nodes", PORT_TILE_NODES)
+        for k in ("threads_per_tile", "threads_big", "threads_global"):
+            self.plan_kw.setdefault(k, PORT_THREADS)
         self.fallback = fallback and model is not None
         red, ports = zip(*[reduce_desc(d, model.cut_depth if model else CUT_DEPTH) for d in self.descs])
         red = [replace(r, probes=[(0, 0.5)]) for r in red]
