@@ -133,6 +133,8 @@ struct bc_plan {
   size_t device_bytes = 0;
   // launch classes after the first run concurrently on these streams
   cudaStream_t aux[2] = {nullptr, nullptr};
+  cudaStream_t init_stream = nullptr;  // highest priority: the initial reset
+  int aux_prio = 0;                    // priority of the aux streams (that of the last caller's stream)
   bool dry = false;
   unsigned long long* d_timers = nullptr;
   std::vector<std::array<int64_t, 6>> tile_stats;
@@ -192,6 +194,7 @@ static void free_plan(bc_plan* p) {
     if (p->aux[k]) cudaStreamDestroy(p->aux[k]);
     if (p->ev_join[k]) cudaEventDestroy(p->ev_join[k]);
   }
+  if (p->init_stream) cudaStreamDestroy(p->init_stream);
   if (p->ev_fork) cudaEventDestroy(p->ev_fork);
   if (p->graph_exec) cudaGraphExecDestroy(p->graph_exec);
   if (p->graph) cudaGraphDestroy(p->graph);
@@ -1007,6 +1010,22 @@ static bc_status enqueue_run(bc_plan* p, int64_t n_steps, double dt, void* strea
     return st;
   }
   const int64_t per_launch = net ? std::min<int64_t>(p->steps_per_launch, p->net_k) : p->steps_per_launch;
+  if (p->classes.size() > 1) {
+    // the forked class streams take the priority of the caller's stream; work still
+    // queued on the streams they replace completes, and this run's forks are ordered
+    // after it through the caller's stream (the last run joined into it)
+    int prio = 0;
+    BC_CUDA(cudaStreamGetPriority(static_cast<cudaStream_t>(stream), &prio));
+    if (prio != p->aux_prio) {
+      for (int k = 0; k < 2; ++k) {
+        cudaStream_t ns = nullptr;
+        BC_CUDA(cudaStreamCreateWithPriority(&ns, cudaStreamNonBlocking, prio));
+        if (p->aux[k]) cudaStreamDestroy(p->aux[k]);
+        p->aux[k] = ns;
+      }
+      p->aux_prio = prio;
+    }
+  }
   int64_t done = 0;
   while (done < n_steps) {
     const int32_t k = int32_t(std::min<int64_t>(per_launch, n_steps - done));
@@ -1625,10 +1644,14 @@ bc_status bc_plan_create(const bc_batch_spec* spec, const bc_plan_options* opts_
     BC_TRYC(cudaEventCreateWithFlags(&p->ev_join[k], cudaEventDisableTiming));
   }
   BC_TRYC(cudaEventCreateWithFlags(&p->ev_fork, cudaEventDisableTiming));
+  int prio_least = 0, prio_greatest = 0;
+  BC_TRYC(cudaDeviceGetStreamPriorityRange(&prio_least, &prio_greatest));
+  BC_TRYC(cudaStreamCreateWithPriority(&p->init_stream, cudaStreamNonBlocking, prio_greatest));
   *out = p;
-  // the initial reset runs on the plan's own non-blocking stream, so that creating
-  // a plan does not wait for work other plans have queued on the legacy stream
-  return bc_reset(p, p->aux[0]);
+  // The initial reset runs on the plan's own non-blocking stream of the highest
+  // priority: creating a plan waits neither for work other plans have queued on
+  // the legacy stream nor, behind their pending blocks, for free SM slots.
+  return bc_reset(p, p->init_stream);
 }
 
 bc_status bc_lower_cell(const bc_batch_spec* spec, int64_t cell, int32_t* n_cv, int32_t* n_node, double* cv_area,

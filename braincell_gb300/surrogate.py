@@ -23,7 +23,9 @@ flagged cells are run again with their full morphology (per-cell fallback).
 
 from __future__ import annotations
 
+import gc
 import math
+import os
 import time
 from dataclasses import dataclass, field, replace
 
@@ -36,8 +38,6 @@ __all__ = ["CUT_DEPTH", "PACKAGED_MODEL", "Port", "SurrogateModel", "branch_dept
            "ports_to_batch", "make_training_descs", "collect_trajectories", "train_surrogate", "run_surrogate",
            "fallback_plan_options", "SurrogateRunner",
            "SurrogateRun", "save_model", "load_model"]
-
-import os
 
 CUT_DEPTH = 4
 PACKAGED_MODEL = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data", "surrogate_uneven.npz")
@@ -465,6 +465,23 @@ class SurrogateRunner:
         main = self._main
         sid = int(main.cuda_stream)
         torch.cuda.current_stream(self.device).synchronize()
+        # The host loop below is on the critical path of the fallback (flag reads,
+        # plan builds, launches): the cyclic garbage collector is paused for its
+        # length, since a full collection of a large heap takes tens of ms.
+        gc_on = gc.isenabled()
+        gc.disable()
+        try:
+            return self._run(n_steps, dt)
+        finally:
+            if gc_on:
+                gc.enable()
+
+    def _run(self, n_steps: int, dt: float) -> SurrogateRun:
+        import torch
+
+        plan = self.plan
+        main = self._main
+        sid = int(main.cuda_stream)
         n = len(self.descs)
         spl = int(plan.info["steps_per_launch"])
         watch = self.fallback and self.n_ports > 0
@@ -479,9 +496,13 @@ class SurrogateRunner:
         queued = []
         done = 0
 
+        # the first launches are short, so that the envelope exits of the first
+        # stimulus onsets are seen (and their full solves started) early
+        lead = [max(1, spl // 4), max(1, spl // 4), max(1, spl // 2)]
+
         def enqueue():
             nonlocal done
-            k = min(spl, n_steps - done)
+            k = min(lead.pop(0) if lead else spl, n_steps - done)
             plan.run(k, dt, stream=sid, check=False)
             done += k
             ev = torch.cuda.Event()
@@ -505,7 +526,10 @@ class SurrogateRunner:
                 new = np.nonzero((flags != 0) & ~flagged)[0]
                 if new.size:
                     flagged[new] = True
-                    side = torch.cuda.Stream(self.device)
+                    # high priority: the block scheduler gives the fallback's tiles the
+                    # next free SM slots ahead of the queued reduced launches, so the
+                    # full solve runs at its own step latency
+                    side = torch.cuda.Stream(self.device, priority=-1)
                     fp = self._fallback_plan(new)
                     fp.run(n_steps, dt, stream=int(side.cuda_stream), check=False)
                     fallbacks.append((new, fp, side))
