@@ -20,6 +20,7 @@ from __future__ import annotations
 import argparse
 import json
 import os
+import shutil
 import subprocess
 import sys
 import threading
@@ -89,7 +90,9 @@ def _traffic_per_node_launch():
 
 
 class ClockSampler:
-    """nvidia-smi SM clock / throttle sampling while the timed region runs."""
+    """nvidia-smi SM clock / throttle sampling while the timed region runs: one
+    ``nvidia-smi -lms 200`` process for the whole region (one NVML session, no
+    process started per sample), its lines read by a thread."""
 
     FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
               "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
@@ -98,28 +101,38 @@ class ClockSampler:
     def __init__(self, device: int):
         self.device = device
         self.samples = []
-        self._stop = threading.Event()
+        self._p = None
         self._t = None
 
-    def _run(self):
-        while not self._stop.is_set():
-            try:
-                out = subprocess.run(
-                    ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits"],
-                    capture_output=True, text=True, timeout=5)
-                if out.returncode == 0:
-                    self.samples.append([x.strip() for x in out.stdout.strip().split(",")])
-            except Exception:
-                pass
-            self._stop.wait(0.2)
+    def _read(self):
+        for line in self._p.stdout:
+            parts = [x.strip() for x in line.strip().split(",")]
+            if len(parts) >= 3:
+                self.samples.append(parts)
 
     def __enter__(self):
-        self._t = threading.Thread(target=self._run, daemon=True)
+        cmd = ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+               "-lms", "200"]
+        if shutil.which("stdbuf"):
+            cmd = ["stdbuf", "-oL"] + cmd  # a line per sample through the pipe
+        try:
+            self._p = subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self._p = None
+            return self
+        self._t = threading.Thread(target=self._read, daemon=True)
         self._t.start()
         return self
 
     def __exit__(self, *exc):
-        self._stop.set()
+        if self._p is None:
+            return
+        self._p.terminate()
+        try:
+            self._p.wait(timeout=10)
+        except subprocess.TimeoutExpired:
+            self._p.kill()
+            self._p.wait(timeout=10)
         if self._t is not None:
             self._t.join(timeout=10)
 
