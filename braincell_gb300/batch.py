@@ -21,6 +21,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from . import _abi
+from . import catalogue
 from .catalogue import region_record
 from .mech import CableProperty, CurrentClamp, CurrentProbe, ExpSyn, MechanismProbe, StateProbe
 
@@ -346,6 +347,14 @@ PROBE_CURRENTS = {
     "KM_RI2021_SC": _abi.BC_CUR_KM,
 }
 ION_CURRENTS = {"na": _abi.BC_CUR_ION_NA, "k": _abi.BC_CUR_ION_K, "ca": _abi.BC_CUR_ION_CA}
+
+
+# same-form classes record through the views of the class whose kernel they use
+for _cls, _kern in catalogue.SAME_FORM.items():
+    for (_c, _f), _view in list(PROBE_STATES.items()):
+        if _c == _kern:
+            PROBE_STATES[(_cls, _f)] = _view
+    PROBE_CURRENTS[_cls] = PROBE_CURRENTS[_kern]
 
 
 def probe_field_of(decl, mechs) -> int:

@@ -13,6 +13,16 @@ Every class name, parameter name and default below is the reference's:
 * ``Na_HH1952``   -- channel/sodium.py:293  (g_max 120, q10 3, temp = temp_ref = 36 degC, V_sh -45)
 * ``K_HH1952``    -- channel/potassium.py:341 (g_max 10, q10 3, temp = temp_ref = 36 degC, V_sh -45)
 * ``KM_RI2021_SC``-- channel/potassium.py:1597 (g_max 0.25, temp 30 degC; gate q10 3 at 22 degC)
+* ``Na_TM1991``   -- channel/sodium.py:174  (g_max 120, q10 1, temp = temp_ref = 36 degC, V_sh -63)
+* ``K_TM1991``    -- channel/potassium.py:218 (g_max 10, q10 1, temp = temp_ref = 36 degC, V_sh -60)
+* ``CaHT_HM1992`` -- channel/calcium.py:511 (g_max 2, q10_p 3.55, q10_q 3, temp_ref 24 degC, V_sh 25)
+
+Same-form classes: Na_TM1991 has Na_Ba2002's Traub-Miles rate functions written
+in terms of V_sh - V (sodium.py:275-289 against :154-170), K_TM1991 has
+KDR_Ba2002's (potassium.py:331-337 against :208-214), and CaHT_HM1992 has
+CaT_HM1992's (calcium.py:645-663 against :355-373); only their defaults differ.
+Each fills the parameter record and kernel slot of its same-form class, so a
+region cannot carry both classes of one pair.
 * ions: ``SodiumFixed`` E 50 (ion/sodium.py:149), ``PotassiumFixed`` E -95
   (ion/potassium.py:151), ``CalciumFixed`` E 120 (ion/calcium.py:187) -- the
   defaults used when no ion is painted (_compute/ions.py:107-113);
@@ -30,7 +40,7 @@ import numpy as np
 from . import _abi
 from .mech import CableProperty, Channel, Ion, celsius2kelvin
 
-__all__ = ["CHANNELS", "IONS", "region_record", "q10_phi"]
+__all__ = ["CHANNELS", "IONS", "SAME_FORM", "kernel_class", "region_record", "q10_phi"]
 
 T36 = celsius2kelvin(36.0)
 T24 = celsius2kelvin(24.0)
@@ -53,7 +63,14 @@ CHANNELS: dict[str, dict[str, float]] = {
     "Na_HH1952": {"g_max": 120.0, "temp": T36, "q10": 3.0, "temp_ref": T36, "V_sh": -45.0},
     "K_HH1952": {"g_max": 10.0, "temp": T36, "q10": 3.0, "temp_ref": T36, "V_sh": -45.0},
     "KM_RI2021_SC": {"g_max": 0.25, "temp": T30},
+    "Na_TM1991": {"g_max": 120.0, "temp": T36, "q10": 1.0, "temp_ref": T36, "V_sh": -63.0},
+    "K_TM1991": {"g_max": 10.0, "temp": T36, "q10": 1.0, "temp_ref": T36, "V_sh": -60.0},
+    "CaHT_HM1992": {
+        "g_max": 2.0, "temp": T36, "q10_p": 3.55, "temp_ref_p": T24, "q10_q": 3.0, "temp_ref_q": T24, "V_sh": 25.0,
+    },
 }
+# class -> the class whose kernel (rate functions, parameter slots, states) it uses
+SAME_FORM = {"Na_TM1991": "Na_Ba2002", "K_TM1991": "KDR_Ba2002", "CaHT_HM1992": "CaT_HM1992"}
 # gate temperature factors fixed by a class (not constructor parameters)
 KM_Q10, KM_TEMP_REF = 3.0, T22
 _ALIASES = {"leaky": "IL"}
@@ -66,6 +83,11 @@ IONS: dict[str, dict[str, float]] = {
         "temp": T36, "d": 1.0, "tau": 5.0, "C_rest": 2.4e-4, "Co": 2.0, "Ci_initializer": 2.4e-4,
     },
 }
+
+
+def kernel_class(name: str) -> str:
+    """The class whose kernel a channel class runs on (itself unless same-form)."""
+    return SAME_FORM.get(name, name)
 
 
 def q10_phi(q10: float, temp: float, temp_ref: float) -> float:
@@ -94,6 +116,7 @@ def region_record(mechs, cable: CableProperty) -> tuple[int, np.ndarray]:
     rec[_abi.BC_P_EK] = IONS["PotassiumFixed"]["E"]
     rec[_abi.BC_P_ECA] = IONS["CalciumFixed"]["E"]
     bits = 0
+    kernel_owner: dict[str, str] = {}
     last: dict[str, object] = {}
     for m in mechs:
         last[m.class_name if m.class_name not in _ALIASES else _ALIASES[m.class_name]] = m
@@ -122,6 +145,12 @@ def region_record(mechs, cable: CableProperty) -> tuple[int, np.ndarray]:
         if name not in CHANNELS:
             raise ValueError(f"Unsupported channel class {name!r}; supported: {sorted(CHANNELS)}.")
         p = _params(CHANNELS, name, decl)
+        kname = kernel_class(name)
+        if kname in kernel_owner:
+            raise ValueError(f"{name} and {kernel_owner[kname]} run on the same kernel mechanism and cannot be "
+                             "painted on one region.")
+        kernel_owner[kname] = name
+        name = kname
         if name == "IL":
             bits |= _abi.BC_M_IL
             rec[_abi.BC_P_IL_G], rec[_abi.BC_P_IL_E] = p["g_max"], p["E"]

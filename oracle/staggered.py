@@ -90,6 +90,10 @@ CHANNEL_DEFAULTS = {
     "Na_HH1952": dict(g_max=120.0, temp=_c2k(36.0), q10=3.0, temp_ref=_c2k(36.0), V_sh=-45.0),  # sodium.py:371-380
     "K_HH1952": dict(g_max=10.0, temp=_c2k(36.0), q10=3.0, temp_ref=_c2k(36.0), V_sh=-45.0),  # potassium.py:433-441
     "KM_RI2021_SC": dict(g_max=0.25, temp=_c2k(30.0)),  # potassium.py:1716-1721
+    "Na_TM1991": dict(g_max=120.0, temp=_c2k(36.0), q10=1.0, temp_ref=_c2k(36.0), V_sh=-63.0),  # sodium.py:261-265
+    "K_TM1991": dict(g_max=10.0, temp=_c2k(36.0), q10=1.0, temp_ref=_c2k(36.0), V_sh=-60.0),  # potassium.py:317-321
+    "CaHT_HM1992": dict(g_max=2.0, temp=_c2k(36.0), q10_p=3.55, temp_ref_p=_c2k(24.0), q10_q=3.0,
+                        temp_ref_q=_c2k(24.0), V_sh=25.0),  # calcium.py:627-633
 }
 ION_DEFAULTS = {
     "SodiumFixed": dict(E=50.0),
@@ -327,6 +331,23 @@ def rates(name: str, V, p: dict, Ci=None):
     if name == "K_HH1952":  # potassium.py:450-456
         Vp = V - p["V_sh"]
         return {"p": ("ab", 0.1 / exprel(-(Vp + 10.0) / 10.0), 0.125 * np.exp(-(Vp + 20.0) / 80.0))}
+    if name == "Na_TM1991":  # sodium.py:275-289, written as there (V_sh - V)
+        t = p["V_sh"] - V
+        return {
+            "p": ("ab", 0.32 * 4.0 / exprel((13.0 + t) / 4.0), 0.28 * 5.0 / exprel((-t - 40.0) / 5.0)),
+            "q": ("ab", 0.128 * np.exp((17.0 + t) / 18.0), 4.0 / (1.0 + np.exp(-(-t - 40.0) / 5.0))),
+        }
+    if name == "K_TM1991":  # potassium.py:331-337, written as there (V_sh - V)
+        t = p["V_sh"] - V
+        return {"p": ("ab", 0.032 * 5.0 / exprel((15.0 + t) / 5.0), 0.5 * np.exp((10.0 + t) / 40.0))}
+    if name == "CaHT_HM1992":  # calcium.py:645-663
+        Vs = V - p["V_sh"]
+        return {
+            "p": ("it", 1.0 / (1.0 + np.exp(-(Vs + 59.0) / 6.2)),
+                  1.0 / (np.exp(-(Vs + 132.0) / 16.7) + np.exp((Vs + 16.8) / 18.2)) + 0.612),
+            "q": ("it", 1.0 / (1.0 + np.exp((Vs + 83.0) / 4.0)),
+                  np.where(Vs >= -80.0, np.exp(-(Vs + 22.0) / 10.5) + 28.0, np.exp((Vs + 467.0) / 66.6))),
+        }
     if name == "KM_RI2021_SC":  # potassium.py:1735-1748
         a = 0.0033 * np.exp((V + 30.0) / 40.0)
         b = 0.0033 * np.exp((V + 30.0) / -20.0)
@@ -344,9 +365,13 @@ _GATES = {  # (gate, power, phi-key)
     "Na_HH1952": (("p", 3, "phi"), ("q", 1, "phi")),
     "K_HH1952": (("p", 4, "phi"),),
     "KM_RI2021_SC": (("n", 1, "phi"),),
+    "Na_TM1991": (("p", 3, "phi"), ("q", 1, "phi")),
+    "K_TM1991": (("p", 4, "phi"),),
+    "CaHT_HM1992": (("p", 2, "phi_p"), ("q", 1, "phi_q")),
 }
 _ION_OF = {"Na_Ba2002": "na", "KDR_Ba2002": "k", "CaL_IS2008": "ca", "CaT_HM1992": "ca",
-           "K_Leak": "k", "AHP_De1994": "k", "Na_HH1952": "na", "K_HH1952": "k", "KM_RI2021_SC": "k"}
+           "K_Leak": "k", "AHP_De1994": "k", "Na_HH1952": "na", "K_HH1952": "k", "KM_RI2021_SC": "k",
+           "Na_TM1991": "na", "K_TM1991": "k", "CaHT_HM1992": "ca"}
 
 
 def _resolve(table: dict, decl) -> dict:
@@ -356,11 +381,11 @@ def _resolve(table: dict, decl) -> dict:
             raise ValueError(f"{decl.class_name}: unknown parameter {k!r}.")
         p[k] = float(v)
     name = decl.class_name
-    if name in ("Na_Ba2002", "KDR_Ba2002", "HCN_HM1992", "Na_HH1952", "K_HH1952"):
+    if name in ("Na_Ba2002", "KDR_Ba2002", "HCN_HM1992", "Na_HH1952", "K_HH1952", "Na_TM1991", "K_TM1991"):
         p["phi"] = p["q10"] ** ((p["temp"] - p["temp_ref"]) / 10.0)
     elif name == "KM_RI2021_SC":  # Gate("n", q10=3.0, temp_ref=22 degC), potassium.py:1710
         p["phi"] = 3.0 ** ((p["temp"] - (273.15 + 22.0)) / 10.0)
-    elif name in ("CaL_IS2008", "CaT_HM1992"):
+    elif name in ("CaL_IS2008", "CaT_HM1992", "CaHT_HM1992"):
         p["phi_p"] = p["q10_p"] ** ((p["temp"] - p["temp_ref_p"]) / 10.0)
         p["phi_q"] = p["q10_q"] ** ((p["temp"] - p["temp_ref_q"]) / 10.0)
     return p
@@ -872,11 +897,11 @@ class OracleCell:
         return total
 
     def _ca_current(self, pv):
-        """``Ion.current`` of the calcium ion (sum of CaL + CaT), uA/cm^2."""
+        """``Ion.current`` of the calcium ion (sum over its channels), uA/cm^2."""
         I = np.zeros_like(pv)
         E_ca = self._E_ca()
-        for name in ("CaL_IS2008", "CaT_HM1992"):
-            if name in self.chan:
+        for name in self.chan:
+            if _ION_OF.get(name) == "ca":
                 I = I + self.chan[name]["g_max"] * self._gate_product(name) * (E_ca - pv)
         return I
 

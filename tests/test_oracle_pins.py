@@ -211,3 +211,40 @@ def test_km_rates_and_temperature_factor():
     np.testing.assert_allclose(r["n"][2], 1 / (a + b), rtol=1e-12)
     assert q10_phi(KM_Q10, celsius2kelvin(30.0), KM_TEMP_REF) == pytest.approx(3.0 ** 0.8)
     assert q10_phi(3.0, celsius2kelvin(46.0), celsius2kelvin(36.0)) == pytest.approx(3.0)  # potassium_test.py:113-121
+
+
+@pytest.mark.parametrize("cls,kern", [("Na_TM1991", "Na_Ba2002"), ("K_TM1991", "KDR_Ba2002"),
+                                      ("CaHT_HM1992", "CaT_HM1992")])
+def test_same_form_classes_match_their_kernel_class(cls, kern):
+    # The TM1991 classes restate the Traub-Miles rates in terms of V_sh - V
+    # (sodium.py:275-289, potassium.py:331-337) and CaHT_HM1992 repeats CaT_HM1992's
+    # (calcium.py:645-663); with the same V_sh the gate rates are equal, which is why
+    # the catalogue runs them on the kernel class with their own defaults.
+    from braincell_gb300 import catalogue
+
+    assert catalogue.kernel_class(cls) == kern
+    p = dict(O.CHANNEL_DEFAULTS[cls])
+    q = dict(O.CHANNEL_DEFAULTS[kern], V_sh=p["V_sh"])
+    V = np.concatenate([np.linspace(-120.0, 60.0, 721), p["V_sh"] + np.array([13.0, 15.0, 40.0, -80.0])])
+    a, b = O.rates(cls, V, p), O.rates(kern, V, q)
+    assert a.keys() == b.keys()
+    for g in a:
+        assert a[g][0] == b[g][0]
+        for k in (1, 2):
+            np.testing.assert_allclose(a[g][k], b[g][k], rtol=1e-12, atol=0.0)
+
+
+def test_same_form_defaults_and_exclusion():
+    from braincell_gb300 import _abi, catalogue
+    from braincell_gb300.mech import CableProperty, Channel
+
+    bits, rec = catalogue.region_record([Channel("Na_TM1991"), Channel("K_TM1991", g_max=5.0),
+                                         Channel("CaHT_HM1992")], CableProperty())
+    assert bits == _abi.BC_M_NA | _abi.BC_M_KDR | _abi.BC_M_CAT
+    assert (rec[_abi.BC_P_NA_G], rec[_abi.BC_P_NA_VSH], rec[_abi.BC_P_NA_PHI]) == (120.0, -63.0, 1.0)
+    assert (rec[_abi.BC_P_KDR_G], rec[_abi.BC_P_KDR_VSH], rec[_abi.BC_P_KDR_PHI]) == (5.0, -60.0, 1.0)
+    assert rec[_abi.BC_P_CAT_VSH] == 25.0
+    assert rec[_abi.BC_P_CAT_PHIP] == pytest.approx(3.55 ** 1.2) and rec[_abi.BC_P_CAT_PHIQ] == pytest.approx(3.0 ** 1.2)
+    for pair in (("Na_TM1991", "Na_Ba2002"), ("KDR_Ba2002", "K_TM1991"), ("CaT_HM1992", "CaHT_HM1992")):
+        with pytest.raises(ValueError, match="same kernel"):
+            catalogue.region_record([Channel(pair[0]), Channel(pair[1])], CableProperty())
