@@ -34,9 +34,11 @@ BC_M_CADET = 1 << 8
 BC_M_NAHH = 1 << 9
 BC_M_KHH = 1 << 10
 BC_M_KM = 1 << 11
-BC_M_ALL = 0xFFF
+BC_M_KA1 = 1 << 12
+BC_M_KA2 = 1 << 13
+BC_M_ALL = 0x3FFF
 
-BC_NPARAM = 48
+BC_NPARAM = 56
 BC_P_INVCM = 0
 BC_P_VREST = 1
 BC_P_ENA = 2
@@ -81,6 +83,14 @@ BC_P_KHH_VSH = 40
 BC_P_KHH_PHI = 41
 BC_P_KM_G = 42
 BC_P_KM_PHI = 43
+BC_P_KA1_G = 44
+BC_P_KA1_VSH = 45
+BC_P_KA1_PHIP = 46
+BC_P_KA1_PHIQ = 47
+BC_P_KA2_G = 48
+BC_P_KA2_VSH = 49
+BC_P_KA2_PHIP = 50
+BC_P_KA2_PHIQ = 51
 
 BC_PREC_F32 = 0
 BC_PREC_F64 = 1
@@ -104,7 +114,9 @@ BC_CUR_KM = 10
 BC_CUR_ION_NA = 11
 BC_CUR_ION_K = 12
 BC_CUR_ION_CA = 13
-BC_NCUR = 14
+BC_CUR_KA1 = 14
+BC_CUR_KA2 = 15
+BC_NCUR = 16
 
 BC_STATE_V = 0
 BC_STATE_NA_P = 1
@@ -121,7 +133,11 @@ BC_STATE_NAHH_P = 11
 BC_STATE_NAHH_Q = 12
 BC_STATE_KHH_P = 13
 BC_STATE_KM_N = 14
-BC_NSTATE_VIEW = 15
+BC_STATE_KA1_P = 15
+BC_STATE_KA1_Q = 16
+BC_STATE_KA2_P = 17
+BC_STATE_KA2_Q = 18
+BC_NSTATE_VIEW = 19
 BC_NOALLOC_MAX_CV = 262144
 
 STATE_NAMES = {
@@ -140,6 +156,10 @@ STATE_NAMES = {
     "NaHH_q": BC_STATE_NAHH_Q,
     "KHH_p": BC_STATE_KHH_P,
     "KM_n": BC_STATE_KM_N,
+    "KA1_p": BC_STATE_KA1_P,
+    "KA1_q": BC_STATE_KA1_Q,
+    "KA2_p": BC_STATE_KA2_P,
+    "KA2_q": BC_STATE_KA2_Q,
 }
 
 _p = C.POINTER

@@ -336,6 +336,8 @@ PROBE_STATES = {
     ("Na_HH1952", "p"): _abi.BC_STATE_NAHH_P, ("Na_HH1952", "q"): _abi.BC_STATE_NAHH_Q,
     ("K_HH1952", "p"): _abi.BC_STATE_KHH_P,
     ("KM_RI2021_SC", "n"): _abi.BC_STATE_KM_N,
+    ("KA1_HM1992", "p"): _abi.BC_STATE_KA1_P, ("KA1_HM1992", "q"): _abi.BC_STATE_KA1_Q,
+    ("KA2_HM1992", "p"): _abi.BC_STATE_KA2_P, ("KA2_HM1992", "q"): _abi.BC_STATE_KA2_Q,
 }
 
 
@@ -344,7 +346,7 @@ PROBE_CURRENTS = {
     "IL": _abi.BC_CUR_IL, "K_Leak": _abi.BC_CUR_KLEAK, "Na_Ba2002": _abi.BC_CUR_NA, "KDR_Ba2002": _abi.BC_CUR_KDR,
     "CaL_IS2008": _abi.BC_CUR_CAL, "CaT_HM1992": _abi.BC_CUR_CAT, "HCN_HM1992": _abi.BC_CUR_HCN,
     "AHP_De1994": _abi.BC_CUR_AHP, "Na_HH1952": _abi.BC_CUR_NAHH, "K_HH1952": _abi.BC_CUR_KHH,
-    "KM_RI2021_SC": _abi.BC_CUR_KM,
+    "KM_RI2021_SC": _abi.BC_CUR_KM, "KA1_HM1992": _abi.BC_CUR_KA1, "KA2_HM1992": _abi.BC_CUR_KA2,
 }
 ION_CURRENTS = {"na": _abi.BC_CUR_ION_NA, "k": _abi.BC_CUR_ION_K, "ca": _abi.BC_CUR_ION_CA}
 

@@ -16,6 +16,8 @@ Every class name, parameter name and default below is the reference's:
 * ``Na_TM1991``   -- channel/sodium.py:174  (g_max 120, q10 1, temp = temp_ref = 36 degC, V_sh -63)
 * ``K_TM1991``    -- channel/potassium.py:218 (g_max 10, q10 1, temp = temp_ref = 36 degC, V_sh -60)
 * ``CaHT_HM1992`` -- channel/calcium.py:511 (g_max 2, q10_p 3.55, q10_q 3, temp_ref 24 degC, V_sh 25)
+* ``KA1_HM1992``  -- channel/potassium.py:460 (g_max 30, q10_p = q10_q = 1, temp = temp_refs = 36 degC, V_sh 0)
+* ``KA2_HM1992``  -- channel/potassium.py:614 (g_max 20, otherwise as KA1_HM1992)
 
 Same-form classes: Na_TM1991 has Na_Ba2002's Traub-Miles rate functions written
 in terms of V_sh - V (sodium.py:275-289 against :154-170), K_TM1991 has
@@ -67,6 +69,12 @@ CHANNELS: dict[str, dict[str, float]] = {
     "K_TM1991": {"g_max": 10.0, "temp": T36, "q10": 1.0, "temp_ref": T36, "V_sh": -60.0},
     "CaHT_HM1992": {
         "g_max": 2.0, "temp": T36, "q10_p": 3.55, "temp_ref_p": T24, "q10_q": 3.0, "temp_ref_q": T24, "V_sh": 25.0,
+    },
+    "KA1_HM1992": {
+        "g_max": 30.0, "temp": T36, "q10_p": 1.0, "temp_ref_p": T36, "q10_q": 1.0, "temp_ref_q": T36, "V_sh": 0.0,
+    },
+    "KA2_HM1992": {
+        "g_max": 20.0, "temp": T36, "q10_p": 1.0, "temp_ref_p": T36, "q10_q": 1.0, "temp_ref_q": T36, "V_sh": 0.0,
     },
 }
 # class -> the class whose kernel (rate functions, parameter slots, states) it uses
@@ -196,6 +204,13 @@ def region_record(mechs, cable: CableProperty) -> tuple[int, np.ndarray]:
             bits |= _abi.BC_M_KM
             rec[_abi.BC_P_KM_G] = p["g_max"]
             rec[_abi.BC_P_KM_PHI] = q10_phi(KM_Q10, p["temp"], KM_TEMP_REF)
+        elif name in ("KA1_HM1992", "KA2_HM1992"):
+            one = name == "KA1_HM1992"
+            bits |= _abi.BC_M_KA1 if one else _abi.BC_M_KA2
+            base = _abi.BC_P_KA1_G if one else _abi.BC_P_KA2_G
+            rec[base], rec[base + 1] = p["g_max"], p["V_sh"]
+            rec[base + 2] = q10_phi(p["q10_p"], p["temp"], p["temp_ref_p"])
+            rec[base + 3] = q10_phi(p["q10_q"], p["temp"], p["temp_ref_q"])
     if bits & (_abi.BC_M_AHP) and not bits & _abi.BC_M_CADET:
         # AHP reads Ci from the calcium ion; with a fixed Ca ion Ci is the class default.
         rec[_abi.BC_P_CA_CI0] = 5e-5

@@ -276,6 +276,16 @@ __device__ __forceinline__ double probe_current(const Real* st, int N, const Rea
       }
       case BC_CUR_KM:
         return (m & BC_M_KM) ? P[BC_P_KM_G] * st[kSlotKMN * N] * (P[BC_P_EK] - v) : Real(0);
+      case BC_CUR_KA1: {
+        if (!(m & BC_M_KA1)) return Real(0);
+        const Real p2 = st[kSlotKA1P * N] * st[kSlotKA1P * N];
+        return P[BC_P_KA1_G] * p2 * p2 * st[kSlotKA1Q * N] * (P[BC_P_EK] - v);
+      }
+      case BC_CUR_KA2: {
+        if (!(m & BC_M_KA2)) return Real(0);
+        const Real p2 = st[kSlotKA2P * N] * st[kSlotKA2P * N];
+        return P[BC_P_KA2_G] * p2 * p2 * st[kSlotKA2Q * N] * (P[BC_P_EK] - v);
+      }
     }
     return Real(0);
   };
@@ -284,7 +294,7 @@ __device__ __forceinline__ double probe_current(const Real* st, int N, const Rea
       return double(cur(BC_CUR_NA)) + double(cur(BC_CUR_NAHH));
     case BC_CUR_ION_K:
       return double(cur(BC_CUR_KDR)) + double(cur(BC_CUR_KLEAK)) + double(cur(BC_CUR_AHP)) + double(cur(BC_CUR_KHH)) +
-             double(cur(BC_CUR_KM));
+             double(cur(BC_CUR_KM)) + double(cur(BC_CUR_KA1)) + double(cur(BC_CUR_KA2));
     case BC_CUR_ION_CA:
       return double(cur(BC_CUR_CAL)) + double(cur(BC_CUR_CAT));
     default:
@@ -292,10 +302,28 @@ __device__ __forceinline__ double probe_current(const Real* st, int N, const Rea
   }
 }
 
-// Channels outside the main workloads' mix (classic Hodgkin-Huxley Na / K and the
-// M current): kept out of line so that their registers do not weigh on the
-// common path; same exp-Euler steps and ohmic currents as the others.
-constexpr uint32_t kExtraChannels = BC_M_NAHH | BC_M_KHH | BC_M_KM;
+// Channels outside the main workloads' mix (classic Hodgkin-Huxley Na / K, the
+// M current, the A current): kept out of line so that their registers do not
+// weigh on the common path; same exp-Euler steps and ohmic currents as the others.
+constexpr uint32_t kExtraChannels = BC_M_NAHH | BC_M_KHH | BC_M_KM | BC_M_KA1 | BC_M_KA2;
+
+// One A-current mechanism (p^4 q, E_K) in slots (sp, sq) with parameters from pg.
+template <typename Real>
+__device__ __forceinline__ void a_current(Real* st, int N, const Real* P, int sp, int sq, int pg, Real mid,
+                                          Real inv_slope, Real v, Real dt, bool advance, Real& G, Real& I) {
+  Real p = st[sp * N], q = st[sq * N];
+  if (advance) {
+    const KARates<Real> r(v, P[pg + 1], mid, inv_slope);
+    p = gate_it(p, r.pinf, r.ptau, P[pg + 2], dt);
+    q = gate_it(q, r.qinf, r.qtau, P[pg + 3], dt);
+    st[sp * N] = p;
+    st[sq * N] = q;
+  }
+  const Real p2 = p * p;
+  const Real g = P[pg] * p2 * p2 * q;
+  G += g;
+  I += g * (P[BC_P_EK] - v);
+}
 
 template <typename Real>
 __device__ __noinline__ void extra_channels(Real* st, int N, const Real* P, uint32_t m, Real v, Real dt, bool advance,
@@ -337,6 +365,10 @@ __device__ __noinline__ void extra_channels(Real* st, int N, const Real* P, uint
     G += g;
     I += g * (P[BC_P_EK] - v);
   }
+  if (m & BC_M_KA1)
+    a_current(st, N, P, kSlotKA1P, kSlotKA1Q, BC_P_KA1_G, Real(kKA1Mid), Real(kKA1InvSlope), v, dt, advance, G, I);
+  if (m & BC_M_KA2)
+    a_current(st, N, P, kSlotKA2P, kSlotKA2Q, BC_P_KA2_G, Real(kKA2Mid), Real(kKA2InvSlope), v, dt, advance, G, I);
 }
 
 // One node's mechanisms.  `st` points at the node's slot-0 state (stride N).
@@ -512,6 +544,16 @@ __device__ __forceinline__ void steady_states(const Real* P, uint32_t m, Real* s
     st[kSlotKHHP * N] = r.a / (r.a + r.b);
   }
   if (m & BC_M_KM) st[kSlotKMN * N] = KMRates<Real>(v).ninf;
+  if (m & BC_M_KA1) {
+    const KARates<Real> r(v, P[BC_P_KA1_VSH], Real(kKA1Mid), Real(kKA1InvSlope));
+    st[kSlotKA1P * N] = r.pinf;
+    st[kSlotKA1Q * N] = r.qinf;
+  }
+  if (m & BC_M_KA2) {
+    const KARates<Real> r(v, P[BC_P_KA2_VSH], Real(kKA2Mid), Real(kKA2InvSlope));
+    st[kSlotKA2P * N] = r.pinf;
+    st[kSlotKA2Q * N] = r.qinf;
+  }
 }
 
 // Row i of the next linear system: diag = 1 + dt (D + G / cm), rhs = dt I / cm

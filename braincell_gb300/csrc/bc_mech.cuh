@@ -12,6 +12,7 @@
 //   Na_HH1952        channel/sodium.py:384-399
 //   K_HH1952         channel/potassium.py:450-456
 //   KM_RI2021_SC     channel/potassium.py:1735-1748
+//   KA1_HM1992       channel/potassium.py:592-611, KA2_HM1992 :743-762
 //   CalciumDetailed  ion/calcium.py:499-505, Nernst E: ion/_base.py:463-469
 // CUDA's own exp / expm1 / log are called; nothing of the math library is
 // re-implemented here.
@@ -174,6 +175,25 @@ struct KMRates {
   }
 };
 
+// KA1_HM1992 / KA2_HM1992 (A current): the two classes differ only in the
+// activation midpoint and slope (KA1: -60 mV / 8.5, KA2: -36 mV / 20); V' = V - V_sh.
+template <typename Real>
+struct KARates {
+  Real pinf, ptau, qinf, qtau;
+  __device__ __forceinline__ KARates(Real v, Real vsh, Real pmid, Real pinv_slope) {
+    const Real vp = v - vsh;
+    pinf = rdiv(Real(1), Real(1) + rexp(-(vp + pmid) * pinv_slope));
+    ptau = rdiv(Real(1), rexp((vp + Real(35.8)) * Real(1.0 / 19.7)) + rexp(-(vp + Real(79.7)) * Real(1.0 / 12.7))) +
+           Real(0.37);
+    qinf = rdiv(Real(1), Real(1) + rexp((vp + Real(78)) * Real(1.0 / 6)));
+    qtau = vp < Real(-63)
+               ? rdiv(Real(1), rexp((vp + Real(46)) * Real(0.2)) + rexp(-(vp + Real(238)) * Real(1.0 / 37.5)))
+               : Real(19);
+  }
+};
+constexpr double kKA1Mid = 60.0, kKA1InvSlope = 1.0 / 8.5;
+constexpr double kKA2Mid = 36.0, kKA2InvSlope = 1.0 / 20.0;
+
 // Fixed state slot of every mechanism state in the [slot][node] state array.
 constexpr int kSlotNaP = 0;
 constexpr int kSlotNaQ = 1;
@@ -190,7 +210,11 @@ constexpr int kSlotNaHHP = 11;
 constexpr int kSlotNaHHQ = 12;
 constexpr int kSlotKHHP = 13;
 constexpr int kSlotKMN = 14;
-constexpr int kNumSlots = 15;
+constexpr int kSlotKA1P = 15;
+constexpr int kSlotKA1Q = 16;
+constexpr int kSlotKA2P = 17;
+constexpr int kSlotKA2Q = 18;
+constexpr int kNumSlots = 19;
 
 constexpr double kFaraday = 96485.33212;   // C/mol
 constexpr double kGasR = 8.314462618;      // J/(mol K)

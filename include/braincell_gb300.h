@@ -53,10 +53,12 @@ typedef int32_t bc_status;
 #define BC_M_NAHH (1u << 9)      /* channel/sodium.py:293     Na_HH1952   p^3 q, E_Na          */
 #define BC_M_KHH (1u << 10)      /* channel/potassium.py:341  K_HH1952    p^4, E_K             */
 #define BC_M_KM (1u << 11)       /* channel/potassium.py:1597 KM_RI2021_SC n, E_K              */
-#define BC_M_ALL 0xFFFu
+#define BC_M_KA1 (1u << 12)      /* channel/potassium.py:460  KA1_HM1992  p^4 q, E_K           */
+#define BC_M_KA2 (1u << 13)      /* channel/potassium.py:614  KA2_HM1992  p^4 q, E_K           */
+#define BC_M_ALL 0x3FFFu
 
 /* Per-region parameter record (double[BC_NPARAM]); index names below. */
-#define BC_NPARAM 48
+#define BC_NPARAM 56
 #define BC_P_INVCM 0      /* 1 / membrane capacitance, cm^2/uF                 */
 #define BC_P_VREST 1      /* voltage used by reset (mV)                        */
 #define BC_P_ENA 2        /* fixed reversal potentials (mV)                    */
@@ -101,6 +103,14 @@ typedef int32_t bc_status;
 #define BC_P_KHH_PHI 41
 #define BC_P_KM_G 42
 #define BC_P_KM_PHI 43
+#define BC_P_KA1_G 44
+#define BC_P_KA1_VSH 45
+#define BC_P_KA1_PHIP 46
+#define BC_P_KA1_PHIQ 47
+#define BC_P_KA2_G 48
+#define BC_P_KA2_VSH 49
+#define BC_P_KA2_PHIP 50
+#define BC_P_KA2_PHIQ 51
 
 /* ------------------------------------------------------------------ batch spec */
 /*
@@ -305,7 +315,11 @@ bc_status bc_check(bc_plan_t plan, void* stream);
 #define BC_STATE_NAHH_Q 12
 #define BC_STATE_KHH_P 13
 #define BC_STATE_KM_N 14
-#define BC_NSTATE_VIEW 15
+#define BC_STATE_KA1_P 15
+#define BC_STATE_KA1_Q 16
+#define BC_STATE_KA2_P 17
+#define BC_STATE_KA2_Q 18
+#define BC_NSTATE_VIEW 19
 /* Current probes (mech/_point.py CurrentProbe, _multi_compartment/probes.py:184-258):
    probe_field = BC_PROBE_CURRENT + one of the codes below records that current
    density (uA/cm^2, outward negative as g (E - V)) after the step.             */
@@ -324,7 +338,9 @@ bc_status bc_check(bc_plan_t plan, void* stream);
 #define BC_CUR_ION_NA 11 /* sum over the sodium channels    */
 #define BC_CUR_ION_K 12  /* sum over the potassium channels */
 #define BC_CUR_ION_CA 13 /* sum over the calcium channels   */
-#define BC_NCUR 14
+#define BC_CUR_KA1 14    /* KA1_HM1992  */
+#define BC_CUR_KA2 15    /* KA2_HM1992  */
+#define BC_NCUR 16
 bc_status bc_state_download(bc_plan_t plan, int32_t which, double* out /* [n_cv] */, void* stream);
 bc_status bc_state_upload(bc_plan_t plan, int32_t which, const double* in /* [n_cv] */, void* stream);
 

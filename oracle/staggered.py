@@ -94,6 +94,10 @@ CHANNEL_DEFAULTS = {
     "K_TM1991": dict(g_max=10.0, temp=_c2k(36.0), q10=1.0, temp_ref=_c2k(36.0), V_sh=-60.0),  # potassium.py:317-321
     "CaHT_HM1992": dict(g_max=2.0, temp=_c2k(36.0), q10_p=3.55, temp_ref_p=_c2k(24.0), q10_q=3.0,
                         temp_ref_q=_c2k(24.0), V_sh=25.0),  # calcium.py:627-633
+    "KA1_HM1992": dict(g_max=30.0, temp=_c2k(36.0), q10_p=1.0, temp_ref_p=_c2k(36.0), q10_q=1.0,
+                       temp_ref_q=_c2k(36.0), V_sh=0.0),  # potassium.py:574-580
+    "KA2_HM1992": dict(g_max=20.0, temp=_c2k(36.0), q10_p=1.0, temp_ref_p=_c2k(36.0), q10_q=1.0,
+                       temp_ref_q=_c2k(36.0), V_sh=0.0),  # potassium.py:725-731
 }
 ION_DEFAULTS = {
     "SodiumFixed": dict(E=50.0),
@@ -348,6 +352,15 @@ def rates(name: str, V, p: dict, Ci=None):
             "q": ("it", 1.0 / (1.0 + np.exp((Vs + 83.0) / 4.0)),
                   np.where(Vs >= -80.0, np.exp(-(Vs + 22.0) / 10.5) + 28.0, np.exp((Vs + 467.0) / 66.6))),
         }
+    if name in ("KA1_HM1992", "KA2_HM1992"):  # potassium.py:592-611 and :743-762
+        Vs = V - p["V_sh"]
+        mid, slope = (60.0, 8.5) if name == "KA1_HM1992" else (36.0, 20.0)
+        return {
+            "p": ("it", 1.0 / (1.0 + np.exp(-(Vs + mid) / slope)),
+                  1.0 / (np.exp((Vs + 35.8) / 19.7) + np.exp(-(Vs + 79.7) / 12.7)) + 0.37),
+            "q": ("it", 1.0 / (1.0 + np.exp((Vs + 78.0) / 6.0)),
+                  np.where(Vs < -63.0, 1.0 / (np.exp((Vs + 46.0) / 5.0) + np.exp(-(Vs + 238.0) / 37.5)), 19.0)),
+        }
     if name == "KM_RI2021_SC":  # potassium.py:1735-1748
         a = 0.0033 * np.exp((V + 30.0) / 40.0)
         b = 0.0033 * np.exp((V + 30.0) / -20.0)
@@ -368,10 +381,12 @@ _GATES = {  # (gate, power, phi-key)
     "Na_TM1991": (("p", 3, "phi"), ("q", 1, "phi")),
     "K_TM1991": (("p", 4, "phi"),),
     "CaHT_HM1992": (("p", 2, "phi_p"), ("q", 1, "phi_q")),
+    "KA1_HM1992": (("p", 4, "phi_p"), ("q", 1, "phi_q")),
+    "KA2_HM1992": (("p", 4, "phi_p"), ("q", 1, "phi_q")),
 }
 _ION_OF = {"Na_Ba2002": "na", "KDR_Ba2002": "k", "CaL_IS2008": "ca", "CaT_HM1992": "ca",
            "K_Leak": "k", "AHP_De1994": "k", "Na_HH1952": "na", "K_HH1952": "k", "KM_RI2021_SC": "k",
-           "Na_TM1991": "na", "K_TM1991": "k", "CaHT_HM1992": "ca"}
+           "Na_TM1991": "na", "K_TM1991": "k", "CaHT_HM1992": "ca", "KA1_HM1992": "k", "KA2_HM1992": "k"}
 
 
 def _resolve(table: dict, decl) -> dict:
@@ -385,7 +400,7 @@ def _resolve(table: dict, decl) -> dict:
         p["phi"] = p["q10"] ** ((p["temp"] - p["temp_ref"]) / 10.0)
     elif name == "KM_RI2021_SC":  # Gate("n", q10=3.0, temp_ref=22 degC), potassium.py:1710
         p["phi"] = 3.0 ** ((p["temp"] - (273.15 + 22.0)) / 10.0)
-    elif name in ("CaL_IS2008", "CaT_HM1992", "CaHT_HM1992"):
+    elif name in ("CaL_IS2008", "CaT_HM1992", "CaHT_HM1992", "KA1_HM1992", "KA2_HM1992"):
         p["phi_p"] = p["q10_p"] ** ((p["temp"] - p["temp_ref_p"]) / 10.0)
         p["phi_q"] = p["q10_q"] ** ((p["temp"] - p["temp_ref_q"]) / 10.0)
     return p

@@ -248,3 +248,32 @@ def test_same_form_defaults_and_exclusion():
     for pair in (("Na_TM1991", "Na_Ba2002"), ("KDR_Ba2002", "K_TM1991"), ("CaT_HM1992", "CaHT_HM1992")):
         with pytest.raises(ValueError, match="same kernel"):
             catalogue.region_record([Channel(pair[0]), Channel(pair[1])], CableProperty())
+
+
+def test_a_current_rates():
+    # KA1_HM1992 / KA2_HM1992 (potassium.py:592-611, :743-762): activation midpoints
+    # -60 and -36 mV, the same inactivation in both classes, and tau_q applying the
+    # expression strictly below V' = -63 and 19 ms at and above it (the branches do
+    # not meet: about 23.4 ms just below, as the class docstring notes).
+    p1, p2 = dict(O.CHANNEL_DEFAULTS["KA1_HM1992"]), dict(O.CHANNEL_DEFAULTS["KA2_HM1992"])
+    assert O.rates("KA1_HM1992", np.array(-60.0), p1)["p"][1] == pytest.approx(0.5)
+    assert O.rates("KA2_HM1992", np.array(-36.0), p2)["p"][1] == pytest.approx(0.5)
+    V = np.linspace(-120.0, 40.0, 641)
+    a, b = O.rates("KA1_HM1992", V, p1), O.rates("KA2_HM1992", V, p2)
+    np.testing.assert_array_equal(a["q"][1], b["q"][1])
+    np.testing.assert_array_equal(a["q"][2], b["q"][2])
+    np.testing.assert_array_equal(a["p"][2], b["p"][2])
+    assert float(O.rates("KA1_HM1992", np.array(-63.0), p1)["q"][2]) == 19.0
+    below = float(O.rates("KA1_HM1992", np.array(-63.0 - 1e-9), p1)["q"][2])
+    assert below == pytest.approx(23.4, abs=0.05)
+
+
+def test_a_current_records():
+    from braincell_gb300 import _abi, catalogue
+    from braincell_gb300.mech import CableProperty, Channel
+
+    bits, rec = catalogue.region_record([Channel("KA1_HM1992"), Channel("KA2_HM1992", g_max=7.0, V_sh=2.0)],
+                                        CableProperty())
+    assert bits == _abi.BC_M_KA1 | _abi.BC_M_KA2
+    assert list(rec[_abi.BC_P_KA1_G:_abi.BC_P_KA1_PHIQ + 1]) == [30.0, 0.0, 1.0, 1.0]
+    assert list(rec[_abi.BC_P_KA2_G:_abi.BC_P_KA2_PHIQ + 1]) == [7.0, 2.0, 1.0, 1.0]
