@@ -23,6 +23,8 @@ Same-form classes: Na_TM1991 has Na_Ba2002's Traub-Miles rate functions written
 in terms of V_sh - V (sodium.py:275-289 against :154-170), K_TM1991 has
 KDR_Ba2002's (potassium.py:331-337 against :208-214), and CaHT_HM1992 has
 CaT_HM1992's (calcium.py:645-663 against :355-373); only their defaults differ.
+KM_MA2020_GoC and KM_MA2020_GrC (potassium.py:4419, :5182) repeat KM_RI2021_SC's
+rates, gate temperature factor and defaults.
 Each fills the parameter record and kernel slot of its same-form class, so a
 region cannot carry both classes of one pair.
 * ions: ``SodiumFixed`` E 50 (ion/sodium.py:149), ``PotassiumFixed`` E -95
@@ -70,6 +72,8 @@ CHANNELS: dict[str, dict[str, float]] = {
     "CaHT_HM1992": {
         "g_max": 2.0, "temp": T36, "q10_p": 3.55, "temp_ref_p": T24, "q10_q": 3.0, "temp_ref_q": T24, "V_sh": 25.0,
     },
+    "KM_MA2020_GoC": {"g_max": 0.25, "temp": T30},
+    "KM_MA2020_GrC": {"g_max": 0.25, "temp": T30},
     "KA1_HM1992": {
         "g_max": 30.0, "temp": T36, "q10_p": 1.0, "temp_ref_p": T36, "q10_q": 1.0, "temp_ref_q": T36, "V_sh": 0.0,
     },
@@ -78,7 +82,8 @@ CHANNELS: dict[str, dict[str, float]] = {
     },
 }
 # class -> the class whose kernel (rate functions, parameter slots, states) it uses
-SAME_FORM = {"Na_TM1991": "Na_Ba2002", "K_TM1991": "KDR_Ba2002", "CaHT_HM1992": "CaT_HM1992"}
+SAME_FORM = {"Na_TM1991": "Na_Ba2002", "K_TM1991": "KDR_Ba2002", "CaHT_HM1992": "CaT_HM1992",
+             "KM_MA2020_GoC": "KM_RI2021_SC", "KM_MA2020_GrC": "KM_RI2021_SC"}
 # gate temperature factors fixed by a class (not constructor parameters)
 KM_Q10, KM_TEMP_REF = 3.0, T22
 _ALIASES = {"leaky": "IL"}

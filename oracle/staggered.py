@@ -94,6 +94,8 @@ CHANNEL_DEFAULTS = {
     "K_TM1991": dict(g_max=10.0, temp=_c2k(36.0), q10=1.0, temp_ref=_c2k(36.0), V_sh=-60.0),  # potassium.py:317-321
     "CaHT_HM1992": dict(g_max=2.0, temp=_c2k(36.0), q10_p=3.55, temp_ref_p=_c2k(24.0), q10_q=3.0,
                         temp_ref_q=_c2k(24.0), V_sh=25.0),  # calcium.py:627-633
+    "KM_MA2020_GoC": dict(g_max=0.25, temp=_c2k(30.0)),  # potassium.py:4537-4538
+    "KM_MA2020_GrC": dict(g_max=0.25, temp=_c2k(30.0)),  # potassium.py:5301-5302
     "KA1_HM1992": dict(g_max=30.0, temp=_c2k(36.0), q10_p=1.0, temp_ref_p=_c2k(36.0), q10_q=1.0,
                        temp_ref_q=_c2k(36.0), V_sh=0.0),  # potassium.py:574-580
     "KA2_HM1992": dict(g_max=20.0, temp=_c2k(36.0), q10_p=1.0, temp_ref_p=_c2k(36.0), q10_q=1.0,
@@ -361,7 +363,7 @@ def rates(name: str, V, p: dict, Ci=None):
             "q": ("it", 1.0 / (1.0 + np.exp((Vs + 78.0) / 6.0)),
                   np.where(Vs < -63.0, 1.0 / (np.exp((Vs + 46.0) / 5.0) + np.exp(-(Vs + 238.0) / 37.5)), 19.0)),
         }
-    if name == "KM_RI2021_SC":  # potassium.py:1735-1748
+    if name in ("KM_RI2021_SC", "KM_MA2020_GoC", "KM_MA2020_GrC"):  # potassium.py:1735-1748, :4553-4567, :5317-5331
         a = 0.0033 * np.exp((V + 30.0) / 40.0)
         b = 0.0033 * np.exp((V + 30.0) / -20.0)
         return {"n": ("it", 1.0 / (1.0 + np.exp(-(V + 35.0) / 6.0)), 1.0 / (a + b))}
@@ -378,6 +380,8 @@ _GATES = {  # (gate, power, phi-key)
     "Na_HH1952": (("p", 3, "phi"), ("q", 1, "phi")),
     "K_HH1952": (("p", 4, "phi"),),
     "KM_RI2021_SC": (("n", 1, "phi"),),
+    "KM_MA2020_GoC": (("n", 1, "phi"),),
+    "KM_MA2020_GrC": (("n", 1, "phi"),),
     "Na_TM1991": (("p", 3, "phi"), ("q", 1, "phi")),
     "K_TM1991": (("p", 4, "phi"),),
     "CaHT_HM1992": (("p", 2, "phi_p"), ("q", 1, "phi_q")),
@@ -386,7 +390,8 @@ _GATES = {  # (gate, power, phi-key)
 }
 _ION_OF = {"Na_Ba2002": "na", "KDR_Ba2002": "k", "CaL_IS2008": "ca", "CaT_HM1992": "ca",
            "K_Leak": "k", "AHP_De1994": "k", "Na_HH1952": "na", "K_HH1952": "k", "KM_RI2021_SC": "k",
-           "Na_TM1991": "na", "K_TM1991": "k", "CaHT_HM1992": "ca", "KA1_HM1992": "k", "KA2_HM1992": "k"}
+           "Na_TM1991": "na", "K_TM1991": "k", "CaHT_HM1992": "ca", "KA1_HM1992": "k", "KA2_HM1992": "k",
+           "KM_MA2020_GoC": "k", "KM_MA2020_GrC": "k"}
 
 
 def _resolve(table: dict, decl) -> dict:
@@ -398,7 +403,8 @@ def _resolve(table: dict, decl) -> dict:
     name = decl.class_name
     if name in ("Na_Ba2002", "KDR_Ba2002", "HCN_HM1992", "Na_HH1952", "K_HH1952", "Na_TM1991", "K_TM1991"):
         p["phi"] = p["q10"] ** ((p["temp"] - p["temp_ref"]) / 10.0)
-    elif name == "KM_RI2021_SC":  # Gate("n", q10=3.0, temp_ref=22 degC), potassium.py:1710
+    elif name in ("KM_RI2021_SC", "KM_MA2020_GoC", "KM_MA2020_GrC"):
+        # Gate("n", q10=3.0, temp_ref=22 degC): potassium.py:1710, :4532, :5296
         p["phi"] = 3.0 ** ((p["temp"] - (273.15 + 22.0)) / 10.0)
     elif name in ("CaL_IS2008", "CaT_HM1992", "CaHT_HM1992", "KA1_HM1992", "KA2_HM1992"):
         p["phi_p"] = p["q10_p"] ** ((p["temp"] - p["temp_ref_p"]) / 10.0)

@@ -214,7 +214,8 @@ def test_km_rates_and_temperature_factor():
 
 
 @pytest.mark.parametrize("cls,kern", [("Na_TM1991", "Na_Ba2002"), ("K_TM1991", "KDR_Ba2002"),
-                                      ("CaHT_HM1992", "CaT_HM1992")])
+                                      ("CaHT_HM1992", "CaT_HM1992"), ("KM_MA2020_GoC", "KM_RI2021_SC"),
+                                      ("KM_MA2020_GrC", "KM_RI2021_SC")])
 def test_same_form_classes_match_their_kernel_class(cls, kern):
     # The TM1991 classes restate the Traub-Miles rates in terms of V_sh - V
     # (sodium.py:275-289, potassium.py:331-337) and CaHT_HM1992 repeats CaT_HM1992's
@@ -224,7 +225,10 @@ def test_same_form_classes_match_their_kernel_class(cls, kern):
 
     assert catalogue.kernel_class(cls) == kern
     p = dict(O.CHANNEL_DEFAULTS[cls])
-    q = dict(O.CHANNEL_DEFAULTS[kern], V_sh=p["V_sh"])
+    q = dict(O.CHANNEL_DEFAULTS[kern], **({"V_sh": p["V_sh"]} if "V_sh" in p else {}))
+    if "V_sh" not in p:  # no shift parameter: the defaults themselves agree
+        assert p == O.CHANNEL_DEFAULTS[kern]
+        p["V_sh"] = 0.0
     V = np.concatenate([np.linspace(-120.0, 60.0, 721), p["V_sh"] + np.array([13.0, 15.0, 40.0, -80.0])])
     a, b = O.rates(cls, V, p), O.rates(kern, V, q)
     assert a.keys() == b.keys()
