@@ -457,13 +457,10 @@ class SurrogateRunner:
     def run(self, n_steps: int, dt: float = 0.025) -> SurrogateRun:
         import torch
 
-        plan = self.plan
         if not hasattr(self, "_main"):
             # a non-blocking stream: the legacy default stream would order the
             # fallback streams' work behind the reduced launches
             self._main = torch.cuda.Stream(self.device)
-        main = self._main
-        sid = int(main.cuda_stream)
         torch.cuda.current_stream(self.device).synchronize()
         # The host loop below is on the critical path of the fallback (flag reads,
         # plan builds, launches): the cyclic garbage collector is paused for its
