@@ -19,6 +19,7 @@ conductance densities, uF/cm^2, ohm*cm, kelvin, mM.
 from __future__ import annotations
 
 import math
+import warnings
 from dataclasses import dataclass, field
 from typing import Sequence
 
@@ -93,10 +94,31 @@ class _Density:
         return f"{type(self).__name__}({self.class_name!r}, {self.params})"
 
 
+# The reference keeps the class names from before its rename (the new name with a
+# leading ``I``) as deprecated aliases that warn and resolve to the new class
+# (channel/__init__.py:49-86); a declaration under an old name resolves the same way.
+DEPRECATED_CHANNEL_NAMES = {
+    "INa_HH1952": "Na_HH1952", "INa_Ba2002": "Na_Ba2002", "INa_TM1991": "Na_TM1991", "IK_HH1952": "K_HH1952",
+    "IK_TM1991": "K_TM1991", "IK_Leak": "K_Leak", "IKDR_Ba2002": "KDR_Ba2002", "IKNI_Ya1989": "KNI_Ya1989",
+    "IKA1_HM1992": "KA1_HM1992", "IKA2_HM1992": "KA2_HM1992", "IKK2A_HM1992": "KK2A_HM1992",
+    "IKK2B_HM1992": "KK2B_HM1992", "ICaN_IS2008": "CaN_IS2008", "ICaL_IS2008": "CaL_IS2008",
+    "ICaT_HM1992": "CaT_HM1992", "ICaT_HP1992": "CaT_HP1992", "ICaHT_HM1992": "CaHT_HM1992",
+    "ICaHT_Re1993": "CaHT_Re1993", "IAHP_De1994": "AHP_De1994",
+}
+
+
 class Channel(_Density):
     """Distributed ion-channel declaration: ``Channel("Na_Ba2002", g_max=120.0)``."""
 
     category = "channel"
+
+    def __init__(self, class_name, *, name: str | None = None, **params) -> None:
+        if isinstance(class_name, str) and class_name in DEPRECATED_CHANNEL_NAMES:
+            new = DEPRECATED_CHANNEL_NAMES[class_name]
+            warnings.warn(f"{class_name} is deprecated and will be removed; use {new} instead.", DeprecationWarning,
+                          stacklevel=2)
+            class_name = new
+        super().__init__(class_name, name=name, **params)
 
 
 class Ion(_Density):

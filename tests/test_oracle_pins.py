@@ -281,3 +281,16 @@ def test_a_current_records():
     assert bits == _abi.BC_M_KA1 | _abi.BC_M_KA2
     assert list(rec[_abi.BC_P_KA1_G:_abi.BC_P_KA1_PHIQ + 1]) == [30.0, 0.0, 1.0, 1.0]
     assert list(rec[_abi.BC_P_KA2_G:_abi.BC_P_KA2_PHIQ + 1]) == [7.0, 2.0, 1.0, 1.0]
+
+
+def test_deprecated_channel_names_resolve():
+    # channel/__init__.py:49-86: the pre-rename names warn and give the renamed class
+    from braincell_gb300 import catalogue
+    from braincell_gb300.mech import CableProperty, Channel
+
+    with pytest.warns(DeprecationWarning, match="use KA1_HM1992"):
+        old = Channel("IKA1_HM1992", g_max=3.0)
+    assert old.class_name == "KA1_HM1992" and old.instance_name == "KA1_HM1992"
+    a = catalogue.region_record([old], CableProperty())
+    b = catalogue.region_record([Channel("KA1_HM1992", g_max=3.0)], CableProperty())
+    assert a[0] == b[0] and (a[1] == b[1]).all()
