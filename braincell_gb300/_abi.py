@@ -36,9 +36,11 @@ BC_M_KHH = 1 << 10
 BC_M_KM = 1 << 11
 BC_M_KA1 = 1 << 12
 BC_M_KA2 = 1 << 13
-BC_M_ALL = 0x3FFF
+BC_M_KK2A = 1 << 14
+BC_M_KK2B = 1 << 15
+BC_M_ALL = 0xFFFF
 
-BC_NPARAM = 56
+BC_NPARAM = 64
 BC_P_INVCM = 0
 BC_P_VREST = 1
 BC_P_ENA = 2
@@ -91,6 +93,14 @@ BC_P_KA2_G = 48
 BC_P_KA2_VSH = 49
 BC_P_KA2_PHIP = 50
 BC_P_KA2_PHIQ = 51
+BC_P_KK2A_G = 52
+BC_P_KK2A_VSH = 53
+BC_P_KK2A_PHIP = 54
+BC_P_KK2A_PHIQ = 55
+BC_P_KK2B_G = 56
+BC_P_KK2B_VSH = 57
+BC_P_KK2B_PHIP = 58
+BC_P_KK2B_PHIQ = 59
 
 BC_PREC_F32 = 0
 BC_PREC_F64 = 1
@@ -116,7 +126,9 @@ BC_CUR_ION_K = 12
 BC_CUR_ION_CA = 13
 BC_CUR_KA1 = 14
 BC_CUR_KA2 = 15
-BC_NCUR = 16
+BC_CUR_KK2A = 16
+BC_CUR_KK2B = 17
+BC_NCUR = 18
 
 BC_STATE_V = 0
 BC_STATE_NA_P = 1
@@ -137,7 +149,11 @@ BC_STATE_KA1_P = 15
 BC_STATE_KA1_Q = 16
 BC_STATE_KA2_P = 17
 BC_STATE_KA2_Q = 18
-BC_NSTATE_VIEW = 19
+BC_STATE_KK2A_P = 19
+BC_STATE_KK2A_Q = 20
+BC_STATE_KK2B_P = 21
+BC_STATE_KK2B_Q = 22
+BC_NSTATE_VIEW = 23
 BC_NOALLOC_MAX_CV = 262144
 
 STATE_NAMES = {
@@ -160,6 +176,10 @@ STATE_NAMES = {
     "KA1_q": BC_STATE_KA1_Q,
     "KA2_p": BC_STATE_KA2_P,
     "KA2_q": BC_STATE_KA2_Q,
+    "KK2A_p": BC_STATE_KK2A_P,
+    "KK2A_q": BC_STATE_KK2A_Q,
+    "KK2B_p": BC_STATE_KK2B_P,
+    "KK2B_q": BC_STATE_KK2B_Q,
 }
 
 _p = C.POINTER

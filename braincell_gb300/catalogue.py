@@ -18,6 +18,8 @@ Every class name, parameter name and default below is the reference's:
 * ``CaHT_HM1992`` -- channel/calcium.py:511 (g_max 2, q10_p 3.55, q10_q 3, temp_ref 24 degC, V_sh 25)
 * ``KA1_HM1992``  -- channel/potassium.py:460 (g_max 30, q10_p = q10_q = 1, temp = temp_refs = 36 degC, V_sh 0)
 * ``KA2_HM1992``  -- channel/potassium.py:614 (g_max 20, otherwise as KA1_HM1992)
+* ``KK2A_HM1992`` -- channel/potassium.py:765 (g_max 10, q10_p = q10_q = 1, temp = temp_refs = 36 degC, V_sh 0)
+* ``KK2B_HM1992`` -- channel/potassium.py:899 (as KK2A_HM1992)
 
 Same-form classes: Na_TM1991 has Na_Ba2002's Traub-Miles rate functions written
 in terms of V_sh - V (sodium.py:275-289 against :154-170), K_TM1991 has
@@ -80,6 +82,12 @@ CHANNELS: dict[str, dict[str, float]] = {
     "KA2_HM1992": {
         "g_max": 20.0, "temp": T36, "q10_p": 1.0, "temp_ref_p": T36, "q10_q": 1.0, "temp_ref_q": T36, "V_sh": 0.0,
     },
+    "KK2A_HM1992": {
+        "g_max": 10.0, "temp": T36, "q10_p": 1.0, "temp_ref_p": T36, "q10_q": 1.0, "temp_ref_q": T36, "V_sh": 0.0,
+    },
+    "KK2B_HM1992": {
+        "g_max": 10.0, "temp": T36, "q10_p": 1.0, "temp_ref_p": T36, "q10_q": 1.0, "temp_ref_q": T36, "V_sh": 0.0,
+    },
 }
 # class -> the class whose kernel (rate functions, parameter slots, states) it uses
 SAME_FORM = {"Na_TM1991": "Na_Ba2002", "K_TM1991": "KDR_Ba2002", "CaHT_HM1992": "CaT_HM1992",
@@ -95,6 +103,13 @@ IONS: dict[str, dict[str, float]] = {
     "CalciumDetailed": {
         "temp": T36, "d": 1.0, "tau": 5.0, "C_rest": 2.4e-4, "Co": 2.0, "Ci_initializer": 2.4e-4,
     },
+}
+
+
+# classes whose record is (g_max, V_sh, phi_p, phi_q) at a base index: mechanism bit, base
+_PQ_RECORDS = {
+    "KA1_HM1992": (_abi.BC_M_KA1, _abi.BC_P_KA1_G), "KA2_HM1992": (_abi.BC_M_KA2, _abi.BC_P_KA2_G),
+    "KK2A_HM1992": (_abi.BC_M_KK2A, _abi.BC_P_KK2A_G), "KK2B_HM1992": (_abi.BC_M_KK2B, _abi.BC_P_KK2B_G),
 }
 
 
@@ -209,10 +224,9 @@ def region_record(mechs, cable: CableProperty) -> tuple[int, np.ndarray]:
             bits |= _abi.BC_M_KM
             rec[_abi.BC_P_KM_G] = p["g_max"]
             rec[_abi.BC_P_KM_PHI] = q10_phi(KM_Q10, p["temp"], KM_TEMP_REF)
-        elif name in ("KA1_HM1992", "KA2_HM1992"):
-            one = name == "KA1_HM1992"
-            bits |= _abi.BC_M_KA1 if one else _abi.BC_M_KA2
-            base = _abi.BC_P_KA1_G if one else _abi.BC_P_KA2_G
+        elif name in _PQ_RECORDS:
+            bit, base = _PQ_RECORDS[name]
+            bits |= bit
             rec[base], rec[base + 1] = p["g_max"], p["V_sh"]
             rec[base + 2] = q10_phi(p["q10_p"], p["temp"], p["temp_ref_p"])
             rec[base + 3] = q10_phi(p["q10_q"], p["temp"], p["temp_ref_q"])

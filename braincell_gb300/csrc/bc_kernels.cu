@@ -286,6 +286,10 @@ __device__ __forceinline__ double probe_current(const Real* st, int N, const Rea
         const Real p2 = st[kSlotKA2P * N] * st[kSlotKA2P * N];
         return P[BC_P_KA2_G] * p2 * p2 * st[kSlotKA2Q * N] * (P[BC_P_EK] - v);
       }
+      case BC_CUR_KK2A:
+        return (m & BC_M_KK2A) ? P[BC_P_KK2A_G] * st[kSlotKK2AP * N] * st[kSlotKK2AQ * N] * (P[BC_P_EK] - v) : Real(0);
+      case BC_CUR_KK2B:
+        return (m & BC_M_KK2B) ? P[BC_P_KK2B_G] * st[kSlotKK2BP * N] * st[kSlotKK2BQ * N] * (P[BC_P_EK] - v) : Real(0);
     }
     return Real(0);
   };
@@ -294,7 +298,8 @@ __device__ __forceinline__ double probe_current(const Real* st, int N, const Rea
       return double(cur(BC_CUR_NA)) + double(cur(BC_CUR_NAHH));
     case BC_CUR_ION_K:
       return double(cur(BC_CUR_KDR)) + double(cur(BC_CUR_KLEAK)) + double(cur(BC_CUR_AHP)) + double(cur(BC_CUR_KHH)) +
-             double(cur(BC_CUR_KM)) + double(cur(BC_CUR_KA1)) + double(cur(BC_CUR_KA2));
+             double(cur(BC_CUR_KM)) + double(cur(BC_CUR_KA1)) + double(cur(BC_CUR_KA2)) + double(cur(BC_CUR_KK2A)) +
+             double(cur(BC_CUR_KK2B));
     case BC_CUR_ION_CA:
       return double(cur(BC_CUR_CAL)) + double(cur(BC_CUR_CAT));
     default:
@@ -303,9 +308,10 @@ __device__ __forceinline__ double probe_current(const Real* st, int N, const Rea
 }
 
 // Channels outside the main workloads' mix (classic Hodgkin-Huxley Na / K, the
-// M current, the A current): kept out of line so that their registers do not
-// weigh on the common path; same exp-Euler steps and ohmic currents as the others.
-constexpr uint32_t kExtraChannels = BC_M_NAHH | BC_M_KHH | BC_M_KM | BC_M_KA1 | BC_M_KA2;
+// M current, the A current, the slow K2 current): kept out of line so that their
+// registers do not weigh on the common path; same exp-Euler steps and ohmic
+// currents as the others.
+constexpr uint32_t kExtraChannels = BC_M_NAHH | BC_M_KHH | BC_M_KM | BC_M_KA1 | BC_M_KA2 | BC_M_KK2A | BC_M_KK2B;
 
 // One A-current mechanism (p^4 q, E_K) in slots (sp, sq) with parameters from pg.
 template <typename Real>
@@ -321,6 +327,23 @@ __device__ __forceinline__ void a_current(Real* st, int N, const Real* P, int sp
   }
   const Real p2 = p * p;
   const Real g = P[pg] * p2 * p2 * q;
+  G += g;
+  I += g * (P[BC_P_EK] - v);
+}
+
+// One slow K2 mechanism (p q, E_K) in slots (sp, sq) with parameters from pg.
+template <typename Real>
+__device__ __forceinline__ void k2_current(Real* st, int N, const Real* P, int sp, int sq, int pg, bool b_form, Real v,
+                                           Real dt, bool advance, Real& G, Real& I) {
+  Real p = st[sp * N], q = st[sq * N];
+  if (advance) {
+    const K2Rates<Real> r(v, P[pg + 1], b_form);
+    p = gate_it(p, r.pinf, r.ptau, P[pg + 2], dt);
+    q = gate_it(q, r.qinf, r.qtau, P[pg + 3], dt);
+    st[sp * N] = p;
+    st[sq * N] = q;
+  }
+  const Real g = P[pg] * p * q;
   G += g;
   I += g * (P[BC_P_EK] - v);
 }
@@ -369,6 +392,8 @@ __device__ __noinline__ void extra_channels(Real* st, int N, const Real* P, uint
     a_current(st, N, P, kSlotKA1P, kSlotKA1Q, BC_P_KA1_G, Real(kKA1Mid), Real(kKA1InvSlope), v, dt, advance, G, I);
   if (m & BC_M_KA2)
     a_current(st, N, P, kSlotKA2P, kSlotKA2Q, BC_P_KA2_G, Real(kKA2Mid), Real(kKA2InvSlope), v, dt, advance, G, I);
+  if (m & BC_M_KK2A) k2_current(st, N, P, kSlotKK2AP, kSlotKK2AQ, BC_P_KK2A_G, false, v, dt, advance, G, I);
+  if (m & BC_M_KK2B) k2_current(st, N, P, kSlotKK2BP, kSlotKK2BQ, BC_P_KK2B_G, true, v, dt, advance, G, I);
 }
 
 // One node's mechanisms.  `st` points at the node's slot-0 state (stride N).
@@ -553,6 +578,16 @@ __device__ __forceinline__ void steady_states(const Real* P, uint32_t m, Real* s
     const KARates<Real> r(v, P[BC_P_KA2_VSH], Real(kKA2Mid), Real(kKA2InvSlope));
     st[kSlotKA2P * N] = r.pinf;
     st[kSlotKA2Q * N] = r.qinf;
+  }
+  if (m & BC_M_KK2A) {
+    const K2Rates<Real> r(v, P[BC_P_KK2A_VSH], false);
+    st[kSlotKK2AP * N] = r.pinf;
+    st[kSlotKK2AQ * N] = r.qinf;
+  }
+  if (m & BC_M_KK2B) {
+    const K2Rates<Real> r(v, P[BC_P_KK2B_VSH], true);
+    st[kSlotKK2BP * N] = r.pinf;
+    st[kSlotKK2BQ * N] = r.qinf;
   }
 }
 

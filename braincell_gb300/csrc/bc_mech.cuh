@@ -13,6 +13,7 @@
 //   K_HH1952         channel/potassium.py:450-456
 //   KM_RI2021_SC     channel/potassium.py:1735-1748
 //   KA1_HM1992       channel/potassium.py:592-611, KA2_HM1992 :743-762
+//   KK2A_HM1992      channel/potassium.py:881-895, KK2B_HM1992 :1023-1041
 //   CalciumDetailed  ion/calcium.py:499-505, Nernst E: ion/_base.py:463-469
 // CUDA's own exp / expm1 / log are called; nothing of the math library is
 // re-implemented here.
@@ -191,6 +192,22 @@ struct KARates {
                : Real(19);
   }
 };
+// KK2A_HM1992 / KK2B_HM1992 (slow I_K2): the same activation and inactivation
+// curves; tau_q is 120 ms + a bell for KK2A, and for KK2B the bell strictly below
+// V' = -70 and 8.9 ms at and above it.
+template <typename Real>
+struct K2Rates {
+  Real pinf, ptau, qinf, qtau;
+  __device__ __forceinline__ K2Rates(Real v, Real vsh, bool b_form) {
+    const Real vp = v - vsh;
+    pinf = rdiv(Real(1), Real(1) + rexp(-(vp + Real(43)) * Real(1.0 / 17)));
+    ptau = rdiv(Real(1), rexp((vp - Real(81)) * Real(1.0 / 25.6)) + rexp(-(vp + Real(132)) * Real(1.0 / 18))) +
+           Real(9.9);
+    qinf = rdiv(Real(1), Real(1) + rexp((vp + Real(58)) * Real(1.0 / 10.6)));
+    const Real bell = rdiv(Real(1), rexp((vp - Real(1329)) * Real(0.005)) + rexp(-(vp + Real(130)) * Real(1.0 / 7.1)));
+    qtau = b_form ? (vp < Real(-70) ? bell : Real(8.9)) : bell + Real(120);
+  }
+};
 constexpr double kKA1Mid = 60.0, kKA1InvSlope = 1.0 / 8.5;
 constexpr double kKA2Mid = 36.0, kKA2InvSlope = 1.0 / 20.0;
 
@@ -214,7 +231,11 @@ constexpr int kSlotKA1P = 15;
 constexpr int kSlotKA1Q = 16;
 constexpr int kSlotKA2P = 17;
 constexpr int kSlotKA2Q = 18;
-constexpr int kNumSlots = 19;
+constexpr int kSlotKK2AP = 19;
+constexpr int kSlotKK2AQ = 20;
+constexpr int kSlotKK2BP = 21;
+constexpr int kSlotKK2BQ = 22;
+constexpr int kNumSlots = 23;
 
 constexpr double kFaraday = 96485.33212;   // C/mol
 constexpr double kGasR = 8.314462618;      // J/(mol K)

@@ -1140,7 +1140,8 @@ bc_status bc_plan_create(const bc_batch_spec* spec, const bc_plan_options* opts_
   p->cell_ncv.resize(s.n_cells);
   for (int64_t c = 0; c < s.n_cells; ++c) p->cell_ncv[c] = cells[c].n_cv;
   for (int64_t k = 0; k < s.n_cells * s.n_regions; ++k)
-    p->extra = p->extra || (s.region_mech[k] & (BC_M_NAHH | BC_M_KHH | BC_M_KM | BC_M_KA1 | BC_M_KA2)) != 0;
+    p->extra = p->extra || (s.region_mech[k] & (BC_M_NAHH | BC_M_KHH | BC_M_KM | BC_M_KA1 | BC_M_KA2 | BC_M_KK2A |
+                                                 BC_M_KK2B)) != 0;
   for (int64_t k = 0; k < s.n_cells * s.n_regions; ++k)
     if (s.region_mech[k] & ~BC_M_ALL) {
       delete p;
@@ -1191,8 +1192,8 @@ bc_status bc_plan_create(const bc_batch_spec* spec, const bc_plan_options* opts_
       static const uint32_t cur_owner[BC_NCUR] = {
           BC_M_IL,  BC_M_KLEAK, BC_M_NA,   BC_M_KDR, BC_M_CAL,           BC_M_CAT,
           BC_M_HCN, BC_M_AHP,   BC_M_NAHH, BC_M_KHH, BC_M_KM,            BC_M_NA | BC_M_NAHH,
-          BC_M_KDR | BC_M_KLEAK | BC_M_AHP | BC_M_KHH | BC_M_KM | BC_M_KA1 | BC_M_KA2,
-          BC_M_CAL | BC_M_CAT,  BC_M_KA1,  BC_M_KA2};
+          BC_M_KDR | BC_M_KLEAK | BC_M_AHP | BC_M_KHH | BC_M_KM | BC_M_KA1 | BC_M_KA2 | BC_M_KK2A | BC_M_KK2B,
+          BC_M_CAL | BC_M_CAT,  BC_M_KA1,  BC_M_KA2, BC_M_KK2A, BC_M_KK2B};
       const int32_t rg = cells[c].region[v];
       if (rg < 0 || !(s.region_mech[c * s.n_regions + rg] & cur_owner[field - BC_PROBE_CURRENT])) {
         delete p;
@@ -1203,7 +1204,8 @@ bc_status bc_plan_create(const bc_batch_spec* spec, const bc_plan_options* opts_
       static const uint32_t owner[BC_NSTATE_VIEW] = {0,          BC_M_NA,    BC_M_NA,    BC_M_KDR,   BC_M_CAL,
                                                      BC_M_CAL,   BC_M_CAT,   BC_M_CAT,   BC_M_HCN,   BC_M_AHP,
                                                      BC_M_CADET, BC_M_NAHH,  BC_M_NAHH,  BC_M_KHH,   BC_M_KM,
-                                                     BC_M_KA1,   BC_M_KA1,   BC_M_KA2,   BC_M_KA2};
+                                                     BC_M_KA1,   BC_M_KA1,   BC_M_KA2,   BC_M_KA2,
+                                                     BC_M_KK2A,  BC_M_KK2A,  BC_M_KK2B,  BC_M_KK2B};
       const int32_t rg = cells[c].region[v];
       if (rg < 0 || !(s.region_mech[c * s.n_regions + rg] & owner[field])) {
         delete p;
@@ -1946,6 +1948,10 @@ static bc_status view_offsets(bc_plan* p, int32_t which, std::vector<int64_t>& h
       case BC_STATE_KA1_Q: slot = (m & BC_M_KA1) ? kSlotKA1Q : -1; break;
       case BC_STATE_KA2_P: slot = (m & BC_M_KA2) ? kSlotKA2P : -1; break;
       case BC_STATE_KA2_Q: slot = (m & BC_M_KA2) ? kSlotKA2Q : -1; break;
+      case BC_STATE_KK2A_P: slot = (m & BC_M_KK2A) ? kSlotKK2AP : -1; break;
+      case BC_STATE_KK2A_Q: slot = (m & BC_M_KK2A) ? kSlotKK2AQ : -1; break;
+      case BC_STATE_KK2B_P: slot = (m & BC_M_KK2B) ? kSlotKK2BP : -1; break;
+      case BC_STATE_KK2B_Q: slot = (m & BC_M_KK2B) ? kSlotKK2BQ : -1; break;
     }
     if (slot < 0) continue;
     // states live in the separate state array: offsets are tagged by +state_tag
@@ -2032,11 +2038,13 @@ static void noalloc_offset(const bc_plan* p, int32_t which, int64_t k, int64_t* 
   static const uint32_t kBit[BC_NSTATE_VIEW] = {0,        BC_M_NA,    BC_M_NA,   BC_M_KDR,  BC_M_CAL,
                                                 BC_M_CAL, BC_M_CAT,   BC_M_CAT,  BC_M_HCN,  BC_M_AHP,
                                                 BC_M_CADET, BC_M_NAHH, BC_M_NAHH, BC_M_KHH, BC_M_KM,
-                                                BC_M_KA1,   BC_M_KA1,  BC_M_KA2,  BC_M_KA2};
+                                                BC_M_KA1,   BC_M_KA1,  BC_M_KA2,  BC_M_KA2,
+                                                BC_M_KK2A,  BC_M_KK2A, BC_M_KK2B, BC_M_KK2B};
   static const int kSlot[BC_NSTATE_VIEW] = {-1,        kSlotNaP,   kSlotNaQ,   kSlotKdrP,  kSlotCalP,
                                             kSlotCalQ, kSlotCatP,  kSlotCatQ,  kSlotHcnP,  kSlotAhpP,
                                             kSlotCaHi, kSlotNaHHP, kSlotNaHHQ, kSlotKHHP,  kSlotKMN,
-                                            kSlotKA1P, kSlotKA1Q,  kSlotKA2P,  kSlotKA2Q};
+                                            kSlotKA1P, kSlotKA1Q,  kSlotKA2P,  kSlotKA2Q,
+                                            kSlotKK2AP, kSlotKK2AQ, kSlotKK2BP, kSlotKK2BQ};
   if (!(p->cv_mech[k] & kBit[which])) return;
   *hi = kStateTag + (d.state_offset + int64_t(kSlot[which]) * d.n_nodes + j) * rs;
   if (which == BC_STATE_CA_CI) *lo = kStateTag + (d.state_offset + int64_t(kSlotCaLo) * d.n_nodes + j) * rs;

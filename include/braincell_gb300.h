@@ -55,10 +55,12 @@ typedef int32_t bc_status;
 #define BC_M_KM (1u << 11)       /* channel/potassium.py:1597 KM_RI2021_SC n, E_K              */
 #define BC_M_KA1 (1u << 12)      /* channel/potassium.py:460  KA1_HM1992  p^4 q, E_K           */
 #define BC_M_KA2 (1u << 13)      /* channel/potassium.py:614  KA2_HM1992  p^4 q, E_K           */
-#define BC_M_ALL 0x3FFFu
+#define BC_M_KK2A (1u << 14)     /* channel/potassium.py:765  KK2A_HM1992 p q, E_K             */
+#define BC_M_KK2B (1u << 15)     /* channel/potassium.py:899  KK2B_HM1992 p q, E_K             */
+#define BC_M_ALL 0xFFFFu
 
 /* Per-region parameter record (double[BC_NPARAM]); index names below. */
-#define BC_NPARAM 56
+#define BC_NPARAM 64
 #define BC_P_INVCM 0      /* 1 / membrane capacitance, cm^2/uF                 */
 #define BC_P_VREST 1      /* voltage used by reset (mV)                        */
 #define BC_P_ENA 2        /* fixed reversal potentials (mV)                    */
@@ -111,6 +113,14 @@ typedef int32_t bc_status;
 #define BC_P_KA2_VSH 49
 #define BC_P_KA2_PHIP 50
 #define BC_P_KA2_PHIQ 51
+#define BC_P_KK2A_G 52
+#define BC_P_KK2A_VSH 53
+#define BC_P_KK2A_PHIP 54
+#define BC_P_KK2A_PHIQ 55
+#define BC_P_KK2B_G 56
+#define BC_P_KK2B_VSH 57
+#define BC_P_KK2B_PHIP 58
+#define BC_P_KK2B_PHIQ 59
 
 /* ------------------------------------------------------------------ batch spec */
 /*
@@ -319,7 +329,11 @@ bc_status bc_check(bc_plan_t plan, void* stream);
 #define BC_STATE_KA1_Q 16
 #define BC_STATE_KA2_P 17
 #define BC_STATE_KA2_Q 18
-#define BC_NSTATE_VIEW 19
+#define BC_STATE_KK2A_P 19
+#define BC_STATE_KK2A_Q 20
+#define BC_STATE_KK2B_P 21
+#define BC_STATE_KK2B_Q 22
+#define BC_NSTATE_VIEW 23
 /* Current probes (mech/_point.py CurrentProbe, _multi_compartment/probes.py:184-258):
    probe_field = BC_PROBE_CURRENT + one of the codes below records that current
    density (uA/cm^2, outward negative as g (E - V)) after the step.             */
@@ -340,7 +354,9 @@ bc_status bc_check(bc_plan_t plan, void* stream);
 #define BC_CUR_ION_CA 13 /* sum over the calcium channels   */
 #define BC_CUR_KA1 14    /* KA1_HM1992  */
 #define BC_CUR_KA2 15    /* KA2_HM1992  */
-#define BC_NCUR 16
+#define BC_CUR_KK2A 16   /* KK2A_HM1992 */
+#define BC_CUR_KK2B 17   /* KK2B_HM1992 */
+#define BC_NCUR 18
 bc_status bc_state_download(bc_plan_t plan, int32_t which, double* out /* [n_cv] */, void* stream);
 bc_status bc_state_upload(bc_plan_t plan, int32_t which, const double* in /* [n_cv] */, void* stream);
 

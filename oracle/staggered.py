@@ -100,6 +100,10 @@ CHANNEL_DEFAULTS = {
                        temp_ref_q=_c2k(36.0), V_sh=0.0),  # potassium.py:574-580
     "KA2_HM1992": dict(g_max=20.0, temp=_c2k(36.0), q10_p=1.0, temp_ref_p=_c2k(36.0), q10_q=1.0,
                        temp_ref_q=_c2k(36.0), V_sh=0.0),  # potassium.py:725-731
+    "KK2A_HM1992": dict(g_max=10.0, temp=_c2k(36.0), q10_p=1.0, temp_ref_p=_c2k(36.0), q10_q=1.0,
+                        temp_ref_q=_c2k(36.0), V_sh=0.0),  # potassium.py:863-869
+    "KK2B_HM1992": dict(g_max=10.0, temp=_c2k(36.0), q10_p=1.0, temp_ref_p=_c2k(36.0), q10_q=1.0,
+                        temp_ref_q=_c2k(36.0), V_sh=0.0),  # potassium.py:1005-1011
 }
 ION_DEFAULTS = {
     "SodiumFixed": dict(E=50.0),
@@ -363,6 +367,15 @@ def rates(name: str, V, p: dict, Ci=None):
             "q": ("it", 1.0 / (1.0 + np.exp((Vs + 78.0) / 6.0)),
                   np.where(Vs < -63.0, 1.0 / (np.exp((Vs + 46.0) / 5.0) + np.exp(-(Vs + 238.0) / 37.5)), 19.0)),
         }
+    if name in ("KK2A_HM1992", "KK2B_HM1992"):  # potassium.py:881-895 and :1023-1041
+        Vs = V - p["V_sh"]
+        bell = 1.0 / (np.exp((Vs - 1329.0) / 200.0) + np.exp(-(Vs + 130.0) / 7.1))
+        qtau = bell + 120.0 if name == "KK2A_HM1992" else np.where(Vs < -70.0, bell, 8.9)
+        return {
+            "p": ("it", 1.0 / (1.0 + np.exp(-(Vs + 43.0) / 17.0)),
+                  1.0 / (np.exp((Vs - 81.0) / 25.6) + np.exp(-(Vs + 132.0) / 18.0)) + 9.9),
+            "q": ("it", 1.0 / (1.0 + np.exp((Vs + 58.0) / 10.6)), qtau),
+        }
     if name in ("KM_RI2021_SC", "KM_MA2020_GoC", "KM_MA2020_GrC"):  # potassium.py:1735-1748, :4553-4567, :5317-5331
         a = 0.0033 * np.exp((V + 30.0) / 40.0)
         b = 0.0033 * np.exp((V + 30.0) / -20.0)
@@ -387,11 +400,13 @@ _GATES = {  # (gate, power, phi-key)
     "CaHT_HM1992": (("p", 2, "phi_p"), ("q", 1, "phi_q")),
     "KA1_HM1992": (("p", 4, "phi_p"), ("q", 1, "phi_q")),
     "KA2_HM1992": (("p", 4, "phi_p"), ("q", 1, "phi_q")),
+    "KK2A_HM1992": (("p", 1, "phi_p"), ("q", 1, "phi_q")),
+    "KK2B_HM1992": (("p", 1, "phi_p"), ("q", 1, "phi_q")),
 }
 _ION_OF = {"Na_Ba2002": "na", "KDR_Ba2002": "k", "CaL_IS2008": "ca", "CaT_HM1992": "ca",
            "K_Leak": "k", "AHP_De1994": "k", "Na_HH1952": "na", "K_HH1952": "k", "KM_RI2021_SC": "k",
            "Na_TM1991": "na", "K_TM1991": "k", "CaHT_HM1992": "ca", "KA1_HM1992": "k", "KA2_HM1992": "k",
-           "KM_MA2020_GoC": "k", "KM_MA2020_GrC": "k"}
+           "KM_MA2020_GoC": "k", "KM_MA2020_GrC": "k", "KK2A_HM1992": "k", "KK2B_HM1992": "k"}
 
 
 def _resolve(table: dict, decl) -> dict:
@@ -406,7 +421,8 @@ def _resolve(table: dict, decl) -> dict:
     elif name in ("KM_RI2021_SC", "KM_MA2020_GoC", "KM_MA2020_GrC"):
         # Gate("n", q10=3.0, temp_ref=22 degC): potassium.py:1710, :4532, :5296
         p["phi"] = 3.0 ** ((p["temp"] - (273.15 + 22.0)) / 10.0)
-    elif name in ("CaL_IS2008", "CaT_HM1992", "CaHT_HM1992", "KA1_HM1992", "KA2_HM1992"):
+    elif name in ("CaL_IS2008", "CaT_HM1992", "CaHT_HM1992", "KA1_HM1992", "KA2_HM1992", "KK2A_HM1992",
+                  "KK2B_HM1992"):
         p["phi_p"] = p["q10_p"] ** ((p["temp"] - p["temp_ref_p"]) / 10.0)
         p["phi_q"] = p["q10_q"] ** ((p["temp"] - p["temp_ref_q"]) / 10.0)
     return p

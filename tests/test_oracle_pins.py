@@ -274,13 +274,18 @@ def test_a_current_rates():
 
 def test_a_current_records():
     from braincell_gb300 import _abi, catalogue
-    from braincell_gb300.mech import CableProperty, Channel
+    from braincell_gb300.mech import CableProperty, Channel, celsius2kelvin as T
 
     bits, rec = catalogue.region_record([Channel("KA1_HM1992"), Channel("KA2_HM1992", g_max=7.0, V_sh=2.0)],
                                         CableProperty())
     assert bits == _abi.BC_M_KA1 | _abi.BC_M_KA2
     assert list(rec[_abi.BC_P_KA1_G:_abi.BC_P_KA1_PHIQ + 1]) == [30.0, 0.0, 1.0, 1.0]
     assert list(rec[_abi.BC_P_KA2_G:_abi.BC_P_KA2_PHIQ + 1]) == [7.0, 2.0, 1.0, 1.0]
+    bits, rec = catalogue.region_record([Channel("KK2A_HM1992", temp=T(26.0)), Channel("KK2B_HM1992", g_max=4.0)],
+                                        CableProperty())
+    assert bits == _abi.BC_M_KK2A | _abi.BC_M_KK2B
+    assert list(rec[_abi.BC_P_KK2A_G:_abi.BC_P_KK2A_PHIQ + 1]) == [10.0, 0.0, 1.0, 1.0]  # q10 1: phi 1 at any temp
+    assert list(rec[_abi.BC_P_KK2B_G:_abi.BC_P_KK2B_PHIQ + 1]) == [4.0, 0.0, 1.0, 1.0]
 
 
 def test_deprecated_channel_names_resolve():
@@ -294,3 +299,21 @@ def test_deprecated_channel_names_resolve():
     a = catalogue.region_record([old], CableProperty())
     b = catalogue.region_record([Channel("KA1_HM1992", g_max=3.0)], CableProperty())
     assert a[0] == b[0] and (a[1] == b[1]).all()
+
+
+def test_slow_k2_rates():
+    # KK2A_HM1992 / KK2B_HM1992 (potassium.py:881-895, :1023-1041): the same
+    # activation and inactivation curves; KK2A's tau_q is 120 ms + a bell, KK2B's is
+    # the bell strictly below V' = -70 (about 885 ms just below, as its docstring
+    # notes) and 8.9 ms at and above.
+    pa, pb = dict(O.CHANNEL_DEFAULTS["KK2A_HM1992"]), dict(O.CHANNEL_DEFAULTS["KK2B_HM1992"])
+    V = np.linspace(-120.0, 40.0, 641)
+    a, b = O.rates("KK2A_HM1992", V, pa), O.rates("KK2B_HM1992", V, pb)
+    for k in (1, 2):
+        np.testing.assert_array_equal(a["p"][k], b["p"][k])
+    np.testing.assert_array_equal(a["q"][1], b["q"][1])
+    assert float(O.rates("KK2B_HM1992", np.array(-70.0), pb)["q"][2]) == 8.9
+    below = float(O.rates("KK2B_HM1992", np.array(-70.0 - 1e-9), pb)["q"][2])
+    assert below == pytest.approx(885.0, rel=0.01)
+    assert float(O.rates("KK2A_HM1992", np.array(-70.0), pa)["q"][2]) == pytest.approx(below + 120.0, rel=1e-6)
+    assert O.rates("KK2A_HM1992", np.array(-43.0), pa)["p"][1] == pytest.approx(0.5)

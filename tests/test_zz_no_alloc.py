@@ -48,7 +48,7 @@ def _calcium_desc():
 
 def _hh_batch():
     # a cell with the classic Hodgkin-Huxley channels, the M current and both A-current
-    # components, so that every state view has values somewhere in the batch
+    # and slow K2 components, so that every state view has values somewhere in the batch
     from braincell_gb300 import Branch, Cell, Morphology
     from braincell_gb300.batch import lower_cell
     from braincell_gb300.mech import AllRegion, CableProperty, Channel, CVPerBranch, branch_in
@@ -59,7 +59,7 @@ def _hh_batch():
     c.paint(AllRegion(), CableProperty(), Channel("IL", g_max=0.3, E=-54.4))
     c.paint(branch_in("type", "soma"), Channel("Na_HH1952"), Channel("K_HH1952", g_max=36.0))
     c.paint(branch_in("type", "basal_dendrite"), Channel("KM_RI2021_SC"), Channel("KA1_HM1992", g_max=3.0),
-            Channel("KA2_HM1992", g_max=2.0))
+            Channel("KA2_HM1992", g_max=2.0), Channel("KK2A_HM1992", g_max=1.0), Channel("KK2B_HM1992", g_max=1.0))
     return lower_cell(c)
 
 
