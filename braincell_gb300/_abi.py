@@ -38,7 +38,8 @@ BC_M_KA1 = 1 << 12
 BC_M_KA2 = 1 << 13
 BC_M_KK2A = 1 << 14
 BC_M_KK2B = 1 << 15
-BC_M_ALL = 0xFFFF
+BC_M_KNI = 1 << 16
+BC_M_ALL = 0x1FFFF
 
 BC_NPARAM = 64
 BC_P_INVCM = 0
@@ -101,6 +102,10 @@ BC_P_KK2B_G = 56
 BC_P_KK2B_VSH = 57
 BC_P_KK2B_PHIP = 58
 BC_P_KK2B_PHIQ = 59
+BC_P_KNI_G = 60
+BC_P_KNI_VSH = 61
+BC_P_KNI_PHI = 62
+BC_P_KNI_TAUMAX = 63
 
 BC_PREC_F32 = 0
 BC_PREC_F64 = 1
@@ -128,7 +133,8 @@ BC_CUR_KA1 = 14
 BC_CUR_KA2 = 15
 BC_CUR_KK2A = 16
 BC_CUR_KK2B = 17
-BC_NCUR = 18
+BC_CUR_KNI = 18
+BC_NCUR = 19
 
 BC_STATE_V = 0
 BC_STATE_NA_P = 1
@@ -153,7 +159,8 @@ BC_STATE_KK2A_P = 19
 BC_STATE_KK2A_Q = 20
 BC_STATE_KK2B_P = 21
 BC_STATE_KK2B_Q = 22
-BC_NSTATE_VIEW = 23
+BC_STATE_KNI_P = 23
+BC_NSTATE_VIEW = 24
 BC_NOALLOC_MAX_CV = 262144
 
 STATE_NAMES = {
@@ -180,6 +187,7 @@ STATE_NAMES = {
     "KK2A_q": BC_STATE_KK2A_Q,
     "KK2B_p": BC_STATE_KK2B_P,
     "KK2B_q": BC_STATE_KK2B_Q,
+    "KNI_p": BC_STATE_KNI_P,
 }
 
 _p = C.POINTER

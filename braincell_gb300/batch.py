@@ -340,6 +340,7 @@ PROBE_STATES = {
     ("KA2_HM1992", "p"): _abi.BC_STATE_KA2_P, ("KA2_HM1992", "q"): _abi.BC_STATE_KA2_Q,
     ("KK2A_HM1992", "p"): _abi.BC_STATE_KK2A_P, ("KK2A_HM1992", "q"): _abi.BC_STATE_KK2A_Q,
     ("KK2B_HM1992", "p"): _abi.BC_STATE_KK2B_P, ("KK2B_HM1992", "q"): _abi.BC_STATE_KK2B_Q,
+    ("KNI_Ya1989", "p"): _abi.BC_STATE_KNI_P,
 }
 
 
@@ -349,7 +350,7 @@ PROBE_CURRENTS = {
     "CaL_IS2008": _abi.BC_CUR_CAL, "CaT_HM1992": _abi.BC_CUR_CAT, "HCN_HM1992": _abi.BC_CUR_HCN,
     "AHP_De1994": _abi.BC_CUR_AHP, "Na_HH1952": _abi.BC_CUR_NAHH, "K_HH1952": _abi.BC_CUR_KHH,
     "KM_RI2021_SC": _abi.BC_CUR_KM, "KA1_HM1992": _abi.BC_CUR_KA1, "KA2_HM1992": _abi.BC_CUR_KA2,
-    "KK2A_HM1992": _abi.BC_CUR_KK2A, "KK2B_HM1992": _abi.BC_CUR_KK2B,
+    "KK2A_HM1992": _abi.BC_CUR_KK2A, "KK2B_HM1992": _abi.BC_CUR_KK2B, "KNI_Ya1989": _abi.BC_CUR_KNI,
 }
 ION_CURRENTS = {"na": _abi.BC_CUR_ION_NA, "k": _abi.BC_CUR_ION_K, "ca": _abi.BC_CUR_ION_CA}
 

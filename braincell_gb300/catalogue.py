@@ -20,6 +20,7 @@ Every class name, parameter name and default below is the reference's:
 * ``KA2_HM1992``  -- channel/potassium.py:614 (g_max 20, otherwise as KA1_HM1992)
 * ``KK2A_HM1992`` -- channel/potassium.py:765 (g_max 10, q10_p = q10_q = 1, temp = temp_refs = 36 degC, V_sh 0)
 * ``KK2B_HM1992`` -- channel/potassium.py:899 (as KK2A_HM1992)
+* ``KNI_Ya1989``  -- channel/potassium.py:1045 (g_max 0.004, q10 1, temp = temp_ref = 36 degC, tau_max 4 s, V_sh 0)
 
 Same-form classes: Na_TM1991 has Na_Ba2002's Traub-Miles rate functions written
 in terms of V_sh - V (sodium.py:275-289 against :154-170), K_TM1991 has
@@ -88,6 +89,7 @@ CHANNELS: dict[str, dict[str, float]] = {
     "KK2B_HM1992": {
         "g_max": 10.0, "temp": T36, "q10_p": 1.0, "temp_ref_p": T36, "q10_q": 1.0, "temp_ref_q": T36, "V_sh": 0.0,
     },
+    "KNI_Ya1989": {"g_max": 0.004, "temp": T36, "q10": 1.0, "temp_ref": T36, "tau_max": 4e3, "V_sh": 0.0},
 }
 # class -> the class whose kernel (rate functions, parameter slots, states) it uses
 SAME_FORM = {"Na_TM1991": "Na_Ba2002", "K_TM1991": "KDR_Ba2002", "CaHT_HM1992": "CaT_HM1992",
@@ -224,6 +226,11 @@ def region_record(mechs, cable: CableProperty) -> tuple[int, np.ndarray]:
             bits |= _abi.BC_M_KM
             rec[_abi.BC_P_KM_G] = p["g_max"]
             rec[_abi.BC_P_KM_PHI] = q10_phi(KM_Q10, p["temp"], KM_TEMP_REF)
+        elif name == "KNI_Ya1989":
+            bits |= _abi.BC_M_KNI
+            rec[_abi.BC_P_KNI_G], rec[_abi.BC_P_KNI_VSH] = p["g_max"], p["V_sh"]
+            rec[_abi.BC_P_KNI_PHI] = q10_phi(p["q10"], p["temp"], p["temp_ref"])
+            rec[_abi.BC_P_KNI_TAUMAX] = p["tau_max"]
         elif name in _PQ_RECORDS:
             bit, base = _PQ_RECORDS[name]
             bits |= bit

@@ -290,6 +290,8 @@ __device__ __forceinline__ double probe_current(const Real* st, int N, const Rea
         return (m & BC_M_KK2A) ? P[BC_P_KK2A_G] * st[kSlotKK2AP * N] * st[kSlotKK2AQ * N] * (P[BC_P_EK] - v) : Real(0);
       case BC_CUR_KK2B:
         return (m & BC_M_KK2B) ? P[BC_P_KK2B_G] * st[kSlotKK2BP * N] * st[kSlotKK2BQ * N] * (P[BC_P_EK] - v) : Real(0);
+      case BC_CUR_KNI:
+        return (m & BC_M_KNI) ? P[BC_P_KNI_G] * st[kSlotKNIP * N] * (P[BC_P_EK] - v) : Real(0);
     }
     return Real(0);
   };
@@ -299,7 +301,7 @@ __device__ __forceinline__ double probe_current(const Real* st, int N, const Rea
     case BC_CUR_ION_K:
       return double(cur(BC_CUR_KDR)) + double(cur(BC_CUR_KLEAK)) + double(cur(BC_CUR_AHP)) + double(cur(BC_CUR_KHH)) +
              double(cur(BC_CUR_KM)) + double(cur(BC_CUR_KA1)) + double(cur(BC_CUR_KA2)) + double(cur(BC_CUR_KK2A)) +
-             double(cur(BC_CUR_KK2B));
+             double(cur(BC_CUR_KK2B)) + double(cur(BC_CUR_KNI));
     case BC_CUR_ION_CA:
       return double(cur(BC_CUR_CAL)) + double(cur(BC_CUR_CAT));
     default:
@@ -308,10 +310,11 @@ __device__ __forceinline__ double probe_current(const Real* st, int N, const Rea
 }
 
 // Channels outside the main workloads' mix (classic Hodgkin-Huxley Na / K, the
-// M current, the A current, the slow K2 current): kept out of line so that their
-// registers do not weigh on the common path; same exp-Euler steps and ohmic
-// currents as the others.
-constexpr uint32_t kExtraChannels = BC_M_NAHH | BC_M_KHH | BC_M_KM | BC_M_KA1 | BC_M_KA2 | BC_M_KK2A | BC_M_KK2B;
+// M current, the A current, the slow K2 current, the slow non-inactivating K
+// current): kept out of line so that their registers do not weigh on the common
+// path; same exp-Euler steps and ohmic currents as the others.
+constexpr uint32_t kExtraChannels =
+    BC_M_NAHH | BC_M_KHH | BC_M_KM | BC_M_KA1 | BC_M_KA2 | BC_M_KK2A | BC_M_KK2B | BC_M_KNI;
 
 // One A-current mechanism (p^4 q, E_K) in slots (sp, sq) with parameters from pg.
 template <typename Real>
@@ -394,6 +397,17 @@ __device__ __noinline__ void extra_channels(Real* st, int N, const Real* P, uint
     a_current(st, N, P, kSlotKA2P, kSlotKA2Q, BC_P_KA2_G, Real(kKA2Mid), Real(kKA2InvSlope), v, dt, advance, G, I);
   if (m & BC_M_KK2A) k2_current(st, N, P, kSlotKK2AP, kSlotKK2AQ, BC_P_KK2A_G, false, v, dt, advance, G, I);
   if (m & BC_M_KK2B) k2_current(st, N, P, kSlotKK2BP, kSlotKK2BQ, BC_P_KK2B_G, true, v, dt, advance, G, I);
+  if (m & BC_M_KNI) {
+    Real p = st[kSlotKNIP * N];
+    if (advance) {
+      const KNIRates<Real> r(v, P[BC_P_KNI_VSH], P[BC_P_KNI_TAUMAX]);
+      p = gate_it(p, r.pinf, r.ptau, P[BC_P_KNI_PHI], dt);
+      st[kSlotKNIP * N] = p;
+    }
+    const Real g = P[BC_P_KNI_G] * p;
+    G += g;
+    I += g * (P[BC_P_EK] - v);
+  }
 }
 
 // One node's mechanisms.  `st` points at the node's slot-0 state (stride N).
@@ -589,6 +603,7 @@ __device__ __forceinline__ void steady_states(const Real* P, uint32_t m, Real* s
     st[kSlotKK2BP * N] = r.pinf;
     st[kSlotKK2BQ * N] = r.qinf;
   }
+  if (m & BC_M_KNI) st[kSlotKNIP * N] = KNIRates<Real>(v, P[BC_P_KNI_VSH], P[BC_P_KNI_TAUMAX]).pinf;
 }
 
 // Row i of the next linear system: diag = 1 + dt (D + G / cm), rhs = dt I / cm

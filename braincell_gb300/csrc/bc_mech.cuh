@@ -14,6 +14,7 @@
 //   KM_RI2021_SC     channel/potassium.py:1735-1748
 //   KA1_HM1992       channel/potassium.py:592-611, KA2_HM1992 :743-762
 //   KK2A_HM1992      channel/potassium.py:881-895, KK2B_HM1992 :1023-1041
+//   KNI_Ya1989       channel/potassium.py:1156-1163
 //   CalciumDetailed  ion/calcium.py:499-505, Nernst E: ion/_base.py:463-469
 // CUDA's own exp / expm1 / log are called; nothing of the math library is
 // re-implemented here.
@@ -208,6 +209,16 @@ struct K2Rates {
     qtau = b_form ? (vp < Real(-70) ? bell : Real(8.9)) : bell + Real(120);
   }
 };
+// KNI_Ya1989 (slow non-inactivating K): V' = V - V_sh, tau_max a parameter (ms).
+template <typename Real>
+struct KNIRates {
+  Real pinf, ptau;
+  __device__ __forceinline__ KNIRates(Real v, Real vsh, Real tau_max) {
+    const Real x = v - vsh + Real(35);
+    pinf = rdiv(Real(1), Real(1) + rexp(-x * Real(0.1)));
+    ptau = rdiv(tau_max, Real(3.3) * rexp(x * Real(0.05)) + rexp(-x * Real(0.05)));
+  }
+};
 constexpr double kKA1Mid = 60.0, kKA1InvSlope = 1.0 / 8.5;
 constexpr double kKA2Mid = 36.0, kKA2InvSlope = 1.0 / 20.0;
 
@@ -235,7 +246,8 @@ constexpr int kSlotKK2AP = 19;
 constexpr int kSlotKK2AQ = 20;
 constexpr int kSlotKK2BP = 21;
 constexpr int kSlotKK2BQ = 22;
-constexpr int kNumSlots = 23;
+constexpr int kSlotKNIP = 23;
+constexpr int kNumSlots = 24;
 
 constexpr double kFaraday = 96485.33212;   // C/mol
 constexpr double kGasR = 8.314462618;      // J/(mol K)

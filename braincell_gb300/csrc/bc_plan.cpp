@@ -1141,7 +1141,7 @@ bc_status bc_plan_create(const bc_batch_spec* spec, const bc_plan_options* opts_
   for (int64_t c = 0; c < s.n_cells; ++c) p->cell_ncv[c] = cells[c].n_cv;
   for (int64_t k = 0; k < s.n_cells * s.n_regions; ++k)
     p->extra = p->extra || (s.region_mech[k] & (BC_M_NAHH | BC_M_KHH | BC_M_KM | BC_M_KA1 | BC_M_KA2 | BC_M_KK2A |
-                                                 BC_M_KK2B)) != 0;
+                                                 BC_M_KK2B | BC_M_KNI)) != 0;
   for (int64_t k = 0; k < s.n_cells * s.n_regions; ++k)
     if (s.region_mech[k] & ~BC_M_ALL) {
       delete p;
@@ -1192,8 +1192,8 @@ bc_status bc_plan_create(const bc_batch_spec* spec, const bc_plan_options* opts_
       static const uint32_t cur_owner[BC_NCUR] = {
           BC_M_IL,  BC_M_KLEAK, BC_M_NA,   BC_M_KDR, BC_M_CAL,           BC_M_CAT,
           BC_M_HCN, BC_M_AHP,   BC_M_NAHH, BC_M_KHH, BC_M_KM,            BC_M_NA | BC_M_NAHH,
-          BC_M_KDR | BC_M_KLEAK | BC_M_AHP | BC_M_KHH | BC_M_KM | BC_M_KA1 | BC_M_KA2 | BC_M_KK2A | BC_M_KK2B,
-          BC_M_CAL | BC_M_CAT,  BC_M_KA1,  BC_M_KA2, BC_M_KK2A, BC_M_KK2B};
+          BC_M_KDR | BC_M_KLEAK | BC_M_AHP | BC_M_KHH | BC_M_KM | BC_M_KA1 | BC_M_KA2 | BC_M_KK2A | BC_M_KK2B | BC_M_KNI,
+          BC_M_CAL | BC_M_CAT,  BC_M_KA1,  BC_M_KA2, BC_M_KK2A, BC_M_KK2B, BC_M_KNI};
       const int32_t rg = cells[c].region[v];
       if (rg < 0 || !(s.region_mech[c * s.n_regions + rg] & cur_owner[field - BC_PROBE_CURRENT])) {
         delete p;
@@ -1205,7 +1205,8 @@ bc_status bc_plan_create(const bc_batch_spec* spec, const bc_plan_options* opts_
                                                      BC_M_CAL,   BC_M_CAT,   BC_M_CAT,   BC_M_HCN,   BC_M_AHP,
                                                      BC_M_CADET, BC_M_NAHH,  BC_M_NAHH,  BC_M_KHH,   BC_M_KM,
                                                      BC_M_KA1,   BC_M_KA1,   BC_M_KA2,   BC_M_KA2,
-                                                     BC_M_KK2A,  BC_M_KK2A,  BC_M_KK2B,  BC_M_KK2B};
+                                                     BC_M_KK2A,  BC_M_KK2A,  BC_M_KK2B,  BC_M_KK2B,
+                                                     BC_M_KNI};
       const int32_t rg = cells[c].region[v];
       if (rg < 0 || !(s.region_mech[c * s.n_regions + rg] & owner[field])) {
         delete p;
@@ -1952,6 +1953,7 @@ static bc_status view_offsets(bc_plan* p, int32_t which, std::vector<int64_t>& h
       case BC_STATE_KK2A_Q: slot = (m & BC_M_KK2A) ? kSlotKK2AQ : -1; break;
       case BC_STATE_KK2B_P: slot = (m & BC_M_KK2B) ? kSlotKK2BP : -1; break;
       case BC_STATE_KK2B_Q: slot = (m & BC_M_KK2B) ? kSlotKK2BQ : -1; break;
+      case BC_STATE_KNI_P: slot = (m & BC_M_KNI) ? kSlotKNIP : -1; break;
     }
     if (slot < 0) continue;
     // states live in the separate state array: offsets are tagged by +state_tag
@@ -2039,12 +2041,14 @@ static void noalloc_offset(const bc_plan* p, int32_t which, int64_t k, int64_t* 
                                                 BC_M_CAL, BC_M_CAT,   BC_M_CAT,  BC_M_HCN,  BC_M_AHP,
                                                 BC_M_CADET, BC_M_NAHH, BC_M_NAHH, BC_M_KHH, BC_M_KM,
                                                 BC_M_KA1,   BC_M_KA1,  BC_M_KA2,  BC_M_KA2,
-                                                BC_M_KK2A,  BC_M_KK2A, BC_M_KK2B, BC_M_KK2B};
+                                                BC_M_KK2A,  BC_M_KK2A, BC_M_KK2B, BC_M_KK2B,
+                                                BC_M_KNI};
   static const int kSlot[BC_NSTATE_VIEW] = {-1,        kSlotNaP,   kSlotNaQ,   kSlotKdrP,  kSlotCalP,
                                             kSlotCalQ, kSlotCatP,  kSlotCatQ,  kSlotHcnP,  kSlotAhpP,
                                             kSlotCaHi, kSlotNaHHP, kSlotNaHHQ, kSlotKHHP,  kSlotKMN,
                                             kSlotKA1P, kSlotKA1Q,  kSlotKA2P,  kSlotKA2Q,
-                                            kSlotKK2AP, kSlotKK2AQ, kSlotKK2BP, kSlotKK2BQ};
+                                            kSlotKK2AP, kSlotKK2AQ, kSlotKK2BP, kSlotKK2BQ,
+                                            kSlotKNIP};
   if (!(p->cv_mech[k] & kBit[which])) return;
   *hi = kStateTag + (d.state_offset + int64_t(kSlot[which]) * d.n_nodes + j) * rs;
   if (which == BC_STATE_CA_CI) *lo = kStateTag + (d.state_offset + int64_t(kSlotCaLo) * d.n_nodes + j) * rs;

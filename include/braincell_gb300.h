@@ -57,7 +57,8 @@ typedef int32_t bc_status;
 #define BC_M_KA2 (1u << 13)      /* channel/potassium.py:614  KA2_HM1992  p^4 q, E_K           */
 #define BC_M_KK2A (1u << 14)     /* channel/potassium.py:765  KK2A_HM1992 p q, E_K             */
 #define BC_M_KK2B (1u << 15)     /* channel/potassium.py:899  KK2B_HM1992 p q, E_K             */
-#define BC_M_ALL 0xFFFFu
+#define BC_M_KNI (1u << 16)      /* channel/potassium.py:1045 KNI_Ya1989  p, E_K               */
+#define BC_M_ALL 0x1FFFFu
 
 /* Per-region parameter record (double[BC_NPARAM]); index names below. */
 #define BC_NPARAM 64
@@ -121,6 +122,10 @@ typedef int32_t bc_status;
 #define BC_P_KK2B_VSH 57
 #define BC_P_KK2B_PHIP 58
 #define BC_P_KK2B_PHIQ 59
+#define BC_P_KNI_G 60
+#define BC_P_KNI_VSH 61
+#define BC_P_KNI_PHI 62
+#define BC_P_KNI_TAUMAX 63  /* ms */
 
 /* ------------------------------------------------------------------ batch spec */
 /*
@@ -333,7 +338,8 @@ bc_status bc_check(bc_plan_t plan, void* stream);
 #define BC_STATE_KK2A_Q 20
 #define BC_STATE_KK2B_P 21
 #define BC_STATE_KK2B_Q 22
-#define BC_NSTATE_VIEW 23
+#define BC_STATE_KNI_P 23
+#define BC_NSTATE_VIEW 24
 /* Current probes (mech/_point.py CurrentProbe, _multi_compartment/probes.py:184-258):
    probe_field = BC_PROBE_CURRENT + one of the codes below records that current
    density (uA/cm^2, outward negative as g (E - V)) after the step.             */
@@ -356,7 +362,8 @@ bc_status bc_check(bc_plan_t plan, void* stream);
 #define BC_CUR_KA2 15    /* KA2_HM1992  */
 #define BC_CUR_KK2A 16   /* KK2A_HM1992 */
 #define BC_CUR_KK2B 17   /* KK2B_HM1992 */
-#define BC_NCUR 18
+#define BC_CUR_KNI 18    /* KNI_Ya1989  */
+#define BC_NCUR 19
 bc_status bc_state_download(bc_plan_t plan, int32_t which, double* out /* [n_cv] */, void* stream);
 bc_status bc_state_upload(bc_plan_t plan, int32_t which, const double* in /* [n_cv] */, void* stream);
 

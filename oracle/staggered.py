@@ -104,6 +104,8 @@ CHANNEL_DEFAULTS = {
                         temp_ref_q=_c2k(36.0), V_sh=0.0),  # potassium.py:863-869
     "KK2B_HM1992": dict(g_max=10.0, temp=_c2k(36.0), q10_p=1.0, temp_ref_p=_c2k(36.0), q10_q=1.0,
                         temp_ref_q=_c2k(36.0), V_sh=0.0),  # potassium.py:1005-1011
+    "KNI_Ya1989": dict(g_max=0.004, temp=_c2k(36.0), q10=1.0, temp_ref=_c2k(36.0), tau_max=4e3,
+                       V_sh=0.0),  # potassium.py:1140-1145
 }
 ION_DEFAULTS = {
     "SodiumFixed": dict(E=50.0),
@@ -367,6 +369,10 @@ def rates(name: str, V, p: dict, Ci=None):
             "q": ("it", 1.0 / (1.0 + np.exp((Vs + 78.0) / 6.0)),
                   np.where(Vs < -63.0, 1.0 / (np.exp((Vs + 46.0) / 5.0) + np.exp(-(Vs + 238.0) / 37.5)), 19.0)),
         }
+    if name == "KNI_Ya1989":  # potassium.py:1156-1163
+        t = V - p["V_sh"] + 35.0
+        return {"p": ("it", 1.0 / (1.0 + np.exp(-(V - p["V_sh"] + 35.0) / 10.0)),
+                      p["tau_max"] / (3.3 * np.exp(t / 20.0) + np.exp(-t / 20.0)))}
     if name in ("KK2A_HM1992", "KK2B_HM1992"):  # potassium.py:881-895 and :1023-1041
         Vs = V - p["V_sh"]
         bell = 1.0 / (np.exp((Vs - 1329.0) / 200.0) + np.exp(-(Vs + 130.0) / 7.1))
@@ -402,11 +408,13 @@ _GATES = {  # (gate, power, phi-key)
     "KA2_HM1992": (("p", 4, "phi_p"), ("q", 1, "phi_q")),
     "KK2A_HM1992": (("p", 1, "phi_p"), ("q", 1, "phi_q")),
     "KK2B_HM1992": (("p", 1, "phi_p"), ("q", 1, "phi_q")),
+    "KNI_Ya1989": (("p", 1, "phi"),),
 }
 _ION_OF = {"Na_Ba2002": "na", "KDR_Ba2002": "k", "CaL_IS2008": "ca", "CaT_HM1992": "ca",
            "K_Leak": "k", "AHP_De1994": "k", "Na_HH1952": "na", "K_HH1952": "k", "KM_RI2021_SC": "k",
            "Na_TM1991": "na", "K_TM1991": "k", "CaHT_HM1992": "ca", "KA1_HM1992": "k", "KA2_HM1992": "k",
-           "KM_MA2020_GoC": "k", "KM_MA2020_GrC": "k", "KK2A_HM1992": "k", "KK2B_HM1992": "k"}
+           "KM_MA2020_GoC": "k", "KM_MA2020_GrC": "k", "KK2A_HM1992": "k", "KK2B_HM1992": "k",
+           "KNI_Ya1989": "k"}
 
 
 def _resolve(table: dict, decl) -> dict:
@@ -416,7 +424,8 @@ def _resolve(table: dict, decl) -> dict:
             raise ValueError(f"{decl.class_name}: unknown parameter {k!r}.")
         p[k] = float(v)
     name = decl.class_name
-    if name in ("Na_Ba2002", "KDR_Ba2002", "HCN_HM1992", "Na_HH1952", "K_HH1952", "Na_TM1991", "K_TM1991"):
+    if name in ("Na_Ba2002", "KDR_Ba2002", "HCN_HM1992", "Na_HH1952", "K_HH1952", "Na_TM1991", "K_TM1991",
+                "KNI_Ya1989"):
         p["phi"] = p["q10"] ** ((p["temp"] - p["temp_ref"]) / 10.0)
     elif name in ("KM_RI2021_SC", "KM_MA2020_GoC", "KM_MA2020_GrC"):
         # Gate("n", q10=3.0, temp_ref=22 degC): potassium.py:1710, :4532, :5296

@@ -317,3 +317,17 @@ def test_slow_k2_rates():
     assert below == pytest.approx(885.0, rel=0.01)
     assert float(O.rates("KK2A_HM1992", np.array(-70.0), pa)["q"][2]) == pytest.approx(below + 120.0, rel=1e-6)
     assert O.rates("KK2A_HM1992", np.array(-43.0), pa)["p"][1] == pytest.approx(0.5)
+
+
+def test_kni_rates_and_record():
+    # KNI_Ya1989 (potassium.py:1156-1163): p_inf is 1/2 at V' = -35 mV, where
+    # tau = tau_max / (3.3 + 1); tau_max is a constructor parameter in ms.
+    from braincell_gb300 import _abi, catalogue
+    from braincell_gb300.mech import CableProperty, Channel
+
+    p = dict(O.CHANNEL_DEFAULTS["KNI_Ya1989"])
+    r = O.rates("KNI_Ya1989", np.array(-35.0), p)["p"]
+    assert r[1] == pytest.approx(0.5) and r[2] == pytest.approx(4000.0 / 4.3)
+    bits, rec = catalogue.region_record([Channel("KNI_Ya1989", tau_max=2000.0, V_sh=-3.0)], CableProperty())
+    assert bits == _abi.BC_M_KNI
+    assert list(rec[_abi.BC_P_KNI_G:_abi.BC_P_KNI_TAUMAX + 1]) == [0.004, -3.0, 1.0, 2000.0]

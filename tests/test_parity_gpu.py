@@ -292,8 +292,9 @@ def test_classic_hh_and_m_current(precision, tol):
 
 def _tm_cell(precision):
     """Traub-Miles soma (Na_TM1991, K_TM1991) with both A-current components
-    (KA1_HM1992, KA2_HM1992), both slow K2 components (KK2A_HM1992, KK2B_HM1992)
-    and CaHT_HM1992 dendrites over dynamic calcium: the
+    (KA1_HM1992, KA2_HM1992), both slow K2 components (KK2A_HM1992, KK2B_HM1992),
+    KNI_Ya1989 (tau_max shortened to 40 ms so that it moves within the run) and
+    CaHT_HM1992 dendrites over dynamic calcium: the
     same-form classes run on the Na_Ba2002 / KDR_Ba2002 / CaT_HM1992 kernels with
     their own defaults, while the oracle evaluates their own rate forms."""
     from braincell_gb300 import Branch, Cell, Morphology
@@ -308,7 +309,7 @@ def _tm_cell(precision):
     c.paint(AllRegion(), CableProperty(), Channel("IL", g_max=0.1, E=-65.0))
     c.paint(branch_in("type", "soma"), Channel("Na_TM1991", g_max=100.0), Channel("K_TM1991", g_max=30.0),
             Channel("KA1_HM1992", g_max=6.0), Channel("KA2_HM1992", g_max=4.0), Channel("KK2A_HM1992", g_max=2.0),
-            Channel("KK2B_HM1992", g_max=2.0))
+            Channel("KK2B_HM1992", g_max=2.0), Channel("KNI_Ya1989", g_max=1.0, tau_max=40.0))
     c.paint(branch_in("type", "basal_dendrite"), Channel("CaHT_HM1992", g_max=1.5),
             Ion("CalciumDetailed", C_rest=5e-5, tau=10.0, d=0.5, Ci_initializer=5e-5))
     c.place(RootLocation(0.5), CurrentClamp(delay=2.0, durations=20.0, amplitudes=0.5))
@@ -317,7 +318,7 @@ def _tm_cell(precision):
             MechanismProbe("CaHT_HM1992", "q", name="caht_q"))
     c.place(RootLocation(0.5), MechanismProbe("KA2_HM1992", "q", name="ka2_q"),
             CurrentProbe(mechanism="KA1_HM1992", name="i_ka1"), MechanismProbe("KK2B_HM1992", "q", name="kk2b_q"),
-            CurrentProbe(ion="k", name="i_k"))
+            CurrentProbe(ion="k", name="i_k"), MechanismProbe("KNI_Ya1989", "p", name="kni_p"))
     return c
 
 

@@ -59,7 +59,8 @@ def _hh_batch():
     c.paint(AllRegion(), CableProperty(), Channel("IL", g_max=0.3, E=-54.4))
     c.paint(branch_in("type", "soma"), Channel("Na_HH1952"), Channel("K_HH1952", g_max=36.0))
     c.paint(branch_in("type", "basal_dendrite"), Channel("KM_RI2021_SC"), Channel("KA1_HM1992", g_max=3.0),
-            Channel("KA2_HM1992", g_max=2.0), Channel("KK2A_HM1992", g_max=1.0), Channel("KK2B_HM1992", g_max=1.0))
+            Channel("KA2_HM1992", g_max=2.0), Channel("KK2A_HM1992", g_max=1.0), Channel("KK2B_HM1992", g_max=1.0),
+            Channel("KNI_Ya1989"))
     return lower_cell(c)
 
 
