@@ -29,25 +29,28 @@ namespace bc {
 // Accurate functions (both precisions): used where FP32 rounding matters
 // (exp-Euler decay factors, exprel near its removable singularity, Nernst log).
 __device__ __forceinline__ float dexpm1(float x) { return expm1f(x); }
-__device__ __forceinline__ double dexpm1(double x) { return expm1(x); }
+__host__ __device__ __forceinline__ double dexpm1(double x) { return expm1(x); }
 __device__ __forceinline__ float dlog(float x) { return logf(x); }
-__device__ __forceinline__ double dlog(double x) { return log(x); }
+__host__ __device__ __forceinline__ double dlog(double x) { return log(x); }
 __device__ __forceinline__ float dpow(float x, float y) { return powf(x, y); }
-__device__ __forceinline__ double dpow(double x, double y) { return pow(x, y); }
+__host__ __device__ __forceinline__ double dpow(double x, double y) { return pow(x, y); }
+// The FP64 forms and the rate structures are also host functions, so that a host
+// build of this header can check the FP64 rates against the oracle on a CPU; the
+// FP32 forms stay device-only.
 // Rate-function arithmetic: FP32 uses the hardware approximations (__expf, and
 // a * rcp.approx(b) for a / b: a few ulp, far below what the rates need); FP64
 // stays exact so the FP64 build remains an oracle-grade run of the same kernels.
 __device__ __forceinline__ float rexp(float x) { return __expf(x); }
 __device__ __forceinline__ float aexp(float x) { return expf(x); }
-__device__ __forceinline__ double aexp(double x) { return exp(x); }
-__device__ __forceinline__ double rexp(double x) { return exp(x); }
+__host__ __device__ __forceinline__ double aexp(double x) { return exp(x); }
+__host__ __device__ __forceinline__ double rexp(double x) { return exp(x); }
 __device__ __forceinline__ float rcp_approx(float x) {
   float r;
   asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
   return r;
 }
 __device__ __forceinline__ float rdiv(float a, float b) { return a * rcp_approx(b); }
-__device__ __forceinline__ double rdiv(double a, double b) { return a / b; }
+__host__ __device__ __forceinline__ double rdiv(double a, double b) { return a / b; }
 
 // e^x - 1 for the exp-Euler decay of a gate (x = dt * lambda <= 0).  FP32: for
 // |x| < 1/4 the Taylor series of e^x - 1 to x^6 (truncation < 5e-8 relative, the
@@ -57,11 +60,11 @@ __device__ __forceinline__ float decay_em1(float x) {
   const float p = x * (1.0f + x * (0.5f + x * (1.0f / 6.0f + x * (1.0f / 24.0f + x * (1.0f / 120.0f + x * (1.0f / 720.0f))))));
   return fabsf(x) < 0.25f ? p : __expf(x) - 1.0f;
 }
-__device__ __forceinline__ double decay_em1(double x) { return expm1(x); }
+__host__ __device__ __forceinline__ double decay_em1(double x) { return expm1(x); }
 
 // exprel(x) = (e^x - 1) / x, exprel(0) = 1
 template <typename Real>
-__device__ __forceinline__ Real exprel(Real x) {
+__host__ __device__ __forceinline__ Real exprel(Real x) {
   return x == Real(0) ? Real(1) : dexpm1(x) / x;
 }
 
@@ -86,7 +89,7 @@ __device__ __forceinline__ Real gate_it(Real x, Real inf, Real tau, Real phi, Re
 template <typename Real>
 struct NaRates {
   Real ap, bp, aq, bq;
-  __device__ __forceinline__ NaRates(Real v, Real vsh) {
+  __host__ __device__ __forceinline__ NaRates(Real v, Real vsh) {
     const Real vp = v - vsh;
     ap = Real(0.32 * 4.0) / exprel(-(vp - Real(13)) * Real(1.0 / 4));
     bp = Real(0.28 * 5.0) / exprel((vp - Real(40)) * Real(1.0 / 5));
@@ -98,7 +101,7 @@ struct NaRates {
 template <typename Real>
 struct KdrRates {
   Real a, b;
-  __device__ __forceinline__ KdrRates(Real v, Real vsh) {
+  __host__ __device__ __forceinline__ KdrRates(Real v, Real vsh) {
     const Real vp = v - vsh;
     a = Real(0.032 * 5.0) / exprel(-(vp - Real(15)) * Real(1.0 / 5));
     b = Real(0.5) * aexp(-(vp - Real(10)) * Real(1.0 / 40));
@@ -107,7 +110,7 @@ struct KdrRates {
 
 // 1 / (e^-y + e^y) = z / (1 + z^2) with z = e^y
 template <typename Real>
-__device__ __forceinline__ Real inv_cosh2(Real y) {
+__host__ __device__ __forceinline__ Real inv_cosh2(Real y) {
   const Real z = rexp(y);
   return rdiv(z, Real(1) + z * z);
 }
@@ -115,7 +118,7 @@ __device__ __forceinline__ Real inv_cosh2(Real y) {
 template <typename Real>
 struct CaLRates {
   Real pinf, ptau, qinf, qtau;
-  __device__ __forceinline__ CaLRates(Real v, Real vsh) {
+  __host__ __device__ __forceinline__ CaLRates(Real v, Real vsh) {
     const Real vs = v - vsh;
     pinf = rdiv(Real(1), Real(1) + rexp(-(vs + Real(10)) * Real(1.0 / 4)));
     ptau = Real(0.4) + Real(0.7) * inv_cosh2((vs + Real(5)) * Real(1.0 / 15));
@@ -127,7 +130,7 @@ struct CaLRates {
 template <typename Real>
 struct CaTRates {
   Real pinf, ptau, qinf, qtau;
-  __device__ __forceinline__ CaTRates(Real v, Real vsh) {
+  __host__ __device__ __forceinline__ CaTRates(Real v, Real vsh) {
     const Real vs = v - vsh;
     pinf = rdiv(Real(1), Real(1) + rexp(-(vs + Real(59)) * Real(1.0 / 6.2)));
     ptau = rdiv(Real(1), rexp(-(vs + Real(132)) * Real(1.0 / 16.7)) + rexp((vs + Real(16.8)) * Real(1.0 / 18.2))) + Real(0.612);
@@ -139,7 +142,7 @@ struct CaTRates {
 template <typename Real>
 struct HcnRates {
   Real pinf, ptau;
-  __device__ __forceinline__ HcnRates(Real v) {
+  __host__ __device__ __forceinline__ HcnRates(Real v) {
     pinf = rdiv(Real(1), Real(1) + rexp((v + Real(75)) * Real(1.0 / 5.5)));
     ptau = rdiv(Real(1), rexp(Real(-0.086) * v - Real(14.59)) + rexp(Real(0.0701) * v - Real(1.87)));
   }
@@ -148,7 +151,7 @@ struct HcnRates {
 template <typename Real>
 struct NaHHRates {
   Real ap, bp, aq, bq;
-  __device__ __forceinline__ NaHHRates(Real v, Real vsh) {
+  __host__ __device__ __forceinline__ NaHHRates(Real v, Real vsh) {
     const Real vp = v - vsh;
     ap = Real(1) / exprel(-(vp - Real(5)) * Real(0.1));
     bp = Real(4) * aexp(-(vp + Real(20)) * Real(1.0 / 18));
@@ -160,7 +163,7 @@ struct NaHHRates {
 template <typename Real>
 struct KHHRates {
   Real a, b;
-  __device__ __forceinline__ KHHRates(Real v, Real vsh) {
+  __host__ __device__ __forceinline__ KHHRates(Real v, Real vsh) {
     const Real vp = v - vsh;
     a = Real(0.1) / exprel(-(vp + Real(10)) * Real(0.1));
     b = Real(0.125) * aexp(-(vp + Real(20)) * Real(1.0 / 80));
@@ -170,7 +173,7 @@ struct KHHRates {
 template <typename Real>
 struct KMRates {
   Real ninf, ntau;
-  __device__ __forceinline__ KMRates(Real v) {
+  __host__ __device__ __forceinline__ KMRates(Real v) {
     ninf = rdiv(Real(1), Real(1) + rexp(-(v + Real(35)) * Real(1.0 / 6)));
     ntau = rdiv(Real(1), Real(0.0033) * rexp((v + Real(30)) * Real(1.0 / 40)) +
                              Real(0.0033) * rexp(-(v + Real(30)) * Real(1.0 / 20)));
@@ -182,7 +185,7 @@ struct KMRates {
 template <typename Real>
 struct KARates {
   Real pinf, ptau, qinf, qtau;
-  __device__ __forceinline__ KARates(Real v, Real vsh, Real pmid, Real pinv_slope) {
+  __host__ __device__ __forceinline__ KARates(Real v, Real vsh, Real pmid, Real pinv_slope) {
     const Real vp = v - vsh;
     pinf = rdiv(Real(1), Real(1) + rexp(-(vp + pmid) * pinv_slope));
     ptau = rdiv(Real(1), rexp((vp + Real(35.8)) * Real(1.0 / 19.7)) + rexp(-(vp + Real(79.7)) * Real(1.0 / 12.7))) +
@@ -199,7 +202,7 @@ struct KARates {
 template <typename Real>
 struct K2Rates {
   Real pinf, ptau, qinf, qtau;
-  __device__ __forceinline__ K2Rates(Real v, Real vsh, bool b_form) {
+  __host__ __device__ __forceinline__ K2Rates(Real v, Real vsh, bool b_form) {
     const Real vp = v - vsh;
     pinf = rdiv(Real(1), Real(1) + rexp(-(vp + Real(43)) * Real(1.0 / 17)));
     ptau = rdiv(Real(1), rexp((vp - Real(81)) * Real(1.0 / 25.6)) + rexp(-(vp + Real(132)) * Real(1.0 / 18))) +
@@ -213,7 +216,7 @@ struct K2Rates {
 template <typename Real>
 struct KNIRates {
   Real pinf, ptau;
-  __device__ __forceinline__ KNIRates(Real v, Real vsh, Real tau_max) {
+  __host__ __device__ __forceinline__ KNIRates(Real v, Real vsh, Real tau_max) {
     const Real x = v - vsh + Real(35);
     pinf = rdiv(Real(1), Real(1) + rexp(-x * Real(0.1)));
     ptau = rdiv(tau_max, Real(3.3) * rexp(x * Real(0.05)) + rexp(-x * Real(0.05)));

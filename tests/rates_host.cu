@@ -1,0 +1,43 @@
+// Test harness: the FP64 rate structures of the step kernel's mechanism header,
+// compiled for the host, so that tests/test_rates_host.py can compare them with
+// the oracle's rate functions on a CPU.  Not part of the library.
+#include "../braincell_gb300/csrc/bc_mech.cuh"
+
+using namespace bc;
+
+// Kernel rate structure `which` at n voltages v (mV) with parameters prm (V_sh
+// first; KNI: V_sh, tau_max).  out[4 i .. 4 i + 3] receives the gate rates in the
+// oracle's order: per gate (alpha, beta) or (inf, tau); unused entries are 0.
+// Returns 0, or -1 for an unknown structure.
+extern "C" int bc_test_rates(int which, const double* v, int n, const double* prm, double* out) {
+  for (int i = 0; i < n; ++i) {
+    double* o = out + 4 * i;
+    o[0] = o[1] = o[2] = o[3] = 0.0;
+    const double x = v[i];
+    switch (which) {
+      case 0: { const NaRates<double> r(x, prm[0]); o[0] = r.ap; o[1] = r.bp; o[2] = r.aq; o[3] = r.bq; break; }
+      case 1: { const KdrRates<double> r(x, prm[0]); o[0] = r.a; o[1] = r.b; break; }
+      case 2: { const CaLRates<double> r(x, prm[0]); o[0] = r.pinf; o[1] = r.ptau; o[2] = r.qinf; o[3] = r.qtau; break; }
+      case 3: { const CaTRates<double> r(x, prm[0]); o[0] = r.pinf; o[1] = r.ptau; o[2] = r.qinf; o[3] = r.qtau; break; }
+      case 4: { const HcnRates<double> r(x); o[0] = r.pinf; o[1] = r.ptau; break; }
+      case 5: { const NaHHRates<double> r(x, prm[0]); o[0] = r.ap; o[1] = r.bp; o[2] = r.aq; o[3] = r.bq; break; }
+      case 6: { const KHHRates<double> r(x, prm[0]); o[0] = r.a; o[1] = r.b; break; }
+      case 7: { const KMRates<double> r(x); o[0] = r.ninf; o[1] = r.ntau; break; }
+      case 8: {
+        const KARates<double> r(x, prm[0], kKA1Mid, kKA1InvSlope);
+        o[0] = r.pinf; o[1] = r.ptau; o[2] = r.qinf; o[3] = r.qtau;
+        break;
+      }
+      case 9: {
+        const KARates<double> r(x, prm[0], kKA2Mid, kKA2InvSlope);
+        o[0] = r.pinf; o[1] = r.ptau; o[2] = r.qinf; o[3] = r.qtau;
+        break;
+      }
+      case 10: { const K2Rates<double> r(x, prm[0], false); o[0] = r.pinf; o[1] = r.ptau; o[2] = r.qinf; o[3] = r.qtau; break; }
+      case 11: { const K2Rates<double> r(x, prm[0], true); o[0] = r.pinf; o[1] = r.ptau; o[2] = r.qinf; o[3] = r.qtau; break; }
+      case 12: { const KNIRates<double> r(x, prm[0], prm[1]); o[0] = r.pinf; o[1] = r.ptau; break; }
+      default: return -1;
+    }
+  }
+  return 0;
+}

@@ -1,0 +1,79 @@
+"""The step kernel's FP64 rate structures (``bc_mech.cuh``), compiled for the host,
+against the oracle's rate functions over a voltage grid: a CPU check of the device
+rate arithmetic for every kernel channel, including the classes that only the GPU
+parity tests exercise in a full simulation.  Needs nvcc (no GPU)."""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+from oracle import staggered as O
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+# harness index -> (oracle class, kernel parameters from the class defaults)
+CASES = {
+    0: ("Na_Ba2002", ("V_sh",)), 1: ("KDR_Ba2002", ("V_sh",)), 2: ("CaL_IS2008", ("V_sh",)),
+    3: ("CaT_HM1992", ("V_sh",)), 4: ("HCN_HM1992", ()), 5: ("Na_HH1952", ("V_sh",)), 6: ("K_HH1952", ("V_sh",)),
+    7: ("KM_RI2021_SC", ()), 8: ("KA1_HM1992", ("V_sh",)), 9: ("KA2_HM1992", ("V_sh",)),
+    10: ("KK2A_HM1992", ("V_sh",)), 11: ("KK2B_HM1992", ("V_sh",)), 12: ("KNI_Ya1989", ("V_sh", "tau_max")),
+}
+
+
+@pytest.fixture(scope="module")
+def rates_lib(tmp_path_factory):
+    nvcc = os.environ.get("NVCC") or shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(nvcc):
+        pytest.skip("nvcc is not available")
+    out = str(tmp_path_factory.mktemp("rates") / "librates_host.so")
+    cmd = [nvcc, "-x", "cu", "-shared", "-Xcompiler", "-fPIC", "-std=c++17", "-O2",
+           "-gencode=arch=compute_103a,code=sm_103a", os.path.join(HERE, "rates_host.cu"), "-o", out]
+    subprocess.run(cmd, check=True, capture_output=True, text=True)
+    lib = C.CDLL(out)
+    lib.bc_test_rates.argtypes = [C.c_int, C.POINTER(C.c_double), C.c_int, C.POINTER(C.c_double),
+                                  C.POINTER(C.c_double)]
+    lib.bc_test_rates.restype = C.c_int
+    return lib
+
+
+def _kernel(lib, which, V, prm):
+    V = np.ascontiguousarray(V, np.float64)
+    prm = np.ascontiguousarray(prm, np.float64)
+    out = np.zeros((V.size, 4))
+    dp = C.POINTER(C.c_double)
+    assert lib.bc_test_rates(which, V.ctypes.data_as(dp), V.size, prm.ctypes.data_as(dp), out.ctypes.data_as(dp)) == 0
+    return out
+
+
+@pytest.mark.parametrize("which", sorted(CASES))
+@pytest.mark.parametrize("shift", [0.0, 7.5])
+def test_kernel_rates_match_oracle(rates_lib, which, shift):
+    name, keys = CASES[which]
+    p = dict(O.CHANNEL_DEFAULTS[name])
+    if "V_sh" in keys:
+        p["V_sh"] = p["V_sh"] + shift
+    # a grid with the removable singularities of exprel and the branch points of the
+    # piecewise time constants (KA -63, KK2B -70, CaT -80 relative to V_sh)
+    V = np.linspace(-130.0, 60.0, 1901)
+    if "V_sh" in keys:
+        V = np.concatenate([V, p["V_sh"] + np.array([13.0, 15.0, 40.0, -5.0, -63.0, -70.0, -80.0, -10.0])])
+    got = _kernel(rates_lib, which, V, [p[k] for k in keys])
+    ref = O.rates(name, V, p)
+    cols = [c for g in ref for c in (ref[g][1], ref[g][2])]
+    for k, col in enumerate(cols):
+        np.testing.assert_allclose(got[:, k], np.broadcast_to(col, V.shape), rtol=1e-12, atol=1e-300,
+                                   err_msg=f"{name} rate column {k}")
+
+
+def test_unknown_structure_is_rejected(rates_lib):
+    assert rates_lib.bc_test_rates(99, None, 0, None, None) == 0  # no voltages: nothing to evaluate
+    v = np.zeros(1)
+    out = np.zeros(4)
+    dp = C.POINTER(C.c_double)
+    assert rates_lib.bc_test_rates(99, v.ctypes.data_as(dp), 1, v.ctypes.data_as(dp), out.ctypes.data_as(dp)) == -1
