@@ -89,3 +89,72 @@ def test_dry_plan_has_no_device_state(native_lib):
     p = Plan(W.descs_to_batch(W.small(1)), dry_run=True)
     with pytest.raises(_abi.BCError, match="dry_run"):
         p.run(1, 0.025)
+
+
+def _probe_plan(decls, field):
+    from braincell_gb300 import Branch, Cell, Morphology
+    from braincell_gb300.batch import lower_cell
+    from braincell_gb300.mech import AllRegion, CableProperty, CVPerBranch, RootLocation, StateProbe
+    from braincell_gb300.runtime import Plan
+
+    m = Morphology.from_root(Branch.from_lengths(lengths=[20.0], radii=[10.0, 10.0], type="soma"), name="soma")
+    c = Cell(m, cv_policy=CVPerBranch())
+    c.paint(AllRegion(), CableProperty(), *decls)
+    c.place(RootLocation(0.5), StateProbe())
+    b = lower_cell(c)
+    b.probe_field[:] = field
+    return Plan(b, dry_run=True)
+
+
+def _decl(cls):
+    from braincell_gb300.mech import Channel, Ion
+
+    return Ion(cls) if cls == "CalciumDetailed" else Channel(cls)
+
+
+_VIEW_CASES = sorted({(v, c) for (c, _f), v in __import__("braincell_gb300.batch", fromlist=["x"]).PROBE_STATES.items()
+                      if c not in __import__("braincell_gb300.catalogue", fromlist=["x"]).SAME_FORM})
+_CUR_CASES = sorted({(v, c) for c, v in __import__("braincell_gb300.batch", fromlist=["x"]).PROBE_CURRENTS.items()
+                     if c not in __import__("braincell_gb300.catalogue", fromlist=["x"]).SAME_FORM})
+
+
+@pytest.mark.parametrize("view,cls", _VIEW_CASES)
+def test_planner_state_view_owner_table(view, cls):
+    # the planner accepts a mechanism probe only where the mechanism owning the view is
+    # painted (bc_plan.cpp owner table), whatever else is painted there
+    from braincell_gb300 import _abi
+    from braincell_gb300.mech import Channel
+
+    _probe_plan([Channel("IL"), _decl(cls)], view).close()
+    other = "KNI_Ya1989" if cls != "KNI_Ya1989" else "KM_RI2021_SC"
+    with pytest.raises(_abi.BCError, match="no such mechanism"):
+        _probe_plan([Channel("IL"), Channel(other)], view)
+
+
+@pytest.mark.parametrize("code,cls", _CUR_CASES)
+def test_planner_current_owner_table(code, cls):
+    from braincell_gb300 import _abi
+    from braincell_gb300.mech import Channel
+
+    field = _abi.BC_PROBE_CURRENT + code
+    _probe_plan([_decl(cls)], field).close()
+    other = "HCN_HM1992" if cls != "HCN_HM1992" else "K_Leak"
+    with pytest.raises(_abi.BCError, match="no such mechanism"):
+        _probe_plan([Channel(other)], field)
+
+
+@pytest.mark.parametrize("ion,members", [("na", ("Na_Ba2002", "Na_HH1952")),
+                                         ("k", ("KDR_Ba2002", "K_Leak", "AHP_De1994", "K_HH1952", "KM_RI2021_SC",
+                                                "KA1_HM1992", "KA2_HM1992", "KK2A_HM1992", "KK2B_HM1992",
+                                                "KNI_Ya1989")),
+                                         ("ca", ("CaL_IS2008", "CaT_HM1992"))])
+def test_planner_ion_current_owner_table(ion, members):
+    from braincell_gb300 import _abi
+    from braincell_gb300.batch import ION_CURRENTS
+    from braincell_gb300.mech import Channel
+
+    field = _abi.BC_PROBE_CURRENT + ION_CURRENTS[ion]
+    for cls in members:
+        _probe_plan([Channel(cls)], field).close()
+    with pytest.raises(_abi.BCError, match="no such mechanism"):
+        _probe_plan([Channel("HCN_HM1992")], field)
