@@ -5,6 +5,8 @@ import numpy as np
 import pytest
 
 from braincell_gb300 import _abi
+from braincell_gb300 import batch as _batch
+from braincell_gb300 import catalogue as _catalogue
 from braincell_gb300 import workloads as W
 from braincell_gb300.batch import CellBatch
 from braincell_gb300.runtime import Plan
@@ -112,10 +114,9 @@ def _decl(cls):
     return Ion(cls) if cls == "CalciumDetailed" else Channel(cls)
 
 
-_VIEW_CASES = sorted({(v, c) for (c, _f), v in __import__("braincell_gb300.batch", fromlist=["x"]).PROBE_STATES.items()
-                      if c not in __import__("braincell_gb300.catalogue", fromlist=["x"]).SAME_FORM})
-_CUR_CASES = sorted({(v, c) for c, v in __import__("braincell_gb300.batch", fromlist=["x"]).PROBE_CURRENTS.items()
-                     if c not in __import__("braincell_gb300.catalogue", fromlist=["x"]).SAME_FORM})
+# one case per view / current code, named by its kernel class (same-form classes share them)
+_VIEW_CASES = sorted({(v, c) for (c, _f), v in _batch.PROBE_STATES.items() if c not in _catalogue.SAME_FORM})
+_CUR_CASES = sorted({(v, c) for c, v in _batch.PROBE_CURRENTS.items() if c not in _catalogue.SAME_FORM})
 
 
 @pytest.mark.parametrize("view,cls", _VIEW_CASES)
