@@ -107,6 +107,12 @@ BC_P_KNI_VSH = 61
 BC_P_KNI_PHI = 62
 BC_P_KNI_TAUMAX = 63
 
+BC_ABI_VERSION = 200
+
+BC_VARIANT_LEAN = 0
+BC_VARIANT_EXTRA = 1
+BC_VARIANT_PORTS = 2
+
 BC_PREC_F32 = 0
 BC_PREC_F64 = 1
 
@@ -287,7 +293,10 @@ class PlanInfo(C.Structure):
         ("max_phases", C.c_int64),
         ("max_chain_nodes", C.c_int64),
         ("state_slots", C.c_int32),
-        ("reserved", C.c_int32 * 7),
+        ("n_smem_tiles", C.c_int32),
+        ("n_launch_classes", C.c_int32),
+        ("kernel_variant", C.c_int32),
+        ("reserved", C.c_int32 * 4),
     ]
 
     def as_dict(self) -> dict:
@@ -370,6 +379,13 @@ def lib():
             fn = getattr(handle, name)
             fn.restype = restype
             fn.argtypes = argtypes
+        # a library of another ABI version lays out its records differently
+        # (parameter record size, state views): refuse it rather than misread it
+        version = int(handle.bc_version())
+        if version != BC_ABI_VERSION:
+            raise ImportError(f"braincell_gb300 native library at {LIB_PATH} has ABI version {version}, this package "
+                              f"expects {BC_ABI_VERSION}; rebuild it with "
+                              "`python -c 'import braincell_gb300.build as b; b.build_native(force=True)'`.")
         _lib = handle
         return _lib
 

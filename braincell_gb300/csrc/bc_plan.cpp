@@ -853,7 +853,9 @@ static bc_status ensure_traces(bc_plan* p, int64_t records, void* stream) {
 }
 
 // Kernel variant of a plan (see launch_tiles).
-static int kernel_variant(const bc_plan* p) { return p->n_ports > 0 ? 2 : (p->extra ? 1 : 0); }
+static int kernel_variant(const bc_plan* p) {
+  return p->n_ports > 0 ? BC_VARIANT_PORTS : (p->extra ? BC_VARIANT_EXTRA : BC_VARIANT_LEAN);
+}
 
 static LaunchArgs base_args(bc_plan* p) {
   LaunchArgs a{};
@@ -1077,7 +1079,7 @@ extern "C" {
 
 const char* bc_last_error(void) { return g_error.c_str(); }
 
-int32_t bc_version(void) { return 100; }
+int32_t bc_version(void) { return BC_ABI_VERSION; }
 
 void bc_default_options(bc_plan_options* o) {
   std::memset(o, 0, sizeof(*o));
@@ -1703,8 +1705,9 @@ bc_status bc_plan_info(bc_plan_t p, bc_plan_info_t* info) {
   info->max_phases = p->max_phases;
   info->max_chain_nodes = p->max_chain_nodes;
   info->state_slots = p->state_slots;
-  info->reserved[0] = p->n_smem_tiles;
-  info->reserved[1] = int32_t(p->classes.size());
+  info->n_smem_tiles = int32_t(p->n_smem_tiles);
+  info->n_launch_classes = int32_t(p->classes.size());
+  info->kernel_variant = kernel_variant(p);
   return BC_OK;
 }
 

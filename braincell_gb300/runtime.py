@@ -82,8 +82,6 @@ class Plan:
         info = _abi.PlanInfo()
         _abi.check(lib.bc_plan_info(self._h, C.byref(info)))
         self.info = info.as_dict()
-        self.info["n_smem_tiles"] = int(info.reserved[0])
-        self.info["n_launch_classes"] = int(info.reserved[1])
         self.n_cv = int(info.n_cv)
         self.n_cells = int(info.n_cells)
         self.n_probes = int(info.n_probes)

@@ -257,13 +257,24 @@ typedef struct bc_plan_info_t {
   int64_t max_phases;            /* largest barrier-phase count of any tile          */
   int64_t max_chain_nodes;       /* longest per-thread node walk (critical path)     */
   int32_t state_slots;           /* per-node mechanism state slots                   */
-  int32_t reserved[7];
+  int32_t n_smem_tiles;          /* tiles resident in shared memory                  */
+  int32_t n_launch_classes;      /* kernel launches per fused step block             */
+  int32_t kernel_variant;        /* BC_VARIANT_* the plan launches                   */
+  int32_t reserved[4];
 } bc_plan_info_t;
+/* Step-kernel variants: lean (the main channel mix only), extra (synapses, spike
+ * sources, mechanism and current probes, the channels outside the main mix), ports
+ * (extra plus subtree-surrogate GRU ports). */
+#define BC_VARIANT_LEAN 0
+#define BC_VARIANT_EXTRA 1
+#define BC_VARIANT_PORTS 2
 
 /* ------------------------------------------------------------------ entry points */
 /* Thread-local text of the last failure (never NULL). */
 const char* bc_last_error(void);
-/* ABI version: major * 10000 + minor * 100 + patch. */
+/* ABI version: major * 10000 + minor * 100 + patch.  0.2.0: the 64-entry parameter
+ * record, the A / K2 / KNI mechanisms, named plan-info fields. */
+#define BC_ABI_VERSION 200
 int32_t bc_version(void);
 /* Fill opts with defaults. */
 void bc_default_options(bc_plan_options* opts);

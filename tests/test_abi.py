@@ -58,7 +58,7 @@ def test_struct_sizes(native_lib):
 
 
 def test_version_and_defaults(native_lib):
-    assert native_lib.bc_version() >= 100
+    assert native_lib.bc_version() == _abi.BC_ABI_VERSION
     o = _abi.PlanOptions()
     native_lib.bc_default_options(C.byref(o))
     assert o.precision == _abi.BC_PREC_F32 and o.record_every == 1 and o.lane_nodes > 0

@@ -159,3 +159,27 @@ def test_planner_ion_current_owner_table(ion, members):
         _probe_plan([Channel(cls)], field).close()
     with pytest.raises(_abi.BCError, match="no such mechanism"):
         _probe_plan([Channel("HCN_HM1992")], field)
+
+
+@pytest.mark.parametrize("cls,variant", [("IL", _abi.BC_VARIANT_LEAN), ("Na_Ba2002", _abi.BC_VARIANT_LEAN),
+                                         ("CaT_HM1992", _abi.BC_VARIANT_LEAN), ("Na_HH1952", _abi.BC_VARIANT_EXTRA),
+                                         ("K_HH1952", _abi.BC_VARIANT_EXTRA), ("KM_RI2021_SC", _abi.BC_VARIANT_EXTRA),
+                                         ("KA1_HM1992", _abi.BC_VARIANT_EXTRA), ("KA2_HM1992", _abi.BC_VARIANT_EXTRA),
+                                         ("KK2A_HM1992", _abi.BC_VARIANT_EXTRA), ("KK2B_HM1992", _abi.BC_VARIANT_EXTRA),
+                                         ("KNI_Ya1989", _abi.BC_VARIANT_EXTRA), ("K_TM1991", _abi.BC_VARIANT_LEAN)])
+def test_kernel_variant_follows_the_painted_channels(cls, variant):
+    # the lean kernel carries only the main mix: a plan with any channel outside it
+    # must launch the extra variant, which is the one that evaluates those channels
+    from braincell_gb300.mech import Channel
+
+    p = _probe_plan([Channel(cls)], _abi.BC_STATE_V)
+    assert p.info["kernel_variant"] == variant
+    p.close()
+
+
+def test_mechanism_probe_selects_the_extra_variant():
+    from braincell_gb300.mech import Channel
+
+    p = _probe_plan([Channel("Na_Ba2002")], _abi.BC_STATE_NA_P)
+    assert p.info["kernel_variant"] == _abi.BC_VARIANT_EXTRA
+    p.close()
