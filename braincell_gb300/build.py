@@ -40,6 +40,8 @@ def _flags(debug: bool) -> list[str]:
         "-fPIC",
         "-Xcompiler",
         "-Wall",
+        "-Xcompiler",
+        "-pthread",
         "--expt-relaxed-constexpr",
         "-I" + os.path.join(HERE, "..", "include"),
     ]
@@ -85,7 +87,7 @@ def build_native(force: bool = False, verbose: bool = False, debug: bool = False
         raise RuntimeError("nvcc failed:\n" + "\n".join(errors))
     os.makedirs(os.path.dirname(os.path.abspath(lib_path)), exist_ok=True)
     tmp = lib_path + ".tmp"
-    link = [nvcc, "-shared", GENCODE, "-o", tmp] + objs + ["-cudart", "static"]
+    link = [nvcc, "-shared", GENCODE, "-o", tmp] + objs + ["-cudart", "static", "-lpthread"]
     r = subprocess.run(link, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n" + r.stdout)

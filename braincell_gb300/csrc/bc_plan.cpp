@@ -12,13 +12,16 @@
 
 #include <algorithm>
 #include <array>
+#include <atomic>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <mutex>
 #include <numeric>
 #include <queue>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "bc_internal.h"
@@ -212,6 +215,32 @@ struct CellSched {
   std::vector<Chain> chains;   // ordered by level ascending
   int32_t max_level = 0;
 };
+
+// fn(i) for i in [0, n) on up to BC_PLAN_THREADS host threads (default: the
+// hardware threads, at most 32), in chunks of 64 items; one thread when n is
+// small.  fn must touch only item i's outputs.
+template <class F>
+static void parallel_for(int64_t n, F&& fn) {
+  int64_t nt = int64_t(std::thread::hardware_concurrency());
+  if (const char* e = std::getenv("BC_PLAN_THREADS")) nt = std::atoll(e);
+  nt = std::max<int64_t>(1, std::min<int64_t>({nt, 32, (n + 63) / 64}));
+  if (nt <= 1) {
+    for (int64_t i = 0; i < n; ++i) fn(i);
+    return;
+  }
+  std::atomic<int64_t> next{0};
+  auto work = [&]() {
+    for (;;) {
+      const int64_t i0 = next.fetch_add(64);
+      if (i0 >= n) return;
+      for (int64_t i = i0; i < std::min<int64_t>(n, i0 + 64); ++i) fn(i);
+    }
+  };
+  std::vector<std::thread> pool;
+  for (int64_t t = 1; t < nt; ++t) pool.emplace_back(work);
+  work();
+  for (auto& th : pool) th.join();
+}
 
 static void decompose(const LoweredCell& lc, CellSched& cs) {
   const int32_t n = lc.n_node;
@@ -1129,14 +1158,28 @@ bc_status bc_plan_create(const bc_batch_spec* spec, const bc_plan_options* opts_
   // ---------------------------------------------------- lower
   std::vector<LoweredCell> cells(s.n_cells);
   std::vector<int64_t> cv_base(s.n_cells + 1, 0);
-  for (int64_t c = 0; c < s.n_cells; ++c) {
-    bc_status st = lower_cell(s, c, cells[c]);
-    if (st != BC_OK) {
-      delete p;
-      return st;
+  {
+    // cells lower independently; the failure reported is that of the first failing
+    // cell in cell order, as a sequential pass would report it
+    std::vector<bc_status> lst(s.n_cells, BC_OK);
+    std::vector<std::string> lmsg(s.n_cells);
+    parallel_for(s.n_cells, [&](int64_t c) {
+      try {
+        lst[c] = lower_cell(s, c, cells[c]);
+        if (lst[c] != BC_OK) lmsg[c] = bc_last_error();
+      } catch (const std::exception& ex) {
+        lst[c] = BC_ERR_CAPACITY;
+        lmsg[c] = std::string("lowering cell ") + std::to_string(c) + ": " + ex.what();
+      }
+    });
+    for (int64_t c = 0; c < s.n_cells; ++c) {
+      if (lst[c] != BC_OK) {
+        delete p;
+        return fail(lst[c], lmsg[c]);
+      }
+      cv_base[c + 1] = cv_base[c] + cells[c].n_cv;
+      p->n_nodes += cells[c].n_node;
     }
-    cv_base[c + 1] = cv_base[c] + cells[c].n_cv;
-    p->n_nodes += cells[c].n_node;
   }
   p->n_cv = cv_base[s.n_cells];
   p->cell_ncv.resize(s.n_cells);
@@ -1346,7 +1389,7 @@ bc_status bc_plan_create(const bc_batch_spec* spec, const bc_plan_options* opts_
   }
   // ---------------------------------------------------- schedules
   std::vector<CellSched> sched(s.n_cells);
-  for (int64_t c = 0; c < s.n_cells; ++c) decompose(cells[c], sched[c]);
+  parallel_for(s.n_cells, [&](int64_t c) { decompose(cells[c], sched[c]); });
   // ---------------------------------------------------- tile packing
   const size_t rs = p->real_size;
   const size_t smem_cap = dry ? size_t(232448) : max_optin_smem(opts.device);

@@ -183,3 +183,34 @@ def test_mechanism_probe_selects_the_extra_variant():
     p = _probe_plan([Channel("Na_Ba2002")], _abi.BC_STATE_NA_P)
     assert p.info["kernel_variant"] == _abi.BC_VARIANT_EXTRA
     p.close()
+
+
+def test_threaded_planner_matches_sequential(monkeypatch):
+    # cells lower and decompose on host threads (BC_PLAN_THREADS); the plan must not
+    # depend on how many
+    b = W.descs_to_batch(W.uneven(700))
+    kw = dict(precision="f32", tile_nodes=2500, threads_per_tile=512, threads_big=512, dry_run=True)
+    out = []
+    for n in ("1", "3", "8"):
+        monkeypatch.setenv("BC_PLAN_THREADS", n)
+        p = Plan(b, **kw)
+        out.append((p.info, p.tile_stats()))
+        p.close()
+    for info, stats in out[1:]:
+        assert info == out[0][0]
+        np.testing.assert_array_equal(stats, out[0][1])
+
+
+def test_threaded_planner_reports_the_first_failing_cell(monkeypatch):
+    b = W.descs_to_batch(W.uneven(700))
+    for c in (300, 650):  # a child listed before its parent in two cells
+        k = int(b.cell_branch_offsets[c])
+        assert int(b.cell_branch_offsets[c + 1]) - k >= 3
+        b.branch_parent[k + 1] = 2
+    msgs = []
+    for n in ("1", "8"):
+        monkeypatch.setenv("BC_PLAN_THREADS", n)
+        with pytest.raises(_abi.BCError, match="cell 300") as e:
+            Plan(b, dry_run=True)
+        msgs.append(str(e.value))
+    assert msgs[0] == msgs[1]
