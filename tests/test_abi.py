@@ -75,3 +75,13 @@ def test_invalid_spec_is_rejected_on_host(native_lib):
 def test_null_plan_arguments(native_lib):
     assert native_lib.bc_plan_destroy(None) == _abi.BC_ERR_INVALID
     assert native_lib.bc_run(None, 1, 0.025, None) == _abi.BC_ERR_INVALID
+
+
+def test_loader_refuses_another_abi_version(native_lib, monkeypatch):
+    # a library whose records are laid out for another version must not be used
+    monkeypatch.setattr(_abi, "_lib", None)
+    monkeypatch.setattr(_abi, "BC_ABI_VERSION", _abi.BC_ABI_VERSION + 1)
+    with pytest.raises(ImportError, match="ABI version"):
+        _abi.lib()
+    monkeypatch.undo()
+    assert _abi.lib() is not None and _abi.lib().bc_version() == _abi.BC_ABI_VERSION
