@@ -58,7 +58,8 @@ def build_native(force: bool = False, verbose: bool = False, debug: bool = False
     lib_path = out or LIB
     srcs = [os.path.join(CSRC, s) for s in SOURCES]
     deps = srcs + [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith((".h", ".cuh"))]
-    deps.append(os.path.join(HERE, "..", "include", "braincell_gb300.h"))
+    inc = os.path.join(HERE, "..", "include")
+    deps += [os.path.join(inc, h) for h in os.listdir(inc) if h.endswith(".h")]
     if not force and os.path.exists(lib_path):
         lib_m = os.path.getmtime(lib_path)
         if all(os.path.getmtime(d) <= lib_m for d in deps if os.path.exists(d)):

@@ -24,6 +24,7 @@
 #include <thread>
 #include <vector>
 
+#include "../../include/braincell_gb300_debug.h"
 #include "bc_internal.h"
 #include "bc_mech.cuh"
 
@@ -218,7 +219,9 @@ struct CellSched {
 
 // fn(i) for i in [0, n) on up to BC_PLAN_THREADS host threads (default: the
 // hardware threads, at most 32), in chunks of 64 items; one thread when n is
-// small.  fn must touch only item i's outputs.
+// small.  fn must touch only item i's outputs and must not throw.  When a
+// worker thread cannot be started, the threads already running (and the
+// calling thread) take its share: the items are claimed from one counter.
 template <class F>
 static void parallel_for(int64_t n, F&& fn) {
   int64_t nt = int64_t(std::thread::hardware_concurrency());
@@ -237,7 +240,12 @@ static void parallel_for(int64_t n, F&& fn) {
     }
   };
   std::vector<std::thread> pool;
-  for (int64_t t = 1; t < nt; ++t) pool.emplace_back(work);
+  try {
+    pool.reserve(size_t(nt - 1));
+    for (int64_t t = 1; t < nt; ++t) pool.emplace_back(work);
+  } catch (const std::exception&) {
+    // std::system_error (no thread) or bad_alloc: carry on with what started
+  }
   work();
   for (auto& th : pool) th.join();
 }
@@ -1389,7 +1397,24 @@ bc_status bc_plan_create(const bc_batch_spec* spec, const bc_plan_options* opts_
   }
   // ---------------------------------------------------- schedules
   std::vector<CellSched> sched(s.n_cells);
-  parallel_for(s.n_cells, [&](int64_t c) { decompose(cells[c], sched[c]); });
+  {
+    // as for the lowering: per-cell outcomes, the first failing cell reported
+    std::vector<std::string> dmsg(s.n_cells);
+    std::vector<char> dbad(s.n_cells, 0);
+    parallel_for(s.n_cells, [&](int64_t c) {
+      try {
+        decompose(cells[c], sched[c]);
+      } catch (const std::exception& ex) {
+        dbad[c] = 1;
+        dmsg[c] = std::string("scheduling cell ") + std::to_string(c) + ": " + ex.what();
+      }
+    });
+    for (int64_t c = 0; c < s.n_cells; ++c)
+      if (dbad[c]) {
+        delete p;
+        return fail(BC_ERR_CAPACITY, dmsg[c]);
+      }
+  }
   // ---------------------------------------------------- tile packing
   const size_t rs = p->real_size;
   const size_t smem_cap = dry ? size_t(232448) : max_optin_smem(opts.device);
@@ -2110,6 +2135,13 @@ bc_status bc_state_download_noalloc(bc_plan_t p, int32_t which, double* out, voi
                                     " (BC_NOALLOC_MAX_CV); use bc_state_download");
   BC_NEED_DEVICE(p);
   BC_CUDA(cudaSetDevice(p->device));
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  // The call copies from pageable host memory and synchronises the stream, and
+  // neither is allowed while the stream is being captured into a graph.
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  BC_CUDA(cudaStreamIsCapturing(s, &cap));
+  if (cap != cudaStreamCaptureStatusNone)
+    return fail(BC_ERR_INVALID, "bc_state_download_noalloc: the stream is being captured; call it outside capture");
   unsigned char* scratch = nullptr;
   bc_status st = noalloc_scratch(p->device, &scratch);
   if (st != BC_OK) return st;
@@ -2124,13 +2156,23 @@ bc_status bc_state_download_noalloc(bc_plan_t p, int32_t which, double* out, voi
   int64_t* d_hi = reinterpret_cast<int64_t*>(scratch);
   int64_t* d_lo = d_hi + BC_NOALLOC_MAX_CV;
   double* d_val = reinterpret_cast<double*>(d_lo + BC_NOALLOC_MAX_CV);
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
-  BC_CUDA(cudaMemcpyAsync(d_hi, h_hi, size_t(n) * 8, cudaMemcpyHostToDevice, s));
-  BC_CUDA(cudaMemcpyAsync(d_lo, h_lo, size_t(n) * 8, cudaMemcpyHostToDevice, s));
+  // Once something is enqueued, every return waits for the stream first, so that
+  // no copy or kernel of this call still uses the shared scratch when the next,
+  // serialised call (perhaps on another stream) writes it.
+  auto failed = [&](const std::string& what, cudaError_t e) {
+    (void)cudaStreamSynchronize(s);
+    return fail(BC_ERR_CUDA, what + ": " + cudaGetErrorString(e));
+  };
+  cudaError_t e = cudaMemcpyAsync(d_hi, h_hi, size_t(n) * 8, cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) return failed("offset upload", e);
+  e = cudaMemcpyAsync(d_lo, h_lo, size_t(n) * 8, cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) return failed("offset upload", e);
   const int ke = launch_view_impl(p->d_blob, p->d_state, p->precision, d_hi, d_lo, d_val, n, false, stream);
-  if (ke) return fail(BC_ERR_CUDA, std::string("view kernel: ") + cudaGetErrorString(cudaError_t(ke)));
-  BC_CUDA(cudaMemcpyAsync(out, d_val, size_t(n) * 8, cudaMemcpyDeviceToHost, s));
-  BC_CUDA(cudaStreamSynchronize(s));
+  if (ke) return failed("view kernel", cudaError_t(ke));
+  e = cudaMemcpyAsync(out, d_val, size_t(n) * 8, cudaMemcpyDeviceToHost, s);
+  if (e != cudaSuccess) return failed("value download", e);
+  e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return fail(BC_ERR_CUDA, std::string("cudaStreamSynchronize: ") + cudaGetErrorString(e));
   return BC_OK;
 }
 

@@ -390,10 +390,12 @@ bc_status bc_state_upload(bc_plan_t plan, int32_t which, const double* in /* [n_
  * sized for BC_NOALLOC_MAX_CV compartments (24 bytes each on the device: 6 MiB).
  * Plans with more CVs are rejected with BC_ERR_INVALID (use bc_state_download).
  * The first call on each device looks up the scratch address (cudaGetSymbolAddress)
- * and caches it; make that first call before any stream capture begins.  The
- * scratch is shared by every plan of the process: calls that overlap in time (from
- * several host threads) race on it, so the caller must serialise them.  Returns
- * once `out` holds the values (the stream is synchronised). */
+ * and caches it.  Never call it on a stream that is being captured into a CUDA
+ * graph: it copies from pageable host memory and synchronises the stream, so it
+ * returns BC_ERR_INVALID there.  The scratch is shared by every plan of the
+ * process: calls that overlap in time (from several host threads) race on it, so
+ * the caller must serialise them.  Returns once `out` holds the values (the stream
+ * is synchronised, on failures too once anything was enqueued). */
 #define BC_NOALLOC_MAX_CV 262144
 bc_status bc_state_download_noalloc(bc_plan_t plan, int32_t which, double* out /* [n_cv] */, void* stream);
 
@@ -454,11 +456,6 @@ bc_status bc_gru_grad_sqnorm(const float* grads, float* out, void* stream);
    clears grads.                                                                */
 bc_status bc_gru_adam(float* params, float* grads, float* m, float* v, int64_t step, float lr, float beta1,
                       float beta2, float eps, float clip_scale, void* stream);
-
-/* Diagnostics: cycles summed over CTAs (as seen by each CTA's first thread) in
- * forward elimination, back-substitution, node update and probes/pulses.  Only a
- * library compiled with -DBC_PHASE_TIMERS records them; otherwise all zero. */
-bc_status bc_debug_phase_cycles(bc_plan_t plan, uint64_t* out4, int32_t reset);
 
 /* Current step counter (number of steps taken since reset). */
 bc_status bc_step_count(bc_plan_t plan, int64_t* steps);

@@ -12,6 +12,7 @@ from braincell_gb300 import _abi
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 HEADER = os.path.join(ROOT, "include", "braincell_gb300.h")
+INCLUDE = os.path.join(ROOT, "include")
 
 
 def _header_text():
@@ -19,8 +20,19 @@ def _header_text():
 
 
 def declared_functions():
-    txt = _header_text()
-    return sorted(set(re.findall(r"^\s*(?:bc_status|const char\*|int32_t|void)\s+(bc_[a-z0-9_]+)\s*\(", txt, re.M)))
+    """Entry points declared in every header under include/ (the stable ABI and the
+    tuning-diagnostics header)."""
+    names = set()
+    for fn in sorted(os.listdir(INCLUDE)):
+        if fn.endswith(".h"):
+            txt = open(os.path.join(INCLUDE, fn)).read()
+            names |= set(re.findall(r"^\s*(?:bc_status|const char\*|int32_t|void)\s+(bc_[a-z0-9_]+)\s*\(", txt, re.M))
+    return sorted(names)
+
+
+def test_debug_entry_points_stay_out_of_the_stable_header():
+    assert "bc_debug_phase_cycles" not in _header_text()
+    assert "bc_debug_phase_cycles" in declared_functions()
 
 
 def test_every_declared_symbol_is_exported(native_lib):
