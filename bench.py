@@ -9,8 +9,10 @@ staggered steps), FP32 with float-float voltage.  One benchmark "step" is one
 full 200 ms simulation of all 10,000 cells from reset.  Inputs are generated
 (seeded), there is no dataset.
 
-``python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]``
-prints one JSON line.  Under torchrun (N > 1) every rank simulates its own copy of
+``python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+[--workload uneven|large]`` prints one JSON line.  ``--workload large`` measures the
+large-cell configuration instead (256 cells of 10,000-20,000 compartments with
+dynamic calcium, 4,000 steps; one bench step is one 100 ms simulation).  Under torchrun (N > 1) every rank simulates its own copy of
 the workload (replicas only: cells are independent, no data-path collective) and
 rank 0 prints the aggregate.
 """
@@ -34,9 +36,20 @@ import numpy as np  # noqa: E402
 
 METRIC = "compartment-steps/s on 1 GB300, plain vs surrogate at <=0.1 ms spike-time error"
 UNIT = "compartment-steps/s"
-BYTES_PER_COMPARTMENT_STEP = 56  # state read+written per compartment-step by a per-step kernel (V, gates, Ca, coefficients)
 DT = 0.025
-SIM_STEPS = 8000
+# Per workload: generator, default size, simulated steps and the algorithmic bytes of
+# one compartment-step (8 B per mutable FP32 word read and written, 4 B per static
+# word read: uneven 5 mutable (V, V_lo, CaL p, q, HCN p) + 4 static (parent, alpha,
+# beta, d0) = 56 B; large adds Ci, Ci_lo, CaT p, q, AHP p = 96 B).
+WORKLOADS = {
+    "uneven": dict(cells=10000, seed=1, sim_steps=8000, bytes=56,
+                   text="uneven-morphology batch: 10,000 cells, 50-2000 compartments, 200 ms at dt 0.025 ms "
+                        "(8,000 staggered steps), FP32 + float-float V"),
+    "large": dict(cells=256, seed=2, sim_steps=4000, bytes=96,
+                  text="large cells: 256 cells of 10,000-20,000 compartments on ~300 branches, CalciumDetailed + "
+                       "CaT + AHP dendrites, 500 Poisson pulses per cell, 100 ms at dt 0.025 ms (4,000 steps), "
+                       "FP32 + float-float V and Ci"),
+}
 
 
 def _args():
@@ -45,8 +58,9 @@ def _args():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--cells", type=int, default=10000)
-    ap.add_argument("--sim-steps", type=int, default=SIM_STEPS)
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="uneven")
+    ap.add_argument("--cells", type=int, default=None)
+    ap.add_argument("--sim-steps", type=int, default=None)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--tile-nodes", type=int, default=2500)
     ap.add_argument("--threads", type=int, default=512)
@@ -57,7 +71,21 @@ def _args():
     ap.add_argument("--surrogate-threads", type=int, default=384)
     ap.add_argument("--surrogate-tile-nodes", type=int, default=1800)
     ap.add_argument("--accuracy-cells", type=int, default=300)
-    return ap.parse_args()
+    a = ap.parse_args()
+    wl = WORKLOADS[a.workload]
+    a.cells = wl["cells"] if a.cells is None else a.cells
+    a.sim_steps = wl["sim_steps"] if a.sim_steps is None else a.sim_steps
+    if a.workload != "uneven":
+        a.no_surrogate = True  # the surrogate is trained on the uneven family
+    return a
+
+
+def _descs(workload, n, seed=None, indices=None):
+    from braincell_gb300 import workloads as W
+
+    make = {"uneven": W.uneven, "large": W.large}[workload]
+    seed = WORKLOADS[workload]["seed"] if seed is None else seed
+    return make(n, seed=seed) if indices is None else make(seed=seed, indices=list(indices))
 
 
 def _dist():
@@ -76,15 +104,18 @@ def _peaks():
         return 6800.0, "fallback"
 
 
-def _traffic_per_node_launch():
+def _traffic_per_node_launch(workload):
     """Measured DRAM bytes per tile node per launch (ncu summary under profiles/), if present.
 
-    A launch stages each tile's blob into shared memory once and writes V back once,
-    whatever number of steps it fuses, so its traffic scales with the nodes it holds.
+    Uneven workload: a launch stages each tile's blob into shared memory once and
+    writes V back once, whatever number of steps it fuses, so its traffic scales
+    with the nodes it holds.  Large workload: global-memory tiles, whose traffic per
+    launch scales with nodes x fused steps; the summary gives it per node and step.
     """
+    name = {"uneven": "tile_step_uneven.json", "large": "tile_step_large.json"}[workload]
     try:
-        with open(os.path.join(ROOT, "profiles", "tile_step_uneven.json")) as f:
-            return float(json.load(f)["dram_bytes_per_node_per_launch"])
+        with open(os.path.join(ROOT, "profiles", name)) as f:
+            return json.load(f)
     except Exception:
         return None
 
@@ -164,19 +195,20 @@ def _cpu_model() -> str:
     return f"{name or platform.processor() or 'unknown'} ({platform.machine()}, {os.cpu_count()} logical cores)"
 
 
-def _oracle_cells(indices, seed=1):
+def _oracle_cells(indices, workload="uneven"):
     from braincell_gb300 import workloads as W
     from oracle.staggered import OracleCell
 
-    return [OracleCell(W.desc_to_cell(d)) for d in W.uneven(indices=list(indices), seed=seed)]
+    return [OracleCell(W.desc_to_cell(d)) for d in _descs(workload, 0, indices=indices)]
 
 
-def cpu_baseline(cells: int = 8, steps: int = 1000, seed: int = 1):
+def cpu_baseline(workload="uneven"):
     """The float64 oracle (one core) on a bounded sample of the same workload: the
     cells are built (lowering, assembly, scheduling) before the clock starts, and
     only their time steps are timed."""
+    cells, steps = (8, 1000) if workload == "uneven" else (1, 500)
     t0 = time.perf_counter()
-    oc = _oracle_cells(range(cells), seed)
+    oc = _oracle_cells(range(cells), workload)
     setup = time.perf_counter() - t0
     ncv = sum(c.n_cv for c in oc)
     t0 = time.perf_counter()
@@ -190,10 +222,10 @@ def cpu_baseline(cells: int = 8, steps: int = 1000, seed: int = 1):
             "setup_s_untimed": round(setup, 3), "timed_s": round(el, 3), "cpu": _cpu_model()}
 
 
-def _reference_worker(conn, indices, seed):
+def _reference_worker(conn, indices, workload):
     """One process of the reference arm: builds its cells once, then advances them
     by the requested number of steps per message and answers with the work done."""
-    cells = _oracle_cells(indices, seed)
+    cells = _oracle_cells(indices, workload)
     conn.send(sum(c.n_cv for c in cells))
     while True:
         steps = conn.recv()
@@ -220,9 +252,9 @@ def run_reference(a):
     if rank != 0:
         return
     cores = os.cpu_count() or 1
-    steps_per = 200
-    n_cells = 4 * cores
-    sizes = [sum(d.ncv) for d in W.uneven(indices=range(n_cells))]
+    steps_per = 200 if a.workload == "uneven" else 20
+    n_cells = 4 * cores if a.workload == "uneven" else cores
+    sizes = [sum(d.ncv) for d in _descs(a.workload, 0, indices=range(n_cells))]
     shares = [[] for _ in range(cores)]
     load = [0] * cores
     for i in sorted(range(n_cells), key=lambda i: -sizes[i]):
@@ -234,7 +266,7 @@ def run_reference(a):
     t0 = time.perf_counter()
     for k in range(cores):
         here, there = ctx.Pipe()
-        pr = ctx.Process(target=_reference_worker, args=(there, shares[k], 1), daemon=True)
+        pr = ctx.Process(target=_reference_worker, args=(there, shares[k], a.workload), daemon=True)
         pr.start()
         pipes.append(here)
         procs.append(pr)
@@ -264,8 +296,7 @@ def run_reference(a):
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": a.gpus, "steps": a.steps,
         "warmup": a.warmup, "ms_per_step": 1e3 * el / a.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "uneven-morphology batch (10,000 cells, 50-2000 compartments, 200 ms at dt 0.025 ms)",
-                   "sample": sample},
+        "config": {"workload": WORKLOADS[a.workload]["text"], "sample": sample},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample,
                          "cpu": _cpu_model()},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -286,6 +317,102 @@ def _spike_errors(sp, ref):
         if k:
             errs.extend(np.abs(np.asarray(x[:k]) - np.asarray(y[:k])).tolist())
     return np.asarray(errs), mis
+
+
+def _first_crossing(trace):
+    """Index of the first step at which the voltage reaches 0 mV from below (trace
+    length if it never does)."""
+    hit = np.nonzero((trace[1:] >= 0.0) & (trace[:-1] < 0.0))[0]
+    return int(hit[0]) + 1 if hit.size else trace.size
+
+
+def _onset(trace, dvdt=10.0):
+    """Index of the first step whose voltage rate exceeds dvdt mV/ms (trace length if none)."""
+    hit = np.nonzero(np.diff(trace) / DT > dvdt)[0]
+    return int(hit[0]) + 1 if hit.size else trace.size
+
+
+def _upstroke(trace, dvdt=10.0):
+    """Start of the first spike's upstroke: the last step before the first 0 mV
+    crossing whose voltage rate was at most dvdt mV/ms (trace length if no spike)."""
+    k = _first_crossing(trace)
+    if k >= trace.size:
+        return trace.size
+    calm = np.nonzero(np.diff(trace[:k]) / DT <= dvdt)[0]
+    return int(calm[-1]) + 1 if calm.size else 0
+
+
+def plain_accuracy(a, descs, local, n_oracle=2):
+    """Accuracy of the plain solve, judged by the target's own words.
+
+    * FP32 against the FP64 build of the same kernels (the on-GPU oracle run) on the
+      first ``a.accuracy_cells`` cells for the whole simulation: the largest soma
+      |dV| before the first 0 mV crossing (and, for reference, before the dV/dt >
+      10 mV/ms onset), spike-time differences of paired spikes and the cells whose
+      spike counts differ.
+    * FP64 against the float64 CPU oracle on ``n_oracle`` cells, whole simulation:
+      the largest |dV| over the soma trace, spikes included.
+    """
+    from dataclasses import replace
+
+    from braincell_gb300 import workloads as W
+    from braincell_gb300.runtime import Plan
+
+    n = min(a.accuracy_cells, len(descs))
+    sub = [replace(d, probes=[(0, 0.5)]) for d in descs[:n]]
+    out = {"cells": n, "steps": a.sim_steps}
+    runs = {}
+    for prec in ("f32", "f64"):
+        p = Plan(W.descs_to_batch(sub), precision=prec, device=local, record_every=1, max_spikes=256)
+        p.run(a.sim_steps, DT)
+        runs[prec] = (p.traces(), p.spikes())
+        p.close()
+    (t32, s32), (t64, s64) = runs["f32"], runs["f64"]
+    to_cross, to_onset, to_up, gap = [], [], [], []
+    for c in range(n):
+        k = _first_crossing(t64[c])
+        j = _onset(t64[c])
+        u = _upstroke(t64[c])
+        to_cross.append(float(np.abs(t32[c, :k] - t64[c, :k]).max()) if k else 0.0)
+        to_onset.append(float(np.abs(t32[c, :j] - t64[c, :j]).max()) if j else 0.0)
+        to_up.append(float(np.abs(t32[c, :u] - t64[c, :u]).max()) if u else 0.0)
+        if k < t64.shape[1]:
+            gap.append(k - j)
+    to_up = np.asarray(to_up)
+    e, mis = _spike_errors(s32, s64)
+    to_cross = np.asarray(to_cross)
+    out["fp32_vs_fp64_gpu"] = {
+        "max_abs_dv_before_first_crossing_mV": float(to_cross.max()),
+        "median_abs_dv_before_first_crossing_mV": float(np.median(to_cross)),
+        "cells_within_1e-3_mV_to_first_crossing": int((to_cross <= 1e-3).sum()),
+        "max_abs_dv_before_first_upstroke_mV": float(to_up.max()),
+        "cells_within_1e-3_mV_to_first_upstroke": int((to_up <= 1e-3).sum()),
+        "max_abs_dv_before_onset_mV": float(max(to_onset)),
+        "onset_to_crossing_steps": {"median": float(np.median(gap)) if gap else None,
+                                    "max": int(max(gap)) if gap else None},
+        "spike_time_diff_ms": {"max": float(e.max()) if e.size else None,
+                               "median": float(np.median(e)) if e.size else None,
+                               "spikes_paired": int(e.size),
+                               "within_0.05_ms": int((e <= 0.05).sum()) if e.size else 0},
+        "cells_with_spike_count_mismatch": mis,
+        "spiking_cells": int(sum(1 for x in s64 if len(x))),
+    }
+    if n_oracle:
+        from oracle.staggered import OracleCell
+
+        worst, sp_worst = 0.0, 0.0
+        for c in range(min(n_oracle, n)):
+            oc = OracleCell(W.desc_to_cell(sub[c]))
+            otr, osp = oc.run(DT, a.sim_steps)
+            worst = max(worst, float(np.abs(otr[0, 0] - t64[c]).max()))
+            ref = np.asarray(osp[0][0])
+            if len(ref) != len(s64[c]):
+                sp_worst = float("inf")
+            elif len(ref):
+                sp_worst = max(sp_worst, float(np.abs(ref - s64[c]).max()))
+        out["fp64_gpu_vs_cpu_oracle"] = {"cells": min(n_oracle, n), "max_abs_dv_whole_run_mV": worst,
+                                         "spike_time_diff_max_ms": sp_worst}
+    return out
 
 
 def surrogate_leg(a, descs, local, sid, stream, plain_ms):
@@ -372,7 +499,8 @@ def run_ours(a):
     torch.cuda.set_device(local)
     build_native()
     # replicas only: every rank runs its own copy of the workload (its own seed)
-    descs = W.uneven(a.cells, seed=1 + rank)
+    descs = _descs(a.workload, a.cells, seed=WORKLOADS[a.workload]["seed"] + rank)
+    nbytes = WORKLOADS[a.workload]["bytes"]
     batch = W.descs_to_batch(descs)
     plan = Plan(batch, precision="f32", device=local, tile_nodes=a.tile_nodes, threads_per_tile=a.threads,
                 threads_big=a.threads_big, steps_per_launch=a.steps_per_launch, record_every=0,
@@ -438,15 +566,19 @@ def run_ours(a):
     d2h = 8 * n_cv + 4 * int(counts.size)
 
     peak, peak_kind = _peaks()
-    achieved_gbs = BYTES_PER_COMPARTMENT_STEP * n_cv * a.sim_steps / (kernel_ms * 1e-3) / 1e9
-    traffic_per_node = _traffic_per_node_launch()
+    achieved_gbs = nbytes * n_cv * a.sim_steps / (kernel_ms * 1e-3) / 1e9
     units_per_launch = n_cv * info["steps_per_launch"]
+    prof = _traffic_per_node_launch(a.workload)
+    traffic = None
+    if prof and "dram_bytes_per_node_per_launch" in prof:
+        traffic = prof["dram_bytes_per_node_per_launch"] * info["n_nodes"]
+    elif prof and "dram_bytes_per_node_step" in prof:
+        traffic = prof["dram_bytes_per_node_step"] * info["n_nodes"] * info["steps_per_launch"]
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
         "ms_per_step": ms / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded generator; no dataset)",
-        "config": {"workload": "uneven-morphology batch: 10,000 cells, 50-2000 compartments, 200 ms at dt 0.025 ms "
-                               "(8,000 staggered steps), FP32 + float-float V",
+        "config": {"workload": WORKLOADS[a.workload]["text"],
                    "cells_per_gpu": a.cells, "compartments_per_gpu": n_cv, "sim_steps": a.sim_steps,
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                    "l2": "inputs larger than L2 (tile blobs + state arrays > 129 MB)",
@@ -454,23 +586,28 @@ def run_ours(a):
                    "tile_nodes": info["tile_nodes"], "steps_per_launch": info["steps_per_launch"],
                    "lane_nodes": a.lane_nodes},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d_total), "d2h_bytes_per_step": int(d2h),
-                "path": "bc_state_upload (V) -> bc_run (8,000 steps) -> bc_state_download (V) + bc_spike_download"},
+                "path": f"bc_state_upload (V) -> bc_run ({a.sim_steps:,} steps) -> bc_state_download (V) + "
+                        "bc_spike_download"},
         "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": peak, "unit": "GB/s",
                      "frac": achieved_gbs / peak, "peak_kind": peak_kind,
-                     "traffic": (traffic_per_node * info["n_nodes"]) if traffic_per_node else None,
-                     "algorithmic_bytes_per_launch": BYTES_PER_COMPARTMENT_STEP * units_per_launch,
+                     "traffic": traffic, "bytes_per_compartment_step": nbytes,
+                     "algorithmic_bytes_per_launch": nbytes * units_per_launch,
                      "kernel_ms_per_sim": kernel_ms, "launches_per_sim": launches_per_sim},
         "gpu_launches": a.steps * (1 + launches_per_sim),
         "clocks": clocks.summary(),
         "wall_s_timed": t_wall,
     }
+    if a.accuracy_cells:
+        # the float64 CPU oracle takes ~16 ms per step of one large cell: the large
+        # workload's CPU-oracle parity is in the tests (1,000 steps of a full-size cell)
+        line["plain_accuracy"] = plain_accuracy(a, descs, local, n_oracle=2 if a.workload == "uneven" else 0)
     if not a.no_surrogate:
         sur = surrogate_leg(a, descs, local, sid, stream, ms / a.steps)
         sur["value"] = sur["value"] * world  # every rank runs its own replica
         line["surrogate"] = sur
         line["gpu_launches"] += a.steps * sur["gpu_launches_per_step"]
     if rank == 0 and world == 1 and not a.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline()
+        line["cpu_baseline"] = cpu_baseline(a.workload)
     if rank == 0:
         print(json.dumps(line), flush=True)
     plan.close()

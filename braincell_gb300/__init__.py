@@ -6,6 +6,7 @@ Public surface (mirrors the reference's names on this path):
 * declarations -- ``mech`` (CableProperty, Channel, Ion, CurrentClamp, StateProbe,
   regions / locsets, CV policies)
 * :class:`Cell` -- paint / place / init_state / reset_state / update / run
+* :class:`SingleCompartment` -- point neurons, ``update(I_ext)`` per step
 * ``quad`` -- integrator registry with ``"gb300_staggered"`` registered
 * :class:`CellBatch` / :class:`Plan` -- many heterogeneous cells in one device plan
 """
@@ -15,6 +16,7 @@ from .batch import CellBatch, concat_batches, lower_cell
 from .cell import Cell, RunResult
 from .morph import Branch, Morphology
 from .runtime import Plan
+from .single import SingleCompartment
 
 __all__ = [
     "Branch",
@@ -23,6 +25,7 @@ __all__ = [
     "RunResult",
     "CellBatch",
     "Plan",
+    "SingleCompartment",
     "concat_batches",
     "lower_cell",
     "environ",

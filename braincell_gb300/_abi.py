@@ -107,7 +107,7 @@ BC_P_KNI_VSH = 61
 BC_P_KNI_PHI = 62
 BC_P_KNI_TAUMAX = 63
 
-BC_ABI_VERSION = 200
+BC_ABI_VERSION = 300
 
 BC_VARIANT_LEAN = 0
 BC_VARIANT_EXTRA = 1
@@ -166,7 +166,8 @@ BC_STATE_KK2A_Q = 20
 BC_STATE_KK2B_P = 21
 BC_STATE_KK2B_Q = 22
 BC_STATE_KNI_P = 23
-BC_NSTATE_VIEW = 24
+BC_STATE_V_LAST = 24
+BC_NSTATE_VIEW = 25
 BC_NOALLOC_MAX_CV = 262144
 
 STATE_NAMES = {
@@ -194,6 +195,7 @@ STATE_NAMES = {
     "KK2B_p": BC_STATE_KK2B_P,
     "KK2B_q": BC_STATE_KK2B_Q,
     "KNI_p": BC_STATE_KNI_P,
+    "V_last": BC_STATE_V_LAST,
 }
 
 _p = C.POINTER
@@ -325,6 +327,8 @@ SIGNATURES = {
     "bc_state_download": (C.c_int32, [C.c_void_p, C.c_int32, _p(C.c_double), C.c_void_p]),
     "bc_state_upload": (C.c_int32, [C.c_void_p, C.c_int32, _p(C.c_double), C.c_void_p]),
     "bc_state_download_noalloc": (C.c_int32, [C.c_void_p, C.c_int32, _p(C.c_double), C.c_void_p]),
+    "bc_spike_state_download": (C.c_int32, [C.c_void_p, C.c_double, _p(C.c_double), C.c_void_p]),
+    "bc_pulse_set_amp": (C.c_int32, [C.c_void_p, _p(C.c_double), C.c_void_p]),
     "bc_network_spikes": (C.c_int32, [C.c_void_p, _p(C.c_int32), _p(C.c_int64), C.c_int64, _p(C.c_int64), C.c_void_p]),
     "bc_synapse_download": (C.c_int32, [C.c_void_p, _p(C.c_double), C.c_void_p]),
     "bc_probe_count": (C.c_int32, [C.c_void_p, _p(C.c_int64)]),

@@ -172,11 +172,10 @@ class Cell:
             self.init_state()
         if environ.get("dt", None) is None:
             raise ValueError("Cell.update(...) requires environ['dt'] to be set.")
-        last_V = self.V
         self.solver(self)
-        V = self.V
-        spk = ((V - self.V_th) >= 0.0) & ((self.V_th - last_V) > 0.0)
-        self.spike = spk.astype(np.float64)
+        # get_spike(last_V, V) per CV (_base.py:421-431), from the voltage the device
+        # kept at the start of the step
+        self.spike = self._runtime.spike_state(self.V_th).reshape(self.varshape)
         return self.spike
 
     def run(self, *, dt: float, duration: float) -> RunResult:
@@ -194,6 +193,8 @@ class Cell:
             raise TypeError("The selected solver provides no batch runner for Cell.run().")
         t0 = self.current_time if environ.get("dt", None) == dt else self._runtime.step_count * dt
         traces = runner(self, n_steps=n_steps, dt=dt)  # [n_probe_total, n_steps]
+        # Cell.spike holds the last step's per-CV indicator, as after n calls of update()
+        self.spike = self._runtime.spike_state(self.V_th).reshape(self.varshape)
         P = int(np.prod(self.pop_size))
         nprobe = len(names)
         tr = traces.reshape(P, nprobe, -1)

@@ -1535,6 +1535,10 @@ __global__ void __launch_bounds__(kVar == 2 ? BC_PORT_MAX_THREADS : 1024, kVar =
       const Real v_old = hi, lo_old = lo;
       ff_add(hi, lo, tv.dr[i].y);
       tv.v[i] = make_pair(hi, lo);
+      if (last) {  // last_V of the per-CV spike indicator (cell.py:2384-2386)
+        tv.state[size_t(kSlotVLastHi) * tv.N + i] = v_old;
+        tv.state[size_t(kSlotVLastLo) * tv.N + i] = lo_old;
+      }
       if (!is_finite_real(hi)) s_status = kStatusNonfinite;
       const uint16_t pr = pr_cur;
       Real G = Real(0), I = Real(0);
@@ -1651,6 +1655,8 @@ __global__ void reset_kernel(LaunchArgs a, const double* vinit, const int64_t* v
   for (int i = threadIdx.x; i < tv.n_real; i += blockDim.x) {
     const Real v = Real(vi[i]);
     tv.v[i] = make_pair(v, Real(0));
+    tv.state[size_t(kSlotVLastHi) * tv.N + i] = v;  // no step taken: no crossing
+    tv.state[size_t(kSlotVLastLo) * tv.N + i] = Real(0);
     const uint16_t pr = tv.pidx[i];
     if (pr == kBoundary) continue;
     const Real* P = tv.params + size_t(pr) * BC_NPARAM;

@@ -250,7 +250,11 @@ constexpr int kSlotKK2AQ = 20;
 constexpr int kSlotKK2BP = 21;
 constexpr int kSlotKK2BQ = 22;
 constexpr int kSlotKNIP = 23;
-constexpr int kNumSlots = 24;
+// membrane voltage at the start of the last step taken (float-float), written on
+// the last step of every launch: the `last_V` of the per-CV spike indicator
+constexpr int kSlotVLastHi = 24;
+constexpr int kSlotVLastLo = 25;
+constexpr int kNumSlots = 26;
 
 constexpr double kFaraday = 96485.33212;   // C/mol
 constexpr double kGasR = 8.314462618;      // J/(mol K)

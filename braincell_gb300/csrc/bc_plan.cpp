@@ -83,6 +83,8 @@ struct bc_plan {
   std::vector<int32_t> cv_tile, cv_node;
   std::vector<uint32_t> cv_mech;
   std::vector<bc::PulseRec> pulses;
+  std::vector<int64_t> pulse_src;   // spec pulse id of each record (records are in tile / node order)
+  std::vector<double> pulse_scale;  // record amp per nA
   double pulses_dt = -1.0;
   std::vector<double> probe_vrest;
   // synapses and connections (host copies; device mirrors below)
@@ -329,6 +331,8 @@ struct TileOut {
   std::vector<unsigned char> blob;
   std::vector<double> vinit;
   std::vector<PulseRec> pulses;
+  std::vector<int64_t> pulse_src;     // spec pulse id of each pulse record
+  std::vector<double> pulse_scale;    // record amp per nA of the spec pulse
   std::vector<PortRec> ports;         // stim_begin / stim_end relative to port_pulses
   std::vector<PulseRec> port_pulses;  // amp in nA
   std::vector<std::pair<int64_t, int32_t>> cv_local;  // (global cv id, local node)
@@ -742,13 +746,15 @@ static bc_status build_tile(const BuildCtx& cx, const TileBuild& tb, int T, Tile
               area = lc.cv_area[k];
               break;
             }
-          pr.amp = s.pulse_amp[pid] * 1e5 / area;  // uA/cm^2
+          out.pulse_scale.push_back(1e5 / area);  // nA -> uA/cm^2
         } else {
-          pr.amp = s.pulse_amp[pid] * 1e-3;  // mV/ms on a row with the 1 uF dummy capacitance
+          out.pulse_scale.push_back(1e-3);  // nA -> mV/ms on a row with the 1 uF dummy capacitance
         }
+        pr.amp = s.pulse_amp[pid] * out.pulse_scale.back();
         pr.t_on = s.pulse_t_on[pid];
         pr.t_off = s.pulse_t_off[pid];
         out.pulses.push_back(pr);
+        out.pulse_src.push_back(pid);
         ++kp;
       }
       specs[q].pulse_end = int32_t(out.pulses.size());
@@ -1237,9 +1243,9 @@ bc_status bc_plan_create(const bc_batch_spec* spec, const bc_plan_options* opts_
     }
     const int32_t field = s.probe_field ? s.probe_field[k] : BC_STATE_V;
     const bool is_current = field >= BC_PROBE_CURRENT && field < BC_PROBE_CURRENT + BC_NCUR;
-    if (!is_current && (field < 0 || field >= BC_NSTATE_VIEW)) {
+    if (!is_current && (field < 0 || field >= BC_NSTATE_VIEW || field == BC_STATE_V_LAST)) {
       delete p;
-      return fail(BC_ERR_INVALID, "probe_field is not a BC_STATE_* view or a BC_PROBE_CURRENT code");
+      return fail(BC_ERR_INVALID, "probe_field is not a recordable BC_STATE_* view or a BC_PROBE_CURRENT code");
     }
     if (is_current) {
       static const uint32_t cur_owner[BC_NCUR] = {
@@ -1259,7 +1265,7 @@ bc_status bc_plan_create(const bc_batch_spec* spec, const bc_plan_options* opts_
                                                      BC_M_CADET, BC_M_NAHH,  BC_M_NAHH,  BC_M_KHH,   BC_M_KM,
                                                      BC_M_KA1,   BC_M_KA1,   BC_M_KA2,   BC_M_KA2,
                                                      BC_M_KK2A,  BC_M_KK2A,  BC_M_KK2B,  BC_M_KK2B,
-                                                     BC_M_KNI};
+                                                     BC_M_KNI,   0};
       const int32_t rg = cells[c].region[v];
       if (rg < 0 || !(s.region_mech[c * s.n_regions + rg] & owner[field])) {
         delete p;
@@ -1586,6 +1592,8 @@ bc_status bc_plan_create(const bc_batch_spec* spec, const bc_plan_options* opts_
     d.pulse_offset = int64_t(p->pulses.size());
     d.n_pulses = int32_t(to.pulses.size());
     p->pulses.insert(p->pulses.end(), to.pulses.begin(), to.pulses.end());
+    p->pulse_src.insert(p->pulse_src.end(), to.pulse_src.begin(), to.pulse_src.end());
+    p->pulse_scale.insert(p->pulse_scale.end(), to.pulse_scale.begin(), to.pulse_scale.end());
     d.port_offset = int64_t(p->ports.size());
     d.n_ports = int32_t(to.ports.size());
     for (PortRec r : to.ports) {
@@ -2025,11 +2033,16 @@ static bc_status view_offsets(bc_plan* p, int32_t which, std::vector<int64_t>& h
       case BC_STATE_KK2B_P: slot = (m & BC_M_KK2B) ? kSlotKK2BP : -1; break;
       case BC_STATE_KK2B_Q: slot = (m & BC_M_KK2B) ? kSlotKK2BQ : -1; break;
       case BC_STATE_KNI_P: slot = (m & BC_M_KNI) ? kSlotKNIP : -1; break;
+      case BC_STATE_V_LAST:
+        slot = kSlotVLastHi;
+        has_lo = true;
+        break;
     }
     if (slot < 0) continue;
     // states live in the separate state array: offsets are tagged by +state_tag
+    const int lo_slot = which == BC_STATE_V_LAST ? kSlotVLastLo : kSlotCaLo;
     hi[k] = kStateTag + (d.state_offset + int64_t(slot) * d.n_nodes + j) * int64_t(rs);
-    if (has_lo) lo[k] = kStateTag + (d.state_offset + int64_t(kSlotCaLo) * d.n_nodes + j) * int64_t(rs);
+    if (has_lo) lo[k] = kStateTag + (d.state_offset + int64_t(lo_slot) * d.n_nodes + j) * int64_t(rs);
   }
   return BC_OK;
 }
@@ -2069,7 +2082,36 @@ bc_status bc_state_download(bc_plan_t p, int32_t which, double* out, void* strea
 }
 
 bc_status bc_state_upload(bc_plan_t p, int32_t which, const double* in, void* stream) {
-  return view_io(p, which, const_cast<double*>(in), true, stream);
+  bc_status st = view_io(p, which, const_cast<double*>(in), true, stream);
+  // a new voltage starts a fresh history: no step has crossed anything since
+  if (st == BC_OK && which == BC_STATE_V) st = view_io(p, BC_STATE_V_LAST, const_cast<double*>(in), true, stream);
+  return st;
+}
+
+bc_status bc_pulse_set_amp(bc_plan_t p, const double* amp_nA, void* stream) {
+  if (!p || (!amp_nA && p->n_pulses > 0)) return fail(BC_ERR_INVALID, "null argument");
+  BC_NEED_DEVICE(p);
+  if (p->pulses.empty()) return BC_OK;
+  BC_CUDA(cudaSetDevice(p->device));
+  for (int64_t q = 0; q < p->n_pulses; ++q)
+    if (!std::isfinite(amp_nA[q])) return fail(BC_ERR_INVALID, "bc_pulse_set_amp: non-finite amplitude");
+  for (size_t k = 0; k < p->pulses.size(); ++k) p->pulses[k].amp = amp_nA[p->pulse_src[k]] * p->pulse_scale[k];
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  // the records also carry the step bounds of the last dt; pageable source: wait
+  BC_CUDA(cudaMemcpyAsync(p->d_pulses, p->pulses.data(), p->pulses.size() * sizeof(PulseRec), cudaMemcpyHostToDevice,
+                          st));
+  BC_CUDA(cudaStreamSynchronize(st));
+  return BC_OK;
+}
+
+bc_status bc_spike_state_download(bc_plan_t p, double v_th, double* out, void* stream) {
+  if (!p || !out) return fail(BC_ERR_INVALID, "null argument");
+  std::vector<double> last(size_t(p->n_cv));
+  bc_status st = view_io(p, BC_STATE_V, out, false, stream);
+  if (st == BC_OK && p->n_cv > 0) st = view_io(p, BC_STATE_V_LAST, last.data(), false, stream);
+  if (st != BC_OK) return st;
+  for (int64_t k = 0; k < p->n_cv; ++k) out[k] = (last[size_t(k)] < v_th && out[k] >= v_th) ? 1.0 : 0.0;
+  return BC_OK;
 }
 
 // ------------------------------------------------------------------ no-allocation download
@@ -2113,16 +2155,17 @@ static void noalloc_offset(const bc_plan* p, int32_t which, int64_t k, int64_t* 
                                                 BC_M_CADET, BC_M_NAHH, BC_M_NAHH, BC_M_KHH, BC_M_KM,
                                                 BC_M_KA1,   BC_M_KA1,  BC_M_KA2,  BC_M_KA2,
                                                 BC_M_KK2A,  BC_M_KK2A, BC_M_KK2B, BC_M_KK2B,
-                                                BC_M_KNI};
+                                                BC_M_KNI,   BC_M_ALL};
   static const int kSlot[BC_NSTATE_VIEW] = {-1,        kSlotNaP,   kSlotNaQ,   kSlotKdrP,  kSlotCalP,
                                             kSlotCalQ, kSlotCatP,  kSlotCatQ,  kSlotHcnP,  kSlotAhpP,
                                             kSlotCaHi, kSlotNaHHP, kSlotNaHHQ, kSlotKHHP,  kSlotKMN,
                                             kSlotKA1P, kSlotKA1Q,  kSlotKA2P,  kSlotKA2Q,
                                             kSlotKK2AP, kSlotKK2AQ, kSlotKK2BP, kSlotKK2BQ,
-                                            kSlotKNIP};
-  if (!(p->cv_mech[k] & kBit[which])) return;
+                                            kSlotKNIP,  kSlotVLastHi};
+  if (which != BC_STATE_V_LAST && !(p->cv_mech[k] & kBit[which])) return;
   *hi = kStateTag + (d.state_offset + int64_t(kSlot[which]) * d.n_nodes + j) * rs;
   if (which == BC_STATE_CA_CI) *lo = kStateTag + (d.state_offset + int64_t(kSlotCaLo) * d.n_nodes + j) * rs;
+  if (which == BC_STATE_V_LAST) *lo = kStateTag + (d.state_offset + int64_t(kSlotVLastLo) * d.n_nodes + j) * rs;
 }
 
 bc_status bc_state_download_noalloc(bc_plan_t p, int32_t which, double* out, void* stream) {

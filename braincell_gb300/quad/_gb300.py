@@ -27,10 +27,27 @@ __all__ = ["gb300_staggered_step"]
     description="Staggered DHS voltage / exp-Euler channel step fused into sm_103a kernels.",
 )
 def gb300_staggered_step(target, *args):
-    """Advance ``target`` (a node-tree Cell) by one staggered step of ``environ['dt']``."""
+    """Advance ``target`` by one staggered step of ``environ['dt']``.
+
+    A node-tree ``Cell`` is called as ``solver(cell)`` (``cell.py:2379``); a
+    ``SingleCompartment`` as ``solver(neuron, I_ext)`` (``_single_compartment/
+    base.py:275``), ``I_ext`` being the step's external current density (nA/cm^2).
+    """
+    from ..single import SingleCompartment
+
+    if isinstance(target, SingleCompartment):
+        if len(args) > 1:
+            raise TypeError("gb300_staggered_step takes at most one argument (I_ext) for a SingleCompartment.")
+        dt = environ.get("dt")
+        if target._runtime is None:
+            target.init_state()
+        target._set_input(args[0] if args else 0.0)
+        target._runtime.run(1, float(dt))
+        return
     if not (hasattr(target, "batch") and hasattr(target, "morpho")):
         raise TypeError(
-            f"The gb300_staggered integrator needs a node-tree Cell target, got {type(target).__name__}."
+            f"The gb300_staggered integrator needs a node-tree Cell or a SingleCompartment target, "
+            f"got {type(target).__name__}."
         )
     if args:
         raise TypeError("gb300_staggered_step takes no extra arguments for a Cell target.")
@@ -42,7 +59,10 @@ def gb300_staggered_step(target, *args):
 
 def _init_target(cell):
     from ..runtime import Plan
+    from ..single import SingleCompartment
 
+    if isinstance(cell, SingleCompartment):
+        return Plan(cell.batch(cell._v0), record_every=0, **cell.solver_options)
     return Plan(cell.batch(), **cell.solver_options)
 
 

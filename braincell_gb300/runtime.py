@@ -181,6 +181,22 @@ class Plan:
         )
         return out
 
+    def spike_state(self, v_th: float = 0.0, stream=None) -> np.ndarray:
+        """Per-CV spike indicator of the last step taken (1.0 where V_last < v_th <= V),
+        the reference's ``Cell.spike`` after a step; all zero after a reset."""
+        out = np.empty(self.n_cv, dtype=np.float64)
+        _abi.check(self._lib.bc_spike_state_download(self._h, float(v_th), out.ctypes.data_as(C.POINTER(C.c_double)),
+                                                     self._stream(stream)))
+        return out
+
+    def set_pulse_amps(self, amps_nA, stream=None) -> None:
+        """New amplitudes (nA) for every clamp pulse of the batch, in batch order."""
+        arr = np.ascontiguousarray(np.asarray(amps_nA, dtype=np.float64).reshape(-1))
+        if arr.size != int(self.batch.pulse_cell.size):
+            raise ValueError(f"expected {self.batch.pulse_cell.size} amplitudes, got {arr.size}")
+        _abi.check(self._lib.bc_pulse_set_amp(self._h, arr.ctypes.data_as(C.POINTER(C.c_double)),
+                                              self._stream(stream)))
+
     def set_state(self, name: str, values, stream=None) -> None:
         which = _abi.STATE_NAMES[name]
         arr = np.ascontiguousarray(np.broadcast_to(np.asarray(values, dtype=np.float64), (self.n_cv,)))

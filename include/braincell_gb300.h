@@ -273,8 +273,9 @@ typedef struct bc_plan_info_t {
 /* Thread-local text of the last failure (never NULL). */
 const char* bc_last_error(void);
 /* ABI version: major * 10000 + minor * 100 + patch.  0.2.0: the 64-entry parameter
- * record, the A / K2 / KNI mechanisms, named plan-info fields. */
-#define BC_ABI_VERSION 200
+ * record, the A / K2 / KNI mechanisms, named plan-info fields.  0.3.0: the V_last
+ * state view (BC_NSTATE_VIEW 25), bc_spike_state_download, bc_pulse_set_amp. */
+#define BC_ABI_VERSION 300
 int32_t bc_version(void);
 /* Fill opts with defaults. */
 void bc_default_options(bc_plan_options* opts);
@@ -350,7 +351,9 @@ bc_status bc_check(bc_plan_t plan, void* stream);
 #define BC_STATE_KK2B_P 21
 #define BC_STATE_KK2B_Q 22
 #define BC_STATE_KNI_P 23
-#define BC_NSTATE_VIEW 24
+#define BC_STATE_V_LAST 24 /* V at the start of the last step taken (= V after a reset);
+                              not a probe field                                    */
+#define BC_NSTATE_VIEW 25
 /* Current probes (mech/_point.py CurrentProbe, _multi_compartment/probes.py:184-258):
    probe_field = BC_PROBE_CURRENT + one of the codes below records that current
    density (uA/cm^2, outward negative as g (E - V)) after the step.             */
@@ -376,6 +379,17 @@ bc_status bc_check(bc_plan_t plan, void* stream);
 #define BC_CUR_KNI 18    /* KNI_Ya1989  */
 #define BC_NCUR 19
 bc_status bc_state_download(bc_plan_t plan, int32_t which, double* out /* [n_cv] */, void* stream);
+/* Set the amplitude (nA) of every current-clamp pulse of the batch spec, in spec
+ * order (amp_nA[n_pulses]); times and locations are unchanged.  Takes effect from
+ * the next step.  The time-varying input of a stepped model goes through this:
+ * SingleCompartment.update(I_ext) (_single_compartment/base.py:252-278) passes a
+ * new external current every step, which here is one pulse per neuron. */
+bc_status bc_pulse_set_amp(bc_plan_t plan, const double* amp_nA, void* stream);
+/* Per-CV spike indicator of the last step taken: out[k] = 1 where CV k's voltage
+ * crossed v_th upward during that step (V_last < v_th <= V), else 0; all 0 after a
+ * reset.  Replaces reading Cell.spike, which the reference sets every step from
+ * get_spike(last_V, V) (_base.py:421-431, _multi_compartment/cell.py:2384-2386). */
+bc_status bc_spike_state_download(bc_plan_t plan, double v_th, double* out /* [n_cv] */, void* stream);
 bc_status bc_state_upload(bc_plan_t plan, int32_t which, const double* in /* [n_cv] */, void* stream);
 
 /* bc_state_download without any allocation.  No counterpart in the reference: its

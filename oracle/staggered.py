@@ -60,6 +60,10 @@ __all__ = [
     "compute_peel_levels",
     "build_backsub_indices",
     "exprel",
+    "exp_euler",
+    "gate_step",
+    "nernst_ca_mV",
+    "ca_detailed_rate",
     "rates",
     "CHANNEL_DEFAULTS",
     "ION_DEFAULTS",
@@ -300,6 +304,38 @@ def exprel(x):
     small = np.abs(x) < 1e-300
     xs = np.where(small, 1.0, x)
     return np.where(small, 1.0, np.expm1(xs) / xs)
+
+
+def exp_euler(x, f, lam, dt: float):
+    """One exponential-Euler step of x' = f(x) with diagonal Jacobian lam:
+    x + dt * exprel(dt * lam) * f (quad/_exp_euler.py:330-478)."""
+    return x + dt * exprel(dt * lam) * f
+
+
+def gate_step(x, kind: str, a, b, phi, dt: float):
+    """Exp-Euler step of one HH gate (channel/_base.py:575-588): ``kind`` "ab" for
+    x' = phi (a (1 - x) - b x), "it" for x' = phi (a - x) / b (a = x_inf, b = tau)."""
+    if kind == "ab":
+        f = phi * (a * (1.0 - x) - b * x)
+        lam = -phi * (a + b)
+    else:
+        f = phi * (a - x) / b
+        lam = -phi / b
+    return exp_euler(x, f, lam, dt)
+
+
+def nernst_ca_mV(temp, Co, Ci):
+    """Calcium reversal potential (mV): R T / (2 F) ln(Co / Ci) (ion/_base.py:463-469)."""
+    return 1e3 * GAS_R * temp / (2.0 * FARADAY) * np.log(Co / Ci)
+
+
+def ca_detailed_rate(I_ca, Ci, d, tau, C_rest):
+    """CalciumDetailed dCi/dt (mM/ms) (ion/calcium.py:499-505): the influx
+    max(I_ca / (2 F d), 0) of the ion's total current I_ca = sum g (E_Ca - V)
+    (uA/cm^2, positive inward), over a shell of depth d (um), plus the decay
+    (C_rest - Ci) / tau."""
+    drive = np.maximum(I_ca * 10.0 / (2.0 * FARADAY * d), 0.0)
+    return drive + (C_rest - Ci) / tau
 
 
 def rates(name: str, V, p: dict, Ci=None):
@@ -883,7 +919,7 @@ class OracleCell:
         if self.Ci is None:
             return self.E_ca_fixed
         cd = self.ca_dyn
-        nernst = 1e3 * GAS_R * cd["temp"] / (2.0 * FARADAY) * np.log(cd["Co"] / np.where(cd["mask"], self.Ci, 1.0))
+        nernst = nernst_ca_mV(cd["temp"], cd["Co"], np.where(cd["mask"], self.Ci, 1.0))
         return np.where(cd["mask"], nernst, self.E_ca_fixed)
 
     def _gate_product(self, name):
@@ -1033,12 +1069,8 @@ class OracleCell:
         # a11 (a): dependent ion self states -- Ci with the cached step-start current
         if self.Ci is not None:
             cd = self.ca_dyn
-            d_m = cd["d"]
-            drive = I_ca_cached * 10.0 / (2.0 * FARADAY * d_m)
-            drive = np.maximum(drive, 0.0)
-            f = drive + (cd["C_rest"] - self.Ci) / cd["tau"]
-            lam = -1.0 / cd["tau"]
-            Ci_new = self.Ci + dt * exprel(dt * lam) * f
+            f = ca_detailed_rate(I_ca_cached, self.Ci, cd["d"], cd["tau"], cd["C_rest"])
+            Ci_new = exp_euler(self.Ci, f, -1.0 / cd["tau"], dt)
             self.Ci = np.where(cd["mask"], Ci_new, self.Ci)
         # a11 (c): dependent channels, exp-Euler per gate at the new voltage (and new Ci)
         Ci_now = self._ci_for_channels()
@@ -1048,16 +1080,8 @@ class OracleCell:
                 continue
             r = rates(name, pv_new, ch, Ci=Ci_now)
             for gate, _power, phik in _GATES[name]:
-                x = self.gates[(name, gate)]
-                phi = ch[phik]
                 kind, a, b = r[gate]
-                if kind == "ab":
-                    f = phi * (a * (1.0 - x) - b * x)
-                    lam = -phi * (a + b)
-                else:
-                    f = phi * (a - x) / b
-                    lam = -phi / b
-                new_gates[(name, gate)] = x + dt * exprel(dt * lam) * f
+                new_gates[(name, gate)] = gate_step(self.gates[(name, gate)], kind, a, b, ch[phik], dt)
         self.gates.update(new_gates)
         # a16: spike = last_V < V_th <= V
         spk = ((V_new - self.V_th) >= 0.0) & ((self.V_th - last_V) > 0.0)

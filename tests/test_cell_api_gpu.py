@@ -115,3 +115,38 @@ def test_swc_morphology_matches_oracle():
     oc = OracleCell(_swc_cell("f64"))
     otr, _ = oc.run(0.025, 400)
     np.testing.assert_allclose(tr, otr[0, 0], atol=1e-8)
+
+
+def test_per_cv_spike_state_matches_oracle():
+    # Cell.spike is the per-CV get_spike(last_V, V) of the last step (cell.py:2384-2386):
+    # after every update(), and after a fused run that ends on a crossing step
+    from braincell_gb300.runtime import Plan
+
+    d = W._small_desc(0)
+    d.pulses = [(0, 0.5, 1.0, 30.0, 1.2)]
+    cell = W.desc_to_cell(d, precision="f64")
+    cell.init_state()
+    assert cell.spike.sum() == 0
+    oc = OracleCell(W.desc_to_cell(d))
+    crossing_steps = []
+    with environ.context(dt=0.025):
+        for k in range(800):
+            s = cell.update()
+            o = oc.step(0.025)
+            np.testing.assert_array_equal(s[0], o[0], err_msg=f"step {k}")
+            if o.sum():
+                crossing_steps.append(k + 1)
+    assert len(crossing_steps) >= 2
+    n = crossing_steps[1]
+    p = Plan(W.descs_to_batch([d]), precision="f64", steps_per_launch=37)
+    p.run(n, 0.025)
+    ref = OracleCell(W.desc_to_cell(d))
+    for _ in range(n):
+        spk = ref.step(0.025)
+    assert spk.sum() >= 1
+    np.testing.assert_array_equal(p.spike_state(0.0), spk[0])
+    # an upload starts a fresh history: no crossing until the next step
+    p.set_state("V", p.state("V"))
+    assert p.spike_state(0.0).sum() == 0
+    p.reset()
+    assert p.spike_state(0.0).sum() == 0

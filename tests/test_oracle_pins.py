@@ -331,3 +331,105 @@ def test_kni_rates_and_record():
     bits, rec = catalogue.region_record([Channel("KNI_Ya1989", tau_max=2000.0, V_sh=-3.0)], CableProperty())
     assert bits == _abi.BC_M_KNI
     assert list(rec[_abi.BC_P_KNI_G:_abi.BC_P_KNI_TAUMAX + 1]) == [0.004, -3.0, 1.0, 2000.0]
+
+
+# ------------------------------------------------------------------ defaults, phi, currents, calcium
+
+
+@pytest.mark.parametrize("case", GOLD["defaults"], ids=lambda c: c["class"])
+def test_reference_defaults(case):
+    # the oracle and the product catalogue both hold the reference's constructor defaults
+    from braincell_gb300 import catalogue
+
+    oracle_table = O.CHANNEL_DEFAULTS if case["kind"] == "channel" else O.ION_DEFAULTS
+    product_table = catalogue.CHANNELS if case["kind"] == "channel" else catalogue.IONS
+    for k, v in case["values"].items():
+        assert oracle_table[case["class"]][k] == pytest.approx(v, rel=1e-12), (case["src"], k)
+        assert product_table[case["class"]][k] == pytest.approx(v, rel=1e-12), (case["src"], k)
+
+
+@pytest.mark.parametrize("case", GOLD["gate_phi"], ids=lambda c: c["src"].split()[0])
+def test_gate_phi_known_answers(case):
+    from braincell_gb300 import catalogue
+    from braincell_gb300.mech import CableProperty, Channel
+
+    for cls in case["classes"]:
+        p = O._resolve(O.CHANNEL_DEFAULTS, Channel(cls, **case["params"]))
+        for key, phi in case["phi"].items():
+            assert p[key] == pytest.approx(phi, abs=case["atol"]), (cls, key)
+        # the product record carries the same factors (its phi slots)
+        _, rec = catalogue.region_record([Channel(cls, **case["params"])], CableProperty())
+        k = catalogue.kernel_class(cls)
+        slots = {"CaT_HM1992": (_abi_slot("CAT_PHIP"), _abi_slot("CAT_PHIQ")),
+                 "CaL_IS2008": (_abi_slot("CAL_PHIP"), _abi_slot("CAL_PHIQ")),
+                 "HCN_HM1992": (_abi_slot("HCN_PHI"),)}[k]
+        assert [rec[s] for s in slots] == pytest.approx(list(case["phi"].values()), abs=case["atol"])
+
+
+def _abi_slot(name):
+    from braincell_gb300 import _abi
+
+    return getattr(_abi, "BC_P_" + name)
+
+
+@pytest.mark.parametrize("case", GOLD["currents"], ids=lambda c: c["class"])
+def test_current_known_answers(case):
+    # HCN current g_max p (E - V), evaluated the way the oracle evaluates channel currents
+    from braincell_gb300 import Branch, Cell, Morphology
+    from braincell_gb300.mech import AllRegion, CableProperty, Channel
+
+    soma = Branch.from_lengths(lengths=[20.0], radii=[10.0, 10.0], type="soma")
+    c = Cell(Morphology.from_root(soma, name="soma"))
+    c.paint(AllRegion(), CableProperty(resting_potential=case["V"]), Channel(case["class"], **case["params"]))
+    oc = O.OracleCell(c)
+    for g, v in case["gates"].items():
+        oc.gates[(case["class"], g)][:] = v
+    pv = oc.cv_to_point(oc.V)
+    I, dI = oc._channel_currents(pv)
+    mid = oc.cv_mid[0]
+    assert I[0, mid] == pytest.approx(case["current"], abs=case["atol"])
+    assert dI[0, mid] == pytest.approx(-case["params"]["g_max"] * case["gates"]["p"], abs=1e-12)
+
+
+def test_calcium_detailed_known_answers():
+    cases = {c["src"].split()[1]: c for c in GOLD["calcium_detailed"]}
+    dflt = O.ION_DEFAULTS["CalciumDetailed"]
+    c = cases["test_E_zero_when_internal_equals_external"]
+    assert O.nernst_ca_mV(dflt["temp"], dflt["Co"], c["Ci"]) == pytest.approx(c["E"], abs=c["atol"])
+    c = cases["test_derivative_without_current_matches_leak_formula"]
+    got = O.ca_detailed_rate(c["I_ca"], c["Ci"], dflt["d"], c["tau"], c["C_rest"])
+    assert got == pytest.approx(c["dCi_dt"], abs=c["atol"])
+    c = cases["test_E_updates_with_C_dynamically"]
+    assert O.nernst_ca_mV(dflt["temp"], dflt["Co"], c["Ci_high"]) < O.nernst_ca_mV(dflt["temp"], dflt["Co"], c["Ci_low"])
+    # an inward calcium current only ever adds calcium; an outward one is clipped to no influx
+    assert O.ca_detailed_rate(-5.0, 1e-4, 1.0, 5.0, 1e-4) == 0.0
+    assert O.ca_detailed_rate(5.0, 1e-4, 1.0, 5.0, 1e-4) > 0.0
+
+
+# ------------------------------------------------------------------ exp-Euler against the closed form
+
+
+@pytest.mark.parametrize("name,gate", [("CaL_IS2008", "q"), ("Na_Ba2002", "p"), ("HCN_HM1992", "p"),
+                                       ("KDR_Ba2002", "p")])
+def test_gate_exp_euler_is_the_exact_exponential(name, gate):
+    # at fixed V a gate ODE is linear, x' = (x_inf - x) / tau_eff, so one exp-Euler
+    # step must equal the closed-form x_inf + (x - x_inf) exp(-dt / tau_eff)
+    p = O._resolve(O.CHANNEL_DEFAULTS, _decl(name))
+    phik = {g: k for g, _, k in O._GATES[name]}[gate]
+    V = np.linspace(-90.0, 30.0, 25)
+    kind, a, b = O.rates(name, V, p)[gate]
+    if kind == "ab":
+        xinf, tau = a / (a + b), 1.0 / (p[phik] * (a + b))
+    else:
+        xinf, tau = a, b / p[phik]
+    for dt in (0.025, 0.5, 7.0):
+        x0 = np.full_like(V, 0.3)
+        got = O.gate_step(x0, kind, a, b, p[phik], dt)
+        want = xinf + (x0 - xinf) * np.exp(-dt / tau)
+        np.testing.assert_allclose(got, want, rtol=1e-12, atol=1e-15)
+
+
+def _decl(name):
+    from braincell_gb300.mech import Channel
+
+    return Channel(name)

@@ -74,6 +74,35 @@ def test_small_workload_f64():
     _check(W.small(2), 1000, "f64", TOL_F64_MV, oracle_cells=[0])
 
 
+def test_small_workload_f64_whole_run_every_cv():
+    # the small configuration in FP64: all 16 cells, all 4,000 steps; every CV's
+    # voltage against the oracle every 250 steps, the soma every step, and the spikes
+    descs = W.small(16)
+    p = Plan(W.descs_to_batch(descs), precision="f64", record_every=1, max_spikes=64)
+    oc = OracleCell(W.desc_to_cell(descs[0]))
+    soma = []
+    worst = 0.0
+    for _ in range(16):
+        p.run(250, DT)
+        for _ in range(250):
+            oc.step(DT)
+            soma.append(oc.V[0, 0])
+        V = p.state("V").reshape(16, oc.n_cv)
+        worst = max(worst, float(np.abs(V - oc.V[0]).max()))
+    assert worst <= TOL_F64_MV, f"max |dV| over all CVs and checkpoints {worst:.3e} mV"
+    tr = p.traces()
+    assert tr.shape == (16, 4000)
+    assert np.abs(tr - np.asarray(soma)).max() <= TOL_F64_MV
+    # (the 0.2 nA soma clamp charges this cell's dendritic load without a spike;
+    # spiking runs are compared in the tests below)
+    _, osp = OracleCell(W.desc_to_cell(descs[0])).run(DT, 4000)
+    ref = np.asarray(osp[0][0])
+    for sp in p.spikes():
+        assert len(sp) == len(ref)
+        if len(ref):
+            assert np.abs(sp - ref).max() <= 1e-9
+
+
 def test_small_workload_f32():
     _check(W.small(16), 4000, "f32", TOL_F32_MV, oracle_cells=[0, 15])
 
