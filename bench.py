@@ -70,7 +70,10 @@ def _args():
     ap.add_argument("--no-surrogate", action="store_true")
     ap.add_argument("--surrogate-threads", type=int, default=384)
     ap.add_argument("--surrogate-tile-nodes", type=int, default=1800)
-    ap.add_argument("--accuracy-cells", type=int, default=300)
+    ap.add_argument("--accuracy-cells", type=int, default=1000)
+    ap.add_argument("--mixed-cells", type=int, default=10000)
+    ap.add_argument("--mixed-steps", type=int, default=20000)
+    ap.add_argument("--no-mixed", action="store_true")
     a = ap.parse_args()
     wl = WORKLOADS[a.workload]
     a.cells = wl["cells"] if a.cells is None else a.cells
@@ -306,6 +309,21 @@ def run_reference(a):
     print(json.dumps(line), flush=True)
 
 
+def _spike_report(sp, ref, bar_ms=0.1):
+    """Spike-time agreement of paired spikes (in order, within cells of equal count):
+    median, p99 and max error, the share within ``bar_ms``, and the cells whose
+    counts differ (with the spikes they hold in the reference)."""
+    e, mis = _spike_errors(sp, ref)
+    unpaired = sum(abs(len(x) - len(y)) for x, y in zip(sp, ref))
+    return {"median_ms": float(np.median(e)) if e.size else None,
+            "p99_ms": float(np.percentile(e, 99)) if e.size else None,
+            "max_ms": float(e.max()) if e.size else None,
+            "spikes_paired": int(e.size),
+            f"share_within_{bar_ms}_ms": float((e <= bar_ms).mean()) if e.size else None,
+            "cells_with_spike_count_mismatch": mis, "spikes_unpaired": int(unpaired),
+            "spiking_cells_reference": int(sum(1 for y in ref if len(y)))}
+
+
 def _spike_errors(sp, ref):
     """Spike-time errors (ms) of spikes paired in order within cells of equal count, and
     the number of cells whose counts differ."""
@@ -466,20 +484,108 @@ def surrogate_leg(a, descs, local, sid, stream, plain_ms):
         tr64, sp64 = ref.traces(), ref.spikes()
         ref.close()
         r = S.run_surrogate(sub, model, a.sim_steps, record_every=1, fallback=True, device=local)
-        e, mis = _spike_errors(r.spikes, sp64)
         rms = np.sqrt(np.mean((r.traces - tr64) ** 2, axis=1))
         lin = S.run_surrogate(sub, None, a.sim_steps, record_every=1, fallback=False, device=local)
         rms_lin = np.sqrt(np.mean((lin.traces - tr64) ** 2, axis=1))
         out["accuracy"] = {
-            "cells": n_acc, "against": "FP64 plain solve on the GPU", "fallback_rate": r.fallback_rate,
-            "spike_time_error_ms": {"median": float(np.median(e)) if e.size else None,
-                                    "p99": float(np.percentile(e, 99)) if e.size else None,
-                                    "spikes_paired": int(e.size)},
-            "cells_with_spike_count_mismatch": mis,
-            "soma_rms_mV": {"median": float(np.median(rms)), "mean": float(np.mean(rms))},
+            "cells": n_acc, "against": "FP64 plain solve on the GPU",
+            "held_out": "seed 1 cells; the model was trained on seed 3 cells only",
+            "fallback_rate": r.fallback_rate,
+            "spike_time_error": _spike_report(r.spikes, sp64),
+            "soma_rms_mV": {"median": float(np.median(rms)), "mean": float(np.mean(rms)),
+                            "p99": float(np.percentile(rms, 99))},
             "without_network_soma_rms_mV": {"median": float(np.median(rms_lin)), "mean": float(np.mean(rms_lin))},
         }
     out["model"] = {k: model.info.get(k) for k in ("n_traj", "epochs", "updates", "train_s", "val_mse_after")}
+    return out
+
+
+def mixed_leg(a, local, model, record_every=4):
+    """The mixed production run: ``a.mixed_cells`` cells of the uneven family drawn
+    with seed 4, 30 % of them (a seeded draw) kept at full morphology and 70 % with
+    their distal subtrees as GRU ports and per-cell fallback, ``a.mixed_steps``
+    steps of 0.025 ms (500 ms), FP32 state with BF16 GRU weights.
+
+    Reports compartment-steps/s of the plain form (every cell at full morphology,
+    the same launch shape as the headline) and of the mixed form (full-morphology
+    compartments counted for every cell), both host-clocked from reset to the end of
+    every stream, the fallback rate, and accuracy against the FP64 plain solve on
+    the first ``a.accuracy_cells`` cells (spike times from every spike; somatic RMS
+    from the soma voltage sampled every ``record_every`` steps)."""
+    import torch
+
+    from braincell_gb300 import surrogate as S
+    from braincell_gb300 import workloads as W
+    from braincell_gb300.runtime import Plan
+
+    n, steps = a.mixed_cells, a.mixed_steps
+    descs = W.uneven(n, seed=4)
+    full = np.sort(np.random.default_rng(4).choice(n, size=int(round(0.3 * n)), replace=False))
+    total_cv = int(sum(int(sum(d.ncv)) for d in descs))
+    out = {"cells": n, "steps": steps, "full_morphology_cells": int(full.size), "compartments": total_cv,
+           "selection": "uneven generator seed 4; full-morphology cells drawn with default_rng(4)"}
+    # plain form
+    plan = Plan(W.descs_to_batch(descs), precision="f32", device=local, tile_nodes=a.tile_nodes,
+                threads_per_tile=a.threads, threads_big=a.threads_big, steps_per_launch=a.steps_per_launch,
+                record_every=0, lane_nodes=a.lane_nodes)
+    st = torch.cuda.Stream(local)
+    sid = int(st.cuda_stream)
+    plan.reset(stream=sid)
+    plan.run(2 * a.steps_per_launch, DT, stream=sid)
+    walls = []
+    for _ in range(2):
+        torch.cuda.synchronize(local)
+        t0 = time.perf_counter()
+        plan.reset(stream=sid)
+        plan.run(steps, DT, stream=sid, check=False)
+        st.synchronize()
+        walls.append((time.perf_counter() - t0) * 1e3)
+        plan.check(stream=sid)
+    plan.close()
+    ms_plain = float(np.median(walls))
+    out["plain"] = {"value": total_cv * steps / (ms_plain * 1e-3), "unit": UNIT, "ms": ms_plain,
+                    "ms_all_runs": [round(w, 1) for w in walls]}
+    # mixed surrogate form
+    T = a.surrogate_threads
+    kw = dict(tile_nodes=a.surrogate_tile_nodes, threads_per_tile=T, threads_big=T, threads_global=T,
+              steps_per_launch=a.steps_per_launch, lane_nodes=a.lane_nodes)
+    runner = S.SurrogateRunner(descs, model, precision="f32", device=local, plan_kw=kw, full_cells=full)
+    runner.run(2 * a.steps_per_launch, DT)
+    runs = [runner.run(steps, DT) for _ in range(3)]
+    runner.close()
+    ms = float(np.median([r.wall_ms for r in runs]))
+    res = runs[-1]
+    out["surrogate"] = {"value": total_cv * steps / (ms * 1e-3), "unit": UNIT + " (full-morphology compartments)",
+                        "ms": ms, "ms_all_runs": [round(r.wall_ms, 1) for r in runs],
+                        "speedup_vs_plain": ms_plain / ms, "fallback_cells": int(res.fallback_cells.size),
+                        "fallback_rate": res.fallback_rate, "n_ports": runner.n_ports,
+                        "reduced_compartments": int(runner.plan.n_cv)}
+    # accuracy on the first cells (same full / port split) against the FP64 plain solve
+    m = min(a.accuracy_cells, n)
+    if m:
+        from dataclasses import replace
+
+        sub = [replace(d, probes=[(0, 0.5)]) for d in descs[:m]]
+        ref = Plan(W.descs_to_batch(sub), precision="f64", device=local, record_every=record_every, max_spikes=512)
+        ref.run(steps, DT)
+        tr64, sp64 = ref.traces(), ref.spikes()
+        ref.close()
+        sub_full = full[full < m]
+        r = S.run_surrogate(descs[:m], model, steps, record_every=record_every, fallback=True, device=local,
+                            plan_kw=kw, full_cells=sub_full)
+        port_cells = np.setdiff1d(np.arange(m), sub_full)
+        rms = np.sqrt(np.mean((r.traces - tr64) ** 2, axis=1))
+        out["accuracy"] = {
+            "cells": m, "port_cells": int(port_cells.size), "against": "FP64 plain solve on the GPU",
+            "fallback_rate": r.fallback_rate,
+            "spike_time_error_all_cells": _spike_report(r.spikes, sp64),
+            "spike_time_error_port_cells": _spike_report([r.spikes[i] for i in port_cells],
+                                                         [sp64[i] for i in port_cells]),
+            "soma_rms_mV": {"median": float(np.median(rms)), "mean": float(np.mean(rms)),
+                            "p99": float(np.percentile(rms, 99)),
+                            "port_cells_median": float(np.median(rms[port_cells]))},
+            "soma_sampled_every_steps": record_every,
+        }
     return out
 
 
@@ -606,6 +712,10 @@ def run_ours(a):
         sur["value"] = sur["value"] * world  # every rank runs its own replica
         line["surrogate"] = sur
         line["gpu_launches"] += a.steps * sur["gpu_launches_per_step"]
+        if not a.no_mixed and rank == 0:
+            from braincell_gb300 import surrogate as S
+
+            line["mixed_production"] = mixed_leg(a, local, S.load_model(S.PACKAGED_MODEL))
     if rank == 0 and world == 1 and not a.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(a.workload)
     if rank == 0:

@@ -42,6 +42,12 @@ bc_status lower_cell(const bc_batch_spec& spec, int64_t c, LoweredCell& out);
 int32_t locate_node(const bc_batch_spec& spec, int64_t c, const LoweredCell& lc, int32_t branch, double x);
 
 // ----------------------------------------------------------------- device records
+// Stride (in reals) of the per-(cell, region) parameter records in a tile blob: one
+// more than BC_NPARAM, so that the records of different regions start in different
+// shared-memory banks (the lanes of a warp read the records of their own nodes'
+// regions; at a stride of 64 words they would all fall in one bank).
+constexpr int kParamStride = BC_NPARAM + 1;
+
 // A chain: nodes [start, start+count) of the tile, bottom (deepest) first; node
 // start+k+1 is the parent of node start+k and top_parent is the parent of the top
 // node (-1 at a root).  The record owns the consecutive contribution slots
@@ -71,6 +77,15 @@ struct SlotRec {
   uint8_t steps;
   uint8_t unit;
   uint16_t off[32];
+};
+
+// A warp group of a tile: warps [warp_begin, warp_begin + n_warps) run the tree
+// phases phase_begin .. phase_begin + n_phases - 1 of the tile's phase table (whose
+// slots hold only the group's cells) and update nodes [node_begin, node_end),
+// synchronising on a barrier of their own.
+struct GroupRec {
+  int32_t warp_begin, n_warps, phase_begin, n_phases, node_begin, node_end;
+  int32_t pad[2];
 };
 
 // Per-tile descriptor (global memory, read-only).
@@ -110,6 +125,8 @@ struct TileDesc {
   int32_t off_pstage;       // the GRU weight fragments and wo (kGruSmemBytes), then per-port staging
                             // records (PortStage), then PortLocal records, inside the
                             // scratch area; -1: none
+  int32_t n_groups;         // warp groups (GroupRec table at off_groups); 1 = the whole CTA
+  int32_t off_groups;
 };
 
 // ------------------------------------------------------------- subtree surrogate

@@ -613,7 +613,7 @@ __device__ __forceinline__ void write_row(const TileView<Real>& tv, int i, uint1
   if (pr == kBoundary) {
     tv.dr[i] = make_pair(dt * tv.diag0[i], Real(0));
   } else {
-    const Real invcm = tv.params[size_t(pr) * BC_NPARAM + BC_P_INVCM];
+    const Real invcm = tv.params[size_t(pr) * kParamStride + BC_P_INVCM];
     tv.dr[i] = make_pair(Real(1) + dt * (tv.diag0[i] + invcm * G), dt * invcm * I);
   }
 }
@@ -661,7 +661,7 @@ __device__ __forceinline__ void add_node_pulses(const TileView<Real>& tv, const 
     if (pr == kBoundary)
       tv.dr[i].y += dt * Real(p.amp);
     else
-      tv.dr[i].y += dt * tv.params[size_t(pr) * BC_NPARAM + BC_P_INVCM] * Real(p.amp);
+      tv.dr[i].y += dt * tv.params[size_t(pr) * kParamStride + BC_P_INVCM] * Real(p.amp);
   }
 }
 
@@ -1377,6 +1377,15 @@ __device__ __forceinline__ bool is_finite_real(Real x) {
   return isfinite(x);
 }
 
+// Barrier of a warp group: the named barrier 1 + g over the group's threads, or the
+// CTA barrier when the tile is one group.
+__device__ __forceinline__ void group_sync(bool grouped, int g, int n_threads) {
+  if (grouped)
+    asm volatile("bar.sync %0, %1;" ::"r"(1 + g), "r"(n_threads) : "memory");
+  else
+    __syncthreads();
+}
+
 // ------------------------------------------------------------------ the step kernel
 // kVar: 0 = lean (no optional mechanism), 1 = extra (synapses, network,
 // out-of-line channels), 2 = extra + subtree-surrogate ports.
@@ -1448,7 +1457,7 @@ __global__ void __launch_bounds__(kVar == 2 ? BC_PORT_MAX_THREADS : 1024, kVar =
     Real G = Real(0), I = Real(0);
     if (pr != kBoundary) {
       const Real v = tv.v[i].x;
-      node_mechanisms(tv.state + i, tv.N, tv.params + size_t(pr) * BC_NPARAM, tv.mech[pr], v, v, dt, false, G, I);
+      node_mechanisms(tv.state + i, tv.N, tv.params + size_t(pr) * kParamStride, tv.mech[pr], v, v, dt, false, G, I);
     }
     const uint16_t sp = tv.spec[i];
     if (sp != kNoSpecial) {
@@ -1497,18 +1506,25 @@ __global__ void __launch_bounds__(kVar == 2 ? BC_PORT_MAX_THREADS : 1024, kVar =
   do {                \
   } while (0)
 #endif
+  // This warp's group: its own phases, nodes and barrier (td.n_groups = 1: the CTA).
+  const GroupRec* groups = reinterpret_cast<const GroupRec*>(base + td.off_groups);
+  int grp = 0;
+  while (grp + 1 < td.n_groups && warp >= groups[grp + 1].warp_begin) ++grp;
+  const GroupRec gr = groups[grp];
+  const bool grouped = td.n_groups > 1;
+  const int gwarp = warp - gr.warp_begin, gT = gr.n_warps * 32, gtid = tid - gr.warp_begin * 32;
   for (int s = 0; s < a.n_steps; ++s) {
     const int64_t step = a.step0 + s;
     // forward elimination, leaves first
-    for (int p = 0; p < tv.n_phases; ++p) {
-      eliminate_phase<Real, kSmem>(tv, p, warp, n_warps, lane, dt);
-      __syncthreads();
+    for (int p = 0; p < gr.n_phases; ++p) {
+      eliminate_phase<Real, kSmem>(tv, gr.phase_begin + p, gwarp, gr.n_warps, lane, dt);
+      group_sync(grouped, grp, gT);
     }
     BC_TICK(0);
     // back-substitution, root first
-    for (int p = tv.n_phases - 1; p >= 0; --p) {
-      backsub_phase<Real, kSmem>(tv, p, warp, n_warps, lane, dt);
-      __syncthreads();
+    for (int p = gr.n_phases - 1; p >= 0; --p) {
+      backsub_phase<Real, kSmem>(tv, gr.phase_begin + p, gwarp, gr.n_warps, lane, dt);
+      group_sync(grouped, grp, gT);
     }
     BC_TICK(1);
     // V update, mechanism states, next row, probes and next pulses
@@ -1519,16 +1535,17 @@ __global__ void __launch_bounds__(kVar == 2 ? BC_PORT_MAX_THREADS : 1024, kVar =
     // iteration ahead so that their latency overlaps this node's arithmetic.
     NodeStates<Real> cur;
     uint16_t pr_cur = kBoundary;
-    if (tid < tv.n_real) {
-      pr_cur = tv.pidx[tid];
-      if (pr_cur != kBoundary) load_states(tv.state + tid, tv.N, tv.mech[pr_cur], cur);
+    const int i0 = gr.node_begin + gtid;
+    if (i0 < gr.node_end) {
+      pr_cur = tv.pidx[i0];
+      if (pr_cur != kBoundary) load_states(tv.state + i0, tv.N, tv.mech[pr_cur], cur);
     }
-    for (int i = tid; i < tv.n_real; i += T) {
+    for (int i = i0; i < gr.node_end; i += gT) {
       NodeStates<Real> nxt;
       uint16_t pr_nxt = kBoundary;
-      if (i + T < tv.n_real) {
-        pr_nxt = tv.pidx[i + T];
-        if (pr_nxt != kBoundary) load_states(tv.state + i + T, tv.N, tv.mech[pr_nxt], nxt);
+      if (i + gT < gr.node_end) {
+        pr_nxt = tv.pidx[i + gT];
+        if (pr_nxt != kBoundary) load_states(tv.state + i + gT, tv.N, tv.mech[pr_nxt], nxt);
       }
       const Pair<Real> vv = tv.v[i];
       Real hi = vv.x, lo = vv.y;
@@ -1543,7 +1560,7 @@ __global__ void __launch_bounds__(kVar == 2 ? BC_PORT_MAX_THREADS : 1024, kVar =
       const uint16_t pr = pr_cur;
       Real G = Real(0), I = Real(0);
       if (pr != kBoundary)
-        node_mechanisms_loaded<Real, kExtra>(cur, tv.state + i, tv.N, tv.params + size_t(pr) * BC_NPARAM, tv.mech[pr],
+        node_mechanisms_loaded<Real, kExtra>(cur, tv.state + i, tv.N, tv.params + size_t(pr) * kParamStride, tv.mech[pr],
                                              v_old, hi, dt, true, G, I);
       cur = nxt;
       pr_cur = pr_nxt;
@@ -1577,7 +1594,7 @@ __global__ void __launch_bounds__(kVar == 2 ? BC_PORT_MAX_THREADS : 1024, kVar =
         if (!last) add_node_pulses(tv, pulses, sr, i, pr, step + 1, dt);
       }
     }
-    __syncthreads();
+    group_sync(grouped, grp, gT);
     if (kExtra && record && td.n_xprobes > 0) {
       // mechanism probes (plans with them run the extra variant): state views after the update
       const ProbeRef* pl = reinterpret_cast<const ProbeRef*>(reinterpret_cast<const unsigned char*>(tv.specs) +
@@ -1590,7 +1607,7 @@ __global__ void __launch_bounds__(kVar == 2 ? BC_PORT_MAX_THREADS : 1024, kVar =
         if (r.field >= BC_PROBE_CURRENT) {
           const uint16_t pr = tv.pidx[r.node];
           const Pair<Real> vv = tv.v[r.node];
-          val = probe_current(tv.state + r.node, tv.N, tv.params + size_t(pr) * BC_NPARAM, tv.mech[pr], vv.x + vv.y,
+          val = probe_current(tv.state + r.node, tv.N, tv.params + size_t(pr) * kParamStride, tv.mech[pr], vv.x + vv.y,
                               r.field - BC_PROBE_CURRENT);
         } else {
           val = probe_state(tv.state + r.node, tv.N, r.field);
@@ -1659,7 +1676,7 @@ __global__ void reset_kernel(LaunchArgs a, const double* vinit, const int64_t* v
     tv.state[size_t(kSlotVLastLo) * tv.N + i] = Real(0);
     const uint16_t pr = tv.pidx[i];
     if (pr == kBoundary) continue;
-    const Real* P = tv.params + size_t(pr) * BC_NPARAM;
+    const Real* P = tv.params + size_t(pr) * kParamStride;
     steady_states(P, tv.mech[pr], tv.state + i, tv.N, v);
   }
 }

@@ -404,10 +404,12 @@ class SurrogateRun:
     launches: int                 # kernel launches: resets, reduced-plan launches, fallback launches
     spikes: list                  # per cell: soma spike times (ms), fallback cells from the full solve
     traces: np.ndarray | None = None  # [n_cells, T] soma voltage when record_every > 0
+    full_cells: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int64))  # kept at full morphology
 
     @property
     def fallback_rate(self) -> float:
-        return float(self.fallback_cells.size) / max(len(self.spikes), 1)
+        """Fallbacks over the cells that ran with ports."""
+        return float(self.fallback_cells.size) / max(len(self.spikes) - self.full_cells.size, 1)
 
 
 class SurrogateRunner:
@@ -421,7 +423,12 @@ class SurrogateRunner:
     the network."""
 
     def __init__(self, descs, model: SurrogateModel | None, *, precision: str = "f32", record_every: int = 0,
-                 device: int = 0, plan_kw: dict | None = None, fallback: bool = True):
+                 device: int = 0, plan_kw: dict | None = None, fallback: bool = True, full_cells=None,
+                 full_plan_kw: dict | None = None):
+        """``full_cells``: indices of cells that keep their full morphology for the
+        whole run (a mixed population); they run from t = 0 in a plain plan of
+        their own (``full_plan_kw``, default: the fallback's launch shape) on a
+        stream beside the reduced launches."""
         from .gru import NPARAM
         from .runtime import Plan
 
@@ -433,9 +440,18 @@ class SurrogateRunner:
         for k in ("threads_per_tile", "threads_big", "threads_global"):
             self.plan_kw.setdefault(k, PORT_THREADS)
         self.fallback = fallback and model is not None
-        red, ports = zip(*[reduce_desc(d, model.cut_depth if model else CUT_DEPTH) for d in self.descs])
-        red = [replace(r, probes=[(0, 0.5)]) for r in red]
-        self.batch = ports_to_batch(list(red), list(ports))
+        n = len(self.descs)
+        full = np.zeros(n, bool)
+        if full_cells is not None:
+            full[np.asarray(full_cells, dtype=np.int64)] = True
+        self.full_idx = np.nonzero(full)[0]
+        self.red_idx = np.nonzero(~full)[0]
+        red, ports = [], []
+        for i in self.red_idx:
+            r, pts = reduce_desc(self.descs[i], model.cut_depth if model else CUT_DEPTH)
+            red.append(replace(r, probes=[(0, 0.5)]))
+            ports.append(pts)
+        self.batch = ports_to_batch(red, ports)
         self.plan = Plan(self.batch, precision=precision, record_every=record_every, max_spikes=256, device=device,
                          **self.plan_kw)
         self.n_ports = int(self.batch.port_cell.size)
@@ -444,6 +460,12 @@ class SurrogateRunner:
                 self.plan.set_surrogate(np.zeros(NPARAM, np.float32), (V_SCALE, 1.0, -1e4, 1e4, 1e9))
             else:
                 self.plan.set_surrogate(model.theta, model.norm())
+        self.full_plan = None
+        if self.full_idx.size:
+            fd = [replace(self.descs[i], probes=[(0, 0.5)]) for i in self.full_idx]
+            kw = dict(full_plan_kw) if full_plan_kw is not None else fallback_plan_options(fd, self.plan_kw)
+            self.full_plan = Plan(descs_to_batch(fd), precision=precision, record_every=record_every, max_spikes=256,
+                                  device=device, **kw)
         self.full_cv = int(sum(int(sum(d.ncv)) for d in self.descs))
 
     def _fallback_plan(self, cells):
@@ -479,12 +501,20 @@ class SurrogateRunner:
         plan = self.plan
         main = self._main
         sid = int(main.cuda_stream)
-        n = len(self.descs)
+        n_red = self.red_idx.size
         spl = int(plan.info["steps_per_launch"])
         watch = self.fallback and self.n_ports > 0
         t0 = time.perf_counter()
         plan.reset(stream=sid)
-        flagged = np.zeros(n, bool)
+        if self.full_plan is not None:
+            # the full-morphology cells of a mixed population: the whole run, enqueued
+            # at once on their own stream, beside the reduced launches
+            if not hasattr(self, "_full_stream"):
+                self._full_stream = torch.cuda.Stream(self.device)
+            fs = int(self._full_stream.cuda_stream)
+            self.full_plan.reset(stream=fs)
+            self.full_plan.run(n_steps, dt, stream=fs, check=False)
+        flagged = np.zeros(n_red, bool)
         fallbacks = []
         if not hasattr(self, "_flag_stream"):
             self._flag_stream = torch.cuda.Stream(self.device)
@@ -527,40 +557,63 @@ class SurrogateRunner:
                     # next free SM slots ahead of the queued reduced launches, so the
                     # full solve runs at its own step latency
                     side = torch.cuda.Stream(self.device, priority=-1)
-                    fp = self._fallback_plan(new)
+                    fp = self._fallback_plan(self.red_idx[new])
                     fp.run(n_steps, dt, stream=int(side.cuda_stream), check=False)
                     fallbacks.append((new, fp, side))
         plan.check(stream=sid)
         for _, fp, side in fallbacks:
             fp.check(stream=int(side.cuda_stream))
+        if self.full_plan is not None:
+            self.full_plan.check(stream=int(self._full_stream.cuda_stream))
         torch.cuda.synchronize(self.device)
         wall = (time.perf_counter() - t0) * 1e3
-        spikes = plan.spikes(stream=sid)
-        traces = plan.traces(stream=sid) if self.record_every else None
-        fb_launches = 0
+        n = len(self.descs)
+        spikes = [None] * n
+        traces = None
+        red_sp = plan.spikes(stream=sid)
+        red_tr = plan.traces(stream=sid) if self.record_every else None
+        if red_tr is not None or self.full_plan is not None and self.record_every:
+            T = (red_tr if red_tr is not None else self.full_plan.traces()).shape[1]
+            traces = np.zeros((n, T))
+        for j, i in enumerate(self.red_idx):
+            spikes[i] = red_sp[j]
+            if traces is not None and red_tr is not None:
+                traces[i] = red_tr[j]
+        launches = 1 + -(-n_steps // spl) * int(plan.info["n_launch_classes"])
+        if self.full_plan is not None:
+            fp = self.full_plan
+            launches += 1 + -(-n_steps // int(fp.info["steps_per_launch"])) * int(fp.info["n_launch_classes"])
+            fsp = fp.spikes()
+            ftr = fp.traces() if self.record_every else None
+            for j, i in enumerate(self.full_idx):
+                spikes[i] = fsp[j]
+                if traces is not None:
+                    traces[i] = ftr[j]
         for cells, fp, side in fallbacks:
-            fb_launches += 1 + -(-n_steps // int(fp.info["steps_per_launch"])) * int(fp.info["n_launch_classes"])
+            launches += 1 + -(-n_steps // int(fp.info["steps_per_launch"])) * int(fp.info["n_launch_classes"])
             fsp = fp.spikes(stream=int(side.cuda_stream))
             ftr = fp.traces(stream=int(side.cuda_stream)) if self.record_every else None
-            for j, i in enumerate(cells):
+            for j, i in enumerate(self.red_idx[cells]):
                 spikes[i] = fsp[j]
                 if traces is not None:
                     traces[i] = ftr[j]
             fp.close()
-        launches = 1 + -(-n_steps // spl) * int(plan.info["n_launch_classes"])
         return SurrogateRun(reduced_cv=int(plan.n_cv), full_cv=self.full_cv, n_ports=self.n_ports,
-                            fallback_cells=np.nonzero(flagged)[0], wall_ms=wall, launches=launches + fb_launches,
-                            spikes=list(spikes), traces=traces)
+                            fallback_cells=self.red_idx[np.nonzero(flagged)[0]], wall_ms=wall, launches=launches,
+                            spikes=list(spikes), traces=traces, full_cells=self.full_idx)
 
     def close(self) -> None:
         self.plan.close()
+        if self.full_plan is not None:
+            self.full_plan.close()
 
 
 def run_surrogate(descs, model: SurrogateModel | None, n_steps: int, dt: float = 0.025, *, precision: str = "f32",
-                  record_every: int = 0, fallback: bool = True, device: int = 0, plan_kw: dict | None = None):
+                  record_every: int = 0, fallback: bool = True, device: int = 0, plan_kw: dict | None = None,
+                  full_cells=None):
     """One run of :class:`SurrogateRunner` (the plan is built and released here)."""
     r = SurrogateRunner(descs, model, precision=precision, record_every=record_every, device=device,
-                        plan_kw=plan_kw, fallback=fallback)
+                        plan_kw=plan_kw, fallback=fallback, full_cells=full_cells)
     try:
         return r.run(n_steps, dt)
     finally:

@@ -243,7 +243,11 @@ typedef struct bc_plan_options {
   float reserved_b;         /* must be 0                                             */
   int32_t dry_run;          /* 1: lower and schedule only (no CUDA calls); the plan
                                answers bc_plan_info / bc_plan_tile_stats only         */
-  int32_t reserved[2];
+  int32_t warp_groups;      /* independent warp groups per tile (1..15): the tile's
+                               cells are split into groups, each run by its own warps
+                               on a barrier of its own; plans that use the extra or
+                               port kernel variant always use 1; 0 = auto (1)      */
+  int32_t reserved[1];
 } bc_plan_options;
 
 typedef struct bc_plan* bc_plan_t;

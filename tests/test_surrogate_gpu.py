@@ -192,6 +192,34 @@ def test_fallback_replaces_flagged_cells_with_the_full_solve(native_lib, cuda_de
     np.testing.assert_allclose(r.traces[r.fallback_cells], full.traces(), rtol=0, atol=1e-9)
 
 
+def test_mixed_population_full_cells_match_the_plain_solve(native_lib, cuda_device):
+    # a mixed population (some cells keep their full morphology from t = 0, the rest
+    # run with ports and fallback): the full cells are exactly the plain solve's,
+    # the port cells exactly those of an unmixed surrogate run
+    from dataclasses import replace
+
+    from braincell_gb300 import surrogate as S
+
+    m = S.load_model(S.PACKAGED_MODEL)
+    descs = W.uneven(20, seed=4)
+    full_idx = np.array([1, 4, 5, 11, 17])
+    r = S.run_surrogate(descs, m, 2000, record_every=1, fallback=True, full_cells=full_idx)
+    assert np.array_equal(r.full_cells, full_idx) and not np.isin(r.fallback_cells, full_idx).any()
+    fd = [replace(descs[i], probes=[(0, 0.5)]) for i in full_idx]
+    ref = Plan(W.descs_to_batch(fd), precision="f32", record_every=1, **S.fallback_plan_options(fd, threads=512))
+    ref.run(2000, DT)
+    np.testing.assert_allclose(r.traces[full_idx], ref.traces(), rtol=0, atol=1e-9)
+    # the port cells as in an unmixed run (tile packing changes the order of the GRU's
+    # per-port partial sums, so agreement is to rounding, judged on the spikes)
+    rest = np.setdiff1d(np.arange(len(descs)), full_idx)
+    alone = S.run_surrogate([descs[i] for i in rest], m, 2000, record_every=1, fallback=True)
+    for j, i in enumerate(rest):
+        assert len(r.spikes[i]) == len(alone.spikes[j])
+        if len(alone.spikes[j]):
+            assert np.abs(np.asarray(r.spikes[i]) - np.asarray(alone.spikes[j])).max() <= 0.05
+    assert np.array_equal(np.sort(r.fallback_cells), np.sort(rest[alone.fallback_cells]))
+
+
 def test_training_pipeline_learns(native_lib, cuda_device):
     """Trajectories from the plain solver, GPU training with the library's kernels:
     a short run lowers the held-out loss."""
