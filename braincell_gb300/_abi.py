@@ -274,8 +274,7 @@ class PlanOptions(C.Structure):
         ("narrow_lane_nodes", C.c_int32),
         ("reserved_b", C.c_float),
         ("dry_run", C.c_int32),
-        ("warp_groups", C.c_int32),
-        ("reserved", C.c_int32 * 1),
+        ("reserved", C.c_int32 * 2),
     ]
 
 
@@ -346,9 +345,10 @@ SIGNATURES = {
     "bc_gru_forward": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int32,
                                    C.c_int64, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                    C.c_void_p]),
+    "bc_gru_backward_workspace": (C.c_int64, [C.c_int32]),
     "bc_gru_backward": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int32,
                                     C.c_int64, C.c_int32, C.c_void_p, C.c_void_p, C.c_float, C.c_void_p,
-                                    C.c_void_p]),
+                                    C.c_void_p, C.c_void_p]),
     "bc_gru_grad_sqnorm": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "bc_gru_adam": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_float, C.c_float,
                                 C.c_float, C.c_float, C.c_float, C.c_void_p]),

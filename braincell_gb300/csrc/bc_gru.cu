@@ -55,7 +55,7 @@ struct BwdArgs {
   const float* acts;
   const float* yout;
   float gscale;
-  float* grads;
+  float* partial;  // [gridDim.x][kGruNParam]: this CTA's gradient, every entry written
 };
 
 __device__ __forceinline__ size_t act_index(int k, int batch, int T, int b, int t, int j) {
@@ -300,16 +300,17 @@ __global__ void __launch_bounds__(kThreads) gru_bwd_kernel(BwdArgs a) {
       carry[e] = dh_dir[e] + dHs[cur][row][j];
     }
   }
-  float* G = a.grads;
+  // This CTA's gradient goes to its own row of the partial buffer, each entry
+  // written by exactly one lane; bc_gru_backward then sums the rows in CTA order,
+  // so the gradient is the same bit for bit on every run.
+  float* G = a.partial + size_t(blockIdx.x) * kGruNParam;
 #pragma unroll
   for (int i = 0; i < 12; ++i) {
     const int q = 12 * w + i;
     const int mi = q >> 3, ni = q & 7;
     const int n0 = mi * 16 + g, k0 = ni * 8 + 2 * tq;
-    atomicAdd(&G[kGruOffWh + n0 * kGruH + k0], accw[i][0]);
-    atomicAdd(&G[kGruOffWh + n0 * kGruH + k0 + 1], accw[i][1]);
-    atomicAdd(&G[kGruOffWh + (n0 + 8) * kGruH + k0], accw[i][2]);
-    atomicAdd(&G[kGruOffWh + (n0 + 8) * kGruH + k0 + 1], accw[i][3]);
+    *reinterpret_cast<float2*>(&G[kGruOffWh + n0 * kGruH + k0]) = make_float2(accw[i][0], accw[i][1]);
+    *reinterpret_cast<float2*>(&G[kGruOffWh + (n0 + 8) * kGruH + k0]) = make_float2(accw[i][2], accw[i][3]);
   }
   // the per-unit sums: reduce over the 8 lanes that share a unit (same tq)
 #pragma unroll
@@ -323,7 +324,7 @@ __global__ void __launch_bounds__(kThreads) gru_bwd_kernel(BwdArgs a) {
         v += __shfl_xor_sync(0xffffffffu, v, 4);
         v += __shfl_xor_sync(0xffffffffu, v, 8);
         v += __shfl_xor_sync(0xffffffffu, v, 16);
-        if (g == 0) atomicAdd(&G[kGruOffWx + (q * kGruH + j) * kGruX + i], v);
+        if (g == 0) G[kGruOffWx + (q * kGruH + j) * kGruX + i] = v;
       }
       float vb = gbx[q][u], vh = gbh[q][u];
       vb += __shfl_xor_sync(0xffffffffu, vb, 4);
@@ -333,21 +334,30 @@ __global__ void __launch_bounds__(kThreads) gru_bwd_kernel(BwdArgs a) {
       vh += __shfl_xor_sync(0xffffffffu, vh, 8);
       vh += __shfl_xor_sync(0xffffffffu, vh, 16);
       if (g == 0) {
-        atomicAdd(&G[kGruOffBx + q * kGruH + j], vb);
-        atomicAdd(&G[kGruOffBh + q * kGruH + j], vh);
+        G[kGruOffBx + q * kGruH + j] = vb;
+        G[kGruOffBh + q * kGruH + j] = vh;
       }
     }
     float vo = gwo[u];
     vo += __shfl_xor_sync(0xffffffffu, vo, 4);
     vo += __shfl_xor_sync(0xffffffffu, vo, 8);
     vo += __shfl_xor_sync(0xffffffffu, vo, 16);
-    if (g == 0) atomicAdd(&G[kGruOffWo + j], vo);
+    if (g == 0) G[kGruOffWo + j] = vo;
   }
   if (w == 0) {
     float vb = tq == 0 ? gbo : 0.0f;
 #pragma unroll
     for (int s = 1; s < 32; s <<= 1) vb += __shfl_xor_sync(0xffffffffu, vb, s);
-    if (lane == 0) atomicAdd(&G[kGruOffBo], vb);
+    if (lane == 0) G[kGruOffBo] = vb;
+  }
+}
+
+// grads[i] += sum over the CTAs c = 0, 1, ... of partial[c][i], in that order.
+__global__ void gru_grad_reduce_kernel(const float* partial, int n_cta, float* grads) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < kGruNParam; i += gridDim.x * blockDim.x) {
+    float s = 0.0f;
+    for (int c = 0; c < n_cta; ++c) s += partial[size_t(c) * kGruNParam + i];
+    grads[i] += s;
   }
 }
 
@@ -434,16 +444,25 @@ bc_status bc_gru_forward(const float* params, const uint32_t* wext, const float*
   return launch_status(cudaGetLastError(), "gru_fwd_kernel");
 }
 
+int64_t bc_gru_backward_workspace(int32_t batch) {
+  return batch > 0 ? int64_t((batch + kRows - 1) / kRows) * kGruNParam : 0;
+}
+
 bc_status bc_gru_backward(const float* params, const uint32_t* wht, const float* x, const float* y, int64_t t_total,
                           const int32_t* seq, int32_t batch, int64_t t0, int32_t T, const float* acts,
-                          const float* yout, float gscale, float* grads, void* stream) {
-  if (!params || !wht || !x || !y || !seq || !acts || !yout || !grads)
+                          const float* yout, float gscale, float* grads, float* workspace, void* stream) {
+  if (!params || !wht || !x || !y || !seq || !acts || !yout || !grads || !workspace)
     return fail(BC_ERR_INVALID, "bc_gru_backward: null buffer");
   if (batch <= 0 || T <= 0 || t0 < 0 || t0 + T > t_total)
     return fail(BC_ERR_INVALID, "bc_gru_backward: window outside the sequences");
-  BwdArgs a{params, wht, x, y, t_total, seq, batch, t0, T, acts, yout, gscale, grads};
-  gru_bwd_kernel<<<(batch + kRows - 1) / kRows, kThreads, 0, static_cast<cudaStream_t>(stream)>>>(a);
-  return launch_status(cudaGetLastError(), "gru_bwd_kernel");
+  const int n_cta = (batch + kRows - 1) / kRows;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  BwdArgs a{params, wht, x, y, t_total, seq, batch, t0, T, acts, yout, gscale, workspace};
+  gru_bwd_kernel<<<n_cta, kThreads, 0, st>>>(a);
+  bc_status s = launch_status(cudaGetLastError(), "gru_bwd_kernel");
+  if (s != BC_OK) return s;
+  gru_grad_reduce_kernel<<<(kGruNParam + 255) / 256, 256, 0, st>>>(workspace, n_cta, grads);
+  return launch_status(cudaGetLastError(), "gru_grad_reduce_kernel");
 }
 
 bc_status bc_gru_grad_sqnorm(const float* grads, float* out, void* stream) {

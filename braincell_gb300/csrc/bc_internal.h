@@ -79,15 +79,6 @@ struct SlotRec {
   uint16_t off[32];
 };
 
-// A warp group of a tile: warps [warp_begin, warp_begin + n_warps) run the tree
-// phases phase_begin .. phase_begin + n_phases - 1 of the tile's phase table (whose
-// slots hold only the group's cells) and update nodes [node_begin, node_end),
-// synchronising on a barrier of their own.
-struct GroupRec {
-  int32_t warp_begin, n_warps, phase_begin, n_phases, node_begin, node_end;
-  int32_t pad[2];
-};
-
 // Per-tile descriptor (global memory, read-only).
 struct TileDesc {
   int64_t blob_offset;      // bytes into the plan's blob buffer (16-B aligned)
@@ -125,8 +116,6 @@ struct TileDesc {
   int32_t off_pstage;       // the GRU weight fragments and wo (kGruSmemBytes), then per-port staging
                             // records (PortStage), then PortLocal records, inside the
                             // scratch area; -1: none
-  int32_t n_groups;         // warp groups (GroupRec table at off_groups); 1 = the whole CTA
-  int32_t off_groups;
 };
 
 // ------------------------------------------------------------- subtree surrogate

@@ -1377,15 +1377,6 @@ __device__ __forceinline__ bool is_finite_real(Real x) {
   return isfinite(x);
 }
 
-// Barrier of a warp group: the named barrier 1 + g over the group's threads, or the
-// CTA barrier when the tile is one group.
-__device__ __forceinline__ void group_sync(bool grouped, int g, int n_threads) {
-  if (grouped)
-    asm volatile("bar.sync %0, %1;" ::"r"(1 + g), "r"(n_threads) : "memory");
-  else
-    __syncthreads();
-}
-
 // ------------------------------------------------------------------ the step kernel
 // kVar: 0 = lean (no optional mechanism), 1 = extra (synapses, network,
 // out-of-line channels), 2 = extra + subtree-surrogate ports.
@@ -1506,25 +1497,18 @@ __global__ void __launch_bounds__(kVar == 2 ? BC_PORT_MAX_THREADS : 1024, kVar =
   do {                \
   } while (0)
 #endif
-  // This warp's group: its own phases, nodes and barrier (td.n_groups = 1: the CTA).
-  const GroupRec* groups = reinterpret_cast<const GroupRec*>(base + td.off_groups);
-  int grp = 0;
-  while (grp + 1 < td.n_groups && warp >= groups[grp + 1].warp_begin) ++grp;
-  const GroupRec gr = groups[grp];
-  const bool grouped = td.n_groups > 1;
-  const int gwarp = warp - gr.warp_begin, gT = gr.n_warps * 32, gtid = tid - gr.warp_begin * 32;
   for (int s = 0; s < a.n_steps; ++s) {
     const int64_t step = a.step0 + s;
     // forward elimination, leaves first
-    for (int p = 0; p < gr.n_phases; ++p) {
-      eliminate_phase<Real, kSmem>(tv, gr.phase_begin + p, gwarp, gr.n_warps, lane, dt);
-      group_sync(grouped, grp, gT);
+    for (int p = 0; p < tv.n_phases; ++p) {
+      eliminate_phase<Real, kSmem>(tv, p, warp, n_warps, lane, dt);
+      __syncthreads();
     }
     BC_TICK(0);
     // back-substitution, root first
-    for (int p = gr.n_phases - 1; p >= 0; --p) {
-      backsub_phase<Real, kSmem>(tv, gr.phase_begin + p, gwarp, gr.n_warps, lane, dt);
-      group_sync(grouped, grp, gT);
+    for (int p = tv.n_phases - 1; p >= 0; --p) {
+      backsub_phase<Real, kSmem>(tv, p, warp, n_warps, lane, dt);
+      __syncthreads();
     }
     BC_TICK(1);
     // V update, mechanism states, next row, probes and next pulses
@@ -1535,17 +1519,16 @@ __global__ void __launch_bounds__(kVar == 2 ? BC_PORT_MAX_THREADS : 1024, kVar =
     // iteration ahead so that their latency overlaps this node's arithmetic.
     NodeStates<Real> cur;
     uint16_t pr_cur = kBoundary;
-    const int i0 = gr.node_begin + gtid;
-    if (i0 < gr.node_end) {
-      pr_cur = tv.pidx[i0];
-      if (pr_cur != kBoundary) load_states(tv.state + i0, tv.N, tv.mech[pr_cur], cur);
+    if (tid < tv.n_real) {
+      pr_cur = tv.pidx[tid];
+      if (pr_cur != kBoundary) load_states(tv.state + tid, tv.N, tv.mech[pr_cur], cur);
     }
-    for (int i = i0; i < gr.node_end; i += gT) {
+    for (int i = tid; i < tv.n_real; i += T) {
       NodeStates<Real> nxt;
       uint16_t pr_nxt = kBoundary;
-      if (i + gT < gr.node_end) {
-        pr_nxt = tv.pidx[i + gT];
-        if (pr_nxt != kBoundary) load_states(tv.state + i + gT, tv.N, tv.mech[pr_nxt], nxt);
+      if (i + T < tv.n_real) {
+        pr_nxt = tv.pidx[i + T];
+        if (pr_nxt != kBoundary) load_states(tv.state + i + T, tv.N, tv.mech[pr_nxt], nxt);
       }
       const Pair<Real> vv = tv.v[i];
       Real hi = vv.x, lo = vv.y;
@@ -1594,7 +1577,7 @@ __global__ void __launch_bounds__(kVar == 2 ? BC_PORT_MAX_THREADS : 1024, kVar =
         if (!last) add_node_pulses(tv, pulses, sr, i, pr, step + 1, dt);
       }
     }
-    group_sync(grouped, grp, gT);
+    __syncthreads();
     if (kExtra && record && td.n_xprobes > 0) {
       // mechanism probes (plans with them run the extra variant): state views after the update
       const ProbeRef* pl = reinterpret_cast<const ProbeRef*>(reinterpret_cast<const unsigned char*>(tv.specs) +

@@ -67,7 +67,6 @@ struct bc_plan {
   int tile_nodes = 0;
   int lane_nodes = 1;
   int narrow_lane_nodes = 1;
-  int warp_groups = 1;
   int steps_per_launch = 1000;
   int record_every = 1;
   int max_spikes = 64;
@@ -359,7 +358,6 @@ struct BuildCtx {
   int state_slots;
   int lane_nodes;  // nodes a lane walks serially in a warp slot
   int narrow_lane_nodes;  // the same in phases with fewer nodes than 32 x warps
-  int warp_groups;  // independent warp groups per tile (1: the whole CTA is one group)
 };
 
 template <typename Real>
@@ -397,59 +395,15 @@ static bc_status build_tile(const BuildCtx& cx, const TileBuild& tb, int T, Tile
     n_real += lc.n_node;
   }
   const int W = std::max(1, T / 32);
-  // -------- warp groups: the tile's cells split into G groups of whole cells, each
-  // run by its own warps, which synchronise among themselves only (a named barrier
-  // per group), so that the tree levels of one group do not wait for another's.
-  // Cells go to the least-loaded group (by nodes, largest first); warps are dealt
-  // out in proportion to the groups' nodes, at least one each.
-  const int G = std::max(1, std::min({cx.warp_groups, W, 15, int(cell_list.size())}));
-  std::vector<std::vector<size_t>> gcells(G);
-  std::vector<int64_t> gload(G, 0);
-  {
-    std::vector<size_t> ord(cell_list.size());
-    std::iota(ord.begin(), ord.end(), size_t(0));
-    std::stable_sort(ord.begin(), ord.end(), [&](size_t a, size_t b) {
-      return (*cx.cells)[cell_list[a]].n_node > (*cx.cells)[cell_list[b]].n_node;
-    });
-    for (size_t li : ord) {
-      const int g = int(std::min_element(gload.begin(), gload.end()) - gload.begin());
-      gcells[g].push_back(li);
-      gload[g] += (*cx.cells)[cell_list[li]].n_node;
-    }
-    for (auto& v : gcells) std::sort(v.begin(), v.end());
-  }
-  std::vector<int32_t> gwarps(G, 1);
-  {
-    const int64_t total = std::max<int64_t>(1, std::accumulate(gload.begin(), gload.end(), int64_t(0)));
-    int left = W - G;
-    // largest remainders: proportional shares of the W - G warps beyond the first
-    std::vector<std::pair<double, int>> rem;
-    for (int g = 0; g < G; ++g) {
-      const double want = double(W) * double(gload[g]) / double(total) - 1.0;
-      const int base = std::max(0, std::min(left, int(want)));
-      gwarps[g] += base;
-      left -= base;
-      rem.push_back({want - base, g});
-    }
-    std::sort(rem.begin(), rem.end(), [](const std::pair<double, int>& a, const std::pair<double, int>& b) {
-      return a.first > b.first;
-    });
-    for (size_t q = 0; left > 0; q = (q + 1) % rem.size(), --left) gwarps[rem[q].second] += 1;
-  }
   const int C_wide = std::max(1, cx.lane_nodes);
   const int C_narrow = cx.narrow_lane_nodes > 0 ? cx.narrow_lane_nodes : C_wide;
   std::vector<ChainRec> chains;
   std::vector<RecSpec> rec_src;
   std::vector<SlotRec> slots;
-  std::vector<int32_t> phase_ptr;
-  std::vector<GroupRec> groups(G);
   int32_t next_node = 0;
   int64_t crit = 0;
-  int n_phases_max = 0;
-  int32_t warp_at = 0;
-  for (int g = 0; g < G; ++g) {
   std::vector<std::vector<CRef>> levels;
-  for (size_t li : gcells[g]) {
+  for (size_t li = 0; li < cell_list.size(); ++li) {
     const CellSched& cs = (*cx.sched)[cell_list[li]];
     for (size_t k = 0; k < cs.chains.size(); ++k) {
       const int32_t lv = cs.chains[k].level;
@@ -461,17 +415,7 @@ static bc_status build_tile(const BuildCtx& cx, const TileBuild& tb, int T, Tile
   for (auto& v : levels)
     if (!v.empty()) phases.push_back(std::move(v));
   const int n_phases = int(phases.size());
-  const int Wg = gwarps[g];
-  GroupRec& gr = groups[g];
-  gr.warp_begin = warp_at;
-  gr.n_warps = Wg;
-  gr.phase_begin = int32_t(phase_ptr.size());
-  gr.n_phases = n_phases;
-  gr.node_begin = next_node;
-  warp_at += Wg;
-  n_phases_max = std::max(n_phases_max, n_phases);
-  phase_ptr.resize(phase_ptr.size() + size_t(n_phases) + 1, 0);
-  int64_t gcrit = 0;
+  std::vector<int32_t> phase_ptr(size_t(n_phases) + 1, 0);
   // A lane plan: the chains (whole, or one chain's part) of one lane.
   struct Lane {
     std::vector<CRef> whole;  // serial slots: whole chains
@@ -491,7 +435,7 @@ static bc_status build_tile(const BuildCtx& cx, const TileBuild& tb, int T, Tile
     // chains there are walked serially (C_narrow) rather than scanned
     int64_t phase_nodes = 0;
     for (const CRef& c : v) phase_nodes += c.L;
-    const int C = phase_nodes < int64_t(32) * Wg ? C_narrow : C_wide;
+    const int C = phase_nodes < int64_t(32) * W ? C_narrow : C_wide;
     std::vector<Slot> ps;
     // chains longer than a lane's share: split into near-equal parts over lanes
     std::vector<Lane> lanes;
@@ -552,8 +496,8 @@ static bc_status build_tile(const BuildCtx& cx, const TileBuild& tb, int T, Tile
     }
     // dearest slots first: warp w takes slots w, w + W, ...
     std::stable_sort(ps.begin(), ps.end(), [](const Slot& a, const Slot& b) { return a.cost > b.cost; });
-    std::vector<int64_t> warp_cost(Wg, 0);
-    phase_ptr[size_t(gr.phase_begin) + p] = int32_t(slots.size());
+    std::vector<int64_t> warp_cost(W, 0);
+    phase_ptr[p] = int32_t(slots.size());
     for (size_t si = 0; si < ps.size(); ++si) {
       const Slot& s = ps[si];
       SlotRec sr{};
@@ -593,15 +537,11 @@ static bc_status build_tile(const BuildCtx& cx, const TileBuild& tb, int T, Tile
       sr.unit = uint8_t(s.scan && sr.n_count == lane ? 1 : 0);
       for (; lane < 32; ++lane) sr.off[lane] = uint16_t(sr.n_count);
       slots.push_back(sr);
-      warp_cost[si % Wg] += s.cost;
+      warp_cost[si % W] += s.cost;
     }
-    gcrit += *std::max_element(warp_cost.begin(), warp_cost.end());
+    crit += *std::max_element(warp_cost.begin(), warp_cost.end());
   }
-  phase_ptr[size_t(gr.phase_begin) + n_phases] = int32_t(slots.size());
-  gr.node_end = next_node;
-  crit = std::max(crit, gcrit);
-  }  // warp groups
-  const int n_phases = n_phases_max;
+  phase_ptr[n_phases] = int32_t(slots.size());
   out.crit = crit;
   if (chains.size() >= 0xFFFF) return fail(BC_ERR_CAPACITY, "too many chains in one tile");
   // -------- links: parents and contribution slots
@@ -690,9 +630,6 @@ static bc_status build_tile(const BuildCtx& cx, const TileBuild& tb, int T, Tile
   off = align16(off + slots.size() * sizeof(SlotRec));
   d.off_phase = int32_t(off);
   off = align16(off + phase_ptr.size() * 4);
-  d.off_groups = int32_t(off);
-  d.n_groups = G;
-  off = align16(off + groups.size() * sizeof(GroupRec));
   d.off_crec = int32_t(off);
   off = align16(off + N * 2);
   d.off_params = int32_t(off);
@@ -893,7 +830,6 @@ static bc_status build_tile(const BuildCtx& cx, const TileBuild& tb, int T, Tile
   std::memcpy(b.data() + d.off_chains, chains.data(), chains.size() * sizeof(ChainRec));
   if (!slots.empty()) std::memcpy(b.data() + d.off_slots, slots.data(), slots.size() * sizeof(SlotRec));
   std::memcpy(b.data() + d.off_phase, phase_ptr.data(), phase_ptr.size() * 4);
-  std::memcpy(b.data() + d.off_groups, groups.data(), groups.size() * sizeof(GroupRec));
   std::memcpy(b.data() + d.off_crec, crec.data(), crec.size() * 2);
   out.desc = d;
   return BC_OK;
@@ -1235,11 +1171,6 @@ bc_status bc_plan_create(const bc_batch_spec* spec, const bc_plan_options* opts_
   p->steps_per_launch = opts.steps_per_launch > 0 ? opts.steps_per_launch : 1000;
   p->lane_nodes = opts.lane_nodes > 0 ? opts.lane_nodes : 1;
   p->narrow_lane_nodes = opts.narrow_lane_nodes > 0 ? opts.narrow_lane_nodes : p->lane_nodes;
-  if (opts.warp_groups < 0 || opts.warp_groups > 15) {
-    delete p;
-    return fail(BC_ERR_INVALID, "warp_groups must be 0 (auto) or 1..15");
-  }
-  p->warp_groups = opts.warp_groups > 0 ? opts.warp_groups : 1;
   p->n_cells = s.n_cells;
   // ---------------------------------------------------- lower
   std::vector<LoweredCell> cells(s.n_cells);
@@ -1453,9 +1384,6 @@ bc_status bc_plan_create(const bc_batch_spec* spec, const bc_plan_options* opts_
   p->n_synapses = s.n_synapses;
   p->n_connections = s.n_connections;
   p->extra = p->extra || s.n_synapses > 0 || s.n_connections > 0;
-  // the extra and port variants run CTA-wide passes after the update (probes, spike
-  // records, GRU ports): their tiles are one warp group
-  if (p->extra) p->warp_groups = 1;
   p->syn_tau.assign(s.syn_tau, s.syn_tau + s.n_synapses);
   p->syn_e.assign(s.syn_e, s.syn_e + s.n_synapses);
   p->syn_scale = syn_scale;
@@ -1566,8 +1494,7 @@ bc_status bc_plan_create(const bc_batch_spec* spec, const bc_plan_options* opts_
     if (tile_nodes - nn > 0) room.emplace(tile_nodes - nn, builds.size() - 1);
   }
   BuildCtx cx{&s, &cells, &sched, &cv_base, &cell_pulses, &cell_probes, &pulse_node, &probe_node, &cell_syns, &is_src,
-              &cell_ports, &port_pulse_ids, p->precision, S, p->lane_nodes, p->narrow_lane_nodes,
-              p->warp_groups};
+              &cell_ports, &port_pulse_ids, p->precision, S, p->lane_nodes, p->narrow_lane_nodes};
   std::vector<TileOut> outs;
   outs.reserve(builds.size());
   // Packed tiles: tile_nodes sets how many CTAs share an SM (by the per-node

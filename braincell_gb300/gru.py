@@ -79,6 +79,8 @@ class GRUTrainer:
         theta = init_params(seed) if theta0 is None else np.asarray(theta0, np.float32)
         self.params = torch.as_tensor(theta.copy()).to(self.dev)
         self.grads = torch.zeros(NPARAM, dtype=f32, device=self.dev)
+        # per-CTA gradient rows of the backward, summed in a fixed order
+        self.work = torch.zeros(int(self._lib.bc_gru_backward_workspace(self.batch)), dtype=f32, device=self.dev)
         self.m = torch.zeros(NPARAM, dtype=f32, device=self.dev)
         self.v = torch.zeros(NPARAM, dtype=f32, device=self.dev)
         self.wext = torch.zeros(4 * H * (H + 16) // 2, dtype=torch.int32, device=self.dev)
@@ -113,7 +115,8 @@ class GRUTrainer:
     def backward_window(self, b: int, t0: int, T: int) -> None:
         _abi.check(self._lib.bc_gru_backward(
             _ptr(self.params), _ptr(self.wht), _ptr(self.x), _ptr(self.y), self.t_total, _ptr(self.seq), b, t0, T,
-            _ptr(self.acts), _ptr(self.yout), C.c_float(2.0 / (b * T)), _ptr(self.grads), self._stream()))
+            _ptr(self.acts), _ptr(self.yout), C.c_float(2.0 / (b * T)), _ptr(self.grads), _ptr(self.work),
+            self._stream()))
 
     def adam_step(self) -> None:
         self.step_count += 1

@@ -50,7 +50,6 @@ class Plan:
         threads_big: int = 0,
         threads_global: int = 0,
         dry_run: bool = False,
-        warp_groups: int = 0,
     ) -> None:
         if precision not in _PREC:
             raise ValueError(f"precision must be one of {sorted(_PREC)}, got {precision!r}.")
@@ -73,7 +72,6 @@ class Plan:
         opts.threads_big = int(threads_big)
         opts.threads_global = int(threads_global)
         opts.dry_run = int(bool(dry_run))
-        opts.warp_groups = int(warp_groups)
         spec, keep = batch.to_spec()
         handle = C.c_void_p()
         _abi.check(lib.bc_plan_create(C.byref(spec), C.byref(opts), C.byref(handle)))

@@ -243,11 +243,7 @@ typedef struct bc_plan_options {
   float reserved_b;         /* must be 0                                             */
   int32_t dry_run;          /* 1: lower and schedule only (no CUDA calls); the plan
                                answers bc_plan_info / bc_plan_tile_stats only         */
-  int32_t warp_groups;      /* independent warp groups per tile (1..15): the tile's
-                               cells are split into groups, each run by its own warps
-                               on a barrier of its own; plans that use the extra or
-                               port kernel variant always use 1; 0 = auto (1)      */
-  int32_t reserved[1];
+  int32_t reserved[2];
 } bc_plan_options;
 
 typedef struct bc_plan* bc_plan_t;
@@ -278,7 +274,8 @@ typedef struct bc_plan_info_t {
 const char* bc_last_error(void);
 /* ABI version: major * 10000 + minor * 100 + patch.  0.2.0: the 64-entry parameter
  * record, the A / K2 / KNI mechanisms, named plan-info fields.  0.3.0: the V_last
- * state view (BC_NSTATE_VIEW 25), bc_spike_state_download, bc_pulse_set_amp. */
+ * state view (BC_NSTATE_VIEW 25), bc_spike_state_download, bc_pulse_set_amp, the
+ * workspace of bc_gru_backward (bit-reproducible gradients). */
 #define BC_ABI_VERSION 300
 int32_t bc_version(void);
 /* Fill opts with defaults. */
@@ -466,9 +463,15 @@ bc_status bc_gru_pack(const float* params, uint32_t* wext, uint32_t* wht, void* 
 bc_status bc_gru_forward(const float* params, const uint32_t* wext, const float* x, const float* y, int64_t t_total,
                          const int32_t* seq, int32_t batch, int64_t t0, int32_t T, float* h, float* acts,
                          float* yout, double* loss, void* stream);
+/* The backward writes each CTA's gradient (16 sequences each) into its own row
+   of workspace (bc_gru_backward_workspace(batch) floats, device memory, no
+   initialisation needed) and then adds the rows to grads in a fixed order: the
+   gradient is bit-reproducible from run to run.                              */
+int64_t bc_gru_backward_workspace(int32_t batch);
 bc_status bc_gru_backward(const float* params, const uint32_t* wht, const float* x, const float* y,
                           int64_t t_total, const int32_t* seq, int32_t batch, int64_t t0, int32_t T,
-                          const float* acts, const float* yout, float gscale, float* grads, void* stream);
+                          const float* acts, const float* yout, float gscale, float* grads, float* workspace,
+                          void* stream);
 bc_status bc_gru_grad_sqnorm(const float* grads, float* out, void* stream);
 /* One Adam step (bias-corrected, step >= 1) on params with grads * clip_scale;
    clears grads.                                                                */

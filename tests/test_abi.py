@@ -26,7 +26,7 @@ def declared_functions():
     for fn in sorted(os.listdir(INCLUDE)):
         if fn.endswith(".h"):
             txt = open(os.path.join(INCLUDE, fn)).read()
-            names |= set(re.findall(r"^\s*(?:bc_status|const char\*|int32_t|void)\s+(bc_[a-z0-9_]+)\s*\(", txt, re.M))
+            names |= set(re.findall(r"^\s*(?:bc_status|const char\*|int32_t|int64_t|void)\s+(bc_[a-z0-9_]+)\s*\(", txt, re.M))
     return sorted(names)
 
 

@@ -79,3 +79,21 @@ def test_gru_training_reduces_loss(native_lib, cuda_device):
     th = tr.theta()
     ys, _, _ = G.forward(th.astype(np.float64), x[:4].astype(np.float64), np.zeros((4, G.H)))
     np.testing.assert_allclose(tr.predict(x[:4]), ys, atol=5e-4)
+
+
+def test_backward_gradients_are_bit_reproducible(native_lib, cuda_device):
+    # the per-CTA gradient rows are summed in a fixed order: two runs of the same
+    # window give the same gradient bit for bit (a batch of several CTAs)
+    from braincell_gb300.gru import GRUTrainer
+    from braincell_gb300 import surrogate as S
+
+    m = S.load_model(S.PACKAGED_MODEL)
+    rng = np.random.default_rng(1)
+    x = rng.normal(size=(96, 30, G.X)).astype(np.float32)
+    y = rng.normal(scale=0.5, size=(96, 30)).astype(np.float32)
+    tr = GRUTrainer(x, y, m.theta, batch=96, window=30)
+    ids = np.arange(96)
+    _, g1, _ = tr.gradient(ids, 0, 30)
+    _, g2, _ = tr.gradient(ids, 0, 30)
+    assert np.array_equal(g1, g2)
+    assert np.count_nonzero(g1) > 0.9 * g1.size

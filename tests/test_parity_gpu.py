@@ -174,22 +174,6 @@ def test_warp_count_does_not_change_results():
     np.testing.assert_array_equal(a[3], b[3])
 
 
-@pytest.mark.parametrize("groups", [2, 4, 15])
-def test_warp_groups_match_one_group_and_oracle(groups):
-    # a tile's cells split into independent warp groups (named barriers) give the
-    # same solve as one CTA-wide group: FP64 to rounding, and the oracle's answer
-    descs = W.uneven(indices=range(60))
-    a = _gpu(descs, 300, "f64", warp_groups=1)
-    b = _gpu(descs, 300, "f64", warp_groups=groups)
-    np.testing.assert_allclose(b[3], a[3], rtol=0, atol=1e-10)
-    np.testing.assert_allclose(b[1], a[1], rtol=0, atol=1e-10)
-    for c in (0, 7, 33):
-        _, otr, _ = _oracle(descs[c], 300)
-        assert np.abs(otr - b[1][c]).max() <= TOL_F64_MV
-    f32 = _gpu(descs, 300, "f32", warp_groups=groups)
-    np.testing.assert_allclose(f32[3], a[3], rtol=0, atol=1e-3)
-
-
 def test_global_memory_tiles_f64():
     # one cell too large for shared memory runs from its global-memory blob
     d = W.large(indices=[1], n_range=(4200, 4300), n_branches=40, n_pulses=20, duration=5.0)[0]
