@@ -25,6 +25,10 @@ constexpr int kHPad = kGruH + 8;        // fp32 row stride of the hidden tile
 constexpr int kGPad = kGru3H + 8;       // bf16 row stride of dG [row][n]
 constexpr int kRPad = kRows + 8;        // bf16 row stride of dG^T [n][row] and h^T [k][row]
 constexpr int kDPad = kGruH + 4;        // fp32 row stride of dh [row][k]
+// Row stride (floats) of the per-CTA gradient rows of the backward: kGruNParam
+// rounded up to a multiple of 4, so that every row starts on a 16-byte boundary
+// (the recurrent block is stored as float2 pairs).
+constexpr int kPartialStride = (kGruNParam + 3) & ~3;
 
 struct FwdArgs {
   const float* params;
@@ -55,7 +59,7 @@ struct BwdArgs {
   const float* acts;
   const float* yout;
   float gscale;
-  float* partial;  // [gridDim.x][kGruNParam]: this CTA's gradient, every entry written
+  float* partial;  // [gridDim.x][kPartialStride]: this CTA's gradient, every entry written
 };
 
 __device__ __forceinline__ size_t act_index(int k, int batch, int T, int b, int t, int j) {
@@ -303,7 +307,7 @@ __global__ void __launch_bounds__(kThreads) gru_bwd_kernel(BwdArgs a) {
   // This CTA's gradient goes to its own row of the partial buffer, each entry
   // written by exactly one lane; bc_gru_backward then sums the rows in CTA order,
   // so the gradient is the same bit for bit on every run.
-  float* G = a.partial + size_t(blockIdx.x) * kGruNParam;
+  float* G = a.partial + size_t(blockIdx.x) * kPartialStride;
 #pragma unroll
   for (int i = 0; i < 12; ++i) {
     const int q = 12 * w + i;
@@ -356,7 +360,7 @@ __global__ void __launch_bounds__(kThreads) gru_bwd_kernel(BwdArgs a) {
 __global__ void gru_grad_reduce_kernel(const float* partial, int n_cta, float* grads) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < kGruNParam; i += gridDim.x * blockDim.x) {
     float s = 0.0f;
-    for (int c = 0; c < n_cta; ++c) s += partial[size_t(c) * kGruNParam + i];
+    for (int c = 0; c < n_cta; ++c) s += partial[size_t(c) * kPartialStride + i];
     grads[i] += s;
   }
 }
@@ -445,7 +449,7 @@ bc_status bc_gru_forward(const float* params, const uint32_t* wext, const float*
 }
 
 int64_t bc_gru_backward_workspace(int32_t batch) {
-  return batch > 0 ? int64_t((batch + kRows - 1) / kRows) * kGruNParam : 0;
+  return batch > 0 ? int64_t((batch + kRows - 1) / kRows) * kPartialStride : 0;
 }
 
 bc_status bc_gru_backward(const float* params, const uint32_t* wht, const float* x, const float* y, int64_t t_total,
@@ -455,6 +459,8 @@ bc_status bc_gru_backward(const float* params, const uint32_t* wht, const float*
     return fail(BC_ERR_INVALID, "bc_gru_backward: null buffer");
   if (batch <= 0 || T <= 0 || t0 < 0 || t0 + T > t_total)
     return fail(BC_ERR_INVALID, "bc_gru_backward: window outside the sequences");
+  if (reinterpret_cast<uintptr_t>(workspace) % 16 != 0)
+    return fail(BC_ERR_INVALID, "bc_gru_backward: workspace must be 16-byte aligned");
   const int n_cta = (batch + kRows - 1) / kRows;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   BwdArgs a{params, wht, x, y, t_total, seq, batch, t0, T, acts, yout, gscale, workspace};
