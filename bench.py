@@ -108,13 +108,13 @@ def _peaks():
 
 
 def _traffic_per_node_launch(workload):
-    """Measured DRAM bytes per tile node per launch (ncu summary under profiles/), if present.
+    """Measured DRAM traffic model of the dominant kernel (ncu summary under profiles/).
 
-    Uneven workload: a launch stages each tile's blob into shared memory once and
-    writes V back once, whatever number of steps it fuses, so its traffic scales
-    with the nodes it holds.  Large workload: global-memory tiles, whose traffic per
-    launch scales with nodes x fused steps; the summary gives it per node and step.
-    """
+    A launch moves a fixed part per tile node (the blob staged into shared memory
+    once and V written back once) plus a part per node and fused step (the
+    mechanism states streamed every step, and for global-memory tiles the blob and
+    scratch).  The summary gives both, fitted from ncu captures of launches of two
+    lengths on cases larger than L2."""
     name = {"uneven": "tile_step_uneven.json", "large": "tile_step_large.json"}[workload]
     try:
         with open(os.path.join(ROOT, "profiles", name)) as f:
@@ -415,6 +415,12 @@ def plain_accuracy(a, descs, local, n_oracle=2):
         "cells_with_spike_count_mismatch": mis,
         "spiking_cells": int(sum(1 for x in s64 if len(x))),
     }
+    # the target's own window: spike times over the first 100 ms
+    early = [(np.asarray(x)[np.asarray(x) < 100.0], np.asarray(y)[np.asarray(y) < 100.0]) for x, y in zip(s32, s64)]
+    e100, mis100 = _spike_errors([x for x, _ in early], [y for _, y in early])
+    out["fp32_vs_fp64_gpu"]["first_100_ms"] = {
+        "spike_time_diff_max_ms": float(e100.max()) if e100.size else None, "spikes_paired": int(e100.size),
+        "within_0.05_ms": int((e100 <= 0.05).sum()) if e100.size else 0, "cells_with_spike_count_mismatch": mis100}
     if n_oracle:
         from oracle.staggered import OracleCell
 
@@ -676,10 +682,9 @@ def run_ours(a):
     units_per_launch = n_cv * info["steps_per_launch"]
     prof = _traffic_per_node_launch(a.workload)
     traffic = None
-    if prof and "dram_bytes_per_node_per_launch" in prof:
-        traffic = prof["dram_bytes_per_node_per_launch"] * info["n_nodes"]
-    elif prof and "dram_bytes_per_node_step" in prof:
-        traffic = prof["dram_bytes_per_node_step"] * info["n_nodes"] * info["steps_per_launch"]
+    if prof and "dram_bytes_per_node_step" in prof:
+        traffic = info["n_nodes"] * (prof.get("dram_bytes_per_node_launch_fixed", 0.0)
+                                     + prof["dram_bytes_per_node_step"] * info["steps_per_launch"])
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
         "ms_per_step": ms / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,

@@ -112,6 +112,7 @@ BC_ABI_VERSION = 300
 BC_VARIANT_LEAN = 0
 BC_VARIANT_EXTRA = 1
 BC_VARIANT_PORTS = 2
+BC_VARIANT_PORTS_LEAN = 3
 
 BC_PREC_F32 = 0
 BC_PREC_F64 = 1

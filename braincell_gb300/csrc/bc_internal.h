@@ -290,7 +290,8 @@ struct LaunchArgs {
 // Host-callable launchers implemented in bc_kernels.cu.
 // variant: 0 = the lean kernel; 1 = the plan uses synapses, a network, mechanism
 // probes, or a mechanism of the out-of-line set (classic HH Na / K, M current);
-// 2 = as 1 plus subtree-surrogate ports.
+// 2 = as 1 plus subtree-surrogate ports; 3 = the lean kernel plus ports (a plan
+// whose only optional feature is its ports).
 int launch_tiles(const LaunchArgs& a, int precision, bool smem, int threads, size_t smem_bytes, int variant,
                  void* stream);
 // Kernel-node parameters of the same launch for a CUDA graph.  kernelParams

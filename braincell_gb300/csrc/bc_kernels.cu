@@ -1379,14 +1379,15 @@ __device__ __forceinline__ bool is_finite_real(Real x) {
 
 // ------------------------------------------------------------------ the step kernel
 // kVar: 0 = lean (no optional mechanism), 1 = extra (synapses, network,
-// out-of-line channels), 2 = extra + subtree-surrogate ports.
-// The port variant runs at most BC_PORT_MAX_THREADS threads per CTA and asks for
-// BC_PORT_MIN_CTAS resident CTAs per SM (its register budget).
+// out-of-line channels), 2 = extra + subtree-surrogate ports, 3 = lean + ports
+// (plans whose only optional feature is the ports).
+// The port variants run at most BC_PORT_MAX_THREADS threads per CTA and ask for
+// BC_PORT_MIN_CTAS resident CTAs per SM (their register budget).
 template <typename Real, bool kSmem, int kVar>
-__global__ void __launch_bounds__(kVar == 2 ? BC_PORT_MAX_THREADS : 1024, kVar == 2 ? BC_PORT_MIN_CTAS : 1)
+__global__ void __launch_bounds__(kVar >= 2 ? BC_PORT_MAX_THREADS : 1024, kVar >= 2 ? BC_PORT_MIN_CTAS : 1)
     tile_step_kernel(LaunchArgs a) {
-  constexpr bool kExtra = kVar >= 1;
-  constexpr bool kPorts = kVar == 2;
+  constexpr bool kExtra = kVar == 1 || kVar == 2;
+  constexpr bool kPorts = kVar >= 2;
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) uint64_t bar;
   __shared__ int s_status;
@@ -1721,8 +1722,10 @@ int launch_tiles(const LaunchArgs& a, int precision, bool smem, int threads, siz
       return launch_tiles_x<0>(a, precision, smem, threads, smem_bytes, st);
     case 1:
       return launch_tiles_x<1>(a, precision, smem, threads, smem_bytes, st);
-    default:
+    case 2:
       return launch_tiles_x<2>(a, precision, smem, threads, smem_bytes, st);
+    default:
+      return launch_tiles_x<3>(a, precision, smem, threads, smem_bytes, st);
   }
 }
 
@@ -1765,8 +1768,11 @@ int tile_node_params(const LaunchArgs* a, int precision, bool smem, int threads,
     case 1:
       e = node_x<1>(a, precision, smem, threads, smem_bytes, np);
       break;
-    default:
+    case 2:
       e = node_x<2>(a, precision, smem, threads, smem_bytes, np);
+      break;
+    default:
+      e = node_x<3>(a, precision, smem, threads, smem_bytes, np);
       break;
   }
   np->kernelParams = reinterpret_cast<void**>(const_cast<LaunchArgs**>(hold));

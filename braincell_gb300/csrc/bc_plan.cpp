@@ -900,7 +900,8 @@ static bc_status ensure_traces(bc_plan* p, int64_t records, void* stream) {
 
 // Kernel variant of a plan (see launch_tiles).
 static int kernel_variant(const bc_plan* p) {
-  return p->n_ports > 0 ? BC_VARIANT_PORTS : (p->extra ? BC_VARIANT_EXTRA : BC_VARIANT_LEAN);
+  if (p->n_ports > 0) return p->extra ? BC_VARIANT_PORTS : BC_VARIANT_PORTS_LEAN;
+  return p->extra ? BC_VARIANT_EXTRA : BC_VARIANT_LEAN;
 }
 
 static LaunchArgs base_args(bc_plan* p) {
@@ -1377,7 +1378,6 @@ bc_status bc_plan_create(const bc_batch_spec* spec, const bc_plan_options* opts_
     port_pulse_ids[k].push_back(q);
   }
   p->n_ports = s.n_ports;
-  p->extra = p->extra || s.n_ports > 0;
   // every cell of a network records its spikes (the output of a network run);
   // only cells with connections have events to deliver
   if (s.n_connections > 0) std::fill(is_src.begin(), is_src.end(), char(1));

@@ -264,10 +264,13 @@ typedef struct bc_plan_info_t {
 } bc_plan_info_t;
 /* Step-kernel variants: lean (the main channel mix only), extra (synapses, spike
  * sources, mechanism and current probes, the channels outside the main mix), ports
- * (extra plus subtree-surrogate GRU ports). */
+ * (extra plus subtree-surrogate GRU ports), ports on the lean kernel. */
 #define BC_VARIANT_LEAN 0
 #define BC_VARIANT_EXTRA 1
 #define BC_VARIANT_PORTS 2
+#define BC_VARIANT_PORTS_LEAN 3 /* ports on the lean kernel: plans with ports and no other
+                                   optional feature (no synapses, mechanism probes or
+                                   channels outside the main mix)                  */
 
 /* ------------------------------------------------------------------ entry points */
 /* Thread-local text of the last failure (never NULL). */

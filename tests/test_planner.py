@@ -214,3 +214,24 @@ def test_threaded_planner_reports_the_first_failing_cell(monkeypatch):
             Plan(b, dry_run=True)
         msgs.append(str(e.value))
     assert msgs[0] == msgs[1]
+
+
+def test_ports_pick_the_lean_port_variant_unless_another_feature_needs_the_extra_one():
+    # a plan whose only optional feature is its GRU ports runs the lean kernel with
+    # ports; a mechanism probe beside the ports needs the extra variant's probe pass
+    from dataclasses import replace
+
+    from braincell_gb300 import surrogate as S
+    from braincell_gb300 import workloads as W
+    from braincell_gb300.runtime import Plan
+
+    d = next(x for x in W.uneven(40, seed=1) if S.reduce_desc(x)[1])
+    red, ports = S.reduce_desc(d)
+    b = S.ports_to_batch([replace(red, probes=[(0, 0.5)])], [ports])
+    p = Plan(b, precision="f32", dry_run=True, threads_per_tile=384, threads_big=384, threads_global=384)
+    assert p.info["kernel_variant"] == _abi.BC_VARIANT_PORTS_LEAN
+    p.close()
+    b.probe_field = np.asarray([_abi.BC_STATE_NA_P], np.int32)
+    p = Plan(b, precision="f32", dry_run=True, threads_per_tile=384, threads_big=384, threads_global=384)
+    assert p.info["kernel_variant"] == _abi.BC_VARIANT_PORTS
+    p.close()
