@@ -66,7 +66,9 @@ def _args():
     ap.add_argument("--threads", type=int, default=512)
     ap.add_argument("--threads-big", type=int, default=512)
     ap.add_argument("--steps-per-launch", type=int, default=1000)
-    ap.add_argument("--lane-nodes", type=int, default=1)
+    ap.add_argument("--lane-nodes", type=int, default=10)
+    ap.add_argument("--narrow-lane-nodes", type=int, default=1)
+    ap.add_argument("--lane-cell-nodes", type=int, default=0)
     ap.add_argument("--no-surrogate", action="store_true")
     ap.add_argument("--surrogate-threads", type=int, default=384)
     ap.add_argument("--surrogate-tile-nodes", type=int, default=1800)
@@ -454,7 +456,7 @@ def surrogate_leg(a, descs, local, sid, stream, plain_ms):
     model = S.load_model(os.path.join(ROOT, "braincell_gb300", "data", "surrogate_uneven.npz"))
     T = a.surrogate_threads
     kw = dict(tile_nodes=a.surrogate_tile_nodes, threads_per_tile=T, threads_big=T, threads_global=T,
-              steps_per_launch=a.steps_per_launch, lane_nodes=a.lane_nodes)
+              steps_per_launch=a.steps_per_launch, lane_nodes=a.lane_nodes, narrow_lane_nodes=a.narrow_lane_nodes)
     t0 = time.perf_counter()
     runner = S.SurrogateRunner(descs, model, precision="f32", device=local, plan_kw=kw)
     t_setup = time.perf_counter() - t0
@@ -533,7 +535,7 @@ def mixed_leg(a, local, model, record_every=4):
     # plain form
     plan = Plan(W.descs_to_batch(descs), precision="f32", device=local, tile_nodes=a.tile_nodes,
                 threads_per_tile=a.threads, threads_big=a.threads_big, steps_per_launch=a.steps_per_launch,
-                record_every=0, lane_nodes=a.lane_nodes)
+                record_every=0, lane_nodes=a.lane_nodes, narrow_lane_nodes=a.narrow_lane_nodes)
     st = torch.cuda.Stream(local)
     sid = int(st.cuda_stream)
     plan.reset(stream=sid)
@@ -554,7 +556,7 @@ def mixed_leg(a, local, model, record_every=4):
     # mixed surrogate form
     T = a.surrogate_threads
     kw = dict(tile_nodes=a.surrogate_tile_nodes, threads_per_tile=T, threads_big=T, threads_global=T,
-              steps_per_launch=a.steps_per_launch, lane_nodes=a.lane_nodes)
+              steps_per_launch=a.steps_per_launch, lane_nodes=a.lane_nodes, narrow_lane_nodes=a.narrow_lane_nodes)
     runner = S.SurrogateRunner(descs, model, precision="f32", device=local, plan_kw=kw, full_cells=full)
     runner.run(2 * a.steps_per_launch, DT)
     runs = [runner.run(steps, DT) for _ in range(3)]
@@ -616,7 +618,7 @@ def run_ours(a):
     batch = W.descs_to_batch(descs)
     plan = Plan(batch, precision="f32", device=local, tile_nodes=a.tile_nodes, threads_per_tile=a.threads,
                 threads_big=a.threads_big, steps_per_launch=a.steps_per_launch, record_every=0,
-                lane_nodes=a.lane_nodes)
+                lane_nodes=a.lane_nodes, narrow_lane_nodes=a.narrow_lane_nodes, lane_cell_nodes=a.lane_cell_nodes)
     info = plan.info
     n_cv = plan.n_cv
     stream = torch.cuda.current_stream(local)
@@ -695,7 +697,8 @@ def run_ours(a):
                    "l2": "inputs larger than L2 (tile blobs + state arrays > 129 MB)",
                    "tiles": info["n_tiles"], "threads_per_tile": info["threads_per_tile"],
                    "tile_nodes": info["tile_nodes"], "steps_per_launch": info["steps_per_launch"],
-                   "lane_nodes": a.lane_nodes},
+                   "lane_nodes": a.lane_nodes, "narrow_lane_nodes": a.narrow_lane_nodes,
+                   "lane_cell_nodes": a.lane_cell_nodes},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d_total), "d2h_bytes_per_step": int(d2h),
                 "path": f"bc_state_upload (V) -> bc_run ({a.sim_steps:,} steps) -> bc_state_download (V) + "
                         "bc_spike_download"},

@@ -275,7 +275,8 @@ class PlanOptions(C.Structure):
         ("narrow_lane_nodes", C.c_int32),
         ("reserved_b", C.c_float),
         ("dry_run", C.c_int32),
-        ("reserved", C.c_int32 * 2),
+        ("lane_cell_nodes", C.c_int32),
+        ("reserved", C.c_int32 * 1),
     ]
 
 

@@ -116,7 +116,15 @@ struct TileDesc {
   int32_t off_pstage;       // the GRU weight fragments and wo (kGruSmemBytes), then per-port staging
                             // records (PortStage), then PortLocal records, inside the
                             // scratch area; -1: none
+  // lane tiles (one small cell per thread): node v of lane l is tile node v * L + l
+  // (L = threads of the launch); crec holds each node's parent v (0xFFFF at the
+  // root); off_lane_n: int32 node count per lane (0: no cell).  -1 otherwise.
+  int32_t off_lane_n;
+  int32_t lane_kmax;        // largest node count of the tile's cells (lane tiles)
 };
+
+// Threads (= cells) per lane tile.
+constexpr int kLaneThreads = 128;
 
 // ------------------------------------------------------------- subtree surrogate
 // GRU sizes and the layout of its flat FP32 parameter vector (training master
@@ -299,6 +307,11 @@ int launch_tiles(const LaunchArgs& a, int precision, bool smem, int threads, siz
 // call that consumes the parameters returns (it copies the argument).
 int tile_node_params(const LaunchArgs* a, int precision, bool smem, int threads, size_t smem_bytes, int variant,
                      cudaKernelNodeParams* np, const LaunchArgs** hold);
+// Lane tiles: each thread runs one whole small cell (serial Hines elimination
+// and back-substitution over its nodes, then its update), no barriers in a step.
+int launch_lanes(const LaunchArgs& a, int precision, int threads, bool extra, void* stream);
+int lane_node_params(const LaunchArgs* a, int precision, int threads, bool extra, cudaKernelNodeParams* np,
+                     const LaunchArgs** hold);
 int launch_reset_impl(const LaunchArgs& a, int precision, int threads, const double* vinit, const int64_t* voff,
                       void* stream);
 // View offsets: byte offsets into the blob, or kStateTag + byte offset into the state array.

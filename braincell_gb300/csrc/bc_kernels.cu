@@ -1645,6 +1645,164 @@ __global__ void __launch_bounds__(kVar >= 2 ? BC_PORT_MAX_THREADS : 1024, kVar >
   }
 }
 
+// ------------------------------------------------------------------ lane tiles
+// One small cell per thread: node v of the thread's cell is tile node v * L + lane
+// (L = blockDim.x), so the threads of a warp touching "their" node v touch
+// consecutive addresses of every per-node array (blob, solver scratch, states).
+// Parents precede their children in the node order (v_parent < v), so elimination
+// runs v = n-1 .. 1 folding each node into its parent, and back-substitution runs
+// v = 0 .. n-1.  The rows are those of the tile kernel (increment form,
+// float-float V); a thread touches only its own cell, so a step needs no barrier.
+// Plans with lane tiles have no synapses, network, mechanism probes or ports;
+// kExtra adds the channels outside the main mix.
+template <typename Real, bool kExtra>
+__global__ void __launch_bounds__(kLaneThreads) lane_step_kernel(LaunchArgs a) {
+  __shared__ int s_status;
+  const TileDesc td = a.tiles[blockIdx.x];
+  unsigned char* base = a.blob + td.blob_offset;
+  TileView<Real> tv;
+  tv.bind(td, base, a.scratch + td.scratch_offset, a.state);
+  const int L = blockDim.x, lane = threadIdx.x;
+  const int n = reinterpret_cast<const int32_t*>(base + td.off_lane_n)[lane];
+  const uint16_t* par = tv.crec;  // parent v of each node
+  const Real dt = Real(a.dt);
+  const PulseRec* pulses = a.pulses + td.pulse_offset;
+  if (lane == 0) s_status = 0;
+  __syncthreads();
+  // the rows of the first step from the current state
+  for (int k = 0; k < n; ++k) {
+    const int i = k * L + lane;
+    const uint16_t pr = tv.pidx[i];
+    Real G = Real(0), I = Real(0);
+    if (pr != kBoundary) {
+      NodeStates<Real> st;
+      load_states(tv.state + i, tv.N, tv.mech[pr], st);
+      const Real v = tv.v[i].x;
+      node_mechanisms_loaded<Real, kExtra>(st, tv.state + i, tv.N, tv.params + size_t(pr) * kParamStride, tv.mech[pr],
+                                           v, v, dt, false, G, I);
+    }
+    write_row(tv, i, pr, dt, G, I);
+    const uint16_t sp = tv.spec[i];
+    if (sp != kNoSpecial) add_node_pulses(tv, pulses, tv.specs[sp], i, pr, a.step0, dt);
+  }
+  for (int s = 0; s < a.n_steps; ++s) {
+    const int64_t step = a.step0 + s;
+    // elimination, deepest node first
+    for (int k = n - 1; k >= 1; --k) {
+      const int i = k * L + lane, ip = int(par[i]) * L + lane;
+      const Pair<Real> q = tv.dr[i];
+      const Pair<Real> c = coef<Real, false>(tv, i, dt);
+      const Real delta = vdelta<Real>(tv.v[i], tv.v[ip]);
+      const Real inv = pivot_rcp(q.x);
+      const Real Rp = q.y - c.x * delta;
+      tv.dr[i] = make_pair(inv, Rp);
+      const Real w = c.y * inv;
+      Pair<Real> pp = tv.dr[ip];
+      pp.x -= c.x * w;
+      pp.y += w * Rp + c.y * delta;
+      tv.dr[ip] = pp;
+    }
+    // the root, then back-substitution root first
+    if (n > 0) {
+      const Pair<Real> q = tv.dr[lane];
+      const Real inv = pivot_rcp(q.x);
+      tv.dr[lane] = make_pair(inv, q.y * inv);
+    }
+    for (int k = 1; k < n; ++k) {
+      const int i = k * L + lane, ip = int(par[i]) * L + lane;
+      const Pair<Real> q = tv.dr[i];
+      const Real al = coef<Real, false>(tv, i, dt).x;
+      tv.dr[i].y = (q.y + al * tv.dr[ip].y) * q.x;
+    }
+    // update: V += x, mechanisms, the next row, probes and next pulses
+    const bool last = s + 1 == a.n_steps;
+    const int64_t k_since = step + 1 - a.trace_base;
+    const bool record = a.record_every > 0 && k_since % a.record_every == 0;
+    for (int k = 0; k < n; ++k) {
+      const int i = k * L + lane;
+      const Pair<Real> vv = tv.v[i];
+      Real hi = vv.x, lo = vv.y;
+      const Real v_old = hi, lo_old = lo;
+      ff_add(hi, lo, tv.dr[i].y);
+      tv.v[i] = make_pair(hi, lo);
+      if (last) {  // last_V of the per-CV spike indicator
+        tv.state[size_t(kSlotVLastHi) * tv.N + i] = v_old;
+        tv.state[size_t(kSlotVLastLo) * tv.N + i] = lo_old;
+      }
+      if (!is_finite_real(hi)) s_status = kStatusNonfinite;
+      const uint16_t pr = tv.pidx[i];
+      Real G = Real(0), I = Real(0);
+      if (pr != kBoundary) {
+        NodeStates<Real> st;
+        load_states(tv.state + i, tv.N, tv.mech[pr], st);
+        node_mechanisms_loaded<Real, kExtra>(st, tv.state + i, tv.N, tv.params + size_t(pr) * kParamStride,
+                                             tv.mech[pr], v_old, hi, dt, true, G, I);
+      }
+      if (!last) write_row(tv, i, pr, dt, G, I);
+      const uint16_t sp = tv.spec[i];
+      if (sp != kNoSpecial) {
+        const SpecRec sr = tv.specs[sp];
+        if (sr.probe >= 0) {
+          const double v1 = double(hi) + double(lo), v0 = double(v_old) + double(lo_old);
+          if (v0 < 0.0 && v1 >= 0.0) {
+            const int cnt = a.spike_count[sr.probe];
+            if (cnt < a.max_spikes)
+              a.spike_times[int64_t(sr.probe) * a.max_spikes + cnt] =
+                  double(step) * a.dt + a.dt * (0.0 - v0) / (v1 - v0);
+            a.spike_count[sr.probe] = cnt + 1;
+          }
+          if (record) {
+            const int64_t slot = k_since / a.record_every - 1;
+            if (slot >= 0 && slot < a.trace_cap) a.traces[slot * a.n_probes_total + sr.probe] = v1;
+          }
+        }
+        if (!last) add_node_pulses(tv, pulses, sr, i, pr, step + 1, dt);
+      }
+    }
+  }
+  __syncthreads();
+  if (lane == 0 && s_status) atomicOr(a.status, s_status);
+}
+
+static void* lane_kernel(int precision, bool extra) {
+  if (precision == BC_PREC_F64)
+    return extra ? reinterpret_cast<void*>(lane_step_kernel<double, true>)
+                 : reinterpret_cast<void*>(lane_step_kernel<double, false>);
+  return extra ? reinterpret_cast<void*>(lane_step_kernel<float, true>)
+               : reinterpret_cast<void*>(lane_step_kernel<float, false>);
+}
+
+int launch_lanes(const LaunchArgs& a, int precision, int threads, bool extra, void* stream) {
+  if (a.n_tiles <= 0) return 0;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (threads != kLaneThreads) return int(cudaErrorInvalidConfiguration);
+  if (precision == BC_PREC_F64) {
+    if (extra)
+      lane_step_kernel<double, true><<<a.n_tiles, threads, 0, st>>>(a);
+    else
+      lane_step_kernel<double, false><<<a.n_tiles, threads, 0, st>>>(a);
+  } else {
+    if (extra)
+      lane_step_kernel<float, true><<<a.n_tiles, threads, 0, st>>>(a);
+    else
+      lane_step_kernel<float, false><<<a.n_tiles, threads, 0, st>>>(a);
+  }
+  return int(cudaGetLastError());
+}
+
+int lane_node_params(const LaunchArgs* a, int precision, int threads, bool extra, cudaKernelNodeParams* np,
+                     const LaunchArgs** hold) {
+  if (threads != kLaneThreads) return int(cudaErrorInvalidConfiguration);
+  *hold = a;
+  np->func = lane_kernel(precision, extra);
+  np->gridDim = dim3(a->n_tiles, 1, 1);
+  np->blockDim = dim3(threads, 1, 1);
+  np->sharedMemBytes = 0u;
+  np->extra = nullptr;
+  np->kernelParams = reinterpret_cast<void**>(const_cast<LaunchArgs**>(hold));
+  return 0;
+}
+
 // Reset: V from the initial image, gates at steady state, Ci = Ci0.
 template <typename Real>
 __global__ void reset_kernel(LaunchArgs a, const double* vinit, const int64_t* vinit_off) {

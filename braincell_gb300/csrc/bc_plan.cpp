@@ -52,9 +52,20 @@ struct CellSched;
 
 }  // namespace bc
 
+// launch classes: 0 packed shared-memory tiles, 1 one big cell per shared-memory
+// tile, 2 global-memory tiles, 3 lane tiles (one small cell per thread)
+constexpr int kMaxClasses = 4;
+// Serial-walk lengths of the warp slots (lane_nodes / narrow_lane_nodes).  Swept on
+// GB300 over the 10,000-cell uneven population (FP32, 1,000 steps per launch):
+// lane_nodes 1 / 4 / 8 / 10 / 12 with narrow phases at 1 ran 2.18 / 2.24 / 2.35 /
+// 2.38 / 2.33e10 compartment-steps/s; narrow phases at 2 instead of 1 cost 23%.
+constexpr int kDefaultLaneNodes = 10;
+constexpr int kDefaultNarrowLaneNodes = 1;
+
 struct LaunchClass {
   int first = 0, count = 0, threads = 256;
   bool smem = true;
+  bool lane = false;  // lane tiles: one cell per thread (lane_step_kernel)
   size_t smem_bytes = 0;
 };
 
@@ -138,13 +149,13 @@ struct bc_plan {
   int64_t step = 0;
   size_t device_bytes = 0;
   // launch classes after the first run concurrently on these streams
-  cudaStream_t aux[2] = {nullptr, nullptr};
+  cudaStream_t aux[kMaxClasses - 1] = {nullptr, nullptr, nullptr};
   cudaStream_t init_stream = nullptr;  // highest priority: the initial reset
   int aux_prio = 0;                    // priority of the aux streams (that of the last caller's stream)
   bool dry = false;
   unsigned long long* d_timers = nullptr;
   std::vector<std::array<int64_t, 6>> tile_stats;
-  cudaEvent_t ev_fork = nullptr, ev_join[2] = {nullptr, nullptr};
+  cudaEvent_t ev_fork = nullptr, ev_join[kMaxClasses - 1] = {nullptr, nullptr, nullptr};
   // CUDA graph of one run (use_graph): per launch class a chain of kernel nodes,
   // rebuilt when the launch pattern changes, otherwise only re-parameterised.
   cudaGraph_t graph = nullptr;
@@ -196,7 +207,7 @@ static void free_plan(bc_plan* p) {
   cudaFree(p->d_port_h);
   cudaFree(p->d_port_flags);
   cudaFree(p->d_gru);
-  for (int k = 0; k < 2; ++k) {
+  for (int k = 0; k < kMaxClasses - 1; ++k) {
     if (p->aux[k]) cudaStreamDestroy(p->aux[k]);
     if (p->ev_join[k]) cudaEventDestroy(p->ev_join[k]);
   }
@@ -411,9 +422,10 @@ static bc_status build_tile(const BuildCtx& cx, const TileBuild& tb, int T, Tile
       levels[lv].push_back({int32_t(li), int32_t(k), int32_t(cs.chains[k].nodes.size())});
     }
   }
+  const bool lane = tb.cls == 3;  // a lane tile has no chains, phases or warp slots
   std::vector<std::vector<CRef>> phases;
   for (auto& v : levels)
-    if (!v.empty()) phases.push_back(std::move(v));
+    if (!v.empty() && !lane) phases.push_back(std::move(v));
   const int n_phases = int(phases.size());
   std::vector<int32_t> phase_ptr(size_t(n_phases) + 1, 0);
   // A lane plan: the chains (whole, or one chain's part) of one lane.
@@ -543,6 +555,22 @@ static bc_status build_tile(const BuildCtx& cx, const TileBuild& tb, int T, Tile
   }
   phase_ptr[n_phases] = int32_t(slots.size());
   out.crit = crit;
+  // lane tile: node v of the cell in lane l is tile node v * T + l
+  std::vector<int32_t> lane_n;
+  int32_t lane_kmax = 0;
+  if (lane) {
+    if (int64_t(cell_list.size()) > T) return fail(BC_ERR_INVALID, "internal: lane tile with more cells than threads");
+    lane_n.assign(size_t(T), 0);
+    for (size_t li = 0; li < cell_list.size(); ++li) {
+      const LoweredCell& lc = (*cx.cells)[cell_list[li]];
+      lane_n[li] = lc.n_node;
+      lane_kmax = std::max(lane_kmax, lc.n_node);
+      for (int32_t v = 0; v < lc.n_node; ++v) node_tile[li][v] = v * T + int32_t(li);
+    }
+    if (lane_kmax >= 0xFFFF) return fail(BC_ERR_CAPACITY, "a lane-tile cell has too many nodes");
+    n_real = int64_t(lane_kmax) * T;
+    out.crit = lane_kmax;
+  }
   if (chains.size() >= 0xFFFF) return fail(BC_ERR_CAPACITY, "too many chains in one tile");
   // -------- links: parents and contribution slots
   // A record owns the consecutive contribution slots aux .. aux + n_child, one per
@@ -573,6 +601,13 @@ static bc_status build_tile(const BuildCtx& cx, const TileBuild& tb, int T, Tile
   std::vector<uint16_t> crec(size_t(n_real), 0);
   for (size_t k = 0; k < chains.size(); ++k)
     for (int32_t q = 0; q < chains[k].count; ++q) crec[size_t(chains[k].start + q)] = uint16_t(k);
+  if (lane) {  // lane tiles: the parent's node index v within the cell (0xFFFF at the root)
+    for (size_t li = 0; li < cell_list.size(); ++li) {
+      const LoweredCell& lc = (*cx.cells)[cell_list[li]];
+      for (int32_t v = 0; v < lc.n_node; ++v)
+        crec[size_t(node_tile[li][v])] = lc.parent[v] >= 0 ? uint16_t(lc.parent[v]) : uint16_t(0xFFFF);
+    }
+  }
   // -------- special nodes: clamp pulses (sorted by node) and probes
   std::vector<std::pair<int32_t, int64_t>> tpulse, tprobe;  // (tile node, pulse / probe id)
   for (size_t li = 0; li < cell_list.size(); ++li) {
@@ -640,6 +675,12 @@ static bc_status build_tile(const BuildCtx& cx, const TileBuild& tb, int T, Tile
   off = align16(off + tsyn.size() * 4);
   d.off_plist = int32_t(off);
   off = align16(off + tprobe.size() * sizeof(ProbeRef));
+  d.off_lane_n = -1;
+  d.lane_kmax = lane_kmax;
+  if (lane) {
+    d.off_lane_n = int32_t(off);
+    off = align16(off + size_t(T) * 4);
+  }
   d.n_cells = int32_t(cell_list.size());
   d.off_ncell = -1;
   d.off_srccell = -1;
@@ -681,6 +722,11 @@ static bc_status build_tile(const BuildCtx& cx, const TileBuild& tb, int T, Tile
   std::vector<unsigned char>& b = out.blob;
   b.assign(d.blob_bytes, 0);
   out.vinit.assign(n_real, 0.0);
+  if (lane) {  // holes of the lane grid are boundary rows the kernel never visits
+    std::vector<uint16_t> hole(size_t(N), 0xFFFF);
+    std::memcpy(b.data() + d.off_pidx, hole.data(), hole.size() * 2);
+    std::memcpy(b.data() + d.off_lane_n, lane_n.data(), lane_n.size() * 4);
+  }
   auto putr = [&](size_t base_off, size_t idx, double v) {
     if (rs == 8)
       put<double>(b, base_off, idx, v);
@@ -1014,8 +1060,9 @@ static bc_status enqueue_run_graph(bc_plan* p, int64_t n_steps, double dt, void*
         const LaunchClass& lcz = p->classes[ci];
         cudaKernelNodeParams np{};
         const LaunchArgs* hold = nullptr;
-        int e = tile_node_params(&args[size_t(j) * nc + ci], p->precision, lcz.smem, lcz.threads, lcz.smem_bytes, kernel_variant(p), &np,
-                                 &hold);
+        int e = lcz.lane ? lane_node_params(&args[size_t(j) * nc + ci], p->precision, lcz.threads, p->extra, &np, &hold)
+                         : tile_node_params(&args[size_t(j) * nc + ci], p->precision, lcz.smem, lcz.threads, lcz.smem_bytes,
+                                            kernel_variant(p), &np, &hold);
         if (e) return fail(BC_ERR_CUDA, std::string("graph node: ") + cudaGetErrorString(cudaError_t(e)));
         cudaGraphNode_t dep = j > 0 ? p->graph_nodes[size_t(j - 1) * nc + ci] : nullptr;
         BC_CUDA(cudaGraphAddKernelNode(&p->graph_nodes[size_t(j) * nc + ci], p->graph, dep ? &dep : nullptr,
@@ -1031,8 +1078,9 @@ static bc_status enqueue_run_graph(bc_plan* p, int64_t n_steps, double dt, void*
         const LaunchClass& lcz = p->classes[ci];
         cudaKernelNodeParams np{};
         const LaunchArgs* hold = nullptr;
-        int e = tile_node_params(&args[size_t(j) * nc + ci], p->precision, lcz.smem, lcz.threads, lcz.smem_bytes, kernel_variant(p), &np,
-                                 &hold);
+        int e = lcz.lane ? lane_node_params(&args[size_t(j) * nc + ci], p->precision, lcz.threads, p->extra, &np, &hold)
+                         : tile_node_params(&args[size_t(j) * nc + ci], p->precision, lcz.smem, lcz.threads, lcz.smem_bytes,
+                                            kernel_variant(p), &np, &hold);
         if (e) return fail(BC_ERR_CUDA, std::string("graph node: ") + cudaGetErrorString(cudaError_t(e)));
         BC_CUDA(cudaGraphExecKernelNodeSetParams(p->graph_exec, p->graph_nodes[size_t(j) * nc + ci], &np));
       }
@@ -1066,7 +1114,7 @@ static bc_status enqueue_run(bc_plan* p, int64_t n_steps, double dt, void* strea
     int prio = 0;
     BC_CUDA(cudaStreamGetPriority(static_cast<cudaStream_t>(stream), &prio));
     if (prio != p->aux_prio) {
-      for (int k = 0; k < 2; ++k) {
+      for (int k = 0; k < kMaxClasses - 1; ++k) {
         cudaStream_t ns = nullptr;
         BC_CUDA(cudaStreamCreateWithPriority(&ns, cudaStreamNonBlocking, prio));
         if (p->aux[k]) cudaStreamDestroy(p->aux[k]);
@@ -1096,7 +1144,8 @@ static bc_status enqueue_run(bc_plan* p, int64_t n_steps, double dt, void* strea
       }
       a.tiles = p->d_tiles + lcz.first;
       a.n_tiles = lcz.count;
-      int e = launch_tiles(a, p->precision, lcz.smem, lcz.threads, lcz.smem_bytes, kernel_variant(p), st);
+      int e = lcz.lane ? launch_lanes(a, p->precision, lcz.threads, p->extra, st)
+                       : launch_tiles(a, p->precision, lcz.smem, lcz.threads, lcz.smem_bytes, kernel_variant(p), st);
       if (e) return fail(BC_ERR_CUDA, std::string("tile kernel launch: ") + cudaGetErrorString(cudaError_t(e)));
       if (ci > 0) {
         BC_CUDA(cudaEventRecord(p->ev_join[ci - 1], st));
@@ -1133,7 +1182,8 @@ void bc_default_options(bc_plan_options* o) {
   o->precision = BC_PREC_F32;
   o->threads_per_tile = 0;
   o->tile_nodes = 0;
-  o->lane_nodes = 1;
+  o->lane_nodes = kDefaultLaneNodes;
+  o->narrow_lane_nodes = kDefaultNarrowLaneNodes;
   o->steps_per_launch = 0;
   o->record_every = 1;
   o->max_spikes = 64;
@@ -1170,8 +1220,8 @@ bc_status bc_plan_create(const bc_batch_spec* spec, const bc_plan_options* opts_
   p->max_spikes = opts.max_spikes;
   p->use_graph = opts.use_graph;
   p->steps_per_launch = opts.steps_per_launch > 0 ? opts.steps_per_launch : 1000;
-  p->lane_nodes = opts.lane_nodes > 0 ? opts.lane_nodes : 1;
-  p->narrow_lane_nodes = opts.narrow_lane_nodes > 0 ? opts.narrow_lane_nodes : p->lane_nodes;
+  p->lane_nodes = opts.lane_nodes > 0 ? opts.lane_nodes : kDefaultLaneNodes;
+  p->narrow_lane_nodes = opts.narrow_lane_nodes > 0 ? opts.narrow_lane_nodes : kDefaultNarrowLaneNodes;
   p->n_cells = s.n_cells;
   // ---------------------------------------------------- lower
   std::vector<LoweredCell> cells(s.n_cells);
@@ -1283,7 +1333,9 @@ bc_status bc_plan_create(const bc_batch_spec* spec, const bc_plan_options* opts_
   p->n_probes = s.n_probes;
   p->n_pulses = s.n_pulses;
   // mechanism probes are recorded by the extra kernel variant only
-  for (int64_t k = 0; s.probe_field && k < s.n_probes; ++k) p->extra = p->extra || s.probe_field[k] != BC_STATE_V;
+  bool mech_probes = false;
+  for (int64_t k = 0; s.probe_field && k < s.n_probes; ++k) mech_probes = mech_probes || s.probe_field[k] != BC_STATE_V;
+  p->extra = p->extra || mech_probes;
   // ---------------------------------------------------- synapses / connections
   std::vector<std::vector<std::pair<int64_t, int32_t>>> cell_syns(s.n_cells);
   std::vector<char> is_src(s.n_cells, 0);
@@ -1455,7 +1507,7 @@ bc_status bc_plan_create(const bc_batch_spec* spec, const bc_plan_options* opts_
     return fail(BC_ERR_INVALID, "plans with surrogate ports run at most " + std::to_string(BC_PORT_MAX_THREADS) +
                                     " threads per tile");
   }
-  const int class_threads[3] = {T_packed, T_big, T_glob};
+  const int class_threads[kMaxClasses] = {T_packed, T_big, T_glob, kLaneThreads};
   p->threads = T_packed;
   p->threads_global = T_glob;
   std::vector<int64_t> order(s.n_cells);
@@ -1464,10 +1516,32 @@ bc_status bc_plan_create(const bc_batch_spec* spec, const bc_plan_options* opts_
                    [&](int64_t a, int64_t b) { return cells[a].n_node > cells[b].n_node; });
   std::vector<TileBuild> builds;
   std::vector<int64_t> fill;
+  // Lane tiles: cells of at most lane_cell_nodes tree nodes, kLaneThreads per tile
+  // in decreasing size (a tile's threads then walk near-equal trees).  The lane
+  // kernel runs the channels (out-of-line ones included when the plan has them) and
+  // voltage probes, but no synapses, network, mechanism probes or ports.
+  std::vector<char> in_lane(s.n_cells, 0);
+  const bool lane_ok = !mech_probes && s.n_synapses == 0 && s.n_connections == 0 && s.n_ports == 0;
+  if (opts.lane_cell_nodes > 0 && lane_ok) {
+    std::vector<int64_t> lane_cells;
+    for (int64_t c : order)
+      if (cells[c].n_node <= opts.lane_cell_nodes) lane_cells.push_back(c);
+    for (size_t q = 0; q < lane_cells.size(); q += kLaneThreads) {
+      TileBuild tb;
+      tb.cls = 3;
+      for (size_t r = q; r < std::min(lane_cells.size(), q + kLaneThreads); ++r) {
+        tb.cells.push_back(lane_cells[r]);
+        in_lane[lane_cells[r]] = 1;
+      }
+      builds.push_back(tb);
+      fill.push_back(0);
+    }
+  }
   // best-fit decreasing: each cell goes to the open packed tile with the least room
   // that still holds it (free room -> tile index), else opens a new tile
   std::multimap<int64_t, size_t> room;
   for (int64_t c : order) {
+    if (in_lane[c]) continue;
     const int64_t nn = cells[c].n_node;
     if (nn > tile_nodes) {
       TileBuild tb;
@@ -1516,30 +1590,38 @@ bc_status bc_plan_create(const bc_batch_spec* spec, const bc_plan_options* opts_
     }
     const size_t need = size_t(to.desc.blob_bytes) + size_t(to.desc.scratch_bytes);
     const size_t limit = builds[t].cls == 0 ? packed_budget : smem_budget;
-    if (builds[t].cls != 2 && need > limit) {
+    if (builds[t].cls < 2 && need > limit) {
       if (builds[t].cells.size() > 1) {
-        // split: move the last cell into the best-fitting packed tile not built yet
-        // (or a new one) and rebuild this one
-        const int64_t c = builds[t].cells.back();
-        const int64_t nn = cells[c].n_node;
-        builds[t].cells.pop_back();
-        fill[t] -= nn;
-        size_t dest = builds.size();
-        for (auto it = room.lower_bound(nn); it != room.end(); ++it)
-          if (it->second > t) {
-            dest = it->second;
-            room.erase(it);
-            break;
+        // split: move the last cells into the best-fitting packed tiles not built yet
+        // (or new ones) and rebuild this one.  As many cells move at once as the
+        // overflow's share of the tile (at least one), so a tile of many small cells
+        // whose per-cell records outgrow the node estimate is rebuilt a few times,
+        // not once per cell.
+        const size_t n_in = builds[t].cells.size();
+        size_t n_move = size_t(std::ceil(double(n_in) * double(need - limit) / double(need)));
+        n_move = std::max<size_t>(1, std::min(n_move, n_in - 1));
+        for (size_t q = 0; q < n_move; ++q) {
+          const int64_t c = builds[t].cells.back();
+          const int64_t nn = cells[c].n_node;
+          builds[t].cells.pop_back();
+          fill[t] -= nn;
+          size_t dest = builds.size();
+          for (auto it = room.lower_bound(nn); it != room.end(); ++it)
+            if (it->second > t) {
+              dest = it->second;
+              room.erase(it);
+              break;
+            }
+          if (dest == builds.size()) {
+            TileBuild nb;
+            nb.cls = 0;
+            builds.push_back(nb);
+            fill.push_back(0);
           }
-        if (dest == builds.size()) {
-          TileBuild nb;
-          nb.cls = 0;
-          builds.push_back(nb);
-          fill.push_back(0);
+          builds[dest].cells.push_back(c);
+          fill[dest] += nn;
+          if (tile_nodes - fill[dest] > 0 && builds[dest].cells.size() < 4096) room.emplace(tile_nodes - fill[dest], dest);
         }
-        builds[dest].cells.push_back(c);
-        fill[dest] += nn;
-        if (tile_nodes - fill[dest] > 0) room.emplace(tile_nodes - fill[dest], dest);
         --t;
         continue;
       }
@@ -1554,11 +1636,12 @@ bc_status bc_plan_create(const bc_batch_spec* spec, const bc_plan_options* opts_
   }
   // tiles ordered by class; one launch per class
   std::vector<size_t> tord;
-  for (int cl = 0; cl < 3; ++cl) {
+  for (int cl = 0; cl < kMaxClasses; ++cl) {
     LaunchClass lcz;
     lcz.first = int(tord.size());
     lcz.threads = class_threads[cl];
     lcz.smem = cl < 2;
+    lcz.lane = cl == 3;
     for (size_t t = 0; t < builds.size(); ++t)
       if (builds[t].cls == cl) {
         tord.push_back(t);
@@ -1586,7 +1669,7 @@ bc_status bc_plan_create(const bc_batch_spec* spec, const bc_plan_options* opts_
     blob_total = align16(blob_total + d.blob_bytes);
     d.state_offset = state_total;
     state_total += int64_t(S) * d.n_nodes;
-    if (builds[tord[k]].cls == 2) {
+    if (builds[tord[k]].cls >= 2) {  // global-memory and lane tiles: solver scratch in HBM
       d.scratch_offset = int64_t(scratch_total);
       scratch_total = align16(scratch_total + d.scratch_bytes);
     } else {
@@ -1725,7 +1808,7 @@ bc_status bc_plan_create(const bc_batch_spec* spec, const bc_plan_options* opts_
     free_plan(p);
     return fail(BC_ERR_CAPACITY, "tile shared memory exceeds the device limit");
   }
-  for (int k = 0; k < 2; ++k) {
+  for (int k = 0; k < kMaxClasses - 1; ++k) {
     BC_TRYC(cudaStreamCreateWithFlags(&p->aux[k], cudaStreamNonBlocking));
     BC_TRYC(cudaEventCreateWithFlags(&p->ev_join[k], cudaEventDisableTiming));
   }

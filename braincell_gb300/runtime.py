@@ -50,6 +50,7 @@ class Plan:
         threads_big: int = 0,
         threads_global: int = 0,
         dry_run: bool = False,
+        lane_cell_nodes: int = 0,
     ) -> None:
         if precision not in _PREC:
             raise ValueError(f"precision must be one of {sorted(_PREC)}, got {precision!r}.")
@@ -72,6 +73,7 @@ class Plan:
         opts.threads_big = int(threads_big)
         opts.threads_global = int(threads_global)
         opts.dry_run = int(bool(dry_run))
+        opts.lane_cell_nodes = int(lane_cell_nodes)
         spec, keep = batch.to_spec()
         handle = C.c_void_p()
         _abi.check(lib.bc_plan_create(C.byref(spec), C.byref(opts), C.byref(handle)))

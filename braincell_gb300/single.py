@@ -18,7 +18,9 @@ steady state at each neuron's own voltage, as the reference's channel
 ``reset_state(V)`` puts them.  (The reference's default draws U(-70, -60) mV; the
 default here is -65 mV.)
 
-On the GB300 step the population is one device plan of ``size`` one-CV cylinders.
+On the GB300 step the population is one device plan of ``size`` one-CV cylinders,
+run one neuron per GPU thread (lane tiles; ``solver_options=dict(lane_cell_nodes=0)``
+packs them into CTA tiles instead).
 The ``"gb300_staggered"`` solver advances it by the staggered scheme restricted to one
 compartment: the ionic current linearised at V_n, one implicit voltage step, then
 calcium from the step-start current and every gate by exp-Euler at the new voltage.

@@ -31,7 +31,7 @@ __all__ = ["TuneResult", "autotune", "sample_cells", "measure_plan"]
 
 TILE_THREADS = ((2500, 512), (2000, 512), (2500, 384), (2000, 256), (1500, 256), (4800, 1024))
 PORT_MAX_THREADS = 384
-LANE_NODES = (1, 2)
+LANE_NODES = (10, 4, 1)
 STEPS_PER_LAUNCH = (1000, 250)
 
 

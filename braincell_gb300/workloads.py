@@ -160,9 +160,9 @@ def _random_tree(rng, n_dend_cv: int, p_branch: float, max_depth: int, max_branc
     return parent
 
 
-def _uneven_desc(seed: int, i: int) -> CellDesc:
+def _uneven_desc(seed: int, i: int, n_range=(50, 2000)) -> CellDesc:
     rng = np.random.default_rng([seed, i])
-    n_total = int(round(math.exp(rng.uniform(math.log(50.0), math.log(2000.0)))))
+    n_total = int(round(math.exp(rng.uniform(math.log(float(n_range[0])), math.log(float(n_range[1]))))))
     n_dend = max(n_total - 1, 3)
     parent = _random_tree(rng, n_dend, 0.7, 8, max(3, n_dend // 4))
     nb = len(parent)
@@ -193,9 +193,11 @@ def _uneven_desc(seed: int, i: int) -> CellDesc:
     )
 
 
-def uneven(n_cells: int = 10000, seed: int = 1, indices=None) -> list[CellDesc]:
+def uneven(n_cells: int = 10000, seed: int = 1, indices=None, n_range=(50, 2000)) -> list[CellDesc]:
+    """Cells with log-uniform compartment counts in ``n_range`` (default: the uneven
+    population, 50 to 2,000); a smaller range gives a population of small cells."""
     idx = range(n_cells) if indices is None else indices
-    return [_uneven_desc(seed, int(i)) for i in idx]
+    return [_uneven_desc(seed, int(i), n_range) for i in idx]
 
 
 # ----------------------------------------------------------------------------- large

@@ -226,7 +226,7 @@ typedef struct bc_plan_options {
   int32_t tile_nodes;       /* node budget per tile (shared-memory size); 0 = auto   */
   int32_t lane_nodes;       /* nodes a lane walks serially inside a warp slot; longer
                                chains are spread over lanes joined by shuffle scans;
-                               0 = auto (1)                                          */
+                               0 = auto (10)                                         */
   int32_t steps_per_launch; /* time steps fused per kernel launch; 0 = auto          */
   int32_t record_every;     /* probe sampling period in steps (>= 1)                 */
   int32_t max_spikes;       /* spike times kept per probe                            */
@@ -239,11 +239,15 @@ typedef struct bc_plan_options {
                                tile_nodes; 0 = auto                                   */
   int32_t threads_global;   /* CTA size for global-memory tiles; 0 = auto            */
   int32_t narrow_lane_nodes; /* lane_nodes for narrow phases (fewer nodes than one
-                               warp slot per warp); 0 = same as lane_nodes        */
+                               warp slot per warp); 0 = auto (1)                  */
   float reserved_b;         /* must be 0                                             */
   int32_t dry_run;          /* 1: lower and schedule only (no CUDA calls); the plan
                                answers bc_plan_info / bc_plan_tile_stats only         */
-  int32_t reserved[2];
+  int32_t lane_cell_nodes;  /* cells of at most this many tree nodes run one per thread
+                               (serial solve per cell, cells interleaved node by node in
+                               global memory) instead of in packed tiles; plans without
+                               synapses, connections, mechanism probes or ports; 0 = off */
+  int32_t reserved[1];
 } bc_plan_options;
 
 typedef struct bc_plan* bc_plan_t;
@@ -295,7 +299,8 @@ bc_status bc_plan_info(bc_plan_t plan, bc_plan_info_t* info);
 /* Per-tile schedule statistics, 6 int64 per tile in launch order: real nodes,
  * chain records, barrier phases, critical-path estimate (node visits of the
  * busiest thread summed over phases), launch class (0 packed shared-memory tile,
- * 1 single-cell shared-memory tile, 2 global-memory tile), shared bytes. */
+ * 1 single-cell shared-memory tile, 2 global-memory tile, 3 lane tile: one cell per
+ * thread), shared bytes. */
 bc_status bc_plan_tile_stats(bc_plan_t plan, int64_t* out /* [n_tiles * 6] */);
 
 /* The native lowering of one cell, for checking against other assemblies (host

@@ -1,0 +1,139 @@
+"""Lane tiles: small cells run one per thread (plan option ``lane_cell_nodes``).
+
+Cells of at most ``lane_cell_nodes`` tree nodes are taken out of the packed tiles
+and grouped 128 to a CTA, largest first; node v of the cell in lane l sits at tile
+node v * 128 + l, so a warp's 32 cells read every per-node array with unit stride.
+Each thread eliminates its own tree deepest node first and back-substitutes root
+first: the same rows, increment form and float-float voltage as the tile kernel.
+
+CPU: the planner's assignment (dry-run plans).  GPU: FP64 against the float64
+oracle at 1e-8 mV over the whole run (spikes included), FP32 against the tile path
+of the same cells, mixed lane / packed plans, and CUDA-graph replay.
+"""
+
+import numpy as np
+import pytest
+
+from braincell_gb300 import _abi
+from braincell_gb300 import workloads as W
+from braincell_gb300.runtime import Plan
+from oracle.staggered import OracleCell
+
+DT = 0.025
+LANE = 128
+
+
+def _tree_nodes(d):
+    # the point tree: the root, and per branch one node per CV plus its distal end
+    return 1 + int(sum(d.ncv)) + len(d.ncv)
+
+
+def _small(n, seed=3, n_range=(3, 60)):
+    return W.uneven(n, seed=seed, n_range=n_range)
+
+
+def test_small_cells_go_to_lane_tiles(native_lib):
+    descs = _small(300, seed=5, n_range=(5, 400))
+    nodes = np.array([_tree_nodes(d) for d in descs])
+    limit = 100
+    lane = np.sort(nodes[nodes <= limit])[::-1]
+    assert 128 < lane.size < 300
+    p = Plan(W.descs_to_batch(descs), dry_run=True, lane_cell_nodes=limit)
+    st = p.tile_stats()
+    cls = st[:, 4]
+    n_lane = -(-lane.size // LANE)
+    assert (cls == 3).sum() == n_lane
+    # a lane tile holds 128 cells' worth of node rows: 128 x its largest cell
+    want = [LANE * lane[k * LANE] for k in range(n_lane)]
+    np.testing.assert_array_equal(np.sort(st[cls == 3, 0])[::-1], want)
+    assert st[cls == 3, 2].max() == 0  # no barrier phases
+    # the other cells fill the packed tiles exactly
+    assert st[cls != 3, 0].sum() == nodes[nodes > limit].sum()
+    p.close()
+    q = Plan(W.descs_to_batch(descs), dry_run=True)
+    assert (q.tile_stats()[:, 4] != 3).all()
+    q.close()
+
+
+def test_lane_tiles_stay_off_with_mechanism_probes(native_lib):
+    b = W.descs_to_batch(_small(20))
+    b.probe_field = np.full(b.probe_cell.size, _abi.BC_STATE_NA_P, np.int32)
+    p = Plan(b, dry_run=True, lane_cell_nodes=1000)
+    assert (p.tile_stats()[:, 4] != 3).all()
+    p.close()
+
+
+def _run(descs, n_steps, precision, **kw):
+    b = W.descs_to_batch(descs)
+    p = Plan(b, precision=precision, record_every=1, **kw)
+    p.run(n_steps, DT)
+    out = p.traces(), p.spikes(), p.state("V"), p.tile_stats()[:, 4]
+    p.close()
+    return out
+
+
+@pytest.mark.gpu
+def test_lane_tiles_f64_match_the_oracle(cuda_device):
+    descs = _small(40)
+    n = 800
+    tr, sp, V, cls = _run(descs, n, "f64", device=cuda_device, lane_cell_nodes=10_000)
+    assert (cls == 3).all()
+    off = np.concatenate([[0], np.cumsum([int(sum(d.ncv)) for d in descs])])
+    fired = 0
+    for c in (0, 7, 19, 33, 39):
+        oc = OracleCell(W.desc_to_cell(descs[c]))
+        otr, osp = oc.run(DT, n)
+        assert np.abs(otr[0, 0] - tr[c]).max() <= 1e-8, f"cell {c}"
+        assert np.abs(oc.V[0] - V[off[c]:off[c + 1]]).max() <= 1e-8
+        ref = np.asarray(osp[0][0])
+        assert len(sp[c]) == ref.size
+        if ref.size:
+            assert np.abs(sp[c] - ref).max() <= 1e-9
+        fired += ref.size
+    assert fired > 0
+
+
+@pytest.mark.gpu
+def test_lane_tiles_f32_match_the_tile_path(cuda_device):
+    descs = _small(300, seed=11, n_range=(3, 120))
+    n = 2000
+    a_tr, a_sp, a_V, a_cls = _run(descs, n, "f32", device=cuda_device, lane_cell_nodes=10_000)
+    b_tr, b_sp, b_V, b_cls = _run(descs, n, "f32", device=cuda_device)
+    assert (a_cls == 3).all() and (b_cls != 3).all()
+    n_spk = 0
+    for c in range(len(descs)):
+        rate = np.diff(b_tr[c]) / DT
+        hit = np.nonzero(rate > 10.0)[0]
+        first = int(hit[0]) + 1 if hit.size else n
+        if first:
+            assert np.abs(a_tr[c, :first] - b_tr[c, :first]).max() <= 1e-3, f"cell {c}"
+        assert len(a_sp[c]) == len(b_sp[c]), f"cell {c}"
+        if len(b_sp[c]):
+            assert np.abs(a_sp[c] - b_sp[c]).max() <= 0.05
+        n_spk += len(b_sp[c])
+    assert n_spk > 100
+
+
+@pytest.mark.gpu
+def test_mixed_lane_and_packed_tiles_f64(cuda_device):
+    descs = _small(60, seed=9, n_range=(3, 300))
+    nodes = np.array([_tree_nodes(d) for d in descs])
+    n = 600
+    tr, sp, V, cls = _run(descs, n, "f64", device=cuda_device, lane_cell_nodes=80)
+    assert (cls == 3).any() and (cls != 3).any()
+    small, big = np.nonzero(nodes <= 80)[0], np.nonzero(nodes > 80)[0]
+    for c in (*small[:2], *big[:2]):
+        oc = OracleCell(W.desc_to_cell(descs[c]))
+        otr, osp = oc.run(DT, n)
+        assert np.abs(otr[0, 0] - tr[c]).max() <= 1e-8, f"cell {c}"
+        assert len(sp[c]) == len(osp[0][0])
+
+
+@pytest.mark.gpu
+def test_lane_tiles_graph_replay_is_bit_identical(cuda_device):
+    descs = _small(200, seed=4)
+    kw = dict(device=cuda_device, lane_cell_nodes=10_000, steps_per_launch=64)
+    a = _run(descs, 300, "f32", **kw)
+    b = _run(descs, 300, "f32", use_graph=True, **kw)
+    np.testing.assert_array_equal(a[0], b[0])
+    np.testing.assert_array_equal(a[2], b[2])

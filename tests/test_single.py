@@ -79,12 +79,17 @@ def test_single_compartment_declarations():
 @pytest.mark.gpu
 @pytest.mark.parametrize("mix", [_hh, _calcium], ids=["hh", "calcium"])
 @pytest.mark.parametrize("precision", ["f64", "f32"])
-def test_single_compartment_update_matches_oracle(native_lib, cuda_device, mix, precision):
+@pytest.mark.parametrize("lanes", [0, 3], ids=["tiles", "lanes"])
+def test_single_compartment_update_matches_oracle(native_lib, cuda_device, mix, precision, lanes):
+    # lanes = 3: every neuron (a 3-node tree) runs one per thread on the lane kernel;
+    # the HH mix runs its out-of-line channels there
     n = 8
     v0 = np.linspace(-70.0, -60.0, n)
     sc = SingleCompartment(n, length=LENGTH, radius=RADIUS, V_initializer=v0,
-                           solver_options=dict(precision=precision, device=cuda_device), **mix())
+                           solver_options=dict(precision=precision, device=cuda_device, lane_cell_nodes=lanes),
+                           **mix())
     sc.init_state()
+    assert (sc._runtime.tile_stats()[:, 4] == 3).all() == bool(lanes)
     oc = OracleSingleCompartment(n, list(mix().values()), V_init=v0)
     np.testing.assert_allclose(sc.V, oc.V, atol=1e-12 if precision == "f64" else 1e-5)
     tol = 1e-8 if precision == "f64" else None

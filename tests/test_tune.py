@@ -37,7 +37,7 @@ def test_sample_is_seeded_and_bounded():
 
 
 def test_coordinate_search_finds_the_best_options():
-    best = {"tile_nodes": 2000, "threads_per_tile": 256, "lane_nodes": 2, "steps_per_launch": 250}
+    best = {"tile_nodes": 2000, "threads_per_tile": 256, "lane_nodes": 4, "steps_per_launch": 250}
 
     def fake(sample, o):
         assert sample.n_cells == 20
