@@ -687,6 +687,18 @@ def run_ours(a):
     if prof and "dram_bytes_per_node_step" in prof:
         traffic = info["n_nodes"] * (prof.get("dram_bytes_per_node_launch_fixed", 0.0)
                                      + prof["dram_bytes_per_node_step"] * info["steps_per_launch"])
+    clk = clocks.summary()
+    sm_bound = None
+    if prof and "warp_inst_per_node_step" in prof and clk.get("sm_mhz"):
+        # the issue limit of this design: 4 warp schedulers per SM issue one warp
+        # instruction per cycle each; ncu's instruction count per node-step (the
+        # 1,000-cell capture) sets the node-steps/s that rate allows
+        n_sm = torch.cuda.get_device_properties(local).multi_processor_count
+        issue = 4.0 * n_sm * clk["sm_mhz"] * 1e6
+        bound = issue / prof["warp_inst_per_node_step"] * 32.0 * n_cv / info["n_nodes"] * world
+        sm_bound = {"bound": "sm_issue", "value": bound, "unit": UNIT, "frac": value / bound,
+                    "warp_inst_per_node_step": prof["warp_inst_per_node_step"], "sms": n_sm,
+                    "sm_mhz": clk["sm_mhz"]}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
         "ms_per_step": ms / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -707,8 +719,9 @@ def run_ours(a):
                      "traffic": traffic, "bytes_per_compartment_step": nbytes,
                      "algorithmic_bytes_per_launch": nbytes * units_per_launch,
                      "kernel_ms_per_sim": kernel_ms, "launches_per_sim": launches_per_sim},
+        "sm_bound": sm_bound,
         "gpu_launches": a.steps * (1 + launches_per_sim),
-        "clocks": clocks.summary(),
+        "clocks": clk,
         "wall_s_timed": t_wall,
     }
     if a.accuracy_cells:

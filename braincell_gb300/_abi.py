@@ -39,9 +39,12 @@ BC_M_KA2 = 1 << 13
 BC_M_KK2A = 1 << 14
 BC_M_KK2B = 1 << 15
 BC_M_KNI = 1 << 16
-BC_M_ALL = 0x1FFFF
+BC_M_NAV16 = 1 << 17
+BC_M_KCA22 = 1 << 18
+BC_M_KCA11 = 1 << 19
+BC_M_ALL = 0xFFFFF
 
-BC_NPARAM = 64
+BC_NPARAM = 74
 BC_P_INVCM = 0
 BC_P_VREST = 1
 BC_P_ENA = 2
@@ -106,8 +109,17 @@ BC_P_KNI_G = 60
 BC_P_KNI_VSH = 61
 BC_P_KNI_PHI = 62
 BC_P_KNI_TAUMAX = 63
+BC_P_NAV16_G = 64
+BC_P_NAV16_PHI = 65
+BC_P_KCA22_G = 66
+BC_P_KCA22_PHI = 67
+BC_P_KCA22_DIFF = 68
+BC_P_KCA11_G = 69
+BC_P_KCA11_PHI = 70
+BC_P_KCA11_QO = 71
+BC_P_KCA11_QC = 72
 
-BC_ABI_VERSION = 300
+BC_ABI_VERSION = 400
 
 BC_VARIANT_LEAN = 0
 BC_VARIANT_EXTRA = 1
@@ -121,7 +133,7 @@ BC_GRU_HIDDEN = 64
 BC_GRU_INPUTS = 4
 BC_SURROGATE_NORM = 5
 
-BC_PROBE_CURRENT = 32
+BC_PROBE_CURRENT = 64
 BC_CUR_IL = 0
 BC_CUR_KLEAK = 1
 BC_CUR_NA = 2
@@ -141,7 +153,10 @@ BC_CUR_KA2 = 15
 BC_CUR_KK2A = 16
 BC_CUR_KK2B = 17
 BC_CUR_KNI = 18
-BC_NCUR = 19
+BC_CUR_NAV16 = 19
+BC_CUR_KCA22 = 20
+BC_CUR_KCA11 = 21
+BC_NCUR = 22
 
 BC_STATE_V = 0
 BC_STATE_NA_P = 1
@@ -168,7 +183,18 @@ BC_STATE_KK2B_P = 21
 BC_STATE_KK2B_Q = 22
 BC_STATE_KNI_P = 23
 BC_STATE_V_LAST = 24
-BC_NSTATE_VIEW = 25
+BC_STATE_NAV16_C1 = 25
+BC_STATE_NAV16_O = 35
+BC_STATE_KCA22_C2 = 37
+BC_STATE_KCA11_C1 = 42
+BC_NSTATE_VIEW = 51
+# the independent states of each Markov scheme, in view order (first appearance in
+# the scheme's transition list, the dependent state left out)
+MARKOV_STATES = {
+    "Nav1p6_MA2020_GoC": (BC_STATE_NAV16_C1, ("C1", "C2", "C3", "C4", "C5", "I1", "I2", "I3", "I4", "I5", "O", "B")),
+    "Kca2p2_MA2020_GoC": (BC_STATE_KCA22_C2, ("C2", "C3", "C4", "O1", "O2")),
+    "Kca1p1_MA2020_GoC": (BC_STATE_KCA11_C1, ("C1", "C2", "C3", "C4", "O0", "O1", "O2", "O3", "O4")),
+}
 BC_NOALLOC_MAX_CV = 262144
 
 STATE_NAMES = {
@@ -198,6 +224,9 @@ STATE_NAMES = {
     "KNI_p": BC_STATE_KNI_P,
     "V_last": BC_STATE_V_LAST,
 }
+for _cls, (_base, _names) in MARKOV_STATES.items():
+    for _k, _n in enumerate(_names):
+        STATE_NAMES[f"{_cls.split('_')[0]}_{_n}"] = _base + _k
 
 _p = C.POINTER
 

@@ -342,6 +342,9 @@ PROBE_STATES = {
     ("KK2B_HM1992", "p"): _abi.BC_STATE_KK2B_P, ("KK2B_HM1992", "q"): _abi.BC_STATE_KK2B_Q,
     ("KNI_Ya1989", "p"): _abi.BC_STATE_KNI_P,
 }
+for _cls, (_base, _names) in _abi.MARKOV_STATES.items():
+    for _k, _n in enumerate(_names):
+        PROBE_STATES[(_cls, _n)] = _base + _k
 
 
 # CurrentProbe: mechanism class -> BC_CUR_* code; ion name -> the ion's total
@@ -351,6 +354,8 @@ PROBE_CURRENTS = {
     "AHP_De1994": _abi.BC_CUR_AHP, "Na_HH1952": _abi.BC_CUR_NAHH, "K_HH1952": _abi.BC_CUR_KHH,
     "KM_RI2021_SC": _abi.BC_CUR_KM, "KA1_HM1992": _abi.BC_CUR_KA1, "KA2_HM1992": _abi.BC_CUR_KA2,
     "KK2A_HM1992": _abi.BC_CUR_KK2A, "KK2B_HM1992": _abi.BC_CUR_KK2B, "KNI_Ya1989": _abi.BC_CUR_KNI,
+    "Nav1p6_MA2020_GoC": _abi.BC_CUR_NAV16, "Kca2p2_MA2020_GoC": _abi.BC_CUR_KCA22,
+    "Kca1p1_MA2020_GoC": _abi.BC_CUR_KCA11,
 }
 ION_CURRENTS = {"na": _abi.BC_CUR_ION_NA, "k": _abi.BC_CUR_ION_K, "ca": _abi.BC_CUR_ION_CA}
 

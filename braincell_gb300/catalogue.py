@@ -21,13 +21,21 @@ Every class name, parameter name and default below is the reference's:
 * ``KK2A_HM1992`` -- channel/potassium.py:765 (g_max 10, q10_p = q10_q = 1, temp = temp_refs = 36 degC, V_sh 0)
 * ``KK2B_HM1992`` -- channel/potassium.py:899 (as KK2A_HM1992)
 * ``KNI_Ya1989``  -- channel/potassium.py:1045 (g_max 0.004, q10 1, temp = temp_ref = 36 degC, tau_max 4 s, V_sh 0)
+* ``Nav1p6_MA2020_GoC`` -- channel/sodium.py:727 (Markov; g_max 16, temp 22 degC, phi = 3^((T - 22 degC) / 10))
+* ``Kca2p2_MA2020_GoC`` -- channel/potassium_calcium.py:613 (Markov; g_max 38, q10_base 3, diff 3, temp 22 degC,
+  phi = q10_base^((T - 23 degC) / 10))
+* ``Kca1p1_MA2020_GoC`` -- channel/potassium_calcium.py:1107 (Markov; g_max 10, q10_base 3, temp 22 degC, phi as
+  Kca2p2; alpha(V) = exp(0.73 F V / R T), beta(V) = exp(-0.67 F V / R T))
 
 Same-form classes: Na_TM1991 has Na_Ba2002's Traub-Miles rate functions written
 in terms of V_sh - V (sodium.py:275-289 against :154-170), K_TM1991 has
 KDR_Ba2002's (potassium.py:331-337 against :208-214), and CaHT_HM1992 has
 CaT_HM1992's (calcium.py:645-663 against :355-373); only their defaults differ.
 KM_MA2020_GoC and KM_MA2020_GrC (potassium.py:4419, :5182) repeat KM_RI2021_SC's
-rates, gate temperature factor and defaults.
+rates, gate temperature factor and defaults.  The Markov channels' cell-type variants
+repeat their base class unchanged (Nav1p6_MA2024_PC / _MA2025_BC / _RI2021_SC,
+sodium.py:943-1190; Kca2p2 and Kca1p1 _MA2025_BC / _MA2020_GrC / _MA2024_PC /
+_RI2021_SC, potassium_calcium.py).
 Each fills the parameter record and kernel slot of its same-form class, so a
 region cannot carry both classes of one pair.
 * ions: ``SodiumFixed`` E 50 (ion/sodium.py:149), ``PotassiumFixed`` E -95
@@ -53,6 +61,8 @@ T36 = celsius2kelvin(36.0)
 T24 = celsius2kelvin(24.0)
 T22 = celsius2kelvin(22.0)
 T30 = celsius2kelvin(30.0)
+FARADAY = 96485.33212  # C/mol
+GAS_R = 8.314462618  # J/(mol K)
 
 CHANNELS: dict[str, dict[str, float]] = {
     "IL": {"g_max": 0.1, "E": -70.0},
@@ -90,10 +100,22 @@ CHANNELS: dict[str, dict[str, float]] = {
         "g_max": 10.0, "temp": T36, "q10_p": 1.0, "temp_ref_p": T36, "q10_q": 1.0, "temp_ref_q": T36, "V_sh": 0.0,
     },
     "KNI_Ya1989": {"g_max": 0.004, "temp": T36, "q10": 1.0, "temp_ref": T36, "tau_max": 4e3, "V_sh": 0.0},
+    "Nav1p6_MA2020_GoC": {"g_max": 16.0, "temp": T22},
+    "Kca2p2_MA2020_GoC": {"g_max": 38.0, "q10_base": 3.0, "diff": 3.0, "temp": T22},
+    "Kca1p1_MA2020_GoC": {"g_max": 10.0, "q10_base": 3.0, "temp": T22},
+}
+MARKOV_VARIANTS = {
+    "Nav1p6_MA2020_GoC": ("Nav1p6_MA2024_PC", "Nav1p6_MA2025_BC", "Nav1p6_RI2021_SC"),
+    "Kca2p2_MA2020_GoC": ("Kca2p2_MA2025_BC", "Kca2p2_MA2020_GrC", "Kca2p2_MA2024_PC", "Kca2p2_RI2021_SC"),
+    "Kca1p1_MA2020_GoC": ("Kca1p1_MA2025_BC", "Kca1p1_MA2020_GrC", "Kca1p1_MA2024_PC", "Kca1p1_RI2021_SC"),
 }
 # class -> the class whose kernel (rate functions, parameter slots, states) it uses
 SAME_FORM = {"Na_TM1991": "Na_Ba2002", "K_TM1991": "KDR_Ba2002", "CaHT_HM1992": "CaT_HM1992",
              "KM_MA2020_GoC": "KM_RI2021_SC", "KM_MA2020_GrC": "KM_RI2021_SC"}
+for _base, _variants in MARKOV_VARIANTS.items():
+    for _v in _variants:
+        CHANNELS[_v] = dict(CHANNELS[_base])
+        SAME_FORM[_v] = _base
 # gate temperature factors fixed by a class (not constructor parameters)
 KM_Q10, KM_TEMP_REF = 3.0, T22
 _ALIASES = {"leaky": "IL"}
@@ -231,14 +253,29 @@ def region_record(mechs, cable: CableProperty) -> tuple[int, np.ndarray]:
             rec[_abi.BC_P_KNI_G], rec[_abi.BC_P_KNI_VSH] = p["g_max"], p["V_sh"]
             rec[_abi.BC_P_KNI_PHI] = q10_phi(p["q10"], p["temp"], p["temp_ref"])
             rec[_abi.BC_P_KNI_TAUMAX] = p["tau_max"]
+        elif name == "Nav1p6_MA2020_GoC":
+            bits |= _abi.BC_M_NAV16
+            rec[_abi.BC_P_NAV16_G] = p["g_max"]
+            rec[_abi.BC_P_NAV16_PHI] = q10_phi(3.0, p["temp"], T22)
+        elif name == "Kca2p2_MA2020_GoC":
+            bits |= _abi.BC_M_KCA22
+            rec[_abi.BC_P_KCA22_G], rec[_abi.BC_P_KCA22_DIFF] = p["g_max"], p["diff"]
+            rec[_abi.BC_P_KCA22_PHI] = q10_phi(p["q10_base"], p["temp"], celsius2kelvin(23.0))
+        elif name == "Kca1p1_MA2020_GoC":
+            bits |= _abi.BC_M_KCA11
+            rec[_abi.BC_P_KCA11_G] = p["g_max"]
+            rec[_abi.BC_P_KCA11_PHI] = q10_phi(p["q10_base"], p["temp"], celsius2kelvin(23.0))
+            rec[_abi.BC_P_KCA11_QO] = 0.73 * FARADAY * 1e-3 / (GAS_R * p["temp"])
+            rec[_abi.BC_P_KCA11_QC] = -0.67 * FARADAY * 1e-3 / (GAS_R * p["temp"])
         elif name in _PQ_RECORDS:
             bit, base = _PQ_RECORDS[name]
             bits |= bit
             rec[base], rec[base + 1] = p["g_max"], p["V_sh"]
             rec[base + 2] = q10_phi(p["q10_p"], p["temp"], p["temp_ref_p"])
             rec[base + 3] = q10_phi(p["q10_q"], p["temp"], p["temp_ref_q"])
-    if bits & (_abi.BC_M_AHP) and not bits & _abi.BC_M_CADET:
-        # AHP reads Ci from the calcium ion; with a fixed Ca ion Ci is the class default.
+    if bits & (_abi.BC_M_AHP | _abi.BC_M_KCA22 | _abi.BC_M_KCA11) and not bits & _abi.BC_M_CADET:
+        # AHP and the Kca channels read Ci from the calcium ion; with a fixed Ca ion
+        # Ci is the class default.
         rec[_abi.BC_P_CA_CI0] = 5e-5
         rec[_abi.BC_P_CA_CREST] = 5e-5
     return bits, rec

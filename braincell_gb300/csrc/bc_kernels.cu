@@ -217,7 +217,8 @@ __device__ __forceinline__ void load_states(const Real* st, int N, uint32_t m, N
 template <typename Real>
 __device__ __forceinline__ double probe_state(const Real* st, int N, int field) {
   if (field == BC_STATE_CA_CI) return double(st[kSlotCaHi * N]) + double(st[kSlotCaLo * N]);
-  const int slot = field <= BC_STATE_AHP_P ? field - 1 : field;  // slots 9, 10 hold Ci
+  // slots 9, 10 hold Ci; the Markov views 25.. sit one above their slots 26..
+  const int slot = field <= BC_STATE_AHP_P ? field - 1 : (field >= BC_STATE_NAV16_C1 ? field + 1 : field);
   return double(st[slot * N]);
 }
 
@@ -292,16 +293,28 @@ __device__ __forceinline__ double probe_current(const Real* st, int N, const Rea
         return (m & BC_M_KK2B) ? P[BC_P_KK2B_G] * st[kSlotKK2BP * N] * st[kSlotKK2BQ * N] * (P[BC_P_EK] - v) : Real(0);
       case BC_CUR_KNI:
         return (m & BC_M_KNI) ? P[BC_P_KNI_G] * st[kSlotKNIP * N] * (P[BC_P_EK] - v) : Real(0);
+      case BC_CUR_NAV16:
+        return (m & BC_M_NAV16) ? P[BC_P_NAV16_G] * st[(kSlotNav16 + 10) * N] * (P[BC_P_ENA] - v) : Real(0);
+      case BC_CUR_KCA22:
+        return (m & BC_M_KCA22)
+                   ? P[BC_P_KCA22_G] * (st[(kSlotKca22 + 3) * N] + st[(kSlotKca22 + 4) * N]) * (P[BC_P_EK] - v)
+                   : Real(0);
+      case BC_CUR_KCA11: {
+        if (!(m & BC_M_KCA11)) return Real(0);
+        Real o = Real(0);
+        for (int k = 4; k < 9; ++k) o += st[(kSlotKca11 + k) * N];
+        return P[BC_P_KCA11_G] * o * (P[BC_P_EK] - v);
+      }
     }
     return Real(0);
   };
   switch (code) {
     case BC_CUR_ION_NA:
-      return double(cur(BC_CUR_NA)) + double(cur(BC_CUR_NAHH));
+      return double(cur(BC_CUR_NA)) + double(cur(BC_CUR_NAHH)) + double(cur(BC_CUR_NAV16));
     case BC_CUR_ION_K:
       return double(cur(BC_CUR_KDR)) + double(cur(BC_CUR_KLEAK)) + double(cur(BC_CUR_AHP)) + double(cur(BC_CUR_KHH)) +
              double(cur(BC_CUR_KM)) + double(cur(BC_CUR_KA1)) + double(cur(BC_CUR_KA2)) + double(cur(BC_CUR_KK2A)) +
-             double(cur(BC_CUR_KK2B)) + double(cur(BC_CUR_KNI));
+             double(cur(BC_CUR_KK2B)) + double(cur(BC_CUR_KNI)) + double(cur(BC_CUR_KCA22)) + double(cur(BC_CUR_KCA11));
     case BC_CUR_ION_CA:
       return double(cur(BC_CUR_CAL)) + double(cur(BC_CUR_CAT));
     default:
@@ -313,8 +326,12 @@ __device__ __forceinline__ double probe_current(const Real* st, int N, const Rea
 // M current, the A current, the slow K2 current, the slow non-inactivating K
 // current): kept out of line so that their registers do not weigh on the common
 // path; same exp-Euler steps and ohmic currents as the others.
-constexpr uint32_t kExtraChannels =
-    BC_M_NAHH | BC_M_KHH | BC_M_KM | BC_M_KA1 | BC_M_KA2 | BC_M_KK2A | BC_M_KK2B | BC_M_KNI;
+constexpr uint32_t kExtraChannels = BC_M_NAHH | BC_M_KHH | BC_M_KM | BC_M_KA1 | BC_M_KA2 | BC_M_KK2A | BC_M_KK2B |
+                                   BC_M_KNI | BC_M_NAV16 | BC_M_KCA22 | BC_M_KCA11;
+
+__device__ __forceinline__ MarkovGraph nav16_graph() { return MarkovGraph{13, 17, 12, kSlotNav16, kNav16Src, kNav16Dst}; }
+__device__ __forceinline__ MarkovGraph kca22_graph() { return MarkovGraph{6, 5, 0, kSlotKca22, kKca22Src, kKca22Dst}; }
+__device__ __forceinline__ MarkovGraph kca11_graph() { return MarkovGraph{10, 13, 0, kSlotKca11, kKca11Src, kKca11Dst}; }
 
 // One A-current mechanism (p^4 q, E_K) in slots (sp, sq) with parameters from pg.
 template <typename Real>
@@ -352,7 +369,8 @@ __device__ __forceinline__ void k2_current(Real* st, int N, const Real* P, int s
 }
 
 template <typename Real>
-__device__ __noinline__ void extra_channels(Real* st, int N, const Real* P, uint32_t m, Real v, Real dt, bool advance,
+__device__ __noinline__ void extra_channels(Real* st, int N, const Real* P, uint32_t m, Real v, Real ci, Real dt,
+                                            bool advance,
                                             Real& G, Real& I) {
   if (m & BC_M_NAHH) {
     Real p = st[kSlotNaHHP * N], q = st[kSlotNaHHQ * N];
@@ -407,6 +425,40 @@ __device__ __noinline__ void extra_channels(Real* st, int N, const Real* P, uint
     const Real g = P[BC_P_KNI_G] * p;
     G += g;
     I += g * (P[BC_P_EK] - v);
+  }
+  // Markov channels: the reference's independent-integration family, advanced
+  // after the gates (cell.py:2204-2217), each at the new V and Ci
+  if (m & (BC_M_NAV16 | BC_M_KCA22 | BC_M_KCA11)) {
+    Real kf[17], kb[17];
+    if (m & BC_M_NAV16) {
+      if (advance) {
+        nav16_rates(v, P[BC_P_NAV16_PHI], kf, kb);
+        markov_advance(st, N, nav16_graph(), kf, kb, dt);
+      }
+      const Real g = P[BC_P_NAV16_G] * st[(kSlotNav16 + 10) * N];  // O
+      G += g;
+      I += g * (P[BC_P_ENA] - v);
+    }
+    if (m & BC_M_KCA22) {
+      if (advance) {
+        kca22_rates(ci, P[BC_P_KCA22_PHI], P[BC_P_KCA22_DIFF], kf, kb);
+        markov_advance(st, N, kca22_graph(), kf, kb, dt);
+      }
+      const Real g = P[BC_P_KCA22_G] * (st[(kSlotKca22 + 3) * N] + st[(kSlotKca22 + 4) * N]);  // O1 + O2
+      G += g;
+      I += g * (P[BC_P_EK] - v);
+    }
+    if (m & BC_M_KCA11) {
+      if (advance) {
+        kca11_rates(v, ci, P[BC_P_KCA11_PHI], P[BC_P_KCA11_QO], P[BC_P_KCA11_QC], kf, kb);
+        markov_advance(st, N, kca11_graph(), kf, kb, dt);
+      }
+      Real o = Real(0);
+      for (int k = 4; k < 9; ++k) o += st[(kSlotKca11 + k) * N];  // O0 .. O4
+      const Real g = P[BC_P_KCA11_G] * o;
+      G += g;
+      I += g * (P[BC_P_EK] - v);
+    }
   }
 }
 
@@ -526,15 +578,19 @@ __device__ __forceinline__ void node_mechanisms_loaded(const NodeStates<Real>& s
     G += g;
     I += g * (P[BC_P_EK] - v);
   }
-  if (kExtra && (m & kExtraChannels)) extra_channels(st, N, P, m, v_new, dt, advance, G, I);
+  if (kExtra && (m & kExtraChannels)) {
+    // the calcium the Markov Kca channels bind: the new Ci of a dynamic ion, else the fixed one
+    const Real ci = (m & BC_M_CADET) ? cahi + calo : P[BC_P_CA_CI0];
+    extra_channels(st, N, P, m, v_new, ci, dt, advance, G, I);
+  }
 }
 
-template <typename Real>
+template <typename Real, bool kExtra = true>
 __device__ __forceinline__ void node_mechanisms(Real* st, int N, const Real* P, uint32_t m, Real v_old, Real v_new,
                                                 Real dt, bool advance, Real& G, Real& I) {
   NodeStates<Real> s;
   load_states(st, N, m, s);
-  node_mechanisms_loaded(s, st, N, P, m, v_old, v_new, dt, advance, G, I);
+  node_mechanisms_loaded<Real, kExtra>(s, st, N, P, m, v_old, v_new, dt, advance, G, I);
 }
 
 // Steady state of every gate at v (HH.reset_state), Ci = Ci0.
@@ -604,6 +660,23 @@ __device__ __forceinline__ void steady_states(const Real* P, uint32_t m, Real* s
     st[kSlotKK2BQ * N] = r.qinf;
   }
   if (m & BC_M_KNI) st[kSlotKNIP * N] = KNIRates<Real>(v, P[BC_P_KNI_VSH], P[BC_P_KNI_TAUMAX]).pinf;
+  if (m & (BC_M_NAV16 | BC_M_KCA22 | BC_M_KCA11)) {
+    // Markov channels start at their stationary distribution (reset_steady_state)
+    Real kf[17], kb[17];
+    const Real ci = P[BC_P_CA_CI0];
+    if (m & BC_M_NAV16) {
+      nav16_rates(v, P[BC_P_NAV16_PHI], kf, kb);
+      markov_steady(st, N, nav16_graph(), kf, kb);
+    }
+    if (m & BC_M_KCA22) {
+      kca22_rates(ci, P[BC_P_KCA22_PHI], P[BC_P_KCA22_DIFF], kf, kb);
+      markov_steady(st, N, kca22_graph(), kf, kb);
+    }
+    if (m & BC_M_KCA11) {
+      kca11_rates(v, ci, P[BC_P_KCA11_PHI], P[BC_P_KCA11_QO], P[BC_P_KCA11_QC], kf, kb);
+      markov_steady(st, N, kca11_graph(), kf, kb);
+    }
+  }
 }
 
 // Row i of the next linear system: diag = 1 + dt (D + G / cm), rhs = dt I / cm
@@ -1449,7 +1522,8 @@ __global__ void __launch_bounds__(kVar >= 2 ? BC_PORT_MAX_THREADS : 1024, kVar >
     Real G = Real(0), I = Real(0);
     if (pr != kBoundary) {
       const Real v = tv.v[i].x;
-      node_mechanisms(tv.state + i, tv.N, tv.params + size_t(pr) * kParamStride, tv.mech[pr], v, v, dt, false, G, I);
+      node_mechanisms<Real, kExtra>(tv.state + i, tv.N, tv.params + size_t(pr) * kParamStride, tv.mech[pr], v, v, dt,
+                                    false, G, I);
     }
     const uint16_t sp = tv.spec[i];
     if (sp != kNoSpecial) {

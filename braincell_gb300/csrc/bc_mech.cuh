@@ -16,6 +16,9 @@
 //   KK2A_HM1992      channel/potassium.py:881-895, KK2B_HM1992 :1023-1041
 //   KNI_Ya1989       channel/potassium.py:1156-1163
 //   CalciumDetailed  ion/calcium.py:499-505, Nernst E: ion/_base.py:463-469
+//   Markov channels  channel/_base.py:677-1125 (template), quad/_backward_euler.py:31-64;
+//                    Nav1p6_MA2020_GoC sodium.py:727-940, Kca2p2_MA2020_GoC
+//                    potassium_calcium.py:613-790, Kca1p1_MA2020_GoC :1107-1353
 // CUDA's own exp / expm1 / log are called; nothing of the math library is
 // re-implemented here.
 #pragma once
@@ -262,5 +265,214 @@ constexpr double kGasR = 8.314462618;      // J/(mol K)
 constexpr double kNernstCa = 1e3 * kGasR / (2.0 * kFaraday);
 // uA/cm^2 -> mM/ms influx per um of shell depth: 10 / (2 F)
 constexpr double kCaDrive = 10.0 / (2.0 * kFaraday);
+
+// ---------------------------------------------------------------- Markov channels
+// The independent states of each scheme (channel/_base.py:677-1125: every state but
+// the dependent one, which is 1 - their sum), in the order they first appear in the
+// scheme's transition list.  Plans with a Markov channel carry kNumSlotsMarkov
+// slots per node; the others kNumSlots.
+constexpr int kSlotNav16 = 26;  // Nav1p6_MA2020_GoC: C1..C5, I1..I5, O, B
+constexpr int kSlotKca22 = 38;  // Kca2p2_MA2020_GoC: C2, C3, C4, O1, O2
+constexpr int kSlotKca11 = 43;  // Kca1p1_MA2020_GoC: C1..C4, O0..O4
+constexpr int kNumSlotsMarkov = 52;
+constexpr int kMarkovMaxStates = 13;
+
+// A transition graph: states 0 .. ns-1 (dep is eliminated), pair k moves src -> dst
+// at kf[k] * s[src] and back at kb[k] * s[dst].
+struct MarkovGraph {
+  int ns, np, dep, slot0;
+  const int8_t* src;
+  const int8_t* dst;
+};
+
+// sodium.py:840-858: C1 0 .. C5 4, I1 5 .. I5 9, O 10, B 11, I6 12
+static __device__ __constant__ const int8_t kNav16Src[17] = {0, 1, 2, 3, 0, 5, 1, 6, 2, 7, 3, 8, 4, 4, 10, 9, 10};
+static __device__ __constant__ const int8_t kNav16Dst[17] = {1, 2, 3, 4, 5, 6, 6, 7, 7, 8, 8, 9, 9, 10, 11, 12, 12};
+// potassium_calcium.py:717-724: C1 0, C2 1, C3 2, C4 3, O1 4, O2 5
+static __device__ __constant__ const int8_t kKca22Src[5] = {0, 1, 2, 2, 3};
+static __device__ __constant__ const int8_t kKca22Dst[5] = {1, 2, 3, 4, 5};
+// potassium_calcium.py:1213-1228: C0 0 .. C4 4, O0 5 .. O4 9
+static __device__ __constant__ const int8_t kKca11Src[13] = {0, 1, 2, 3, 5, 6, 7, 8, 0, 1, 2, 3, 4};
+static __device__ __constant__ const int8_t kKca11Dst[13] = {1, 2, 3, 4, 6, 7, 8, 9, 5, 6, 7, 8, 9};
+
+// Nav1p6 rates (sodium.py:903-935; constants :874-898 with x3 = x5 = 1e12,
+// x4 = -1e12 and the V shifts 0): alfac = (Oon / Con)^(1/4), btfac = (Ooff / Coff)^(1/4).
+template <typename Real>
+__device__ __forceinline__ void nav16_rates(Real v, Real phi, Real* kf, Real* kb) {
+  const Real al = Real(150), be = Real(3), ga = Real(150), de = Real(40), ep = Real(1.75), ze = Real(0.03);
+  const Real con = Real(0.005), coff = Real(0.5), oon = Real(0.75), ooff = Real(0.005);
+  const double af[5] = {1.0, 3.4996355115805833, 12.24744871391589, 42.861606445481996, 150.0};
+  const double bf[5] = {1.0, 0.31622776601683794, 0.1, 0.03162277660168379, 0.01};
+  const Real ea = aexp(v / Real(20)) * phi, eb = aexp(v / Real(-20)) * phi;
+  const Real e3 = aexp(v / Real(1e12)) * phi, e4 = aexp(v / Real(-1e12)) * phi, e6 = aexp(v / Real(-25)) * phi;
+  const Real e5 = aexp(v / Real(1e12)) * phi;
+  const Real alfac = Real(af[1]), btfac = Real(bf[1]);
+  // pair order: C1C2 C2C3 C3C4 C4C5 C1I1 I1I2 C2I2 I2I3 C3I3 I3I4 C4I4 I4I5 C5I5 C5O OB I5I6 OI6
+  kf[0] = Real(4) * al * ea;  kb[0] = Real(1) * be * eb;
+  kf[1] = Real(3) * al * ea;  kb[1] = Real(2) * be * eb;
+  kf[2] = Real(2) * al * ea;  kb[2] = Real(3) * be * eb;
+  kf[3] = Real(1) * al * ea;  kb[3] = Real(4) * be * eb;
+  kf[4] = con * phi;          kb[4] = coff * phi;
+  kf[5] = Real(4) * al * alfac * ea;  kb[5] = Real(1) * be * btfac * eb;
+  kf[6] = con * Real(af[1]) * phi;    kb[6] = coff * Real(bf[1]) * phi;
+  kf[7] = Real(3) * al * alfac * ea;  kb[7] = Real(2) * be * btfac * eb;
+  kf[8] = con * Real(af[2]) * phi;    kb[8] = coff * Real(bf[2]) * phi;
+  kf[9] = Real(2) * al * alfac * ea;  kb[9] = Real(3) * be * btfac * eb;
+  kf[10] = con * Real(af[3]) * phi;   kb[10] = coff * Real(bf[3]) * phi;
+  kf[11] = Real(1) * al * alfac * ea; kb[11] = Real(4) * be * btfac * eb;
+  kf[12] = con * Real(af[4]) * phi;   kb[12] = coff * Real(bf[4]) * phi;
+  kf[13] = ga * e3;                   kb[13] = de * e4;
+  kf[14] = ep * e5;                   kb[14] = ze * e6;
+  kf[15] = ga * e3;                   kb[15] = de * e4;
+  kf[16] = oon * phi;                 kb[16] = ooff * phi;
+}
+
+// Kca2p2 rates (potassium_calcium.py:760-790; constants :740-753): the
+// calcium-binding steps at k phi Ci / diff, the others at k phi.
+template <typename Real>
+__device__ __forceinline__ void kca22_rates(Real ci, Real phi, Real diff, Real* kf, Real* kb) {
+  const Real c = phi * ci / diff;
+  kf[0] = Real(200) * c;       kb[0] = Real(80e-3) * phi;
+  kf[1] = Real(160) * c;       kb[1] = Real(80e-3) * phi;
+  kf[2] = Real(80) * c;        kb[2] = Real(200e-3) * phi;
+  kf[3] = Real(160e-3) * phi;  kb[3] = Real(1) * phi;
+  kf[4] = Real(1.2) * phi;     kb[4] = Real(100e-3) * phi;
+}
+
+// Kca1p1 rates (potassium_calcium.py:1277-1353; constants :1243-1265): binding at
+// (4 - i) Ci k1, unbinding at (i + 1) Kc k1 (closed) or (i + 1) Ko k1 (open),
+// opening at pf_i exp(Qo F V / R T), closing at pb_i exp(Qc F V / R T), all x phi.
+template <typename Real>
+__device__ __forceinline__ void kca11_rates(Real v, Real ci, Real phi, Real qo, Real qc, Real* kf, Real* kb) {
+  const double pf[5] = {2.39e-3, 7.0e-3, 40e-3, 295e-3, 557e-3};
+  const double pb[5] = {3936e-3, 1152e-3, 659e-3, 486e-3, 92e-3};
+  const Real on = Real(1e3) * phi * ci;
+  const Real a = aexp(qo * v) * phi, b = aexp(qc * v) * phi;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    kf[i] = Real(4 - i) * on;
+    kb[i] = Real(i + 1) * Real(11.0e-3 * 1e3) * phi;
+    kf[4 + i] = Real(4 - i) * on;
+    kb[4 + i] = Real(i + 1) * Real(1.1e-3 * 1e3) * phi;
+  }
+#pragma unroll
+  for (int i = 0; i < 5; ++i) {
+    kf[8 + i] = Real(pf[i]) * a;
+    kb[8 + i] = Real(pb[i]) * b;
+  }
+}
+
+// Gaussian elimination with partial pivoting of the n x n system in A[.][0..n-1]
+// with its right-hand side in A[.][n]; the solution replaces column n.
+template <typename Real>
+__device__ __forceinline__ void dense_solve(Real (*A)[kMarkovMaxStates + 1], int n) {
+  for (int c = 0; c < n; ++c) {
+    int piv = c;
+    Real best = fabs(A[c][c]);
+    for (int r = c + 1; r < n; ++r)
+      if (fabs(A[r][c]) > best) {
+        best = fabs(A[r][c]);
+        piv = r;
+      }
+    if (piv != c)
+      for (int k = c; k <= n; ++k) {
+        const Real t = A[c][k];
+        A[c][k] = A[piv][k];
+        A[piv][k] = t;
+      }
+    for (int r = c + 1; r < n; ++r) {
+      const Real l = A[r][c] / A[c][c];
+      if (l != Real(0))
+        for (int k = c + 1; k <= n; ++k) A[r][k] -= l * A[c][k];
+    }
+  }
+  for (int c = n - 1; c >= 0; --c) {
+    Real x = A[c][n];
+    for (int k = c + 1; k < n; ++k) x -= A[c][k] * A[k][n];
+    A[c][n] = x / A[c][c];
+  }
+}
+
+// One linearised backward-Euler step (quad/_backward_euler.py:31-64) of a Markov
+// scheme's independent states in slots slot0.. of the node's state column: the
+// kinetics see each independent state clipped to [0, 1] and the dependent state as
+// 1 - the raw sum (channel/_base.py:852-878, 1105-1125); J = df/dy there (d clip /
+// dy = 1 on [0, 1], 0 outside); (I - dt J) dy = dt f; y += dy.
+template <typename Real>
+__device__ void markov_advance(Real* st, int N, const MarkovGraph& g, const Real* kf, const Real* kb, Real dt) {
+  Real A[kMarkovMaxStates][kMarkovMaxStates + 1];
+  Real s[kMarkovMaxStates], msk[kMarkovMaxStates];
+  const int ni = g.ns - 1;
+  Real sum = Real(0);
+  for (int k = 0; k < g.ns; ++k) {
+    if (k == g.dep) continue;
+    const int j = k < g.dep ? k : k - 1;
+    const Real y = st[(g.slot0 + j) * N];
+    sum += y;
+    s[k] = y < Real(0) ? Real(0) : (y > Real(1) ? Real(1) : y);
+    msk[k] = (y >= Real(0) && y <= Real(1)) ? Real(1) : Real(0);
+  }
+  s[g.dep] = Real(1) - sum;
+  msk[g.dep] = Real(0);
+  for (int r = 0; r < ni; ++r)
+    for (int c = 0; c <= ni; ++c) A[r][c] = Real(0);
+  // A[.][0..ni-1] = J, A[.][ni] = f
+  for (int p = 0; p < g.np; ++p) {
+    const int a = g.src[p], b = g.dst[p];
+    for (int dir = 0; dir < 2; ++dir) {
+      const int by = dir ? b : a, to = dir ? a : b;
+      const Real rate = dir ? kb[p] : kf[p];
+      const Real fl = rate * s[by];
+      const int rf = by == g.dep ? -1 : (by < g.dep ? by : by - 1);
+      const int rt = to == g.dep ? -1 : (to < g.dep ? to : to - 1);
+      if (rf >= 0) A[rf][ni] -= fl;
+      if (rt >= 0) A[rt][ni] += fl;
+      if (by == g.dep) {  // d s_dep / d y_j = -1 for every j
+        if (rt >= 0)
+          for (int c = 0; c < ni; ++c) A[rt][c] -= rate;
+      } else {
+        const Real d = rate * msk[by];
+        A[rf][rf] -= d;
+        if (rt >= 0) A[rt][rf] += d;
+      }
+    }
+  }
+  for (int r = 0; r < ni; ++r) {
+    for (int c = 0; c < ni; ++c) A[r][c] = (r == c ? Real(1) : Real(0)) - dt * A[r][c];
+    A[r][ni] *= dt;
+  }
+  dense_solve(A, ni);
+  for (int j = 0; j < ni; ++j) st[(g.slot0 + j) * N] += A[j][ni];
+}
+
+// Stationary distribution of a scheme (channel/_base.py:1033-1091): the generator
+// with the dependent state's row replaced by ones = 1, solved, clipped at 0 and
+// renormalised; the independent states are stored.
+template <typename Real>
+__device__ void markov_steady(Real* st, int N, const MarkovGraph& g, const Real* kf, const Real* kb) {
+  Real A[kMarkovMaxStates][kMarkovMaxStates + 1];
+  const int n = g.ns;
+  for (int r = 0; r < n; ++r)
+    for (int c = 0; c <= n; ++c) A[r][c] = Real(0);
+  for (int p = 0; p < g.np; ++p) {
+    const int a = g.src[p], b = g.dst[p];
+    A[a][a] -= kf[p];
+    A[b][a] += kf[p];
+    A[a][b] += kb[p];
+    A[b][b] -= kb[p];
+  }
+  for (int c = 0; c < n; ++c) A[g.dep][c] = Real(1);
+  A[g.dep][n] = Real(1);
+  dense_solve(A, n);
+  Real tot = Real(0);
+  for (int k = 0; k < n; ++k) {
+    A[k][n] = A[k][n] < Real(0) ? Real(0) : A[k][n];
+    tot += A[k][n];
+  }
+  for (int k = 0; k < n; ++k) {
+    if (k == g.dep) continue;
+    st[(g.slot0 + (k < g.dep ? k : k - 1)) * N] = A[k][n] / tot;
+  }
+}
 
 }  // namespace bc

@@ -62,6 +62,33 @@ constexpr int kMaxClasses = 4;
 constexpr int kDefaultLaneNodes = 10;
 constexpr int kDefaultNarrowLaneNodes = 1;
 
+constexpr uint32_t kMarkovBits = BC_M_NAV16 | BC_M_KCA22 | BC_M_KCA11;
+
+namespace bc {
+
+// The mechanism bit that owns a BC_STATE_* view and the state slot holding it (V:
+// in the tile blob, no slot; V_last: every node; Ci and V_last also have a low word).
+static void state_view(int32_t which, uint32_t* bit, int* slot) {
+  static const uint32_t kBit[BC_STATE_NAV16_C1] = {
+      0,         BC_M_NA,   BC_M_NA,   BC_M_KDR,  BC_M_CAL,  BC_M_CAL,  BC_M_CAT,   BC_M_CAT,  BC_M_HCN,
+      BC_M_AHP,  BC_M_CADET, BC_M_NAHH, BC_M_NAHH, BC_M_KHH, BC_M_KM,   BC_M_KA1,   BC_M_KA1,  BC_M_KA2,
+      BC_M_KA2,  BC_M_KK2A, BC_M_KK2A, BC_M_KK2B, BC_M_KK2B, BC_M_KNI,  BC_M_ALL};
+  static const int kSlot[BC_STATE_NAV16_C1] = {
+      -1,         kSlotNaP,   kSlotNaQ,   kSlotKdrP,  kSlotCalP,  kSlotCalQ,  kSlotCatP,  kSlotCatQ,  kSlotHcnP,
+      kSlotAhpP,  kSlotCaHi,  kSlotNaHHP, kSlotNaHHQ, kSlotKHHP,  kSlotKMN,   kSlotKA1P,  kSlotKA1Q,  kSlotKA2P,
+      kSlotKA2Q,  kSlotKK2AP, kSlotKK2AQ, kSlotKK2BP, kSlotKK2BQ, kSlotKNIP,  kSlotVLastHi};
+  if (which < BC_STATE_NAV16_C1) {
+    *bit = kBit[which];
+    *slot = kSlot[which];
+    return;
+  }
+  // Markov views 25 .. 50 sit in slots 26 .. 51
+  *bit = which < BC_STATE_KCA22_C2 ? BC_M_NAV16 : (which < BC_STATE_KCA11_C1 ? BC_M_KCA22 : BC_M_KCA11);
+  *slot = which + 1;
+}
+
+}  // namespace bc
+
 struct LaunchClass {
   int first = 0, count = 0, threads = 256;
   bool smem = true;
@@ -1254,13 +1281,15 @@ bc_status bc_plan_create(const bc_batch_spec* spec, const bc_plan_options* opts_
   for (int64_t c = 0; c < s.n_cells; ++c) p->cell_ncv[c] = cells[c].n_cv;
   for (int64_t k = 0; k < s.n_cells * s.n_regions; ++k)
     p->extra = p->extra || (s.region_mech[k] & (BC_M_NAHH | BC_M_KHH | BC_M_KM | BC_M_KA1 | BC_M_KA2 | BC_M_KK2A |
-                                                 BC_M_KK2B | BC_M_KNI)) != 0;
+                                                 BC_M_KK2B | BC_M_KNI | kMarkovBits)) != 0;
   for (int64_t k = 0; k < s.n_cells * s.n_regions; ++k)
     if (s.region_mech[k] & ~BC_M_ALL) {
       delete p;
       return fail(BC_ERR_INVALID, "unknown mechanism bits in region_mech");
     }
-  const int S = kNumSlots;
+  bool markov = false;
+  for (int64_t k = 0; k < s.n_cells * s.n_regions; ++k) markov = markov || (s.region_mech[k] & kMarkovBits) != 0;
+  const int S = markov ? kNumSlotsMarkov : kNumSlots;  // the Markov states only where a plan has them
   p->state_slots = S;
   // ---------------------------------------------------- pulses / probes -> nodes
   std::vector<std::vector<int64_t>> cell_pulses(s.n_cells), cell_probes(s.n_cells);
@@ -1304,9 +1333,10 @@ bc_status bc_plan_create(const bc_batch_spec* spec, const bc_plan_options* opts_
     if (is_current) {
       static const uint32_t cur_owner[BC_NCUR] = {
           BC_M_IL,  BC_M_KLEAK, BC_M_NA,   BC_M_KDR, BC_M_CAL,           BC_M_CAT,
-          BC_M_HCN, BC_M_AHP,   BC_M_NAHH, BC_M_KHH, BC_M_KM,            BC_M_NA | BC_M_NAHH,
-          BC_M_KDR | BC_M_KLEAK | BC_M_AHP | BC_M_KHH | BC_M_KM | BC_M_KA1 | BC_M_KA2 | BC_M_KK2A | BC_M_KK2B | BC_M_KNI,
-          BC_M_CAL | BC_M_CAT,  BC_M_KA1,  BC_M_KA2, BC_M_KK2A, BC_M_KK2B, BC_M_KNI};
+          BC_M_HCN, BC_M_AHP,   BC_M_NAHH, BC_M_KHH, BC_M_KM,            BC_M_NA | BC_M_NAHH | BC_M_NAV16,
+          BC_M_KDR | BC_M_KLEAK | BC_M_AHP | BC_M_KHH | BC_M_KM | BC_M_KA1 | BC_M_KA2 | BC_M_KK2A | BC_M_KK2B | BC_M_KNI |
+              BC_M_KCA22 | BC_M_KCA11,
+          BC_M_CAL | BC_M_CAT,  BC_M_KA1,  BC_M_KA2, BC_M_KK2A, BC_M_KK2B, BC_M_KNI, BC_M_NAV16, BC_M_KCA22, BC_M_KCA11};
       const int32_t rg = cells[c].region[v];
       if (rg < 0 || !(s.region_mech[c * s.n_regions + rg] & cur_owner[field - BC_PROBE_CURRENT])) {
         delete p;
@@ -1314,14 +1344,11 @@ bc_status bc_plan_create(const bc_batch_spec* spec, const bc_plan_options* opts_
       }
     } else if (field != BC_STATE_V) {
       // the mechanism that owns the state must be present at the probed CV
-      static const uint32_t owner[BC_NSTATE_VIEW] = {0,          BC_M_NA,    BC_M_NA,    BC_M_KDR,   BC_M_CAL,
-                                                     BC_M_CAL,   BC_M_CAT,   BC_M_CAT,   BC_M_HCN,   BC_M_AHP,
-                                                     BC_M_CADET, BC_M_NAHH,  BC_M_NAHH,  BC_M_KHH,   BC_M_KM,
-                                                     BC_M_KA1,   BC_M_KA1,   BC_M_KA2,   BC_M_KA2,
-                                                     BC_M_KK2A,  BC_M_KK2A,  BC_M_KK2B,  BC_M_KK2B,
-                                                     BC_M_KNI,   0};
+      uint32_t owner = 0;
+      int slot = -1;
+      state_view(field, &owner, &slot);
       const int32_t rg = cells[c].region[v];
-      if (rg < 0 || !(s.region_mech[c * s.n_regions + rg] & owner[field])) {
+      if (rg < 0 || !(s.region_mech[c * s.n_regions + rg] & owner)) {
         delete p;
         return fail(BC_ERR_INVALID, "probe field: no such mechanism at the probed location");
       }
@@ -2089,41 +2116,11 @@ static bc_status view_offsets(bc_plan* p, int32_t which, std::vector<int64_t>& h
       lo[k] = hi[k] + rs;
       continue;
     }
-    const uint32_t m = p->cv_mech[k];
+    uint32_t bit = 0;
     int slot = -1;
-    bool has_lo = false;
-    switch (which) {
-      case BC_STATE_NA_P: slot = (m & BC_M_NA) ? kSlotNaP : -1; break;
-      case BC_STATE_NA_Q: slot = (m & BC_M_NA) ? kSlotNaQ : -1; break;
-      case BC_STATE_KDR_P: slot = (m & BC_M_KDR) ? kSlotKdrP : -1; break;
-      case BC_STATE_CAL_P: slot = (m & BC_M_CAL) ? kSlotCalP : -1; break;
-      case BC_STATE_CAL_Q: slot = (m & BC_M_CAL) ? kSlotCalQ : -1; break;
-      case BC_STATE_CAT_P: slot = (m & BC_M_CAT) ? kSlotCatP : -1; break;
-      case BC_STATE_CAT_Q: slot = (m & BC_M_CAT) ? kSlotCatQ : -1; break;
-      case BC_STATE_HCN_P: slot = (m & BC_M_HCN) ? kSlotHcnP : -1; break;
-      case BC_STATE_AHP_P: slot = (m & BC_M_AHP) ? kSlotAhpP : -1; break;
-      case BC_STATE_CA_CI:
-        slot = (m & BC_M_CADET) ? kSlotCaHi : -1;
-        has_lo = true;
-        break;
-      case BC_STATE_NAHH_P: slot = (m & BC_M_NAHH) ? kSlotNaHHP : -1; break;
-      case BC_STATE_NAHH_Q: slot = (m & BC_M_NAHH) ? kSlotNaHHQ : -1; break;
-      case BC_STATE_KHH_P: slot = (m & BC_M_KHH) ? kSlotKHHP : -1; break;
-      case BC_STATE_KM_N: slot = (m & BC_M_KM) ? kSlotKMN : -1; break;
-      case BC_STATE_KA1_P: slot = (m & BC_M_KA1) ? kSlotKA1P : -1; break;
-      case BC_STATE_KA1_Q: slot = (m & BC_M_KA1) ? kSlotKA1Q : -1; break;
-      case BC_STATE_KA2_P: slot = (m & BC_M_KA2) ? kSlotKA2P : -1; break;
-      case BC_STATE_KA2_Q: slot = (m & BC_M_KA2) ? kSlotKA2Q : -1; break;
-      case BC_STATE_KK2A_P: slot = (m & BC_M_KK2A) ? kSlotKK2AP : -1; break;
-      case BC_STATE_KK2A_Q: slot = (m & BC_M_KK2A) ? kSlotKK2AQ : -1; break;
-      case BC_STATE_KK2B_P: slot = (m & BC_M_KK2B) ? kSlotKK2BP : -1; break;
-      case BC_STATE_KK2B_Q: slot = (m & BC_M_KK2B) ? kSlotKK2BQ : -1; break;
-      case BC_STATE_KNI_P: slot = (m & BC_M_KNI) ? kSlotKNIP : -1; break;
-      case BC_STATE_V_LAST:
-        slot = kSlotVLastHi;
-        has_lo = true;
-        break;
-    }
+    state_view(which, &bit, &slot);
+    if (which != BC_STATE_V_LAST && !(p->cv_mech[k] & bit)) slot = -1;
+    const bool has_lo = which == BC_STATE_CA_CI || which == BC_STATE_V_LAST;
     if (slot < 0) continue;
     // states live in the separate state array: offsets are tagged by +state_tag
     const int lo_slot = which == BC_STATE_V_LAST ? kSlotVLastLo : kSlotCaLo;
@@ -2236,20 +2233,11 @@ static void noalloc_offset(const bc_plan* p, int32_t which, int64_t k, int64_t* 
     *lo = *hi + rs;
     return;
   }
-  static const uint32_t kBit[BC_NSTATE_VIEW] = {0,        BC_M_NA,    BC_M_NA,   BC_M_KDR,  BC_M_CAL,
-                                                BC_M_CAL, BC_M_CAT,   BC_M_CAT,  BC_M_HCN,  BC_M_AHP,
-                                                BC_M_CADET, BC_M_NAHH, BC_M_NAHH, BC_M_KHH, BC_M_KM,
-                                                BC_M_KA1,   BC_M_KA1,  BC_M_KA2,  BC_M_KA2,
-                                                BC_M_KK2A,  BC_M_KK2A, BC_M_KK2B, BC_M_KK2B,
-                                                BC_M_KNI,   BC_M_ALL};
-  static const int kSlot[BC_NSTATE_VIEW] = {-1,        kSlotNaP,   kSlotNaQ,   kSlotKdrP,  kSlotCalP,
-                                            kSlotCalQ, kSlotCatP,  kSlotCatQ,  kSlotHcnP,  kSlotAhpP,
-                                            kSlotCaHi, kSlotNaHHP, kSlotNaHHQ, kSlotKHHP,  kSlotKMN,
-                                            kSlotKA1P, kSlotKA1Q,  kSlotKA2P,  kSlotKA2Q,
-                                            kSlotKK2AP, kSlotKK2AQ, kSlotKK2BP, kSlotKK2BQ,
-                                            kSlotKNIP,  kSlotVLastHi};
-  if (which != BC_STATE_V_LAST && !(p->cv_mech[k] & kBit[which])) return;
-  *hi = kStateTag + (d.state_offset + int64_t(kSlot[which]) * d.n_nodes + j) * rs;
+  uint32_t bit = 0;
+  int slot = -1;
+  state_view(which, &bit, &slot);
+  if (which != BC_STATE_V_LAST && !(p->cv_mech[k] & bit)) return;
+  *hi = kStateTag + (d.state_offset + int64_t(slot) * d.n_nodes + j) * rs;
   if (which == BC_STATE_CA_CI) *lo = kStateTag + (d.state_offset + int64_t(kSlotCaLo) * d.n_nodes + j) * rs;
   if (which == BC_STATE_V_LAST) *lo = kStateTag + (d.state_offset + int64_t(kSlotVLastLo) * d.n_nodes + j) * rs;
 }

@@ -58,10 +58,16 @@ typedef int32_t bc_status;
 #define BC_M_KK2A (1u << 14)     /* channel/potassium.py:765  KK2A_HM1992 p q, E_K             */
 #define BC_M_KK2B (1u << 15)     /* channel/potassium.py:899  KK2B_HM1992 p q, E_K             */
 #define BC_M_KNI (1u << 16)      /* channel/potassium.py:1045 KNI_Ya1989  p, E_K               */
-#define BC_M_ALL 0x1FFFFu
+/* Markov channels (channel/_base.py:677-1125), each advanced by one linearised
+ * backward-Euler step (quad/_backward_euler.py:31-64) at the new V and Ci, after
+ * the gates, as the reference's independent-integration family is. */
+#define BC_M_NAV16 (1u << 17)    /* channel/sodium.py:727     Nav1p6_MA2020_GoC 13 states, g O, E_Na    */
+#define BC_M_KCA22 (1u << 18)    /* channel/potassium_calcium.py:613 Kca2p2_MA2020_GoC 6 states, E_K */
+#define BC_M_KCA11 (1u << 19)    /* channel/potassium_calcium.py:1107 Kca1p1_MA2020_GoC 10 states, E_K */
+#define BC_M_ALL 0xFFFFFu
 
 /* Per-region parameter record (double[BC_NPARAM]); index names below. */
-#define BC_NPARAM 64
+#define BC_NPARAM 74
 #define BC_P_INVCM 0      /* 1 / membrane capacitance, cm^2/uF                 */
 #define BC_P_VREST 1      /* voltage used by reset (mV)                        */
 #define BC_P_ENA 2        /* fixed reversal potentials (mV)                    */
@@ -126,6 +132,16 @@ typedef int32_t bc_status;
 #define BC_P_KNI_VSH 61
 #define BC_P_KNI_PHI 62
 #define BC_P_KNI_TAUMAX 63  /* ms */
+#define BC_P_NAV16_G 64
+#define BC_P_NAV16_PHI 65   /* 3^((T - 22 degC) / 10)                               */
+#define BC_P_KCA22_G 66
+#define BC_P_KCA22_PHI 67   /* q10^((T - 23 degC) / 10)                             */
+#define BC_P_KCA22_DIFF 68  /* divisor of the calcium-binding rates                 */
+#define BC_P_KCA11_G 69
+#define BC_P_KCA11_PHI 70   /* q10^((T - 23 degC) / 10)                             */
+#define BC_P_KCA11_QO 71    /* Qo F / (R T) per mV: alpha(V) = exp(QO V)            */
+#define BC_P_KCA11_QC 72    /* Qc F / (R T) per mV: beta(V) = exp(QC V)             */
+/* 73: reserved (0) */
 
 /* ------------------------------------------------------------------ batch spec */
 /*
@@ -282,8 +298,10 @@ const char* bc_last_error(void);
 /* ABI version: major * 10000 + minor * 100 + patch.  0.2.0: the 64-entry parameter
  * record, the A / K2 / KNI mechanisms, named plan-info fields.  0.3.0: the V_last
  * state view (BC_NSTATE_VIEW 25), bc_spike_state_download, bc_pulse_set_amp, the
- * workspace of bc_gru_backward (bit-reproducible gradients). */
-#define BC_ABI_VERSION 300
+ * workspace of bc_gru_backward (bit-reproducible gradients).  0.4.0: the Markov
+ * channels (BC_M_NAV16 / KCA22 / KCA11, a 74-entry parameter record, state views
+ * 25-50, BC_PROBE_CURRENT 64), lane tiles (bc_plan_options.lane_cell_nodes). */
+#define BC_ABI_VERSION 400
 int32_t bc_version(void);
 /* Fill opts with defaults. */
 void bc_default_options(bc_plan_options* opts);
@@ -362,11 +380,17 @@ bc_status bc_check(bc_plan_t plan, void* stream);
 #define BC_STATE_KNI_P 23
 #define BC_STATE_V_LAST 24 /* V at the start of the last step taken (= V after a reset);
                               not a probe field                                    */
-#define BC_NSTATE_VIEW 25
+/* Markov states: the independent states of each scheme, in the order they first
+   appear in its transition list (the dependent state is 1 - their sum).         */
+#define BC_STATE_NAV16_C1 25 /* .. C5 29, I1 30 .. I5 34, O 35, B 36 (I6 dependent) */
+#define BC_STATE_NAV16_O 35
+#define BC_STATE_KCA22_C2 37 /* C3 38, C4 39, O1 40, O2 41 (C1 dependent)           */
+#define BC_STATE_KCA11_C1 42 /* C2 43, C3 44, C4 45, O0 46 .. O4 50 (C0 dependent) */
+#define BC_NSTATE_VIEW 51
 /* Current probes (mech/_point.py CurrentProbe, _multi_compartment/probes.py:184-258):
    probe_field = BC_PROBE_CURRENT + one of the codes below records that current
    density (uA/cm^2, outward negative as g (E - V)) after the step.             */
-#define BC_PROBE_CURRENT 32
+#define BC_PROBE_CURRENT 64
 #define BC_CUR_IL 0
 #define BC_CUR_KLEAK 1
 #define BC_CUR_NA 2      /* Na_Ba2002   */
@@ -386,7 +410,10 @@ bc_status bc_check(bc_plan_t plan, void* stream);
 #define BC_CUR_KK2A 16   /* KK2A_HM1992 */
 #define BC_CUR_KK2B 17   /* KK2B_HM1992 */
 #define BC_CUR_KNI 18    /* KNI_Ya1989  */
-#define BC_NCUR 19
+#define BC_CUR_NAV16 19  /* Nav1p6_MA2020_GoC */
+#define BC_CUR_KCA22 20  /* Kca2p2_MA2020_GoC */
+#define BC_CUR_KCA11 21  /* Kca1p1_MA2020_GoC */
+#define BC_NCUR 22
 bc_status bc_state_download(bc_plan_t plan, int32_t which, double* out /* [n_cv] */, void* stream);
 /* Set the amplitude (nA) of every current-clamp pulse of the batch spec, in spec
  * order (amp_nA[n_pulses]); times and locations are unchanged.  Takes effect from

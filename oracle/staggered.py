@@ -48,6 +48,8 @@ from dataclasses import dataclass
 
 import numpy as np
 
+from oracle import markov as MK
+
 __all__ = [
     "OracleCell",
     "Frustum",
@@ -111,6 +113,8 @@ CHANNEL_DEFAULTS = {
     "KNI_Ya1989": dict(g_max=0.004, temp=_c2k(36.0), q10=1.0, temp_ref=_c2k(36.0), tau_max=4e3,
                        V_sh=0.0),  # potassium.py:1140-1145
 }
+# Markov channels (channel/_base.py:677-1125): restated in oracle/markov.py
+CHANNEL_DEFAULTS.update({k: dict(v) for k, v in MK.MARKOV_DEFAULTS.items()})
 ION_DEFAULTS = {
     "SodiumFixed": dict(E=50.0),
     "PotassiumFixed": dict(E=-95.0),
@@ -450,7 +454,7 @@ _ION_OF = {"Na_Ba2002": "na", "KDR_Ba2002": "k", "CaL_IS2008": "ca", "CaT_HM1992
            "K_Leak": "k", "AHP_De1994": "k", "Na_HH1952": "na", "K_HH1952": "k", "KM_RI2021_SC": "k",
            "Na_TM1991": "na", "K_TM1991": "k", "CaHT_HM1992": "ca", "KA1_HM1992": "k", "KA2_HM1992": "k",
            "KM_MA2020_GoC": "k", "KM_MA2020_GrC": "k", "KK2A_HM1992": "k", "KK2B_HM1992": "k",
-           "KNI_Ya1989": "k"}
+           "KNI_Ya1989": "k", "Nav1p6_MA2020_GoC": "na", "Kca2p2_MA2020_GoC": "k", "Kca1p1_MA2020_GoC": "k"}
 
 
 def _resolve(table: dict, decl) -> dict:
@@ -470,6 +474,8 @@ def _resolve(table: dict, decl) -> dict:
                   "KK2B_HM1992"):
         p["phi_p"] = p["q10_p"] ** ((p["temp"] - p["temp_ref_p"]) / 10.0)
         p["phi_q"] = p["q10_q"] ** ((p["temp"] - p["temp_ref_q"]) / 10.0)
+    elif name in MK.SCHEMES:
+        p = MK.scheme_params(name, p)
     return p
 
 
@@ -891,6 +897,15 @@ class OracleCell:
             for gate, _power, _phik in _GATES[name]:
                 kind, a, b = r[gate]
                 self.gates[(name, gate)] = (a / (a + b) if kind == "ab" else a) * np.ones((P, n))
+        # Markov channels start at their stationary distribution at V_init
+        # (Nav1p6 / Kca2p2 / Kca1p1 reset_state -> Markov.reset_steady_state)
+        for name, ch in self.chan.items():
+            if name not in MK.SCHEMES:
+                continue
+            sch = MK.SCHEMES[name]
+            ss = MK.steady_state(sch, sch.rates(pv, self._ci_for_channels(), ch))
+            for st in sch.independent:
+                self.gates[(name, st)] = ss[st] * np.ones((P, n))
         self.spike = np.zeros((P, self.n_cv))
         self.syn_g = np.zeros((P, len(self.syn_points)))  # uS
         self.syn_pending = np.zeros((P, len(self.syn_points)))
@@ -923,6 +938,9 @@ class OracleCell:
         return np.where(cd["mask"], nernst, self.E_ca_fixed)
 
     def _gate_product(self, name):
+        if name in MK.SCHEMES:  # the open occupancy of the raw stored states
+            sch = MK.SCHEMES[name]
+            return MK.open_fraction(sch, {st: self.gates[(name, st)] for st in sch.independent})
         prod = 1.0
         for gate, power, _ in _GATES[name]:
             x = self.gates[(name, gate)]
@@ -1083,6 +1101,16 @@ class OracleCell:
                 kind, a, b = r[gate]
                 new_gates[(name, gate)] = gate_step(self.gates[(name, gate)], kind, a, b, ch[phik], dt)
         self.gates.update(new_gates)
+        # a11 (d): independent channels through their own solver (cell.py:2204-2217):
+        # Markov states by one backward-Euler step at the new voltage and Ci
+        for name, ch in self.chan.items():
+            if name not in MK.SCHEMES:
+                continue
+            sch = MK.SCHEMES[name]
+            y = MK.backward_euler(sch, {st: self.gates[(name, st)] for st in sch.independent},
+                                  sch.rates(pv_new, Ci_now, ch), dt)
+            for st in sch.independent:
+                self.gates[(name, st)] = y[st]
         # a16: spike = last_V < V_th <= V
         spk = ((V_new - self.V_th) >= 0.0) & ((self.V_th - last_V) > 0.0)
         self.spike = spk.astype(np.float64)
