@@ -695,7 +695,7 @@ def run_ours(a):
         # 1,000-cell capture) sets the node-steps/s that rate allows
         n_sm = torch.cuda.get_device_properties(local).multi_processor_count
         issue = 4.0 * n_sm * clk["sm_mhz"] * 1e6
-        bound = issue / prof["warp_inst_per_node_step"] * 32.0 * n_cv / info["n_nodes"] * world
+        bound = issue / prof["warp_inst_per_node_step"] * n_cv / info["n_nodes"] * world
         sm_bound = {"bound": "sm_issue", "value": bound, "unit": UNIT, "frac": value / bound,
                     "warp_inst_per_node_step": prof["warp_inst_per_node_step"], "sms": n_sm,
                     "sm_mhz": clk["sm_mhz"]}

@@ -60,7 +60,8 @@ def _hh_batch():
     c.paint(branch_in("type", "soma"), Channel("Na_HH1952"), Channel("K_HH1952", g_max=36.0))
     c.paint(branch_in("type", "basal_dendrite"), Channel("KM_RI2021_SC"), Channel("KA1_HM1992", g_max=3.0),
             Channel("KA2_HM1992", g_max=2.0), Channel("KK2A_HM1992", g_max=1.0), Channel("KK2B_HM1992", g_max=1.0),
-            Channel("KNI_Ya1989"))
+            Channel("KNI_Ya1989"), Channel("Nav1p6_MA2020_GoC", g_max=2.0), Channel("Kca2p2_MA2020_GoC", g_max=1.0),
+            Channel("Kca1p1_MA2020_GoC", g_max=1.0))  # and the Markov channels' state views
     return lower_cell(c)
 
 
