@@ -72,6 +72,7 @@ def _args():
     ap.add_argument("--no-surrogate", action="store_true")
     ap.add_argument("--surrogate-threads", type=int, default=384)
     ap.add_argument("--surrogate-tile-nodes", type=int, default=1800)
+    ap.add_argument("--surrogate-lane-nodes", type=int, default=6)
     ap.add_argument("--accuracy-cells", type=int, default=1000)
     ap.add_argument("--mixed-cells", type=int, default=10000)
     ap.add_argument("--mixed-steps", type=int, default=20000)
@@ -456,7 +457,8 @@ def surrogate_leg(a, descs, local, sid, stream, plain_ms):
     model = S.load_model(os.path.join(ROOT, "braincell_gb300", "data", "surrogate_uneven.npz"))
     T = a.surrogate_threads
     kw = dict(tile_nodes=a.surrogate_tile_nodes, threads_per_tile=T, threads_big=T, threads_global=T,
-              steps_per_launch=a.steps_per_launch, lane_nodes=a.lane_nodes, narrow_lane_nodes=a.narrow_lane_nodes)
+              steps_per_launch=a.steps_per_launch, lane_nodes=a.surrogate_lane_nodes,
+              narrow_lane_nodes=a.narrow_lane_nodes)
     t0 = time.perf_counter()
     runner = S.SurrogateRunner(descs, model, precision="f32", device=local, plan_kw=kw)
     t_setup = time.perf_counter() - t0
@@ -556,7 +558,8 @@ def mixed_leg(a, local, model, record_every=4):
     # mixed surrogate form
     T = a.surrogate_threads
     kw = dict(tile_nodes=a.surrogate_tile_nodes, threads_per_tile=T, threads_big=T, threads_global=T,
-              steps_per_launch=a.steps_per_launch, lane_nodes=a.lane_nodes, narrow_lane_nodes=a.narrow_lane_nodes)
+              steps_per_launch=a.steps_per_launch, lane_nodes=a.surrogate_lane_nodes,
+              narrow_lane_nodes=a.narrow_lane_nodes)
     runner = S.SurrogateRunner(descs, model, precision="f32", device=local, plan_kw=kw, full_cells=full)
     runner.run(2 * a.steps_per_launch, DT)
     runs = [runner.run(steps, DT) for _ in range(3)]

@@ -48,6 +48,9 @@ V_SCALE = 10.0       # mV
 # nodes each; 384 threads is the port kernel's register budget at two per SM.
 PORT_TILE_NODES = 1800
 PORT_THREADS = 384
+# Serial-walk length of the reduced tiles' warp slots: a GB300 sweep of the 10,000-cell
+# reduced run (1,000-step launches) gave 76.4 / 74.4 / 75.4 ms per 1,000 steps at 4 / 6 / 10.
+PORT_LANE_NODES = 6
 # Fallback (full-morphology) plans run the kernel without ports in large tiles.
 FALLBACK_TILE_NODES = 2500
 S_SCALE = 0.1        # nA: stimulus input scale (the step kernel's constant)
@@ -437,6 +440,7 @@ class SurrogateRunner:
         self.precision, self.record_every, self.device = precision, int(record_every), int(device)
         self.plan_kw = dict(plan_kw or {})
         self.plan_kw.setdefault("tile_nodes", PORT_TILE_NODES)
+        self.plan_kw.setdefault("lane_nodes", PORT_LANE_NODES)
         for k in ("threads_per_tile", "threads_big", "threads_global"):
             self.plan_kw.setdefault(k, PORT_THREADS)
         self.fallback = fallback and model is not None
