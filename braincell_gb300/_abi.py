@@ -42,9 +42,15 @@ BC_M_KNI = 1 << 16
 BC_M_NAV16 = 1 << 17
 BC_M_KCA22 = 1 << 18
 BC_M_KCA11 = 1 << 19
-BC_M_ALL = 0xFFFFF
+BC_M_KV34 = 1 << 20
+BC_M_KV43 = 1 << 21
+BC_M_KV11 = 1 << 22
+BC_M_KIR23 = 1 << 23
+BC_M_HCN1F = 1 << 24
+BC_M_HCN1H = 1 << 25
+BC_M_ALL = 0x3FFFFFF
 
-BC_NPARAM = 74
+BC_NPARAM = 90
 BC_P_INVCM = 0
 BC_P_VREST = 1
 BC_P_ENA = 2
@@ -118,6 +124,20 @@ BC_P_KCA11_G = 69
 BC_P_KCA11_PHI = 70
 BC_P_KCA11_QO = 71
 BC_P_KCA11_QC = 72
+BC_P_KV34_G = 74
+BC_P_KV34_PHI = 75
+BC_P_KV43_G = 76
+BC_P_KV43_PHI = 77
+BC_P_KV11_G = 78
+BC_P_KV11_PHI = 79
+BC_P_KIR23_G = 80
+BC_P_KIR23_PHI = 81
+BC_P_HCN1F_G = 82
+BC_P_HCN1F_E = 83
+BC_P_HCN1F_PHI = 84
+BC_P_HCN1H_G = 85
+BC_P_HCN1H_E = 86
+BC_P_HCN1H_PHI = 87
 
 BC_ABI_VERSION = 400
 
@@ -156,7 +176,13 @@ BC_CUR_KNI = 18
 BC_CUR_NAV16 = 19
 BC_CUR_KCA22 = 20
 BC_CUR_KCA11 = 21
-BC_NCUR = 22
+BC_CUR_KV34 = 22
+BC_CUR_KV43 = 23
+BC_CUR_KV11 = 24
+BC_CUR_KIR23 = 25
+BC_CUR_HCN1F = 26
+BC_CUR_HCN1H = 27
+BC_NCUR = 28
 
 BC_STATE_V = 0
 BC_STATE_NA_P = 1
@@ -187,7 +213,16 @@ BC_STATE_NAV16_C1 = 25
 BC_STATE_NAV16_O = 35
 BC_STATE_KCA22_C2 = 37
 BC_STATE_KCA11_C1 = 42
-BC_NSTATE_VIEW = 51
+BC_STATE_KV34_M = 51
+BC_STATE_KV34_H = 52
+BC_STATE_KV43_A = 53
+BC_STATE_KV43_B = 54
+BC_STATE_KV11_N = 55
+BC_STATE_KIR23_D = 56
+BC_STATE_HCN1F_FAST = 57
+BC_STATE_HCN1F_SLOW = 58
+BC_STATE_HCN1H_H = 59
+BC_NSTATE_VIEW = 60
 # the independent states of each Markov scheme, in view order (first appearance in
 # the scheme's transition list, the dependent state left out)
 MARKOV_STATES = {
@@ -223,6 +258,15 @@ STATE_NAMES = {
     "KK2B_q": BC_STATE_KK2B_Q,
     "KNI_p": BC_STATE_KNI_P,
     "V_last": BC_STATE_V_LAST,
+    "Kv3p4_m": BC_STATE_KV34_M,
+    "Kv3p4_h": BC_STATE_KV34_H,
+    "Kv4p3_a": BC_STATE_KV43_A,
+    "Kv4p3_b": BC_STATE_KV43_B,
+    "Kv1p1_n": BC_STATE_KV11_N,
+    "Kir2p3_d": BC_STATE_KIR23_D,
+    "HCN1_o_fast": BC_STATE_HCN1F_FAST,
+    "HCN1_o_slow": BC_STATE_HCN1F_SLOW,
+    "HCN1_h": BC_STATE_HCN1H_H,
 }
 for _cls, (_base, _names) in MARKOV_STATES.items():
     for _k, _n in enumerate(_names):
@@ -305,7 +349,7 @@ class PlanOptions(C.Structure):
         ("reserved_b", C.c_float),
         ("dry_run", C.c_int32),
         ("lane_cell_nodes", C.c_int32),
-        ("reserved", C.c_int32 * 1),
+        ("tile_order", C.c_int32),
     ]
 
 

@@ -342,6 +342,13 @@ PROBE_STATES = {
     ("KK2B_HM1992", "p"): _abi.BC_STATE_KK2B_P, ("KK2B_HM1992", "q"): _abi.BC_STATE_KK2B_Q,
     ("KNI_Ya1989", "p"): _abi.BC_STATE_KNI_P,
 }
+PROBE_STATES.update({
+    ("Kv3p4_MA2020_GoC", "m"): _abi.BC_STATE_KV34_M, ("Kv3p4_MA2020_GoC", "h"): _abi.BC_STATE_KV34_H,
+    ("Kv4p3_MA2020_GoC", "a"): _abi.BC_STATE_KV43_A, ("Kv4p3_MA2020_GoC", "b"): _abi.BC_STATE_KV43_B,
+    ("Kv1p1_MA2020_GoC", "n"): _abi.BC_STATE_KV11_N, ("Kir2p3_MA2020_GrC", "d"): _abi.BC_STATE_KIR23_D,
+    ("HCN1_MA2020_GoC", "o_fast"): _abi.BC_STATE_HCN1F_FAST, ("HCN1_MA2020_GoC", "o_slow"): _abi.BC_STATE_HCN1F_SLOW,
+    ("HCN1_MA2024_PC", "h"): _abi.BC_STATE_HCN1H_H,
+})
 for _cls, (_base, _names) in _abi.MARKOV_STATES.items():
     for _k, _n in enumerate(_names):
         PROBE_STATES[(_cls, _n)] = _base + _k
@@ -356,6 +363,8 @@ PROBE_CURRENTS = {
     "KK2A_HM1992": _abi.BC_CUR_KK2A, "KK2B_HM1992": _abi.BC_CUR_KK2B, "KNI_Ya1989": _abi.BC_CUR_KNI,
     "Nav1p6_MA2020_GoC": _abi.BC_CUR_NAV16, "Kca2p2_MA2020_GoC": _abi.BC_CUR_KCA22,
     "Kca1p1_MA2020_GoC": _abi.BC_CUR_KCA11,
+    "Kv3p4_MA2020_GoC": _abi.BC_CUR_KV34, "Kv4p3_MA2020_GoC": _abi.BC_CUR_KV43, "Kv1p1_MA2020_GoC": _abi.BC_CUR_KV11,
+    "Kir2p3_MA2020_GrC": _abi.BC_CUR_KIR23, "HCN1_MA2020_GoC": _abi.BC_CUR_HCN1F, "HCN1_MA2024_PC": _abi.BC_CUR_HCN1H,
 }
 ION_CURRENTS = {"na": _abi.BC_CUR_ION_NA, "k": _abi.BC_CUR_ION_K, "ca": _abi.BC_CUR_ION_CA}
 

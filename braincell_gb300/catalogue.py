@@ -26,6 +26,15 @@ Every class name, parameter name and default below is the reference's:
   phi = q10_base^((T - 23 degC) / 10))
 * ``Kca1p1_MA2020_GoC`` -- channel/potassium_calcium.py:1107 (Markov; g_max 10, q10_base 3, temp 22 degC, phi as
   Kca2p2; alpha(V) = exp(0.73 F V / R T), beta(V) = exp(-0.67 F V / R T))
+* ``Kv3p4_MA2020_GoC`` -- channel/potassium.py:4750 (g_max 4, temp 22 degC; gates q10 3 at 37 degC)
+* ``Kv4p3_MA2020_GoC`` -- channel/potassium.py:4964 (g_max 3.2, temp 22 degC; gates q10 3 at 25.5 degC; the GrC / PC /
+  BC / SC variants default to 30 degC)
+* ``Kv1p1_MA2020_GoC`` -- channel/potassium.py:4570 (g_max 4, temp 22 degC, gateCurrent 0; gate q10 2.7 at 22 degC)
+* ``Kir2p3_MA2020_GrC`` -- channel/potassium.py:5334 (g_max 0.9, temp 30 degC; gate q10 3 at 20 degC)
+* ``HCN1_MA2020_GoC`` -- channel/hyperpolarization_activated.py:675 (g_max 0.05, E -20 mV, temp 22 degC; gates q10 3
+  and g Q10 1.5, both at 23 degC)
+* ``HCN1_MA2024_PC`` -- channel/hyperpolarization_activated.py:411 (g_max 0.1, E -34.4 mV, temp 23 degC; gate q10 3
+  at 37 degC)
 
 Same-form classes: Na_TM1991 has Na_Ba2002's Traub-Miles rate functions written
 in terms of V_sh - V (sodium.py:275-289 against :154-170), K_TM1991 has
@@ -61,6 +70,7 @@ T36 = celsius2kelvin(36.0)
 T24 = celsius2kelvin(24.0)
 T22 = celsius2kelvin(22.0)
 T30 = celsius2kelvin(30.0)
+T37 = celsius2kelvin(37.0)
 FARADAY = 96485.33212  # C/mol
 GAS_R = 8.314462618  # J/(mol K)
 
@@ -103,6 +113,21 @@ CHANNELS: dict[str, dict[str, float]] = {
     "Nav1p6_MA2020_GoC": {"g_max": 16.0, "temp": T22},
     "Kca2p2_MA2020_GoC": {"g_max": 38.0, "q10_base": 3.0, "diff": 3.0, "temp": T22},
     "Kca1p1_MA2020_GoC": {"g_max": 10.0, "q10_base": 3.0, "temp": T22},
+    "Kv3p4_MA2020_GoC": {"g_max": 4.0, "temp": T22},
+    "Kv4p3_MA2020_GoC": {"g_max": 3.2, "temp": T22},
+    "Kv1p1_MA2020_GoC": {"g_max": 4.0, "temp": T22, "gateCurrent": 0.0},
+    "Kir2p3_MA2020_GrC": {"g_max": 0.9, "temp": T30},
+    "HCN1_MA2020_GoC": {"g_max": 0.05, "E": -20.0, "temp": T22},
+    "HCN1_MA2024_PC": {"g_max": 0.1, "E": -34.4, "temp": celsius2kelvin(23.0)},
+}
+# cell-type variants with their base class's kinetics; own defaults where they differ
+KINETIC_VARIANTS = {
+    "Kv3p4_MA2020_GoC": {v: {} for v in ("Kv3p4_MA2020_GrC", "Kv3p4_MA2024_PC", "Kv3p4_MA2025_BC", "Kv3p4_RI2021_SC")},
+    "Kv4p3_MA2020_GoC": {v: {"temp": T30} for v in ("Kv4p3_MA2020_GrC", "Kv4p3_MA2024_PC", "Kv4p3_MA2025_BC",
+                                                      "Kv4p3_RI2021_SC")},
+    "Kv1p1_MA2020_GoC": {v: {} for v in ("Kv1p1_MA2020_GrC", "Kv1p1_MA2024_PC", "Kv1p1_MA2025_BC", "Kv1p1_RI2021_SC")},
+    "Kir2p3_MA2020_GrC": {v: {} for v in ("Kir2p3_MA2024_PC", "Kir2p3_MA2025_BC", "Kir2p3_RI2021_SC")},
+    "HCN1_MA2024_PC": {v: {} for v in ("HCN1_MA2025_BC", "HCN1_RI2021_SC")},
 }
 MARKOV_VARIANTS = {
     "Nav1p6_MA2020_GoC": ("Nav1p6_MA2024_PC", "Nav1p6_MA2025_BC", "Nav1p6_RI2021_SC"),
@@ -115,6 +140,10 @@ SAME_FORM = {"Na_TM1991": "Na_Ba2002", "K_TM1991": "KDR_Ba2002", "CaHT_HM1992": 
 for _base, _variants in MARKOV_VARIANTS.items():
     for _v in _variants:
         CHANNELS[_v] = dict(CHANNELS[_base])
+        SAME_FORM[_v] = _base
+for _base, _variants in KINETIC_VARIANTS.items():
+    for _v, _own in _variants.items():
+        CHANNELS[_v] = {**CHANNELS[_base], **_own}
         SAME_FORM[_v] = _base
 # gate temperature factors fixed by a class (not constructor parameters)
 KM_Q10, KM_TEMP_REF = 3.0, T22
@@ -267,6 +296,33 @@ def region_record(mechs, cable: CableProperty) -> tuple[int, np.ndarray]:
             rec[_abi.BC_P_KCA11_PHI] = q10_phi(p["q10_base"], p["temp"], celsius2kelvin(23.0))
             rec[_abi.BC_P_KCA11_QO] = 0.73 * FARADAY * 1e-3 / (GAS_R * p["temp"])
             rec[_abi.BC_P_KCA11_QC] = -0.67 * FARADAY * 1e-3 / (GAS_R * p["temp"])
+        elif name == "Kv3p4_MA2020_GoC":
+            bits |= _abi.BC_M_KV34
+            rec[_abi.BC_P_KV34_G] = p["g_max"]
+            rec[_abi.BC_P_KV34_PHI] = q10_phi(3.0, p["temp"], T37)
+        elif name == "Kv4p3_MA2020_GoC":
+            bits |= _abi.BC_M_KV43
+            rec[_abi.BC_P_KV43_G] = p["g_max"]
+            rec[_abi.BC_P_KV43_PHI] = q10_phi(3.0, p["temp"], celsius2kelvin(25.5))
+        elif name == "Kv1p1_MA2020_GoC":
+            if p["gateCurrent"] != 0.0:
+                raise ValueError(f"{decl.class_name}: the gating current (gateCurrent != 0) is not built.")
+            bits |= _abi.BC_M_KV11
+            rec[_abi.BC_P_KV11_G] = p["g_max"]
+            rec[_abi.BC_P_KV11_PHI] = q10_phi(2.7, p["temp"], T22)
+        elif name == "Kir2p3_MA2020_GrC":
+            bits |= _abi.BC_M_KIR23
+            rec[_abi.BC_P_KIR23_G] = p["g_max"]
+            rec[_abi.BC_P_KIR23_PHI] = q10_phi(3.0, p["temp"], celsius2kelvin(20.0))
+        elif name == "HCN1_MA2020_GoC":
+            bits |= _abi.BC_M_HCN1F
+            rec[_abi.BC_P_HCN1F_G] = p["g_max"] * q10_phi(1.5, p["temp"], celsius2kelvin(23.0))
+            rec[_abi.BC_P_HCN1F_E] = p["E"]
+            rec[_abi.BC_P_HCN1F_PHI] = q10_phi(3.0, p["temp"], celsius2kelvin(23.0))
+        elif name == "HCN1_MA2024_PC":
+            bits |= _abi.BC_M_HCN1H
+            rec[_abi.BC_P_HCN1H_G], rec[_abi.BC_P_HCN1H_E] = p["g_max"], p["E"]
+            rec[_abi.BC_P_HCN1H_PHI] = q10_phi(3.0, p["temp"], T37)
         elif name in _PQ_RECORDS:
             bit, base = _PQ_RECORDS[name]
             bits |= bit

@@ -305,6 +305,29 @@ __device__ __forceinline__ double probe_current(const Real* st, int N, const Rea
         for (int k = 4; k < 9; ++k) o += st[(kSlotKca11 + k) * N];
         return P[BC_P_KCA11_G] * o * (P[BC_P_EK] - v);
       }
+      case BC_CUR_KV34: {
+        if (!(m & BC_M_KV34)) return Real(0);
+        const Real a = st[kSlotKv34M * N];
+        return P[BC_P_KV34_G] * a * a * a * st[kSlotKv34H * N] * (P[BC_P_EK] - v);
+      }
+      case BC_CUR_KV43: {
+        if (!(m & BC_M_KV43)) return Real(0);
+        const Real a = st[kSlotKv43A * N];
+        return P[BC_P_KV43_G] * a * a * a * st[kSlotKv43B * N] * (P[BC_P_EK] - v);
+      }
+      case BC_CUR_KV11: {
+        if (!(m & BC_M_KV11)) return Real(0);
+        const Real n2 = st[kSlotKv11N * N] * st[kSlotKv11N * N];
+        return P[BC_P_KV11_G] * n2 * n2 * (P[BC_P_EK] - v);
+      }
+      case BC_CUR_KIR23:
+        return (m & BC_M_KIR23) ? P[BC_P_KIR23_G] * st[kSlotKir23D * N] * (P[BC_P_EK] - v) : Real(0);
+      case BC_CUR_HCN1F:
+        return (m & BC_M_HCN1F)
+                   ? P[BC_P_HCN1F_G] * (st[kSlotHcn1Fast * N] + st[kSlotHcn1Slow * N]) * (P[BC_P_HCN1F_E] - v)
+                   : Real(0);
+      case BC_CUR_HCN1H:
+        return (m & BC_M_HCN1H) ? P[BC_P_HCN1H_G] * st[kSlotHcn1H * N] * (P[BC_P_HCN1H_E] - v) : Real(0);
     }
     return Real(0);
   };
@@ -314,7 +337,8 @@ __device__ __forceinline__ double probe_current(const Real* st, int N, const Rea
     case BC_CUR_ION_K:
       return double(cur(BC_CUR_KDR)) + double(cur(BC_CUR_KLEAK)) + double(cur(BC_CUR_AHP)) + double(cur(BC_CUR_KHH)) +
              double(cur(BC_CUR_KM)) + double(cur(BC_CUR_KA1)) + double(cur(BC_CUR_KA2)) + double(cur(BC_CUR_KK2A)) +
-             double(cur(BC_CUR_KK2B)) + double(cur(BC_CUR_KNI)) + double(cur(BC_CUR_KCA22)) + double(cur(BC_CUR_KCA11));
+             double(cur(BC_CUR_KK2B)) + double(cur(BC_CUR_KNI)) + double(cur(BC_CUR_KCA22)) + double(cur(BC_CUR_KCA11)) +
+             double(cur(BC_CUR_KV34)) + double(cur(BC_CUR_KV43)) + double(cur(BC_CUR_KV11)) + double(cur(BC_CUR_KIR23));
     case BC_CUR_ION_CA:
       return double(cur(BC_CUR_CAL)) + double(cur(BC_CUR_CAT));
     default:
@@ -326,8 +350,9 @@ __device__ __forceinline__ double probe_current(const Real* st, int N, const Rea
 // M current, the A current, the slow K2 current, the slow non-inactivating K
 // current): kept out of line so that their registers do not weigh on the common
 // path; same exp-Euler steps and ohmic currents as the others.
+constexpr uint32_t kCerebellarChannels = BC_M_KV34 | BC_M_KV43 | BC_M_KV11 | BC_M_KIR23 | BC_M_HCN1F | BC_M_HCN1H;
 constexpr uint32_t kExtraChannels = BC_M_NAHH | BC_M_KHH | BC_M_KM | BC_M_KA1 | BC_M_KA2 | BC_M_KK2A | BC_M_KK2B |
-                                   BC_M_KNI | BC_M_NAV16 | BC_M_KCA22 | BC_M_KCA11;
+                                   BC_M_KNI | BC_M_NAV16 | BC_M_KCA22 | BC_M_KCA11 | kCerebellarChannels;
 
 __device__ __forceinline__ MarkovGraph nav16_graph() { return MarkovGraph{13, 17, 12, kSlotNav16, kNav16Src, kNav16Dst}; }
 __device__ __forceinline__ MarkovGraph kca22_graph() { return MarkovGraph{6, 5, 0, kSlotKca22, kKca22Src, kKca22Dst}; }
@@ -366,6 +391,86 @@ __device__ __forceinline__ void k2_current(Real* st, int N, const Real* P, int s
   const Real g = P[pg] * p * q;
   G += g;
   I += g * (P[BC_P_EK] - v);
+}
+
+// The cerebellar HH channels: exp-Euler gates at v, ohmic currents (HCN1 with its
+// own reversal potential; HCN1_MA2020_GoC's g carries its Q10 factor already).
+template <typename Real>
+__device__ __forceinline__ void cerebellar_channels(Real* st, int N, const Real* P, uint32_t m, Real v, Real dt,
+                                                    bool advance, Real& G, Real& I) {
+  if (m & BC_M_KV34) {
+    Real a = st[kSlotKv34M * N], b = st[kSlotKv34H * N];
+    if (advance) {
+      const Kv34Rates<Real> r(v);
+      a = gate_it(a, r.minf, r.mtau, P[BC_P_KV34_PHI], dt);
+      b = gate_it(b, r.hinf, r.htau, P[BC_P_KV34_PHI], dt);
+      st[kSlotKv34M * N] = a;
+      st[kSlotKv34H * N] = b;
+    }
+    const Real g = P[BC_P_KV34_G] * a * a * a * b;
+    G += g;
+    I += g * (P[BC_P_EK] - v);
+  }
+  if (m & BC_M_KV43) {
+    Real a = st[kSlotKv43A * N], b = st[kSlotKv43B * N];
+    if (advance) {
+      const Kv43Rates<Real> r(v);
+      a = gate_it(a, r.ainf, r.atau, P[BC_P_KV43_PHI], dt);
+      b = gate_it(b, r.binf, r.btau, P[BC_P_KV43_PHI], dt);
+      st[kSlotKv43A * N] = a;
+      st[kSlotKv43B * N] = b;
+    }
+    const Real g = P[BC_P_KV43_G] * a * a * a * b;
+    G += g;
+    I += g * (P[BC_P_EK] - v);
+  }
+  if (m & BC_M_KV11) {
+    Real n = st[kSlotKv11N * N];
+    if (advance) {
+      const Kv11Rates<Real> r(v);
+      n = gate_ab<Real, true>(n, r.a, r.b, P[BC_P_KV11_PHI], dt);
+      st[kSlotKv11N * N] = n;
+    }
+    const Real n2 = n * n;
+    const Real g = P[BC_P_KV11_G] * n2 * n2;
+    G += g;
+    I += g * (P[BC_P_EK] - v);
+  }
+  if (m & BC_M_KIR23) {
+    Real d = st[kSlotKir23D * N];
+    if (advance) {
+      const Kir23Rates<Real> r(v);
+      d = gate_ab<Real, true>(d, r.a, r.b, P[BC_P_KIR23_PHI], dt);
+      st[kSlotKir23D * N] = d;
+    }
+    const Real g = P[BC_P_KIR23_G] * d;
+    G += g;
+    I += g * (P[BC_P_EK] - v);
+  }
+  if (m & BC_M_HCN1F) {
+    Real f = st[kSlotHcn1Fast * N], sl = st[kSlotHcn1Slow * N];
+    if (advance) {
+      const Hcn1fRates<Real> r(v);
+      f = gate_it(f, r.finf, r.ftau, P[BC_P_HCN1F_PHI], dt);
+      sl = gate_it(sl, r.sinf, r.stau, P[BC_P_HCN1F_PHI], dt);
+      st[kSlotHcn1Fast * N] = f;
+      st[kSlotHcn1Slow * N] = sl;
+    }
+    const Real g = P[BC_P_HCN1F_G] * (f + sl);
+    G += g;
+    I += g * (P[BC_P_HCN1F_E] - v);
+  }
+  if (m & BC_M_HCN1H) {
+    Real h = st[kSlotHcn1H * N];
+    if (advance) {
+      const Hcn1hRates<Real> r(v);
+      h = gate_it(h, r.hinf, r.htau, P[BC_P_HCN1H_PHI], dt);
+      st[kSlotHcn1H * N] = h;
+    }
+    const Real g = P[BC_P_HCN1H_G] * h;
+    G += g;
+    I += g * (P[BC_P_HCN1H_E] - v);
+  }
 }
 
 template <typename Real>
@@ -426,6 +531,7 @@ __device__ __noinline__ void extra_channels(Real* st, int N, const Real* P, uint
     G += g;
     I += g * (P[BC_P_EK] - v);
   }
+  if (m & kCerebellarChannels) cerebellar_channels(st, N, P, m, v, dt, advance, G, I);
   // Markov channels: the reference's independent-integration family, advanced
   // after the gates (cell.py:2204-2217), each at the new V and Ci
   if (m & (BC_M_NAV16 | BC_M_KCA22 | BC_M_KCA11)) {
@@ -660,6 +766,30 @@ __device__ __forceinline__ void steady_states(const Real* P, uint32_t m, Real* s
     st[kSlotKK2BQ * N] = r.qinf;
   }
   if (m & BC_M_KNI) st[kSlotKNIP * N] = KNIRates<Real>(v, P[BC_P_KNI_VSH], P[BC_P_KNI_TAUMAX]).pinf;
+  if (m & BC_M_KV34) {
+    const Kv34Rates<Real> r(v);
+    st[kSlotKv34M * N] = r.minf;
+    st[kSlotKv34H * N] = r.hinf;
+  }
+  if (m & BC_M_KV43) {
+    const Kv43Rates<Real> r(v);
+    st[kSlotKv43A * N] = r.ainf;
+    st[kSlotKv43B * N] = r.binf;
+  }
+  if (m & BC_M_KV11) {
+    const Kv11Rates<Real> r(v);
+    st[kSlotKv11N * N] = r.a / (r.a + r.b);
+  }
+  if (m & BC_M_KIR23) {
+    const Kir23Rates<Real> r(v);
+    st[kSlotKir23D * N] = r.a / (r.a + r.b);
+  }
+  if (m & BC_M_HCN1F) {
+    const Hcn1fRates<Real> r(v);
+    st[kSlotHcn1Fast * N] = r.finf;
+    st[kSlotHcn1Slow * N] = r.sinf;
+  }
+  if (m & BC_M_HCN1H) st[kSlotHcn1H * N] = Hcn1hRates<Real>(v).hinf;
   if (m & (BC_M_NAV16 | BC_M_KCA22 | BC_M_KCA11)) {
     // Markov channels start at their stationary distribution (reset_steady_state)
     Real kf[17], kb[17];

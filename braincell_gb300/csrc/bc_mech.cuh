@@ -266,6 +266,90 @@ constexpr double kNernstCa = 1e3 * kGasR / (2.0 * kFaraday);
 // uA/cm^2 -> mM/ms influx per um of shell depth: 10 / (2 F)
 constexpr double kCaDrive = 10.0 / (2.0 * kFaraday);
 
+// ------------------------------------------------------- cerebellar HH channels
+// Kv3p4_MA2020_GoC (channel/potassium.py:4750): m^3 h on V' = V + 11 mV (the
+// junction potential), inf / tau forms in seconds scaled to ms.
+template <typename Real>
+struct Kv34Rates {
+  Real minf, mtau, hinf, htau;
+  __host__ __device__ __forceinline__ explicit Kv34Rates(Real v) {
+    const Real x = v + Real(11);
+    minf = Real(1) / (Real(1) + aexp(-(x + Real(24)) / Real(15.4)));
+    const Real mt = x < Real(-35) ? (Real(3.4225e-5) + Real(0.00498) * aexp(x / Real(28.29))) * Real(3)
+                                  : Real(0.00012851) + Real(1) / (aexp((x + Real(100.7)) / Real(12.9)) +
+                                                                  aexp((x - Real(56)) / Real(-23.1)));
+    mtau = Real(1000) * mt;
+    hinf = Real(0.31) + Real(0.69) / (Real(1) + aexp((x + Real(5.802)) / Real(11.2)));
+    const Real y = (x + Real(56.3)) / Real(49.6);
+    const Real ht = x > Real(0) ? Real(0.0012) + Real(0.0023) * aexp(Real(-0.141) * x)
+                                : Real(1.2202e-05) + Real(0.012) * aexp(-(y * y));
+    htau = Real(1000) * ht;
+  }
+};
+
+// Kv4p3_MA2020_GoC (channel/potassium.py:4964): a^3 b, inf sigmoids and
+// tau = 1 / (alpha + beta) with sigm(x, y) = 1 / (exp(x / y) + 1) (:73-74).
+template <typename Real>
+struct Kv43Rates {
+  Real ainf, atau, binf, btau;
+  __host__ __device__ __forceinline__ explicit Kv43Rates(Real v) {
+    const Real aa = Real(0.8147) / (aexp((v + Real(9.17203)) / Real(-23.3271)) + Real(1));
+    const Real ab = Real(0.1655) / aexp((v + Real(18.2791)) / Real(19.4718));
+    const Real ba = Real(0.0368) / (aexp((v + Real(111.332)) / Real(12.8433)) + Real(1));
+    const Real bb = Real(0.0345) / (aexp((v + Real(49.9537)) / Real(-8.90123)) + Real(1));
+    ainf = Real(1) / (Real(1) + aexp((v + Real(38)) / Real(-17)));
+    atau = Real(1) / (aa + ab);
+    binf = Real(1) / (Real(1) + aexp((v + Real(78.8)) / Real(8.4)));
+    btau = Real(1) / (ba + bb);
+  }
+};
+
+// Kv1p1_MA2020_GoC (channel/potassium.py:4570): n^4, alpha / beta form.
+template <typename Real>
+struct Kv11Rates {
+  Real a, b;
+  __host__ __device__ __forceinline__ explicit Kv11Rates(Real v) {
+    a = Real(0.12889) * aexp((v + Real(45)) / Real(33.90877));
+    b = Real(0.12889) * aexp(-(v + Real(45)) / Real(12.42101));
+  }
+};
+
+// Kir2p3_MA2020_GrC (channel/potassium.py:5334): d, alpha / beta form.
+template <typename Real>
+struct Kir23Rates {
+  Real a, b;
+  __host__ __device__ __forceinline__ explicit Kir23Rates(Real v) {
+    a = Real(0.13289) * aexp((v + Real(83.94)) / Real(-24.3902));
+    b = Real(0.16994) * aexp((v + Real(83.94)) / Real(35.714));
+  }
+};
+
+// HCN1_MA2020_GoC (channel/hyperpolarization_activated.py:675): two gates whose
+// steady states split o_inf by r(V) = 0.002096 V + 0.97596.
+template <typename Real>
+struct Hcn1fRates {
+  Real finf, ftau, sinf, stau;
+  __host__ __device__ __forceinline__ explicit Hcn1fRates(Real v) {
+    const Real o = Real(1) / (Real(1) + aexp((v + Real(72.49)) * Real(0.11305)));
+    const Real r = Real(0.002096) * v + Real(0.97596);
+    finf = r * o;
+    sinf = (Real(1) - r) * o;
+    ftau = aexp((Real(0.01371) * v + Real(3.368)) * Real(2.30259));
+    stau = aexp((Real(0.01451) * v + Real(4.056)) * Real(2.30259));
+  }
+};
+
+// HCN1_MA2024_PC (channel/hyperpolarization_activated.py:411): h, with the
+// half-activation voltages shifted by the 9.3 mV junction potential.
+template <typename Real>
+struct Hcn1hRates {
+  Real hinf, htau;
+  __host__ __device__ __forceinline__ explicit Hcn1hRates(Real v) {
+    hinf = Real(1) / (Real(1) + aexp((v + Real(99.6)) / Real(9.67)));
+    htau = Real(1) / (Real(0.0018) * (aexp((v + Real(77.3)) / Real(-22)) + aexp((v + Real(77.3)) / Real(7.14))));
+  }
+};
+
 // ---------------------------------------------------------------- Markov channels
 // The independent states of each scheme (channel/_base.py:677-1125: every state but
 // the dependent one, which is 1 - their sum), in the order they first appear in the
@@ -275,6 +359,18 @@ constexpr int kSlotNav16 = 26;  // Nav1p6_MA2020_GoC: C1..C5, I1..I5, O, B
 constexpr int kSlotKca22 = 38;  // Kca2p2_MA2020_GoC: C2, C3, C4, O1, O2
 constexpr int kSlotKca11 = 43;  // Kca1p1_MA2020_GoC: C1..C4, O0..O4
 constexpr int kNumSlotsMarkov = 52;
+// Cerebellar HH channels (after the Markov states; plans with one carry
+// kNumSlotsCerebellar slots per node)
+constexpr int kSlotKv34M = 52;
+constexpr int kSlotKv34H = 53;
+constexpr int kSlotKv43A = 54;
+constexpr int kSlotKv43B = 55;
+constexpr int kSlotKv11N = 56;
+constexpr int kSlotKir23D = 57;
+constexpr int kSlotHcn1Fast = 58;
+constexpr int kSlotHcn1Slow = 59;
+constexpr int kSlotHcn1H = 60;
+constexpr int kNumSlotsCerebellar = 61;
 constexpr int kMarkovMaxStates = 13;
 
 // A transition graph: states 0 .. ns-1 (dep is eliminated), pair k moves src -> dst

@@ -63,6 +63,7 @@ constexpr int kDefaultLaneNodes = 10;
 constexpr int kDefaultNarrowLaneNodes = 1;
 
 constexpr uint32_t kMarkovBits = BC_M_NAV16 | BC_M_KCA22 | BC_M_KCA11;
+constexpr uint32_t kCerebellarBits = BC_M_KV34 | BC_M_KV43 | BC_M_KV11 | BC_M_KIR23 | BC_M_HCN1F | BC_M_HCN1H;
 
 namespace bc {
 
@@ -82,8 +83,13 @@ static void state_view(int32_t which, uint32_t* bit, int* slot) {
     *slot = kSlot[which];
     return;
   }
-  // Markov views 25 .. 50 sit in slots 26 .. 51
-  *bit = which < BC_STATE_KCA22_C2 ? BC_M_NAV16 : (which < BC_STATE_KCA11_C1 ? BC_M_KCA22 : BC_M_KCA11);
+  // Markov views 25 .. 50 and the cerebellar gates 51 .. 59 sit in slots 26 .. 60
+  static const uint32_t kCereb[BC_NSTATE_VIEW - BC_STATE_KV34_M] = {
+      BC_M_KV34, BC_M_KV34, BC_M_KV43, BC_M_KV43, BC_M_KV11, BC_M_KIR23, BC_M_HCN1F, BC_M_HCN1F, BC_M_HCN1H};
+  if (which >= BC_STATE_KV34_M)
+    *bit = kCereb[which - BC_STATE_KV34_M];
+  else
+    *bit = which < BC_STATE_KCA22_C2 ? BC_M_NAV16 : (which < BC_STATE_KCA11_C1 ? BC_M_KCA22 : BC_M_KCA11);
   *slot = which + 1;
 }
 
@@ -1231,6 +1237,7 @@ bc_status bc_plan_create(const bc_batch_spec* spec, const bc_plan_options* opts_
   if (s.n_regions <= 0) return fail(BC_ERR_INVALID, "n_regions must be > 0");
   if (opts.precision != BC_PREC_F32 && opts.precision != BC_PREC_F64)
     return fail(BC_ERR_INVALID, "precision must be BC_PREC_F32 or BC_PREC_F64");
+  if (opts.tile_order < 0 || opts.tile_order > 1) return fail(BC_ERR_INVALID, "tile_order must be 0 or 1");
   if (opts.threads_per_tile < 0 || opts.threads_per_tile > 1024 || opts.threads_per_tile % 32)
     return fail(BC_ERR_INVALID, "threads_per_tile must be 0 or a multiple of 32 up to 1024");
   if (opts.record_every < 0 || opts.max_spikes < 0) return fail(BC_ERR_INVALID, "record_every/max_spikes must be >= 0");
@@ -1281,15 +1288,17 @@ bc_status bc_plan_create(const bc_batch_spec* spec, const bc_plan_options* opts_
   for (int64_t c = 0; c < s.n_cells; ++c) p->cell_ncv[c] = cells[c].n_cv;
   for (int64_t k = 0; k < s.n_cells * s.n_regions; ++k)
     p->extra = p->extra || (s.region_mech[k] & (BC_M_NAHH | BC_M_KHH | BC_M_KM | BC_M_KA1 | BC_M_KA2 | BC_M_KK2A |
-                                                 BC_M_KK2B | BC_M_KNI | kMarkovBits)) != 0;
+                                                 BC_M_KK2B | BC_M_KNI | kMarkovBits | kCerebellarBits)) != 0;
   for (int64_t k = 0; k < s.n_cells * s.n_regions; ++k)
     if (s.region_mech[k] & ~BC_M_ALL) {
       delete p;
       return fail(BC_ERR_INVALID, "unknown mechanism bits in region_mech");
     }
-  bool markov = false;
-  for (int64_t k = 0; k < s.n_cells * s.n_regions; ++k) markov = markov || (s.region_mech[k] & kMarkovBits) != 0;
-  const int S = markov ? kNumSlotsMarkov : kNumSlots;  // the Markov states only where a plan has them
+  uint32_t all_bits = 0;
+  for (int64_t k = 0; k < s.n_cells * s.n_regions; ++k) all_bits |= s.region_mech[k];
+  // the Markov and cerebellar states only where a plan has them
+  const int S = (all_bits & kCerebellarBits) ? kNumSlotsCerebellar
+                                             : ((all_bits & kMarkovBits) ? kNumSlotsMarkov : kNumSlots);
   p->state_slots = S;
   // ---------------------------------------------------- pulses / probes -> nodes
   std::vector<std::vector<int64_t>> cell_pulses(s.n_cells), cell_probes(s.n_cells);
@@ -1335,8 +1344,9 @@ bc_status bc_plan_create(const bc_batch_spec* spec, const bc_plan_options* opts_
           BC_M_IL,  BC_M_KLEAK, BC_M_NA,   BC_M_KDR, BC_M_CAL,           BC_M_CAT,
           BC_M_HCN, BC_M_AHP,   BC_M_NAHH, BC_M_KHH, BC_M_KM,            BC_M_NA | BC_M_NAHH | BC_M_NAV16,
           BC_M_KDR | BC_M_KLEAK | BC_M_AHP | BC_M_KHH | BC_M_KM | BC_M_KA1 | BC_M_KA2 | BC_M_KK2A | BC_M_KK2B | BC_M_KNI |
-              BC_M_KCA22 | BC_M_KCA11,
-          BC_M_CAL | BC_M_CAT,  BC_M_KA1,  BC_M_KA2, BC_M_KK2A, BC_M_KK2B, BC_M_KNI, BC_M_NAV16, BC_M_KCA22, BC_M_KCA11};
+              BC_M_KCA22 | BC_M_KCA11 | BC_M_KV34 | BC_M_KV43 | BC_M_KV11 | BC_M_KIR23,
+          BC_M_CAL | BC_M_CAT,  BC_M_KA1,  BC_M_KA2, BC_M_KK2A, BC_M_KK2B, BC_M_KNI, BC_M_NAV16, BC_M_KCA22, BC_M_KCA11,
+          BC_M_KV34, BC_M_KV43, BC_M_KV11, BC_M_KIR23, BC_M_HCN1F, BC_M_HCN1H};
       const int32_t rg = cells[c].region[v];
       if (rg < 0 || !(s.region_mech[c * s.n_regions + rg] & cur_owner[field - BC_PROBE_CURRENT])) {
         delete p;
@@ -1675,6 +1685,14 @@ bc_status bc_plan_create(const bc_batch_spec* spec, const bc_plan_options* opts_
         const size_t need = size_t(outs[t].desc.blob_bytes) + size_t(outs[t].desc.scratch_bytes);
         if (lcz.smem) lcz.smem_bytes = std::max(lcz.smem_bytes, need);
       }
+    if (opts.tile_order == 0) {
+      // longest estimated step first: the block scheduler hands out CTAs in index
+      // order, so the tiles left for the last, partly filled wave are the short ones
+      std::stable_sort(tord.begin() + lcz.first, tord.end(), [&](size_t x, size_t y) {
+        if (outs[x].crit != outs[y].crit) return outs[x].crit > outs[y].crit;
+        return outs[x].desc.n_real_nodes > outs[y].desc.n_real_nodes;
+      });
+    }
     lcz.count = int(tord.size()) - lcz.first;
     if (lcz.count > 0) p->classes.push_back(lcz);
   }

@@ -51,6 +51,7 @@ class Plan:
         threads_global: int = 0,
         dry_run: bool = False,
         lane_cell_nodes: int = 0,
+        tile_order: int = 0,
     ) -> None:
         if precision not in _PREC:
             raise ValueError(f"precision must be one of {sorted(_PREC)}, got {precision!r}.")
@@ -74,6 +75,7 @@ class Plan:
         opts.threads_global = int(threads_global)
         opts.dry_run = int(bool(dry_run))
         opts.lane_cell_nodes = int(lane_cell_nodes)
+        opts.tile_order = int(tile_order)
         spec, keep = batch.to_spec()
         handle = C.c_void_p()
         _abi.check(lib.bc_plan_create(C.byref(spec), C.byref(opts), C.byref(handle)))

@@ -64,10 +64,19 @@ typedef int32_t bc_status;
 #define BC_M_NAV16 (1u << 17)    /* channel/sodium.py:727     Nav1p6_MA2020_GoC 13 states, g O, E_Na    */
 #define BC_M_KCA22 (1u << 18)    /* channel/potassium_calcium.py:613 Kca2p2_MA2020_GoC 6 states, E_K */
 #define BC_M_KCA11 (1u << 19)    /* channel/potassium_calcium.py:1107 Kca1p1_MA2020_GoC 10 states, E_K */
-#define BC_M_ALL 0xFFFFFu
+/* Cerebellar HH channels of the MA2020 / MA2024 / MA2025 / RI2021 models (each kernel
+ * also serves the cell-type variants that share its kinetics). */
+#define BC_M_KV34 (1u << 20)     /* channel/potassium.py:4750 Kv3p4_MA2020_GoC  m^3 h, E_K (V + 11 mV) */
+#define BC_M_KV43 (1u << 21)     /* channel/potassium.py:4964 Kv4p3_MA2020_GoC  a^3 b, E_K          */
+#define BC_M_KV11 (1u << 22)     /* channel/potassium.py:4570 Kv1p1_MA2020_GoC  n^4, E_K            */
+#define BC_M_KIR23 (1u << 23)    /* channel/potassium.py:5334 Kir2p3_MA2020_GrC d, E_K              */
+#define BC_M_HCN1F (1u << 24)    /* channel/hyperpolarization_activated.py:675 HCN1_MA2020_GoC
+                                    o_fast + o_slow, own E, Q10 1.5 on g                             */
+#define BC_M_HCN1H (1u << 25)    /* channel/hyperpolarization_activated.py:411 HCN1_MA2024_PC h, own E */
+#define BC_M_ALL 0x3FFFFFFu
 
 /* Per-region parameter record (double[BC_NPARAM]); index names below. */
-#define BC_NPARAM 74
+#define BC_NPARAM 90
 #define BC_P_INVCM 0      /* 1 / membrane capacitance, cm^2/uF                 */
 #define BC_P_VREST 1      /* voltage used by reset (mV)                        */
 #define BC_P_ENA 2        /* fixed reversal potentials (mV)                    */
@@ -142,6 +151,21 @@ typedef int32_t bc_status;
 #define BC_P_KCA11_QO 71    /* Qo F / (R T) per mV: alpha(V) = exp(QO V)            */
 #define BC_P_KCA11_QC 72    /* Qc F / (R T) per mV: beta(V) = exp(QC V)             */
 /* 73: reserved (0) */
+#define BC_P_KV34_G 74
+#define BC_P_KV34_PHI 75    /* 3^((T - 37 degC) / 10)                               */
+#define BC_P_KV43_G 76
+#define BC_P_KV43_PHI 77    /* 3^((T - 25.5 degC) / 10)                             */
+#define BC_P_KV11_G 78
+#define BC_P_KV11_PHI 79    /* 2.7^((T - 22 degC) / 10)                             */
+#define BC_P_KIR23_G 80
+#define BC_P_KIR23_PHI 81   /* 3^((T - 20 degC) / 10)                               */
+#define BC_P_HCN1F_G 82     /* g_max x 1.5^((T - 23 degC) / 10)                     */
+#define BC_P_HCN1F_E 83
+#define BC_P_HCN1F_PHI 84   /* 3^((T - 23 degC) / 10)                               */
+#define BC_P_HCN1H_G 85
+#define BC_P_HCN1H_E 86
+#define BC_P_HCN1H_PHI 87   /* 3^((T - 37 degC) / 10)                               */
+/* 88, 89: reserved (0) */
 
 /* ------------------------------------------------------------------ batch spec */
 /*
@@ -263,7 +287,10 @@ typedef struct bc_plan_options {
                                (serial solve per cell, cells interleaved node by node in
                                global memory) instead of in packed tiles; plans without
                                synapses, connections, mechanism probes or ports; 0 = off */
-  int32_t reserved[1];
+  int32_t tile_order;       /* launch order of the tiles of a class: 0 = longest
+                               estimated step first (critical path, then nodes), so
+                               the last wave of CTAs is made of short tiles; 1 = the
+                               order the packer built them                         */
 } bc_plan_options;
 
 typedef struct bc_plan* bc_plan_t;
@@ -300,7 +327,9 @@ const char* bc_last_error(void);
  * state view (BC_NSTATE_VIEW 25), bc_spike_state_download, bc_pulse_set_amp, the
  * workspace of bc_gru_backward (bit-reproducible gradients).  0.4.0: the Markov
  * channels (BC_M_NAV16 / KCA22 / KCA11, a 74-entry parameter record, state views
- * 25-50, BC_PROBE_CURRENT 64), lane tiles (bc_plan_options.lane_cell_nodes). */
+ * 25-50, BC_PROBE_CURRENT 64), lane tiles (bc_plan_options.lane_cell_nodes,
+ * tile_order), the cerebellar HH channels (BC_M_KV34 .. HCN1H, a 90-entry parameter
+ * record, state views 51-59). */
 #define BC_ABI_VERSION 400
 int32_t bc_version(void);
 /* Fill opts with defaults. */
@@ -386,7 +415,16 @@ bc_status bc_check(bc_plan_t plan, void* stream);
 #define BC_STATE_NAV16_O 35
 #define BC_STATE_KCA22_C2 37 /* C3 38, C4 39, O1 40, O2 41 (C1 dependent)           */
 #define BC_STATE_KCA11_C1 42 /* C2 43, C3 44, C4 45, O0 46 .. O4 50 (C0 dependent) */
-#define BC_NSTATE_VIEW 51
+#define BC_STATE_KV34_M 51
+#define BC_STATE_KV34_H 52
+#define BC_STATE_KV43_A 53
+#define BC_STATE_KV43_B 54
+#define BC_STATE_KV11_N 55
+#define BC_STATE_KIR23_D 56
+#define BC_STATE_HCN1F_FAST 57
+#define BC_STATE_HCN1F_SLOW 58
+#define BC_STATE_HCN1H_H 59
+#define BC_NSTATE_VIEW 60
 /* Current probes (mech/_point.py CurrentProbe, _multi_compartment/probes.py:184-258):
    probe_field = BC_PROBE_CURRENT + one of the codes below records that current
    density (uA/cm^2, outward negative as g (E - V)) after the step.             */
@@ -413,7 +451,13 @@ bc_status bc_check(bc_plan_t plan, void* stream);
 #define BC_CUR_NAV16 19  /* Nav1p6_MA2020_GoC */
 #define BC_CUR_KCA22 20  /* Kca2p2_MA2020_GoC */
 #define BC_CUR_KCA11 21  /* Kca1p1_MA2020_GoC */
-#define BC_NCUR 22
+#define BC_CUR_KV34 22   /* Kv3p4_MA2020_GoC  */
+#define BC_CUR_KV43 23   /* Kv4p3_MA2020_GoC  */
+#define BC_CUR_KV11 24   /* Kv1p1_MA2020_GoC  */
+#define BC_CUR_KIR23 25  /* Kir2p3_MA2020_GrC */
+#define BC_CUR_HCN1F 26  /* HCN1_MA2020_GoC   */
+#define BC_CUR_HCN1H 27  /* HCN1_MA2024_PC    */
+#define BC_NCUR 28
 bc_status bc_state_download(bc_plan_t plan, int32_t which, double* out /* [n_cv] */, void* stream);
 /* Set the amplitude (nA) of every current-clamp pulse of the batch spec, in spec
  * order (amp_nA[n_pulses]); times and locations are unchanged.  Takes effect from

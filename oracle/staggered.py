@@ -113,6 +113,32 @@ CHANNEL_DEFAULTS = {
     "KNI_Ya1989": dict(g_max=0.004, temp=_c2k(36.0), q10=1.0, temp_ref=_c2k(36.0), tau_max=4e3,
                        V_sh=0.0),  # potassium.py:1140-1145
 }
+CHANNEL_DEFAULTS.update({
+    "Kv3p4_MA2020_GoC": dict(g_max=4.0, temp=_c2k(22.0)),  # potassium.py:4750 (__init__)
+    "Kv4p3_MA2020_GoC": dict(g_max=3.2, temp=_c2k(22.0)),  # potassium.py:4964
+    "Kv1p1_MA2020_GoC": dict(g_max=4.0, temp=_c2k(22.0), gateCurrent=0.0),  # potassium.py:4570
+    "Kir2p3_MA2020_GrC": dict(g_max=0.9, temp=_c2k(30.0)),  # potassium.py:5334
+    "HCN1_MA2020_GoC": dict(g_max=0.05, E=-20.0, temp=_c2k(22.0)),  # hyperpolarization_activated.py:675
+    "HCN1_MA2024_PC": dict(g_max=0.1, E=-34.4, temp=_c2k(23.0)),  # hyperpolarization_activated.py:411
+})
+# cell-type variants that run their base class's kinetics, with their own defaults
+# where they differ (each class body is the base's: potassium.py, hyperpolarization_activated.py)
+_VARIANTS = {
+    **{v: ("Kv3p4_MA2020_GoC", {}) for v in ("Kv3p4_MA2020_GrC", "Kv3p4_MA2024_PC", "Kv3p4_MA2025_BC",
+                                              "Kv3p4_RI2021_SC")},
+    **{v: ("Kv4p3_MA2020_GoC", {"temp": _c2k(30.0)}) for v in ("Kv4p3_MA2020_GrC", "Kv4p3_MA2024_PC",
+                                                                "Kv4p3_MA2025_BC", "Kv4p3_RI2021_SC")},
+    **{v: ("Kv1p1_MA2020_GoC", {}) for v in ("Kv1p1_MA2020_GrC", "Kv1p1_MA2024_PC", "Kv1p1_MA2025_BC",
+                                              "Kv1p1_RI2021_SC")},
+    **{v: ("Kir2p3_MA2020_GrC", {}) for v in ("Kir2p3_MA2024_PC", "Kir2p3_MA2025_BC", "Kir2p3_RI2021_SC")},
+    **{v: ("HCN1_MA2024_PC", {}) for v in ("HCN1_MA2025_BC", "HCN1_RI2021_SC")},
+}
+
+
+def _base_class(name: str) -> str:
+    return _VARIANTS[name][0] if name in _VARIANTS else name
+
+
 # Markov channels (channel/_base.py:677-1125): restated in oracle/markov.py
 CHANNEL_DEFAULTS.update({k: dict(v) for k, v in MK.MARKOV_DEFAULTS.items()})
 ION_DEFAULTS = {
@@ -422,6 +448,34 @@ def rates(name: str, V, p: dict, Ci=None):
                   1.0 / (np.exp((Vs - 81.0) / 25.6) + np.exp(-(Vs + 132.0) / 18.0)) + 9.9),
             "q": ("it", 1.0 / (1.0 + np.exp((Vs + 58.0) / 10.6)), qtau),
         }
+    if name == "Kv3p4_MA2020_GoC":  # potassium.py:4750: V' = V + 11 mV, times in s x 1000
+        x = V + 11.0
+        mt = np.where(x < -35.0, (3.4225e-5 + 0.00498 * np.exp(x / 28.29)) * 3.0,
+                      0.00012851 + 1.0 / (np.exp((x + 100.7) / 12.9) + np.exp((x - 56.0) / -23.1)))
+        ht = np.where(x > 0.0, 0.0012 + 0.0023 * np.exp(-0.141 * x),
+                      1.2202e-05 + 0.012 * np.exp(-(((x + 56.3) / 49.6) ** 2)))
+        return {"m": ("it", 1.0 / (1.0 + np.exp(-(x + 24.0) / 15.4)), 1000.0 * mt),
+                "h": ("it", 0.31 + 0.69 / (1.0 + np.exp((x + 5.802) / 11.2)), 1000.0 * ht)}
+    if name == "Kv4p3_MA2020_GoC":  # potassium.py:4964, sigm(x, y) = 1 / (exp(x / y) + 1) (:73-74)
+        def sigm(x, y):
+            return 1.0 / (np.exp(x / y) + 1.0)
+        aa, ab = 0.8147 * sigm(V + 9.17203, -23.3271), 0.1655 / np.exp((V + 18.2791) / 19.4718)
+        ba, bb = 0.0368 * sigm(V + 111.332, 12.8433), 0.0345 * sigm(V + 49.9537, -8.90123)
+        return {"a": ("it", 1.0 / (1.0 + np.exp((V + 38.0) / -17.0)), 1.0 / (aa + ab)),
+                "b": ("it", 1.0 / (1.0 + np.exp((V + 78.8) / 8.4)), 1.0 / (ba + bb))}
+    if name == "Kv1p1_MA2020_GoC":  # potassium.py:4570
+        return {"n": ("ab", 0.12889 * np.exp(-(V + 45.0) / -33.90877), 0.12889 * np.exp(-(V + 45.0) / 12.42101))}
+    if name == "Kir2p3_MA2020_GrC":  # potassium.py:5334
+        return {"d": ("ab", 0.13289 * np.exp((V + 83.94) / -24.3902), 0.16994 * np.exp((V + 83.94) / 35.714))}
+    if name == "HCN1_MA2020_GoC":  # hyperpolarization_activated.py:675
+        o = 1.0 / (1.0 + np.exp((V - -72.49) * 0.11305))
+        r = 0.002096 * V + 0.97596
+        return {"o_fast": ("it", r * o, np.exp(((0.01371 * V) - -3.368) * 2.30259)),
+                "o_slow": ("it", (1.0 - r) * o, np.exp(((0.01451 * V) - -4.056) * 2.30259))}
+    if name == "HCN1_MA2024_PC":  # hyperpolarization_activated.py:411, half voltages minus the 9.3 mV ljp
+        vh, v1 = -90.3 - 9.3, -68.0 - 9.3
+        return {"h": ("it", 1.0 / (1.0 + np.exp((V - vh) / 9.67)),
+                      1.0 / (0.0018 * (np.exp((V - v1) / -22.0) + np.exp((V - v1) / 7.14))))}
     if name in ("KM_RI2021_SC", "KM_MA2020_GoC", "KM_MA2020_GrC"):  # potassium.py:1735-1748, :4553-4567, :5317-5331
         a = 0.0033 * np.exp((V + 30.0) / 40.0)
         b = 0.0033 * np.exp((V + 30.0) / -20.0)
@@ -449,21 +503,31 @@ _GATES = {  # (gate, power, phi-key)
     "KK2A_HM1992": (("p", 1, "phi_p"), ("q", 1, "phi_q")),
     "KK2B_HM1992": (("p", 1, "phi_p"), ("q", 1, "phi_q")),
     "KNI_Ya1989": (("p", 1, "phi"),),
+    "Kv3p4_MA2020_GoC": (("m", 3, "phi"), ("h", 1, "phi")),
+    "Kv4p3_MA2020_GoC": (("a", 3, "phi"), ("b", 1, "phi")),
+    "Kv1p1_MA2020_GoC": (("n", 4, "phi"),),
+    "Kir2p3_MA2020_GrC": (("d", 1, "phi"),),
+    "HCN1_MA2020_GoC": (("o_fast", 1, "phi"), ("o_slow", 1, "phi")),
+    "HCN1_MA2024_PC": (("h", 1, "phi"),),
 }
 _ION_OF = {"Na_Ba2002": "na", "KDR_Ba2002": "k", "CaL_IS2008": "ca", "CaT_HM1992": "ca",
            "K_Leak": "k", "AHP_De1994": "k", "Na_HH1952": "na", "K_HH1952": "k", "KM_RI2021_SC": "k",
            "Na_TM1991": "na", "K_TM1991": "k", "CaHT_HM1992": "ca", "KA1_HM1992": "k", "KA2_HM1992": "k",
            "KM_MA2020_GoC": "k", "KM_MA2020_GrC": "k", "KK2A_HM1992": "k", "KK2B_HM1992": "k",
-           "KNI_Ya1989": "k", "Nav1p6_MA2020_GoC": "na", "Kca2p2_MA2020_GoC": "k", "Kca1p1_MA2020_GoC": "k"}
+           "KNI_Ya1989": "k", "Nav1p6_MA2020_GoC": "na", "Kca2p2_MA2020_GoC": "k", "Kca1p1_MA2020_GoC": "k",
+           "Kv3p4_MA2020_GoC": "k", "Kv4p3_MA2020_GoC": "k", "Kv1p1_MA2020_GoC": "k", "Kir2p3_MA2020_GrC": "k"}
+# channels with their own reversal potential (HHTypedNeuron root, not an ion)
+_OWN_E = ("HCN_HM1992", "HCN1_MA2020_GoC", "HCN1_MA2024_PC")
 
 
 def _resolve(table: dict, decl) -> dict:
-    p = dict(table[decl.class_name])
+    base, own = _VARIANTS.get(decl.class_name, (decl.class_name, {}))
+    p = {**table[base], **own}
     for k, v in decl.params.items():
         if k not in p:
             raise ValueError(f"{decl.class_name}: unknown parameter {k!r}.")
         p[k] = float(v)
-    name = decl.class_name
+    name = base
     if name in ("Na_Ba2002", "KDR_Ba2002", "HCN_HM1992", "Na_HH1952", "K_HH1952", "Na_TM1991", "K_TM1991",
                 "KNI_Ya1989"):
         p["phi"] = p["q10"] ** ((p["temp"] - p["temp_ref"]) / 10.0)
@@ -476,6 +540,21 @@ def _resolve(table: dict, decl) -> dict:
         p["phi_q"] = p["q10_q"] ** ((p["temp"] - p["temp_ref_q"]) / 10.0)
     elif name in MK.SCHEMES:
         p = MK.scheme_params(name, p)
+    elif name == "Kv3p4_MA2020_GoC":  # Gate q10 3 at 37 degC
+        p["phi"] = 3.0 ** ((p["temp"] - _c2k(37.0)) / 10.0)
+    elif name == "Kv4p3_MA2020_GoC":  # Gate q10 3 at 25.5 degC
+        p["phi"] = 3.0 ** ((p["temp"] - _c2k(25.5)) / 10.0)
+    elif name == "Kv1p1_MA2020_GoC":  # Gate q10 2.7 at 22 degC
+        if p["gateCurrent"] != 0.0:
+            raise ValueError("Kv1p1 gating current not restated")
+        p["phi"] = 2.7 ** ((p["temp"] - _c2k(22.0)) / 10.0)
+    elif name == "Kir2p3_MA2020_GrC":  # Gate q10 3 at 20 degC
+        p["phi"] = 3.0 ** ((p["temp"] - _c2k(20.0)) / 10.0)
+    elif name == "HCN1_MA2020_GoC":  # gates q10 3 and the conductance Q10_diff 1.5, at 23 degC
+        p["phi"] = 3.0 ** ((p["temp"] - _c2k(23.0)) / 10.0)
+        p["gbar_phi"] = 1.5 ** ((p["temp"] - _c2k(23.0)) / 10.0)
+    elif name == "HCN1_MA2024_PC":  # Gate q10 3 at 37 degC
+        p["phi"] = 3.0 ** ((p["temp"] - _c2k(37.0)) / 10.0)
     return p
 
 
@@ -728,7 +807,7 @@ class OracleCell:
         for b, decls in enumerate(self.branch_mechs):
             last = {}
             for d in decls:
-                last[("IL" if d.class_name == "leaky" else d.class_name)] = d
+                last[("IL" if d.class_name == "leaky" else _base_class(d.class_name))] = d
             pts = self.cv_mid[self.branch_cv_ids[b]]
             for name, d in last.items():
                 if isinstance(d, Ion):
@@ -828,7 +907,7 @@ class OracleCell:
                         names[m.instance_name] = m.class_name
         if d.mechanism not in names:
             raise KeyError(f"no mechanism named {d.mechanism!r} at the probe")
-        cls = names[d.mechanism]
+        cls = _base_class(names[d.mechanism])
         if d.field == "Ci":
             return ("Ci",)
         return ("gate", cls, d.field)
@@ -938,6 +1017,8 @@ class OracleCell:
         return np.where(cd["mask"], nernst, self.E_ca_fixed)
 
     def _gate_product(self, name):
+        if name == "HCN1_MA2020_GoC":  # g (o_fast + o_slow) with the conductance's own Q10 factor
+            return self.chan[name]["gbar_phi"] * (self.gates[(name, "o_fast")] + self.gates[(name, "o_slow")])
         if name in MK.SCHEMES:  # the open occupancy of the raw stored states
             sch = MK.SCHEMES[name]
             return MK.open_fraction(sch, {st: self.gates[(name, st)] for st in sch.independent})
@@ -960,7 +1041,7 @@ class OracleCell:
                 fac = 1.0
             elif name == "K_Leak":
                 E, fac = self.E_k, 1.0
-            elif name == "HCN_HM1992":
+            elif name in _OWN_E:
                 E, fac = ch["E"], self._gate_product(name)
             else:
                 E, fac = E_of[_ION_OF[name]], self._gate_product(name)
@@ -981,7 +1062,7 @@ class OracleCell:
                 E, fac = ch["E"], 1.0
             elif name == "K_Leak":
                 E, fac = self.E_k, 1.0
-            elif name == "HCN_HM1992":
+            elif name in _OWN_E:
                 E, fac = ch["E"], self._gate_product(name)
             else:
                 E, fac = E_of[_ION_OF[name]], self._gate_product(name)

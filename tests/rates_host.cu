@@ -36,6 +36,12 @@ extern "C" int bc_test_rates(int which, const double* v, int n, const double* pr
       case 10: { const K2Rates<double> r(x, prm[0], false); o[0] = r.pinf; o[1] = r.ptau; o[2] = r.qinf; o[3] = r.qtau; break; }
       case 11: { const K2Rates<double> r(x, prm[0], true); o[0] = r.pinf; o[1] = r.ptau; o[2] = r.qinf; o[3] = r.qtau; break; }
       case 12: { const KNIRates<double> r(x, prm[0], prm[1]); o[0] = r.pinf; o[1] = r.ptau; break; }
+      case 13: { const Kv34Rates<double> r(x); o[0] = r.minf; o[1] = r.mtau; o[2] = r.hinf; o[3] = r.htau; break; }
+      case 14: { const Kv43Rates<double> r(x); o[0] = r.ainf; o[1] = r.atau; o[2] = r.binf; o[3] = r.btau; break; }
+      case 15: { const Kv11Rates<double> r(x); o[0] = r.a; o[1] = r.b; break; }
+      case 16: { const Kir23Rates<double> r(x); o[0] = r.a; o[1] = r.b; break; }
+      case 17: { const Hcn1fRates<double> r(x); o[0] = r.finf; o[1] = r.ftau; o[2] = r.sinf; o[3] = r.stau; break; }
+      case 18: { const Hcn1hRates<double> r(x); o[0] = r.hinf; o[1] = r.htau; break; }
       default: return -1;
     }
   }

@@ -63,7 +63,7 @@ def _bad(b: CellBatch, **kw):
 
 @pytest.mark.parametrize("mutate,msg", [
     (lambda b: _bad(b, branch_region=np.full_like(b.branch_region, 7)), "region"),
-    (lambda b: _bad(b, region_mech=np.full_like(b.region_mech, 1 << 20)), "mechanism"),
+    (lambda b: _bad(b, region_mech=np.full_like(b.region_mech, 1 << 30)), "mechanism"),
     (lambda b: _bad(b, pulse_t_off=b.pulse_t_on - 1.0), "pulse_t_off"),
     (lambda b: _bad(b, probe_branch=np.full_like(b.probe_branch, 99)), "probe"),
 ])

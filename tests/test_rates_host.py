@@ -23,6 +23,8 @@ CASES = {
     3: ("CaT_HM1992", ("V_sh",)), 4: ("HCN_HM1992", ()), 5: ("Na_HH1952", ("V_sh",)), 6: ("K_HH1952", ("V_sh",)),
     7: ("KM_RI2021_SC", ()), 8: ("KA1_HM1992", ("V_sh",)), 9: ("KA2_HM1992", ("V_sh",)),
     10: ("KK2A_HM1992", ("V_sh",)), 11: ("KK2B_HM1992", ("V_sh",)), 12: ("KNI_Ya1989", ("V_sh", "tau_max")),
+    13: ("Kv3p4_MA2020_GoC", ()), 14: ("Kv4p3_MA2020_GoC", ()), 15: ("Kv1p1_MA2020_GoC", ()),
+    16: ("Kir2p3_MA2020_GrC", ()), 17: ("HCN1_MA2020_GoC", ()), 18: ("HCN1_MA2024_PC", ()),
 }
 
 
@@ -61,6 +63,8 @@ def test_kernel_rates_match_oracle(rates_lib, which, shift):
     # a grid with the removable singularities of exprel and the branch points of the
     # piecewise time constants (KA -63, KK2B -70, CaT -80 relative to V_sh)
     V = np.linspace(-130.0, 60.0, 1901)
+    if name == "Kv3p4_MA2020_GoC":  # the branch points of its time constants (V + 11 = -35 and 0)
+        V = np.concatenate([V, [-46.0, -11.0]])
     if "V_sh" in keys:
         V = np.concatenate([V, p["V_sh"] + np.array([13.0, 15.0, 40.0, -5.0, -63.0, -70.0, -80.0, -10.0])])
     got = _kernel(rates_lib, which, V, [p[k] for k in keys])

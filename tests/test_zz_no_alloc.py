@@ -61,7 +61,10 @@ def _hh_batch():
     c.paint(branch_in("type", "basal_dendrite"), Channel("KM_RI2021_SC"), Channel("KA1_HM1992", g_max=3.0),
             Channel("KA2_HM1992", g_max=2.0), Channel("KK2A_HM1992", g_max=1.0), Channel("KK2B_HM1992", g_max=1.0),
             Channel("KNI_Ya1989"), Channel("Nav1p6_MA2020_GoC", g_max=2.0), Channel("Kca2p2_MA2020_GoC", g_max=1.0),
-            Channel("Kca1p1_MA2020_GoC", g_max=1.0))  # and the Markov channels' state views
+            Channel("Kca1p1_MA2020_GoC", g_max=1.0),  # and the Markov and cerebellar channels' state views
+            Channel("Kv3p4_MA2020_GoC", g_max=0.5), Channel("Kv4p3_MA2020_GoC", g_max=0.5),
+            Channel("Kv1p1_MA2020_GoC", g_max=0.2), Channel("Kir2p3_MA2020_GrC", g_max=0.2),
+            Channel("HCN1_MA2020_GoC", g_max=0.05), Channel("HCN1_MA2024_PC", g_max=0.05))
     return lower_cell(c)
 
 
