@@ -458,7 +458,7 @@ def surrogate_leg(a, descs, local, sid, stream, plain_ms):
     T = a.surrogate_threads
     kw = dict(tile_nodes=a.surrogate_tile_nodes, threads_per_tile=T, threads_big=T, threads_global=T,
               steps_per_launch=a.steps_per_launch, lane_nodes=a.surrogate_lane_nodes,
-              narrow_lane_nodes=a.narrow_lane_nodes)
+              narrow_lane_nodes=a.narrow_lane_nodes, tile_order=1)
     t0 = time.perf_counter()
     runner = S.SurrogateRunner(descs, model, precision="f32", device=local, plan_kw=kw)
     t_setup = time.perf_counter() - t0
@@ -559,7 +559,7 @@ def mixed_leg(a, local, model, record_every=4):
     T = a.surrogate_threads
     kw = dict(tile_nodes=a.surrogate_tile_nodes, threads_per_tile=T, threads_big=T, threads_global=T,
               steps_per_launch=a.steps_per_launch, lane_nodes=a.surrogate_lane_nodes,
-              narrow_lane_nodes=a.narrow_lane_nodes)
+              narrow_lane_nodes=a.narrow_lane_nodes, tile_order=1)
     runner = S.SurrogateRunner(descs, model, precision="f32", device=local, plan_kw=kw, full_cells=full)
     runner.run(2 * a.steps_per_launch, DT)
     runs = [runner.run(steps, DT) for _ in range(3)]

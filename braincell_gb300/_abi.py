@@ -124,6 +124,9 @@ BC_P_KCA11_G = 69
 BC_P_KCA11_PHI = 70
 BC_P_KCA11_QO = 71
 BC_P_KCA11_QC = 72
+BC_P_NAV16_OON = 73
+BC_P_NAV16_ALFAC = 88
+BC_P_NAV16_EPS = 89
 BC_P_KV34_G = 74
 BC_P_KV34_PHI = 75
 BC_P_KV43_G = 76

@@ -352,6 +352,9 @@ PROBE_STATES.update({
 for _cls, (_base, _names) in _abi.MARKOV_STATES.items():
     for _k, _n in enumerate(_names):
         PROBE_STATES[(_cls, _n)] = _base + _k
+        if _cls == "Nav1p6_MA2020_GoC":  # Nav1p1 runs the same scheme in the same states
+            for _nav11 in ("Nav1p1_MA2025_BC", "Nav1p1_RI2021_SC"):
+                PROBE_STATES[(_nav11, _n)] = _base + _k
 
 
 # CurrentProbe: mechanism class -> BC_CUR_* code; ion name -> the ion's total
@@ -363,6 +366,7 @@ PROBE_CURRENTS = {
     "KK2A_HM1992": _abi.BC_CUR_KK2A, "KK2B_HM1992": _abi.BC_CUR_KK2B, "KNI_Ya1989": _abi.BC_CUR_KNI,
     "Nav1p6_MA2020_GoC": _abi.BC_CUR_NAV16, "Kca2p2_MA2020_GoC": _abi.BC_CUR_KCA22,
     "Kca1p1_MA2020_GoC": _abi.BC_CUR_KCA11,
+    "Nav1p1_MA2025_BC": _abi.BC_CUR_NAV16, "Nav1p1_RI2021_SC": _abi.BC_CUR_NAV16,
     "Kv3p4_MA2020_GoC": _abi.BC_CUR_KV34, "Kv4p3_MA2020_GoC": _abi.BC_CUR_KV43, "Kv1p1_MA2020_GoC": _abi.BC_CUR_KV11,
     "Kir2p3_MA2020_GrC": _abi.BC_CUR_KIR23, "HCN1_MA2020_GoC": _abi.BC_CUR_HCN1F, "HCN1_MA2024_PC": _abi.BC_CUR_HCN1H,
 }

@@ -22,6 +22,8 @@ Every class name, parameter name and default below is the reference's:
 * ``KK2B_HM1992`` -- channel/potassium.py:899 (as KK2A_HM1992)
 * ``KNI_Ya1989``  -- channel/potassium.py:1045 (g_max 0.004, q10 1, temp = temp_ref = 36 degC, tau_max 4 s, V_sh 0)
 * ``Nav1p6_MA2020_GoC`` -- channel/sodium.py:727 (Markov; g_max 16, temp 22 degC, phi = 3^((T - 22 degC) / 10))
+* ``Nav1p1_MA2025_BC`` / ``Nav1p1_RI2021_SC`` -- channel/sodium.py:1188, :1351 (the Nav1.6 scheme with Oon 2.3,
+  epsilon 1e-12, phi = 2.7^((T - 22 degC) / 10); g_max 8, temp 22 degC, gateCurrent 0)
 * ``Kca2p2_MA2020_GoC`` -- channel/potassium_calcium.py:613 (Markov; g_max 38, q10_base 3, diff 3, temp 22 degC,
   phi = q10_base^((T - 23 degC) / 10))
 * ``Kca1p1_MA2020_GoC`` -- channel/potassium_calcium.py:1107 (Markov; g_max 10, q10_base 3, temp 22 degC, phi as
@@ -111,6 +113,8 @@ CHANNELS: dict[str, dict[str, float]] = {
     },
     "KNI_Ya1989": {"g_max": 0.004, "temp": T36, "q10": 1.0, "temp_ref": T36, "tau_max": 4e3, "V_sh": 0.0},
     "Nav1p6_MA2020_GoC": {"g_max": 16.0, "temp": T22},
+    "Nav1p1_MA2025_BC": {"g_max": 8.0, "temp": T22, "gateCurrent": 0.0},
+    "Nav1p1_RI2021_SC": {"g_max": 8.0, "temp": T22, "gateCurrent": 0.0},
     "Kca2p2_MA2020_GoC": {"g_max": 38.0, "q10_base": 3.0, "diff": 3.0, "temp": T22},
     "Kca1p1_MA2020_GoC": {"g_max": 10.0, "q10_base": 3.0, "temp": T22},
     "Kv3p4_MA2020_GoC": {"g_max": 4.0, "temp": T22},
@@ -145,6 +149,8 @@ for _base, _variants in KINETIC_VARIANTS.items():
     for _v, _own in _variants.items():
         CHANNELS[_v] = {**CHANNELS[_base], **_own}
         SAME_FORM[_v] = _base
+# classes with a parameter record of their own on another class's kernel mechanism
+_SHARED_KERNEL = {"Nav1p1_MA2025_BC": "Nav1p6_MA2020_GoC", "Nav1p1_RI2021_SC": "Nav1p6_MA2020_GoC"}
 # gate temperature factors fixed by a class (not constructor parameters)
 KM_Q10, KM_TEMP_REF = 3.0, T22
 _ALIASES = {"leaky": "IL"}
@@ -227,10 +233,11 @@ def region_record(mechs, cable: CableProperty) -> tuple[int, np.ndarray]:
             raise ValueError(f"Unsupported channel class {name!r}; supported: {sorted(CHANNELS)}.")
         p = _params(CHANNELS, name, decl)
         kname = kernel_class(name)
-        if kname in kernel_owner:
-            raise ValueError(f"{name} and {kernel_owner[kname]} run on the same kernel mechanism and cannot be "
+        owner_key = _SHARED_KERNEL.get(kname, kname)
+        if owner_key in kernel_owner:
+            raise ValueError(f"{name} and {kernel_owner[owner_key]} run on the same kernel mechanism and cannot be "
                              "painted on one region.")
-        kernel_owner[kname] = name
+        kernel_owner[owner_key] = name
         name = kname
         if name == "IL":
             bits |= _abi.BC_M_IL
@@ -286,6 +293,17 @@ def region_record(mechs, cable: CableProperty) -> tuple[int, np.ndarray]:
             bits |= _abi.BC_M_NAV16
             rec[_abi.BC_P_NAV16_G] = p["g_max"]
             rec[_abi.BC_P_NAV16_PHI] = q10_phi(3.0, p["temp"], T22)
+            rec[_abi.BC_P_NAV16_OON], rec[_abi.BC_P_NAV16_EPS] = 0.75, 1.75
+            rec[_abi.BC_P_NAV16_ALFAC] = (0.75 / 0.005) ** 0.25
+        elif name in ("Nav1p1_MA2025_BC", "Nav1p1_RI2021_SC"):
+            # the Nav1.6 scheme with Oon 2.3, epsilon 1e-12 and phi 2.7^((T - 22 degC) / 10)
+            if p["gateCurrent"] != 0.0:
+                raise ValueError(f"{decl.class_name}: the gating current (gateCurrent != 0) is not built.")
+            bits |= _abi.BC_M_NAV16
+            rec[_abi.BC_P_NAV16_G] = p["g_max"]
+            rec[_abi.BC_P_NAV16_PHI] = q10_phi(2.7, p["temp"], T22)
+            rec[_abi.BC_P_NAV16_OON], rec[_abi.BC_P_NAV16_EPS] = 2.3, 1e-12
+            rec[_abi.BC_P_NAV16_ALFAC] = (2.3 / 0.005) ** 0.25
         elif name == "Kca2p2_MA2020_GoC":
             bits |= _abi.BC_M_KCA22
             rec[_abi.BC_P_KCA22_G], rec[_abi.BC_P_KCA22_DIFF] = p["g_max"], p["diff"]

@@ -538,7 +538,7 @@ __device__ __noinline__ void extra_channels(Real* st, int N, const Real* P, uint
     Real kf[17], kb[17];
     if (m & BC_M_NAV16) {
       if (advance) {
-        nav16_rates(v, P[BC_P_NAV16_PHI], kf, kb);
+        nav16_rates(v, P[BC_P_NAV16_PHI], P[BC_P_NAV16_OON], P[BC_P_NAV16_ALFAC], P[BC_P_NAV16_EPS], kf, kb);
         markov_advance(st, N, nav16_graph(), kf, kb, dt);
       }
       const Real g = P[BC_P_NAV16_G] * st[(kSlotNav16 + 10) * N];  // O
@@ -795,7 +795,7 @@ __device__ __forceinline__ void steady_states(const Real* P, uint32_t m, Real* s
     Real kf[17], kb[17];
     const Real ci = P[BC_P_CA_CI0];
     if (m & BC_M_NAV16) {
-      nav16_rates(v, P[BC_P_NAV16_PHI], kf, kb);
+      nav16_rates(v, P[BC_P_NAV16_PHI], P[BC_P_NAV16_OON], P[BC_P_NAV16_ALFAC], P[BC_P_NAV16_EPS], kf, kb);
       markov_steady(st, N, nav16_graph(), kf, kb);
     }
     if (m & BC_M_KCA22) {

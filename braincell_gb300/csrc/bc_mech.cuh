@@ -391,18 +391,20 @@ static __device__ __constant__ const int8_t kKca22Dst[5] = {1, 2, 3, 4, 5};
 static __device__ __constant__ const int8_t kKca11Src[13] = {0, 1, 2, 3, 5, 6, 7, 8, 0, 1, 2, 3, 4};
 static __device__ __constant__ const int8_t kKca11Dst[13] = {1, 2, 3, 4, 6, 7, 8, 9, 5, 6, 7, 8, 9};
 
-// Nav1p6 rates (sodium.py:903-935; constants :874-898 with x3 = x5 = 1e12,
-// x4 = -1e12 and the V shifts 0): alfac = (Oon / Con)^(1/4), btfac = (Ooff / Coff)^(1/4).
+// Nav1.6-scheme rates (sodium.py:903-935; constants :874-898 with x3 = x5 = 1e12,
+// x4 = -1e12 and the V shifts 0).  Oon, alfac = (Oon / Con)^(1/4) and epsilon come
+// from the parameter record: Nav1p1_MA2025_BC (sodium.py:1188) runs the same scheme
+// with Oon 2.3 and epsilon 1e-12.
 template <typename Real>
-__device__ __forceinline__ void nav16_rates(Real v, Real phi, Real* kf, Real* kb) {
-  const Real al = Real(150), be = Real(3), ga = Real(150), de = Real(40), ep = Real(1.75), ze = Real(0.03);
-  const Real con = Real(0.005), coff = Real(0.5), oon = Real(0.75), ooff = Real(0.005);
-  const double af[5] = {1.0, 3.4996355115805833, 12.24744871391589, 42.861606445481996, 150.0};
-  const double bf[5] = {1.0, 0.31622776601683794, 0.1, 0.03162277660168379, 0.01};
+__device__ __forceinline__ void nav16_rates(Real v, Real phi, Real oon, Real alfac, Real ep, Real* kf, Real* kb) {
+  const Real al = Real(150), be = Real(3), ga = Real(150), de = Real(40), ze = Real(0.03);
+  const Real con = Real(0.005), coff = Real(0.5), ooff = Real(0.005);
+  const double bf[5] = {1.0, 0.31622776601683794, 0.1, 0.03162277660168379, 0.01};  // (Ooff / Coff)^(k/4)
   const Real ea = aexp(v / Real(20)) * phi, eb = aexp(v / Real(-20)) * phi;
   const Real e3 = aexp(v / Real(1e12)) * phi, e4 = aexp(v / Real(-1e12)) * phi, e6 = aexp(v / Real(-25)) * phi;
   const Real e5 = aexp(v / Real(1e12)) * phi;
-  const Real alfac = Real(af[1]), btfac = Real(bf[1]);
+  const Real a2 = alfac * alfac, a3 = a2 * alfac, a4 = a3 * alfac;
+  const Real btfac = Real(bf[1]);
   // pair order: C1C2 C2C3 C3C4 C4C5 C1I1 I1I2 C2I2 I2I3 C3I3 I3I4 C4I4 I4I5 C5I5 C5O OB I5I6 OI6
   kf[0] = Real(4) * al * ea;  kb[0] = Real(1) * be * eb;
   kf[1] = Real(3) * al * ea;  kb[1] = Real(2) * be * eb;
@@ -410,13 +412,13 @@ __device__ __forceinline__ void nav16_rates(Real v, Real phi, Real* kf, Real* kb
   kf[3] = Real(1) * al * ea;  kb[3] = Real(4) * be * eb;
   kf[4] = con * phi;          kb[4] = coff * phi;
   kf[5] = Real(4) * al * alfac * ea;  kb[5] = Real(1) * be * btfac * eb;
-  kf[6] = con * Real(af[1]) * phi;    kb[6] = coff * Real(bf[1]) * phi;
+  kf[6] = con * alfac * phi;          kb[6] = coff * Real(bf[1]) * phi;
   kf[7] = Real(3) * al * alfac * ea;  kb[7] = Real(2) * be * btfac * eb;
-  kf[8] = con * Real(af[2]) * phi;    kb[8] = coff * Real(bf[2]) * phi;
+  kf[8] = con * a2 * phi;             kb[8] = coff * Real(bf[2]) * phi;
   kf[9] = Real(2) * al * alfac * ea;  kb[9] = Real(3) * be * btfac * eb;
-  kf[10] = con * Real(af[3]) * phi;   kb[10] = coff * Real(bf[3]) * phi;
+  kf[10] = con * a3 * phi;            kb[10] = coff * Real(bf[3]) * phi;
   kf[11] = Real(1) * al * alfac * ea; kb[11] = Real(4) * be * btfac * eb;
-  kf[12] = con * Real(af[4]) * phi;   kb[12] = coff * Real(bf[4]) * phi;
+  kf[12] = con * a4 * phi;            kb[12] = coff * Real(bf[4]) * phi;
   kf[13] = ga * e3;                   kb[13] = de * e4;
   kf[14] = ep * e5;                   kb[14] = ze * e6;
   kf[15] = ga * e3;                   kb[15] = de * e4;

@@ -1685,7 +1685,7 @@ bc_status bc_plan_create(const bc_batch_spec* spec, const bc_plan_options* opts_
         const size_t need = size_t(outs[t].desc.blob_bytes) + size_t(outs[t].desc.scratch_bytes);
         if (lcz.smem) lcz.smem_bytes = std::max(lcz.smem_bytes, need);
       }
-    if (opts.tile_order == 0) {
+    if (opts.tile_order == 1) {
       // longest estimated step first: the block scheduler hands out CTAs in index
       // order, so the tiles left for the last, partly filled wave are the short ones
       std::stable_sort(tord.begin() + lcz.first, tord.end(), [&](size_t x, size_t y) {

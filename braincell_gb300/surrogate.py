@@ -51,6 +51,9 @@ PORT_THREADS = 384
 # Serial-walk length of the reduced tiles' warp slots: a GB300 sweep of the 10,000-cell
 # reduced run (1,000-step launches) gave 76.4 / 74.4 / 75.4 ms per 1,000 steps at 4 / 6 / 10.
 PORT_LANE_NODES = 6
+# Reduced plans launch their longest tiles first (tile_order 1): 74.0-74.3 against
+# 74.7-74.9 ms per 1,000 steps in build order on the same GB300.
+PORT_TILE_ORDER = 1
 # Fallback (full-morphology) plans run the kernel without ports in large tiles.
 FALLBACK_TILE_NODES = 2500
 S_SCALE = 0.1        # nA: stimulus input scale (the step kernel's constant)
@@ -394,6 +397,7 @@ def fallback_plan_options(descs, base: dict | None = None, threads: int = 512, n
     kw["threads_big"] = max(threads, 512)
     kw["threads_global"] = 512
     kw.pop("lane_nodes", None)
+    kw.pop("tile_order", None)
     return kw
 
 
@@ -441,6 +445,7 @@ class SurrogateRunner:
         self.plan_kw = dict(plan_kw or {})
         self.plan_kw.setdefault("tile_nodes", PORT_TILE_NODES)
         self.plan_kw.setdefault("lane_nodes", PORT_LANE_NODES)
+        self.plan_kw.setdefault("tile_order", PORT_TILE_ORDER)
         for k in ("threads_per_tile", "threads_big", "threads_global"):
             self.plan_kw.setdefault(k, PORT_THREADS)
         self.fallback = fallback and model is not None

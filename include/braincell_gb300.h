@@ -150,7 +150,7 @@ typedef int32_t bc_status;
 #define BC_P_KCA11_PHI 70   /* q10^((T - 23 degC) / 10)                             */
 #define BC_P_KCA11_QO 71    /* Qo F / (R T) per mV: alpha(V) = exp(QO V)            */
 #define BC_P_KCA11_QC 72    /* Qc F / (R T) per mV: beta(V) = exp(QC V)             */
-/* 73: reserved (0) */
+#define BC_P_NAV16_OON 73   /* the Nav1.6 scheme's Oon (Nav1p6 0.75, Nav1p1 2.3)    */
 #define BC_P_KV34_G 74
 #define BC_P_KV34_PHI 75    /* 3^((T - 37 degC) / 10)                               */
 #define BC_P_KV43_G 76
@@ -165,7 +165,8 @@ typedef int32_t bc_status;
 #define BC_P_HCN1H_G 85
 #define BC_P_HCN1H_E 86
 #define BC_P_HCN1H_PHI 87   /* 3^((T - 37 degC) / 10)                               */
-/* 88, 89: reserved (0) */
+#define BC_P_NAV16_ALFAC 88 /* (Oon / Con)^(1/4)                                    */
+#define BC_P_NAV16_EPS 89   /* epsilon, the open -> blocked rate (Nav1p1: 1e-12)   */
 
 /* ------------------------------------------------------------------ batch spec */
 /*
@@ -287,10 +288,10 @@ typedef struct bc_plan_options {
                                (serial solve per cell, cells interleaved node by node in
                                global memory) instead of in packed tiles; plans without
                                synapses, connections, mechanism probes or ports; 0 = off */
-  int32_t tile_order;       /* launch order of the tiles of a class: 0 = longest
+  int32_t tile_order;       /* launch order of the tiles of a class: 0 = the order the
+                               packer built them (largest cells first); 1 = longest
                                estimated step first (critical path, then nodes), so
-                               the last wave of CTAs is made of short tiles; 1 = the
-                               order the packer built them                         */
+                               the last wave of CTAs is made of short tiles         */
 } bc_plan_options;
 
 typedef struct bc_plan* bc_plan_t;

@@ -72,10 +72,11 @@ class MarkovScheme:
 
 
 def _nav16_rates(V, Ci, p):
-    """channel/sodium.py:903-935 with the constants of :874-898."""
+    """channel/sodium.py:903-935 with the constants of :874-898; Nav1p1_MA2025_BC
+    (:1188) replaces Oon (2.3) and epsilon (1e-12)."""
     phi = p["phi"]
-    Con, Coff, Oon, Ooff = 0.005, 0.5, 0.75, 0.005
-    alpha, beta, gamma, delta, epsilon, zeta = 150.0, 3.0, 150.0, 40.0, 1.75, 0.03
+    Con, Coff, Oon, Ooff = 0.005, 0.5, p.get("Oon", 0.75), 0.005
+    alpha, beta, gamma, delta, epsilon, zeta = 150.0, 3.0, 150.0, 40.0, p.get("epsilon", 1.75), 0.03
     x1, x2, x3, x4, x5, x6 = 20.0, -20.0, 1e12, -1e12, 1e12, -25.0
     vshifta = vshifti = vshiftk = 0.0
     alfac = (Oon / Con) ** 0.25
@@ -143,7 +144,16 @@ def _kca11_rates(V, Ci, p):
     return r
 
 
+_NAV_PAIRS = (("C1", "C2", "f01", "b01"), ("C2", "C3", "f02", "b02"), ("C3", "C4", "f03", "b03"),
+              ("C4", "C5", "f04", "b04"), ("C1", "I1", "fi1", "bi1"), ("I1", "I2", "f11", "b11"),
+              ("C2", "I2", "fi2", "bi2"), ("I2", "I3", "f12", "b12"), ("C3", "I3", "fi3", "bi3"),
+              ("I3", "I4", "f13", "b13"), ("C4", "I4", "fi4", "bi4"), ("I4", "I5", "f14", "b14"),
+              ("C5", "I5", "fi5", "bi5"), ("C5", "O", "f0O", "b0O"), ("O", "B", "fip", "bip"),
+              ("I5", "I6", "f1n", "b1n"), ("O", "I6", "fin", "bin"))  # sodium.py:840-858
+
 SCHEMES = {
+    "Nav1p1_MA2025_BC": MarkovScheme("Nav1p1_MA2025_BC", _NAV_PAIRS, "I6", ("O",), "na", _nav16_rates),
+    "Nav1p1_RI2021_SC": MarkovScheme("Nav1p1_RI2021_SC", _NAV_PAIRS, "I6", ("O",), "na", _nav16_rates),
     "Nav1p6_MA2020_GoC": MarkovScheme(
         "Nav1p6_MA2020_GoC",
         (("C1", "C2", "f01", "b01"), ("C2", "C3", "f02", "b02"), ("C3", "C4", "f03", "b03"),
@@ -173,6 +183,9 @@ _T22 = 273.15 + 22.0
 # constructor defaults: sodium.py:862-866, potassium_calcium.py:726-735, :1230-1238
 MARKOV_DEFAULTS = {
     "Nav1p6_MA2020_GoC": dict(g_max=16.0, temp=_T22),
+    # sodium.py:1188-1222 (RI2021_SC inherits it, :1351)
+    "Nav1p1_MA2025_BC": dict(g_max=8.0, temp=_T22, Oon=2.3, epsilon=1e-12, gateCurrent=0.0),
+    "Nav1p1_RI2021_SC": dict(g_max=8.0, temp=_T22, Oon=2.3, epsilon=1e-12, gateCurrent=0.0),
     "Kca2p2_MA2020_GoC": dict(g_max=38.0, q10_base=3.0, diff=3.0, temp=_T22),
     "Kca1p1_MA2020_GoC": dict(g_max=10.0, q10_base=3.0, temp=_T22),
 }
@@ -185,6 +198,10 @@ def scheme_params(name: str, p: dict) -> dict:
     out = dict(p)
     if name == "Nav1p6_MA2020_GoC":
         out["phi"] = 3.0 ** ((p["temp"] - _T22) / 10.0)
+    elif name.startswith("Nav1p1"):  # sodium.py:1212: phi = 2.7^((T - 22 degC) / 10)
+        if p.get("gateCurrent", 0.0) != 0.0:
+            raise ValueError("Nav1p1 gating current not restated")
+        out["phi"] = 2.7 ** ((p["temp"] - _T22) / 10.0)
     else:
         out["phi"] = p["q10_base"] ** ((p["temp"] - (273.15 + 23.0)) / 10.0)
     return out

@@ -515,7 +515,8 @@ _ION_OF = {"Na_Ba2002": "na", "KDR_Ba2002": "k", "CaL_IS2008": "ca", "CaT_HM1992
            "Na_TM1991": "na", "K_TM1991": "k", "CaHT_HM1992": "ca", "KA1_HM1992": "k", "KA2_HM1992": "k",
            "KM_MA2020_GoC": "k", "KM_MA2020_GrC": "k", "KK2A_HM1992": "k", "KK2B_HM1992": "k",
            "KNI_Ya1989": "k", "Nav1p6_MA2020_GoC": "na", "Kca2p2_MA2020_GoC": "k", "Kca1p1_MA2020_GoC": "k",
-           "Kv3p4_MA2020_GoC": "k", "Kv4p3_MA2020_GoC": "k", "Kv1p1_MA2020_GoC": "k", "Kir2p3_MA2020_GrC": "k"}
+           "Kv3p4_MA2020_GoC": "k", "Kv4p3_MA2020_GoC": "k", "Kv1p1_MA2020_GoC": "k", "Kir2p3_MA2020_GrC": "k",
+           "Nav1p1_MA2025_BC": "na", "Nav1p1_RI2021_SC": "na"}
 # channels with their own reversal potential (HHTypedNeuron root, not an ion)
 _OWN_E = ("HCN_HM1992", "HCN1_MA2020_GoC", "HCN1_MA2024_PC")
 

@@ -20,7 +20,7 @@ from braincell_gb300.mech import (AllRegion, CableProperty, Channel, CurrentClam
 DT = 0.025
 
 
-def _cell(precision="f64", pop_size=1, amp=0.4, mech_probes=True):
+def _cell(precision="f64", pop_size=1, amp=0.4, mech_probes=True, nav="Nav1p6_MA2020_GoC"):
     soma = Branch.from_lengths(lengths=[20.0], radii=[10.0, 10.0], type="soma")
     m = Morphology.from_root(soma, name="soma")
     m.attach(parent="soma", child_branch=Branch.from_lengths(lengths=[120.0], radii=[1.0, 0.6], type="dendrite"),
@@ -28,7 +28,7 @@ def _cell(precision="f64", pop_size=1, amp=0.4, mech_probes=True):
     c = Cell(m, cv_policy=CVPerBranch(4), precision=precision, pop_size=pop_size)
     c.paint(AllRegion(), CableProperty(), Channel("IL", g_max=0.2, E=-65.0),
             Ion("CalciumDetailed", C_rest=5e-5, tau=20.0, d=0.5, Ci_initializer=5e-5))
-    c.paint(branch_in("type", "soma"), Channel("Nav1p6_MA2020_GoC", g_max=60.0, name="nav"),
+    c.paint(branch_in("type", "soma"), Channel(nav, g_max=60.0, name="nav"),
             Channel("KDR_Ba2002", g_max=20.0), Channel("Kca2p2_MA2020_GoC", g_max=1.0, name="sk"),
             Channel("Kca1p1_MA2020_GoC", g_max=2.0, name="bk"), Channel("CaL_IS2008", g_max=1.0))
     c.paint(branch_in("type", "dendrite"), Channel("CaL_IS2008", g_max=2.0))
@@ -62,15 +62,17 @@ def test_markov_plans_run_the_extra_variant_with_the_markov_slots(native_lib):
 
 
 @pytest.mark.gpu
-def test_markov_cell_f64_matches_oracle(native_lib, cuda_device):
+@pytest.mark.parametrize("nav", ["Nav1p6_MA2020_GoC", "Nav1p1_MA2025_BC"])
+def test_markov_cell_f64_matches_oracle(native_lib, cuda_device, nav):
+    # Nav1p1_MA2025_BC: the same 13-state scheme with its own Oon, epsilon and phi
     from braincell_gb300.runtime import Plan
     from oracle.staggered import OracleCell
 
     n = 1400
-    p = Plan(_cell().batch(), precision="f64", record_every=1, device=cuda_device)
+    p = Plan(_cell(nav=nav).batch(), precision="f64", record_every=1, device=cuda_device)
     p.run(n, DT)
     gpu = p.traces()[:, :]
-    oc = OracleCell(_cell())
+    oc = OracleCell(_cell(nav=nav))
     ref, osp = oc.run(DT, n)
     ref = ref[0]
     assert gpu.shape == ref.shape == (9, n)
