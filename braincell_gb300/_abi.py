@@ -48,9 +48,12 @@ BC_M_KV11 = 1 << 22
 BC_M_KIR23 = 1 << 23
 BC_M_HCN1F = 1 << 24
 BC_M_HCN1H = 1 << 25
-BC_M_ALL = 0x3FFFFFF
+BC_M_CAHVA = 1 << 26
+BC_M_CAV23 = 1 << 27
+BC_M_CAV32 = 1 << 28
+BC_M_ALL = 0x1FFFFFFF
 
-BC_NPARAM = 90
+BC_NPARAM = 96
 BC_P_INVCM = 0
 BC_P_VREST = 1
 BC_P_ENA = 2
@@ -127,6 +130,11 @@ BC_P_KCA11_QC = 72
 BC_P_NAV16_OON = 73
 BC_P_NAV16_ALFAC = 88
 BC_P_NAV16_EPS = 89
+BC_P_CAHVA_G = 90
+BC_P_CAHVA_PHI = 91
+BC_P_CAV23_G = 92
+BC_P_CAV32_G = 93
+BC_P_CAV32_VSH = 94
 BC_P_KV34_G = 74
 BC_P_KV34_PHI = 75
 BC_P_KV43_G = 76
@@ -156,7 +164,7 @@ BC_GRU_HIDDEN = 64
 BC_GRU_INPUTS = 4
 BC_SURROGATE_NORM = 5
 
-BC_PROBE_CURRENT = 64
+BC_PROBE_CURRENT = 128
 BC_CUR_IL = 0
 BC_CUR_KLEAK = 1
 BC_CUR_NA = 2
@@ -185,7 +193,10 @@ BC_CUR_KV11 = 24
 BC_CUR_KIR23 = 25
 BC_CUR_HCN1F = 26
 BC_CUR_HCN1H = 27
-BC_NCUR = 28
+BC_CUR_CAHVA = 28
+BC_CUR_CAV23 = 29
+BC_CUR_CAV32 = 30
+BC_NCUR = 31
 
 BC_STATE_V = 0
 BC_STATE_NA_P = 1
@@ -225,7 +236,13 @@ BC_STATE_KIR23_D = 56
 BC_STATE_HCN1F_FAST = 57
 BC_STATE_HCN1F_SLOW = 58
 BC_STATE_HCN1H_H = 59
-BC_NSTATE_VIEW = 60
+BC_STATE_CAHVA_S = 60
+BC_STATE_CAHVA_U = 61
+BC_STATE_CAV23_M = 62
+BC_STATE_CAV23_H = 63
+BC_STATE_CAV32_M = 64
+BC_STATE_CAV32_H = 65
+BC_NSTATE_VIEW = 66
 # the independent states of each Markov scheme, in view order (first appearance in
 # the scheme's transition list, the dependent state left out)
 MARKOV_STATES = {
@@ -270,6 +287,12 @@ STATE_NAMES = {
     "HCN1_o_fast": BC_STATE_HCN1F_FAST,
     "HCN1_o_slow": BC_STATE_HCN1F_SLOW,
     "HCN1_h": BC_STATE_HCN1H_H,
+    "CaHVA_s": BC_STATE_CAHVA_S,
+    "CaHVA_u": BC_STATE_CAHVA_U,
+    "Cav2p3_m": BC_STATE_CAV23_M,
+    "Cav2p3_h": BC_STATE_CAV23_H,
+    "Cav3p2_m": BC_STATE_CAV32_M,
+    "Cav3p2_h": BC_STATE_CAV32_H,
 }
 for _cls, (_base, _names) in MARKOV_STATES.items():
     for _k, _n in enumerate(_names):

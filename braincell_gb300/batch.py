@@ -348,6 +348,9 @@ PROBE_STATES.update({
     ("Kv1p1_MA2020_GoC", "n"): _abi.BC_STATE_KV11_N, ("Kir2p3_MA2020_GrC", "d"): _abi.BC_STATE_KIR23_D,
     ("HCN1_MA2020_GoC", "o_fast"): _abi.BC_STATE_HCN1F_FAST, ("HCN1_MA2020_GoC", "o_slow"): _abi.BC_STATE_HCN1F_SLOW,
     ("HCN1_MA2024_PC", "h"): _abi.BC_STATE_HCN1H_H,
+    ("CaHVA_MA2020_GoC", "s"): _abi.BC_STATE_CAHVA_S, ("CaHVA_MA2020_GoC", "u"): _abi.BC_STATE_CAHVA_U,
+    ("Cav2p3_MA2020_GoC", "m"): _abi.BC_STATE_CAV23_M, ("Cav2p3_MA2020_GoC", "h"): _abi.BC_STATE_CAV23_H,
+    ("Cav3p2_RI2021_SC", "m"): _abi.BC_STATE_CAV32_M, ("Cav3p2_RI2021_SC", "h"): _abi.BC_STATE_CAV32_H,
 })
 for _cls, (_base, _names) in _abi.MARKOV_STATES.items():
     for _k, _n in enumerate(_names):
@@ -369,6 +372,7 @@ PROBE_CURRENTS = {
     "Nav1p1_MA2025_BC": _abi.BC_CUR_NAV16, "Nav1p1_RI2021_SC": _abi.BC_CUR_NAV16,
     "Kv3p4_MA2020_GoC": _abi.BC_CUR_KV34, "Kv4p3_MA2020_GoC": _abi.BC_CUR_KV43, "Kv1p1_MA2020_GoC": _abi.BC_CUR_KV11,
     "Kir2p3_MA2020_GrC": _abi.BC_CUR_KIR23, "HCN1_MA2020_GoC": _abi.BC_CUR_HCN1F, "HCN1_MA2024_PC": _abi.BC_CUR_HCN1H,
+    "CaHVA_MA2020_GoC": _abi.BC_CUR_CAHVA, "Cav2p3_MA2020_GoC": _abi.BC_CUR_CAV23, "Cav3p2_RI2021_SC": _abi.BC_CUR_CAV32,
 }
 ION_CURRENTS = {"na": _abi.BC_CUR_ION_NA, "k": _abi.BC_CUR_ION_K, "ca": _abi.BC_CUR_ION_CA}
 

@@ -37,6 +37,10 @@ Every class name, parameter name and default below is the reference's:
   and g Q10 1.5, both at 23 degC)
 * ``HCN1_MA2024_PC`` -- channel/hyperpolarization_activated.py:411 (g_max 0.1, E -34.4 mV, temp 23 degC; gate q10 3
   at 37 degC)
+* ``CaHVA_MA2020_GoC`` / ``_GrC`` -- channel/calcium.py:4333, :4499 (g_max 0.46, temp 30 degC; gates q10 3 at 20 degC)
+* ``Cav2p3_MA2020_GoC`` -- channel/calcium.py:4672 (g_max 0, temp 34 degC; gates without a temperature factor)
+* ``Cav3p2_RI2021_SC`` -- channel/calcium.py:3636 (g_max 8e-4, V_sh 0, temp 36 degC; m phi 5^1.2, the h time constant
+  carrying 3^1.2); the MA2025_BC and MA2024_PC classes inherit it
 
 Same-form classes: Na_TM1991 has Na_Ba2002's Traub-Miles rate functions written
 in terms of V_sh - V (sodium.py:275-289 against :154-170), K_TM1991 has
@@ -123,6 +127,9 @@ CHANNELS: dict[str, dict[str, float]] = {
     "Kir2p3_MA2020_GrC": {"g_max": 0.9, "temp": T30},
     "HCN1_MA2020_GoC": {"g_max": 0.05, "E": -20.0, "temp": T22},
     "HCN1_MA2024_PC": {"g_max": 0.1, "E": -34.4, "temp": celsius2kelvin(23.0)},
+    "CaHVA_MA2020_GoC": {"g_max": 0.46, "temp": T30},
+    "Cav2p3_MA2020_GoC": {"g_max": 0.0, "temp": celsius2kelvin(34.0)},
+    "Cav3p2_RI2021_SC": {"g_max": 8.0e-4, "V_sh": 0.0, "temp": T36},
 }
 # cell-type variants with their base class's kinetics; own defaults where they differ
 KINETIC_VARIANTS = {
@@ -132,6 +139,8 @@ KINETIC_VARIANTS = {
     "Kv1p1_MA2020_GoC": {v: {} for v in ("Kv1p1_MA2020_GrC", "Kv1p1_MA2024_PC", "Kv1p1_MA2025_BC", "Kv1p1_RI2021_SC")},
     "Kir2p3_MA2020_GrC": {v: {} for v in ("Kir2p3_MA2024_PC", "Kir2p3_MA2025_BC", "Kir2p3_RI2021_SC")},
     "HCN1_MA2024_PC": {v: {} for v in ("HCN1_MA2025_BC", "HCN1_RI2021_SC")},
+    "CaHVA_MA2020_GoC": {"CaHVA_MA2020_GrC": {}},
+    "Cav3p2_RI2021_SC": {v: {} for v in ("Cav3p2_MA2025_BC", "Cav3p2_MA2024_PC")},
 }
 MARKOV_VARIANTS = {
     "Nav1p6_MA2020_GoC": ("Nav1p6_MA2024_PC", "Nav1p6_MA2025_BC", "Nav1p6_RI2021_SC"),
@@ -341,6 +350,16 @@ def region_record(mechs, cable: CableProperty) -> tuple[int, np.ndarray]:
             bits |= _abi.BC_M_HCN1H
             rec[_abi.BC_P_HCN1H_G], rec[_abi.BC_P_HCN1H_E] = p["g_max"], p["E"]
             rec[_abi.BC_P_HCN1H_PHI] = q10_phi(3.0, p["temp"], T37)
+        elif name == "CaHVA_MA2020_GoC":
+            bits |= _abi.BC_M_CAHVA
+            rec[_abi.BC_P_CAHVA_G] = p["g_max"]
+            rec[_abi.BC_P_CAHVA_PHI] = q10_phi(3.0, p["temp"], celsius2kelvin(20.0))
+        elif name == "Cav2p3_MA2020_GoC":
+            bits |= _abi.BC_M_CAV23
+            rec[_abi.BC_P_CAV23_G] = p["g_max"]
+        elif name == "Cav3p2_RI2021_SC":
+            bits |= _abi.BC_M_CAV32
+            rec[_abi.BC_P_CAV32_G], rec[_abi.BC_P_CAV32_VSH] = p["g_max"], p["V_sh"]
         elif name in _PQ_RECORDS:
             bit, base = _PQ_RECORDS[name]
             bits |= bit

@@ -47,6 +47,9 @@ int32_t locate_node(const bc_batch_spec& spec, int64_t c, const LoweredCell& lc,
 // shared-memory banks (the lanes of a warp read the records of their own nodes'
 // regions; at a stride of 64 words they would all fall in one bank).
 constexpr int kParamStride = BC_NPARAM + 1;
+// Plans on the lean kernel variants read only the main mix's entries (up to
+// BC_P_CA_CI0): their records keep those, on an odd stride as well.
+constexpr int kParamStrideCore = BC_P_CA_CI0 + 2;
 
 // A chain: nodes [start, start+count) of the tile, bottom (deepest) first; node
 // start+k+1 is the parent of node start+k and top_parent is the parent of the top
@@ -92,7 +95,7 @@ struct TileDesc {
   int32_t n_pulses;
   int64_t pulse_offset;     // into plan pulse array
   int32_t n_xprobes;        // mechanism probes of the tile (ProbeRef list at off_plist)
-  int32_t pad0;
+  int32_t param_stride;     // reals per parameter record (kParamStride or kParamStrideCore)
   int64_t probe_offset;     // into plan probe array
   // byte offsets inside the blob
   int32_t off_v;            // (V_hi, V_lo) pairs

@@ -133,6 +133,7 @@ struct TileView {
   const int32_t* srccell;   // per tile cell: global id of a spike source, -1 otherwise
   int32_t* stamp;           // per tile cell: last step with a crossing
   int N, n_real, n_phases, n_cells;
+  int pstride;  // reals per parameter record
   bool has_src;
 
   __device__ __forceinline__ void bind(const TileDesc& td, unsigned char* base, unsigned char* scratch, void* gstate) {
@@ -158,6 +159,7 @@ struct TileView {
     srccell = has_src ? reinterpret_cast<const int32_t*>(base + td.off_srccell) : nullptr;
     stamp = has_src ? reinterpret_cast<int32_t*>(scratch + td.off_stamp) : nullptr;
     n_cells = td.n_cells;
+    pstride = td.param_stride;
     N = td.n_nodes;
     n_real = td.n_real_nodes;
     n_phases = td.n_phases;
@@ -210,6 +212,29 @@ __device__ __forceinline__ void load_states(const Real* st, int N, uint32_t m, N
     s.cahi = st[kSlotCaHi * N];
     s.calo = st[kSlotCaLo * N];
   }
+}
+
+// The cerebellar calcium channels' current density at v from the states in st and
+// the calcium reversal potential eca: the step-start current the calcium shell
+// integrates (with CaL and CaT), and the ohmic terms of the row.
+template <typename Real>
+__device__ __forceinline__ Real cerebellar_ca_current(const Real* st, int N, const Real* P, uint32_t m, Real v, Real eca,
+                                                      Real* g_out) {
+  Real g = Real(0);
+  if (m & BC_M_CAHVA) {
+    const Real s = st[kSlotCaHvaS * N];
+    g += P[BC_P_CAHVA_G] * s * s * st[kSlotCaHvaU * N];
+  }
+  if (m & BC_M_CAV23) {
+    const Real a = st[kSlotCav23M * N];
+    g += P[BC_P_CAV23_G] * a * a * a * st[kSlotCav23H * N];
+  }
+  if (m & BC_M_CAV32) {
+    const Real a = st[kSlotCav32M * N];
+    g += P[BC_P_CAV32_G] * a * a * st[kSlotCav32H * N];
+  }
+  if (g_out) *g_out = g;
+  return g * (eca - v);
 }
 
 // The value a mechanism probe records: state view `field` (a BC_STATE_* other
@@ -328,6 +353,12 @@ __device__ __forceinline__ double probe_current(const Real* st, int N, const Rea
                    : Real(0);
       case BC_CUR_HCN1H:
         return (m & BC_M_HCN1H) ? P[BC_P_HCN1H_G] * st[kSlotHcn1H * N] * (P[BC_P_HCN1H_E] - v) : Real(0);
+      case BC_CUR_CAHVA:
+        return cerebellar_ca_current(st, N, P, m & BC_M_CAHVA, v, eca(), (Real*)nullptr);
+      case BC_CUR_CAV23:
+        return cerebellar_ca_current(st, N, P, m & BC_M_CAV23, v, eca(), (Real*)nullptr);
+      case BC_CUR_CAV32:
+        return cerebellar_ca_current(st, N, P, m & BC_M_CAV32, v, eca(), (Real*)nullptr);
     }
     return Real(0);
   };
@@ -340,7 +371,8 @@ __device__ __forceinline__ double probe_current(const Real* st, int N, const Rea
              double(cur(BC_CUR_KK2B)) + double(cur(BC_CUR_KNI)) + double(cur(BC_CUR_KCA22)) + double(cur(BC_CUR_KCA11)) +
              double(cur(BC_CUR_KV34)) + double(cur(BC_CUR_KV43)) + double(cur(BC_CUR_KV11)) + double(cur(BC_CUR_KIR23));
     case BC_CUR_ION_CA:
-      return double(cur(BC_CUR_CAL)) + double(cur(BC_CUR_CAT));
+      return double(cur(BC_CUR_CAL)) + double(cur(BC_CUR_CAT)) + double(cur(BC_CUR_CAHVA)) + double(cur(BC_CUR_CAV23)) +
+             double(cur(BC_CUR_CAV32));
     default:
       return double(cur(code));
   }
@@ -350,7 +382,9 @@ __device__ __forceinline__ double probe_current(const Real* st, int N, const Rea
 // M current, the A current, the slow K2 current, the slow non-inactivating K
 // current): kept out of line so that their registers do not weigh on the common
 // path; same exp-Euler steps and ohmic currents as the others.
-constexpr uint32_t kCerebellarChannels = BC_M_KV34 | BC_M_KV43 | BC_M_KV11 | BC_M_KIR23 | BC_M_HCN1F | BC_M_HCN1H;
+constexpr uint32_t kCerebellarCaChannels = BC_M_CAHVA | BC_M_CAV23 | BC_M_CAV32;
+constexpr uint32_t kCerebellarChannels =
+    BC_M_KV34 | BC_M_KV43 | BC_M_KV11 | BC_M_KIR23 | BC_M_HCN1F | BC_M_HCN1H | kCerebellarCaChannels;
 constexpr uint32_t kExtraChannels = BC_M_NAHH | BC_M_KHH | BC_M_KM | BC_M_KA1 | BC_M_KA2 | BC_M_KK2A | BC_M_KK2B |
                                    BC_M_KNI | BC_M_NAV16 | BC_M_KCA22 | BC_M_KCA11 | kCerebellarChannels;
 
@@ -394,10 +428,11 @@ __device__ __forceinline__ void k2_current(Real* st, int N, const Real* P, int s
 }
 
 // The cerebellar HH channels: exp-Euler gates at v, ohmic currents (HCN1 with its
-// own reversal potential; HCN1_MA2020_GoC's g carries its Q10 factor already).
+// own reversal potential; HCN1_MA2020_GoC's g carries its Q10 factor already; the
+// calcium channels in E_Ca of the calcium ci after this step's shell update).
 template <typename Real>
-__device__ __forceinline__ void cerebellar_channels(Real* st, int N, const Real* P, uint32_t m, Real v, Real dt,
-                                                    bool advance, Real& G, Real& I) {
+__device__ __forceinline__ void cerebellar_channels(Real* st, int N, const Real* P, uint32_t m, Real v, Real ci,
+                                                    Real dt, bool advance, Real& G, Real& I) {
   if (m & BC_M_KV34) {
     Real a = st[kSlotKv34M * N], b = st[kSlotKv34H * N];
     if (advance) {
@@ -471,6 +506,30 @@ __device__ __forceinline__ void cerebellar_channels(Real* st, int N, const Real*
     G += g;
     I += g * (P[BC_P_HCN1H_E] - v);
   }
+  if (m & kCerebellarCaChannels) {
+    if (advance) {
+      if (m & BC_M_CAHVA) {
+        const CaHvaRates<Real> r(v);
+        st[kSlotCaHvaS * N] = gate_ab<Real, true>(st[kSlotCaHvaS * N], r.sa, r.sb, P[BC_P_CAHVA_PHI], dt);
+        st[kSlotCaHvaU * N] = gate_ab<Real, true>(st[kSlotCaHvaU * N], r.ua, r.ub, P[BC_P_CAHVA_PHI], dt);
+      }
+      if (m & BC_M_CAV23) {
+        const Cav23Rates<Real> r(v);
+        st[kSlotCav23M * N] = gate_it(st[kSlotCav23M * N], r.minf, r.mtau, Real(1), dt);
+        st[kSlotCav23H * N] = gate_it(st[kSlotCav23H * N], r.hinf, r.htau, Real(1), dt);
+      }
+      if (m & BC_M_CAV32) {
+        const Cav32Rates<Real> r(v, P[BC_P_CAV32_VSH]);
+        st[kSlotCav32M * N] = gate_it(st[kSlotCav32M * N], r.minf, r.mtau, Real(kCav32PhiM), dt);
+        st[kSlotCav32H * N] = gate_it(st[kSlotCav32H * N], r.hinf, r.htau, Real(1), dt);
+      }
+    }
+    const Real eca =
+        (m & BC_M_CADET) ? Real(kNernstCa) * P[BC_P_CA_TEMP] * dlog(P[BC_P_CA_CO] / ci) : P[BC_P_ECA];
+    Real g = Real(0);
+    I += cerebellar_ca_current(st, N, P, m, v, eca, &g);
+    G += g;
+  }
 }
 
 template <typename Real>
@@ -531,7 +590,7 @@ __device__ __noinline__ void extra_channels(Real* st, int N, const Real* P, uint
     G += g;
     I += g * (P[BC_P_EK] - v);
   }
-  if (m & kCerebellarChannels) cerebellar_channels(st, N, P, m, v, dt, advance, G, I);
+  if (m & kCerebellarChannels) cerebellar_channels(st, N, P, m, v, ci, dt, advance, G, I);
   // Markov channels: the reference's independent-integration family, advanced
   // after the gates (cell.py:2204-2217), each at the new V and Ci
   if (m & (BC_M_NAV16 | BC_M_KCA22 | BC_M_KCA11)) {
@@ -587,6 +646,7 @@ __device__ __forceinline__ void node_mechanisms_loaded(const NodeStates<Real>& s
       Real ica = Real(0);
       if (m & BC_M_CAL) ica += P[BC_P_CAL_G] * calp * calp * calq * (eca - v_old);
       if (m & BC_M_CAT) ica += P[BC_P_CAT_G] * catp * catp * catq * (eca - v_old);
+      if (kExtra && (m & kCerebellarCaChannels)) ica += cerebellar_ca_current(st, N, P, m, v_old, eca, (Real*)nullptr);
       Real drive = ica * Real(kCaDrive) / P[BC_P_CA_D];
       drive = drive > Real(0) ? drive : Real(0);
       const Real tau = P[BC_P_CA_TAU];
@@ -790,6 +850,21 @@ __device__ __forceinline__ void steady_states(const Real* P, uint32_t m, Real* s
     st[kSlotHcn1Slow * N] = r.sinf;
   }
   if (m & BC_M_HCN1H) st[kSlotHcn1H * N] = Hcn1hRates<Real>(v).hinf;
+  if (m & BC_M_CAHVA) {
+    const CaHvaRates<Real> r(v);
+    st[kSlotCaHvaS * N] = r.sa / (r.sa + r.sb);
+    st[kSlotCaHvaU * N] = r.ua / (r.ua + r.ub);
+  }
+  if (m & BC_M_CAV23) {
+    const Cav23Rates<Real> r(v);
+    st[kSlotCav23M * N] = r.minf;
+    st[kSlotCav23H * N] = r.hinf;
+  }
+  if (m & BC_M_CAV32) {
+    const Cav32Rates<Real> r(v, P[BC_P_CAV32_VSH]);
+    st[kSlotCav32M * N] = r.minf;
+    st[kSlotCav32H * N] = r.hinf;
+  }
   if (m & (BC_M_NAV16 | BC_M_KCA22 | BC_M_KCA11)) {
     // Markov channels start at their stationary distribution (reset_steady_state)
     Real kf[17], kb[17];
@@ -816,7 +891,7 @@ __device__ __forceinline__ void write_row(const TileView<Real>& tv, int i, uint1
   if (pr == kBoundary) {
     tv.dr[i] = make_pair(dt * tv.diag0[i], Real(0));
   } else {
-    const Real invcm = tv.params[size_t(pr) * kParamStride + BC_P_INVCM];
+    const Real invcm = tv.params[size_t(pr) * tv.pstride + BC_P_INVCM];
     tv.dr[i] = make_pair(Real(1) + dt * (tv.diag0[i] + invcm * G), dt * invcm * I);
   }
 }
@@ -864,7 +939,7 @@ __device__ __forceinline__ void add_node_pulses(const TileView<Real>& tv, const 
     if (pr == kBoundary)
       tv.dr[i].y += dt * Real(p.amp);
     else
-      tv.dr[i].y += dt * tv.params[size_t(pr) * kParamStride + BC_P_INVCM] * Real(p.amp);
+      tv.dr[i].y += dt * tv.params[size_t(pr) * tv.pstride + BC_P_INVCM] * Real(p.amp);
   }
 }
 
@@ -1652,7 +1727,7 @@ __global__ void __launch_bounds__(kVar >= 2 ? BC_PORT_MAX_THREADS : 1024, kVar >
     Real G = Real(0), I = Real(0);
     if (pr != kBoundary) {
       const Real v = tv.v[i].x;
-      node_mechanisms<Real, kExtra>(tv.state + i, tv.N, tv.params + size_t(pr) * kParamStride, tv.mech[pr], v, v, dt,
+      node_mechanisms<Real, kExtra>(tv.state + i, tv.N, tv.params + size_t(pr) * tv.pstride, tv.mech[pr], v, v, dt,
                                     false, G, I);
     }
     const uint16_t sp = tv.spec[i];
@@ -1748,7 +1823,7 @@ __global__ void __launch_bounds__(kVar >= 2 ? BC_PORT_MAX_THREADS : 1024, kVar >
       const uint16_t pr = pr_cur;
       Real G = Real(0), I = Real(0);
       if (pr != kBoundary)
-        node_mechanisms_loaded<Real, kExtra>(cur, tv.state + i, tv.N, tv.params + size_t(pr) * kParamStride, tv.mech[pr],
+        node_mechanisms_loaded<Real, kExtra>(cur, tv.state + i, tv.N, tv.params + size_t(pr) * tv.pstride, tv.mech[pr],
                                              v_old, hi, dt, true, G, I);
       cur = nxt;
       pr_cur = pr_nxt;
@@ -1795,7 +1870,7 @@ __global__ void __launch_bounds__(kVar >= 2 ? BC_PORT_MAX_THREADS : 1024, kVar >
         if (r.field >= BC_PROBE_CURRENT) {
           const uint16_t pr = tv.pidx[r.node];
           const Pair<Real> vv = tv.v[r.node];
-          val = probe_current(tv.state + r.node, tv.N, tv.params + size_t(pr) * kParamStride, tv.mech[pr], vv.x + vv.y,
+          val = probe_current(tv.state + r.node, tv.N, tv.params + size_t(pr) * tv.pstride, tv.mech[pr], vv.x + vv.y,
                               r.field - BC_PROBE_CURRENT);
         } else {
           val = probe_state(tv.state + r.node, tv.N, r.field);
@@ -1882,7 +1957,7 @@ __global__ void __launch_bounds__(kLaneThreads, sizeof(Real) == 4 ? 8 : 4) lane_
       NodeStates<Real> st;
       load_states(tv.state + i, tv.N, tv.mech[pr], st);
       const Real v = tv.v[i].x;
-      node_mechanisms_loaded<Real, kExtra>(st, tv.state + i, tv.N, tv.params + size_t(pr) * kParamStride, tv.mech[pr],
+      node_mechanisms_loaded<Real, kExtra>(st, tv.state + i, tv.N, tv.params + size_t(pr) * tv.pstride, tv.mech[pr],
                                            v, v, dt, false, G, I);
     }
     write_row(tv, i, pr, dt, G, I);
@@ -2005,7 +2080,7 @@ __global__ void __launch_bounds__(kLaneThreads, sizeof(Real) == 4 ? 8 : 4) lane_
       const uint16_t pr = pr_cur;
       Real G = Real(0), I = Real(0);
       if (pr != kBoundary)
-        node_mechanisms_loaded<Real, kExtra>(cur, tv.state + i, tv.N, tv.params + size_t(pr) * kParamStride,
+        node_mechanisms_loaded<Real, kExtra>(cur, tv.state + i, tv.N, tv.params + size_t(pr) * tv.pstride,
                                              tv.mech[pr], v_old, hi, dt, true, G, I);
       cur = nxt;
       pr_cur = pr_nxt;
@@ -2089,7 +2164,7 @@ __global__ void reset_kernel(LaunchArgs a, const double* vinit, const int64_t* v
     tv.state[size_t(kSlotVLastLo) * tv.N + i] = Real(0);
     const uint16_t pr = tv.pidx[i];
     if (pr == kBoundary) continue;
-    const Real* P = tv.params + size_t(pr) * kParamStride;
+    const Real* P = tv.params + size_t(pr) * tv.pstride;
     steady_states(P, tv.mech[pr], tv.state + i, tv.N, v);
   }
 }

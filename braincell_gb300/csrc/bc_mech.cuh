@@ -350,6 +350,49 @@ struct Hcn1hRates {
   }
 };
 
+// CaHVA_MA2020_GoC (channel/calcium.py:4333; the GrC class, :4499, is identical):
+// s^2 u, alpha / beta exponentials.
+template <typename Real>
+struct CaHvaRates {
+  Real sa, sb, ua, ub;
+  __host__ __device__ __forceinline__ explicit CaHvaRates(Real v) {
+    sa = Real(0.04944) * aexp((v + Real(29.06)) / Real(15.873));
+    sb = Real(0.08298) * aexp((v + Real(18.66)) / Real(-25.641));
+    ua = Real(0.0013) * aexp((v + Real(48)) / Real(-18.183));
+    ub = Real(0.0013) * aexp((v + Real(48)) / Real(83.33));
+  }
+};
+
+// Cav2p3_MA2020_GoC (channel/calcium.py:4672): m^3 h, fixed time constants.
+template <typename Real>
+struct Cav23Rates {
+  Real minf, mtau, hinf, htau;
+  __host__ __device__ __forceinline__ explicit Cav23Rates(Real v) {
+    minf = Real(1) / (Real(1) + aexp((v + Real(48.5)) / Real(-3)));
+    hinf = Real(1) / (Real(1) + aexp((v + Real(53)) / Real(1)));
+    mtau = Real(50);
+    htau = Real(5);
+  }
+};
+
+// Cav3p2_RI2021_SC (channel/calcium.py:3636; the BC and PC classes inherit it): m^2 h
+// on V + V_sh; the h time constant carries its own 36 degC factor 3^1.2.
+template <typename Real>
+struct Cav32Rates {
+  Real minf, mtau, hinf, htau;
+  __host__ __device__ __forceinline__ Cav32Rates(Real v0, Real vsh) {
+    const Real v = v0 + vsh;
+    minf = Real(1) / (Real(1) + aexp(-(v + Real(54.8)) / Real(7.4)));
+    hinf = Real(1) / (Real(1) + aexp((v + Real(85.5)) / Real(7.18)));
+    mtau = Real(1.9) + Real(1) / (aexp((v + Real(37)) / Real(11.9)) + aexp(-(v + Real(131.6)) / Real(21)));
+    const Real phi_h = Real(3.7371928188465517);  // 3^((36 - 24) / 10)
+    htau = Real(13.7) + (Real(1942) + aexp((v + Real(164)) / Real(9.2))) / (Real(1) + aexp((v + Real(89.3)) / Real(3.7))) /
+                            phi_h;
+  }
+};
+// Cav3p2's m gate temperature factor, 5^((36 - 24) / 10)
+constexpr double kCav32PhiM = 6.898648307306074;
+
 // ---------------------------------------------------------------- Markov channels
 // The independent states of each scheme (channel/_base.py:677-1125: every state but
 // the dependent one, which is 1 - their sum), in the order they first appear in the
@@ -370,7 +413,13 @@ constexpr int kSlotKir23D = 57;
 constexpr int kSlotHcn1Fast = 58;
 constexpr int kSlotHcn1Slow = 59;
 constexpr int kSlotHcn1H = 60;
-constexpr int kNumSlotsCerebellar = 61;
+constexpr int kSlotCaHvaS = 61;
+constexpr int kSlotCaHvaU = 62;
+constexpr int kSlotCav23M = 63;
+constexpr int kSlotCav23H = 64;
+constexpr int kSlotCav32M = 65;
+constexpr int kSlotCav32H = 66;
+constexpr int kNumSlotsCerebellar = 67;
 constexpr int kMarkovMaxStates = 13;
 
 // A transition graph: states 0 .. ns-1 (dep is eliminated), pair k moves src -> dst

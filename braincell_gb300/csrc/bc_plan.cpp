@@ -63,7 +63,8 @@ constexpr int kDefaultLaneNodes = 10;
 constexpr int kDefaultNarrowLaneNodes = 1;
 
 constexpr uint32_t kMarkovBits = BC_M_NAV16 | BC_M_KCA22 | BC_M_KCA11;
-constexpr uint32_t kCerebellarBits = BC_M_KV34 | BC_M_KV43 | BC_M_KV11 | BC_M_KIR23 | BC_M_HCN1F | BC_M_HCN1H;
+constexpr uint32_t kCerebellarBits = BC_M_KV34 | BC_M_KV43 | BC_M_KV11 | BC_M_KIR23 | BC_M_HCN1F | BC_M_HCN1H |
+                                     BC_M_CAHVA | BC_M_CAV23 | BC_M_CAV32;
 
 namespace bc {
 
@@ -83,9 +84,10 @@ static void state_view(int32_t which, uint32_t* bit, int* slot) {
     *slot = kSlot[which];
     return;
   }
-  // Markov views 25 .. 50 and the cerebellar gates 51 .. 59 sit in slots 26 .. 60
+  // Markov views 25 .. 50 and the cerebellar gates 51 .. 65 sit in slots 26 .. 66
   static const uint32_t kCereb[BC_NSTATE_VIEW - BC_STATE_KV34_M] = {
-      BC_M_KV34, BC_M_KV34, BC_M_KV43, BC_M_KV43, BC_M_KV11, BC_M_KIR23, BC_M_HCN1F, BC_M_HCN1F, BC_M_HCN1H};
+      BC_M_KV34,  BC_M_KV34,  BC_M_KV43,  BC_M_KV43,  BC_M_KV11,  BC_M_KIR23, BC_M_HCN1F, BC_M_HCN1F,
+      BC_M_HCN1H, BC_M_CAHVA, BC_M_CAHVA, BC_M_CAV23, BC_M_CAV23, BC_M_CAV32, BC_M_CAV32};
   if (which >= BC_STATE_KV34_M)
     *bit = kCereb[which - BC_STATE_KV34_M];
   else
@@ -402,6 +404,7 @@ struct BuildCtx {
   int state_slots;
   int lane_nodes;  // nodes a lane walks serially in a warp slot
   int narrow_lane_nodes;  // the same in phases with fewer nodes than 32 x warps
+  int param_stride;       // reals per parameter record in the tile blobs
 };
 
 template <typename Real>
@@ -678,6 +681,7 @@ static bc_status build_tile(const BuildCtx& cx, const TileBuild& tb, int T, Tile
   const int64_t n_params = int64_t(cell_list.size()) * R;
   if (n_params >= 0xFFFF) return fail(BC_ERR_CAPACITY, "too many parameter records in one tile");
   TileDesc d{};
+  d.param_stride = cx.param_stride;
   size_t off = 0;
   d.off_v = int32_t(off);
   off = align16(off + 2 * N * rs);
@@ -701,7 +705,7 @@ static bc_status build_tile(const BuildCtx& cx, const TileBuild& tb, int T, Tile
   d.off_crec = int32_t(off);
   off = align16(off + N * 2);
   d.off_params = int32_t(off);
-  off = align16(off + size_t(n_params) * kParamStride * rs);
+  off = align16(off + size_t(n_params) * cx.param_stride * rs);
   d.off_mech = int32_t(off);
   off = align16(off + size_t(n_params) * 4);
   d.off_syn = int32_t(off);
@@ -781,7 +785,8 @@ static bc_status build_tile(const BuildCtx& cx, const TileBuild& tb, int T, Tile
     }
     for (int r = 0; r < R; ++r) {
       const int64_t rc = c * R + r;
-      for (int k = 0; k < BC_NPARAM; ++k) putr(d.off_params, (li * R + r) * kParamStride + k, s.region_params[rc * BC_NPARAM + k]);
+      for (int k = 0; k < std::min(BC_NPARAM, cx.param_stride - 1); ++k)
+        putr(d.off_params, (li * R + r) * cx.param_stride + k, s.region_params[rc * BC_NPARAM + k]);
       const uint32_t m = s.region_mech[rc];
       std::memcpy(b.data() + d.off_mech + (li * R + r) * 4, &m, 4);
     }
@@ -1345,8 +1350,9 @@ bc_status bc_plan_create(const bc_batch_spec* spec, const bc_plan_options* opts_
           BC_M_HCN, BC_M_AHP,   BC_M_NAHH, BC_M_KHH, BC_M_KM,            BC_M_NA | BC_M_NAHH | BC_M_NAV16,
           BC_M_KDR | BC_M_KLEAK | BC_M_AHP | BC_M_KHH | BC_M_KM | BC_M_KA1 | BC_M_KA2 | BC_M_KK2A | BC_M_KK2B | BC_M_KNI |
               BC_M_KCA22 | BC_M_KCA11 | BC_M_KV34 | BC_M_KV43 | BC_M_KV11 | BC_M_KIR23,
-          BC_M_CAL | BC_M_CAT,  BC_M_KA1,  BC_M_KA2, BC_M_KK2A, BC_M_KK2B, BC_M_KNI, BC_M_NAV16, BC_M_KCA22, BC_M_KCA11,
-          BC_M_KV34, BC_M_KV43, BC_M_KV11, BC_M_KIR23, BC_M_HCN1F, BC_M_HCN1H};
+          BC_M_CAL | BC_M_CAT | BC_M_CAHVA | BC_M_CAV23 | BC_M_CAV32,  BC_M_KA1,  BC_M_KA2, BC_M_KK2A, BC_M_KK2B, BC_M_KNI,
+          BC_M_NAV16, BC_M_KCA22, BC_M_KCA11, BC_M_KV34, BC_M_KV43, BC_M_KV11, BC_M_KIR23, BC_M_HCN1F, BC_M_HCN1H,
+          BC_M_CAHVA, BC_M_CAV23, BC_M_CAV32};
       const int32_t rg = cells[c].region[v];
       if (rg < 0 || !(s.region_mech[c * s.n_regions + rg] & cur_owner[field - BC_PROBE_CURRENT])) {
         delete p;
@@ -1605,7 +1611,8 @@ bc_status bc_plan_create(const bc_batch_spec* spec, const bc_plan_options* opts_
     if (tile_nodes - nn > 0) room.emplace(tile_nodes - nn, builds.size() - 1);
   }
   BuildCtx cx{&s, &cells, &sched, &cv_base, &cell_pulses, &cell_probes, &pulse_node, &probe_node, &cell_syns, &is_src,
-              &cell_ports, &port_pulse_ids, p->precision, S, p->lane_nodes, p->narrow_lane_nodes};
+              &cell_ports, &port_pulse_ids, p->precision, S, p->lane_nodes, p->narrow_lane_nodes,
+              p->extra ? kParamStride : kParamStrideCore};
   std::vector<TileOut> outs;
   outs.reserve(builds.size());
   // Packed tiles: tile_nodes sets how many CTAs share an SM (by the per-node

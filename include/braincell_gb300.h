@@ -73,10 +73,15 @@ typedef int32_t bc_status;
 #define BC_M_HCN1F (1u << 24)    /* channel/hyperpolarization_activated.py:675 HCN1_MA2020_GoC
                                     o_fast + o_slow, own E, Q10 1.5 on g                             */
 #define BC_M_HCN1H (1u << 25)    /* channel/hyperpolarization_activated.py:411 HCN1_MA2024_PC h, own E */
-#define BC_M_ALL 0x3FFFFFFu
+/* Cerebellar calcium channels: ohmic in E_Ca, their step-start current feeding a
+ * CalciumDetailed shell like CaL and CaT. */
+#define BC_M_CAHVA (1u << 26)    /* channel/calcium.py:4333 CaHVA_MA2020_GoC s^2 u, E_Ca              */
+#define BC_M_CAV23 (1u << 27)    /* channel/calcium.py:4672 Cav2p3_MA2020_GoC m^3 h, E_Ca             */
+#define BC_M_CAV32 (1u << 28)    /* channel/calcium.py:3636 Cav3p2_RI2021_SC m^2 h, E_Ca              */
+#define BC_M_ALL 0x1FFFFFFFu
 
 /* Per-region parameter record (double[BC_NPARAM]); index names below. */
-#define BC_NPARAM 90
+#define BC_NPARAM 96
 #define BC_P_INVCM 0      /* 1 / membrane capacitance, cm^2/uF                 */
 #define BC_P_VREST 1      /* voltage used by reset (mV)                        */
 #define BC_P_ENA 2        /* fixed reversal potentials (mV)                    */
@@ -167,6 +172,12 @@ typedef int32_t bc_status;
 #define BC_P_HCN1H_PHI 87   /* 3^((T - 37 degC) / 10)                               */
 #define BC_P_NAV16_ALFAC 88 /* (Oon / Con)^(1/4)                                    */
 #define BC_P_NAV16_EPS 89   /* epsilon, the open -> blocked rate (Nav1p1: 1e-12)   */
+#define BC_P_CAHVA_G 90
+#define BC_P_CAHVA_PHI 91   /* 3^((T - 20 degC) / 10)                               */
+#define BC_P_CAV23_G 92
+#define BC_P_CAV32_G 93
+#define BC_P_CAV32_VSH 94
+/* 95: reserved (0) */
 
 /* ------------------------------------------------------------------ batch spec */
 /*
@@ -328,9 +339,9 @@ const char* bc_last_error(void);
  * state view (BC_NSTATE_VIEW 25), bc_spike_state_download, bc_pulse_set_amp, the
  * workspace of bc_gru_backward (bit-reproducible gradients).  0.4.0: the Markov
  * channels (BC_M_NAV16 / KCA22 / KCA11, a 74-entry parameter record, state views
- * 25-50, BC_PROBE_CURRENT 64), lane tiles (bc_plan_options.lane_cell_nodes,
- * tile_order), the cerebellar HH channels (BC_M_KV34 .. HCN1H, a 90-entry parameter
- * record, state views 51-59). */
+ * 25-50), lane tiles (bc_plan_options.lane_cell_nodes, tile_order), the cerebellar
+ * HH and calcium channels (BC_M_KV34 .. CAV32, a 96-entry parameter record, state
+ * views 51-65, BC_PROBE_CURRENT 128). */
 #define BC_ABI_VERSION 400
 int32_t bc_version(void);
 /* Fill opts with defaults. */
@@ -425,11 +436,17 @@ bc_status bc_check(bc_plan_t plan, void* stream);
 #define BC_STATE_HCN1F_FAST 57
 #define BC_STATE_HCN1F_SLOW 58
 #define BC_STATE_HCN1H_H 59
-#define BC_NSTATE_VIEW 60
+#define BC_STATE_CAHVA_S 60
+#define BC_STATE_CAHVA_U 61
+#define BC_STATE_CAV23_M 62
+#define BC_STATE_CAV23_H 63
+#define BC_STATE_CAV32_M 64
+#define BC_STATE_CAV32_H 65
+#define BC_NSTATE_VIEW 66
 /* Current probes (mech/_point.py CurrentProbe, _multi_compartment/probes.py:184-258):
    probe_field = BC_PROBE_CURRENT + one of the codes below records that current
    density (uA/cm^2, outward negative as g (E - V)) after the step.             */
-#define BC_PROBE_CURRENT 64
+#define BC_PROBE_CURRENT 128
 #define BC_CUR_IL 0
 #define BC_CUR_KLEAK 1
 #define BC_CUR_NA 2      /* Na_Ba2002   */
@@ -458,7 +475,10 @@ bc_status bc_check(bc_plan_t plan, void* stream);
 #define BC_CUR_KIR23 25  /* Kir2p3_MA2020_GrC */
 #define BC_CUR_HCN1F 26  /* HCN1_MA2020_GoC   */
 #define BC_CUR_HCN1H 27  /* HCN1_MA2024_PC    */
-#define BC_NCUR 28
+#define BC_CUR_CAHVA 28  /* CaHVA_MA2020_GoC  */
+#define BC_CUR_CAV23 29  /* Cav2p3_MA2020_GoC */
+#define BC_CUR_CAV32 30  /* Cav3p2_RI2021_SC  */
+#define BC_NCUR 31
 bc_status bc_state_download(bc_plan_t plan, int32_t which, double* out /* [n_cv] */, void* stream);
 /* Set the amplitude (nA) of every current-clamp pulse of the batch spec, in spec
  * order (amp_nA[n_pulses]); times and locations are unchanged.  Takes effect from

@@ -120,6 +120,9 @@ CHANNEL_DEFAULTS.update({
     "Kir2p3_MA2020_GrC": dict(g_max=0.9, temp=_c2k(30.0)),  # potassium.py:5334
     "HCN1_MA2020_GoC": dict(g_max=0.05, E=-20.0, temp=_c2k(22.0)),  # hyperpolarization_activated.py:675
     "HCN1_MA2024_PC": dict(g_max=0.1, E=-34.4, temp=_c2k(23.0)),  # hyperpolarization_activated.py:411
+    "CaHVA_MA2020_GoC": dict(g_max=0.46, temp=_c2k(30.0)),  # calcium.py:4333
+    "Cav2p3_MA2020_GoC": dict(g_max=0.0, temp=_c2k(34.0)),  # calcium.py:4672
+    "Cav3p2_RI2021_SC": dict(g_max=8.0e-4, V_sh=0.0, temp=_c2k(36.0)),  # calcium.py:3636
 })
 # cell-type variants that run their base class's kinetics, with their own defaults
 # where they differ (each class body is the base's: potassium.py, hyperpolarization_activated.py)
@@ -132,6 +135,8 @@ _VARIANTS = {
                                               "Kv1p1_RI2021_SC")},
     **{v: ("Kir2p3_MA2020_GrC", {}) for v in ("Kir2p3_MA2024_PC", "Kir2p3_MA2025_BC", "Kir2p3_RI2021_SC")},
     **{v: ("HCN1_MA2024_PC", {}) for v in ("HCN1_MA2025_BC", "HCN1_RI2021_SC")},
+    "CaHVA_MA2020_GrC": ("CaHVA_MA2020_GoC", {}),
+    **{v: ("Cav3p2_RI2021_SC", {}) for v in ("Cav3p2_MA2025_BC", "Cav3p2_MA2024_PC")},
 }
 
 
@@ -476,6 +481,20 @@ def rates(name: str, V, p: dict, Ci=None):
         vh, v1 = -90.3 - 9.3, -68.0 - 9.3
         return {"h": ("it", 1.0 / (1.0 + np.exp((V - vh) / 9.67)),
                       1.0 / (0.0018 * (np.exp((V - v1) / -22.0) + np.exp((V - v1) / 7.14))))}
+    if name == "CaHVA_MA2020_GoC":  # calcium.py:4333
+        return {"s": ("ab", 0.04944 * np.exp((V - -29.06) / 15.873), 0.08298 * np.exp((V - -18.66) / -25.641)),
+                "u": ("ab", 0.0013 * np.exp((V - -48.0) / -18.183), 0.0013 * np.exp((V - -48.0) / 83.33))}
+    if name == "Cav2p3_MA2020_GoC":  # calcium.py:4672
+        one = np.ones_like(V)
+        return {"m": ("it", 1.0 / (1.0 + np.exp((V + 48.5) / -3.0)), 50.0 * one),
+                "h": ("it", 1.0 / (1.0 + np.exp((V + 53.0) / 1.0)), 5.0 * one)}
+    if name == "Cav3p2_RI2021_SC":  # calcium.py:3636, on V + V_sh; tau_h carries 3^((36 - 24) / 10)
+        Vs = V + p["V_sh"]
+        phi_h = 3.0 ** ((36.0 - 24.0) / 10.0)
+        term = (1942.0 + np.exp((Vs + 164.0) / 9.2)) / (1.0 + np.exp((Vs + 89.3) / 3.7))
+        return {"m": ("it", 1.0 / (1.0 + np.exp(-(Vs + 54.8) / 7.4)),
+                      1.9 + 1.0 / (np.exp((Vs + 37.0) / 11.9) + np.exp(-(Vs + 131.6) / 21.0))),
+                "h": ("it", 1.0 / (1.0 + np.exp((Vs + 85.5) / 7.18)), 13.7 + term / phi_h)}
     if name in ("KM_RI2021_SC", "KM_MA2020_GoC", "KM_MA2020_GrC"):  # potassium.py:1735-1748, :4553-4567, :5317-5331
         a = 0.0033 * np.exp((V + 30.0) / 40.0)
         b = 0.0033 * np.exp((V + 30.0) / -20.0)
@@ -509,6 +528,9 @@ _GATES = {  # (gate, power, phi-key)
     "Kir2p3_MA2020_GrC": (("d", 1, "phi"),),
     "HCN1_MA2020_GoC": (("o_fast", 1, "phi"), ("o_slow", 1, "phi")),
     "HCN1_MA2024_PC": (("h", 1, "phi"),),
+    "CaHVA_MA2020_GoC": (("s", 2, "phi"), ("u", 1, "phi")),
+    "Cav2p3_MA2020_GoC": (("m", 3, "phi"), ("h", 1, "phi")),
+    "Cav3p2_RI2021_SC": (("m", 2, "phi_m"), ("h", 1, "phi")),
 }
 _ION_OF = {"Na_Ba2002": "na", "KDR_Ba2002": "k", "CaL_IS2008": "ca", "CaT_HM1992": "ca",
            "K_Leak": "k", "AHP_De1994": "k", "Na_HH1952": "na", "K_HH1952": "k", "KM_RI2021_SC": "k",
@@ -516,7 +538,8 @@ _ION_OF = {"Na_Ba2002": "na", "KDR_Ba2002": "k", "CaL_IS2008": "ca", "CaT_HM1992
            "KM_MA2020_GoC": "k", "KM_MA2020_GrC": "k", "KK2A_HM1992": "k", "KK2B_HM1992": "k",
            "KNI_Ya1989": "k", "Nav1p6_MA2020_GoC": "na", "Kca2p2_MA2020_GoC": "k", "Kca1p1_MA2020_GoC": "k",
            "Kv3p4_MA2020_GoC": "k", "Kv4p3_MA2020_GoC": "k", "Kv1p1_MA2020_GoC": "k", "Kir2p3_MA2020_GrC": "k",
-           "Nav1p1_MA2025_BC": "na", "Nav1p1_RI2021_SC": "na"}
+           "Nav1p1_MA2025_BC": "na", "Nav1p1_RI2021_SC": "na",
+           "CaHVA_MA2020_GoC": "ca", "Cav2p3_MA2020_GoC": "ca", "Cav3p2_RI2021_SC": "ca"}
 # channels with their own reversal potential (HHTypedNeuron root, not an ion)
 _OWN_E = ("HCN_HM1992", "HCN1_MA2020_GoC", "HCN1_MA2024_PC")
 
@@ -556,6 +579,13 @@ def _resolve(table: dict, decl) -> dict:
         p["gbar_phi"] = 1.5 ** ((p["temp"] - _c2k(23.0)) / 10.0)
     elif name == "HCN1_MA2024_PC":  # Gate q10 3 at 37 degC
         p["phi"] = 3.0 ** ((p["temp"] - _c2k(37.0)) / 10.0)
+    elif name == "CaHVA_MA2020_GoC":  # Gates q10 3 at 20 degC
+        p["phi"] = 3.0 ** ((p["temp"] - _c2k(20.0)) / 10.0)
+    elif name == "Cav2p3_MA2020_GoC":  # Gates without q10 or phi: factor 1
+        p["phi"] = 1.0
+    elif name == "Cav3p2_RI2021_SC":  # Gate("m", phi=5^((36 - 24) / 10)); h: 1
+        p["phi_m"] = 5.0 ** ((36.0 - 24.0) / 10.0)
+        p["phi"] = 1.0
     return p
 
 

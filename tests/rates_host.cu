@@ -42,6 +42,9 @@ extern "C" int bc_test_rates(int which, const double* v, int n, const double* pr
       case 16: { const Kir23Rates<double> r(x); o[0] = r.a; o[1] = r.b; break; }
       case 17: { const Hcn1fRates<double> r(x); o[0] = r.finf; o[1] = r.ftau; o[2] = r.sinf; o[3] = r.stau; break; }
       case 18: { const Hcn1hRates<double> r(x); o[0] = r.hinf; o[1] = r.htau; break; }
+      case 19: { const CaHvaRates<double> r(x); o[0] = r.sa; o[1] = r.sb; o[2] = r.ua; o[3] = r.ub; break; }
+      case 20: { const Cav23Rates<double> r(x); o[0] = r.minf; o[1] = r.mtau; o[2] = r.hinf; o[3] = r.htau; break; }
+      case 21: { const Cav32Rates<double> r(x, prm[0]); o[0] = r.minf; o[1] = r.mtau; o[2] = r.hinf; o[3] = r.htau; break; }
       default: return -1;
     }
   }

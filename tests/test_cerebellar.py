@@ -1,12 +1,13 @@
-"""Cerebellar HH channels of the MA2020 / MA2024 / MA2025 / RI2021 models: Kv3p4, Kv4p3,
-Kv1p1, Kir2p3 and the two HCN1 forms, with the cell-type variants that share their
-kinetics.
+"""Cerebellar channels of the MA2020 / MA2024 / MA2025 / RI2021 models: Kv3p4, Kv4p3,
+Kv1p1, Kir2p3, the two HCN1 forms and the calcium channels CaHVA, Cav2p3 and Cav3p2,
+with the cell-type variants that share their kinetics.
 
 CPU: the published known answers of the reference docstrings (Kv1p1's n_inf = 1/2 at
 -45 mV and the half-maximal n^4 near -29.9 mV, channel/potassium.py:4570), and the
 variants' parameter records against their base class's.  GPU: a soma / dendrite cell
 carrying all six kernels against the float64 oracle (FP64 at 1e-8 mV over the whole run,
-gate and current probes, spikes) and FP32 against FP64.
+gate and current probes, spikes) and FP32 against FP64; a dendrite with the three
+calcium channels on a CalciumDetailed shell (their step-start current drives Ci).
 """
 
 import numpy as np
@@ -14,8 +15,8 @@ import pytest
 
 from braincell_gb300 import Branch, Cell, Morphology
 from braincell_gb300 import _abi, catalogue
-from braincell_gb300.mech import (AllRegion, CableProperty, Channel, CurrentClamp, CurrentProbe, CVPerBranch,
-                                  MechanismProbe, RootLocation, StateProbe, branch_in)
+from braincell_gb300.mech import (AllRegion, CableProperty, Channel, CurrentClamp, CurrentProbe, CVPerBranch, Ion,
+                                  MechanismProbe, RootLocation, StateProbe, at, branch_in)
 from oracle import staggered as O
 
 DT = 0.025
@@ -69,7 +70,7 @@ def _cell(precision="f64"):
             MechanismProbe("ka", "a", name="kv43_a"), MechanismProbe("hcn_f", "o_slow", name="hcn_slow"),
             CurrentProbe(mechanism="ka", name="i_ka"), CurrentProbe(mechanism="hcn_f", name="i_hcn"),
             CurrentProbe(ion="k", name="i_k"))
-    c.place(RootLocation(0.5), StateProbe(name="v2"))
+    c.place(at(1, 0.5), StateProbe(name="v_dend"))
     return c
 
 
@@ -120,3 +121,53 @@ def test_cerebellar_cell_f32_meets_the_bar(native_lib, cuda_device):
     assert np.abs(t32[:onset] - t64[:onset]).max() <= 1e-3
     assert len(s32) == len(s64) >= 2
     assert np.abs(np.asarray(s32) - np.asarray(s64)).max() <= 0.05
+
+
+def _ca_cell(precision="f64"):
+    soma = Branch.from_lengths(lengths=[20.0], radii=[10.0, 10.0], type="soma")
+    m = Morphology.from_root(soma, name="soma")
+    m.attach(parent="soma", child_branch=Branch.from_lengths(lengths=[150.0], radii=[1.0, 0.6], type="dendrite"),
+             child_name="d0")
+    c = Cell(m, cv_policy=CVPerBranch(5), precision=precision)
+    c.paint(AllRegion(), CableProperty(), Channel("IL", g_max=0.1, E=-65.0))
+    c.paint(branch_in("type", "soma"), Channel("Na_Ba2002", g_max=120.0), Channel("KDR_Ba2002", g_max=40.0))
+    c.paint(branch_in("type", "dendrite"), Channel("CaHVA_MA2020_GrC", g_max=0.5),
+            Channel("Cav2p3_MA2020_GoC", g_max=0.3), Channel("Cav3p2_MA2024_PC", g_max=0.4, V_sh=5.0),
+            Channel("Kv4p3_MA2020_GoC", g_max=0.5),
+            Ion("CalciumDetailed", C_rest=5e-5, tau=20.0, d=0.5, Ci_initializer=5e-5))
+    c.place(RootLocation(0.5), CurrentClamp(delay=2.0, durations=20.0, amplitudes=0.4), StateProbe(name="v"))
+    c.place(at(1, 0.5), StateProbe(name="v_dend"), MechanismProbe("CalciumDetailed", "Ci", name="ci"),
+            MechanismProbe("Cav3p2_MA2024_PC", "h", name="cav32_h"), CurrentProbe(ion="ca", name="i_ca"),
+            CurrentProbe(mechanism="CaHVA_MA2020_GrC", name="i_hva"))
+    return c
+
+
+def test_calcium_channel_probe_lowering():
+    b = _ca_cell().batch()
+    base = _abi.BC_PROBE_CURRENT
+    np.testing.assert_array_equal(b.probe_field, [0, 0, _abi.BC_STATE_CA_CI, _abi.BC_STATE_CAV32_H,
+                                                  base + _abi.BC_CUR_ION_CA, base + _abi.BC_CUR_CAHVA])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision,tol_v,tol_ci", [("f64", 1e-8, 1e-12), ("f32", None, 1e-6)])
+def test_calcium_channels_drive_the_shell_like_the_oracle(native_lib, cuda_device, precision, tol_v, tol_ci):
+    from braincell_gb300.runtime import Plan
+
+    n = 1000
+    p = Plan(_ca_cell(precision).batch(), precision=precision, record_every=1, device=cuda_device)
+    p.run(n, DT)
+    gpu = p.traces()
+    p.close()
+    ref, osp = O.OracleCell(_ca_cell()).run(DT, n)
+    ref = ref[0]
+    assert ref[2].max() > 2.0 * ref[2][0]  # the shell fills from the dendritic channels
+    if precision == "f64":
+        np.testing.assert_allclose(gpu[:2], ref[:2], rtol=0, atol=tol_v)
+        np.testing.assert_allclose(gpu[3], ref[3], rtol=0, atol=1e-10)
+        np.testing.assert_allclose(gpu[4:], ref[4:], rtol=1e-8, atol=1e-9)
+        np.testing.assert_allclose(gpu[2], ref[2], rtol=1e-9, atol=tol_ci)
+    else:
+        onset = int(np.nonzero(np.diff(ref[0]) / DT > 10.0)[0][0]) + 1
+        assert np.abs(gpu[0][:onset] - ref[0][:onset]).max() <= 1e-3
+        np.testing.assert_allclose(gpu[2][:onset], ref[2][:onset], rtol=1e-5, atol=tol_ci)

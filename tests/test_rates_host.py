@@ -25,6 +25,7 @@ CASES = {
     10: ("KK2A_HM1992", ("V_sh",)), 11: ("KK2B_HM1992", ("V_sh",)), 12: ("KNI_Ya1989", ("V_sh", "tau_max")),
     13: ("Kv3p4_MA2020_GoC", ()), 14: ("Kv4p3_MA2020_GoC", ()), 15: ("Kv1p1_MA2020_GoC", ()),
     16: ("Kir2p3_MA2020_GrC", ()), 17: ("HCN1_MA2020_GoC", ()), 18: ("HCN1_MA2024_PC", ()),
+    19: ("CaHVA_MA2020_GoC", ()), 20: ("Cav2p3_MA2020_GoC", ()), 21: ("Cav3p2_RI2021_SC", ("V_sh",)),
 }
 
 
