@@ -465,11 +465,15 @@ def surrogate_leg(a, descs, local, sid, stream, plain_ms):
     for _ in range(a.warmup):
         runner.run(a.sim_steps, DT)
     torch.cuda.synchronize()
-    walls, res = [], None
+    walls, res, lines = [], None, []
     with ClockSampler(local) as clocks:
         for _ in range(max(a.steps, 5)):
             res = runner.run(a.sim_steps, DT)
             walls.append(res.wall_ms)
+            fb = res.timeline.get("fallbacks", [])
+            lines.append({"reduced_ms": round(res.timeline.get("reduced_ms", 0.0), 1),
+                          "fallback_end_ms": round(max((f[2] for f in fb), default=0.0), 1),
+                          "batches": [[f[0], f[1], round(f[2], 1)] for f in fb]})
     ms = float(np.median(walls))
     info = runner.plan.info
     out = {"value": runner.full_cv * a.sim_steps / (ms * 1e-3),
@@ -480,6 +484,10 @@ def surrogate_leg(a, descs, local, sid, stream, plain_ms):
            "tiles": info["n_tiles"], "gpu_launches_per_step": res.launches,
            "clocks": clocks.summary(), "setup_s": round(t_setup, 2),
            "runs": len(walls), "ms_all_runs": [round(w, 1) for w in walls],
+           "timeline": {"runs": lines,
+                        "what": "device clock from the reset: end of the last reduced launch, end of the last "
+                                "fallback solve, and per fallback batch [steps done when its flags were read, "
+                                "cells, end ms]"},
            "timed": "median over the runs, host clock: reset + the reduced cells with GRU ports launch by launch, "
                     "flags read after each launch, the full solve of newly flagged cells from t = 0 on "
                     "high-priority side streams (plans built inside the timed region), until every stream is done"}

@@ -412,6 +412,9 @@ class SurrogateRun:
     spikes: list                  # per cell: soma spike times (ms), fallback cells from the full solve
     traces: np.ndarray | None = None  # [n_cells, T] soma voltage when record_every > 0
     full_cells: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int64))  # kept at full morphology
+    # device clock from the reset: "reduced_ms" at the end of the last reduced launch,
+    # "fallbacks" one (steps seen when the flags were read, cells, end ms) per batch
+    timeline: dict = field(default_factory=dict)
 
     @property
     def fallback_rate(self) -> float:
@@ -515,6 +518,8 @@ class SurrogateRunner:
         watch = self.fallback and self.n_ports > 0
         t0 = time.perf_counter()
         plan.reset(stream=sid)
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev0.record(main)
         if self.full_plan is not None:
             # the full-morphology cells of a mixed population: the whole run, enqueued
             # at once on their own stream, beside the reduced launches
@@ -541,15 +546,17 @@ class SurrogateRunner:
             k = min(lead.pop(0) if lead else spl, n_steps - done)
             plan.run(k, dt, stream=sid, check=False)
             done += k
-            ev = torch.cuda.Event()
+            ev = torch.cuda.Event(enable_timing=True)
             ev.record(main)
-            queued.append(ev)
+            queued.append((ev, done))
 
         enqueue()
         if done < n_steps:
             enqueue()
+        last_ev = None
         while queued:
-            ev = queued.pop(0)
+            ev, seen = queued.pop(0)
+            last_ev = ev
             flags = None
             if watch:
                 self._flag_stream.wait_event(ev)
@@ -568,14 +575,19 @@ class SurrogateRunner:
                     side = torch.cuda.Stream(self.device, priority=-1)
                     fp = self._fallback_plan(self.red_idx[new])
                     fp.run(n_steps, dt, stream=int(side.cuda_stream), check=False)
-                    fallbacks.append((new, fp, side))
+                    fe = torch.cuda.Event(enable_timing=True)
+                    fe.record(side)
+                    fallbacks.append((new, fp, side, seen, fe))
         plan.check(stream=sid)
-        for _, fp, side in fallbacks:
+        for _, fp, side, _, _ in fallbacks:
             fp.check(stream=int(side.cuda_stream))
         if self.full_plan is not None:
             self.full_plan.check(stream=int(self._full_stream.cuda_stream))
         torch.cuda.synchronize(self.device)
         wall = (time.perf_counter() - t0) * 1e3
+        timeline = {"reduced_ms": ev0.elapsed_time(last_ev) if last_ev is not None else 0.0,
+                    "fallbacks": [(int(seen), int(cells.size), ev0.elapsed_time(fe))
+                                  for cells, _, _, seen, fe in fallbacks]}
         n = len(self.descs)
         spikes = [None] * n
         traces = None
@@ -598,7 +610,7 @@ class SurrogateRunner:
                 spikes[i] = fsp[j]
                 if traces is not None:
                     traces[i] = ftr[j]
-        for cells, fp, side in fallbacks:
+        for cells, fp, side, _, _ in fallbacks:
             launches += 1 + -(-n_steps // int(fp.info["steps_per_launch"])) * int(fp.info["n_launch_classes"])
             fsp = fp.spikes(stream=int(side.cuda_stream))
             ftr = fp.traces(stream=int(side.cuda_stream)) if self.record_every else None
@@ -609,7 +621,7 @@ class SurrogateRunner:
             fp.close()
         return SurrogateRun(reduced_cv=int(plan.n_cv), full_cv=self.full_cv, n_ports=self.n_ports,
                             fallback_cells=self.red_idx[np.nonzero(flagged)[0]], wall_ms=wall, launches=launches,
-                            spikes=list(spikes), traces=traces, full_cells=self.full_idx)
+                            spikes=list(spikes), traces=traces, full_cells=self.full_idx, timeline=timeline)
 
     def close(self) -> None:
         self.plan.close()

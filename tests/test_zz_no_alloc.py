@@ -64,7 +64,9 @@ def _hh_batch():
             Channel("Kca1p1_MA2020_GoC", g_max=1.0),  # and the Markov and cerebellar channels' state views
             Channel("Kv3p4_MA2020_GoC", g_max=0.5), Channel("Kv4p3_MA2020_GoC", g_max=0.5),
             Channel("Kv1p1_MA2020_GoC", g_max=0.2), Channel("Kir2p3_MA2020_GrC", g_max=0.2),
-            Channel("HCN1_MA2020_GoC", g_max=0.05), Channel("HCN1_MA2024_PC", g_max=0.05))
+            Channel("HCN1_MA2020_GoC", g_max=0.05), Channel("HCN1_MA2024_PC", g_max=0.05),
+            Channel("CaHVA_MA2020_GoC", g_max=0.05), Channel("Cav2p3_MA2020_GoC", g_max=0.05),
+            Channel("Cav3p2_RI2021_SC", g_max=0.05))
     return lower_cell(c)
 
 
