@@ -472,8 +472,8 @@ def surrogate_leg(a, descs, local, sid, stream, plain_ms):
             walls.append(res.wall_ms)
             fb = res.timeline.get("fallbacks", [])
             lines.append({"reduced_ms": round(res.timeline.get("reduced_ms", 0.0), 1),
-                          "fallback_end_ms": round(max((f[2] for f in fb), default=0.0), 1),
-                          "batches": [[f[0], f[1], round(f[2], 1)] for f in fb]})
+                          "fallback_end_ms": round(max((f[3] for f in fb), default=0.0), 1),
+                          "batches": [[f[0], f[1], round(f[2], 1), round(f[3], 1)] for f in fb]})
     ms = float(np.median(walls))
     info = runner.plan.info
     out = {"value": runner.full_cv * a.sim_steps / (ms * 1e-3),
@@ -487,7 +487,7 @@ def surrogate_leg(a, descs, local, sid, stream, plain_ms):
            "timeline": {"runs": lines,
                         "what": "device clock from the reset: end of the last reduced launch, end of the last "
                                 "fallback solve, and per fallback batch [steps done when its flags were read, "
-                                "cells, end ms]"},
+                                "cells, start ms, end ms]"},
            "timed": "median over the runs, host clock: reset + the reduced cells with GRU ports launch by launch, "
                     "flags read after each launch, the full solve of newly flagged cells from t = 0 on "
                     "high-priority side streams (plans built inside the timed region), until every stream is done"}

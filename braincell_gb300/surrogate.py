@@ -413,7 +413,7 @@ class SurrogateRun:
     traces: np.ndarray | None = None  # [n_cells, T] soma voltage when record_every > 0
     full_cells: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int64))  # kept at full morphology
     # device clock from the reset: "reduced_ms" at the end of the last reduced launch,
-    # "fallbacks" one (steps seen when the flags were read, cells, end ms) per batch
+    # "fallbacks" one (steps seen when the flags were read, cells, start ms, end ms) per batch
     timeline: dict = field(default_factory=dict)
 
     @property
@@ -574,10 +574,11 @@ class SurrogateRunner:
                     # full solve runs at its own step latency
                     side = torch.cuda.Stream(self.device, priority=-1)
                     fp = self._fallback_plan(self.red_idx[new])
+                    fs, fe = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                    fs.record(side)
                     fp.run(n_steps, dt, stream=int(side.cuda_stream), check=False)
-                    fe = torch.cuda.Event(enable_timing=True)
                     fe.record(side)
-                    fallbacks.append((new, fp, side, seen, fe))
+                    fallbacks.append((new, fp, side, seen, (fs, fe)))
         plan.check(stream=sid)
         for _, fp, side, _, _ in fallbacks:
             fp.check(stream=int(side.cuda_stream))
@@ -586,7 +587,7 @@ class SurrogateRunner:
         torch.cuda.synchronize(self.device)
         wall = (time.perf_counter() - t0) * 1e3
         timeline = {"reduced_ms": ev0.elapsed_time(last_ev) if last_ev is not None else 0.0,
-                    "fallbacks": [(int(seen), int(cells.size), ev0.elapsed_time(fe))
+                    "fallbacks": [(int(seen), int(cells.size), ev0.elapsed_time(fe[0]), ev0.elapsed_time(fe[1]))
                                   for cells, _, _, seen, fe in fallbacks]}
         n = len(self.descs)
         spikes = [None] * n
