@@ -57,7 +57,9 @@ region cannot carry both classes of one pair.
   (ion/potassium.py:151), ``CalciumFixed`` E 120 (ion/calcium.py:187) -- the
   defaults used when no ion is painted (_compute/ions.py:107-113);
   ``CalciumDetailed`` (ion/calcium.py:286: temp 36 degC, d 1 um, tau 5 ms,
-  C_rest 2.4e-4 mM, Co 2 mM, Ci0 2.4e-4 mM).
+  C_rest 2.4e-4 mM, Co 2 mM, Ci0 2.4e-4 mM); ``SodiumInitNernst``,
+  ``PotassiumInitNernst`` and ``CalciumInitNernst`` (ion/_base.py:261: fixed Ci / Co,
+  E = R T / (z F) ln(Co / Ci) set once, temp 36 degC and the family's Ci, Co, valence).
 
 The gate temperature factor is ``phi = q10 ** ((temp - temp_ref) / 10 K)``
 (channel/_base.py:517-532).
@@ -171,7 +173,25 @@ IONS: dict[str, dict[str, float]] = {
     "CalciumDetailed": {
         "temp": T36, "d": 1.0, "tau": 5.0, "C_rest": 2.4e-4, "Co": 2.0, "Ci_initializer": 2.4e-4,
     },
+    # fixed Ci / Co with E set once from Nernst at init and reset (ion/_base.py:261-360);
+    # the family defaults Ci, Co, valence: ion/sodium.py:82-84, ion/potassium.py:83-85,
+    # ion/calcium.py:120-122, temp 36 C (ion/sodium.py:235)
+    "SodiumInitNernst": {"temp": T36, "Ci": 10.0, "Co": 140.0, "valence": 1.0},
+    "PotassiumInitNernst": {"temp": T36, "Ci": 54.4, "Co": 2.5, "valence": 1.0},
+    "CalciumInitNernst": {"temp": T36, "Ci": 5e-5, "Co": 2.0, "valence": 2.0},
 }
+# the reversal-potential slot each fixed-E ion family sets
+_E_SLOT = {"SodiumFixed": _abi.BC_P_ENA, "PotassiumFixed": _abi.BC_P_EK, "CalciumFixed": _abi.BC_P_ECA,
+           "SodiumInitNernst": _abi.BC_P_ENA, "PotassiumInitNernst": _abi.BC_P_EK,
+           "CalciumInitNernst": _abi.BC_P_ECA}
+
+
+def nernst_mV(temp: float, valence: float, Co: float, Ci: float) -> float:
+    """R T / (z F) ln(Co / Ci) in mV, the stored E of an InitNernst ion
+    (ion/_base.py:350-356)."""
+    if not (Co > 0.0 and Ci > 0.0) or valence == 0.0:
+        raise ValueError(f"Nernst potential needs Co > 0, Ci > 0 and valence != 0 (got {Co}, {Ci}, {valence}).")
+    return 1e3 * GAS_R * float(temp) / (float(valence) * FARADAY) * float(np.log(Co / Ci))
 
 
 # classes whose record is (g_max, V_sh, phi_p, phi_q) at a base index: mechanism bit, base
@@ -221,12 +241,8 @@ def region_record(mechs, cable: CableProperty) -> tuple[int, np.ndarray]:
             if name not in IONS:
                 raise ValueError(f"Unsupported ion class {name!r}; supported: {sorted(IONS)}.")
             p = _params(IONS, name, decl)
-            if name == "SodiumFixed":
-                rec[_abi.BC_P_ENA] = p["E"]
-            elif name == "PotassiumFixed":
-                rec[_abi.BC_P_EK] = p["E"]
-            elif name == "CalciumFixed":
-                rec[_abi.BC_P_ECA] = p["E"]
+            if name in _E_SLOT:
+                rec[_E_SLOT[name]] = p["E"] if "E" in p else nernst_mV(p["temp"], p["valence"], p["Co"], p["Ci"])
             else:
                 bits |= _abi.BC_M_CADET
                 rec[_abi.BC_P_CA_D] = p["d"]

@@ -151,6 +151,11 @@ ION_DEFAULTS = {
     "PotassiumFixed": dict(E=-95.0),
     "CalciumFixed": dict(E=120.0),
     "CalciumDetailed": dict(temp=_c2k(36.0), d=1.0, tau=5.0, C_rest=2.4e-4, Co=2.0, Ci_initializer=2.4e-4),
+    # InitNernst ions: fixed Ci / Co, E stored from Nernst (ion/_base.py:350-356) with the
+    # family defaults (ion/sodium.py:82-84, ion/potassium.py:83-85, ion/calcium.py:120-122)
+    "SodiumInitNernst": dict(temp=_c2k(36.0), Ci=10.0, Co=140.0, valence=1),
+    "PotassiumInitNernst": dict(temp=_c2k(36.0), Ci=54.4, Co=2.5, valence=1),
+    "CalciumInitNernst": dict(temp=_c2k(36.0), Ci=5e-5, Co=2.0, valence=2),
 }
 _CA_FIXED_CI = 5e-5  # Calcium.default_Ci (ion/calcium.py:120)
 
@@ -849,6 +854,10 @@ class OracleCell:
                         self.E_k[pts] = p["E"]
                     elif name == "CalciumFixed":
                         self.E_ca_fixed[pts] = p["E"]
+                    elif name.endswith("InitNernst"):
+                        e = 1e3 * GAS_R * p["temp"] / (p["valence"] * FARADAY) * np.log(p["Co"] / p["Ci"])
+                        {"Sodium": self.E_na, "Potassium": self.E_k, "Calcium": self.E_ca_fixed}[
+                            name[: -len("InitNernst")]][pts] = e
                     elif name == "CalciumDetailed":
                         if self.ca_dyn is None:
                             self.ca_dyn = {k: np.zeros(n) for k in ("d", "tau", "C_rest", "Co", "temp", "Ci0")}
