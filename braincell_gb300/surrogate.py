@@ -434,11 +434,13 @@ class SurrogateRunner:
 
     def __init__(self, descs, model: SurrogateModel | None, *, precision: str = "f32", record_every: int = 0,
                  device: int = 0, plan_kw: dict | None = None, fallback: bool = True, full_cells=None,
-                 full_plan_kw: dict | None = None):
+                 full_plan_kw: dict | None = None, fallback_kw: dict | None = None, fallback_priority: int = -1):
         """``full_cells``: indices of cells that keep their full morphology for the
         whole run (a mixed population); they run from t = 0 in a plain plan of
         their own (``full_plan_kw``, default: the fallback's launch shape) on a
-        stream beside the reduced launches."""
+        stream beside the reduced launches.  ``fallback_kw`` overrides plan options
+        of the fallback solves, and ``fallback_priority`` is their streams' priority
+        (-1 high, 0 the reduced launches' own)."""
         from .gru import NPARAM
         from .runtime import Plan
 
@@ -452,6 +454,8 @@ class SurrogateRunner:
         for k in ("threads_per_tile", "threads_big", "threads_global"):
             self.plan_kw.setdefault(k, PORT_THREADS)
         self.fallback = fallback and model is not None
+        self.fallback_kw = dict(fallback_kw or {})
+        self.fallback_priority = int(fallback_priority)
         n = len(self.descs)
         full = np.zeros(n, bool)
         if full_cells is not None:
@@ -485,6 +489,7 @@ class SurrogateRunner:
 
         fd = [replace(self.descs[i], probes=[(0, 0.5)]) for i in cells]
         kw = fallback_plan_options(fd, self.plan_kw, threads=512)
+        kw.update(self.fallback_kw)
         return Plan(descs_to_batch(fd), precision=self.precision, record_every=self.record_every, max_spikes=256,
                     device=self.device, **kw)
 
@@ -572,7 +577,7 @@ class SurrogateRunner:
                     # high priority: the block scheduler gives the fallback's tiles the
                     # next free SM slots ahead of the queued reduced launches, so the
                     # full solve runs at its own step latency
-                    side = torch.cuda.Stream(self.device, priority=-1)
+                    side = torch.cuda.Stream(self.device, priority=self.fallback_priority)
                     fp = self._fallback_plan(self.red_idx[new])
                     fs, fe = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
                     fs.record(side)
