@@ -484,11 +484,14 @@ class SurrogateRunner:
                                   device=device, **kw)
         self.full_cv = int(sum(int(sum(d.ncv)) for d in self.descs))
 
-    def _fallback_plan(self, cells):
+    def _fallback_plan(self, cells, n_steps: int):
         from .runtime import Plan
 
         fd = [replace(self.descs[i], probes=[(0, 0.5)]) for i in cells]
         kw = fallback_plan_options(fd, self.plan_kw, threads=512)
+        # the whole run in one launch: each fallback tile takes an SM slot once and keeps
+        # it, instead of queueing for a free slot behind the reduced tiles every launch
+        kw["steps_per_launch"] = max(1, int(n_steps))
         kw.update(self.fallback_kw)
         return Plan(descs_to_batch(fd), precision=self.precision, record_every=self.record_every, max_spikes=256,
                     device=self.device, **kw)
@@ -578,7 +581,7 @@ class SurrogateRunner:
                     # next free SM slots ahead of the queued reduced launches, so the
                     # full solve runs at its own step latency
                     side = torch.cuda.Stream(self.device, priority=self.fallback_priority)
-                    fp = self._fallback_plan(self.red_idx[new])
+                    fp = self._fallback_plan(self.red_idx[new], n_steps)
                     fs, fe = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
                     fs.record(side)
                     fp.run(n_steps, dt, stream=int(side.cuda_stream), check=False)

@@ -65,4 +65,5 @@ def test_init_nernst_cell_matches_oracle(native_lib, cuda_device):
     np.testing.assert_allclose(np.asarray(sp), np.asarray(osp[0][0]), rtol=0, atol=1e-9)
     # 1e-8 mV, or a time shift within the spike-time bar on the upstrokes
     slope = np.abs(np.gradient(ref[0, 0], 0.025))
-    assert (np.abs(gpu[0] - ref[0, 0]) <= 1e-8 + 1e-9 * slope).all()
+    assert gpu.shape == ref[0, 0].shape
+    assert (np.abs(gpu - ref[0, 0]) <= 1e-8 + 1e-9 * slope).all()
