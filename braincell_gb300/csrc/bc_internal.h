@@ -169,10 +169,10 @@ __host__ __device__ constexpr int gru_frag_slot(int q, int kk) { return q < 3 ? 
 // Launch shape of the kernel variant with ports: at most BC_PORT_MAX_THREADS
 // threads per tile, register budget for BC_PORT_MIN_CTAS resident tiles per SM.
 #ifndef BC_PORT_MAX_THREADS
-#define BC_PORT_MAX_THREADS 384
+#define BC_PORT_MAX_THREADS 768
 #endif
 #ifndef BC_PORT_MIN_CTAS
-#define BC_PORT_MIN_CTAS 2
+#define BC_PORT_MIN_CTAS 1
 #endif
 
 // Per-step staging of a port inside the tile's scratch: the GRU inputs, the
