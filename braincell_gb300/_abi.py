@@ -51,9 +51,24 @@ BC_M_HCN1H = 1 << 25
 BC_M_CAHVA = 1 << 26
 BC_M_CAV23 = 1 << 27
 BC_M_CAV32 = 1 << 28
-BC_M_ALL = 0x1FFFFFFF
+BC_M_EXT = 1 << 29  # extension channels, listed as BC_X_* bits in the record's BC_P_EXT_MASK
+BC_M_ALL = 0x3FFFFFFF
 
-BC_NPARAM = 96
+BC_X_HCN2 = 1 << 0
+BC_X_KV33 = 1 << 1
+BC_X_KV22 = 1 << 2
+BC_X_KV15 = 1 << 3
+BC_X_NAF = 1 << 4
+BC_X_NAP = 1 << 5
+BC_X_NAIO = 1 << 6
+BC_X_FKDR = 1 << 7
+BC_X_SKDR = 1 << 8
+BC_X_KDRIO = 1 << 9
+BC_X_HCNDCN = 1 << 10
+BC_X_HCNIO = 1 << 11
+BC_X_ALL = 0xFFF
+
+BC_NPARAM = 160
 BC_P_INVCM = 0
 BC_P_VREST = 1
 BC_P_ENA = 2
@@ -149,8 +164,30 @@ BC_P_HCN1F_PHI = 84
 BC_P_HCN1H_G = 85
 BC_P_HCN1H_E = 86
 BC_P_HCN1H_PHI = 87
+BC_P_EXT_MASK = 96
+BC_P_HCN2_G = 97
+BC_P_HCN2_E = 98
+BC_P_HCN2_PHI = 99
+BC_P_KV33_G = 100
+BC_P_KV33_PHI = 101
+BC_P_KV22_G = 102
+BC_P_KV15_G = 103
+BC_P_KV15_Q10 = 104
+BC_P_KV15_TACT = 105
+BC_P_KV15_TINF = 106
+BC_P_KV15_TINS = 107
+BC_P_NAF_G = 108
+BC_P_NAP_G = 109
+BC_P_NAIO_G = 110
+BC_P_FKDR_G = 111
+BC_P_SKDR_G = 112
+BC_P_KDRIO_G = 113
+BC_P_HCNDCN_G = 114
+BC_P_HCNDCN_E = 115
+BC_P_HCNIO_G = 116
+BC_P_HCNIO_E = 117
 
-BC_ABI_VERSION = 400
+BC_ABI_VERSION = 500
 
 BC_VARIANT_LEAN = 0
 BC_VARIANT_EXTRA = 1
@@ -196,7 +233,19 @@ BC_CUR_HCN1H = 27
 BC_CUR_CAHVA = 28
 BC_CUR_CAV23 = 29
 BC_CUR_CAV32 = 30
-BC_NCUR = 31
+BC_CUR_HCN2 = 31
+BC_CUR_KV33 = 32
+BC_CUR_KV22 = 33
+BC_CUR_KV15 = 34
+BC_CUR_NAF = 35
+BC_CUR_NAP = 36
+BC_CUR_NAIO = 37
+BC_CUR_FKDR = 38
+BC_CUR_SKDR = 39
+BC_CUR_KDRIO = 40
+BC_CUR_HCNDCN = 41
+BC_CUR_HCNIO = 42
+BC_NCUR = 43
 
 BC_STATE_V = 0
 BC_STATE_NA_P = 1
@@ -242,7 +291,26 @@ BC_STATE_CAV23_M = 62
 BC_STATE_CAV23_H = 63
 BC_STATE_CAV32_M = 64
 BC_STATE_CAV32_H = 65
-BC_NSTATE_VIEW = 66
+BC_STATE_HCN2_FAST = 66
+BC_STATE_HCN2_SLOW = 67
+BC_STATE_KV33_N = 68
+BC_STATE_KV22_M = 69
+BC_STATE_KV22_H = 70
+BC_STATE_KV15_M = 71
+BC_STATE_KV15_N = 72
+BC_STATE_KV15_U = 73
+BC_STATE_NAF_M = 74
+BC_STATE_NAF_H = 75
+BC_STATE_NAP_M = 76
+BC_STATE_NAP_H = 77
+BC_STATE_NAIO_M = 78
+BC_STATE_NAIO_H = 79
+BC_STATE_FKDR_M = 80
+BC_STATE_SKDR_M = 81
+BC_STATE_KDRIO_N = 82
+BC_STATE_HCNDCN_M = 83
+BC_STATE_HCNIO_Q = 84
+BC_NSTATE_VIEW = 85
 # the independent states of each Markov scheme, in view order (first appearance in
 # the scheme's transition list, the dependent state left out)
 MARKOV_STATES = {
@@ -293,6 +361,25 @@ STATE_NAMES = {
     "Cav2p3_h": BC_STATE_CAV23_H,
     "Cav3p2_m": BC_STATE_CAV32_M,
     "Cav3p2_h": BC_STATE_CAV32_H,
+    "HCN2_o_fast": BC_STATE_HCN2_FAST,
+    "HCN2_o_slow": BC_STATE_HCN2_SLOW,
+    "Kv3p3_n": BC_STATE_KV33_N,
+    "Kv2p2_m": BC_STATE_KV22_M,
+    "Kv2p2_h": BC_STATE_KV22_H,
+    "Kv1p5_m": BC_STATE_KV15_M,
+    "Kv1p5_n": BC_STATE_KV15_N,
+    "Kv1p5_u": BC_STATE_KV15_U,
+    "NaF_m": BC_STATE_NAF_M,
+    "NaF_h": BC_STATE_NAF_H,
+    "NaP_m": BC_STATE_NAP_M,
+    "NaP_h": BC_STATE_NAP_H,
+    "NaIO_m": BC_STATE_NAIO_M,
+    "NaIO_h": BC_STATE_NAIO_H,
+    "fKdr_m": BC_STATE_FKDR_M,
+    "sKdr_m": BC_STATE_SKDR_M,
+    "KdrIO_n": BC_STATE_KDRIO_N,
+    "HCNDCN_m": BC_STATE_HCNDCN_M,
+    "HCNIO_q": BC_STATE_HCNIO_Q,
 }
 for _cls, (_base, _names) in MARKOV_STATES.items():
     for _k, _n in enumerate(_names):

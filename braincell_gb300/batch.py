@@ -351,6 +351,18 @@ PROBE_STATES.update({
     ("CaHVA_MA2020_GoC", "s"): _abi.BC_STATE_CAHVA_S, ("CaHVA_MA2020_GoC", "u"): _abi.BC_STATE_CAHVA_U,
     ("Cav2p3_MA2020_GoC", "m"): _abi.BC_STATE_CAV23_M, ("Cav2p3_MA2020_GoC", "h"): _abi.BC_STATE_CAV23_H,
     ("Cav3p2_RI2021_SC", "m"): _abi.BC_STATE_CAV32_M, ("Cav3p2_RI2021_SC", "h"): _abi.BC_STATE_CAV32_H,
+    # extension channels
+    ("HCN2_MA2020_GoC", "o_fast"): _abi.BC_STATE_HCN2_FAST, ("HCN2_MA2020_GoC", "o_slow"): _abi.BC_STATE_HCN2_SLOW,
+    ("Kv3p3_MA2024_PC", "n"): _abi.BC_STATE_KV33_N,
+    ("Kv2p2_0010_MA2020_GrC", "m"): _abi.BC_STATE_KV22_M, ("Kv2p2_0010_MA2020_GrC", "h"): _abi.BC_STATE_KV22_H,
+    ("Kv1p5_MA2024_PC", "m"): _abi.BC_STATE_KV15_M, ("Kv1p5_MA2024_PC", "n"): _abi.BC_STATE_KV15_N,
+    ("Kv1p5_MA2024_PC", "u"): _abi.BC_STATE_KV15_U,
+    ("NaF_SU2015_DCN", "m"): _abi.BC_STATE_NAF_M, ("NaF_SU2015_DCN", "h"): _abi.BC_STATE_NAF_H,
+    ("NaP_SU2015_DCN", "m"): _abi.BC_STATE_NAP_M, ("NaP_SU2015_DCN", "h"): _abi.BC_STATE_NAP_H,
+    ("Na_ZH2019_IO", "m"): _abi.BC_STATE_NAIO_M, ("Na_ZH2019_IO", "h"): _abi.BC_STATE_NAIO_H,
+    ("fKdr_SU2015_DCN", "m"): _abi.BC_STATE_FKDR_M, ("sKdr_SU2015_DCN", "m"): _abi.BC_STATE_SKDR_M,
+    ("Kdr_ZH2019_IO", "n"): _abi.BC_STATE_KDRIO_N, ("HCN_SU2015_DCN", "m"): _abi.BC_STATE_HCNDCN_M,
+    ("HCN_ZH2019_IO", "q"): _abi.BC_STATE_HCNIO_Q,
 })
 for _cls, (_base, _names) in _abi.MARKOV_STATES.items():
     for _k, _n in enumerate(_names):
@@ -373,6 +385,11 @@ PROBE_CURRENTS = {
     "Kv3p4_MA2020_GoC": _abi.BC_CUR_KV34, "Kv4p3_MA2020_GoC": _abi.BC_CUR_KV43, "Kv1p1_MA2020_GoC": _abi.BC_CUR_KV11,
     "Kir2p3_MA2020_GrC": _abi.BC_CUR_KIR23, "HCN1_MA2020_GoC": _abi.BC_CUR_HCN1F, "HCN1_MA2024_PC": _abi.BC_CUR_HCN1H,
     "CaHVA_MA2020_GoC": _abi.BC_CUR_CAHVA, "Cav2p3_MA2020_GoC": _abi.BC_CUR_CAV23, "Cav3p2_RI2021_SC": _abi.BC_CUR_CAV32,
+    "HCN2_MA2020_GoC": _abi.BC_CUR_HCN2, "Kv3p3_MA2024_PC": _abi.BC_CUR_KV33,
+    "Kv2p2_0010_MA2020_GrC": _abi.BC_CUR_KV22, "Kv1p5_MA2024_PC": _abi.BC_CUR_KV15, "NaF_SU2015_DCN": _abi.BC_CUR_NAF,
+    "NaP_SU2015_DCN": _abi.BC_CUR_NAP, "Na_ZH2019_IO": _abi.BC_CUR_NAIO, "fKdr_SU2015_DCN": _abi.BC_CUR_FKDR,
+    "sKdr_SU2015_DCN": _abi.BC_CUR_SKDR, "Kdr_ZH2019_IO": _abi.BC_CUR_KDRIO, "HCN_SU2015_DCN": _abi.BC_CUR_HCNDCN,
+    "HCN_ZH2019_IO": _abi.BC_CUR_HCNIO,
 }
 ION_CURRENTS = {"na": _abi.BC_CUR_ION_NA, "k": _abi.BC_CUR_ION_K, "ca": _abi.BC_CUR_ION_CA}
 

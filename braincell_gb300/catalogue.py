@@ -132,6 +132,35 @@ CHANNELS: dict[str, dict[str, float]] = {
     "CaHVA_MA2020_GoC": {"g_max": 0.46, "temp": T30},
     "Cav2p3_MA2020_GoC": {"g_max": 0.0, "temp": celsius2kelvin(34.0)},
     "Cav3p2_RI2021_SC": {"g_max": 8.0e-4, "V_sh": 0.0, "temp": T36},
+    # extension channels (record entries after BC_P_EXT_MASK)
+    "HCN2_MA2020_GoC": {"g_max": 0.08, "E": -20.0, "temp": T22},
+    "Kv3p3_MA2024_PC": {"g_max": 5.0, "temp": T22, "gateCurrent": 0.0},
+    "Kv2p2_0010_MA2020_GrC": {"g_max": 0.01, "BBiD": 10.0},
+    "Kv1p5_MA2024_PC": {"g_max": 0.13195, "temp": celsius2kelvin(37.0), "Tauact": 1.0, "Tauinactf": 1.0,
+                        "Tauinacts": 1.0},
+    "NaF_SU2015_DCN": {"g_max": 0.01},
+    "NaP_SU2015_DCN": {"g_max": 0.01},
+    "Na_ZH2019_IO": {"g_max": 70.0},
+    "fKdr_SU2015_DCN": {"g_max": 0.01},
+    "sKdr_SU2015_DCN": {"g_max": 0.01},
+    "Kdr_ZH2019_IO": {"g_max": 18.0},
+    "HCN_SU2015_DCN": {"g_max": 0.01, "E": -45.0},
+    "HCN_ZH2019_IO": {"g_max": 0.15, "E": -43.0},
+}
+# extension channels: class -> (BC_X_* bit, record entry of g_max, record entry of E or None)
+_EXT = {
+    "HCN2_MA2020_GoC": (_abi.BC_X_HCN2, _abi.BC_P_HCN2_G, _abi.BC_P_HCN2_E),
+    "Kv3p3_MA2024_PC": (_abi.BC_X_KV33, _abi.BC_P_KV33_G, None),
+    "Kv2p2_0010_MA2020_GrC": (_abi.BC_X_KV22, _abi.BC_P_KV22_G, None),
+    "Kv1p5_MA2024_PC": (_abi.BC_X_KV15, _abi.BC_P_KV15_G, None),
+    "NaF_SU2015_DCN": (_abi.BC_X_NAF, _abi.BC_P_NAF_G, None),
+    "NaP_SU2015_DCN": (_abi.BC_X_NAP, _abi.BC_P_NAP_G, None),
+    "Na_ZH2019_IO": (_abi.BC_X_NAIO, _abi.BC_P_NAIO_G, None),
+    "fKdr_SU2015_DCN": (_abi.BC_X_FKDR, _abi.BC_P_FKDR_G, None),
+    "sKdr_SU2015_DCN": (_abi.BC_X_SKDR, _abi.BC_P_SKDR_G, None),
+    "Kdr_ZH2019_IO": (_abi.BC_X_KDRIO, _abi.BC_P_KDRIO_G, None),
+    "HCN_SU2015_DCN": (_abi.BC_X_HCNDCN, _abi.BC_P_HCNDCN_G, _abi.BC_P_HCNDCN_E),
+    "HCN_ZH2019_IO": (_abi.BC_X_HCNIO, _abi.BC_P_HCNIO_G, _abi.BC_P_HCNIO_E),
 }
 # cell-type variants with their base class's kinetics; own defaults where they differ
 KINETIC_VARIANTS = {
@@ -376,6 +405,26 @@ def region_record(mechs, cable: CableProperty) -> tuple[int, np.ndarray]:
         elif name == "Cav3p2_RI2021_SC":
             bits |= _abi.BC_M_CAV32
             rec[_abi.BC_P_CAV32_G], rec[_abi.BC_P_CAV32_VSH] = p["g_max"], p["V_sh"]
+        elif name in _EXT:
+            xbit, g_slot, e_slot = _EXT[name]
+            bits |= _abi.BC_M_EXT
+            rec[_abi.BC_P_EXT_MASK] = float(int(rec[_abi.BC_P_EXT_MASK]) | xbit)
+            g = p["g_max"]
+            if name == "HCN2_MA2020_GoC":  # the conductance's own Q10 1.5 and the gates' q10 3, at 23 degC
+                g *= q10_phi(1.5, p["temp"], celsius2kelvin(23.0))
+                rec[_abi.BC_P_HCN2_PHI] = q10_phi(3.0, p["temp"], celsius2kelvin(23.0))
+            elif name == "Kv3p3_MA2024_PC":
+                if p["gateCurrent"] != 0.0:
+                    raise ValueError(f"{decl.class_name}: the gating current (gateCurrent != 0) is not built.")
+                rec[_abi.BC_P_KV33_PHI] = q10_phi(2.7, p["temp"], T22)
+            elif name == "Kv1p5_MA2024_PC":
+                rec[_abi.BC_P_KV15_Q10] = q10_phi(2.2, p["temp"], celsius2kelvin(37.0))
+                rec[_abi.BC_P_KV15_TACT] = p["Tauact"]
+                rec[_abi.BC_P_KV15_TINF] = p["Tauinactf"]
+                rec[_abi.BC_P_KV15_TINS] = p["Tauinacts"]
+            rec[g_slot] = g
+            if e_slot is not None:
+                rec[e_slot] = p["E"]
         elif name in _PQ_RECORDS:
             bit, base = _PQ_RECORDS[name]
             bits |= bit

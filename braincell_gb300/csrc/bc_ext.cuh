@@ -1,0 +1,444 @@
+// Extension channels: classes outside the mechanism bits of the main record,
+// listed per region as BC_X_* bits in the record entry BC_P_EXT_MASK and run by
+// the extra kernel variant.  Each is an exp-Euler HH channel as the others are
+// (gates at the new V, ohmic current in its ion's E or its own E); Kv1p5's
+// current carries a voltage factor, so its conductance term is the negative
+// V-derivative of the current, as the reference's autodiff linearisation takes
+// it (quad/_staggered.py:763-795).
+//
+// Rate functions, as published in the reference:
+//   HCN2_MA2020_GoC        channel/hyperpolarization_activated.py:838-1008
+//   Kv3p3_MA2024_PC        channel/potassium.py:2937-3124
+//   Kv2p2_0010_MA2020_GrC  channel/potassium.py:5664-5804
+//   Kv1p5_MA2024_PC        channel/potassium.py:2735-2935
+//   NaF_SU2015_DCN         channel/sodium.py:402-498
+//   NaP_SU2015_DCN         channel/sodium.py:500-596
+//   Na_ZH2019_IO           channel/sodium.py:598-725
+//   fKdr_SU2015_DCN        channel/potassium.py:1374-1483
+//   sKdr_SU2015_DCN        channel/potassium.py:1485-1595
+//   Kdr_ZH2019_IO          channel/potassium.py:6238-6374
+//   HCN_SU2015_DCN         channel/hyperpolarization_activated.py:1010-1107
+//   HCN_ZH2019_IO          channel/hyperpolarization_activated.py:1109-1217
+#pragma once
+
+#include "bc_mech.cuh"
+
+namespace bc {
+
+// State slots, after the cerebellar channels' (a plan with extension channels
+// carries kNumSlotsExt slots per node); view BC_STATE_* k sits in slot k + 1.
+constexpr int kSlotHcn2F = 67;
+constexpr int kSlotHcn2S = 68;
+constexpr int kSlotKv33N = 69;
+constexpr int kSlotKv22M = 70;
+constexpr int kSlotKv22H = 71;
+constexpr int kSlotKv15M = 72;
+constexpr int kSlotKv15N = 73;
+constexpr int kSlotKv15U = 74;
+constexpr int kSlotNafM = 75;
+constexpr int kSlotNafH = 76;
+constexpr int kSlotNapM = 77;
+constexpr int kSlotNapH = 78;
+constexpr int kSlotNaioM = 79;
+constexpr int kSlotNaioH = 80;
+constexpr int kSlotFkdrM = 81;
+constexpr int kSlotSkdrM = 82;
+constexpr int kSlotKdrioN = 83;
+constexpr int kSlotHcndcnM = 84;
+constexpr int kSlotHcnioQ = 85;
+constexpr int kNumSlotsExt = 86;
+
+// x / (1 - e^-x) = 1 / exprel(-x), finite at x = 0 (the reference's
+// _x_over_one_minus_exp_neg_stable, channel/sodium.py:50-55)
+template <typename Real>
+__host__ __device__ __forceinline__ Real x_over_1mexp(Real x) {
+  return Real(1) / exprel(-x);
+}
+
+// HCN2_MA2020_GoC: o_inf split by r(V), clamped to 0 above -64.7 mV and to 1
+// below -108.7 mV; time constants exp((tC V - tD) tE).
+template <typename Real>
+struct Hcn2Rates {
+  Real finf, ftau, sinf, stau;
+  __host__ __device__ __forceinline__ explicit Hcn2Rates(Real v) {
+    const Real o = Real(1) / (Real(1) + aexp((v + Real(81.95)) * Real(0.1661)));
+    const Real r = v >= Real(-64.70) ? Real(0) : (v <= Real(-108.70) ? Real(1) : Real(-0.0227) * v - Real(1.4694));
+    finf = r * o;
+    sinf = (Real(1) - r) * o;
+    ftau = aexp((Real(0.0269) * v + Real(5.6111)) * Real(2.3026));
+    stau = aexp((Real(0.0152) * v + Real(5.2944)) * Real(2.3026));
+  }
+};
+
+// Kv3p3_MA2024_PC: n, alpha / beta = 0.22 exp(-+(V + 16) / 26.5).
+template <typename Real>
+struct Kv33Rates {
+  Real a, b;
+  __host__ __device__ __forceinline__ explicit Kv33Rates(Real v) {
+    a = Real(0.22) * aexp(-(v + Real(16)) / Real(-26.5));
+    b = Real(0.22) * aexp(-(v + Real(16)) / Real(26.5));
+  }
+};
+
+// Kv2p2_0010_MA2020_GrC: m and h, inf / tau.
+template <typename Real>
+struct Kv22Rates {
+  Real minf, mtau, hinf, htau;
+  __host__ __device__ __forceinline__ explicit Kv22Rates(Real v) {
+    minf = Real(1) / (Real(1) + aexp((v - Real(5)) / Real(-12)));
+    const Real d = Real(1) + aexp((v + Real(46.56)) / Real(-44.14));
+    mtau = Real(130) / d;
+    hinf = Real(1) / (Real(1) + aexp((v + Real(16.3)) / Real(4.8)));
+    htau = Real(10000) / d;
+  }
+};
+
+// Kv1p5_MA2024_PC: m^3 n u; the Q10 factor q scales the m and n rates, the
+// Tau* parameters scale the time constants.
+template <typename Real>
+struct Kv15Rates {
+  Real minf, mtau, ninf, ntau, uinf;
+  __host__ __device__ __forceinline__ Kv15Rates(Real v, Real q, Real tact, Real tinf) {
+    minf = Real(1) / (Real(1) + aexp(-(v + Real(30.3)) / Real(9.6)));
+    const Real am = q * Real(0.65) / (aexp(-(v + Real(10)) / Real(8.5)) + aexp(-(v - Real(30)) / Real(59)));
+    const Real bm = q * Real(0.65) / (Real(2.5) + aexp((v + Real(82)) / Real(17)));
+    mtau = Real(1) / (am + bm) / Real(3) * tact;
+    ninf = Real(0.25) + Real(1) / (Real(1.35) + aexp((v + Real(7)) / Real(14)));
+    const Real an = q * Real(0.001) / (Real(2.4) + Real(10.9) * aexp(-(v + Real(90)) / Real(78)));
+    const Real bn = q * Real(0.001) * aexp((v - Real(168)) / Real(16));
+    ntau = Real(1) / (an + bn) / Real(3) * tinf;
+    uinf = Real(0.1) + Real(1) / (Real(1.1) + aexp((v + Real(7)) / Real(14)));
+  }
+};
+// u's time constant: 6800 ms x Tauinacts
+constexpr double kKv15TauU = 6800.0;
+
+// Kv1p5's voltage factor f(V) = 0.1 + s, s = 1 / (1 + exp(-(V - 15) / 13)), and
+// its derivative s (1 - s) / 13.
+template <typename Real>
+__host__ __device__ __forceinline__ void kv15_vfactor(Real v, Real& f, Real& df) {
+  const Real s = Real(1) / (Real(1) + aexp(-(v - Real(15)) / Real(13)));
+  f = Real(0.1) + s;
+  df = s * (Real(1) - s) / Real(13);
+}
+
+// NaF_SU2015_DCN: m^3 h, inf / tau (qdeltat = 1).
+template <typename Real>
+struct NafRates {
+  Real minf, mtau, hinf, htau;
+  __host__ __device__ __forceinline__ explicit NafRates(Real v) {
+    minf = Real(1) / (Real(1) + aexp((v + Real(45)) / Real(-7.3)));
+    mtau = Real(5.83) / (aexp((v - Real(6.4)) / Real(-9)) + aexp((v + Real(97)) / Real(17))) + Real(0.025);
+    hinf = Real(1) / (Real(1) + aexp((v + Real(42)) / Real(5.9)));
+    htau = Real(16.67) / (aexp((v - Real(8.3)) / Real(-29)) + aexp((v + Real(66)) / Real(9))) + Real(0.2);
+  }
+};
+
+// NaP_SU2015_DCN: m^3 h, inf / tau, m's tau 50 ms.
+template <typename Real>
+struct NapRates {
+  Real minf, mtau, hinf, htau;
+  __host__ __device__ __forceinline__ explicit NapRates(Real v) {
+    minf = Real(1) / (Real(1) + aexp((v + Real(70)) / Real(-4.1)));
+    mtau = Real(50);
+    hinf = Real(1) / (Real(1) + aexp((v + Real(80)) / Real(4)));
+    htau = Real(1750) / (Real(1) + aexp((v + Real(65)) / Real(-8))) + Real(250);
+  }
+};
+
+// Na_ZH2019_IO: m^3 h from alpha / beta, m's tau 0.001 ms, h's 250 / (a + b).
+template <typename Real>
+struct NaioRates {
+  Real minf, mtau, hinf, htau;
+  __host__ __device__ __forceinline__ explicit NaioRates(Real v) {
+    const Real am = x_over_1mexp((v + Real(41)) / Real(10));
+    const Real bm = Real(9) * aexp(-(v + Real(66)) / Real(20));
+    const Real ah = Real(5) * aexp(-(v + Real(60)) / Real(15));
+    const Real bh = Real(10) * x_over_1mexp((v + Real(50)) / Real(10));
+    minf = am / (am + bm);
+    mtau = Real(0.001);
+    hinf = ah / (ah + bh);
+    htau = Real(250) / (ah + bh);
+  }
+};
+
+// fKdr / sKdr_SU2015_DCN: m^4, inf = 1 / (1 + exp((V + vh) / k)),
+// tau = c / (exp((V + vh) / k1) + exp((V + vh) / k2)) + t0 (qdeltat = 1).
+template <typename Real>
+struct Su2015KdrRates {
+  Real minf, mtau;
+  __host__ __device__ __forceinline__ Su2015KdrRates(Real v, Real vh, Real k, Real c, Real k1, Real k2, Real t0) {
+    const Real x = v + vh;
+    minf = Real(1) / (Real(1) + aexp(x / k));
+    mtau = c / (aexp(x / k1) + aexp(x / k2)) + t0;
+  }
+};
+template <typename Real>
+__host__ __device__ __forceinline__ Su2015KdrRates<Real> fkdr_rates(Real v) {
+  return Su2015KdrRates<Real>(v, Real(40), Real(-7.8), Real(13.9), Real(12), Real(-13), Real(0.1));
+}
+template <typename Real>
+__host__ __device__ __forceinline__ Su2015KdrRates<Real> skdr_rates(Real v) {
+  return Su2015KdrRates<Real>(v, Real(50), Real(-9.1), Real(14.95), Real(21.74), Real(-13.91), Real(0.05));
+}
+
+// Kdr_ZH2019_IO: n^4 from alpha / beta, tau 10 / (a + b).
+template <typename Real>
+struct KdrioRates {
+  Real ninf, ntau;
+  __host__ __device__ __forceinline__ explicit KdrioRates(Real v) {
+    const Real a = Real(10) * x_over_1mexp((v + Real(41)) / Real(10));
+    const Real b = Real(12.5) * aexp(-(v + Real(51)) / Real(80));
+    ninf = a / (a + b);
+    ntau = Real(10) / (a + b);
+  }
+};
+
+// HCN_SU2015_DCN: m^2, m's tau 400 ms.
+template <typename Real>
+struct HcndcnRates {
+  Real minf, mtau;
+  __host__ __device__ __forceinline__ explicit HcndcnRates(Real v) {
+    minf = Real(1) / (Real(1) + aexp((v + Real(80)) / Real(5)));
+    mtau = Real(400);
+  }
+};
+
+// HCN_ZH2019_IO: q, tau = 1 / (exp(-0.086 V - 14.6) + exp(0.07 V - 1.87)).
+template <typename Real>
+struct HcnioRates {
+  Real qinf, qtau;
+  __host__ __device__ __forceinline__ explicit HcnioRates(Real v) {
+    qinf = Real(1) / (Real(1) + aexp((v + Real(75)) / Real(5.5)));
+    qtau = Real(1) / (aexp(Real(-0.086) * v - Real(14.6)) + aexp(Real(0.07) * v - Real(1.87)));
+  }
+};
+
+// The region's BC_X_* bits (an integer stored as a record real).
+template <typename Real>
+__host__ __device__ __forceinline__ uint32_t ext_mask(const Real* P) {
+  return uint32_t(P[BC_P_EXT_MASK]);
+}
+
+// One extension channel's current at v with the node's stored gates (0 where the
+// region does not carry it); *gv receives -dI/dV when not null.
+template <typename Real>
+__device__ __forceinline__ Real ext_current(const Real* st, int N, const Real* P, uint32_t x, Real v, int code,
+                                            Real* gv) {
+  Real g = Real(0), e = Real(0), gd = Real(0);
+  bool has = false;
+  switch (code) {
+    case BC_CUR_HCN2:
+      if ((has = (x & BC_X_HCN2) != 0)) {
+        g = P[BC_P_HCN2_G] * (st[kSlotHcn2F * N] + st[kSlotHcn2S * N]);
+        e = P[BC_P_HCN2_E];
+      }
+      break;
+    case BC_CUR_KV33:
+      if ((has = (x & BC_X_KV33) != 0)) {
+        const Real n2 = st[kSlotKv33N * N] * st[kSlotKv33N * N];
+        g = P[BC_P_KV33_G] * n2 * n2;
+        e = P[BC_P_EK];
+      }
+      break;
+    case BC_CUR_KV22:
+      if ((has = (x & BC_X_KV22) != 0)) {
+        g = P[BC_P_KV22_G] * st[kSlotKv22M * N] * st[kSlotKv22H * N];
+        e = P[BC_P_EK];
+      }
+      break;
+    case BC_CUR_KV15:
+      if ((has = (x & BC_X_KV15) != 0)) {
+        const Real m = st[kSlotKv15M * N];
+        const Real gg = P[BC_P_KV15_G] * m * m * m * st[kSlotKv15N * N] * st[kSlotKv15U * N];
+        Real f, df;
+        kv15_vfactor(v, f, df);
+        e = P[BC_P_EK];
+        g = gg * f;
+        // I = gg f (E - V): -dI/dV = gg (f - f' (E - V))
+        gd = gg * (f - df * (e - v));
+      }
+      break;
+    case BC_CUR_NAF:
+      if ((has = (x & BC_X_NAF) != 0)) {
+        const Real m = st[kSlotNafM * N];
+        g = P[BC_P_NAF_G] * m * m * m * st[kSlotNafH * N];
+        e = P[BC_P_ENA];
+      }
+      break;
+    case BC_CUR_NAP:
+      if ((has = (x & BC_X_NAP) != 0)) {
+        const Real m = st[kSlotNapM * N];
+        g = P[BC_P_NAP_G] * m * m * m * st[kSlotNapH * N];
+        e = P[BC_P_ENA];
+      }
+      break;
+    case BC_CUR_NAIO:
+      if ((has = (x & BC_X_NAIO) != 0)) {
+        const Real m = st[kSlotNaioM * N];
+        g = P[BC_P_NAIO_G] * m * m * m * st[kSlotNaioH * N];
+        e = P[BC_P_ENA];
+      }
+      break;
+    case BC_CUR_FKDR:
+      if ((has = (x & BC_X_FKDR) != 0)) {
+        const Real m2 = st[kSlotFkdrM * N] * st[kSlotFkdrM * N];
+        g = P[BC_P_FKDR_G] * m2 * m2;
+        e = P[BC_P_EK];
+      }
+      break;
+    case BC_CUR_SKDR:
+      if ((has = (x & BC_X_SKDR) != 0)) {
+        const Real m2 = st[kSlotSkdrM * N] * st[kSlotSkdrM * N];
+        g = P[BC_P_SKDR_G] * m2 * m2;
+        e = P[BC_P_EK];
+      }
+      break;
+    case BC_CUR_KDRIO:
+      if ((has = (x & BC_X_KDRIO) != 0)) {
+        const Real n2 = st[kSlotKdrioN * N] * st[kSlotKdrioN * N];
+        g = P[BC_P_KDRIO_G] * n2 * n2;
+        e = P[BC_P_EK];
+      }
+      break;
+    case BC_CUR_HCNDCN:
+      if ((has = (x & BC_X_HCNDCN) != 0)) {
+        const Real m = st[kSlotHcndcnM * N];
+        g = P[BC_P_HCNDCN_G] * m * m;
+        e = P[BC_P_HCNDCN_E];
+      }
+      break;
+    case BC_CUR_HCNIO:
+      if ((has = (x & BC_X_HCNIO) != 0)) {
+        g = P[BC_P_HCNIO_G] * st[kSlotHcnioQ * N];
+        e = P[BC_P_HCNIO_E];
+      }
+      break;
+  }
+  if (!has) return Real(0);
+  if (gv) *gv = code == BC_CUR_KV15 ? gd : g;
+  return g * (e - v);
+}
+
+// Gate update of one node's extension channels at v (exp-Euler, as the others).
+template <typename Real>
+__device__ __forceinline__ void ext_gates(Real* st, int N, const Real* P, uint32_t x, Real v, Real dt) {
+  if (x & BC_X_HCN2) {
+    const Hcn2Rates<Real> r(v);
+    const Real phi = P[BC_P_HCN2_PHI];
+    st[kSlotHcn2F * N] = gate_it(st[kSlotHcn2F * N], r.finf, r.ftau, phi, dt);
+    st[kSlotHcn2S * N] = gate_it(st[kSlotHcn2S * N], r.sinf, r.stau, phi, dt);
+  }
+  if (x & BC_X_KV33) {
+    const Kv33Rates<Real> r(v);
+    st[kSlotKv33N * N] = gate_ab<Real, true>(st[kSlotKv33N * N], r.a, r.b, P[BC_P_KV33_PHI], dt);
+  }
+  if (x & BC_X_KV22) {
+    const Kv22Rates<Real> r(v);
+    st[kSlotKv22M * N] = gate_it(st[kSlotKv22M * N], r.minf, r.mtau, Real(1), dt);
+    st[kSlotKv22H * N] = gate_it(st[kSlotKv22H * N], r.hinf, r.htau, Real(1), dt);
+  }
+  if (x & BC_X_KV15) {
+    const Kv15Rates<Real> r(v, P[BC_P_KV15_Q10], P[BC_P_KV15_TACT], P[BC_P_KV15_TINF]);
+    st[kSlotKv15M * N] = gate_it(st[kSlotKv15M * N], r.minf, r.mtau, Real(1), dt);
+    st[kSlotKv15N * N] = gate_it(st[kSlotKv15N * N], r.ninf, r.ntau, Real(1), dt);
+    st[kSlotKv15U * N] = gate_it(st[kSlotKv15U * N], r.uinf, Real(kKv15TauU) * P[BC_P_KV15_TINS], Real(1), dt);
+  }
+  if (x & BC_X_NAF) {
+    const NafRates<Real> r(v);
+    st[kSlotNafM * N] = gate_it(st[kSlotNafM * N], r.minf, r.mtau, Real(1), dt);
+    st[kSlotNafH * N] = gate_it(st[kSlotNafH * N], r.hinf, r.htau, Real(1), dt);
+  }
+  if (x & BC_X_NAP) {
+    const NapRates<Real> r(v);
+    st[kSlotNapM * N] = gate_it(st[kSlotNapM * N], r.minf, r.mtau, Real(1), dt);
+    st[kSlotNapH * N] = gate_it(st[kSlotNapH * N], r.hinf, r.htau, Real(1), dt);
+  }
+  if (x & BC_X_NAIO) {
+    const NaioRates<Real> r(v);
+    st[kSlotNaioM * N] = gate_it(st[kSlotNaioM * N], r.minf, r.mtau, Real(1), dt);
+    st[kSlotNaioH * N] = gate_it(st[kSlotNaioH * N], r.hinf, r.htau, Real(1), dt);
+  }
+  if (x & BC_X_FKDR) {
+    const Su2015KdrRates<Real> r = fkdr_rates(v);
+    st[kSlotFkdrM * N] = gate_it(st[kSlotFkdrM * N], r.minf, r.mtau, Real(1), dt);
+  }
+  if (x & BC_X_SKDR) {
+    const Su2015KdrRates<Real> r = skdr_rates(v);
+    st[kSlotSkdrM * N] = gate_it(st[kSlotSkdrM * N], r.minf, r.mtau, Real(1), dt);
+  }
+  if (x & BC_X_KDRIO) {
+    const KdrioRates<Real> r(v);
+    st[kSlotKdrioN * N] = gate_it(st[kSlotKdrioN * N], r.ninf, r.ntau, Real(1), dt);
+  }
+  if (x & BC_X_HCNDCN) {
+    const HcndcnRates<Real> r(v);
+    st[kSlotHcndcnM * N] = gate_it(st[kSlotHcndcnM * N], r.minf, r.mtau, Real(1), dt);
+  }
+  if (x & BC_X_HCNIO) {
+    const HcnioRates<Real> r(v);
+    st[kSlotHcnioQ * N] = gate_it(st[kSlotHcnioQ * N], r.qinf, r.qtau, Real(1), dt);
+  }
+}
+
+// A node's extension channels: gates at v (when advancing), then their G and I.
+template <typename Real>
+__device__ __noinline__ void ext_channels(Real* st, int N, const Real* P, Real v, Real dt, bool advance, Real& G,
+                                          Real& I) {
+  const uint32_t x = ext_mask(P);
+  if (advance) ext_gates(st, N, P, x, v, dt);
+  for (int code = BC_CUR_HCN2; code <= BC_CUR_HCNIO; ++code) {
+    Real g = Real(0);
+    const Real i = ext_current(st, N, P, x, v, code, &g);
+    G += g;
+    I += i;
+  }
+}
+
+// Steady states of the extension channels' gates at v (HH.reset_state).
+template <typename Real>
+__device__ __forceinline__ void ext_steady(const Real* P, Real* st, int N, Real v) {
+  const uint32_t x = ext_mask(P);
+  if (x & BC_X_HCN2) {
+    const Hcn2Rates<Real> r(v);
+    st[kSlotHcn2F * N] = r.finf;
+    st[kSlotHcn2S * N] = r.sinf;
+  }
+  if (x & BC_X_KV33) {
+    const Kv33Rates<Real> r(v);
+    st[kSlotKv33N * N] = r.a / (r.a + r.b);
+  }
+  if (x & BC_X_KV22) {
+    const Kv22Rates<Real> r(v);
+    st[kSlotKv22M * N] = r.minf;
+    st[kSlotKv22H * N] = r.hinf;
+  }
+  if (x & BC_X_KV15) {
+    const Kv15Rates<Real> r(v, P[BC_P_KV15_Q10], P[BC_P_KV15_TACT], P[BC_P_KV15_TINF]);
+    st[kSlotKv15M * N] = r.minf;
+    st[kSlotKv15N * N] = r.ninf;
+    st[kSlotKv15U * N] = r.uinf;
+  }
+  if (x & BC_X_NAF) {
+    const NafRates<Real> r(v);
+    st[kSlotNafM * N] = r.minf;
+    st[kSlotNafH * N] = r.hinf;
+  }
+  if (x & BC_X_NAP) {
+    const NapRates<Real> r(v);
+    st[kSlotNapM * N] = r.minf;
+    st[kSlotNapH * N] = r.hinf;
+  }
+  if (x & BC_X_NAIO) {
+    const NaioRates<Real> r(v);
+    st[kSlotNaioM * N] = r.minf;
+    st[kSlotNaioH * N] = r.hinf;
+  }
+  if (x & BC_X_FKDR) st[kSlotFkdrM * N] = fkdr_rates(v).minf;
+  if (x & BC_X_SKDR) st[kSlotSkdrM * N] = skdr_rates(v).minf;
+  if (x & BC_X_KDRIO) st[kSlotKdrioN * N] = KdrioRates<Real>(v).ninf;
+  if (x & BC_X_HCNDCN) st[kSlotHcndcnM * N] = HcndcnRates<Real>(v).minf;
+  if (x & BC_X_HCNIO) st[kSlotHcnioQ * N] = HcnioRates<Real>(v).qinf;
+}
+
+}  // namespace bc

@@ -47,8 +47,10 @@ int32_t locate_node(const bc_batch_spec& spec, int64_t c, const LoweredCell& lc,
 // shared-memory banks (the lanes of a warp read the records of their own nodes'
 // regions; at a stride of 64 words they would all fall in one bank).
 constexpr int kParamStride = BC_NPARAM + 1;
-// Plans on the lean kernel variants read only the main mix's entries (up to
+// Plans on the extra variant without extension channels read the entries before
+// BC_P_EXT_MASK only, and plans on the lean variants only the main mix's (up to
 // BC_P_CA_CI0): their records keep those, on an odd stride as well.
+constexpr int kParamStrideExtra = BC_P_EXT_MASK + 1;
 constexpr int kParamStrideCore = BC_P_CA_CI0 + 2;
 
 // A chain: nodes [start, start+count) of the tile, bottom (deepest) first; node

@@ -30,6 +30,7 @@
 #include "bc_gru.cuh"
 #include "bc_internal.h"
 #include "bc_mech.cuh"
+#include "bc_ext.cuh"
 
 namespace bc {
 
@@ -359,17 +360,24 @@ __device__ __forceinline__ double probe_current(const Real* st, int N, const Rea
         return cerebellar_ca_current(st, N, P, m & BC_M_CAV23, v, eca(), (Real*)nullptr);
       case BC_CUR_CAV32:
         return cerebellar_ca_current(st, N, P, m & BC_M_CAV32, v, eca(), (Real*)nullptr);
+      default:
+        // extension channels: the record's list exists only where BC_M_EXT is set
+        if (c >= BC_CUR_HCN2 && c <= BC_CUR_HCNIO && (m & BC_M_EXT))
+          return ext_current(st, N, P, ext_mask(P), v, c, (Real*)nullptr);
     }
     return Real(0);
   };
   switch (code) {
     case BC_CUR_ION_NA:
-      return double(cur(BC_CUR_NA)) + double(cur(BC_CUR_NAHH)) + double(cur(BC_CUR_NAV16));
+      return double(cur(BC_CUR_NA)) + double(cur(BC_CUR_NAHH)) + double(cur(BC_CUR_NAV16)) + double(cur(BC_CUR_NAF)) +
+             double(cur(BC_CUR_NAP)) + double(cur(BC_CUR_NAIO));
     case BC_CUR_ION_K:
       return double(cur(BC_CUR_KDR)) + double(cur(BC_CUR_KLEAK)) + double(cur(BC_CUR_AHP)) + double(cur(BC_CUR_KHH)) +
              double(cur(BC_CUR_KM)) + double(cur(BC_CUR_KA1)) + double(cur(BC_CUR_KA2)) + double(cur(BC_CUR_KK2A)) +
              double(cur(BC_CUR_KK2B)) + double(cur(BC_CUR_KNI)) + double(cur(BC_CUR_KCA22)) + double(cur(BC_CUR_KCA11)) +
-             double(cur(BC_CUR_KV34)) + double(cur(BC_CUR_KV43)) + double(cur(BC_CUR_KV11)) + double(cur(BC_CUR_KIR23));
+             double(cur(BC_CUR_KV34)) + double(cur(BC_CUR_KV43)) + double(cur(BC_CUR_KV11)) + double(cur(BC_CUR_KIR23)) +
+             double(cur(BC_CUR_KV33)) + double(cur(BC_CUR_KV22)) + double(cur(BC_CUR_KV15)) + double(cur(BC_CUR_FKDR)) +
+             double(cur(BC_CUR_SKDR)) + double(cur(BC_CUR_KDRIO));
     case BC_CUR_ION_CA:
       return double(cur(BC_CUR_CAL)) + double(cur(BC_CUR_CAT)) + double(cur(BC_CUR_CAHVA)) + double(cur(BC_CUR_CAV23)) +
              double(cur(BC_CUR_CAV32));
@@ -386,7 +394,7 @@ constexpr uint32_t kCerebellarCaChannels = BC_M_CAHVA | BC_M_CAV23 | BC_M_CAV32;
 constexpr uint32_t kCerebellarChannels =
     BC_M_KV34 | BC_M_KV43 | BC_M_KV11 | BC_M_KIR23 | BC_M_HCN1F | BC_M_HCN1H | kCerebellarCaChannels;
 constexpr uint32_t kExtraChannels = BC_M_NAHH | BC_M_KHH | BC_M_KM | BC_M_KA1 | BC_M_KA2 | BC_M_KK2A | BC_M_KK2B |
-                                   BC_M_KNI | BC_M_NAV16 | BC_M_KCA22 | BC_M_KCA11 | kCerebellarChannels;
+                                   BC_M_KNI | BC_M_NAV16 | BC_M_KCA22 | BC_M_KCA11 | kCerebellarChannels | BC_M_EXT;
 
 __device__ __forceinline__ MarkovGraph nav16_graph() { return MarkovGraph{13, 17, 12, kSlotNav16, kNav16Src, kNav16Dst}; }
 __device__ __forceinline__ MarkovGraph kca22_graph() { return MarkovGraph{6, 5, 0, kSlotKca22, kKca22Src, kKca22Dst}; }
@@ -625,6 +633,8 @@ __device__ __noinline__ void extra_channels(Real* st, int N, const Real* P, uint
       I += g * (P[BC_P_EK] - v);
     }
   }
+  // the extension channels listed in the record (gates independent of the above)
+  if (m & BC_M_EXT) ext_channels(st, N, P, v, dt, advance, G, I);
 }
 
 // One node's mechanisms.  `st` points at the node's slot-0 state (stride N).
@@ -865,6 +875,7 @@ __device__ __forceinline__ void steady_states(const Real* P, uint32_t m, Real* s
     st[kSlotCav32M * N] = r.minf;
     st[kSlotCav32H * N] = r.hinf;
   }
+  if (m & BC_M_EXT) ext_steady(P, st, N, v);
   if (m & (BC_M_NAV16 | BC_M_KCA22 | BC_M_KCA11)) {
     // Markov channels start at their stationary distribution (reset_steady_state)
     Real kf[17], kb[17];

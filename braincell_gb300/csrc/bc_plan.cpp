@@ -27,6 +27,7 @@
 #include "../../include/braincell_gb300_debug.h"
 #include "bc_internal.h"
 #include "bc_mech.cuh"
+#include "bc_ext.cuh"
 
 namespace bc {
 
@@ -68,9 +69,18 @@ constexpr uint32_t kCerebellarBits = BC_M_KV34 | BC_M_KV43 | BC_M_KV11 | BC_M_KI
 
 namespace bc {
 
+// A region's mechanism bits, with its extension channels' BC_X_* bits (from the
+// record) in the high word: the owner masks of state views and current probes.
+constexpr uint64_t ext_bits(uint32_t x) { return uint64_t(x) << 32; }
+static inline uint64_t region_bits(const bc_batch_spec& s, int64_t k) {
+  uint64_t b = s.region_mech[k];
+  if (b & BC_M_EXT) b |= ext_bits(uint32_t(s.region_params[k * BC_NPARAM + BC_P_EXT_MASK]));
+  return b;
+}
+
 // The mechanism bit that owns a BC_STATE_* view and the state slot holding it (V:
 // in the tile blob, no slot; V_last: every node; Ci and V_last also have a low word).
-static void state_view(int32_t which, uint32_t* bit, int* slot) {
+static void state_view(int32_t which, uint64_t* bit, int* slot) {
   static const uint32_t kBit[BC_STATE_NAV16_C1] = {
       0,         BC_M_NA,   BC_M_NA,   BC_M_KDR,  BC_M_CAL,  BC_M_CAL,  BC_M_CAT,   BC_M_CAT,  BC_M_HCN,
       BC_M_AHP,  BC_M_CADET, BC_M_NAHH, BC_M_NAHH, BC_M_KHH, BC_M_KM,   BC_M_KA1,   BC_M_KA1,  BC_M_KA2,
@@ -88,7 +98,14 @@ static void state_view(int32_t which, uint32_t* bit, int* slot) {
   static const uint32_t kCereb[BC_NSTATE_VIEW - BC_STATE_KV34_M] = {
       BC_M_KV34,  BC_M_KV34,  BC_M_KV43,  BC_M_KV43,  BC_M_KV11,  BC_M_KIR23, BC_M_HCN1F, BC_M_HCN1F,
       BC_M_HCN1H, BC_M_CAHVA, BC_M_CAHVA, BC_M_CAV23, BC_M_CAV23, BC_M_CAV32, BC_M_CAV32};
-  if (which >= BC_STATE_KV34_M)
+  // extension channels' gates 66 .. 84 in slots 67 .. 85
+  static const uint32_t kExt[BC_NSTATE_VIEW - BC_STATE_HCN2_FAST] = {
+      BC_X_HCN2, BC_X_HCN2, BC_X_KV33, BC_X_KV22,  BC_X_KV22,  BC_X_KV15,  BC_X_KV15,
+      BC_X_KV15, BC_X_NAF,  BC_X_NAF,  BC_X_NAP,   BC_X_NAP,   BC_X_NAIO,  BC_X_NAIO,
+      BC_X_FKDR, BC_X_SKDR, BC_X_KDRIO, BC_X_HCNDCN, BC_X_HCNIO};
+  if (which >= BC_STATE_HCN2_FAST)
+    *bit = ext_bits(kExt[which - BC_STATE_HCN2_FAST]);
+  else if (which >= BC_STATE_KV34_M)
     *bit = kCereb[which - BC_STATE_KV34_M];
   else
     *bit = which < BC_STATE_KCA22_C2 ? BC_M_NAV16 : (which < BC_STATE_KCA11_C1 ? BC_M_KCA22 : BC_M_KCA11);
@@ -127,7 +144,7 @@ struct bc_plan {
   size_t smem_bytes = 0;
   std::vector<int64_t> cell_ncv;
   std::vector<int32_t> cv_tile, cv_node;
-  std::vector<uint32_t> cv_mech;
+  std::vector<uint64_t> cv_mech;  // region bits, extension channels' BC_X_* bits in the high word
   std::vector<bc::PulseRec> pulses;
   std::vector<int64_t> pulse_src;   // spec pulse id of each record (records are in tile / node order)
   std::vector<double> pulse_scale;  // record amp per nA
@@ -382,7 +399,7 @@ struct TileOut {
   std::vector<PortRec> ports;         // stim_begin / stim_end relative to port_pulses
   std::vector<PulseRec> port_pulses;  // amp in nA
   std::vector<std::pair<int64_t, int32_t>> cv_local;  // (global cv id, local node)
-  std::vector<uint32_t> cv_mech;
+  std::vector<uint64_t> cv_mech;
   int64_t crit = 0;
 };
 
@@ -795,7 +812,7 @@ static bc_status build_tile(const BuildCtx& cx, const TileBuild& tb, int T, Tile
     for (int32_t k = 0; k < lc.n_cv; ++k) {
       const int32_t v = lc.cv_node[k];
       out.cv_local.push_back({base + k, node_tile[li][v]});
-      out.cv_mech.push_back(s.region_mech[c * R + lc.region[v]]);
+      out.cv_mech.push_back(region_bits(s, c * R + lc.region[v]));
     }
   }
   // special records: pulses in node order, probe ids
@@ -1293,17 +1310,27 @@ bc_status bc_plan_create(const bc_batch_spec* spec, const bc_plan_options* opts_
   for (int64_t c = 0; c < s.n_cells; ++c) p->cell_ncv[c] = cells[c].n_cv;
   for (int64_t k = 0; k < s.n_cells * s.n_regions; ++k)
     p->extra = p->extra || (s.region_mech[k] & (BC_M_NAHH | BC_M_KHH | BC_M_KM | BC_M_KA1 | BC_M_KA2 | BC_M_KK2A |
-                                                 BC_M_KK2B | BC_M_KNI | kMarkovBits | kCerebellarBits)) != 0;
-  for (int64_t k = 0; k < s.n_cells * s.n_regions; ++k)
+                                                 BC_M_KK2B | BC_M_KNI | kMarkovBits | kCerebellarBits | BC_M_EXT)) != 0;
+  for (int64_t k = 0; k < s.n_cells * s.n_regions; ++k) {
     if (s.region_mech[k] & ~BC_M_ALL) {
       delete p;
       return fail(BC_ERR_INVALID, "unknown mechanism bits in region_mech");
     }
+    if (s.region_mech[k] & BC_M_EXT) {
+      // the record lists its extension channels: an integer of known BC_X_* bits, not 0
+      const double x = s.region_params[k * BC_NPARAM + BC_P_EXT_MASK];
+      if (!(x >= 1.0 && x <= double(BC_X_ALL)) || x != std::floor(x) || (uint32_t(x) & ~BC_X_ALL)) {
+        delete p;
+        return fail(BC_ERR_INVALID, "a region with BC_M_EXT needs BC_X_* bits in its record's BC_P_EXT_MASK");
+      }
+    }
+  }
   uint32_t all_bits = 0;
   for (int64_t k = 0; k < s.n_cells * s.n_regions; ++k) all_bits |= s.region_mech[k];
-  // the Markov and cerebellar states only where a plan has them
-  const int S = (all_bits & kCerebellarBits) ? kNumSlotsCerebellar
-                                             : ((all_bits & kMarkovBits) ? kNumSlotsMarkov : kNumSlots);
+  // the Markov, cerebellar and extension states only where a plan has them
+  const int S = (all_bits & BC_M_EXT) ? kNumSlotsExt
+                                      : ((all_bits & kCerebellarBits) ? kNumSlotsCerebellar
+                                                                      : ((all_bits & kMarkovBits) ? kNumSlotsMarkov : kNumSlots));
   p->state_slots = S;
   // ---------------------------------------------------- pulses / probes -> nodes
   std::vector<std::vector<int64_t>> cell_pulses(s.n_cells), cell_probes(s.n_cells);
@@ -1345,26 +1372,31 @@ bc_status bc_plan_create(const bc_batch_spec* spec, const bc_plan_options* opts_
       return fail(BC_ERR_INVALID, "probe_field is not a recordable BC_STATE_* view or a BC_PROBE_CURRENT code");
     }
     if (is_current) {
-      static const uint32_t cur_owner[BC_NCUR] = {
+      static const uint64_t cur_owner[BC_NCUR] = {
           BC_M_IL,  BC_M_KLEAK, BC_M_NA,   BC_M_KDR, BC_M_CAL,           BC_M_CAT,
-          BC_M_HCN, BC_M_AHP,   BC_M_NAHH, BC_M_KHH, BC_M_KM,            BC_M_NA | BC_M_NAHH | BC_M_NAV16,
+          BC_M_HCN, BC_M_AHP,   BC_M_NAHH, BC_M_KHH, BC_M_KM,
+          BC_M_NA | BC_M_NAHH | BC_M_NAV16 | ext_bits(BC_X_NAF | BC_X_NAP | BC_X_NAIO),
           BC_M_KDR | BC_M_KLEAK | BC_M_AHP | BC_M_KHH | BC_M_KM | BC_M_KA1 | BC_M_KA2 | BC_M_KK2A | BC_M_KK2B | BC_M_KNI |
-              BC_M_KCA22 | BC_M_KCA11 | BC_M_KV34 | BC_M_KV43 | BC_M_KV11 | BC_M_KIR23,
+              BC_M_KCA22 | BC_M_KCA11 | BC_M_KV34 | BC_M_KV43 | BC_M_KV11 | BC_M_KIR23 |
+              ext_bits(BC_X_KV33 | BC_X_KV22 | BC_X_KV15 | BC_X_FKDR | BC_X_SKDR | BC_X_KDRIO),
           BC_M_CAL | BC_M_CAT | BC_M_CAHVA | BC_M_CAV23 | BC_M_CAV32,  BC_M_KA1,  BC_M_KA2, BC_M_KK2A, BC_M_KK2B, BC_M_KNI,
           BC_M_NAV16, BC_M_KCA22, BC_M_KCA11, BC_M_KV34, BC_M_KV43, BC_M_KV11, BC_M_KIR23, BC_M_HCN1F, BC_M_HCN1H,
-          BC_M_CAHVA, BC_M_CAV23, BC_M_CAV32};
+          BC_M_CAHVA, BC_M_CAV23, BC_M_CAV32,
+          ext_bits(BC_X_HCN2), ext_bits(BC_X_KV33), ext_bits(BC_X_KV22), ext_bits(BC_X_KV15), ext_bits(BC_X_NAF),
+          ext_bits(BC_X_NAP), ext_bits(BC_X_NAIO), ext_bits(BC_X_FKDR), ext_bits(BC_X_SKDR), ext_bits(BC_X_KDRIO),
+          ext_bits(BC_X_HCNDCN), ext_bits(BC_X_HCNIO)};
       const int32_t rg = cells[c].region[v];
-      if (rg < 0 || !(s.region_mech[c * s.n_regions + rg] & cur_owner[field - BC_PROBE_CURRENT])) {
+      if (rg < 0 || !(region_bits(s, c * s.n_regions + rg) & cur_owner[field - BC_PROBE_CURRENT])) {
         delete p;
         return fail(BC_ERR_INVALID, "probe current: no such mechanism at the probed location");
       }
     } else if (field != BC_STATE_V) {
       // the mechanism that owns the state must be present at the probed CV
-      uint32_t owner = 0;
+      uint64_t owner = 0;
       int slot = -1;
       state_view(field, &owner, &slot);
       const int32_t rg = cells[c].region[v];
-      if (rg < 0 || !(s.region_mech[c * s.n_regions + rg] & owner)) {
+      if (rg < 0 || !(region_bits(s, c * s.n_regions + rg) & owner)) {
         delete p;
         return fail(BC_ERR_INVALID, "probe field: no such mechanism at the probed location");
       }
@@ -1612,7 +1644,7 @@ bc_status bc_plan_create(const bc_batch_spec* spec, const bc_plan_options* opts_
   }
   BuildCtx cx{&s, &cells, &sched, &cv_base, &cell_pulses, &cell_probes, &pulse_node, &probe_node, &cell_syns, &is_src,
               &cell_ports, &port_pulse_ids, p->precision, S, p->lane_nodes, p->narrow_lane_nodes,
-              p->extra ? kParamStride : kParamStrideCore};
+              p->extra ? ((all_bits & BC_M_EXT) ? kParamStride : kParamStrideExtra) : kParamStrideCore};
   std::vector<TileOut> outs;
   outs.reserve(builds.size());
   // Packed tiles: tile_nodes sets how many CTAs share an SM (by the per-node
@@ -2141,7 +2173,7 @@ static bc_status view_offsets(bc_plan* p, int32_t which, std::vector<int64_t>& h
       lo[k] = hi[k] + rs;
       continue;
     }
-    uint32_t bit = 0;
+    uint64_t bit = 0;
     int slot = -1;
     state_view(which, &bit, &slot);
     if (which != BC_STATE_V_LAST && !(p->cv_mech[k] & bit)) slot = -1;
@@ -2258,7 +2290,7 @@ static void noalloc_offset(const bc_plan* p, int32_t which, int64_t k, int64_t* 
     *lo = *hi + rs;
     return;
   }
-  uint32_t bit = 0;
+  uint64_t bit = 0;
   int slot = -1;
   state_view(which, &bit, &slot);
   if (which != BC_STATE_V_LAST && !(p->cv_mech[k] & bit)) return;

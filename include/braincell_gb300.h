@@ -78,10 +78,31 @@ typedef int32_t bc_status;
 #define BC_M_CAHVA (1u << 26)    /* channel/calcium.py:4333 CaHVA_MA2020_GoC s^2 u, E_Ca              */
 #define BC_M_CAV23 (1u << 27)    /* channel/calcium.py:4672 Cav2p3_MA2020_GoC m^3 h, E_Ca             */
 #define BC_M_CAV32 (1u << 28)    /* channel/calcium.py:3636 Cav3p2_RI2021_SC m^2 h, E_Ca              */
-#define BC_M_ALL 0x1FFFFFFFu
+/* Extension channels (extra kernel variant): a region that carries any sets
+ * BC_M_EXT and lists them as BC_X_* bits in its record entry BC_P_EXT_MASK (an
+ * integer below 2^24, exact in FP32); their parameters follow that entry. */
+#define BC_M_EXT (1u << 29)
+#define BC_M_ALL 0x3FFFFFFFu
+
+#define BC_X_HCN2 (1u << 0)    /* channel/hyperpolarization_activated.py:838 HCN2_MA2020_GoC
+                                  o_fast + o_slow, own E, Q10 1.5 on g                        */
+#define BC_X_KV33 (1u << 1)    /* channel/potassium.py:2937 Kv3p3_MA2024_PC n^4, E_K          */
+#define BC_X_KV22 (1u << 2)    /* channel/potassium.py:5664 Kv2p2_0010_MA2020_GrC m h, E_K    */
+#define BC_X_KV15 (1u << 3)    /* channel/potassium.py:2735 Kv1p5_MA2024_PC m^3 n u f(V), E_K */
+#define BC_X_NAF (1u << 4)     /* channel/sodium.py:402 NaF_SU2015_DCN m^3 h, E_Na            */
+#define BC_X_NAP (1u << 5)     /* channel/sodium.py:500 NaP_SU2015_DCN m^3 h, E_Na            */
+#define BC_X_NAIO (1u << 6)    /* channel/sodium.py:598 Na_ZH2019_IO m^3 h, E_Na              */
+#define BC_X_FKDR (1u << 7)    /* channel/potassium.py:1374 fKdr_SU2015_DCN m^4, E_K          */
+#define BC_X_SKDR (1u << 8)    /* channel/potassium.py:1485 sKdr_SU2015_DCN m^4, E_K          */
+#define BC_X_KDRIO (1u << 9)   /* channel/potassium.py:6238 Kdr_ZH2019_IO n^4, E_K            */
+#define BC_X_HCNDCN (1u << 10) /* channel/hyperpolarization_activated.py:1010 HCN_SU2015_DCN
+                                  m^2, own E                                                  */
+#define BC_X_HCNIO (1u << 11)  /* channel/hyperpolarization_activated.py:1109 HCN_ZH2019_IO
+                                  q, own E                                                    */
+#define BC_X_ALL 0xFFFu
 
 /* Per-region parameter record (double[BC_NPARAM]); index names below. */
-#define BC_NPARAM 96
+#define BC_NPARAM 160
 #define BC_P_INVCM 0      /* 1 / membrane capacitance, cm^2/uF                 */
 #define BC_P_VREST 1      /* voltage used by reset (mV)                        */
 #define BC_P_ENA 2        /* fixed reversal potentials (mV)                    */
@@ -178,6 +199,29 @@ typedef int32_t bc_status;
 #define BC_P_CAV32_G 93
 #define BC_P_CAV32_VSH 94
 /* 95: reserved (0) */
+#define BC_P_EXT_MASK 96    /* BC_X_* bits of the region's extension channels       */
+#define BC_P_HCN2_G 97      /* g_max x 1.5^((T - 23 degC) / 10)                     */
+#define BC_P_HCN2_E 98
+#define BC_P_HCN2_PHI 99    /* 3^((T - 23 degC) / 10)                               */
+#define BC_P_KV33_G 100
+#define BC_P_KV33_PHI 101   /* 2.7^((T - 22 degC) / 10)                             */
+#define BC_P_KV22_G 102
+#define BC_P_KV15_G 103
+#define BC_P_KV15_Q10 104   /* 2.2^((T - 37 degC) / 10), on the m and n rates       */
+#define BC_P_KV15_TACT 105  /* Tauact, Tauinactf, Tauinacts: time-constant scales   */
+#define BC_P_KV15_TINF 106
+#define BC_P_KV15_TINS 107
+#define BC_P_NAF_G 108
+#define BC_P_NAP_G 109
+#define BC_P_NAIO_G 110
+#define BC_P_FKDR_G 111
+#define BC_P_SKDR_G 112
+#define BC_P_KDRIO_G 113
+#define BC_P_HCNDCN_G 114
+#define BC_P_HCNDCN_E 115
+#define BC_P_HCNIO_G 116
+#define BC_P_HCNIO_E 117
+/* 118 .. 159: reserved for further extension channels (0) */
 
 /* ------------------------------------------------------------------ batch spec */
 /*
@@ -341,8 +385,10 @@ const char* bc_last_error(void);
  * channels (BC_M_NAV16 / KCA22 / KCA11, a 74-entry parameter record, state views
  * 25-50), lane tiles (bc_plan_options.lane_cell_nodes, tile_order), the cerebellar
  * HH and calcium channels (BC_M_KV34 .. CAV32, a 96-entry parameter record, state
- * views 51-65, BC_PROBE_CURRENT 128). */
-#define BC_ABI_VERSION 400
+ * views 51-65, BC_PROBE_CURRENT 128).  0.5.0: extension channels (BC_M_EXT with
+ * BC_X_* bits in the record's BC_P_EXT_MASK, a 160-entry parameter record, state
+ * views 66-84, current codes 31-42). */
+#define BC_ABI_VERSION 500
 int32_t bc_version(void);
 /* Fill opts with defaults. */
 void bc_default_options(bc_plan_options* opts);
@@ -442,7 +488,27 @@ bc_status bc_check(bc_plan_t plan, void* stream);
 #define BC_STATE_CAV23_H 63
 #define BC_STATE_CAV32_M 64
 #define BC_STATE_CAV32_H 65
-#define BC_NSTATE_VIEW 66
+/* extension channels' gates */
+#define BC_STATE_HCN2_FAST 66
+#define BC_STATE_HCN2_SLOW 67
+#define BC_STATE_KV33_N 68
+#define BC_STATE_KV22_M 69
+#define BC_STATE_KV22_H 70
+#define BC_STATE_KV15_M 71
+#define BC_STATE_KV15_N 72
+#define BC_STATE_KV15_U 73
+#define BC_STATE_NAF_M 74
+#define BC_STATE_NAF_H 75
+#define BC_STATE_NAP_M 76
+#define BC_STATE_NAP_H 77
+#define BC_STATE_NAIO_M 78
+#define BC_STATE_NAIO_H 79
+#define BC_STATE_FKDR_M 80
+#define BC_STATE_SKDR_M 81
+#define BC_STATE_KDRIO_N 82
+#define BC_STATE_HCNDCN_M 83
+#define BC_STATE_HCNIO_Q 84
+#define BC_NSTATE_VIEW 85
 /* Current probes (mech/_point.py CurrentProbe, _multi_compartment/probes.py:184-258):
    probe_field = BC_PROBE_CURRENT + one of the codes below records that current
    density (uA/cm^2, outward negative as g (E - V)) after the step.             */
@@ -478,7 +544,19 @@ bc_status bc_check(bc_plan_t plan, void* stream);
 #define BC_CUR_CAHVA 28  /* CaHVA_MA2020_GoC  */
 #define BC_CUR_CAV23 29  /* Cav2p3_MA2020_GoC */
 #define BC_CUR_CAV32 30  /* Cav3p2_RI2021_SC  */
-#define BC_NCUR 31
+#define BC_CUR_HCN2 31   /* HCN2_MA2020_GoC        */
+#define BC_CUR_KV33 32   /* Kv3p3_MA2024_PC        */
+#define BC_CUR_KV22 33   /* Kv2p2_0010_MA2020_GrC  */
+#define BC_CUR_KV15 34   /* Kv1p5_MA2024_PC        */
+#define BC_CUR_NAF 35    /* NaF_SU2015_DCN         */
+#define BC_CUR_NAP 36    /* NaP_SU2015_DCN         */
+#define BC_CUR_NAIO 37   /* Na_ZH2019_IO           */
+#define BC_CUR_FKDR 38   /* fKdr_SU2015_DCN        */
+#define BC_CUR_SKDR 39   /* sKdr_SU2015_DCN        */
+#define BC_CUR_KDRIO 40  /* Kdr_ZH2019_IO          */
+#define BC_CUR_HCNDCN 41 /* HCN_SU2015_DCN         */
+#define BC_CUR_HCNIO 42  /* HCN_ZH2019_IO          */
+#define BC_NCUR 43
 bc_status bc_state_download(bc_plan_t plan, int32_t which, double* out /* [n_cv] */, void* stream);
 /* Set the amplitude (nA) of every current-clamp pulse of the batch spec, in spec
  * order (amp_nA[n_pulses]); times and locations are unchanged.  Takes effect from

@@ -124,6 +124,22 @@ CHANNEL_DEFAULTS.update({
     "Cav2p3_MA2020_GoC": dict(g_max=0.0, temp=_c2k(34.0)),  # calcium.py:4672
     "Cav3p2_RI2021_SC": dict(g_max=8.0e-4, V_sh=0.0, temp=_c2k(36.0)),  # calcium.py:3636
 })
+# extension channels (conductances in mS/cm^2)
+CHANNEL_DEFAULTS.update({
+    "HCN2_MA2020_GoC": dict(g_max=0.08, E=-20.0, temp=_c2k(22.0)),  # hyperpolarization_activated.py:838
+    "Kv3p3_MA2024_PC": dict(g_max=5.0, temp=_c2k(22.0), gateCurrent=0.0),  # potassium.py:2937 (0.005 S/cm^2)
+    "Kv2p2_0010_MA2020_GrC": dict(g_max=0.01, BBiD=10.0),  # potassium.py:5664
+    "Kv1p5_MA2024_PC": dict(g_max=0.13195, temp=_c2k(37.0), Tauact=1.0, Tauinactf=1.0,
+                            Tauinacts=1.0),  # potassium.py:2735 (0.13195e-3 S/cm^2)
+    "NaF_SU2015_DCN": dict(g_max=0.01),  # sodium.py:402
+    "NaP_SU2015_DCN": dict(g_max=0.01),  # sodium.py:500
+    "Na_ZH2019_IO": dict(g_max=70.0),  # sodium.py:598
+    "fKdr_SU2015_DCN": dict(g_max=0.01),  # potassium.py:1374
+    "sKdr_SU2015_DCN": dict(g_max=0.01),  # potassium.py:1485
+    "Kdr_ZH2019_IO": dict(g_max=18.0),  # potassium.py:6238
+    "HCN_SU2015_DCN": dict(g_max=0.01, E=-45.0),  # hyperpolarization_activated.py:1010
+    "HCN_ZH2019_IO": dict(g_max=0.15, E=-43.0),  # hyperpolarization_activated.py:1109
+})
 # cell-type variants that run their base class's kinetics, with their own defaults
 # where they differ (each class body is the base's: potassium.py, hyperpolarization_activated.py)
 _VARIANTS = {
@@ -378,6 +394,20 @@ def ca_detailed_rate(I_ca, Ci, d, tau, C_rest):
     return drive + (C_rest - Ci) / tau
 
 
+def _x_over_1mexp(x):
+    """x / (1 - e^-x), with 1 + x / 2 for |x| < 1e-6 (channel/sodium.py:50-55)."""
+    x = np.asarray(x, dtype=float)
+    small = np.abs(x) < 1e-6
+    safe = np.where(small, 1.0, x)
+    return np.where(small, 1.0 + x / 2.0, safe / (1.0 - np.exp(-safe)))
+
+
+def kv15_vfactor(V):
+    """Kv1p5_MA2024_PC's voltage factor f(V) and f'(V) (potassium.py:2735-2935)."""
+    s = 1.0 / (1.0 + np.exp(-(V - 15.0) / 13.0))
+    return 0.1 + s, s * (1.0 - s) / 13.0
+
+
 def rates(name: str, V, p: dict, Ci=None):
     """Gate rate functions, keyed by gate: returns {gate: ("ab", alpha, beta) | ("it", inf, tau)}."""
     if name == "Na_Ba2002":  # sodium.py:154-170
@@ -500,6 +530,51 @@ def rates(name: str, V, p: dict, Ci=None):
         return {"m": ("it", 1.0 / (1.0 + np.exp(-(Vs + 54.8) / 7.4)),
                       1.9 + 1.0 / (np.exp((Vs + 37.0) / 11.9) + np.exp(-(Vs + 131.6) / 21.0))),
                 "h": ("it", 1.0 / (1.0 + np.exp((Vs + 85.5) / 7.18)), 13.7 + term / phi_h)}
+    if name == "HCN2_MA2020_GoC":  # hyperpolarization_activated.py:838-1008
+        o = 1.0 / (1.0 + np.exp((V - -81.95) * 0.1661))
+        r = np.where(V >= -64.70, 0.0, np.where(V <= -108.70, 1.0, -0.0227 * V + -1.4694))
+        return {"o_fast": ("it", r * o, np.exp(((0.0269 * V) - -5.6111) * 2.3026)),
+                "o_slow": ("it", (1.0 - r) * o, np.exp(((0.0152 * V) - -5.2944) * 2.3026))}
+    if name == "Kv3p3_MA2024_PC":  # potassium.py:2937-3124
+        return {"n": ("ab", 0.22 * np.exp(-(V + 16.0) / -26.5), 0.22 * np.exp(-(V + 16.0) / 26.5))}
+    if name == "Kv2p2_0010_MA2020_GrC":  # potassium.py:5664-5804
+        return {"m": ("it", 1.0 / (1.0 + np.exp((V - 5.0) / -12.0)), 130.0 / (1.0 + np.exp((V + 46.56) / -44.14))),
+                "h": ("it", 1.0 / (1.0 + np.exp((V + 16.3) / 4.8)), 10000.0 / (1.0 + np.exp((V + 46.56) / -44.14)))}
+    if name == "Kv1p5_MA2024_PC":  # potassium.py:2735-2935; q10 2.2 at 37 degC on the m and n rates
+        q = 2.2 ** (((p["temp"] - _c2k(37.0))) / 10.0)
+        am = q * 0.65 / (np.exp(-(V + 10.0) / 8.5) + np.exp(-(V - 30.0) / 59.0))
+        bm = q * 0.65 / (2.5 + np.exp((V + 82.0) / 17.0))
+        an = q * 0.001 / (2.4 + 10.9 * np.exp(-(V + 90.0) / 78.0))
+        bn = q * 0.001 * np.exp((V - 168.0) / 16.0)
+        return {"m": ("it", 1.0 / (1.0 + np.exp(-(V + 30.3) / 9.6)), 1.0 / (am + bm) / 3.0 * p["Tauact"]),
+                "n": ("it", 0.25 + 1.0 / (1.35 + np.exp((V + 7.0) / 14.0)), 1.0 / (an + bn) / 3.0 * p["Tauinactf"]),
+                "u": ("it", 0.1 + 1.0 / (1.1 + np.exp((V + 7.0) / 14.0)), 6800.0 * p["Tauinacts"] * np.ones_like(V))}
+    if name == "NaF_SU2015_DCN":  # sodium.py:402-498 (qdeltat 1)
+        return {"m": ("it", 1.0 / (1.0 + np.exp((V + 45.0) / -7.3)),
+                      5.83 / (np.exp((V - 6.4) / -9.0) + np.exp((V + 97.0) / 17.0)) + 0.025),
+                "h": ("it", 1.0 / (1.0 + np.exp((V + 42.0) / 5.9)),
+                      16.67 / (np.exp((V - 8.3) / -29.0) + np.exp((V + 66.0) / 9.0)) + 0.2)}
+    if name == "NaP_SU2015_DCN":  # sodium.py:500-596
+        return {"m": ("it", 1.0 / (1.0 + np.exp((V + 70.0) / -4.1)), 50.0 * np.ones_like(V)),
+                "h": ("it", 1.0 / (1.0 + np.exp((V + 80.0) / 4.0)), 1750.0 / (1.0 + np.exp((V + 65.0) / -8.0)) + 250.0)}
+    if name == "Na_ZH2019_IO":  # sodium.py:598-725
+        am, bm = _x_over_1mexp((V + 41.0) / 10.0), 9.0 * np.exp(-(V + 66.0) / 20.0)
+        ah, bh = 5.0 * np.exp(-(V + 60.0) / 15.0), 10.0 * _x_over_1mexp((V + 50.0) / 10.0)
+        return {"m": ("it", am / (am + bm), 0.001 * np.ones_like(V)), "h": ("it", ah / (ah + bh), 250.0 / (ah + bh))}
+    if name == "fKdr_SU2015_DCN":  # potassium.py:1374-1483
+        return {"m": ("it", 1.0 / (1.0 + np.exp((V + 40.0) / -7.8)),
+                      13.9 / (np.exp((V + 40.0) / 12.0) + np.exp((V + 40.0) / -13.0)) + 0.1)}
+    if name == "sKdr_SU2015_DCN":  # potassium.py:1485-1595
+        return {"m": ("it", 1.0 / (1.0 + np.exp((V + 50.0) / -9.1)),
+                      14.95 / (np.exp((V + 50.0) / 21.74) + np.exp((V + 50.0) / -13.91)) + 0.05)}
+    if name == "Kdr_ZH2019_IO":  # potassium.py:6238-6374
+        a, b = 10.0 * _x_over_1mexp((V + 41.0) / 10.0), 12.5 * np.exp(-(V + 51.0) / 80.0)
+        return {"n": ("it", a / (a + b), 10.0 / (a + b))}
+    if name == "HCN_SU2015_DCN":  # hyperpolarization_activated.py:1010-1107
+        return {"m": ("it", 1.0 / (1.0 + np.exp((V + 80.0) / 5.0)), 400.0 * np.ones_like(V))}
+    if name == "HCN_ZH2019_IO":  # hyperpolarization_activated.py:1109-1217
+        return {"q": ("it", 1.0 / (1.0 + np.exp((V + 75.0) / 5.5)),
+                      1.0 / (np.exp(-0.086 * V - 14.6) + np.exp(0.07 * V - 1.87)))}
     if name in ("KM_RI2021_SC", "KM_MA2020_GoC", "KM_MA2020_GrC"):  # potassium.py:1735-1748, :4553-4567, :5317-5331
         a = 0.0033 * np.exp((V + 30.0) / 40.0)
         b = 0.0033 * np.exp((V + 30.0) / -20.0)
@@ -536,6 +611,18 @@ _GATES = {  # (gate, power, phi-key)
     "CaHVA_MA2020_GoC": (("s", 2, "phi"), ("u", 1, "phi")),
     "Cav2p3_MA2020_GoC": (("m", 3, "phi"), ("h", 1, "phi")),
     "Cav3p2_RI2021_SC": (("m", 2, "phi_m"), ("h", 1, "phi")),
+    "HCN2_MA2020_GoC": (("o_fast", 1, "phi"), ("o_slow", 1, "phi")),
+    "Kv3p3_MA2024_PC": (("n", 4, "phi"),),
+    "Kv2p2_0010_MA2020_GrC": (("m", 1, "phi"), ("h", 1, "phi")),
+    "Kv1p5_MA2024_PC": (("m", 3, "phi"), ("n", 1, "phi"), ("u", 1, "phi")),
+    "NaF_SU2015_DCN": (("m", 3, "phi"), ("h", 1, "phi")),
+    "NaP_SU2015_DCN": (("m", 3, "phi"), ("h", 1, "phi")),
+    "Na_ZH2019_IO": (("m", 3, "phi"), ("h", 1, "phi")),
+    "fKdr_SU2015_DCN": (("m", 4, "phi"),),
+    "sKdr_SU2015_DCN": (("m", 4, "phi"),),
+    "Kdr_ZH2019_IO": (("n", 4, "phi"),),
+    "HCN_SU2015_DCN": (("m", 2, "phi"),),
+    "HCN_ZH2019_IO": (("q", 1, "phi"),),
 }
 _ION_OF = {"Na_Ba2002": "na", "KDR_Ba2002": "k", "CaL_IS2008": "ca", "CaT_HM1992": "ca",
            "K_Leak": "k", "AHP_De1994": "k", "Na_HH1952": "na", "K_HH1952": "k", "KM_RI2021_SC": "k",
@@ -544,9 +631,12 @@ _ION_OF = {"Na_Ba2002": "na", "KDR_Ba2002": "k", "CaL_IS2008": "ca", "CaT_HM1992
            "KNI_Ya1989": "k", "Nav1p6_MA2020_GoC": "na", "Kca2p2_MA2020_GoC": "k", "Kca1p1_MA2020_GoC": "k",
            "Kv3p4_MA2020_GoC": "k", "Kv4p3_MA2020_GoC": "k", "Kv1p1_MA2020_GoC": "k", "Kir2p3_MA2020_GrC": "k",
            "Nav1p1_MA2025_BC": "na", "Nav1p1_RI2021_SC": "na",
-           "CaHVA_MA2020_GoC": "ca", "Cav2p3_MA2020_GoC": "ca", "Cav3p2_RI2021_SC": "ca"}
+           "CaHVA_MA2020_GoC": "ca", "Cav2p3_MA2020_GoC": "ca", "Cav3p2_RI2021_SC": "ca",
+           "Kv3p3_MA2024_PC": "k", "Kv2p2_0010_MA2020_GrC": "k", "Kv1p5_MA2024_PC": "k", "NaF_SU2015_DCN": "na",
+           "NaP_SU2015_DCN": "na", "Na_ZH2019_IO": "na", "fKdr_SU2015_DCN": "k", "sKdr_SU2015_DCN": "k",
+           "Kdr_ZH2019_IO": "k"}
 # channels with their own reversal potential (HHTypedNeuron root, not an ion)
-_OWN_E = ("HCN_HM1992", "HCN1_MA2020_GoC", "HCN1_MA2024_PC")
+_OWN_E = ("HCN_HM1992", "HCN1_MA2020_GoC", "HCN1_MA2024_PC", "HCN2_MA2020_GoC", "HCN_SU2015_DCN", "HCN_ZH2019_IO")
 
 
 def _resolve(table: dict, decl) -> dict:
@@ -591,6 +681,16 @@ def _resolve(table: dict, decl) -> dict:
     elif name == "Cav3p2_RI2021_SC":  # Gate("m", phi=5^((36 - 24) / 10)); h: 1
         p["phi_m"] = 5.0 ** ((36.0 - 24.0) / 10.0)
         p["phi"] = 1.0
+    elif name == "HCN2_MA2020_GoC":  # gates q10 3 and the conductance Q10_diff 1.5, at 23 degC
+        p["phi"] = 3.0 ** ((p["temp"] - _c2k(23.0)) / 10.0)
+        p["gbar_phi"] = 1.5 ** ((p["temp"] - _c2k(23.0)) / 10.0)
+    elif name == "Kv3p3_MA2024_PC":  # Gate q10 2.7 at 22 degC
+        if p["gateCurrent"] != 0.0:
+            raise ValueError("Kv3p3 gating current not restated")
+        p["phi"] = 2.7 ** ((p["temp"] - _c2k(22.0)) / 10.0)
+    elif name in ("Kv2p2_0010_MA2020_GrC", "Kv1p5_MA2024_PC", "NaF_SU2015_DCN", "NaP_SU2015_DCN", "Na_ZH2019_IO",
+                  "fKdr_SU2015_DCN", "sKdr_SU2015_DCN", "Kdr_ZH2019_IO", "HCN_SU2015_DCN", "HCN_ZH2019_IO"):
+        p["phi"] = 1.0  # gates without q10 or phi (Kv1p5's Q10 sits in its rates)
     return p
 
 
@@ -1057,7 +1157,7 @@ class OracleCell:
         return np.where(cd["mask"], nernst, self.E_ca_fixed)
 
     def _gate_product(self, name):
-        if name == "HCN1_MA2020_GoC":  # g (o_fast + o_slow) with the conductance's own Q10 factor
+        if name in ("HCN1_MA2020_GoC", "HCN2_MA2020_GoC"):  # g (o_fast + o_slow) with the conductance's Q10 factor
             return self.chan[name]["gbar_phi"] * (self.gates[(name, "o_fast")] + self.gates[(name, "o_slow")])
         if name in MK.SCHEMES:  # the open occupancy of the raw stored states
             sch = MK.SCHEMES[name]
@@ -1086,6 +1186,11 @@ class OracleCell:
             else:
                 E, fac = E_of[_ION_OF[name]], self._gate_product(name)
             geff = g * fac
+            if name == "Kv1p5_MA2024_PC":  # g f(V) gates (E - V): dI/dV = g gates (f'(V) (E - V) - f(V))
+                f, df = kv15_vfactor(pv)
+                I = I + geff * f * (E - pv)
+                dI = dI + geff * (df * (E - pv) - f)
+                continue
             I = I + geff * (E - pv)
             dI = dI - geff
         return I, dI
@@ -1106,6 +1211,8 @@ class OracleCell:
                 E, fac = ch["E"], self._gate_product(name)
             else:
                 E, fac = E_of[_ION_OF[name]], self._gate_product(name)
+            if name == "Kv1p5_MA2024_PC":
+                fac = fac * kv15_vfactor(pv)[0]
             cur = ch["g_max"] * fac * (E - pv)
             return cur[:, pid] if np.ndim(cur) == 2 else np.full(self.P, float(cur))
 

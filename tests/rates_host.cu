@@ -1,18 +1,19 @@
 // Test harness: the FP64 rate structures of the step kernel's mechanism header,
 // compiled for the host, so that tests/test_rates_host.py can compare them with
 // the oracle's rate functions on a CPU.  Not part of the library.
-#include "../braincell_gb300/csrc/bc_mech.cuh"
+#include "../braincell_gb300/csrc/bc_ext.cuh"
 
 using namespace bc;
 
 // Kernel rate structure `which` at n voltages v (mV) with parameters prm (V_sh
-// first; KNI: V_sh, tau_max).  out[4 i .. 4 i + 3] receives the gate rates in the
-// oracle's order: per gate (alpha, beta) or (inf, tau); unused entries are 0.
+// first; KNI: V_sh, tau_max; Kv1p5: its Q10 factor, Tauact, Tauinactf, Tauinacts).
+// out[6 i .. 6 i + 5] receives the gate rates in the oracle's order: per gate
+// (alpha, beta) or (inf, tau); unused entries are 0.
 // Returns 0, or -1 for an unknown structure.
 extern "C" int bc_test_rates(int which, const double* v, int n, const double* prm, double* out) {
   for (int i = 0; i < n; ++i) {
-    double* o = out + 4 * i;
-    o[0] = o[1] = o[2] = o[3] = 0.0;
+    double* o = out + 6 * i;
+    o[0] = o[1] = o[2] = o[3] = o[4] = o[5] = 0.0;
     const double x = v[i];
     switch (which) {
       case 0: { const NaRates<double> r(x, prm[0]); o[0] = r.ap; o[1] = r.bp; o[2] = r.aq; o[3] = r.bq; break; }
@@ -45,6 +46,22 @@ extern "C" int bc_test_rates(int which, const double* v, int n, const double* pr
       case 19: { const CaHvaRates<double> r(x); o[0] = r.sa; o[1] = r.sb; o[2] = r.ua; o[3] = r.ub; break; }
       case 20: { const Cav23Rates<double> r(x); o[0] = r.minf; o[1] = r.mtau; o[2] = r.hinf; o[3] = r.htau; break; }
       case 21: { const Cav32Rates<double> r(x, prm[0]); o[0] = r.minf; o[1] = r.mtau; o[2] = r.hinf; o[3] = r.htau; break; }
+      case 22: { const Hcn2Rates<double> r(x); o[0] = r.finf; o[1] = r.ftau; o[2] = r.sinf; o[3] = r.stau; break; }
+      case 23: { const Kv33Rates<double> r(x); o[0] = r.a; o[1] = r.b; break; }
+      case 24: { const Kv22Rates<double> r(x); o[0] = r.minf; o[1] = r.mtau; o[2] = r.hinf; o[3] = r.htau; break; }
+      case 25: {
+        const Kv15Rates<double> r(x, prm[0], prm[1], prm[2]);
+        o[0] = r.minf; o[1] = r.mtau; o[2] = r.ninf; o[3] = r.ntau; o[4] = r.uinf; o[5] = kKv15TauU * prm[3];
+        break;
+      }
+      case 26: { const NafRates<double> r(x); o[0] = r.minf; o[1] = r.mtau; o[2] = r.hinf; o[3] = r.htau; break; }
+      case 27: { const NapRates<double> r(x); o[0] = r.minf; o[1] = r.mtau; o[2] = r.hinf; o[3] = r.htau; break; }
+      case 28: { const NaioRates<double> r(x); o[0] = r.minf; o[1] = r.mtau; o[2] = r.hinf; o[3] = r.htau; break; }
+      case 29: { const Su2015KdrRates<double> r = fkdr_rates(x); o[0] = r.minf; o[1] = r.mtau; break; }
+      case 30: { const Su2015KdrRates<double> r = skdr_rates(x); o[0] = r.minf; o[1] = r.mtau; break; }
+      case 31: { const KdrioRates<double> r(x); o[0] = r.ninf; o[1] = r.ntau; break; }
+      case 32: { const HcndcnRates<double> r(x); o[0] = r.minf; o[1] = r.mtau; break; }
+      case 33: { const HcnioRates<double> r(x); o[0] = r.qinf; o[1] = r.qtau; break; }
       default: return -1;
     }
   }

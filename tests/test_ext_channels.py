@@ -1,0 +1,139 @@
+"""Extension channels (BC_M_EXT with BC_X_* bits in the record): HCN2_MA2020_GoC,
+Kv3p3_MA2024_PC, Kv2p2_0010_MA2020_GrC, Kv1p5_MA2024_PC, the SU2015 DCN sodium /
+potassium / HCN classes and the ZH2019 IO sodium / potassium / HCN classes.
+
+CPU: the records and their mask, the planner's check of the mask, and the owner
+tables (through the planner tests).  GPU: a DCN-like cell and an IO-like cell
+against the float64 oracle (FP64 at 1e-8 mV, or within a 1e-9 ms time shift on the
+upstrokes; gate and current probes, spikes), and FP32 against FP64.
+"""
+
+import numpy as np
+import pytest
+
+from braincell_gb300 import Branch, Cell, Morphology, _abi, catalogue
+from braincell_gb300.mech import (AllRegion, CableProperty, Channel, CurrentClamp, CurrentProbe, CVPerBranch,
+                                  MechanismProbe, RootLocation, StateProbe, at, branch_in)
+from oracle import staggered as O
+
+DT = 0.025
+SHIFT_MS = 1e-9
+
+
+def _close(gpu, ref, atol, rtol=0.0, what=""):
+    """|gpu - ref| <= atol + rtol |ref| + SHIFT_MS |d ref / dt| (the spike-time bar as a
+    time shift on the fast upstrokes)."""
+    gpu, ref = np.atleast_2d(gpu), np.atleast_2d(ref)
+    bound = atol + rtol * np.abs(ref) + SHIFT_MS * np.abs(np.gradient(ref, DT, axis=-1))
+    bad = np.abs(gpu - ref) > bound
+    assert not bad.any(), f"{what}: {int(bad.sum())} samples off, worst {float((np.abs(gpu - ref) - bound).max()):.3e}"
+
+
+def test_extension_records():
+    cable = CableProperty()
+    bits, rec = catalogue.region_record([Channel("HCN2_MA2020_GoC"), Channel("Kv1p5_MA2024_PC", temp=O._c2k(30.0)),
+                                         Channel("Na_ZH2019_IO")], cable)
+    assert bits == _abi.BC_M_EXT
+    assert int(rec[_abi.BC_P_EXT_MASK]) == _abi.BC_X_HCN2 | _abi.BC_X_KV15 | _abi.BC_X_NAIO
+    # HCN2's conductance carries its Q10 1.5 factor, its gates q10 3, both at 23 degC
+    assert rec[_abi.BC_P_HCN2_G] == pytest.approx(0.08 * 1.5 ** (-0.1), rel=1e-12)
+    assert rec[_abi.BC_P_HCN2_PHI] == pytest.approx(3.0 ** (-0.1), rel=1e-12)
+    assert rec[_abi.BC_P_KV15_Q10] == pytest.approx(2.2 ** (-0.7), rel=1e-12)
+    assert rec[_abi.BC_P_NAIO_G] == 70.0
+    # the defaults of the reference classes, in mS/cm^2 (Kv3p3 0.005 S/cm^2, Kv1p5 0.13195e-3 S/cm^2)
+    _, rec = catalogue.region_record([Channel("Kv3p3_MA2024_PC"), Channel("Kv1p5_MA2024_PC")], cable)
+    assert rec[_abi.BC_P_KV33_G] == 5.0 and rec[_abi.BC_P_KV15_G] == pytest.approx(0.13195)
+    # no extension channel: no mask, no bit
+    bits, rec = catalogue.region_record([Channel("IL")], cable)
+    assert not bits & _abi.BC_M_EXT and rec[_abi.BC_P_EXT_MASK] == 0.0
+    with pytest.raises(ValueError, match="gating current"):
+        catalogue.region_record([Channel("Kv3p3_MA2024_PC", gateCurrent=1.0)], cable)
+
+
+def test_planner_checks_the_extension_mask(native_lib):
+    from braincell_gb300.batch import lower_cell
+    from braincell_gb300.runtime import Plan
+
+    b = lower_cell(_io_cell())
+    Plan(b, dry_run=True).close()
+    for bad in (0.0, 0.5, float(_abi.BC_X_ALL + 1)):
+        b2 = lower_cell(_io_cell())
+        b2.region_params = b2.region_params.copy()
+        b2.region_params[:, _abi.BC_P_EXT_MASK] = bad
+        with pytest.raises(_abi.BCError, match="BC_P_EXT_MASK"):
+            Plan(b2, dry_run=True)
+
+
+def _dcn_cell(precision="f64"):
+    soma = Branch.from_lengths(lengths=[20.0], radii=[10.0, 10.0], type="soma")
+    m = Morphology.from_root(soma, name="soma")
+    m.attach(parent="soma", child_branch=Branch.from_lengths(lengths=[150.0], radii=[1.2, 0.6], type="dendrite"),
+             child_name="d0")
+    c = Cell(m, cv_policy=CVPerBranch(5), precision=precision)
+    c.paint(AllRegion(), CableProperty(), Channel("IL", g_max=0.05, E=-65.0))
+    c.paint(branch_in("type", "soma"), Channel("NaF_SU2015_DCN", g_max=40.0), Channel("NaP_SU2015_DCN", g_max=0.2),
+            Channel("fKdr_SU2015_DCN", g_max=15.0), Channel("sKdr_SU2015_DCN", g_max=4.0),
+            Channel("HCN_SU2015_DCN", g_max=0.3))
+    c.paint(branch_in("type", "dendrite"), Channel("Kv1p5_MA2024_PC", g_max=0.5), Channel("Kv3p3_MA2024_PC", g_max=1.0),
+            Channel("Kv2p2_0010_MA2020_GrC", g_max=0.5), Channel("HCN2_MA2020_GoC", g_max=0.3))
+    c.place(RootLocation(0.5), CurrentClamp(delay=2.0, durations=20.0, amplitudes=0.3), StateProbe(name="v"),
+            MechanismProbe("NaF_SU2015_DCN", "h", name="naf_h"), CurrentProbe(mechanism="NaF_SU2015_DCN", name="i_naf"),
+            CurrentProbe(ion="na", name="i_na"))
+    c.place(at(1, 0.5), StateProbe(name="v_dend"), MechanismProbe("Kv1p5_MA2024_PC", "m", name="kv15_m"),
+            MechanismProbe("HCN2_MA2020_GoC", "o_slow", name="hcn2_s"),
+            CurrentProbe(mechanism="Kv1p5_MA2024_PC", name="i_kv15"), CurrentProbe(ion="k", name="i_k"))
+    return c
+
+
+def _io_cell(precision="f64"):
+    soma = Branch.from_lengths(lengths=[20.0], radii=[10.0, 10.0], type="soma")
+    c = Cell(Morphology.from_root(soma, name="soma"), cv_policy=CVPerBranch(), precision=precision)
+    c.paint(AllRegion(), CableProperty(), Channel("IL", g_max=0.1, E=-65.0), Channel("Na_ZH2019_IO"),
+            Channel("Kdr_ZH2019_IO"), Channel("HCN_ZH2019_IO"))
+    c.place(RootLocation(0.5), CurrentClamp(delay=2.0, durations=15.0, amplitudes=0.5), StateProbe(name="v"),
+            MechanismProbe("Kdr_ZH2019_IO", "n", name="kdr_n"), MechanismProbe("HCN_ZH2019_IO", "q", name="hcn_q"),
+            CurrentProbe(mechanism="Na_ZH2019_IO", name="i_na"))
+    return c
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("make,n", [(_dcn_cell, 1000), (_io_cell, 800)], ids=["dcn", "io"])
+def test_extension_cells_f64_match_oracle(native_lib, cuda_device, make, n):
+    from braincell_gb300.runtime import Plan
+
+    p = Plan(make().batch(), precision="f64", record_every=1, device=cuda_device)
+    p.run(n, DT)
+    gpu, sp = p.traces(), p.spikes()[0]
+    oc = O.OracleCell(make())
+    ref, osp = oc.run(DT, n)
+    ref = ref[0]
+    fields = make().batch().probe_field
+    for k, f in enumerate(fields):
+        if f == _abi.BC_STATE_V:
+            _close(gpu[k], ref[k], 1e-8, what=f"V probe {k}")
+        elif f >= _abi.BC_PROBE_CURRENT:
+            _close(gpu[k], ref[k], 1e-9, rtol=1e-8, what=f"current probe {k}")
+        else:
+            _close(gpu[k], ref[k], 1e-10, what=f"state probe {k}")
+    assert len(sp) == len(osp[0][0]) >= 2
+    assert np.abs(np.asarray(sp) - np.asarray(osp[0][0])).max() <= 1e-9
+    np.testing.assert_allclose(p.state("V"), oc.V[0], rtol=0, atol=1e-8)
+    p.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("make", [_dcn_cell, _io_cell], ids=["dcn", "io"])
+def test_extension_cells_f32_meet_the_bar(native_lib, cuda_device, make):
+    from braincell_gb300.runtime import Plan
+
+    out = {}
+    for prec in ("f32", "f64"):
+        p = Plan(make(prec).batch(), precision=prec, record_every=1, device=cuda_device)
+        p.run(800, DT)
+        out[prec] = (p.traces()[0], p.spikes()[0])
+        p.close()
+    (t32, s32), (t64, s64) = out["f32"], out["f64"]
+    onset = int(np.nonzero(np.diff(t64) / DT > 10.0)[0][0]) + 1
+    assert np.abs(t32[:onset] - t64[:onset]).max() <= 1e-3
+    assert len(s32) == len(s64) >= 2
+    assert np.abs(np.asarray(s32) - np.asarray(s64)).max() <= 0.05

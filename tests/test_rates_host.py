@@ -26,6 +26,11 @@ CASES = {
     13: ("Kv3p4_MA2020_GoC", ()), 14: ("Kv4p3_MA2020_GoC", ()), 15: ("Kv1p1_MA2020_GoC", ()),
     16: ("Kir2p3_MA2020_GrC", ()), 17: ("HCN1_MA2020_GoC", ()), 18: ("HCN1_MA2024_PC", ()),
     19: ("CaHVA_MA2020_GoC", ()), 20: ("Cav2p3_MA2020_GoC", ()), 21: ("Cav3p2_RI2021_SC", ("V_sh",)),
+    # extension channels
+    22: ("HCN2_MA2020_GoC", ()), 23: ("Kv3p3_MA2024_PC", ()), 24: ("Kv2p2_0010_MA2020_GrC", ()),
+    25: ("Kv1p5_MA2024_PC", ("q10f", "Tauact", "Tauinactf", "Tauinacts")), 26: ("NaF_SU2015_DCN", ()),
+    27: ("NaP_SU2015_DCN", ()), 28: ("Na_ZH2019_IO", ()), 29: ("fKdr_SU2015_DCN", ()), 30: ("sKdr_SU2015_DCN", ()),
+    31: ("Kdr_ZH2019_IO", ()), 32: ("HCN_SU2015_DCN", ()), 33: ("HCN_ZH2019_IO", ()),
 }
 
 
@@ -48,7 +53,7 @@ def rates_lib(tmp_path_factory):
 def _kernel(lib, which, V, prm):
     V = np.ascontiguousarray(V, np.float64)
     prm = np.ascontiguousarray(prm, np.float64)
-    out = np.zeros((V.size, 4))
+    out = np.zeros((V.size, 6))
     dp = C.POINTER(C.c_double)
     assert lib.bc_test_rates(which, V.ctypes.data_as(dp), V.size, prm.ctypes.data_as(dp), out.ctypes.data_as(dp)) == 0
     return out
@@ -61,11 +66,19 @@ def test_kernel_rates_match_oracle(rates_lib, which, shift):
     p = dict(O.CHANNEL_DEFAULTS[name])
     if "V_sh" in keys:
         p["V_sh"] = p["V_sh"] + shift
+    if name == "Kv1p5_MA2024_PC":  # a temperature off 37 degC and non-unit time-constant scales when shifted
+        p["temp"] += shift
+        p["Tauact"], p["Tauinacts"] = 1.0 + shift / 10.0, 1.0 + shift / 5.0
+        p["q10f"] = 2.2 ** ((p["temp"] - O._c2k(37.0)) / 10.0)
     # a grid with the removable singularities of exprel and the branch points of the
     # piecewise time constants (KA -63, KK2B -70, CaT -80 relative to V_sh)
     V = np.linspace(-130.0, 60.0, 1901)
     if name == "Kv3p4_MA2020_GoC":  # the branch points of its time constants (V + 11 = -35 and 0)
         V = np.concatenate([V, [-46.0, -11.0]])
+    if name == "HCN2_MA2020_GoC":  # the ends of r(V)'s linear piece
+        V = np.concatenate([V, [-64.70, -108.70]])
+    if name in ("Na_ZH2019_IO", "Kdr_ZH2019_IO"):  # the removable singularities of x / (1 - e^-x)
+        V = np.concatenate([V, [-41.0, -50.0, -41.0 + 1e-7, -50.0 - 1e-7]])
     if "V_sh" in keys:
         V = np.concatenate([V, p["V_sh"] + np.array([13.0, 15.0, 40.0, -5.0, -63.0, -70.0, -80.0, -10.0])])
     got = _kernel(rates_lib, which, V, [p[k] for k in keys])
@@ -79,6 +92,6 @@ def test_kernel_rates_match_oracle(rates_lib, which, shift):
 def test_unknown_structure_is_rejected(rates_lib):
     assert rates_lib.bc_test_rates(99, None, 0, None, None) == 0  # no voltages: nothing to evaluate
     v = np.zeros(1)
-    out = np.zeros(4)
+    out = np.zeros(6)  # six rate entries per voltage
     dp = C.POINTER(C.c_double)
     assert rates_lib.bc_test_rates(99, v.ctypes.data_as(dp), 1, v.ctypes.data_as(dp), out.ctypes.data_as(dp)) == -1

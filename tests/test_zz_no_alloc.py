@@ -66,7 +66,14 @@ def _hh_batch():
             Channel("Kv1p1_MA2020_GoC", g_max=0.2), Channel("Kir2p3_MA2020_GrC", g_max=0.2),
             Channel("HCN1_MA2020_GoC", g_max=0.05), Channel("HCN1_MA2024_PC", g_max=0.05),
             Channel("CaHVA_MA2020_GoC", g_max=0.05), Channel("Cav2p3_MA2020_GoC", g_max=0.05),
-            Channel("Cav3p2_RI2021_SC", g_max=0.05))
+            Channel("Cav3p2_RI2021_SC", g_max=0.05),
+            # and the extension channels' views
+            Channel("HCN2_MA2020_GoC", g_max=0.05), Channel("Kv3p3_MA2024_PC", g_max=0.2),
+            Channel("Kv2p2_0010_MA2020_GrC", g_max=0.2), Channel("Kv1p5_MA2024_PC", g_max=0.2),
+            Channel("NaF_SU2015_DCN", g_max=0.2), Channel("NaP_SU2015_DCN", g_max=0.05),
+            Channel("Na_ZH2019_IO", g_max=0.2), Channel("fKdr_SU2015_DCN", g_max=0.2),
+            Channel("sKdr_SU2015_DCN", g_max=0.2), Channel("Kdr_ZH2019_IO", g_max=0.2),
+            Channel("HCN_SU2015_DCN", g_max=0.05), Channel("HCN_ZH2019_IO", g_max=0.05))
     return lower_cell(c)
 
 
