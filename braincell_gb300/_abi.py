@@ -66,7 +66,10 @@ BC_X_SKDR = 1 << 8
 BC_X_KDRIO = 1 << 9
 BC_X_HCNDCN = 1 << 10
 BC_X_HCNIO = 1 << 11
-BC_X_ALL = 0xFFF
+BC_X_CATHP = 1 << 12
+BC_X_CAHTRE = 1 << 13
+BC_X_CALDCN = 1 << 14
+BC_X_ALL = 0x7FFF
 
 BC_NPARAM = 160
 BC_P_INVCM = 0
@@ -186,6 +189,16 @@ BC_P_HCNDCN_G = 114
 BC_P_HCNDCN_E = 115
 BC_P_HCNIO_G = 116
 BC_P_HCNIO_E = 117
+BC_P_CATHP_G = 118
+BC_P_CATHP_VSH = 119
+BC_P_CATHP_PHIP = 120
+BC_P_CATHP_PHIQ = 121
+BC_P_CAHTRE_G = 122
+BC_P_CAHTRE_VSH = 123
+BC_P_CAHTRE_PHIP = 124
+BC_P_CAHTRE_PHIQ = 125
+BC_P_CALDCN_G = 126
+BC_P_CALDCN_E = 127
 
 BC_ABI_VERSION = 500
 
@@ -245,7 +258,10 @@ BC_CUR_SKDR = 39
 BC_CUR_KDRIO = 40
 BC_CUR_HCNDCN = 41
 BC_CUR_HCNIO = 42
-BC_NCUR = 43
+BC_CUR_CATHP = 43
+BC_CUR_CAHTRE = 44
+BC_CUR_CALDCN = 45
+BC_NCUR = 46
 
 BC_STATE_V = 0
 BC_STATE_NA_P = 1
@@ -310,7 +326,13 @@ BC_STATE_SKDR_M = 81
 BC_STATE_KDRIO_N = 82
 BC_STATE_HCNDCN_M = 83
 BC_STATE_HCNIO_Q = 84
-BC_NSTATE_VIEW = 85
+BC_STATE_CATHP_P = 85
+BC_STATE_CATHP_Q = 86
+BC_STATE_CAHTRE_P = 87
+BC_STATE_CAHTRE_Q = 88
+BC_STATE_CALDCN_M = 89
+BC_STATE_CALDCN_H = 90
+BC_NSTATE_VIEW = 91
 # the independent states of each Markov scheme, in view order (first appearance in
 # the scheme's transition list, the dependent state left out)
 MARKOV_STATES = {
@@ -380,6 +402,12 @@ STATE_NAMES = {
     "KdrIO_n": BC_STATE_KDRIO_N,
     "HCNDCN_m": BC_STATE_HCNDCN_M,
     "HCNIO_q": BC_STATE_HCNIO_Q,
+    "CaTHP_p": BC_STATE_CATHP_P,
+    "CaTHP_q": BC_STATE_CATHP_Q,
+    "CaHTRe_p": BC_STATE_CAHTRE_P,
+    "CaHTRe_q": BC_STATE_CAHTRE_Q,
+    "CaLDCN_m": BC_STATE_CALDCN_M,
+    "CaLDCN_h": BC_STATE_CALDCN_H,
 }
 for _cls, (_base, _names) in MARKOV_STATES.items():
     for _k, _n in enumerate(_names):

@@ -363,6 +363,9 @@ PROBE_STATES.update({
     ("fKdr_SU2015_DCN", "m"): _abi.BC_STATE_FKDR_M, ("sKdr_SU2015_DCN", "m"): _abi.BC_STATE_SKDR_M,
     ("Kdr_ZH2019_IO", "n"): _abi.BC_STATE_KDRIO_N, ("HCN_SU2015_DCN", "m"): _abi.BC_STATE_HCNDCN_M,
     ("HCN_ZH2019_IO", "q"): _abi.BC_STATE_HCNIO_Q,
+    ("CaT_HP1992", "p"): _abi.BC_STATE_CATHP_P, ("CaT_HP1992", "q"): _abi.BC_STATE_CATHP_Q,
+    ("CaHT_Re1993", "p"): _abi.BC_STATE_CAHTRE_P, ("CaHT_Re1993", "q"): _abi.BC_STATE_CAHTRE_Q,
+    ("CaL_SU2015_DCN", "m"): _abi.BC_STATE_CALDCN_M, ("CaL_SU2015_DCN", "h"): _abi.BC_STATE_CALDCN_H,
 })
 for _cls, (_base, _names) in _abi.MARKOV_STATES.items():
     for _k, _n in enumerate(_names):
@@ -389,7 +392,8 @@ PROBE_CURRENTS = {
     "Kv2p2_0010_MA2020_GrC": _abi.BC_CUR_KV22, "Kv1p5_MA2024_PC": _abi.BC_CUR_KV15, "NaF_SU2015_DCN": _abi.BC_CUR_NAF,
     "NaP_SU2015_DCN": _abi.BC_CUR_NAP, "Na_ZH2019_IO": _abi.BC_CUR_NAIO, "fKdr_SU2015_DCN": _abi.BC_CUR_FKDR,
     "sKdr_SU2015_DCN": _abi.BC_CUR_SKDR, "Kdr_ZH2019_IO": _abi.BC_CUR_KDRIO, "HCN_SU2015_DCN": _abi.BC_CUR_HCNDCN,
-    "HCN_ZH2019_IO": _abi.BC_CUR_HCNIO,
+    "HCN_ZH2019_IO": _abi.BC_CUR_HCNIO, "CaT_HP1992": _abi.BC_CUR_CATHP, "CaHT_Re1993": _abi.BC_CUR_CAHTRE,
+    "CaL_SU2015_DCN": _abi.BC_CUR_CALDCN,
 }
 ION_CURRENTS = {"na": _abi.BC_CUR_ION_NA, "k": _abi.BC_CUR_ION_K, "ca": _abi.BC_CUR_ION_CA}
 

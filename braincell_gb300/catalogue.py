@@ -42,6 +42,26 @@ Every class name, parameter name and default below is the reference's:
 * ``Cav3p2_RI2021_SC`` -- channel/calcium.py:3636 (g_max 8e-4, V_sh 0, temp 36 degC; m phi 5^1.2, the h time constant
   carrying 3^1.2); the MA2025_BC and MA2024_PC classes inherit it
 
+Extension channels (bit BC_M_EXT; the region's record lists them as BC_X_* bits in
+BC_P_EXT_MASK, their parameters after it; conductances in mS/cm^2):
+* ``HCN2_MA2020_GoC`` -- channel/hyperpolarization_activated.py:838 (g_max 0.08, E -20 mV, temp 22 degC; gates q10 3
+  and g Q10 1.5 at 23 degC)
+* ``Kv3p3_MA2024_PC`` -- channel/potassium.py:2937 (g_max 5, temp 22 degC, gateCurrent 0; gate q10 2.7 at 22 degC)
+* ``Kv2p2_0010_MA2020_GrC`` -- channel/potassium.py:5664 (g_max 0.01, BBiD 10, unused by the rates)
+* ``Kv1p5_MA2024_PC`` -- channel/potassium.py:2735 (g_max 0.13195, temp 37 degC, Tauact / Tauinactf / Tauinacts 1;
+  rates scaled by 2.2^((T - 37 degC) / 10); current times 0.1 + 1 / (1 + exp(-(V - 15) / 13)))
+* ``NaF_SU2015_DCN``, ``NaP_SU2015_DCN`` -- channel/sodium.py:402, :500 (g_max 0.01)
+* ``Na_ZH2019_IO`` -- channel/sodium.py:598 (g_max 70)
+* ``fKdr_SU2015_DCN``, ``sKdr_SU2015_DCN`` -- channel/potassium.py:1374, :1485 (g_max 0.01)
+* ``Kdr_ZH2019_IO`` -- channel/potassium.py:6238 (g_max 18)
+* ``HCN_SU2015_DCN`` -- channel/hyperpolarization_activated.py:1010 (g_max 0.01, E -45 mV)
+* ``HCN_ZH2019_IO`` -- channel/hyperpolarization_activated.py:1109 (g_max 0.15, E -43 mV)
+* ``CaT_HP1992`` -- channel/calcium.py:377 (g_max 1.75, temp 36 degC, q10_p 5 / q10_q 3 at 24 degC, V_sh -3 mV)
+* ``CaHT_Re1993`` -- channel/calcium.py:667 (g_max 1, temp 36 degC, q10 2.3 at 23 degC, V_sh 0)
+* ``CaL_SU2015_DCN`` -- channel/calcium.py:1066 (g_max 0.01, E 139 mV, qdeltat 1; not a calcium-ion channel)
+* ``Kv1p5_MA2020_GrC`` -- channel/potassium_sodium.py:38 on Kv1p5_MA2024_PC's kernel (its nonspecific current,
+  gnonspec, 0 by default: only 0 is built)
+
 Same-form classes: Na_TM1991 has Na_Ba2002's Traub-Miles rate functions written
 in terms of V_sh - V (sodium.py:275-289 against :154-170), K_TM1991 has
 KDR_Ba2002's (potassium.py:331-337 against :208-214), and CaHT_HM1992 has
@@ -146,6 +166,11 @@ CHANNELS: dict[str, dict[str, float]] = {
     "Kdr_ZH2019_IO": {"g_max": 18.0},
     "HCN_SU2015_DCN": {"g_max": 0.01, "E": -45.0},
     "HCN_ZH2019_IO": {"g_max": 0.15, "E": -43.0},
+    "CaT_HP1992": {"g_max": 1.75, "temp": T36, "q10_p": 5.0, "temp_ref_p": celsius2kelvin(24.0), "q10_q": 3.0,
+                   "temp_ref_q": celsius2kelvin(24.0), "V_sh": -3.0},
+    "CaHT_Re1993": {"g_max": 1.0, "temp": T36, "q10_p": 2.3, "temp_ref_p": celsius2kelvin(23.0), "q10_q": 2.3,
+                    "temp_ref_q": celsius2kelvin(23.0), "V_sh": 0.0},
+    "CaL_SU2015_DCN": {"g_max": 0.01, "E": 139.0, "qdeltat": 1.0},
 }
 # extension channels: class -> (BC_X_* bit, record entry of g_max, record entry of E or None)
 _EXT = {
@@ -161,6 +186,9 @@ _EXT = {
     "Kdr_ZH2019_IO": (_abi.BC_X_KDRIO, _abi.BC_P_KDRIO_G, None),
     "HCN_SU2015_DCN": (_abi.BC_X_HCNDCN, _abi.BC_P_HCNDCN_G, _abi.BC_P_HCNDCN_E),
     "HCN_ZH2019_IO": (_abi.BC_X_HCNIO, _abi.BC_P_HCNIO_G, _abi.BC_P_HCNIO_E),
+    "CaT_HP1992": (_abi.BC_X_CATHP, _abi.BC_P_CATHP_G, None),
+    "CaHT_Re1993": (_abi.BC_X_CAHTRE, _abi.BC_P_CAHTRE_G, None),
+    "CaL_SU2015_DCN": (_abi.BC_X_CALDCN, _abi.BC_P_CALDCN_G, _abi.BC_P_CALDCN_E),
 }
 # cell-type variants with their base class's kinetics; own defaults where they differ
 KINETIC_VARIANTS = {
@@ -189,6 +217,11 @@ for _base, _variants in KINETIC_VARIANTS.items():
     for _v, _own in _variants.items():
         CHANNELS[_v] = {**CHANNELS[_base], **_own}
         SAME_FORM[_v] = _base
+# Kv1p5_MA2020_GrC (potassium_sodium.py:38-259) is Kv1p5_MA2024_PC's kinetics and K
+# current plus a nonspecific current of conductance gnonspec, 0 by default; only
+# gnonspec = 0 is built
+CHANNELS["Kv1p5_MA2020_GrC"] = {**CHANNELS["Kv1p5_MA2024_PC"], "gnonspec": 0.0}
+SAME_FORM["Kv1p5_MA2020_GrC"] = "Kv1p5_MA2024_PC"
 # classes with a parameter record of their own on another class's kernel mechanism
 _SHARED_KERNEL = {"Nav1p1_MA2025_BC": "Nav1p6_MA2020_GoC", "Nav1p1_RI2021_SC": "Nav1p6_MA2020_GoC"}
 # gate temperature factors fixed by a class (not constructor parameters)
@@ -418,10 +451,19 @@ def region_record(mechs, cable: CableProperty) -> tuple[int, np.ndarray]:
                     raise ValueError(f"{decl.class_name}: the gating current (gateCurrent != 0) is not built.")
                 rec[_abi.BC_P_KV33_PHI] = q10_phi(2.7, p["temp"], T22)
             elif name == "Kv1p5_MA2024_PC":
+                if p.get("gnonspec", 0.0) != 0.0:
+                    raise ValueError(f"{decl.class_name}: the nonspecific current (gnonspec != 0) is not built.")
                 rec[_abi.BC_P_KV15_Q10] = q10_phi(2.2, p["temp"], celsius2kelvin(37.0))
                 rec[_abi.BC_P_KV15_TACT] = p["Tauact"]
                 rec[_abi.BC_P_KV15_TINF] = p["Tauinactf"]
                 rec[_abi.BC_P_KV15_TINS] = p["Tauinacts"]
+            elif name in ("CaT_HP1992", "CaHT_Re1993"):
+                base = g_slot
+                rec[base + 1] = p["V_sh"]
+                rec[base + 2] = q10_phi(p["q10_p"], p["temp"], p["temp_ref_p"])
+                rec[base + 3] = q10_phi(p["q10_q"], p["temp"], p["temp_ref_q"])
+            elif name == "CaL_SU2015_DCN" and p["qdeltat"] != 1.0:
+                raise ValueError(f"{decl.class_name}: qdeltat other than 1 is not built.")
             rec[g_slot] = g
             if e_slot is not None:
                 rec[e_slot] = p["E"]

@@ -19,6 +19,11 @@
 //   Kdr_ZH2019_IO          channel/potassium.py:6238-6374
 //   HCN_SU2015_DCN         channel/hyperpolarization_activated.py:1010-1107
 //   HCN_ZH2019_IO          channel/hyperpolarization_activated.py:1109-1217
+//   CaT_HP1992             channel/calcium.py:377-509
+//   CaHT_Re1993            channel/calcium.py:667-788
+//   CaL_SU2015_DCN         channel/calcium.py:1066-1219
+// CaT_HP1992 and CaHT_Re1993 carry calcium: their step-start current joins the
+// calcium shell's drive, as CaL's and CaT's do.
 #pragma once
 
 #include "bc_mech.cuh"
@@ -46,7 +51,13 @@ constexpr int kSlotSkdrM = 82;
 constexpr int kSlotKdrioN = 83;
 constexpr int kSlotHcndcnM = 84;
 constexpr int kSlotHcnioQ = 85;
-constexpr int kNumSlotsExt = 86;
+constexpr int kSlotCathpP = 86;
+constexpr int kSlotCathpQ = 87;
+constexpr int kSlotCahtreP = 88;
+constexpr int kSlotCahtreQ = 89;
+constexpr int kSlotCaldcnM = 90;
+constexpr int kSlotCaldcnH = 91;
+constexpr int kNumSlotsExt = 92;
 
 // x / (1 - e^-x) = 1 / exprel(-x), finite at x = 0 (the reference's
 // _x_over_one_minus_exp_neg_stable, channel/sodium.py:50-55)
@@ -214,6 +225,46 @@ struct HcnioRates {
   }
 };
 
+// CaT_HP1992: p^2 q on V - V_sh, inf / tau.
+template <typename Real>
+struct CathpRates {
+  Real pinf, ptau, qinf, qtau;
+  __host__ __device__ __forceinline__ CathpRates(Real v, Real vsh) {
+    const Real x = v - vsh;
+    pinf = Real(1) / (Real(1) + aexp(-(x + Real(52)) / Real(7.4)));
+    ptau = Real(3) + Real(1) / (aexp((x + Real(27)) / Real(10)) + aexp(-(x + Real(102)) / Real(15)));
+    qinf = Real(1) / (Real(1) + aexp((x + Real(80)) / Real(5)));
+    qtau = Real(85) + Real(1) / (aexp((x + Real(48)) / Real(4)) + aexp(-(x + Real(407)) / Real(50)));
+  }
+};
+
+// CaHT_Re1993: p^2 q from alpha / beta of t = V_sh - V; alpha_p's
+// d / (e^(d / 3.8) - 1) (d = t - 27) is 3.8 / exprel(d / 3.8), finite at d = 0.
+template <typename Real>
+struct CahtreRates {
+  Real ap, bp, aq, bq;
+  __host__ __device__ __forceinline__ CahtreRates(Real v, Real vsh) {
+    const Real t = vsh - v;
+    ap = Real(0.055 * 3.8) / exprel((t - Real(27)) / Real(3.8));
+    bp = Real(0.94) * aexp((t - Real(75)) / Real(17));
+    aq = Real(0.000457) * aexp((t - Real(13)) / Real(50));
+    bq = Real(0.0065) / (aexp((t - Real(15)) / Real(28)) + Real(1));
+  }
+};
+
+// CaL_SU2015_DCN: m^2 h, h's tau piecewise at -81 mV (qdeltat = 1).
+template <typename Real>
+struct CaldcnRates {
+  Real minf, mtau, hinf, htau;
+  __host__ __device__ __forceinline__ explicit CaldcnRates(Real v) {
+    minf = Real(1) / (Real(1) + aexp((v + Real(56)) / Real(-6.2)));
+    mtau = Real(0.333) / (aexp((v + Real(131)) / Real(-16.7)) + aexp((v + Real(15.8)) / Real(18.2))) + Real(0.204);
+    hinf = Real(1) / (Real(1) + aexp((v + Real(80)) / Real(4)));
+    htau = v < Real(-81) ? Real(0.333) * aexp((v + Real(466)) / Real(66))
+                         : Real(0.333) * aexp((v + Real(21)) / Real(-10.5)) + Real(9.32);
+  }
+};
+
 // The region's BC_X_* bits (an integer stored as a record real).
 template <typename Real>
 __host__ __device__ __forceinline__ uint32_t ext_mask(const Real* P) {
@@ -223,8 +274,8 @@ __host__ __device__ __forceinline__ uint32_t ext_mask(const Real* P) {
 // One extension channel's current at v with the node's stored gates (0 where the
 // region does not carry it); *gv receives -dI/dV when not null.
 template <typename Real>
-__device__ __forceinline__ Real ext_current(const Real* st, int N, const Real* P, uint32_t x, Real v, int code,
-                                            Real* gv) {
+__device__ __forceinline__ Real ext_current(const Real* st, int N, const Real* P, uint32_t x, Real v, Real eca,
+                                            int code, Real* gv) {
   Real g = Real(0), e = Real(0), gd = Real(0);
   bool has = false;
   switch (code) {
@@ -314,6 +365,27 @@ __device__ __forceinline__ Real ext_current(const Real* st, int N, const Real* P
         e = P[BC_P_HCNIO_E];
       }
       break;
+    case BC_CUR_CATHP:
+      if ((has = (x & BC_X_CATHP) != 0)) {
+        const Real p = st[kSlotCathpP * N];
+        g = P[BC_P_CATHP_G] * p * p * st[kSlotCathpQ * N];
+        e = eca;
+      }
+      break;
+    case BC_CUR_CAHTRE:
+      if ((has = (x & BC_X_CAHTRE) != 0)) {
+        const Real p = st[kSlotCahtreP * N];
+        g = P[BC_P_CAHTRE_G] * p * p * st[kSlotCahtreQ * N];
+        e = eca;
+      }
+      break;
+    case BC_CUR_CALDCN:
+      if ((has = (x & BC_X_CALDCN) != 0)) {
+        const Real m = st[kSlotCaldcnM * N];
+        g = P[BC_P_CALDCN_G] * m * m * st[kSlotCaldcnH * N];
+        e = P[BC_P_CALDCN_E];
+      }
+      break;
   }
   if (!has) return Real(0);
   if (gv) *gv = code == BC_CUR_KV15 ? gd : g;
@@ -379,20 +451,45 @@ __device__ __forceinline__ void ext_gates(Real* st, int N, const Real* P, uint32
     const HcnioRates<Real> r(v);
     st[kSlotHcnioQ * N] = gate_it(st[kSlotHcnioQ * N], r.qinf, r.qtau, Real(1), dt);
   }
+  if (x & BC_X_CATHP) {
+    const CathpRates<Real> r(v, P[BC_P_CATHP_VSH]);
+    st[kSlotCathpP * N] = gate_it(st[kSlotCathpP * N], r.pinf, r.ptau, P[BC_P_CATHP_PHIP], dt);
+    st[kSlotCathpQ * N] = gate_it(st[kSlotCathpQ * N], r.qinf, r.qtau, P[BC_P_CATHP_PHIQ], dt);
+  }
+  if (x & BC_X_CAHTRE) {
+    const CahtreRates<Real> r(v, P[BC_P_CAHTRE_VSH]);
+    st[kSlotCahtreP * N] = gate_ab<Real, true>(st[kSlotCahtreP * N], r.ap, r.bp, P[BC_P_CAHTRE_PHIP], dt);
+    st[kSlotCahtreQ * N] = gate_ab<Real, true>(st[kSlotCahtreQ * N], r.aq, r.bq, P[BC_P_CAHTRE_PHIQ], dt);
+  }
+  if (x & BC_X_CALDCN) {
+    const CaldcnRates<Real> r(v);
+    st[kSlotCaldcnM * N] = gate_it(st[kSlotCaldcnM * N], r.minf, r.mtau, Real(1), dt);
+    st[kSlotCaldcnH * N] = gate_it(st[kSlotCaldcnH * N], r.hinf, r.htau, Real(1), dt);
+  }
 }
 
 // A node's extension channels: gates at v (when advancing), then their G and I.
+// eca: E_Ca of the calcium after this step's shell update (the calcium channels).
 template <typename Real>
-__device__ __noinline__ void ext_channels(Real* st, int N, const Real* P, Real v, Real dt, bool advance, Real& G,
-                                          Real& I) {
+__device__ __noinline__ void ext_channels(Real* st, int N, const Real* P, Real v, Real eca, Real dt, bool advance,
+                                          Real& G, Real& I) {
   const uint32_t x = ext_mask(P);
   if (advance) ext_gates(st, N, P, x, v, dt);
-  for (int code = BC_CUR_HCN2; code <= BC_CUR_HCNIO; ++code) {
+  for (int code = BC_CUR_HCN2; code <= BC_CUR_CALDCN; ++code) {
     Real g = Real(0);
-    const Real i = ext_current(st, N, P, x, v, code, &g);
+    const Real i = ext_current(st, N, P, x, v, eca, code, &g);
     G += g;
     I += i;
   }
+}
+
+// The calcium current of the extension channels that carry calcium, at the
+// step-start gates, v and E_Ca (their share of the calcium shell's drive).
+template <typename Real>
+__device__ __noinline__ Real ext_ca_current(const Real* st, int N, const Real* P, Real v, Real eca) {
+  const uint32_t x = ext_mask(P);
+  return ext_current(st, N, P, x, v, eca, BC_CUR_CATHP, (Real*)nullptr) +
+         ext_current(st, N, P, x, v, eca, BC_CUR_CAHTRE, (Real*)nullptr);
 }
 
 // Steady states of the extension channels' gates at v (HH.reset_state).
@@ -439,6 +536,21 @@ __device__ __forceinline__ void ext_steady(const Real* P, Real* st, int N, Real 
   if (x & BC_X_KDRIO) st[kSlotKdrioN * N] = KdrioRates<Real>(v).ninf;
   if (x & BC_X_HCNDCN) st[kSlotHcndcnM * N] = HcndcnRates<Real>(v).minf;
   if (x & BC_X_HCNIO) st[kSlotHcnioQ * N] = HcnioRates<Real>(v).qinf;
+  if (x & BC_X_CATHP) {
+    const CathpRates<Real> r(v, P[BC_P_CATHP_VSH]);
+    st[kSlotCathpP * N] = r.pinf;
+    st[kSlotCathpQ * N] = r.qinf;
+  }
+  if (x & BC_X_CAHTRE) {
+    const CahtreRates<Real> r(v, P[BC_P_CAHTRE_VSH]);
+    st[kSlotCahtreP * N] = r.ap / (r.ap + r.bp);
+    st[kSlotCahtreQ * N] = r.aq / (r.aq + r.bq);
+  }
+  if (x & BC_X_CALDCN) {
+    const CaldcnRates<Real> r(v);
+    st[kSlotCaldcnM * N] = r.minf;
+    st[kSlotCaldcnH * N] = r.hinf;
+  }
 }
 
 }  // namespace bc

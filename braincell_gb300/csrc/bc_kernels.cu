@@ -362,8 +362,9 @@ __device__ __forceinline__ double probe_current(const Real* st, int N, const Rea
         return cerebellar_ca_current(st, N, P, m & BC_M_CAV32, v, eca(), (Real*)nullptr);
       default:
         // extension channels: the record's list exists only where BC_M_EXT is set
-        if (c >= BC_CUR_HCN2 && c <= BC_CUR_HCNIO && (m & BC_M_EXT))
-          return ext_current(st, N, P, ext_mask(P), v, c, (Real*)nullptr);
+        if (c >= BC_CUR_HCN2 && c <= BC_CUR_CALDCN && (m & BC_M_EXT))
+          return ext_current(st, N, P, ext_mask(P), v, (c == BC_CUR_CATHP || c == BC_CUR_CAHTRE) ? eca() : Real(0), c,
+                             (Real*)nullptr);
     }
     return Real(0);
   };
@@ -380,7 +381,7 @@ __device__ __forceinline__ double probe_current(const Real* st, int N, const Rea
              double(cur(BC_CUR_SKDR)) + double(cur(BC_CUR_KDRIO));
     case BC_CUR_ION_CA:
       return double(cur(BC_CUR_CAL)) + double(cur(BC_CUR_CAT)) + double(cur(BC_CUR_CAHVA)) + double(cur(BC_CUR_CAV23)) +
-             double(cur(BC_CUR_CAV32));
+             double(cur(BC_CUR_CAV32)) + double(cur(BC_CUR_CATHP)) + double(cur(BC_CUR_CAHTRE));
     default:
       return double(cur(code));
   }
@@ -633,8 +634,13 @@ __device__ __noinline__ void extra_channels(Real* st, int N, const Real* P, uint
       I += g * (P[BC_P_EK] - v);
     }
   }
-  // the extension channels listed in the record (gates independent of the above)
-  if (m & BC_M_EXT) ext_channels(st, N, P, v, dt, advance, G, I);
+  // the extension channels listed in the record (gates independent of the above),
+  // the calcium ones in E_Ca of the calcium after this step's shell update
+  if (m & BC_M_EXT) {
+    const Real eca =
+        (m & BC_M_CADET) ? Real(kNernstCa) * P[BC_P_CA_TEMP] * dlog(P[BC_P_CA_CO] / ci) : P[BC_P_ECA];
+    ext_channels(st, N, P, v, eca, dt, advance, G, I);
+  }
 }
 
 // One node's mechanisms.  `st` points at the node's slot-0 state (stride N).
@@ -657,6 +663,7 @@ __device__ __forceinline__ void node_mechanisms_loaded(const NodeStates<Real>& s
       if (m & BC_M_CAL) ica += P[BC_P_CAL_G] * calp * calp * calq * (eca - v_old);
       if (m & BC_M_CAT) ica += P[BC_P_CAT_G] * catp * catp * catq * (eca - v_old);
       if (kExtra && (m & kCerebellarCaChannels)) ica += cerebellar_ca_current(st, N, P, m, v_old, eca, (Real*)nullptr);
+      if (kExtra && (m & BC_M_EXT)) ica += ext_ca_current(st, N, P, v_old, eca);
       Real drive = ica * Real(kCaDrive) / P[BC_P_CA_D];
       drive = drive > Real(0) ? drive : Real(0);
       const Real tau = P[BC_P_CA_TAU];

@@ -99,7 +99,10 @@ typedef int32_t bc_status;
                                   m^2, own E                                                  */
 #define BC_X_HCNIO (1u << 11)  /* channel/hyperpolarization_activated.py:1109 HCN_ZH2019_IO
                                   q, own E                                                    */
-#define BC_X_ALL 0xFFFu
+#define BC_X_CATHP (1u << 12)  /* channel/calcium.py:377 CaT_HP1992 p^2 q, E_Ca (Ci drive)   */
+#define BC_X_CAHTRE (1u << 13) /* channel/calcium.py:667 CaHT_Re1993 p^2 q, E_Ca (Ci drive)  */
+#define BC_X_CALDCN (1u << 14) /* channel/calcium.py:1066 CaL_SU2015_DCN m^2 h, own E        */
+#define BC_X_ALL 0x7FFFu
 
 /* Per-region parameter record (double[BC_NPARAM]); index names below. */
 #define BC_NPARAM 160
@@ -221,7 +224,17 @@ typedef int32_t bc_status;
 #define BC_P_HCNDCN_E 115
 #define BC_P_HCNIO_G 116
 #define BC_P_HCNIO_E 117
-/* 118 .. 159: reserved for further extension channels (0) */
+#define BC_P_CATHP_G 118
+#define BC_P_CATHP_VSH 119
+#define BC_P_CATHP_PHIP 120 /* q10_p^((T - temp_ref_p) / 10)                        */
+#define BC_P_CATHP_PHIQ 121
+#define BC_P_CAHTRE_G 122
+#define BC_P_CAHTRE_VSH 123
+#define BC_P_CAHTRE_PHIP 124
+#define BC_P_CAHTRE_PHIQ 125
+#define BC_P_CALDCN_G 126
+#define BC_P_CALDCN_E 127
+/* 128 .. 159: reserved for further extension channels (0) */
 
 /* ------------------------------------------------------------------ batch spec */
 /*
@@ -387,7 +400,7 @@ const char* bc_last_error(void);
  * HH and calcium channels (BC_M_KV34 .. CAV32, a 96-entry parameter record, state
  * views 51-65, BC_PROBE_CURRENT 128).  0.5.0: extension channels (BC_M_EXT with
  * BC_X_* bits in the record's BC_P_EXT_MASK, a 160-entry parameter record, state
- * views 66-84, current codes 31-42). */
+ * views 66-90, current codes 31-45). */
 #define BC_ABI_VERSION 500
 int32_t bc_version(void);
 /* Fill opts with defaults. */
@@ -508,7 +521,13 @@ bc_status bc_check(bc_plan_t plan, void* stream);
 #define BC_STATE_KDRIO_N 82
 #define BC_STATE_HCNDCN_M 83
 #define BC_STATE_HCNIO_Q 84
-#define BC_NSTATE_VIEW 85
+#define BC_STATE_CATHP_P 85
+#define BC_STATE_CATHP_Q 86
+#define BC_STATE_CAHTRE_P 87
+#define BC_STATE_CAHTRE_Q 88
+#define BC_STATE_CALDCN_M 89
+#define BC_STATE_CALDCN_H 90
+#define BC_NSTATE_VIEW 91
 /* Current probes (mech/_point.py CurrentProbe, _multi_compartment/probes.py:184-258):
    probe_field = BC_PROBE_CURRENT + one of the codes below records that current
    density (uA/cm^2, outward negative as g (E - V)) after the step.             */
@@ -556,7 +575,10 @@ bc_status bc_check(bc_plan_t plan, void* stream);
 #define BC_CUR_KDRIO 40  /* Kdr_ZH2019_IO          */
 #define BC_CUR_HCNDCN 41 /* HCN_SU2015_DCN         */
 #define BC_CUR_HCNIO 42  /* HCN_ZH2019_IO          */
-#define BC_NCUR 43
+#define BC_CUR_CATHP 43  /* CaT_HP1992             */
+#define BC_CUR_CAHTRE 44 /* CaHT_Re1993            */
+#define BC_CUR_CALDCN 45 /* CaL_SU2015_DCN         */
+#define BC_NCUR 46
 bc_status bc_state_download(bc_plan_t plan, int32_t which, double* out /* [n_cv] */, void* stream);
 /* Set the amplitude (nA) of every current-clamp pulse of the batch spec, in spec
  * order (amp_nA[n_pulses]); times and locations are unchanged.  Takes effect from

@@ -139,6 +139,11 @@ CHANNEL_DEFAULTS.update({
     "Kdr_ZH2019_IO": dict(g_max=18.0),  # potassium.py:6238
     "HCN_SU2015_DCN": dict(g_max=0.01, E=-45.0),  # hyperpolarization_activated.py:1010
     "HCN_ZH2019_IO": dict(g_max=0.15, E=-43.0),  # hyperpolarization_activated.py:1109
+    "CaT_HP1992": dict(g_max=1.75, temp=_c2k(36.0), q10_p=5.0, temp_ref_p=_c2k(24.0), q10_q=3.0,
+                       temp_ref_q=_c2k(24.0), V_sh=-3.0),  # calcium.py:377
+    "CaHT_Re1993": dict(g_max=1.0, temp=_c2k(36.0), q10_p=2.3, temp_ref_p=_c2k(23.0), q10_q=2.3,
+                        temp_ref_q=_c2k(23.0), V_sh=0.0),  # calcium.py:667
+    "CaL_SU2015_DCN": dict(g_max=0.01, E=139.0, qdeltat=1.0),  # calcium.py:1066
 })
 # cell-type variants that run their base class's kinetics, with their own defaults
 # where they differ (each class body is the base's: potassium.py, hyperpolarization_activated.py)
@@ -152,6 +157,9 @@ _VARIANTS = {
     **{v: ("Kir2p3_MA2020_GrC", {}) for v in ("Kir2p3_MA2024_PC", "Kir2p3_MA2025_BC", "Kir2p3_RI2021_SC")},
     **{v: ("HCN1_MA2024_PC", {}) for v in ("HCN1_MA2025_BC", "HCN1_RI2021_SC")},
     "CaHVA_MA2020_GrC": ("CaHVA_MA2020_GoC", {}),
+    # potassium_sodium.py:38-259: Kv1p5_MA2024_PC's kinetics and K current, plus a
+    # nonspecific current of conductance gnonspec (0 by default; only 0 is restated)
+    "Kv1p5_MA2020_GrC": ("Kv1p5_MA2024_PC", {"gnonspec": 0.0}),
     **{v: ("Cav3p2_RI2021_SC", {}) for v in ("Cav3p2_MA2025_BC", "Cav3p2_MA2024_PC")},
 }
 
@@ -575,6 +583,21 @@ def rates(name: str, V, p: dict, Ci=None):
     if name == "HCN_ZH2019_IO":  # hyperpolarization_activated.py:1109-1217
         return {"q": ("it", 1.0 / (1.0 + np.exp((V + 75.0) / 5.5)),
                       1.0 / (np.exp(-0.086 * V - 14.6) + np.exp(0.07 * V - 1.87)))}
+    if name == "CaT_HP1992":  # calcium.py:377-509, on V - V_sh
+        x = V - p["V_sh"]
+        return {"p": ("it", 1.0 / (1.0 + np.exp(-(x + 52.0) / 7.4)),
+                      3.0 + 1.0 / (np.exp((x + 27.0) / 10.0) + np.exp(-(x + 102.0) / 15.0))),
+                "q": ("it", 1.0 / (1.0 + np.exp((x + 80.0) / 5.0)),
+                      85.0 + 1.0 / (np.exp((x + 48.0) / 4.0) + np.exp(-(x + 407.0) / 50.0)))}
+    if name == "CaHT_Re1993":  # calcium.py:667-788, t = V_sh - V; d / (e^(d/3.8) - 1) = 3.8 / exprel(d / 3.8)
+        t = p["V_sh"] - V
+        return {"p": ("ab", 0.055 * 3.8 / exprel((t - 27.0) / 3.8), 0.94 * np.exp((-75.0 + t) / 17.0)),
+                "q": ("ab", 0.000457 * np.exp((-13.0 + t) / 50.0), 0.0065 / (np.exp((-15.0 + t) / 28.0) + 1.0))}
+    if name == "CaL_SU2015_DCN":  # calcium.py:1066-1219
+        ht = np.where(V < -81.0, 0.333 * np.exp((V + 466.0) / 66.0), 0.333 * np.exp((V + 21.0) / -10.5) + 9.32)
+        return {"m": ("it", 1.0 / (1.0 + np.exp((V + 56.0) / -6.2)),
+                      (0.333 / (np.exp((V + 131.0) / -16.7) + np.exp((V + 15.8) / 18.2)) + 0.204) / p["qdeltat"]),
+                "h": ("it", 1.0 / (1.0 + np.exp((V + 80.0) / 4.0)), ht / p["qdeltat"])}
     if name in ("KM_RI2021_SC", "KM_MA2020_GoC", "KM_MA2020_GrC"):  # potassium.py:1735-1748, :4553-4567, :5317-5331
         a = 0.0033 * np.exp((V + 30.0) / 40.0)
         b = 0.0033 * np.exp((V + 30.0) / -20.0)
@@ -623,6 +646,9 @@ _GATES = {  # (gate, power, phi-key)
     "Kdr_ZH2019_IO": (("n", 4, "phi"),),
     "HCN_SU2015_DCN": (("m", 2, "phi"),),
     "HCN_ZH2019_IO": (("q", 1, "phi"),),
+    "CaT_HP1992": (("p", 2, "phi_p"), ("q", 1, "phi_q")),
+    "CaHT_Re1993": (("p", 2, "phi_p"), ("q", 1, "phi_q")),
+    "CaL_SU2015_DCN": (("m", 2, "phi"), ("h", 1, "phi")),
 }
 _ION_OF = {"Na_Ba2002": "na", "KDR_Ba2002": "k", "CaL_IS2008": "ca", "CaT_HM1992": "ca",
            "K_Leak": "k", "AHP_De1994": "k", "Na_HH1952": "na", "K_HH1952": "k", "KM_RI2021_SC": "k",
@@ -634,9 +660,10 @@ _ION_OF = {"Na_Ba2002": "na", "KDR_Ba2002": "k", "CaL_IS2008": "ca", "CaT_HM1992
            "CaHVA_MA2020_GoC": "ca", "Cav2p3_MA2020_GoC": "ca", "Cav3p2_RI2021_SC": "ca",
            "Kv3p3_MA2024_PC": "k", "Kv2p2_0010_MA2020_GrC": "k", "Kv1p5_MA2024_PC": "k", "NaF_SU2015_DCN": "na",
            "NaP_SU2015_DCN": "na", "Na_ZH2019_IO": "na", "fKdr_SU2015_DCN": "k", "sKdr_SU2015_DCN": "k",
-           "Kdr_ZH2019_IO": "k"}
+           "Kdr_ZH2019_IO": "k", "CaT_HP1992": "ca", "CaHT_Re1993": "ca"}
 # channels with their own reversal potential (HHTypedNeuron root, not an ion)
-_OWN_E = ("HCN_HM1992", "HCN1_MA2020_GoC", "HCN1_MA2024_PC", "HCN2_MA2020_GoC", "HCN_SU2015_DCN", "HCN_ZH2019_IO")
+_OWN_E = ("HCN_HM1992", "HCN1_MA2020_GoC", "HCN1_MA2024_PC", "HCN2_MA2020_GoC", "HCN_SU2015_DCN", "HCN_ZH2019_IO",
+          "CaL_SU2015_DCN")
 
 
 def _resolve(table: dict, decl) -> dict:
@@ -654,7 +681,7 @@ def _resolve(table: dict, decl) -> dict:
         # Gate("n", q10=3.0, temp_ref=22 degC): potassium.py:1710, :4532, :5296
         p["phi"] = 3.0 ** ((p["temp"] - (273.15 + 22.0)) / 10.0)
     elif name in ("CaL_IS2008", "CaT_HM1992", "CaHT_HM1992", "KA1_HM1992", "KA2_HM1992", "KK2A_HM1992",
-                  "KK2B_HM1992"):
+                  "KK2B_HM1992", "CaT_HP1992", "CaHT_Re1993"):
         p["phi_p"] = p["q10_p"] ** ((p["temp"] - p["temp_ref_p"]) / 10.0)
         p["phi_q"] = p["q10_q"] ** ((p["temp"] - p["temp_ref_q"]) / 10.0)
     elif name in MK.SCHEMES:
@@ -684,12 +711,16 @@ def _resolve(table: dict, decl) -> dict:
     elif name == "HCN2_MA2020_GoC":  # gates q10 3 and the conductance Q10_diff 1.5, at 23 degC
         p["phi"] = 3.0 ** ((p["temp"] - _c2k(23.0)) / 10.0)
         p["gbar_phi"] = 1.5 ** ((p["temp"] - _c2k(23.0)) / 10.0)
-    elif name == "Kv3p3_MA2024_PC":  # Gate q10 2.7 at 22 degC
+    if p.get("gnonspec", 0.0) != 0.0:
+        raise ValueError("Kv1p5_MA2020_GrC's nonspecific current (gnonspec != 0) not restated")
+    p.pop("gnonspec", None)
+    if name == "Kv3p3_MA2024_PC":  # Gate q10 2.7 at 22 degC
         if p["gateCurrent"] != 0.0:
             raise ValueError("Kv3p3 gating current not restated")
         p["phi"] = 2.7 ** ((p["temp"] - _c2k(22.0)) / 10.0)
     elif name in ("Kv2p2_0010_MA2020_GrC", "Kv1p5_MA2024_PC", "NaF_SU2015_DCN", "NaP_SU2015_DCN", "Na_ZH2019_IO",
-                  "fKdr_SU2015_DCN", "sKdr_SU2015_DCN", "Kdr_ZH2019_IO", "HCN_SU2015_DCN", "HCN_ZH2019_IO"):
+                  "fKdr_SU2015_DCN", "sKdr_SU2015_DCN", "Kdr_ZH2019_IO", "HCN_SU2015_DCN", "HCN_ZH2019_IO",
+                  "CaL_SU2015_DCN"):
         p["phi"] = 1.0  # gates without q10 or phi (Kv1p5's Q10 sits in its rates)
     return p
 

@@ -62,6 +62,9 @@ extern "C" int bc_test_rates(int which, const double* v, int n, const double* pr
       case 31: { const KdrioRates<double> r(x); o[0] = r.ninf; o[1] = r.ntau; break; }
       case 32: { const HcndcnRates<double> r(x); o[0] = r.minf; o[1] = r.mtau; break; }
       case 33: { const HcnioRates<double> r(x); o[0] = r.qinf; o[1] = r.qtau; break; }
+      case 34: { const CathpRates<double> r(x, prm[0]); o[0] = r.pinf; o[1] = r.ptau; o[2] = r.qinf; o[3] = r.qtau; break; }
+      case 35: { const CahtreRates<double> r(x, prm[0]); o[0] = r.ap; o[1] = r.bp; o[2] = r.aq; o[3] = r.bq; break; }
+      case 36: { const CaldcnRates<double> r(x); o[0] = r.minf; o[1] = r.mtau; o[2] = r.hinf; o[3] = r.htau; break; }
       default: return -1;
     }
   }

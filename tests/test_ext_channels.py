@@ -1,6 +1,7 @@
 """Extension channels (BC_M_EXT with BC_X_* bits in the record): HCN2_MA2020_GoC,
-Kv3p3_MA2024_PC, Kv2p2_0010_MA2020_GrC, Kv1p5_MA2024_PC, the SU2015 DCN sodium /
-potassium / HCN classes and the ZH2019 IO sodium / potassium / HCN classes.
+Kv3p3_MA2024_PC, Kv2p2_0010_MA2020_GrC, Kv1p5_MA2024_PC (and Kv1p5_MA2020_GrC on its
+kernel), the SU2015 DCN sodium / potassium / HCN / CaL classes, the ZH2019 IO sodium /
+potassium / HCN classes, and CaT_HP1992 and CaHT_Re1993 driving a CalciumDetailed shell.
 
 CPU: the records and their mask, the planner's check of the mask, and the owner
 tables (through the planner tests).  GPU: a DCN-like cell and an IO-like cell
@@ -12,7 +13,7 @@ import numpy as np
 import pytest
 
 from braincell_gb300 import Branch, Cell, Morphology, _abi, catalogue
-from braincell_gb300.mech import (AllRegion, CableProperty, Channel, CurrentClamp, CurrentProbe, CVPerBranch,
+from braincell_gb300.mech import (AllRegion, CableProperty, Channel, CurrentClamp, CurrentProbe, CVPerBranch, Ion,
                                   MechanismProbe, RootLocation, StateProbe, at, branch_in)
 from oracle import staggered as O
 
@@ -96,8 +97,35 @@ def _io_cell(precision="f64"):
     return c
 
 
+def _ca_cell(precision="f64"):
+    soma = Branch.from_lengths(lengths=[20.0], radii=[10.0, 10.0], type="soma")
+    m = Morphology.from_root(soma, name="soma")
+    m.attach(parent="soma", child_branch=Branch.from_lengths(lengths=[150.0], radii=[1.0, 0.6], type="dendrite"),
+             child_name="d0")
+    c = Cell(m, cv_policy=CVPerBranch(5), precision=precision)
+    c.paint(AllRegion(), CableProperty(), Channel("IL", g_max=0.1, E=-65.0))
+    c.paint(branch_in("type", "soma"), Channel("Na_Ba2002", g_max=120.0), Channel("KDR_Ba2002", g_max=40.0),
+            Channel("CaL_SU2015_DCN", g_max=0.5), Channel("Kv1p5_MA2020_GrC", g_max=1.0))
+    c.paint(branch_in("type", "dendrite"), Channel("CaT_HP1992", g_max=0.5), Channel("CaHT_Re1993", g_max=0.5),
+            Ion("CalciumDetailed", C_rest=5e-5, tau=20.0, d=0.5, Ci_initializer=5e-5))
+    c.place(RootLocation(0.5), CurrentClamp(delay=2.0, durations=20.0, amplitudes=0.4), StateProbe(name="v"),
+            MechanismProbe("CaL_SU2015_DCN", "h", name="cal_h"), CurrentProbe(mechanism="Kv1p5_MA2020_GrC", name="i_kv"))
+    c.place(at(1, 0.5), StateProbe(name="v_dend"), MechanismProbe("CalciumDetailed", "Ci", name="ci"),
+            MechanismProbe("CaT_HP1992", "p", name="cat_p"), MechanismProbe("CaHT_Re1993", "q", name="caht_q"),
+            CurrentProbe(ion="ca", name="i_ca"), CurrentProbe(mechanism="CaHT_Re1993", name="i_caht"))
+    return c
+
+
+def test_kv15_grc_runs_on_the_pc_kernel():
+    cable = CableProperty()
+    assert catalogue.region_record([Channel("Kv1p5_MA2020_GrC", g_max=0.3)], cable)[1].tolist() == \
+        catalogue.region_record([Channel("Kv1p5_MA2024_PC", g_max=0.3)], cable)[1].tolist()
+    with pytest.raises(ValueError, match="gnonspec"):
+        catalogue.region_record([Channel("Kv1p5_MA2020_GrC", gnonspec=1e-4)], cable)
+
+
 @pytest.mark.gpu
-@pytest.mark.parametrize("make,n", [(_dcn_cell, 1000), (_io_cell, 800)], ids=["dcn", "io"])
+@pytest.mark.parametrize("make,n", [(_dcn_cell, 1000), (_io_cell, 800), (_ca_cell, 1000)], ids=["dcn", "io", "ca"])
 def test_extension_cells_f64_match_oracle(native_lib, cuda_device, make, n):
     from braincell_gb300.runtime import Plan
 
@@ -113,6 +141,8 @@ def test_extension_cells_f64_match_oracle(native_lib, cuda_device, make, n):
             _close(gpu[k], ref[k], 1e-8, what=f"V probe {k}")
         elif f >= _abi.BC_PROBE_CURRENT:
             _close(gpu[k], ref[k], 1e-9, rtol=1e-8, what=f"current probe {k}")
+        elif f == _abi.BC_STATE_CA_CI:
+            _close(gpu[k], ref[k], 1e-12, rtol=1e-9, what=f"Ci probe {k}")
         else:
             _close(gpu[k], ref[k], 1e-10, what=f"state probe {k}")
     assert len(sp) == len(osp[0][0]) >= 2
@@ -122,7 +152,7 @@ def test_extension_cells_f64_match_oracle(native_lib, cuda_device, make, n):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("make", [_dcn_cell, _io_cell], ids=["dcn", "io"])
+@pytest.mark.parametrize("make", [_dcn_cell, _io_cell, _ca_cell], ids=["dcn", "io", "ca"])
 def test_extension_cells_f32_meet_the_bar(native_lib, cuda_device, make):
     from braincell_gb300.runtime import Plan
 

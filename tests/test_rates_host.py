@@ -31,6 +31,7 @@ CASES = {
     25: ("Kv1p5_MA2024_PC", ("q10f", "Tauact", "Tauinactf", "Tauinacts")), 26: ("NaF_SU2015_DCN", ()),
     27: ("NaP_SU2015_DCN", ()), 28: ("Na_ZH2019_IO", ()), 29: ("fKdr_SU2015_DCN", ()), 30: ("sKdr_SU2015_DCN", ()),
     31: ("Kdr_ZH2019_IO", ()), 32: ("HCN_SU2015_DCN", ()), 33: ("HCN_ZH2019_IO", ()),
+    34: ("CaT_HP1992", ("V_sh",)), 35: ("CaHT_Re1993", ("V_sh",)), 36: ("CaL_SU2015_DCN", ()),
 }
 
 
@@ -79,6 +80,10 @@ def test_kernel_rates_match_oracle(rates_lib, which, shift):
         V = np.concatenate([V, [-64.70, -108.70]])
     if name in ("Na_ZH2019_IO", "Kdr_ZH2019_IO"):  # the removable singularities of x / (1 - e^-x)
         V = np.concatenate([V, [-41.0, -50.0, -41.0 + 1e-7, -50.0 - 1e-7]])
+    if name == "CaHT_Re1993":  # alpha_p's removable singularity at V = V_sh - 27 mV
+        V = np.concatenate([V, p["V_sh"] - 27.0 + np.array([0.0, 1e-7, -1e-7])])
+    if name == "CaL_SU2015_DCN":  # the branch point of h's time constant
+        V = np.concatenate([V, [-81.0, -81.0 + 1e-9]])
     if "V_sh" in keys:
         V = np.concatenate([V, p["V_sh"] + np.array([13.0, 15.0, 40.0, -5.0, -63.0, -70.0, -80.0, -10.0])])
     got = _kernel(rates_lib, which, V, [p[k] for k in keys])
