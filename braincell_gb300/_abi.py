@@ -69,7 +69,10 @@ BC_X_HCNIO = 1 << 11
 BC_X_CATHP = 1 << 12
 BC_X_CAHTRE = 1 << 13
 BC_X_CALDCN = 1 << 14
-BC_X_ALL = 0x7FFF
+BC_X_KCA31 = 1 << 15
+BC_X_SKDCN = 1 << 16
+BC_X_KKV = 1 << 17
+BC_X_ALL = 0x3FFFF
 
 BC_NPARAM = 160
 BC_P_INVCM = 0
@@ -199,6 +202,14 @@ BC_P_CAHTRE_PHIP = 124
 BC_P_CAHTRE_PHIQ = 125
 BC_P_CALDCN_G = 126
 BC_P_CALDCN_E = 127
+BC_P_KCA31_G = 128
+BC_P_SKDCN_G = 129
+BC_P_KKV_G = 130
+BC_P_KKV_VSH = 131
+BC_P_KKV_RA = 132
+BC_P_KKV_RB = 133
+BC_P_KKV_Q = 134
+BC_P_KKV_V12 = 135
 
 BC_ABI_VERSION = 500
 
@@ -261,7 +272,10 @@ BC_CUR_HCNIO = 42
 BC_CUR_CATHP = 43
 BC_CUR_CAHTRE = 44
 BC_CUR_CALDCN = 45
-BC_NCUR = 46
+BC_CUR_KCA31 = 46
+BC_CUR_SKDCN = 47
+BC_CUR_KKV = 48
+BC_NCUR = 49
 
 BC_STATE_V = 0
 BC_STATE_NA_P = 1
@@ -332,7 +346,10 @@ BC_STATE_CAHTRE_P = 87
 BC_STATE_CAHTRE_Q = 88
 BC_STATE_CALDCN_M = 89
 BC_STATE_CALDCN_H = 90
-BC_NSTATE_VIEW = 91
+BC_STATE_KCA31_P = 91
+BC_STATE_SKDCN_Z = 92
+BC_STATE_KKV_N = 93
+BC_NSTATE_VIEW = 94
 # the independent states of each Markov scheme, in view order (first appearance in
 # the scheme's transition list, the dependent state left out)
 MARKOV_STATES = {
@@ -408,6 +425,9 @@ STATE_NAMES = {
     "CaHTRe_q": BC_STATE_CAHTRE_Q,
     "CaLDCN_m": BC_STATE_CALDCN_M,
     "CaLDCN_h": BC_STATE_CALDCN_H,
+    "Kca3p1_p": BC_STATE_KCA31_P,
+    "SKDCN_z": BC_STATE_SKDCN_Z,
+    "KKv_n": BC_STATE_KKV_N,
 }
 for _cls, (_base, _names) in MARKOV_STATES.items():
     for _k, _n in enumerate(_names):

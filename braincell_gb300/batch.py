@@ -366,6 +366,8 @@ PROBE_STATES.update({
     ("CaT_HP1992", "p"): _abi.BC_STATE_CATHP_P, ("CaT_HP1992", "q"): _abi.BC_STATE_CATHP_Q,
     ("CaHT_Re1993", "p"): _abi.BC_STATE_CAHTRE_P, ("CaHT_Re1993", "q"): _abi.BC_STATE_CAHTRE_Q,
     ("CaL_SU2015_DCN", "m"): _abi.BC_STATE_CALDCN_M, ("CaL_SU2015_DCN", "h"): _abi.BC_STATE_CALDCN_H,
+    ("Kca3p1_MA2020_GoC", "p"): _abi.BC_STATE_KCA31_P, ("SK_SU2015_DCN", "z"): _abi.BC_STATE_SKDCN_Z,
+    ("K_Kv_test", "n"): _abi.BC_STATE_KKV_N,
 })
 for _cls, (_base, _names) in _abi.MARKOV_STATES.items():
     for _k, _n in enumerate(_names):
@@ -393,7 +395,8 @@ PROBE_CURRENTS = {
     "NaP_SU2015_DCN": _abi.BC_CUR_NAP, "Na_ZH2019_IO": _abi.BC_CUR_NAIO, "fKdr_SU2015_DCN": _abi.BC_CUR_FKDR,
     "sKdr_SU2015_DCN": _abi.BC_CUR_SKDR, "Kdr_ZH2019_IO": _abi.BC_CUR_KDRIO, "HCN_SU2015_DCN": _abi.BC_CUR_HCNDCN,
     "HCN_ZH2019_IO": _abi.BC_CUR_HCNIO, "CaT_HP1992": _abi.BC_CUR_CATHP, "CaHT_Re1993": _abi.BC_CUR_CAHTRE,
-    "CaL_SU2015_DCN": _abi.BC_CUR_CALDCN,
+    "CaL_SU2015_DCN": _abi.BC_CUR_CALDCN, "Kca3p1_MA2020_GoC": _abi.BC_CUR_KCA31, "SK_SU2015_DCN": _abi.BC_CUR_SKDCN,
+    "K_Kv_test": _abi.BC_CUR_KKV,
 }
 ION_CURRENTS = {"na": _abi.BC_CUR_ION_NA, "k": _abi.BC_CUR_ION_K, "ca": _abi.BC_CUR_ION_CA}
 

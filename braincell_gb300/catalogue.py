@@ -61,6 +61,10 @@ BC_P_EXT_MASK, their parameters after it; conductances in mS/cm^2):
 * ``CaL_SU2015_DCN`` -- channel/calcium.py:1066 (g_max 0.01, E 139 mV, qdeltat 1; not a calcium-ion channel)
 * ``Kv1p5_MA2020_GrC`` -- channel/potassium_sodium.py:38 on Kv1p5_MA2024_PC's kernel (its nonspecific current,
   gnonspec, 0 by default: only 0 is built)
+* ``Kca3p1_MA2020_GoC`` -- channel/potassium_calcium.py:299 (g_max 120; q10_base and temp accepted, unused); the
+  MA2025_BC and MA2024_PC classes (:452, :533) repeat it
+* ``SK_SU2015_DCN`` -- channel/potassium_calcium.py:189 (g_max 0.01, qdeltat 1)
+* ``K_Kv_test`` -- channel/potassium.py:1239 (g_max 0, V_sh 0, Ra 0.02, Rb 0.006, q 9 mV, v12 25 mV; Q10_n 1)
 
 Same-form classes: Na_TM1991 has Na_Ba2002's Traub-Miles rate functions written
 in terms of V_sh - V (sodium.py:275-289 against :154-170), K_TM1991 has
@@ -171,6 +175,10 @@ CHANNELS: dict[str, dict[str, float]] = {
     "CaHT_Re1993": {"g_max": 1.0, "temp": T36, "q10_p": 2.3, "temp_ref_p": celsius2kelvin(23.0), "q10_q": 2.3,
                     "temp_ref_q": celsius2kelvin(23.0), "V_sh": 0.0},
     "CaL_SU2015_DCN": {"g_max": 0.01, "E": 139.0, "qdeltat": 1.0},
+    "Kca3p1_MA2020_GoC": {"g_max": 120.0, "q10_base": 3.0, "temp": T22},
+    "SK_SU2015_DCN": {"g_max": 0.01, "qdeltat": 1.0},
+    "K_Kv_test": {"g_max": 0.0, "V_sh": 0.0, "temp": celsius2kelvin(25.0), "Ra": 0.02, "Rb": 0.006, "q": 9.0,
+                  "v12": 25.0},
 }
 # extension channels: class -> (BC_X_* bit, record entry of g_max, record entry of E or None)
 _EXT = {
@@ -189,6 +197,9 @@ _EXT = {
     "CaT_HP1992": (_abi.BC_X_CATHP, _abi.BC_P_CATHP_G, None),
     "CaHT_Re1993": (_abi.BC_X_CAHTRE, _abi.BC_P_CAHTRE_G, None),
     "CaL_SU2015_DCN": (_abi.BC_X_CALDCN, _abi.BC_P_CALDCN_G, _abi.BC_P_CALDCN_E),
+    "Kca3p1_MA2020_GoC": (_abi.BC_X_KCA31, _abi.BC_P_KCA31_G, None),
+    "SK_SU2015_DCN": (_abi.BC_X_SKDCN, _abi.BC_P_SKDCN_G, None),
+    "K_Kv_test": (_abi.BC_X_KKV, _abi.BC_P_KKV_G, None),
 }
 # cell-type variants with their base class's kinetics; own defaults where they differ
 KINETIC_VARIANTS = {
@@ -200,6 +211,7 @@ KINETIC_VARIANTS = {
     "HCN1_MA2024_PC": {v: {} for v in ("HCN1_MA2025_BC", "HCN1_RI2021_SC")},
     "CaHVA_MA2020_GoC": {"CaHVA_MA2020_GrC": {}},
     "Cav3p2_RI2021_SC": {v: {} for v in ("Cav3p2_MA2025_BC", "Cav3p2_MA2024_PC")},
+    "Kca3p1_MA2020_GoC": {v: {} for v in ("Kca3p1_MA2025_BC", "Kca3p1_MA2024_PC")},
 }
 MARKOV_VARIANTS = {
     "Nav1p6_MA2020_GoC": ("Nav1p6_MA2024_PC", "Nav1p6_MA2025_BC", "Nav1p6_RI2021_SC"),
@@ -462,8 +474,14 @@ def region_record(mechs, cable: CableProperty) -> tuple[int, np.ndarray]:
                 rec[base + 1] = p["V_sh"]
                 rec[base + 2] = q10_phi(p["q10_p"], p["temp"], p["temp_ref_p"])
                 rec[base + 3] = q10_phi(p["q10_q"], p["temp"], p["temp_ref_q"])
-            elif name == "CaL_SU2015_DCN" and p["qdeltat"] != 1.0:
+            elif name in ("CaL_SU2015_DCN", "SK_SU2015_DCN") and p["qdeltat"] != 1.0:
                 raise ValueError(f"{decl.class_name}: qdeltat other than 1 is not built.")
+            elif name == "K_Kv_test":
+                if p["q"] == 0.0:
+                    raise ValueError(f"{decl.class_name}: q must not be 0.")
+                for k, slot in (("V_sh", _abi.BC_P_KKV_VSH), ("Ra", _abi.BC_P_KKV_RA), ("Rb", _abi.BC_P_KKV_RB),
+                                ("q", _abi.BC_P_KKV_Q), ("v12", _abi.BC_P_KKV_V12)):
+                    rec[slot] = p[k]
             rec[g_slot] = g
             if e_slot is not None:
                 rec[e_slot] = p["E"]
@@ -473,7 +491,9 @@ def region_record(mechs, cable: CableProperty) -> tuple[int, np.ndarray]:
             rec[base], rec[base + 1] = p["g_max"], p["V_sh"]
             rec[base + 2] = q10_phi(p["q10_p"], p["temp"], p["temp_ref_p"])
             rec[base + 3] = q10_phi(p["q10_q"], p["temp"], p["temp_ref_q"])
-    if bits & (_abi.BC_M_AHP | _abi.BC_M_KCA22 | _abi.BC_M_KCA11) and not bits & _abi.BC_M_CADET:
+    ci_gated = bits & (_abi.BC_M_AHP | _abi.BC_M_KCA22 | _abi.BC_M_KCA11) or \
+        int(rec[_abi.BC_P_EXT_MASK]) & (_abi.BC_X_KCA31 | _abi.BC_X_SKDCN)
+    if ci_gated and not bits & _abi.BC_M_CADET:
         # AHP and the Kca channels read Ci from the calcium ion; with a fixed Ca ion
         # Ci is the class default.
         rec[_abi.BC_P_CA_CI0] = 5e-5

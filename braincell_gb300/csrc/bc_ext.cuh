@@ -22,8 +22,12 @@
 //   CaT_HP1992             channel/calcium.py:377-509
 //   CaHT_Re1993            channel/calcium.py:667-788
 //   CaL_SU2015_DCN         channel/calcium.py:1066-1219
+//   Kca3p1_MA2020_GoC      channel/potassium_calcium.py:299-450
+//   SK_SU2015_DCN          channel/potassium_calcium.py:189-297
+//   K_Kv_test              channel/potassium.py:1239-1372
 // CaT_HP1992 and CaHT_Re1993 carry calcium: their step-start current joins the
-// calcium shell's drive, as CaL's and CaT's do.
+// calcium shell's drive, as CaL's and CaT's do.  Kca3p1 and SK read Ci: the new Ci
+// of a dynamic calcium ion, else the fixed one (BC_P_CA_CI0), as AHP_De1994 does.
 #pragma once
 
 #include "bc_mech.cuh"
@@ -57,7 +61,10 @@ constexpr int kSlotCahtreP = 88;
 constexpr int kSlotCahtreQ = 89;
 constexpr int kSlotCaldcnM = 90;
 constexpr int kSlotCaldcnH = 91;
-constexpr int kNumSlotsExt = 92;
+constexpr int kSlotKca31P = 92;
+constexpr int kSlotSkdcnZ = 93;
+constexpr int kSlotKkvN = 94;
+constexpr int kNumSlotsExt = 95;
 
 // x / (1 - e^-x) = 1 / exprel(-x), finite at x = 0 (the reference's
 // _x_over_one_minus_exp_neg_stable, channel/sodium.py:50-55)
@@ -265,6 +272,46 @@ struct CaldcnRates {
   }
 };
 
+// Kca3p1_MA2020_GoC: p, alpha = exp((V + 70) / 27) c(Ci), beta = 0.05, with
+// c = 500 (0.015 - Ci) / (exp((0.015 - Ci) / 0.0013) - 1) below Ci = 0.01 mM and its
+// value at 0.01 above (temperature parameters accepted but unused, phi 1).
+template <typename Real>
+struct Kca31Rates {
+  Real a, b;
+  __host__ __device__ __forceinline__ Kca31Rates(Real v, Real ci) {
+    const Real c = ci < Real(0.01) ? Real(500 * 0.0013) / exprel((Real(0.015) - ci) / Real(0.0013))
+                                   : Real(500 * 0.0013) / exprel(Real(0.005 / 0.0013));
+    a = aexp((v + Real(70)) / Real(27)) * c;
+    b = Real(0.05);
+  }
+};
+
+// SK_SU2015_DCN: z, inf = Ci^4 / (Ci^4 + 8.1e-15), tau = 1 - 186.67 Ci below
+// Ci = 0.005 mM, else 0.0667 ms (qdeltat = 1).
+template <typename Real>
+struct SkdcnRates {
+  Real zinf, ztau;
+  __host__ __device__ __forceinline__ explicit SkdcnRates(Real ci) {
+    const Real c2 = ci * ci;
+    const Real c4 = c2 * c2;
+    zinf = c4 / (c4 + Real(8.1e-15));
+    ztau = ci < Real(0.005) ? Real(1) - Real(186.67) * ci : Real(0.0667);
+  }
+};
+
+// K_Kv_test: n on y = V - V_sh - v12; inf = 1 / (1 + exp(-y / q)),
+// 1 / tau = Ra y / (1 - e^(-y / q)) - Rb y / (1 - e^(y / q)), i.e.
+// q (Ra x/(1 - e^-x) at x = y / q + Rb the same at -y / q), finite at y = 0.
+template <typename Real>
+struct KkvRates {
+  Real ninf, ntau;
+  __host__ __device__ __forceinline__ KkvRates(Real v, Real vsh, Real ra, Real rb, Real q, Real v12) {
+    const Real y = v - vsh - v12;
+    ninf = Real(1) / (Real(1) + aexp(-y / q));
+    ntau = Real(1) / (q * (ra * x_over_1mexp(y / q) + rb * x_over_1mexp(-y / q)));
+  }
+};
+
 // The region's BC_X_* bits (an integer stored as a record real).
 template <typename Real>
 __host__ __device__ __forceinline__ uint32_t ext_mask(const Real* P) {
@@ -386,6 +433,24 @@ __device__ __forceinline__ Real ext_current(const Real* st, int N, const Real* P
         e = P[BC_P_CALDCN_E];
       }
       break;
+    case BC_CUR_KCA31:
+      if ((has = (x & BC_X_KCA31) != 0)) {
+        g = P[BC_P_KCA31_G] * st[kSlotKca31P * N];
+        e = P[BC_P_EK];
+      }
+      break;
+    case BC_CUR_SKDCN:
+      if ((has = (x & BC_X_SKDCN) != 0)) {
+        g = P[BC_P_SKDCN_G] * st[kSlotSkdcnZ * N];
+        e = P[BC_P_EK];
+      }
+      break;
+    case BC_CUR_KKV:
+      if ((has = (x & BC_X_KKV) != 0)) {
+        g = P[BC_P_KKV_G] * st[kSlotKkvN * N];
+        e = P[BC_P_EK];
+      }
+      break;
   }
   if (!has) return Real(0);
   if (gv) *gv = code == BC_CUR_KV15 ? gd : g;
@@ -394,7 +459,7 @@ __device__ __forceinline__ Real ext_current(const Real* st, int N, const Real* P
 
 // Gate update of one node's extension channels at v (exp-Euler, as the others).
 template <typename Real>
-__device__ __forceinline__ void ext_gates(Real* st, int N, const Real* P, uint32_t x, Real v, Real dt) {
+__device__ __forceinline__ void ext_gates(Real* st, int N, const Real* P, uint32_t x, Real v, Real ci, Real dt) {
   if (x & BC_X_HCN2) {
     const Hcn2Rates<Real> r(v);
     const Real phi = P[BC_P_HCN2_PHI];
@@ -466,16 +531,29 @@ __device__ __forceinline__ void ext_gates(Real* st, int N, const Real* P, uint32
     st[kSlotCaldcnM * N] = gate_it(st[kSlotCaldcnM * N], r.minf, r.mtau, Real(1), dt);
     st[kSlotCaldcnH * N] = gate_it(st[kSlotCaldcnH * N], r.hinf, r.htau, Real(1), dt);
   }
+  if (x & BC_X_KCA31) {
+    const Kca31Rates<Real> r(v, ci);
+    st[kSlotKca31P * N] = gate_ab<Real, true>(st[kSlotKca31P * N], r.a, r.b, Real(1), dt);
+  }
+  if (x & BC_X_SKDCN) {
+    const SkdcnRates<Real> r(ci);
+    st[kSlotSkdcnZ * N] = gate_it(st[kSlotSkdcnZ * N], r.zinf, r.ztau, Real(1), dt);
+  }
+  if (x & BC_X_KKV) {
+    const KkvRates<Real> r(v, P[BC_P_KKV_VSH], P[BC_P_KKV_RA], P[BC_P_KKV_RB], P[BC_P_KKV_Q], P[BC_P_KKV_V12]);
+    st[kSlotKkvN * N] = gate_it(st[kSlotKkvN * N], r.ninf, r.ntau, Real(1), dt);
+  }
 }
 
 // A node's extension channels: gates at v (when advancing), then their G and I.
-// eca: E_Ca of the calcium after this step's shell update (the calcium channels).
+// ci and eca: Ci and E_Ca after this step's shell update (the calcium-gated and
+// the calcium channels).
 template <typename Real>
-__device__ __noinline__ void ext_channels(Real* st, int N, const Real* P, Real v, Real eca, Real dt, bool advance,
-                                          Real& G, Real& I) {
+__device__ __noinline__ void ext_channels(Real* st, int N, const Real* P, Real v, Real ci, Real eca, Real dt,
+                                          bool advance, Real& G, Real& I) {
   const uint32_t x = ext_mask(P);
-  if (advance) ext_gates(st, N, P, x, v, dt);
-  for (int code = BC_CUR_HCN2; code <= BC_CUR_CALDCN; ++code) {
+  if (advance) ext_gates(st, N, P, x, v, ci, dt);
+  for (int code = BC_CUR_HCN2; code <= BC_CUR_KKV; ++code) {
     Real g = Real(0);
     const Real i = ext_current(st, N, P, x, v, eca, code, &g);
     G += g;
@@ -551,6 +629,15 @@ __device__ __forceinline__ void ext_steady(const Real* P, Real* st, int N, Real 
     st[kSlotCaldcnM * N] = r.minf;
     st[kSlotCaldcnH * N] = r.hinf;
   }
+  // the calcium-gated channels at the reset Ci
+  if (x & BC_X_KCA31) {
+    const Kca31Rates<Real> r(v, P[BC_P_CA_CI0]);
+    st[kSlotKca31P * N] = r.a / (r.a + r.b);
+  }
+  if (x & BC_X_SKDCN) st[kSlotSkdcnZ * N] = SkdcnRates<Real>(P[BC_P_CA_CI0]).zinf;
+  if (x & BC_X_KKV)
+    st[kSlotKkvN * N] =
+        KkvRates<Real>(v, P[BC_P_KKV_VSH], P[BC_P_KKV_RA], P[BC_P_KKV_RB], P[BC_P_KKV_Q], P[BC_P_KKV_V12]).ninf;
 }
 
 }  // namespace bc

@@ -362,7 +362,7 @@ __device__ __forceinline__ double probe_current(const Real* st, int N, const Rea
         return cerebellar_ca_current(st, N, P, m & BC_M_CAV32, v, eca(), (Real*)nullptr);
       default:
         // extension channels: the record's list exists only where BC_M_EXT is set
-        if (c >= BC_CUR_HCN2 && c <= BC_CUR_CALDCN && (m & BC_M_EXT))
+        if (c >= BC_CUR_HCN2 && c <= BC_CUR_KKV && (m & BC_M_EXT))
           return ext_current(st, N, P, ext_mask(P), v, (c == BC_CUR_CATHP || c == BC_CUR_CAHTRE) ? eca() : Real(0), c,
                              (Real*)nullptr);
     }
@@ -378,7 +378,8 @@ __device__ __forceinline__ double probe_current(const Real* st, int N, const Rea
              double(cur(BC_CUR_KK2B)) + double(cur(BC_CUR_KNI)) + double(cur(BC_CUR_KCA22)) + double(cur(BC_CUR_KCA11)) +
              double(cur(BC_CUR_KV34)) + double(cur(BC_CUR_KV43)) + double(cur(BC_CUR_KV11)) + double(cur(BC_CUR_KIR23)) +
              double(cur(BC_CUR_KV33)) + double(cur(BC_CUR_KV22)) + double(cur(BC_CUR_KV15)) + double(cur(BC_CUR_FKDR)) +
-             double(cur(BC_CUR_SKDR)) + double(cur(BC_CUR_KDRIO));
+             double(cur(BC_CUR_SKDR)) + double(cur(BC_CUR_KDRIO)) + double(cur(BC_CUR_KCA31)) + double(cur(BC_CUR_SKDCN)) +
+             double(cur(BC_CUR_KKV));
     case BC_CUR_ION_CA:
       return double(cur(BC_CUR_CAL)) + double(cur(BC_CUR_CAT)) + double(cur(BC_CUR_CAHVA)) + double(cur(BC_CUR_CAV23)) +
              double(cur(BC_CUR_CAV32)) + double(cur(BC_CUR_CATHP)) + double(cur(BC_CUR_CAHTRE));
@@ -639,7 +640,7 @@ __device__ __noinline__ void extra_channels(Real* st, int N, const Real* P, uint
   if (m & BC_M_EXT) {
     const Real eca =
         (m & BC_M_CADET) ? Real(kNernstCa) * P[BC_P_CA_TEMP] * dlog(P[BC_P_CA_CO] / ci) : P[BC_P_ECA];
-    ext_channels(st, N, P, v, eca, dt, advance, G, I);
+    ext_channels(st, N, P, v, ci, eca, dt, advance, G, I);
   }
 }
 

@@ -102,7 +102,10 @@ typedef int32_t bc_status;
 #define BC_X_CATHP (1u << 12)  /* channel/calcium.py:377 CaT_HP1992 p^2 q, E_Ca (Ci drive)   */
 #define BC_X_CAHTRE (1u << 13) /* channel/calcium.py:667 CaHT_Re1993 p^2 q, E_Ca (Ci drive)  */
 #define BC_X_CALDCN (1u << 14) /* channel/calcium.py:1066 CaL_SU2015_DCN m^2 h, own E        */
-#define BC_X_ALL 0x7FFFu
+#define BC_X_KCA31 (1u << 15)  /* channel/potassium_calcium.py:299 Kca3p1_MA2020_GoC p(V, Ci), E_K */
+#define BC_X_SKDCN (1u << 16)  /* channel/potassium_calcium.py:189 SK_SU2015_DCN z(Ci), E_K  */
+#define BC_X_KKV (1u << 17)    /* channel/potassium.py:1239 K_Kv_test n, E_K                 */
+#define BC_X_ALL 0x3FFFFu
 
 /* Per-region parameter record (double[BC_NPARAM]); index names below. */
 #define BC_NPARAM 160
@@ -234,7 +237,15 @@ typedef int32_t bc_status;
 #define BC_P_CAHTRE_PHIQ 125
 #define BC_P_CALDCN_G 126
 #define BC_P_CALDCN_E 127
-/* 128 .. 159: reserved for further extension channels (0) */
+#define BC_P_KCA31_G 128
+#define BC_P_SKDCN_G 129
+#define BC_P_KKV_G 130
+#define BC_P_KKV_VSH 131
+#define BC_P_KKV_RA 132     /* 1/(mV ms) */
+#define BC_P_KKV_RB 133
+#define BC_P_KKV_Q 134      /* mV        */
+#define BC_P_KKV_V12 135    /* mV        */
+/* 136 .. 159: reserved for further extension channels (0) */
 
 /* ------------------------------------------------------------------ batch spec */
 /*
@@ -400,7 +411,7 @@ const char* bc_last_error(void);
  * HH and calcium channels (BC_M_KV34 .. CAV32, a 96-entry parameter record, state
  * views 51-65, BC_PROBE_CURRENT 128).  0.5.0: extension channels (BC_M_EXT with
  * BC_X_* bits in the record's BC_P_EXT_MASK, a 160-entry parameter record, state
- * views 66-90, current codes 31-45). */
+ * views 66-93, current codes 31-48). */
 #define BC_ABI_VERSION 500
 int32_t bc_version(void);
 /* Fill opts with defaults. */
@@ -527,7 +538,10 @@ bc_status bc_check(bc_plan_t plan, void* stream);
 #define BC_STATE_CAHTRE_Q 88
 #define BC_STATE_CALDCN_M 89
 #define BC_STATE_CALDCN_H 90
-#define BC_NSTATE_VIEW 91
+#define BC_STATE_KCA31_P 91
+#define BC_STATE_SKDCN_Z 92
+#define BC_STATE_KKV_N 93
+#define BC_NSTATE_VIEW 94
 /* Current probes (mech/_point.py CurrentProbe, _multi_compartment/probes.py:184-258):
    probe_field = BC_PROBE_CURRENT + one of the codes below records that current
    density (uA/cm^2, outward negative as g (E - V)) after the step.             */
@@ -578,7 +592,10 @@ bc_status bc_check(bc_plan_t plan, void* stream);
 #define BC_CUR_CATHP 43  /* CaT_HP1992             */
 #define BC_CUR_CAHTRE 44 /* CaHT_Re1993            */
 #define BC_CUR_CALDCN 45 /* CaL_SU2015_DCN         */
-#define BC_NCUR 46
+#define BC_CUR_KCA31 46  /* Kca3p1_MA2020_GoC      */
+#define BC_CUR_SKDCN 47  /* SK_SU2015_DCN          */
+#define BC_CUR_KKV 48    /* K_Kv_test              */
+#define BC_NCUR 49
 bc_status bc_state_download(bc_plan_t plan, int32_t which, double* out /* [n_cv] */, void* stream);
 /* Set the amplitude (nA) of every current-clamp pulse of the batch spec, in spec
  * order (amp_nA[n_pulses]); times and locations are unchanged.  Takes effect from

@@ -144,6 +144,9 @@ CHANNEL_DEFAULTS.update({
     "CaHT_Re1993": dict(g_max=1.0, temp=_c2k(36.0), q10_p=2.3, temp_ref_p=_c2k(23.0), q10_q=2.3,
                         temp_ref_q=_c2k(23.0), V_sh=0.0),  # calcium.py:667
     "CaL_SU2015_DCN": dict(g_max=0.01, E=139.0, qdeltat=1.0),  # calcium.py:1066
+    "Kca3p1_MA2020_GoC": dict(g_max=120.0, q10_base=3.0, temp=_c2k(22.0)),  # potassium_calcium.py:299
+    "SK_SU2015_DCN": dict(g_max=0.01, qdeltat=1.0),  # potassium_calcium.py:189
+    "K_Kv_test": dict(g_max=0.0, V_sh=0.0, temp=_c2k(25.0), Ra=0.02, Rb=0.006, q=9.0, v12=25.0),  # potassium.py:1239
 })
 # cell-type variants that run their base class's kinetics, with their own defaults
 # where they differ (each class body is the base's: potassium.py, hyperpolarization_activated.py)
@@ -160,6 +163,7 @@ _VARIANTS = {
     # potassium_sodium.py:38-259: Kv1p5_MA2024_PC's kinetics and K current, plus a
     # nonspecific current of conductance gnonspec (0 by default; only 0 is restated)
     "Kv1p5_MA2020_GrC": ("Kv1p5_MA2024_PC", {"gnonspec": 0.0}),
+    **{v: ("Kca3p1_MA2020_GoC", {}) for v in ("Kca3p1_MA2025_BC", "Kca3p1_MA2024_PC")},
     **{v: ("Cav3p2_RI2021_SC", {}) for v in ("Cav3p2_MA2025_BC", "Cav3p2_MA2024_PC")},
 }
 
@@ -598,6 +602,20 @@ def rates(name: str, V, p: dict, Ci=None):
         return {"m": ("it", 1.0 / (1.0 + np.exp((V + 56.0) / -6.2)),
                       (0.333 / (np.exp((V + 131.0) / -16.7) + np.exp((V + 15.8) / 18.2)) + 0.204) / p["qdeltat"]),
                 "h": ("it", 1.0 / (1.0 + np.exp((V + 80.0) / 4.0)), ht / p["qdeltat"])}
+    if name == "Kca3p1_MA2020_GoC":  # potassium_calcium.py:299-450 (q10_base and temp unused)
+        ci = np.asarray(Ci, dtype=float)
+        c1 = 500.0 * 0.0013 / exprel((0.015 - ci) / 0.0013)
+        c2 = 500.0 * 0.005 / (np.exp(0.005 / 0.0013) - 1.0)
+        a = np.exp((V + 70.0) / 27.0) * np.where(ci < 0.01, c1, c2)
+        return {"p": ("ab", a, 0.05 * np.ones_like(a))}
+    if name == "SK_SU2015_DCN":  # potassium_calcium.py:189-297
+        ci = np.asarray(Ci, dtype=float) * np.ones_like(V)
+        return {"z": ("it", ci ** 4 / (ci ** 4 + 8.1e-15), np.where(ci < 0.005, 1.0 - 186.67 * ci, 0.0667) / p["qdeltat"])}
+    if name == "K_Kv_test":  # potassium.py:1239-1372; y / (1 - e^(-y/q)) taken through its limit at y = 0
+        y = V - p["V_sh"] - p["v12"]
+        q = p["q"]
+        denom = q * (p["Ra"] * _x_over_1mexp(y / q) + p["Rb"] * _x_over_1mexp(-y / q))
+        return {"n": ("it", 1.0 / (1.0 + np.exp(-y / q)), 1.0 / denom)}
     if name in ("KM_RI2021_SC", "KM_MA2020_GoC", "KM_MA2020_GrC"):  # potassium.py:1735-1748, :4553-4567, :5317-5331
         a = 0.0033 * np.exp((V + 30.0) / 40.0)
         b = 0.0033 * np.exp((V + 30.0) / -20.0)
@@ -649,6 +667,9 @@ _GATES = {  # (gate, power, phi-key)
     "CaT_HP1992": (("p", 2, "phi_p"), ("q", 1, "phi_q")),
     "CaHT_Re1993": (("p", 2, "phi_p"), ("q", 1, "phi_q")),
     "CaL_SU2015_DCN": (("m", 2, "phi"), ("h", 1, "phi")),
+    "Kca3p1_MA2020_GoC": (("p", 1, "phi"),),
+    "SK_SU2015_DCN": (("z", 1, "phi"),),
+    "K_Kv_test": (("n", 1, "phi"),),
 }
 _ION_OF = {"Na_Ba2002": "na", "KDR_Ba2002": "k", "CaL_IS2008": "ca", "CaT_HM1992": "ca",
            "K_Leak": "k", "AHP_De1994": "k", "Na_HH1952": "na", "K_HH1952": "k", "KM_RI2021_SC": "k",
@@ -660,7 +681,8 @@ _ION_OF = {"Na_Ba2002": "na", "KDR_Ba2002": "k", "CaL_IS2008": "ca", "CaT_HM1992
            "CaHVA_MA2020_GoC": "ca", "Cav2p3_MA2020_GoC": "ca", "Cav3p2_RI2021_SC": "ca",
            "Kv3p3_MA2024_PC": "k", "Kv2p2_0010_MA2020_GrC": "k", "Kv1p5_MA2024_PC": "k", "NaF_SU2015_DCN": "na",
            "NaP_SU2015_DCN": "na", "Na_ZH2019_IO": "na", "fKdr_SU2015_DCN": "k", "sKdr_SU2015_DCN": "k",
-           "Kdr_ZH2019_IO": "k", "CaT_HP1992": "ca", "CaHT_Re1993": "ca"}
+           "Kdr_ZH2019_IO": "k", "CaT_HP1992": "ca", "CaHT_Re1993": "ca", "Kca3p1_MA2020_GoC": "k",
+           "SK_SU2015_DCN": "k", "K_Kv_test": "k"}
 # channels with their own reversal potential (HHTypedNeuron root, not an ion)
 _OWN_E = ("HCN_HM1992", "HCN1_MA2020_GoC", "HCN1_MA2024_PC", "HCN2_MA2020_GoC", "HCN_SU2015_DCN", "HCN_ZH2019_IO",
           "CaL_SU2015_DCN")
@@ -720,7 +742,7 @@ def _resolve(table: dict, decl) -> dict:
         p["phi"] = 2.7 ** ((p["temp"] - _c2k(22.0)) / 10.0)
     elif name in ("Kv2p2_0010_MA2020_GrC", "Kv1p5_MA2024_PC", "NaF_SU2015_DCN", "NaP_SU2015_DCN", "Na_ZH2019_IO",
                   "fKdr_SU2015_DCN", "sKdr_SU2015_DCN", "Kdr_ZH2019_IO", "HCN_SU2015_DCN", "HCN_ZH2019_IO",
-                  "CaL_SU2015_DCN"):
+                  "CaL_SU2015_DCN", "Kca3p1_MA2020_GoC", "SK_SU2015_DCN", "K_Kv_test"):
         p["phi"] = 1.0  # gates without q10 or phi (Kv1p5's Q10 sits in its rates)
     return p
 

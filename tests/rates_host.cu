@@ -6,7 +6,8 @@
 using namespace bc;
 
 // Kernel rate structure `which` at n voltages v (mV) with parameters prm (V_sh
-// first; KNI: V_sh, tau_max; Kv1p5: its Q10 factor, Tauact, Tauinactf, Tauinacts).
+// first; KNI: V_sh, tau_max; Kv1p5: its Q10 factor, Tauact, Tauinactf, Tauinacts;
+// Kca3p1 and SK: Ci (mM); K_Kv_test: V_sh, Ra, Rb, q, v12).
 // out[6 i .. 6 i + 5] receives the gate rates in the oracle's order: per gate
 // (alpha, beta) or (inf, tau); unused entries are 0.
 // Returns 0, or -1 for an unknown structure.
@@ -65,6 +66,13 @@ extern "C" int bc_test_rates(int which, const double* v, int n, const double* pr
       case 34: { const CathpRates<double> r(x, prm[0]); o[0] = r.pinf; o[1] = r.ptau; o[2] = r.qinf; o[3] = r.qtau; break; }
       case 35: { const CahtreRates<double> r(x, prm[0]); o[0] = r.ap; o[1] = r.bp; o[2] = r.aq; o[3] = r.bq; break; }
       case 36: { const CaldcnRates<double> r(x); o[0] = r.minf; o[1] = r.mtau; o[2] = r.hinf; o[3] = r.htau; break; }
+      case 37: { const Kca31Rates<double> r(x, prm[0]); o[0] = r.a; o[1] = r.b; break; }
+      case 38: { const SkdcnRates<double> r(prm[0]); o[0] = r.zinf; o[1] = r.ztau; break; }
+      case 39: {
+        const KkvRates<double> r(x, prm[0], prm[1], prm[2], prm[3], prm[4]);
+        o[0] = r.ninf; o[1] = r.ntau;
+        break;
+      }
       default: return -1;
     }
   }

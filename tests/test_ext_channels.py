@@ -1,7 +1,8 @@
 """Extension channels (BC_M_EXT with BC_X_* bits in the record): HCN2_MA2020_GoC,
 Kv3p3_MA2024_PC, Kv2p2_0010_MA2020_GrC, Kv1p5_MA2024_PC (and Kv1p5_MA2020_GrC on its
 kernel), the SU2015 DCN sodium / potassium / HCN / CaL classes, the ZH2019 IO sodium /
-potassium / HCN classes, and CaT_HP1992 and CaHT_Re1993 driving a CalciumDetailed shell.
+potassium / HCN classes, CaT_HP1992 and CaHT_Re1993 driving a CalciumDetailed shell, the
+calcium-gated Kca3p1 (and its BC / PC classes) and SK_SU2015_DCN, and K_Kv_test.
 
 CPU: the records and their mask, the planner's check of the mask, and the owner
 tables (through the planner tests).  GPU: a DCN-like cell and an IO-like cell
@@ -116,6 +117,27 @@ def _ca_cell(precision="f64"):
     return c
 
 
+def _kca_cell(precision="f64"):
+    soma = Branch.from_lengths(lengths=[20.0], radii=[10.0, 10.0], type="soma")
+    m = Morphology.from_root(soma, name="soma")
+    m.attach(parent="soma", child_branch=Branch.from_lengths(lengths=[150.0], radii=[1.0, 0.6], type="dendrite"),
+             child_name="d0")
+    c = Cell(m, cv_policy=CVPerBranch(5), precision=precision)
+    c.paint(AllRegion(), CableProperty(), Channel("IL", g_max=0.1, E=-65.0))
+    # the soma's SK sees the fixed Ci; the dendrite's Kca3p1 and SK the shell's Ci
+    c.paint(branch_in("type", "soma"), Channel("Na_Ba2002", g_max=120.0), Channel("KDR_Ba2002", g_max=30.0),
+            Channel("K_Kv_test", g_max=0.5), Channel("SK_SU2015_DCN", g_max=0.05))
+    c.paint(branch_in("type", "dendrite"), Channel("CaHT_Re1993", g_max=1.0), Channel("Kca3p1_MA2024_PC", g_max=0.3),
+            Channel("SK_SU2015_DCN", g_max=0.3),
+            Ion("CalciumDetailed", C_rest=5e-5, tau=20.0, d=0.5, Ci_initializer=5e-5))
+    c.place(RootLocation(0.5), CurrentClamp(delay=2.0, durations=20.0, amplitudes=0.5), StateProbe(name="v"),
+            MechanismProbe("K_Kv_test", "n", name="kkv_n"), CurrentProbe(mechanism="SK_SU2015_DCN", name="i_sk_soma"))
+    c.place(at(1, 0.5), StateProbe(name="v_dend"), MechanismProbe("CalciumDetailed", "Ci", name="ci"),
+            MechanismProbe("Kca3p1_MA2024_PC", "p", name="kca31_p"), MechanismProbe("SK_SU2015_DCN", "z", name="sk_z"),
+            CurrentProbe(ion="k", name="i_k"))
+    return c
+
+
 def test_kv15_grc_runs_on_the_pc_kernel():
     cable = CableProperty()
     assert catalogue.region_record([Channel("Kv1p5_MA2020_GrC", g_max=0.3)], cable)[1].tolist() == \
@@ -125,7 +147,8 @@ def test_kv15_grc_runs_on_the_pc_kernel():
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("make,n", [(_dcn_cell, 1000), (_io_cell, 800), (_ca_cell, 1000)], ids=["dcn", "io", "ca"])
+@pytest.mark.parametrize("make,n", [(_dcn_cell, 1000), (_io_cell, 800), (_ca_cell, 1000), (_kca_cell, 1000)],
+                         ids=["dcn", "io", "ca", "kca"])
 def test_extension_cells_f64_match_oracle(native_lib, cuda_device, make, n):
     from braincell_gb300.runtime import Plan
 
@@ -152,7 +175,7 @@ def test_extension_cells_f64_match_oracle(native_lib, cuda_device, make, n):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("make", [_dcn_cell, _io_cell, _ca_cell], ids=["dcn", "io", "ca"])
+@pytest.mark.parametrize("make", [_dcn_cell, _io_cell, _ca_cell, _kca_cell], ids=["dcn", "io", "ca", "kca"])
 def test_extension_cells_f32_meet_the_bar(native_lib, cuda_device, make):
     from braincell_gb300.runtime import Plan
 

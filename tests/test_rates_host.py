@@ -32,6 +32,8 @@ CASES = {
     27: ("NaP_SU2015_DCN", ()), 28: ("Na_ZH2019_IO", ()), 29: ("fKdr_SU2015_DCN", ()), 30: ("sKdr_SU2015_DCN", ()),
     31: ("Kdr_ZH2019_IO", ()), 32: ("HCN_SU2015_DCN", ()), 33: ("HCN_ZH2019_IO", ()),
     34: ("CaT_HP1992", ("V_sh",)), 35: ("CaHT_Re1993", ("V_sh",)), 36: ("CaL_SU2015_DCN", ()),
+    37: ("Kca3p1_MA2020_GoC", ("Ci",)), 38: ("SK_SU2015_DCN", ("Ci",)),
+    39: ("K_Kv_test", ("V_sh", "Ra", "Rb", "q", "v12")),
 }
 
 
@@ -86,8 +88,13 @@ def test_kernel_rates_match_oracle(rates_lib, which, shift):
         V = np.concatenate([V, [-81.0, -81.0 + 1e-9]])
     if "V_sh" in keys:
         V = np.concatenate([V, p["V_sh"] + np.array([13.0, 15.0, 40.0, -5.0, -63.0, -70.0, -80.0, -10.0])])
+    # the calcium-gated classes at a Ci on each side of their branch points (0.005, 0.01 mM)
+    p["Ci"] = {0.0: 2e-3, 7.5: 0.012}[shift] if name == "Kca3p1_MA2020_GoC" else \
+        ({0.0: 1e-4, 7.5: 0.007}[shift] if name == "SK_SU2015_DCN" else None)
+    if name == "K_Kv_test":  # its removable singularity at V = V_sh + v12
+        V = np.concatenate([V, p["V_sh"] + p["v12"] + np.array([0.0, 1e-7, -1e-7])])
     got = _kernel(rates_lib, which, V, [p[k] for k in keys])
-    ref = O.rates(name, V, p)
+    ref = O.rates(name, V, p, Ci=p["Ci"])
     cols = [c for g in ref for c in (ref[g][1], ref[g][2])]
     for k, col in enumerate(cols):
         np.testing.assert_allclose(got[:, k], np.broadcast_to(col, V.shape), rtol=1e-12, atol=1e-300,
