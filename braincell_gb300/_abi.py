@@ -72,7 +72,9 @@ BC_X_CALDCN = 1 << 14
 BC_X_KCA31 = 1 << 15
 BC_X_SKDCN = 1 << 16
 BC_X_KKV = 1 << 17
-BC_X_ALL = 0x3FFFF
+BC_X_CAN = 1 << 18
+BC_X_CAIO = 1 << 19
+BC_X_ALL = 0xFFFFF
 
 BC_NPARAM = 160
 BC_P_INVCM = 0
@@ -210,6 +212,13 @@ BC_P_KKV_RA = 132
 BC_P_KKV_RB = 133
 BC_P_KKV_Q = 134
 BC_P_KKV_V12 = 135
+BC_P_CAN_G = 136
+BC_P_CAN_E = 137
+BC_P_CAN_PHI = 138
+BC_P_CAIO_G = 139
+BC_P_CAIO_E = 140
+BC_P_CAIO_MID = 141
+BC_P_CAIO_FREEZE = 142
 
 BC_ABI_VERSION = 500
 
@@ -275,7 +284,9 @@ BC_CUR_CALDCN = 45
 BC_CUR_KCA31 = 46
 BC_CUR_SKDCN = 47
 BC_CUR_KKV = 48
-BC_NCUR = 49
+BC_CUR_CAN = 49
+BC_CUR_CAIO = 50
+BC_NCUR = 51
 
 BC_STATE_V = 0
 BC_STATE_NA_P = 1
@@ -349,7 +360,9 @@ BC_STATE_CALDCN_H = 90
 BC_STATE_KCA31_P = 91
 BC_STATE_SKDCN_Z = 92
 BC_STATE_KKV_N = 93
-BC_NSTATE_VIEW = 94
+BC_STATE_CAN_P = 94
+BC_STATE_CAIO_H = 95
+BC_NSTATE_VIEW = 96
 # the independent states of each Markov scheme, in view order (first appearance in
 # the scheme's transition list, the dependent state left out)
 MARKOV_STATES = {
@@ -428,6 +441,8 @@ STATE_NAMES = {
     "Kca3p1_p": BC_STATE_KCA31_P,
     "SKDCN_z": BC_STATE_SKDCN_Z,
     "KKv_n": BC_STATE_KKV_N,
+    "CaN_p": BC_STATE_CAN_P,
+    "CaIO_h": BC_STATE_CAIO_H,
 }
 for _cls, (_base, _names) in MARKOV_STATES.items():
     for _k, _n in enumerate(_names):

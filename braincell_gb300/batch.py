@@ -367,7 +367,8 @@ PROBE_STATES.update({
     ("CaHT_Re1993", "p"): _abi.BC_STATE_CAHTRE_P, ("CaHT_Re1993", "q"): _abi.BC_STATE_CAHTRE_Q,
     ("CaL_SU2015_DCN", "m"): _abi.BC_STATE_CALDCN_M, ("CaL_SU2015_DCN", "h"): _abi.BC_STATE_CALDCN_H,
     ("Kca3p1_MA2020_GoC", "p"): _abi.BC_STATE_KCA31_P, ("SK_SU2015_DCN", "z"): _abi.BC_STATE_SKDCN_Z,
-    ("K_Kv_test", "n"): _abi.BC_STATE_KKV_N,
+    ("K_Kv_test", "n"): _abi.BC_STATE_KKV_N, ("CaN_IS2008", "p"): _abi.BC_STATE_CAN_P,
+    ("Ca_ZH2019_IO", "h"): _abi.BC_STATE_CAIO_H,
 })
 for _cls, (_base, _names) in _abi.MARKOV_STATES.items():
     for _k, _n in enumerate(_names):
@@ -396,7 +397,7 @@ PROBE_CURRENTS = {
     "sKdr_SU2015_DCN": _abi.BC_CUR_SKDR, "Kdr_ZH2019_IO": _abi.BC_CUR_KDRIO, "HCN_SU2015_DCN": _abi.BC_CUR_HCNDCN,
     "HCN_ZH2019_IO": _abi.BC_CUR_HCNIO, "CaT_HP1992": _abi.BC_CUR_CATHP, "CaHT_Re1993": _abi.BC_CUR_CAHTRE,
     "CaL_SU2015_DCN": _abi.BC_CUR_CALDCN, "Kca3p1_MA2020_GoC": _abi.BC_CUR_KCA31, "SK_SU2015_DCN": _abi.BC_CUR_SKDCN,
-    "K_Kv_test": _abi.BC_CUR_KKV,
+    "K_Kv_test": _abi.BC_CUR_KKV, "CaN_IS2008": _abi.BC_CUR_CAN, "Ca_ZH2019_IO": _abi.BC_CUR_CAIO,
 }
 ION_CURRENTS = {"na": _abi.BC_CUR_ION_NA, "k": _abi.BC_CUR_ION_K, "ca": _abi.BC_CUR_ION_CA}
 

@@ -65,6 +65,10 @@ BC_P_EXT_MASK, their parameters after it; conductances in mS/cm^2):
   MA2025_BC and MA2024_PC classes (:452, :533) repeat it
 * ``SK_SU2015_DCN`` -- channel/potassium_calcium.py:189 (g_max 0.01, qdeltat 1)
 * ``K_Kv_test`` -- channel/potassium.py:1239 (g_max 0, V_sh 0, Ra 0.02, Rb 0.006, q 9 mV, v12 25 mV; Q10_n 1)
+* ``CaN_IS2008`` -- channel/calcium.py:108 (g_max 1, E 10 mV, temp 36 degC, q10 1 at 36 degC; current times
+  Ci / (Ci + 0.2 mM), carried by the calcium ion)
+* ``Ca_ZH2019_IO`` / ``_Frozen`` -- channel/calcium.py:4837 (g_max 0.4, E 120 mV, mMidV -61 mV, freeze_m_inf true;
+  the Frozen class pins it)
 
 Same-form classes: Na_TM1991 has Na_Ba2002's Traub-Miles rate functions written
 in terms of V_sh - V (sodium.py:275-289 against :154-170), K_TM1991 has
@@ -179,6 +183,8 @@ CHANNELS: dict[str, dict[str, float]] = {
     "SK_SU2015_DCN": {"g_max": 0.01, "qdeltat": 1.0},
     "K_Kv_test": {"g_max": 0.0, "V_sh": 0.0, "temp": celsius2kelvin(25.0), "Ra": 0.02, "Rb": 0.006, "q": 9.0,
                   "v12": 25.0},
+    "CaN_IS2008": {"E": 10.0, "g_max": 1.0, "temp": T36, "q10": 1.0, "temp_ref": T36},
+    "Ca_ZH2019_IO": {"g_max": 0.4, "E": 120.0, "mMidV": -61.0, "freeze_m_inf": 1.0},
 }
 # extension channels: class -> (BC_X_* bit, record entry of g_max, record entry of E or None)
 _EXT = {
@@ -200,6 +206,8 @@ _EXT = {
     "Kca3p1_MA2020_GoC": (_abi.BC_X_KCA31, _abi.BC_P_KCA31_G, None),
     "SK_SU2015_DCN": (_abi.BC_X_SKDCN, _abi.BC_P_SKDCN_G, None),
     "K_Kv_test": (_abi.BC_X_KKV, _abi.BC_P_KKV_G, None),
+    "CaN_IS2008": (_abi.BC_X_CAN, _abi.BC_P_CAN_G, _abi.BC_P_CAN_E),
+    "Ca_ZH2019_IO": (_abi.BC_X_CAIO, _abi.BC_P_CAIO_G, _abi.BC_P_CAIO_E),
 }
 # cell-type variants with their base class's kinetics; own defaults where they differ
 KINETIC_VARIANTS = {
@@ -234,6 +242,9 @@ for _base, _variants in KINETIC_VARIANTS.items():
 # gnonspec = 0 is built
 CHANNELS["Kv1p5_MA2020_GrC"] = {**CHANNELS["Kv1p5_MA2024_PC"], "gnonspec": 0.0}
 SAME_FORM["Kv1p5_MA2020_GrC"] = "Kv1p5_MA2024_PC"
+# Ca_ZH2019_IO_Frozen (calcium.py) is Ca_ZH2019_IO with freeze_m_inf pinned to True
+CHANNELS["Ca_ZH2019_IO_Frozen"] = dict(CHANNELS["Ca_ZH2019_IO"])
+SAME_FORM["Ca_ZH2019_IO_Frozen"] = "Ca_ZH2019_IO"
 # classes with a parameter record of their own on another class's kernel mechanism
 _SHARED_KERNEL = {"Nav1p1_MA2025_BC": "Nav1p6_MA2020_GoC", "Nav1p1_RI2021_SC": "Nav1p6_MA2020_GoC"}
 # gate temperature factors fixed by a class (not constructor parameters)
@@ -476,6 +487,12 @@ def region_record(mechs, cable: CableProperty) -> tuple[int, np.ndarray]:
                 rec[base + 3] = q10_phi(p["q10_q"], p["temp"], p["temp_ref_q"])
             elif name in ("CaL_SU2015_DCN", "SK_SU2015_DCN") and p["qdeltat"] != 1.0:
                 raise ValueError(f"{decl.class_name}: qdeltat other than 1 is not built.")
+            elif name == "CaN_IS2008":
+                rec[_abi.BC_P_CAN_PHI] = q10_phi(p["q10"], p["temp"], p["temp_ref"])
+            elif name == "Ca_ZH2019_IO":
+                rec[_abi.BC_P_CAIO_MID] = p["mMidV"]
+                frozen = decl.class_name == "Ca_ZH2019_IO_Frozen" or bool(p["freeze_m_inf"])
+                rec[_abi.BC_P_CAIO_FREEZE] = 1.0 if frozen else 0.0
             elif name == "K_Kv_test":
                 if p["q"] == 0.0:
                     raise ValueError(f"{decl.class_name}: q must not be 0.")
@@ -492,7 +509,7 @@ def region_record(mechs, cable: CableProperty) -> tuple[int, np.ndarray]:
             rec[base + 2] = q10_phi(p["q10_p"], p["temp"], p["temp_ref_p"])
             rec[base + 3] = q10_phi(p["q10_q"], p["temp"], p["temp_ref_q"])
     ci_gated = bits & (_abi.BC_M_AHP | _abi.BC_M_KCA22 | _abi.BC_M_KCA11) or \
-        int(rec[_abi.BC_P_EXT_MASK]) & (_abi.BC_X_KCA31 | _abi.BC_X_SKDCN)
+        int(rec[_abi.BC_P_EXT_MASK]) & (_abi.BC_X_KCA31 | _abi.BC_X_SKDCN | _abi.BC_X_CAN)
     if ci_gated and not bits & _abi.BC_M_CADET:
         # AHP and the Kca channels read Ci from the calcium ion; with a fixed Ca ion
         # Ci is the class default.

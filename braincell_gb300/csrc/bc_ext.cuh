@@ -25,8 +25,10 @@
 //   Kca3p1_MA2020_GoC      channel/potassium_calcium.py:299-450
 //   SK_SU2015_DCN          channel/potassium_calcium.py:189-297
 //   K_Kv_test              channel/potassium.py:1239-1372
-// CaT_HP1992 and CaHT_Re1993 carry calcium: their step-start current joins the
-// calcium shell's drive, as CaL's and CaT's do.  Kca3p1 and SK read Ci: the new Ci
+//   CaN_IS2008             channel/calcium.py:108-220
+//   Ca_ZH2019_IO           channel/calcium.py:4837-4979
+// CaT_HP1992, CaHT_Re1993 and CaN_IS2008 (in its own E) carry calcium: their
+// step-start current joins the calcium shell's drive, as CaL's and CaT's do.  Kca3p1 and SK read Ci: the new Ci
 // of a dynamic calcium ion, else the fixed one (BC_P_CA_CI0), as AHP_De1994 does.
 #pragma once
 
@@ -64,7 +66,9 @@ constexpr int kSlotCaldcnH = 91;
 constexpr int kSlotKca31P = 92;
 constexpr int kSlotSkdcnZ = 93;
 constexpr int kSlotKkvN = 94;
-constexpr int kNumSlotsExt = 95;
+constexpr int kSlotCanP = 95;
+constexpr int kSlotCaioH = 96;
+constexpr int kNumSlotsExt = 97;
 
 // x / (1 - e^-x) = 1 / exprel(-x), finite at x = 0 (the reference's
 // _x_over_one_minus_exp_neg_stable, channel/sodium.py:50-55)
@@ -312,6 +316,34 @@ struct KkvRates {
   }
 };
 
+// CaN_IS2008: p, inf / tau (its current carries Ci / (Ci + 0.2 mM)).
+template <typename Real>
+struct CanRates {
+  Real pinf, ptau;
+  __host__ __device__ __forceinline__ explicit CanRates(Real v) {
+    pinf = Real(1) / (Real(1) + aexp(-(v + Real(43)) / Real(5.2)));
+    ptau = Real(2.7) / (aexp(-(v + Real(55)) / Real(15)) + aexp((v + Real(55)) / Real(15))) + Real(1.6);
+  }
+};
+
+// Ca_ZH2019_IO: h, inf / tau; the current's instantaneous m_inf = 1 / t^3 with
+// t = 1 + exp((mMidV - V) / 4.2), and dm_inf/dV = 3 (t - 1) / (4.2 t^4).
+template <typename Real>
+struct CaioRates {
+  Real hinf, htau;
+  __host__ __device__ __forceinline__ explicit CaioRates(Real v) {
+    hinf = Real(1) / (Real(1) + aexp((v + Real(85.5)) / Real(8.6)));
+    htau = Real(40) + Real(30) * (Real(1) / (Real(1) + aexp((v + Real(84)) / Real(7.3)))) * aexp((v + Real(160)) / Real(30));
+  }
+};
+template <typename Real>
+__host__ __device__ __forceinline__ void caio_minf(Real v, Real mid, Real& m, Real& dm) {
+  const Real t = Real(1) + aexp((mid - v) / Real(4.2));
+  const Real t3 = t * t * t;
+  m = Real(1) / t3;
+  dm = Real(3) * (t - Real(1)) / (Real(4.2) * t3 * t);
+}
+
 // The region's BC_X_* bits (an integer stored as a record real).
 template <typename Real>
 __host__ __device__ __forceinline__ uint32_t ext_mask(const Real* P) {
@@ -321,8 +353,8 @@ __host__ __device__ __forceinline__ uint32_t ext_mask(const Real* P) {
 // One extension channel's current at v with the node's stored gates (0 where the
 // region does not carry it); *gv receives -dI/dV when not null.
 template <typename Real>
-__device__ __forceinline__ Real ext_current(const Real* st, int N, const Real* P, uint32_t x, Real v, Real eca,
-                                            int code, Real* gv) {
+__device__ __forceinline__ Real ext_current(const Real* st, int N, const Real* P, uint32_t x, Real v, Real ci,
+                                            Real eca, int code, Real* gv) {
   Real g = Real(0), e = Real(0), gd = Real(0);
   bool has = false;
   switch (code) {
@@ -451,9 +483,26 @@ __device__ __forceinline__ Real ext_current(const Real* st, int N, const Real* P
         e = P[BC_P_EK];
       }
       break;
+    case BC_CUR_CAN:
+      if ((has = (x & BC_X_CAN) != 0)) {
+        g = P[BC_P_CAN_G] * (ci / (ci + Real(0.2))) * st[kSlotCanP * N];
+        e = P[BC_P_CAN_E];
+      }
+      break;
+    case BC_CUR_CAIO:
+      if ((has = (x & BC_X_CAIO) != 0)) {
+        Real m, dm;
+        caio_minf(v, P[BC_P_CAIO_MID], m, dm);
+        const Real gh = P[BC_P_CAIO_G] * st[kSlotCaioH * N];
+        e = P[BC_P_CAIO_E];
+        g = gh * m;
+        // a frozen m_inf stays out of the linearisation, as the reference's stop_gradient does
+        gd = P[BC_P_CAIO_FREEZE] != Real(0) ? g : gh * (m - dm * (e - v));
+      }
+      break;
   }
   if (!has) return Real(0);
-  if (gv) *gv = code == BC_CUR_KV15 ? gd : g;
+  if (gv) *gv = (code == BC_CUR_KV15 || code == BC_CUR_CAIO) ? gd : g;
   return g * (e - v);
 }
 
@@ -543,6 +592,14 @@ __device__ __forceinline__ void ext_gates(Real* st, int N, const Real* P, uint32
     const KkvRates<Real> r(v, P[BC_P_KKV_VSH], P[BC_P_KKV_RA], P[BC_P_KKV_RB], P[BC_P_KKV_Q], P[BC_P_KKV_V12]);
     st[kSlotKkvN * N] = gate_it(st[kSlotKkvN * N], r.ninf, r.ntau, Real(1), dt);
   }
+  if (x & BC_X_CAN) {
+    const CanRates<Real> r(v);
+    st[kSlotCanP * N] = gate_it(st[kSlotCanP * N], r.pinf, r.ptau, P[BC_P_CAN_PHI], dt);
+  }
+  if (x & BC_X_CAIO) {
+    const CaioRates<Real> r(v);
+    st[kSlotCaioH * N] = gate_it(st[kSlotCaioH * N], r.hinf, r.htau, Real(1), dt);
+  }
 }
 
 // A node's extension channels: gates at v (when advancing), then their G and I.
@@ -553,21 +610,22 @@ __device__ __noinline__ void ext_channels(Real* st, int N, const Real* P, Real v
                                           bool advance, Real& G, Real& I) {
   const uint32_t x = ext_mask(P);
   if (advance) ext_gates(st, N, P, x, v, ci, dt);
-  for (int code = BC_CUR_HCN2; code <= BC_CUR_KKV; ++code) {
+  for (int code = BC_CUR_HCN2; code <= BC_CUR_CAIO; ++code) {
     Real g = Real(0);
-    const Real i = ext_current(st, N, P, x, v, eca, code, &g);
+    const Real i = ext_current(st, N, P, x, v, ci, eca, code, &g);
     G += g;
     I += i;
   }
 }
 
 // The calcium current of the extension channels that carry calcium, at the
-// step-start gates, v and E_Ca (their share of the calcium shell's drive).
+// step-start gates, v, Ci and E_Ca (their share of the calcium shell's drive).
 template <typename Real>
-__device__ __noinline__ Real ext_ca_current(const Real* st, int N, const Real* P, Real v, Real eca) {
+__device__ __noinline__ Real ext_ca_current(const Real* st, int N, const Real* P, Real v, Real ci, Real eca) {
   const uint32_t x = ext_mask(P);
-  return ext_current(st, N, P, x, v, eca, BC_CUR_CATHP, (Real*)nullptr) +
-         ext_current(st, N, P, x, v, eca, BC_CUR_CAHTRE, (Real*)nullptr);
+  return ext_current(st, N, P, x, v, ci, eca, BC_CUR_CATHP, (Real*)nullptr) +
+         ext_current(st, N, P, x, v, ci, eca, BC_CUR_CAHTRE, (Real*)nullptr) +
+         ext_current(st, N, P, x, v, ci, eca, BC_CUR_CAN, (Real*)nullptr);
 }
 
 // Steady states of the extension channels' gates at v (HH.reset_state).
@@ -638,6 +696,8 @@ __device__ __forceinline__ void ext_steady(const Real* P, Real* st, int N, Real 
   if (x & BC_X_KKV)
     st[kSlotKkvN * N] =
         KkvRates<Real>(v, P[BC_P_KKV_VSH], P[BC_P_KKV_RA], P[BC_P_KKV_RB], P[BC_P_KKV_Q], P[BC_P_KKV_V12]).ninf;
+  if (x & BC_X_CAN) st[kSlotCanP * N] = CanRates<Real>(v).pinf;
+  if (x & BC_X_CAIO) st[kSlotCaioH * N] = CaioRates<Real>(v).hinf;
 }
 
 }  // namespace bc

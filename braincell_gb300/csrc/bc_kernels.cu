@@ -362,9 +362,11 @@ __device__ __forceinline__ double probe_current(const Real* st, int N, const Rea
         return cerebellar_ca_current(st, N, P, m & BC_M_CAV32, v, eca(), (Real*)nullptr);
       default:
         // extension channels: the record's list exists only where BC_M_EXT is set
-        if (c >= BC_CUR_HCN2 && c <= BC_CUR_KKV && (m & BC_M_EXT))
-          return ext_current(st, N, P, ext_mask(P), v, (c == BC_CUR_CATHP || c == BC_CUR_CAHTRE) ? eca() : Real(0), c,
-                             (Real*)nullptr);
+        if (c >= BC_CUR_HCN2 && c <= BC_CUR_CAIO && (m & BC_M_EXT)) {
+          const Real ci = (m & BC_M_CADET) ? st[kSlotCaHi * N] + st[kSlotCaLo * N] : P[BC_P_CA_CI0];
+          return ext_current(st, N, P, ext_mask(P), v, ci, (c == BC_CUR_CATHP || c == BC_CUR_CAHTRE) ? eca() : Real(0),
+                             c, (Real*)nullptr);
+        }
     }
     return Real(0);
   };
@@ -382,7 +384,7 @@ __device__ __forceinline__ double probe_current(const Real* st, int N, const Rea
              double(cur(BC_CUR_KKV));
     case BC_CUR_ION_CA:
       return double(cur(BC_CUR_CAL)) + double(cur(BC_CUR_CAT)) + double(cur(BC_CUR_CAHVA)) + double(cur(BC_CUR_CAV23)) +
-             double(cur(BC_CUR_CAV32)) + double(cur(BC_CUR_CATHP)) + double(cur(BC_CUR_CAHTRE));
+             double(cur(BC_CUR_CAV32)) + double(cur(BC_CUR_CATHP)) + double(cur(BC_CUR_CAHTRE)) + double(cur(BC_CUR_CAN));
     default:
       return double(cur(code));
   }
@@ -664,7 +666,7 @@ __device__ __forceinline__ void node_mechanisms_loaded(const NodeStates<Real>& s
       if (m & BC_M_CAL) ica += P[BC_P_CAL_G] * calp * calp * calq * (eca - v_old);
       if (m & BC_M_CAT) ica += P[BC_P_CAT_G] * catp * catp * catq * (eca - v_old);
       if (kExtra && (m & kCerebellarCaChannels)) ica += cerebellar_ca_current(st, N, P, m, v_old, eca, (Real*)nullptr);
-      if (kExtra && (m & BC_M_EXT)) ica += ext_ca_current(st, N, P, v_old, eca);
+      if (kExtra && (m & BC_M_EXT)) ica += ext_ca_current(st, N, P, v_old, ci, eca);
       Real drive = ica * Real(kCaDrive) / P[BC_P_CA_D];
       drive = drive > Real(0) ? drive : Real(0);
       const Real tau = P[BC_P_CA_TAU];

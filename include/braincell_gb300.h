@@ -105,7 +105,10 @@ typedef int32_t bc_status;
 #define BC_X_KCA31 (1u << 15)  /* channel/potassium_calcium.py:299 Kca3p1_MA2020_GoC p(V, Ci), E_K */
 #define BC_X_SKDCN (1u << 16)  /* channel/potassium_calcium.py:189 SK_SU2015_DCN z(Ci), E_K  */
 #define BC_X_KKV (1u << 17)    /* channel/potassium.py:1239 K_Kv_test n, E_K                 */
-#define BC_X_ALL 0x3FFFFu
+#define BC_X_CAN (1u << 18)    /* channel/calcium.py:108 CaN_IS2008 p Ci/(Ci + 0.2), own E
+                                  (a calcium-ion current: joins the Ci drive)                 */
+#define BC_X_CAIO (1u << 19)   /* channel/calcium.py:4837 Ca_ZH2019_IO m_inf(V)^1 h, own E   */
+#define BC_X_ALL 0xFFFFFu
 
 /* Per-region parameter record (double[BC_NPARAM]); index names below. */
 #define BC_NPARAM 160
@@ -245,7 +248,14 @@ typedef int32_t bc_status;
 #define BC_P_KKV_RB 133
 #define BC_P_KKV_Q 134      /* mV        */
 #define BC_P_KKV_V12 135    /* mV        */
-/* 136 .. 159: reserved for further extension channels (0) */
+#define BC_P_CAN_G 136
+#define BC_P_CAN_E 137
+#define BC_P_CAN_PHI 138    /* q10^((T - temp_ref) / 10)                            */
+#define BC_P_CAIO_G 139
+#define BC_P_CAIO_E 140
+#define BC_P_CAIO_MID 141   /* mMidV (mV)                                           */
+#define BC_P_CAIO_FREEZE 142 /* 1: m_inf held out of the linearisation (freeze_m_inf) */
+/* 143 .. 159: reserved for further extension channels (0) */
 
 /* ------------------------------------------------------------------ batch spec */
 /*
@@ -411,7 +421,7 @@ const char* bc_last_error(void);
  * HH and calcium channels (BC_M_KV34 .. CAV32, a 96-entry parameter record, state
  * views 51-65, BC_PROBE_CURRENT 128).  0.5.0: extension channels (BC_M_EXT with
  * BC_X_* bits in the record's BC_P_EXT_MASK, a 160-entry parameter record, state
- * views 66-93, current codes 31-48). */
+ * views 66-95, current codes 31-50). */
 #define BC_ABI_VERSION 500
 int32_t bc_version(void);
 /* Fill opts with defaults. */
@@ -541,7 +551,9 @@ bc_status bc_check(bc_plan_t plan, void* stream);
 #define BC_STATE_KCA31_P 91
 #define BC_STATE_SKDCN_Z 92
 #define BC_STATE_KKV_N 93
-#define BC_NSTATE_VIEW 94
+#define BC_STATE_CAN_P 94
+#define BC_STATE_CAIO_H 95
+#define BC_NSTATE_VIEW 96
 /* Current probes (mech/_point.py CurrentProbe, _multi_compartment/probes.py:184-258):
    probe_field = BC_PROBE_CURRENT + one of the codes below records that current
    density (uA/cm^2, outward negative as g (E - V)) after the step.             */
@@ -595,7 +607,9 @@ bc_status bc_check(bc_plan_t plan, void* stream);
 #define BC_CUR_KCA31 46  /* Kca3p1_MA2020_GoC      */
 #define BC_CUR_SKDCN 47  /* SK_SU2015_DCN          */
 #define BC_CUR_KKV 48    /* K_Kv_test              */
-#define BC_NCUR 49
+#define BC_CUR_CAN 49    /* CaN_IS2008             */
+#define BC_CUR_CAIO 50   /* Ca_ZH2019_IO           */
+#define BC_NCUR 51
 bc_status bc_state_download(bc_plan_t plan, int32_t which, double* out /* [n_cv] */, void* stream);
 /* Set the amplitude (nA) of every current-clamp pulse of the batch spec, in spec
  * order (amp_nA[n_pulses]); times and locations are unchanged.  Takes effect from

@@ -147,7 +147,21 @@ CHANNEL_DEFAULTS.update({
     "Kca3p1_MA2020_GoC": dict(g_max=120.0, q10_base=3.0, temp=_c2k(22.0)),  # potassium_calcium.py:299
     "SK_SU2015_DCN": dict(g_max=0.01, qdeltat=1.0),  # potassium_calcium.py:189
     "K_Kv_test": dict(g_max=0.0, V_sh=0.0, temp=_c2k(25.0), Ra=0.02, Rb=0.006, q=9.0, v12=25.0),  # potassium.py:1239
+    "CaN_IS2008": dict(E=10.0, g_max=1.0, temp=_c2k(36.0), q10=1.0, temp_ref=_c2k(36.0)),  # calcium.py:108
+    "Ca_ZH2019_IO": dict(g_max=0.4, E=120.0, mMidV=-61.0, freeze_m_inf=1.0),  # calcium.py:4837
 })
+
+
+def can_modulation(Ci):
+    """CaN_IS2008's current factor Ci / (Ci + 0.2 mM) (calcium.py:108-220)."""
+    return Ci / (Ci + 0.2)
+
+
+def caio_minf(V, mid):
+    """Ca_ZH2019_IO's instantaneous m_inf = 1 / (1 + exp((mMidV - V) / 4.2))^3 and its
+    V-derivative (calcium.py:4837-4979)."""
+    t = 1.0 + np.exp((mid - V) / 4.2)
+    return 1.0 / t ** 3, 3.0 * (t - 1.0) / (4.2 * t ** 4)
 # cell-type variants that run their base class's kinetics, with their own defaults
 # where they differ (each class body is the base's: potassium.py, hyperpolarization_activated.py)
 _VARIANTS = {
@@ -164,6 +178,7 @@ _VARIANTS = {
     # nonspecific current of conductance gnonspec (0 by default; only 0 is restated)
     "Kv1p5_MA2020_GrC": ("Kv1p5_MA2024_PC", {"gnonspec": 0.0}),
     **{v: ("Kca3p1_MA2020_GoC", {}) for v in ("Kca3p1_MA2025_BC", "Kca3p1_MA2024_PC")},
+    "Ca_ZH2019_IO_Frozen": ("Ca_ZH2019_IO", {}),  # freeze_m_inf pinned to True (calcium.py, the subclass)
     **{v: ("Cav3p2_RI2021_SC", {}) for v in ("Cav3p2_MA2025_BC", "Cav3p2_MA2024_PC")},
 }
 
@@ -616,6 +631,12 @@ def rates(name: str, V, p: dict, Ci=None):
         q = p["q"]
         denom = q * (p["Ra"] * _x_over_1mexp(y / q) + p["Rb"] * _x_over_1mexp(-y / q))
         return {"n": ("it", 1.0 / (1.0 + np.exp(-y / q)), 1.0 / denom)}
+    if name == "CaN_IS2008":  # calcium.py:108-220
+        return {"p": ("it", 1.0 / (1.0 + np.exp(-(V + 43.0) / 5.2)),
+                      2.7 / (np.exp(-(V + 55.0) / 15.0) + np.exp((V + 55.0) / 15.0)) + 1.6)}
+    if name == "Ca_ZH2019_IO":  # calcium.py:4837-4979
+        return {"h": ("it", 1.0 / (1.0 + np.exp((V + 85.5) / 8.6)),
+                      40.0 + 30.0 * (1.0 / (1.0 + np.exp((V + 84.0) / 7.3))) * np.exp((V + 160.0) / 30.0))}
     if name in ("KM_RI2021_SC", "KM_MA2020_GoC", "KM_MA2020_GrC"):  # potassium.py:1735-1748, :4553-4567, :5317-5331
         a = 0.0033 * np.exp((V + 30.0) / 40.0)
         b = 0.0033 * np.exp((V + 30.0) / -20.0)
@@ -670,6 +691,8 @@ _GATES = {  # (gate, power, phi-key)
     "Kca3p1_MA2020_GoC": (("p", 1, "phi"),),
     "SK_SU2015_DCN": (("z", 1, "phi"),),
     "K_Kv_test": (("n", 1, "phi"),),
+    "CaN_IS2008": (("p", 1, "phi"),),
+    "Ca_ZH2019_IO": (("h", 1, "phi"),),
 }
 _ION_OF = {"Na_Ba2002": "na", "KDR_Ba2002": "k", "CaL_IS2008": "ca", "CaT_HM1992": "ca",
            "K_Leak": "k", "AHP_De1994": "k", "Na_HH1952": "na", "K_HH1952": "k", "KM_RI2021_SC": "k",
@@ -682,10 +705,10 @@ _ION_OF = {"Na_Ba2002": "na", "KDR_Ba2002": "k", "CaL_IS2008": "ca", "CaT_HM1992
            "Kv3p3_MA2024_PC": "k", "Kv2p2_0010_MA2020_GrC": "k", "Kv1p5_MA2024_PC": "k", "NaF_SU2015_DCN": "na",
            "NaP_SU2015_DCN": "na", "Na_ZH2019_IO": "na", "fKdr_SU2015_DCN": "k", "sKdr_SU2015_DCN": "k",
            "Kdr_ZH2019_IO": "k", "CaT_HP1992": "ca", "CaHT_Re1993": "ca", "Kca3p1_MA2020_GoC": "k",
-           "SK_SU2015_DCN": "k", "K_Kv_test": "k"}
+           "SK_SU2015_DCN": "k", "K_Kv_test": "k", "CaN_IS2008": "ca"}
 # channels with their own reversal potential (HHTypedNeuron root, not an ion)
 _OWN_E = ("HCN_HM1992", "HCN1_MA2020_GoC", "HCN1_MA2024_PC", "HCN2_MA2020_GoC", "HCN_SU2015_DCN", "HCN_ZH2019_IO",
-          "CaL_SU2015_DCN")
+          "CaL_SU2015_DCN", "CaN_IS2008", "Ca_ZH2019_IO")
 
 
 def _resolve(table: dict, decl) -> dict:
@@ -733,6 +756,8 @@ def _resolve(table: dict, decl) -> dict:
     elif name == "HCN2_MA2020_GoC":  # gates q10 3 and the conductance Q10_diff 1.5, at 23 degC
         p["phi"] = 3.0 ** ((p["temp"] - _c2k(23.0)) / 10.0)
         p["gbar_phi"] = 1.5 ** ((p["temp"] - _c2k(23.0)) / 10.0)
+    if name == "CaN_IS2008":  # Gate("p", q10, temp_ref)
+        p["phi"] = p["q10"] ** ((p["temp"] - p["temp_ref"]) / 10.0)
     if p.get("gnonspec", 0.0) != 0.0:
         raise ValueError("Kv1p5_MA2020_GrC's nonspecific current (gnonspec != 0) not restated")
     p.pop("gnonspec", None)
@@ -742,7 +767,7 @@ def _resolve(table: dict, decl) -> dict:
         p["phi"] = 2.7 ** ((p["temp"] - _c2k(22.0)) / 10.0)
     elif name in ("Kv2p2_0010_MA2020_GrC", "Kv1p5_MA2024_PC", "NaF_SU2015_DCN", "NaP_SU2015_DCN", "Na_ZH2019_IO",
                   "fKdr_SU2015_DCN", "sKdr_SU2015_DCN", "Kdr_ZH2019_IO", "HCN_SU2015_DCN", "HCN_ZH2019_IO",
-                  "CaL_SU2015_DCN", "Kca3p1_MA2020_GoC", "SK_SU2015_DCN", "K_Kv_test"):
+                  "CaL_SU2015_DCN", "Kca3p1_MA2020_GoC", "SK_SU2015_DCN", "K_Kv_test", "Ca_ZH2019_IO"):
         p["phi"] = 1.0  # gates without q10 or phi (Kv1p5's Q10 sits in its rates)
     return p
 
@@ -1210,6 +1235,8 @@ class OracleCell:
         return np.where(cd["mask"], nernst, self.E_ca_fixed)
 
     def _gate_product(self, name):
+        if name == "CaN_IS2008":  # p Ci / (Ci + 0.2 mM)
+            return can_modulation(self._ci_for_channels()) * self.gates[(name, "p")]
         if name in ("HCN1_MA2020_GoC", "HCN2_MA2020_GoC"):  # g (o_fast + o_slow) with the conductance's Q10 factor
             return self.chan[name]["gbar_phi"] * (self.gates[(name, "o_fast")] + self.gates[(name, "o_slow")])
         if name in MK.SCHEMES:  # the open occupancy of the raw stored states
@@ -1244,6 +1271,12 @@ class OracleCell:
                 I = I + geff * f * (E - pv)
                 dI = dI + geff * (df * (E - pv) - f)
                 continue
+            if name == "Ca_ZH2019_IO":  # g m_inf(V) h (E - V); a frozen m_inf is out of the derivative
+                m, dm = caio_minf(pv, ch["mMidV"])
+                I = I + geff * m * (E - pv)
+                frozen = ch["freeze_m_inf"] != 0.0
+                dI = dI - geff * m + np.where(frozen, 0.0, geff * dm * (E - pv))
+                continue
             I = I + geff * (E - pv)
             dI = dI - geff
         return I, dI
@@ -1266,6 +1299,8 @@ class OracleCell:
                 E, fac = E_of[_ION_OF[name]], self._gate_product(name)
             if name == "Kv1p5_MA2024_PC":
                 fac = fac * kv15_vfactor(pv)[0]
+            if name == "Ca_ZH2019_IO":
+                fac = fac * caio_minf(pv, ch["mMidV"])[0]
             cur = ch["g_max"] * fac * (E - pv)
             return cur[:, pid] if np.ndim(cur) == 2 else np.full(self.P, float(cur))
 
@@ -1283,7 +1318,8 @@ class OracleCell:
         E_ca = self._E_ca()
         for name in self.chan:
             if _ION_OF.get(name) == "ca":
-                I = I + self.chan[name]["g_max"] * self._gate_product(name) * (E_ca - pv)
+                E = self.chan[name]["E"] if name in _OWN_E else E_ca  # CaN_IS2008 carries calcium in its own E
+                I = I + self.chan[name]["g_max"] * self._gate_product(name) * (E - pv)
         return I
 
     def _clamp_nA(self, clamps, t: float):

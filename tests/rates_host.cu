@@ -73,6 +73,8 @@ extern "C" int bc_test_rates(int which, const double* v, int n, const double* pr
         o[0] = r.ninf; o[1] = r.ntau;
         break;
       }
+      case 40: { const CanRates<double> r(x); o[0] = r.pinf; o[1] = r.ptau; break; }
+      case 41: { const CaioRates<double> r(x); o[0] = r.hinf; o[1] = r.htau; break; }
       default: return -1;
     }
   }

@@ -2,7 +2,8 @@
 Kv3p3_MA2024_PC, Kv2p2_0010_MA2020_GrC, Kv1p5_MA2024_PC (and Kv1p5_MA2020_GrC on its
 kernel), the SU2015 DCN sodium / potassium / HCN / CaL classes, the ZH2019 IO sodium /
 potassium / HCN classes, CaT_HP1992 and CaHT_Re1993 driving a CalciumDetailed shell, the
-calcium-gated Kca3p1 (and its BC / PC classes) and SK_SU2015_DCN, and K_Kv_test.
+calcium-gated Kca3p1 (and its BC / PC classes) and SK_SU2015_DCN, K_Kv_test, CaN_IS2008
+(Ci-modulated, carried by calcium in its own E) and Ca_ZH2019_IO (and its Frozen class).
 
 CPU: the records and their mask, the planner's check of the mask, and the owner
 tables (through the planner tests).  GPU: a DCN-like cell and an IO-like cell
@@ -138,6 +139,30 @@ def _kca_cell(precision="f64"):
     return c
 
 
+def _can_cell(precision="f64", frozen=True):
+    soma = Branch.from_lengths(lengths=[20.0], radii=[10.0, 10.0], type="soma")
+    m = Morphology.from_root(soma, name="soma")
+    m.attach(parent="soma", child_branch=Branch.from_lengths(lengths=[150.0], radii=[1.0, 0.6], type="dendrite"),
+             child_name="d0")
+    c = Cell(m, cv_policy=CVPerBranch(5), precision=precision)
+    c.paint(AllRegion(), CableProperty(), Channel("IL", g_max=0.1, E=-65.0))
+    # Ca_ZH2019_IO with m_inf held out of the linearisation (the Frozen class) or in it
+    io = Channel("Ca_ZH2019_IO_Frozen", g_max=0.5) if frozen else Channel("Ca_ZH2019_IO", g_max=0.5, freeze_m_inf=False)
+    c.paint(branch_in("type", "soma"), Channel("Na_ZH2019_IO"), Channel("Kdr_ZH2019_IO"), io)
+    c.paint(branch_in("type", "dendrite"), Channel("CaHT_Re1993", g_max=0.5), Channel("CaN_IS2008", g_max=0.5),
+            Ion("CalciumDetailed", C_rest=5e-5, tau=20.0, d=0.5, Ci_initializer=5e-5))
+    c.place(RootLocation(0.5), CurrentClamp(delay=2.0, durations=20.0, amplitudes=0.4), StateProbe(name="v"),
+            CurrentProbe(mechanism="Ca_ZH2019_IO_Frozen" if frozen else "Ca_ZH2019_IO", name="i_caio"))
+    c.place(at(1, 0.5), StateProbe(name="v_dend"), MechanismProbe("CalciumDetailed", "Ci", name="ci"),
+            MechanismProbe("CaN_IS2008", "p", name="can_p"), CurrentProbe(mechanism="CaN_IS2008", name="i_can"),
+            CurrentProbe(ion="ca", name="i_ca"))
+    return c
+
+
+def _can_cell_unfrozen(precision="f64"):
+    return _can_cell(precision, frozen=False)
+
+
 def test_kv15_grc_runs_on_the_pc_kernel():
     cable = CableProperty()
     assert catalogue.region_record([Channel("Kv1p5_MA2020_GrC", g_max=0.3)], cable)[1].tolist() == \
@@ -147,8 +172,9 @@ def test_kv15_grc_runs_on_the_pc_kernel():
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("make,n", [(_dcn_cell, 1000), (_io_cell, 800), (_ca_cell, 1000), (_kca_cell, 1000)],
-                         ids=["dcn", "io", "ca", "kca"])
+@pytest.mark.parametrize("make,n", [(_dcn_cell, 1000), (_io_cell, 800), (_ca_cell, 1000), (_kca_cell, 1000),
+                                    (_can_cell, 1000), (_can_cell_unfrozen, 1000)],
+                         ids=["dcn", "io", "ca", "kca", "can", "can_unfrozen"])
 def test_extension_cells_f64_match_oracle(native_lib, cuda_device, make, n):
     from braincell_gb300.runtime import Plan
 
@@ -175,7 +201,8 @@ def test_extension_cells_f64_match_oracle(native_lib, cuda_device, make, n):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("make", [_dcn_cell, _io_cell, _ca_cell, _kca_cell], ids=["dcn", "io", "ca", "kca"])
+@pytest.mark.parametrize("make", [_dcn_cell, _io_cell, _ca_cell, _kca_cell, _can_cell],
+                         ids=["dcn", "io", "ca", "kca", "can"])
 def test_extension_cells_f32_meet_the_bar(native_lib, cuda_device, make):
     from braincell_gb300.runtime import Plan
 

@@ -33,7 +33,7 @@ CASES = {
     31: ("Kdr_ZH2019_IO", ()), 32: ("HCN_SU2015_DCN", ()), 33: ("HCN_ZH2019_IO", ()),
     34: ("CaT_HP1992", ("V_sh",)), 35: ("CaHT_Re1993", ("V_sh",)), 36: ("CaL_SU2015_DCN", ()),
     37: ("Kca3p1_MA2020_GoC", ("Ci",)), 38: ("SK_SU2015_DCN", ("Ci",)),
-    39: ("K_Kv_test", ("V_sh", "Ra", "Rb", "q", "v12")),
+    39: ("K_Kv_test", ("V_sh", "Ra", "Rb", "q", "v12")), 40: ("CaN_IS2008", ()), 41: ("Ca_ZH2019_IO", ()),
 }
 
 
