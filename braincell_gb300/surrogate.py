@@ -434,13 +434,15 @@ class SurrogateRunner:
 
     def __init__(self, descs, model: SurrogateModel | None, *, precision: str = "f32", record_every: int = 0,
                  device: int = 0, plan_kw: dict | None = None, fallback: bool = True, full_cells=None,
-                 full_plan_kw: dict | None = None, fallback_kw: dict | None = None, fallback_priority: int = -1):
+                 full_plan_kw: dict | None = None, fallback_kw: dict | None = None, fallback_priority: int = -1,
+                 tail_split: bool = True):
         """``full_cells``: indices of cells that keep their full morphology for the
         whole run (a mixed population); they run from t = 0 in a plain plan of
         their own (``full_plan_kw``, default: the fallback's launch shape) on a
         stream beside the reduced launches.  ``fallback_kw`` overrides plan options
         of the fallback solves, and ``fallback_priority`` is their streams' priority
-        (-1 high, 0 the reduced launches' own)."""
+        (-1 high, 0 the reduced launches' own).  ``tail_split`` runs the last launch's
+        worth of steps as launches of a half, a quarter and a quarter."""
         from .gru import NPARAM
         from .runtime import Plan
 
@@ -456,6 +458,7 @@ class SurrogateRunner:
         self.fallback = fallback and model is not None
         self.fallback_kw = dict(fallback_kw or {})
         self.fallback_priority = int(fallback_priority)
+        self.tail_split = bool(tail_split)
         n = len(self.descs)
         full = np.zeros(n, bool)
         if full_cells is not None:
@@ -552,6 +555,11 @@ class SurrogateRunner:
         def enqueue():
             nonlocal done
             k = min(lead.pop(0) if lead else spl, n_steps - done)
+            # the last launch's worth of steps in halves down to a quarter launch, so
+            # that an exit near the end is read (and its full solve started) sooner
+            r = n_steps - done
+            if self.tail_split and not lead and r <= spl:
+                k = r if r <= max(1, spl // 4) else max(max(1, spl // 4), r // 2)
             plan.run(k, dt, stream=sid, check=False)
             done += k
             ev = torch.cuda.Event(enable_timing=True)
