@@ -74,7 +74,8 @@ BC_X_SKDCN = 1 << 16
 BC_X_KKV = 1 << 17
 BC_X_CAN = 1 << 18
 BC_X_CAIO = 1 << 19
-BC_X_ALL = 0xFFFFF
+BC_X_NAVGRC = 1 << 20
+BC_X_ALL = 0x1FFFFF
 
 BC_NPARAM = 160
 BC_P_INVCM = 0
@@ -219,6 +220,8 @@ BC_P_CAIO_G = 139
 BC_P_CAIO_E = 140
 BC_P_CAIO_MID = 141
 BC_P_CAIO_FREEZE = 142
+BC_P_NAVGRC_G = 143
+BC_P_NAVGRC_PHI = 144
 
 BC_ABI_VERSION = 500
 
@@ -286,7 +289,8 @@ BC_CUR_SKDCN = 47
 BC_CUR_KKV = 48
 BC_CUR_CAN = 49
 BC_CUR_CAIO = 50
-BC_NCUR = 51
+BC_CUR_NAVGRC = 51
+BC_NCUR = 52
 
 BC_STATE_V = 0
 BC_STATE_NA_P = 1
@@ -362,13 +366,16 @@ BC_STATE_SKDCN_Z = 92
 BC_STATE_KKV_N = 93
 BC_STATE_CAN_P = 94
 BC_STATE_CAIO_H = 95
-BC_NSTATE_VIEW = 96
+BC_STATE_NAVGRC_C1 = 96
+BC_STATE_NAVGRC_O = 106
+BC_NSTATE_VIEW = 108
 # the independent states of each Markov scheme, in view order (first appearance in
 # the scheme's transition list, the dependent state left out)
 MARKOV_STATES = {
     "Nav1p6_MA2020_GoC": (BC_STATE_NAV16_C1, ("C1", "C2", "C3", "C4", "C5", "I1", "I2", "I3", "I4", "I5", "O", "B")),
     "Kca2p2_MA2020_GoC": (BC_STATE_KCA22_C2, ("C2", "C3", "C4", "O1", "O2")),
     "Kca1p1_MA2020_GoC": (BC_STATE_KCA11_C1, ("C1", "C2", "C3", "C4", "O0", "O1", "O2", "O3", "O4")),
+    "Nav_MA2020_GrC": (BC_STATE_NAVGRC_C1, ("C1", "C2", "C3", "C4", "C5", "I1", "I2", "I3", "I4", "I5", "O", "OB")),
 }
 BC_NOALLOC_MAX_CV = 262144
 

@@ -398,6 +398,7 @@ PROBE_CURRENTS = {
     "HCN_ZH2019_IO": _abi.BC_CUR_HCNIO, "CaT_HP1992": _abi.BC_CUR_CATHP, "CaHT_Re1993": _abi.BC_CUR_CAHTRE,
     "CaL_SU2015_DCN": _abi.BC_CUR_CALDCN, "Kca3p1_MA2020_GoC": _abi.BC_CUR_KCA31, "SK_SU2015_DCN": _abi.BC_CUR_SKDCN,
     "K_Kv_test": _abi.BC_CUR_KKV, "CaN_IS2008": _abi.BC_CUR_CAN, "Ca_ZH2019_IO": _abi.BC_CUR_CAIO,
+    "Nav_MA2020_GrC": _abi.BC_CUR_NAVGRC,
 }
 ION_CURRENTS = {"na": _abi.BC_CUR_ION_NA, "k": _abi.BC_CUR_ION_K, "ca": _abi.BC_CUR_ION_CA}
 

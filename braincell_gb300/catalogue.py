@@ -67,6 +67,8 @@ BC_P_EXT_MASK, their parameters after it; conductances in mS/cm^2):
 * ``K_Kv_test`` -- channel/potassium.py:1239 (g_max 0, V_sh 0, Ra 0.02, Rb 0.006, q 9 mV, v12 25 mV; Q10_n 1)
 * ``CaN_IS2008`` -- channel/calcium.py:108 (g_max 1, E 10 mV, temp 36 degC, q10 1 at 36 degC; current times
   Ci / (Ci + 0.2 mM), carried by the calcium ion)
+* ``Nav_MA2020_GrC`` -- channel/sodium.py:1427 (g_max 13, temp 32 degC; phi 3^((T - 20 degC) / 10)): a Markov
+  scheme on the Nav1.6 graph with its own rate constants
 * ``Ca_ZH2019_IO`` / ``_Frozen`` -- channel/calcium.py:4837 (g_max 0.4, E 120 mV, mMidV -61 mV, freeze_m_inf true;
   the Frozen class pins it)
 
@@ -185,6 +187,7 @@ CHANNELS: dict[str, dict[str, float]] = {
                   "v12": 25.0},
     "CaN_IS2008": {"E": 10.0, "g_max": 1.0, "temp": T36, "q10": 1.0, "temp_ref": T36},
     "Ca_ZH2019_IO": {"g_max": 0.4, "E": 120.0, "mMidV": -61.0, "freeze_m_inf": 1.0},
+    "Nav_MA2020_GrC": {"g_max": 13.0, "temp": celsius2kelvin(32.0)},
 }
 # extension channels: class -> (BC_X_* bit, record entry of g_max, record entry of E or None)
 _EXT = {
@@ -208,6 +211,7 @@ _EXT = {
     "K_Kv_test": (_abi.BC_X_KKV, _abi.BC_P_KKV_G, None),
     "CaN_IS2008": (_abi.BC_X_CAN, _abi.BC_P_CAN_G, _abi.BC_P_CAN_E),
     "Ca_ZH2019_IO": (_abi.BC_X_CAIO, _abi.BC_P_CAIO_G, _abi.BC_P_CAIO_E),
+    "Nav_MA2020_GrC": (_abi.BC_X_NAVGRC, _abi.BC_P_NAVGRC_G, None),
 }
 # cell-type variants with their base class's kinetics; own defaults where they differ
 KINETIC_VARIANTS = {
@@ -489,6 +493,8 @@ def region_record(mechs, cable: CableProperty) -> tuple[int, np.ndarray]:
                 raise ValueError(f"{decl.class_name}: qdeltat other than 1 is not built.")
             elif name == "CaN_IS2008":
                 rec[_abi.BC_P_CAN_PHI] = q10_phi(p["q10"], p["temp"], p["temp_ref"])
+            elif name == "Nav_MA2020_GrC":  # phi = 3^((T - 20 degC) / 10) (sodium.py, __init__)
+                rec[_abi.BC_P_NAVGRC_PHI] = q10_phi(3.0, p["temp"], celsius2kelvin(20.0))
             elif name == "Ca_ZH2019_IO":
                 rec[_abi.BC_P_CAIO_MID] = p["mMidV"]
                 frozen = decl.class_name == "Ca_ZH2019_IO_Frozen" or bool(p["freeze_m_inf"])

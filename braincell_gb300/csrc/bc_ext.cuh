@@ -27,6 +27,7 @@
 //   K_Kv_test              channel/potassium.py:1239-1372
 //   CaN_IS2008             channel/calcium.py:108-220
 //   Ca_ZH2019_IO           channel/calcium.py:4837-4979
+//   Nav_MA2020_GrC         channel/sodium.py:1427-1666 (on the Markov solver of bc_mech.cuh)
 // CaT_HP1992, CaHT_Re1993 and CaN_IS2008 (in its own E) carry calcium: their
 // step-start current joins the calcium shell's drive, as CaL's and CaT's do.  Kca3p1 and SK read Ci: the new Ci
 // of a dynamic calcium ion, else the fixed one (BC_P_CA_CI0), as AHP_De1994 does.
@@ -68,7 +69,8 @@ constexpr int kSlotSkdcnZ = 93;
 constexpr int kSlotKkvN = 94;
 constexpr int kSlotCanP = 95;
 constexpr int kSlotCaioH = 96;
-constexpr int kNumSlotsExt = 97;
+constexpr int kSlotNavGrc = 97;  // C1..C5, I1..I5, O, OB in 97..108 (I6 dependent)
+constexpr int kNumSlotsExt = 109;
 
 // x / (1 - e^-x) = 1 / exprel(-x), finite at x = 0 (the reference's
 // _x_over_one_minus_exp_neg_stable, channel/sodium.py:50-55)
@@ -344,6 +346,48 @@ __host__ __device__ __forceinline__ void caio_minf(Real v, Real mid, Real& m, Re
   dm = Real(3) * (t - Real(1)) / (Real(4.2) * t3 * t);
 }
 
+// Nav_MA2020_GrC: the Nav1.6 transition graph (the same 13 states and 17 pairs, in
+// the pair order of the Nav1.6 tables) with the GrC class's rates: alfa = A_a
+// e^(V / 13.99), beta = A_b e^(-V / 13.99), teta = A_t e^(-V / 25), gamma, delta,
+// epsilon, Con, Coff, Oon, Ooff constants, all times phi; a = (Oon / Con)^(1/4),
+// b = (Ooff / Coff)^(1/4); the C->C rates n1..n4 alfa (back n4..n1 beta).
+__device__ __forceinline__ MarkovGraph navgrc_graph() {
+  return MarkovGraph{13, 17, 12, kSlotNavGrc, kNav16Src, kNav16Dst};
+}
+template <typename Real>
+__device__ __forceinline__ void navgrc_rates(Real v, Real phi, Real* kf, Real* kb) {
+  const Real alfa = phi * Real(353.91) * aexp(v / Real(13.99));
+  const Real beta = phi * Real(1.272) * aexp(-v / Real(13.99));
+  const Real teta = phi * Real(0.0201) * aexp(-v / Real(25));
+  const Real gamma = phi * Real(150), delta = phi * Real(40), eps = phi * Real(1.75);
+  const Real con = phi * Real(0.005), coff = phi * Real(0.5), oon = phi * Real(0.75), ooff = phi * Real(0.005);
+  const Real a = dpow(oon / con, Real(0.25)), b = dpow(ooff / coff, Real(0.25));
+  const Real n[4] = {Real(5.422), Real(3.279), Real(1.83), Real(0.738)};
+  // pairs (Nav1.6 order): C1C2 C2C3 C3C4 C4C5 C1I1 I1I2 C2I2 I2I3 C3I3 I3I4 C4I4 I4I5 C5I5 C5O OB I5I6 OI6
+  const int cc[4] = {0, 1, 2, 3}, ii[4] = {5, 7, 9, 11}, ci[5] = {4, 6, 8, 10, 12};
+  Real ak = Real(1), bk = Real(1);
+  for (int k = 0; k < 4; ++k) {
+    kf[cc[k]] = n[k] * alfa;
+    kb[cc[k]] = n[3 - k] * beta;
+    kf[ii[k]] = n[k] * alfa * a;
+    kb[ii[k]] = n[3 - k] * beta * b;
+  }
+  for (int k = 0; k < 5; ++k) {
+    kf[ci[k]] = con * ak;
+    kb[ci[k]] = coff * bk;
+    ak *= a;
+    bk *= b;
+  }
+  kf[13] = gamma;  // C5 -> O
+  kb[13] = delta;
+  kf[14] = eps;    // O -> OB
+  kb[14] = teta;
+  kf[15] = gamma;  // I5 -> I6
+  kb[15] = delta;
+  kf[16] = oon;    // O -> I6
+  kb[16] = ooff;
+}
+
 // The region's BC_X_* bits (an integer stored as a record real).
 template <typename Real>
 __host__ __device__ __forceinline__ uint32_t ext_mask(const Real* P) {
@@ -489,6 +533,12 @@ __device__ __forceinline__ Real ext_current(const Real* st, int N, const Real* P
         e = P[BC_P_CAN_E];
       }
       break;
+    case BC_CUR_NAVGRC:
+      if ((has = (x & BC_X_NAVGRC) != 0)) {
+        g = P[BC_P_NAVGRC_G] * st[(kSlotNavGrc + 10) * N];  // O
+        e = P[BC_P_ENA];
+      }
+      break;
     case BC_CUR_CAIO:
       if ((has = (x & BC_X_CAIO) != 0)) {
         Real m, dm;
@@ -600,6 +650,12 @@ __device__ __forceinline__ void ext_gates(Real* st, int N, const Real* P, uint32
     const CaioRates<Real> r(v);
     st[kSlotCaioH * N] = gate_it(st[kSlotCaioH * N], r.hinf, r.htau, Real(1), dt);
   }
+  // the Markov scheme after the gates, by one linearised backward-Euler step
+  if (x & BC_X_NAVGRC) {
+    Real kf[17], kb[17];
+    navgrc_rates(v, P[BC_P_NAVGRC_PHI], kf, kb);
+    markov_advance(st, N, navgrc_graph(), kf, kb, dt);
+  }
 }
 
 // A node's extension channels: gates at v (when advancing), then their G and I.
@@ -610,7 +666,7 @@ __device__ __noinline__ void ext_channels(Real* st, int N, const Real* P, Real v
                                           bool advance, Real& G, Real& I) {
   const uint32_t x = ext_mask(P);
   if (advance) ext_gates(st, N, P, x, v, ci, dt);
-  for (int code = BC_CUR_HCN2; code <= BC_CUR_CAIO; ++code) {
+  for (int code = BC_CUR_HCN2; code <= BC_CUR_NAVGRC; ++code) {
     Real g = Real(0);
     const Real i = ext_current(st, N, P, x, v, ci, eca, code, &g);
     G += g;
@@ -698,6 +754,11 @@ __device__ __forceinline__ void ext_steady(const Real* P, Real* st, int N, Real 
         KkvRates<Real>(v, P[BC_P_KKV_VSH], P[BC_P_KKV_RA], P[BC_P_KKV_RB], P[BC_P_KKV_Q], P[BC_P_KKV_V12]).ninf;
   if (x & BC_X_CAN) st[kSlotCanP * N] = CanRates<Real>(v).pinf;
   if (x & BC_X_CAIO) st[kSlotCaioH * N] = CaioRates<Real>(v).hinf;
+  if (x & BC_X_NAVGRC) {  // the stationary distribution (reset_steady_state)
+    Real kf[17], kb[17];
+    navgrc_rates(v, P[BC_P_NAVGRC_PHI], kf, kb);
+    markov_steady(st, N, navgrc_graph(), kf, kb);
+  }
 }
 
 }  // namespace bc

@@ -362,7 +362,7 @@ __device__ __forceinline__ double probe_current(const Real* st, int N, const Rea
         return cerebellar_ca_current(st, N, P, m & BC_M_CAV32, v, eca(), (Real*)nullptr);
       default:
         // extension channels: the record's list exists only where BC_M_EXT is set
-        if (c >= BC_CUR_HCN2 && c <= BC_CUR_CAIO && (m & BC_M_EXT)) {
+        if (c >= BC_CUR_HCN2 && c <= BC_CUR_NAVGRC && (m & BC_M_EXT)) {
           const Real ci = (m & BC_M_CADET) ? st[kSlotCaHi * N] + st[kSlotCaLo * N] : P[BC_P_CA_CI0];
           return ext_current(st, N, P, ext_mask(P), v, ci, (c == BC_CUR_CATHP || c == BC_CUR_CAHTRE) ? eca() : Real(0),
                              c, (Real*)nullptr);
@@ -373,7 +373,7 @@ __device__ __forceinline__ double probe_current(const Real* st, int N, const Rea
   switch (code) {
     case BC_CUR_ION_NA:
       return double(cur(BC_CUR_NA)) + double(cur(BC_CUR_NAHH)) + double(cur(BC_CUR_NAV16)) + double(cur(BC_CUR_NAF)) +
-             double(cur(BC_CUR_NAP)) + double(cur(BC_CUR_NAIO));
+             double(cur(BC_CUR_NAP)) + double(cur(BC_CUR_NAIO)) + double(cur(BC_CUR_NAVGRC));
     case BC_CUR_ION_K:
       return double(cur(BC_CUR_KDR)) + double(cur(BC_CUR_KLEAK)) + double(cur(BC_CUR_AHP)) + double(cur(BC_CUR_KHH)) +
              double(cur(BC_CUR_KM)) + double(cur(BC_CUR_KA1)) + double(cur(BC_CUR_KA2)) + double(cur(BC_CUR_KK2A)) +

@@ -30,7 +30,9 @@ Restated from the reference:
   - ``Kca2p2_MA2020_GoC`` (``channel/potassium_calcium.py:613-790``): 6 states,
     ``C1`` dependent, current g (O1 + O2) (E_K - V), calcium-bound rates;
   - ``Kca1p1_MA2020_GoC`` (``channel/potassium_calcium.py:1107-1353``): 10 states,
-    ``C0`` dependent, current g (O0 + ... + O4) (E_K - V).
+    ``C0`` dependent, current g (O0 + ... + O4) (E_K - V);
+  - ``Nav_MA2020_GrC`` (``channel/sodium.py:1427-1666``): the Nav1.6 graph's 13 states
+    (``OB`` for B), ``I6`` dependent, its own rate constants, current g O (E_Na - V).
 
 Units: mV, ms, mM, K.
 """
@@ -106,6 +108,35 @@ def _nav16_rates(V, Ci, p):
     return r
 
 
+def _navgrc_rates(V, Ci, p):
+    """channel/sodium.py:1427-1666 (Nav_MA2020_GrC): alfa / beta / teta exponentials and
+    constant gamma, delta, epsilon, Con, Coff, Oon, Ooff, all times phi; the C and I
+    chains carry n1..n4 (back n4..n1)."""
+    phi = p["phi"]
+    one = np.ones_like(V)
+    alfa = phi * 353.91 * np.exp(V / 13.99)
+    beta = phi * 1.272 * np.exp(-V / 13.99)
+    teta = phi * 0.0201 * np.exp(-V / 25.0)
+    gamma, delta, eps = phi * 150.0 * one, phi * 40.0 * one, phi * 1.75 * one
+    Con, Coff, Oon, Ooff = phi * 0.005, phi * 0.5, phi * 0.75, phi * 0.005
+    a, b = (Oon / Con) ** 0.25, (Ooff / Coff) ** 0.25
+    n = (5.422, 3.279, 1.83, 0.738)
+    r = {}
+    for k in range(4):
+        r[f"f0{k + 1}"] = n[k] * alfa
+        r[f"b0{k + 1}"] = n[3 - k] * beta
+        r[f"f1{k + 1}"] = n[k] * alfa * a
+        r[f"b1{k + 1}"] = n[3 - k] * beta * b
+    for k in range(1, 6):
+        r[f"fi{k}"] = Con * a ** (k - 1) * one
+        r[f"bi{k}"] = Coff * b ** (k - 1) * one
+    r["f0O"], r["b0O"] = gamma, delta
+    r["fip"], r["bip"] = eps, teta
+    r["f1n"], r["b1n"] = gamma, delta
+    r["fin"], r["bin"] = Oon * one, Ooff * one
+    return r
+
+
 def _kca22_rates(V, Ci, p):
     """channel/potassium_calcium.py:760-790 with the constants of :740-753."""
     phi, diff = p["phi"], p["diff"]
@@ -177,6 +208,15 @@ SCHEMES = {
          ("C1", "O1", "f1", "b1"), ("C2", "O2", "f2", "b2"), ("C3", "O3", "f3", "b3"),
          ("C4", "O4", "f4", "b4")),  # potassium_calcium.py:1213-1228
         "C0", ("O0", "O1", "O2", "O3", "O4"), "k", _kca11_rates),
+    "Nav_MA2020_GrC": MarkovScheme(
+        "Nav_MA2020_GrC",
+        (("C1", "C2", "f01", "b01"), ("C2", "C3", "f02", "b02"), ("C3", "C4", "f03", "b03"),
+         ("C4", "C5", "f04", "b04"), ("C5", "O", "f0O", "b0O"), ("O", "OB", "fip", "bip"),
+         ("I1", "I2", "f11", "b11"), ("I2", "I3", "f12", "b12"), ("I3", "I4", "f13", "b13"),
+         ("I4", "I5", "f14", "b14"), ("C1", "I1", "fi1", "bi1"), ("C2", "I2", "fi2", "bi2"),
+         ("C3", "I3", "fi3", "bi3"), ("C4", "I4", "fi4", "bi4"), ("C5", "I5", "fi5", "bi5"),
+         ("O", "I6", "fin", "bin"), ("I5", "I6", "f1n", "b1n")),  # sodium.py:1427-1666 (pairs)
+        "I6", ("O",), "na", _navgrc_rates),
 }
 
 _T22 = 273.15 + 22.0
@@ -188,6 +228,7 @@ MARKOV_DEFAULTS = {
     "Nav1p1_RI2021_SC": dict(g_max=8.0, temp=_T22, Oon=2.3, epsilon=1e-12, gateCurrent=0.0),
     "Kca2p2_MA2020_GoC": dict(g_max=38.0, q10_base=3.0, diff=3.0, temp=_T22),
     "Kca1p1_MA2020_GoC": dict(g_max=10.0, q10_base=3.0, temp=_T22),
+    "Nav_MA2020_GrC": dict(g_max=13.0, temp=273.15 + 32.0),  # sodium.py:1427 (__init__)
 }
 
 
@@ -198,6 +239,8 @@ def scheme_params(name: str, p: dict) -> dict:
     out = dict(p)
     if name == "Nav1p6_MA2020_GoC":
         out["phi"] = 3.0 ** ((p["temp"] - _T22) / 10.0)
+    elif name == "Nav_MA2020_GrC":  # phi = 3^((T - 20 degC) / 10)
+        out["phi"] = 3.0 ** ((p["temp"] - (273.15 + 20.0)) / 10.0)
     elif name.startswith("Nav1p1"):  # sodium.py:1212: phi = 2.7^((T - 22 degC) / 10)
         if p.get("gateCurrent", 0.0) != 0.0:
             raise ValueError("Nav1p1 gating current not restated")

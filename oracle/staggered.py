@@ -705,7 +705,7 @@ _ION_OF = {"Na_Ba2002": "na", "KDR_Ba2002": "k", "CaL_IS2008": "ca", "CaT_HM1992
            "Kv3p3_MA2024_PC": "k", "Kv2p2_0010_MA2020_GrC": "k", "Kv1p5_MA2024_PC": "k", "NaF_SU2015_DCN": "na",
            "NaP_SU2015_DCN": "na", "Na_ZH2019_IO": "na", "fKdr_SU2015_DCN": "k", "sKdr_SU2015_DCN": "k",
            "Kdr_ZH2019_IO": "k", "CaT_HP1992": "ca", "CaHT_Re1993": "ca", "Kca3p1_MA2020_GoC": "k",
-           "SK_SU2015_DCN": "k", "K_Kv_test": "k", "CaN_IS2008": "ca"}
+           "SK_SU2015_DCN": "k", "K_Kv_test": "k", "CaN_IS2008": "ca", "Nav_MA2020_GrC": "na"}
 # channels with their own reversal potential (HHTypedNeuron root, not an ion)
 _OWN_E = ("HCN_HM1992", "HCN1_MA2020_GoC", "HCN1_MA2024_PC", "HCN2_MA2020_GoC", "HCN_SU2015_DCN", "HCN_ZH2019_IO",
           "CaL_SU2015_DCN", "CaN_IS2008", "Ca_ZH2019_IO")

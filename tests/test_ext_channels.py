@@ -3,7 +3,8 @@ Kv3p3_MA2024_PC, Kv2p2_0010_MA2020_GrC, Kv1p5_MA2024_PC (and Kv1p5_MA2020_GrC on
 kernel), the SU2015 DCN sodium / potassium / HCN / CaL classes, the ZH2019 IO sodium /
 potassium / HCN classes, CaT_HP1992 and CaHT_Re1993 driving a CalciumDetailed shell, the
 calcium-gated Kca3p1 (and its BC / PC classes) and SK_SU2015_DCN, K_Kv_test, CaN_IS2008
-(Ci-modulated, carried by calcium in its own E) and Ca_ZH2019_IO (and its Frozen class).
+(Ci-modulated, carried by calcium in its own E), Ca_ZH2019_IO (and its Frozen class), and
+the Markov scheme Nav_MA2020_GrC.
 
 CPU: the records and their mask, the planner's check of the mask, and the owner
 tables (through the planner tests).  GPU: a DCN-like cell and an IO-like cell
@@ -163,6 +164,18 @@ def _can_cell_unfrozen(precision="f64"):
     return _can_cell(precision, frozen=False)
 
 
+def _grc_cell(precision="f64"):
+    soma = Branch.from_lengths(lengths=[20.0], radii=[10.0, 10.0], type="soma")
+    c = Cell(Morphology.from_root(soma, name="soma"), cv_policy=CVPerBranch(), precision=precision)
+    c.paint(AllRegion(), CableProperty(), Channel("IL", g_max=0.1, E=-65.0), Channel("Nav_MA2020_GrC", g_max=40.0),
+            Channel("Kdr_ZH2019_IO", g_max=18.0), Channel("Kv2p2_0010_MA2020_GrC", g_max=1.0))
+    c.place(RootLocation(0.5), CurrentClamp(delay=2.0, durations=15.0, amplitudes=0.4), StateProbe(name="v"),
+            MechanismProbe("Nav_MA2020_GrC", "O", name="nav_o"), MechanismProbe("Nav_MA2020_GrC", "OB", name="nav_ob"),
+            MechanismProbe("Nav_MA2020_GrC", "I3", name="nav_i3"), CurrentProbe(mechanism="Nav_MA2020_GrC", name="i_nav"),
+            CurrentProbe(ion="na", name="i_na"))
+    return c
+
+
 def test_kv15_grc_runs_on_the_pc_kernel():
     cable = CableProperty()
     assert catalogue.region_record([Channel("Kv1p5_MA2020_GrC", g_max=0.3)], cable)[1].tolist() == \
@@ -173,8 +186,8 @@ def test_kv15_grc_runs_on_the_pc_kernel():
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("make,n", [(_dcn_cell, 1000), (_io_cell, 800), (_ca_cell, 1000), (_kca_cell, 1000),
-                                    (_can_cell, 1000), (_can_cell_unfrozen, 1000)],
-                         ids=["dcn", "io", "ca", "kca", "can", "can_unfrozen"])
+                                    (_can_cell, 1000), (_can_cell_unfrozen, 1000), (_grc_cell, 800)],
+                         ids=["dcn", "io", "ca", "kca", "can", "can_unfrozen", "grc"])
 def test_extension_cells_f64_match_oracle(native_lib, cuda_device, make, n):
     from braincell_gb300.runtime import Plan
 
@@ -201,8 +214,8 @@ def test_extension_cells_f64_match_oracle(native_lib, cuda_device, make, n):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("make", [_dcn_cell, _io_cell, _ca_cell, _kca_cell, _can_cell],
-                         ids=["dcn", "io", "ca", "kca", "can"])
+@pytest.mark.parametrize("make", [_dcn_cell, _io_cell, _ca_cell, _kca_cell, _can_cell, _grc_cell],
+                         ids=["dcn", "io", "ca", "kca", "can", "grc"])
 def test_extension_cells_f32_meet_the_bar(native_lib, cuda_device, make):
     from braincell_gb300.runtime import Plan
 

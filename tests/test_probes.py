@@ -57,7 +57,7 @@ def test_mechanism_probe_errors(native_lib):
     b.probe_field[0] = _abi.BC_STATE_CAL_P  # the soma has no CaL
     with pytest.raises(BCError, match="no such mechanism"):
         Plan(b, dry_run=True)
-    b.probe_field[0] = 99
+    b.probe_field[0] = _abi.BC_NSTATE_VIEW  # the first code past the state views
     with pytest.raises(BCError, match="probe_field"):
         Plan(b, dry_run=True)
 
