@@ -75,7 +75,8 @@ BC_X_KKV = 1 << 17
 BC_X_CAN = 1 << 18
 BC_X_CAIO = 1 << 19
 BC_X_NAVGRC = 1 << 20
-BC_X_ALL = 0x1FFFFF
+BC_X_CAV31 = 1 << 21
+BC_X_ALL = 0x3FFFFF
 
 BC_NPARAM = 160
 BC_P_INVCM = 0
@@ -222,6 +223,10 @@ BC_P_CAIO_MID = 141
 BC_P_CAIO_FREEZE = 142
 BC_P_NAVGRC_G = 143
 BC_P_NAVGRC_PHI = 144
+BC_P_CAV31_G = 145
+BC_P_CAV31_QT = 146
+BC_P_CAV31_TGHK = 147
+BC_P_CAV31_FREEZE = 148
 
 BC_ABI_VERSION = 500
 
@@ -290,7 +295,8 @@ BC_CUR_KKV = 48
 BC_CUR_CAN = 49
 BC_CUR_CAIO = 50
 BC_CUR_NAVGRC = 51
-BC_NCUR = 52
+BC_CUR_CAV31 = 52
+BC_NCUR = 53
 
 BC_STATE_V = 0
 BC_STATE_NA_P = 1
@@ -368,7 +374,9 @@ BC_STATE_CAN_P = 94
 BC_STATE_CAIO_H = 95
 BC_STATE_NAVGRC_C1 = 96
 BC_STATE_NAVGRC_O = 106
-BC_NSTATE_VIEW = 108
+BC_STATE_CAV31_P = 108
+BC_STATE_CAV31_Q = 109
+BC_NSTATE_VIEW = 110
 # the independent states of each Markov scheme, in view order (first appearance in
 # the scheme's transition list, the dependent state left out)
 MARKOV_STATES = {
@@ -450,6 +458,8 @@ STATE_NAMES = {
     "KKv_n": BC_STATE_KKV_N,
     "CaN_p": BC_STATE_CAN_P,
     "CaIO_h": BC_STATE_CAIO_H,
+    "Cav3p1_p": BC_STATE_CAV31_P,
+    "Cav3p1_q": BC_STATE_CAV31_Q,
 }
 for _cls, (_base, _names) in MARKOV_STATES.items():
     for _k, _n in enumerate(_names):

@@ -67,6 +67,9 @@ BC_P_EXT_MASK, their parameters after it; conductances in mS/cm^2):
 * ``K_Kv_test`` -- channel/potassium.py:1239 (g_max 0, V_sh 0, Ra 0.02, Rb 0.006, q 9 mV, v12 25 mV; Q10_n 1)
 * ``CaN_IS2008`` -- channel/calcium.py:108 (g_max 1, E 10 mV, temp 36 degC, q10 1 at 36 degC; current times
   Ci / (Ci + 0.2 mM), carried by the calcium ion)
+* ``Cav3p1_MA2020_GoC`` -- channel/calcium.py:1972 (permeability g_max 2.5e-4 cm/s, temp 22 degC, q10 3 at 37 degC
+  dividing the time constants; GHK drive at temp + 0.04 K); Cav3p1_MA2024_PC repeats it, and the two _Frozen classes
+  hold the drive out of the linearisation
 * ``Nav_MA2020_GrC`` -- channel/sodium.py:1427 (g_max 13, temp 32 degC; phi 3^((T - 20 degC) / 10)): a Markov
   scheme on the Nav1.6 graph with its own rate constants
 * ``Ca_ZH2019_IO`` / ``_Frozen`` -- channel/calcium.py:4837 (g_max 0.4, E 120 mV, mMidV -61 mV, freeze_m_inf true;
@@ -188,6 +191,8 @@ CHANNELS: dict[str, dict[str, float]] = {
     "CaN_IS2008": {"E": 10.0, "g_max": 1.0, "temp": T36, "q10": 1.0, "temp_ref": T36},
     "Ca_ZH2019_IO": {"g_max": 0.4, "E": 120.0, "mMidV": -61.0, "freeze_m_inf": 1.0},
     "Nav_MA2020_GrC": {"g_max": 13.0, "temp": celsius2kelvin(32.0)},
+    # a permeability in cm/s (calcium.py:1972: 2.5e-4 cm/s)
+    "Cav3p1_MA2020_GoC": {"g_max": 2.5e-4, "V_sh": 0.0, "temp": T22, "q10": 3.0, "temp_ref": celsius2kelvin(37.0)},
 }
 # extension channels: class -> (BC_X_* bit, record entry of g_max, record entry of E or None)
 _EXT = {
@@ -212,7 +217,11 @@ _EXT = {
     "CaN_IS2008": (_abi.BC_X_CAN, _abi.BC_P_CAN_G, _abi.BC_P_CAN_E),
     "Ca_ZH2019_IO": (_abi.BC_X_CAIO, _abi.BC_P_CAIO_G, _abi.BC_P_CAIO_E),
     "Nav_MA2020_GrC": (_abi.BC_X_NAVGRC, _abi.BC_P_NAVGRC_G, None),
+    "Cav3p1_MA2020_GoC": (_abi.BC_X_CAV31, _abi.BC_P_CAV31_G, None),
 }
+# Cav3p1 classes with the GHK drive frozen for the linearisation (calcium.py, the
+# _Frozen subclasses: the forward current is the base class's)
+_GHK_FROZEN = ("Cav3p1_MA2020_GoC_Frozen", "Cav3p1_MA2024_PC_Frozen")
 # cell-type variants with their base class's kinetics; own defaults where they differ
 KINETIC_VARIANTS = {
     "Kv3p4_MA2020_GoC": {v: {} for v in ("Kv3p4_MA2020_GrC", "Kv3p4_MA2024_PC", "Kv3p4_MA2025_BC", "Kv3p4_RI2021_SC")},
@@ -246,6 +255,11 @@ for _base, _variants in KINETIC_VARIANTS.items():
 # gnonspec = 0 is built
 CHANNELS["Kv1p5_MA2020_GrC"] = {**CHANNELS["Kv1p5_MA2024_PC"], "gnonspec": 0.0}
 SAME_FORM["Kv1p5_MA2020_GrC"] = "Kv1p5_MA2024_PC"
+# Cav3p1_MA2024_PC overrides nothing of Cav3p1_MA2020_GoC; the _Frozen classes differ
+# only in the linearisation
+for _v in ("Cav3p1_MA2024_PC",) + _GHK_FROZEN:
+    CHANNELS[_v] = dict(CHANNELS["Cav3p1_MA2020_GoC"])
+    SAME_FORM[_v] = "Cav3p1_MA2020_GoC"
 # Ca_ZH2019_IO_Frozen (calcium.py) is Ca_ZH2019_IO with freeze_m_inf pinned to True
 CHANNELS["Ca_ZH2019_IO_Frozen"] = dict(CHANNELS["Ca_ZH2019_IO"])
 SAME_FORM["Ca_ZH2019_IO_Frozen"] = "Ca_ZH2019_IO"
@@ -493,6 +507,10 @@ def region_record(mechs, cable: CableProperty) -> tuple[int, np.ndarray]:
                 raise ValueError(f"{decl.class_name}: qdeltat other than 1 is not built.")
             elif name == "CaN_IS2008":
                 rec[_abi.BC_P_CAN_PHI] = q10_phi(p["q10"], p["temp"], p["temp_ref"])
+            elif name == "Cav3p1_MA2020_GoC":
+                rec[_abi.BC_P_CAV31_QT] = q10_phi(p["q10"], p["temp"], p["temp_ref"])
+                rec[_abi.BC_P_CAV31_TGHK] = p["temp"] + 0.04  # the model file's Kelvin offset
+                rec[_abi.BC_P_CAV31_FREEZE] = 1.0 if decl.class_name in _GHK_FROZEN else 0.0
             elif name == "Nav_MA2020_GrC":  # phi = 3^((T - 20 degC) / 10) (sodium.py, __init__)
                 rec[_abi.BC_P_NAVGRC_PHI] = q10_phi(3.0, p["temp"], celsius2kelvin(20.0))
             elif name == "Ca_ZH2019_IO":
@@ -515,7 +533,9 @@ def region_record(mechs, cable: CableProperty) -> tuple[int, np.ndarray]:
             rec[base + 2] = q10_phi(p["q10_p"], p["temp"], p["temp_ref_p"])
             rec[base + 3] = q10_phi(p["q10_q"], p["temp"], p["temp_ref_q"])
     ci_gated = bits & (_abi.BC_M_AHP | _abi.BC_M_KCA22 | _abi.BC_M_KCA11) or \
-        int(rec[_abi.BC_P_EXT_MASK]) & (_abi.BC_X_KCA31 | _abi.BC_X_SKDCN | _abi.BC_X_CAN)
+        int(rec[_abi.BC_P_EXT_MASK]) & (_abi.BC_X_KCA31 | _abi.BC_X_SKDCN | _abi.BC_X_CAN | _abi.BC_X_CAV31)
+    if int(rec[_abi.BC_P_EXT_MASK]) & _abi.BC_X_CAV31 and not bits & _abi.BC_M_CADET:
+        rec[_abi.BC_P_CA_CO] = 2.0  # the GHK drive's Co: the fixed calcium ion's (ion/calcium.py:121)
     if ci_gated and not bits & _abi.BC_M_CADET:
         # AHP and the Kca channels read Ci from the calcium ion; with a fixed Ca ion
         # Ci is the class default.

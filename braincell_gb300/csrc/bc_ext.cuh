@@ -28,6 +28,7 @@
 //   CaN_IS2008             channel/calcium.py:108-220
 //   Ca_ZH2019_IO           channel/calcium.py:4837-4979
 //   Nav_MA2020_GrC         channel/sodium.py:1427-1666 (on the Markov solver of bc_mech.cuh)
+//   Cav3p1_MA2020_GoC      channel/calcium.py:1972-2202 (GHK drive, calcium.py:78-86)
 // CaT_HP1992, CaHT_Re1993 and CaN_IS2008 (in its own E) carry calcium: their
 // step-start current joins the calcium shell's drive, as CaL's and CaT's do.  Kca3p1 and SK read Ci: the new Ci
 // of a dynamic calcium ion, else the fixed one (BC_P_CA_CI0), as AHP_De1994 does.
@@ -70,7 +71,9 @@ constexpr int kSlotKkvN = 94;
 constexpr int kSlotCanP = 95;
 constexpr int kSlotCaioH = 96;
 constexpr int kSlotNavGrc = 97;  // C1..C5, I1..I5, O, OB in 97..108 (I6 dependent)
-constexpr int kNumSlotsExt = 109;
+constexpr int kSlotCav31P = 109;
+constexpr int kSlotCav31Q = 110;
+constexpr int kNumSlotsExt = 111;
 
 // x / (1 - e^-x) = 1 / exprel(-x), finite at x = 0 (the reference's
 // _x_over_one_minus_exp_neg_stable, channel/sodium.py:50-55)
@@ -388,6 +391,43 @@ __device__ __forceinline__ void navgrc_rates(Real v, Real phi, Real* kf, Real* k
   kb[16] = ooff;
 }
 
+// Cav3p1_MA2020_GoC: p^2 q; inf sigmoids, p's tau 1 ms at V <= -90 mV and
+// (1 + 1 / (e^((V + 40) / 9) + e^((V + 102) / -18))) / qt above, q's
+// (15 + 1 / e^((V + 32) / 7)) / qt.
+template <typename Real>
+struct Cav31Rates {
+  Real pinf, ptau, qinf, qtau;
+  __host__ __device__ __forceinline__ Cav31Rates(Real v, Real qt) {
+    pinf = Real(1) / (Real(1) + aexp((v + Real(52)) / Real(-5)));
+    qinf = Real(1) / (Real(1) + aexp((v + Real(72)) / Real(7)));
+    ptau = v <= Real(-90) ? Real(1)
+                          : (Real(1) + Real(1) / (aexp((v + Real(40)) / Real(9)) + aexp((v + Real(102)) / Real(-18)))) / qt;
+    qtau = (Real(15) + Real(1) / aexp((v + Real(32)) / Real(7))) / qt;
+  }
+};
+
+// The Cav3.1 GHK drive (calcium.py:78-86, with the model file's F = 9.6485e4 C/mol and
+// R = 8.3145 J/(K mol)): z = 2, zeta = z F V / (R T), drive = z F zeta (ci - co e^-zeta)
+// / (1 - e^-zeta), and z F (ci - co e^-zeta)(1 + zeta / 2) where |1 - e^-zeta| < 1e-6.
+// With a permeability g in cm/s and ci, co in mM, -g drive is in uA/cm^2.  *dd
+// receives d drive / dV (per mV), the derivative of the branch taken.
+template <typename Real>
+__host__ __device__ __forceinline__ Real cav31_drive(Real v, Real ci, Real co, Real tghk, Real& dd) {
+  const Real zf = Real(2 * 9.6485e4);
+  const Real k = zf / (Real(8.3145) * tghk) * Real(1e-3);  // zeta per mV
+  const Real z = k * v;
+  const Real em = aexp(-z);
+  const Real num = ci - co * em;
+  const Real den = Real(1) - em;
+  const Real ad = den < Real(0) ? -den : den;
+  if (ad < Real(1e-6)) {
+    dd = zf * k * (co * em * (Real(1) + z / Real(2)) + num / Real(2));
+    return zf * num * (Real(1) + z / Real(2));
+  }
+  dd = zf * k * ((num + z * co * em) / den - z * num * em / (den * den));
+  return zf * z * num / den;
+}
+
 // The region's BC_X_* bits (an integer stored as a record real).
 template <typename Real>
 __host__ __device__ __forceinline__ uint32_t ext_mask(const Real* P) {
@@ -539,6 +579,17 @@ __device__ __forceinline__ Real ext_current(const Real* st, int N, const Real* P
         e = P[BC_P_ENA];
       }
       break;
+    case BC_CUR_CAV31:
+      if ((has = (x & BC_X_CAV31) != 0)) {
+        const Real p = st[kSlotCav31P * N];
+        const Real gp = P[BC_P_CAV31_G] * p * p * st[kSlotCav31Q * N];
+        Real dd;
+        const Real drive = cav31_drive(v, ci, P[BC_P_CA_CO], P[BC_P_CAV31_TGHK], dd);
+        // I = -g p^2 q drive: -dI/dV = g p^2 q d drive / dV, 0 with the drive frozen
+        if (gv) *gv = P[BC_P_CAV31_FREEZE] != Real(0) ? Real(0) : gp * dd;
+        return -gp * drive;
+      }
+      return Real(0);
     case BC_CUR_CAIO:
       if ((has = (x & BC_X_CAIO) != 0)) {
         Real m, dm;
@@ -650,6 +701,11 @@ __device__ __forceinline__ void ext_gates(Real* st, int N, const Real* P, uint32
     const CaioRates<Real> r(v);
     st[kSlotCaioH * N] = gate_it(st[kSlotCaioH * N], r.hinf, r.htau, Real(1), dt);
   }
+  if (x & BC_X_CAV31) {
+    const Cav31Rates<Real> r(v, P[BC_P_CAV31_QT]);
+    st[kSlotCav31P * N] = gate_it(st[kSlotCav31P * N], r.pinf, r.ptau, Real(1), dt);
+    st[kSlotCav31Q * N] = gate_it(st[kSlotCav31Q * N], r.qinf, r.qtau, Real(1), dt);
+  }
   // the Markov scheme after the gates, by one linearised backward-Euler step
   if (x & BC_X_NAVGRC) {
     Real kf[17], kb[17];
@@ -666,7 +722,7 @@ __device__ __noinline__ void ext_channels(Real* st, int N, const Real* P, Real v
                                           bool advance, Real& G, Real& I) {
   const uint32_t x = ext_mask(P);
   if (advance) ext_gates(st, N, P, x, v, ci, dt);
-  for (int code = BC_CUR_HCN2; code <= BC_CUR_NAVGRC; ++code) {
+  for (int code = BC_CUR_HCN2; code <= BC_CUR_CAV31; ++code) {
     Real g = Real(0);
     const Real i = ext_current(st, N, P, x, v, ci, eca, code, &g);
     G += g;
@@ -681,7 +737,8 @@ __device__ __noinline__ Real ext_ca_current(const Real* st, int N, const Real* P
   const uint32_t x = ext_mask(P);
   return ext_current(st, N, P, x, v, ci, eca, BC_CUR_CATHP, (Real*)nullptr) +
          ext_current(st, N, P, x, v, ci, eca, BC_CUR_CAHTRE, (Real*)nullptr) +
-         ext_current(st, N, P, x, v, ci, eca, BC_CUR_CAN, (Real*)nullptr);
+         ext_current(st, N, P, x, v, ci, eca, BC_CUR_CAN, (Real*)nullptr) +
+         ext_current(st, N, P, x, v, ci, eca, BC_CUR_CAV31, (Real*)nullptr);
 }
 
 // Steady states of the extension channels' gates at v (HH.reset_state).
@@ -754,6 +811,11 @@ __device__ __forceinline__ void ext_steady(const Real* P, Real* st, int N, Real 
         KkvRates<Real>(v, P[BC_P_KKV_VSH], P[BC_P_KKV_RA], P[BC_P_KKV_RB], P[BC_P_KKV_Q], P[BC_P_KKV_V12]).ninf;
   if (x & BC_X_CAN) st[kSlotCanP * N] = CanRates<Real>(v).pinf;
   if (x & BC_X_CAIO) st[kSlotCaioH * N] = CaioRates<Real>(v).hinf;
+  if (x & BC_X_CAV31) {
+    const Cav31Rates<Real> r(v, P[BC_P_CAV31_QT]);
+    st[kSlotCav31P * N] = r.pinf;
+    st[kSlotCav31Q * N] = r.qinf;
+  }
   if (x & BC_X_NAVGRC) {  // the stationary distribution (reset_steady_state)
     Real kf[17], kb[17];
     navgrc_rates(v, P[BC_P_NAVGRC_PHI], kf, kb);

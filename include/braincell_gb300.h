@@ -110,7 +110,9 @@ typedef int32_t bc_status;
 #define BC_X_CAIO (1u << 19)   /* channel/calcium.py:4837 Ca_ZH2019_IO m_inf(V)^1 h, own E   */
 #define BC_X_NAVGRC (1u << 20) /* channel/sodium.py:1427 Nav_MA2020_GrC 13-state Markov scheme
                                   (the Nav1.6 graph), g O, E_Na                               */
-#define BC_X_ALL 0x1FFFFFu
+#define BC_X_CAV31 (1u << 21)  /* channel/calcium.py:1972 Cav3p1_MA2020_GoC p^2 q, GHK drive
+                                  (permeability g in cm/s; a calcium-ion current)            */
+#define BC_X_ALL 0x3FFFFFu
 
 /* Per-region parameter record (double[BC_NPARAM]); index names below. */
 #define BC_NPARAM 160
@@ -259,7 +261,11 @@ typedef int32_t bc_status;
 #define BC_P_CAIO_FREEZE 142 /* 1: m_inf held out of the linearisation (freeze_m_inf) */
 #define BC_P_NAVGRC_G 143
 #define BC_P_NAVGRC_PHI 144 /* 3^((T - 20 degC) / 10)                               */
-/* 145 .. 159: reserved for further extension channels (0) */
+#define BC_P_CAV31_G 145    /* permeability (cm/s)                                  */
+#define BC_P_CAV31_QT 146   /* q10^((T - temp_ref) / 10): the time constants' divisor */
+#define BC_P_CAV31_TGHK 147 /* the GHK temperature T + 0.04 K                       */
+#define BC_P_CAV31_FREEZE 148 /* 1: the drive held out of the linearisation (Frozen) */
+/* 149 .. 159: reserved for further extension channels (0) */
 
 /* ------------------------------------------------------------------ batch spec */
 /*
@@ -425,7 +431,7 @@ const char* bc_last_error(void);
  * HH and calcium channels (BC_M_KV34 .. CAV32, a 96-entry parameter record, state
  * views 51-65, BC_PROBE_CURRENT 128).  0.5.0: extension channels (BC_M_EXT with
  * BC_X_* bits in the record's BC_P_EXT_MASK, a 160-entry parameter record, state
- * views 66-107, current codes 31-51). */
+ * views 66-109, current codes 31-52). */
 #define BC_ABI_VERSION 500
 int32_t bc_version(void);
 /* Fill opts with defaults. */
@@ -559,7 +565,9 @@ bc_status bc_check(bc_plan_t plan, void* stream);
 #define BC_STATE_CAIO_H 95
 #define BC_STATE_NAVGRC_C1 96 /* .. C5 100, I1 101 .. I5 105, O 106, OB 107 (I6 dependent) */
 #define BC_STATE_NAVGRC_O 106
-#define BC_NSTATE_VIEW 108
+#define BC_STATE_CAV31_P 108
+#define BC_STATE_CAV31_Q 109
+#define BC_NSTATE_VIEW 110
 /* Current probes (mech/_point.py CurrentProbe, _multi_compartment/probes.py:184-258):
    probe_field = BC_PROBE_CURRENT + one of the codes below records that current
    density (uA/cm^2, outward negative as g (E - V)) after the step.             */
@@ -616,7 +624,8 @@ bc_status bc_check(bc_plan_t plan, void* stream);
 #define BC_CUR_CAN 49    /* CaN_IS2008             */
 #define BC_CUR_CAIO 50   /* Ca_ZH2019_IO           */
 #define BC_CUR_NAVGRC 51 /* Nav_MA2020_GrC         */
-#define BC_NCUR 52
+#define BC_CUR_CAV31 52  /* Cav3p1_MA2020_GoC      */
+#define BC_NCUR 53
 bc_status bc_state_download(bc_plan_t plan, int32_t which, double* out /* [n_cv] */, void* stream);
 /* Set the amplitude (nA) of every current-clamp pulse of the batch spec, in spec
  * order (amp_nA[n_pulses]); times and locations are unchanged.  Takes effect from

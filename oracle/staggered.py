@@ -149,7 +149,27 @@ CHANNEL_DEFAULTS.update({
     "K_Kv_test": dict(g_max=0.0, V_sh=0.0, temp=_c2k(25.0), Ra=0.02, Rb=0.006, q=9.0, v12=25.0),  # potassium.py:1239
     "CaN_IS2008": dict(E=10.0, g_max=1.0, temp=_c2k(36.0), q10=1.0, temp_ref=_c2k(36.0)),  # calcium.py:108
     "Ca_ZH2019_IO": dict(g_max=0.4, E=120.0, mMidV=-61.0, freeze_m_inf=1.0),  # calcium.py:4837
+    # permeability in cm/s (calcium.py:1972)
+    "Cav3p1_MA2020_GoC": dict(g_max=2.5e-4, V_sh=0.0, temp=_c2k(22.0), q10=3.0, temp_ref=_c2k(37.0)),
 })
+
+
+def cav31_drive(V, ci, co, temp):
+    """The Cav3.1 GHK drive (calcium.py:78-86) with the model file's constants
+    F = 9.6485e4, R = 8.3145 and T + 0.04 K; z = 2.  Returns (drive, d drive / dV per mV)
+    for ci, co in mM and V in mV; -g drive (g in cm/s) is in uA/cm^2."""
+    zf = 2.0 * 9.6485e4
+    k = zf / (8.3145 * (temp + 0.04)) * 1e-3
+    z = k * V
+    em = np.exp(-z)
+    num = ci - co * em
+    den = 1.0 - em
+    small = np.abs(den) < 1e-6
+    safe = np.where(small, 1.0, den)
+    drive = np.where(small, zf * num * (1.0 + z / 2.0), zf * z * num / safe)
+    dd = np.where(small, zf * k * (co * em * (1.0 + z / 2.0) + num / 2.0),
+                  zf * k * ((num + z * co * em) / safe - z * num * em / safe ** 2))
+    return drive, dd
 
 
 def can_modulation(Ci):
@@ -179,6 +199,9 @@ _VARIANTS = {
     "Kv1p5_MA2020_GrC": ("Kv1p5_MA2024_PC", {"gnonspec": 0.0}),
     **{v: ("Kca3p1_MA2020_GoC", {}) for v in ("Kca3p1_MA2025_BC", "Kca3p1_MA2024_PC")},
     "Ca_ZH2019_IO_Frozen": ("Ca_ZH2019_IO", {}),  # freeze_m_inf pinned to True (calcium.py, the subclass)
+    # Cav3p1_MA2024_PC overrides nothing; the _Frozen classes hold the GHK drive out of the linearisation
+    **{v: ("Cav3p1_MA2020_GoC", {}) for v in ("Cav3p1_MA2024_PC", "Cav3p1_MA2020_GoC_Frozen",
+                                               "Cav3p1_MA2024_PC_Frozen")},
     **{v: ("Cav3p2_RI2021_SC", {}) for v in ("Cav3p2_MA2025_BC", "Cav3p2_MA2024_PC")},
 }
 
@@ -631,6 +654,11 @@ def rates(name: str, V, p: dict, Ci=None):
         q = p["q"]
         denom = q * (p["Ra"] * _x_over_1mexp(y / q) + p["Rb"] * _x_over_1mexp(-y / q))
         return {"n": ("it", 1.0 / (1.0 + np.exp(-y / q)), 1.0 / denom)}
+    if name == "Cav3p1_MA2020_GoC":  # calcium.py:1972-2202; the time constants divided by qt
+        qt = p["q10"] ** ((p["temp"] - p["temp_ref"]) / 10.0)
+        pt = np.where(V <= -90.0, 1.0, (1.0 + 1.0 / (np.exp((V + 40.0) / 9.0) + np.exp((V + 102.0) / -18.0))) / qt)
+        return {"p": ("it", 1.0 / (1.0 + np.exp((V - -52.0) / -5.0)), pt),
+                "q": ("it", 1.0 / (1.0 + np.exp((V - -72.0) / 7.0)), (15.0 + 1.0 / np.exp((V + 32.0) / 7.0)) / qt)}
     if name == "CaN_IS2008":  # calcium.py:108-220
         return {"p": ("it", 1.0 / (1.0 + np.exp(-(V + 43.0) / 5.2)),
                       2.7 / (np.exp(-(V + 55.0) / 15.0) + np.exp((V + 55.0) / 15.0)) + 1.6)}
@@ -693,6 +721,7 @@ _GATES = {  # (gate, power, phi-key)
     "K_Kv_test": (("n", 1, "phi"),),
     "CaN_IS2008": (("p", 1, "phi"),),
     "Ca_ZH2019_IO": (("h", 1, "phi"),),
+    "Cav3p1_MA2020_GoC": (("p", 2, "phi"), ("q", 1, "phi")),
 }
 _ION_OF = {"Na_Ba2002": "na", "KDR_Ba2002": "k", "CaL_IS2008": "ca", "CaT_HM1992": "ca",
            "K_Leak": "k", "AHP_De1994": "k", "Na_HH1952": "na", "K_HH1952": "k", "KM_RI2021_SC": "k",
@@ -705,7 +734,8 @@ _ION_OF = {"Na_Ba2002": "na", "KDR_Ba2002": "k", "CaL_IS2008": "ca", "CaT_HM1992
            "Kv3p3_MA2024_PC": "k", "Kv2p2_0010_MA2020_GrC": "k", "Kv1p5_MA2024_PC": "k", "NaF_SU2015_DCN": "na",
            "NaP_SU2015_DCN": "na", "Na_ZH2019_IO": "na", "fKdr_SU2015_DCN": "k", "sKdr_SU2015_DCN": "k",
            "Kdr_ZH2019_IO": "k", "CaT_HP1992": "ca", "CaHT_Re1993": "ca", "Kca3p1_MA2020_GoC": "k",
-           "SK_SU2015_DCN": "k", "K_Kv_test": "k", "CaN_IS2008": "ca", "Nav_MA2020_GrC": "na"}
+           "SK_SU2015_DCN": "k", "K_Kv_test": "k", "CaN_IS2008": "ca", "Nav_MA2020_GrC": "na",
+           "Cav3p1_MA2020_GoC": "ca"}
 # channels with their own reversal potential (HHTypedNeuron root, not an ion)
 _OWN_E = ("HCN_HM1992", "HCN1_MA2020_GoC", "HCN1_MA2024_PC", "HCN2_MA2020_GoC", "HCN_SU2015_DCN", "HCN_ZH2019_IO",
           "CaL_SU2015_DCN", "CaN_IS2008", "Ca_ZH2019_IO")
@@ -758,6 +788,8 @@ def _resolve(table: dict, decl) -> dict:
         p["gbar_phi"] = 1.5 ** ((p["temp"] - _c2k(23.0)) / 10.0)
     if name == "CaN_IS2008":  # Gate("p", q10, temp_ref)
         p["phi"] = p["q10"] ** ((p["temp"] - p["temp_ref"]) / 10.0)
+    if name == "Cav3p1_MA2020_GoC":  # the _Frozen classes hold the GHK drive out of the linearisation
+        p["ghk_frozen"] = 1.0 if decl.class_name.endswith("_Frozen") else 0.0
     if p.get("gnonspec", 0.0) != 0.0:
         raise ValueError("Kv1p5_MA2020_GrC's nonspecific current (gnonspec != 0) not restated")
     p.pop("gnonspec", None)
@@ -767,7 +799,8 @@ def _resolve(table: dict, decl) -> dict:
         p["phi"] = 2.7 ** ((p["temp"] - _c2k(22.0)) / 10.0)
     elif name in ("Kv2p2_0010_MA2020_GrC", "Kv1p5_MA2024_PC", "NaF_SU2015_DCN", "NaP_SU2015_DCN", "Na_ZH2019_IO",
                   "fKdr_SU2015_DCN", "sKdr_SU2015_DCN", "Kdr_ZH2019_IO", "HCN_SU2015_DCN", "HCN_ZH2019_IO",
-                  "CaL_SU2015_DCN", "Kca3p1_MA2020_GoC", "SK_SU2015_DCN", "K_Kv_test", "Ca_ZH2019_IO"):
+                  "CaL_SU2015_DCN", "Kca3p1_MA2020_GoC", "SK_SU2015_DCN", "K_Kv_test", "Ca_ZH2019_IO",
+                  "Cav3p1_MA2020_GoC"):
         p["phi"] = 1.0  # gates without q10 or phi (Kv1p5's Q10 sits in its rates)
     return p
 
@@ -1227,6 +1260,13 @@ class OracleCell:
             return self.Ci_fixed
         return np.where(self.ca_dyn["mask"], self.Ci, self.Ci_fixed)
 
+    def _co_for_channels(self):
+        """Co of the calcium ion: the dynamic shell's, else the fixed ion's 2 mM
+        (ion/calcium.py:121)."""
+        if self.ca_dyn is None:
+            return 2.0
+        return np.where(self.ca_dyn["mask"], self.ca_dyn["Co"], 2.0)
+
     def _E_ca(self):
         if self.Ci is None:
             return self.E_ca_fixed
@@ -1271,6 +1311,11 @@ class OracleCell:
                 I = I + geff * f * (E - pv)
                 dI = dI + geff * (df * (E - pv) - f)
                 continue
+            if name == "Cav3p1_MA2020_GoC":  # -g p^2 q drive(V, Ci, Co): dI/dV = -g p^2 q d drive / dV
+                drive, dd = cav31_drive(pv, self._ci_for_channels(), self._co_for_channels(), ch["temp"])
+                I = I - geff * drive
+                dI = dI - np.where(ch["ghk_frozen"] != 0.0, 0.0, geff * dd)
+                continue
             if name == "Ca_ZH2019_IO":  # g m_inf(V) h (E - V); a frozen m_inf is out of the derivative
                 m, dm = caio_minf(pv, ch["mMidV"])
                 I = I + geff * m * (E - pv)
@@ -1301,6 +1346,10 @@ class OracleCell:
                 fac = fac * kv15_vfactor(pv)[0]
             if name == "Ca_ZH2019_IO":
                 fac = fac * caio_minf(pv, ch["mMidV"])[0]
+            if name == "Cav3p1_MA2020_GoC":
+                cur = -ch["g_max"] * fac * cav31_drive(pv, self._ci_for_channels(), self._co_for_channels(),
+                                                       ch["temp"])[0]
+                return cur[:, pid] if np.ndim(cur) == 2 else np.full(self.P, float(cur))
             cur = ch["g_max"] * fac * (E - pv)
             return cur[:, pid] if np.ndim(cur) == 2 else np.full(self.P, float(cur))
 
@@ -1318,6 +1367,11 @@ class OracleCell:
         E_ca = self._E_ca()
         for name in self.chan:
             if _ION_OF.get(name) == "ca":
+                if name == "Cav3p1_MA2020_GoC":  # the GHK drive
+                    ch = self.chan[name]
+                    I = I - ch["g_max"] * self._gate_product(name) * cav31_drive(
+                        pv, self._ci_for_channels(), self._co_for_channels(), ch["temp"])[0]
+                    continue
                 E = self.chan[name]["E"] if name in _OWN_E else E_ca  # CaN_IS2008 carries calcium in its own E
                 I = I + self.chan[name]["g_max"] * self._gate_product(name) * (E - pv)
         return I

@@ -4,7 +4,8 @@ kernel), the SU2015 DCN sodium / potassium / HCN / CaL classes, the ZH2019 IO so
 potassium / HCN classes, CaT_HP1992 and CaHT_Re1993 driving a CalciumDetailed shell, the
 calcium-gated Kca3p1 (and its BC / PC classes) and SK_SU2015_DCN, K_Kv_test, CaN_IS2008
 (Ci-modulated, carried by calcium in its own E), Ca_ZH2019_IO (and its Frozen class), and
-the Markov scheme Nav_MA2020_GrC.
+the Markov scheme Nav_MA2020_GrC, and Cav3p1 (GoC, PC and their _Frozen classes) with its
+GHK drive.
 
 CPU: the records and their mask, the planner's check of the mask, and the owner
 tables (through the planner tests).  GPU: a DCN-like cell and an IO-like cell
@@ -176,6 +177,27 @@ def _grc_cell(precision="f64"):
     return c
 
 
+def _cav31_cell(precision="f64"):
+    soma = Branch.from_lengths(lengths=[20.0], radii=[10.0, 10.0], type="soma")
+    m = Morphology.from_root(soma, name="soma")
+    m.attach(parent="soma", child_branch=Branch.from_lengths(lengths=[150.0], radii=[1.0, 0.6], type="dendrite"),
+             child_name="d0")
+    c = Cell(m, cv_policy=CVPerBranch(5), precision=precision)
+    c.paint(AllRegion(), CableProperty(), Channel("IL", g_max=0.1, E=-65.0))
+    # the soma: the Frozen class on the fixed calcium ion; the dendrite: the GHK drive in
+    # the linearisation, on a CalciumDetailed shell that it fills
+    c.paint(branch_in("type", "soma"), Channel("Na_Ba2002", g_max=120.0), Channel("KDR_Ba2002", g_max=40.0),
+            Channel("Cav3p1_MA2024_PC_Frozen", g_max=1e-4))
+    c.paint(branch_in("type", "dendrite"), Channel("Cav3p1_MA2020_GoC", g_max=2.5e-4),
+            Ion("CalciumDetailed", C_rest=5e-5, tau=20.0, d=0.5, Ci_initializer=5e-5))
+    c.place(RootLocation(0.5), CurrentClamp(delay=2.0, durations=20.0, amplitudes=0.3), StateProbe(name="v"),
+            CurrentProbe(mechanism="Cav3p1_MA2024_PC_Frozen", name="i_cav_soma"))
+    c.place(at(1, 0.5), StateProbe(name="v_dend"), MechanismProbe("CalciumDetailed", "Ci", name="ci"),
+            MechanismProbe("Cav3p1_MA2020_GoC", "p", name="cav_p"), MechanismProbe("Cav3p1_MA2020_GoC", "q", name="cav_q"),
+            CurrentProbe(mechanism="Cav3p1_MA2020_GoC", name="i_cav"), CurrentProbe(ion="ca", name="i_ca"))
+    return c
+
+
 def test_kv15_grc_runs_on_the_pc_kernel():
     cable = CableProperty()
     assert catalogue.region_record([Channel("Kv1p5_MA2020_GrC", g_max=0.3)], cable)[1].tolist() == \
@@ -186,8 +208,9 @@ def test_kv15_grc_runs_on_the_pc_kernel():
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("make,n", [(_dcn_cell, 1000), (_io_cell, 800), (_ca_cell, 1000), (_kca_cell, 1000),
-                                    (_can_cell, 1000), (_can_cell_unfrozen, 1000), (_grc_cell, 800)],
-                         ids=["dcn", "io", "ca", "kca", "can", "can_unfrozen", "grc"])
+                                    (_can_cell, 1000), (_can_cell_unfrozen, 1000), (_grc_cell, 800),
+                                    (_cav31_cell, 1000)],
+                         ids=["dcn", "io", "ca", "kca", "can", "can_unfrozen", "grc", "cav31"])
 def test_extension_cells_f64_match_oracle(native_lib, cuda_device, make, n):
     from braincell_gb300.runtime import Plan
 
@@ -214,8 +237,8 @@ def test_extension_cells_f64_match_oracle(native_lib, cuda_device, make, n):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("make", [_dcn_cell, _io_cell, _ca_cell, _kca_cell, _can_cell, _grc_cell],
-                         ids=["dcn", "io", "ca", "kca", "can", "grc"])
+@pytest.mark.parametrize("make", [_dcn_cell, _io_cell, _ca_cell, _kca_cell, _can_cell, _grc_cell, _cav31_cell],
+                         ids=["dcn", "io", "ca", "kca", "can", "grc", "cav31"])
 def test_extension_cells_f32_meet_the_bar(native_lib, cuda_device, make):
     from braincell_gb300.runtime import Plan
 
