@@ -76,7 +76,8 @@ BC_X_CAN = 1 << 18
 BC_X_CAIO = 1 << 19
 BC_X_NAVGRC = 1 << 20
 BC_X_CAV31 = 1 << 21
-BC_X_ALL = 0x3FFFFF
+BC_X_CAV33 = 1 << 22
+BC_X_ALL = 0x7FFFFF
 
 BC_NPARAM = 160
 BC_P_INVCM = 0
@@ -227,6 +228,11 @@ BC_P_CAV31_G = 145
 BC_P_CAV31_QT = 146
 BC_P_CAV31_TGHK = 147
 BC_P_CAV31_FREEZE = 148
+BC_P_CAV33_G = 149
+BC_P_CAV33_PHI = 150
+BC_P_CAV33_TGHK = 151
+BC_P_CAV33_VSH = 152
+BC_P_CAV33_FREEZE = 153
 
 BC_ABI_VERSION = 500
 
@@ -296,7 +302,8 @@ BC_CUR_CAN = 49
 BC_CUR_CAIO = 50
 BC_CUR_NAVGRC = 51
 BC_CUR_CAV31 = 52
-BC_NCUR = 53
+BC_CUR_CAV33 = 53
+BC_NCUR = 54
 
 BC_STATE_V = 0
 BC_STATE_NA_P = 1
@@ -376,7 +383,9 @@ BC_STATE_NAVGRC_C1 = 96
 BC_STATE_NAVGRC_O = 106
 BC_STATE_CAV31_P = 108
 BC_STATE_CAV31_Q = 109
-BC_NSTATE_VIEW = 110
+BC_STATE_CAV33_N = 110
+BC_STATE_CAV33_L = 111
+BC_NSTATE_VIEW = 112
 # the independent states of each Markov scheme, in view order (first appearance in
 # the scheme's transition list, the dependent state left out)
 MARKOV_STATES = {
@@ -460,6 +469,8 @@ STATE_NAMES = {
     "CaIO_h": BC_STATE_CAIO_H,
     "Cav3p1_p": BC_STATE_CAV31_P,
     "Cav3p1_q": BC_STATE_CAV31_Q,
+    "Cav3p3_n": BC_STATE_CAV33_N,
+    "Cav3p3_l": BC_STATE_CAV33_L,
 }
 for _cls, (_base, _names) in MARKOV_STATES.items():
     for _k, _n in enumerate(_names):

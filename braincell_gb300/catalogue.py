@@ -70,6 +70,9 @@ BC_P_EXT_MASK, their parameters after it; conductances in mS/cm^2):
 * ``Cav3p1_MA2020_GoC`` -- channel/calcium.py:1972 (permeability g_max 2.5e-4 cm/s, temp 22 degC, q10 3 at 37 degC
   dividing the time constants; GHK drive at temp + 0.04 K); Cav3p1_MA2024_PC repeats it, and the two _Frozen classes
   hold the drive out of the linearisation
+* ``Cav3p3_RI2021_SC`` -- channel/calcium.py:4033 (perm 1e-4 cm/s, g_scale 1e-5, temp 36 degC, V_sh 0; gates q10 2.3
+  at 28 degC; GHK drive at temp - 0.01 K); Cav3p3_MA2024_PC repeats it and its _Frozen class holds the drive out of
+  the linearisation
 * ``Nav_MA2020_GrC`` -- channel/sodium.py:1427 (g_max 13, temp 32 degC; phi 3^((T - 20 degC) / 10)): a Markov
   scheme on the Nav1.6 graph with its own rate constants
 * ``Ca_ZH2019_IO`` / ``_Frozen`` -- channel/calcium.py:4837 (g_max 0.4, E 120 mV, mMidV -61 mV, freeze_m_inf true;
@@ -193,6 +196,8 @@ CHANNELS: dict[str, dict[str, float]] = {
     "Nav_MA2020_GrC": {"g_max": 13.0, "temp": celsius2kelvin(32.0)},
     # a permeability in cm/s (calcium.py:1972: 2.5e-4 cm/s)
     "Cav3p1_MA2020_GoC": {"g_max": 2.5e-4, "V_sh": 0.0, "temp": T22, "q10": 3.0, "temp_ref": celsius2kelvin(37.0)},
+    # permeability perm in cm/s times g_scale (calcium.py:4033); no g_max parameter
+    "Cav3p3_RI2021_SC": {"perm": 1.0e-4, "g_scale": 1.0e-5, "temp": T36, "V_sh": 0.0},
 }
 # extension channels: class -> (BC_X_* bit, record entry of g_max, record entry of E or None)
 _EXT = {
@@ -218,10 +223,11 @@ _EXT = {
     "Ca_ZH2019_IO": (_abi.BC_X_CAIO, _abi.BC_P_CAIO_G, _abi.BC_P_CAIO_E),
     "Nav_MA2020_GrC": (_abi.BC_X_NAVGRC, _abi.BC_P_NAVGRC_G, None),
     "Cav3p1_MA2020_GoC": (_abi.BC_X_CAV31, _abi.BC_P_CAV31_G, None),
+    "Cav3p3_RI2021_SC": (_abi.BC_X_CAV33, _abi.BC_P_CAV33_G, None),
 }
 # Cav3p1 classes with the GHK drive frozen for the linearisation (calcium.py, the
 # _Frozen subclasses: the forward current is the base class's)
-_GHK_FROZEN = ("Cav3p1_MA2020_GoC_Frozen", "Cav3p1_MA2024_PC_Frozen")
+_GHK_FROZEN = ("Cav3p1_MA2020_GoC_Frozen", "Cav3p1_MA2024_PC_Frozen", "Cav3p3_MA2024_PC_Frozen")
 # cell-type variants with their base class's kinetics; own defaults where they differ
 KINETIC_VARIANTS = {
     "Kv3p4_MA2020_GoC": {v: {} for v in ("Kv3p4_MA2020_GrC", "Kv3p4_MA2024_PC", "Kv3p4_MA2025_BC", "Kv3p4_RI2021_SC")},
@@ -257,9 +263,14 @@ CHANNELS["Kv1p5_MA2020_GrC"] = {**CHANNELS["Kv1p5_MA2024_PC"], "gnonspec": 0.0}
 SAME_FORM["Kv1p5_MA2020_GrC"] = "Kv1p5_MA2024_PC"
 # Cav3p1_MA2024_PC overrides nothing of Cav3p1_MA2020_GoC; the _Frozen classes differ
 # only in the linearisation
-for _v in ("Cav3p1_MA2024_PC",) + _GHK_FROZEN:
+for _v in ("Cav3p1_MA2024_PC", "Cav3p1_MA2020_GoC_Frozen", "Cav3p1_MA2024_PC_Frozen"):
     CHANNELS[_v] = dict(CHANNELS["Cav3p1_MA2020_GoC"])
     SAME_FORM[_v] = "Cav3p1_MA2020_GoC"
+# Cav3p3_MA2024_PC overrides nothing of Cav3p3_RI2021_SC; its _Frozen class differs only
+# in the linearisation
+for _v in ("Cav3p3_MA2024_PC", "Cav3p3_MA2024_PC_Frozen"):
+    CHANNELS[_v] = dict(CHANNELS["Cav3p3_RI2021_SC"])
+    SAME_FORM[_v] = "Cav3p3_RI2021_SC"
 # Ca_ZH2019_IO_Frozen (calcium.py) is Ca_ZH2019_IO with freeze_m_inf pinned to True
 CHANNELS["Ca_ZH2019_IO_Frozen"] = dict(CHANNELS["Ca_ZH2019_IO"])
 SAME_FORM["Ca_ZH2019_IO_Frozen"] = "Ca_ZH2019_IO"
@@ -483,7 +494,7 @@ def region_record(mechs, cable: CableProperty) -> tuple[int, np.ndarray]:
             xbit, g_slot, e_slot = _EXT[name]
             bits |= _abi.BC_M_EXT
             rec[_abi.BC_P_EXT_MASK] = float(int(rec[_abi.BC_P_EXT_MASK]) | xbit)
-            g = p["g_max"]
+            g = p["g_scale"] * p["perm"] if name == "Cav3p3_RI2021_SC" else p["g_max"]
             if name == "HCN2_MA2020_GoC":  # the conductance's own Q10 1.5 and the gates' q10 3, at 23 degC
                 g *= q10_phi(1.5, p["temp"], celsius2kelvin(23.0))
                 rec[_abi.BC_P_HCN2_PHI] = q10_phi(3.0, p["temp"], celsius2kelvin(23.0))
@@ -511,6 +522,11 @@ def region_record(mechs, cable: CableProperty) -> tuple[int, np.ndarray]:
                 rec[_abi.BC_P_CAV31_QT] = q10_phi(p["q10"], p["temp"], p["temp_ref"])
                 rec[_abi.BC_P_CAV31_TGHK] = p["temp"] + 0.04  # the model file's Kelvin offset
                 rec[_abi.BC_P_CAV31_FREEZE] = 1.0 if decl.class_name in _GHK_FROZEN else 0.0
+            elif name == "Cav3p3_RI2021_SC":
+                rec[_abi.BC_P_CAV33_PHI] = q10_phi(2.3, p["temp"], celsius2kelvin(28.0))
+                rec[_abi.BC_P_CAV33_TGHK] = p["temp"] - 0.01  # the model file's Kelvin offset
+                rec[_abi.BC_P_CAV33_VSH] = p["V_sh"]
+                rec[_abi.BC_P_CAV33_FREEZE] = 1.0 if decl.class_name in _GHK_FROZEN else 0.0
             elif name == "Nav_MA2020_GrC":  # phi = 3^((T - 20 degC) / 10) (sodium.py, __init__)
                 rec[_abi.BC_P_NAVGRC_PHI] = q10_phi(3.0, p["temp"], celsius2kelvin(20.0))
             elif name == "Ca_ZH2019_IO":
@@ -533,8 +549,9 @@ def region_record(mechs, cable: CableProperty) -> tuple[int, np.ndarray]:
             rec[base + 2] = q10_phi(p["q10_p"], p["temp"], p["temp_ref_p"])
             rec[base + 3] = q10_phi(p["q10_q"], p["temp"], p["temp_ref_q"])
     ci_gated = bits & (_abi.BC_M_AHP | _abi.BC_M_KCA22 | _abi.BC_M_KCA11) or \
-        int(rec[_abi.BC_P_EXT_MASK]) & (_abi.BC_X_KCA31 | _abi.BC_X_SKDCN | _abi.BC_X_CAN | _abi.BC_X_CAV31)
-    if int(rec[_abi.BC_P_EXT_MASK]) & _abi.BC_X_CAV31 and not bits & _abi.BC_M_CADET:
+        int(rec[_abi.BC_P_EXT_MASK]) & (_abi.BC_X_KCA31 | _abi.BC_X_SKDCN | _abi.BC_X_CAN | _abi.BC_X_CAV31 |
+                                         _abi.BC_X_CAV33)
+    if int(rec[_abi.BC_P_EXT_MASK]) & (_abi.BC_X_CAV31 | _abi.BC_X_CAV33) and not bits & _abi.BC_M_CADET:
         rec[_abi.BC_P_CA_CO] = 2.0  # the GHK drive's Co: the fixed calcium ion's (ion/calcium.py:121)
     if ci_gated and not bits & _abi.BC_M_CADET:
         # AHP and the Kca channels read Ci from the calcium ion; with a fixed Ca ion

@@ -29,6 +29,7 @@
 //   Ca_ZH2019_IO           channel/calcium.py:4837-4979
 //   Nav_MA2020_GrC         channel/sodium.py:1427-1666 (on the Markov solver of bc_mech.cuh)
 //   Cav3p1_MA2020_GoC      channel/calcium.py:1972-2202 (GHK drive, calcium.py:78-86)
+//   Cav3p3_RI2021_SC       channel/calcium.py:4033-4255 (GHK drive, calcium.py:89-97)
 // CaT_HP1992, CaHT_Re1993 and CaN_IS2008 (in its own E) carry calcium: their
 // step-start current joins the calcium shell's drive, as CaL's and CaT's do.  Kca3p1 and SK read Ci: the new Ci
 // of a dynamic calcium ion, else the fixed one (BC_P_CA_CI0), as AHP_De1994 does.
@@ -73,7 +74,9 @@ constexpr int kSlotCaioH = 96;
 constexpr int kSlotNavGrc = 97;  // C1..C5, I1..I5, O, OB in 97..108 (I6 dependent)
 constexpr int kSlotCav31P = 109;
 constexpr int kSlotCav31Q = 110;
-constexpr int kNumSlotsExt = 111;
+constexpr int kSlotCav33N = 111;
+constexpr int kSlotCav33L = 112;
+constexpr int kNumSlotsExt = 113;
 
 // x / (1 - e^-x) = 1 / exprel(-x), finite at x = 0 (the reference's
 // _x_over_one_minus_exp_neg_stable, channel/sodium.py:50-55)
@@ -428,6 +431,41 @@ __host__ __device__ __forceinline__ Real cav31_drive(Real v, Real ci, Real co, R
   return zf * z * num / den;
 }
 
+// Cav3p3_RI2021_SC: n^2 l on V - V_sh; inf sigmoids, piecewise time constants at -60 mV.
+template <typename Real>
+struct Cav33Rates {
+  Real ninf, ntau, linf, ltau;
+  __host__ __device__ __forceinline__ Cav33Rates(Real v, Real vsh) {
+    const Real x = v - vsh;
+    ninf = Real(1) / (Real(1) + aexp(-(x + Real(41.5)) / Real(6.2)));
+    linf = Real(1) / (Real(1) + aexp(-(x + Real(69.8)) / Real(-6.1)));
+    ntau = x > Real(-60) ? Real(7.2) + Real(0.02) * aexp(-x / Real(14.7)) : Real(0.875) * aexp((x + Real(120)) / Real(41));
+    ltau = x > Real(-60) ? Real(79.5) + Real(2) * aexp(-x / Real(9.3)) : Real(260);
+  }
+};
+
+// The Cav3.3 GHK drive (calcium.py:89-97, the model file's F = 96520 C/mol and
+// R = 8.3134 J/(K mol)): z = 2, w = z F V / (R T), drive = -z F (co - ci e^w) w /
+// (e^w - 1), and -z F (co - ci e^w)(1 - w / 2) where |e^w - 1| < 1e-6; *dd receives
+// d drive / dV (per mV) of the branch taken.
+template <typename Real>
+__host__ __device__ __forceinline__ Real cav33_drive(Real v, Real ci, Real co, Real tghk, Real& dd) {
+  const Real zf = Real(2 * 96520.0);
+  const Real k = zf / (Real(8.3134) * tghk) * Real(1e-3);  // w per mV
+  const Real w = k * v;
+  const Real ep = aexp(w);
+  const Real num = co - ci * ep;
+  const Real den = ep - Real(1);
+  const Real ad = den < Real(0) ? -den : den;
+  if (ad < Real(1e-6)) {
+    dd = -zf * k * (-ci * ep * (Real(1) - w / Real(2)) - num / Real(2));
+    return -zf * num * (Real(1) - w / Real(2));
+  }
+  // d/dw [num w / den] = (-ci e^w w + num) / den - num w e^w / den^2
+  dd = -zf * k * ((num - ci * ep * w) / den - num * w * ep / (den * den));
+  return -zf * num * w / den;
+}
+
 // The region's BC_X_* bits (an integer stored as a record real).
 template <typename Real>
 __host__ __device__ __forceinline__ uint32_t ext_mask(const Real* P) {
@@ -590,6 +628,16 @@ __device__ __forceinline__ Real ext_current(const Real* st, int N, const Real* P
         return -gp * drive;
       }
       return Real(0);
+    case BC_CUR_CAV33:
+      if ((has = (x & BC_X_CAV33) != 0)) {
+        const Real n = st[kSlotCav33N * N];
+        const Real gp = P[BC_P_CAV33_G] * n * n * st[kSlotCav33L * N];
+        Real dd;
+        const Real drive = cav33_drive(v - P[BC_P_CAV33_VSH], ci, P[BC_P_CA_CO], P[BC_P_CAV33_TGHK], dd);
+        if (gv) *gv = P[BC_P_CAV33_FREEZE] != Real(0) ? Real(0) : gp * dd;
+        return -gp * drive;
+      }
+      return Real(0);
     case BC_CUR_CAIO:
       if ((has = (x & BC_X_CAIO) != 0)) {
         Real m, dm;
@@ -706,6 +754,12 @@ __device__ __forceinline__ void ext_gates(Real* st, int N, const Real* P, uint32
     st[kSlotCav31P * N] = gate_it(st[kSlotCav31P * N], r.pinf, r.ptau, Real(1), dt);
     st[kSlotCav31Q * N] = gate_it(st[kSlotCav31Q * N], r.qinf, r.qtau, Real(1), dt);
   }
+  if (x & BC_X_CAV33) {
+    const Cav33Rates<Real> r(v, P[BC_P_CAV33_VSH]);
+    const Real phi = P[BC_P_CAV33_PHI];
+    st[kSlotCav33N * N] = gate_it(st[kSlotCav33N * N], r.ninf, r.ntau, phi, dt);
+    st[kSlotCav33L * N] = gate_it(st[kSlotCav33L * N], r.linf, r.ltau, phi, dt);
+  }
   // the Markov scheme after the gates, by one linearised backward-Euler step
   if (x & BC_X_NAVGRC) {
     Real kf[17], kb[17];
@@ -722,7 +776,7 @@ __device__ __noinline__ void ext_channels(Real* st, int N, const Real* P, Real v
                                           bool advance, Real& G, Real& I) {
   const uint32_t x = ext_mask(P);
   if (advance) ext_gates(st, N, P, x, v, ci, dt);
-  for (int code = BC_CUR_HCN2; code <= BC_CUR_CAV31; ++code) {
+  for (int code = BC_CUR_HCN2; code <= BC_CUR_CAV33; ++code) {
     Real g = Real(0);
     const Real i = ext_current(st, N, P, x, v, ci, eca, code, &g);
     G += g;
@@ -738,7 +792,8 @@ __device__ __noinline__ Real ext_ca_current(const Real* st, int N, const Real* P
   return ext_current(st, N, P, x, v, ci, eca, BC_CUR_CATHP, (Real*)nullptr) +
          ext_current(st, N, P, x, v, ci, eca, BC_CUR_CAHTRE, (Real*)nullptr) +
          ext_current(st, N, P, x, v, ci, eca, BC_CUR_CAN, (Real*)nullptr) +
-         ext_current(st, N, P, x, v, ci, eca, BC_CUR_CAV31, (Real*)nullptr);
+         ext_current(st, N, P, x, v, ci, eca, BC_CUR_CAV31, (Real*)nullptr) +
+         ext_current(st, N, P, x, v, ci, eca, BC_CUR_CAV33, (Real*)nullptr);
 }
 
 // Steady states of the extension channels' gates at v (HH.reset_state).
@@ -815,6 +870,11 @@ __device__ __forceinline__ void ext_steady(const Real* P, Real* st, int N, Real 
     const Cav31Rates<Real> r(v, P[BC_P_CAV31_QT]);
     st[kSlotCav31P * N] = r.pinf;
     st[kSlotCav31Q * N] = r.qinf;
+  }
+  if (x & BC_X_CAV33) {
+    const Cav33Rates<Real> r(v, P[BC_P_CAV33_VSH]);
+    st[kSlotCav33N * N] = r.ninf;
+    st[kSlotCav33L * N] = r.linf;
   }
   if (x & BC_X_NAVGRC) {  // the stationary distribution (reset_steady_state)
     Real kf[17], kb[17];

@@ -151,7 +151,26 @@ CHANNEL_DEFAULTS.update({
     "Ca_ZH2019_IO": dict(g_max=0.4, E=120.0, mMidV=-61.0, freeze_m_inf=1.0),  # calcium.py:4837
     # permeability in cm/s (calcium.py:1972)
     "Cav3p1_MA2020_GoC": dict(g_max=2.5e-4, V_sh=0.0, temp=_c2k(22.0), q10=3.0, temp_ref=_c2k(37.0)),
+    # permeability perm (cm/s) times g_scale (calcium.py:4033)
+    "Cav3p3_RI2021_SC": dict(perm=1.0e-4, g_scale=1.0e-5, temp=_c2k(36.0), V_sh=0.0),
 })
+
+
+def cav33_drive(V, ci, co, temp):
+    """The Cav3.3 GHK drive (calcium.py:89-97) with the model file's F = 96520, R = 8.3134
+    and T - 0.01 K; z = 2.  Returns (drive, d drive / dV per mV)."""
+    zf = 2.0 * 96520.0
+    k = zf / (8.3134 * (temp - 0.01)) * 1e-3
+    w = k * V
+    ep = np.exp(w)
+    num = co - ci * ep
+    den = ep - 1.0
+    small = np.abs(den) < 1e-6
+    safe = np.where(small, 1.0, den)
+    drive = np.where(small, -zf * num * (1.0 - w / 2.0), -zf * num * w / safe)
+    dd = np.where(small, -zf * k * (-ci * ep * (1.0 - w / 2.0) - num / 2.0),
+                  -zf * k * ((num - ci * ep * w) / safe - num * w * ep / safe ** 2))
+    return drive, dd
 
 
 def cav31_drive(V, ci, co, temp):
@@ -202,6 +221,7 @@ _VARIANTS = {
     # Cav3p1_MA2024_PC overrides nothing; the _Frozen classes hold the GHK drive out of the linearisation
     **{v: ("Cav3p1_MA2020_GoC", {}) for v in ("Cav3p1_MA2024_PC", "Cav3p1_MA2020_GoC_Frozen",
                                                "Cav3p1_MA2024_PC_Frozen")},
+    **{v: ("Cav3p3_RI2021_SC", {}) for v in ("Cav3p3_MA2024_PC", "Cav3p3_MA2024_PC_Frozen")},
     **{v: ("Cav3p2_RI2021_SC", {}) for v in ("Cav3p2_MA2025_BC", "Cav3p2_MA2024_PC")},
 }
 
@@ -659,6 +679,12 @@ def rates(name: str, V, p: dict, Ci=None):
         pt = np.where(V <= -90.0, 1.0, (1.0 + 1.0 / (np.exp((V + 40.0) / 9.0) + np.exp((V + 102.0) / -18.0))) / qt)
         return {"p": ("it", 1.0 / (1.0 + np.exp((V - -52.0) / -5.0)), pt),
                 "q": ("it", 1.0 / (1.0 + np.exp((V - -72.0) / 7.0)), (15.0 + 1.0 / np.exp((V + 32.0) / 7.0)) / qt)}
+    if name == "Cav3p3_RI2021_SC":  # calcium.py:4033-4255, on V - V_sh
+        x = V - p["V_sh"]
+        return {"n": ("it", 1.0 / (1.0 + np.exp(-(x - -41.5) / 6.2)),
+                      np.where(x > -60.0, 7.2 + 0.02 * np.exp(-x / 14.7), 0.875 * np.exp((x + 120.0) / 41.0))),
+                "l": ("it", 1.0 / (1.0 + np.exp(-(x - -69.8) / -6.1)),
+                      np.where(x > -60.0, 79.5 + 2.0 * np.exp(-x / 9.3), 260.0))}
     if name == "CaN_IS2008":  # calcium.py:108-220
         return {"p": ("it", 1.0 / (1.0 + np.exp(-(V + 43.0) / 5.2)),
                       2.7 / (np.exp(-(V + 55.0) / 15.0) + np.exp((V + 55.0) / 15.0)) + 1.6)}
@@ -722,6 +748,7 @@ _GATES = {  # (gate, power, phi-key)
     "CaN_IS2008": (("p", 1, "phi"),),
     "Ca_ZH2019_IO": (("h", 1, "phi"),),
     "Cav3p1_MA2020_GoC": (("p", 2, "phi"), ("q", 1, "phi")),
+    "Cav3p3_RI2021_SC": (("n", 2, "phi"), ("l", 1, "phi")),
 }
 _ION_OF = {"Na_Ba2002": "na", "KDR_Ba2002": "k", "CaL_IS2008": "ca", "CaT_HM1992": "ca",
            "K_Leak": "k", "AHP_De1994": "k", "Na_HH1952": "na", "K_HH1952": "k", "KM_RI2021_SC": "k",
@@ -735,7 +762,7 @@ _ION_OF = {"Na_Ba2002": "na", "KDR_Ba2002": "k", "CaL_IS2008": "ca", "CaT_HM1992
            "NaP_SU2015_DCN": "na", "Na_ZH2019_IO": "na", "fKdr_SU2015_DCN": "k", "sKdr_SU2015_DCN": "k",
            "Kdr_ZH2019_IO": "k", "CaT_HP1992": "ca", "CaHT_Re1993": "ca", "Kca3p1_MA2020_GoC": "k",
            "SK_SU2015_DCN": "k", "K_Kv_test": "k", "CaN_IS2008": "ca", "Nav_MA2020_GrC": "na",
-           "Cav3p1_MA2020_GoC": "ca"}
+           "Cav3p1_MA2020_GoC": "ca", "Cav3p3_RI2021_SC": "ca"}
 # channels with their own reversal potential (HHTypedNeuron root, not an ion)
 _OWN_E = ("HCN_HM1992", "HCN1_MA2020_GoC", "HCN1_MA2024_PC", "HCN2_MA2020_GoC", "HCN_SU2015_DCN", "HCN_ZH2019_IO",
           "CaL_SU2015_DCN", "CaN_IS2008", "Ca_ZH2019_IO")
@@ -788,8 +815,11 @@ def _resolve(table: dict, decl) -> dict:
         p["gbar_phi"] = 1.5 ** ((p["temp"] - _c2k(23.0)) / 10.0)
     if name == "CaN_IS2008":  # Gate("p", q10, temp_ref)
         p["phi"] = p["q10"] ** ((p["temp"] - p["temp_ref"]) / 10.0)
-    if name == "Cav3p1_MA2020_GoC":  # the _Frozen classes hold the GHK drive out of the linearisation
+    if name in ("Cav3p1_MA2020_GoC", "Cav3p3_RI2021_SC"):  # the _Frozen classes: the GHK drive out of the linearisation
         p["ghk_frozen"] = 1.0 if decl.class_name.endswith("_Frozen") else 0.0
+    if name == "Cav3p3_RI2021_SC":  # Gates q10 2.3 at 28 degC; g = g_scale perm
+        p["phi"] = 2.3 ** ((p["temp"] - _c2k(28.0)) / 10.0)
+        p["g_max"] = p["g_scale"] * p["perm"]
     if p.get("gnonspec", 0.0) != 0.0:
         raise ValueError("Kv1p5_MA2020_GrC's nonspecific current (gnonspec != 0) not restated")
     p.pop("gnonspec", None)
@@ -1260,6 +1290,12 @@ class OracleCell:
             return self.Ci_fixed
         return np.where(self.ca_dyn["mask"], self.Ci, self.Ci_fixed)
 
+    def _ghk(self, name, ch, pv):
+        """(drive, d drive / dV) of a GHK calcium channel at the point voltages."""
+        if name == "Cav3p1_MA2020_GoC":
+            return cav31_drive(pv, self._ci_for_channels(), self._co_for_channels(), ch["temp"])
+        return cav33_drive(pv - ch["V_sh"], self._ci_for_channels(), self._co_for_channels(), ch["temp"])
+
     def _co_for_channels(self):
         """Co of the calcium ion: the dynamic shell's, else the fixed ion's 2 mM
         (ion/calcium.py:121)."""
@@ -1311,8 +1347,8 @@ class OracleCell:
                 I = I + geff * f * (E - pv)
                 dI = dI + geff * (df * (E - pv) - f)
                 continue
-            if name == "Cav3p1_MA2020_GoC":  # -g p^2 q drive(V, Ci, Co): dI/dV = -g p^2 q d drive / dV
-                drive, dd = cav31_drive(pv, self._ci_for_channels(), self._co_for_channels(), ch["temp"])
+            if name in ("Cav3p1_MA2020_GoC", "Cav3p3_RI2021_SC"):  # -g gates drive(V): dI/dV = -g gates d drive / dV
+                drive, dd = self._ghk(name, ch, pv)
                 I = I - geff * drive
                 dI = dI - np.where(ch["ghk_frozen"] != 0.0, 0.0, geff * dd)
                 continue
@@ -1346,9 +1382,8 @@ class OracleCell:
                 fac = fac * kv15_vfactor(pv)[0]
             if name == "Ca_ZH2019_IO":
                 fac = fac * caio_minf(pv, ch["mMidV"])[0]
-            if name == "Cav3p1_MA2020_GoC":
-                cur = -ch["g_max"] * fac * cav31_drive(pv, self._ci_for_channels(), self._co_for_channels(),
-                                                       ch["temp"])[0]
+            if name in ("Cav3p1_MA2020_GoC", "Cav3p3_RI2021_SC"):
+                cur = -ch["g_max"] * fac * self._ghk(name, ch, pv)[0]
                 return cur[:, pid] if np.ndim(cur) == 2 else np.full(self.P, float(cur))
             cur = ch["g_max"] * fac * (E - pv)
             return cur[:, pid] if np.ndim(cur) == 2 else np.full(self.P, float(cur))
@@ -1367,10 +1402,9 @@ class OracleCell:
         E_ca = self._E_ca()
         for name in self.chan:
             if _ION_OF.get(name) == "ca":
-                if name == "Cav3p1_MA2020_GoC":  # the GHK drive
+                if name in ("Cav3p1_MA2020_GoC", "Cav3p3_RI2021_SC"):  # the GHK drive
                     ch = self.chan[name]
-                    I = I - ch["g_max"] * self._gate_product(name) * cav31_drive(
-                        pv, self._ci_for_channels(), self._co_for_channels(), ch["temp"])[0]
+                    I = I - ch["g_max"] * self._gate_product(name) * self._ghk(name, ch, pv)[0]
                     continue
                 E = self.chan[name]["E"] if name in _OWN_E else E_ca  # CaN_IS2008 carries calcium in its own E
                 I = I + self.chan[name]["g_max"] * self._gate_product(name) * (E - pv)

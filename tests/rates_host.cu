@@ -76,6 +76,13 @@ extern "C" int bc_test_rates(int which, const double* v, int n, const double* pr
       case 40: { const CanRates<double> r(x); o[0] = r.pinf; o[1] = r.ptau; break; }
       case 41: { const CaioRates<double> r(x); o[0] = r.hinf; o[1] = r.htau; break; }
       case 42: { const Cav31Rates<double> r(x, prm[0]); o[0] = r.pinf; o[1] = r.ptau; o[2] = r.qinf; o[3] = r.qtau; break; }
+      case 44: { const Cav33Rates<double> r(x, prm[0]); o[0] = r.ninf; o[1] = r.ntau; o[2] = r.linf; o[3] = r.ltau; break; }
+      case 45: {  // the Cav3.3 GHK drive and its V-derivative at ci = prm[0], co = prm[1], T = prm[2]
+        double dd;
+        o[0] = cav33_drive(x, prm[0], prm[1], prm[2], dd);
+        o[1] = dd;
+        break;
+      }
       case 43: {  // the GHK drive and its V-derivative at ci = prm[0], co = prm[1], T = prm[2]
         double dd;
         o[0] = cav31_drive(x, prm[0], prm[1], prm[2], dd);

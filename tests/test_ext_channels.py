@@ -5,7 +5,7 @@ potassium / HCN classes, CaT_HP1992 and CaHT_Re1993 driving a CalciumDetailed sh
 calcium-gated Kca3p1 (and its BC / PC classes) and SK_SU2015_DCN, K_Kv_test, CaN_IS2008
 (Ci-modulated, carried by calcium in its own E), Ca_ZH2019_IO (and its Frozen class), and
 the Markov scheme Nav_MA2020_GrC, and Cav3p1 (GoC, PC and their _Frozen classes) with its
-GHK drive.
+GHK drive, and Cav3p3 (RI2021_SC, MA2024_PC and its _Frozen class) with its own.
 
 CPU: the records and their mask, the planner's check of the mask, and the owner
 tables (through the planner tests).  GPU: a DCN-like cell and an IO-like cell
@@ -189,12 +189,26 @@ def _cav31_cell(precision="f64"):
     c.paint(branch_in("type", "soma"), Channel("Na_Ba2002", g_max=120.0), Channel("KDR_Ba2002", g_max=40.0),
             Channel("Cav3p1_MA2024_PC_Frozen", g_max=1e-4))
     c.paint(branch_in("type", "dendrite"), Channel("Cav3p1_MA2020_GoC", g_max=2.5e-4),
+            Channel("Cav3p3_RI2021_SC", perm=2e-4, g_scale=1.0, V_sh=3.0),
             Ion("CalciumDetailed", C_rest=5e-5, tau=20.0, d=0.5, Ci_initializer=5e-5))
     c.place(RootLocation(0.5), CurrentClamp(delay=2.0, durations=20.0, amplitudes=0.3), StateProbe(name="v"),
             CurrentProbe(mechanism="Cav3p1_MA2024_PC_Frozen", name="i_cav_soma"))
     c.place(at(1, 0.5), StateProbe(name="v_dend"), MechanismProbe("CalciumDetailed", "Ci", name="ci"),
             MechanismProbe("Cav3p1_MA2020_GoC", "p", name="cav_p"), MechanismProbe("Cav3p1_MA2020_GoC", "q", name="cav_q"),
-            CurrentProbe(mechanism="Cav3p1_MA2020_GoC", name="i_cav"), CurrentProbe(ion="ca", name="i_ca"))
+            CurrentProbe(mechanism="Cav3p1_MA2020_GoC", name="i_cav"), CurrentProbe(ion="ca", name="i_ca"),
+            MechanismProbe("Cav3p3_RI2021_SC", "l", name="cav33_l"), CurrentProbe(mechanism="Cav3p3_RI2021_SC",
+                                                                                name="i_cav33"))
+    return c
+
+
+def _cav33_frozen_cell(precision="f64"):
+    soma = Branch.from_lengths(lengths=[20.0], radii=[10.0, 10.0], type="soma")
+    c = Cell(Morphology.from_root(soma, name="soma"), cv_policy=CVPerBranch(), precision=precision)
+    c.paint(AllRegion(), CableProperty(), Channel("IL", g_max=0.1, E=-65.0), Channel("Na_Ba2002", g_max=120.0),
+            Channel("KDR_Ba2002", g_max=40.0), Channel("Cav3p3_MA2024_PC_Frozen", perm=2e-4, g_scale=1.0),
+            Ion("CalciumDetailed", C_rest=5e-5, tau=20.0, d=0.5, Ci_initializer=5e-5))
+    c.place(RootLocation(0.5), CurrentClamp(delay=2.0, durations=20.0, amplitudes=0.3), StateProbe(name="v"),
+            MechanismProbe("CalciumDetailed", "Ci", name="ci"), CurrentProbe(ion="ca", name="i_ca"))
     return c
 
 
@@ -209,8 +223,8 @@ def test_kv15_grc_runs_on_the_pc_kernel():
 @pytest.mark.gpu
 @pytest.mark.parametrize("make,n", [(_dcn_cell, 1000), (_io_cell, 800), (_ca_cell, 1000), (_kca_cell, 1000),
                                     (_can_cell, 1000), (_can_cell_unfrozen, 1000), (_grc_cell, 800),
-                                    (_cav31_cell, 1000)],
-                         ids=["dcn", "io", "ca", "kca", "can", "can_unfrozen", "grc", "cav31"])
+                                    (_cav31_cell, 1000), (_cav33_frozen_cell, 1000)],
+                         ids=["dcn", "io", "ca", "kca", "can", "can_unfrozen", "grc", "cav31", "cav33_frozen"])
 def test_extension_cells_f64_match_oracle(native_lib, cuda_device, make, n):
     from braincell_gb300.runtime import Plan
 

@@ -34,7 +34,7 @@ CASES = {
     34: ("CaT_HP1992", ("V_sh",)), 35: ("CaHT_Re1993", ("V_sh",)), 36: ("CaL_SU2015_DCN", ()),
     37: ("Kca3p1_MA2020_GoC", ("Ci",)), 38: ("SK_SU2015_DCN", ("Ci",)),
     39: ("K_Kv_test", ("V_sh", "Ra", "Rb", "q", "v12")), 40: ("CaN_IS2008", ()), 41: ("Ca_ZH2019_IO", ()),
-    42: ("Cav3p1_MA2020_GoC", ("qt",)),
+    42: ("Cav3p1_MA2020_GoC", ("qt",)), 44: ("Cav3p3_RI2021_SC", ("V_sh",)),
 }
 
 
@@ -94,6 +94,8 @@ def test_kernel_rates_match_oracle(rates_lib, which, shift):
         ({0.0: 1e-4, 7.5: 0.007}[shift] if name == "SK_SU2015_DCN" else None)
     if name == "K_Kv_test":  # its removable singularity at V = V_sh + v12
         V = np.concatenate([V, p["V_sh"] + p["v12"] + np.array([0.0, 1e-7, -1e-7])])
+    if name == "Cav3p3_RI2021_SC":  # the -60 mV branch point of its time constants
+        V = np.concatenate([V, p["V_sh"] - 60.0 + np.array([0.0, 1e-9])])
     if name == "Cav3p1_MA2020_GoC":  # at a temperature off its reference, where qt != 1; the -90 mV branch point
         p["temp"] += shift
         p["qt"] = p["q10"] ** ((p["temp"] - p["temp_ref"]) / 10.0)
@@ -106,19 +108,21 @@ def test_kernel_rates_match_oracle(rates_lib, which, shift):
                                    err_msg=f"{name} rate column {k}")
 
 
+@pytest.mark.parametrize("which", [43, 45], ids=["cav3p1", "cav3p3"])
 @pytest.mark.parametrize("ci,co,temp", [(5e-5, 2.0, 295.15), (1e-3, 2.0, 310.15), (2.0, 2.0, 300.0)])
-def test_ghk_drive_matches_oracle(rates_lib, ci, co, temp):
-    # the Cav3.1 GHK drive and its V-derivative, across 0 mV (the small-|1 - e^-zeta| branch)
+def test_ghk_drive_matches_oracle(rates_lib, which, ci, co, temp):
+    # the Cav3.1 / Cav3.3 GHK drives and their V-derivatives, across 0 mV (the small branch)
+    fn, off = (O.cav31_drive, 0.04) if which == 43 else (O.cav33_drive, -0.01)
     V = np.concatenate([np.linspace(-100.0, 60.0, 1601), [0.0, 1e-7, -1e-7, 1e-4]])
-    got = _kernel(rates_lib, 43, V, [ci, co, temp + 0.04])  # the kernel takes the GHK temperature itself
-    drive, dd = O.cav31_drive(V, ci, co, temp)
+    got = _kernel(rates_lib, which, V, [ci, co, temp + off])  # the kernel takes the GHK temperature itself
+    drive, dd = fn(V, ci, co, temp)
     np.testing.assert_allclose(got[:, 0], drive, rtol=1e-12, atol=1e-9)
     np.testing.assert_allclose(got[:, 1], dd, rtol=1e-10, atol=1e-9)
     # the derivative against a central difference away from the branch switch
     h = 1e-4
     Vs = np.linspace(-90.0, 50.0, 141) + 0.37
-    fd = (O.cav31_drive(Vs + h, ci, co, temp)[0] - O.cav31_drive(Vs - h, ci, co, temp)[0]) / (2 * h)
-    np.testing.assert_allclose(O.cav31_drive(Vs, ci, co, temp)[1], fd, rtol=1e-6, atol=1e-6)
+    fd = (fn(Vs + h, ci, co, temp)[0] - fn(Vs - h, ci, co, temp)[0]) / (2 * h)
+    np.testing.assert_allclose(fn(Vs, ci, co, temp)[1], fd, rtol=1e-6, atol=1e-6)
 
 
 def test_unknown_structure_is_rejected(rates_lib):
