@@ -77,7 +77,9 @@ BC_X_CAIO = 1 << 19
 BC_X_NAVGRC = 1 << 20
 BC_X_CAV31 = 1 << 21
 BC_X_CAV33 = 1 << 22
-BC_X_ALL = 0x7FFFFF
+BC_X_CAV12 = 1 << 23
+BC_X_CAV13 = 1 << 24
+BC_X_ALL = 0x1FFFFFF
 
 BC_NPARAM = 160
 BC_P_INVCM = 0
@@ -233,6 +235,10 @@ BC_P_CAV33_PHI = 150
 BC_P_CAV33_TGHK = 151
 BC_P_CAV33_VSH = 152
 BC_P_CAV33_FREEZE = 153
+BC_P_CAV12_G = 154
+BC_P_CAV12_PHI = 155
+BC_P_CAV13_G = 156
+BC_P_CAV13_PHI = 157
 
 BC_ABI_VERSION = 500
 
@@ -303,7 +309,9 @@ BC_CUR_CAIO = 50
 BC_CUR_NAVGRC = 51
 BC_CUR_CAV31 = 52
 BC_CUR_CAV33 = 53
-BC_NCUR = 54
+BC_CUR_CAV12 = 54
+BC_CUR_CAV13 = 55
+BC_NCUR = 56
 
 BC_STATE_V = 0
 BC_STATE_NA_P = 1
@@ -385,7 +393,9 @@ BC_STATE_CAV31_P = 108
 BC_STATE_CAV31_Q = 109
 BC_STATE_CAV33_N = 110
 BC_STATE_CAV33_L = 111
-BC_NSTATE_VIEW = 112
+BC_STATE_CAV12_M = 112
+BC_STATE_CAV13_M = 115
+BC_NSTATE_VIEW = 118
 # the independent states of each Markov scheme, in view order (first appearance in
 # the scheme's transition list, the dependent state left out)
 MARKOV_STATES = {
@@ -471,6 +481,12 @@ STATE_NAMES = {
     "Cav3p1_q": BC_STATE_CAV31_Q,
     "Cav3p3_n": BC_STATE_CAV33_N,
     "Cav3p3_l": BC_STATE_CAV33_L,
+    "Cav1p2_m": BC_STATE_CAV12_M,
+    "Cav1p2_h": BC_STATE_CAV12_M + 1,
+    "Cav1p2_n": BC_STATE_CAV12_M + 2,
+    "Cav1p3_m": BC_STATE_CAV13_M,
+    "Cav1p3_h": BC_STATE_CAV13_M + 1,
+    "Cav1p3_n": BC_STATE_CAV13_M + 2,
 }
 for _cls, (_base, _names) in MARKOV_STATES.items():
     for _k, _n in enumerate(_names):

@@ -371,6 +371,9 @@ PROBE_STATES.update({
     ("Ca_ZH2019_IO", "h"): _abi.BC_STATE_CAIO_H,
     ("Cav3p1_MA2020_GoC", "p"): _abi.BC_STATE_CAV31_P, ("Cav3p1_MA2020_GoC", "q"): _abi.BC_STATE_CAV31_Q,
     ("Cav3p3_RI2021_SC", "n"): _abi.BC_STATE_CAV33_N, ("Cav3p3_RI2021_SC", "l"): _abi.BC_STATE_CAV33_L,
+    **{(c, g): base + k for c, base in (("Cav1p2_MA2020_GoC", _abi.BC_STATE_CAV12_M),
+                                        ("Cav1p3_MA2020_GoC", _abi.BC_STATE_CAV13_M))
+       for k, g in enumerate(("m", "h", "n"))},
 })
 for _cls, (_base, _names) in _abi.MARKOV_STATES.items():
     for _k, _n in enumerate(_names):
@@ -401,7 +404,7 @@ PROBE_CURRENTS = {
     "CaL_SU2015_DCN": _abi.BC_CUR_CALDCN, "Kca3p1_MA2020_GoC": _abi.BC_CUR_KCA31, "SK_SU2015_DCN": _abi.BC_CUR_SKDCN,
     "K_Kv_test": _abi.BC_CUR_KKV, "CaN_IS2008": _abi.BC_CUR_CAN, "Ca_ZH2019_IO": _abi.BC_CUR_CAIO,
     "Nav_MA2020_GrC": _abi.BC_CUR_NAVGRC, "Cav3p1_MA2020_GoC": _abi.BC_CUR_CAV31,
-    "Cav3p3_RI2021_SC": _abi.BC_CUR_CAV33,
+    "Cav3p3_RI2021_SC": _abi.BC_CUR_CAV33, "Cav1p2_MA2020_GoC": _abi.BC_CUR_CAV12, "Cav1p3_MA2020_GoC": _abi.BC_CUR_CAV13,
 }
 ION_CURRENTS = {"na": _abi.BC_CUR_ION_NA, "k": _abi.BC_CUR_ION_K, "ca": _abi.BC_CUR_ION_CA}
 

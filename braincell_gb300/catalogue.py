@@ -73,6 +73,8 @@ BC_P_EXT_MASK, their parameters after it; conductances in mS/cm^2):
 * ``Cav3p3_RI2021_SC`` -- channel/calcium.py:4033 (perm 1e-4 cm/s, g_scale 1e-5, temp 36 degC, V_sh 0; gates q10 2.3
   at 28 degC; GHK drive at temp - 0.01 K); Cav3p3_MA2024_PC repeats it and its _Frozen class holds the drive out of
   the linearisation
+* ``Cav1p2_MA2020_GoC`` / ``Cav1p3_MA2020_GoC`` -- channel/calcium.py:1408, :1683 (g_max 0.2 / 0.005, temp 22 degC,
+  q10 1 at 22 degC; n_inf = kf / (kf + Ci)); their MA2025_BC classes repeat them
 * ``Nav_MA2020_GrC`` -- channel/sodium.py:1427 (g_max 13, temp 32 degC; phi 3^((T - 20 degC) / 10)): a Markov
   scheme on the Nav1.6 graph with its own rate constants
 * ``Ca_ZH2019_IO`` / ``_Frozen`` -- channel/calcium.py:4837 (g_max 0.4, E 120 mV, mMidV -61 mV, freeze_m_inf true;
@@ -198,6 +200,9 @@ CHANNELS: dict[str, dict[str, float]] = {
     "Cav3p1_MA2020_GoC": {"g_max": 2.5e-4, "V_sh": 0.0, "temp": T22, "q10": 3.0, "temp_ref": celsius2kelvin(37.0)},
     # permeability perm in cm/s times g_scale (calcium.py:4033); no g_max parameter
     "Cav3p3_RI2021_SC": {"perm": 1.0e-4, "g_scale": 1.0e-5, "temp": T36, "V_sh": 0.0},
+    # 0.0002 and 0.000005 S/cm^2 (calcium.py:1408, :1683); V_sh accepted, unused by the rates
+    "Cav1p2_MA2020_GoC": {"g_max": 0.2, "V_sh": 0.0, "temp": T22, "q10": 1.0, "temp_ref": T22},
+    "Cav1p3_MA2020_GoC": {"g_max": 0.005, "V_sh": 0.0, "temp": T22, "q10": 1.0, "temp_ref": T22},
 }
 # extension channels: class -> (BC_X_* bit, record entry of g_max, record entry of E or None)
 _EXT = {
@@ -224,6 +229,8 @@ _EXT = {
     "Nav_MA2020_GrC": (_abi.BC_X_NAVGRC, _abi.BC_P_NAVGRC_G, None),
     "Cav3p1_MA2020_GoC": (_abi.BC_X_CAV31, _abi.BC_P_CAV31_G, None),
     "Cav3p3_RI2021_SC": (_abi.BC_X_CAV33, _abi.BC_P_CAV33_G, None),
+    "Cav1p2_MA2020_GoC": (_abi.BC_X_CAV12, _abi.BC_P_CAV12_G, None),
+    "Cav1p3_MA2020_GoC": (_abi.BC_X_CAV13, _abi.BC_P_CAV13_G, None),
 }
 # Cav3p1 classes with the GHK drive frozen for the linearisation (calcium.py, the
 # _Frozen subclasses: the forward current is the base class's)
@@ -239,6 +246,8 @@ KINETIC_VARIANTS = {
     "CaHVA_MA2020_GoC": {"CaHVA_MA2020_GrC": {}},
     "Cav3p2_RI2021_SC": {v: {} for v in ("Cav3p2_MA2025_BC", "Cav3p2_MA2024_PC")},
     "Kca3p1_MA2020_GoC": {v: {} for v in ("Kca3p1_MA2025_BC", "Kca3p1_MA2024_PC")},
+    "Cav1p2_MA2020_GoC": {"Cav1p2_MA2025_BC": {}},
+    "Cav1p3_MA2020_GoC": {"Cav1p3_MA2025_BC": {}},
 }
 MARKOV_VARIANTS = {
     "Nav1p6_MA2020_GoC": ("Nav1p6_MA2024_PC", "Nav1p6_MA2025_BC", "Nav1p6_RI2021_SC"),
@@ -527,6 +536,9 @@ def region_record(mechs, cable: CableProperty) -> tuple[int, np.ndarray]:
                 rec[_abi.BC_P_CAV33_TGHK] = p["temp"] - 0.01  # the model file's Kelvin offset
                 rec[_abi.BC_P_CAV33_VSH] = p["V_sh"]
                 rec[_abi.BC_P_CAV33_FREEZE] = 1.0 if decl.class_name in _GHK_FROZEN else 0.0
+            elif name in ("Cav1p2_MA2020_GoC", "Cav1p3_MA2020_GoC"):
+                rec[_abi.BC_P_CAV12_PHI if name == "Cav1p2_MA2020_GoC" else _abi.BC_P_CAV13_PHI] = \
+                    q10_phi(p["q10"], p["temp"], p["temp_ref"])
             elif name == "Nav_MA2020_GrC":  # phi = 3^((T - 20 degC) / 10) (sodium.py, __init__)
                 rec[_abi.BC_P_NAVGRC_PHI] = q10_phi(3.0, p["temp"], celsius2kelvin(20.0))
             elif name == "Ca_ZH2019_IO":
@@ -550,7 +562,7 @@ def region_record(mechs, cable: CableProperty) -> tuple[int, np.ndarray]:
             rec[base + 3] = q10_phi(p["q10_q"], p["temp"], p["temp_ref_q"])
     ci_gated = bits & (_abi.BC_M_AHP | _abi.BC_M_KCA22 | _abi.BC_M_KCA11) or \
         int(rec[_abi.BC_P_EXT_MASK]) & (_abi.BC_X_KCA31 | _abi.BC_X_SKDCN | _abi.BC_X_CAN | _abi.BC_X_CAV31 |
-                                         _abi.BC_X_CAV33)
+                                         _abi.BC_X_CAV33 | _abi.BC_X_CAV12 | _abi.BC_X_CAV13)
     if int(rec[_abi.BC_P_EXT_MASK]) & (_abi.BC_X_CAV31 | _abi.BC_X_CAV33) and not bits & _abi.BC_M_CADET:
         rec[_abi.BC_P_CA_CO] = 2.0  # the GHK drive's Co: the fixed calcium ion's (ion/calcium.py:121)
     if ci_gated and not bits & _abi.BC_M_CADET:

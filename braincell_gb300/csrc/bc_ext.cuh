@@ -30,6 +30,8 @@
 //   Nav_MA2020_GrC         channel/sodium.py:1427-1666 (on the Markov solver of bc_mech.cuh)
 //   Cav3p1_MA2020_GoC      channel/calcium.py:1972-2202 (GHK drive, calcium.py:78-86)
 //   Cav3p3_RI2021_SC       channel/calcium.py:4033-4255 (GHK drive, calcium.py:89-97)
+//   Cav1p2_MA2020_GoC      channel/calcium.py:1408-1599
+//   Cav1p3_MA2020_GoC      channel/calcium.py:1683-1886
 // CaT_HP1992, CaHT_Re1993 and CaN_IS2008 (in its own E) carry calcium: their
 // step-start current joins the calcium shell's drive, as CaL's and CaT's do.  Kca3p1 and SK read Ci: the new Ci
 // of a dynamic calcium ion, else the fixed one (BC_P_CA_CI0), as AHP_De1994 does.
@@ -76,7 +78,9 @@ constexpr int kSlotCav31P = 109;
 constexpr int kSlotCav31Q = 110;
 constexpr int kSlotCav33N = 111;
 constexpr int kSlotCav33L = 112;
-constexpr int kNumSlotsExt = 113;
+constexpr int kSlotCav12 = 113;  // m, h, n
+constexpr int kSlotCav13 = 116;  // m, h, n
+constexpr int kNumSlotsExt = 119;
 
 // x / (1 - e^-x) = 1 / exprel(-x), finite at x = 0 (the reference's
 // _x_over_one_minus_exp_neg_stable, channel/sodium.py:50-55)
@@ -466,6 +470,33 @@ __host__ __device__ __forceinline__ Real cav33_drive(Real v, Real ci, Real co, R
   return -zf * num * w / den;
 }
 
+// Cav1p2 / Cav1p3_MA2020_GoC: m h n, ohmic in E_Ca; m_inf = 1 / (1 + e^((V - vm) / km)),
+// h_inf = VDI / (1 + e^((V - vh) / kh)) + 1 - VDI, n_inf = kf / (kf + Ci) (kf 5e-4 mM),
+// m_tau = 1 / (A k / exprel((V + c) / k) + B e^(V / 31.4)) (the reference's
+// A (V + c) / (e^((V + c) / k) - 1), finite at V = -c), h_tau 44.3 ms, n_tau 0.5 ms.
+struct Cav1Consts {
+  double vm, km, vh, kh, vdi, a, c, k, b;
+};
+// the two classes' constants: Cav1p2 (c12) and Cav1p3
+__host__ __device__ __forceinline__ Cav1Consts cav1_consts(bool c12) {
+  return c12 ? Cav1Consts{-8.9, -6.7, -55.0, 8.0, 0.17, 39800.0, 8.124, 9.005, 990.0}
+             : Cav1Consts{-40.0, -5.0, -37.0, 5.0, 1.0, 39800.0, 67.24, 15.005, 3500.0};
+}
+template <typename Real>
+struct Cav1Rates {
+  Real minf, mtau, hinf, ninf;
+  __host__ __device__ __forceinline__ Cav1Rates(Real v, Real ci, Cav1Consts q) {
+    minf = Real(1) / (Real(1) + aexp((v - Real(q.vm)) / Real(q.km)));
+    hinf = Real(q.vdi) / (Real(1) + aexp((v - Real(q.vh)) / Real(q.kh))) + (Real(1) - Real(q.vdi));
+    ninf = Real(0.0005) / (Real(0.0005) + ci);
+    const Real am = Real(q.a * q.k) / exprel((v + Real(q.c)) / Real(q.k));
+    const Real bm = Real(q.b) * aexp(v / Real(31.4));
+    mtau = Real(1) / (am + bm);
+  }
+};
+constexpr double kCav1TauH = 44.3;
+constexpr double kCav1TauN = 0.5;
+
 // The region's BC_X_* bits (an integer stored as a record real).
 template <typename Real>
 __host__ __device__ __forceinline__ uint32_t ext_mask(const Real* P) {
@@ -638,6 +669,16 @@ __device__ __forceinline__ Real ext_current(const Real* st, int N, const Real* P
         return -gp * drive;
       }
       return Real(0);
+    case BC_CUR_CAV12:
+    case BC_CUR_CAV13: {
+      const bool c12 = code == BC_CUR_CAV12;
+      if ((has = (x & (c12 ? BC_X_CAV12 : BC_X_CAV13)) != 0)) {
+        const int s0 = c12 ? kSlotCav12 : kSlotCav13;
+        g = P[c12 ? BC_P_CAV12_G : BC_P_CAV13_G] * st[s0 * N] * st[(s0 + 1) * N] * st[(s0 + 2) * N];
+        e = eca;
+      }
+      break;
+    }
     case BC_CUR_CAIO:
       if ((has = (x & BC_X_CAIO) != 0)) {
         Real m, dm;
@@ -760,6 +801,15 @@ __device__ __forceinline__ void ext_gates(Real* st, int N, const Real* P, uint32
     st[kSlotCav33N * N] = gate_it(st[kSlotCav33N * N], r.ninf, r.ntau, phi, dt);
     st[kSlotCav33L * N] = gate_it(st[kSlotCav33L * N], r.linf, r.ltau, phi, dt);
   }
+  for (int c = 0; c < 2; ++c) {
+    if (!(x & (c == 0 ? BC_X_CAV12 : BC_X_CAV13))) continue;
+    const int s0 = c == 0 ? kSlotCav12 : kSlotCav13;
+    const Real phi = P[c == 0 ? BC_P_CAV12_PHI : BC_P_CAV13_PHI];
+    const Cav1Rates<Real> r(v, ci, cav1_consts(c == 0));
+    st[s0 * N] = gate_it(st[s0 * N], r.minf, r.mtau, phi, dt);
+    st[(s0 + 1) * N] = gate_it(st[(s0 + 1) * N], r.hinf, Real(kCav1TauH), phi, dt);
+    st[(s0 + 2) * N] = gate_it(st[(s0 + 2) * N], r.ninf, Real(kCav1TauN), phi, dt);
+  }
   // the Markov scheme after the gates, by one linearised backward-Euler step
   if (x & BC_X_NAVGRC) {
     Real kf[17], kb[17];
@@ -776,7 +826,7 @@ __device__ __noinline__ void ext_channels(Real* st, int N, const Real* P, Real v
                                           bool advance, Real& G, Real& I) {
   const uint32_t x = ext_mask(P);
   if (advance) ext_gates(st, N, P, x, v, ci, dt);
-  for (int code = BC_CUR_HCN2; code <= BC_CUR_CAV33; ++code) {
+  for (int code = BC_CUR_HCN2; code <= BC_CUR_CAV13; ++code) {
     Real g = Real(0);
     const Real i = ext_current(st, N, P, x, v, ci, eca, code, &g);
     G += g;
@@ -793,7 +843,9 @@ __device__ __noinline__ Real ext_ca_current(const Real* st, int N, const Real* P
          ext_current(st, N, P, x, v, ci, eca, BC_CUR_CAHTRE, (Real*)nullptr) +
          ext_current(st, N, P, x, v, ci, eca, BC_CUR_CAN, (Real*)nullptr) +
          ext_current(st, N, P, x, v, ci, eca, BC_CUR_CAV31, (Real*)nullptr) +
-         ext_current(st, N, P, x, v, ci, eca, BC_CUR_CAV33, (Real*)nullptr);
+         ext_current(st, N, P, x, v, ci, eca, BC_CUR_CAV33, (Real*)nullptr) +
+         ext_current(st, N, P, x, v, ci, eca, BC_CUR_CAV12, (Real*)nullptr) +
+         ext_current(st, N, P, x, v, ci, eca, BC_CUR_CAV13, (Real*)nullptr);
 }
 
 // Steady states of the extension channels' gates at v (HH.reset_state).
@@ -875,6 +927,14 @@ __device__ __forceinline__ void ext_steady(const Real* P, Real* st, int N, Real 
     const Cav33Rates<Real> r(v, P[BC_P_CAV33_VSH]);
     st[kSlotCav33N * N] = r.ninf;
     st[kSlotCav33L * N] = r.linf;
+  }
+  for (int c = 0; c < 2; ++c) {  // at the reset Ci
+    if (!(x & (c == 0 ? BC_X_CAV12 : BC_X_CAV13))) continue;
+    const int s0 = c == 0 ? kSlotCav12 : kSlotCav13;
+    const Cav1Rates<Real> r(v, P[BC_P_CA_CI0], cav1_consts(c == 0));
+    st[s0 * N] = r.minf;
+    st[(s0 + 1) * N] = r.hinf;
+    st[(s0 + 2) * N] = r.ninf;
   }
   if (x & BC_X_NAVGRC) {  // the stationary distribution (reset_steady_state)
     Real kf[17], kb[17];

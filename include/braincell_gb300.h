@@ -114,7 +114,9 @@ typedef int32_t bc_status;
                                   (permeability g in cm/s; a calcium-ion current)            */
 #define BC_X_CAV33 (1u << 22)  /* channel/calcium.py:4033 Cav3p3_RI2021_SC n^2 l, GHK drive
                                   (g_scale x perm in cm/s; a calcium-ion current)            */
-#define BC_X_ALL 0x7FFFFFu
+#define BC_X_CAV12 (1u << 23)  /* channel/calcium.py:1408 Cav1p2_MA2020_GoC m h n(Ci), E_Ca    */
+#define BC_X_CAV13 (1u << 24)  /* channel/calcium.py:1683 Cav1p3_MA2020_GoC m h n(Ci), E_Ca    */
+#define BC_X_ALL 0x1FFFFFFu
 
 /* Per-region parameter record (double[BC_NPARAM]); index names below. */
 #define BC_NPARAM 160
@@ -272,7 +274,11 @@ typedef int32_t bc_status;
 #define BC_P_CAV33_TGHK 151 /* the GHK temperature T - 0.01 K                       */
 #define BC_P_CAV33_VSH 152
 #define BC_P_CAV33_FREEZE 153 /* 1: the drive held out of the linearisation (Frozen) */
-/* 154 .. 159: reserved for further extension channels (0) */
+#define BC_P_CAV12_G 154
+#define BC_P_CAV12_PHI 155  /* q10^((T - temp_ref) / 10)                            */
+#define BC_P_CAV13_G 156
+#define BC_P_CAV13_PHI 157
+/* 158, 159: reserved for further extension channels (0) */
 
 /* ------------------------------------------------------------------ batch spec */
 /*
@@ -438,7 +444,7 @@ const char* bc_last_error(void);
  * HH and calcium channels (BC_M_KV34 .. CAV32, a 96-entry parameter record, state
  * views 51-65, BC_PROBE_CURRENT 128).  0.5.0: extension channels (BC_M_EXT with
  * BC_X_* bits in the record's BC_P_EXT_MASK, a 160-entry parameter record, state
- * views 66-111, current codes 31-53). */
+ * views 66-117, current codes 31-55). */
 #define BC_ABI_VERSION 500
 int32_t bc_version(void);
 /* Fill opts with defaults. */
@@ -576,7 +582,9 @@ bc_status bc_check(bc_plan_t plan, void* stream);
 #define BC_STATE_CAV31_Q 109
 #define BC_STATE_CAV33_N 110
 #define BC_STATE_CAV33_L 111
-#define BC_NSTATE_VIEW 112
+#define BC_STATE_CAV12_M 112 /* M, H, N: 112 .. 114 */
+#define BC_STATE_CAV13_M 115 /* M, H, N: 115 .. 117 */
+#define BC_NSTATE_VIEW 118
 /* Current probes (mech/_point.py CurrentProbe, _multi_compartment/probes.py:184-258):
    probe_field = BC_PROBE_CURRENT + one of the codes below records that current
    density (uA/cm^2, outward negative as g (E - V)) after the step.             */
@@ -635,7 +643,9 @@ bc_status bc_check(bc_plan_t plan, void* stream);
 #define BC_CUR_NAVGRC 51 /* Nav_MA2020_GrC         */
 #define BC_CUR_CAV31 52  /* Cav3p1_MA2020_GoC      */
 #define BC_CUR_CAV33 53  /* Cav3p3_RI2021_SC       */
-#define BC_NCUR 54
+#define BC_CUR_CAV12 54  /* Cav1p2_MA2020_GoC      */
+#define BC_CUR_CAV13 55  /* Cav1p3_MA2020_GoC      */
+#define BC_NCUR 56
 bc_status bc_state_download(bc_plan_t plan, int32_t which, double* out /* [n_cv] */, void* stream);
 /* Set the amplitude (nA) of every current-clamp pulse of the batch spec, in spec
  * order (amp_nA[n_pulses]); times and locations are unchanged.  Takes effect from

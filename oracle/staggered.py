@@ -153,6 +153,8 @@ CHANNEL_DEFAULTS.update({
     "Cav3p1_MA2020_GoC": dict(g_max=2.5e-4, V_sh=0.0, temp=_c2k(22.0), q10=3.0, temp_ref=_c2k(37.0)),
     # permeability perm (cm/s) times g_scale (calcium.py:4033)
     "Cav3p3_RI2021_SC": dict(perm=1.0e-4, g_scale=1.0e-5, temp=_c2k(36.0), V_sh=0.0),
+    "Cav1p2_MA2020_GoC": dict(g_max=0.2, V_sh=0.0, temp=_c2k(22.0), q10=1.0, temp_ref=_c2k(22.0)),  # calcium.py:1408
+    "Cav1p3_MA2020_GoC": dict(g_max=0.005, V_sh=0.0, temp=_c2k(22.0), q10=1.0, temp_ref=_c2k(22.0)),  # :1683
 })
 
 
@@ -222,6 +224,7 @@ _VARIANTS = {
     **{v: ("Cav3p1_MA2020_GoC", {}) for v in ("Cav3p1_MA2024_PC", "Cav3p1_MA2020_GoC_Frozen",
                                                "Cav3p1_MA2024_PC_Frozen")},
     **{v: ("Cav3p3_RI2021_SC", {}) for v in ("Cav3p3_MA2024_PC", "Cav3p3_MA2024_PC_Frozen")},
+    "Cav1p2_MA2025_BC": ("Cav1p2_MA2020_GoC", {}), "Cav1p3_MA2025_BC": ("Cav1p3_MA2020_GoC", {}),
     **{v: ("Cav3p2_RI2021_SC", {}) for v in ("Cav3p2_MA2025_BC", "Cav3p2_MA2024_PC")},
 }
 
@@ -685,6 +688,17 @@ def rates(name: str, V, p: dict, Ci=None):
                       np.where(x > -60.0, 7.2 + 0.02 * np.exp(-x / 14.7), 0.875 * np.exp((x + 120.0) / 41.0))),
                 "l": ("it", 1.0 / (1.0 + np.exp(-(x - -69.8) / -6.1)),
                       np.where(x > -60.0, 79.5 + 2.0 * np.exp(-x / 9.3), 260.0))}
+    if name in ("Cav1p2_MA2020_GoC", "Cav1p3_MA2020_GoC"):  # calcium.py:1408-1599, :1683-1886
+        ci = np.asarray(Ci, dtype=float) * np.ones_like(V)
+        one = np.ones_like(V)
+        if name == "Cav1p2_MA2020_GoC":
+            minf, vdi, hinf_x = 1.0 / (1.0 + np.exp((V + 8.9) / -6.7)), 0.17, np.exp((V + 55.0) / 8.0)
+            am, bm = 39800.0 * 9.005 / exprel((V + 8.124) / 9.005), 990.0 * np.exp(V / 31.4)
+        else:
+            minf, vdi, hinf_x = 1.0 / (np.exp((V - -40.0) / -5.0) + 1.0), 1.0, np.exp((V - -37.0) / 5.0)
+            am, bm = 39800.0 * 15.005 / exprel((V + 67.24) / 15.005), 3500.0 * np.exp(V / 31.4)
+        return {"m": ("it", minf, 1.0 / (am + bm)), "h": ("it", vdi / (1.0 + hinf_x) + (1.0 - vdi), 44.3 * one),
+                "n": ("it", 0.0005 / (0.0005 + ci), 0.5 * one)}
     if name == "CaN_IS2008":  # calcium.py:108-220
         return {"p": ("it", 1.0 / (1.0 + np.exp(-(V + 43.0) / 5.2)),
                       2.7 / (np.exp(-(V + 55.0) / 15.0) + np.exp((V + 55.0) / 15.0)) + 1.6)}
@@ -749,6 +763,8 @@ _GATES = {  # (gate, power, phi-key)
     "Ca_ZH2019_IO": (("h", 1, "phi"),),
     "Cav3p1_MA2020_GoC": (("p", 2, "phi"), ("q", 1, "phi")),
     "Cav3p3_RI2021_SC": (("n", 2, "phi"), ("l", 1, "phi")),
+    "Cav1p2_MA2020_GoC": (("m", 1, "phi"), ("h", 1, "phi"), ("n", 1, "phi")),
+    "Cav1p3_MA2020_GoC": (("m", 1, "phi"), ("h", 1, "phi"), ("n", 1, "phi")),
 }
 _ION_OF = {"Na_Ba2002": "na", "KDR_Ba2002": "k", "CaL_IS2008": "ca", "CaT_HM1992": "ca",
            "K_Leak": "k", "AHP_De1994": "k", "Na_HH1952": "na", "K_HH1952": "k", "KM_RI2021_SC": "k",
@@ -762,7 +778,7 @@ _ION_OF = {"Na_Ba2002": "na", "KDR_Ba2002": "k", "CaL_IS2008": "ca", "CaT_HM1992
            "NaP_SU2015_DCN": "na", "Na_ZH2019_IO": "na", "fKdr_SU2015_DCN": "k", "sKdr_SU2015_DCN": "k",
            "Kdr_ZH2019_IO": "k", "CaT_HP1992": "ca", "CaHT_Re1993": "ca", "Kca3p1_MA2020_GoC": "k",
            "SK_SU2015_DCN": "k", "K_Kv_test": "k", "CaN_IS2008": "ca", "Nav_MA2020_GrC": "na",
-           "Cav3p1_MA2020_GoC": "ca", "Cav3p3_RI2021_SC": "ca"}
+           "Cav3p1_MA2020_GoC": "ca", "Cav3p3_RI2021_SC": "ca", "Cav1p2_MA2020_GoC": "ca", "Cav1p3_MA2020_GoC": "ca"}
 # channels with their own reversal potential (HHTypedNeuron root, not an ion)
 _OWN_E = ("HCN_HM1992", "HCN1_MA2020_GoC", "HCN1_MA2024_PC", "HCN2_MA2020_GoC", "HCN_SU2015_DCN", "HCN_ZH2019_IO",
           "CaL_SU2015_DCN", "CaN_IS2008", "Ca_ZH2019_IO")
@@ -813,7 +829,7 @@ def _resolve(table: dict, decl) -> dict:
     elif name == "HCN2_MA2020_GoC":  # gates q10 3 and the conductance Q10_diff 1.5, at 23 degC
         p["phi"] = 3.0 ** ((p["temp"] - _c2k(23.0)) / 10.0)
         p["gbar_phi"] = 1.5 ** ((p["temp"] - _c2k(23.0)) / 10.0)
-    if name == "CaN_IS2008":  # Gate("p", q10, temp_ref)
+    if name in ("CaN_IS2008", "Cav1p2_MA2020_GoC", "Cav1p3_MA2020_GoC"):  # Gates (q10, temp_ref)
         p["phi"] = p["q10"] ** ((p["temp"] - p["temp_ref"]) / 10.0)
     if name in ("Cav3p1_MA2020_GoC", "Cav3p3_RI2021_SC"):  # the _Frozen classes: the GHK drive out of the linearisation
         p["ghk_frozen"] = 1.0 if decl.class_name.endswith("_Frozen") else 0.0

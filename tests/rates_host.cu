@@ -76,6 +76,12 @@ extern "C" int bc_test_rates(int which, const double* v, int n, const double* pr
       case 40: { const CanRates<double> r(x); o[0] = r.pinf; o[1] = r.ptau; break; }
       case 41: { const CaioRates<double> r(x); o[0] = r.hinf; o[1] = r.htau; break; }
       case 42: { const Cav31Rates<double> r(x, prm[0]); o[0] = r.pinf; o[1] = r.ptau; o[2] = r.qinf; o[3] = r.qtau; break; }
+      case 46:
+      case 47: {  // Cav1p2 / Cav1p3 at Ci = prm[0]: (m_inf, m_tau, h_inf, h_tau, n_inf, n_tau)
+        const Cav1Rates<double> r(x, prm[0], cav1_consts(which == 46));
+        o[0] = r.minf; o[1] = r.mtau; o[2] = r.hinf; o[3] = kCav1TauH; o[4] = r.ninf; o[5] = kCav1TauN;
+        break;
+      }
       case 44: { const Cav33Rates<double> r(x, prm[0]); o[0] = r.ninf; o[1] = r.ntau; o[2] = r.linf; o[3] = r.ltau; break; }
       case 45: {  // the Cav3.3 GHK drive and its V-derivative at ci = prm[0], co = prm[1], T = prm[2]
         double dd;

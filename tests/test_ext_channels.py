@@ -5,7 +5,8 @@ potassium / HCN classes, CaT_HP1992 and CaHT_Re1993 driving a CalciumDetailed sh
 calcium-gated Kca3p1 (and its BC / PC classes) and SK_SU2015_DCN, K_Kv_test, CaN_IS2008
 (Ci-modulated, carried by calcium in its own E), Ca_ZH2019_IO (and its Frozen class), and
 the Markov scheme Nav_MA2020_GrC, and Cav3p1 (GoC, PC and their _Frozen classes) with its
-GHK drive, and Cav3p3 (RI2021_SC, MA2024_PC and its _Frozen class) with its own.
+GHK drive, Cav3p3 (RI2021_SC, MA2024_PC and its _Frozen class) with its own, and the
+Ci-inactivated Cav1p2 / Cav1p3 (and their BC classes).
 
 CPU: the records and their mask, the planner's check of the mask, and the owner
 tables (through the planner tests).  GPU: a DCN-like cell and an IO-like cell
@@ -187,9 +188,9 @@ def _cav31_cell(precision="f64"):
     # the soma: the Frozen class on the fixed calcium ion; the dendrite: the GHK drive in
     # the linearisation, on a CalciumDetailed shell that it fills
     c.paint(branch_in("type", "soma"), Channel("Na_Ba2002", g_max=120.0), Channel("KDR_Ba2002", g_max=40.0),
-            Channel("Cav3p1_MA2024_PC_Frozen", g_max=1e-4))
+            Channel("Cav3p1_MA2024_PC_Frozen", g_max=1e-4), Channel("Cav1p3_MA2025_BC", g_max=0.3))
     c.paint(branch_in("type", "dendrite"), Channel("Cav3p1_MA2020_GoC", g_max=2.5e-4),
-            Channel("Cav3p3_RI2021_SC", perm=2e-4, g_scale=1.0, V_sh=3.0),
+            Channel("Cav3p3_RI2021_SC", perm=2e-4, g_scale=1.0, V_sh=3.0), Channel("Cav1p2_MA2020_GoC", g_max=0.5),
             Ion("CalciumDetailed", C_rest=5e-5, tau=20.0, d=0.5, Ci_initializer=5e-5))
     c.place(RootLocation(0.5), CurrentClamp(delay=2.0, durations=20.0, amplitudes=0.3), StateProbe(name="v"),
             CurrentProbe(mechanism="Cav3p1_MA2024_PC_Frozen", name="i_cav_soma"))
@@ -197,7 +198,9 @@ def _cav31_cell(precision="f64"):
             MechanismProbe("Cav3p1_MA2020_GoC", "p", name="cav_p"), MechanismProbe("Cav3p1_MA2020_GoC", "q", name="cav_q"),
             CurrentProbe(mechanism="Cav3p1_MA2020_GoC", name="i_cav"), CurrentProbe(ion="ca", name="i_ca"),
             MechanismProbe("Cav3p3_RI2021_SC", "l", name="cav33_l"), CurrentProbe(mechanism="Cav3p3_RI2021_SC",
-                                                                                name="i_cav33"))
+                                                                                name="i_cav33"),
+            MechanismProbe("Cav1p2_MA2020_GoC", "n", name="cav12_n"), CurrentProbe(mechanism="Cav1p2_MA2020_GoC",
+                                                                                 name="i_cav12"))
     return c
 
 

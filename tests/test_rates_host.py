@@ -35,6 +35,7 @@ CASES = {
     37: ("Kca3p1_MA2020_GoC", ("Ci",)), 38: ("SK_SU2015_DCN", ("Ci",)),
     39: ("K_Kv_test", ("V_sh", "Ra", "Rb", "q", "v12")), 40: ("CaN_IS2008", ()), 41: ("Ca_ZH2019_IO", ()),
     42: ("Cav3p1_MA2020_GoC", ("qt",)), 44: ("Cav3p3_RI2021_SC", ("V_sh",)),
+    46: ("Cav1p2_MA2020_GoC", ("Ci",)), 47: ("Cav1p3_MA2020_GoC", ("Ci",)),
 }
 
 
@@ -91,7 +92,10 @@ def test_kernel_rates_match_oracle(rates_lib, which, shift):
         V = np.concatenate([V, p["V_sh"] + np.array([13.0, 15.0, 40.0, -5.0, -63.0, -70.0, -80.0, -10.0])])
     # the calcium-gated classes at a Ci on each side of their branch points (0.005, 0.01 mM)
     p["Ci"] = {0.0: 2e-3, 7.5: 0.012}[shift] if name == "Kca3p1_MA2020_GoC" else \
-        ({0.0: 1e-4, 7.5: 0.007}[shift] if name == "SK_SU2015_DCN" else None)
+        ({0.0: 1e-4, 7.5: 0.007}[shift] if name in ("SK_SU2015_DCN", "Cav1p2_MA2020_GoC", "Cav1p3_MA2020_GoC")
+         else None)
+    if name in ("Cav1p2_MA2020_GoC", "Cav1p3_MA2020_GoC"):  # m_alpha's removable singularity at V = -c
+        V = np.concatenate([V, [-8.124, -67.24, -8.124 + 1e-7]])
     if name == "K_Kv_test":  # its removable singularity at V = V_sh + v12
         V = np.concatenate([V, p["V_sh"] + p["v12"] + np.array([0.0, 1e-7, -1e-7])])
     if name == "Cav3p3_RI2021_SC":  # the -60 mV branch point of its time constants
