@@ -79,9 +79,10 @@ BC_X_CAV31 = 1 << 21
 BC_X_CAV33 = 1 << 22
 BC_X_CAV12 = 1 << 23
 BC_X_CAV13 = 1 << 24
-BC_X_ALL = 0x1FFFFFF
+BC_X_CAV21 = 1 << 25
+BC_X_ALL = 0x3FFFFFF
 
-BC_NPARAM = 160
+BC_NPARAM = 164
 BC_P_INVCM = 0
 BC_P_VREST = 1
 BC_P_ENA = 2
@@ -239,6 +240,10 @@ BC_P_CAV12_G = 154
 BC_P_CAV12_PHI = 155
 BC_P_CAV13_G = 156
 BC_P_CAV13_PHI = 157
+BC_P_CAV21_G = 158
+BC_P_CAV21_VSH = 159
+BC_P_CAV21_PHI = 160
+BC_P_CAV21_TGHK = 161
 
 BC_ABI_VERSION = 500
 
@@ -311,7 +316,8 @@ BC_CUR_CAV31 = 52
 BC_CUR_CAV33 = 53
 BC_CUR_CAV12 = 54
 BC_CUR_CAV13 = 55
-BC_NCUR = 56
+BC_CUR_CAV21 = 56
+BC_NCUR = 57
 
 BC_STATE_V = 0
 BC_STATE_NA_P = 1
@@ -395,7 +401,8 @@ BC_STATE_CAV33_N = 110
 BC_STATE_CAV33_L = 111
 BC_STATE_CAV12_M = 112
 BC_STATE_CAV13_M = 115
-BC_NSTATE_VIEW = 118
+BC_STATE_CAV21_M = 118
+BC_NSTATE_VIEW = 119
 # the independent states of each Markov scheme, in view order (first appearance in
 # the scheme's transition list, the dependent state left out)
 MARKOV_STATES = {
@@ -487,6 +494,7 @@ STATE_NAMES = {
     "Cav1p3_m": BC_STATE_CAV13_M,
     "Cav1p3_h": BC_STATE_CAV13_M + 1,
     "Cav1p3_n": BC_STATE_CAV13_M + 2,
+    "Cav2p1_m": BC_STATE_CAV21_M,
 }
 for _cls, (_base, _names) in MARKOV_STATES.items():
     for _k, _n in enumerate(_names):

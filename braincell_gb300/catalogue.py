@@ -75,6 +75,9 @@ BC_P_EXT_MASK, their parameters after it; conductances in mS/cm^2):
   the linearisation
 * ``Cav1p2_MA2020_GoC`` / ``Cav1p3_MA2020_GoC`` -- channel/calcium.py:1408, :1683 (g_max 0.2 / 0.005, temp 22 degC,
   q10 1 at 22 degC; n_inf = kf / (kf + Ci)); their MA2025_BC classes repeat them
+* ``Cav2p1_RI2021_SC`` -- channel/calcium.py:2767 (permeability g_max 2.2e-4 cm/s, V_sh 0, temp 23 degC; gate q10 3 at
+  23 degC; the shared GHK drive of channel/_base.py:47); the MA2024_PC and MA2025_BC classes repeat it (their _Frozen
+  classes, on another GHK helper, are not built)
 * ``Nav_MA2020_GrC`` -- channel/sodium.py:1427 (g_max 13, temp 32 degC; phi 3^((T - 20 degC) / 10)): a Markov
   scheme on the Nav1.6 graph with its own rate constants
 * ``Ca_ZH2019_IO`` / ``_Frozen`` -- channel/calcium.py:4837 (g_max 0.4, E 120 mV, mMidV -61 mV, freeze_m_inf true;
@@ -203,6 +206,8 @@ CHANNELS: dict[str, dict[str, float]] = {
     # 0.0002 and 0.000005 S/cm^2 (calcium.py:1408, :1683); V_sh accepted, unused by the rates
     "Cav1p2_MA2020_GoC": {"g_max": 0.2, "V_sh": 0.0, "temp": T22, "q10": 1.0, "temp_ref": T22},
     "Cav1p3_MA2020_GoC": {"g_max": 0.005, "V_sh": 0.0, "temp": T22, "q10": 1.0, "temp_ref": T22},
+    # a permeability in cm/s (calcium.py:2767: 2.2e-4 cm/s)
+    "Cav2p1_RI2021_SC": {"g_max": 2.2e-4, "V_sh": 0.0, "temp": celsius2kelvin(23.0)},
 }
 # extension channels: class -> (BC_X_* bit, record entry of g_max, record entry of E or None)
 _EXT = {
@@ -231,6 +236,7 @@ _EXT = {
     "Cav3p3_RI2021_SC": (_abi.BC_X_CAV33, _abi.BC_P_CAV33_G, None),
     "Cav1p2_MA2020_GoC": (_abi.BC_X_CAV12, _abi.BC_P_CAV12_G, None),
     "Cav1p3_MA2020_GoC": (_abi.BC_X_CAV13, _abi.BC_P_CAV13_G, None),
+    "Cav2p1_RI2021_SC": (_abi.BC_X_CAV21, _abi.BC_P_CAV21_G, None),
 }
 # Cav3p1 classes with the GHK drive frozen for the linearisation (calcium.py, the
 # _Frozen subclasses: the forward current is the base class's)
@@ -248,6 +254,7 @@ KINETIC_VARIANTS = {
     "Kca3p1_MA2020_GoC": {v: {} for v in ("Kca3p1_MA2025_BC", "Kca3p1_MA2024_PC")},
     "Cav1p2_MA2020_GoC": {"Cav1p2_MA2025_BC": {}},
     "Cav1p3_MA2020_GoC": {"Cav1p3_MA2025_BC": {}},
+    "Cav2p1_RI2021_SC": {v: {} for v in ("Cav2p1_MA2024_PC", "Cav2p1_MA2025_BC")},
 }
 MARKOV_VARIANTS = {
     "Nav1p6_MA2020_GoC": ("Nav1p6_MA2024_PC", "Nav1p6_MA2025_BC", "Nav1p6_RI2021_SC"),
@@ -539,6 +546,10 @@ def region_record(mechs, cable: CableProperty) -> tuple[int, np.ndarray]:
             elif name in ("Cav1p2_MA2020_GoC", "Cav1p3_MA2020_GoC"):
                 rec[_abi.BC_P_CAV12_PHI if name == "Cav1p2_MA2020_GoC" else _abi.BC_P_CAV13_PHI] = \
                     q10_phi(p["q10"], p["temp"], p["temp_ref"])
+            elif name == "Cav2p1_RI2021_SC":  # Gate q10 3 at 23 degC; the shared GHK at temp
+                rec[_abi.BC_P_CAV21_VSH] = p["V_sh"]
+                rec[_abi.BC_P_CAV21_PHI] = q10_phi(3.0, p["temp"], celsius2kelvin(23.0))
+                rec[_abi.BC_P_CAV21_TGHK] = p["temp"]
             elif name == "Nav_MA2020_GrC":  # phi = 3^((T - 20 degC) / 10) (sodium.py, __init__)
                 rec[_abi.BC_P_NAVGRC_PHI] = q10_phi(3.0, p["temp"], celsius2kelvin(20.0))
             elif name == "Ca_ZH2019_IO":
@@ -562,8 +573,9 @@ def region_record(mechs, cable: CableProperty) -> tuple[int, np.ndarray]:
             rec[base + 3] = q10_phi(p["q10_q"], p["temp"], p["temp_ref_q"])
     ci_gated = bits & (_abi.BC_M_AHP | _abi.BC_M_KCA22 | _abi.BC_M_KCA11) or \
         int(rec[_abi.BC_P_EXT_MASK]) & (_abi.BC_X_KCA31 | _abi.BC_X_SKDCN | _abi.BC_X_CAN | _abi.BC_X_CAV31 |
-                                         _abi.BC_X_CAV33 | _abi.BC_X_CAV12 | _abi.BC_X_CAV13)
-    if int(rec[_abi.BC_P_EXT_MASK]) & (_abi.BC_X_CAV31 | _abi.BC_X_CAV33) and not bits & _abi.BC_M_CADET:
+                                         _abi.BC_X_CAV33 | _abi.BC_X_CAV12 | _abi.BC_X_CAV13 | _abi.BC_X_CAV21)
+    if int(rec[_abi.BC_P_EXT_MASK]) & (_abi.BC_X_CAV31 | _abi.BC_X_CAV33 | _abi.BC_X_CAV21) and \
+            not bits & _abi.BC_M_CADET:
         rec[_abi.BC_P_CA_CO] = 2.0  # the GHK drive's Co: the fixed calcium ion's (ion/calcium.py:121)
     if ci_gated and not bits & _abi.BC_M_CADET:
         # AHP and the Kca channels read Ci from the calcium ion; with a fixed Ca ion

@@ -32,6 +32,7 @@
 //   Cav3p3_RI2021_SC       channel/calcium.py:4033-4255 (GHK drive, calcium.py:89-97)
 //   Cav1p2_MA2020_GoC      channel/calcium.py:1408-1599
 //   Cav1p3_MA2020_GoC      channel/calcium.py:1683-1886
+//   Cav2p1_RI2021_SC       channel/calcium.py:2767-2953 (GHK drive, channel/_base.py:47)
 // CaT_HP1992, CaHT_Re1993 and CaN_IS2008 (in its own E) carry calcium: their
 // step-start current joins the calcium shell's drive, as CaL's and CaT's do.  Kca3p1 and SK read Ci: the new Ci
 // of a dynamic calcium ion, else the fixed one (BC_P_CA_CI0), as AHP_De1994 does.
@@ -80,7 +81,8 @@ constexpr int kSlotCav33N = 111;
 constexpr int kSlotCav33L = 112;
 constexpr int kSlotCav12 = 113;  // m, h, n
 constexpr int kSlotCav13 = 116;  // m, h, n
-constexpr int kNumSlotsExt = 119;
+constexpr int kSlotCav21M = 119;
+constexpr int kNumSlotsExt = 120;
 
 // x / (1 - e^-x) = 1 / exprel(-x), finite at x = 0 (the reference's
 // _x_over_one_minus_exp_neg_stable, channel/sodium.py:50-55)
@@ -418,22 +420,49 @@ struct Cav31Rates {
 // / (1 - e^-zeta), and z F (ci - co e^-zeta)(1 + zeta / 2) where |1 - e^-zeta| < 1e-6.
 // With a permeability g in cm/s and ci, co in mM, -g drive is in uA/cm^2.  *dd
 // receives d drive / dV (per mV), the derivative of the branch taken.
+// The constant-field form z F zeta (ci - co e^-zeta) / (1 - e^-zeta) for z = 2 with
+// the Faraday and gas constants F, R; `le` takes the small branch at |1 - e^-zeta|
+// <= 1e-6 (the shared ghk_flux) rather than < 1e-6 (the Cav3.1 model file's helper).
 template <typename Real>
-__host__ __device__ __forceinline__ Real cav31_drive(Real v, Real ci, Real co, Real tghk, Real& dd) {
-  const Real zf = Real(2 * 9.6485e4);
-  const Real k = zf / (Real(8.3145) * tghk) * Real(1e-3);  // zeta per mV
+__host__ __device__ __forceinline__ Real ghk_drive2(Real v, Real ci, Real co, Real tghk, double F, double R, bool le,
+                                                   Real& dd) {
+  const Real zf = Real(2 * F);
+  const Real k = zf / (Real(R) * tghk) * Real(1e-3);  // zeta per mV
   const Real z = k * v;
   const Real em = aexp(-z);
   const Real num = ci - co * em;
   const Real den = Real(1) - em;
   const Real ad = den < Real(0) ? -den : den;
-  if (ad < Real(1e-6)) {
+  if (le ? ad <= Real(1e-6) : ad < Real(1e-6)) {
     dd = zf * k * (co * em * (Real(1) + z / Real(2)) + num / Real(2));
     return zf * num * (Real(1) + z / Real(2));
   }
   dd = zf * k * ((num + z * co * em) / den - z * num * em / (den * den));
   return zf * z * num / den;
 }
+template <typename Real>
+__host__ __device__ __forceinline__ Real cav31_drive(Real v, Real ci, Real co, Real tghk, Real& dd) {
+  return ghk_drive2(v, ci, co, tghk, 9.6485e4, 8.3145, false, dd);
+}
+// the shared ghk_flux (channel/_base.py:47) with brainunit's CODATA constants
+template <typename Real>
+__host__ __device__ __forceinline__ Real ghk_codata_drive(Real v, Real ci, Real co, Real temp, Real& dd) {
+  return ghk_drive2(v, ci, co, temp, kFaraday, kGasR, true, dd);
+}
+
+// Cav2p1_RI2021_SC: m^3 on V - V_sh; m_inf = 1 / (1 + e^(-(V + 29.458) / 8.429)), m_tau
+// 0.2702 + 1.1622 e^(-(V + 26.798)^2 / 164.19) at V >= -40 mV, else 0.6923 e^(V / 1089.372).
+template <typename Real>
+struct Cav21Rates {
+  Real minf, mtau;
+  __host__ __device__ __forceinline__ Cav21Rates(Real v, Real vsh) {
+    const Real x = v - vsh;
+    minf = Real(1) / (Real(1) + aexp(-(x + Real(29.458)) / Real(8.429)));
+    const Real y = x + Real(26.798);
+    mtau = x >= Real(-40) ? Real(0.2702) + Real(1.1622) * aexp(-(y * y) / Real(164.19))
+                          : Real(0.6923) * aexp(x / Real(1089.372));
+  }
+};
 
 // Cav3p3_RI2021_SC: n^2 l on V - V_sh; inf sigmoids, piecewise time constants at -60 mV.
 template <typename Real>
@@ -679,6 +708,16 @@ __device__ __forceinline__ Real ext_current(const Real* st, int N, const Real* P
       }
       break;
     }
+    case BC_CUR_CAV21:
+      if ((has = (x & BC_X_CAV21) != 0)) {
+        const Real m = st[kSlotCav21M * N];
+        const Real gp = P[BC_P_CAV21_G] * m * m * m;
+        Real dd;
+        const Real drive = ghk_codata_drive(v - P[BC_P_CAV21_VSH], ci, P[BC_P_CA_CO], P[BC_P_CAV21_TGHK], dd);
+        if (gv) *gv = gp * dd;
+        return -gp * drive;
+      }
+      return Real(0);
     case BC_CUR_CAIO:
       if ((has = (x & BC_X_CAIO) != 0)) {
         Real m, dm;
@@ -810,6 +849,10 @@ __device__ __forceinline__ void ext_gates(Real* st, int N, const Real* P, uint32
     st[(s0 + 1) * N] = gate_it(st[(s0 + 1) * N], r.hinf, Real(kCav1TauH), phi, dt);
     st[(s0 + 2) * N] = gate_it(st[(s0 + 2) * N], r.ninf, Real(kCav1TauN), phi, dt);
   }
+  if (x & BC_X_CAV21) {
+    const Cav21Rates<Real> r(v, P[BC_P_CAV21_VSH]);
+    st[kSlotCav21M * N] = gate_it(st[kSlotCav21M * N], r.minf, r.mtau, P[BC_P_CAV21_PHI], dt);
+  }
   // the Markov scheme after the gates, by one linearised backward-Euler step
   if (x & BC_X_NAVGRC) {
     Real kf[17], kb[17];
@@ -826,7 +869,7 @@ __device__ __noinline__ void ext_channels(Real* st, int N, const Real* P, Real v
                                           bool advance, Real& G, Real& I) {
   const uint32_t x = ext_mask(P);
   if (advance) ext_gates(st, N, P, x, v, ci, dt);
-  for (int code = BC_CUR_HCN2; code <= BC_CUR_CAV13; ++code) {
+  for (int code = BC_CUR_HCN2; code <= BC_CUR_CAV21; ++code) {
     Real g = Real(0);
     const Real i = ext_current(st, N, P, x, v, ci, eca, code, &g);
     G += g;
@@ -845,7 +888,8 @@ __device__ __noinline__ Real ext_ca_current(const Real* st, int N, const Real* P
          ext_current(st, N, P, x, v, ci, eca, BC_CUR_CAV31, (Real*)nullptr) +
          ext_current(st, N, P, x, v, ci, eca, BC_CUR_CAV33, (Real*)nullptr) +
          ext_current(st, N, P, x, v, ci, eca, BC_CUR_CAV12, (Real*)nullptr) +
-         ext_current(st, N, P, x, v, ci, eca, BC_CUR_CAV13, (Real*)nullptr);
+         ext_current(st, N, P, x, v, ci, eca, BC_CUR_CAV13, (Real*)nullptr) +
+         ext_current(st, N, P, x, v, ci, eca, BC_CUR_CAV21, (Real*)nullptr);
 }
 
 // Steady states of the extension channels' gates at v (HH.reset_state).
@@ -936,6 +980,7 @@ __device__ __forceinline__ void ext_steady(const Real* P, Real* st, int N, Real 
     st[(s0 + 1) * N] = r.hinf;
     st[(s0 + 2) * N] = r.ninf;
   }
+  if (x & BC_X_CAV21) st[kSlotCav21M * N] = Cav21Rates<Real>(v, P[BC_P_CAV21_VSH]).minf;
   if (x & BC_X_NAVGRC) {  // the stationary distribution (reset_steady_state)
     Real kf[17], kb[17];
     navgrc_rates(v, P[BC_P_NAVGRC_PHI], kf, kb);

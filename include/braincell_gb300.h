@@ -116,10 +116,12 @@ typedef int32_t bc_status;
                                   (g_scale x perm in cm/s; a calcium-ion current)            */
 #define BC_X_CAV12 (1u << 23)  /* channel/calcium.py:1408 Cav1p2_MA2020_GoC m h n(Ci), E_Ca    */
 #define BC_X_CAV13 (1u << 24)  /* channel/calcium.py:1683 Cav1p3_MA2020_GoC m h n(Ci), E_Ca    */
-#define BC_X_ALL 0x1FFFFFFu
+#define BC_X_CAV21 (1u << 25)  /* channel/calcium.py:2767 Cav2p1_RI2021_SC m^3, GHK drive (the
+                                  shared ghk_flux, channel/_base.py:47; g in cm/s)           */
+#define BC_X_ALL 0x3FFFFFFu
 
 /* Per-region parameter record (double[BC_NPARAM]); index names below. */
-#define BC_NPARAM 160
+#define BC_NPARAM 164
 #define BC_P_INVCM 0      /* 1 / membrane capacitance, cm^2/uF                 */
 #define BC_P_VREST 1      /* voltage used by reset (mV)                        */
 #define BC_P_ENA 2        /* fixed reversal potentials (mV)                    */
@@ -278,7 +280,11 @@ typedef int32_t bc_status;
 #define BC_P_CAV12_PHI 155  /* q10^((T - temp_ref) / 10)                            */
 #define BC_P_CAV13_G 156
 #define BC_P_CAV13_PHI 157
-/* 158, 159: reserved for further extension channels (0) */
+#define BC_P_CAV21_G 158    /* permeability (cm/s)                                  */
+#define BC_P_CAV21_VSH 159
+#define BC_P_CAV21_PHI 160  /* 3^((T - 23 degC) / 10)                               */
+#define BC_P_CAV21_TGHK 161 /* the GHK temperature T (K)                            */
+/* 162, 163: reserved (0) */
 
 /* ------------------------------------------------------------------ batch spec */
 /*
@@ -443,8 +449,8 @@ const char* bc_last_error(void);
  * 25-50), lane tiles (bc_plan_options.lane_cell_nodes, tile_order), the cerebellar
  * HH and calcium channels (BC_M_KV34 .. CAV32, a 96-entry parameter record, state
  * views 51-65, BC_PROBE_CURRENT 128).  0.5.0: extension channels (BC_M_EXT with
- * BC_X_* bits in the record's BC_P_EXT_MASK, a 160-entry parameter record, state
- * views 66-117, current codes 31-55). */
+ * BC_X_* bits in the record's BC_P_EXT_MASK, a 164-entry parameter record, state
+ * views 66-118, current codes 31-56). */
 #define BC_ABI_VERSION 500
 int32_t bc_version(void);
 /* Fill opts with defaults. */
@@ -584,7 +590,8 @@ bc_status bc_check(bc_plan_t plan, void* stream);
 #define BC_STATE_CAV33_L 111
 #define BC_STATE_CAV12_M 112 /* M, H, N: 112 .. 114 */
 #define BC_STATE_CAV13_M 115 /* M, H, N: 115 .. 117 */
-#define BC_NSTATE_VIEW 118
+#define BC_STATE_CAV21_M 118
+#define BC_NSTATE_VIEW 119
 /* Current probes (mech/_point.py CurrentProbe, _multi_compartment/probes.py:184-258):
    probe_field = BC_PROBE_CURRENT + one of the codes below records that current
    density (uA/cm^2, outward negative as g (E - V)) after the step.             */
@@ -645,7 +652,8 @@ bc_status bc_check(bc_plan_t plan, void* stream);
 #define BC_CUR_CAV33 53  /* Cav3p3_RI2021_SC       */
 #define BC_CUR_CAV12 54  /* Cav1p2_MA2020_GoC      */
 #define BC_CUR_CAV13 55  /* Cav1p3_MA2020_GoC      */
-#define BC_NCUR 56
+#define BC_CUR_CAV21 56  /* Cav2p1_RI2021_SC       */
+#define BC_NCUR 57
 bc_status bc_state_download(bc_plan_t plan, int32_t which, double* out /* [n_cv] */, void* stream);
 /* Set the amplitude (nA) of every current-clamp pulse of the batch spec, in spec
  * order (amp_nA[n_pulses]); times and locations are unchanged.  Takes effect from

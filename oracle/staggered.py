@@ -155,7 +155,26 @@ CHANNEL_DEFAULTS.update({
     "Cav3p3_RI2021_SC": dict(perm=1.0e-4, g_scale=1.0e-5, temp=_c2k(36.0), V_sh=0.0),
     "Cav1p2_MA2020_GoC": dict(g_max=0.2, V_sh=0.0, temp=_c2k(22.0), q10=1.0, temp_ref=_c2k(22.0)),  # calcium.py:1408
     "Cav1p3_MA2020_GoC": dict(g_max=0.005, V_sh=0.0, temp=_c2k(22.0), q10=1.0, temp_ref=_c2k(22.0)),  # :1683
+    "Cav2p1_RI2021_SC": dict(g_max=2.2e-4, V_sh=0.0, temp=_c2k(23.0)),  # calcium.py:2767 (cm/s)
 })
+
+
+def ghk_codata_drive(V, ci, co, temp):
+    """The shared ghk_flux (channel/_base.py:47) for z = 2 with the CODATA F and R of
+    the CalciumDetailed restatement (FARADAY, GAS_R), the small branch at
+    |1 - e^-zeta| <= 1e-6.  Returns (drive, d drive / dV per mV)."""
+    zf = 2.0 * FARADAY
+    k = zf / (GAS_R * temp) * 1e-3
+    z = k * V
+    em = np.exp(-z)
+    num = ci - co * em
+    den = 1.0 - em
+    small = np.abs(den) <= 1e-6
+    safe = np.where(small, 1.0, den)
+    drive = np.where(small, zf * num * (1.0 + z / 2.0), zf * z * num / safe)
+    dd = np.where(small, zf * k * (co * em * (1.0 + z / 2.0) + num / 2.0),
+                  zf * k * ((num + z * co * em) / safe - z * num * em / safe ** 2))
+    return drive, dd
 
 
 def cav33_drive(V, ci, co, temp):
@@ -225,6 +244,7 @@ _VARIANTS = {
                                                "Cav3p1_MA2024_PC_Frozen")},
     **{v: ("Cav3p3_RI2021_SC", {}) for v in ("Cav3p3_MA2024_PC", "Cav3p3_MA2024_PC_Frozen")},
     "Cav1p2_MA2025_BC": ("Cav1p2_MA2020_GoC", {}), "Cav1p3_MA2025_BC": ("Cav1p3_MA2020_GoC", {}),
+    **{v: ("Cav2p1_RI2021_SC", {}) for v in ("Cav2p1_MA2024_PC", "Cav2p1_MA2025_BC")},
     **{v: ("Cav3p2_RI2021_SC", {}) for v in ("Cav3p2_MA2025_BC", "Cav3p2_MA2024_PC")},
 }
 
@@ -688,6 +708,10 @@ def rates(name: str, V, p: dict, Ci=None):
                       np.where(x > -60.0, 7.2 + 0.02 * np.exp(-x / 14.7), 0.875 * np.exp((x + 120.0) / 41.0))),
                 "l": ("it", 1.0 / (1.0 + np.exp(-(x - -69.8) / -6.1)),
                       np.where(x > -60.0, 79.5 + 2.0 * np.exp(-x / 9.3), 260.0))}
+    if name == "Cav2p1_RI2021_SC":  # calcium.py:2767-2953, on V - V_sh
+        x = V - p["V_sh"]
+        mt = np.where(x >= -40.0, 0.2702 + 1.1622 * np.exp(-((x + 26.798) ** 2) / 164.19), 0.6923 * np.exp(x / 1089.372))
+        return {"m": ("it", 1.0 / (1.0 + np.exp(-(x - -29.458) / 8.429)), mt)}
     if name in ("Cav1p2_MA2020_GoC", "Cav1p3_MA2020_GoC"):  # calcium.py:1408-1599, :1683-1886
         ci = np.asarray(Ci, dtype=float) * np.ones_like(V)
         one = np.ones_like(V)
@@ -765,6 +789,7 @@ _GATES = {  # (gate, power, phi-key)
     "Cav3p3_RI2021_SC": (("n", 2, "phi"), ("l", 1, "phi")),
     "Cav1p2_MA2020_GoC": (("m", 1, "phi"), ("h", 1, "phi"), ("n", 1, "phi")),
     "Cav1p3_MA2020_GoC": (("m", 1, "phi"), ("h", 1, "phi"), ("n", 1, "phi")),
+    "Cav2p1_RI2021_SC": (("m", 3, "phi"),),
 }
 _ION_OF = {"Na_Ba2002": "na", "KDR_Ba2002": "k", "CaL_IS2008": "ca", "CaT_HM1992": "ca",
            "K_Leak": "k", "AHP_De1994": "k", "Na_HH1952": "na", "K_HH1952": "k", "KM_RI2021_SC": "k",
@@ -778,7 +803,10 @@ _ION_OF = {"Na_Ba2002": "na", "KDR_Ba2002": "k", "CaL_IS2008": "ca", "CaT_HM1992
            "NaP_SU2015_DCN": "na", "Na_ZH2019_IO": "na", "fKdr_SU2015_DCN": "k", "sKdr_SU2015_DCN": "k",
            "Kdr_ZH2019_IO": "k", "CaT_HP1992": "ca", "CaHT_Re1993": "ca", "Kca3p1_MA2020_GoC": "k",
            "SK_SU2015_DCN": "k", "K_Kv_test": "k", "CaN_IS2008": "ca", "Nav_MA2020_GrC": "na",
-           "Cav3p1_MA2020_GoC": "ca", "Cav3p3_RI2021_SC": "ca", "Cav1p2_MA2020_GoC": "ca", "Cav1p3_MA2020_GoC": "ca"}
+           "Cav3p1_MA2020_GoC": "ca", "Cav3p3_RI2021_SC": "ca", "Cav1p2_MA2020_GoC": "ca", "Cav1p3_MA2020_GoC": "ca",
+           "Cav2p1_RI2021_SC": "ca"}
+# calcium channels with a GHK current (-g gates drive) instead of an ohmic one
+_GHK = ("Cav3p1_MA2020_GoC", "Cav3p3_RI2021_SC", "Cav2p1_RI2021_SC")
 # channels with their own reversal potential (HHTypedNeuron root, not an ion)
 _OWN_E = ("HCN_HM1992", "HCN1_MA2020_GoC", "HCN1_MA2024_PC", "HCN2_MA2020_GoC", "HCN_SU2015_DCN", "HCN_ZH2019_IO",
           "CaL_SU2015_DCN", "CaN_IS2008", "Ca_ZH2019_IO")
@@ -829,6 +857,8 @@ def _resolve(table: dict, decl) -> dict:
     elif name == "HCN2_MA2020_GoC":  # gates q10 3 and the conductance Q10_diff 1.5, at 23 degC
         p["phi"] = 3.0 ** ((p["temp"] - _c2k(23.0)) / 10.0)
         p["gbar_phi"] = 1.5 ** ((p["temp"] - _c2k(23.0)) / 10.0)
+    if name == "Cav2p1_RI2021_SC":  # Gate q10 3 at 23 degC
+        p["phi"] = 3.0 ** ((p["temp"] - _c2k(23.0)) / 10.0)
     if name in ("CaN_IS2008", "Cav1p2_MA2020_GoC", "Cav1p3_MA2020_GoC"):  # Gates (q10, temp_ref)
         p["phi"] = p["q10"] ** ((p["temp"] - p["temp_ref"]) / 10.0)
     if name in ("Cav3p1_MA2020_GoC", "Cav3p3_RI2021_SC"):  # the _Frozen classes: the GHK drive out of the linearisation
@@ -1310,6 +1340,8 @@ class OracleCell:
         """(drive, d drive / dV) of a GHK calcium channel at the point voltages."""
         if name == "Cav3p1_MA2020_GoC":
             return cav31_drive(pv, self._ci_for_channels(), self._co_for_channels(), ch["temp"])
+        if name == "Cav2p1_RI2021_SC":
+            return ghk_codata_drive(pv - ch["V_sh"], self._ci_for_channels(), self._co_for_channels(), ch["temp"])
         return cav33_drive(pv - ch["V_sh"], self._ci_for_channels(), self._co_for_channels(), ch["temp"])
 
     def _co_for_channels(self):
@@ -1363,10 +1395,11 @@ class OracleCell:
                 I = I + geff * f * (E - pv)
                 dI = dI + geff * (df * (E - pv) - f)
                 continue
-            if name in ("Cav3p1_MA2020_GoC", "Cav3p3_RI2021_SC"):  # -g gates drive(V): dI/dV = -g gates d drive / dV
+            if name in _GHK:  # -g gates drive(V): dI/dV = -g gates d drive / dV
                 drive, dd = self._ghk(name, ch, pv)
                 I = I - geff * drive
-                dI = dI - np.where(ch["ghk_frozen"] != 0.0, 0.0, geff * dd)
+                frozen = ch.get("ghk_frozen", 0.0)  # Cav2p1 has no _Frozen class built
+                dI = dI - np.where(np.asarray(frozen) != 0.0, 0.0, geff * dd)
                 continue
             if name == "Ca_ZH2019_IO":  # g m_inf(V) h (E - V); a frozen m_inf is out of the derivative
                 m, dm = caio_minf(pv, ch["mMidV"])
@@ -1398,7 +1431,7 @@ class OracleCell:
                 fac = fac * kv15_vfactor(pv)[0]
             if name == "Ca_ZH2019_IO":
                 fac = fac * caio_minf(pv, ch["mMidV"])[0]
-            if name in ("Cav3p1_MA2020_GoC", "Cav3p3_RI2021_SC"):
+            if name in _GHK:
                 cur = -ch["g_max"] * fac * self._ghk(name, ch, pv)[0]
                 return cur[:, pid] if np.ndim(cur) == 2 else np.full(self.P, float(cur))
             cur = ch["g_max"] * fac * (E - pv)
@@ -1418,7 +1451,7 @@ class OracleCell:
         E_ca = self._E_ca()
         for name in self.chan:
             if _ION_OF.get(name) == "ca":
-                if name in ("Cav3p1_MA2020_GoC", "Cav3p3_RI2021_SC"):  # the GHK drive
+                if name in _GHK:  # the GHK drive
                     ch = self.chan[name]
                     I = I - ch["g_max"] * self._gate_product(name) * self._ghk(name, ch, pv)[0]
                     continue

@@ -6,7 +6,8 @@ calcium-gated Kca3p1 (and its BC / PC classes) and SK_SU2015_DCN, K_Kv_test, CaN
 (Ci-modulated, carried by calcium in its own E), Ca_ZH2019_IO (and its Frozen class), and
 the Markov scheme Nav_MA2020_GrC, and Cav3p1 (GoC, PC and their _Frozen classes) with its
 GHK drive, Cav3p3 (RI2021_SC, MA2024_PC and its _Frozen class) with its own, and the
-Ci-inactivated Cav1p2 / Cav1p3 (and their BC classes).
+Ci-inactivated Cav1p2 / Cav1p3 (and their BC classes), and Cav2p1 (SC, PC, BC) on the
+shared GHK drive.
 
 CPU: the records and their mask, the planner's check of the mask, and the owner
 tables (through the planner tests).  GPU: a DCN-like cell and an IO-like cell
@@ -209,9 +210,12 @@ def _cav33_frozen_cell(precision="f64"):
     c = Cell(Morphology.from_root(soma, name="soma"), cv_policy=CVPerBranch(), precision=precision)
     c.paint(AllRegion(), CableProperty(), Channel("IL", g_max=0.1, E=-65.0), Channel("Na_Ba2002", g_max=120.0),
             Channel("KDR_Ba2002", g_max=40.0), Channel("Cav3p3_MA2024_PC_Frozen", perm=2e-4, g_scale=1.0),
+            Channel("Cav2p1_MA2025_BC", g_max=2e-5, V_sh=-2.0),
             Ion("CalciumDetailed", C_rest=5e-5, tau=20.0, d=0.5, Ci_initializer=5e-5))
     c.place(RootLocation(0.5), CurrentClamp(delay=2.0, durations=20.0, amplitudes=0.3), StateProbe(name="v"),
-            MechanismProbe("CalciumDetailed", "Ci", name="ci"), CurrentProbe(ion="ca", name="i_ca"))
+            MechanismProbe("CalciumDetailed", "Ci", name="ci"), CurrentProbe(ion="ca", name="i_ca"),
+            MechanismProbe("Cav2p1_MA2025_BC", "m", name="cav21_m"), CurrentProbe(mechanism="Cav2p1_MA2025_BC",
+                                                                                name="i_cav21"))
     return c
 
 
