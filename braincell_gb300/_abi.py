@@ -244,6 +244,7 @@ BC_P_CAV21_G = 158
 BC_P_CAV21_VSH = 159
 BC_P_CAV21_PHI = 160
 BC_P_CAV21_TGHK = 161
+BC_P_EXT_MASK_HI = 162
 
 BC_ABI_VERSION = 500
 

@@ -331,6 +331,11 @@ _PQ_RECORDS = {
 }
 
 
+def ext_mask(rec) -> int:
+    """The BC_X_* bits a record lists (BC_P_EXT_MASK, and BC_P_EXT_MASK_HI for bits 24 up)."""
+    return int(rec[_abi.BC_P_EXT_MASK]) | (int(rec[_abi.BC_P_EXT_MASK_HI]) << 24)
+
+
 def kernel_class(name: str) -> str:
     """The class whose kernel a channel class runs on (itself unless same-form)."""
     return SAME_FORM.get(name, name)
@@ -509,7 +514,8 @@ def region_record(mechs, cable: CableProperty) -> tuple[int, np.ndarray]:
         elif name in _EXT:
             xbit, g_slot, e_slot = _EXT[name]
             bits |= _abi.BC_M_EXT
-            rec[_abi.BC_P_EXT_MASK] = float(int(rec[_abi.BC_P_EXT_MASK]) | xbit)
+            mask = ext_mask(rec) | xbit  # two record reals, each exact in FP32
+            rec[_abi.BC_P_EXT_MASK], rec[_abi.BC_P_EXT_MASK_HI] = float(mask & 0xFFFFFF), float(mask >> 24)
             g = p["g_scale"] * p["perm"] if name == "Cav3p3_RI2021_SC" else p["g_max"]
             if name == "HCN2_MA2020_GoC":  # the conductance's own Q10 1.5 and the gates' q10 3, at 23 degC
                 g *= q10_phi(1.5, p["temp"], celsius2kelvin(23.0))
@@ -572,9 +578,9 @@ def region_record(mechs, cable: CableProperty) -> tuple[int, np.ndarray]:
             rec[base + 2] = q10_phi(p["q10_p"], p["temp"], p["temp_ref_p"])
             rec[base + 3] = q10_phi(p["q10_q"], p["temp"], p["temp_ref_q"])
     ci_gated = bits & (_abi.BC_M_AHP | _abi.BC_M_KCA22 | _abi.BC_M_KCA11) or \
-        int(rec[_abi.BC_P_EXT_MASK]) & (_abi.BC_X_KCA31 | _abi.BC_X_SKDCN | _abi.BC_X_CAN | _abi.BC_X_CAV31 |
+        ext_mask(rec) & (_abi.BC_X_KCA31 | _abi.BC_X_SKDCN | _abi.BC_X_CAN | _abi.BC_X_CAV31 |
                                          _abi.BC_X_CAV33 | _abi.BC_X_CAV12 | _abi.BC_X_CAV13 | _abi.BC_X_CAV21)
-    if int(rec[_abi.BC_P_EXT_MASK]) & (_abi.BC_X_CAV31 | _abi.BC_X_CAV33 | _abi.BC_X_CAV21) and \
+    if ext_mask(rec) & (_abi.BC_X_CAV31 | _abi.BC_X_CAV33 | _abi.BC_X_CAV21) and \
             not bits & _abi.BC_M_CADET:
         rec[_abi.BC_P_CA_CO] = 2.0  # the GHK drive's Co: the fixed calcium ion's (ion/calcium.py:121)
     if ci_gated and not bits & _abi.BC_M_CADET:

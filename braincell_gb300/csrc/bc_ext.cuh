@@ -526,10 +526,10 @@ struct Cav1Rates {
 constexpr double kCav1TauH = 44.3;
 constexpr double kCav1TauN = 0.5;
 
-// The region's BC_X_* bits (an integer stored as a record real).
+// The region's BC_X_* bits: two record reals, each an integer below 2^24 (exact in FP32).
 template <typename Real>
 __host__ __device__ __forceinline__ uint32_t ext_mask(const Real* P) {
-  return uint32_t(P[BC_P_EXT_MASK]);
+  return uint32_t(P[BC_P_EXT_MASK]) | (uint32_t(P[BC_P_EXT_MASK_HI]) << 24);
 }
 
 // One extension channel's current at v with the node's stored gates (0 where the

@@ -74,7 +74,9 @@ namespace bc {
 constexpr uint64_t ext_bits(uint32_t x) { return uint64_t(x) << 32; }
 static inline uint64_t region_bits(const bc_batch_spec& s, int64_t k) {
   uint64_t b = s.region_mech[k];
-  if (b & BC_M_EXT) b |= ext_bits(uint32_t(s.region_params[k * BC_NPARAM + BC_P_EXT_MASK]));
+  if (b & BC_M_EXT)
+    b |= ext_bits(uint32_t(s.region_params[k * BC_NPARAM + BC_P_EXT_MASK]) |
+                  (uint32_t(s.region_params[k * BC_NPARAM + BC_P_EXT_MASK_HI]) << 24));
   return b;
 }
 
@@ -1322,9 +1324,14 @@ bc_status bc_plan_create(const bc_batch_spec* spec, const bc_plan_options* opts_
       return fail(BC_ERR_INVALID, "unknown mechanism bits in region_mech");
     }
     if (s.region_mech[k] & BC_M_EXT) {
-      // the record lists its extension channels: an integer of known BC_X_* bits, not 0
-      const double x = s.region_params[k * BC_NPARAM + BC_P_EXT_MASK];
-      if (!(x >= 1.0 && x <= double(BC_X_ALL)) || x != std::floor(x) || (uint32_t(x) & ~BC_X_ALL)) {
+      // the record lists its extension channels: integers of known BC_X_* bits (low 24 and
+      // the rest), not all 0
+      const double lo = s.region_params[k * BC_NPARAM + BC_P_EXT_MASK];
+      const double hi = s.region_params[k * BC_NPARAM + BC_P_EXT_MASK_HI];
+      const bool ints = lo >= 0.0 && lo < 16777216.0 && lo == std::floor(lo) && hi >= 0.0 && hi < 256.0 &&
+                        hi == std::floor(hi);
+      const uint32_t x = ints ? uint32_t(lo) | (uint32_t(hi) << 24) : 0u;
+      if (!ints || x == 0u || (x & ~BC_X_ALL)) {
         delete p;
         return fail(BC_ERR_INVALID, "a region with BC_M_EXT needs BC_X_* bits in its record's BC_P_EXT_MASK");
       }

@@ -79,8 +79,9 @@ typedef int32_t bc_status;
 #define BC_M_CAV23 (1u << 27)    /* channel/calcium.py:4672 Cav2p3_MA2020_GoC m^3 h, E_Ca             */
 #define BC_M_CAV32 (1u << 28)    /* channel/calcium.py:3636 Cav3p2_RI2021_SC m^2 h, E_Ca              */
 /* Extension channels (extra kernel variant): a region that carries any sets
- * BC_M_EXT and lists them as BC_X_* bits in its record entry BC_P_EXT_MASK (an
- * integer below 2^24, exact in FP32); their parameters follow that entry. */
+ * BC_M_EXT and lists them as BC_X_* bits in its record: bits 0-23 in BC_P_EXT_MASK,
+ * bits 24 and up in BC_P_EXT_MASK_HI (each an integer below 2^24, exact in FP32);
+ * their parameters follow BC_P_EXT_MASK. */
 #define BC_M_EXT (1u << 29)
 #define BC_M_ALL 0x3FFFFFFFu
 
@@ -218,7 +219,7 @@ typedef int32_t bc_status;
 #define BC_P_CAV32_G 93
 #define BC_P_CAV32_VSH 94
 /* 95: reserved (0) */
-#define BC_P_EXT_MASK 96    /* BC_X_* bits of the region's extension channels       */
+#define BC_P_EXT_MASK 96    /* BC_X_* bits 0-23 of the region's extension channels  */
 #define BC_P_HCN2_G 97      /* g_max x 1.5^((T - 23 degC) / 10)                     */
 #define BC_P_HCN2_E 98
 #define BC_P_HCN2_PHI 99    /* 3^((T - 23 degC) / 10)                               */
@@ -284,7 +285,8 @@ typedef int32_t bc_status;
 #define BC_P_CAV21_VSH 159
 #define BC_P_CAV21_PHI 160  /* 3^((T - 23 degC) / 10)                               */
 #define BC_P_CAV21_TGHK 161 /* the GHK temperature T (K)                            */
-/* 162, 163: reserved (0) */
+#define BC_P_EXT_MASK_HI 162 /* BC_X_* bits 24 and up, shifted down by 24           */
+/* 163: reserved (0) */
 
 /* ------------------------------------------------------------------ batch spec */
 /*

@@ -50,6 +50,10 @@ def test_extension_records():
     # the defaults of the reference classes, in mS/cm^2 (Kv3p3 0.005 S/cm^2, Kv1p5 0.13195e-3 S/cm^2)
     _, rec = catalogue.region_record([Channel("Kv3p3_MA2024_PC"), Channel("Kv1p5_MA2024_PC")], cable)
     assert rec[_abi.BC_P_KV33_G] == 5.0 and rec[_abi.BC_P_KV15_G] == pytest.approx(0.13195)
+    # bits 24 and up go to a second record entry, so that both stay exact in an FP32 record
+    _, rec = catalogue.region_record([Channel("HCN2_MA2020_GoC"), Channel("Cav2p1_RI2021_SC")], cable)
+    assert rec[_abi.BC_P_EXT_MASK] == _abi.BC_X_HCN2 and rec[_abi.BC_P_EXT_MASK_HI] == _abi.BC_X_CAV21 >> 24
+    assert catalogue.ext_mask(rec.astype(np.float32)) == _abi.BC_X_HCN2 | _abi.BC_X_CAV21
     # no extension channel: no mask, no bit
     bits, rec = catalogue.region_record([Channel("IL")], cable)
     assert not bits & _abi.BC_M_EXT and rec[_abi.BC_P_EXT_MASK] == 0.0
