@@ -262,8 +262,9 @@ def test_extension_cells_f64_match_oracle(native_lib, cuda_device, make, n):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("make", [_dcn_cell, _io_cell, _ca_cell, _kca_cell, _can_cell, _grc_cell, _cav31_cell],
-                         ids=["dcn", "io", "ca", "kca", "can", "grc", "cav31"])
+@pytest.mark.parametrize("make", [_dcn_cell, _io_cell, _ca_cell, _kca_cell, _can_cell, _grc_cell, _cav31_cell,
+                                  _cav33_frozen_cell],
+                         ids=["dcn", "io", "ca", "kca", "can", "grc", "cav31", "cav33_cav21"])
 def test_extension_cells_f32_meet_the_bar(native_lib, cuda_device, make):
     from braincell_gb300.runtime import Plan
 
