@@ -80,9 +80,11 @@ BC_X_CAV33 = 1 << 22
 BC_X_CAV12 = 1 << 23
 BC_X_CAV13 = 1 << 24
 BC_X_CAV21 = 1 << 25
-BC_X_ALL = 0x3FFFFFF
+BC_X_CAHVADCN = 1 << 26
+BC_X_CALVADCN = 1 << 27
+BC_X_ALL = 0xFFFFFFF
 
-BC_NPARAM = 164
+BC_NPARAM = 168
 BC_P_INVCM = 0
 BC_P_VREST = 1
 BC_P_ENA = 2
@@ -245,6 +247,10 @@ BC_P_CAV21_VSH = 159
 BC_P_CAV21_PHI = 160
 BC_P_CAV21_TGHK = 161
 BC_P_EXT_MASK_HI = 162
+BC_P_CAHVADCN_G = 163
+BC_P_CAHVADCN_T = 164
+BC_P_CALVADCN_G = 165
+BC_P_CALVADCN_T = 166
 
 BC_ABI_VERSION = 500
 
@@ -318,7 +324,9 @@ BC_CUR_CAV33 = 53
 BC_CUR_CAV12 = 54
 BC_CUR_CAV13 = 55
 BC_CUR_CAV21 = 56
-BC_NCUR = 57
+BC_CUR_CAHVADCN = 57
+BC_CUR_CALVADCN = 58
+BC_NCUR = 59
 
 BC_STATE_V = 0
 BC_STATE_NA_P = 1
@@ -403,7 +411,10 @@ BC_STATE_CAV33_L = 111
 BC_STATE_CAV12_M = 112
 BC_STATE_CAV13_M = 115
 BC_STATE_CAV21_M = 118
-BC_NSTATE_VIEW = 119
+BC_STATE_CAHVADCN_M = 119
+BC_STATE_CALVADCN_M = 120
+BC_STATE_CALVADCN_H = 121
+BC_NSTATE_VIEW = 122
 # the independent states of each Markov scheme, in view order (first appearance in
 # the scheme's transition list, the dependent state left out)
 MARKOV_STATES = {
@@ -496,6 +507,9 @@ STATE_NAMES = {
     "Cav1p3_h": BC_STATE_CAV13_M + 1,
     "Cav1p3_n": BC_STATE_CAV13_M + 2,
     "Cav2p1_m": BC_STATE_CAV21_M,
+    "CaHVADCN_m": BC_STATE_CAHVADCN_M,
+    "CaLVADCN_m": BC_STATE_CALVADCN_M,
+    "CaLVADCN_h": BC_STATE_CALVADCN_H,
 }
 for _cls, (_base, _names) in MARKOV_STATES.items():
     for _k, _n in enumerate(_names):

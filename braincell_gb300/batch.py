@@ -374,7 +374,8 @@ PROBE_STATES.update({
     **{(c, g): base + k for c, base in (("Cav1p2_MA2020_GoC", _abi.BC_STATE_CAV12_M),
                                         ("Cav1p3_MA2020_GoC", _abi.BC_STATE_CAV13_M))
        for k, g in enumerate(("m", "h", "n"))},
-    ("Cav2p1_RI2021_SC", "m"): _abi.BC_STATE_CAV21_M,
+    ("Cav2p1_RI2021_SC", "m"): _abi.BC_STATE_CAV21_M, ("CaHVA_SU2015_DCN", "m"): _abi.BC_STATE_CAHVADCN_M,
+    ("CaLVA_SU2015_DCN", "m"): _abi.BC_STATE_CALVADCN_M, ("CaLVA_SU2015_DCN", "h"): _abi.BC_STATE_CALVADCN_H,
 })
 for _cls, (_base, _names) in _abi.MARKOV_STATES.items():
     for _k, _n in enumerate(_names):
@@ -406,7 +407,8 @@ PROBE_CURRENTS = {
     "K_Kv_test": _abi.BC_CUR_KKV, "CaN_IS2008": _abi.BC_CUR_CAN, "Ca_ZH2019_IO": _abi.BC_CUR_CAIO,
     "Nav_MA2020_GrC": _abi.BC_CUR_NAVGRC, "Cav3p1_MA2020_GoC": _abi.BC_CUR_CAV31,
     "Cav3p3_RI2021_SC": _abi.BC_CUR_CAV33, "Cav1p2_MA2020_GoC": _abi.BC_CUR_CAV12, "Cav1p3_MA2020_GoC": _abi.BC_CUR_CAV13,
-    "Cav2p1_RI2021_SC": _abi.BC_CUR_CAV21,
+    "Cav2p1_RI2021_SC": _abi.BC_CUR_CAV21, "CaHVA_SU2015_DCN": _abi.BC_CUR_CAHVADCN,
+    "CaLVA_SU2015_DCN": _abi.BC_CUR_CALVADCN,
 }
 ION_CURRENTS = {"na": _abi.BC_CUR_ION_NA, "k": _abi.BC_CUR_ION_K, "ca": _abi.BC_CUR_ION_CA}
 

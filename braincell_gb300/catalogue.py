@@ -78,6 +78,9 @@ BC_P_EXT_MASK, their parameters after it; conductances in mS/cm^2):
 * ``Cav2p1_RI2021_SC`` -- channel/calcium.py:2767 (permeability g_max 2.2e-4 cm/s, V_sh 0, temp 23 degC; gate q10 3 at
   23 degC; the shared GHK drive of channel/_base.py:47); the MA2024_PC and MA2025_BC classes repeat it (their _Frozen
   classes, on another GHK helper, are not built)
+* ``CaHVA_SU2015_DCN`` / ``CaLVA_SU2015_DCN`` -- channel/calcium.py:924, :1221 (perm 7.5e-6 / 1 cm/s, temp 36 degC,
+  qdeltat 1; the model's drive (4.47814e6 V / T)(ci - co A) / 1000 / (1 - A), A = e^(-23.20764929 V / T); CaLVA on
+  CaL_SU2015_DCN's gates)
 * ``Nav_MA2020_GrC`` -- channel/sodium.py:1427 (g_max 13, temp 32 degC; phi 3^((T - 20 degC) / 10)): a Markov
   scheme on the Nav1.6 graph with its own rate constants
 * ``Ca_ZH2019_IO`` / ``_Frozen`` -- channel/calcium.py:4837 (g_max 0.4, E 120 mV, mMidV -61 mV, freeze_m_inf true;
@@ -208,6 +211,9 @@ CHANNELS: dict[str, dict[str, float]] = {
     "Cav1p3_MA2020_GoC": {"g_max": 0.005, "V_sh": 0.0, "temp": T22, "q10": 1.0, "temp_ref": T22},
     # a permeability in cm/s (calcium.py:2767: 2.2e-4 cm/s)
     "Cav2p1_RI2021_SC": {"g_max": 2.2e-4, "V_sh": 0.0, "temp": celsius2kelvin(23.0)},
+    # permeabilities in cm/s (calcium.py:924, 7.5e-6; the CaLVA class, 1.0)
+    "CaHVA_SU2015_DCN": {"perm": 7.5e-6, "temp": T36, "qdeltat": 1.0},
+    "CaLVA_SU2015_DCN": {"perm": 1.0, "temp": T36, "qdeltat": 1.0},
 }
 # extension channels: class -> (BC_X_* bit, record entry of g_max, record entry of E or None)
 _EXT = {
@@ -237,6 +243,8 @@ _EXT = {
     "Cav1p2_MA2020_GoC": (_abi.BC_X_CAV12, _abi.BC_P_CAV12_G, None),
     "Cav1p3_MA2020_GoC": (_abi.BC_X_CAV13, _abi.BC_P_CAV13_G, None),
     "Cav2p1_RI2021_SC": (_abi.BC_X_CAV21, _abi.BC_P_CAV21_G, None),
+    "CaHVA_SU2015_DCN": (_abi.BC_X_CAHVADCN, _abi.BC_P_CAHVADCN_G, None),
+    "CaLVA_SU2015_DCN": (_abi.BC_X_CALVADCN, _abi.BC_P_CALVADCN_G, None),
 }
 # Cav3p1 classes with the GHK drive frozen for the linearisation (calcium.py, the
 # _Frozen subclasses: the forward current is the base class's)
@@ -516,7 +524,8 @@ def region_record(mechs, cable: CableProperty) -> tuple[int, np.ndarray]:
             bits |= _abi.BC_M_EXT
             mask = ext_mask(rec) | xbit  # two record reals, each exact in FP32
             rec[_abi.BC_P_EXT_MASK], rec[_abi.BC_P_EXT_MASK_HI] = float(mask & 0xFFFFFF), float(mask >> 24)
-            g = p["g_scale"] * p["perm"] if name == "Cav3p3_RI2021_SC" else p["g_max"]
+            g = p["g_scale"] * p["perm"] if name == "Cav3p3_RI2021_SC" else \
+                (p["perm"] if name in ("CaHVA_SU2015_DCN", "CaLVA_SU2015_DCN") else p["g_max"])
             if name == "HCN2_MA2020_GoC":  # the conductance's own Q10 1.5 and the gates' q10 3, at 23 degC
                 g *= q10_phi(1.5, p["temp"], celsius2kelvin(23.0))
                 rec[_abi.BC_P_HCN2_PHI] = q10_phi(3.0, p["temp"], celsius2kelvin(23.0))
@@ -536,6 +545,10 @@ def region_record(mechs, cable: CableProperty) -> tuple[int, np.ndarray]:
                 rec[base + 1] = p["V_sh"]
                 rec[base + 2] = q10_phi(p["q10_p"], p["temp"], p["temp_ref_p"])
                 rec[base + 3] = q10_phi(p["q10_q"], p["temp"], p["temp_ref_q"])
+            elif name in ("CaHVA_SU2015_DCN", "CaLVA_SU2015_DCN"):
+                if p["qdeltat"] != 1.0:
+                    raise ValueError(f"{decl.class_name}: qdeltat other than 1 is not built.")
+                rec[_abi.BC_P_CAHVADCN_T if name == "CaHVA_SU2015_DCN" else _abi.BC_P_CALVADCN_T] = p["temp"]
             elif name in ("CaL_SU2015_DCN", "SK_SU2015_DCN") and p["qdeltat"] != 1.0:
                 raise ValueError(f"{decl.class_name}: qdeltat other than 1 is not built.")
             elif name == "CaN_IS2008":
@@ -579,8 +592,10 @@ def region_record(mechs, cable: CableProperty) -> tuple[int, np.ndarray]:
             rec[base + 3] = q10_phi(p["q10_q"], p["temp"], p["temp_ref_q"])
     ci_gated = bits & (_abi.BC_M_AHP | _abi.BC_M_KCA22 | _abi.BC_M_KCA11) or \
         ext_mask(rec) & (_abi.BC_X_KCA31 | _abi.BC_X_SKDCN | _abi.BC_X_CAN | _abi.BC_X_CAV31 |
-                                         _abi.BC_X_CAV33 | _abi.BC_X_CAV12 | _abi.BC_X_CAV13 | _abi.BC_X_CAV21)
-    if ext_mask(rec) & (_abi.BC_X_CAV31 | _abi.BC_X_CAV33 | _abi.BC_X_CAV21) and \
+                                         _abi.BC_X_CAV33 | _abi.BC_X_CAV12 | _abi.BC_X_CAV13 | _abi.BC_X_CAV21 |
+                                         _abi.BC_X_CAHVADCN | _abi.BC_X_CALVADCN)
+    if ext_mask(rec) & (_abi.BC_X_CAV31 | _abi.BC_X_CAV33 | _abi.BC_X_CAV21 | _abi.BC_X_CAHVADCN |
+                        _abi.BC_X_CALVADCN) and \
             not bits & _abi.BC_M_CADET:
         rec[_abi.BC_P_CA_CO] = 2.0  # the GHK drive's Co: the fixed calcium ion's (ion/calcium.py:121)
     if ci_gated and not bits & _abi.BC_M_CADET:

@@ -33,6 +33,8 @@
 //   Cav1p2_MA2020_GoC      channel/calcium.py:1408-1599
 //   Cav1p3_MA2020_GoC      channel/calcium.py:1683-1886
 //   Cav2p1_RI2021_SC       channel/calcium.py:2767-2953 (GHK drive, channel/_base.py:47)
+//   CaHVA_SU2015_DCN       channel/calcium.py:924-1064
+//   CaLVA_SU2015_DCN       channel/calcium.py:1221-1406 (CaL_SU2015_DCN's gates)
 // CaT_HP1992, CaHT_Re1993 and CaN_IS2008 (in its own E) carry calcium: their
 // step-start current joins the calcium shell's drive, as CaL's and CaT's do.  Kca3p1 and SK read Ci: the new Ci
 // of a dynamic calcium ion, else the fixed one (BC_P_CA_CI0), as AHP_De1994 does.
@@ -82,7 +84,10 @@ constexpr int kSlotCav33L = 112;
 constexpr int kSlotCav12 = 113;  // m, h, n
 constexpr int kSlotCav13 = 116;  // m, h, n
 constexpr int kSlotCav21M = 119;
-constexpr int kNumSlotsExt = 120;
+constexpr int kSlotCahvadcnM = 120;
+constexpr int kSlotCalvadcnM = 121;
+constexpr int kSlotCalvadcnH = 122;
+constexpr int kNumSlotsExt = 123;
 
 // x / (1 - e^-x) = 1 / exprel(-x), finite at x = 0 (the reference's
 // _x_over_one_minus_exp_neg_stable, channel/sodium.py:50-55)
@@ -526,6 +531,40 @@ struct Cav1Rates {
 constexpr double kCav1TauH = 44.3;
 constexpr double kCav1TauN = 0.5;
 
+// CaHVA_SU2015_DCN: m^3; m_inf = 1 / (1 + e^((V + 34.5) / -9)), m_tau = 1 / (31.746 /
+// (e^((V - 5) / -13.89) + 1) + 3.97e-4 (V + 8.9) / (e^((V + 8.9) / 5) - 1)) (qdeltat 1),
+// the second term as 3.97e-4 5 / exprel((V + 8.9) / 5).
+template <typename Real>
+struct CahvadcnRates {
+  Real minf, mtau;
+  __host__ __device__ __forceinline__ explicit CahvadcnRates(Real v) {
+    minf = Real(1) / (Real(1) + aexp((v + Real(34.5)) / Real(-9)));
+    const Real act = Real(31.746) / (aexp((v - Real(5)) / Real(-13.89)) + Real(1));
+    const Real cor = Real(3.97e-4 * 5.0) / exprel((v + Real(8.9)) / Real(5));
+    mtau = Real(1) / (act + cor);
+  }
+};
+
+// The SU2015 DCN calcium drive (calcium.py:924-1064): A = e^-x, x = 23.20764929 V / T,
+// (4.47814e6 V / T)(ci / 1000 - co A / 1000) / (1 - A) in mA/cm^2 per cm/s, i.e.
+// c S(x)(ci - co A) uA/cm^2 per cm/s with c = 4.47814e6 / 23.20764929 and S(x) = x / (1 -
+// e^-x) (the reference's expression, finite at V = 0).  *dd receives its V-derivative.
+template <typename Real>
+__host__ __device__ __forceinline__ Real su2015_drive(Real v, Real ci, Real co, Real temp, Real& dd) {
+  const Real c = Real(4.47814e6 / 23.20764929);
+  const Real kx = Real(23.20764929) / temp;  // x per mV
+  const Real x = kx * v;
+  const Real a = aexp(-x);
+  const Real sx = x_over_1mexp(x);
+  const Real ax = x < Real(0) ? -x : x;
+  // S'(x) = (1 - e^-x - x e^-x) / (1 - e^-x)^2, 1/2 + x/6 near 0
+  const Real den = Real(1) - a;
+  const Real ds = ax < Real(1e-4) ? Real(0.5) + x / Real(6) : (den - x * a) / (den * den);
+  const Real num = ci - co * a;
+  dd = c * kx * (ds * num + sx * co * a);
+  return c * sx * num;
+}
+
 // The region's BC_X_* bits: two record reals, each an integer below 2^24 (exact in FP32).
 template <typename Real>
 __host__ __device__ __forceinline__ uint32_t ext_mask(const Real* P) {
@@ -718,6 +757,26 @@ __device__ __forceinline__ Real ext_current(const Real* st, int N, const Real* P
         return -gp * drive;
       }
       return Real(0);
+    case BC_CUR_CAHVADCN:
+    case BC_CUR_CALVADCN: {
+      const bool hva = code == BC_CUR_CAHVADCN;
+      if ((has = (x & (hva ? BC_X_CAHVADCN : BC_X_CALVADCN)) != 0)) {
+        Real gates;
+        if (hva) {
+          const Real m = st[kSlotCahvadcnM * N];
+          gates = m * m * m;
+        } else {
+          const Real m = st[kSlotCalvadcnM * N];
+          gates = m * m * st[kSlotCalvadcnH * N];
+        }
+        const Real gp = P[hva ? BC_P_CAHVADCN_G : BC_P_CALVADCN_G] * gates;
+        Real dd;
+        const Real drive = su2015_drive(v, ci, P[BC_P_CA_CO], P[hva ? BC_P_CAHVADCN_T : BC_P_CALVADCN_T], dd);
+        if (gv) *gv = gp * dd;
+        return -gp * drive;
+      }
+      return Real(0);
+    }
     case BC_CUR_CAIO:
       if ((has = (x & BC_X_CAIO) != 0)) {
         Real m, dm;
@@ -853,6 +912,15 @@ __device__ __forceinline__ void ext_gates(Real* st, int N, const Real* P, uint32
     const Cav21Rates<Real> r(v, P[BC_P_CAV21_VSH]);
     st[kSlotCav21M * N] = gate_it(st[kSlotCav21M * N], r.minf, r.mtau, P[BC_P_CAV21_PHI], dt);
   }
+  if (x & BC_X_CAHVADCN) {
+    const CahvadcnRates<Real> r(v);
+    st[kSlotCahvadcnM * N] = gate_it(st[kSlotCahvadcnM * N], r.minf, r.mtau, Real(1), dt);
+  }
+  if (x & BC_X_CALVADCN) {
+    const CaldcnRates<Real> r(v);
+    st[kSlotCalvadcnM * N] = gate_it(st[kSlotCalvadcnM * N], r.minf, r.mtau, Real(1), dt);
+    st[kSlotCalvadcnH * N] = gate_it(st[kSlotCalvadcnH * N], r.hinf, r.htau, Real(1), dt);
+  }
   // the Markov scheme after the gates, by one linearised backward-Euler step
   if (x & BC_X_NAVGRC) {
     Real kf[17], kb[17];
@@ -869,7 +937,7 @@ __device__ __noinline__ void ext_channels(Real* st, int N, const Real* P, Real v
                                           bool advance, Real& G, Real& I) {
   const uint32_t x = ext_mask(P);
   if (advance) ext_gates(st, N, P, x, v, ci, dt);
-  for (int code = BC_CUR_HCN2; code <= BC_CUR_CAV21; ++code) {
+  for (int code = BC_CUR_HCN2; code <= BC_CUR_CALVADCN; ++code) {
     Real g = Real(0);
     const Real i = ext_current(st, N, P, x, v, ci, eca, code, &g);
     G += g;
@@ -889,7 +957,9 @@ __device__ __noinline__ Real ext_ca_current(const Real* st, int N, const Real* P
          ext_current(st, N, P, x, v, ci, eca, BC_CUR_CAV33, (Real*)nullptr) +
          ext_current(st, N, P, x, v, ci, eca, BC_CUR_CAV12, (Real*)nullptr) +
          ext_current(st, N, P, x, v, ci, eca, BC_CUR_CAV13, (Real*)nullptr) +
-         ext_current(st, N, P, x, v, ci, eca, BC_CUR_CAV21, (Real*)nullptr);
+         ext_current(st, N, P, x, v, ci, eca, BC_CUR_CAV21, (Real*)nullptr) +
+         ext_current(st, N, P, x, v, ci, eca, BC_CUR_CAHVADCN, (Real*)nullptr) +
+         ext_current(st, N, P, x, v, ci, eca, BC_CUR_CALVADCN, (Real*)nullptr);
 }
 
 // Steady states of the extension channels' gates at v (HH.reset_state).
@@ -981,6 +1051,12 @@ __device__ __forceinline__ void ext_steady(const Real* P, Real* st, int N, Real 
     st[(s0 + 2) * N] = r.ninf;
   }
   if (x & BC_X_CAV21) st[kSlotCav21M * N] = Cav21Rates<Real>(v, P[BC_P_CAV21_VSH]).minf;
+  if (x & BC_X_CAHVADCN) st[kSlotCahvadcnM * N] = CahvadcnRates<Real>(v).minf;
+  if (x & BC_X_CALVADCN) {
+    const CaldcnRates<Real> r(v);
+    st[kSlotCalvadcnM * N] = r.minf;
+    st[kSlotCalvadcnH * N] = r.hinf;
+  }
   if (x & BC_X_NAVGRC) {  // the stationary distribution (reset_steady_state)
     Real kf[17], kb[17];
     navgrc_rates(v, P[BC_P_NAVGRC_PHI], kf, kb);

@@ -362,7 +362,7 @@ __device__ __forceinline__ double probe_current(const Real* st, int N, const Rea
         return cerebellar_ca_current(st, N, P, m & BC_M_CAV32, v, eca(), (Real*)nullptr);
       default:
         // extension channels: the record's list exists only where BC_M_EXT is set
-        if (c >= BC_CUR_HCN2 && c <= BC_CUR_CAV21 && (m & BC_M_EXT)) {
+        if (c >= BC_CUR_HCN2 && c <= BC_CUR_CALVADCN && (m & BC_M_EXT)) {
           const Real ci = (m & BC_M_CADET) ? st[kSlotCaHi * N] + st[kSlotCaLo * N] : P[BC_P_CA_CI0];
           const bool ohmic_ca = c == BC_CUR_CATHP || c == BC_CUR_CAHTRE || c == BC_CUR_CAV12 || c == BC_CUR_CAV13;
           return ext_current(st, N, P, ext_mask(P), v, ci, ohmic_ca ? eca() : Real(0),
@@ -387,7 +387,7 @@ __device__ __forceinline__ double probe_current(const Real* st, int N, const Rea
       return double(cur(BC_CUR_CAL)) + double(cur(BC_CUR_CAT)) + double(cur(BC_CUR_CAHVA)) + double(cur(BC_CUR_CAV23)) +
              double(cur(BC_CUR_CAV32)) + double(cur(BC_CUR_CATHP)) + double(cur(BC_CUR_CAHTRE)) + double(cur(BC_CUR_CAN)) +
              double(cur(BC_CUR_CAV31)) + double(cur(BC_CUR_CAV33)) + double(cur(BC_CUR_CAV12)) + double(cur(BC_CUR_CAV13)) +
-             double(cur(BC_CUR_CAV21));
+             double(cur(BC_CUR_CAV21)) + double(cur(BC_CUR_CAHVADCN)) + double(cur(BC_CUR_CALVADCN));
     default:
       return double(cur(code));
   }

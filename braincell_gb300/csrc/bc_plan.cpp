@@ -100,7 +100,7 @@ static void state_view(int32_t which, uint64_t* bit, int* slot) {
   static const uint32_t kCereb[BC_NSTATE_VIEW - BC_STATE_KV34_M] = {
       BC_M_KV34,  BC_M_KV34,  BC_M_KV43,  BC_M_KV43,  BC_M_KV11,  BC_M_KIR23, BC_M_HCN1F, BC_M_HCN1F,
       BC_M_HCN1H, BC_M_CAHVA, BC_M_CAHVA, BC_M_CAV23, BC_M_CAV23, BC_M_CAV32, BC_M_CAV32};
-  // extension channels' states 66 .. 118 in slots 67 .. 119
+  // extension channels' states 66 .. 121 in slots 67 .. 122
   static const uint32_t kExt[BC_NSTATE_VIEW - BC_STATE_HCN2_FAST] = {
       BC_X_HCN2, BC_X_HCN2, BC_X_KV33, BC_X_KV22,  BC_X_KV22,  BC_X_KV15,  BC_X_KV15,
       BC_X_KV15, BC_X_NAF,  BC_X_NAF,  BC_X_NAP,   BC_X_NAP,   BC_X_NAIO,  BC_X_NAIO,
@@ -109,7 +109,7 @@ static void state_view(int32_t which, uint64_t* bit, int* slot) {
       BC_X_CAN, BC_X_CAIO, BC_X_NAVGRC, BC_X_NAVGRC, BC_X_NAVGRC, BC_X_NAVGRC, BC_X_NAVGRC, BC_X_NAVGRC,
       BC_X_NAVGRC, BC_X_NAVGRC, BC_X_NAVGRC, BC_X_NAVGRC, BC_X_NAVGRC, BC_X_NAVGRC, BC_X_CAV31, BC_X_CAV31,
       BC_X_CAV33, BC_X_CAV33, BC_X_CAV12, BC_X_CAV12, BC_X_CAV12, BC_X_CAV13, BC_X_CAV13, BC_X_CAV13,
-      BC_X_CAV21};
+      BC_X_CAV21, BC_X_CAHVADCN, BC_X_CALVADCN, BC_X_CALVADCN};
   if (which >= BC_STATE_HCN2_FAST)
     *bit = ext_bits(kExt[which - BC_STATE_HCN2_FAST]);
   else if (which >= BC_STATE_KV34_M)
@@ -1393,7 +1393,8 @@ bc_status bc_plan_create(const bc_batch_spec* spec, const bc_plan_options* opts_
               ext_bits(BC_X_KV33 | BC_X_KV22 | BC_X_KV15 | BC_X_FKDR | BC_X_SKDR | BC_X_KDRIO | BC_X_KCA31 |
                        BC_X_SKDCN | BC_X_KKV),
           BC_M_CAL | BC_M_CAT | BC_M_CAHVA | BC_M_CAV23 | BC_M_CAV32 | ext_bits(BC_X_CATHP | BC_X_CAHTRE | BC_X_CAN | BC_X_CAV31 | BC_X_CAV33 |
-                                                                  BC_X_CAV12 | BC_X_CAV13 | BC_X_CAV21),
+                                                                  BC_X_CAV12 | BC_X_CAV13 | BC_X_CAV21 |
+                                                                  BC_X_CAHVADCN | BC_X_CALVADCN),
           BC_M_KA1,  BC_M_KA2, BC_M_KK2A, BC_M_KK2B, BC_M_KNI,
           BC_M_NAV16, BC_M_KCA22, BC_M_KCA11, BC_M_KV34, BC_M_KV43, BC_M_KV11, BC_M_KIR23, BC_M_HCN1F, BC_M_HCN1H,
           BC_M_CAHVA, BC_M_CAV23, BC_M_CAV32,
@@ -1402,7 +1403,7 @@ bc_status bc_plan_create(const bc_batch_spec* spec, const bc_plan_options* opts_
           ext_bits(BC_X_HCNDCN), ext_bits(BC_X_HCNIO), ext_bits(BC_X_CATHP), ext_bits(BC_X_CAHTRE),
           ext_bits(BC_X_CALDCN), ext_bits(BC_X_KCA31), ext_bits(BC_X_SKDCN), ext_bits(BC_X_KKV), ext_bits(BC_X_CAN),
           ext_bits(BC_X_CAIO), ext_bits(BC_X_NAVGRC), ext_bits(BC_X_CAV31), ext_bits(BC_X_CAV33), ext_bits(BC_X_CAV12),
-          ext_bits(BC_X_CAV13), ext_bits(BC_X_CAV21)};
+          ext_bits(BC_X_CAV13), ext_bits(BC_X_CAV21), ext_bits(BC_X_CAHVADCN), ext_bits(BC_X_CALVADCN)};
       const int32_t rg = cells[c].region[v];
       if (rg < 0 || !(region_bits(s, c * s.n_regions + rg) & cur_owner[field - BC_PROBE_CURRENT])) {
         delete p;

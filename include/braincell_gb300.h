@@ -119,10 +119,12 @@ typedef int32_t bc_status;
 #define BC_X_CAV13 (1u << 24)  /* channel/calcium.py:1683 Cav1p3_MA2020_GoC m h n(Ci), E_Ca    */
 #define BC_X_CAV21 (1u << 25)  /* channel/calcium.py:2767 Cav2p1_RI2021_SC m^3, GHK drive (the
                                   shared ghk_flux, channel/_base.py:47; g in cm/s)           */
-#define BC_X_ALL 0x3FFFFFFu
+#define BC_X_CAHVADCN (1u << 26) /* channel/calcium.py:924 CaHVA_SU2015_DCN m^3, SU2015 GHK drive */
+#define BC_X_CALVADCN (1u << 27) /* channel/calcium.py:1221 CaLVA_SU2015_DCN m^2 h, same drive   */
+#define BC_X_ALL 0xFFFFFFFu
 
 /* Per-region parameter record (double[BC_NPARAM]); index names below. */
-#define BC_NPARAM 164
+#define BC_NPARAM 168
 #define BC_P_INVCM 0      /* 1 / membrane capacitance, cm^2/uF                 */
 #define BC_P_VREST 1      /* voltage used by reset (mV)                        */
 #define BC_P_ENA 2        /* fixed reversal potentials (mV)                    */
@@ -286,7 +288,11 @@ typedef int32_t bc_status;
 #define BC_P_CAV21_PHI 160  /* 3^((T - 23 degC) / 10)                               */
 #define BC_P_CAV21_TGHK 161 /* the GHK temperature T (K)                            */
 #define BC_P_EXT_MASK_HI 162 /* BC_X_* bits 24 and up, shifted down by 24           */
-/* 163: reserved (0) */
+#define BC_P_CAHVADCN_G 163 /* permeability perm (cm/s)                            */
+#define BC_P_CAHVADCN_T 164 /* temperature (K) of its drive                         */
+#define BC_P_CALVADCN_G 165
+#define BC_P_CALVADCN_T 166
+/* 167: reserved (0) */
 
 /* ------------------------------------------------------------------ batch spec */
 /*
@@ -451,8 +457,8 @@ const char* bc_last_error(void);
  * 25-50), lane tiles (bc_plan_options.lane_cell_nodes, tile_order), the cerebellar
  * HH and calcium channels (BC_M_KV34 .. CAV32, a 96-entry parameter record, state
  * views 51-65, BC_PROBE_CURRENT 128).  0.5.0: extension channels (BC_M_EXT with
- * BC_X_* bits in the record's BC_P_EXT_MASK, a 164-entry parameter record, state
- * views 66-118, current codes 31-56). */
+ * BC_X_* bits in the record's BC_P_EXT_MASK / _HI, a 168-entry parameter record,
+ * state views 66-121, current codes 31-58). */
 #define BC_ABI_VERSION 500
 int32_t bc_version(void);
 /* Fill opts with defaults. */
@@ -593,7 +599,10 @@ bc_status bc_check(bc_plan_t plan, void* stream);
 #define BC_STATE_CAV12_M 112 /* M, H, N: 112 .. 114 */
 #define BC_STATE_CAV13_M 115 /* M, H, N: 115 .. 117 */
 #define BC_STATE_CAV21_M 118
-#define BC_NSTATE_VIEW 119
+#define BC_STATE_CAHVADCN_M 119
+#define BC_STATE_CALVADCN_M 120
+#define BC_STATE_CALVADCN_H 121
+#define BC_NSTATE_VIEW 122
 /* Current probes (mech/_point.py CurrentProbe, _multi_compartment/probes.py:184-258):
    probe_field = BC_PROBE_CURRENT + one of the codes below records that current
    density (uA/cm^2, outward negative as g (E - V)) after the step.             */
@@ -655,7 +664,9 @@ bc_status bc_check(bc_plan_t plan, void* stream);
 #define BC_CUR_CAV12 54  /* Cav1p2_MA2020_GoC      */
 #define BC_CUR_CAV13 55  /* Cav1p3_MA2020_GoC      */
 #define BC_CUR_CAV21 56  /* Cav2p1_RI2021_SC       */
-#define BC_NCUR 57
+#define BC_CUR_CAHVADCN 57 /* CaHVA_SU2015_DCN     */
+#define BC_CUR_CALVADCN 58 /* CaLVA_SU2015_DCN     */
+#define BC_NCUR 59
 bc_status bc_state_download(bc_plan_t plan, int32_t which, double* out /* [n_cv] */, void* stream);
 /* Set the amplitude (nA) of every current-clamp pulse of the batch spec, in spec
  * order (amp_nA[n_pulses]); times and locations are unchanged.  Takes effect from

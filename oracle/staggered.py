@@ -156,7 +156,27 @@ CHANNEL_DEFAULTS.update({
     "Cav1p2_MA2020_GoC": dict(g_max=0.2, V_sh=0.0, temp=_c2k(22.0), q10=1.0, temp_ref=_c2k(22.0)),  # calcium.py:1408
     "Cav1p3_MA2020_GoC": dict(g_max=0.005, V_sh=0.0, temp=_c2k(22.0), q10=1.0, temp_ref=_c2k(22.0)),  # :1683
     "Cav2p1_RI2021_SC": dict(g_max=2.2e-4, V_sh=0.0, temp=_c2k(23.0)),  # calcium.py:2767 (cm/s)
+    "CaHVA_SU2015_DCN": dict(perm=7.5e-6, temp=_c2k(36.0), qdeltat=1.0),  # calcium.py:924 (cm/s)
+    "CaLVA_SU2015_DCN": dict(perm=1.0, temp=_c2k(36.0), qdeltat=1.0),  # calcium.py:1221 (cm/s)
 })
+
+
+def su2015_drive(V, ci, co, temp):
+    """The SU2015 DCN calcium drive (calcium.py:924-1064): (4.47814e6 V / T)(ci - co A) /
+    1000 / (1 - A) mA/cm^2 per cm/s with A = e^-x, x = 23.20764929 V / T, written as
+    c S(x)(ci - co A) uA/cm^2 per cm/s (c = 4.47814e6 / 23.20764929, S(x) = x / (1 - e^-x);
+    the same value, finite at V = 0).  Returns (drive, d drive / dV per mV)."""
+    c = 4.47814e6 / 23.20764929
+    kx = 23.20764929 / temp
+    x = kx * V
+    a = np.exp(-x)
+    small = np.abs(x) < 1e-4
+    xs = np.where(small, 1.0, x)
+    sx = np.where(small, 1.0 + x / 2.0, xs / (1.0 - np.exp(-xs)))
+    den = 1.0 - np.exp(-xs)
+    ds = np.where(small, 0.5 + x / 6.0, (den - xs * np.exp(-xs)) / den ** 2)
+    num = ci - co * a
+    return c * sx * num, c * kx * (ds * num + sx * co * a)
 
 
 def ghk_codata_drive(V, ci, co, temp):
@@ -708,6 +728,12 @@ def rates(name: str, V, p: dict, Ci=None):
                       np.where(x > -60.0, 7.2 + 0.02 * np.exp(-x / 14.7), 0.875 * np.exp((x + 120.0) / 41.0))),
                 "l": ("it", 1.0 / (1.0 + np.exp(-(x - -69.8) / -6.1)),
                       np.where(x > -60.0, 79.5 + 2.0 * np.exp(-x / 9.3), 260.0))}
+    if name == "CaHVA_SU2015_DCN":  # calcium.py:924-1064
+        act = 31.746 / (np.exp((V - 5.0) / -13.89) + 1.0)
+        cor = 3.97e-4 * 5.0 / exprel((V + 8.9) / 5.0)
+        return {"m": ("it", 1.0 / (1.0 + np.exp((V + 34.5) / -9.0)), 1.0 / (act + cor) / p["qdeltat"])}
+    if name == "CaLVA_SU2015_DCN":  # calcium.py:1221-1406: CaL_SU2015_DCN's gates
+        return rates("CaL_SU2015_DCN", V, {"qdeltat": p["qdeltat"]})
     if name == "Cav2p1_RI2021_SC":  # calcium.py:2767-2953, on V - V_sh
         x = V - p["V_sh"]
         mt = np.where(x >= -40.0, 0.2702 + 1.1622 * np.exp(-((x + 26.798) ** 2) / 164.19), 0.6923 * np.exp(x / 1089.372))
@@ -790,6 +816,8 @@ _GATES = {  # (gate, power, phi-key)
     "Cav1p2_MA2020_GoC": (("m", 1, "phi"), ("h", 1, "phi"), ("n", 1, "phi")),
     "Cav1p3_MA2020_GoC": (("m", 1, "phi"), ("h", 1, "phi"), ("n", 1, "phi")),
     "Cav2p1_RI2021_SC": (("m", 3, "phi"),),
+    "CaHVA_SU2015_DCN": (("m", 3, "phi"),),
+    "CaLVA_SU2015_DCN": (("m", 2, "phi"), ("h", 1, "phi")),
 }
 _ION_OF = {"Na_Ba2002": "na", "KDR_Ba2002": "k", "CaL_IS2008": "ca", "CaT_HM1992": "ca",
            "K_Leak": "k", "AHP_De1994": "k", "Na_HH1952": "na", "K_HH1952": "k", "KM_RI2021_SC": "k",
@@ -804,9 +832,9 @@ _ION_OF = {"Na_Ba2002": "na", "KDR_Ba2002": "k", "CaL_IS2008": "ca", "CaT_HM1992
            "Kdr_ZH2019_IO": "k", "CaT_HP1992": "ca", "CaHT_Re1993": "ca", "Kca3p1_MA2020_GoC": "k",
            "SK_SU2015_DCN": "k", "K_Kv_test": "k", "CaN_IS2008": "ca", "Nav_MA2020_GrC": "na",
            "Cav3p1_MA2020_GoC": "ca", "Cav3p3_RI2021_SC": "ca", "Cav1p2_MA2020_GoC": "ca", "Cav1p3_MA2020_GoC": "ca",
-           "Cav2p1_RI2021_SC": "ca"}
+           "Cav2p1_RI2021_SC": "ca", "CaHVA_SU2015_DCN": "ca", "CaLVA_SU2015_DCN": "ca"}
 # calcium channels with a GHK current (-g gates drive) instead of an ohmic one
-_GHK = ("Cav3p1_MA2020_GoC", "Cav3p3_RI2021_SC", "Cav2p1_RI2021_SC")
+_GHK = ("Cav3p1_MA2020_GoC", "Cav3p3_RI2021_SC", "Cav2p1_RI2021_SC", "CaHVA_SU2015_DCN", "CaLVA_SU2015_DCN")
 # channels with their own reversal potential (HHTypedNeuron root, not an ion)
 _OWN_E = ("HCN_HM1992", "HCN1_MA2020_GoC", "HCN1_MA2024_PC", "HCN2_MA2020_GoC", "HCN_SU2015_DCN", "HCN_ZH2019_IO",
           "CaL_SU2015_DCN", "CaN_IS2008", "Ca_ZH2019_IO")
@@ -859,6 +887,9 @@ def _resolve(table: dict, decl) -> dict:
         p["gbar_phi"] = 1.5 ** ((p["temp"] - _c2k(23.0)) / 10.0)
     if name == "Cav2p1_RI2021_SC":  # Gate q10 3 at 23 degC
         p["phi"] = 3.0 ** ((p["temp"] - _c2k(23.0)) / 10.0)
+    if name in ("CaHVA_SU2015_DCN", "CaLVA_SU2015_DCN"):  # gates without a temperature factor; g = perm
+        p["phi"] = 1.0
+        p["g_max"] = p["perm"]
     if name in ("CaN_IS2008", "Cav1p2_MA2020_GoC", "Cav1p3_MA2020_GoC"):  # Gates (q10, temp_ref)
         p["phi"] = p["q10"] ** ((p["temp"] - p["temp_ref"]) / 10.0)
     if name in ("Cav3p1_MA2020_GoC", "Cav3p3_RI2021_SC"):  # the _Frozen classes: the GHK drive out of the linearisation
@@ -1342,6 +1373,8 @@ class OracleCell:
             return cav31_drive(pv, self._ci_for_channels(), self._co_for_channels(), ch["temp"])
         if name == "Cav2p1_RI2021_SC":
             return ghk_codata_drive(pv - ch["V_sh"], self._ci_for_channels(), self._co_for_channels(), ch["temp"])
+        if name in ("CaHVA_SU2015_DCN", "CaLVA_SU2015_DCN"):
+            return su2015_drive(pv, self._ci_for_channels(), self._co_for_channels(), ch["temp"])
         return cav33_drive(pv - ch["V_sh"], self._ci_for_channels(), self._co_for_channels(), ch["temp"])
 
     def _co_for_channels(self):

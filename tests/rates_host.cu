@@ -89,6 +89,13 @@ extern "C" int bc_test_rates(int which, const double* v, int n, const double* pr
         o[1] = dd;
         break;
       }
+      case 50: { const CahvadcnRates<double> r(x); o[0] = r.minf; o[1] = r.mtau; break; }
+      case 51: {  // the SU2015 drive and its V-derivative at ci = prm[0], co = prm[1], T = prm[2]
+        double dd;
+        o[0] = su2015_drive(x, prm[0], prm[1], prm[2], dd);
+        o[1] = dd;
+        break;
+      }
       case 44: { const Cav33Rates<double> r(x, prm[0]); o[0] = r.ninf; o[1] = r.ntau; o[2] = r.linf; o[3] = r.ltau; break; }
       case 45: {  // the Cav3.3 GHK drive and its V-derivative at ci = prm[0], co = prm[1], T = prm[2]
         double dd;

@@ -7,7 +7,7 @@ calcium-gated Kca3p1 (and its BC / PC classes) and SK_SU2015_DCN, K_Kv_test, CaN
 the Markov scheme Nav_MA2020_GrC, and Cav3p1 (GoC, PC and their _Frozen classes) with its
 GHK drive, Cav3p3 (RI2021_SC, MA2024_PC and its _Frozen class) with its own, and the
 Ci-inactivated Cav1p2 / Cav1p3 (and their BC classes), and Cav2p1 (SC, PC, BC) on the
-shared GHK drive.
+shared GHK drive, and the SU2015 DCN CaHVA / CaLVA on their own drive (the DCN cell).
 
 CPU: the records and their mask, the planner's check of the mask, and the owner
 tables (through the planner tests).  GPU: a DCN-like cell and an IO-like cell
@@ -86,13 +86,15 @@ def _dcn_cell(precision="f64"):
             Channel("fKdr_SU2015_DCN", g_max=15.0), Channel("sKdr_SU2015_DCN", g_max=4.0),
             Channel("HCN_SU2015_DCN", g_max=0.3))
     c.paint(branch_in("type", "dendrite"), Channel("Kv1p5_MA2024_PC", g_max=0.5), Channel("Kv3p3_MA2024_PC", g_max=1.0),
-            Channel("Kv2p2_0010_MA2020_GrC", g_max=0.5), Channel("HCN2_MA2020_GoC", g_max=0.3))
+            Channel("Kv2p2_0010_MA2020_GrC", g_max=0.5), Channel("HCN2_MA2020_GoC", g_max=0.3),
+            Channel("CaHVA_SU2015_DCN", perm=2e-4), Channel("CaLVA_SU2015_DCN", perm=5e-5))
     c.place(RootLocation(0.5), CurrentClamp(delay=2.0, durations=20.0, amplitudes=0.3), StateProbe(name="v"),
             MechanismProbe("NaF_SU2015_DCN", "h", name="naf_h"), CurrentProbe(mechanism="NaF_SU2015_DCN", name="i_naf"),
             CurrentProbe(ion="na", name="i_na"))
     c.place(at(1, 0.5), StateProbe(name="v_dend"), MechanismProbe("Kv1p5_MA2024_PC", "m", name="kv15_m"),
             MechanismProbe("HCN2_MA2020_GoC", "o_slow", name="hcn2_s"),
-            CurrentProbe(mechanism="Kv1p5_MA2024_PC", name="i_kv15"), CurrentProbe(ion="k", name="i_k"))
+            CurrentProbe(mechanism="Kv1p5_MA2024_PC", name="i_kv15"), CurrentProbe(ion="k", name="i_k"),
+            MechanismProbe("CaLVA_SU2015_DCN", "h", name="calva_h"), CurrentProbe(ion="ca", name="i_ca"))
     return c
 
 

@@ -36,6 +36,7 @@ CASES = {
     39: ("K_Kv_test", ("V_sh", "Ra", "Rb", "q", "v12")), 40: ("CaN_IS2008", ()), 41: ("Ca_ZH2019_IO", ()),
     42: ("Cav3p1_MA2020_GoC", ("qt",)), 44: ("Cav3p3_RI2021_SC", ("V_sh",)),
     46: ("Cav1p2_MA2020_GoC", ("Ci",)), 47: ("Cav1p3_MA2020_GoC", ("Ci",)), 48: ("Cav2p1_RI2021_SC", ("V_sh",)),
+    50: ("CaHVA_SU2015_DCN", ()),
 }
 
 
@@ -112,11 +113,12 @@ def test_kernel_rates_match_oracle(rates_lib, which, shift):
                                    err_msg=f"{name} rate column {k}")
 
 
-@pytest.mark.parametrize("which", [43, 45, 49], ids=["cav3p1", "cav3p3", "shared"])
+@pytest.mark.parametrize("which", [43, 45, 49, 51], ids=["cav3p1", "cav3p3", "shared", "su2015"])
 @pytest.mark.parametrize("ci,co,temp", [(5e-5, 2.0, 295.15), (1e-3, 2.0, 310.15), (2.0, 2.0, 300.0)])
 def test_ghk_drive_matches_oracle(rates_lib, which, ci, co, temp):
     # the Cav3.1 / Cav3.3 GHK drives and their V-derivatives, across 0 mV (the small branch)
-    fn, off = {43: (O.cav31_drive, 0.04), 45: (O.cav33_drive, -0.01), 49: (O.ghk_codata_drive, 0.0)}[which]
+    fn, off = {43: (O.cav31_drive, 0.04), 45: (O.cav33_drive, -0.01), 49: (O.ghk_codata_drive, 0.0),
+               51: (O.su2015_drive, 0.0)}[which]
     V = np.concatenate([np.linspace(-100.0, 60.0, 1601), [0.0, 1e-7, -1e-7, 1e-4]])
     got = _kernel(rates_lib, which, V, [ci, co, temp + off])  # the kernel takes the GHK temperature itself
     drive, dd = fn(V, ci, co, temp)

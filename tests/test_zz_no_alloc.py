@@ -80,7 +80,8 @@ def _hh_batch():
             Channel("CaN_IS2008", g_max=0.05), Channel("Ca_ZH2019_IO", g_max=0.05),
             Channel("Nav_MA2020_GrC", g_max=0.2), Channel("Cav3p1_MA2020_GoC", g_max=1e-5),
             Channel("Cav3p3_RI2021_SC"), Channel("Cav1p2_MA2020_GoC", g_max=0.01), Channel("Cav1p3_MA2020_GoC"),
-            Channel("Cav2p1_RI2021_SC", g_max=1e-6))
+            Channel("Cav2p1_RI2021_SC", g_max=1e-6), Channel("CaHVA_SU2015_DCN"),
+            Channel("CaLVA_SU2015_DCN", perm=1e-6))
     return lower_cell(c)
 
 
