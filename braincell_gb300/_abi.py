@@ -251,6 +251,7 @@ BC_P_CAHVADCN_G = 163
 BC_P_CAHVADCN_T = 164
 BC_P_CALVADCN_G = 165
 BC_P_CALVADCN_T = 166
+BC_P_CAV21_FROZEN = 167
 
 BC_ABI_VERSION = 500
 

@@ -76,8 +76,8 @@ BC_P_EXT_MASK, their parameters after it; conductances in mS/cm^2):
 * ``Cav1p2_MA2020_GoC`` / ``Cav1p3_MA2020_GoC`` -- channel/calcium.py:1408, :1683 (g_max 0.2 / 0.005, temp 22 degC,
   q10 1 at 22 degC; n_inf = kf / (kf + Ci)); their MA2025_BC classes repeat them
 * ``Cav2p1_RI2021_SC`` -- channel/calcium.py:2767 (permeability g_max 2.2e-4 cm/s, V_sh 0, temp 23 degC; gate q10 3 at
-  23 degC; the shared GHK drive of channel/_base.py:47); the MA2024_PC and MA2025_BC classes repeat it (their _Frozen
-  classes, on another GHK helper, are not built)
+  23 degC; the shared GHK drive of channel/_base.py:47); the MA2024_PC and MA2025_BC classes repeat it, and the three
+  _Frozen classes run the Cav3.1 model-file GHK at a stop-gradient V
 * ``CaHVA_SU2015_DCN`` / ``CaLVA_SU2015_DCN`` -- channel/calcium.py:924, :1221 (perm 7.5e-6 / 1 cm/s, temp 36 degC,
   qdeltat 1; the model's drive (4.47814e6 V / T)(ci - co A) / 1000 / (1 - A), A = e^(-23.20764929 V / T); CaLVA on
   CaL_SU2015_DCN's gates)
@@ -248,7 +248,8 @@ _EXT = {
 }
 # Cav3p1 classes with the GHK drive frozen for the linearisation (calcium.py, the
 # _Frozen subclasses: the forward current is the base class's)
-_GHK_FROZEN = ("Cav3p1_MA2020_GoC_Frozen", "Cav3p1_MA2024_PC_Frozen", "Cav3p3_MA2024_PC_Frozen")
+_GHK_FROZEN = ("Cav3p1_MA2020_GoC_Frozen", "Cav3p1_MA2024_PC_Frozen", "Cav3p3_MA2024_PC_Frozen",
+               "Cav2p1_MA2024_PC_Frozen", "Cav2p1_MA2025_BC_Frozen", "Cav2p1_RI2021_SC_Frozen")
 # cell-type variants with their base class's kinetics; own defaults where they differ
 KINETIC_VARIANTS = {
     "Kv3p4_MA2020_GoC": {v: {} for v in ("Kv3p4_MA2020_GrC", "Kv3p4_MA2024_PC", "Kv3p4_MA2025_BC", "Kv3p4_RI2021_SC")},
@@ -295,6 +296,11 @@ for _v in ("Cav3p1_MA2024_PC", "Cav3p1_MA2020_GoC_Frozen", "Cav3p1_MA2024_PC_Fro
 for _v in ("Cav3p3_MA2024_PC", "Cav3p3_MA2024_PC_Frozen"):
     CHANNELS[_v] = dict(CHANNELS["Cav3p3_RI2021_SC"])
     SAME_FORM[_v] = "Cav3p3_RI2021_SC"
+# the Cav2p1 _Frozen classes: Cav2p1's gates and defaults, the Cav3.1 model-file GHK at a
+# stop-gradient V (their record differs from the base class's in the drive entries)
+for _v in ("Cav2p1_MA2024_PC_Frozen", "Cav2p1_MA2025_BC_Frozen", "Cav2p1_RI2021_SC_Frozen"):
+    CHANNELS[_v] = dict(CHANNELS["Cav2p1_RI2021_SC"])
+    SAME_FORM[_v] = "Cav2p1_RI2021_SC"
 # Ca_ZH2019_IO_Frozen (calcium.py) is Ca_ZH2019_IO with freeze_m_inf pinned to True
 CHANNELS["Ca_ZH2019_IO_Frozen"] = dict(CHANNELS["Ca_ZH2019_IO"])
 SAME_FORM["Ca_ZH2019_IO_Frozen"] = "Ca_ZH2019_IO"
@@ -568,7 +574,10 @@ def region_record(mechs, cable: CableProperty) -> tuple[int, np.ndarray]:
             elif name == "Cav2p1_RI2021_SC":  # Gate q10 3 at 23 degC; the shared GHK at temp
                 rec[_abi.BC_P_CAV21_VSH] = p["V_sh"]
                 rec[_abi.BC_P_CAV21_PHI] = q10_phi(3.0, p["temp"], celsius2kelvin(23.0))
-                rec[_abi.BC_P_CAV21_TGHK] = p["temp"]
+                # the _Frozen classes' drive is the Cav3.1 model-file GHK (at T + 0.04 K)
+                frozen = decl.class_name in _GHK_FROZEN
+                rec[_abi.BC_P_CAV21_TGHK] = p["temp"] + (0.04 if frozen else 0.0)
+                rec[_abi.BC_P_CAV21_FROZEN] = 1.0 if frozen else 0.0
             elif name == "Nav_MA2020_GrC":  # phi = 3^((T - 20 degC) / 10) (sodium.py, __init__)
                 rec[_abi.BC_P_NAVGRC_PHI] = q10_phi(3.0, p["temp"], celsius2kelvin(20.0))
             elif name == "Ca_ZH2019_IO":

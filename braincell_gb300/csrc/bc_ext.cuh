@@ -752,8 +752,12 @@ __device__ __forceinline__ Real ext_current(const Real* st, int N, const Real* P
         const Real m = st[kSlotCav21M * N];
         const Real gp = P[BC_P_CAV21_G] * m * m * m;
         Real dd;
-        const Real drive = ghk_codata_drive(v - P[BC_P_CAV21_VSH], ci, P[BC_P_CA_CO], P[BC_P_CAV21_TGHK], dd);
-        if (gv) *gv = gp * dd;
+        // the _Frozen classes: the Cav3.1 model-file GHK at a stop-gradient V (row conductance 0)
+        const bool frozen = P[BC_P_CAV21_FROZEN] != Real(0);
+        const Real vs = v - P[BC_P_CAV21_VSH];
+        const Real drive = frozen ? cav31_drive(vs, ci, P[BC_P_CA_CO], P[BC_P_CAV21_TGHK], dd)
+                                  : ghk_codata_drive(vs, ci, P[BC_P_CA_CO], P[BC_P_CAV21_TGHK], dd);
+        if (gv) *gv = frozen ? Real(0) : gp * dd;
         return -gp * drive;
       }
       return Real(0);

@@ -292,7 +292,9 @@ typedef int32_t bc_status;
 #define BC_P_CAHVADCN_T 164 /* temperature (K) of its drive                         */
 #define BC_P_CALVADCN_G 165
 #define BC_P_CALVADCN_T 166
-/* 167: reserved (0) */
+#define BC_P_CAV21_FROZEN 167 /* 1: the _Frozen classes' drive (the Cav3.1 model-file GHK
+                                 at T + 0.04 K, in BC_P_CAV21_TGHK) held out of the
+                                 linearisation                                        */
 
 /* ------------------------------------------------------------------ batch spec */
 /*

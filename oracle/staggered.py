@@ -264,7 +264,8 @@ _VARIANTS = {
                                                "Cav3p1_MA2024_PC_Frozen")},
     **{v: ("Cav3p3_RI2021_SC", {}) for v in ("Cav3p3_MA2024_PC", "Cav3p3_MA2024_PC_Frozen")},
     "Cav1p2_MA2025_BC": ("Cav1p2_MA2020_GoC", {}), "Cav1p3_MA2025_BC": ("Cav1p3_MA2020_GoC", {}),
-    **{v: ("Cav2p1_RI2021_SC", {}) for v in ("Cav2p1_MA2024_PC", "Cav2p1_MA2025_BC")},
+    **{v: ("Cav2p1_RI2021_SC", {}) for v in ("Cav2p1_MA2024_PC", "Cav2p1_MA2025_BC", "Cav2p1_MA2024_PC_Frozen",
+                                              "Cav2p1_MA2025_BC_Frozen", "Cav2p1_RI2021_SC_Frozen")},
     **{v: ("Cav3p2_RI2021_SC", {}) for v in ("Cav3p2_MA2025_BC", "Cav3p2_MA2024_PC")},
 }
 
@@ -892,7 +893,7 @@ def _resolve(table: dict, decl) -> dict:
         p["g_max"] = p["perm"]
     if name in ("CaN_IS2008", "Cav1p2_MA2020_GoC", "Cav1p3_MA2020_GoC"):  # Gates (q10, temp_ref)
         p["phi"] = p["q10"] ** ((p["temp"] - p["temp_ref"]) / 10.0)
-    if name in ("Cav3p1_MA2020_GoC", "Cav3p3_RI2021_SC"):  # the _Frozen classes: the GHK drive out of the linearisation
+    if name in ("Cav3p1_MA2020_GoC", "Cav3p3_RI2021_SC", "Cav2p1_RI2021_SC"):  # _Frozen: drive out of the linearisation
         p["ghk_frozen"] = 1.0 if decl.class_name.endswith("_Frozen") else 0.0
     if name == "Cav3p3_RI2021_SC":  # Gates q10 2.3 at 28 degC; g = g_scale perm
         p["phi"] = 2.3 ** ((p["temp"] - _c2k(28.0)) / 10.0)
@@ -1371,8 +1372,11 @@ class OracleCell:
         """(drive, d drive / dV) of a GHK calcium channel at the point voltages."""
         if name == "Cav3p1_MA2020_GoC":
             return cav31_drive(pv, self._ci_for_channels(), self._co_for_channels(), ch["temp"])
-        if name == "Cav2p1_RI2021_SC":
-            return ghk_codata_drive(pv - ch["V_sh"], self._ci_for_channels(), self._co_for_channels(), ch["temp"])
+        if name == "Cav2p1_RI2021_SC":  # the _Frozen classes: the Cav3.1 model-file helper (calcium.py, their current)
+            args = (pv - ch["V_sh"], self._ci_for_channels(), self._co_for_channels(), ch["temp"])
+            shared, nmodl = ghk_codata_drive(*args), cav31_drive(*args)
+            fr = np.asarray(ch["ghk_frozen"]) != 0.0
+            return np.where(fr, nmodl[0], shared[0]), np.where(fr, nmodl[1], shared[1])
         if name in ("CaHVA_SU2015_DCN", "CaLVA_SU2015_DCN"):
             return su2015_drive(pv, self._ci_for_channels(), self._co_for_channels(), ch["temp"])
         return cav33_drive(pv - ch["V_sh"], self._ci_for_channels(), self._co_for_channels(), ch["temp"])

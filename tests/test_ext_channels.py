@@ -195,12 +195,14 @@ def _cav31_cell(precision="f64"):
     # the soma: the Frozen class on the fixed calcium ion; the dendrite: the GHK drive in
     # the linearisation, on a CalciumDetailed shell that it fills
     c.paint(branch_in("type", "soma"), Channel("Na_Ba2002", g_max=120.0), Channel("KDR_Ba2002", g_max=40.0),
-            Channel("Cav3p1_MA2024_PC_Frozen", g_max=1e-4), Channel("Cav1p3_MA2025_BC", g_max=0.3))
+            Channel("Cav3p1_MA2024_PC_Frozen", g_max=1e-4), Channel("Cav1p3_MA2025_BC", g_max=0.3),
+            Channel("Cav2p1_RI2021_SC_Frozen", g_max=3e-5, V_sh=1.0))
     c.paint(branch_in("type", "dendrite"), Channel("Cav3p1_MA2020_GoC", g_max=2.5e-4),
             Channel("Cav3p3_RI2021_SC", perm=2e-4, g_scale=1.0, V_sh=3.0), Channel("Cav1p2_MA2020_GoC", g_max=0.5),
             Ion("CalciumDetailed", C_rest=5e-5, tau=20.0, d=0.5, Ci_initializer=5e-5))
     c.place(RootLocation(0.5), CurrentClamp(delay=2.0, durations=20.0, amplitudes=0.3), StateProbe(name="v"),
-            CurrentProbe(mechanism="Cav3p1_MA2024_PC_Frozen", name="i_cav_soma"))
+            CurrentProbe(mechanism="Cav3p1_MA2024_PC_Frozen", name="i_cav_soma"),
+            CurrentProbe(mechanism="Cav2p1_RI2021_SC_Frozen", name="i_cav21_frozen"))
     c.place(at(1, 0.5), StateProbe(name="v_dend"), MechanismProbe("CalciumDetailed", "Ci", name="ci"),
             MechanismProbe("Cav3p1_MA2020_GoC", "p", name="cav_p"), MechanismProbe("Cav3p1_MA2020_GoC", "q", name="cav_q"),
             CurrentProbe(mechanism="Cav3p1_MA2020_GoC", name="i_cav"), CurrentProbe(ion="ca", name="i_ca"),
