@@ -68,8 +68,8 @@ BC_P_EXT_MASK, their parameters after it; conductances in mS/cm^2):
 * ``CaN_IS2008`` -- channel/calcium.py:108 (g_max 1, E 10 mV, temp 36 degC, q10 1 at 36 degC; current times
   Ci / (Ci + 0.2 mM), carried by the calcium ion)
 * ``Cav3p1_MA2020_GoC`` -- channel/calcium.py:1972 (permeability g_max 2.5e-4 cm/s, temp 22 degC, q10 3 at 37 degC
-  dividing the time constants; GHK drive at temp + 0.04 K); Cav3p1_MA2024_PC repeats it, and the two _Frozen classes
-  hold the drive out of the linearisation
+  dividing the time constants; GHK drive at temp + 0.04 K); Cav3p1_MA2024_PC repeats it, the two _Frozen classes
+  hold the drive out of the linearisation, and Cav3p1Test_PC24 (:2577) runs the gates with a fixed 1 mV drive
 * ``Cav3p3_RI2021_SC`` -- channel/calcium.py:4033 (perm 1e-4 cm/s, g_scale 1e-5, temp 36 degC, V_sh 0; gates q10 2.3
   at 28 degC; GHK drive at temp - 0.01 K); Cav3p3_MA2024_PC repeats it and its _Frozen class holds the drive out of
   the linearisation
@@ -291,6 +291,10 @@ SAME_FORM["Kv1p5_MA2020_GrC"] = "Kv1p5_MA2024_PC"
 for _v in ("Cav3p1_MA2024_PC", "Cav3p1_MA2020_GoC_Frozen", "Cav3p1_MA2024_PC_Frozen"):
     CHANNELS[_v] = dict(CHANNELS["Cav3p1_MA2020_GoC"])
     SAME_FORM[_v] = "Cav3p1_MA2020_GoC"
+# Cav3p1Test_PC24 (calcium.py:2577): Cav3p1's gates, g_max in mS/cm^2 (2.5e-4 S/cm^2), a
+# fixed 1 mV drive
+CHANNELS["Cav3p1Test_PC24"] = {"g_max": 0.25, "temp": T22, "q10": 3.0, "temp_ref": celsius2kelvin(37.0)}
+SAME_FORM["Cav3p1Test_PC24"] = "Cav3p1_MA2020_GoC"
 # Cav3p3_MA2024_PC overrides nothing of Cav3p3_RI2021_SC; its _Frozen class differs only
 # in the linearisation
 for _v in ("Cav3p3_MA2024_PC", "Cav3p3_MA2024_PC_Frozen"):
@@ -562,7 +566,8 @@ def region_record(mechs, cable: CableProperty) -> tuple[int, np.ndarray]:
             elif name == "Cav3p1_MA2020_GoC":
                 rec[_abi.BC_P_CAV31_QT] = q10_phi(p["q10"], p["temp"], p["temp_ref"])
                 rec[_abi.BC_P_CAV31_TGHK] = p["temp"] + 0.04  # the model file's Kelvin offset
-                rec[_abi.BC_P_CAV31_FREEZE] = 1.0 if decl.class_name in _GHK_FROZEN else 0.0
+                rec[_abi.BC_P_CAV31_FREEZE] = 2.0 if decl.class_name == "Cav3p1Test_PC24" else \
+                    (1.0 if decl.class_name in _GHK_FROZEN else 0.0)
             elif name == "Cav3p3_RI2021_SC":
                 rec[_abi.BC_P_CAV33_PHI] = q10_phi(2.3, p["temp"], celsius2kelvin(28.0))
                 rec[_abi.BC_P_CAV33_TGHK] = p["temp"] - 0.01  # the model file's Kelvin offset

@@ -720,6 +720,11 @@ __device__ __forceinline__ Real ext_current(const Real* st, int N, const Real* P
       if ((has = (x & BC_X_CAV31) != 0)) {
         const Real p = st[kSlotCav31P * N];
         const Real gp = P[BC_P_CAV31_G] * p * p * st[kSlotCav31Q * N];
+        // Cav3p1Test_PC24 (calcium.py:2577): the same gates with a fixed 1 mV drive
+        if (P[BC_P_CAV31_FREEZE] == Real(2)) {
+          if (gv) *gv = Real(0);
+          return -gp;
+        }
         Real dd;
         const Real drive = cav31_drive(v, ci, P[BC_P_CA_CO], P[BC_P_CAV31_TGHK], dd);
         // I = -g p^2 q drive: -dI/dV = g p^2 q d drive / dV, 0 with the drive frozen

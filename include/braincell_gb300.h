@@ -273,7 +273,8 @@ typedef int32_t bc_status;
 #define BC_P_CAV31_G 145    /* permeability (cm/s)                                  */
 #define BC_P_CAV31_QT 146   /* q10^((T - temp_ref) / 10): the time constants' divisor */
 #define BC_P_CAV31_TGHK 147 /* the GHK temperature T + 0.04 K                       */
-#define BC_P_CAV31_FREEZE 148 /* 1: the drive held out of the linearisation (Frozen) */
+#define BC_P_CAV31_FREEZE 148 /* 1: the drive held out of the linearisation (Frozen);
+                                 2: Cav3p1Test_PC24's fixed 1 mV drive (g in mS/cm^2)  */
 #define BC_P_CAV33_G 149    /* g_scale x perm (cm/s)                                */
 #define BC_P_CAV33_PHI 150  /* 2.3^((T - 28 degC) / 10)                             */
 #define BC_P_CAV33_TGHK 151 /* the GHK temperature T - 0.01 K                       */

@@ -156,6 +156,8 @@ CHANNEL_DEFAULTS.update({
     "Cav1p2_MA2020_GoC": dict(g_max=0.2, V_sh=0.0, temp=_c2k(22.0), q10=1.0, temp_ref=_c2k(22.0)),  # calcium.py:1408
     "Cav1p3_MA2020_GoC": dict(g_max=0.005, V_sh=0.0, temp=_c2k(22.0), q10=1.0, temp_ref=_c2k(22.0)),  # :1683
     "Cav2p1_RI2021_SC": dict(g_max=2.2e-4, V_sh=0.0, temp=_c2k(23.0)),  # calcium.py:2767 (cm/s)
+    # calcium.py:2577: Cav3p1's gates, g in mS/cm^2, current -g p^2 q (1 mV)
+    "Cav3p1Test_PC24": dict(g_max=0.25, temp=_c2k(22.0), q10=3.0, temp_ref=_c2k(37.0)),
     "CaHVA_SU2015_DCN": dict(perm=7.5e-6, temp=_c2k(36.0), qdeltat=1.0),  # calcium.py:924 (cm/s)
     "CaLVA_SU2015_DCN": dict(perm=1.0, temp=_c2k(36.0), qdeltat=1.0),  # calcium.py:1221 (cm/s)
 })
@@ -718,6 +720,8 @@ def rates(name: str, V, p: dict, Ci=None):
         q = p["q"]
         denom = q * (p["Ra"] * _x_over_1mexp(y / q) + p["Rb"] * _x_over_1mexp(-y / q))
         return {"n": ("it", 1.0 / (1.0 + np.exp(-y / q)), 1.0 / denom)}
+    if name == "Cav3p1Test_PC24":  # calcium.py:2577-2765: Cav3p1's rates
+        return rates("Cav3p1_MA2020_GoC", V, p, Ci)
     if name == "Cav3p1_MA2020_GoC":  # calcium.py:1972-2202; the time constants divided by qt
         qt = p["q10"] ** ((p["temp"] - p["temp_ref"]) / 10.0)
         pt = np.where(V <= -90.0, 1.0, (1.0 + 1.0 / (np.exp((V + 40.0) / 9.0) + np.exp((V + 102.0) / -18.0))) / qt)
@@ -813,6 +817,7 @@ _GATES = {  # (gate, power, phi-key)
     "CaN_IS2008": (("p", 1, "phi"),),
     "Ca_ZH2019_IO": (("h", 1, "phi"),),
     "Cav3p1_MA2020_GoC": (("p", 2, "phi"), ("q", 1, "phi")),
+    "Cav3p1Test_PC24": (("p", 2, "phi"), ("q", 1, "phi")),
     "Cav3p3_RI2021_SC": (("n", 2, "phi"), ("l", 1, "phi")),
     "Cav1p2_MA2020_GoC": (("m", 1, "phi"), ("h", 1, "phi"), ("n", 1, "phi")),
     "Cav1p3_MA2020_GoC": (("m", 1, "phi"), ("h", 1, "phi"), ("n", 1, "phi")),
@@ -833,9 +838,11 @@ _ION_OF = {"Na_Ba2002": "na", "KDR_Ba2002": "k", "CaL_IS2008": "ca", "CaT_HM1992
            "Kdr_ZH2019_IO": "k", "CaT_HP1992": "ca", "CaHT_Re1993": "ca", "Kca3p1_MA2020_GoC": "k",
            "SK_SU2015_DCN": "k", "K_Kv_test": "k", "CaN_IS2008": "ca", "Nav_MA2020_GrC": "na",
            "Cav3p1_MA2020_GoC": "ca", "Cav3p3_RI2021_SC": "ca", "Cav1p2_MA2020_GoC": "ca", "Cav1p3_MA2020_GoC": "ca",
-           "Cav2p1_RI2021_SC": "ca", "CaHVA_SU2015_DCN": "ca", "CaLVA_SU2015_DCN": "ca"}
+           "Cav2p1_RI2021_SC": "ca", "CaHVA_SU2015_DCN": "ca", "CaLVA_SU2015_DCN": "ca",
+           "Cav3p1Test_PC24": "ca"}
 # calcium channels with a GHK current (-g gates drive) instead of an ohmic one
-_GHK = ("Cav3p1_MA2020_GoC", "Cav3p3_RI2021_SC", "Cav2p1_RI2021_SC", "CaHVA_SU2015_DCN", "CaLVA_SU2015_DCN")
+_GHK = ("Cav3p1_MA2020_GoC", "Cav3p3_RI2021_SC", "Cav2p1_RI2021_SC", "CaHVA_SU2015_DCN", "CaLVA_SU2015_DCN",
+        "Cav3p1Test_PC24")
 # channels with their own reversal potential (HHTypedNeuron root, not an ion)
 _OWN_E = ("HCN_HM1992", "HCN1_MA2020_GoC", "HCN1_MA2024_PC", "HCN2_MA2020_GoC", "HCN_SU2015_DCN", "HCN_ZH2019_IO",
           "CaL_SU2015_DCN", "CaN_IS2008", "Ca_ZH2019_IO")
@@ -895,6 +902,9 @@ def _resolve(table: dict, decl) -> dict:
         p["phi"] = p["q10"] ** ((p["temp"] - p["temp_ref"]) / 10.0)
     if name in ("Cav3p1_MA2020_GoC", "Cav3p3_RI2021_SC", "Cav2p1_RI2021_SC"):  # _Frozen: drive out of the linearisation
         p["ghk_frozen"] = 1.0 if decl.class_name.endswith("_Frozen") else 0.0
+    if name == "Cav3p1Test_PC24":  # Cav3p1's gates with the fixed 1 mV drive
+        p["phi"] = 1.0
+        p["ghk_frozen"] = 2.0
     if name == "Cav3p3_RI2021_SC":  # Gates q10 2.3 at 28 degC; g = g_scale perm
         p["phi"] = 2.3 ** ((p["temp"] - _c2k(28.0)) / 10.0)
         p["g_max"] = p["g_scale"] * p["perm"]
@@ -1372,6 +1382,8 @@ class OracleCell:
         """(drive, d drive / dV) of a GHK calcium channel at the point voltages."""
         if name == "Cav3p1_MA2020_GoC":
             return cav31_drive(pv, self._ci_for_channels(), self._co_for_channels(), ch["temp"])
+        if name == "Cav3p1Test_PC24":  # the fixed 1 mV drive
+            return np.ones_like(pv), np.zeros_like(pv)
         if name == "Cav2p1_RI2021_SC":  # the _Frozen classes: the Cav3.1 model-file helper (calcium.py, their current)
             args = (pv - ch["V_sh"], self._ci_for_channels(), self._co_for_channels(), ch["temp"])
             shared, nmodl = ghk_codata_drive(*args), cav31_drive(*args)

@@ -102,10 +102,10 @@ def _io_cell(precision="f64"):
     soma = Branch.from_lengths(lengths=[20.0], radii=[10.0, 10.0], type="soma")
     c = Cell(Morphology.from_root(soma, name="soma"), cv_policy=CVPerBranch(), precision=precision)
     c.paint(AllRegion(), CableProperty(), Channel("IL", g_max=0.1, E=-65.0), Channel("Na_ZH2019_IO"),
-            Channel("Kdr_ZH2019_IO"), Channel("HCN_ZH2019_IO"))
+            Channel("Kdr_ZH2019_IO"), Channel("HCN_ZH2019_IO"), Channel("Cav3p1Test_PC24", g_max=0.5))
     c.place(RootLocation(0.5), CurrentClamp(delay=2.0, durations=15.0, amplitudes=0.5), StateProbe(name="v"),
             MechanismProbe("Kdr_ZH2019_IO", "n", name="kdr_n"), MechanismProbe("HCN_ZH2019_IO", "q", name="hcn_q"),
-            CurrentProbe(mechanism="Na_ZH2019_IO", name="i_na"))
+            CurrentProbe(mechanism="Na_ZH2019_IO", name="i_na"), CurrentProbe(mechanism="Cav3p1Test_PC24", name="i_t"))
     return c
 
 
